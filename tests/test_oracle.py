@@ -1,0 +1,179 @@
+"""The oracle against the reference's own golden values and tests (CPU only).
+
+Pins reproduced here (each names the reference test it restates):
+  * traverse! doctest, src/cwbvh/traverse_macro.rs:17-57 -> original prim 62
+  * check_flat_subdivided_plane_normals, tests/mod.rs:104-124 -> 65,536 +Y hits
+  * obj_cwbvh test, examples/obj_cwbvh.rs:142-181 -> hash 1343358762, 5 presets
+  * degenerate builds, tests/mod.rs:34-88 -> build and miss
+  * build_bvh_with_varying_prim_counts, tests/mod.rs:90-102 -> validate
+  * test_reinsertion, src/bvh2/reinsertion.rs:394-438 -> validate
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from obvhs_gb300 import test_util as T
+from obvhs_gb300.params import PRESETS, BvhBuildParams, SortPrecision
+
+import helpers as H
+
+ALL = list(PRESETS)
+F32_MAX = np.float32(3.4028235e38)
+
+
+def _interleave_ref(x, y, z, bits):
+    code = 0
+    for b in range(bits):
+        code |= ((x >> b) & 1) << (3 * b)
+        code |= ((y >> b) & 1) << (3 * b + 1)
+        code |= ((z >> b) & 1) << (3 * b + 2)
+    return code
+
+
+@pytest.mark.parametrize("precision,bits", [(0, 21), (1, 42)])
+def test_morton_matches_bit_interleave(precision, bits):
+    """morton_encode_u64/u128_unorm (src/ploc/morton.rs:55-89) equal a plain
+    bit interleave of the truncated, masked grid coordinates."""
+    rng = np.random.default_rng(7)
+    n = 300
+    c = rng.uniform(-3, 5, size=(n, 3)).astype(np.float32)
+    aabbs = np.concatenate([c, c], 1)
+    codes, order = O.morton(aabbs, precision)
+    mn = aabbs[:, :3].min(0)
+    mx = aabbs[:, 3:].max(0)
+    # Aabb::diagonal() is an f32 subtraction, widened afterwards (ploc/mod.rs:287)
+    scale = 1.0 / (mx - mn).astype(np.float64)
+    offset = -mn.astype(np.float64) * scale
+    for i in range(n):
+        p = c[i].astype(np.float64) * scale + offset
+        q = [int(v * float(1 << bits)) if v > 0 else 0 for v in p]
+        q = [min(v, (1 << 64) - 1) & ((1 << bits) - 1) for v in q]
+        want = _interleave_ref(q[0], q[1], q[2], bits)
+        got = int(codes[i, 0]) | (int(codes[i, 1]) << 64)
+        assert got == want, i
+    keys = [(int(codes[i, 0]) | (int(codes[i, 1]) << 64), i) for i in range(n)]
+    assert [k[1] for k in sorted(keys)] == list(order)
+
+
+def test_morton_edge_cases():
+    """unorm 1.0 -> 2^21 masks to 0; NaN/negative saturate to 0 (Rust `as`)."""
+    aabbs = np.array([[0, 0, 0, 0, 0, 0], [1, 1, 1, 1, 1, 1]], np.float32)
+    codes, _ = O.morton(aabbs, 0)
+    assert int(codes[0, 0]) == 0 and int(codes[1, 0]) == 0
+    codes, _ = O.morton(aabbs, 1)
+    assert int(codes[1, 0]) == 0 and int(codes[1, 1]) == 0
+    inf = np.array([[-np.inf] * 3 + [np.inf] * 3] * 4, np.float32)
+    codes, order = O.morton(inf, 0)
+    assert not codes.any() and list(order) == [0, 1, 2, 3]
+
+
+@pytest.mark.parametrize("preset", ALL)
+def test_doctest_hit_prim_62(preset):
+    tris, ray = H.doctest_scene()
+    b = O.build(tris=tris, params=PRESETS[preset]())
+    ids, t, _ = O.traverse(b.cw_nodes, b.cw_pidx, tris, ray)
+    assert ids[0] == H.DOCTEST_PRIM
+    assert np.isfinite(t[0])
+
+
+def test_flat_plane_normals():
+    tris, rays = H.plane_scene()
+    b = O.build(tris=tris, params=BvhBuildParams.medium_build())
+    _, _, bid = O.traverse(b.cw_nodes, b.cw_pidx, tris, rays)
+    assert (bid != 0xFFFFFFFF).all()
+    # tests/mod.rs:110 indexes the ORIGINAL tris by the BVH-order id.
+    n = T.compute_normal(tris[bid])
+    assert np.all(n == np.array([0, 1, 0], np.float32))
+
+
+@pytest.mark.parametrize("preset", ["fastest", "fast", "medium", "slow", "very_slow"])
+def test_kitchen_hash(preset):
+    tris = H.kitchen_tris()
+    rays = H.kitchen_rays()
+    b = O.build(tris=tris, params=PRESETS[preset](), nthreads=4)
+    _, _, bid = O.traverse(b.cw_nodes, b.cw_pidx, tris, rays)
+    assert H.kitchen_hash(tris, b.cw_pidx, bid, rays) == H.KITCHEN_HASH
+
+
+EMPTY = np.array([[F32_MAX] * 3 + [-F32_MAX] * 3], np.float32)
+INF10 = np.array([[-np.inf] * 3 + [np.inf] * 3] * 10, np.float32)
+MAX10 = np.array([[-F32_MAX] * 3 + [F32_MAX] * 3] * 10, np.float32)
+NOTHING = np.zeros((0, 6), np.float32)
+
+
+@pytest.mark.parametrize("preset", ALL)
+@pytest.mark.parametrize("aabbs", [EMPTY, INF10, MAX10, NOTHING], ids=["empty", "inf", "max", "nothing"])
+def test_degenerate_bvh2_builds(preset, aabbs):
+    """build_bvh2_with_{empty_aabb,many_inf,many_max,nothing} (tests/mod.rs:34-78):
+    PLOC + reinsertion build and produce a structurally valid tree."""
+    p = PRESETS[preset]()
+    nodes, pidx, md, _ = O.ploc(aabbs, search_distance=p.ploc_search_distance, sort_precision=p.sort_precision,
+                                search_depth_threshold=p.search_depth_threshold)
+    assert len(nodes) == max(2 * len(aabbs) - 1, 0)
+    if len(nodes):
+        nodes, _ = O.reinsertion(nodes, pidx, md, p.reinsertion_batch_ratio)
+        assert O.validate_bvh2(nodes, pidx, md, aabbs)[0] == 0
+
+
+@pytest.mark.parametrize("preset", ALL)
+@pytest.mark.parametrize("aabbs", [EMPTY, NOTHING], ids=["empty", "nothing"])
+def test_degenerate_cwbvh_builds_miss(preset, aabbs):
+    """build_cwbvh_with_{empty_aabb,nothing} (tests/mod.rs:61-88)."""
+    b = O.build(aabbs=aabbs, params=PRESETS[preset]())
+    if len(aabbs) == 0:
+        assert len(b.cw_nodes) == 0
+    ray = T.make_rays([[0, 0, 1]], [[0, 0, -1]])
+    dummy = np.zeros((max(len(aabbs), 1), 9), np.float32)  # triangles that never hit
+    ids, _, _ = O.traverse(b.cw_nodes, b.cw_pidx, dummy, ray)
+    assert ids[0] == 0xFFFFFFFF
+
+
+def test_cwbvh_of_infinite_boxes_is_an_error():
+    """With infinite half areas every distribution cost is inf, no split is
+    chosen and the reference would index decisions out of range
+    (src/cwbvh/bvh2_to_cwbvh.rs:281-291,361-369); the oracle reports it."""
+    with pytest.raises(RuntimeError):
+        O.build(aabbs=INF10, params=BvhBuildParams.medium_build())
+
+
+def test_varying_prim_counts_validate():
+    tris_all = T.height_to_triangles(T.flat_heights(4, 4), 4, 4)
+    for n in range(len(tris_all) - 1, 0, -1):
+        tris = tris_all[:n]
+        aabbs = T.tri_aabbs(tris)
+        for preset in ALL:
+            p = PRESETS[preset]()
+            b = O.build(tris=tris, params=p)
+            r, _ = O.validate_bvh2(b.bvh2_nodes, b.bvh2_pidx, b.max_depth, aabbs, tight=not p.pre_split,
+                                   splits=p.pre_split)
+            assert r == 0, (n, preset, "bvh2", r)
+            r, _ = O.validate_cwbvh(b.cw_nodes, b.cw_pidx, aabbs, splits=p.pre_split)
+            assert r == 0, (n, preset, "cwbvh", r)
+
+
+def test_reinsertion_validates_demoscene():
+    tris = T.demoscene(32, 0)
+    aabbs = T.tri_aabbs(tris)
+    nodes, pidx, md, _ = O.ploc(aabbs, search_distance=2, sort_precision=SortPrecision.U64,
+                                search_depth_threshold=1)
+    assert O.validate_bvh2(nodes, pidx, md, aabbs)[0] == 0
+    nodes2, stats = O.reinsertion(nodes, pidx, md, 0.25)
+    assert stats[0] > 0
+    assert O.validate_bvh2(nodes2, pidx, md, aabbs, tight=True)[0] == 0
+    nodes3, _ = O.reinsertion(nodes2, pidx, md, 0.5)
+    assert O.validate_bvh2(nodes3, pidx, md, aabbs, tight=True)[0] == 0
+    assert O.sah_bvh2(nodes3) <= O.sah_bvh2(nodes) * 1.0001
+
+
+def test_tri_aabbs_match_numpy():
+    tris = T.demoscene(16, 3)
+    assert np.array_equal(O.tri_aabbs(tris).view(np.uint32), T.tri_aabbs(tris).view(np.uint32))
+
+
+def test_triangle_intersect_kats():
+    """Triangle::intersect (src/triangle.rs:35-76): hit, miss, and tmin/tmax."""
+    tri = np.array([[-1, -1, 0, 1, -1, 0, 0, 1, 0]], np.float32)
+    assert O.tri_intersect(tri, T.make_rays([[0, 0, -2]], [[0, 0, 1]])) == 2.0
+    assert O.tri_intersect(tri, T.make_rays([[5, 0, -2]], [[0, 0, 1]])) == np.inf
+    assert O.tri_intersect(tri, T.make_rays([[0, 0, -2]], [[0, 0, 1]], tmax=1.5)) == np.inf
+    assert O.tri_intersect(tri, T.make_rays([[0, 0, -2]], [[0, 0, 1]], tmin=2.5)) == np.inf
