@@ -1,0 +1,184 @@
+/* obvhs_gb300.h -- C ABI of the GB300 (sm_103a) BVH library.
+ *
+ * Drop-in for the hot path of the Rust crate obvhs 0.3.1: PLOC BVH2 build,
+ * reinsertion, spatial pre-splits, BVH2 -> CWBVH8 conversion and CWBVH
+ * closest-hit / occlusion traversal.  Every entry point names the reference
+ * interface it replaces.  Plain pointers and sizes only; no exceptions cross
+ * this boundary; every function returns an obvhs_status (0 = success) and
+ * obvhs_ctx_last_error() describes the last failure.
+ *
+ * Memory: functions taking `device_ptrs` read their array arguments from
+ * device memory when it is non-zero (stream-ordered on the context's stream;
+ * the caller synchronises), and from host memory otherwise (the call copies
+ * and returns when the results are on the host).
+ *
+ * Threading: a context owns one CUDA stream and its scratch buffers; use a
+ * context from one thread at a time.
+ *
+ * Array layouts
+ *   triangles  float[n][9]   v0 xyz, v1 xyz, v2 xyz         (Triangle, src/triangle.rs:9-13)
+ *   aabbs      float[n][6]   min xyz, max xyz               (Aabb, src/aabb.rs:13-16)
+ *   bvh2 nodes 32 bytes      min xyz f32, prim_count u32, max xyz f32, first_index u32
+ *                            (Bvh2Node small layout, src/bvh2/node.rs:14-36)
+ *   cwbvh nodes 80 bytes     CwBvhNode byte layout (src/cwbvh/node.rs:12-54)
+ *   rays       obvhs_ray     origin, tmin, direction, tmax  (Ray, src/ray.rs:17-30;
+ *                            inv_direction is computed on the device as Ray::new does)
+ *   hits       obvhs_hit     original primitive id (primitive_indices already applied,
+ *                            0xffffffff = miss) and t (+inf = miss)
+ */
+#ifndef OBVHS_GB300_H
+#define OBVHS_GB300_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define OBVHS_API __attribute__((visibility("default")))
+#else
+#define OBVHS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  OBVHS_OK = 0,
+  OBVHS_ERR_INVALID_ARG = -1, /* bad argument (the reference would panic or not compile) */
+  OBVHS_ERR_CUDA = -2,        /* CUDA runtime error */
+  OBVHS_ERR_OOM = -3,         /* device allocation failed or exceeded the context budget */
+  OBVHS_ERR_BAD_INPUT = -4,   /* NaN coordinates, leaves with >1 primitive, or non-finite
+                                 CWBVH costs; the reference panics or indexes out of range */
+  OBVHS_ERR_LIMIT = -5,       /* a bounded device loop or stack reached its limit */
+  OBVHS_ERR_DEVICE = -6       /* a kernel set its status word */
+} obvhs_status;
+
+typedef struct obvhs_ctx obvhs_ctx;
+typedef struct obvhs_bvh2 obvhs_bvh2;
+typedef struct obvhs_cwbvh obvhs_cwbvh;
+
+typedef struct {
+  float origin[3];
+  float tmin;
+  float direction[3];
+  float tmax;
+} obvhs_ray;
+
+typedef struct {
+  uint32_t primitive_id;
+  float t;
+} obvhs_hit;
+
+/* BvhBuildParams (src/lib.rs:296-319).  ploc_search_distance is the radius
+ * 1..32 (PlocSearchDistance values 1,2,6,14,24,32, or any radius as
+ * build_ploc::<SEARCH_DISTANCE> allows); sort_precision 0 = U64, 1 = U128. */
+typedef struct {
+  int32_t pre_split;
+  uint32_t ploc_search_distance;
+  uint32_t search_depth_threshold;
+  float reinsertion_batch_ratio;
+  float post_collapse_reinsertion_batch_ratio_multiplier;
+  uint32_t sort_precision;
+  uint32_t max_prims_per_leaf;
+  float collapse_traversal_cost;
+} obvhs_build_params;
+
+/* Per-build statistics. */
+typedef struct {
+  double core_build_ms;     /* device time of pre-split + PLOC + reinsertion + conversion */
+  uint32_t leaf_count;      /* leaves given to PLOC (after pre-splits) */
+  uint32_t ploc_passes;     /* PLOC merge passes */
+  uint64_t ploc_sum_counts; /* sum over passes of live clusters */
+  uint64_t reinsertions;    /* reinsertions applied */
+  uint64_t kernel_launches; /* kernels launched by the call */
+} obvhs_build_stats;
+
+/* ---- context ------------------------------------------------------------ */
+/* Creates a context on `device` with its own stream.  hbm_budget_bytes caps
+ * the context's scratch buffers (0 = no cap).  No reference counterpart: the
+ * reference's builders own their Vec scratch (src/ploc/mod.rs:34-45). */
+OBVHS_API int obvhs_ctx_create(int device, uint64_t hbm_budget_bytes, obvhs_ctx** out);
+OBVHS_API int obvhs_ctx_destroy(obvhs_ctx* ctx);
+OBVHS_API const char* obvhs_ctx_last_error(const obvhs_ctx* ctx);
+/* The context's cudaStream_t. */
+OBVHS_API void* obvhs_ctx_stream(obvhs_ctx* ctx);
+OBVHS_API int obvhs_ctx_synchronize(obvhs_ctx* ctx);
+/* Kernels launched by this context so far. */
+OBVHS_API uint64_t obvhs_ctx_kernel_launches(const obvhs_ctx* ctx);
+
+/* ---- BVH2 --------------------------------------------------------------- */
+/* PlocBuilder::build / build_ploc::<SEARCH_DISTANCE> (src/ploc/mod.rs:95-251):
+ * leaves Bvh2Node::new(aabbs[i], 1, indices[i]) (indices NULL = 0..n),
+ * Morton sort (U64/U128), PLOC merging with radius search_distance (1..32),
+ * distance 1 for the first search_depth_threshold passes. */
+OBVHS_API int obvhs_ploc_build(obvhs_ctx* ctx, const float* aabbs, const uint32_t* indices, uint32_t n,
+                     uint32_t search_distance, uint32_t sort_precision, uint32_t search_depth_threshold,
+                     int device_ptrs, obvhs_bvh2** out, obvhs_build_stats* stats);
+/* Bvh2 fields: nodes.len(), primitive_indices.len(), max_depth (src/bvh2/mod.rs:31-85). */
+OBVHS_API int obvhs_bvh2_info(const obvhs_bvh2* bvh, uint32_t* n_nodes, uint32_t* n_prims, uint32_t* max_depth);
+/* Copies the nodes (32-byte layout) and primitive_indices to the host. */
+OBVHS_API int obvhs_bvh2_download(obvhs_ctx* ctx, const obvhs_bvh2* bvh, void* nodes32, uint32_t* prim_indices);
+/* Creates a device BVH2 from host arrays (e.g. a tree built elsewhere). */
+OBVHS_API int obvhs_bvh2_upload(obvhs_ctx* ctx, const void* nodes32, uint32_t n_nodes, const uint32_t* prim_indices,
+                      uint32_t n_prims, uint32_t max_depth, obvhs_bvh2** out);
+OBVHS_API int obvhs_bvh2_free(obvhs_bvh2* bvh);
+
+/* ReinsertionOptimizer::run (src/bvh2/reinsertion.rs:40-57), in place.
+ * ratio_sequence NULL = the reference's default 1/1, 1/3, ..., 1/31. */
+OBVHS_API int obvhs_reinsertion_run(obvhs_ctx* ctx, obvhs_bvh2* bvh, float batch_size_ratio, const float* ratio_sequence,
+                          uint32_t n_ratios, uint64_t* applied);
+
+/* ---- pre-splits ----------------------------------------------------------- */
+/* split_aabbs_preset over Triangle::aabb (src/splits.rs:16-34,
+ * src/cwbvh/builder.rs:31-43).  Writes the grown AABB and index lists to
+ * host arrays of capacity `cap`; *m receives the count (if m > cap nothing is
+ * copied and OBVHS_ERR_INVALID_ARG is returned with *m set). */
+OBVHS_API int obvhs_split_aabbs_preset(obvhs_ctx* ctx, const float* triangles, uint32_t n, float* aabbs_out,
+                             uint32_t* indices_out, uint32_t cap, uint32_t* m);
+
+/* ---- CWBVH -------------------------------------------------------------- */
+/* bvh2_to_cwbvh (src/cwbvh/bvh2_to_cwbvh.rs:490-510).  max_prims_per_leaf
+ * 1..3; the output node and primitive order equals the reference's. */
+OBVHS_API int obvhs_bvh2_to_cwbvh(obvhs_ctx* ctx, const obvhs_bvh2* bvh, uint32_t max_prims_per_leaf, int order_children,
+                        obvhs_cwbvh** out);
+/* build_cwbvh_from_tris (src/cwbvh/builder.rs:20-85): [pre-split] -> PLOC ->
+ * reinsertion -> bvh2_to_cwbvh(max_prims.clamp(1,3), true).  The triangles
+ * are also attached for traversal. */
+OBVHS_API int obvhs_build_cwbvh_from_tris(obvhs_ctx* ctx, const float* triangles, uint32_t n, const obvhs_build_params* params,
+                                int device_ptrs, obvhs_cwbvh** out, obvhs_build_stats* stats);
+/* build_cwbvh (src/cwbvh/builder.rs:97-123): from AABBs; pre_split ignored. */
+OBVHS_API int obvhs_build_cwbvh(obvhs_ctx* ctx, const float* aabbs, uint32_t n, const obvhs_build_params* params,
+                      int device_ptrs, obvhs_cwbvh** out, obvhs_build_stats* stats);
+/* CwBvh fields: nodes.len(), primitive_indices.len(), total_aabb (src/cwbvh/mod.rs:43-55). */
+OBVHS_API int obvhs_cwbvh_info(const obvhs_cwbvh* bvh, uint32_t* n_nodes, uint32_t* n_prims, float total_aabb[6]);
+/* Copies nodes (80-byte layout) and primitive_indices to the host. */
+OBVHS_API int obvhs_cwbvh_download(obvhs_ctx* ctx, const obvhs_cwbvh* bvh, void* nodes80, uint32_t* prim_indices);
+/* Creates a device CWBVH from host arrays (e.g. a CwBvh serialised by the reference). */
+OBVHS_API int obvhs_cwbvh_upload(obvhs_ctx* ctx, const void* nodes80, uint32_t n_nodes, const uint32_t* prim_indices,
+                       uint32_t n_prims, obvhs_cwbvh** out);
+/* Attaches triangles (original order; indexed through primitive_indices, as
+ * the reference's intersection closures do: src/cwbvh/mod.rs:141-146). */
+OBVHS_API int obvhs_cwbvh_set_triangles(obvhs_ctx* ctx, obvhs_cwbvh* bvh, const float* triangles, uint32_t n, int device_ptrs);
+OBVHS_API int obvhs_cwbvh_free(obvhs_cwbvh* bvh);
+
+/* ---- traversal ------------------------------------------------------------ */
+/* CwBvh::ray_traverse with Triangle::intersect as the closure
+ * (src/cwbvh/mod.rs:169-198, src/triangle.rs:35-76): closest hit per ray. */
+OBVHS_API int obvhs_ray_traverse(obvhs_ctx* ctx, const obvhs_cwbvh* bvh, const obvhs_ray* rays, uint32_t n, obvhs_hit* hits,
+                       int device_ptrs);
+/* CwBvh::ray_traverse_miss (src/cwbvh/mod.rs:201-225): miss[i] = 1 when ray i
+ * hits nothing in [tmin, tmax), 0 when it is occluded. */
+OBVHS_API int obvhs_ray_traverse_miss(obvhs_ctx* ctx, const obvhs_cwbvh* bvh, const obvhs_ray* rays, uint32_t n, uint8_t* miss,
+                            int device_ptrs);
+
+/* ---- stage-level access for parity checks ------------------------------- */
+/* sort_nodes_by_morton (src/ploc/mod.rs:771-847) on Bvh2Node::new(aabbs[i])
+ * leaves: codes in input order (u64 pairs: lo, hi; hi = 0 for U64) and the
+ * stable sorted order. */
+OBVHS_API int obvhs_morton_sort(obvhs_ctx* ctx, const float* aabbs, uint32_t n, uint32_t sort_precision, uint64_t* codes,
+                      uint32_t* order);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OBVHS_GB300_H */

@@ -1,0 +1,413 @@
+"""Host-side mirror of obvhs's builder and traversal API over the CUDA library.
+
+Names, argument meaning and error behaviour follow the Rust crate:
+  PlocBuilder.build / build_ploc            src/ploc/mod.rs:95-251
+  ReinsertionOptimizer.run                  src/bvh2/reinsertion.rs:40-57
+  split_aabbs_preset                        src/splits.rs:16-34
+  bvh2_to_cwbvh                             src/cwbvh/bvh2_to_cwbvh.rs:490-510
+  build_cwbvh_from_tris / build_cwbvh       src/cwbvh/builder.rs:20-123
+  CwBvh.ray_traverse / ray_traverse_miss    src/cwbvh/mod.rs:169-225
+Every call runs on the GPU through libobvhs_gb300.so; there is no CPU path.
+Where the reference panics (PlocSearchDistance::from, a leaf with several
+primitives, a NaN box) these raise ObvhsError / ValueError.
+
+Arrays are numpy (host) or torch CUDA tensors (device, zero-copy):
+  triangles float32 (n, 9); aabbs float32 (n, 6); rays float32 (n, 8) =
+  origin xyz, tmin, direction xyz, tmax.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as N
+from .params import BvhBuildParams, PlocSearchDistance, SortPrecision
+
+INVALID = 0xFFFFFFFF
+
+
+def _is_cuda_tensor(x) -> bool:
+    return hasattr(x, "is_cuda") and hasattr(x, "data_ptr") and bool(x.is_cuda)
+
+
+def _prep(x, dtype, cols):
+    """Returns (pointer, n_rows, device_flag, keepalive)."""
+    if _is_cuda_tensor(x):
+        import torch
+
+        want = {np.float32: torch.float32, np.uint32: torch.int32}[dtype]
+        if x.dtype != want and not (dtype is np.uint32 and x.dtype == torch.int32):
+            raise TypeError(f"expected a {want} tensor")
+        x = x.contiguous()
+        torch.cuda.synchronize(x.device)
+        n = x.numel() // cols if cols else x.numel()
+        return ctypes.c_void_p(x.data_ptr()), n, 1, x
+    a = np.ascontiguousarray(x, dtype=dtype)
+    if cols:
+        a = a.reshape(-1, cols)
+    return a.ctypes.data_as(ctypes.c_void_p), (len(a) if cols else a.size), 0, a
+
+
+class Context:
+    """A CUDA stream plus grow-only scratch buffers on one device (one thread
+    at a time), standing in for the reference builders' reusable Vecs."""
+
+    _default = None
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        self.lib = N.load()
+        h = ctypes.c_void_p()
+        r = self.lib.obvhs_ctx_create(device, hbm_budget_bytes, ctypes.byref(h))
+        if r != 0:
+            raise N.ObvhsError(r, f"cannot create a context on device {device}")
+        self.h = h
+        self.device = device
+
+    @classmethod
+    def default(cls) -> "Context":
+        if cls._default is None:
+            cls._default = Context(0)
+        return cls._default
+
+    def check(self, r: int):
+        if r != 0:
+            msg = self.lib.obvhs_ctx_last_error(self.h)
+            raise N.ObvhsError(r, msg.decode() if msg else "")
+
+    def synchronize(self):
+        self.check(self.lib.obvhs_ctx_synchronize(self.h))
+
+    @property
+    def stream(self) -> int:
+        return self.lib.obvhs_ctx_stream(self.h) or 0
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.lib.obvhs_ctx_kernel_launches(self.h))
+
+    def close(self):
+        if self.h:
+            self.lib.obvhs_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _ctx(ctx):
+    return ctx or Context.default()
+
+
+@dataclass
+class BuildStats:
+    core_build_ms: float
+    leaf_count: int
+    ploc_passes: int
+    ploc_sum_counts: int
+    reinsertions: int
+    kernel_launches: int
+
+    @staticmethod
+    def from_c(s: N.BuildStats) -> "BuildStats":
+        return BuildStats(s.core_build_ms, s.leaf_count, s.ploc_passes, s.ploc_sum_counts, s.reinsertions,
+                          s.kernel_launches)
+
+
+class Bvh2:
+    """A device-resident binary BVH (src/bvh2/mod.rs:31-85): 32-byte nodes
+    (min, prim_count, max, first_index) and primitive_indices."""
+
+    def __init__(self, ctx: Context, handle: ctypes.c_void_p, stats: BuildStats | None = None):
+        self.ctx = ctx
+        self.h = handle
+        self.stats = stats
+
+    def info(self):
+        a, b, c = N.U32(), N.U32(), N.U32()
+        self.ctx.check(self.ctx.lib.obvhs_bvh2_info(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    @property
+    def max_depth(self) -> int:
+        return self.info()[2]
+
+    def download(self):
+        nn, npr, _ = self.info()
+        nodes = np.zeros((nn, 32), np.uint8)
+        pidx = np.zeros(npr, np.uint32)
+        self.ctx.check(self.ctx.lib.obvhs_bvh2_download(self.ctx.h, self.h, nodes.ctypes.data_as(ctypes.c_void_p),
+                                                        pidx.ctypes.data_as(ctypes.c_void_p)))
+        return nodes, pidx
+
+    @property
+    def nodes(self) -> np.ndarray:
+        return self.download()[0]
+
+    @property
+    def primitive_indices(self) -> np.ndarray:
+        return self.download()[1]
+
+    @staticmethod
+    def upload(nodes, primitive_indices, max_depth=96, ctx: Context | None = None) -> "Bvh2":
+        ctx = _ctx(ctx)
+        nodes = np.ascontiguousarray(nodes, dtype=np.uint8).reshape(-1, 32)
+        pidx = np.ascontiguousarray(primitive_indices, dtype=np.uint32)
+        h = ctypes.c_void_p()
+        ctx.check(ctx.lib.obvhs_bvh2_upload(ctx.h, nodes.ctypes.data_as(ctypes.c_void_p), len(nodes),
+                                            pidx.ctypes.data_as(ctypes.c_void_p), len(pidx), max_depth,
+                                            ctypes.byref(h)))
+        return Bvh2(ctx, h)
+
+    def free(self):
+        if self.h:
+            self.ctx.lib.obvhs_bvh2_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class PlocBuilder:
+    """PLOC BVH2 builder (src/ploc/mod.rs:34-251).  Scratch lives in the context."""
+
+    def __init__(self, ctx: Context | None = None):
+        self.ctx = _ctx(ctx)
+
+    @staticmethod
+    def with_capacity(prim_count: int, ctx: Context | None = None) -> "PlocBuilder":
+        return PlocBuilder(ctx)
+
+    def build(self, search_distance, aabbs, indices=None, sort_precision=SortPrecision.U64,
+              search_depth_threshold: int = 0) -> Bvh2:
+        """`search_distance` is a PlocSearchDistance (radius 1, 2, 6, 14, 24, 32)."""
+        sd = PlocSearchDistance(int(search_distance))
+        return self.build_ploc(int(sd), aabbs, indices, sort_precision, search_depth_threshold)
+
+    def build_ploc(self, search_distance: int, aabbs, indices=None, sort_precision=SortPrecision.U64,
+                   search_depth_threshold: int = 0) -> Bvh2:
+        """build_ploc::<SEARCH_DISTANCE>: any radius 1..=32."""
+        if not 1 <= int(search_distance) <= 32:
+            raise ValueError("SEARCH_DISTANCE should be <= 32")
+        ctx = self.ctx
+        pa, n, dev, keep_a = _prep(aabbs, np.float32, 6)
+        if indices is not None:
+            pi, ni, devi, keep_i = _prep(indices, np.uint32, 0)
+            if ni != n or devi != dev:
+                raise ValueError("indices must match aabbs in length and memory space")
+        else:
+            pi, keep_i = None, None
+        h = ctypes.c_void_p()
+        st = N.BuildStats()
+        ctx.check(ctx.lib.obvhs_ploc_build(ctx.h, pa, pi, n, int(search_distance), int(sort_precision),
+                                           int(search_depth_threshold), dev, ctypes.byref(h), ctypes.byref(st)))
+        del keep_a, keep_i
+        return Bvh2(ctx, h, BuildStats.from_c(st))
+
+
+class ReinsertionOptimizer:
+    """Parallel reinsertion (src/bvh2/reinsertion.rs:24-57)."""
+
+    def run(self, bvh: Bvh2, batch_size_ratio: float, ratio_sequence=None) -> int:
+        ctx = bvh.ctx
+        applied = N.U64()
+        if ratio_sequence is None:
+            ctx.check(ctx.lib.obvhs_reinsertion_run(ctx.h, bvh.h, float(batch_size_ratio), None, 0,
+                                                    ctypes.byref(applied)))
+        else:
+            seq = np.ascontiguousarray(ratio_sequence, dtype=np.float32)
+            ctx.check(ctx.lib.obvhs_reinsertion_run(ctx.h, bvh.h, float(batch_size_ratio),
+                                                    seq.ctypes.data_as(ctypes.c_void_p), len(seq),
+                                                    ctypes.byref(applied)))
+        return int(applied.value)
+
+
+def split_aabbs_preset(triangles, ctx: Context | None = None):
+    """Triangle AABBs with large triangles split (src/splits.rs:16-34): returns
+    (aabbs (m, 6), indices (m,))."""
+    ctx = _ctx(ctx)
+    t = np.ascontiguousarray(triangles, dtype=np.float32).reshape(-1, 9)
+    m = N.U32()
+    cap = max(len(t) * 2, 16)
+    while True:
+        a = np.zeros((cap, 6), np.float32)
+        ix = np.zeros(cap, np.uint32)
+        r = ctx.lib.obvhs_split_aabbs_preset(ctx.h, t.ctypes.data_as(ctypes.c_void_p), len(t),
+                                             a.ctypes.data_as(ctypes.c_void_p), ix.ctypes.data_as(ctypes.c_void_p),
+                                             cap, ctypes.byref(m))
+        if r == -1 and m.value > cap:
+            cap = m.value
+            continue
+        ctx.check(r)
+        return a[: m.value].copy(), ix[: m.value].copy()
+
+
+class CwBvh:
+    """A device-resident compressed wide BVH8 (src/cwbvh/mod.rs:43-55):
+    80-byte nodes and primitive_indices, plus the triangles used by the
+    traversal calls (Triangle::intersect is the fixed intersection closure)."""
+
+    def __init__(self, ctx: Context, handle: ctypes.c_void_p, stats: BuildStats | None = None):
+        self.ctx = ctx
+        self.h = handle
+        self.stats = stats
+
+    def info(self):
+        a, b = N.U32(), N.U32()
+        box = np.zeros(6, np.float32)
+        self.ctx.check(self.ctx.lib.obvhs_cwbvh_info(self.h, ctypes.byref(a), ctypes.byref(b),
+                                                     box.ctypes.data_as(ctypes.c_void_p)))
+        return a.value, b.value, box
+
+    @property
+    def total_aabb(self) -> np.ndarray:
+        return self.info()[2]
+
+    def download(self):
+        nn, npr, _ = self.info()
+        nodes = np.zeros((nn, 80), np.uint8)
+        pidx = np.zeros(npr, np.uint32)
+        self.ctx.check(self.ctx.lib.obvhs_cwbvh_download(self.ctx.h, self.h, nodes.ctypes.data_as(ctypes.c_void_p),
+                                                         pidx.ctypes.data_as(ctypes.c_void_p)))
+        return nodes, pidx
+
+    @property
+    def nodes(self) -> np.ndarray:
+        return self.download()[0]
+
+    @property
+    def primitive_indices(self) -> np.ndarray:
+        return self.download()[1]
+
+    @staticmethod
+    def upload(nodes, primitive_indices, ctx: Context | None = None) -> "CwBvh":
+        ctx = _ctx(ctx)
+        nodes = np.ascontiguousarray(nodes, dtype=np.uint8).reshape(-1, 80)
+        pidx = np.ascontiguousarray(primitive_indices, dtype=np.uint32)
+        h = ctypes.c_void_p()
+        ctx.check(ctx.lib.obvhs_cwbvh_upload(ctx.h, nodes.ctypes.data_as(ctypes.c_void_p), len(nodes),
+                                             pidx.ctypes.data_as(ctypes.c_void_p), len(pidx), ctypes.byref(h)))
+        return CwBvh(ctx, h)
+
+    def set_triangles(self, triangles):
+        p, n, dev, keep = _prep(triangles, np.float32, 9)
+        self.ctx.check(self.ctx.lib.obvhs_cwbvh_set_triangles(self.ctx.h, self.h, p, n, dev))
+        if dev:
+            self.ctx.synchronize()
+        del keep
+        return self
+
+    def _trav(self, rays, out, fn, width):
+        pr, n, dev, keep = _prep(rays, np.float32, 8)
+        ctx = self.ctx
+        if out is None:
+            if dev:
+                import torch
+
+                out = torch.empty(n * width // 4 if width >= 4 else n, dtype=torch.int32 if width >= 4 else torch.uint8,
+                                  device=rays.device)
+            else:
+                out = np.zeros(n * width // 4 if width >= 4 else n, np.uint32 if width >= 4 else np.uint8)
+        po = ctypes.c_void_p(out.data_ptr()) if dev else out.ctypes.data_as(ctypes.c_void_p)
+        ctx.check(fn(ctx.h, self.h, pr, n, po, dev))
+        if dev:
+            ctx.synchronize()
+        del keep
+        return out
+
+    def ray_traverse(self, rays, out=None):
+        """Closest hit per ray (CwBvh::ray_traverse with Triangle::intersect).
+
+        Host rays: returns (primitive_id uint32 (original ids, 0xffffffff =
+        miss), t float32 (+inf = miss)).  Device rays: returns an int32 tensor
+        of shape (n, 2) holding (id, t bits)."""
+        out = self._trav(rays, out, self.ctx.lib.obvhs_ray_traverse, 8)
+        if _is_cuda_tensor(out):
+            return out.view(-1, 2)
+        o = out.reshape(-1, 2)
+        return o[:, 0].copy(), o[:, 1].copy().view(np.float32)
+
+    def ray_traverse_miss(self, rays, out=None):
+        """True where the ray hits nothing in [tmin, tmax] (CwBvh::ray_traverse_miss)."""
+        out = self._trav(rays, out, self.ctx.lib.obvhs_ray_traverse_miss, 1)
+        if _is_cuda_tensor(out):
+            return out
+        return out.astype(bool)
+
+    def free(self):
+        if self.h:
+            self.ctx.lib.obvhs_cwbvh_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def bvh2_to_cwbvh(bvh2: Bvh2, max_prims_per_leaf: int, order_children: bool,
+                  include_exact_node_aabbs: bool = False) -> CwBvh:
+    if include_exact_node_aabbs:
+        raise NotImplementedError("exact node AABBs are not produced by this library")
+    if not 1 <= max_prims_per_leaf <= 3:
+        raise ValueError("max_prims_per_leaf must be 1..=3")
+    ctx = bvh2.ctx
+    h = ctypes.c_void_p()
+    ctx.check(ctx.lib.obvhs_bvh2_to_cwbvh(ctx.h, bvh2.h, max_prims_per_leaf, int(order_children), ctypes.byref(h)))
+    return CwBvh(ctx, h)
+
+
+def _params(p: BvhBuildParams) -> N.BuildParams:
+    return N.BuildParams(int(bool(p.pre_split)), int(p.ploc_search_distance), int(p.search_depth_threshold),
+                         float(p.reinsertion_batch_ratio), float(p.post_collapse_reinsertion_batch_ratio_multiplier),
+                         int(p.sort_precision), int(p.max_prims_per_leaf), float(p.collapse_traversal_cost))
+
+
+def build_cwbvh_from_tris(triangles, config: BvhBuildParams, ctx: Context | None = None) -> CwBvh:
+    """src/cwbvh/builder.rs:20-85.  The result carries `stats.core_build_ms`
+    (the reference returns it through `&mut Duration`)."""
+    ctx = _ctx(ctx)
+    p, n, dev, keep = _prep(triangles, np.float32, 9)
+    h = ctypes.c_void_p()
+    st = N.BuildStats()
+    prm = _params(config)
+    ctx.check(ctx.lib.obvhs_build_cwbvh_from_tris(ctx.h, p, n, ctypes.byref(prm), dev, ctypes.byref(h),
+                                                  ctypes.byref(st)))
+    if dev:
+        ctx.synchronize()
+    del keep
+    return CwBvh(ctx, h, BuildStats.from_c(st))
+
+
+def build_cwbvh(aabbs, config: BvhBuildParams, ctx: Context | None = None) -> CwBvh:
+    """src/cwbvh/builder.rs:97-123 (pre_split is ignored)."""
+    ctx = _ctx(ctx)
+    p, n, dev, keep = _prep(aabbs, np.float32, 6)
+    h = ctypes.c_void_p()
+    st = N.BuildStats()
+    prm = _params(config)
+    ctx.check(ctx.lib.obvhs_build_cwbvh(ctx.h, p, n, ctypes.byref(prm), dev, ctypes.byref(h), ctypes.byref(st)))
+    if dev:
+        ctx.synchronize()
+    del keep
+    return CwBvh(ctx, h, BuildStats.from_c(st))
+
+
+def morton_sort(aabbs, sort_precision=SortPrecision.U64, ctx: Context | None = None):
+    """Morton codes of the leaf centres (input order, (lo, hi) u64) and the
+    stable sorted order (src/ploc/mod.rs:771-847)."""
+    ctx = _ctx(ctx)
+    a = np.ascontiguousarray(aabbs, dtype=np.float32).reshape(-1, 6)
+    codes = np.zeros((len(a), 2), np.uint64)
+    order = np.zeros(len(a), np.uint32)
+    ctx.check(ctx.lib.obvhs_morton_sort(ctx.h, a.ctypes.data_as(ctypes.c_void_p), len(a), int(sort_precision),
+                                        codes.ctypes.data_as(ctypes.c_void_p), order.ctypes.data_as(ctypes.c_void_p)))
+    return codes, order

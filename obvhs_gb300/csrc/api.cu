@@ -1,0 +1,593 @@
+// api.cu -- the extern "C" entry points declared in include/obvhs_gb300.h.
+#include <cstring>
+#include <vector>
+
+#include "build.h"
+#include "radix_sort.cuh"
+
+namespace {
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int now = -1;
+    cudaGetDevice(&now);
+    if (prev >= 0 && now != prev) cudaSetDevice(prev);
+  }
+};
+
+// Reads and clears the device status word; maps it to an obvhs_status.
+int take_status(BuildCtx& c) {
+  CK(cudaMemcpyAsync(c.h_status, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  uint32_t st = *c.h_status;
+  if (!st) return 0;
+  CK(cudaMemsetAsync(c.d_status, 0, 4, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  if (st & ST_BAD_INPUT) return c.fail(OBVHS_ERR_BAD_INPUT, "input contains NaN or cannot be converted");
+  if (st & (ST_STACK_OVERFLOW | ST_ITER_LIMIT)) return c.fail(OBVHS_ERR_LIMIT, "device loop or stack limit reached");
+  return c.fail(OBVHS_ERR_DEVICE, "device status " + std::to_string(st));
+}
+
+// Stages host input in scratch when device_ptrs == 0.
+const void* stage_in(BuildCtx& c, int slot, const void* p, size_t bytes, int device_ptrs, int* err) {
+  *err = 0;
+  if (device_ptrs || bytes == 0) return p;
+  void* d = c.scratch.get(slot, bytes);
+  if (!d) {
+    *err = c.fail(OBVHS_ERR_OOM, "input staging");
+    return nullptr;
+  }
+  cudaError_t e = cudaMemcpyAsync(d, p, bytes, cudaMemcpyHostToDevice, c.stream);
+  if (e) {
+    *err = c.cuda_fail(e, "input copy");
+    return nullptr;
+  }
+  return d;
+}
+
+__global__ void k_iota_u32(uint32_t* v, uint32_t n) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = i;
+}
+
+struct EventTimer {
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaStream_t s;
+  explicit EventTimer(cudaStream_t st) : s(st) {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s);
+  }
+  double stop_ms() {
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+  }
+  ~EventTimer() {
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+};
+
+// Full pipeline.  tris != NULL: build_cwbvh_from_tris; else build_cwbvh
+// from aabbs.  Inputs are device pointers here.
+int build_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t n, const obvhs_build_params* p,
+                   obvhs_cwbvh** out, obvhs_build_stats* stats) {
+  if (p->ploc_search_distance < 1 || p->ploc_search_distance > 32)
+    return c.fail(OBVHS_ERR_INVALID_ARG, "ploc_search_distance must be 1..32");
+  if (p->sort_precision > 1) return c.fail(OBVHS_ERR_INVALID_ARG, "sort_precision must be 0 (U64) or 1 (U128)");
+  uint64_t launches0 = c.kernel_launches;
+  EventTimer timer(c.stream);
+  Scratch& s = c.scratch;
+  const bool split = tris && p->pre_split;
+  const float* leaf_aabbs = aabbs;
+  const uint32_t* leaf_idx = nullptr;
+  uint32_t m = n;
+  int r;
+  if (split) {
+    float* a = nullptr;
+    uint32_t* ix = nullptr;
+    r = presplit_device(c, tris, n, &a, &ix, &m);
+    if (r) return r;
+    leaf_aabbs = a;
+    leaf_idx = ix;
+  }
+  Bvh2Node* leaves = (Bvh2Node*)s.get(SLOT_LEAVES, (size_t)std::max(m, 1u) * sizeof(Bvh2Node));
+  int* total = (int*)s.get(SLOT_TOTAL, 64);
+  obvhs_bvh2 b2;
+  b2.ctx = &c;
+  b2.n_nodes = m ? 2 * m - 1 : 0;
+  b2.n_prims = m;
+  b2.uses_spatial_splits = split;
+  b2.nodes = (Bvh2Node*)s.get(SLOT_BVH2_NODES, (size_t)std::max(b2.n_nodes, 1u) * sizeof(Bvh2Node));
+  b2.prim_indices = (uint32_t*)s.get(SLOT_BVH2_PIDX, (size_t)std::max(m, 1u) * 4);
+  if (!leaves || !total || !b2.nodes || !b2.prim_indices) return c.fail(OBVHS_ERR_OOM, "scratch");
+  if (split || !tris)
+    r = ploc_leaves(c, nullptr, leaf_aabbs, leaf_idx, m, leaves, total);
+  else
+    r = ploc_leaves(c, tris, nullptr, nullptr, m, leaves, total);
+  if (r) return r;
+  // primitive_indices = the index list given to PLOC
+  if (m) {
+    if (leaf_idx)
+      CK(cudaMemcpyAsync(b2.prim_indices, leaf_idx, (size_t)m * 4, cudaMemcpyDeviceToDevice, c.stream));
+    else {
+      k_iota_u32<<<div_up<uint32_t>(m, 256), 256, 0, c.stream>>>(b2.prim_indices, m);
+      c.kernel_launches++;
+    }
+  }
+  r = take_status(c);
+  if (r) return r;
+  uint32_t passes = 0;
+  uint64_t sum_counts = 0;
+  r = ploc_build_device(c, leaves, m, total, p->ploc_search_distance, (int)p->sort_precision,
+                        p->search_depth_threshold, b2.nodes, &passes, &sum_counts);
+  if (r) return r;
+  b2.max_depth = std::max<uint32_t>(96, passes + 1);
+  uint64_t applied = 0;
+  r = reinsertion_device(c, &b2, p->reinsertion_batch_ratio, nullptr, 0, &applied);
+  if (r) return r;
+  uint32_t mp = p->max_prims_per_leaf < 1 ? 1 : (p->max_prims_per_leaf > 3 ? 3 : p->max_prims_per_leaf);
+  obvhs_cwbvh* cw = new obvhs_cwbvh();
+  cw->ctx = &c;
+  cw->uses_spatial_splits = split;
+  r = cwbvh_convert_device(c, &b2, mp, 1, cw);
+  if (r) {
+    delete cw;
+    return r;
+  }
+  if (tris) {
+    r = reorder_tris_device(c, cw, tris, n);
+    if (r) {
+      obvhs_cwbvh_free(cw);
+      return r;
+    }
+  }
+  double ms = timer.stop_ms();
+  r = take_status(c);
+  if (r) {
+    obvhs_cwbvh_free(cw);
+    return r;
+  }
+  // total_aabb = the BVH2 root's box
+  if (b2.n_nodes) {
+    float root[8];
+    CK(cudaMemcpy(root, b2.nodes, 32, cudaMemcpyDeviceToHost));
+    cw->total_aabb[0] = root[0];
+    cw->total_aabb[1] = root[1];
+    cw->total_aabb[2] = root[2];
+    cw->total_aabb[3] = root[4];
+    cw->total_aabb[4] = root[5];
+    cw->total_aabb[5] = root[6];
+  }
+  if (stats) {
+    stats->core_build_ms = ms;
+    stats->leaf_count = m;
+    stats->ploc_passes = passes;
+    stats->ploc_sum_counts = sum_counts;
+    stats->reinsertions = applied;
+    stats->kernel_launches = c.kernel_launches - launches0;
+  }
+  *out = cw;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int obvhs_ctx_create(int device, uint64_t hbm_budget_bytes, obvhs_ctx** out) {
+  if (!out) return OBVHS_ERR_INVALID_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return OBVHS_ERR_CUDA;
+  }
+  DeviceGuard g(device);
+  obvhs_ctx* c = new obvhs_ctx();
+  c->device = device;
+  c->scratch.budget = hbm_budget_bytes;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&c->d_status, 16) != cudaSuccess || cudaMallocHost(&c->h_status, 16) != cudaSuccess ||
+      cudaMallocHost(&c->h_hist, 16 * 256 * 4) != cudaSuccess || cudaMallocHost(&c->h_small, 4096) != cudaSuccess) {
+    cudaGetLastError();
+    obvhs_ctx_destroy(c);
+    return OBVHS_ERR_CUDA;
+  }
+  c->num_sms = prop.multiProcessorCount;
+  cudaMemset(c->d_status, 0, 16);
+  if (ploc_setup_kernels() != 0) {
+    obvhs_ctx_destroy(c);
+    return OBVHS_ERR_CUDA;
+  }
+  cudaDeviceSynchronize();
+  *out = c;
+  return OBVHS_OK;
+}
+
+int obvhs_ctx_destroy(obvhs_ctx* c) {
+  if (!c) return OBVHS_OK;
+  DeviceGuard g(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->scratch.release();
+  if (c->d_status) cudaFree(c->d_status);
+  if (c->h_status) cudaFreeHost(c->h_status);
+  if (c->h_hist) cudaFreeHost(c->h_hist);
+  if (c->h_small) cudaFreeHost(c->h_small);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return OBVHS_OK;
+}
+
+const char* obvhs_ctx_last_error(const obvhs_ctx* c) { return c ? c->last_error.c_str() : "null context"; }
+void* obvhs_ctx_stream(obvhs_ctx* c) { return c ? (void*)c->stream : nullptr; }
+int obvhs_ctx_synchronize(obvhs_ctx* c) {
+  if (!c) return OBVHS_ERR_INVALID_ARG;
+  DeviceGuard g(c->device);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  return e ? c->cuda_fail(e, "synchronize") : OBVHS_OK;
+}
+uint64_t obvhs_ctx_kernel_launches(const obvhs_ctx* c) { return c ? c->kernel_launches : 0; }
+
+// ---- BVH2 ------------------------------------------------------------------
+
+int obvhs_ploc_build(obvhs_ctx* cp, const float* aabbs, const uint32_t* indices, uint32_t n, uint32_t search_distance,
+                     uint32_t sort_precision, uint32_t search_depth_threshold, int device_ptrs, obvhs_bvh2** out,
+                     obvhs_build_stats* stats) {
+  if (!cp || !out || (n && !aabbs)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  *out = nullptr;
+  if (search_distance < 1 || search_distance > 32) return c.fail(OBVHS_ERR_INVALID_ARG, "search distance must be 1..32");
+  if (sort_precision > 1) return c.fail(OBVHS_ERR_INVALID_ARG, "sort_precision must be 0 or 1");
+  uint64_t l0 = c.kernel_launches;
+  int err = 0;
+  const float* da = (const float*)stage_in(c, SLOT_INPUT, aabbs, (size_t)n * 24, device_ptrs, &err);
+  if (err) return err;
+  const uint32_t* di = indices ? (const uint32_t*)stage_in(c, SLOT_INPUT2, indices, (size_t)n * 4, device_ptrs, &err)
+                               : nullptr;
+  if (err) return err;
+  EventTimer timer(c.stream);
+  obvhs_bvh2* b = new obvhs_bvh2();
+  b->ctx = &c;
+  b->n_nodes = n ? 2 * n - 1 : 0;
+  b->n_prims = n;
+  if (cudaMalloc(&b->nodes, (size_t)std::max(b->n_nodes, 1u) * sizeof(Bvh2Node)) != cudaSuccess ||
+      cudaMalloc(&b->prim_indices, (size_t)std::max(n, 1u) * 4) != cudaSuccess) {
+    cudaGetLastError();
+    obvhs_bvh2_free(b);
+    return c.fail(OBVHS_ERR_OOM, "bvh2 allocation");
+  }
+  Bvh2Node* leaves = (Bvh2Node*)c.scratch.get(SLOT_LEAVES, (size_t)std::max(n, 1u) * sizeof(Bvh2Node));
+  int* total = (int*)c.scratch.get(SLOT_TOTAL, 64);
+  if (!leaves || !total) {
+    obvhs_bvh2_free(b);
+    return c.fail(OBVHS_ERR_OOM, "scratch");
+  }
+  int r = ploc_leaves(c, nullptr, da, di, n, leaves, total);
+  if (!r && n) {
+    if (di) {
+      cudaMemcpyAsync(b->prim_indices, di, (size_t)n * 4, cudaMemcpyDeviceToDevice, c.stream);
+    } else {
+      k_iota_u32<<<div_up<uint32_t>(n, 256), 256, 0, c.stream>>>(b->prim_indices, n);
+      c.kernel_launches++;
+    }
+  }
+  if (!r) r = take_status(c);
+  uint32_t passes = 0;
+  uint64_t sum = 0;
+  if (!r)
+    r = ploc_build_device(c, leaves, n, total, search_distance, (int)sort_precision, search_depth_threshold, b->nodes,
+                          &passes, &sum);
+  double ms = timer.stop_ms();
+  if (!r) r = take_status(c);
+  if (r) {
+    obvhs_bvh2_free(b);
+    return r;
+  }
+  b->max_depth = std::max<uint32_t>(96, passes + 1);
+  if (stats) {
+    memset(stats, 0, sizeof(*stats));
+    stats->core_build_ms = ms;
+    stats->leaf_count = n;
+    stats->ploc_passes = passes;
+    stats->ploc_sum_counts = sum;
+    stats->kernel_launches = c.kernel_launches - l0;
+  }
+  *out = b;
+  return OBVHS_OK;
+}
+
+int obvhs_bvh2_info(const obvhs_bvh2* b, uint32_t* n_nodes, uint32_t* n_prims, uint32_t* max_depth) {
+  if (!b) return OBVHS_ERR_INVALID_ARG;
+  if (n_nodes) *n_nodes = b->n_nodes;
+  if (n_prims) *n_prims = b->n_prims;
+  if (max_depth) *max_depth = b->max_depth;
+  return OBVHS_OK;
+}
+
+int obvhs_bvh2_download(obvhs_ctx* cp, const obvhs_bvh2* b, void* nodes32, uint32_t* prim_indices) {
+  if (!cp || !b) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  if (nodes32 && b->n_nodes)
+    CK(cudaMemcpyAsync(nodes32, b->nodes, (size_t)b->n_nodes * 32, cudaMemcpyDeviceToHost, c.stream));
+  if (prim_indices && b->n_prims)
+    CK(cudaMemcpyAsync(prim_indices, b->prim_indices, (size_t)b->n_prims * 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return OBVHS_OK;
+}
+
+int obvhs_bvh2_upload(obvhs_ctx* cp, const void* nodes32, uint32_t n_nodes, const uint32_t* prim_indices,
+                      uint32_t n_prims, uint32_t max_depth, obvhs_bvh2** out) {
+  if (!cp || !out || (n_nodes && !nodes32) || (n_prims && !prim_indices)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  obvhs_bvh2* b = new obvhs_bvh2();
+  b->ctx = &c;
+  b->n_nodes = n_nodes;
+  b->n_prims = n_prims;
+  b->max_depth = max_depth ? max_depth : 96;
+  if (cudaMalloc(&b->nodes, (size_t)std::max(n_nodes, 1u) * 32) != cudaSuccess ||
+      cudaMalloc(&b->prim_indices, (size_t)std::max(n_prims, 1u) * 4) != cudaSuccess) {
+    cudaGetLastError();
+    obvhs_bvh2_free(b);
+    return c.fail(OBVHS_ERR_OOM, "bvh2 allocation");
+  }
+  if (n_nodes) CK(cudaMemcpyAsync(b->nodes, nodes32, (size_t)n_nodes * 32, cudaMemcpyHostToDevice, c.stream));
+  if (n_prims) CK(cudaMemcpyAsync(b->prim_indices, prim_indices, (size_t)n_prims * 4, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  *out = b;
+  return OBVHS_OK;
+}
+
+int obvhs_bvh2_free(obvhs_bvh2* b) {
+  if (!b) return OBVHS_OK;
+  if (b->nodes) cudaFree(b->nodes);
+  if (b->prim_indices) cudaFree(b->prim_indices);
+  delete b;
+  return OBVHS_OK;
+}
+
+int obvhs_reinsertion_run(obvhs_ctx* cp, obvhs_bvh2* b, float ratio, const float* seq, uint32_t nseq,
+                          uint64_t* applied) {
+  if (!cp || !b) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  uint64_t a = 0;
+  int r = reinsertion_device(c, b, ratio, seq, seq ? nseq : 0, &a);
+  if (!r) r = take_status(c);
+  if (applied) *applied = a;
+  return r;
+}
+
+int obvhs_split_aabbs_preset(obvhs_ctx* cp, const float* triangles, uint32_t n, float* aabbs_out, uint32_t* idx_out,
+                             uint32_t cap, uint32_t* m) {
+  if (!cp || !m || (n && !triangles)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  int err = 0;
+  const float* dt = (const float*)stage_in(c, SLOT_INPUT, triangles, (size_t)n * 36, 0, &err);
+  if (err) return err;
+  float* a = nullptr;
+  uint32_t* ix = nullptr;
+  uint32_t mm = 0;
+  int r = presplit_device(c, dt, n, &a, &ix, &mm);
+  if (!r) r = take_status(c);
+  if (r) return r;
+  *m = mm;
+  if (mm > cap) return c.fail(OBVHS_ERR_INVALID_ARG, "output capacity too small");
+  if (mm) {
+    CK(cudaMemcpyAsync(aabbs_out, a, (size_t)mm * 24, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaMemcpyAsync(idx_out, ix, (size_t)mm * 4, cudaMemcpyDeviceToHost, c.stream));
+  }
+  CK(cudaStreamSynchronize(c.stream));
+  return OBVHS_OK;
+}
+
+// ---- CWBVH -----------------------------------------------------------------
+
+int obvhs_bvh2_to_cwbvh(obvhs_ctx* cp, const obvhs_bvh2* b, uint32_t max_prims, int order_children, obvhs_cwbvh** out) {
+  if (!cp || !b || !out) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  *out = nullptr;
+  if (max_prims < 1 || max_prims > 3) return c.fail(OBVHS_ERR_INVALID_ARG, "max_prims_per_leaf must be 1..3");
+  obvhs_cwbvh* cw = new obvhs_cwbvh();
+  cw->ctx = &c;
+  cw->uses_spatial_splits = b->uses_spatial_splits;
+  int r = cwbvh_convert_device(c, b, max_prims, order_children, cw);
+  if (!r) r = take_status(c);
+  if (r) {
+    obvhs_cwbvh_free(cw);
+    return r;
+  }
+  if (b->n_nodes) {
+    float root[8];
+    CK(cudaMemcpy(root, b->nodes, 32, cudaMemcpyDeviceToHost));
+    const int map[6] = {0, 1, 2, 4, 5, 6};
+    for (int k = 0; k < 6; k++) cw->total_aabb[k] = root[map[k]];
+  }
+  *out = cw;
+  return OBVHS_OK;
+}
+
+int obvhs_build_cwbvh_from_tris(obvhs_ctx* cp, const float* triangles, uint32_t n, const obvhs_build_params* p,
+                                int device_ptrs, obvhs_cwbvh** out, obvhs_build_stats* stats) {
+  if (!cp || !p || !out || (n && !triangles)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  *out = nullptr;
+  int err = 0;
+  const float* dt = (const float*)stage_in(c, SLOT_INPUT, triangles, (size_t)n * 36, device_ptrs, &err);
+  if (err) return err;
+  return build_pipeline(c, dt, nullptr, n, p, out, stats);
+}
+
+int obvhs_build_cwbvh(obvhs_ctx* cp, const float* aabbs, uint32_t n, const obvhs_build_params* p, int device_ptrs,
+                      obvhs_cwbvh** out, obvhs_build_stats* stats) {
+  if (!cp || !p || !out || (n && !aabbs)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  *out = nullptr;
+  int err = 0;
+  const float* da = (const float*)stage_in(c, SLOT_INPUT, aabbs, (size_t)n * 24, device_ptrs, &err);
+  if (err) return err;
+  return build_pipeline(c, nullptr, da, n, p, out, stats);
+}
+
+int obvhs_cwbvh_info(const obvhs_cwbvh* b, uint32_t* n_nodes, uint32_t* n_prims, float total_aabb[6]) {
+  if (!b) return OBVHS_ERR_INVALID_ARG;
+  if (n_nodes) *n_nodes = b->n_nodes;
+  if (n_prims) *n_prims = b->n_prims;
+  if (total_aabb) memcpy(total_aabb, b->total_aabb, 24);
+  return OBVHS_OK;
+}
+
+int obvhs_cwbvh_download(obvhs_ctx* cp, const obvhs_cwbvh* b, void* nodes80, uint32_t* prim_indices) {
+  if (!cp || !b) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  if (nodes80 && b->n_nodes)
+    CK(cudaMemcpyAsync(nodes80, b->nodes, (size_t)b->n_nodes * 80, cudaMemcpyDeviceToHost, c.stream));
+  if (prim_indices && b->n_prims)
+    CK(cudaMemcpyAsync(prim_indices, b->prim_indices, (size_t)b->n_prims * 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return OBVHS_OK;
+}
+
+int obvhs_cwbvh_upload(obvhs_ctx* cp, const void* nodes80, uint32_t n_nodes, const uint32_t* prim_indices,
+                       uint32_t n_prims, obvhs_cwbvh** out) {
+  if (!cp || !out || (n_nodes && !nodes80) || (n_prims && !prim_indices)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  obvhs_cwbvh* b = new obvhs_cwbvh();
+  b->ctx = &c;
+  b->n_nodes = n_nodes;
+  b->n_prims = n_prims;
+  if (cudaMalloc(&b->nodes, (size_t)std::max(n_nodes, 1u) * 80) != cudaSuccess ||
+      cudaMalloc(&b->prim_indices, (size_t)std::max(n_prims, 1u) * 4) != cudaSuccess) {
+    cudaGetLastError();
+    obvhs_cwbvh_free(b);
+    return c.fail(OBVHS_ERR_OOM, "cwbvh allocation");
+  }
+  if (n_nodes) CK(cudaMemcpyAsync(b->nodes, nodes80, (size_t)n_nodes * 80, cudaMemcpyHostToDevice, c.stream));
+  if (n_prims) CK(cudaMemcpyAsync(b->prim_indices, prim_indices, (size_t)n_prims * 4, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  if (n_nodes) {
+    // total_aabb from the root's p and e (CwBvhNode::aabb, src/cwbvh/node.rs:260-265)
+    const uint8_t* r = (const uint8_t*)nodes80;
+    float p[3];
+    memcpy(p, r, 12);
+    for (int k = 0; k < 3; k++) {
+      uint32_t eb = (uint32_t)r[12 + k] << 23;
+      float e;
+      memcpy(&e, &eb, 4);
+      b->total_aabb[k] = p[k];
+      b->total_aabb[3 + k] = p[k] + e * 255.0f;
+    }
+  }
+  *out = b;
+  return OBVHS_OK;
+}
+
+int obvhs_cwbvh_set_triangles(obvhs_ctx* cp, obvhs_cwbvh* b, const float* triangles, uint32_t n, int device_ptrs) {
+  if (!cp || !b || (n && !triangles)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  int err = 0;
+  const float* dt = (const float*)stage_in(c, SLOT_INPUT, triangles, (size_t)n * 36, device_ptrs, &err);
+  if (err) return err;
+  int r = reorder_tris_device(c, b, dt, n);
+  if (!r) r = take_status(c);
+  return r;
+}
+
+int obvhs_cwbvh_free(obvhs_cwbvh* b) {
+  if (!b) return OBVHS_OK;
+  if (b->nodes) cudaFree(b->nodes);
+  if (b->prim_indices) cudaFree(b->prim_indices);
+  if (b->tris) cudaFree(b->tris);
+  delete b;
+  return OBVHS_OK;
+}
+
+// ---- traversal ---------------------------------------------------------------
+
+static int traverse_common(obvhs_ctx* cp, const obvhs_cwbvh* b, const obvhs_ray* rays, uint32_t n, void* out,
+                           int device_ptrs, int mode) {
+  if (!cp || !b || (n && (!rays || !out))) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  int err = 0;
+  const float* dr = (const float*)stage_in(c, SLOT_INPUT2, rays, (size_t)n * 32, device_ptrs, &err);
+  if (err) return err;
+  size_t ob = (size_t)n * (mode == 0 ? 8 : 1);
+  void* dout = out;
+  if (!device_ptrs) {
+    dout = c.scratch.get(SLOT_TRAV_OUT, ob + 16);
+    if (!dout) return c.fail(OBVHS_ERR_OOM, "output staging");
+  }
+  int r = traverse_device(c, b, dr, n, mode == 0 ? (uint32_t*)dout : nullptr, mode == 1 ? (uint8_t*)dout : nullptr,
+                          mode);
+  if (r) return r;
+  if (!device_ptrs && n) CK(cudaMemcpyAsync(out, dout, ob, cudaMemcpyDeviceToHost, c.stream));
+  if (!device_ptrs) return take_status(c);
+  return OBVHS_OK;
+}
+
+int obvhs_ray_traverse(obvhs_ctx* cp, const obvhs_cwbvh* b, const obvhs_ray* rays, uint32_t n, obvhs_hit* hits,
+                       int device_ptrs) {
+  return traverse_common(cp, b, rays, n, hits, device_ptrs, 0);
+}
+
+int obvhs_ray_traverse_miss(obvhs_ctx* cp, const obvhs_cwbvh* b, const obvhs_ray* rays, uint32_t n, uint8_t* miss,
+                            int device_ptrs) {
+  return traverse_common(cp, b, rays, n, miss, device_ptrs, 1);
+}
+
+// ---- stage access ----------------------------------------------------------
+
+int obvhs_morton_sort(obvhs_ctx* cp, const float* aabbs, uint32_t n, uint32_t precision, uint64_t* codes,
+                      uint32_t* order) {
+  if (!cp || (n && (!aabbs || !codes || !order))) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  if (precision > 1) return c.fail(OBVHS_ERR_INVALID_ARG, "sort_precision must be 0 or 1");
+  if (!n) return OBVHS_OK;
+  int err = 0;
+  const float* da = (const float*)stage_in(c, SLOT_INPUT, aabbs, (size_t)n * 24, 0, &err);
+  if (err) return err;
+  Bvh2Node* leaves = (Bvh2Node*)c.scratch.get(SLOT_LEAVES, (size_t)n * sizeof(Bvh2Node));
+  int* total = (int*)c.scratch.get(SLOT_TOTAL, 64);
+  size_t kb = precision ? 16 : 8;
+  void* keys = c.scratch.get(SLOT_KEYS, (size_t)n * kb);
+  if (!leaves || !total || !keys) return c.fail(OBVHS_ERR_OOM, "scratch");
+  int r = ploc_leaves(c, nullptr, da, nullptr, n, leaves, total);
+  if (!r) r = ploc_morton_codes(c, leaves, n, total, (int)precision, keys);
+  if (r) return r;
+  std::vector<uint64_t> tmp((size_t)n * (precision ? 2 : 1));
+  CK(cudaMemcpyAsync(tmp.data(), keys, (size_t)n * kb, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  for (uint32_t i = 0; i < n; i++) {
+    codes[2 * i] = precision ? tmp[2 * i] : tmp[i];
+    codes[2 * i + 1] = precision ? tmp[2 * i + 1] : 0;
+  }
+  uint32_t* ord = nullptr;
+  r = ploc_sort_codes(c, keys, n, (int)precision, &ord);
+  if (r) return r;
+  CK(cudaMemcpyAsync(order, ord, (size_t)n * 4, cudaMemcpyDeviceToHost, c.stream));
+  return take_status(c);
+}
+
+}  // extern "C"

@@ -1,0 +1,183 @@
+// build.h -- internal host-side declarations shared by the .cu files.
+#pragma once
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/obvhs_gb300.h"
+#include "common.cuh"
+
+// Clusters left when PLOC switches to the single-CTA shared-memory tail.
+constexpr uint32_t TAIL_MAX = 2048;
+
+enum ScratchSlot {
+  SLOT_KEYS,
+  SLOT_KEYS_ALT,
+  SLOT_VALS,
+  SLOT_VALS_ALT,
+  SLOT_TILE_HIST,
+  SLOT_ALL_HIST,
+  SLOT_LEAVES,
+  SLOT_TOTAL,
+  SLOT_PLOC_A,
+  SLOT_PLOC_B,
+  SLOT_MERGE,
+  SLOT_PARTIAL,
+  SLOT_PLOC_STATE,
+  SLOT_SPLIT_AABBS,
+  SLOT_SPLIT_IDX,
+  SLOT_SPLIT_CAND,
+  SLOT_SPLIT_CAND2,
+  SLOT_SPLIT_MISC,
+  SLOT_PARENTS,
+  SLOT_FLAGS,
+  SLOT_REINS,
+  SLOT_REINS_KEYS,
+  SLOT_REINS_VALS,
+  SLOT_MIS_STATE,
+  SLOT_MIS_OWNER,
+  SLOT_TOUCHED,
+  SLOT_DECISIONS,
+  SLOT_CW_META,
+  SLOT_FRONTIER_A,
+  SLOT_FRONTIER_B,
+  SLOT_CW_COUNTERS,
+  SLOT_INPUT,
+  SLOT_INPUT2,
+  SLOT_OUTPUT,
+  SLOT_BVH2_NODES,
+  SLOT_BVH2_PIDX,
+  SLOT_TRAV_OUT,
+  SLOT_COUNT
+};
+
+// Grow-only device buffers that a context keeps between calls, like the
+// reference's builders keep their Vecs (src/ploc/mod.rs:34-45).
+struct Scratch {
+  void* ptr[SLOT_COUNT] = {};
+  size_t cap[SLOT_COUNT] = {};
+  size_t total = 0;
+  size_t budget = 0;  // 0 = unlimited
+  void* get(int slot, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (cap[slot] >= bytes) return ptr[slot];
+    if (ptr[slot]) {
+      cudaFree(ptr[slot]);
+      total -= cap[slot];
+      ptr[slot] = nullptr;
+      cap[slot] = 0;
+    }
+    size_t want = bytes + bytes / 4 + 256;
+    if (budget && total + want > budget) want = bytes;
+    if (budget && total + want > budget) return nullptr;
+    void* p = nullptr;
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    ptr[slot] = p;
+    cap[slot] = want;
+    total += want;
+    return p;
+  }
+  void release() {
+    for (int i = 0; i < SLOT_COUNT; i++)
+      if (ptr[i]) cudaFree(ptr[i]);
+    for (int i = 0; i < SLOT_COUNT; i++) {
+      ptr[i] = nullptr;
+      cap[i] = 0;
+    }
+    total = 0;
+  }
+};
+
+struct PlocState {
+  uint32_t count[2];
+  uint32_t insert[2];
+  uint32_t passes;
+  uint32_t pad;
+  unsigned long long sum_counts;
+};
+
+struct obvhs_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  uint32_t* d_status = nullptr;
+  uint32_t* h_status = nullptr;  // pinned
+  uint32_t* h_hist = nullptr;    // pinned, 16 * 256
+  void* h_small = nullptr;       // pinned, 4 KB
+  Scratch scratch;
+  std::string last_error;
+  uint64_t kernel_launches = 0;
+
+  int fail(int code, const std::string& msg) {
+    last_error = msg;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* what) {
+    last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return OBVHS_ERR_CUDA;
+  }
+};
+typedef obvhs_ctx BuildCtx;
+
+#define CK(expr)                                             \
+  do {                                                       \
+    cudaError_t ck_e_ = (expr);                              \
+    if (ck_e_ != cudaSuccess) return c.cuda_fail(ck_e_, #expr); \
+  } while (0)
+
+struct obvhs_bvh2 {
+  obvhs_ctx* ctx = nullptr;
+  Bvh2Node* nodes = nullptr;
+  uint32_t n_nodes = 0;
+  uint32_t* prim_indices = nullptr;
+  uint32_t n_prims = 0;
+  uint32_t max_depth = 96;
+  int uses_spatial_splits = 0;
+};
+
+struct obvhs_cwbvh {
+  obvhs_ctx* ctx = nullptr;
+  CwNode* nodes = nullptr;
+  uint32_t n_nodes = 0;
+  uint32_t* prim_indices = nullptr;
+  uint32_t n_prims = 0;
+  float total_aabb[6] = {0, 0, 0, 0, 0, 0};
+  float4* tris = nullptr;  // BVH order: (v0, id) (v0-v1) (v2-v0), 48 B each
+  uint32_t n_tris = 0;
+  int uses_spatial_splits = 0;
+};
+
+// ploc.cu
+int ploc_leaves(BuildCtx& c, const float* tris, const float* aabbs, const uint32_t* idx, uint32_t n, Bvh2Node* leaves,
+                int* total_keys);
+int ploc_morton_codes(BuildCtx& c, const Bvh2Node* leaves, uint32_t n, const int* total_keys, int precision,
+                      void* codes);
+int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_t** order_out);
+int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* total_keys, uint32_t radius,
+                      int precision, uint32_t depth_threshold, Bvh2Node* out_nodes, uint32_t* passes_out,
+                      uint64_t* sum_counts_out);
+int ploc_setup_kernels();
+
+// presplit.cu
+int presplit_device(BuildCtx& c, const float* tris, uint32_t n, float** aabbs_out, uint32_t** idx_out,
+                    uint32_t* m_out);
+
+// reinsertion.cu
+int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const float* seq, uint32_t nseq,
+                       uint64_t* applied_out);
+int compute_parents_device(BuildCtx& c, const Bvh2Node* nodes, uint32_t n_nodes, uint32_t* parents);
+
+// cwbvh.cu
+int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, int order_children, obvhs_cwbvh* out);
+
+// traverse.cu
+int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint32_t n, uint32_t* hits,
+                    uint8_t* miss, int mode);
+int reorder_tris_device(BuildCtx& c, obvhs_cwbvh* bvh, const float* tris, uint32_t n_tris);

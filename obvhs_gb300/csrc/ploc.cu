@@ -1,0 +1,770 @@
+// ploc.cu -- PLOC BVH2 build on the device.
+//
+// Reference: src/ploc/mod.rs:169-503 (build_ploc / build_ploc_from_leaves),
+// :508-650 (nearest-neighbour search), :771-847 (Morton sort), and
+// src/ploc/morton.rs:35-89 (bit interleave).
+//
+// Per pass the reference (a) picks for every live cluster i an offset
+// merge[i] to its best neighbour, then (b) sweeps i upwards: mutual pairs
+// merge at the larger index (left = cur[i], right = cur[best]), the two
+// children go to bvh.nodes[insert_index-2 .. insert_index-1] with
+// insert_index counting down from 2n-1, the parent (or an unpaired node) is
+// appended to next_nodes.  Here (b) is a scan: emit_i = !mutual || best < i
+// gives the next_nodes slot, merge_i = mutual && best < i gives the k-th
+// merge, whose children land at insert_base - 2(k+1).  The result is the
+// reference's tree bit for bit, given the same sorted leaves.
+//
+// Passes run as four launches on the full grid while many clusters are live;
+// once at most TAIL_MAX remain, one CTA finishes every remaining pass with
+// the clusters held in shared memory.
+#include "build.h"
+#include "radix_sort.cuh"
+
+namespace {
+
+constexpr int BLK = 256;
+
+// --- leaves, total AABB, NaN check --------------------------------------
+
+__device__ __forceinline__ void reduce_box(Box b, int* total_keys, uint32_t* status, bool valid) {
+  // block-wide min/max through shared memory, then one atomic per block
+  __shared__ int s[6][BLK / 32];
+  int k[6];
+  if (valid) {
+    // the reference extends the total by both corners (src/ploc/mod.rs:188-190),
+    // which matters for inverted boxes such as Aabb::empty()
+    k[0] = min(fkey(b.mn.x), fkey(b.mx.x));
+    k[1] = min(fkey(b.mn.y), fkey(b.mx.y));
+    k[2] = min(fkey(b.mn.z), fkey(b.mx.z));
+    k[3] = max(fkey(b.mn.x), fkey(b.mx.x));
+    k[4] = max(fkey(b.mn.y), fkey(b.mx.y));
+    k[5] = max(fkey(b.mn.z), fkey(b.mx.z));
+  } else {
+    k[0] = k[1] = k[2] = 0x7fffffff;
+    k[3] = k[4] = k[5] = (int)0x80000000;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) k[c] = min(k[c], __shfl_xor_sync(0xffffffffu, k[c], o));
+#pragma unroll
+    for (int c = 3; c < 6; c++) k[c] = max(k[c], __shfl_xor_sync(0xffffffffu, k[c], o));
+  }
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+    for (int c = 0; c < 6; c++) s[c][warp] = k[c];
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    int c = threadIdx.x;
+    int v = s[c][0];
+    for (int w = 1; w < BLK / 32; w++) v = c < 3 ? min(v, s[c][w]) : max(v, s[c][w]);
+    if (c < 3)
+      atomicMin(&total_keys[c], v);
+    else
+      atomicMax(&total_keys[c], v);
+  }
+}
+
+__device__ __forceinline__ bool box_has_nan(const Box& b) {
+  return b.mn.x != b.mn.x || b.mn.y != b.mn.y || b.mn.z != b.mn.z || b.mx.x != b.mx.x || b.mx.y != b.mx.y ||
+         b.mx.z != b.mx.z;
+}
+
+// Triangle::aabb (src/triangle.rs:28) + Bvh2Node::new(aabb, 1, indices[i]).
+__global__ void __launch_bounds__(BLK) k_leaves_from_tris(const float* __restrict__ tris, uint32_t n,
+                                                          Bvh2Node* __restrict__ leaves, int* total_keys,
+                                                          uint32_t* status) {
+  uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  bool valid = i < n;
+  Box b{};
+  if (valid) {
+    const float* t = tris + (size_t)i * 9;
+    float3 v0 = make_float3(t[0], t[1], t[2]), v1 = make_float3(t[3], t[4], t[5]), v2 = make_float3(t[6], t[7], t[8]);
+    b.mn = make_float3(smin(smin(v0.x, v1.x), v2.x), smin(smin(v0.y, v1.y), v2.y), smin(smin(v0.z, v1.z), v2.z));
+    b.mx = make_float3(smax(smax(v0.x, v1.x), v2.x), smax(smax(v0.y, v1.y), v2.y), smax(smax(v0.z, v1.z), v2.z));
+    if (box_has_nan(b)) set_status(status, ST_BAD_INPUT);
+    st_node(&leaves[i], make_node(b, 1, i));
+  }
+  reduce_box(b, total_keys, status, valid);
+}
+
+// Leaves from given AABBs (n x 6 floats) and indices (NULL = identity).
+__global__ void __launch_bounds__(BLK) k_leaves_from_aabbs(const float* __restrict__ aabbs, const uint32_t* __restrict__ idx,
+                                                           uint32_t n, Bvh2Node* __restrict__ leaves, int* total_keys,
+                                                           uint32_t* status) {
+  uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  bool valid = i < n;
+  Box b{};
+  if (valid) {
+    const float* a = aabbs + (size_t)i * 6;
+    b.mn = make_float3(a[0], a[1], a[2]);
+    b.mx = make_float3(a[3], a[4], a[5]);
+    if (box_has_nan(b)) set_status(status, ST_BAD_INPUT);
+    st_node(&leaves[i], make_node(b, 1, idx ? idx[i] : i));
+  }
+  reduce_box(b, total_keys, status, valid);
+}
+
+// --- Morton codes (src/ploc/morton.rs, src/ploc/mod.rs:287-288,782-785) ----
+
+__device__ __forceinline__ uint32_t sat_u32(double d) {
+  if (!(d > 0.0)) return 0u;
+  if (d >= 4294967295.0) return 0xffffffffu;
+  return (uint32_t)d;
+}
+__device__ __forceinline__ unsigned long long sat_u64(double d) {
+  if (!(d > 0.0)) return 0ull;
+  if (d >= 18446744073709551615.0) return ~0ull;
+  return (unsigned long long)d;
+}
+__device__ __forceinline__ unsigned long long split3_u64(uint32_t a) {
+  unsigned long long x = a & 0x1fffffull;
+  x = (x | x << 32) & 0x1f00000000ffffull;
+  x = (x | x << 16) & 0x1f0000ff0000ffull;
+  x = (x | x << 8) & 0x100f00f00f00f00full;
+  x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+  x = (x | x << 2) & 0x1249249249249249ull;
+  return x;
+}
+// split_by_3_u128 on a (hi, lo) pair: the 42 input bits spread over 126.
+// Bit b of the input goes to bit 3b; computed per 64-bit half directly.
+__device__ __forceinline__ void split3_u128(unsigned long long a, unsigned long long& lo, unsigned long long& hi) {
+  a &= 0x3ffffffffffull;
+  // low 64 output bits take input bits 0..21 (3b <= 63 -> b <= 21)
+  lo = split3_u64((uint32_t)(a & 0x1fffffu)) | ((a >> 21) & 1ull) << 63;
+  // output bits 64.. take input bits 22..41: bit b -> 3b-64
+  unsigned long long x = a >> 22;  // 20 bits, bit j = input bit 22+j -> output 66+3j -> hi bit 2+3j
+  hi = split3_u64((uint32_t)(x & 0xfffffu)) << 2;
+}
+
+struct Scale {
+  double sx, sy, sz, ox, oy, oz;
+};
+__device__ __forceinline__ Scale make_scale(const int* tk) {
+  float mnx = fkey_inv(tk[0]), mny = fkey_inv(tk[1]), mnz = fkey_inv(tk[2]);
+  float mxx = fkey_inv(tk[3]), mxy = fkey_inv(tk[4]), mxz = fkey_inv(tk[5]);
+  Scale s;
+  s.sx = 1.0 / (double)(mxx - mnx);
+  s.sy = 1.0 / (double)(mxy - mny);
+  s.sz = 1.0 / (double)(mxz - mnz);
+  s.ox = -(double)mnx * s.sx;
+  s.oy = -(double)mny * s.sy;
+  s.oz = -(double)mnz * s.sz;
+  return s;
+}
+
+__global__ void __launch_bounds__(BLK) k_morton64(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
+                                                  unsigned long long* __restrict__ codes) {
+  uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  if (i >= n) return;
+  Scale s = make_scale(total_keys);
+  Bvh2Node nd = ld_node(&leaves[i]);
+  float cx = (nd.b.x + nd.a.x) * 0.5f, cy = (nd.b.y + nd.a.y) * 0.5f, cz = (nd.b.z + nd.a.z) * 0.5f;
+  double px = __dadd_rn(__dmul_rn((double)cx, s.sx), s.ox);
+  double py = __dadd_rn(__dmul_rn((double)cy, s.sy), s.oy);
+  double pz = __dadd_rn(__dmul_rn((double)cz, s.sz), s.oz);
+  const double k = (double)(1u << 21);
+  codes[i] = split3_u64(sat_u32(px * k)) | split3_u64(sat_u32(py * k)) << 1 | split3_u64(sat_u32(pz * k)) << 2;
+}
+
+__global__ void __launch_bounds__(BLK) k_morton128(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
+                                                   U128* __restrict__ codes) {
+  uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  if (i >= n) return;
+  Scale s = make_scale(total_keys);
+  Bvh2Node nd = ld_node(&leaves[i]);
+  float cx = (nd.b.x + nd.a.x) * 0.5f, cy = (nd.b.y + nd.a.y) * 0.5f, cz = (nd.b.z + nd.a.z) * 0.5f;
+  double px = __dadd_rn(__dmul_rn((double)cx, s.sx), s.ox);
+  double py = __dadd_rn(__dmul_rn((double)cy, s.sy), s.oy);
+  double pz = __dadd_rn(__dmul_rn((double)cz, s.sz), s.oz);
+  const double k = (double)(1ull << 42);
+  unsigned long long xl, xh, yl, yh, zl, zh;
+  split3_u128(sat_u64(px * k), xl, xh);
+  split3_u128(sat_u64(py * k), yl, yh);
+  split3_u128(sat_u64(pz * k), zl, zh);
+  // (x) | (y << 1) | (z << 2) on 128-bit values
+  U128 c;
+  c.lo = xl | (yl << 1) | (zl << 2);
+  c.hi = xh | (yh << 1) | (yl >> 63) | (zh << 2) | (zl >> 62);
+  codes[i] = c;
+}
+
+__global__ void __launch_bounds__(BLK) k_gather(const Bvh2Node* __restrict__ in, const uint32_t* __restrict__ order,
+                                                uint32_t n, Bvh2Node* __restrict__ out) {
+  uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  if (i < n) st_node(&out[i], ld_node(&in[order[i]]));
+}
+
+// --- PLOC passes -----------------------------------------------------------
+
+// Pair cost as the reference computes it: the lower index's box first
+// (the SearchCache stores union(A_lo, A_hi), src/ploc/mod.rs:612-619).
+__device__ __forceinline__ float pair_cost(const Box& lo, const Box& hi) { return half_area(box_union(lo, hi)); }
+
+__device__ __forceinline__ Box load_box(const Bvh2Node* p) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+  float4 a = q[0], b = q[1];
+  return Box{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)};
+}
+
+// Nearest-neighbour choice with radius r (src/ploc/mod.rs:624-650): scan
+// j = i-r .. i+r ascending, keep the last j with cost <= best.
+__global__ void __launch_bounds__(BLK) k_ploc_search(const Bvh2Node* __restrict__ cur, const PlocState* st, int parity,
+                                                     int radius, int d1, int8_t* __restrict__ merge) {
+  __shared__ float s_box[(BLK + 64) * 6];
+  const uint32_t count = st->count[parity];
+  if (count <= 1) return;
+  const uint32_t base = blockIdx.x * BLK;
+  if (base >= count) return;
+  const int r = d1 ? 1 : radius;
+  const int64_t lo = (int64_t)base - r;
+  const uint32_t span = BLK + 2 * r;
+  for (uint32_t k = threadIdx.x; k < span; k += BLK) {
+    int64_t j = lo + k;
+    if (j >= 0 && j < (int64_t)count) {
+      Box b = load_box(&cur[j]);
+      float* d = &s_box[k * 6];
+      d[0] = b.mn.x;
+      d[1] = b.mn.y;
+      d[2] = b.mn.z;
+      d[3] = b.mx.x;
+      d[4] = b.mx.y;
+      d[5] = b.mx.z;
+    }
+  }
+  __syncthreads();
+  const uint32_t i = base + threadIdx.x;
+  if (i >= count) return;
+  auto box_at = [&](uint32_t j) {
+    const float* d = &s_box[(j - lo) * 6];
+    return Box{make_float3(d[0], d[1], d[2]), make_float3(d[3], d[4], d[5])};
+  };
+  Box me = box_at(i);
+  int8_t m;
+  if (d1) {
+    // src/ploc/mod.rs:329-382: merge[i] = cost(i-1,i) < cost(i,i+1) ? -1 : 1
+    if (i == count - 1) {
+      m = -1;
+    } else {
+      float c = pair_cost(me, box_at(i + 1));
+      float last = i == 0 ? __int_as_float(0x7f800000) : pair_cost(box_at(i - 1), me);
+      m = last < c ? -1 : 1;
+    }
+  } else {
+    uint32_t begin = i >= (uint32_t)r ? i - r : 0;
+    uint32_t end = min(i + r + 1, count);
+    uint32_t best = i;
+    float best_cost = __int_as_float(0x7f800000);
+    for (uint32_t j = begin; j < i; j++) {
+      float c = pair_cost(box_at(j), me);
+      if (c <= best_cost) {
+        best = j;
+        best_cost = c;
+      }
+    }
+    for (uint32_t j = i + 1; j < end; j++) {
+      float c = pair_cost(me, box_at(j));
+      if (c <= best_cost) {
+        best = j;
+        best_cost = c;
+      }
+    }
+    m = (int8_t)((int)best - (int)i);
+  }
+  merge[i] = m;
+}
+
+__device__ __forceinline__ void ploc_flags(const int8_t* merge, uint32_t i, bool& emit, bool& is_merge, uint32_t& best) {
+  int off = merge[i];
+  best = (uint32_t)((int)i + off);
+  bool mutual = (int)best + (int)merge[best] == (int)i;
+  emit = !mutual || best < i;
+  is_merge = mutual && best < i;
+}
+
+constexpr int ITEMS = 4;
+constexpr int CHUNK = BLK * ITEMS;  // items per block in the flag scan
+
+__global__ void __launch_bounds__(BLK) k_ploc_count(const int8_t* __restrict__ merge, const PlocState* st, int parity,
+                                                    uint2* __restrict__ partial) {
+  const uint32_t count = st->count[parity];
+  if (count <= 1) return;
+  const uint32_t base = blockIdx.x * CHUNK;
+  if (base >= count) return;
+  uint32_t e = 0, m = 0;
+  for (int k = 0; k < ITEMS; k++) {
+    uint32_t i = base + threadIdx.x * ITEMS + k;
+    if (i < count) {
+      bool emit, ism;
+      uint32_t best;
+      ploc_flags(merge, i, emit, ism, best);
+      e += emit;
+      m += ism;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    e += __shfl_xor_sync(0xffffffffu, e, o);
+    m += __shfl_xor_sync(0xffffffffu, m, o);
+  }
+  __shared__ uint32_t se[BLK / 32], sm[BLK / 32];
+  if ((threadIdx.x & 31) == 0) {
+    se[threadIdx.x >> 5] = e;
+    sm[threadIdx.x >> 5] = m;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t te = 0, tm = 0;
+    for (int w = 0; w < BLK / 32; w++) {
+      te += se[w];
+      tm += sm[w];
+    }
+    partial[blockIdx.x] = make_uint2(te, tm);
+  }
+}
+
+// One block: exclusive scan of the per-block (emit, merge) counts.
+__global__ void __launch_bounds__(1024) k_ploc_scan(uint2* __restrict__ partial, PlocState* st, int parity) {
+  const uint32_t count = st->count[parity];
+  if (count <= 1) {
+    if (threadIdx.x == 0) {
+      st->count[parity ^ 1] = count;
+      st->insert[parity ^ 1] = st->insert[parity];
+    }
+    return;
+  }
+  const uint32_t nb = (count + CHUNK - 1) / CHUNK;
+  __shared__ uint32_t we[32], wm[32];
+  __shared__ uint32_t carry_e, carry_m;
+  if (threadIdx.x == 0) {
+    carry_e = 0;
+    carry_m = 0;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint32_t s0 = 0; s0 < nb; s0 += 1024) {
+    uint32_t b = s0 + threadIdx.x;
+    uint2 v = b < nb ? partial[b] : make_uint2(0, 0);
+    uint32_t xe = v.x, xm = v.y;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t ye = __shfl_up_sync(0xffffffffu, xe, o), ym = __shfl_up_sync(0xffffffffu, xm, o);
+      if (lane >= o) {
+        xe += ye;
+        xm += ym;
+      }
+    }
+    if (lane == 31) {
+      we[warp] = xe;
+      wm[warp] = xm;
+    }
+    __syncthreads();
+    uint32_t pe = 0, pm = 0, te = 0, tm = 0;
+    for (int w = 0; w < 32; w++) {
+      if (w < warp) {
+        pe += we[w];
+        pm += wm[w];
+      }
+      te += we[w];
+      tm += wm[w];
+    }
+    if (b < nb) partial[b] = make_uint2(carry_e + pe + xe - v.x, carry_m + pm + xm - v.y);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      carry_e += te;
+      carry_m += tm;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    st->count[parity ^ 1] = carry_e;
+    st->insert[parity ^ 1] = st->insert[parity] - 2 * carry_m;
+    st->passes += 1;
+    st->sum_counts += count;
+  }
+}
+
+__global__ void __launch_bounds__(BLK) k_ploc_scatter(const Bvh2Node* __restrict__ cur, const int8_t* __restrict__ merge,
+                                                      const PlocState* st, int parity, const uint2* __restrict__ partial,
+                                                      Bvh2Node* __restrict__ next, Bvh2Node* __restrict__ out) {
+  const uint32_t count = st->count[parity];
+  if (count <= 1) {
+    // a pass after the root formed: carry the root to the other buffer
+    if (count == 1 && blockIdx.x == 0 && threadIdx.x == 0) st_node(&next[0], ld_node(&cur[0]));
+    return;
+  }
+  const uint32_t base = blockIdx.x * CHUNK;
+  if (base >= count) return;
+  const uint32_t ins_top = st->insert[parity];
+  bool emit[ITEMS], ism[ITEMS];
+  uint32_t best[ITEMS];
+  uint32_t e = 0, m = 0;
+  for (int k = 0; k < ITEMS; k++) {
+    uint32_t i = base + threadIdx.x * ITEMS + k;
+    emit[k] = ism[k] = false;
+    if (i < count) ploc_flags(merge, i, emit[k], ism[k], best[k]);
+    e += emit[k];
+    m += ism[k];
+  }
+  // block exclusive scan of (e, m)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t xe = e, xm = m;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t ye = __shfl_up_sync(0xffffffffu, xe, o), ym = __shfl_up_sync(0xffffffffu, xm, o);
+    if (lane >= o) {
+      xe += ye;
+      xm += ym;
+    }
+  }
+  __shared__ uint32_t we[BLK / 32], wm[BLK / 32];
+  if (lane == 31) {
+    we[warp] = xe;
+    wm[warp] = xm;
+  }
+  __syncthreads();
+  uint32_t pe = 0, pm = 0;
+  for (int w = 0; w < warp; w++) {
+    pe += we[w];
+    pm += wm[w];
+  }
+  uint2 bp = partial[blockIdx.x];
+  uint32_t epos = bp.x + pe + xe - e;
+  uint32_t mpos = bp.y + pm + xm - m;
+  for (int k = 0; k < ITEMS; k++) {
+    uint32_t i = base + threadIdx.x * ITEMS + k;
+    if (!emit[k]) continue;
+    if (ism[k]) {
+      Bvh2Node left = ld_node(&cur[i]);
+      Bvh2Node right = ld_node(&cur[best[k]]);
+      uint32_t ins = ins_top - 2 * (mpos + 1);
+      st_node(&out[ins], left);
+      st_node(&out[ins + 1], right);
+      st_node(&next[epos], make_node(box_union(node_box(left), node_box(right)), 0, ins));
+      mpos++;
+    } else {
+      st_node(&next[epos], ld_node(&cur[i]));
+    }
+    epos++;
+  }
+}
+
+// --- single-CTA tail ---------------------------------------------------------
+
+constexpr int TAIL_THREADS = 1024;
+
+__device__ __forceinline__ Box sbox(const float4* s, uint32_t j) {
+  float4 a = s[2 * j], b = s[2 * j + 1];
+  return Box{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)};
+}
+
+// Finishes every remaining pass (count <= TAIL_MAX) inside one CTA.
+__global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __restrict__ cur_g, PlocState* st, int parity,
+                                                            int radius, uint32_t depth_threshold, uint32_t max_passes,
+                                                            Bvh2Node* __restrict__ out, uint32_t* status) {
+  extern __shared__ float4 smem[];
+  float4* sa = smem;                      // TAIL_MAX nodes (2 float4 each)
+  float4* sb = smem + 2 * TAIL_MAX;       // TAIL_MAX nodes
+  int8_t* sm = reinterpret_cast<int8_t*>(smem + 4 * TAIL_MAX);
+  __shared__ uint32_t s_we[32], s_wm[32];
+  __shared__ uint32_t s_count, s_insert, s_pass;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    s_count = st->count[parity];
+    s_insert = st->insert[parity];
+    s_pass = st->passes;
+  }
+  __syncthreads();
+  uint32_t count = s_count;
+  for (uint32_t j = tid; j < count; j += TAIL_THREADS) {
+    const float4* q = reinterpret_cast<const float4*>(&cur_g[j]);
+    sa[2 * j] = q[0];
+    sa[2 * j + 1] = q[1];
+  }
+  __syncthreads();
+  float4* cur = sa;
+  float4* nxt = sb;
+  uint32_t insert = s_insert;
+  uint32_t pass = s_pass;
+  uint64_t sum = 0;
+  uint32_t iters = 0;
+  while (count > 1) {
+    if (++iters > max_passes) {
+      if (tid == 0) set_status(status, ST_ITER_LIMIT);
+      break;
+    }
+    const bool d1 = radius == 1 || pass < depth_threshold;
+    const int r = d1 ? 1 : radius;
+    // search
+    for (uint32_t i = tid; i < count; i += TAIL_THREADS) {
+      Box me = sbox(cur, i);
+      int8_t m;
+      if (d1) {
+        if (i == count - 1) {
+          m = -1;
+        } else {
+          float c = pair_cost(me, sbox(cur, i + 1));
+          float last = i == 0 ? __int_as_float(0x7f800000) : pair_cost(sbox(cur, i - 1), me);
+          m = last < c ? -1 : 1;
+        }
+      } else {
+        uint32_t begin = i >= (uint32_t)r ? i - r : 0;
+        uint32_t end = min(i + r + 1, count);
+        uint32_t best = i;
+        float bc = __int_as_float(0x7f800000);
+        for (uint32_t j = begin; j < i; j++) {
+          float c = pair_cost(sbox(cur, j), me);
+          if (c <= bc) {
+            best = j;
+            bc = c;
+          }
+        }
+        for (uint32_t j = i + 1; j < end; j++) {
+          float c = pair_cost(me, sbox(cur, j));
+          if (c <= bc) {
+            best = j;
+            bc = c;
+          }
+        }
+        m = (int8_t)((int)best - (int)i);
+      }
+      sm[i] = m;
+    }
+    __syncthreads();
+    // flags: thread tid owns items [tid*IT, tid*IT + IT)
+    constexpr int IT = TAIL_MAX / TAIL_THREADS;
+    bool emit[IT], ism[IT];
+    uint32_t bst[IT];
+    uint32_t e = 0, m = 0;
+#pragma unroll
+    for (int k = 0; k < IT; k++) {
+      uint32_t i = tid * IT + k;
+      emit[k] = ism[k] = false;
+      if (i < count) {
+        int off = sm[i];
+        uint32_t b = (uint32_t)((int)i + off);
+        bool mutual = (int)b + (int)sm[b] == (int)i;
+        emit[k] = !mutual || b < i;
+        ism[k] = mutual && b < i;
+        bst[k] = b;
+      }
+      e += emit[k];
+      m += ism[k];
+    }
+    uint32_t xe = e, xm = m;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t ye = __shfl_up_sync(0xffffffffu, xe, o), ym = __shfl_up_sync(0xffffffffu, xm, o);
+      if (lane >= o) {
+        xe += ye;
+        xm += ym;
+      }
+    }
+    if (lane == 31) {
+      s_we[warp] = xe;
+      s_wm[warp] = xm;
+    }
+    __syncthreads();
+    uint32_t pe = 0, pm = 0, te = 0, tm = 0;
+    for (int w = 0; w < 32; w++) {
+      uint32_t a = s_we[w], b = s_wm[w];
+      if (w < warp) {
+        pe += a;
+        pm += b;
+      }
+      te += a;
+      tm += b;
+    }
+    uint32_t epos = pe + xe - e, mpos = pm + xm - m;
+#pragma unroll
+    for (int k = 0; k < IT; k++) {
+      uint32_t i = tid * IT + k;
+      if (!emit[k]) continue;
+      if (ism[k]) {
+        float4 la = cur[2 * i], lb = cur[2 * i + 1];
+        float4 ra = cur[2 * bst[k]], rb = cur[2 * bst[k] + 1];
+        uint32_t ins = insert - 2 * (mpos + 1);
+        float4* o = reinterpret_cast<float4*>(&out[ins]);
+        o[0] = la;
+        o[1] = lb;
+        o[2] = ra;
+        o[3] = rb;
+        Box u = box_union(Box{make_float3(la.x, la.y, la.z), make_float3(lb.x, lb.y, lb.z)},
+                          Box{make_float3(ra.x, ra.y, ra.z), make_float3(rb.x, rb.y, rb.z)});
+        nxt[2 * epos] = make_float4(u.mn.x, u.mn.y, u.mn.z, __uint_as_float(0u));
+        nxt[2 * epos + 1] = make_float4(u.mx.x, u.mx.y, u.mx.z, __uint_as_float(ins));
+        mpos++;
+      } else {
+        nxt[2 * epos] = cur[2 * i];
+        nxt[2 * epos + 1] = cur[2 * i + 1];
+      }
+      epos++;
+    }
+    sum += count;
+    count = te;
+    insert -= 2 * tm;
+    pass++;
+    float4* t = cur;
+    cur = nxt;
+    nxt = t;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    float4* o = reinterpret_cast<float4*>(&out[0]);
+    o[0] = cur[0];
+    o[1] = cur[1];
+    st->count[parity] = count;
+    st->insert[parity] = insert;
+    st->passes = pass;
+    st->sum_counts += sum;
+  }
+}
+
+__global__ void k_root_copy(const Bvh2Node* cur, Bvh2Node* out) { st_node(&out[0], ld_node(&cur[0])); }
+
+}  // namespace
+
+// ===========================================================================
+
+int ploc_leaves(BuildCtx& c, const float* tris, const float* aabbs, const uint32_t* idx, uint32_t n, Bvh2Node* leaves,
+                int* total_keys) {
+  static const int init[6] = {0x7fffffff, 0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000, (int)0x80000000};
+  CK(cudaMemcpyAsync(total_keys, init, sizeof(init), cudaMemcpyHostToDevice, c.stream));
+  if (!n) return 0;
+  uint32_t g = div_up<uint32_t>(n, BLK);
+  c.kernel_launches++;
+  if (tris)
+    k_leaves_from_tris<<<g, BLK, 0, c.stream>>>(tris, n, leaves, total_keys, c.d_status);
+  else
+    k_leaves_from_aabbs<<<g, BLK, 0, c.stream>>>(aabbs, idx, n, leaves, total_keys, c.d_status);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int ploc_morton_codes(BuildCtx& c, const Bvh2Node* leaves, uint32_t n, const int* total_keys, int precision,
+                      void* codes) {
+  if (!n) return 0;
+  uint32_t g = div_up<uint32_t>(n, BLK);
+  c.kernel_launches++;
+  if (precision)
+    k_morton128<<<g, BLK, 0, c.stream>>>(leaves, n, total_keys, (U128*)codes);
+  else
+    k_morton64<<<g, BLK, 0, c.stream>>>(leaves, n, total_keys, (unsigned long long*)codes);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+// Stable sort of the codes in place of `codes`; *order_out = sorted order.
+int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_t** order_out) {
+  Scratch& s = c.scratch;
+  size_t kb = precision ? sizeof(U128) : sizeof(unsigned long long);
+  void* keys_alt = s.get(SLOT_KEYS_ALT, (size_t)n * kb);
+  uint32_t* vals = (uint32_t*)s.get(SLOT_VALS, (size_t)n * 4);
+  uint32_t* vals_alt = (uint32_t*)s.get(SLOT_VALS_ALT, (size_t)n * 4);
+  uint32_t* tile_hist = (uint32_t*)s.get(SLOT_TILE_HIST, (size_t)radix_tile_count(n) * 256 * 4 + 4);
+  uint32_t* all_hist = (uint32_t*)s.get(SLOT_ALL_HIST, 16 * 256 * 4);
+  if (!keys_alt || !vals || !vals_alt || !tile_hist || !all_hist) return c.fail(OBVHS_ERR_OOM, "scratch");
+  bool alt = false;
+  cudaError_t e;
+  if (precision)
+    e = radix_sort_pairs<U128>((U128*)codes, vals, n, true, (U128*)keys_alt, vals_alt, tile_hist, all_hist,
+                               c.h_hist, c.stream, &alt, &c.kernel_launches);
+  else
+    e = radix_sort_pairs<unsigned long long>((unsigned long long*)codes, vals, n, true,
+                                             (unsigned long long*)keys_alt, vals_alt, tile_hist, all_hist, c.h_hist,
+                                             c.stream, &alt, &c.kernel_launches);
+  if (e) return c.cuda_fail(e, "radix sort");
+  *order_out = alt ? vals_alt : vals;
+  return 0;
+}
+
+int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* total_keys, uint32_t radius,
+                      int precision, uint32_t depth_threshold, Bvh2Node* out_nodes, uint32_t* passes_out,
+                      uint64_t* sum_counts_out) {
+  *passes_out = 0;
+  *sum_counts_out = 0;
+  if (n == 0) return 0;
+  if (radius < 1 || radius > 32) return c.fail(OBVHS_ERR_INVALID_ARG, "search distance must be 1..32");
+  Scratch& s = c.scratch;
+  void* codes = s.get(SLOT_KEYS, (size_t)n * (precision ? sizeof(U128) : sizeof(unsigned long long)));
+  if (!codes) return c.fail(OBVHS_ERR_OOM, "scratch");
+  int r = ploc_morton_codes(c, leaves, n, total_keys, precision, codes);
+  if (r) return r;
+  uint32_t* order = nullptr;
+  r = ploc_sort_codes(c, codes, n, precision, &order);
+  if (r) return r;
+  Bvh2Node* cur = (Bvh2Node*)s.get(SLOT_PLOC_A, (size_t)n * sizeof(Bvh2Node));
+  Bvh2Node* nxt = (Bvh2Node*)s.get(SLOT_PLOC_B, (size_t)n * sizeof(Bvh2Node));
+  int8_t* merge = (int8_t*)s.get(SLOT_MERGE, (size_t)n + 64);
+  uint32_t nb_max = div_up<uint32_t>(n, CHUNK);
+  uint2* partial = (uint2*)s.get(SLOT_PARTIAL, (size_t)nb_max * sizeof(uint2) + 16);
+  PlocState* st = (PlocState*)s.get(SLOT_PLOC_STATE, sizeof(PlocState));
+  if (!cur || !nxt || !merge || !partial || !st) return c.fail(OBVHS_ERR_OOM, "scratch");
+  uint32_t g = div_up<uint32_t>(n, BLK);
+  c.kernel_launches++;
+  k_gather<<<g, BLK, 0, c.stream>>>(leaves, order, n, cur);
+  PlocState h0{};
+  h0.count[0] = n;
+  h0.insert[0] = 2 * n - 1;
+  CK(cudaMemcpyAsync(st, &h0, sizeof(PlocState), cudaMemcpyHostToDevice, c.stream));
+  if (n == 1) {
+    c.kernel_launches++;
+    k_root_copy<<<1, 1, 0, c.stream>>>(cur, out_nodes);
+    CK(cudaGetLastError());
+    return 0;
+  }
+  // multi-block passes while many clusters are live
+  int parity = 0;
+  uint32_t known = n;  // host-side upper bound on the live count
+  uint32_t pass = 0;
+  const uint32_t max_passes = 2 * n + 64;
+  while (known > TAIL_MAX) {
+    const int batch = 4;
+    for (int b = 0; b < batch; b++) {
+      int d1 = (radius == 1 || pass < depth_threshold) ? 1 : 0;
+      uint32_t gs = div_up<uint32_t>(known, BLK);
+      uint32_t gc = div_up<uint32_t>(known, CHUNK);
+      c.kernel_launches++;
+      k_ploc_search<<<gs, BLK, 0, c.stream>>>(cur, st, parity, (int)radius, d1, merge);
+      c.kernel_launches++;
+      k_ploc_count<<<gc, BLK, 0, c.stream>>>(merge, st, parity, partial);
+      c.kernel_launches++;
+      k_ploc_scan<<<1, 1024, 0, c.stream>>>(partial, st, parity);
+      c.kernel_launches++;
+      k_ploc_scatter<<<gc, BLK, 0, c.stream>>>(cur, merge, st, parity, partial, nxt, out_nodes);
+      std::swap(cur, nxt);
+      parity ^= 1;
+      pass++;
+    }
+    CK(cudaGetLastError());
+    PlocState h;
+    CK(cudaMemcpyAsync(&h, st, sizeof(PlocState), cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    known = h.count[parity];
+    pass = h.passes;
+    if (pass > max_passes) return c.fail(OBVHS_ERR_LIMIT, "PLOC pass limit");
+  }
+  if (known > 1) {
+    size_t smem = (size_t)4 * TAIL_MAX * sizeof(float4) + TAIL_MAX + 64;
+    c.kernel_launches++;
+    k_ploc_tail<<<1, TAIL_THREADS, smem, c.stream>>>(cur, st, parity, (int)radius, depth_threshold, max_passes,
+                                                     out_nodes, c.d_status);
+    CK(cudaGetLastError());
+  } else {
+    c.kernel_launches++;
+    k_root_copy<<<1, 1, 0, c.stream>>>(cur, out_nodes);
+    CK(cudaGetLastError());
+  }
+  PlocState h;
+  CK(cudaMemcpyAsync(&h, st, sizeof(PlocState), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  *passes_out = h.passes;
+  *sum_counts_out = h.sum_counts;
+  return 0;
+}
+
+int ploc_setup_kernels() {
+  size_t smem = (size_t)4 * TAIL_MAX * sizeof(float4) + TAIL_MAX + 64;
+  cudaError_t e = cudaFuncSetAttribute(k_ploc_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return e == cudaSuccess ? 0 : -1;
+}

@@ -1,0 +1,434 @@
+// presplit.cu -- spatial pre-splits of large triangles on the device.
+//
+// Reference: src/splits.rs:16-158 (split_aabbs_preset / split_aabbs_precise /
+// split_triangle) and the set-up in src/cwbvh/builder.rs:31-43.
+//
+// Each iteration of the reference walks the candidate list once (its length
+// fixed at the start of the iteration); a candidate's decision reads and
+// writes only its own box, and accepted splits append the right half (and
+// the triangle index) in candidate order.  So an iteration is one parallel
+// decision per candidate plus an order-preserving append (a scan over the
+// accept flags); the candidate list then grows by the appended entries and
+// is filtered by `half_area > thresh_low`, keeping order.
+//
+// The reference averages the triangle half areas with a sequential f32 sum;
+// rounding makes that order-dependent, so one thread sums in input order
+// while the rest of its CTA streams the next chunk into shared memory.
+#include "build.h"
+
+namespace {
+
+constexpr int BLK = 256;
+
+__device__ __forceinline__ Box tri_box(const float* t) {
+  Box b;
+  b.mn = make_float3(smin(smin(t[0], t[3]), t[6]), smin(smin(t[1], t[4]), t[7]), smin(smin(t[2], t[5]), t[8]));
+  b.mx = make_float3(smax(smax(t[0], t[3]), t[6]), smax(smax(t[1], t[4]), t[7]), smax(smax(t[2], t[5]), t[8]));
+  return b;
+}
+
+__global__ void __launch_bounds__(BLK) k_tri_boxes(const float* __restrict__ tris, uint32_t n, float* __restrict__ aabbs,
+                                                   uint32_t* __restrict__ idx, float* __restrict__ ha,
+                                                   int* largest_key, uint32_t* status) {
+  uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  float a = 0.0f;
+  if (i < n) {
+    Box b = tri_box(tris + (size_t)i * 9);
+    if (b.mn.x != b.mn.x || b.mn.y != b.mn.y || b.mn.z != b.mn.z || b.mx.x != b.mx.x || b.mx.y != b.mx.y ||
+        b.mx.z != b.mx.z)
+      set_status(status, ST_BAD_INPUT);
+    float* o = aabbs + (size_t)i * 6;
+    o[0] = b.mn.x;
+    o[1] = b.mn.y;
+    o[2] = b.mn.z;
+    o[3] = b.mx.x;
+    o[4] = b.mx.y;
+    o[5] = b.mx.z;
+    idx[i] = i;
+    a = half_area(b);
+    ha[i] = a;
+  }
+  // largest = f32::max over half areas, starting at 0
+  int k = fkey(a > 0.0f ? a : 0.0f);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) k = max(k, __shfl_xor_sync(0xffffffffu, k, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(largest_key, k);
+}
+
+// Sequential f32 sum of ha[0..n) in index order (src/cwbvh/builder.rs:36-41),
+// then the preset thresholds (src/splits.rs:23-33).
+constexpr int SUM_CHUNK = 4096;
+__global__ void __launch_bounds__(BLK) k_avg_thresholds(const float* __restrict__ ha, uint32_t n, const int* largest_key,
+                                                        float* thr) {
+  __shared__ float buf[2][SUM_CHUNK];
+  const uint32_t nch = (n + SUM_CHUNK - 1) / SUM_CHUNK;
+  float sum = 0.0f;
+  auto load = [&](uint32_t ch, int slot) {
+    uint32_t b = ch * SUM_CHUNK;
+    for (uint32_t j = threadIdx.x; j < SUM_CHUNK; j += BLK) buf[slot][j] = (b + j < n) ? ha[b + j] : 0.0f;
+  };
+  if (nch) load(0, 0);
+  __syncthreads();
+  for (uint32_t ch = 0; ch < nch; ch++) {
+    int slot = ch & 1;
+    if (threadIdx.x == 0) {
+      uint32_t b = ch * SUM_CHUNK;
+      uint32_t m = min((uint32_t)SUM_CHUNK, n - b);
+      const float* p = buf[slot];
+      for (uint32_t j = 0; j < m; j++) sum = __fadd_rn(sum, p[j]);
+    } else if (threadIdx.x >= 32 && ch + 1 < nch) {
+      uint32_t b = (ch + 1) * SUM_CHUNK;
+      for (uint32_t j = threadIdx.x - 32; j < SUM_CHUNK; j += BLK - 32)
+        buf[slot ^ 1][j] = (b + j < n) ? ha[b + j] : 0.0f;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    float avg = sum / (float)n;
+    float largest = fkey_inv(*largest_key);
+    float hi_a = avg * 4.0f, hi_b = avg * 0.9f + largest * 0.1f;
+    thr[0] = avg * 3.0f;                  // area_thresh_low
+    thr[1] = fmaxf(hi_a, hi_b);           // area_thresh_high (f32::max)
+    thr[2] = avg;
+    thr[3] = largest;
+  }
+}
+
+// split_triangle (src/splits.rs:127-158).
+__device__ __forceinline__ float comp(const float3& v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
+__device__ __forceinline__ void extend(Box& b, const float3& p) {
+  b.mn = make_float3(smin(b.mn.x, p.x), smin(b.mn.y, p.y), smin(b.mn.z, p.z));
+  b.mx = make_float3(smax(b.mx.x, p.x), smax(b.mx.y, p.y), smax(b.mx.z, p.z));
+}
+__device__ __forceinline__ void split_triangle(int dim, float pos, const float3 v[4], Box& left, Box& right) {
+  const float M = 3.40282347e+38f;
+  left = Box{make_float3(M, M, M), make_float3(-M, -M, -M)};
+  right = left;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const float3 v0 = v[i], v1 = v[i + 1];
+    const float v0d = comp(v0, dim), v1d = comp(v1, dim);
+    if (v0d <= pos) extend(left, v0);
+    if (v0d >= pos) extend(right, v0);
+    if ((v0d < pos && pos < v1d) || (v1d < pos && pos < v0d)) {
+      const float inv_length = 1.0f / (v1d - v0d);
+      const float s = (pos - v0d) * inv_length;
+      // Vec3A::mul_add is a fused multiply-add
+      const float3 c = make_float3(__fmaf_rn(s, v1.x - v0.x, v0.x), __fmaf_rn(s, v1.y - v0.y, v0.y),
+                                   __fmaf_rn(s, v1.z - v0.z, v0.z));
+      extend(left, c);
+      extend(right, c);
+    }
+  }
+}
+
+__device__ __forceinline__ Box ld_box6(const float* a) {
+  return Box{make_float3(a[0], a[1], a[2]), make_float3(a[3], a[4], a[5])};
+}
+__device__ __forceinline__ void st_box6(float* a, const Box& b) {
+  a[0] = b.mn.x;
+  a[1] = b.mn.y;
+  a[2] = b.mn.z;
+  a[3] = b.mx.x;
+  a[4] = b.mx.y;
+  a[5] = b.mx.z;
+}
+__device__ __forceinline__ void set_comp(float3& v, int a, float x) {
+  if (a == 0) v.x = x;
+  else if (a == 1) v.y = x;
+  else v.z = x;
+}
+
+// One iteration's decision for every candidate (src/splits.rs:72-115).
+__global__ void __launch_bounds__(BLK) k_split(const uint32_t* __restrict__ cand, uint32_t ncand, float* __restrict__ aabbs,
+                                               const uint32_t* __restrict__ idx, const float* __restrict__ tris,
+                                               const float* __restrict__ thr, float* __restrict__ right_out,
+                                               uint32_t* __restrict__ flag) {
+  uint32_t k = blockIdx.x * BLK + threadIdx.x;
+  if (k >= ncand) return;
+  const uint32_t ai = cand[k];
+  const Box box = ld_box6(aabbs + (size_t)ai * 6);
+  const uint32_t ti = idx[ai];
+  float dx = box.mx.x - box.mn.x, dy = box.mx.y - box.mn.y, dz = box.mx.z - box.mn.z;
+  int axis = dx < dy ? (dy < dz ? 2 : 1) : (dx < dz ? 2 : 0);
+  const float* t = tris + (size_t)ti * 9;
+  float3 verts[4] = {make_float3(t[0], t[1], t[2]), make_float3(t[3], t[4], t[5]), make_float3(t[6], t[7], t[8]),
+                     make_float3(t[0], t[1], t[2])};
+  float best = 3.40282347e+38f;
+  Box left = box, right = box;
+  for (uint32_t i = 1; i < 12; i++) {
+    float nf = (float)i / 12.0f;
+    float pos = comp(box.mn, axis) * nf + comp(box.mx, axis) * (1.0f - nf);
+    Box tl = box, tr = box;
+    set_comp(tl.mx, axis, pos);
+    set_comp(tr.mn, axis, pos);
+    Box sl, sr;
+    split_triangle(axis, pos, verts, sl, sr);
+    tl = box_isect(sl, tl);
+    tr = box_isect(sr, tr);
+    float area = half_area(tl) + half_area(tr);
+    if (area < best) {
+      best = area;
+      left = tl;
+      right = tr;
+    }
+  }
+  const float old_cost = half_area(box);
+  const bool accept = (thr[1] > old_cost && best * 1.6f < old_cost) || best * 1.8f < old_cost;
+  if (accept) {
+    st_box6(aabbs + (size_t)ai * 6, left);
+    st_box6(right_out + (size_t)k * 6, right);
+  }
+  flag[k] = accept ? 1u : 0u;
+}
+
+// --- small order-preserving scan (per-block counts, one-block scan, apply) ---
+constexpr int ITEMS = 4;
+constexpr int CHUNK = BLK * ITEMS;
+
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  uint32_t pre = 0, tot = 0;
+  for (int w = 0; w < BLK / 32; w++) {
+    if (w < warp) pre += s_warp[w];
+    tot += s_warp[w];
+  }
+  __syncthreads();
+  if (total) *total = tot;
+  return pre + x - v;
+}
+
+__global__ void __launch_bounds__(BLK) k_count_flags(const uint32_t* __restrict__ flag, uint32_t n, uint32_t* partial) {
+  __shared__ uint32_t s_warp[BLK / 32];
+  uint32_t base = blockIdx.x * CHUNK, c = 0;
+  for (int k = 0; k < ITEMS; k++) {
+    uint32_t i = base + threadIdx.x * ITEMS + k;
+    if (i < n) c += flag[i];
+  }
+  uint32_t tot;
+  block_excl_scan(c, s_warp, &tot);
+  if (threadIdx.x == 0) partial[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_partials(uint32_t* partial, uint32_t nb, uint32_t* total) {
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint32_t s0 = 0; s0 < nb; s0 += 1024) {
+    uint32_t b = s0 + threadIdx.x;
+    uint32_t v = b < nb ? partial[b] : 0;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    uint32_t pre = 0, tot = 0;
+    for (int w = 0; w < 32; w++) {
+      if (w < warp) pre += s_warp[w];
+      tot += s_warp[w];
+    }
+    if (b < nb) partial[b] = carry + pre + x - v;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+// Append accepted right halves at len + rank, in candidate order.
+__global__ void __launch_bounds__(BLK) k_append(const uint32_t* __restrict__ flag, const uint32_t* __restrict__ partial,
+                                                uint32_t ncand, const uint32_t* __restrict__ cand,
+                                                const float* __restrict__ right, uint32_t len, float* __restrict__ aabbs,
+                                                uint32_t* __restrict__ idx, uint32_t* __restrict__ new_cand) {
+  __shared__ uint32_t s_warp[BLK / 32];
+  uint32_t base = blockIdx.x * CHUNK, c = 0;
+  uint32_t f[ITEMS];
+  for (int k = 0; k < ITEMS; k++) {
+    uint32_t i = base + threadIdx.x * ITEMS + k;
+    f[k] = i < ncand ? flag[i] : 0;
+    c += f[k];
+  }
+  uint32_t pos = partial[blockIdx.x] + block_excl_scan(c, s_warp, nullptr);
+  for (int k = 0; k < ITEMS; k++) {
+    uint32_t i = base + threadIdx.x * ITEMS + k;
+    if (!f[k]) continue;
+    uint32_t dst = len + pos;
+    const float* r = right + (size_t)i * 6;
+    float* o = aabbs + (size_t)dst * 6;
+    for (int j = 0; j < 6; j++) o[j] = r[j];
+    idx[dst] = idx[cand[i]];
+    new_cand[pos] = dst;
+    pos++;
+  }
+}
+
+// retain: keep candidates whose box half area exceeds thresh_low, in order.
+__global__ void __launch_bounds__(BLK) k_keep_flags(const uint32_t* __restrict__ cand, uint32_t n,
+                                                    const float* __restrict__ aabbs, const float* __restrict__ thr,
+                                                    uint32_t* __restrict__ flag) {
+  uint32_t k = blockIdx.x * BLK + threadIdx.x;
+  if (k >= n) return;
+  flag[k] = half_area(ld_box6(aabbs + (size_t)cand[k] * 6)) > thr[0] ? 1u : 0u;
+}
+
+__global__ void __launch_bounds__(BLK) k_initial_flags(const float* __restrict__ ha, uint32_t n,
+                                                       const float* __restrict__ thr, uint32_t* __restrict__ flag,
+                                                       uint32_t* __restrict__ ids) {
+  uint32_t k = blockIdx.x * BLK + threadIdx.x;
+  if (k >= n) return;
+  flag[k] = ha[k] > thr[0] ? 1u : 0u;
+  ids[k] = k;
+}
+
+__global__ void __launch_bounds__(BLK) k_compact(const uint32_t* __restrict__ flag, const uint32_t* __restrict__ partial,
+                                                 uint32_t n, const uint32_t* __restrict__ in, uint32_t* __restrict__ out) {
+  __shared__ uint32_t s_warp[BLK / 32];
+  uint32_t base = blockIdx.x * CHUNK, c = 0;
+  uint32_t f[ITEMS];
+  for (int k = 0; k < ITEMS; k++) {
+    uint32_t i = base + threadIdx.x * ITEMS + k;
+    f[k] = i < n ? flag[i] : 0;
+    c += f[k];
+  }
+  uint32_t pos = partial[blockIdx.x] + block_excl_scan(c, s_warp, nullptr);
+  for (int k = 0; k < ITEMS; k++) {
+    uint32_t i = base + threadIdx.x * ITEMS + k;
+    if (f[k]) out[pos++] = in[i];
+  }
+}
+
+}  // namespace
+
+// Order-preserving compaction of in[0..n) by flag; returns the kept count.
+static int compact(BuildCtx& c, const uint32_t* flag, uint32_t n, const uint32_t* in, uint32_t* out, uint32_t* partial,
+                   uint32_t* d_total, uint32_t* kept) {
+  *kept = 0;
+  if (!n) return 0;
+  uint32_t nb = div_up<uint32_t>(n, CHUNK);
+  c.kernel_launches++;
+  k_count_flags<<<nb, BLK, 0, c.stream>>>(flag, n, partial);
+  c.kernel_launches++;
+  k_scan_partials<<<1, 1024, 0, c.stream>>>(partial, nb, d_total);
+  c.kernel_launches++;
+  k_compact<<<nb, BLK, 0, c.stream>>>(flag, partial, n, in, out);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(c.h_small, d_total, 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  *kept = *(uint32_t*)c.h_small;
+  return 0;
+}
+
+// Grows a scratch slot to `need` bytes keeping its first `used` bytes.
+static int grow_keep(BuildCtx& c, int slot, size_t need, size_t used) {
+  Scratch& s = c.scratch;
+  if (s.cap[slot] >= need) return 0;
+  void* p = nullptr;
+  size_t want = need + need / 2;
+  if (cudaMalloc(&p, want) != cudaSuccess) {
+    cudaGetLastError();
+    return c.fail(OBVHS_ERR_OOM, "pre-split growth");
+  }
+  if (used && s.ptr[slot]) {
+    CK(cudaMemcpyAsync(p, s.ptr[slot], used, cudaMemcpyDeviceToDevice, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+  }
+  if (s.ptr[slot]) cudaFree(s.ptr[slot]);
+  s.total += want - s.cap[slot];
+  s.ptr[slot] = p;
+  s.cap[slot] = want;
+  return 0;
+}
+
+int presplit_device(BuildCtx& c, const float* tris, uint32_t n, float** aabbs_out, uint32_t** idx_out,
+                    uint32_t* m_out) {
+  Scratch& s = c.scratch;
+  *m_out = 0;
+  if (n == 0) return 0;
+  size_t cap = (size_t)n + n / 4 + 1024;
+  float* misc = (float*)s.get(SLOT_SPLIT_MISC, 64);
+  float* ha = (float*)s.get(SLOT_INPUT2, (size_t)n * 4);
+  if (!misc || !ha) return c.fail(OBVHS_ERR_OOM, "scratch");
+  int r;
+  if ((r = grow_keep(c, SLOT_SPLIT_AABBS, cap * 24, 0)) || (r = grow_keep(c, SLOT_SPLIT_IDX, cap * 4, 0)) ||
+      (r = grow_keep(c, SLOT_SPLIT_CAND, (size_t)n * 4, 0)) || (r = grow_keep(c, SLOT_SPLIT_CAND2, (size_t)n * 4, 0)) ||
+      (r = grow_keep(c, SLOT_FLAGS, (size_t)n * 4, 0)) ||
+      (r = grow_keep(c, SLOT_PARTIAL, ((size_t)n / CHUNK + 2) * 8, 0)))
+    return r;
+  float* thr = misc;  // [0] low [1] high [2] avg [3] largest
+  int* largest_key = (int*)(misc + 8);
+  uint32_t* d_total = (uint32_t*)(misc + 9);
+  int zero_key = 0;
+  CK(cudaMemcpyAsync(largest_key, &zero_key, 4, cudaMemcpyHostToDevice, c.stream));
+  uint32_t g = div_up<uint32_t>(n, BLK);
+  c.kernel_launches++;
+  k_tri_boxes<<<g, BLK, 0, c.stream>>>(tris, n, (float*)s.ptr[SLOT_SPLIT_AABBS], (uint32_t*)s.ptr[SLOT_SPLIT_IDX], ha,
+                                        largest_key, c.d_status);
+  c.kernel_launches++;
+  k_avg_thresholds<<<1, BLK, 0, c.stream>>>(ha, n, largest_key, thr);
+  c.kernel_launches++;
+  k_initial_flags<<<g, BLK, 0, c.stream>>>(ha, n, thr, (uint32_t*)s.ptr[SLOT_FLAGS], (uint32_t*)s.ptr[SLOT_SPLIT_CAND2]);
+  CK(cudaGetLastError());
+  uint32_t ncand = 0;
+  r = compact(c, (uint32_t*)s.ptr[SLOT_FLAGS], n, (uint32_t*)s.ptr[SLOT_SPLIT_CAND2], (uint32_t*)s.ptr[SLOT_SPLIT_CAND],
+              (uint32_t*)s.ptr[SLOT_PARTIAL], d_total, &ncand);
+  if (r) return r;
+  uint32_t len = n;
+  for (int it = 0; it < 12 && ncand; it++) {
+    // room for every candidate to split once
+    const size_t c2 = (size_t)ncand * 2;
+    if ((r = grow_keep(c, SLOT_SPLIT_AABBS, ((size_t)len + ncand) * 24, (size_t)len * 24)) ||
+        (r = grow_keep(c, SLOT_SPLIT_IDX, ((size_t)len + ncand) * 4, (size_t)len * 4)) ||
+        (r = grow_keep(c, SLOT_SPLIT_CAND, c2 * 4, (size_t)ncand * 4)) || (r = grow_keep(c, SLOT_SPLIT_CAND2, c2 * 4, 0)) ||
+        (r = grow_keep(c, SLOT_FLAGS, c2 * 4, 0)) || (r = grow_keep(c, SLOT_REINS, (size_t)ncand * 24, 0)) ||
+        (r = grow_keep(c, SLOT_PARTIAL, (c2 / CHUNK + 2) * 8, 0)))
+      return r;
+    float* aabbs = (float*)s.ptr[SLOT_SPLIT_AABBS];
+    uint32_t* idx = (uint32_t*)s.ptr[SLOT_SPLIT_IDX];
+    uint32_t* cand = (uint32_t*)s.ptr[SLOT_SPLIT_CAND];
+    uint32_t* cand2 = (uint32_t*)s.ptr[SLOT_SPLIT_CAND2];
+    uint32_t* flag = (uint32_t*)s.ptr[SLOT_FLAGS];
+    float* right = (float*)s.ptr[SLOT_REINS];
+    uint32_t* partial = (uint32_t*)s.ptr[SLOT_PARTIAL];
+    c.kernel_launches++;
+    k_split<<<div_up<uint32_t>(ncand, BLK), BLK, 0, c.stream>>>(cand, ncand, aabbs, idx, tris, thr, right, flag);
+    uint32_t nb = div_up<uint32_t>(ncand, CHUNK);
+    c.kernel_launches++;
+    k_count_flags<<<nb, BLK, 0, c.stream>>>(flag, ncand, partial);
+    c.kernel_launches++;
+    k_scan_partials<<<1, 1024, 0, c.stream>>>(partial, nb, d_total);
+    // the appended entries become candidates after the current ones
+    c.kernel_launches++;
+    k_append<<<nb, BLK, 0, c.stream>>>(flag, partial, ncand, cand, right, len, aabbs, idx, cand + ncand);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(c.h_small, d_total, 4, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    uint32_t added = *(uint32_t*)c.h_small;
+    if (added == 0) break;
+    len += added;
+    uint32_t total = ncand + added;
+    c.kernel_launches++;
+    k_keep_flags<<<div_up<uint32_t>(total, BLK), BLK, 0, c.stream>>>(cand, total, aabbs, thr, flag);
+    CK(cudaGetLastError());
+    r = compact(c, flag, total, cand, cand2, partial, d_total, &ncand);
+    if (r) return r;
+    std::swap(s.ptr[SLOT_SPLIT_CAND], s.ptr[SLOT_SPLIT_CAND2]);
+    std::swap(s.cap[SLOT_SPLIT_CAND], s.cap[SLOT_SPLIT_CAND2]);
+  }
+  *aabbs_out = (float*)s.ptr[SLOT_SPLIT_AABBS];
+  *idx_out = (uint32_t*)s.ptr[SLOT_SPLIT_IDX];
+  *m_out = len;
+  return 0;
+}

@@ -1,0 +1,284 @@
+// traverse.cu -- CWBVH closest-hit and occlusion traversal on the device.
+//
+// Reference: the traverse! macro (src/cwbvh/traverse_macro.rs:59-126),
+// CwBvh::ray_traverse (src/cwbvh/mod.rs:169-198) and ray_traverse_miss
+// (:201-225), CwBvhNode::intersect_ray / get_child_and_index_bits
+// (src/cwbvh/node.rs:86-231, simd.rs:17-100), ray_get_octant_inv4
+// (src/cwbvh/mod.rs:1001-1010), Triangle::intersect (src/triangle.rs:35-76),
+// Ray::new / safe_inverse (src/ray.rs:6-57).
+//
+// Each ray follows the reference's loop step for step: the same group stack
+// (32 entries, clamped like StackStack), the same child priority from the
+// octant, the same primitive order inside a leaf group, and the same float
+// operations, so hit ids and t are bit-identical to the reference's.
+//
+// Layout: nodes are the 80-byte CwBvhNode (five 16-byte loads); triangles
+// are stored in primitive_indices order as four float4: (v0, original id),
+// (v0-v1, n.x), (v2-v0, n.y), (n.z, -, -, -) with n = (v0-v1) x (v2-v0),
+// the values Triangle::intersect computes per test.  Rays are 32 bytes
+// (origin, tmin, dir, tmax); results are 8 bytes (original id, t).
+// Persistent warps take 32 rays at a time from a global counter.
+#include "build.h"
+
+namespace {
+
+constexpr int TBLK = 128;
+
+__device__ __forceinline__ float safe_inverse(float x) {
+  const float eps = 1.1920929e-07f;
+  if (fabsf(x) <= eps) {
+    float s = x != x ? x : (signbit(x) ? -1.0f : 1.0f);
+    return s / eps;
+  }
+  return 1.0f / x;
+}
+
+__device__ __forceinline__ uint32_t byte_of(uint32_t w, int b) { return (w >> (8 * b)) & 0xffu; }
+
+struct NodeQ {
+  uint4 q0, q1, q2, q3, q4;
+};
+
+__device__ __forceinline__ NodeQ load_cw(const CwNode* nodes, uint32_t i) {
+  const uint4* p = nodes[i].q;
+  NodeQ n;
+  n.q0 = __ldg(p);
+  n.q1 = __ldg(p + 1);
+  n.q2 = __ldg(p + 2);
+  n.q3 = __ldg(p + 3);
+  n.q4 = __ldg(p + 4);
+  return n;
+}
+
+// CwBvhNode::intersect_ray -> 32-bit hit mask (hi 8 bits: inner children by
+// traversal priority; lo 24 bits: primitive bits).
+__device__ __forceinline__ uint32_t intersect_node(const NodeQ& n, float3 o, float3 d, float3 inv, float tmax,
+                                                   uint32_t oct_inv4) {
+  const float px = __uint_as_float(n.q0.x), py = __uint_as_float(n.q0.y), pz = __uint_as_float(n.q0.z);
+  const float ex = __uint_as_float(byte_of(n.q0.w, 0) << 23);
+  const float ey = __uint_as_float(byte_of(n.q0.w, 1) << 23);
+  const float ez = __uint_as_float(byte_of(n.q0.w, 2) << 23);
+  const float aix = ex * inv.x, aiy = ey * inv.y, aiz = ez * inv.z;
+  const float aox = (px - o.x) * inv.x, aoy = (py - o.y) * inv.y, aoz = (pz - o.z) * inv.z;
+  const bool rdx = d.x < 0.0f, rdy = d.y < 0.0f, rdz = d.z < 0.0f;
+  // get_child_and_index_bits (src/cwbvh/node.rs:207-231)
+  unsigned long long oct8 = oct_inv4;
+  oct8 |= oct8 << 32;
+  const unsigned long long meta8 = (unsigned long long)n.q1.z | ((unsigned long long)n.q1.w << 32);
+  const unsigned long long is_inner8 = (meta8 & (meta8 << 1)) & 0x1010101010101010ull;
+  const unsigned long long inner_mask8 = (is_inner8 >> 4) * 0xffull;
+  const unsigned long long bit_index8 = (meta8 ^ (oct8 & inner_mask8)) & 0x1f1f1f1f1f1f1f1full;
+  const unsigned long long child_bits8 = (meta8 >> 5) & 0x0707070707070707ull;
+  uint32_t hit = 0;
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const int w = c >> 2, b = c & 3;
+    const float xlo = (float)byte_of(w ? n.q2.y : n.q2.x, b), xhi = (float)byte_of(w ? n.q2.w : n.q2.z, b);
+    const float ylo = (float)byte_of(w ? n.q3.y : n.q3.x, b), yhi = (float)byte_of(w ? n.q3.w : n.q3.z, b);
+    const float zlo = (float)byte_of(w ? n.q4.y : n.q4.x, b), zhi = (float)byte_of(w ? n.q4.w : n.q4.z, b);
+    const float xmin = rdx ? xhi : xlo, xmax = rdx ? xlo : xhi;
+    const float ymin = rdy ? yhi : ylo, ymax = rdy ? ylo : yhi;
+    const float zmin = rdz ? zhi : zlo, zmax = rdz ? zlo : zhi;
+    const float tminx = xmin * aix + aox, tmaxx = xmax * aix + aox;
+    const float tminy = ymin * aiy + aoy, tmaxy = ymax * aiy + aoy;
+    const float tminz = zmin * aiz + aoz, tmaxz = zmax * aiz + aoz;
+    float tmn = smax(tminx, smax(tminy, tminz));
+    float tmx = smin(tmaxx, smin(tmaxy, tmaxz));
+    tmn = smax(tmn, 0.0001f);
+    tmx = smin(tmx, tmax);
+    if (tmn <= tmx) {
+      const uint32_t cb = (uint32_t)(child_bits8 >> (c * 8)) & 0xffu;
+      const uint32_t bi = (uint32_t)(bit_index8 >> (c * 8)) & 0xffu;
+      hit |= cb << bi;
+    }
+  }
+  return hit;
+}
+
+// Triangle::intersect with precomputed e1, e2, n; returns t or +inf.
+__device__ __forceinline__ float intersect_tri(const float4* tri, float3 o, float3 d, float tmin, float tmax,
+                                               uint32_t* orig_id) {
+  const float4 a = __ldg(tri), b = __ldg(tri + 1), c4 = __ldg(tri + 2), e = __ldg(tri + 3);
+  *orig_id = __float_as_uint(a.w);
+  const float3 e1 = make_float3(b.x, b.y, b.z), e2 = make_float3(c4.x, c4.y, c4.z);
+  const float3 n = make_float3(b.w, c4.w, e.x);
+  const float3 c = make_float3(a.x - o.x, a.y - o.y, a.z - o.z);
+  const float3 r = make_float3(d.y * c.z - d.z * c.y, d.z * c.x - d.x * c.z, d.x * c.y - d.y * c.x);
+  const float inv_det = 1.0f / ((n.x * d.x + n.y * d.y) + n.z * d.z);
+  const float u = ((r.x * e2.x + r.y * e2.y) + r.z * e2.z) * inv_det;
+  const float v = ((r.x * e1.x + r.y * e1.y) + r.z * e1.z) * inv_det;
+  const float w = (1.0f - u) - v;
+  const uint32_t h = __float_as_uint(u) | __float_as_uint(v) | __float_as_uint(w);
+  if (inv_det != 0.0f && (h & 0x80000000u) == 0) {
+    const float t = ((n.x * c.x + n.y * c.y) + n.z * c.z) * inv_det;
+    if (t >= tmin && t <= tmax) return t;
+  }
+  return __int_as_float(0x7f800000);
+}
+
+template <int MODE>  // 0 closest hit, 1 occlusion
+__global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ nodes, uint32_t n_nodes,
+                                                   const float4* __restrict__ tris, uint32_t n_prims,
+                                                   const float4* __restrict__ rays,
+                                                   uint32_t nrays, uint2* __restrict__ hits, uint8_t* __restrict__ miss,
+                                                   uint32_t* __restrict__ next_ray, uint32_t* status) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(next_ray, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= nrays) return;
+    const uint32_t ri = base + lane;
+    if (ri >= nrays) continue;
+    const float4 r0 = __ldg(&rays[2 * ri]), r1 = __ldg(&rays[2 * ri + 1]);
+    const float3 o = make_float3(r0.x, r0.y, r0.z), d = make_float3(r1.x, r1.y, r1.z);
+    const float tmin = r0.w, ray_tmax = r1.w;
+    const float3 inv = make_float3(safe_inverse(d.x), safe_inverse(d.y), safe_inverse(d.z));
+    const uint32_t oct = (d.x < 0.0f ? 0u : 0x04040404u) | (d.y < 0.0f ? 0u : 0x02020202u) |
+                         (d.z < 0.0f ? 0u : 0x01010101u);
+    float tmax = ray_tmax;
+    uint32_t hit_id = OBVHS_INVALID;
+    float hit_t = __int_as_float(0x7f800000);
+    uint2 stack[32];
+    uint32_t sp = 0;
+    uint2 cur = n_nodes ? make_uint2(0u, 0x80000000u) : make_uint2(0u, 0u);
+    uint2 prim = make_uint2(0u, 0u);
+    bool done = false;
+    uint32_t guard = 0;
+    while (!done) {
+      if (++guard > (1u << 24)) {
+        set_status(status, ST_ITER_LIMIT);
+        break;
+      }
+      while (prim.y != 0) {
+        const uint32_t lpi = 31u - __clz(prim.y);
+        prim.y &= ~(1u << lpi);
+        const uint32_t pid = prim.x + lpi;
+        if (pid >= n_prims) {
+          set_status(status, ST_BAD_TREE);
+          done = true;
+          break;
+        }
+        uint32_t orig;
+        const float t = intersect_tri(&tris[4 * (size_t)pid], o, d, tmin, MODE == 0 ? tmax : ray_tmax, &orig);
+        if (MODE == 0) {
+          if (t < tmax) {
+            hit_id = orig;
+            hit_t = t;
+            tmax = t;
+          }
+        } else if (t < ray_tmax) {
+          hit_id = orig;
+          hit_t = t;
+          done = true;
+          break;
+        }
+      }
+      if (done) break;
+      prim = make_uint2(0u, 0u);
+      if (cur.y & 0xff000000u) {
+        const uint32_t hits_imask = cur.y;
+        const uint32_t cio = 31u - __clz(hits_imask);
+        const uint32_t cbase = cur.x;
+        cur.y &= ~(1u << cio);
+        if (cur.y & 0xff000000u) {
+          stack[sp] = cur;
+          sp = min(sp + 1, 31u);
+        }
+        const uint32_t slot = (cio - 24) ^ (oct & 0xffu);
+        const uint32_t rel = __popc(hits_imask & ~(0xffffffffu << slot));
+        const uint32_t ni = cbase + rel;
+        if (ni >= n_nodes) {
+          set_status(status, ST_BAD_TREE);
+          break;
+        }
+        const NodeQ node = load_cw(nodes, ni);
+        const uint32_t hm = intersect_node(node, o, d, inv, MODE == 0 ? tmax : ray_tmax, oct);
+        cur.x = node.q1.x;
+        prim.x = node.q1.y;
+        cur.y = (hm & 0xff000000u) | byte_of(node.q0.w, 3);
+        prim.y = hm & 0x00ffffffu;
+      } else {
+        cur = make_uint2(0u, 0u);
+      }
+      if (prim.y == 0 && (cur.y & 0xff000000u) == 0) {
+        if (sp == 0) break;
+        sp = sp ? sp - 1 : 0;
+        cur = stack[sp];
+      }
+    }
+    if (MODE == 0)
+      hits[ri] = make_uint2(hit_id, __float_as_uint(hit_t));
+    else
+      miss[ri] = hit_id == OBVHS_INVALID ? 1 : 0;
+  }
+}
+
+__global__ void k_reorder_tris(const float* __restrict__ tris, uint32_t n_tris, const uint32_t* __restrict__ pidx,
+                               uint32_t n_prims, float4* __restrict__ out, uint32_t* status) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_prims) return;
+  uint32_t id = pidx[k];
+  if (id >= n_tris) {
+    set_status(status, ST_BAD_TREE);
+    id = 0;
+  }
+  const float* t = tris + (size_t)id * 9;
+  const float3 v0 = make_float3(t[0], t[1], t[2]), v1 = make_float3(t[3], t[4], t[5]), v2 = make_float3(t[6], t[7], t[8]);
+  const float3 e1 = make_float3(v0.x - v1.x, v0.y - v1.y, v0.z - v1.z);
+  const float3 e2 = make_float3(v2.x - v0.x, v2.y - v0.y, v2.z - v0.z);
+  const float3 n = make_float3(e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x);
+  out[4 * (size_t)k] = make_float4(v0.x, v0.y, v0.z, __uint_as_float(pidx[k]));
+  out[4 * (size_t)k + 1] = make_float4(e1.x, e1.y, e1.z, n.x);
+  out[4 * (size_t)k + 2] = make_float4(e2.x, e2.y, e2.z, n.y);
+  out[4 * (size_t)k + 3] = make_float4(n.z, 0.0f, 0.0f, 0.0f);
+}
+
+}  // namespace
+
+int reorder_tris_device(BuildCtx& c, obvhs_cwbvh* b, const float* tris, uint32_t n_tris) {
+  if (b->tris) {
+    cudaFree(b->tris);
+    b->tris = nullptr;
+  }
+  b->n_tris = n_tris;
+  if (b->n_prims == 0) return 0;
+  float4* out = nullptr;
+  if (cudaMalloc(&out, (size_t)b->n_prims * 64) != cudaSuccess) {
+    cudaGetLastError();
+    return c.fail(OBVHS_ERR_OOM, "triangle buffer");
+  }
+  c.kernel_launches++;
+  k_reorder_tris<<<div_up<uint32_t>(b->n_prims, 256), 256, 0, c.stream>>>(tris, n_tris, b->prim_indices, b->n_prims,
+                                                                          out, c.d_status);
+  CK(cudaGetLastError());
+  b->tris = out;
+  return 0;
+}
+
+int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint32_t n, uint32_t* hits, uint8_t* miss,
+                    int mode) {
+  if (n == 0) return 0;
+  if (bvh->n_nodes && !bvh->tris) return c.fail(OBVHS_ERR_INVALID_ARG, "no triangles attached to the CWBVH");
+  uint32_t* counter = (uint32_t*)c.scratch.get(SLOT_OUTPUT, 16);
+  if (!counter) return c.fail(OBVHS_ERR_OOM, "scratch");
+  CK(cudaMemsetAsync(counter, 0, 4, c.stream));
+  static int per_sm = 0;
+  if (!per_sm) {
+    int a = 0, b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_traverse<0>, TBLK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_traverse<1>, TBLK, 0);
+    per_sm = std::max(1, std::min(a, b));
+  }
+  uint32_t want = div_up<uint32_t>(n, TBLK);
+  uint32_t grid = std::min<uint32_t>(want, (uint32_t)(per_sm * c.num_sms));
+  c.kernel_launches++;
+  if (mode == 0)
+    k_traverse<0><<<grid, TBLK, 0, c.stream>>>(bvh->nodes, bvh->n_nodes, bvh->tris, bvh->n_prims, (const float4*)rays, n,
+                                               (uint2*)hits, nullptr, counter, c.d_status);
+  else
+    k_traverse<1><<<grid, TBLK, 0, c.stream>>>(bvh->nodes, bvh->n_nodes, bvh->tris, bvh->n_prims, (const float4*)rays, n, nullptr,
+                                               miss, counter, c.d_status);
+  CK(cudaGetLastError());
+  return 0;
+}

@@ -358,7 +358,8 @@ inline int8_t find_best_node(size_t index, const Node* nodes, size_t count, size
   const Aabb& ours = nodes[index].box;
   for (size_t other = begin; other < end; other++) {
     if (other == index) continue;
-    float c = half_area(uni(ours, nodes[other].box));
+    // SearchCache holds union(A_lo, A_hi) for lo < hi (src/ploc/mod.rs:612-619)
+    float c = other < index ? half_area(uni(nodes[other].box, ours)) : half_area(uni(ours, nodes[other].box));
     if (c <= best_cost) {
       best = other;
       best_cost = c;
