@@ -1,0 +1,355 @@
+#!/usr/bin/env python
+"""Benchmark of the BVH hot path on the 1M-triangle clustered scene.
+
+Workload (one "step"): build_cwbvh_from_tris on 1,000,000 triangles in 64
+Gaussian clusters with the slow_build preset (pre-splits, PLOC radius 24 with
+distance 1 for 2 passes, reinsertion ratio 0.2, U128 Morton keys, 3 primitives
+per leaf), plus, timed separately, closest-hit traversal of the 1920x1080
+primary rays and of one cosine-weighted bounce ray per primary hit.
+
+  value       build throughput, Mtris/s, triangles already in HBM
+  e2e         the same build through the public API from pinned host
+              triangles, host->device copy and the CWBVH download included
+  traversal   Mrays/s of the primary and bounce batches (device-resident rays)
+  roofline    the dominant kernel of the step against the measured HBM peak
+  cpu_baseline the C++ restatement of the reference (oracle) on all host cores
+
+--impl reference runs that CPU restatement of the reference's algorithm (the
+Rust crate itself cannot be built on these machines) on the same workload.
+Multi-GPU: every rank builds its own replica (the path does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "PLOC build Mtris/s; CWBVH Mrays/s closest-hit; served p50/p99 latency"
+WORKLOAD = "clustered-1M-slow_build"
+N_TRIS = 1_000_000
+L2_FLUSH_BYTES = 512 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--tris", type=int, default=N_TRIS)
+    return ap.parse_args()
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (clocks and throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload(n):
+    from obvhs_gb300 import scenes as S
+
+    return S.scene2_tris(n), S.scene2_primary_rays()
+
+
+def cpu_build_rate(tris, params, reps, nthreads):
+    """Oracle builds of the full scene on `nthreads` host threads: Mtris/s."""
+    from oracle import oracle as O
+
+    t = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        O.build(tris=tris, params=params, nthreads=nthreads, keep_intermediate=False)
+        t.append(time.perf_counter() - t0)
+    return len(tris) / (sum(t) / len(t)) / 1e6, t
+
+
+def cpu_baseline(tris, params, rays, cores, ctx):
+    """The oracle: two builds, and the primary rays traced on the GPU-built
+    tree with visit/test counters (all host threads)."""
+    from oracle import oracle as O
+
+    rate, times = cpu_build_rate(tris, params, 2, cores)
+    import obvhs_gb300 as G
+
+    cw = G.build_cwbvh_from_tris(tris, params, ctx=ctx)
+    nodes, pidx = cw.download()
+    t0 = time.perf_counter()
+    _, _, _, cnt = O.traverse(nodes, pidx, tris, rays, 0, nthreads=cores, counters=True)
+    dt = time.perf_counter() - t0
+    return rate, times, {"visits": int(cnt[0]), "tests": int(cnt[1]), "mrays_s": len(rays) / dt / 1e6}
+
+
+def run_reference(args):
+    rank, _, world = dist_info()
+    if rank != 0:
+        return
+    from obvhs_gb300.params import BvhBuildParams
+
+    tris, _ = workload(args.tris)
+    cores = os.cpu_count() or 1
+    p = BvhBuildParams.slow_build()
+    for _ in range(args.warmup):
+        cpu_build_rate(tris, p, 1, cores)
+    rate, times = cpu_build_rate(tris, p, args.steps, cores)
+    ms = 1e3 * sum(times) / len(times)
+    sample = f"full {len(tris)}-triangle slow_build per step, {cores} threads"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "Mtris/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded PCG64)",
+        "config": {"workload": WORKLOAD, "n_tris": len(tris), "preset": "slow_build",
+                   "implementation": "C++ restatement of obvhs 0.3.1 (oracle/); the Rust crate cannot be built here"},
+        "cpu_baseline": {"value": rate, "unit": "Mtris/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import torch
+
+    rank, local_rank, world = dist_info()
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    import obvhs_gb300 as G
+    from obvhs_gb300 import scenes as S
+    from obvhs_gb300.params import BvhBuildParams
+
+    ctx = G.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local_rank))
+    tris, rays = workload(args.tris)
+    p = BvhBuildParams.slow_build()
+    d_tris = torch.from_numpy(tris).cuda()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    # rays: primary, and bounce rays from the primary hits
+    cw = G.build_cwbvh_from_tris(d_tris, p, ctx=ctx)
+    pid, pt = cw.ray_traverse(rays)
+    bounce = S.bounce_rays(tris, rays, pid, pt)
+    d_rays = torch.from_numpy(rays).cuda()
+    d_bounce = torch.from_numpy(bounce).cuda()
+    n_nodes, n_prims, _ = cw.info()
+    del cw
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    def timed(fn, steps):
+        """Runs fn() `steps` times; each call is bracketed by CUDA events on the
+        library's stream and followed (outside the timing) by an L2 flush."""
+        ms = []
+        for _ in range(steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+        return ms
+
+    def build_once():
+        b = G.build_cwbvh_from_tris(d_tris, p, ctx=ctx)
+        build_once.last = b
+
+    for _ in range(args.warmup):
+        build_once()
+    barrier()
+    clocks = ClockSampler(local_rank).start() if rank == 0 else None
+    l0 = ctx.kernel_launches
+    t_wall0 = time.perf_counter()
+    build_ms = timed(build_once, args.steps)
+    barrier()
+    t_wall = time.perf_counter() - t_wall0
+    launches = (ctx.kernel_launches - l0) // max(args.steps, 1)
+    stats = build_once.last.stats
+    cw = build_once.last
+
+    # traversal (device-resident rays), each step = primary + bounce batch
+    out_p = torch.empty((len(rays), 2), dtype=torch.int32, device="cuda")
+    out_b = torch.empty((max(len(bounce), 1), 2), dtype=torch.int32, device="cuda")
+    lib = ctx.lib
+    import ctypes
+
+    def trace(r, out):
+        ctx.check(lib.obvhs_ray_traverse(ctx.h, cw.h, ctypes.c_void_p(r.data_ptr()), r.shape[0],
+                                         ctypes.c_void_p(out.data_ptr()), 1))
+
+    for _ in range(args.warmup):
+        trace(d_rays, out_p)
+        trace(d_bounce, out_b)
+    barrier()
+    prim_ms = timed(lambda: trace(d_rays, out_p), args.steps)
+    bounce_ms = timed(lambda: trace(d_bounce, out_b), args.steps) if len(bounce) else [0.0]
+    clk = clocks.stop() if clocks else None
+
+    # e2e through the public API: pinned host triangles in, CWBVH nodes out
+    h_tris = torch.from_numpy(tris).pin_memory()
+    h_nodes = torch.empty((n_nodes, 80), dtype=torch.uint8).pin_memory().numpy()
+    h_prims = torch.empty((n_prims,), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    h_tris_np = h_tris.numpy()
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b = G.build_cwbvh_from_tris(h_tris_np, p, ctx=ctx)
+        ctx.check(lib.obvhs_cwbvh_download(ctx.h, b.h, h_nodes.ctypes.data_as(ctypes.c_void_p),
+                                           h_prims.ctypes.data_as(ctypes.c_void_p)))
+        dt = (time.perf_counter() - t0) * 1e3
+        if i >= args.warmup:
+            e2e_ms.append(dt)
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        del b
+
+    n = len(tris)
+    mean_build = sum(build_ms) / len(build_ms)
+    mean_e2e = sum(e2e_ms) / len(e2e_ms)
+    tot = torch.tensor([mean_build, mean_e2e, sum(prim_ms) / len(prim_ms), sum(bounce_ms) / len(bounce_ms)],
+                       dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(tot, op=dist.ReduceOp.MAX)
+    mean_build, mean_e2e, mean_prim, mean_bounce = tot.tolist()
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    value = world * n / (mean_build * 1e-3) / 1e6
+    e2e = world * n / (mean_e2e * 1e-3) / 1e6
+    prim_rate = world * len(rays) / (mean_prim * 1e-3) / 1e6
+    bounce_rate = world * len(bounce) / (mean_bounce * 1e-3) / 1e6 if mean_bounce > 0 else 0.0
+
+    # CPU baseline (the oracle on this host's cores, bounded sample): two full
+    # builds, and the primary batch traced with node-visit / triangle-test
+    # counters, which also give the traversal's algorithmic bytes.
+    cores = os.cpu_count() or 1
+    cpu_rate, cpu_t, cpu_trace = cpu_baseline(tris, p, rays, cores, ctx)
+
+    # roofline: the primary-ray traversal kernel (one launch per batch, timed
+    # above with CUDA events on the library's stream).  Algorithmic bytes per
+    # ray: 32 (ray) + 8 (hit) + 80 per node visited + 36 per triangle tested.
+    alg_bytes = 40.0 * len(rays) + 80.0 * cpu_trace["visits"] + 36.0 * cpu_trace["tests"]
+    peak, peak_kind = measured_peak()
+    achieved = alg_bytes / (mean_prim * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get("k_traverse_primary_bytes")
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mtris/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": mean_build, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded PCG64 clustered scene)",
+        "config": {"workload": WORKLOAD, "n_tris": n, "preset": "slow_build", "leaves": stats.leaf_count,
+                   "cwbvh_nodes": n_nodes, "primary_rays": len(rays), "bounce_rays": len(bounce),
+                   "l2": "512 MB flush between timed steps", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e, "unit": "Mtris/s", "h2d_bytes_per_step": n * 36,
+                "d2h_bytes_per_step": n_nodes * 80 + n_prims * 4, "ms_per_step": mean_e2e},
+        "traversal": {"primary_mrays_s": prim_rate, "bounce_mrays_s": bounce_rate, "primary_ms": mean_prim,
+                      "bounce_ms": mean_bounce},
+        "build_stages_ms": {"presplit": stats.stage_ms[0], "ploc": stats.stage_ms[1],
+                            "reinsertion": stats.stage_ms[2], "cwbvh": stats.stage_ms[3]},
+        "roofline": {"kernel": "k_traverse<closest> (primary batch)", "bound": "hbm", "achieved": achieved,
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
+                     "bytes_per_ray": alg_bytes / len(rays)},
+        "cpu_baseline": {"value": cpu_rate, "unit": "Mtris/s", "cores": cores, "kind": "port",
+                         "sample": f"2 full {n}-triangle slow_build builds on {cores} threads "
+                                   f"({sum(cpu_t):.1f} s)",
+                         "primary_mrays_s": cpu_trace["mrays_s"]},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "wall_s_timed_builds": t_wall,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -90,6 +90,7 @@ typedef struct {
   uint64_t ploc_sum_counts; /* sum over passes of live clusters */
   uint64_t reinsertions;    /* reinsertions applied */
   uint64_t kernel_launches; /* kernels launched by the call */
+  double stage_ms[4];       /* device time of pre-split, PLOC, reinsertion, conversion */
 } obvhs_build_stats;
 
 /* ---- context ------------------------------------------------------------ */

@@ -55,6 +55,7 @@ class BuildStats(ctypes.Structure):
         ("ploc_sum_counts", U64),
         ("reinsertions", U64),
         ("kernel_launches", U64),
+        ("stage_ms", ctypes.c_double * 4),
     ]
 
 

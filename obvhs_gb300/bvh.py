@@ -111,11 +111,12 @@ class BuildStats:
     ploc_sum_counts: int
     reinsertions: int
     kernel_launches: int
+    stage_ms: tuple = (0.0, 0.0, 0.0, 0.0)  # pre-split, PLOC, reinsertion, conversion
 
     @staticmethod
     def from_c(s: N.BuildStats) -> "BuildStats":
         return BuildStats(s.core_build_ms, s.leaf_count, s.ploc_passes, s.ploc_sum_counts, s.reinsertions,
-                          s.kernel_launches)
+                          s.kernel_launches, tuple(s.stage_ms))
 
 
 class Bvh2:

@@ -55,6 +55,29 @@ __global__ void k_iota_u32(uint32_t* v, uint32_t n) {
   if (i < n) v[i] = i;
 }
 
+// Marks stage boundaries on the stream; elapsed times read after the build.
+struct StageEvents {
+  cudaEvent_t ev[5] = {};
+  int n = 0;
+  explicit StageEvents(cudaStream_t s) {
+    for (auto& e : ev) cudaEventCreate(&e);
+    mark(s);
+  }
+  void mark(cudaStream_t s) {
+    if (n < 5) cudaEventRecord(ev[n++], s);
+  }
+  void read(double* out4) {
+    for (int k = 0; k < 4; k++) {
+      float ms = 0;
+      if (k + 1 < n) cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+      out4[k] = ms;
+    }
+  }
+  ~StageEvents() {
+    for (auto& e : ev) cudaEventDestroy(e);
+  }
+};
+
 struct EventTimer {
   cudaEvent_t a = nullptr, b = nullptr;
   cudaStream_t s;
@@ -85,6 +108,7 @@ int build_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t 
   if (p->sort_precision > 1) return c.fail(OBVHS_ERR_INVALID_ARG, "sort_precision must be 0 (U64) or 1 (U128)");
   uint64_t launches0 = c.kernel_launches;
   EventTimer timer(c.stream);
+  StageEvents stages(c.stream);
   Scratch& s = c.scratch;
   const bool split = tris && p->pre_split;
   const float* leaf_aabbs = aabbs;
@@ -99,6 +123,7 @@ int build_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t 
     leaf_aabbs = a;
     leaf_idx = ix;
   }
+  stages.mark(c.stream);
   Bvh2Node* leaves = (Bvh2Node*)s.get(SLOT_LEAVES, (size_t)std::max(m, 1u) * sizeof(Bvh2Node));
   int* total = (int*)s.get(SLOT_TOTAL, 64);
   obvhs_bvh2 b2;
@@ -130,10 +155,12 @@ int build_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t 
   r = ploc_build_device(c, leaves, m, total, p->ploc_search_distance, (int)p->sort_precision,
                         p->search_depth_threshold, b2.nodes, &passes, &sum_counts);
   if (r) return r;
+  stages.mark(c.stream);
   b2.max_depth = std::max<uint32_t>(96, passes + 1);
   uint64_t applied = 0;
   r = reinsertion_device(c, &b2, p->reinsertion_batch_ratio, nullptr, 0, &applied);
   if (r) return r;
+  stages.mark(c.stream);
   uint32_t mp = p->max_prims_per_leaf < 1 ? 1 : (p->max_prims_per_leaf > 3 ? 3 : p->max_prims_per_leaf);
   obvhs_cwbvh* cw = new obvhs_cwbvh();
   cw->ctx = &c;
@@ -150,6 +177,7 @@ int build_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t 
       return r;
     }
   }
+  stages.mark(c.stream);
   double ms = timer.stop_ms();
   r = take_status(c);
   if (r) {
@@ -174,6 +202,7 @@ int build_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t 
     stats->ploc_sum_counts = sum_counts;
     stats->reinsertions = applied;
     stats->kernel_launches = c.kernel_launches - launches0;
+    stages.read(stats->stage_ms);
   }
   *out = cw;
   return 0;
