@@ -260,6 +260,16 @@ def run_gb300(args):
     bounce_ms = timed(lambda: trace(d_bounce, out_b), args.steps) if len(bounce) else [0.0]
     clk = clocks.stop() if clocks else None
 
+    # per-kernel device time of one build and one primary batch (events around
+    # every launch on the library's stream; not part of the timings above)
+    ctx.set_profiling(True)
+    b = G.build_cwbvh_from_tris(d_tris, p, ctx=ctx)
+    trace(d_rays, out_p)
+    ctx.synchronize()
+    kernel_profile = ctx.profile_report()
+    ctx.set_profiling(False)
+    del b
+
     # e2e through the public API: pinned host triangles in, CWBVH nodes out
     h_tris = torch.from_numpy(tris).pin_memory()
     h_nodes = torch.empty((n_nodes, 80), dtype=torch.uint8).pin_memory().numpy()
@@ -335,6 +345,8 @@ def run_gb300(args):
                                    f"({sum(cpu_t):.1f} s)",
                          "primary_mrays_s": cpu_trace["mrays_s"]},
         "gpu_launches": launches,
+        "kernel_profile_ms": {k: round(v["total_ms"], 4) for k, v in sorted(kernel_profile.items(),
+                                                                             key=lambda kv: -kv[1]["total_ms"])},
         "clocks": clk,
         "wall_s_timed_builds": t_wall,
     }

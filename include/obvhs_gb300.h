@@ -106,6 +106,12 @@ OBVHS_API int obvhs_ctx_synchronize(obvhs_ctx* ctx);
 /* Kernels launched by this context so far. */
 OBVHS_API uint64_t obvhs_ctx_kernel_launches(const obvhs_ctx* ctx);
 
+/* Per-kernel timing: while enabled, every launch is bracketed by CUDA events
+ * on the context's stream.  The report (JSON: kernel -> launches, total_ms,
+ * max_ms) covers the launches since the last report and clears them. */
+OBVHS_API int obvhs_ctx_set_profiling(obvhs_ctx* ctx, int enable);
+OBVHS_API int obvhs_ctx_profile_report(obvhs_ctx* ctx, char* buf, uint64_t cap);
+
 /* ---- BVH2 --------------------------------------------------------------- */
 /* PlocBuilder::build / build_ploc::<SEARCH_DISTANCE> (src/ploc/mod.rs:95-251):
  * leaves Bvh2Node::new(aabbs[i], 1, indices[i]) (indices NULL = 0..n),
@@ -135,6 +141,12 @@ OBVHS_API int obvhs_reinsertion_run(obvhs_ctx* ctx, obvhs_bvh2* bvh, float batch
  * copied and OBVHS_ERR_INVALID_ARG is returned with *m set). */
 OBVHS_API int obvhs_split_aabbs_preset(obvhs_ctx* ctx, const float* triangles, uint32_t n, float* aabbs_out,
                              uint32_t* indices_out, uint32_t cap, uint32_t* m);
+
+/* The set-up of build_cwbvh_from_tris before split_aabbs_preset
+ * (src/cwbvh/builder.rs:31-43, src/splits.rs:23-33): out = {area_thresh_low,
+ * area_thresh_high, average half area, largest half area, sequential f32 sum
+ * of the half areas, blocks summed element by element (as u32 bits)}. */
+OBVHS_API int obvhs_split_thresholds(obvhs_ctx* ctx, const float* triangles, uint32_t n, float out[6]);
 
 /* ---- CWBVH -------------------------------------------------------------- */
 /* bvh2_to_cwbvh (src/cwbvh/bvh2_to_cwbvh.rs:490-510).  max_prims_per_leaf

@@ -67,6 +67,8 @@ SIGNATURES = {
     "obvhs_ctx_stream": (P, [P]),
     "obvhs_ctx_synchronize": (I32, [P]),
     "obvhs_ctx_kernel_launches": (U64, [P]),
+    "obvhs_ctx_set_profiling": (I32, [P, I32]),
+    "obvhs_ctx_profile_report": (I32, [P, P, U64]),
     "obvhs_ploc_build": (I32, [P, P, P, U32, U32, U32, U32, I32, ctypes.POINTER(P), ctypes.POINTER(BuildStats)]),
     "obvhs_bvh2_info": (I32, [P, ctypes.POINTER(U32), ctypes.POINTER(U32), ctypes.POINTER(U32)]),
     "obvhs_bvh2_download": (I32, [P, P, P, P]),
@@ -74,6 +76,7 @@ SIGNATURES = {
     "obvhs_bvh2_free": (I32, [P]),
     "obvhs_reinsertion_run": (I32, [P, P, F32, P, U32, ctypes.POINTER(U64)]),
     "obvhs_split_aabbs_preset": (I32, [P, P, U32, P, P, U32, ctypes.POINTER(U32)]),
+    "obvhs_split_thresholds": (I32, [P, P, U32, P]),
     "obvhs_bvh2_to_cwbvh": (I32, [P, P, U32, I32, ctypes.POINTER(P)]),
     "obvhs_build_cwbvh_from_tris": (I32, [P, P, U32, ctypes.POINTER(BuildParams), I32, ctypes.POINTER(P),
                                           ctypes.POINTER(BuildStats)]),

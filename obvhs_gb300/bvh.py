@@ -87,6 +87,18 @@ class Context:
     def kernel_launches(self) -> int:
         return int(self.lib.obvhs_ctx_kernel_launches(self.h))
 
+    def set_profiling(self, enable: bool):
+        """Brackets every kernel launch with CUDA events on the context's stream."""
+        self.check(self.lib.obvhs_ctx_set_profiling(self.h, int(enable)))
+
+    def profile_report(self) -> dict:
+        """Per-kernel {launches, total_ms, max_ms} since the last report."""
+        import json
+
+        buf = ctypes.create_string_buffer(1 << 16)
+        self.check(self.lib.obvhs_ctx_profile_report(self.h, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
     def close(self):
         if self.h:
             self.lib.obvhs_ctx_destroy(self.h)
@@ -248,6 +260,18 @@ def split_aabbs_preset(triangles, ctx: Context | None = None):
             continue
         ctx.check(r)
         return a[: m.value].copy(), ix[: m.value].copy()
+
+
+def split_thresholds(triangles, ctx: Context | None = None):
+    """(area_thresh_low, area_thresh_high, avg_half_area, largest_half_area,
+    sequential f32 sum, blocks summed element by element) as
+    build_cwbvh_from_tris computes them (src/cwbvh/builder.rs:31-43)."""
+    ctx = _ctx(ctx)
+    t = np.ascontiguousarray(triangles, dtype=np.float32).reshape(-1, 9)
+    out = np.zeros(6, np.float32)
+    ctx.check(ctx.lib.obvhs_split_thresholds(ctx.h, t.ctypes.data_as(ctypes.c_void_p), len(t),
+                                             out.ctypes.data_as(ctypes.c_void_p)))
+    return out
 
 
 class CwBvh:

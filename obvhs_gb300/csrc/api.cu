@@ -144,8 +144,7 @@ int build_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t 
     if (leaf_idx)
       CK(cudaMemcpyAsync(b2.prim_indices, leaf_idx, (size_t)m * 4, cudaMemcpyDeviceToDevice, c.stream));
     else {
-      k_iota_u32<<<div_up<uint32_t>(m, 256), 256, 0, c.stream>>>(b2.prim_indices, m);
-      c.kernel_launches++;
+      KLAUNCH("k_iota_u32", k_iota_u32<<<div_up<uint32_t>(m, 256), 256, 0, c.stream>>>(b2.prim_indices, m));
     }
   }
   r = take_status(c);
@@ -268,6 +267,52 @@ int obvhs_ctx_synchronize(obvhs_ctx* c) {
 }
 uint64_t obvhs_ctx_kernel_launches(const obvhs_ctx* c) { return c ? c->kernel_launches : 0; }
 
+int obvhs_ctx_set_profiling(obvhs_ctx* c, int enable) {
+  if (!c) return OBVHS_ERR_INVALID_ARG;
+  c->profiling = enable != 0;
+  return OBVHS_OK;
+}
+
+int obvhs_ctx_profile_report(obvhs_ctx* c, char* buf, uint64_t cap) {
+  if (!c || !buf || cap == 0) return OBVHS_ERR_INVALID_ARG;
+  DeviceGuard g(c->device);
+  cudaStreamSynchronize(c->stream);
+  struct Agg {
+    std::string name;
+    uint64_t n = 0;
+    double ms = 0, max_ms = 0;
+  };
+  std::vector<Agg> agg;
+  for (auto& r : c->krecs) {
+    float ms = 0;
+    if (r.b) cudaEventElapsedTime(&ms, r.a, r.b);
+    cudaEventDestroy(r.a);
+    if (r.b) cudaEventDestroy(r.b);
+    Agg* a = nullptr;
+    for (auto& x : agg)
+      if (x.name == r.name) a = &x;
+    if (!a) {
+      agg.push_back(Agg{r.name});
+      a = &agg.back();
+    }
+    a->n++;
+    a->ms += ms;
+    a->max_ms = std::max(a->max_ms, (double)ms);
+  }
+  c->krecs.clear();
+  std::string out = "{";
+  for (size_t i = 0; i < agg.size(); i++) {
+    char line[256];
+    snprintf(line, sizeof(line), "%s\"%s\": {\"launches\": %llu, \"total_ms\": %.6f, \"max_ms\": %.6f}", i ? ", " : "",
+             agg[i].name.c_str(), (unsigned long long)agg[i].n, agg[i].ms, agg[i].max_ms);
+    out += line;
+  }
+  out += "}";
+  if (out.size() + 1 > cap) return c->fail(OBVHS_ERR_INVALID_ARG, "report buffer too small");
+  memcpy(buf, out.c_str(), out.size() + 1);
+  return OBVHS_OK;
+}
+
 // ---- BVH2 ------------------------------------------------------------------
 
 int obvhs_ploc_build(obvhs_ctx* cp, const float* aabbs, const uint32_t* indices, uint32_t n, uint32_t search_distance,
@@ -308,8 +353,7 @@ int obvhs_ploc_build(obvhs_ctx* cp, const float* aabbs, const uint32_t* indices,
     if (di) {
       cudaMemcpyAsync(b->prim_indices, di, (size_t)n * 4, cudaMemcpyDeviceToDevice, c.stream);
     } else {
-      k_iota_u32<<<div_up<uint32_t>(n, 256), 256, 0, c.stream>>>(b->prim_indices, n);
-      c.kernel_launches++;
+      KLAUNCH("k_iota_u32", k_iota_u32<<<div_up<uint32_t>(n, 256), 256, 0, c.stream>>>(b->prim_indices, n));
     }
   }
   if (!r) r = take_status(c);
@@ -422,6 +466,19 @@ int obvhs_split_aabbs_preset(obvhs_ctx* cp, const float* triangles, uint32_t n, 
   }
   CK(cudaStreamSynchronize(c.stream));
   return OBVHS_OK;
+}
+
+int obvhs_split_thresholds(obvhs_ctx* cp, const float* triangles, uint32_t n, float out[6]) {
+  if (!cp || !out || (n && !triangles)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  if (n == 0) return c.fail(OBVHS_ERR_INVALID_ARG, "no triangles");
+  int err = 0;
+  const float* dt = (const float*)stage_in(c, SLOT_INPUT, triangles, (size_t)n * 36, 0, &err);
+  if (err) return err;
+  int r = split_thresholds_device(c, dt, n, out);
+  if (!r) r = take_status(c);
+  return r;
 }
 
 // ---- CWBVH -----------------------------------------------------------------

@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -52,6 +53,10 @@ enum ScratchSlot {
   SLOT_BVH2_NODES,
   SLOT_BVH2_PIDX,
   SLOT_TRAV_OUT,
+  SLOT_PENDING,
+  SLOT_DIRTY_LIST,
+  SLOT_STARTS,
+  SLOT_DONE,
   SLOT_COUNT
 };
 
@@ -114,6 +119,25 @@ struct obvhs_ctx {
   Scratch scratch;
   std::string last_error;
   uint64_t kernel_launches = 0;
+  // opt-in per-launch timing (obvhs_ctx_set_profiling)
+  struct KRec {
+    const char* name;
+    cudaEvent_t a, b;
+  };
+  bool profiling = false;
+  std::vector<KRec> krecs;
+  void kbegin(const char* name) {
+    kernel_launches++;
+    if (!profiling) return;
+    KRec r{name, nullptr, nullptr};
+    cudaEventCreate(&r.a);
+    cudaEventCreate(&r.b);
+    cudaEventRecord(r.a, stream);
+    krecs.push_back(r);
+  }
+  void kend() {
+    if (profiling && !krecs.empty()) cudaEventRecord(krecs.back().b, stream);
+  }
 
   int fail(int code, const std::string& msg) {
     last_error = msg;
@@ -125,6 +149,15 @@ struct obvhs_ctx {
   }
 };
 typedef obvhs_ctx BuildCtx;
+
+// Launch wrapper: counts the launch and, when profiling, brackets it with
+// CUDA events on the context's stream.
+#define KLAUNCH(NAME, ...) \
+  do {                     \
+    c.kbegin(NAME);        \
+    __VA_ARGS__;           \
+    c.kend();              \
+  } while (0)
 
 #define CK(expr)                                             \
   do {                                                       \
@@ -167,7 +200,8 @@ int ploc_setup_kernels();
 
 // presplit.cu
 int presplit_device(BuildCtx& c, const float* tris, uint32_t n, float** aabbs_out, uint32_t** idx_out,
-                    uint32_t* m_out);
+                    uint32_t* m_out, bool thresholds_only = false);
+int split_thresholds_device(BuildCtx& c, const float* tris, uint32_t n, float* out6);
 
 // reinsertion.cu
 int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const float* seq, uint32_t nseq,

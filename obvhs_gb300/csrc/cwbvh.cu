@@ -20,7 +20,11 @@
 // prim_base(c_j) + nprim(c_j).  Nodes are then emitted level by level, in
 // parallel, at exactly the reference's positions, so the output is byte for
 // byte the reference's CwBvh.
+#include <cooperative_groups.h>
+
 #include "build.h"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -249,16 +253,11 @@ __device__ __forceinline__ float3 center(const Box& b) {
   return make_float3((b.mx.x + b.mn.x) * 0.5f, (b.mx.y + b.mn.y) * 0.5f, (b.mx.z + b.mn.z) * 0.5f);
 }
 
-__global__ void __launch_bounds__(128) k_emit(const Bvh2Node* __restrict__ nodes, const uint32_t* __restrict__ pidx_in,
-                                              const Dec* __restrict__ dec, const CwMeta* __restrict__ meta,
-                                              const Item* __restrict__ in, const uint32_t* n_in, Item* __restrict__ out,
-                                              uint32_t* n_out, int order_children, uint32_t max_nodes,
-                                              uint32_t max_prims_out, CwNode* __restrict__ cw,
-                                              uint32_t* __restrict__ pidx_out, float* __restrict__ exact,
-                                              uint32_t* status) {
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= *n_in) return;
-  const Item it = in[t];
+__device__ void emit_item(const Bvh2Node* __restrict__ nodes, const uint32_t* __restrict__ pidx_in,
+                          const Dec* __restrict__ dec, const CwMeta* __restrict__ meta, const Item it,
+                          Item* __restrict__ out, uint32_t* n_out, int order_children, uint32_t max_nodes,
+                          uint32_t max_prims_out, CwNode* __restrict__ cw, uint32_t* __restrict__ pidx_out,
+                          float* __restrict__ exact, uint32_t* status) {
   const Bvh2Node nd = ld_node(&nodes[it.bvh2]);
   const Box box = node_box(nd);
   if (exact) {
@@ -444,9 +443,49 @@ __global__ void __launch_bounds__(128) k_emit(const Bvh2Node* __restrict__ nodes
   }
 }
 
-__global__ void k_root_item(Item* f, uint32_t* n) {
-  f[0] = Item{0, 0, 1, 0};
-  *n = 1;
+// All levels in one cooperative launch: level L reads frontier L & 1 (its
+// size in cnt[L % 3]) and appends the next level to the other frontier.
+struct EmitArgs {
+  const Bvh2Node* nodes;
+  const uint32_t* pidx_in;
+  const Dec* dec;
+  const CwMeta* meta;
+  Item* frontier[2];
+  uint32_t* cnt;  // [3]
+  int order_children;
+  uint32_t max_nodes, max_prims_out;
+  CwNode* cw;
+  uint32_t* pidx_out;
+  float* exact;
+  uint32_t* status;
+  uint32_t* processed;
+};
+
+__global__ void __launch_bounds__(128) k_emit_all(EmitArgs a) {
+  cg::grid_group grid = cg::this_grid();
+  const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  if (t0 == 0) {
+    a.frontier[0][0] = Item{0, 0, 1, 0};
+    a.cnt[0] = 1;
+    a.cnt[1] = 0;
+  }
+  grid.sync();
+  for (uint32_t level = 0; level < 64; level++) {
+    const uint32_t n_in = *(volatile uint32_t*)&a.cnt[level % 3];
+    if (n_in == 0) break;
+    if (t0 == 0) a.cnt[(level + 2) % 3] = 0;
+    const Item* in = a.frontier[level & 1];
+    Item* out = a.frontier[(level + 1) & 1];
+    uint32_t mine = 0;
+    for (uint32_t t = t0; t < n_in; t += stride) {
+      emit_item(a.nodes, a.pidx_in, a.dec, a.meta, in[t], out, &a.cnt[(level + 1) % 3], a.order_children,
+                a.max_nodes, a.max_prims_out, a.cw, a.pidx_out, a.exact, a.status);
+      mine++;
+    }
+    if (mine) atomicAdd(a.processed, mine);
+    grid.sync();
+  }
 }
 
 }  // namespace
@@ -466,9 +505,8 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   int r = compute_parents_device(c, b->nodes, n, parents);
   if (r) return r;
   CK(cudaMemsetAsync(flags, 0, (size_t)n * 4, c.stream));
-  c.kernel_launches++;
-  k_costs<<<div_up<uint32_t>(n, BLK), BLK, 0, c.stream>>>(b->nodes, parents, n, max_prims, dec, meta, flags,
-                                                          c.d_status);
+  KLAUNCH("k_costs", k_costs<<<div_up<uint32_t>(n, BLK), BLK, 0, c.stream>>>(b->nodes, parents, n, max_prims, dec, meta, flags,
+                                                          c.d_status));
   CK(cudaGetLastError());
   // sizes of the whole tree
   CwMeta root;
@@ -496,29 +534,20 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
     cudaFree(cwp);
     return c.fail(OBVHS_ERR_OOM, "scratch");
   }
-  uint32_t* nA = counters + 8;
-  uint32_t* nB = counters + 9;
-  c.kernel_launches++;
-  k_root_item<<<1, 1, 0, c.stream>>>(fa, nA);
-  uint32_t level_n = 1, emitted = 0;
-  for (int level = 0; level_n > 0; level++) {
-    if (level > 64 || emitted > n_cw) {
-      cudaFree(cwn);
-      cudaFree(cwp);
-      return c.fail(OBVHS_ERR_LIMIT, "CWBVH emission did not terminate");
-    }
-    CK(cudaMemsetAsync(nB, 0, 4, c.stream));
-    c.kernel_launches++;
-    k_emit<<<div_up<uint32_t>(level_n, 128), 128, 0, c.stream>>>(b->nodes, b->prim_indices, dec, meta, fa, nA, fb, nB,
-                                                                order_children, n_cw, n_pr, cwn, cwp, nullptr,
-                                                                c.d_status);
-    CK(cudaGetLastError());
-    emitted += level_n;
-    CK(cudaMemcpyAsync(&level_n, nB, 4, cudaMemcpyDeviceToHost, c.stream));
-    CK(cudaStreamSynchronize(c.stream));
-    std::swap(fa, fb);
-    std::swap(nA, nB);
+  static int emit_blocks = 0;
+  if (!emit_blocks) {
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_all, 128, 0));
+    emit_blocks = std::max(1, per_sm) * c.num_sms;
   }
+  CK(cudaMemsetAsync(counters + 12, 0, 4, c.stream));
+  EmitArgs ea{b->nodes, b->prim_indices, dec, meta, {fa, fb}, counters + 8, order_children, n_cw, n_pr, cwn, cwp,
+              nullptr, c.d_status, counters + 12};
+  void* args[] = {&ea};
+  uint32_t grid = (uint32_t)std::min<uint64_t>(emit_blocks, std::max<uint64_t>(1, div_up<uint32_t>(n_cw, 128)));
+  CK(cudaLaunchCooperativeKernel((void*)k_emit_all, grid, 128, args, 0, c.stream));
+  uint32_t emitted = 0;
+  CK(cudaMemcpyAsync(&emitted, counters + 12, 4, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaMemcpyAsync(c.h_status, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
   if (*c.h_status || emitted != n_cw) {

@@ -632,11 +632,10 @@ int ploc_leaves(BuildCtx& c, const float* tris, const float* aabbs, const uint32
   CK(cudaMemcpyAsync(total_keys, init, sizeof(init), cudaMemcpyHostToDevice, c.stream));
   if (!n) return 0;
   uint32_t g = div_up<uint32_t>(n, BLK);
-  c.kernel_launches++;
   if (tris)
-    k_leaves_from_tris<<<g, BLK, 0, c.stream>>>(tris, n, leaves, total_keys, c.d_status);
+    KLAUNCH("k_leaves_from_tris", k_leaves_from_tris<<<g, BLK, 0, c.stream>>>(tris, n, leaves, total_keys, c.d_status));
   else
-    k_leaves_from_aabbs<<<g, BLK, 0, c.stream>>>(aabbs, idx, n, leaves, total_keys, c.d_status);
+    KLAUNCH("k_leaves_from_aabbs", k_leaves_from_aabbs<<<g, BLK, 0, c.stream>>>(aabbs, idx, n, leaves, total_keys, c.d_status));
   CK(cudaGetLastError());
   return 0;
 }
@@ -645,11 +644,10 @@ int ploc_morton_codes(BuildCtx& c, const Bvh2Node* leaves, uint32_t n, const int
                       void* codes) {
   if (!n) return 0;
   uint32_t g = div_up<uint32_t>(n, BLK);
-  c.kernel_launches++;
   if (precision)
-    k_morton128<<<g, BLK, 0, c.stream>>>(leaves, n, total_keys, (U128*)codes);
+    KLAUNCH("k_morton128", k_morton128<<<g, BLK, 0, c.stream>>>(leaves, n, total_keys, (U128*)codes));
   else
-    k_morton64<<<g, BLK, 0, c.stream>>>(leaves, n, total_keys, (unsigned long long*)codes);
+    KLAUNCH("k_morton64", k_morton64<<<g, BLK, 0, c.stream>>>(leaves, n, total_keys, (unsigned long long*)codes));
   CK(cudaGetLastError());
   return 0;
 }
@@ -661,18 +659,15 @@ int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_
   void* keys_alt = s.get(SLOT_KEYS_ALT, (size_t)n * kb);
   uint32_t* vals = (uint32_t*)s.get(SLOT_VALS, (size_t)n * 4);
   uint32_t* vals_alt = (uint32_t*)s.get(SLOT_VALS_ALT, (size_t)n * 4);
-  uint32_t* tile_hist = (uint32_t*)s.get(SLOT_TILE_HIST, (size_t)radix_tile_count(n) * 256 * 4 + 4);
-  uint32_t* all_hist = (uint32_t*)s.get(SLOT_ALL_HIST, 16 * 256 * 4);
-  if (!keys_alt || !vals || !vals_alt || !tile_hist || !all_hist) return c.fail(OBVHS_ERR_OOM, "scratch");
+  uint32_t* rs = (uint32_t*)s.get(SLOT_ALL_HIST, radix_scratch_words(n) * 4);
+  if (!keys_alt || !vals || !vals_alt || !rs) return c.fail(OBVHS_ERR_OOM, "scratch");
   bool alt = false;
   cudaError_t e;
   if (precision)
-    e = radix_sort_pairs<U128>((U128*)codes, vals, n, true, (U128*)keys_alt, vals_alt, tile_hist, all_hist,
-                               c.h_hist, c.stream, &alt, &c.kernel_launches);
+    e = radix_sort_pairs<U128>(c, (U128*)codes, vals, n, true, (U128*)keys_alt, vals_alt, rs, &alt);
   else
-    e = radix_sort_pairs<unsigned long long>((unsigned long long*)codes, vals, n, true,
-                                             (unsigned long long*)keys_alt, vals_alt, tile_hist, all_hist, c.h_hist,
-                                             c.stream, &alt, &c.kernel_launches);
+    e = radix_sort_pairs<unsigned long long>(c, (unsigned long long*)codes, vals, n, true,
+                                             (unsigned long long*)keys_alt, vals_alt, rs, &alt);
   if (e) return c.cuda_fail(e, "radix sort");
   *order_out = alt ? vals_alt : vals;
   return 0;
@@ -701,15 +696,13 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   PlocState* st = (PlocState*)s.get(SLOT_PLOC_STATE, sizeof(PlocState));
   if (!cur || !nxt || !merge || !partial || !st) return c.fail(OBVHS_ERR_OOM, "scratch");
   uint32_t g = div_up<uint32_t>(n, BLK);
-  c.kernel_launches++;
-  k_gather<<<g, BLK, 0, c.stream>>>(leaves, order, n, cur);
+  KLAUNCH("k_gather", k_gather<<<g, BLK, 0, c.stream>>>(leaves, order, n, cur));
   PlocState h0{};
   h0.count[0] = n;
   h0.insert[0] = 2 * n - 1;
   CK(cudaMemcpyAsync(st, &h0, sizeof(PlocState), cudaMemcpyHostToDevice, c.stream));
   if (n == 1) {
-    c.kernel_launches++;
-    k_root_copy<<<1, 1, 0, c.stream>>>(cur, out_nodes);
+    KLAUNCH("k_root_copy", k_root_copy<<<1, 1, 0, c.stream>>>(cur, out_nodes));
     CK(cudaGetLastError());
     return 0;
   }
@@ -724,14 +717,10 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
       int d1 = (radius == 1 || pass < depth_threshold) ? 1 : 0;
       uint32_t gs = div_up<uint32_t>(known, BLK);
       uint32_t gc = div_up<uint32_t>(known, CHUNK);
-      c.kernel_launches++;
-      k_ploc_search<<<gs, BLK, 0, c.stream>>>(cur, st, parity, (int)radius, d1, merge);
-      c.kernel_launches++;
-      k_ploc_count<<<gc, BLK, 0, c.stream>>>(merge, st, parity, partial);
-      c.kernel_launches++;
-      k_ploc_scan<<<1, 1024, 0, c.stream>>>(partial, st, parity);
-      c.kernel_launches++;
-      k_ploc_scatter<<<gc, BLK, 0, c.stream>>>(cur, merge, st, parity, partial, nxt, out_nodes);
+      KLAUNCH("k_ploc_search", k_ploc_search<<<gs, BLK, 0, c.stream>>>(cur, st, parity, (int)radius, d1, merge));
+      KLAUNCH("k_ploc_count", k_ploc_count<<<gc, BLK, 0, c.stream>>>(merge, st, parity, partial));
+      KLAUNCH("k_ploc_scan", k_ploc_scan<<<1, 1024, 0, c.stream>>>(partial, st, parity));
+      KLAUNCH("k_ploc_scatter", k_ploc_scatter<<<gc, BLK, 0, c.stream>>>(cur, merge, st, parity, partial, nxt, out_nodes));
       std::swap(cur, nxt);
       parity ^= 1;
       pass++;
@@ -746,13 +735,11 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   }
   if (known > 1) {
     size_t smem = (size_t)4 * TAIL_MAX * sizeof(float4) + TAIL_MAX + 64;
-    c.kernel_launches++;
-    k_ploc_tail<<<1, TAIL_THREADS, smem, c.stream>>>(cur, st, parity, (int)radius, depth_threshold, max_passes,
-                                                     out_nodes, c.d_status);
+    KLAUNCH("k_ploc_tail", k_ploc_tail<<<1, TAIL_THREADS, smem, c.stream>>>(cur, st, parity, (int)radius, depth_threshold, max_passes,
+                                                     out_nodes, c.d_status));
     CK(cudaGetLastError());
   } else {
-    c.kernel_launches++;
-    k_root_copy<<<1, 1, 0, c.stream>>>(cur, out_nodes);
+    KLAUNCH("k_root_copy", k_root_copy<<<1, 1, 0, c.stream>>>(cur, out_nodes));
     CK(cudaGetLastError());
   }
   PlocState h;

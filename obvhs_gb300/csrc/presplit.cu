@@ -55,43 +55,129 @@ __global__ void __launch_bounds__(BLK) k_tri_boxes(const float* __restrict__ tri
   if ((threadIdx.x & 31) == 0) atomicMax(largest_key, k);
 }
 
-// Sequential f32 sum of ha[0..n) in index order (src/cwbvh/builder.rs:36-41),
-// then the preset thresholds (src/splits.rs:23-33).
-constexpr int SUM_CHUNK = 4096;
-__global__ void __launch_bounds__(BLK) k_avg_thresholds(const float* __restrict__ ha, uint32_t n, const int* largest_key,
-                                                        float* thr) {
-  __shared__ float buf[2][SUM_CHUNK];
-  const uint32_t nch = (n + SUM_CHUNK - 1) / SUM_CHUNK;
-  float sum = 0.0f;
-  auto load = [&](uint32_t ch, int slot) {
-    uint32_t b = ch * SUM_CHUNK;
-    for (uint32_t j = threadIdx.x; j < SUM_CHUNK; j += BLK) buf[slot][j] = (b + j < n) ? ha[b + j] : 0.0f;
-  };
-  if (nch) load(0, 0);
+// --- the sequential f32 sum of ha[0..n) (src/cwbvh/builder.rs:36-41) -------
+//
+// s_k = RN(s_{k-1} + a_k) with a_k >= 0 is order dependent, so it must be
+// reproduced exactly.  While s stays inside one binade [2^E, 2^(E+1)), with
+// u = 2^(E-23), adding a is integer arithmetic on the significand S = s/u:
+// S += m + r, where a/u = m + f (f in [0,1)) and r = 0 if f < 1/2, 1 if
+// f > 1/2, and for f == 1/2 (a tie) r makes S+m+r even.  Only the parity of S
+// matters, so a block of elements maps to two increments (start parity even
+// or odd), computed in parallel for three candidate binades around the
+// double-precision prefix.  One thread then chains the blocks exactly,
+// summing a block element by element only when the running sum is not in a
+// candidate binade or would leave its binade inside the block.
+constexpr int SUM_BLOCK = 1024;
+constexpr int NCAND_E = 3;
+
+struct BlockT {
+  long long inc[NCAND_E][2];
+  int e0;  // candidate binades are e0-1, e0, e0+1
+  int valid[NCAND_E];
+};
+
+__global__ void __launch_bounds__(BLK) k_block_dsum(const float* __restrict__ ha, uint32_t n, double* __restrict__ bsum) {
+  __shared__ double sw[BLK / 32];
+  const uint32_t base = blockIdx.x * SUM_BLOCK;
+  double acc = 0.0;
+  for (uint32_t j = threadIdx.x; j < SUM_BLOCK; j += BLK)
+    if (base + j < n) acc += (double)ha[base + j];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = acc;
   __syncthreads();
-  for (uint32_t ch = 0; ch < nch; ch++) {
-    int slot = ch & 1;
-    if (threadIdx.x == 0) {
-      uint32_t b = ch * SUM_CHUNK;
-      uint32_t m = min((uint32_t)SUM_CHUNK, n - b);
-      const float* p = buf[slot];
-      for (uint32_t j = 0; j < m; j++) sum = __fadd_rn(sum, p[j]);
-    } else if (threadIdx.x >= 32 && ch + 1 < nch) {
-      uint32_t b = (ch + 1) * SUM_CHUNK;
-      for (uint32_t j = threadIdx.x - 32; j < SUM_CHUNK; j += BLK - 32)
-        buf[slot ^ 1][j] = (b + j < n) ? ha[b + j] : 0.0f;
-    }
-    __syncthreads();
-  }
   if (threadIdx.x == 0) {
-    float avg = sum / (float)n;
-    float largest = fkey_inv(*largest_key);
-    float hi_a = avg * 4.0f, hi_b = avg * 0.9f + largest * 0.1f;
-    thr[0] = avg * 3.0f;                  // area_thresh_low
-    thr[1] = fmaxf(hi_a, hi_b);           // area_thresh_high (f32::max)
-    thr[2] = avg;
-    thr[3] = largest;
+    double t = 0.0;
+    for (int w = 0; w < BLK / 32; w++) t += sw[w];
+    bsum[blockIdx.x] = t;
   }
+}
+
+__global__ void __launch_bounds__(BLK) k_block_transform(const float* __restrict__ ha, uint32_t n,
+                                                         const double* __restrict__ bsum, BlockT* __restrict__ out) {
+  __shared__ float buf[SUM_BLOCK];
+  __shared__ double sw[BLK / 32];
+  const uint32_t b = blockIdx.x;
+  const uint32_t base = b * SUM_BLOCK;
+  const uint32_t m = min((uint32_t)SUM_BLOCK, n - base);
+  for (uint32_t j = threadIdx.x; j < SUM_BLOCK; j += BLK) buf[j] = j < m ? ha[base + j] : 0.0f;
+  // approximate running sum at the block start: sum of the earlier blocks
+  double acc = 0.0;
+  for (uint32_t k = threadIdx.x; k < b; k += BLK) acc += bsum[k];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  double start = 0.0;
+  for (int w = 0; w < BLK / 32; w++) start += sw[w];
+  int e0 = start > 0.0 ? ilogb(start) : -200;
+  const int t = threadIdx.x;
+  if (t < 2 * NCAND_E) {
+    const int ci = t >> 1, par = t & 1;
+    const int e = e0 - 1 + ci;
+    long long inc = 0;
+    int p = par;
+    bool ok = e >= -126 && e <= 127;
+    const double scale = ok ? ldexp(1.0, 23 - e) : 0.0;  // 1 / u
+    for (uint32_t j = 0; ok && j < m; j++) {
+      double x = (double)buf[j] * scale;
+      if (!(x < 16777216.0)) {  // the element alone leaves the binade (or NaN)
+        ok = false;
+        break;
+      }
+      double fl = floor(x);
+      double f = x - fl;
+      long long mm = (long long)fl;
+      long long r = f < 0.5 ? 0 : (f > 0.5 ? 1 : (((p + mm) & 1) ? 1 : 0));
+      inc += mm + r;
+      p = (int)((p + mm + r) & 1);
+    }
+    out[b].inc[ci][par] = inc;
+    if (par == 0) out[b].valid[ci] = ok ? 1 : 0;
+    if (t == 0) out[b].e0 = e0;
+  }
+}
+
+// One thread chains the blocks; then the preset thresholds
+// (src/splits.rs:23-33).
+__global__ void k_sum_chain(const float* __restrict__ ha, uint32_t n, const BlockT* __restrict__ tr,
+                            const int* largest_key, float* thr) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const uint32_t nb = (n + SUM_BLOCK - 1) / SUM_BLOCK;
+  float s = 0.0f;
+  uint32_t sequential_blocks = 0;
+  for (uint32_t b = 0; b < nb; b++) {
+    const uint32_t base = b * SUM_BLOCK;
+    const uint32_t m = min((uint32_t)SUM_BLOCK, n - base);
+    bool done = false;
+    const uint32_t bits = __float_as_uint(s);
+    const int ex = (int)((bits >> 23) & 0xff);
+    if (ex != 0 && ex != 0xff) {  // normal, positive
+      const int e = ex - 127;
+      const int ci = e - tr[b].e0 + 1;
+      if (ci >= 0 && ci < NCAND_E && tr[b].valid[ci]) {
+        const long long S = (long long)((bits & 0x7fffffu) | 0x800000u);
+        const long long S2 = S + tr[b].inc[ci][S & 1];
+        if (S2 < 16777216ll) {
+          s = __uint_as_float(((uint32_t)ex << 23) | (uint32_t)(S2 - 8388608ll));
+          done = true;
+        }
+      }
+    }
+    if (!done) {
+      for (uint32_t j = 0; j < m; j++) s = __fadd_rn(s, ha[base + j]);
+      sequential_blocks++;
+    }
+  }
+  const float avg = s / (float)n;
+  const float largest = fkey_inv(*largest_key);
+  const float hi_a = avg * 4.0f, hi_b = avg * 0.9f + largest * 0.1f;
+  thr[0] = avg * 3.0f;         // area_thresh_low
+  thr[1] = fmaxf(hi_a, hi_b);  // area_thresh_high (f32::max)
+  thr[2] = avg;
+  thr[3] = largest;
+  thr[4] = s;
+  thr[5] = __uint_as_float(sequential_blocks);
 }
 
 // split_triangle (src/splits.rs:127-158).
@@ -318,12 +404,9 @@ static int compact(BuildCtx& c, const uint32_t* flag, uint32_t n, const uint32_t
   *kept = 0;
   if (!n) return 0;
   uint32_t nb = div_up<uint32_t>(n, CHUNK);
-  c.kernel_launches++;
-  k_count_flags<<<nb, BLK, 0, c.stream>>>(flag, n, partial);
-  c.kernel_launches++;
-  k_scan_partials<<<1, 1024, 0, c.stream>>>(partial, nb, d_total);
-  c.kernel_launches++;
-  k_compact<<<nb, BLK, 0, c.stream>>>(flag, partial, n, in, out);
+  KLAUNCH("k_count_flags", k_count_flags<<<nb, BLK, 0, c.stream>>>(flag, n, partial));
+  KLAUNCH("k_scan_partials", k_scan_partials<<<1, 1024, 0, c.stream>>>(partial, nb, d_total));
+  KLAUNCH("k_compact", k_compact<<<nb, BLK, 0, c.stream>>>(flag, partial, n, in, out));
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(c.h_small, d_total, 4, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
@@ -352,8 +435,19 @@ static int grow_keep(BuildCtx& c, int slot, size_t need, size_t used) {
   return 0;
 }
 
+int split_thresholds_device(BuildCtx& c, const float* tris, uint32_t n, float* out6) {
+  float* a = nullptr;
+  uint32_t* ix = nullptr;
+  uint32_t m = 0;
+  int r = presplit_device(c, tris, n, &a, &ix, &m, true);
+  if (r) return r;
+  CK(cudaMemcpyAsync(out6, c.scratch.ptr[SLOT_SPLIT_MISC], 24, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return 0;
+}
+
 int presplit_device(BuildCtx& c, const float* tris, uint32_t n, float** aabbs_out, uint32_t** idx_out,
-                    uint32_t* m_out) {
+                    uint32_t* m_out, bool thresholds_only) {
   Scratch& s = c.scratch;
   *m_out = 0;
   if (n == 0) return 0;
@@ -367,20 +461,26 @@ int presplit_device(BuildCtx& c, const float* tris, uint32_t n, float** aabbs_ou
       (r = grow_keep(c, SLOT_FLAGS, (size_t)n * 4, 0)) ||
       (r = grow_keep(c, SLOT_PARTIAL, ((size_t)n / CHUNK + 2) * 8, 0)))
     return r;
-  float* thr = misc;  // [0] low [1] high [2] avg [3] largest
+  float* thr = misc;  // [0] low [1] high [2] avg [3] largest [4] sum [5] sequential blocks
   int* largest_key = (int*)(misc + 8);
   uint32_t* d_total = (uint32_t*)(misc + 9);
   int zero_key = 0;
   CK(cudaMemcpyAsync(largest_key, &zero_key, 4, cudaMemcpyHostToDevice, c.stream));
   uint32_t g = div_up<uint32_t>(n, BLK);
-  c.kernel_launches++;
-  k_tri_boxes<<<g, BLK, 0, c.stream>>>(tris, n, (float*)s.ptr[SLOT_SPLIT_AABBS], (uint32_t*)s.ptr[SLOT_SPLIT_IDX], ha,
-                                        largest_key, c.d_status);
-  c.kernel_launches++;
-  k_avg_thresholds<<<1, BLK, 0, c.stream>>>(ha, n, largest_key, thr);
-  c.kernel_launches++;
-  k_initial_flags<<<g, BLK, 0, c.stream>>>(ha, n, thr, (uint32_t*)s.ptr[SLOT_FLAGS], (uint32_t*)s.ptr[SLOT_SPLIT_CAND2]);
+  KLAUNCH("k_tri_boxes", k_tri_boxes<<<g, BLK, 0, c.stream>>>(tris, n, (float*)s.ptr[SLOT_SPLIT_AABBS], (uint32_t*)s.ptr[SLOT_SPLIT_IDX], ha,
+                                        largest_key, c.d_status));
+  {
+    const uint32_t nb = div_up<uint32_t>(n, SUM_BLOCK);
+    double* bsum = (double*)s.get(SLOT_OUTPUT, (size_t)nb * 8 + 16);
+    BlockT* tr = (BlockT*)s.get(SLOT_TILE_HIST, (size_t)nb * sizeof(BlockT) + 16);
+    if (!bsum || !tr) return c.fail(OBVHS_ERR_OOM, "scratch");
+    KLAUNCH("k_block_dsum", k_block_dsum<<<nb, BLK, 0, c.stream>>>(ha, n, bsum));
+    KLAUNCH("k_block_transform", k_block_transform<<<nb, BLK, 0, c.stream>>>(ha, n, bsum, tr));
+    KLAUNCH("k_sum_chain", k_sum_chain<<<1, 32, 0, c.stream>>>(ha, n, tr, largest_key, thr));
+  }
+  KLAUNCH("k_initial_flags", k_initial_flags<<<g, BLK, 0, c.stream>>>(ha, n, thr, (uint32_t*)s.ptr[SLOT_FLAGS], (uint32_t*)s.ptr[SLOT_SPLIT_CAND2]));
   CK(cudaGetLastError());
+  if (thresholds_only) return 0;
   uint32_t ncand = 0;
   r = compact(c, (uint32_t*)s.ptr[SLOT_FLAGS], n, (uint32_t*)s.ptr[SLOT_SPLIT_CAND2], (uint32_t*)s.ptr[SLOT_SPLIT_CAND],
               (uint32_t*)s.ptr[SLOT_PARTIAL], d_total, &ncand);
@@ -402,16 +502,12 @@ int presplit_device(BuildCtx& c, const float* tris, uint32_t n, float** aabbs_ou
     uint32_t* flag = (uint32_t*)s.ptr[SLOT_FLAGS];
     float* right = (float*)s.ptr[SLOT_REINS];
     uint32_t* partial = (uint32_t*)s.ptr[SLOT_PARTIAL];
-    c.kernel_launches++;
-    k_split<<<div_up<uint32_t>(ncand, BLK), BLK, 0, c.stream>>>(cand, ncand, aabbs, idx, tris, thr, right, flag);
+    KLAUNCH("k_split", k_split<<<div_up<uint32_t>(ncand, BLK), BLK, 0, c.stream>>>(cand, ncand, aabbs, idx, tris, thr, right, flag));
     uint32_t nb = div_up<uint32_t>(ncand, CHUNK);
-    c.kernel_launches++;
-    k_count_flags<<<nb, BLK, 0, c.stream>>>(flag, ncand, partial);
-    c.kernel_launches++;
-    k_scan_partials<<<1, 1024, 0, c.stream>>>(partial, nb, d_total);
+    KLAUNCH("k_count_flags", k_count_flags<<<nb, BLK, 0, c.stream>>>(flag, ncand, partial));
+    KLAUNCH("k_scan_partials", k_scan_partials<<<1, 1024, 0, c.stream>>>(partial, nb, d_total));
     // the appended entries become candidates after the current ones
-    c.kernel_launches++;
-    k_append<<<nb, BLK, 0, c.stream>>>(flag, partial, ncand, cand, right, len, aabbs, idx, cand + ncand);
+    KLAUNCH("k_append", k_append<<<nb, BLK, 0, c.stream>>>(flag, partial, ncand, cand, right, len, aabbs, idx, cand + ncand));
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(c.h_small, d_total, 4, cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
@@ -419,8 +515,7 @@ int presplit_device(BuildCtx& c, const float* tris, uint32_t n, float** aabbs_ou
     if (added == 0) break;
     len += added;
     uint32_t total = ncand + added;
-    c.kernel_launches++;
-    k_keep_flags<<<div_up<uint32_t>(total, BLK), BLK, 0, c.stream>>>(cand, total, aabbs, thr, flag);
+    KLAUNCH("k_keep_flags", k_keep_flags<<<div_up<uint32_t>(total, BLK), BLK, 0, c.stream>>>(cand, total, aabbs, thr, flag));
     CK(cudaGetLastError());
     r = compact(c, flag, total, cand, cand2, partial, d_total, &ncand);
     if (r) return r;

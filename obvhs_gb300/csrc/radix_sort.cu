@@ -1,15 +1,35 @@
 // radix_sort.cu -- see radix_sort.cuh.
+//
+// Onesweep-style LSD radix sort (8-bit digits):
+//   k_rs_hist      one read of the keys: a 256-bin histogram per digit
+//   k_rs_scan      exclusive scan of every histogram (global digit bases)
+//   k_rs_pass      per digit: tiles claimed in launch order rank their keys
+//                  stably (warp match + per-warp digit counts), publish their
+//                  digit counts and find their global offsets by decoupled
+//                  look-back over earlier tiles, then scatter.
+// No host synchronisation.  The look-back waits only on tiles that were
+// claimed earlier and are therefore resident; every wait is bounded and sets
+// a status bit instead of spinning forever.
 #include "radix_sort.cuh"
+#include "build.h"
 
 namespace {
 
 constexpr int THREADS = 256;
-constexpr int ROUNDS = RADIX_TILE / THREADS;  // 16
 constexpr int WARPS = THREADS / 32;
+constexpr uint32_t FLAG_AGG = 1u << 30;
+constexpr uint32_t FLAG_INC = 2u << 30;
+constexpr uint32_t VAL_MASK = (1u << 30) - 1;
+constexpr uint32_t SPIN_LIMIT = 1u << 24;
 
 template <class K>
-__global__ void __launch_bounds__(THREADS) k_rs_hist_all(const K* __restrict__ keys, uint32_t n,
-                                                         uint32_t* __restrict__ all_hist) {
+struct Tile {
+  static constexpr int ITEMS = KeyTraits<K>::BYTES >= 16 ? 8 : 16;
+  static constexpr int SIZE = THREADS * ITEMS;
+};
+
+template <class K>
+__global__ void __launch_bounds__(THREADS) k_rs_hist(const K* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist) {
   constexpr int NB = KeyTraits<K>::BYTES;
   __shared__ uint32_t h[NB * 256];
   for (int i = threadIdx.x; i < NB * 256; i += THREADS) h[i] = 0;
@@ -21,95 +41,68 @@ __global__ void __launch_bounds__(THREADS) k_rs_hist_all(const K* __restrict__ k
   }
   __syncthreads();
   for (int i = threadIdx.x; i < NB * 256; i += THREADS)
-    if (h[i]) atomicAdd(&all_hist[i], h[i]);
+    if (h[i]) atomicAdd(&hist[i], h[i]);
 }
 
-template <class K>
-__global__ void __launch_bounds__(THREADS) k_rs_tile_hist(const K* __restrict__ keys, uint32_t n, int byte,
-                                                          uint32_t ntiles, uint32_t* __restrict__ tile_hist) {
-  __shared__ uint32_t h[256];
-  h[threadIdx.x] = 0;
-  __syncthreads();
-  uint32_t base = blockIdx.x * RADIX_TILE;
-#pragma unroll 4
-  for (int r = 0; r < ROUNDS; r++) {
-    uint32_t i = base + r * THREADS + threadIdx.x;
-    if (i < n) atomicAdd(&h[KeyTraits<K>::digit(keys[i], byte)], 1u);
-  }
-  __syncthreads();
-  tile_hist[threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
-}
-
-// One block per digit: exclusive scan of its tile counts, offset by the
-// number of keys with a smaller digit.
-__global__ void __launch_bounds__(THREADS) k_rs_tile_scan(uint32_t* __restrict__ tile_hist, uint32_t ntiles,
-                                                          const uint32_t* __restrict__ digit_hist) {
-  __shared__ uint32_t s_base;
-  __shared__ uint32_t s_warp[WARPS];
-  const uint32_t d = blockIdx.x;
-  if (threadIdx.x == 0) {
-    uint32_t b = 0;
-    for (uint32_t k = 0; k < d; k++) b += digit_hist[k];
-    s_base = b;
-  }
-  __syncthreads();
-  uint32_t carry = s_base;
-  uint32_t* row = tile_hist + (size_t)d * ntiles;
+// block b scans histogram b in place (exclusive)
+__global__ void __launch_bounds__(THREADS) k_rs_scan(uint32_t* hist) {
+  __shared__ uint32_t sw[WARPS];
+  uint32_t* h = hist + blockIdx.x * 256;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (uint32_t start = 0; start < ntiles; start += THREADS) {
-    uint32_t t = start + threadIdx.x;
-    uint32_t v = t < ntiles ? row[t] : 0;
-    uint32_t x = v;
+  uint32_t v = h[threadIdx.x], x = v;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) s_warp[warp] = x;
-    __syncthreads();
-    uint32_t wp = 0, tot = 0;
-    for (int w = 0; w < WARPS; w++) {
-      uint32_t c = s_warp[w];
-      if (w < warp) wp += c;
-      tot += c;
-    }
-    if (t < ntiles) row[t] = carry + wp + x - v;
-    carry += tot;
-    __syncthreads();
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
   }
+  if (lane == 31) sw[warp] = x;
+  __syncthreads();
+  uint32_t pre = 0;
+  for (int w = 0; w < warp; w++) pre += sw[w];
+  h[threadIdx.x] = pre + x - v;
 }
 
 template <class K>
-__global__ void __launch_bounds__(THREADS) k_rs_scatter(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
-                                                        K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
-                                                        uint32_t n, int byte, uint32_t ntiles,
-                                                        const uint32_t* __restrict__ tile_off, bool iota) {
-  __shared__ uint32_t s_off[256];
+__global__ void __launch_bounds__(THREADS) k_rs_pass(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                                                     K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+                                                     uint32_t n, int byte, bool iota,
+                                                     const uint32_t* __restrict__ digit_base,
+                                                     uint32_t* tile_status, uint32_t* tile_counter, uint32_t* status) {
+  constexpr int ITEMS = Tile<K>::ITEMS;
+  constexpr int TS = Tile<K>::SIZE;
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_run[256];       // running digit counts in this tile
   __shared__ uint32_t s_cnt[WARPS][256];
   __shared__ uint32_t s_pre[WARPS][256];
+  __shared__ uint32_t s_off[256];       // global offset of each digit for this tile
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  s_off[tid] = tile_off[(size_t)tid * ntiles + blockIdx.x];
+  if (tid == 0) s_tile = atomicAdd(tile_counter, 1u);
+  s_run[tid] = 0;
 #pragma unroll
   for (int w = 0; w < WARPS; w++) s_cnt[w][tid] = 0;
   __syncthreads();
+  const uint32_t tile = s_tile;
+  const uint32_t base = tile * TS;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  uint32_t base = blockIdx.x * RADIX_TILE;
-  for (int r = 0; r < ROUNDS; r++) {
-    uint32_t i = base + r * THREADS + tid;
-    bool valid = i < n;
-    K k;
-    uint32_t v = 0, d = 256;
+  K key[ITEMS];
+  uint32_t val[ITEMS], rank[ITEMS], dig[ITEMS];
+#pragma unroll
+  for (int r = 0; r < ITEMS; r++) {
+    const uint32_t i = base + r * THREADS + tid;
+    const bool valid = i < n;
+    uint32_t d = 256;
     if (valid) {
-      k = keys_in[i];
-      v = iota ? i : vals_in[i];
-      d = KeyTraits<K>::digit(k, byte);
+      key[r] = keys_in[i];
+      val[r] = iota ? i : vals_in[i];
+      d = KeyTraits<K>::digit(key[r], byte);
     }
-    uint32_t peers = __match_any_sync(0xffffffffu, d);
-    uint32_t lrank = __popc(peers & lt_mask);
+    dig[r] = d;
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t lrank = __popc(peers & lt_mask);
     if (valid && lrank == 0) s_cnt[warp][d] = __popc(peers);
     __syncthreads();
     {
-      uint32_t run = s_off[tid];
+      uint32_t run = s_run[tid];
 #pragma unroll
       for (int w = 0; w < WARPS; w++) {
         uint32_t c = s_cnt[w][tid];
@@ -117,77 +110,94 @@ __global__ void __launch_bounds__(THREADS) k_rs_scatter(const K* __restrict__ ke
         s_cnt[w][tid] = 0;
         run += c;
       }
-      s_off[tid] = run;
+      s_run[tid] = run;
     }
     __syncthreads();
-    if (valid) {
-      uint32_t pos = s_pre[warp][d] + lrank;
-      keys_out[pos] = k;
-      vals_out[pos] = v;
+    rank[r] = valid ? s_pre[warp][d] + lrank : 0;
+  }
+  // publish this tile's count of digit `tid`, then look back for the prefix
+  const uint32_t count = s_run[tid];
+  uint32_t* my = tile_status + (size_t)tile * 256 + tid;
+  uint32_t prefix = 0;
+  if (tile == 0) {
+    atomicExch(my, FLAG_INC | count);
+  } else {
+    atomicExch(my, FLAG_AGG | count);
+    int64_t t = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    while (t >= 0) {
+      uint32_t s = *((volatile uint32_t*)(tile_status + (size_t)t * 256 + tid));
+      if ((s & ~VAL_MASK) == 0) {
+        if (++spins > SPIN_LIMIT) {
+          atomicOr(status, 4u);  // ST_ITER_LIMIT
+          break;
+        }
+        continue;
+      }
+      prefix += s & VAL_MASK;
+      if (s & FLAG_INC) break;
+      t--;
+    }
+    atomicExch(my, FLAG_INC | (prefix + count));
+  }
+  s_off[tid] = digit_base[tid] + prefix;
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < ITEMS; r++) {
+    if (dig[r] < 256) {
+      const uint32_t pos = s_off[dig[r]] + rank[r];
+      keys_out[pos] = key[r];
+      vals_out[pos] = val[r];
     }
   }
 }
 
+__global__ void k_iota(uint32_t* v, uint32_t n) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = i;
+}
+
 }  // namespace
 
-uint32_t radix_tile_count(uint32_t n) { return (n + RADIX_TILE - 1) / RADIX_TILE; }
+uint32_t radix_tile_count(uint32_t n) { return (n + 2047) / 2048; }
+
+size_t radix_scratch_words(uint32_t n) {
+  // 16 histograms of 256 + per pass: tile status (256 per tile) + counter
+  return 16 * 256 + 16 * ((size_t)radix_tile_count(n) * 256 + 32);
+}
 
 template <class K>
-cudaError_t radix_sort_pairs(K* keys, uint32_t* vals, uint32_t n, bool init_iota, K* keys_alt, uint32_t* vals_alt,
-                             uint32_t* tile_hist, uint32_t* all_hist, uint32_t* h_all_hist, cudaStream_t stream,
-                             bool* result_in_alt, uint64_t* launches) {
+cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, bool init_iota, K* keys_alt,
+                             uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt) {
   constexpr int NB = KeyTraits<K>::BYTES;
+  constexpr int TS = Tile<K>::SIZE;
   *result_in_alt = false;
   if (n == 0) return cudaSuccess;
-  cudaError_t e = cudaMemsetAsync(all_hist, 0, NB * 256 * sizeof(uint32_t), stream);
+  const uint32_t ntiles = (n + TS - 1) / TS;
+  uint32_t* hist = scratch;
+  uint32_t* pass_area = scratch + 16 * 256;
+  const size_t pass_words = (size_t)ntiles * 256 + 32;
+  cudaError_t e = cudaMemsetAsync(scratch, 0, (16 * 256 + NB * pass_words) * sizeof(uint32_t), c.stream);
   if (e) return e;
-  uint32_t hist_blocks = (n + THREADS * 16 - 1) / (THREADS * 16);
-  if (hist_blocks > 1024) hist_blocks = 1024;
-  k_rs_hist_all<K><<<hist_blocks, THREADS, 0, stream>>>(keys, n, all_hist);
-  *launches += 1;
-  e = cudaMemcpyAsync(h_all_hist, all_hist, NB * 256 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream);
-  if (e) return e;
-  e = cudaStreamSynchronize(stream);
-  if (e) return e;
-  uint32_t ntiles = radix_tile_count(n);
+  uint32_t hb = (n + THREADS * 16 - 1) / (THREADS * 16);
+  if (hb > 1024) hb = 1024;
+  KLAUNCH("k_rs_hist", k_rs_hist<K><<<hb, THREADS, 0, c.stream>>>(keys, n, hist));
+  KLAUNCH("k_rs_scan", k_rs_scan<<<NB, THREADS, 0, c.stream>>>(hist));
   K* kin = keys;
   uint32_t* vin = vals;
   K* kout = keys_alt;
   uint32_t* vout = vals_alt;
   bool iota = init_iota;
   for (int b = 0; b < NB; b++) {
-    bool constant = false;
-    for (int d = 0; d < 256; d++)
-      if (h_all_hist[b * 256 + d] == n) constant = true;
-    if (constant) continue;
-    k_rs_tile_hist<K><<<ntiles, THREADS, 0, stream>>>(kin, n, b, ntiles, tile_hist);
-    k_rs_tile_scan<<<256, THREADS, 0, stream>>>(tile_hist, ntiles, all_hist + b * 256);
-    k_rs_scatter<K><<<ntiles, THREADS, 0, stream>>>(kin, vin, kout, vout, n, b, ntiles, tile_hist, iota);
-    *launches += 3;
+    uint32_t* ts = pass_area + (size_t)b * pass_words;
+    KLAUNCH("k_rs_pass", k_rs_pass<K><<<ntiles, THREADS, 0, c.stream>>>(kin, vin, kout, vout, n, b, iota,
+                                                                         hist + b * 256, ts + 32, ts, c.d_status));
     iota = false;
-    K* tk = kin;
-    kin = kout;
-    kout = tk;
-    uint32_t* tv = vin;
-    vin = vout;
-    vout = tv;
+    std::swap(kin, kout);
+    std::swap(vin, vout);
     *result_in_alt = !*result_in_alt;
-  }
-  if (iota) {
-    // every digit was constant: the order is the identity
-    extern cudaError_t fill_iota(uint32_t*, uint32_t, cudaStream_t);
-    e = fill_iota(vals, n, stream);
-    *launches += 1;
-    if (e) return e;
   }
   return cudaGetLastError();
 }
-
-namespace {
-__global__ void k_iota(uint32_t* v, uint32_t n) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = i;
-}
-}  // namespace
 
 cudaError_t fill_iota(uint32_t* v, uint32_t n, cudaStream_t s) {
   if (!n) return cudaSuccess;
@@ -197,10 +207,9 @@ cudaError_t fill_iota(uint32_t* v, uint32_t n, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-template cudaError_t radix_sort_pairs<uint32_t>(uint32_t*, uint32_t*, uint32_t, bool, uint32_t*, uint32_t*, uint32_t*,
-                                                uint32_t*, uint32_t*, cudaStream_t, bool*, uint64_t*);
-template cudaError_t radix_sort_pairs<unsigned long long>(unsigned long long*, uint32_t*, uint32_t, bool,
-                                                          unsigned long long*, uint32_t*, uint32_t*, uint32_t*,
-                                                          uint32_t*, cudaStream_t, bool*, uint64_t*);
-template cudaError_t radix_sort_pairs<U128>(U128*, uint32_t*, uint32_t, bool, U128*, uint32_t*, uint32_t*, uint32_t*,
-                                            uint32_t*, cudaStream_t, bool*, uint64_t*);
+template cudaError_t radix_sort_pairs<uint32_t>(obvhs_ctx&, uint32_t*, uint32_t*, uint32_t, bool, uint32_t*, uint32_t*,
+                                                uint32_t*, bool*);
+template cudaError_t radix_sort_pairs<unsigned long long>(obvhs_ctx&, unsigned long long*, uint32_t*, uint32_t, bool,
+                                                          unsigned long long*, uint32_t*, uint32_t*, bool*);
+template cudaError_t radix_sort_pairs<U128>(obvhs_ctx&, U128*, uint32_t*, uint32_t, bool, U128*, uint32_t*, uint32_t*,
+                                            bool*);

@@ -5,12 +5,8 @@
 // The reference's sorts are unstable; this one is stable, so equal keys keep
 // their input order (the oracle breaks ties the same way).
 //
-// Design (per 8-bit digit, skipping digits that are constant over all keys):
-//   1. k_rs_hist_all   one read of the keys -> a 256-bin histogram for every
-//                      digit position (decides which passes can be skipped)
-//   2. k_rs_tile_hist  per 4096-key tile digit counts (digit-major layout)
-//   3. k_rs_tile_scan  per digit, exclusive scan over tiles + digit base
-//   4. k_rs_scatter    stable in-tile ranks with __match_any_sync, scatter
+// Onesweep-style: one histogram pass for all digits, then one kernel per
+// digit with decoupled look-back (see radix_sort.cu).
 #pragma once
 
 #include <cstdint>
@@ -42,22 +38,16 @@ struct KeyTraits<U128> {
   }
 };
 
-struct RadixScratch {
-  void* keys_alt = nullptr;
-  uint32_t* vals_alt = nullptr;
-  uint32_t* tile_hist = nullptr;  // 256 * ntiles
-  uint32_t* all_hist = nullptr;   // 16 * 256
-  uint32_t* h_all_hist = nullptr; // pinned host copy
-};
-
-// Sorts keys[0..n) with values vals[0..n) (vals == identity if init_iota).
-// On return *result_in_alt tells whether the sorted data ended in the
-// scratch ("alt") buffers.  Launches on `stream`; synchronises once to read
-// the digit histogram.  Returns a cudaError_t.
+// Sorts keys[0..n) with values vals[0..n) (vals = 0..n-1 if init_iota).
+// On return *result_in_alt tells whether the sorted data ended in the "alt"
+// buffers.  `scratch` holds radix_scratch_words(n) words; the context's
+// status word receives an error bit if a look-back wait gives up.  Launches
+// on the context's stream; no host synchronisation.
+struct obvhs_ctx;
 template <class K>
-cudaError_t radix_sort_pairs(K* keys, uint32_t* vals, uint32_t n, bool init_iota, K* keys_alt, uint32_t* vals_alt,
-                             uint32_t* tile_hist, uint32_t* all_hist, uint32_t* h_all_hist, cudaStream_t stream,
-                             bool* result_in_alt, uint64_t* launches);
+cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, bool init_iota, K* keys_alt,
+                             uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt);
 
+size_t radix_scratch_words(uint32_t n);
+cudaError_t fill_iota(uint32_t* v, uint32_t n, cudaStream_t s);
 uint32_t radix_tile_count(uint32_t n);
-constexpr int RADIX_TILE = 4096;

@@ -239,12 +239,19 @@ __global__ void k_mis(MisArgs a) {
   }
 }
 
-// reinsert_node (src/bvh2/reinsertion.rs:336-382), structural part.
-__global__ void k_apply(Bvh2Node* __restrict__ nodes, const uint32_t* __restrict__ parents, const Reins* __restrict__ reins,
+// reinsert_node (src/bvh2/reinsertion.rs:336-382): moves the nodes and
+// updates the parent links exactly as the reference does.  Accepted
+// proposals never share a moved node or a child of one, so they run in
+// parallel without conflicts.
+__global__ void k_apply(Bvh2Node* __restrict__ nodes, uint32_t* __restrict__ parents, const Reins* __restrict__ reins,
                         const uint32_t* __restrict__ order, const uint8_t* __restrict__ state, const uint32_t* n_pos,
-                        uint32_t* applied) {
+                        uint32_t* applied, uint2* __restrict__ starts) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= *n_pos || state[k] != 1) return;
+  if (k >= *n_pos) return;
+  if (state[k] != 1) {
+    starts[k] = make_uint2(OBVHS_INVALID, OBVHS_INVALID);
+    return;
+  }
   Reins r = reins[order[k]];
   uint32_t sib = sibling_of(r.from);
   uint32_t parent = parents[r.from];
@@ -256,44 +263,102 @@ __global__ void k_apply(Bvh2Node* __restrict__ nodes, const uint32_t* __restrict
   st_node(&nodes[r.to], inner);
   st_node(&nodes[sib], dst);
   st_node(&nodes[parent], sib_node);
+  if (node_prims(dst) == 0) {
+    parents[node_first(dst)] = sib;
+    parents[node_first(dst) + 1] = sib;
+  }
+  if (node_prims(sib_node) == 0) {
+    parents[node_first(sib_node)] = parent;
+    parents[node_first(sib_node) + 1] = parent;
+  }
+  parents[sib] = r.to;
+  parents[r.from] = r.to;
+  // boxes to refit: `to` and its ancestors, and the ancestors of `parent`
+  starts[k] = make_uint2(r.to, parent);
   atomicAdd(applied, 1u);
 }
 
-// Bottom-up refit of every inner node: the second child to arrive computes
-// the union (Bvh2::refit_from semantics: union(first_child, second_child)).
-__global__ void k_refit(Bvh2Node* nodes, const uint32_t* __restrict__ parents, uint32_t n, uint32_t* flags,
-                        uint32_t* status) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  Bvh2Node me = ld_node(&nodes[i]);
-  if (node_prims(me) == 0 || i == 0) return;
-  uint32_t p = parents[i];
+// Marks every node whose box may have changed and lists it once.
+__device__ __forceinline__ void mark_path(uint32_t x, const uint32_t* parents, uint32_t* dirty, uint32_t* list,
+                                          uint32_t* list_n, uint32_t n) {
   for (uint32_t guard = 0; guard < n; guard++) {
+    if (atomicExch(&dirty[x], 1u) != 0) return;  // the rest of the path is marked already
+    list[atomicAdd(list_n, 1u)] = x;
+    if (x == 0) return;
+    x = parents[x];
+  }
+}
+
+__global__ void k_mark(const uint2* __restrict__ starts, const uint32_t* n_pos, const uint32_t* __restrict__ parents,
+                       uint32_t* dirty, uint32_t* list, uint32_t* list_n, uint32_t n) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= *n_pos) return;
+  uint2 s = starts[k];
+  if (s.x == OBVHS_INVALID) return;
+  mark_path(s.x, parents, dirty, list, list_n, n);
+  if (s.y != 0) mark_path(parents[s.y], parents, dirty, list, list_n, n);
+}
+
+// pending[x] = number of marked children of x.
+__global__ void k_count_dirty(const uint32_t* __restrict__ list, const uint32_t* list_n,
+                              const uint32_t* __restrict__ parents, uint32_t* pending) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= *list_n) return;
+  uint32_t x = list[k];
+  if (x != 0) atomicAdd(&pending[parents[x]], 1u);
+}
+
+__device__ __forceinline__ void refit_one(Bvh2Node* nodes, uint32_t p) {
+  Bvh2Node pn = ld_node(&nodes[p]);
+  uint32_t f = node_first(pn);
+  const float4* q0 = reinterpret_cast<const float4*>(&nodes[f]);
+  const float4* q1 = reinterpret_cast<const float4*>(&nodes[f + 1]);
+  float4 a0 = __ldcg(q0), b0 = __ldcg(q0 + 1), a1 = __ldcg(q1), b1 = __ldcg(q1 + 1);
+  Box u = box_union(Box{make_float3(a0.x, a0.y, a0.z), make_float3(b0.x, b0.y, b0.z)},
+                    Box{make_float3(a1.x, a1.y, a1.z), make_float3(b1.x, b1.y, b1.z)});
+  float4* w = reinterpret_cast<float4*>(&nodes[p]);
+  __stcg(w, make_float4(u.mn.x, u.mn.y, u.mn.z, pn.a.w));
+  __stcg(w + 1, make_float4(u.mx.x, u.mx.y, u.mx.z, pn.b.w));
+}
+
+// Recomputes marked nodes bottom-up (Bvh2::refit_from semantics: union of
+// first and second child).  pending[x] (marked children of x) stays fixed
+// during the kernel; done[x] counts finished ones, and the thread finishing
+// the last marked child of x recomputes x.  Nodes without marked children
+// start the climbs.
+__global__ void k_refit_dirty(Bvh2Node* nodes, const uint32_t* __restrict__ parents, const uint32_t* __restrict__ list,
+                              const uint32_t* list_n, const uint32_t* __restrict__ pending, uint32_t* done, uint32_t n,
+                              uint32_t* status) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= *list_n) return;
+  uint32_t x = list[k];
+  if (pending[x] != 0) return;
+  for (uint32_t guard = 0; guard < n; guard++) {
+    if (node_prims(ld_node(&nodes[x])) == 0) refit_one(nodes, x);
+    if (x == 0) return;
+    x = parents[x];
     __threadfence();
-    if (atomicAdd(&flags[p], 1u) == 0) return;
+    if (atomicAdd(&done[x], 1u) + 1u != pending[x]) return;
     __threadfence();
-    Bvh2Node pn = ld_node(&nodes[p]);
-    uint32_t f = node_first(pn);
-    const float4* q0 = reinterpret_cast<const float4*>(&nodes[f]);
-    const float4* q1 = reinterpret_cast<const float4*>(&nodes[f + 1]);
-    float4 a0 = __ldcg(q0), b0 = __ldcg(q0 + 1), a1 = __ldcg(q1), b1 = __ldcg(q1 + 1);
-    Box u = box_union(Box{make_float3(a0.x, a0.y, a0.z), make_float3(b0.x, b0.y, b0.z)},
-                      Box{make_float3(a1.x, a1.y, a1.z), make_float3(b1.x, b1.y, b1.z)});
-    float4* w = reinterpret_cast<float4*>(&nodes[p]);
-    __stcg(w, make_float4(u.mn.x, u.mn.y, u.mn.z, pn.a.w));
-    __stcg(w + 1, make_float4(u.mx.x, u.mx.y, u.mx.z, pn.b.w));
-    if (p == 0) return;
-    p = parents[p];
   }
   set_status(status, ST_ITER_LIMIT);
+}
+
+__global__ void k_clear_dirty(const uint32_t* __restrict__ list, const uint32_t* list_n, uint32_t* dirty,
+                              uint32_t* pending, uint32_t* done) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= *list_n) return;
+  uint32_t x = list[k];
+  dirty[x] = 0;
+  pending[x] = 0;
+  done[x] = 0;
 }
 
 }  // namespace
 
 int compute_parents_device(BuildCtx& c, const Bvh2Node* nodes, uint32_t n_nodes, uint32_t* parents) {
-  c.kernel_launches++;
   if (!n_nodes) return 0;
-  k_parents<<<div_up<uint32_t>(n_nodes, BLK), BLK, 0, c.stream>>>(nodes, n_nodes, parents);
+  KLAUNCH("k_parents", k_parents<<<div_up<uint32_t>(n_nodes, BLK), BLK, 0, c.stream>>>(nodes, n_nodes, parents));
   CK(cudaGetLastError());
   return 0;
 }
@@ -316,25 +381,30 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
   }
   Scratch& s = c.scratch;
   uint32_t* parents = (uint32_t*)s.get(SLOT_PARENTS, (size_t)len * 4);
-  uint32_t* flags = (uint32_t*)s.get(SLOT_FLAGS, (size_t)len * 4);
+  uint32_t* dirty = (uint32_t*)s.get(SLOT_FLAGS, (size_t)len * 4);
+  uint32_t* pending = (uint32_t*)s.get(SLOT_PENDING, (size_t)len * 4);
+  uint32_t* done = (uint32_t*)s.get(SLOT_DONE, (size_t)len * 4);
+  uint32_t* list = (uint32_t*)s.get(SLOT_DIRTY_LIST, (size_t)len * 4);
+  uint2* starts = (uint2*)s.get(SLOT_STARTS, (size_t)len * 8);
   uint8_t* touched = (uint8_t*)s.get(SLOT_TOUCHED, (size_t)len);
   uint32_t* owner = (uint32_t*)s.get(SLOT_MIS_OWNER, (size_t)len * 4);
   uint32_t* keys = (uint32_t*)s.get(SLOT_REINS_KEYS, (size_t)len * 4);
   uint32_t* vals = (uint32_t*)s.get(SLOT_REINS_VALS, (size_t)len * 4);
   uint32_t* keys_alt = (uint32_t*)s.get(SLOT_KEYS_ALT, (size_t)len * 4);
   uint32_t* vals_alt = (uint32_t*)s.get(SLOT_VALS_ALT, (size_t)len * 4);
-  uint32_t* tile_hist = (uint32_t*)s.get(SLOT_TILE_HIST, (size_t)radix_tile_count(len) * 256 * 4 + 4);
-  uint32_t* all_hist = (uint32_t*)s.get(SLOT_ALL_HIST, 16 * 256 * 4);
+  uint32_t* rs = (uint32_t*)s.get(SLOT_ALL_HIST, radix_scratch_words(len) * 4);
   Reins* reins = (Reins*)s.get(SLOT_REINS, (size_t)len * sizeof(Reins));
   uint8_t* state = (uint8_t*)s.get(SLOT_MIS_STATE, (size_t)len);
   uint32_t* counters = (uint32_t*)s.get(SLOT_CW_COUNTERS, 64);
-  if (!parents || !flags || !touched || !owner || !keys || !vals || !keys_alt || !vals_alt || !tile_hist ||
-      !all_hist || !reins || !state || !counters)
+  if (!parents || !dirty || !pending || !done || !list || !starts || !touched || !owner || !keys || !vals || !keys_alt || !vals_alt || !rs || !reins || !state || !counters)
     return c.fail(OBVHS_ERR_OOM, "scratch");
   // counters: [0] n_pos, [1] applied, [2..4] MIS round counters
   CK(cudaMemsetAsync(counters, 0, 64, c.stream));
   int r = compute_parents_device(c, b->nodes, len, parents);
   if (r) return r;
+  CK(cudaMemsetAsync(dirty, 0, (size_t)len * 4, c.stream));
+  CK(cudaMemsetAsync(pending, 0, (size_t)len * 4, c.stream));
+  CK(cudaMemsetAsync(done, 0, (size_t)len * 4, c.stream));
 
   static int mis_blocks = 0;
   if (!mis_blocks) {
@@ -356,28 +426,23 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
     uint32_t count = node_count - 1;
     if (count == 0) continue;
     // find_candidates
-    c.kernel_launches++;
-    k_cand_keys<<<div_up<uint32_t>(ncand, BLK), BLK, 0, c.stream>>>(b->nodes, take, keys, vals);
+    KLAUNCH("k_cand_keys", k_cand_keys<<<div_up<uint32_t>(ncand, BLK), BLK, 0, c.stream>>>(b->nodes, take, keys, vals));
     bool alt = false;
-    cudaError_t e = radix_sort_pairs<uint32_t>(keys, vals, ncand, false, keys_alt, vals_alt, tile_hist, all_hist,
-                                               c.h_hist, c.stream, &alt, &c.kernel_launches);
+    cudaError_t e = radix_sort_pairs<uint32_t>(c, keys, vals, ncand, false, keys_alt, vals_alt, rs, &alt);
     if (e) return c.cuda_fail(e, "candidate sort");
     const uint32_t* cand = alt ? vals_alt : vals;
     // find_reinsertion for the first `count` candidates
-    c.kernel_launches++;
     if (clamp)
-      k_find<192, true><<<div_up<uint32_t>(count, 128), 128, 0, c.stream>>>(b->nodes, parents, cand, count, cap_rt,
-                                                                              reins, c.d_status);
+      KLAUNCH("k_find", k_find<192, true><<<div_up<uint32_t>(count, 128), 128, 0, c.stream>>>(b->nodes, parents, cand, count, cap_rt,
+                                                                              reins, c.d_status));
     else
-      k_find<1024, false><<<div_up<uint32_t>(count, 128), 128, 0, c.stream>>>(b->nodes, parents, cand, count, cap_rt,
-                                                                                reins, c.d_status);
+      KLAUNCH("k_find", k_find<1024, false><<<div_up<uint32_t>(count, 128), 128, 0, c.stream>>>(b->nodes, parents, cand, count, cap_rt,
+                                                                                reins, c.d_status));
     CK(cudaGetLastError());
     // priority order
     CK(cudaMemsetAsync(counters, 0, 4, c.stream));
-    c.kernel_launches++;
-    k_prio_keys<<<div_up<uint32_t>(count, BLK), BLK, 0, c.stream>>>(reins, count, keys, vals, counters);
-    e = radix_sort_pairs<uint32_t>(keys, vals, count, false, keys_alt, vals_alt, tile_hist, all_hist, c.h_hist,
-                                   c.stream, &alt, &c.kernel_launches);
+    KLAUNCH("k_prio_keys", k_prio_keys<<<div_up<uint32_t>(count, BLK), BLK, 0, c.stream>>>(reins, count, keys, vals, counters));
+    e = radix_sort_pairs<uint32_t>(c, keys, vals, count, false, keys_alt, vals_alt, rs, &alt);
     if (e) return c.cuda_fail(e, "proposal sort");
     const uint32_t* order = alt ? vals_alt : vals;
     // greedy conflict resolution in priority order
@@ -388,16 +453,16 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
     void* args[] = {&ma};
     uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)mis_blocks, std::max<uint64_t>(1, div_up<uint32_t>(count, BLK)));
     CK(cudaLaunchCooperativeKernel((void*)k_mis, grid, BLK, args, 0, c.stream));
-    c.kernel_launches++;
-    k_apply<<<div_up<uint32_t>(count, BLK), BLK, 0, c.stream>>>(b->nodes, parents, reins, order, state, counters,
-                                                                 counters + 1);
-    CK(cudaGetLastError());
-    // parents + refit
-    r = compute_parents_device(c, b->nodes, len, parents);
-    if (r) return r;
-    CK(cudaMemsetAsync(flags, 0, (size_t)len * 4, c.stream));
-    c.kernel_launches++;
-    k_refit<<<div_up<uint32_t>(len, BLK), BLK, 0, c.stream>>>(b->nodes, parents, len, flags, c.d_status);
+    const uint32_t gk = div_up<uint32_t>(count, BLK);
+    KLAUNCH("k_apply", k_apply<<<gk, BLK, 0, c.stream>>>(b->nodes, parents, reins, order, state, counters, counters + 1, starts));
+    KLAUNCH("k_mark", k_mark<<<gk, BLK, 0, c.stream>>>(starts, counters, parents, dirty, list, counters + 5, len));
+    // the list holds at most `len` nodes; its count is only known on the
+    // device, so these launches cover the worst case and exit early
+    const uint32_t gl = div_up<uint32_t>(len, BLK);
+    KLAUNCH("k_count_dirty", k_count_dirty<<<gl, BLK, 0, c.stream>>>(list, counters + 5, parents, pending));
+    KLAUNCH("k_refit_dirty", k_refit_dirty<<<gl, BLK, 0, c.stream>>>(b->nodes, parents, list, counters + 5, pending, done, len, c.d_status));
+    KLAUNCH("k_clear_dirty", k_clear_dirty<<<gl, BLK, 0, c.stream>>>(list, counters + 5, dirty, pending, done));
+    CK(cudaMemsetAsync(counters + 5, 0, 4, c.stream));
     CK(cudaGetLastError());
   }
   uint32_t applied = 0;

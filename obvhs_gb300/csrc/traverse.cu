@@ -248,9 +248,8 @@ int reorder_tris_device(BuildCtx& c, obvhs_cwbvh* b, const float* tris, uint32_t
     cudaGetLastError();
     return c.fail(OBVHS_ERR_OOM, "triangle buffer");
   }
-  c.kernel_launches++;
-  k_reorder_tris<<<div_up<uint32_t>(b->n_prims, 256), 256, 0, c.stream>>>(tris, n_tris, b->prim_indices, b->n_prims,
-                                                                          out, c.d_status);
+  KLAUNCH("k_reorder_tris", k_reorder_tris<<<div_up<uint32_t>(b->n_prims, 256), 256, 0, c.stream>>>(tris, n_tris, b->prim_indices, b->n_prims,
+                                                                          out, c.d_status));
   CK(cudaGetLastError());
   b->tris = out;
   return 0;
@@ -272,13 +271,12 @@ int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint
   }
   uint32_t want = div_up<uint32_t>(n, TBLK);
   uint32_t grid = std::min<uint32_t>(want, (uint32_t)(per_sm * c.num_sms));
-  c.kernel_launches++;
   if (mode == 0)
-    k_traverse<0><<<grid, TBLK, 0, c.stream>>>(bvh->nodes, bvh->n_nodes, bvh->tris, bvh->n_prims, (const float4*)rays, n,
-                                               (uint2*)hits, nullptr, counter, c.d_status);
+    KLAUNCH("k_traverse_closest", k_traverse<0><<<grid, TBLK, 0, c.stream>>>(bvh->nodes, bvh->n_nodes, bvh->tris, bvh->n_prims, (const float4*)rays, n,
+                                               (uint2*)hits, nullptr, counter, c.d_status));
   else
-    k_traverse<1><<<grid, TBLK, 0, c.stream>>>(bvh->nodes, bvh->n_nodes, bvh->tris, bvh->n_prims, (const float4*)rays, n, nullptr,
-                                               miss, counter, c.d_status);
+    KLAUNCH("k_traverse_occluded", k_traverse<1><<<grid, TBLK, 0, c.stream>>>(bvh->nodes, bvh->n_nodes, bvh->tris, bvh->n_prims, (const float4*)rays, n, nullptr,
+                                               miss, counter, c.d_status));
   CK(cudaGetLastError());
   return 0;
 }
