@@ -7,9 +7,13 @@
 //   count_primitives (:197-211)
 //
 // Costs: a parent-counter climb from the leaves (the second child to arrive
-// computes the parent).  The same climb also records, for every BVH2 node X
-// taken as a CWBVH node, ncw(X) = CWBVH nodes in its subtree and
-// lprims(X) = primitives held by X's leaf children.
+// computes the parent).  Besides the 7 decisions, every node records for
+// each decision slot i the aggregate of the CWBVH children that
+// get_children(node, i) yields: the CWBVH nodes below those children and the
+// primitives held by the leaf children.  A child that is itself distributed
+// contributes its own aggregate, so no record needs a tree walk.  Then
+// ncw(X) = 1 + agg(X, 0).nodes is the size of the CWBVH subtree rooted at X
+// and lprims(X) = agg(X, 0).prims the primitives of X's leaf children.
 //
 // Emission: the reference recurses depth-first, so a node's children go to
 // nodes.len() when it is visited and its primitives to
@@ -17,46 +21,48 @@
 // internal children c_1..c_k of X (slot order), child_base(c_1) =
 // child_base(X) + k, child_base(c_j+1) = child_base(c_j) + ncw(c_j) - 1;
 // prim_base(c_1) = prim_base(X) + lprims(X), prim_base(c_j+1) =
-// prim_base(c_j) + nprim(c_j).  Nodes are then emitted level by level, in
-// parallel, at exactly the reference's positions, so the output is byte for
-// byte the reference's CwBvh.
-#include <cooperative_groups.h>
-
+// prim_base(c_j) + nprim(c_j).  A warp per node (lane s = child slot s)
+// takes nodes from a device work queue in which every node's item is
+// published by its parent's warp, so nodes are written at exactly the
+// reference's positions: the output is byte for byte the reference's.
 #include "build.h"
-
-namespace cg = cooperative_groups;
 
 namespace {
 
 constexpr int BLK = 256;
+constexpr int EMIT_THREADS = 128;
 constexpr float PRIM_COST = 0.3f;
 constexpr float DENOM = 1.0f / 255.0f;
+constexpr uint32_t AGG_INVALID = 0xffffffffu;
 
 enum : uint8_t { K_LEAF = 0, K_INTERNAL = 1, K_DISTRIBUTE = 2 };
 constexpr uint8_t DL_INVALID = 7;
 
-struct Dec {
+struct __align__(16) Dec {
   float cost[7];
   uint32_t nprim;
   uint8_t meta[8];  // kind | dl << 2 | dr << 5  (dl/dr 7 = invalid)
+  uint2 agg[7];     // per decision slot: (CWBVH nodes below, leaf primitives)
 };
-static_assert(sizeof(Dec) == 40, "Dec layout");
-
-struct CwMeta {
-  uint32_t ncw;     // CWBVH nodes in the subtree of this node as a CWBVH node (0xffffffff: unusable)
-  uint32_t lprims;  // primitives in its leaf children
-};
+static_assert(sizeof(Dec) == 96, "Dec layout");
 
 struct Item {
   uint32_t bvh2, cw, child_base, prim_base;
 };
 
-// Dec is 40 bytes, so 8-byte aligned: five 8-byte L2 stores.
 __device__ __forceinline__ void st_dec(Dec* dst, const Dec& v) {
-  uint2* w = reinterpret_cast<uint2*>(dst);
-  const uint2* r = reinterpret_cast<const uint2*>(&v);
+  uint4* w = reinterpret_cast<uint4*>(dst);
+  const uint4* r = reinterpret_cast<const uint4*>(&v);
 #pragma unroll
-  for (int k = 0; k < 5; k++) __stcg(w + k, r[k]);
+  for (int k = 0; k < 6; k++) __stcg(w + k, r[k]);
+}
+__device__ __forceinline__ Dec ld_dec_cg(const Dec* src) {
+  Dec v;
+  const uint4* r = reinterpret_cast<const uint4*>(src);
+  uint4* w = reinterpret_cast<uint4*>(&v);
+#pragma unroll
+  for (int k = 0; k < 6; k++) w[k] = __ldcg(r + k);
+  return v;
 }
 
 __device__ __forceinline__ uint8_t mk(uint8_t kind, uint8_t dl, uint8_t dr) {
@@ -66,89 +72,57 @@ __device__ __forceinline__ uint8_t kind_of(uint8_t m) { return m & 3; }
 __device__ __forceinline__ uint8_t dl_of(uint8_t m) { return (m >> 2) & 7; }
 __device__ __forceinline__ uint8_t dr_of(uint8_t m) { return (m >> 5) & 7; }
 
-__device__ __forceinline__ uint8_t ld_meta(const Dec* d, uint32_t node, int i) {
-  return __ldcg(reinterpret_cast<const unsigned char*>(&d[node].meta[i]));
-}
-
-// get_children (src/cwbvh/bvh2_to_cwbvh.rs:346-397) with an explicit stack.
-// Returns the child count, or -1 on an invalid distribution.
-__device__ int get_children(const Bvh2Node* nodes, const Dec* dec, uint32_t x, uint32_t ch[8]) {
-  // stack entries: node | (i << 28) | (expand << 31)
-  uint32_t st[16];
-  int sp = 0, cnt = 0;
-  st[sp++] = x | 0x80000000u;
-  while (sp) {
-    uint32_t e = st[--sp];
-    uint32_t n = e & 0x0fffffffu;
-    if (!(e & 0x80000000u)) {
-      if (cnt >= 8) return -1;
-      ch[cnt++] = n;
-      continue;
-    }
-    int i = (e >> 28) & 7;
-    Bvh2Node nd = ld_node(&nodes[n]);
-    if (node_prims(nd) != 0) {
-      if (cnt >= 8) return -1;
-      ch[cnt++] = n;
-      continue;
-    }
-    uint8_t m = ld_meta(dec, n, i);
-    uint8_t dl = dl_of(m), dr = dr_of(m);
-    if (dl == DL_INVALID || dr == DL_INVALID) return -1;
-    uint32_t f = node_first(nd);
-    if (sp + 2 > 16) return -1;
-    // right first so the left subtree's children come out first
-    st[sp++] = kind_of(ld_meta(dec, f + 1, dr)) == K_DISTRIBUTE ? ((f + 1) | ((uint32_t)dr << 28) | 0x80000000u) : (f + 1);
-    st[sp++] = kind_of(ld_meta(dec, f, dl)) == K_DISTRIBUTE ? (f | ((uint32_t)dl << 28) | 0x80000000u) : f;
+// The aggregate one child contributes when its parent's distribution reaches
+// it with slot budget j: its own distribution if that is DISTRIBUTE, else
+// the child as one CWBVH child (internal: its whole subtree; leaf: prims).
+__device__ __forceinline__ uint2 child_term(const Dec& d, uint32_t j) {
+  if (kind_of(d.meta[j]) == K_DISTRIBUTE) return d.agg[j];
+  if (kind_of(d.meta[0]) == K_INTERNAL) {
+    if (d.agg[0].x == AGG_INVALID) return make_uint2(AGG_INVALID, 0);
+    return make_uint2(1 + d.agg[0].x, 0);
   }
-  return cnt;
+  return make_uint2(0, d.nprim);
 }
 
-__device__ __forceinline__ float ld_cost(const Dec* d, uint32_t node, int i) { return __ldcg(&d[node].cost[i]); }
-
-// calculate_cost_impl for one inner node whose children are complete.
-__device__ void inner_costs(const Bvh2Node* nodes, Dec* dec, CwMeta* meta, uint32_t x, uint32_t max_prims,
-                            uint32_t* status) {
-  Bvh2Node nd = ld_node(&nodes[x]);
+// calculate_cost_impl (src/cwbvh/bvh2_to_cwbvh.rs:257-341) for one inner node
+// whose children are complete, plus the aggregates.
+__device__ void inner_costs(const Bvh2Node* nodes, Dec* dec, uint32_t x, uint32_t max_prims) {
+  const Bvh2Node nd = ld_node(&nodes[x]);
   const float ha = half_area(node_box(nd));
   const uint32_t f = node_first(nd);
-  const uint32_t np = __ldcg(&dec[f].nprim) + __ldcg(&dec[f + 1].nprim);
-  float cl[7], cr[7];
-#pragma unroll
-  for (int k = 0; k < 7; k++) {
-    cl[k] = ld_cost(dec, f, k);
-    cr[k] = ld_cost(dec, f + 1, k);
-  }
-  float cost[7];
-  uint8_t m[7];
+  const Dec L = ld_dec_cg(&dec[f]);
+  const Dec R = ld_dec_cg(&dec[f + 1]);
+  const uint32_t np = L.nprim + R.nprim;
+  Dec out;
   {
-    float cost_leaf = np <= max_prims ? ((float)np * ha) * PRIM_COST : __int_as_float(0x7f800000);
+    const float cost_leaf = np <= max_prims ? ((float)np * ha) * PRIM_COST : __int_as_float(0x7f800000);
     float cd = __int_as_float(0x7f800000);
     uint8_t dl = DL_INVALID, dr = DL_INVALID;
 #pragma unroll
     for (int k = 0; k < 7; k++) {
-      float c = cl[k] + cr[6 - k];
+      const float c = L.cost[k] + R.cost[6 - k];
       if (c < cd) {
         cd = c;
         dl = (uint8_t)k;
         dr = (uint8_t)(6 - k);
       }
     }
-    float ci = cd + ha;
+    const float ci = cd + ha;
     if (cost_leaf < ci) {
-      cost[0] = cost_leaf;
-      m[0] = mk(K_LEAF, dl, dr);
+      out.cost[0] = cost_leaf;
+      out.meta[0] = mk(K_LEAF, dl, dr);
     } else {
-      cost[0] = ci;
-      m[0] = mk(K_INTERNAL, dl, dr);
+      out.cost[0] = ci;
+      out.meta[0] = mk(K_INTERNAL, dl, dr);
     }
   }
 #pragma unroll
   for (int i = 1; i < 7; i++) {
-    float cd = cost[i - 1];
+    float cd = out.cost[i - 1];
     uint8_t dl = DL_INVALID, dr = DL_INVALID;
+#pragma unroll
     for (int k = 0; k < i; k++) {
-      float c = cl[k] + cr[i - k - 1];
+      const float c = L.cost[k] + R.cost[i - k - 1];
       if (c < cd) {
         cd = c;
         dl = (uint8_t)k;
@@ -156,70 +130,52 @@ __device__ void inner_costs(const Bvh2Node* nodes, Dec* dec, CwMeta* meta, uint3
       }
     }
     if (dl != DL_INVALID) {
-      cost[i] = cd;
-      m[i] = mk(K_DISTRIBUTE, dl, dr);
+      out.cost[i] = cd;
+      out.meta[i] = mk(K_DISTRIBUTE, dl, dr);
     } else {
-      cost[i] = cost[i - 1];
-      m[i] = m[i - 1];
+      out.cost[i] = out.cost[i - 1];
+      out.meta[i] = out.meta[i - 1];
     }
-  }
-  Dec out;
-#pragma unroll
-  for (int i = 0; i < 7; i++) {
-    out.cost[i] = cost[i];
-    out.meta[i] = m[i];
   }
   out.meta[7] = 0;
   out.nprim = np;
-  st_dec(&dec[x], out);
-  // subtree sizes of x taken as a CWBVH node
-  uint32_t ch[8];
-  int cnt = get_children(nodes, dec, x, ch);
-  CwMeta cm{0xffffffffu, 0};
-  if (cnt >= 0) {
-    uint32_t ncw = 1, lp = 0;
-    bool ok = true;
-    for (int j = 0; j < cnt; j++) {
-      uint8_t k = kind_of(ld_meta(dec, ch[j], 0));
-      Bvh2Node cn = ld_node(&nodes[ch[j]]);
-      if (node_prims(cn) != 0 || k == K_LEAF) {
-        lp += node_prims(cn) != 0 ? node_prims(cn) : __ldcg(&dec[ch[j]].nprim);
-      } else if (k == K_INTERNAL) {
-        uint32_t s = __ldcg(&meta[ch[j]].ncw);
-        if (s == 0xffffffffu) ok = false;
-        ncw += s;
-      } else {
-        ok = false;
-      }
+#pragma unroll
+  for (int i = 0; i < 7; i++) {
+    const uint8_t dl = dl_of(out.meta[i]), dr = dr_of(out.meta[i]);
+    if (dl == DL_INVALID || dr == DL_INVALID) {
+      out.agg[i] = make_uint2(AGG_INVALID, 0);
+      continue;
     }
-    if (ok) cm = CwMeta{ncw, lp};
+    const uint2 a = child_term(L, dl), b = child_term(R, dr);
+    out.agg[i] = (a.x == AGG_INVALID || b.x == AGG_INVALID) ? make_uint2(AGG_INVALID, 0)
+                                                            : make_uint2(a.x + b.x, a.y + b.y);
   }
-  __stcg(reinterpret_cast<uint2*>(&meta[x]), make_uint2(cm.ncw, cm.lprims));
+  st_dec(&dec[x], out);
 }
 
 __global__ void __launch_bounds__(BLK) k_costs(const Bvh2Node* __restrict__ nodes, const uint32_t* __restrict__ parents,
-                                               uint32_t n, uint32_t max_prims, Dec* dec, CwMeta* meta, uint32_t* flags,
+                                               uint32_t n, uint32_t max_prims, Dec* dec, uint32_t* flags,
                                                uint32_t* status) {
-  uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  const uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i >= n) return;
-  Bvh2Node nd = ld_node(&nodes[i]);
+  const Bvh2Node nd = ld_node(&nodes[i]);
   if (node_prims(nd) == 0) return;
   if (node_prims(nd) != 1) {  // src/cwbvh/bvh2_to_cwbvh.rs:243-247
     set_status(status, ST_BAD_INPUT);
     return;
   }
   {
-    float cl = (half_area(node_box(nd)) * 1.0f) * PRIM_COST;
+    const float cl = (half_area(node_box(nd)) * 1.0f) * PRIM_COST;
     Dec d;
 #pragma unroll
     for (int k = 0; k < 7; k++) {
       d.cost[k] = cl;
       d.meta[k] = mk(K_LEAF, 0, 0);
+      d.agg[k] = make_uint2(0, 1);
     }
     d.meta[7] = 0;
     d.nprim = 1;
     st_dec(&dec[i], d);
-    __stcg(reinterpret_cast<uint2*>(&meta[i]), make_uint2(1u, 1u));
   }
   if (i == 0) return;
   uint32_t p = parents[i];
@@ -227,11 +183,44 @@ __global__ void __launch_bounds__(BLK) k_costs(const Bvh2Node* __restrict__ node
     __threadfence();
     if (atomicAdd(&flags[p], 1u) == 0) return;
     __threadfence();
-    inner_costs(nodes, dec, meta, p, max_prims, status);
+    inner_costs(nodes, dec, p, max_prims);
     if (p == 0) return;
     p = parents[p];
   }
   set_status(status, ST_ITER_LIMIT);
+}
+
+// get_children (src/cwbvh/bvh2_to_cwbvh.rs:346-397) with an explicit stack.
+// Returns the child count, or -1 on an invalid distribution.
+__device__ int get_children(const Bvh2Node* nodes, const Dec* dec, uint32_t x, uint32_t ch[8]) {
+  uint32_t st[16];  // node | (i << 28) | (expand << 31)
+  int sp = 0, cnt = 0;
+  st[sp++] = x | 0x80000000u;
+  while (sp) {
+    const uint32_t e = st[--sp];
+    const uint32_t n = e & 0x0fffffffu;
+    if (!(e & 0x80000000u)) {
+      if (cnt >= 8) return -1;
+      ch[cnt++] = n;
+      continue;
+    }
+    const int i = (e >> 28) & 7;
+    const Bvh2Node nd = ld_node(&nodes[n]);
+    if (node_prims(nd) != 0) {
+      if (cnt >= 8) return -1;
+      ch[cnt++] = n;
+      continue;
+    }
+    const uint8_t m = dec[n].meta[i];
+    const uint8_t dl = dl_of(m), dr = dr_of(m);
+    if (dl == DL_INVALID || dr == DL_INVALID) return -1;
+    const uint32_t f = node_first(nd);
+    if (sp + 2 > 16) return -1;
+    // right first so the left subtree's children come out first
+    st[sp++] = kind_of(dec[f + 1].meta[dr]) == K_DISTRIBUTE ? ((f + 1) | ((uint32_t)dr << 28) | 0x80000000u) : (f + 1);
+    st[sp++] = kind_of(dec[f].meta[dl]) == K_DISTRIBUTE ? (f | ((uint32_t)dl << 28) | 0x80000000u) : f;
+  }
+  return cnt;
 }
 
 __device__ __forceinline__ float pow2f(float c) {
@@ -245,7 +234,7 @@ __device__ __forceinline__ float pow2f(float c) {
 // rounded float log2 (here: double log2 rounded to float) gives the same
 // ceiling for every finite positive float.
 __device__ __forceinline__ float exp_grid(float ext) {
-  float l = __double2float_rn(log2((double)ext));
+  const float l = __double2float_rn(log2((double)ext));
   return pow2f(ceilf(l));
 }
 
@@ -253,239 +242,272 @@ __device__ __forceinline__ float3 center(const Box& b) {
   return make_float3((b.mx.x + b.mn.x) * 0.5f, (b.mx.y + b.mn.y) * 0.5f, (b.mx.z + b.mn.z) * 0.5f);
 }
 
-__device__ void emit_item(const Bvh2Node* __restrict__ nodes, const uint32_t* __restrict__ pidx_in,
-                          const Dec* __restrict__ dec, const CwMeta* __restrict__ meta, const Item it,
-                          Item* __restrict__ out, uint32_t* n_out, int order_children, uint32_t max_nodes,
-                          uint32_t max_prims_out, CwNode* __restrict__ cw, uint32_t* __restrict__ pidx_out,
-                          float* __restrict__ exact, uint32_t* status) {
-  const Bvh2Node nd = ld_node(&nodes[it.bvh2]);
-  const Box box = node_box(nd);
-  if (exact) {
-    float* e6 = exact + (size_t)it.cw * 6;
-    e6[0] = box.mn.x;
-    e6[1] = box.mn.y;
-    e6[2] = box.mn.z;
-    e6[3] = box.mx.x;
-    e6[4] = box.mx.y;
-    e6[5] = box.mx.z;
-  }
-  const float3 p = box.mn;
-  float ex = exp_grid(smax(box.mx.x - box.mn.x, 1e-20f) * DENOM);
-  float ey = exp_grid(smax(box.mx.y - box.mn.y, 1e-20f) * DENOM);
-  float ez = exp_grid(smax(box.mx.z - box.mn.z, 1e-20f) * DENOM);
-  const float rx = 1.0f / ex, ry = 1.0f / ey, rz = 1.0f / ez;
-
-  uint32_t ch[8];
-  int cnt = get_children(nodes, dec, it.bvh2, ch);
-  if (cnt < 0) {
-    set_status(status, ST_BAD_INPUT);
-    return;
-  }
-  uint32_t slots[8];
-#pragma unroll
-  for (int k = 0; k < 8; k++) slots[k] = OBVHS_INVALID;
-  if (order_children) {
-    // order_children (src/cwbvh/bvh2_to_cwbvh.rs:402-467)
-    const float3 pc = center(box);
-    float cost[8][8];
-    for (int c = 0; c < 8; c++)
-      for (int s = 0; s < 8; s++) cost[c][s] = 3.40282347e+38f;
-    for (int c = 0; c < cnt; c++) {
-      float3 cc = center(node_box(ld_node(&nodes[ch[c]])));
-      float3 v = make_float3(cc.x - pc.x, cc.y - pc.y, cc.z - pc.z);
-      for (int s = 0; s < 8; s++) {
-        float dx = (s & 4) ? -1.0f : 1.0f, dy = (s & 2) ? -1.0f : 1.0f, dz = (s & 1) ? -1.0f : 1.0f;
-        cost[c][s] = (dx * v.x + dy * v.y) + dz * v.z;
-      }
-    }
-    int assign[8];
-    bool filled[8];
-    for (int k = 0; k < 8; k++) {
-      assign[k] = -1;
-      filled[k] = false;
-    }
-    for (int it2 = 0; it2 < 8; it2++) {
-      float mc = 3.40282347e+38f;
-      int ms = -1, mi = -1;
-      for (int c = 0; c < cnt; c++)
-        if (assign[c] < 0)
-          for (int s = 0; s < 8; s++)
-            if (!filled[s] && cost[c][s] < mc) {
-              mc = cost[c][s];
-              ms = s;
-              mi = c;
-            }
-      if (ms < 0) break;
-      filled[ms] = true;
-      assign[mi] = ms;
-    }
-    for (int c = 0; c < cnt; c++) {
-      if (assign[c] < 0) {
-        set_status(status, ST_BAD_INPUT);
-        return;
-      }
-      slots[assign[c]] = ch[c];
-    }
-  } else {
-    for (int c = 0; c < cnt; c++) slots[c] = ch[c];
-  }
-
-  uint8_t meta8[8], qlx[8], qhx[8], qly[8], qhy[8], qlz[8], qhz[8];
-  uint8_t imask = 0;
-  uint32_t nprims = 0, nint = 0;
-  uint32_t cbase = it.child_base + 0;  // internal children go first, contiguous
-  // count internal children first (their nodes precede their subtrees)
-  uint32_t n_internal = 0;
-  for (int i = 0; i < 8; i++)
-    if (slots[i] != OBVHS_INVALID) {
-      Bvh2Node cn = ld_node(&nodes[slots[i]]);
-      if (node_prims(cn) == 0 && kind_of(dec[slots[i]].meta[0]) == K_INTERNAL) n_internal++;
-    }
-  uint32_t next_child_base = it.child_base + n_internal;
-  uint32_t next_prim_base = it.prim_base + meta[it.bvh2].lprims;
-  if (node_prims(nd) != 0) next_prim_base = it.prim_base + node_prims(nd);  // a leaf root
-  for (int i = 0; i < 8; i++) {
-    meta8[i] = qlx[i] = qhx[i] = qly[i] = qhy[i] = qlz[i] = qhz[i] = 0;
-    uint32_t c = slots[i];
-    if (c == OBVHS_INVALID) continue;
-    Bvh2Node cn = ld_node(&nodes[c]);
-    Box cb = node_box(cn);
-    float lo[3] = {floorf(((cb.mn.x - p.x) - 0.0f) * rx), floorf(((cb.mn.y - p.y) - 0.0f) * ry),
-                   floorf(((cb.mn.z - p.z) - 0.0f) * rz)};
-    float hi[3] = {ceilf(((cb.mx.x - p.x) + 0.0f) * rx), ceilf(((cb.mx.y - p.y) + 0.0f) * ry),
-                   ceilf(((cb.mx.z - p.z) + 0.0f) * rz)};
-    qlx[i] = (uint8_t)smin(smax(lo[0], 0.0f), 255.0f);
-    qly[i] = (uint8_t)smin(smax(lo[1], 0.0f), 255.0f);
-    qlz[i] = (uint8_t)smin(smax(lo[2], 0.0f), 255.0f);
-    qhx[i] = (uint8_t)smin(smax(hi[0], 0.0f), 255.0f);
-    qhy[i] = (uint8_t)smin(smax(hi[1], 0.0f), 255.0f);
-    qhz[i] = (uint8_t)smin(smax(hi[2], 0.0f), 255.0f);
-    uint8_t kind = node_prims(cn) != 0 ? K_LEAF : kind_of(dec[c].meta[0]);
-    if (kind == K_LEAF) {
-      // count_primitives: DFS of the leaf subtree, left before right
-      uint32_t st[8];
-      int sp = 0;
-      uint32_t pc = 0;
-      st[sp++] = c;
-      while (sp) {
-        uint32_t x = st[--sp];
-        Bvh2Node xn = ld_node(&nodes[x]);
-        if (node_prims(xn) != 0) {
-          uint32_t slot = it.prim_base + nprims + pc;
-          if (slot < max_prims_out) pidx_out[slot] = pidx_in[node_first(xn)];
-          else set_status(status, ST_CAPACITY);
-          pc += node_prims(xn);
-        } else {
-          if (sp + 2 > 8) {
-            set_status(status, ST_BAD_INPUT);
-            break;
-          }
-          st[sp++] = node_first(xn) + 1;
-          st[sp++] = node_first(xn);
-        }
-      }
-      uint8_t u = pc == 1 ? 0x20 : pc == 2 ? 0x60 : pc == 3 ? 0xe0 : 0;
-      if (!u) set_status(status, ST_BAD_INPUT);
-      meta8[i] = (uint8_t)nprims | u;
-      nprims += pc;
-    } else if (kind == K_INTERNAL) {
-      imask |= (uint8_t)(1u << i);
-      meta8[i] = (uint8_t)((24 + i) | 0x20);
-      uint32_t ci = cbase + nint;
-      nint++;
-      uint32_t sub = meta[c].ncw;
-      if (sub == 0xffffffffu) {
-        set_status(status, ST_BAD_INPUT);
-        return;
-      }
-      uint32_t slot = atomicAdd(n_out, 1u);
-      out[slot] = Item{c, ci, next_child_base, next_prim_base};
-      next_child_base += sub - 1;
-      next_prim_base += dec[c].nprim;
-    } else {
-      set_status(status, ST_BAD_INPUT);
-      return;
-    }
-  }
-  if (it.cw >= max_nodes) {
-    set_status(status, ST_CAPACITY);
-    return;
-  }
-  // write the 80-byte node
-  uint8_t bytes[80];
-  uint32_t pb[3] = {__float_as_uint(p.x), __float_as_uint(p.y), __float_as_uint(p.z)};
-  for (int k = 0; k < 3; k++)
-    for (int j = 0; j < 4; j++) bytes[4 * k + j] = (uint8_t)(pb[k] >> (8 * j));
-  bytes[12] = (uint8_t)(__float_as_uint(ex) >> 23);
-  bytes[13] = (uint8_t)(__float_as_uint(ey) >> 23);
-  bytes[14] = (uint8_t)(__float_as_uint(ez) >> 23);
-  bytes[15] = imask;
-  for (int j = 0; j < 4; j++) {
-    bytes[16 + j] = (uint8_t)(it.child_base >> (8 * j));
-    bytes[20 + j] = (uint8_t)(it.prim_base >> (8 * j));
-  }
-  for (int i = 0; i < 8; i++) {
-    bytes[24 + i] = meta8[i];
-    bytes[32 + i] = qlx[i];
-    bytes[40 + i] = qhx[i];
-    bytes[48 + i] = qly[i];
-    bytes[56 + i] = qhy[i];
-    bytes[64 + i] = qlz[i];
-    bytes[72 + i] = qhz[i];
-  }
-  uint4* dst = cw[it.cw].q;
-  for (int k = 0; k < 5; k++) {
-    uint32_t w[4];
-    for (int j = 0; j < 4; j++)
-      w[j] = (uint32_t)bytes[16 * k + 4 * j] | (uint32_t)bytes[16 * k + 4 * j + 1] << 8 |
-             (uint32_t)bytes[16 * k + 4 * j + 2] << 16 | (uint32_t)bytes[16 * k + 4 * j + 3] << 24;
-    dst[k] = make_uint4(w[0], w[1], w[2], w[3]);
-  }
-}
-
-// All levels in one cooperative launch: level L reads frontier L & 1 (its
-// size in cnt[L % 3]) and appends the next level to the other frontier.
+// Emission work queue: items[k] describes CWBVH node k's source; it is
+// published (ready[k] = 1) by the warp that emits its parent.  Warps take
+// indices in order from `head` and append children at `tail`.
 struct EmitArgs {
   const Bvh2Node* nodes;
   const uint32_t* pidx_in;
   const Dec* dec;
-  const CwMeta* meta;
-  Item* frontier[2];
-  uint32_t* cnt;  // [3]
+  Item* items;
+  uint32_t* ready;
+  uint32_t* head;
+  uint32_t* tail;
   int order_children;
   uint32_t max_nodes, max_prims_out;
   CwNode* cw;
   uint32_t* pidx_out;
-  float* exact;
   uint32_t* status;
   uint32_t* processed;
 };
 
-__global__ void __launch_bounds__(128) k_emit_all(EmitArgs a) {
-  cg::grid_group grid = cg::this_grid();
-  const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t stride = gridDim.x * blockDim.x;
-  if (t0 == 0) {
-    a.frontier[0][0] = Item{0, 0, 1, 0};
-    a.cnt[0] = 1;
-    a.cnt[1] = 0;
+// exclusive scan over lanes 0..7 (lanes 8..31 hold 0); *total = sum
+__device__ __forceinline__ uint32_t slot_excl_scan(uint32_t v, int lane, uint32_t* total) {
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
   }
-  grid.sync();
-  for (uint32_t level = 0; level < 64; level++) {
-    const uint32_t n_in = *(volatile uint32_t*)&a.cnt[level % 3];
-    if (n_in == 0) break;
-    if (t0 == 0) a.cnt[(level + 2) % 3] = 0;
-    const Item* in = a.frontier[level & 1];
-    Item* out = a.frontier[(level + 1) & 1];
-    uint32_t mine = 0;
-    for (uint32_t t = t0; t < n_in; t += stride) {
-      emit_item(a.nodes, a.pidx_in, a.dec, a.meta, in[t], out, &a.cnt[(level + 1) % 3], a.order_children,
-                a.max_nodes, a.max_prims_out, a.cw, a.pidx_out, a.exact, a.status);
-      mine++;
+  *total = __shfl_sync(0xffffffffu, x, 7);
+  return x - v;
+}
+
+// convert_to_cwbvh_impl (src/cwbvh/bvh2_to_cwbvh.rs:75-193) for one node;
+// the whole warp works on it, lane s on child slot s.
+__device__ void emit_node(const EmitArgs& a, const Item it, int lane, uint8_t* stage) {
+  const Bvh2Node nd = ld_node(&a.nodes[it.bvh2]);
+  const Box box = node_box(nd);
+  const float3 p = box.mn;
+  const float ex = exp_grid(smax(box.mx.x - box.mn.x, 1e-20f) * DENOM);
+  const float ey = exp_grid(smax(box.mx.y - box.mn.y, 1e-20f) * DENOM);
+  const float ez = exp_grid(smax(box.mx.z - box.mn.z, 1e-20f) * DENOM);
+  const float rx = 1.0f / ex, ry = 1.0f / ey, rz = 1.0f / ez;
+
+  // children (lane 0 walks the distribution), one per lane
+  uint32_t ch[8];
+  int cnt = 0;
+  if (lane == 0) cnt = get_children(a.nodes, a.dec, it.bvh2, ch);
+  cnt = __shfl_sync(0xffffffffu, cnt, 0);
+  if (cnt < 0) {
+    if (lane == 0) set_status(a.status, ST_BAD_INPUT);
+    return;
+  }
+  uint32_t my_child = OBVHS_INVALID;  // child number `lane` before ordering
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const uint32_t v = __shfl_sync(0xffffffffu, lane == 0 ? ch[c] : 0u, 0);
+    if (lane == c && c < cnt) my_child = v;
+  }
+  uint32_t slot_child = OBVHS_INVALID;  // child placed in slot `lane`
+  if (a.order_children) {
+    // order_children (src/cwbvh/bvh2_to_cwbvh.rs:402-467): the cost of
+    // (child c, direction s) sits at idx = 8c + s, two per lane; the greedy
+    // loop takes the smallest cost (first in (c, s) order on ties) among
+    // unassigned children and unfilled slots while one is below f32::MAX.
+    const float3 pc = center(box);
+    float cost[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int idx = lane + 32 * h;
+      const int c = idx >> 3, s = idx & 7;
+      const uint32_t chc = __shfl_sync(0xffffffffu, my_child, c);
+      cost[h] = 3.40282347e+38f;
+      if (c < cnt) {
+        const float3 cc = center(node_box(ld_node(&a.nodes[chc])));
+        const float3 v = make_float3(cc.x - pc.x, cc.y - pc.y, cc.z - pc.z);
+        const float dx = (s & 4) ? -1.0f : 1.0f, dy = (s & 2) ? -1.0f : 1.0f, dz = (s & 1) ? -1.0f : 1.0f;
+        cost[h] = (dx * v.x + dy * v.y) + dz * v.z;
+      }
     }
-    if (mine) atomicAdd(a.processed, mine);
-    grid.sync();
+    uint32_t assigned = 0, filled = 0, assign = 0;  // assign: 3 bits per child
+    for (int iter = 0; iter < 8; iter++) {
+      float bc = 3.40282347e+38f;
+      uint32_t bi = 0xffffffffu;
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const uint32_t idx = lane + 32 * h;
+        const int c = idx >> 3, s = idx & 7;
+        if (c < cnt && !((assigned >> c) & 1) && !((filled >> s) & 1) && cost[h] < bc) {
+          bc = cost[h];
+          bi = idx;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oc = __shfl_xor_sync(0xffffffffu, bc, o);
+        const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (oi != 0xffffffffu && (bi == 0xffffffffu || oc < bc || (oc == bc && oi < bi))) {
+          bc = oc;
+          bi = oi;
+        }
+      }
+      if (bi == 0xffffffffu) break;
+      const int c = bi >> 3, s = bi & 7;
+      assigned |= 1u << c;
+      filled |= 1u << s;
+      assign |= (uint32_t)s << (3 * c);
+    }
+    if (__popc(assigned) != cnt) {
+      if (lane == 0) set_status(a.status, ST_BAD_INPUT);
+      return;
+    }
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const uint32_t v = __shfl_sync(0xffffffffu, my_child, c);
+      if (c < cnt && (int)((assign >> (3 * c)) & 7) == lane) slot_child = v;
+    }
+  } else {
+    slot_child = my_child;
   }
+
+  // per slot: quantised box, kind, primitive count or subtree size
+  const bool has = lane < 8 && slot_child != OBVHS_INVALID;
+  uint8_t q[6] = {0, 0, 0, 0, 0, 0};
+  uint32_t is_int = 0, leaf_pc = 0, sub_nodes = 0, sub_prims = 0;
+  if (has) {
+    const Bvh2Node cn = ld_node(&a.nodes[slot_child]);
+    const Box cb = node_box(cn);
+    const float lo[3] = {floorf(((cb.mn.x - p.x) - 0.0f) * rx), floorf(((cb.mn.y - p.y) - 0.0f) * ry),
+                         floorf(((cb.mn.z - p.z) - 0.0f) * rz)};
+    const float hi[3] = {ceilf(((cb.mx.x - p.x) + 0.0f) * rx), ceilf(((cb.mx.y - p.y) + 0.0f) * ry),
+                         ceilf(((cb.mx.z - p.z) + 0.0f) * rz)};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      q[2 * k] = (uint8_t)smin(smax(lo[k], 0.0f), 255.0f);
+      q[2 * k + 1] = (uint8_t)smin(smax(hi[k], 0.0f), 255.0f);
+    }
+    const Dec& cd = a.dec[slot_child];
+    const uint8_t kind = node_prims(cn) != 0 ? K_LEAF : kind_of(cd.meta[0]);
+    if (kind == K_LEAF) {
+      leaf_pc = node_prims(cn) != 0 ? node_prims(cn) : cd.nprim;
+    } else if (kind == K_INTERNAL) {
+      if (cd.agg[0].x == AGG_INVALID) {
+        set_status(a.status, ST_BAD_INPUT);
+      } else {
+        is_int = 1;
+        sub_nodes = cd.agg[0].x;  // CWBVH nodes below the child's own node
+        sub_prims = cd.nprim;
+      }
+    } else {
+      set_status(a.status, ST_BAD_INPUT);
+    }
+  }
+  uint32_t n_int, n_leafprims, t0, t1;
+  const uint32_t int_rank = slot_excl_scan(is_int, lane, &n_int);
+  const uint32_t leaf_off = slot_excl_scan(leaf_pc, lane, &n_leafprims);
+  const uint32_t sub_node_off = slot_excl_scan(sub_nodes, lane, &t0);
+  const uint32_t sub_prim_off = slot_excl_scan(sub_prims, lane, &t1);
+  uint32_t out_base = 0;
+  if (lane == 0 && n_int) out_base = atomicAdd(a.tail, n_int);
+  out_base = __shfl_sync(0xffffffffu, out_base, 0);
+
+  uint8_t meta = 0;
+  if (has && leaf_pc) {
+    const uint8_t u = leaf_pc == 1 ? 0x20 : leaf_pc == 2 ? 0x60 : leaf_pc == 3 ? 0xe0 : 0;
+    if (!u) set_status(a.status, ST_BAD_INPUT);
+    meta = (uint8_t)leaf_off | u;
+    // count_primitives: DFS of the leaf subtree, left before right
+    uint32_t st[8];
+    int sp = 0;
+    uint32_t k = 0;
+    st[sp++] = slot_child;
+    while (sp) {
+      const uint32_t x = st[--sp];
+      const Bvh2Node xn = ld_node(&a.nodes[x]);
+      if (node_prims(xn) != 0) {
+        const uint32_t slot = it.prim_base + leaf_off + k;
+        if (slot < a.max_prims_out)
+          a.pidx_out[slot] = a.pidx_in[node_first(xn)];
+        else
+          set_status(a.status, ST_CAPACITY);
+        k += node_prims(xn);
+      } else {
+        if (sp + 2 > 8) {
+          set_status(a.status, ST_BAD_INPUT);
+          break;
+        }
+        st[sp++] = node_first(xn) + 1;
+        st[sp++] = node_first(xn);
+      }
+    }
+  } else if (is_int) {
+    meta = (uint8_t)((24 + lane) | 0x20);
+    // the internal children's own nodes come first, then their subtrees
+    const uint32_t cb = it.child_base + n_int + sub_node_off;
+    const uint32_t pb = it.prim_base + n_leafprims + sub_prim_off;
+    const uint32_t q = out_base + int_rank;
+    if (q < a.max_nodes) {
+      a.items[q] = Item{slot_child, it.child_base + int_rank, cb, pb};
+      __threadfence();
+      atomicExch(&a.ready[q], 1u);
+    } else {
+      set_status(a.status, ST_CAPACITY);
+    }
+  }
+  const uint32_t imask = __ballot_sync(0xffffffffu, is_int != 0) & 0xffu;
+
+  // assemble the 80-byte node in shared memory, then five 16-byte stores
+  if (lane == 0) {
+    uint32_t* w = reinterpret_cast<uint32_t*>(stage);
+    w[0] = __float_as_uint(p.x);
+    w[1] = __float_as_uint(p.y);
+    w[2] = __float_as_uint(p.z);
+    w[3] = (__float_as_uint(ex) >> 23) | (__float_as_uint(ey) >> 23) << 8 | (__float_as_uint(ez) >> 23) << 16 |
+           imask << 24;
+    w[4] = it.child_base;
+    w[5] = it.prim_base;
+  }
+  if (lane < 8) {
+    stage[24 + lane] = meta;
+    stage[32 + lane] = q[0];
+    stage[40 + lane] = q[1];
+    stage[48 + lane] = q[2];
+    stage[56 + lane] = q[3];
+    stage[64 + lane] = q[4];
+    stage[72 + lane] = q[5];
+  }
+  __syncwarp();
+  if (it.cw >= a.max_nodes) {
+    if (lane == 0) set_status(a.status, ST_CAPACITY);
+  } else if (lane < 5) {
+    a.cw[it.cw].q[lane] = reinterpret_cast<const uint4*>(stage)[lane];
+  }
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(EMIT_THREADS) k_emit_all(EmitArgs a) {
+  __shared__ __align__(16) uint8_t stage[EMIT_THREADS / 32][80];
+  const int lane = threadIdx.x & 31;
+  uint32_t mine = 0;
+  for (;;) {
+    uint32_t k = 0;
+    if (lane == 0) k = atomicAdd(a.head, 1u);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= a.max_nodes) break;
+    // wait for the parent's warp to publish item k (bounded)
+    uint32_t ok = 1;
+    if (lane == 0) {
+      uint32_t spins = 0;
+      while (*(volatile uint32_t*)&a.ready[k] == 0) {
+        if (++spins > (1u << 22)) {
+          set_status(a.status, ST_ITER_LIMIT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+      __threadfence();
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (!ok) break;
+    // through L2: this SM may hold a stale L1 line from neighbouring items
+    const uint4 raw = __ldcg(reinterpret_cast<const uint4*>(&a.items[k]));
+    const Item it{raw.x, raw.y, raw.z, raw.w};
+    emit_node(a, it, lane, stage[threadIdx.x >> 5]);
+    mine++;
+  }
+  if (lane == 0 && mine) atomicAdd(a.processed, mine);
 }
 
 }  // namespace
@@ -499,26 +521,26 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   uint32_t* parents = (uint32_t*)s.get(SLOT_PARENTS, (size_t)n * 4);
   uint32_t* flags = (uint32_t*)s.get(SLOT_FLAGS, (size_t)n * 4);
   Dec* dec = (Dec*)s.get(SLOT_DECISIONS, (size_t)n * sizeof(Dec));
-  CwMeta* meta = (CwMeta*)s.get(SLOT_CW_META, (size_t)n * sizeof(CwMeta));
   uint32_t* counters = (uint32_t*)s.get(SLOT_CW_COUNTERS, 64);
-  if (!parents || !flags || !dec || !meta || !counters) return c.fail(OBVHS_ERR_OOM, "scratch");
+  if (!parents || !flags || !dec || !counters) return c.fail(OBVHS_ERR_OOM, "scratch");
   int r = compute_parents_device(c, b->nodes, n, parents);
   if (r) return r;
   CK(cudaMemsetAsync(flags, 0, (size_t)n * 4, c.stream));
-  KLAUNCH("k_costs", k_costs<<<div_up<uint32_t>(n, BLK), BLK, 0, c.stream>>>(b->nodes, parents, n, max_prims, dec, meta, flags,
-                                                          c.d_status));
+  KLAUNCH("k_costs", k_costs<<<div_up<uint32_t>(n, BLK), BLK, 0, c.stream>>>(b->nodes, parents, n, max_prims, dec,
+                                                                             flags, c.d_status));
   CK(cudaGetLastError());
-  // sizes of the whole tree
-  CwMeta root;
-  uint32_t root_np = 0;
-  CK(cudaMemcpyAsync(&root, meta, sizeof(CwMeta), cudaMemcpyDeviceToHost, c.stream));
-  CK(cudaMemcpyAsync(&root_np, &dec[0].nprim, 4, cudaMemcpyDeviceToHost, c.stream));
+  // sizes of the whole tree: the root's aggregate (a leaf root is one node)
+  Dec root;
+  CK(cudaMemcpyAsync(&root, dec, sizeof(Dec), cudaMemcpyDeviceToHost, c.stream));
   CK(cudaMemcpyAsync(c.h_status, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
-  if (*c.h_status) return c.fail(OBVHS_ERR_BAD_INPUT, "BVH2 cannot be converted (leaf with more than one primitive, or non-finite costs)");
-  if (root.ncw == 0xffffffffu) return c.fail(OBVHS_ERR_BAD_INPUT, "BVH2 cannot be converted (no finite distribution)");
-  const uint32_t n_cw = root.ncw;
-  const uint32_t n_pr = root_np;
+  if (*c.h_status)
+    return c.fail(OBVHS_ERR_BAD_INPUT, "BVH2 cannot be converted (a leaf holds more than one primitive)");
+  const bool root_leaf = n == 1;
+  if (!root_leaf && root.agg[0].x == AGG_INVALID)
+    return c.fail(OBVHS_ERR_BAD_INPUT, "BVH2 cannot be converted (no finite distribution of the root)");
+  const uint32_t n_cw = root_leaf ? 1 : 1 + root.agg[0].x;
+  const uint32_t n_pr = root.nprim;
   CwNode* cwn = nullptr;
   uint32_t* cwp = nullptr;
   if (cudaMalloc(&cwn, (size_t)n_cw * sizeof(CwNode)) != cudaSuccess ||
@@ -527,9 +549,9 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
     if (cwn) cudaFree(cwn);
     return c.fail(OBVHS_ERR_OOM, "cwbvh output");
   }
-  Item* fa = (Item*)s.get(SLOT_FRONTIER_A, (size_t)n_cw * sizeof(Item));
-  Item* fb = (Item*)s.get(SLOT_FRONTIER_B, (size_t)n_cw * sizeof(Item));
-  if (!fa || !fb) {
+  Item* items = (Item*)s.get(SLOT_FRONTIER_A, (size_t)n_cw * sizeof(Item));
+  uint32_t* ready = (uint32_t*)s.get(SLOT_FRONTIER_B, (size_t)n_cw * 4);
+  if (!items || !ready) {
     cudaFree(cwn);
     cudaFree(cwp);
     return c.fail(OBVHS_ERR_OOM, "scratch");
@@ -537,17 +559,31 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   static int emit_blocks = 0;
   if (!emit_blocks) {
     int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_all, 128, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_all, EMIT_THREADS, 0));
     emit_blocks = std::max(1, per_sm) * c.num_sms;
   }
-  CK(cudaMemsetAsync(counters + 12, 0, 4, c.stream));
-  EmitArgs ea{b->nodes, b->prim_indices, dec, meta, {fa, fb}, counters + 8, order_children, n_cw, n_pr, cwn, cwp,
-              nullptr, c.d_status, counters + 12};
-  void* args[] = {&ea};
-  uint32_t grid = (uint32_t)std::min<uint64_t>(emit_blocks, std::max<uint64_t>(1, div_up<uint32_t>(n_cw, 128)));
-  CK(cudaLaunchCooperativeKernel((void*)k_emit_all, grid, 128, args, 0, c.stream));
+  // queue: item 0 = the root, published; head = 0, tail = 1
+  CK(cudaMemsetAsync(ready, 0, (size_t)n_cw * 4, c.stream));
+  uint32_t* hst = (uint32_t*)c.h_small;
+  hst[0] = 0;
+  hst[1] = 0;
+  hst[2] = 1;
+  hst[3] = 0;  // Item{0, 0, 1, 0}
+  hst[4] = 1;  // ready[0]
+  hst[5] = 0;  // head
+  hst[6] = 1;  // tail
+  hst[7] = 0;  // processed
+  CK(cudaMemcpyAsync(items, hst, 16, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaMemcpyAsync(ready, hst + 4, 4, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaMemcpyAsync(counters + 12, hst + 5, 12, cudaMemcpyHostToDevice, c.stream));
+  EmitArgs ea{b->nodes, b->prim_indices, dec, items, ready, counters + 12, counters + 13, order_children, n_cw, n_pr,
+              cwn, cwp, c.d_status, counters + 14};
+  const uint32_t grid = (uint32_t)std::min<uint64_t>(
+      emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)n_cw * 32, EMIT_THREADS)));
+  KLAUNCH("k_emit_all", k_emit_all<<<grid, EMIT_THREADS, 0, c.stream>>>(ea));
+  CK(cudaGetLastError());
   uint32_t emitted = 0;
-  CK(cudaMemcpyAsync(&emitted, counters + 12, 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(&emitted, counters + 14, 4, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaMemcpyAsync(c.h_status, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
   if (*c.h_status || emitted != n_cw) {

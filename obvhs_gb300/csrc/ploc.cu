@@ -14,9 +14,9 @@
 // merge, whose children land at insert_base - 2(k+1).  The result is the
 // reference's tree bit for bit, given the same sorted leaves.
 //
-// Passes run as four launches on the full grid while many clusters are live;
-// once at most TAIL_MAX remain, one CTA finishes every remaining pass with
-// the clusters held in shared memory.
+// Each pass is one launch (k_ploc_pass) while many clusters are live; once
+// at most TAIL_MAX remain, one CTA finishes every remaining pass with the
+// clusters held in shared memory.
 #include "build.h"
 #include "radix_sort.cuh"
 
@@ -207,22 +207,55 @@ __device__ __forceinline__ Box load_box(const Bvh2Node* p) {
   return Box{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)};
 }
 
-// Nearest-neighbour choice with radius r (src/ploc/mod.rs:624-650): scan
-// j = i-r .. i+r ascending, keep the last j with cost <= best.
-__global__ void __launch_bounds__(BLK) k_ploc_search(const Bvh2Node* __restrict__ cur, const PlocState* st, int parity,
-                                                     int radius, int d1, int8_t* __restrict__ merge) {
-  __shared__ float s_box[(BLK + 64) * 6];
+// --- one fused kernel per pass ---------------------------------------------
+//
+// A tile of PCHUNK clusters computes the merge offsets of its clusters and of
+// a +-radius halo (from boxes staged with a 2*radius halo), derives the emit
+// and merge flags, scans them inside the CTA and gets its output offsets by
+// decoupled look-back over earlier tiles, then writes next_nodes and the
+// merged pairs.  The tile holding the last cluster stores the next count and
+// insert index.  Tiles are claimed in launch order; waits are bounded.
+constexpr int PT = 256;
+constexpr int PITEMS = 4;
+constexpr int PCHUNK = PT * PITEMS;
+constexpr unsigned long long LB_AGG = 1ull << 62, LB_INC = 2ull << 62;
+constexpr unsigned long long LB_VAL = (1ull << 31) - 1;
+
+__global__ void __launch_bounds__(PT) k_ploc_pass(const Bvh2Node* __restrict__ cur, Bvh2Node* __restrict__ next,
+                                                  Bvh2Node* __restrict__ out, PlocState* st, int parity, int radius,
+                                                  int d1, unsigned long long* lb, uint32_t* lb_next, uint32_t lb_words,
+                                                  uint32_t* status) {
+  __shared__ float s_box[(PCHUNK + 4 * 32) * 6];
+  __shared__ int8_t s_merge[PCHUNK + 2 * 32];
+  __shared__ uint32_t s_tile, s_w[PT / 32];
+  __shared__ unsigned long long s_prefix;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // clear the look-back area of the next pass (the previous pass used it)
+  for (uint32_t k = blockIdx.x * PT + tid; k < lb_words; k += gridDim.x * PT) lb_next[k] = 0;
   const uint32_t count = st->count[parity];
-  if (count <= 1) return;
-  const uint32_t base = blockIdx.x * BLK;
+  if (count <= 1) {
+    // a pass after the root formed: carry the root and the state forward
+    if (blockIdx.x == 0 && tid == 0) {
+      if (count == 1) st_node(&next[0], ld_node(&cur[0]));
+      st->count[parity ^ 1] = count;
+      st->insert[parity ^ 1] = st->insert[parity];
+    }
+    return;
+  }
+  uint32_t* counter = reinterpret_cast<uint32_t*>(lb);
+  unsigned long long* tstat = lb + 1;
+  if (tid == 0) s_tile = atomicAdd(counter, 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const uint32_t base = tile * PCHUNK;
   if (base >= count) return;
   const int r = d1 ? 1 : radius;
-  const int64_t lo = (int64_t)base - r;
-  const uint32_t span = BLK + 2 * r;
-  for (uint32_t k = threadIdx.x; k < span; k += BLK) {
-    int64_t j = lo + k;
+  const int64_t box_lo = (int64_t)base - 2 * r;
+  const uint32_t box_span = PCHUNK + 4 * r;
+  for (uint32_t k = tid; k < box_span; k += PT) {
+    const int64_t j = box_lo + k;
     if (j >= 0 && j < (int64_t)count) {
-      Box b = load_box(&cur[j]);
+      const Box b = load_box(&cur[j]);
       float* d = &s_box[k * 6];
       d[0] = b.mn.x;
       d[1] = b.mn.y;
@@ -233,211 +266,124 @@ __global__ void __launch_bounds__(BLK) k_ploc_search(const Bvh2Node* __restrict_
     }
   }
   __syncthreads();
-  const uint32_t i = base + threadIdx.x;
-  if (i >= count) return;
   auto box_at = [&](uint32_t j) {
-    const float* d = &s_box[(j - lo) * 6];
+    const float* d = &s_box[((int64_t)j - box_lo) * 6];
     return Box{make_float3(d[0], d[1], d[2]), make_float3(d[3], d[4], d[5])};
   };
-  Box me = box_at(i);
-  int8_t m;
-  if (d1) {
-    // src/ploc/mod.rs:329-382: merge[i] = cost(i-1,i) < cost(i,i+1) ? -1 : 1
-    if (i == count - 1) {
-      m = -1;
+  // merge offsets for [base - r, base + PCHUNK + r)
+  const int64_t m_lo = (int64_t)base - r;
+  const uint32_t m_span = PCHUNK + 2 * r;
+  for (uint32_t k = tid; k < m_span; k += PT) {
+    const int64_t jj = m_lo + k;
+    if (jj < 0 || jj >= (int64_t)count) continue;
+    const uint32_t i = (uint32_t)jj;
+    const Box me = box_at(i);
+    int8_t m;
+    if (d1) {
+      if (i == count - 1) {
+        m = -1;
+      } else {
+        const float c = pair_cost(me, box_at(i + 1));
+        const float last = i == 0 ? __int_as_float(0x7f800000) : pair_cost(box_at(i - 1), me);
+        m = last < c ? -1 : 1;
+      }
     } else {
-      float c = pair_cost(me, box_at(i + 1));
-      float last = i == 0 ? __int_as_float(0x7f800000) : pair_cost(box_at(i - 1), me);
-      m = last < c ? -1 : 1;
-    }
-  } else {
-    uint32_t begin = i >= (uint32_t)r ? i - r : 0;
-    uint32_t end = min(i + r + 1, count);
-    uint32_t best = i;
-    float best_cost = __int_as_float(0x7f800000);
-    for (uint32_t j = begin; j < i; j++) {
-      float c = pair_cost(box_at(j), me);
-      if (c <= best_cost) {
-        best = j;
-        best_cost = c;
+      const uint32_t begin = i >= (uint32_t)r ? i - r : 0;
+      const uint32_t end = min(i + r + 1, count);
+      uint32_t best = i;
+      float best_cost = __int_as_float(0x7f800000);
+      for (uint32_t j = begin; j < i; j++) {
+        const float c = pair_cost(box_at(j), me);
+        if (c <= best_cost) {
+          best = j;
+          best_cost = c;
+        }
       }
-    }
-    for (uint32_t j = i + 1; j < end; j++) {
-      float c = pair_cost(me, box_at(j));
-      if (c <= best_cost) {
-        best = j;
-        best_cost = c;
+      for (uint32_t j = i + 1; j < end; j++) {
+        const float c = pair_cost(me, box_at(j));
+        if (c <= best_cost) {
+          best = j;
+          best_cost = c;
+        }
       }
+      m = (int8_t)((int)best - (int)i);
     }
-    m = (int8_t)((int)best - (int)i);
-  }
-  merge[i] = m;
-}
-
-__device__ __forceinline__ void ploc_flags(const int8_t* merge, uint32_t i, bool& emit, bool& is_merge, uint32_t& best) {
-  int off = merge[i];
-  best = (uint32_t)((int)i + off);
-  bool mutual = (int)best + (int)merge[best] == (int)i;
-  emit = !mutual || best < i;
-  is_merge = mutual && best < i;
-}
-
-constexpr int ITEMS = 4;
-constexpr int CHUNK = BLK * ITEMS;  // items per block in the flag scan
-
-__global__ void __launch_bounds__(BLK) k_ploc_count(const int8_t* __restrict__ merge, const PlocState* st, int parity,
-                                                    uint2* __restrict__ partial) {
-  const uint32_t count = st->count[parity];
-  if (count <= 1) return;
-  const uint32_t base = blockIdx.x * CHUNK;
-  if (base >= count) return;
-  uint32_t e = 0, m = 0;
-  for (int k = 0; k < ITEMS; k++) {
-    uint32_t i = base + threadIdx.x * ITEMS + k;
-    if (i < count) {
-      bool emit, ism;
-      uint32_t best;
-      ploc_flags(merge, i, emit, ism, best);
-      e += emit;
-      m += ism;
-    }
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    e += __shfl_xor_sync(0xffffffffu, e, o);
-    m += __shfl_xor_sync(0xffffffffu, m, o);
-  }
-  __shared__ uint32_t se[BLK / 32], sm[BLK / 32];
-  if ((threadIdx.x & 31) == 0) {
-    se[threadIdx.x >> 5] = e;
-    sm[threadIdx.x >> 5] = m;
+    s_merge[k] = m;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t te = 0, tm = 0;
-    for (int w = 0; w < BLK / 32; w++) {
-      te += se[w];
-      tm += sm[w];
-    }
-    partial[blockIdx.x] = make_uint2(te, tm);
-  }
-}
-
-// One block: exclusive scan of the per-block (emit, merge) counts.
-__global__ void __launch_bounds__(1024) k_ploc_scan(uint2* __restrict__ partial, PlocState* st, int parity) {
-  const uint32_t count = st->count[parity];
-  if (count <= 1) {
-    if (threadIdx.x == 0) {
-      st->count[parity ^ 1] = count;
-      st->insert[parity ^ 1] = st->insert[parity];
-    }
-    return;
-  }
-  const uint32_t nb = (count + CHUNK - 1) / CHUNK;
-  __shared__ uint32_t we[32], wm[32];
-  __shared__ uint32_t carry_e, carry_m;
-  if (threadIdx.x == 0) {
-    carry_e = 0;
-    carry_m = 0;
-  }
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (uint32_t s0 = 0; s0 < nb; s0 += 1024) {
-    uint32_t b = s0 + threadIdx.x;
-    uint2 v = b < nb ? partial[b] : make_uint2(0, 0);
-    uint32_t xe = v.x, xm = v.y;
+  // flags, packed (emit | merge << 16), CTA-wide exclusive scan
+  bool emit[PITEMS], ism[PITEMS];
+  uint32_t bst[PITEMS];
+  uint32_t packed = 0;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      uint32_t ye = __shfl_up_sync(0xffffffffu, xe, o), ym = __shfl_up_sync(0xffffffffu, xm, o);
-      if (lane >= o) {
-        xe += ye;
-        xm += ym;
-      }
-    }
-    if (lane == 31) {
-      we[warp] = xe;
-      wm[warp] = xm;
-    }
-    __syncthreads();
-    uint32_t pe = 0, pm = 0, te = 0, tm = 0;
-    for (int w = 0; w < 32; w++) {
-      if (w < warp) {
-        pe += we[w];
-        pm += wm[w];
-      }
-      te += we[w];
-      tm += wm[w];
-    }
-    if (b < nb) partial[b] = make_uint2(carry_e + pe + xe - v.x, carry_m + pm + xm - v.y);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      carry_e += te;
-      carry_m += tm;
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    st->count[parity ^ 1] = carry_e;
-    st->insert[parity ^ 1] = st->insert[parity] - 2 * carry_m;
-    st->passes += 1;
-    st->sum_counts += count;
-  }
-}
-
-__global__ void __launch_bounds__(BLK) k_ploc_scatter(const Bvh2Node* __restrict__ cur, const int8_t* __restrict__ merge,
-                                                      const PlocState* st, int parity, const uint2* __restrict__ partial,
-                                                      Bvh2Node* __restrict__ next, Bvh2Node* __restrict__ out) {
-  const uint32_t count = st->count[parity];
-  if (count <= 1) {
-    // a pass after the root formed: carry the root to the other buffer
-    if (count == 1 && blockIdx.x == 0 && threadIdx.x == 0) st_node(&next[0], ld_node(&cur[0]));
-    return;
-  }
-  const uint32_t base = blockIdx.x * CHUNK;
-  if (base >= count) return;
-  const uint32_t ins_top = st->insert[parity];
-  bool emit[ITEMS], ism[ITEMS];
-  uint32_t best[ITEMS];
-  uint32_t e = 0, m = 0;
-  for (int k = 0; k < ITEMS; k++) {
-    uint32_t i = base + threadIdx.x * ITEMS + k;
+  for (int k = 0; k < PITEMS; k++) {
+    const uint32_t i = base + tid * PITEMS + k;
     emit[k] = ism[k] = false;
-    if (i < count) ploc_flags(merge, i, emit[k], ism[k], best[k]);
-    e += emit[k];
-    m += ism[k];
+    bst[k] = i;
+    if (i < count) {
+      const int off = s_merge[(int64_t)i - m_lo];
+      const uint32_t b = (uint32_t)((int)i + off);
+      const bool mutual = (int)b + (int)s_merge[(int64_t)b - m_lo] == (int)i;
+      emit[k] = !mutual || b < i;
+      ism[k] = mutual && b < i;
+      bst[k] = b;
+    }
+    packed += (emit[k] ? 1u : 0u) + (ism[k] ? (1u << 16) : 0u);
   }
-  // block exclusive scan of (e, m)
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t xe = e, xm = m;
+  uint32_t x = packed;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    uint32_t ye = __shfl_up_sync(0xffffffffu, xe, o), ym = __shfl_up_sync(0xffffffffu, xm, o);
-    if (lane >= o) {
-      xe += ye;
-      xm += ym;
-    }
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
   }
-  __shared__ uint32_t we[BLK / 32], wm[BLK / 32];
-  if (lane == 31) {
-    we[warp] = xe;
-    wm[warp] = xm;
+  if (lane == 31) s_w[warp] = x;
+  __syncthreads();
+  uint32_t wpre = 0, tot = 0;
+  for (int w = 0; w < PT / 32; w++) {
+    if (w < warp) wpre += s_w[w];
+    tot += s_w[w];
+  }
+  const uint32_t excl = wpre + x - packed;
+  // decoupled look-back on (emitted, merged) = (low 31 bits, next 31 bits)
+  if (tid == 0) {
+    const unsigned long long agg = (unsigned long long)(tot & 0xffffu) | ((unsigned long long)(tot >> 16) << 31);
+    unsigned long long prefix = 0;
+    if (tile == 0) {
+      atomicExch(&tstat[0], LB_INC | agg);
+    } else {
+      atomicExch(&tstat[tile], LB_AGG | agg);
+      int64_t t = (int64_t)tile - 1;
+      uint32_t spins = 0;
+      while (t >= 0) {
+        const unsigned long long v = *((volatile unsigned long long*)&tstat[t]);
+        if ((v >> 62) == 0) {
+          if (++spins > (1u << 24)) {
+            atomicOr(status, ST_ITER_LIMIT);
+            break;
+          }
+          continue;
+        }
+        prefix += v & ((1ull << 62) - 1);
+        if (v & LB_INC) break;
+        t--;
+      }
+      atomicExch(&tstat[tile], LB_INC | (prefix + agg));
+    }
+    s_prefix = prefix;
   }
   __syncthreads();
-  uint32_t pe = 0, pm = 0;
-  for (int w = 0; w < warp; w++) {
-    pe += we[w];
-    pm += wm[w];
-  }
-  uint2 bp = partial[blockIdx.x];
-  uint32_t epos = bp.x + pe + xe - e;
-  uint32_t mpos = bp.y + pm + xm - m;
-  for (int k = 0; k < ITEMS; k++) {
-    uint32_t i = base + threadIdx.x * ITEMS + k;
+  const unsigned long long pre = s_prefix;
+  const uint32_t pre_e = (uint32_t)(pre & LB_VAL), pre_m = (uint32_t)((pre >> 31) & LB_VAL);
+  const uint32_t ins_top = st->insert[parity];
+  uint32_t epos = pre_e + (excl & 0xffffu), mpos = pre_m + (excl >> 16);
+#pragma unroll
+  for (int k = 0; k < PITEMS; k++) {
+    const uint32_t i = base + tid * PITEMS + k;
     if (!emit[k]) continue;
     if (ism[k]) {
-      Bvh2Node left = ld_node(&cur[i]);
-      Bvh2Node right = ld_node(&cur[best[k]]);
-      uint32_t ins = ins_top - 2 * (mpos + 1);
+      const Bvh2Node left = ld_node(&cur[i]);
+      const Bvh2Node right = ld_node(&cur[bst[k]]);
+      const uint32_t ins = ins_top - 2 * (mpos + 1);
       st_node(&out[ins], left);
       st_node(&out[ins + 1], right);
       st_node(&next[epos], make_node(box_union(node_box(left), node_box(right)), 0, ins));
@@ -446,6 +392,13 @@ __global__ void __launch_bounds__(BLK) k_ploc_scatter(const Bvh2Node* __restrict
       st_node(&next[epos], ld_node(&cur[i]));
     }
     epos++;
+  }
+  // the tile holding the last cluster publishes the next pass's state
+  if (tid == 0 && base + PCHUNK >= count) {
+    st->count[parity ^ 1] = pre_e + (tot & 0xffffu);
+    st->insert[parity ^ 1] = ins_top - 2 * (pre_m + (tot >> 16));
+    st->passes += 1;
+    st->sum_counts += count;
   }
 }
 
@@ -690,11 +643,12 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   if (r) return r;
   Bvh2Node* cur = (Bvh2Node*)s.get(SLOT_PLOC_A, (size_t)n * sizeof(Bvh2Node));
   Bvh2Node* nxt = (Bvh2Node*)s.get(SLOT_PLOC_B, (size_t)n * sizeof(Bvh2Node));
-  int8_t* merge = (int8_t*)s.get(SLOT_MERGE, (size_t)n + 64);
-  uint32_t nb_max = div_up<uint32_t>(n, CHUNK);
-  uint2* partial = (uint2*)s.get(SLOT_PARTIAL, (size_t)nb_max * sizeof(uint2) + 16);
+  // look-back areas of two consecutive passes: [counter word pair, tile words]
+  const uint32_t lb_words = 2 * (div_up<uint32_t>(n, PCHUNK) + 2);  // 32-bit words per area
+  uint32_t* lb_area = (uint32_t*)s.get(SLOT_PARTIAL, (size_t)lb_words * 2 * 4 + 64);
   PlocState* st = (PlocState*)s.get(SLOT_PLOC_STATE, sizeof(PlocState));
-  if (!cur || !nxt || !merge || !partial || !st) return c.fail(OBVHS_ERR_OOM, "scratch");
+  if (!cur || !nxt || !lb_area || !st) return c.fail(OBVHS_ERR_OOM, "scratch");
+  CK(cudaMemsetAsync(lb_area, 0, (size_t)lb_words * 2 * 4, c.stream));
   uint32_t g = div_up<uint32_t>(n, BLK);
   KLAUNCH("k_gather", k_gather<<<g, BLK, 0, c.stream>>>(leaves, order, n, cur));
   PlocState h0{};
@@ -714,13 +668,12 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   while (known > TAIL_MAX) {
     const int batch = 4;
     for (int b = 0; b < batch; b++) {
-      int d1 = (radius == 1 || pass < depth_threshold) ? 1 : 0;
-      uint32_t gs = div_up<uint32_t>(known, BLK);
-      uint32_t gc = div_up<uint32_t>(known, CHUNK);
-      KLAUNCH("k_ploc_search", k_ploc_search<<<gs, BLK, 0, c.stream>>>(cur, st, parity, (int)radius, d1, merge));
-      KLAUNCH("k_ploc_count", k_ploc_count<<<gc, BLK, 0, c.stream>>>(merge, st, parity, partial));
-      KLAUNCH("k_ploc_scan", k_ploc_scan<<<1, 1024, 0, c.stream>>>(partial, st, parity));
-      KLAUNCH("k_ploc_scatter", k_ploc_scatter<<<gc, BLK, 0, c.stream>>>(cur, merge, st, parity, partial, nxt, out_nodes));
+      const int d1 = (radius == 1 || pass < depth_threshold) ? 1 : 0;
+      const uint32_t tiles = div_up<uint32_t>(known, PCHUNK);
+      unsigned long long* lb_cur = reinterpret_cast<unsigned long long*>(lb_area + (size_t)(parity)*lb_words);
+      uint32_t* lb_nxt = lb_area + (size_t)(parity ^ 1) * lb_words;
+      KLAUNCH("k_ploc_pass", k_ploc_pass<<<tiles, PT, 0, c.stream>>>(cur, nxt, out_nodes, st, parity, (int)radius, d1,
+                                                                      lb_cur, lb_nxt, lb_words, c.d_status));
       std::swap(cur, nxt);
       parity ^= 1;
       pass++;

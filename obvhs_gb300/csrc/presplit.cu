@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(BLK) k_tri_boxes(const float* __restrict__ tri
 // double-precision prefix.  One thread then chains the blocks exactly,
 // summing a block element by element only when the running sum is not in a
 // candidate binade or would leave its binade inside the block.
-constexpr int SUM_BLOCK = 1024;
+constexpr int SUM_BLOCK = 256;
 constexpr int NCAND_E = 3;
 
 struct BlockT {
@@ -93,91 +93,190 @@ __global__ void __launch_bounds__(BLK) k_block_dsum(const float* __restrict__ ha
   }
 }
 
+// A block's effect inside one binade: increments (even start, odd start)
+// and whether every element stays below the binade's width.
+struct Mono {
+  long long g0, g1;
+  int ok;
+};
+// `a` then `b`: the parity after `a` selects b's increment.
+__device__ __forceinline__ Mono mono_then(const Mono& a, const Mono& b) {
+  Mono r;
+  r.g0 = a.g0 + ((a.g0 & 1) ? b.g1 : b.g0);
+  r.g1 = a.g1 + (((1 + a.g1) & 1) ? b.g1 : b.g0);
+  r.ok = a.ok & b.ok;
+  return r;
+}
+__device__ __forceinline__ Mono mono_elem(float v, double scale) {
+  const double x = (double)v * scale;
+  if (!(x < 16777216.0)) return Mono{0, 0, 0};  // leaves the binade alone (or NaN)
+  const double fl = floor(x);
+  const double f = x - fl;
+  const long long m = (long long)fl;
+  if (f < 0.5) return Mono{m, m, 1};
+  if (f > 0.5) return Mono{m + 1, m + 1, 1};
+  // a tie rounds to the even significand: S + m + r even
+  return Mono{m + (m & 1), m + ((1 + m) & 1), 1};
+}
+__device__ __forceinline__ Mono shfl_down_mono(const Mono& v, int o) {
+  Mono r;
+  r.g0 = __shfl_down_sync(0xffffffffu, v.g0, o);
+  r.g1 = __shfl_down_sync(0xffffffffu, v.g1, o);
+  r.ok = __shfl_down_sync(0xffffffffu, v.ok, o);
+  return r;
+}
+
 __global__ void __launch_bounds__(BLK) k_block_transform(const float* __restrict__ ha, uint32_t n,
                                                          const double* __restrict__ bsum, BlockT* __restrict__ out) {
-  __shared__ float buf[SUM_BLOCK];
+  constexpr int PER = SUM_BLOCK / BLK;  // consecutive elements per thread
   __shared__ double sw[BLK / 32];
+  __shared__ Mono sm[BLK / 32];
   const uint32_t b = blockIdx.x;
   const uint32_t base = b * SUM_BLOCK;
-  const uint32_t m = min((uint32_t)SUM_BLOCK, n - base);
-  for (uint32_t j = threadIdx.x; j < SUM_BLOCK; j += BLK) buf[j] = j < m ? ha[base + j] : 0.0f;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float v[PER];
+#pragma unroll
+  for (int k = 0; k < PER; k++) {
+    const uint32_t i = base + threadIdx.x * PER + k;
+    v[k] = i < n ? ha[i] : 0.0f;
+  }
   // approximate running sum at the block start: sum of the earlier blocks
   double acc = 0.0;
   for (uint32_t k = threadIdx.x; k < b; k += BLK) acc += bsum[k];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = acc;
+  if (lane == 0) sw[warp] = acc;
   __syncthreads();
   double start = 0.0;
   for (int w = 0; w < BLK / 32; w++) start += sw[w];
-  int e0 = start > 0.0 ? ilogb(start) : -200;
-  const int t = threadIdx.x;
-  if (t < 2 * NCAND_E) {
-    const int ci = t >> 1, par = t & 1;
+  const int e0 = start > 0.0 ? ilogb(start) : -200;
+  for (int ci = 0; ci < NCAND_E; ci++) {
     const int e = e0 - 1 + ci;
-    long long inc = 0;
-    int p = par;
-    bool ok = e >= -126 && e <= 127;
-    const double scale = ok ? ldexp(1.0, 23 - e) : 0.0;  // 1 / u
-    for (uint32_t j = 0; ok && j < m; j++) {
-      double x = (double)buf[j] * scale;
-      if (!(x < 16777216.0)) {  // the element alone leaves the binade (or NaN)
-        ok = false;
-        break;
-      }
-      double fl = floor(x);
-      double f = x - fl;
-      long long mm = (long long)fl;
-      long long r = f < 0.5 ? 0 : (f > 0.5 ? 1 : (((p + mm) & 1) ? 1 : 0));
-      inc += mm + r;
-      p = (int)((p + mm + r) & 1);
+    const bool in_range = e >= -126 && e <= 127;
+    const double scale = in_range ? ldexp(1.0, 23 - e) : 0.0;  // 1 / u
+    Mono t = mono_elem(v[0], scale);
+#pragma unroll
+    for (int k = 1; k < PER; k++) t = mono_then(t, mono_elem(v[k], scale));
+    // ordered reduction: lane order within the warp, then warp order
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const Mono u = shfl_down_mono(t, o);
+      if ((lane & (2 * o - 1)) == 0) t = mono_then(t, u);
     }
-    out[b].inc[ci][par] = inc;
-    if (par == 0) out[b].valid[ci] = ok ? 1 : 0;
-    if (t == 0) out[b].e0 = e0;
+    if (lane == 0) sm[warp] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      Mono r = sm[0];
+      for (int w = 1; w < BLK / 32; w++) r = mono_then(r, sm[w]);
+      out[b].inc[ci][0] = r.g0;
+      out[b].inc[ci][1] = r.g1;
+      out[b].valid[ci] = (r.ok && in_range) ? 1 : 0;
+      if (ci == 0) out[b].e0 = e0;
+    }
+    __syncthreads();
   }
 }
 
-// One thread chains the blocks; then the preset thresholds
-// (src/splits.rs:23-33).
-__global__ void k_sum_chain(const float* __restrict__ ha, uint32_t n, const BlockT* __restrict__ tr,
-                            const int* largest_key, float* thr) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const uint32_t nb = (n + SUM_BLOCK - 1) / SUM_BLOCK;
-  float s = 0.0f;
-  uint32_t sequential_blocks = 0;
-  for (uint32_t b = 0; b < nb; b++) {
-    const uint32_t base = b * SUM_BLOCK;
-    const uint32_t m = min((uint32_t)SUM_BLOCK, n - base);
-    bool done = false;
+// Inclusive warp scan of monoid values in lane order.
+__device__ __forceinline__ Mono mono_warp_scan(Mono v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    Mono u;
+    u.g0 = __shfl_up_sync(0xffffffffu, v.g0, o);
+    u.g1 = __shfl_up_sync(0xffffffffu, v.g1, o);
+    u.ok = __shfl_up_sync(0xffffffffu, v.ok, o);
+    if (lane >= o) v = mono_then(u, v);
+  }
+  return v;
+}
+
+// Advances the exact running sum s over 32 consecutive items whose effects
+// inside s's binade are `mine` (one per lane): returns how many items were
+// applied (the items before the first one that leaves the binade or has no
+// valid effect) and updates s.
+__device__ __forceinline__ int warp_advance(float& s, Mono mine, int lane, int avail) {
+  const uint32_t bits = __float_as_uint(s);
+  const int ex = (int)((bits >> 23) & 0xff);
+  if (ex == 0 || ex == 0xff) return 0;  // zero, denormal or not finite
+  if (lane >= avail) mine = Mono{0, 0, 0};
+  const Mono pre = mono_warp_scan(mine, lane);
+  const long long S = (long long)((bits & 0x7fffffu) | 0x800000u);
+  const long long S2 = S + ((S & 1) ? pre.g1 : pre.g0);
+  const bool good = pre.ok && S2 < 16777216ll;
+  const uint32_t bad = __ballot_sync(0xffffffffu, !good);
+  const int f = bad ? __ffs(bad) - 1 : 32;  // items 0..f-1 apply
+  if (f > 0) {
+    const long long Sf = __shfl_sync(0xffffffffu, S2, f - 1);
+    s = __uint_as_float(((uint32_t)ex << 23) | (uint32_t)(Sf - 8388608ll));
+  }
+  return f;
+}
+
+// Element by element, 32 at a time: the prefix inside the current binade in
+// parallel, the element that leaves it with one exact addition.
+__device__ void warp_sum_range(float& s, const float* __restrict__ ha, uint32_t lo, uint32_t hi, int lane) {
+  uint32_t j = lo;
+  while (j < hi) {
+    const int avail = (int)min(32u, hi - j);
+    const float v = lane < avail ? ha[j + lane] : 0.0f;
     const uint32_t bits = __float_as_uint(s);
     const int ex = (int)((bits >> 23) & 0xff);
-    if (ex != 0 && ex != 0xff) {  // normal, positive
-      const int e = ex - 127;
-      const int ci = e - tr[b].e0 + 1;
-      if (ci >= 0 && ci < NCAND_E && tr[b].valid[ci]) {
-        const long long S = (long long)((bits & 0x7fffffu) | 0x800000u);
-        const long long S2 = S + tr[b].inc[ci][S & 1];
-        if (S2 < 16777216ll) {
-          s = __uint_as_float(((uint32_t)ex << 23) | (uint32_t)(S2 - 8388608ll));
-          done = true;
-        }
-      }
+    int f = 0;
+    if (ex != 0 && ex != 0xff) {
+      const double scale = ldexp(1.0, 23 - (ex - 127));
+      f = warp_advance(s, mono_elem(v, scale), lane, avail);
     }
-    if (!done) {
-      for (uint32_t j = 0; j < m; j++) s = __fadd_rn(s, ha[base + j]);
+    j += f;
+    if (f < avail && j < hi) {
+      s = __fadd_rn(s, __shfl_sync(0xffffffffu, v, f));  // the same value in every lane
+      j++;
+    }
+  }
+}
+
+// One warp chains the block transforms, 32 blocks per step; a block whose
+// transform does not apply is summed element-wise by warp_sum_range.  Then
+// the preset thresholds (src/splits.rs:23-33).
+__global__ void __launch_bounds__(32) k_sum_chain(const float* __restrict__ ha, uint32_t n, const BlockT* __restrict__ tr,
+                                                  const int* largest_key, float* thr) {
+  const int lane = threadIdx.x;
+  const uint32_t nb = (n + SUM_BLOCK - 1) / SUM_BLOCK;
+  float s = 0.0f;
+  uint32_t b = 0, sequential_blocks = 0;
+  uint32_t guard = 0;
+  while (b < nb && ++guard < 4 * nb + 64) {
+    const uint32_t bits = __float_as_uint(s);
+    const int ex = (int)((bits >> 23) & 0xff);
+    int f = 0;
+    if (ex != 0 && ex != 0xff) {
+      const int avail = (int)min(32u, nb - b);
+      Mono mine{0, 0, 0};
+      if (lane < avail) {
+        const BlockT& t = tr[b + lane];
+        const int ci = (ex - 127) - t.e0 + 1;
+        if (ci >= 0 && ci < NCAND_E && t.valid[ci]) mine = Mono{t.inc[ci][0], t.inc[ci][1], 1};
+      }
+      f = warp_advance(s, mine, lane, avail);
+    }
+    b += f;
+    if (b < nb && f < 32) {
+      const uint32_t lo = b * SUM_BLOCK;
+      warp_sum_range(s, ha, lo, min(lo + SUM_BLOCK, n), lane);
+      b++;
       sequential_blocks++;
     }
   }
-  const float avg = s / (float)n;
-  const float largest = fkey_inv(*largest_key);
-  const float hi_a = avg * 4.0f, hi_b = avg * 0.9f + largest * 0.1f;
-  thr[0] = avg * 3.0f;         // area_thresh_low
-  thr[1] = fmaxf(hi_a, hi_b);  // area_thresh_high (f32::max)
-  thr[2] = avg;
-  thr[3] = largest;
-  thr[4] = s;
-  thr[5] = __uint_as_float(sequential_blocks);
+  if (lane == 0) {
+    const float avg = s / (float)n;
+    const float largest = fkey_inv(*largest_key);
+    const float hi_a = avg * 4.0f, hi_b = avg * 0.9f + largest * 0.1f;
+    thr[0] = avg * 3.0f;         // area_thresh_low
+    thr[1] = fmaxf(hi_a, hi_b);  // area_thresh_high (f32::max)
+    thr[2] = avg;
+    thr[3] = largest;
+    thr[4] = s;
+    thr[5] = __uint_as_float(sequential_blocks);
+  }
 }
 
 // split_triangle (src/splits.rs:127-158).

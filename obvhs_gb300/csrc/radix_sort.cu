@@ -62,6 +62,11 @@ __global__ void __launch_bounds__(THREADS) k_rs_scan(uint32_t* hist) {
   h[threadIdx.x] = pre + x - v;
 }
 
+// One digit pass.  Warp w of a tile owns the contiguous keys
+// [w * 32 * ITEMS, (w + 1) * 32 * ITEMS) of the tile, so (warp, round, lane)
+// is input order and each warp ranks its keys stably against its own digit
+// histogram without block barriers; one scan over the warps' histograms per
+// digit then gives every key its place in the tile.
 template <class K>
 __global__ void __launch_bounds__(THREADS) k_rs_pass(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                                                      K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
@@ -71,52 +76,51 @@ __global__ void __launch_bounds__(THREADS) k_rs_pass(const K* __restrict__ keys_
   constexpr int ITEMS = Tile<K>::ITEMS;
   constexpr int TS = Tile<K>::SIZE;
   __shared__ uint32_t s_tile;
-  __shared__ uint32_t s_run[256];       // running digit counts in this tile
-  __shared__ uint32_t s_cnt[WARPS][256];
-  __shared__ uint32_t s_pre[WARPS][256];
-  __shared__ uint32_t s_off[256];       // global offset of each digit for this tile
+  __shared__ uint32_t s_wh[WARPS][256];  // per-warp digit counts, then per-warp exclusive offsets
+  __shared__ uint32_t s_off[256];        // global offset of each digit for this tile
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) s_tile = atomicAdd(tile_counter, 1u);
-  s_run[tid] = 0;
 #pragma unroll
-  for (int w = 0; w < WARPS; w++) s_cnt[w][tid] = 0;
+  for (int w = 0; w < WARPS; w++) s_wh[w][tid] = 0;
   __syncthreads();
   const uint32_t tile = s_tile;
-  const uint32_t base = tile * TS;
+  const uint32_t wbase = tile * TS + warp * 32 * ITEMS;
   const uint32_t lt_mask = (1u << lane) - 1u;
   K key[ITEMS];
   uint32_t val[ITEMS], rank[ITEMS], dig[ITEMS];
 #pragma unroll
   for (int r = 0; r < ITEMS; r++) {
-    const uint32_t i = base + r * THREADS + tid;
-    const bool valid = i < n;
-    uint32_t d = 256;
-    if (valid) {
+    const uint32_t i = wbase + r * 32 + lane;
+    if (i < n) {
       key[r] = keys_in[i];
       val[r] = iota ? i : vals_in[i];
-      d = KeyTraits<K>::digit(key[r], byte);
     }
+  }
+  uint32_t* wh = s_wh[warp];
+#pragma unroll
+  for (int r = 0; r < ITEMS; r++) {
+    const uint32_t i = wbase + r * 32 + lane;
+    const bool valid = i < n;
+    const uint32_t d = valid ? KeyTraits<K>::digit(key[r], byte) : 256u;
     dig[r] = d;
     const uint32_t peers = __match_any_sync(0xffffffffu, d);
     const uint32_t lrank = __popc(peers & lt_mask);
-    if (valid && lrank == 0) s_cnt[warp][d] = __popc(peers);
-    __syncthreads();
-    {
-      uint32_t run = s_run[tid];
+    const uint32_t before = valid ? wh[d] : 0u;
+    __syncwarp();
+    if (valid && lrank == 0) wh[d] = before + __popc(peers);
+    __syncwarp();
+    rank[r] = before + lrank;
+  }
+  __syncthreads();
+  // per digit (thread tid): warp offsets inside the tile and the tile count
+  uint32_t count = 0;
 #pragma unroll
-      for (int w = 0; w < WARPS; w++) {
-        uint32_t c = s_cnt[w][tid];
-        s_pre[w][tid] = run;
-        s_cnt[w][tid] = 0;
-        run += c;
-      }
-      s_run[tid] = run;
-    }
-    __syncthreads();
-    rank[r] = valid ? s_pre[warp][d] + lrank : 0;
+  for (int w = 0; w < WARPS; w++) {
+    const uint32_t c = s_wh[w][tid];
+    s_wh[w][tid] = count;
+    count += c;
   }
   // publish this tile's count of digit `tid`, then look back for the prefix
-  const uint32_t count = s_run[tid];
   uint32_t* my = tile_status + (size_t)tile * 256 + tid;
   uint32_t prefix = 0;
   if (tile == 0) {
@@ -126,16 +130,16 @@ __global__ void __launch_bounds__(THREADS) k_rs_pass(const K* __restrict__ keys_
     int64_t t = (int64_t)tile - 1;
     uint32_t spins = 0;
     while (t >= 0) {
-      uint32_t s = *((volatile uint32_t*)(tile_status + (size_t)t * 256 + tid));
-      if ((s & ~VAL_MASK) == 0) {
+      const uint32_t v = *((volatile uint32_t*)(tile_status + (size_t)t * 256 + tid));
+      if ((v & ~VAL_MASK) == 0) {
         if (++spins > SPIN_LIMIT) {
           atomicOr(status, 4u);  // ST_ITER_LIMIT
           break;
         }
         continue;
       }
-      prefix += s & VAL_MASK;
-      if (s & FLAG_INC) break;
+      prefix += v & VAL_MASK;
+      if (v & FLAG_INC) break;
       t--;
     }
     atomicExch(my, FLAG_INC | (prefix + count));
@@ -145,7 +149,7 @@ __global__ void __launch_bounds__(THREADS) k_rs_pass(const K* __restrict__ keys_
 #pragma unroll
   for (int r = 0; r < ITEMS; r++) {
     if (dig[r] < 256) {
-      const uint32_t pos = s_off[dig[r]] + rank[r];
+      const uint32_t pos = s_off[dig[r]] + wh[dig[r]] + rank[r];
       keys_out[pos] = key[r];
       vals_out[pos] = val[r];
     }

@@ -452,7 +452,7 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
     MisArgs ma{reins, order, counters, parents, state, owner, touched, counters + 2, c.d_status, count + 2};
     void* args[] = {&ma};
     uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)mis_blocks, std::max<uint64_t>(1, div_up<uint32_t>(count, BLK)));
-    CK(cudaLaunchCooperativeKernel((void*)k_mis, grid, BLK, args, 0, c.stream));
+    KLAUNCH("k_mis", CK(cudaLaunchCooperativeKernel((void*)k_mis, grid, BLK, args, 0, c.stream)));
     const uint32_t gk = div_up<uint32_t>(count, BLK);
     KLAUNCH("k_apply", k_apply<<<gk, BLK, 0, c.stream>>>(b->nodes, parents, reins, order, state, counters, counters + 1, starts));
     KLAUNCH("k_mark", k_mark<<<gk, BLK, 0, c.stream>>>(starts, counters, parents, dirty, list, counters + 5, len));
