@@ -49,7 +49,8 @@ typedef enum {
   OBVHS_ERR_BAD_INPUT = -4,   /* NaN coordinates, leaves with >1 primitive, or non-finite
                                  CWBVH costs; the reference panics or indexes out of range */
   OBVHS_ERR_LIMIT = -5,       /* a bounded device loop or stack reached its limit */
-  OBVHS_ERR_DEVICE = -6       /* a kernel set its status word */
+  OBVHS_ERR_DEVICE = -6,      /* a kernel set its status word */
+  OBVHS_ERR_TOO_LARGE = -7    /* input larger than a fixed-capacity entry point accepts */
 } obvhs_status;
 
 typedef struct obvhs_ctx obvhs_ctx;
@@ -189,6 +190,25 @@ OBVHS_API int obvhs_ray_traverse_miss(obvhs_ctx* ctx, const obvhs_cwbvh* bvh, co
  * stable sorted order. */
 OBVHS_API int obvhs_morton_sort(obvhs_ctx* ctx, const float* aabbs, uint32_t n, uint32_t sort_precision, uint64_t* codes,
                       uint32_t* order);
+
+/* ---- allocation-free variant -------------------------------------------- */
+/* No counterpart in the reference.  obvhs_morton_sort for callers that cannot
+ * allocate device memory (an engine that keeps all GPU memory in its own pool,
+ * or frame-time code that cannot afford cudaMalloc's synchronisation).  It
+ * calls no cudaMalloc/cudaFree: its working memory is one fixed array in the
+ * library's device image (about 20 MiB, held on every GPU this function runs
+ * on until the process exits), for at most OBVHS_NOALLOC_MAX_PRIMS boxes;
+ * larger n returns OBVHS_ERR_TOO_LARGE before any GPU work.
+ * aabbs (float[n][6]), codes (u64[n][2], may be NULL) and order (u32[n]) are
+ * DEVICE pointers on the current device; the work runs on `stream` (a
+ * cudaStream_t, NULL = default stream) and the call synchronises that stream
+ * before returning.  Results equal obvhs_morton_sort's.  The first call on a
+ * device looks up the array's device address; make that call before any
+ * stream capture.  All calls on a device share the array: calls whose GPU
+ * work overlaps (other streams or threads) race and must be serialised. */
+#define OBVHS_NOALLOC_MAX_PRIMS 262144u
+OBVHS_API int obvhs_morton_sort_noalloc(const float* aabbs, uint32_t n, uint32_t sort_precision, uint64_t* codes,
+                                        uint32_t* order, void* stream);
 
 #ifdef __cplusplus
 }

@@ -25,6 +25,7 @@ ERRORS = {
     -4: "bad input",
     -5: "device limit reached",
     -6: "device status set",
+    -7: "input larger than the entry point's fixed capacity",
 }
 
 
@@ -90,6 +91,7 @@ SIGNATURES = {
     "obvhs_ray_traverse": (I32, [P, P, P, U32, P, I32]),
     "obvhs_ray_traverse_miss": (I32, [P, P, P, U32, P, I32]),
     "obvhs_morton_sort": (I32, [P, P, U32, U32, P, P]),
+    "obvhs_morton_sort_noalloc": (I32, [P, U32, U32, P, P, P]),
 }
 
 _lib = None
