@@ -53,10 +53,10 @@ enum ScratchSlot {
   SLOT_BVH2_NODES,
   SLOT_BVH2_PIDX,
   SLOT_TRAV_OUT,
-  SLOT_PENDING,
-  SLOT_DIRTY_LIST,
+  SLOT_ARRIVE,
+  SLOT_CONF,
   SLOT_STARTS,
-  SLOT_DONE,
+  SLOT_PLIST,
   SLOT_COUNT
 };
 
