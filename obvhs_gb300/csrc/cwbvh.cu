@@ -25,6 +25,10 @@
 // takes nodes from a device work queue in which every node's item is
 // published by its parent's warp, so nodes are written at exactly the
 // reference's positions: the output is byte for byte the reference's.
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
 #include "build.h"
 
 namespace {
@@ -230,12 +234,20 @@ __device__ __forceinline__ float pow2f(float c) {
   return 0.0f;
 }
 
-// The reference computes ceil(log2(x)) with glibc's log2f; a correctly
-// rounded float log2 (here: double log2 rounded to float) gives the same
-// ceiling for every finite positive float.
-__device__ __forceinline__ float exp_grid(float ext) {
-  const float l = __double2float_rn(log2((double)ext));
-  return pow2f(ceilf(l));
+// The reference computes exp2(ceil(log2(x))) with the C library's log2f
+// (src/cwbvh/bvh2_to_cwbvh.rs:95-99).  For a normal x = 2^k * (1 + m/2^23),
+// ceil(log2f(x)) is k when m == 0 or when log2f rounds down to exactly k,
+// else k + 1; which of the two depends only on whether m reaches a threshold
+// per exponent.  The host finds those thresholds with its own log2f
+// (ceil_log2_thresholds), so the device needs no double-precision log2.
+__device__ __forceinline__ float exp_grid(float ext, const uint32_t* thr) {
+  const uint32_t b = __float_as_uint(ext);
+  const uint32_t e = b >> 23;  // ext > 0
+  if (e == 0xffu) return ext;  // +inf
+  if (e == 0u) return pow2f(ceilf(__double2float_rn(log2((double)ext))));  // subnormal: not reached for ext >= 1e-20/255
+  const uint32_t m = b & 0x7fffffu;
+  const int k = (int)e - 127;
+  return pow2f((float)(m != 0u && m >= thr[e] ? k + 1 : k));
 }
 
 __device__ __forceinline__ float3 center(const Box& b) {
@@ -246,6 +258,7 @@ __device__ __forceinline__ float3 center(const Box& b) {
 // published (ready[k] = 1) by the warp that emits its parent.  Warps take
 // indices in order from `head` and append children at `tail`.
 struct EmitArgs {
+  uint32_t log2_thr[256];  // ceil_log2_thresholds()
   const Bvh2Node* nodes;
   const uint32_t* pidx_in;
   const Dec* dec;
@@ -279,9 +292,9 @@ __device__ void emit_node(const EmitArgs& a, const Item it, int lane, uint8_t* s
   const Bvh2Node nd = ld_node(&a.nodes[it.bvh2]);
   const Box box = node_box(nd);
   const float3 p = box.mn;
-  const float ex = exp_grid(smax(box.mx.x - box.mn.x, 1e-20f) * DENOM);
-  const float ey = exp_grid(smax(box.mx.y - box.mn.y, 1e-20f) * DENOM);
-  const float ez = exp_grid(smax(box.mx.z - box.mn.z, 1e-20f) * DENOM);
+  const float ex = exp_grid(smax(box.mx.x - box.mn.x, 1e-20f) * DENOM, a.log2_thr);
+  const float ey = exp_grid(smax(box.mx.y - box.mn.y, 1e-20f) * DENOM, a.log2_thr);
+  const float ez = exp_grid(smax(box.mx.z - box.mn.z, 1e-20f) * DENOM, a.log2_thr);
   const float rx = 1.0f / ex, ry = 1.0f / ey, rz = 1.0f / ez;
 
   // children (lane 0 walks the distribution), one per lane
@@ -488,14 +501,17 @@ __global__ void __launch_bounds__(EMIT_THREADS) k_emit_all(EmitArgs a) {
     // wait for the parent's warp to publish item k (bounded)
     uint32_t ok = 1;
     if (lane == 0) {
-      uint32_t spins = 0;
+      // exponential back-off: early in the build most warps wait here, and
+      // tight polling starves the warps doing the work
+      uint32_t spins = 0, ns = 32;
       while (*(volatile uint32_t*)&a.ready[k] == 0) {
         if (++spins > (1u << 22)) {
           set_status(a.status, ST_ITER_LIMIT);
           ok = 0;
           break;
         }
-        __nanosleep(64);
+        __nanosleep(ns);
+        if (ns < 2048) ns <<= 1;
       }
       __threadfence();
     }
@@ -511,6 +527,32 @@ __global__ void __launch_bounds__(EMIT_THREADS) k_emit_all(EmitArgs a) {
 }
 
 }  // namespace
+
+// For each float exponent field e (1..254) the smallest mantissa m >= 1 with
+// ceil(log2f(2^(e-127) * (1 + m/2^23))) = e - 126, by binary search on the
+// host's log2f (monotone); 2^23 when no mantissa reaches it.
+static const uint32_t* ceil_log2_thresholds() {
+  static uint32_t thr[256];
+  static std::once_flag once;
+  std::call_once(once, [] {
+    auto up = [](uint32_t e, uint32_t m) {
+      uint32_t bits = (e << 23) | m;
+      float x;
+      std::memcpy(&x, &bits, 4);
+      return std::ceil(std::log2(x)) > (float)((int)e - 127);
+    };
+    thr[0] = thr[255] = 1u << 23;
+    for (uint32_t e = 1; e < 255; e++) {
+      uint32_t lo = 1, hi = 1u << 23;  // answer in [lo, hi]; hi = none
+      while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (up(e, mid)) hi = mid; else lo = mid + 1;
+      }
+      thr[e] = lo;
+    }
+  });
+  return thr;
+}
 
 int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, int order_children, obvhs_cwbvh* out) {
   out->n_nodes = 0;
@@ -576,8 +618,9 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   CK(cudaMemcpyAsync(items, hst, 16, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(ready, hst + 4, 4, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(counters + 12, hst + 5, 12, cudaMemcpyHostToDevice, c.stream));
-  EmitArgs ea{b->nodes, b->prim_indices, dec, items, ready, counters + 12, counters + 13, order_children, n_cw, n_pr,
+  EmitArgs ea{{}, b->nodes, b->prim_indices, dec, items, ready, counters + 12, counters + 13, order_children, n_cw, n_pr,
               cwn, cwp, c.d_status, counters + 14};
+  std::memcpy(ea.log2_thr, ceil_log2_thresholds(), sizeof(ea.log2_thr));
   const uint32_t grid = (uint32_t)std::min<uint64_t>(
       emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)n_cw * 32, EMIT_THREADS)));
   KLAUNCH("k_emit_all", k_emit_all<<<grid, EMIT_THREADS, 0, c.stream>>>(ea));

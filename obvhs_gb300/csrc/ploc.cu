@@ -344,32 +344,43 @@ __global__ void __launch_bounds__(PT) k_ploc_pass(const Bvh2Node* __restrict__ c
     tot += s_w[w];
   }
   const uint32_t excl = wpre + x - packed;
-  // decoupled look-back on (emitted, merged) = (low 31 bits, next 31 bits)
-  if (tid == 0) {
+  // decoupled look-back on (emitted, merged) = (low 31 bits, next 31 bits):
+  // warp 0 reads 32 earlier tiles per step (lane l reads tile t - l; before
+  // tile 0 reads as an inclusive zero) and adds the nearest ones up to the
+  // first inclusive prefix
+  if (warp == 0) {
     const unsigned long long agg = (unsigned long long)(tot & 0xffffu) | ((unsigned long long)(tot >> 16) << 31);
     unsigned long long prefix = 0;
     if (tile == 0) {
-      atomicExch(&tstat[0], LB_INC | agg);
+      if (lane == 0) atomicExch(&tstat[0], LB_INC | agg);
     } else {
-      atomicExch(&tstat[tile], LB_AGG | agg);
+      if (lane == 0) atomicExch(&tstat[tile], LB_AGG | agg);
       int64_t t = (int64_t)tile - 1;
       uint32_t spins = 0;
-      while (t >= 0) {
-        const unsigned long long v = *((volatile unsigned long long*)&tstat[t]);
-        if ((v >> 62) == 0) {
-          if (++spins > (1u << 24)) {
-            atomicOr(status, ST_ITER_LIMIT);
-            break;
-          }
-          continue;
+      for (;;) {
+        const int64_t idx = t - lane;
+        const unsigned long long v = idx >= 0 ? *((volatile unsigned long long*)&tstat[idx]) : (unsigned long long)LB_INC;
+        const uint32_t fl = (uint32_t)(v >> 62);
+        const uint32_t inc = __ballot_sync(0xffffffffu, fl == 2u);
+        const uint32_t not_ready = __ballot_sync(0xffffffffu, fl == 0u);
+        // lanes needed: up to and including the nearest inclusive one
+        const uint32_t need = inc ? (((inc & (0u - inc)) << 1) - 1u) : 0xffffffffu;
+        uint32_t take = need;
+        if (not_ready & need) take = ((not_ready & (0u - not_ready)) - 1u);  // the ready lanes before it
+        unsigned long long part = ((take >> lane) & 1u) ? (v & ((1ull << 62) - 1)) : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+        prefix += part;
+        if (take == need && inc) break;
+        t -= __popc(take);
+        if (take == 0 && ++spins > (1u << 24)) {
+          if (lane == 0) atomicOr(status, ST_ITER_LIMIT);
+          break;
         }
-        prefix += v & ((1ull << 62) - 1);
-        if (v & LB_INC) break;
-        t--;
       }
-      atomicExch(&tstat[tile], LB_INC | (prefix + agg));
+      if (lane == 0) atomicExch(&tstat[tile], LB_INC | (prefix + agg));
     }
-    s_prefix = prefix;
+    if (lane == 0) s_prefix = prefix;
   }
   __syncthreads();
   const unsigned long long pre = s_prefix;

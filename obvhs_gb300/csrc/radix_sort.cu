@@ -21,6 +21,8 @@ constexpr uint32_t FLAG_AGG = 1u << 30;
 constexpr uint32_t FLAG_INC = 2u << 30;
 constexpr uint32_t VAL_MASK = (1u << 30) - 1;
 constexpr uint32_t SPIN_LIMIT = 1u << 24;
+constexpr int LB_WINDOW = 8;
+constexpr int HIST_ITEMS = 8;
 
 template <class K>
 struct Tile {
@@ -28,17 +30,25 @@ struct Tile {
   static constexpr int SIZE = THREADS * ITEMS;
 };
 
+// One tile of HIST_ITEMS keys per thread, all loads issued before the
+// shared-memory counting.
 template <class K>
 __global__ void __launch_bounds__(THREADS) k_rs_hist(const K* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist) {
   constexpr int NB = KeyTraits<K>::BYTES;
   __shared__ uint32_t h[NB * 256];
   for (int i = threadIdx.x; i < NB * 256; i += THREADS) h[i] = 0;
-  __syncthreads();
-  for (uint32_t i = blockIdx.x * THREADS + threadIdx.x; i < n; i += gridDim.x * THREADS) {
-    K k = keys[i];
+  const uint32_t base = blockIdx.x * (THREADS * HIST_ITEMS) + threadIdx.x;
+  K k[HIST_ITEMS];
 #pragma unroll
-    for (int b = 0; b < NB; b++) atomicAdd(&h[b * 256 + KeyTraits<K>::digit(k, b)], 1u);
-  }
+  for (int r = 0; r < HIST_ITEMS; r++)
+    if (base + r * THREADS < n) k[r] = keys[base + r * THREADS];
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < HIST_ITEMS; r++)
+    if (base + r * THREADS < n) {
+#pragma unroll
+      for (int b = 0; b < NB; b++) atomicAdd(&h[b * 256 + KeyTraits<K>::digit(k[r], b)], 1u);
+    }
   __syncthreads();
   for (int i = threadIdx.x; i < NB * 256; i += THREADS)
     if (h[i]) atomicAdd(&hist[i], h[i]);
@@ -68,7 +78,7 @@ __global__ void __launch_bounds__(THREADS) k_rs_scan(uint32_t* hist) {
 // histogram without block barriers; one scan over the warps' histograms per
 // digit then gives every key its place in the tile.
 template <class K>
-__global__ void __launch_bounds__(THREADS) k_rs_pass(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+__global__ void __launch_bounds__(THREADS, 3) k_rs_pass(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                                                      K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                                                      uint32_t n, int byte, bool iota,
                                                      const uint32_t* __restrict__ digit_base,
@@ -120,7 +130,9 @@ __global__ void __launch_bounds__(THREADS) k_rs_pass(const K* __restrict__ keys_
     s_wh[w][tid] = count;
     count += c;
   }
-  // publish this tile's count of digit `tid`, then look back for the prefix
+  // publish this tile's count of digit `tid`, then look back for the prefix,
+  // LB_WINDOW earlier tiles per step (positions before tile 0 read as an
+  // inclusive zero)
   uint32_t* my = tile_status + (size_t)tile * 256 + tid;
   uint32_t prefix = 0;
   if (tile == 0) {
@@ -129,18 +141,30 @@ __global__ void __launch_bounds__(THREADS) k_rs_pass(const K* __restrict__ keys_
     atomicExch(my, FLAG_AGG | count);
     int64_t t = (int64_t)tile - 1;
     uint32_t spins = 0;
-    while (t >= 0) {
-      const uint32_t v = *((volatile uint32_t*)(tile_status + (size_t)t * 256 + tid));
-      if ((v & ~VAL_MASK) == 0) {
-        if (++spins > SPIN_LIMIT) {
-          atomicOr(status, 4u);  // ST_ITER_LIMIT
-          break;
+    for (;;) {
+      uint32_t v[LB_WINDOW];
+#pragma unroll
+      for (int w = 0; w < LB_WINDOW; w++)
+        v[w] = t - w >= 0 ? *((volatile uint32_t*)(tile_status + (size_t)(t - w) * 256 + tid)) : (uint32_t)FLAG_INC;
+      bool stop = false, blocked = false;
+      int adv = 0;
+#pragma unroll
+      for (int w = 0; w < LB_WINDOW; w++) {
+        if (stop || blocked) continue;
+        if ((v[w] & ~VAL_MASK) == 0) {
+          blocked = true;
+        } else {
+          prefix += v[w] & VAL_MASK;
+          adv++;
+          stop = (v[w] & FLAG_INC) != 0;
         }
-        continue;
       }
-      prefix += v & VAL_MASK;
-      if (v & FLAG_INC) break;
-      t--;
+      if (stop) break;
+      t -= adv;
+      if (adv == 0 && ++spins > SPIN_LIMIT) {
+        atomicOr(status, 4u);  // ST_ITER_LIMIT
+        break;
+      }
     }
     atomicExch(my, FLAG_INC | (prefix + count));
   }
@@ -182,8 +206,7 @@ cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, 
   const size_t pass_words = (size_t)ntiles * 256 + 32;
   cudaError_t e = cudaMemsetAsync(scratch, 0, (16 * 256 + NB * pass_words) * sizeof(uint32_t), c.stream);
   if (e) return e;
-  uint32_t hb = (n + THREADS * 16 - 1) / (THREADS * 16);
-  if (hb > 1024) hb = 1024;
+  const uint32_t hb = (n + THREADS * HIST_ITEMS - 1) / (THREADS * HIST_ITEMS);
   KLAUNCH("k_rs_hist", k_rs_hist<K><<<hb, THREADS, 0, c.stream>>>(keys, n, hist));
   KLAUNCH("k_rs_scan", k_rs_scan<<<NB, THREADS, 0, c.stream>>>(hist));
   K* kin = keys;

@@ -34,6 +34,8 @@ namespace cg = cooperative_groups;
 namespace {
 
 constexpr int BLK = 256;
+constexpr int RESOLVE_THREADS = 1024;
+constexpr uint32_t RESOLVE_SMALL = 512;  // proposals one block resolves faster than the grid (one climb per thread)
 
 struct Reins {
   uint32_t from, to;
@@ -70,83 +72,152 @@ __global__ void k_cand_keys(const Bvh2Node* __restrict__ nodes, uint32_t take, u
   vals[i - 1] = i;
 }
 
-// find_reinsertion (src/bvh2/reinsertion.rs:233-334).  CAP entries of
-// (area, node) on a per-thread stack; CLAMP = StackStack semantics (the last
-// slot is overwritten when full), else overflow is an error (the reference's
-// HeapStack panics).
+// find_reinsertion (src/bvh2/reinsertion.rs:233-334) for one candidate, as a
+// state machine advanced one step at a time: a stack pop of the
+// branch-and-bound search below the current pivot, or a climb to the next
+// pivot.  CAP entries of (area, node) on a per-thread stack (one 8-byte local
+// word each); CLAMP = StackStack semantics (the last slot is overwritten when
+// full), else overflow is an error (the reference's HeapStack panics).
 template <int CAP, bool CLAMP>
-__global__ void __launch_bounds__(128) k_find(const Bvh2Node* __restrict__ nodes, const uint32_t* __restrict__ parents,
-                                              const uint32_t* __restrict__ cand, uint32_t count, uint32_t cap_rt,
-                                              Reins* __restrict__ out, uint32_t* status) {
-  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= count) return;
-  const uint32_t node_id = cand[k];
-  float st_a[CAP];
-  uint32_t st_n[CAP];
-  uint32_t sp = 0;
-  const uint32_t cap = CLAMP ? CAP : cap_rt;
-  bool overflow = false;
-  auto push = [&](float a, uint32_t id) {
+struct FindSearch {
+  uint2* st;  // the thread's stack, CAP entries (kept apart so the scalars stay in registers)
+  uint32_t sp, guard, cap;
+  bool overflow;
+  uint32_t node_id, parent_id, sib, pivot_id, best_to;
+  float node_area, area_diff, best_diff;
+  Box box, pivot_bbox;
+
+  __device__ __forceinline__ void push(float a, uint32_t id) {
+    const uint2 v = make_uint2(__float_as_uint(a), id);
     if (CLAMP) {
-      st_a[sp] = a;
-      st_n[sp] = id;
+      st[sp] = v;
       sp = min(sp + 1, (uint32_t)CAP - 1);
     } else if (sp >= cap) {
       overflow = true;
     } else {
-      st_a[sp] = a;
-      st_n[sp] = id;
+      st[sp] = v;
       sp++;
     }
-  };
-  Reins best{node_id, 0, 0.0f, 0};
-  const Box box = node_box(ld_node(&nodes[node_id]));
-  const float node_area = half_area(box);
-  const uint32_t parent_id = parents[node_id];
-  float area_diff = half_area(node_box(ld_node(&nodes[parent_id])));
-  uint32_t sib = sibling_of(node_id);
-  Box pivot_bbox = node_box(ld_node(&nodes[sib]));
-  uint32_t pivot_id = parent_id;
-  uint32_t guard = 0;
-  for (;;) {
+  }
+  __device__ __forceinline__ void start(const Bvh2Node* nodes, const uint32_t* parents, uint32_t node) {
+    node_id = node;
+    best_to = 0;
+    best_diff = 0.0f;
+    box = node_box(ld_node(&nodes[node_id]));
+    node_area = half_area(box);
+    parent_id = parents[node_id];
+    area_diff = half_area(node_box(ld_node(&nodes[parent_id])));
+    sib = sibling_of(node_id);
+    pivot_bbox = node_box(ld_node(&nodes[sib]));
+    pivot_id = parent_id;
+    sp = 0;
+    guard = 0;
+    overflow = false;
     push(area_diff, sib);
-    while (sp != 0 && !overflow) {
+  }
+  // One step; returns true when the search is over.
+  __device__ __forceinline__ bool step(const Bvh2Node* nodes, const uint32_t* parents) {
+    if (sp != 0 && !overflow) {
       if (++guard > (1u << 26)) {
         overflow = true;
-        break;
+        return true;
       }
       sp--;
-      float top_area = st_a[sp];
-      uint32_t top_id = st_n[sp];
-      if (top_area - node_area <= best.area_diff) continue;
-      Bvh2Node dst = ld_node(&nodes[top_id]);
-      float merged = half_area(box_union(node_box(dst), box));
-      float reinsert_area = top_area - merged;
-      if (reinsert_area > best.area_diff) {
-        best.to = top_id;
-        best.area_diff = reinsert_area;
+      const uint2 top = st[sp];
+      const float top_area = __uint_as_float(top.x);
+      if (top_area - node_area <= best_diff) return false;
+      const Bvh2Node dst = ld_node(&nodes[top.y]);
+      const float reinsert_area = top_area - half_area(box_union(node_box(dst), box));
+      if (reinsert_area > best_diff) {
+        best_to = top.y;
+        best_diff = reinsert_area;
       }
       if (node_prims(dst) == 0) {
-        float child_area = reinsert_area + half_area(node_box(dst));
+        const float child_area = reinsert_area + half_area(node_box(dst));
         push(child_area, node_first(dst));
         push(child_area, node_first(dst) + 1);
       }
+      return false;
     }
-    if (overflow) break;
+    if (overflow) return true;
     if (pivot_id != parent_id) {
       pivot_bbox = box_union(pivot_bbox, node_box(ld_node(&nodes[sib])));
       area_diff += half_area(node_box(ld_node(&nodes[pivot_id]))) - half_area(pivot_bbox);
     }
-    if (pivot_id == 0) break;
+    if (pivot_id == 0) return true;
     sib = sibling_of(pivot_id);
     pivot_id = parents[pivot_id];
+    push(area_diff, sib);
+    return false;
   }
-  if (overflow) {
-    set_status(status, ST_STACK_OVERFLOW);
-    best = Reins{0, 0, 0.0f, 0};
+  __device__ __forceinline__ Reins result(const uint32_t* parents, uint32_t* status) const {
+    Reins best{node_id, best_to, best_diff, 0};
+    if (overflow) {
+      set_status(status, ST_STACK_OVERFLOW);
+      best = Reins{0, 0, 0.0f, 0};
+    }
+    if (best.to == sibling_of(best.from) || best.to == parents[best.from]) best = Reins{0, 0, 0.0f, 0};
+    return best;
   }
-  if (best.to == sibling_of(best.from) || best.to == parents[best.from]) best = Reins{0, 0, 0.0f, 0};
-  out[k] = best;
+};
+
+constexpr int FIND_THREADS = 128;
+
+// One candidate per thread.
+template <int CAP, bool CLAMP>
+__global__ void __launch_bounds__(FIND_THREADS) k_find(const Bvh2Node* __restrict__ nodes,
+                                                       const uint32_t* __restrict__ parents,
+                                                       const uint32_t* __restrict__ cand, uint32_t count,
+                                                       uint32_t cap_rt, Reins* __restrict__ out, uint32_t* status) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  uint2 stack[CAP];
+  FindSearch<CAP, CLAMP> f;
+  f.st = stack;
+  f.cap = CLAMP ? CAP : cap_rt;
+  f.start(nodes, parents, cand[k]);
+  while (!f.step(nodes, parents)) {
+  }
+  out[k] = f.result(parents, status);
+}
+
+// More candidates than resident threads: searches differ widely in length,
+// so a thread that finishes one takes the next from a shared counter
+// (warp-aggregated) instead of idling until its warp's longest search ends.
+template <int CAP, bool CLAMP>
+__global__ void __launch_bounds__(FIND_THREADS) k_find_persistent(const Bvh2Node* __restrict__ nodes,
+                                                                  const uint32_t* __restrict__ parents,
+                                                                  const uint32_t* __restrict__ cand, uint32_t count,
+                                                                  uint32_t cap_rt, Reins* __restrict__ out,
+                                                                  uint32_t* next, uint32_t* status) {
+  const int lane = threadIdx.x & 31;
+  uint2 stack[CAP];
+  FindSearch<CAP, CLAMP> f;
+  f.st = stack;
+  f.cap = CLAMP ? CAP : cap_rt;
+  uint32_t k = 0;
+  bool active = false, need = true;
+  for (;;) {
+    const uint32_t want = __ballot_sync(0xffffffffu, need);
+    if (want) {
+      const int leader = __ffs(want) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(next, (uint32_t)__popc(want));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        need = false;
+        k = base + __popc(want & ((1u << lane) - 1u));
+        active = k < count;
+        if (active) f.start(nodes, parents, cand[k]);
+      }
+    }
+    if (!__any_sync(0xffffffffu, active)) break;
+    if (active && f.step(nodes, parents)) {
+      out[k] = f.result(parents, status);
+      active = false;
+      need = true;
+    }
+  }
 }
 
 // Priority of proposal k (lower = earlier): area_diff descending, then
@@ -173,12 +244,12 @@ struct ResolveArgs {
   uint32_t* plist;            // proposals with area_diff > 0 (indices into reins)
   Conf* conf;                 // per plist entry
   uint8_t* state;             // per plist entry: 0 unresolved, 1 accepted, 2 rejected
-  unsigned long long* owner;  // two arrays of n_nodes: lowest claiming key, by round parity
+  unsigned long long* owner;  // three arrays of n_nodes: lowest claiming key, by round mod 3
   uint32_t* touched;          // per node: pass stamp once an accepted proposal touched it
   uint32_t* dirty;            // per node: pass stamp once marked for refit
   uint32_t* arrive;           // per node: pass stamp once one of two marked children is refit
   uint2* starts;              // per plist entry: refit start nodes this proposal marked first
-  uint32_t* ctr;              // this pass: [0] plist size, [1..3] round counters, [4] rounds
+  uint32_t* ctr;              // this pass: [0] plist size, [1..3] round counters, [4] rounds, [5] k_find's counter
   uint32_t* applied;          // running total of applied moves
   uint32_t* status;
   uint32_t stamp;             // pass number, from 1: per-node words from earlier passes read as unset
@@ -210,6 +281,12 @@ __device__ __forceinline__ void stcg_inner(Bvh2Node* p, const Box& u, uint32_t f
   float4* w = reinterpret_cast<float4*>(p);
   __stcg(w, make_float4(u.mn.x, u.mn.y, u.mn.z, __uint_as_float(0u)));
   __stcg(w + 1, make_float4(u.mx.x, u.mx.y, u.mx.z, __uint_as_float(first)));
+}
+
+__device__ __forceinline__ uint32_t atom_exch_acq_rel(uint32_t* p, uint32_t v) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.gpu.global.exch.b32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
 }
 
 // Marks x and its ancestors up to the first node already marked this pass.
@@ -245,12 +322,13 @@ __device__ __forceinline__ void refit_climb(const ResolveArgs& a, uint32_t x) {
     const uint32_t up = a.parents[x];
     const uint32_t sib = sibling_of(x);
     const bool sib_marked = a.dirty[sib] == a.stamp;
+    Box sb = ldcg_box(&a.nodes[sib]);  // final unless the sibling is marked: loads overlap
     if (sib_marked) {
-      __threadfence();
-      if (atomicExch(&a.arrive[up], a.stamp) != a.stamp) return;  // the sibling's climb continues
-      __threadfence();
+      // release: this climb's box stores before the exchange; acquire: the
+      // sibling climb's stores before reading its box again
+      if (atom_exch_acq_rel(&a.arrive[up], a.stamp) != a.stamp) return;  // the sibling's climb continues
+      sb = ldcg_box(&a.nodes[sib]);
     }
-    const Box sb = ldcg_box(&a.nodes[sib]);
     box = (x & 1u) ? box_union(box, sb) : box_union(sb, box);
     stcg_inner(&a.nodes[up], box, left_sibling_of(x));
     x = up;
@@ -258,22 +336,147 @@ __device__ __forceinline__ void refit_climb(const ResolveArgs& a, uint32_t x) {
   set_status(a.status, ST_ITER_LIMIT);
 }
 
+// Steps 2-5 of k_resolve over the P listed proposals, by `nthreads` threads
+// numbered `t0`, with `sync` a barrier over exactly those threads.
+template <class Sync>
+__device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, uint32_t t0, uint32_t nthreads,
+                                             Sync sync, uint32_t* s_rem) {
+  // 2. rounds, one barrier each.  A proposal touching an accepted one is
+  //    rejected; one that owned all five nodes in the previous round's claims
+  //    is accepted; the rest claim their nodes (lowest key wins).  Claims of
+  //    round r live in owner array r % 3; a round resets array (r + 1) % 3 for
+  //    the nodes it claims, the array the next round claims in.  The lowest
+  //    unresolved proposal owns its nodes after claiming, so it is resolved
+  //    one round later: the loop ends.
+  uint32_t* remaining = a.ctr + 1;
+  uint32_t round = 0;
+  for (;; round++) {
+    const unsigned long long* prev = a.owner + (size_t)((round + 2) % 3) * a.n_nodes;
+    unsigned long long* cur = a.owner + (size_t)(round % 3) * a.n_nodes;
+    unsigned long long* nxt = a.owner + (size_t)((round + 1) % 3) * a.n_nodes;
+    if (t0 == 0) remaining[(round + 1) % 3] = 0;
+    if (threadIdx.x == 0) *s_rem = 0;
+    __syncthreads();
+    uint32_t rem = 0;
+    for (uint32_t j = t0; j < P; j += nthreads) {
+      if (a.state[j] != 0) continue;
+      const Conf cf = load_conf(&a.conf[j]);
+      bool hit = false;
+#pragma unroll
+      for (int q = 0; q < 5; q++) hit |= a.touched[cf.c[q]] == a.stamp;
+      if (hit) {
+        a.state[j] = 2;
+        continue;
+      }
+      if (round > 0) {
+        bool own = true;
+#pragma unroll
+        for (int q = 0; q < 5; q++) own &= __ldcg(&prev[cf.c[q]]) == cf.key;
+        if (own) {
+          a.state[j] = 1;
+#pragma unroll
+          for (int q = 0; q < 5; q++) a.touched[cf.c[q]] = a.stamp;
+          continue;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 5; q++) {
+        atomicMin(&cur[cf.c[q]], cf.key);
+        nxt[cf.c[q]] = ~0ull;
+      }
+      rem++;
+    }
+    if (rem) atomicAdd(s_rem, rem);
+    __syncthreads();
+    if (threadIdx.x == 0 && *s_rem) atomicAdd(&remaining[round % 3], *s_rem);
+    sync();
+    const uint32_t left = *(volatile uint32_t*)&remaining[round % 3];
+    if (left == 0) break;
+    if (round + 1 >= a.max_rounds) {
+      if (t0 == 0) set_status(a.status, ST_ITER_LIMIT);
+      break;
+    }
+  }
+  if (t0 == 0) a.ctr[4] = round + 1;
+
+  // 3. reinsert_node: moves the nodes and updates the parent links exactly as
+  //    the reference does.  Accepted proposals share no moved node, no child
+  //    of one and no parent link they read, so they run in parallel.
+  uint32_t applied = 0;
+  for (uint32_t j = t0; j < P; j += nthreads) {
+    if (a.state[j] != 1) continue;
+    const Reins r = a.reins[a.plist[j]];
+    const uint32_t sib = sibling_of(r.from);
+    const uint32_t parent = a.parents[r.from];
+    const Bvh2Node sib_node = ld_node(&a.nodes[sib]);
+    const Bvh2Node dst = ld_node(&a.nodes[r.to]);
+    Bvh2Node inner = dst;
+    inner.a.w = __uint_as_float(0u);
+    inner.b.w = __uint_as_float(left_sibling_of(r.from));
+    st_node(&a.nodes[r.to], inner);
+    st_node(&a.nodes[sib], dst);
+    st_node(&a.nodes[parent], sib_node);
+    if (node_prims(dst) == 0) {
+      a.parents[node_first(dst)] = sib;
+      a.parents[node_first(dst) + 1] = sib;
+    }
+    if (node_prims(sib_node) == 0) {
+      a.parents[node_first(sib_node)] = parent;
+      a.parents[node_first(sib_node) + 1] = parent;
+    }
+    a.parents[sib] = r.to;
+    a.parents[r.from] = r.to;
+    a.starts[j] = make_uint2(r.to, parent);
+    applied++;
+  }
+  if (applied) atomicAdd(a.applied, applied);
+  sync();
+
+  // 4. mark, one thread per start node (two per accepted proposal: `to`,
+  //    and the parent of the old parent of `from`); a start node this thread
+  //    marked first stays in `starts` as one to refit from
+  uint32_t* start_slots = reinterpret_cast<uint32_t*>(a.starts);
+  for (uint32_t i = t0; i < 2 * P; i += nthreads) {
+    const uint32_t j = i >> 1;
+    if (a.state[j] != 1) continue;
+    uint32_t x = start_slots[i];
+    if (i & 1u) x = x != 0 ? a.parents[x] : OBVHS_INVALID;
+    start_slots[i] = (x != OBVHS_INVALID && mark_path(a, x)) ? x : OBVHS_INVALID;
+  }
+  sync();
+
+  // 5. refit from the marked nodes that have no marked children
+  for (uint32_t i = t0; i < 2 * P; i += nthreads) {
+    if (a.state[i >> 1] != 1) continue;
+    const uint32_t x = start_slots[i];
+    if (x == OBVHS_INVALID) continue;
+    const Bvh2Node xn = ld_node(&a.nodes[x]);
+    if (node_prims(xn) == 0) {
+      const uint32_t f = node_first(xn);
+      if (a.dirty[f] == a.stamp || a.dirty[f + 1] == a.stamp) continue;  // a child's climb reaches x
+    }
+    refit_climb(a, x);
+  }
+}
+
 // Everything after find_reinsertion for one pass, in one cooperative launch:
 //   1. list the proposals with area_diff > 0 and gather their conflict sets
-//   2. greedy conflict resolution in priority order (rounds, below)
+//   2. greedy conflict resolution in priority order (rounds)
 //   3. reinsert_node for every accepted proposal (src/bvh2/reinsertion.rs:336-382)
 //   4. mark the nodes whose boxes may change: `to` and its ancestors, and the
 //      ancestors of the old parent of `from`
 //   5. refit the marked nodes bottom-up, starting from marked nodes without
 //      marked children.
-__global__ void __launch_bounds__(BLK) k_resolve(ResolveArgs a) {
+// After step 1, a pass with at most RESOLVE_SMALL proposals continues in
+// block 0 alone (block barriers instead of grid barriers); the other blocks
+// return and take no further part in any barrier.
+__global__ void __launch_bounds__(RESOLVE_THREADS) k_resolve(ResolveArgs a) {
   cg::grid_group grid = cg::this_grid();
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   __shared__ uint32_t s_rem;
-  unsigned long long* owner0 = a.owner;
-  unsigned long long* owner1 = a.owner + a.n_nodes;
+  unsigned long long* owner0 = a.owner;  // round 0 claims
 
   // 1. proposals with a gain (warp-aggregated append), their conflict sets,
   //    and the round-0 claim words reset
@@ -306,127 +509,11 @@ __global__ void __launch_bounds__(BLK) k_resolve(ResolveArgs a) {
   }
   grid.sync();
   const uint32_t P = *(volatile uint32_t*)&a.ctr[0];
-
-  // 2. rounds: proposals touching an accepted one are rejected, the rest
-  //    claim their nodes (lowest key wins) and reset the other parity's
-  //    claim words for the next round; the owners of all five nodes are
-  //    accepted.  The lowest unresolved proposal always wins, so every round
-  //    resolves at least one.
-  uint32_t* remaining = a.ctr + 1;
-  uint32_t round = 0;
-  for (;; round++) {
-    unsigned long long* own_now = (round & 1u) ? owner1 : owner0;
-    unsigned long long* own_next = (round & 1u) ? owner0 : owner1;
-    if (t0 == 0) remaining[(round + 1) % 3] = 0;
-    for (uint32_t j = t0; j < P; j += stride)
-      if (a.state[j] == 0) {
-        const Conf cf = load_conf(&a.conf[j]);
-        bool hit = false;
-#pragma unroll
-        for (int q = 0; q < 5; q++) hit |= a.touched[cf.c[q]] == a.stamp;
-        if (hit) {
-          a.state[j] = 2;
-        } else {
-#pragma unroll
-          for (int q = 0; q < 5; q++) {
-            atomicMin(&own_now[cf.c[q]], cf.key);
-            own_next[cf.c[q]] = ~0ull;
-          }
-        }
-      }
-    grid.sync();
-    if (threadIdx.x == 0) s_rem = 0;
-    __syncthreads();
-    uint32_t rem = 0;
-    for (uint32_t j = t0; j < P; j += stride)
-      if (a.state[j] == 0) {
-        const Conf cf = load_conf(&a.conf[j]);
-        bool own = true;
-#pragma unroll
-        for (int q = 0; q < 5; q++) own &= __ldcg(&own_now[cf.c[q]]) == cf.key;
-        if (own) {
-          a.state[j] = 1;
-#pragma unroll
-          for (int q = 0; q < 5; q++) a.touched[cf.c[q]] = a.stamp;
-        } else {
-          rem++;
-        }
-      }
-    if (rem) atomicAdd(&s_rem, rem);
-    __syncthreads();
-    if (threadIdx.x == 0 && s_rem) atomicAdd(&remaining[round % 3], s_rem);
-    grid.sync();
-    const uint32_t left = *(volatile uint32_t*)&remaining[round % 3];
-    if (left == 0) break;
-    if (round + 1 >= a.max_rounds) {
-      if (t0 == 0) set_status(a.status, ST_ITER_LIMIT);
-      break;
-    }
-  }
-  if (t0 == 0) a.ctr[4] = round + 1;
-
-  // 3. reinsert_node: moves the nodes and updates the parent links exactly as
-  //    the reference does.  Accepted proposals share no moved node, no child
-  //    of one and no parent link they read, so they run in parallel.
-  uint32_t applied = 0;
-  for (uint32_t j = t0; j < P; j += stride) {
-    if (a.state[j] != 1) continue;
-    const Reins r = a.reins[a.plist[j]];
-    const uint32_t sib = sibling_of(r.from);
-    const uint32_t parent = a.parents[r.from];
-    const Bvh2Node sib_node = ld_node(&a.nodes[sib]);
-    const Bvh2Node dst = ld_node(&a.nodes[r.to]);
-    Bvh2Node inner = dst;
-    inner.a.w = __uint_as_float(0u);
-    inner.b.w = __uint_as_float(left_sibling_of(r.from));
-    st_node(&a.nodes[r.to], inner);
-    st_node(&a.nodes[sib], dst);
-    st_node(&a.nodes[parent], sib_node);
-    if (node_prims(dst) == 0) {
-      a.parents[node_first(dst)] = sib;
-      a.parents[node_first(dst) + 1] = sib;
-    }
-    if (node_prims(sib_node) == 0) {
-      a.parents[node_first(sib_node)] = parent;
-      a.parents[node_first(sib_node) + 1] = parent;
-    }
-    a.parents[sib] = r.to;
-    a.parents[r.from] = r.to;
-    a.starts[j] = make_uint2(r.to, parent);
-    applied++;
-  }
-  if (applied) atomicAdd(a.applied, applied);
-  grid.sync();
-
-  // 4. mark; a start node newly marked by this proposal is its to refit
-  for (uint32_t j = t0; j < P; j += stride) {
-    if (a.state[j] != 1) continue;
-    const uint2 st = a.starts[j];
-    uint2 own = make_uint2(OBVHS_INVALID, OBVHS_INVALID);
-    if (mark_path(a, st.x)) own.x = st.x;
-    if (st.y != 0) {
-      const uint32_t pp = a.parents[st.y];
-      if (mark_path(a, pp)) own.y = pp;
-    }
-    a.starts[j] = own;
-  }
-  grid.sync();
-
-  // 5. refit from the marked nodes that have no marked children
-  for (uint32_t j = t0; j < P; j += stride) {
-    if (a.state[j] != 1) continue;
-    const uint2 st = a.starts[j];
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const uint32_t x = h ? st.y : st.x;
-      if (x == OBVHS_INVALID) continue;
-      const Bvh2Node xn = ld_node(&a.nodes[x]);
-      if (node_prims(xn) == 0) {
-        const uint32_t f = node_first(xn);
-        if (a.dirty[f] == a.stamp || a.dirty[f + 1] == a.stamp) continue;  // a child's climb reaches x
-      }
-      refit_climb(a, x);
-    }
+  if (P <= RESOLVE_SMALL) {
+    if (blockIdx.x != 0) return;
+    resolve_body(a, P, threadIdx.x, blockDim.x, [] { __syncthreads(); }, &s_rem);
+  } else {
+    resolve_body(a, P, t0, stride, [&] { grid.sync(); }, &s_rem);
   }
 }
 
@@ -461,7 +548,7 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
   uint32_t* arrive = (uint32_t*)s.get(SLOT_ARRIVE, (size_t)len * 4);
   uint2* starts = (uint2*)s.get(SLOT_STARTS, (size_t)len * 8);
   uint32_t* touched = (uint32_t*)s.get(SLOT_TOUCHED, (size_t)len * 4);
-  unsigned long long* owner = (unsigned long long*)s.get(SLOT_MIS_OWNER, (size_t)len * 16);
+  unsigned long long* owner = (unsigned long long*)s.get(SLOT_MIS_OWNER, (size_t)len * 24);
   Conf* conf = (Conf*)s.get(SLOT_CONF, (size_t)len * sizeof(Conf));
   uint32_t* keys = (uint32_t*)s.get(SLOT_REINS_KEYS, (size_t)len * 4);
   uint32_t* vals = (uint32_t*)s.get(SLOT_REINS_VALS, (size_t)len * 4);
@@ -485,10 +572,16 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
   CK(cudaMemsetAsync(arrive, 0, (size_t)len * 4, c.stream));
   CK(cudaMemsetAsync(touched, 0, (size_t)len * 4, c.stream));
 
+  static int find_blocks = 0;
+  if (!find_blocks) {
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_find_persistent<192, true>, FIND_THREADS, 0));
+    find_blocks = std::max(1, per_sm) * c.num_sms;
+  }
   static int resolve_blocks = 0;
   if (!resolve_blocks) {
     int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resolve, BLK, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resolve, RESOLVE_THREADS, 0));
     resolve_blocks = std::max(1, per_sm) * c.num_sms;
   }
   const bool clamp = (size_t)b->max_depth * 2 <= 192;
@@ -511,19 +604,30 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
     if (e) return c.cuda_fail(e, "candidate sort");
     const uint32_t* cand = alt ? vals_alt : vals;
     // find_reinsertion for the first `count` candidates
-    if (clamp)
-      KLAUNCH("k_find", k_find<192, true><<<div_up<uint32_t>(count, 128), 128, 0, c.stream>>>(b->nodes, parents, cand, count, cap_rt,
-                                                                              reins, c.d_status));
-    else
-      KLAUNCH("k_find", k_find<1024, false><<<div_up<uint32_t>(count, 128), 128, 0, c.stream>>>(b->nodes, parents, cand, count, cap_rt,
-                                                                                reins, c.d_status));
+    uint32_t* pass_ctr = counters + 8 + (size_t)ri * 8;  // [5]: next candidate for k_find
+    const uint32_t fblocks = div_up<uint32_t>(count, FIND_THREADS);
+    if (fblocks > (uint32_t)find_blocks) {
+      if (clamp)
+        KLAUNCH("k_find", k_find_persistent<192, true><<<find_blocks, FIND_THREADS, 0, c.stream>>>(
+                              b->nodes, parents, cand, count, cap_rt, reins, pass_ctr + 5, c.d_status));
+      else
+        KLAUNCH("k_find", k_find_persistent<1024, false><<<find_blocks, FIND_THREADS, 0, c.stream>>>(
+                              b->nodes, parents, cand, count, cap_rt, reins, pass_ctr + 5, c.d_status));
+    } else if (clamp) {
+      KLAUNCH("k_find", k_find<192, true><<<fblocks, FIND_THREADS, 0, c.stream>>>(b->nodes, parents, cand, count, cap_rt,
+                                                                             reins, c.d_status));
+    } else {
+      KLAUNCH("k_find", k_find<1024, false><<<fblocks, FIND_THREADS, 0, c.stream>>>(b->nodes, parents, cand, count,
+                                                                               cap_rt, reins, c.d_status));
+    }
     CK(cudaGetLastError());
     // conflict resolution, moves and refit in one cooperative launch
     ResolveArgs ra{b->nodes, parents, reins, count, plist, conf, state, owner, touched, dirty, arrive, starts,
-                   counters + 8 + (size_t)ri * 8, counters + 1, c.d_status, ri + 1, len, count + 2};
+                   counters + 8 + (size_t)ri * 8, counters + 1, c.d_status, ri + 1, len, count + 3};
     void* args[] = {&ra};
-    uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)resolve_blocks, std::max<uint64_t>(1, div_up<uint32_t>(count, BLK)));
-    KLAUNCH("k_resolve", CK(cudaLaunchCooperativeKernel((void*)k_resolve, grid, BLK, args, 0, c.stream)));
+    uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)resolve_blocks,
+                                                 std::max<uint64_t>(1, div_up<uint32_t>(count, RESOLVE_THREADS)));
+    KLAUNCH("k_resolve", CK(cudaLaunchCooperativeKernel((void*)k_resolve, grid, RESOLVE_THREADS, args, 0, c.stream)));
     CK(cudaGetLastError());
   }
   uint32_t applied = 0;
