@@ -60,6 +60,15 @@ __device__ __forceinline__ Bvh2Node ld_node(const Bvh2Node* p) {
   n.b = q[1];
   return n;
 }
+// Through L2 (ld.cg): for nodes another block may have written earlier in
+// the same kernel, so no stale L1 line can be returned.
+__device__ __forceinline__ Bvh2Node ld_node_cg(const Bvh2Node* p) {
+  Bvh2Node n;
+  const float4* q = reinterpret_cast<const float4*>(p);
+  n.a = __ldcg(q);
+  n.b = __ldcg(q + 1);
+  return n;
+}
 __device__ __forceinline__ void st_node(Bvh2Node* p, const Bvh2Node& n) {
   float4* q = reinterpret_cast<float4*>(p);
   q[0] = n.a;

@@ -14,11 +14,15 @@
 // merge, whose children land at insert_base - 2(k+1).  The result is the
 // reference's tree bit for bit, given the same sorted leaves.
 //
-// Each pass is one launch (k_ploc_pass) while many clusters are live; once
-// at most TAIL_MAX remain, one CTA finishes every remaining pass with the
-// clusters held in shared memory.
+// While more than TAIL_MAX clusters are live, all passes run in one
+// cooperative launch (k_ploc_coop) separated by grid barriers; then one CTA
+// finishes every remaining pass with the clusters held in shared memory.
+#include <cooperative_groups.h>
+
 #include "build.h"
 #include "radix_sort.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -201,215 +205,267 @@ __global__ void __launch_bounds__(BLK) k_gather(const Bvh2Node* __restrict__ in,
 // (the SearchCache stores union(A_lo, A_hi), src/ploc/mod.rs:612-619).
 __device__ __forceinline__ float pair_cost(const Box& lo, const Box& hi) { return half_area(box_union(lo, hi)); }
 
+__device__ __forceinline__ Box load_box_cg(const Bvh2Node* p) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+  const float4 a = __ldcg(q), b = __ldcg(q + 1);
+  return Box{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)};
+}
+
 __device__ __forceinline__ Box load_box(const Bvh2Node* p) {
   const float4* q = reinterpret_cast<const float4*>(p);
   float4 a = q[0], b = q[1];
   return Box{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)};
 }
 
-// --- one fused kernel per pass ---------------------------------------------
-//
-// A tile of PCHUNK clusters computes the merge offsets of its clusters and of
-// a +-radius halo (from boxes staged with a 2*radius halo), derives the emit
-// and merge flags, scans them inside the CTA and gets its output offsets by
-// decoupled look-back over earlier tiles, then writes next_nodes and the
-// merged pairs.  The tile holding the last cluster stores the next count and
-// insert index.  Tiles are claimed in launch order; waits are bounded.
 constexpr int PT = 256;
 constexpr int PITEMS = 4;
 constexpr int PCHUNK = PT * PITEMS;
-constexpr unsigned long long LB_AGG = 1ull << 62, LB_INC = 2ull << 62;
-constexpr unsigned long long LB_VAL = (1ull << 31) - 1;
+constexpr int BOXS = PCHUNK + 4 * 32;  // staged boxes per tile: the tile and a 2 * radius halo each side
 
-__global__ void __launch_bounds__(PT) k_ploc_pass(const Bvh2Node* __restrict__ cur, Bvh2Node* __restrict__ next,
-                                                  Bvh2Node* __restrict__ out, PlocState* st, int parity, int radius,
-                                                  int d1, unsigned long long* lb, uint32_t* lb_next, uint32_t lb_words,
-                                                  uint32_t* status) {
-  __shared__ float s_box[(PCHUNK + 4 * 32) * 6];
-  __shared__ int8_t s_merge[PCHUNK + 2 * 32];
-  __shared__ uint32_t s_tile, s_w[PT / 32];
-  __shared__ unsigned long long s_prefix;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // clear the look-back area of the next pass (the previous pass used it)
-  for (uint32_t k = blockIdx.x * PT + tid; k < lb_words; k += gridDim.x * PT) lb_next[k] = 0;
-  const uint32_t count = st->count[parity];
-  if (count <= 1) {
-    // a pass after the root formed: carry the root and the state forward
-    if (blockIdx.x == 0 && tid == 0) {
-      if (count == 1) st_node(&next[0], ld_node(&cur[0]));
-      st->count[parity ^ 1] = count;
-      st->insert[parity ^ 1] = st->insert[parity];
+// --- all large passes in one cooperative launch ------------------------------
+//
+// Passes run back to back with grid barriers instead of launches.  One block
+// of COOP_GROUPS x PT threads per SM (its registers fill the SM); each group
+// of PT threads works on its own tiles with its own shared memory and named
+// barrier, and tile t goes to block t % G, so consecutive tiles land on
+// different SMs.  A tile holds PT * ipt clusters, ipt = 4, 2 or 1 chosen per
+// pass so that small passes still spread over the GPU.  Per pass:
+//   A  each tile computes the merge offsets of its clusters from boxes staged
+//      with a 2*radius halo (offsets of the +-radius neighbours are recomputed
+//      locally, so the emit/merge flags need no exchange), stores its offsets
+//      and its (emitted, merged) counts;
+//   B  after a grid barrier, each tile's output offsets are the counts of the
+//      tiles before it (a group reduction) plus a scan inside the tile; the
+//      tile writes next_nodes and the merged pairs, and the last tile stores
+//      the next count and insert index.
+// The loop ends once at most TAIL_MAX clusters are live; the single-CTA tail
+// kernel finishes.  Cluster buffers alternate by pass parity (passes & 1).
+constexpr int COOP_GROUPS = 4;
+
+struct PlocCoopArgs {
+  Bvh2Node* buf[2];
+  Bvh2Node* out;
+  PlocState* st;
+  int8_t* merge;   // per cluster: offset to its best neighbour (this pass)
+  uint2* tile_cnt; // per tile: (emitted, merged)
+  int radius;
+  uint32_t depth_threshold;
+  uint32_t max_passes;
+  uint32_t* status;
+};
+
+struct CoopGroupSmem {
+  float box[6 * BOXS];  // structure of arrays: min x, y, z, max x, y, z
+  int8_t merge[PCHUNK + 2 * 32];
+  uint32_t w[PT / 32];
+  uint32_t red[2][PT / 32];
+};
+
+__device__ __forceinline__ void group_sync(int group) {
+  asm volatile("bar.sync %0, %1;" ::"r"(1 + group), "r"(PT) : "memory");
+}
+
+__global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs a) {
+  cg::grid_group grid = cg::this_grid();
+  extern __shared__ __align__(16) unsigned char coop_smem[];
+  const int group = threadIdx.x / PT;
+  CoopGroupSmem& sm = reinterpret_cast<CoopGroupSmem*>(coop_smem)[group];
+  const int tid = threadIdx.x % PT, lane = tid & 31, warp = tid >> 5;
+  const uint32_t G = gridDim.x;
+  const uint32_t first_tile = blockIdx.x + G * (uint32_t)group, tile_step = G * COOP_GROUPS;
+  for (uint32_t iter = 0;; iter++) {
+    const uint32_t pass = *(volatile uint32_t*)&a.st->passes;
+    const int parity = (int)(pass & 1u);
+    const uint32_t count = *(volatile uint32_t*)&a.st->count[parity];
+    if (count <= TAIL_MAX) break;
+    if (iter >= a.max_passes) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) set_status(a.status, ST_ITER_LIMIT);
+      break;
     }
-    return;
-  }
-  uint32_t* counter = reinterpret_cast<uint32_t*>(lb);
-  unsigned long long* tstat = lb + 1;
-  if (tid == 0) s_tile = atomicAdd(counter, 1u);
-  __syncthreads();
-  const uint32_t tile = s_tile;
-  const uint32_t base = tile * PCHUNK;
-  if (base >= count) return;
-  const int r = d1 ? 1 : radius;
-  const int64_t box_lo = (int64_t)base - 2 * r;
-  const uint32_t box_span = PCHUNK + 4 * r;
-  for (uint32_t k = tid; k < box_span; k += PT) {
-    const int64_t j = box_lo + k;
-    if (j >= 0 && j < (int64_t)count) {
-      const Box b = load_box(&cur[j]);
-      float* d = &s_box[k * 6];
-      d[0] = b.mn.x;
-      d[1] = b.mn.y;
-      d[2] = b.mn.z;
-      d[3] = b.mx.x;
-      d[4] = b.mx.y;
-      d[5] = b.mx.z;
-    }
-  }
-  __syncthreads();
-  auto box_at = [&](uint32_t j) {
-    const float* d = &s_box[((int64_t)j - box_lo) * 6];
-    return Box{make_float3(d[0], d[1], d[2]), make_float3(d[3], d[4], d[5])};
-  };
-  // merge offsets for [base - r, base + PCHUNK + r)
-  const int64_t m_lo = (int64_t)base - r;
-  const uint32_t m_span = PCHUNK + 2 * r;
-  for (uint32_t k = tid; k < m_span; k += PT) {
-    const int64_t jj = m_lo + k;
-    if (jj < 0 || jj >= (int64_t)count) continue;
-    const uint32_t i = (uint32_t)jj;
-    const Box me = box_at(i);
-    int8_t m;
-    if (d1) {
-      if (i == count - 1) {
-        m = -1;
-      } else {
-        const float c = pair_cost(me, box_at(i + 1));
-        const float last = i == 0 ? __int_as_float(0x7f800000) : pair_cost(box_at(i - 1), me);
-        m = last < c ? -1 : 1;
-      }
-    } else {
-      const uint32_t begin = i >= (uint32_t)r ? i - r : 0;
-      const uint32_t end = min(i + r + 1, count);
-      uint32_t best = i;
-      float best_cost = __int_as_float(0x7f800000);
-      for (uint32_t j = begin; j < i; j++) {
-        const float c = pair_cost(box_at(j), me);
-        if (c <= best_cost) {
-          best = j;
-          best_cost = c;
+    // no __restrict__ / read-only path: each buffer is written in one pass and
+    // read in the next; loads go through L2 (ld.cg) so no stale line is used
+    const Bvh2Node* cur = parity ? a.buf[1] : a.buf[0];
+    Bvh2Node* next = parity ? a.buf[0] : a.buf[1];
+    const int d1 = (a.radius == 1 || pass < a.depth_threshold) ? 1 : 0;
+    const int r = d1 ? 1 : a.radius;
+    const uint32_t groups = G * COOP_GROUPS;
+    const int ipt = count >= groups * (uint32_t)PCHUNK ? PITEMS : count >= groups * (uint32_t)(PT * 2) ? 2 : 1;
+    const uint32_t chunk = (uint32_t)PT * ipt;
+    const uint32_t ntiles = div_up<uint32_t>(count, chunk);
+
+    // A: merge offsets and tile counts
+    for (uint32_t tile = first_tile; tile < ntiles; tile += tile_step) {
+      const uint32_t base = tile * chunk;
+      const int64_t box_lo = (int64_t)base - 2 * r;
+      const uint32_t box_span = chunk + 4 * r;
+      group_sync(group);  // the previous tile's shared data is consumed
+      for (uint32_t k = tid; k < box_span; k += PT) {
+        const int64_t j = box_lo + k;
+        if (j >= 0 && j < (int64_t)count) {
+          const Box b = load_box_cg(&cur[j]);
+          sm.box[0 * BOXS + k] = b.mn.x;
+          sm.box[1 * BOXS + k] = b.mn.y;
+          sm.box[2 * BOXS + k] = b.mn.z;
+          sm.box[3 * BOXS + k] = b.mx.x;
+          sm.box[4 * BOXS + k] = b.mx.y;
+          sm.box[5 * BOXS + k] = b.mx.z;
         }
       }
-      for (uint32_t j = i + 1; j < end; j++) {
-        const float c = pair_cost(me, box_at(j));
-        if (c <= best_cost) {
-          best = j;
-          best_cost = c;
+      group_sync(group);
+      const int lo32 = (int)box_lo;
+#define PBOX(J)                                                                                              \
+  Box {                                                                                                      \
+    make_float3(sm.box[0 * BOXS + (J)-lo32], sm.box[1 * BOXS + (J)-lo32], sm.box[2 * BOXS + (J)-lo32]),      \
+        make_float3(sm.box[3 * BOXS + (J)-lo32], sm.box[4 * BOXS + (J)-lo32], sm.box[5 * BOXS + (J)-lo32]) \
+  }
+      const int64_t m_lo = (int64_t)base - r;
+      const uint32_t m_span = chunk + 2 * r;
+      for (uint32_t k = tid; k < m_span; k += PT) {
+        const int64_t jj = m_lo + k;
+        if (jj < 0 || jj >= (int64_t)count) continue;
+        const int i = (int)jj;
+        const Box me = PBOX(i);
+        int8_t m;
+        if (d1) {
+          if ((uint32_t)i == count - 1) {
+            m = -1;
+          } else {
+            const float c = pair_cost(me, PBOX(i + 1));
+            const float last = i == 0 ? __int_as_float(0x7f800000) : pair_cost(PBOX(i - 1), me);
+            m = last < c ? -1 : 1;
+          }
+        } else {
+          const int begin = i >= r ? i - r : 0;
+          const int end = min(i + r + 1, (int)count);
+          int best = i;
+          float best_cost = __int_as_float(0x7f800000);
+          for (int j = begin; j < i; j++) {
+            const float c = pair_cost(PBOX(j), me);
+            if (c <= best_cost) {
+              best = j;
+              best_cost = c;
+            }
+          }
+          for (int j = i + 1; j < end; j++) {
+            const float c = pair_cost(me, PBOX(j));
+            if (c <= best_cost) {
+              best = j;
+              best_cost = c;
+            }
+          }
+          m = (int8_t)(best - i);
+        }
+        sm.merge[k] = m;
+      }
+#undef PBOX
+      group_sync(group);
+      uint32_t packed = 0;
+#pragma unroll
+      for (int k = 0; k < PITEMS; k++) {
+        const uint32_t i = base + tid * ipt + k;
+        if (k < ipt && i < count) {
+          const int off = sm.merge[(int64_t)i - m_lo];
+          const uint32_t b = (uint32_t)((int)i + off);
+          const bool mutual = (int)b + (int)sm.merge[(int64_t)b - m_lo] == (int)i;
+          packed += ((!mutual || b < i) ? 1u : 0u) + ((mutual && b < i) ? (1u << 16) : 0u);
+          a.merge[i] = (int8_t)off;
         }
       }
-      m = (int8_t)((int)best - (int)i);
-    }
-    s_merge[k] = m;
-  }
-  __syncthreads();
-  // flags, packed (emit | merge << 16), CTA-wide exclusive scan
-  bool emit[PITEMS], ism[PITEMS];
-  uint32_t bst[PITEMS];
-  uint32_t packed = 0;
 #pragma unroll
-  for (int k = 0; k < PITEMS; k++) {
-    const uint32_t i = base + tid * PITEMS + k;
-    emit[k] = ism[k] = false;
-    bst[k] = i;
-    if (i < count) {
-      const int off = s_merge[(int64_t)i - m_lo];
-      const uint32_t b = (uint32_t)((int)i + off);
-      const bool mutual = (int)b + (int)s_merge[(int64_t)b - m_lo] == (int)i;
-      emit[k] = !mutual || b < i;
-      ism[k] = mutual && b < i;
-      bst[k] = b;
-    }
-    packed += (emit[k] ? 1u : 0u) + (ism[k] ? (1u << 16) : 0u);
-  }
-  uint32_t x = packed;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) s_w[warp] = x;
-  __syncthreads();
-  uint32_t wpre = 0, tot = 0;
-  for (int w = 0; w < PT / 32; w++) {
-    if (w < warp) wpre += s_w[w];
-    tot += s_w[w];
-  }
-  const uint32_t excl = wpre + x - packed;
-  // decoupled look-back on (emitted, merged) = (low 31 bits, next 31 bits):
-  // warp 0 reads 32 earlier tiles per step (lane l reads tile t - l; before
-  // tile 0 reads as an inclusive zero) and adds the nearest ones up to the
-  // first inclusive prefix
-  if (warp == 0) {
-    const unsigned long long agg = (unsigned long long)(tot & 0xffffu) | ((unsigned long long)(tot >> 16) << 31);
-    unsigned long long prefix = 0;
-    if (tile == 0) {
-      if (lane == 0) atomicExch(&tstat[0], LB_INC | agg);
-    } else {
-      if (lane == 0) atomicExch(&tstat[tile], LB_AGG | agg);
-      int64_t t = (int64_t)tile - 1;
-      uint32_t spins = 0;
-      for (;;) {
-        const int64_t idx = t - lane;
-        const unsigned long long v = idx >= 0 ? *((volatile unsigned long long*)&tstat[idx]) : (unsigned long long)LB_INC;
-        const uint32_t fl = (uint32_t)(v >> 62);
-        const uint32_t inc = __ballot_sync(0xffffffffu, fl == 2u);
-        const uint32_t not_ready = __ballot_sync(0xffffffffu, fl == 0u);
-        // lanes needed: up to and including the nearest inclusive one
-        const uint32_t need = inc ? (((inc & (0u - inc)) << 1) - 1u) : 0xffffffffu;
-        uint32_t take = need;
-        if (not_ready & need) take = ((not_ready & (0u - not_ready)) - 1u);  // the ready lanes before it
-        unsigned long long part = ((take >> lane) & 1u) ? (v & ((1ull << 62) - 1)) : 0ull;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-        prefix += part;
-        if (take == need && inc) break;
-        t -= __popc(take);
-        if (take == 0 && ++spins > (1u << 24)) {
-          if (lane == 0) atomicOr(status, ST_ITER_LIMIT);
-          break;
-        }
+      for (int o = 16; o > 0; o >>= 1) packed += __shfl_xor_sync(0xffffffffu, packed, o);
+      if (lane == 0) sm.w[warp] = packed;
+      group_sync(group);
+      if (tid == 0) {
+        uint32_t tot = 0;
+        for (int w = 0; w < PT / 32; w++) tot += sm.w[w];
+        a.tile_cnt[tile] = make_uint2(tot & 0xffffu, tot >> 16);
       }
-      if (lane == 0) atomicExch(&tstat[tile], LB_INC | (prefix + agg));
     }
-    if (lane == 0) s_prefix = prefix;
-  }
-  __syncthreads();
-  const unsigned long long pre = s_prefix;
-  const uint32_t pre_e = (uint32_t)(pre & LB_VAL), pre_m = (uint32_t)((pre >> 31) & LB_VAL);
-  const uint32_t ins_top = st->insert[parity];
-  uint32_t epos = pre_e + (excl & 0xffffu), mpos = pre_m + (excl >> 16);
+    grid.sync();
+
+    // B: offsets and writes
+    const uint32_t ins_top = *(volatile uint32_t*)&a.st->insert[parity];
+    for (uint32_t tile = first_tile; tile < ntiles; tile += tile_step) {
+      const uint32_t base = tile * chunk;
+      // counts of the tiles before this one
+      uint32_t pe = 0, pm = 0;
+      for (uint32_t t = tid; t < tile; t += PT) {
+        const uint2 v = __ldcg(&a.tile_cnt[t]);
+        pe += v.x;
+        pm += v.y;
+      }
 #pragma unroll
-  for (int k = 0; k < PITEMS; k++) {
-    const uint32_t i = base + tid * PITEMS + k;
-    if (!emit[k]) continue;
-    if (ism[k]) {
-      const Bvh2Node left = ld_node(&cur[i]);
-      const Bvh2Node right = ld_node(&cur[bst[k]]);
-      const uint32_t ins = ins_top - 2 * (mpos + 1);
-      st_node(&out[ins], left);
-      st_node(&out[ins + 1], right);
-      st_node(&next[epos], make_node(box_union(node_box(left), node_box(right)), 0, ins));
-      mpos++;
-    } else {
-      st_node(&next[epos], ld_node(&cur[i]));
+      for (int o = 16; o > 0; o >>= 1) {
+        pe += __shfl_xor_sync(0xffffffffu, pe, o);
+        pm += __shfl_xor_sync(0xffffffffu, pm, o);
+      }
+      group_sync(group);  // red / w of the previous tile are consumed
+      if (lane == 0) {
+        sm.red[0][warp] = pe;
+        sm.red[1][warp] = pm;
+      }
+      // flags from the stored offsets, group-wide exclusive scan
+      bool emit[PITEMS], ism[PITEMS];
+      uint32_t bst[PITEMS];
+      uint32_t packed = 0;
+#pragma unroll
+      for (int k = 0; k < PITEMS; k++) {
+        const uint32_t i = base + tid * ipt + k;
+        emit[k] = ism[k] = false;
+        bst[k] = i;
+        if (k < ipt && i < count) {
+          const int off = __ldcg(&a.merge[i]);
+          const uint32_t b = (uint32_t)((int)i + off);
+          const bool mutual = (int)b + (int)__ldcg(&a.merge[b]) == (int)i;
+          emit[k] = !mutual || b < i;
+          ism[k] = mutual && b < i;
+          bst[k] = b;
+        }
+        packed += (emit[k] ? 1u : 0u) + (ism[k] ? (1u << 16) : 0u);
+      }
+      uint32_t x = packed;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      if (lane == 31) sm.w[warp] = x;
+      group_sync(group);
+      uint32_t wpre = 0, tot = 0, pre_e = 0, pre_m = 0;
+      for (int w = 0; w < PT / 32; w++) {
+        if (w < warp) wpre += sm.w[w];
+        tot += sm.w[w];
+        pre_e += sm.red[0][w];
+        pre_m += sm.red[1][w];
+      }
+      const uint32_t excl = wpre + x - packed;
+      uint32_t epos = pre_e + (excl & 0xffffu), mpos = pre_m + (excl >> 16);
+#pragma unroll
+      for (int k = 0; k < PITEMS; k++) {
+        const uint32_t i = base + tid * ipt + k;
+        if (!emit[k]) continue;
+        if (ism[k]) {
+          const Bvh2Node left = ld_node_cg(&cur[i]);
+          const Bvh2Node right = ld_node_cg(&cur[bst[k]]);
+          const uint32_t ins = ins_top - 2 * (mpos + 1);
+          st_node(&a.out[ins], left);
+          st_node(&a.out[ins + 1], right);
+          st_node(&next[epos], make_node(box_union(node_box(left), node_box(right)), 0, ins));
+          mpos++;
+        } else {
+          st_node(&next[epos], ld_node_cg(&cur[i]));
+        }
+        epos++;
+      }
+      if (tid == 0 && tile == ntiles - 1) {
+        a.st->count[parity ^ 1] = pre_e + (tot & 0xffffu);
+        a.st->insert[parity ^ 1] = ins_top - 2 * (pre_m + (tot >> 16));
+        a.st->sum_counts += count;
+        __threadfence();
+        a.st->passes = pass + 1;
+      }
     }
-    epos++;
-  }
-  // the tile holding the last cluster publishes the next pass's state
-  if (tid == 0 && base + PCHUNK >= count) {
-    st->count[parity ^ 1] = pre_e + (tot & 0xffffu);
-    st->insert[parity ^ 1] = ins_top - 2 * (pre_m + (tot >> 16));
-    st->passes += 1;
-    st->sum_counts += count;
+    grid.sync();
   }
 }
 
@@ -423,7 +479,9 @@ __device__ __forceinline__ Box sbox(const float4* s, uint32_t j) {
 }
 
 // Finishes every remaining pass (count <= TAIL_MAX) inside one CTA.
-__global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __restrict__ cur_g, PlocState* st, int parity,
+// The live clusters are in buf[passes & 1].
+__global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __restrict__ buf0,
+                                                            const Bvh2Node* __restrict__ buf1, PlocState* st,
                                                             int radius, uint32_t depth_threshold, uint32_t max_passes,
                                                             Bvh2Node* __restrict__ out, uint32_t* status) {
   extern __shared__ float4 smem[];
@@ -434,11 +492,13 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
   __shared__ uint32_t s_count, s_insert, s_pass;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) {
-    s_count = st->count[parity];
-    s_insert = st->insert[parity];
     s_pass = st->passes;
+    s_count = st->count[s_pass & 1u];
+    s_insert = st->insert[s_pass & 1u];
   }
   __syncthreads();
+  const int parity = (int)(s_pass & 1u);
+  const Bvh2Node* __restrict__ cur_g = parity ? buf1 : buf0;
   uint32_t count = s_count;
   for (uint32_t j = tid; j < count; j += TAIL_THREADS) {
     const float4* q = reinterpret_cast<const float4*>(&cur_g[j]);
@@ -584,7 +644,6 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
   }
 }
 
-__global__ void k_root_copy(const Bvh2Node* cur, Bvh2Node* out) { st_node(&out[0], ld_node(&cur[0])); }
 
 }  // namespace
 
@@ -654,56 +713,36 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   if (r) return r;
   Bvh2Node* cur = (Bvh2Node*)s.get(SLOT_PLOC_A, (size_t)n * sizeof(Bvh2Node));
   Bvh2Node* nxt = (Bvh2Node*)s.get(SLOT_PLOC_B, (size_t)n * sizeof(Bvh2Node));
-  // look-back areas of two consecutive passes: [counter word pair, tile words]
-  const uint32_t lb_words = 2 * (div_up<uint32_t>(n, PCHUNK) + 2);  // 32-bit words per area
-  uint32_t* lb_area = (uint32_t*)s.get(SLOT_PARTIAL, (size_t)lb_words * 2 * 4 + 64);
+  int8_t* merge = (int8_t*)s.get(SLOT_MERGE, (size_t)n);
+  uint2* tile_cnt = (uint2*)s.get(SLOT_PARTIAL, (size_t)div_up<uint32_t>(n, PT) * sizeof(uint2));
   PlocState* st = (PlocState*)s.get(SLOT_PLOC_STATE, sizeof(PlocState));
-  if (!cur || !nxt || !lb_area || !st) return c.fail(OBVHS_ERR_OOM, "scratch");
-  CK(cudaMemsetAsync(lb_area, 0, (size_t)lb_words * 2 * 4, c.stream));
+  if (!cur || !nxt || !merge || !tile_cnt || !st) return c.fail(OBVHS_ERR_OOM, "scratch");
   uint32_t g = div_up<uint32_t>(n, BLK);
   KLAUNCH("k_gather", k_gather<<<g, BLK, 0, c.stream>>>(leaves, order, n, cur));
-  PlocState h0{};
-  h0.count[0] = n;
-  h0.insert[0] = 2 * n - 1;
-  CK(cudaMemcpyAsync(st, &h0, sizeof(PlocState), cudaMemcpyHostToDevice, c.stream));
-  if (n == 1) {
-    KLAUNCH("k_root_copy", k_root_copy<<<1, 1, 0, c.stream>>>(cur, out_nodes));
-    CK(cudaGetLastError());
-    return 0;
-  }
-  // multi-block passes while many clusters are live
-  int parity = 0;
-  uint32_t known = n;  // host-side upper bound on the live count
-  uint32_t pass = 0;
+  PlocState* h0 = reinterpret_cast<PlocState*>(static_cast<char*>(c.h_small) + 1024);  // pinned, asynchronous copy
+  *h0 = PlocState{};
+  h0->count[0] = n;
+  h0->insert[0] = 2 * n - 1;
+  CK(cudaMemcpyAsync(st, h0, sizeof(PlocState), cudaMemcpyHostToDevice, c.stream));
   const uint32_t max_passes = 2 * n + 64;
-  while (known > TAIL_MAX) {
-    const int batch = 4;
-    for (int b = 0; b < batch; b++) {
-      const int d1 = (radius == 1 || pass < depth_threshold) ? 1 : 0;
-      const uint32_t tiles = div_up<uint32_t>(known, PCHUNK);
-      unsigned long long* lb_cur = reinterpret_cast<unsigned long long*>(lb_area + (size_t)(parity)*lb_words);
-      uint32_t* lb_nxt = lb_area + (size_t)(parity ^ 1) * lb_words;
-      KLAUNCH("k_ploc_pass", k_ploc_pass<<<tiles, PT, 0, c.stream>>>(cur, nxt, out_nodes, st, parity, (int)radius, d1,
-                                                                      lb_cur, lb_nxt, lb_words, c.d_status));
-      std::swap(cur, nxt);
-      parity ^= 1;
-      pass++;
+  if (n > TAIL_MAX) {
+    const size_t smem = COOP_GROUPS * sizeof(CoopGroupSmem);
+    static int coop_blocks = 0;
+    if (!coop_blocks) {
+      CK(cudaFuncSetAttribute(k_ploc_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      int per_sm = 0;
+      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ploc_coop, COOP_GROUPS * PT, smem));
+      coop_blocks = std::max(1, per_sm) * c.num_sms;
     }
-    CK(cudaGetLastError());
-    PlocState h;
-    CK(cudaMemcpyAsync(&h, st, sizeof(PlocState), cudaMemcpyDeviceToHost, c.stream));
-    CK(cudaStreamSynchronize(c.stream));
-    known = h.count[parity];
-    pass = h.passes;
-    if (pass > max_passes) return c.fail(OBVHS_ERR_LIMIT, "PLOC pass limit");
+    PlocCoopArgs pa{{cur, nxt}, out_nodes, st, merge, tile_cnt, (int)radius, depth_threshold, max_passes, c.d_status};
+    void* args[] = {&pa};
+    KLAUNCH("k_ploc_coop", CK(cudaLaunchCooperativeKernel((void*)k_ploc_coop, coop_blocks, COOP_GROUPS * PT, args, smem,
+                                                          c.stream)));
   }
-  if (known > 1) {
-    size_t smem = (size_t)4 * TAIL_MAX * sizeof(float4) + TAIL_MAX + 64;
-    KLAUNCH("k_ploc_tail", k_ploc_tail<<<1, TAIL_THREADS, smem, c.stream>>>(cur, st, parity, (int)radius, depth_threshold, max_passes,
-                                                     out_nodes, c.d_status));
-    CK(cudaGetLastError());
-  } else {
-    KLAUNCH("k_root_copy", k_root_copy<<<1, 1, 0, c.stream>>>(cur, out_nodes));
+  {
+    const size_t smem = (size_t)4 * TAIL_MAX * sizeof(float4) + TAIL_MAX + 64;
+    KLAUNCH("k_ploc_tail", k_ploc_tail<<<1, TAIL_THREADS, smem, c.stream>>>(cur, nxt, st, (int)radius, depth_threshold,
+                                                                           max_passes, out_nodes, c.d_status));
     CK(cudaGetLastError());
   }
   PlocState h;

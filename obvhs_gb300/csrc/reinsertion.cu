@@ -294,7 +294,7 @@ __device__ __forceinline__ uint32_t atom_exch_acq_rel(uint32_t* p, uint32_t v) {
 __device__ __forceinline__ bool mark_path(const ResolveArgs& a, uint32_t x) {
   bool first = true, owned = false;
   for (uint32_t guard = 0; guard < a.n_nodes; guard++) {
-    const uint32_t up = a.parents[x];  // independent of the exchange: overlaps it
+    const uint32_t up = __ldcg(&a.parents[x]);  // independent of the exchange: overlaps it
     if (atomicExch(&a.dirty[x], a.stamp) == a.stamp) return owned;
     if (first) owned = true;
     first = false;
@@ -310,7 +310,7 @@ __device__ __forceinline__ bool mark_path(const ResolveArgs& a, uint32_t x) {
 // the second of the two climbs when both children are marked.  Unions are
 // taken first child, second child, as Bvh2::refit_from does.
 __device__ __forceinline__ void refit_climb(const ResolveArgs& a, uint32_t x) {
-  Bvh2Node xn = ld_node(&a.nodes[x]);
+  Bvh2Node xn = ld_node_cg(&a.nodes[x]);
   Box box = node_box(xn);
   if (node_prims(xn) == 0) {
     const uint32_t f = node_first(xn);
@@ -319,9 +319,9 @@ __device__ __forceinline__ void refit_climb(const ResolveArgs& a, uint32_t x) {
   }
   for (uint32_t guard = 0; guard < a.n_nodes; guard++) {
     if (x == 0) return;
-    const uint32_t up = a.parents[x];
+    const uint32_t up = __ldcg(&a.parents[x]);
     const uint32_t sib = sibling_of(x);
-    const bool sib_marked = a.dirty[sib] == a.stamp;
+    const bool sib_marked = __ldcg(&a.dirty[sib]) == a.stamp;
     Box sb = ldcg_box(&a.nodes[sib]);  // final unless the sibling is marked: loads overlap
     if (sib_marked) {
       // release: this climb's box stores before the exchange; acquire: the
@@ -337,7 +337,9 @@ __device__ __forceinline__ void refit_climb(const ResolveArgs& a, uint32_t x) {
 }
 
 // Steps 2-5 of k_resolve over the P listed proposals, by `nthreads` threads
-// numbered `t0`, with `sync` a barrier over exactly those threads.
+// numbered `t0`, with `sync` a barrier over exactly those threads.  Words that
+// other blocks write earlier in the same launch (parents, nodes, touched,
+// dirty) are read through L2 (ld.cg) so no stale L1 line is used.
 template <class Sync>
 __device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, uint32_t t0, uint32_t nthreads,
                                              Sync sync, uint32_t* s_rem) {
@@ -363,7 +365,7 @@ __device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, u
       const Conf cf = load_conf(&a.conf[j]);
       bool hit = false;
 #pragma unroll
-      for (int q = 0; q < 5; q++) hit |= a.touched[cf.c[q]] == a.stamp;
+      for (int q = 0; q < 5; q++) hit |= __ldcg(&a.touched[cf.c[q]]) == a.stamp;
       if (hit) {
         a.state[j] = 2;
         continue;
@@ -407,9 +409,9 @@ __device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, u
     if (a.state[j] != 1) continue;
     const Reins r = a.reins[a.plist[j]];
     const uint32_t sib = sibling_of(r.from);
-    const uint32_t parent = a.parents[r.from];
-    const Bvh2Node sib_node = ld_node(&a.nodes[sib]);
-    const Bvh2Node dst = ld_node(&a.nodes[r.to]);
+    const uint32_t parent = __ldcg(&a.parents[r.from]);
+    const Bvh2Node sib_node = ld_node_cg(&a.nodes[sib]);
+    const Bvh2Node dst = ld_node_cg(&a.nodes[r.to]);
     Bvh2Node inner = dst;
     inner.a.w = __uint_as_float(0u);
     inner.b.w = __uint_as_float(left_sibling_of(r.from));
@@ -438,22 +440,22 @@ __device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, u
   uint32_t* start_slots = reinterpret_cast<uint32_t*>(a.starts);
   for (uint32_t i = t0; i < 2 * P; i += nthreads) {
     const uint32_t j = i >> 1;
-    if (a.state[j] != 1) continue;
-    uint32_t x = start_slots[i];
-    if (i & 1u) x = x != 0 ? a.parents[x] : OBVHS_INVALID;
+    if (__ldcg(&a.state[j]) != 1) continue;  // slots and states were written by other threads
+    uint32_t x = __ldcg(&start_slots[i]);
+    if (i & 1u) x = x != 0 ? __ldcg(&a.parents[x]) : OBVHS_INVALID;
     start_slots[i] = (x != OBVHS_INVALID && mark_path(a, x)) ? x : OBVHS_INVALID;
   }
   sync();
 
   // 5. refit from the marked nodes that have no marked children
   for (uint32_t i = t0; i < 2 * P; i += nthreads) {
-    if (a.state[i >> 1] != 1) continue;
+    if (__ldcg(&a.state[i >> 1]) != 1) continue;
     const uint32_t x = start_slots[i];
     if (x == OBVHS_INVALID) continue;
-    const Bvh2Node xn = ld_node(&a.nodes[x]);
+    const Bvh2Node xn = ld_node_cg(&a.nodes[x]);
     if (node_prims(xn) == 0) {
       const uint32_t f = node_first(xn);
-      if (a.dirty[f] == a.stamp || a.dirty[f + 1] == a.stamp) continue;  // a child's climb reaches x
+      if (__ldcg(&a.dirty[f]) == a.stamp || __ldcg(&a.dirty[f + 1]) == a.stamp) continue;  // a child's climb reaches x
     }
     refit_climb(a, x);
   }
