@@ -147,26 +147,39 @@ int build_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t 
       KLAUNCH("k_iota_u32", k_iota_u32<<<div_up<uint32_t>(m, 256), 256, 0, c.stream>>>(b2.prim_indices, m));
     }
   }
-  r = take_status(c);
-  if (r) return r;
+  // Host round trips inside the build: the pre-split count (when splitting),
+  // one after PLOC (status word, pass count for the reinsertion stack bound,
+  // root leaf test), the CWBVH size (its allocation) and the final status.
+  BuildReadback* rb = reinterpret_cast<BuildReadback*>(static_cast<char*>(c.h_small) + READBACK_OFFSET);
+  std::memset(rb, 0, sizeof(BuildReadback));
   uint32_t passes = 0;
   uint64_t sum_counts = 0;
   r = ploc_build_device(c, leaves, m, total, p->ploc_search_distance, (int)p->sort_precision,
-                        p->search_depth_threshold, b2.nodes, &passes, &sum_counts);
+                        p->search_depth_threshold, b2.nodes, &passes, &sum_counts, &rb->ploc);
   if (r) return r;
   stages.mark(c.stream);
+  if (m) CK(cudaMemcpyAsync(&rb->root_prims, reinterpret_cast<const char*>(b2.nodes) + 12, 4, cudaMemcpyDeviceToHost,
+                            c.stream));
+  CK(cudaMemcpyAsync(&rb->status, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  // NaN boxes drop out of PLOC (no finite merge cost), leaving tree slots
+  // unwritten: stop before anything follows the tree's links
+  if (rb->status) return take_status(c);
+  passes = rb->ploc.passes;
+  sum_counts = rb->ploc.sum_counts;
   b2.max_depth = std::max<uint32_t>(96, passes + 1);
   uint64_t applied = 0;
-  r = reinsertion_device(c, &b2, p->reinsertion_batch_ratio, nullptr, 0, &applied);
+  r = reinsertion_device(c, &b2, p->reinsertion_batch_ratio, nullptr, 0, &applied, m ? (int64_t)rb->root_prims : 1,
+                         &rb->applied);
   if (r) return r;
   stages.mark(c.stream);
   uint32_t mp = p->max_prims_per_leaf < 1 ? 1 : (p->max_prims_per_leaf > 3 ? 3 : p->max_prims_per_leaf);
   obvhs_cwbvh* cw = new obvhs_cwbvh();
   cw->ctx = &c;
   cw->uses_spatial_splits = split;
-  r = cwbvh_convert_device(c, &b2, mp, 1, cw);
+  r = cwbvh_convert_device(c, &b2, mp, 1, cw, &rb->emitted);
   if (r) {
-    delete cw;
+    obvhs_cwbvh_free(cw);
     return r;
   }
   if (tris) {
@@ -177,23 +190,25 @@ int build_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t 
     }
   }
   stages.mark(c.stream);
+  // total_aabb = the BVH2 root's box
+  if (b2.n_nodes) CK(cudaMemcpyAsync(rb->root_box, b2.nodes, 32, cudaMemcpyDeviceToHost, c.stream));
   double ms = timer.stop_ms();
   r = take_status(c);
+  if (!r && cw->n_nodes && rb->emitted != cw->n_nodes)
+    r = c.fail(OBVHS_ERR_BAD_INPUT, "CWBVH emission failed");
   if (r) {
     obvhs_cwbvh_free(cw);
     return r;
   }
-  // total_aabb = the BVH2 root's box
   if (b2.n_nodes) {
-    float root[8];
-    CK(cudaMemcpy(root, b2.nodes, 32, cudaMemcpyDeviceToHost));
-    cw->total_aabb[0] = root[0];
-    cw->total_aabb[1] = root[1];
-    cw->total_aabb[2] = root[2];
-    cw->total_aabb[3] = root[4];
-    cw->total_aabb[4] = root[5];
-    cw->total_aabb[5] = root[6];
+    cw->total_aabb[0] = rb->root_box[0];
+    cw->total_aabb[1] = rb->root_box[1];
+    cw->total_aabb[2] = rb->root_box[2];
+    cw->total_aabb[3] = rb->root_box[4];
+    cw->total_aabb[4] = rb->root_box[5];
+    cw->total_aabb[5] = rb->root_box[6];
   }
+  applied = rb->applied;
   if (stats) {
     stats->core_build_ms = ms;
     stats->leaf_count = m;

@@ -108,6 +108,18 @@ struct PlocState {
   unsigned long long sum_counts;
 };
 
+// Pinned host words a build fills asynchronously and reads after a later
+// synchronisation, at obvhs_ctx::h_small + READBACK_OFFSET.
+constexpr size_t READBACK_OFFSET = 2048;
+struct BuildReadback {
+  PlocState ploc;
+  uint32_t root_prims;
+  uint32_t applied;
+  uint32_t emitted;
+  uint32_t status;
+  float root_box[8];
+};
+
 struct obvhs_ctx {
   int device = 0;
   int num_sms = 0;
@@ -193,9 +205,11 @@ int ploc_leaves(BuildCtx& c, const float* tris, const float* aabbs, const uint32
 int ploc_morton_codes(BuildCtx& c, const Bvh2Node* leaves, uint32_t n, const int* total_keys, int precision,
                       void* codes);
 int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_t** order_out);
+// With `deferred` (pinned host memory) the final PlocState is copied there
+// asynchronously and passes_out / sum_counts_out are left unset.
 int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* total_keys, uint32_t radius,
                       int precision, uint32_t depth_threshold, Bvh2Node* out_nodes, uint32_t* passes_out,
-                      uint64_t* sum_counts_out);
+                      uint64_t* sum_counts_out, PlocState* deferred = nullptr);
 int ploc_setup_kernels();
 
 // presplit.cu
@@ -204,12 +218,19 @@ int presplit_device(BuildCtx& c, const float* tris, uint32_t n, float** aabbs_ou
 int split_thresholds_device(BuildCtx& c, const float* tris, uint32_t n, float* out6);
 
 // reinsertion.cu
+// root_prims: the root's primitive count when the caller knows it (-1:
+// read it here).  With `applied_deferred` (pinned) the applied count is copied
+// there asynchronously instead of to *applied_out.
 int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const float* seq, uint32_t nseq,
-                       uint64_t* applied_out);
+                       uint64_t* applied_out, int64_t root_prims = -1, uint32_t* applied_deferred = nullptr);
 int compute_parents_device(BuildCtx& c, const Bvh2Node* nodes, uint32_t n_nodes, uint32_t* parents);
 
 // cwbvh.cu
-int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, int order_children, obvhs_cwbvh* out);
+// With `emitted_deferred` (pinned) the number of emitted nodes is copied there
+// asynchronously; the caller compares it with out->n_nodes after its final
+// synchronisation and checks the status word.
+int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, int order_children, obvhs_cwbvh* out,
+                         uint32_t* emitted_deferred = nullptr);
 
 // traverse.cu
 int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint32_t n, uint32_t* hits,

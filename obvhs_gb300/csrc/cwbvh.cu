@@ -554,7 +554,8 @@ static const uint32_t* ceil_log2_thresholds() {
   return thr;
 }
 
-int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, int order_children, obvhs_cwbvh* out) {
+int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, int order_children, obvhs_cwbvh* out,
+                         uint32_t* emitted_deferred) {
   out->n_nodes = 0;
   out->n_prims = 0;
   const uint32_t n = b->n_nodes;
@@ -585,8 +586,9 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   const uint32_t n_pr = root.nprim;
   CwNode* cwn = nullptr;
   uint32_t* cwp = nullptr;
-  if (cudaMalloc(&cwn, (size_t)n_cw * sizeof(CwNode)) != cudaSuccess ||
-      cudaMalloc(&cwp, (size_t)std::max(n_pr, 1u) * 4) != cudaSuccess) {
+  // stream-ordered allocations: no device-wide synchronisation
+  if (cudaMallocAsync(&cwn, (size_t)n_cw * sizeof(CwNode), c.stream) != cudaSuccess ||
+      cudaMallocAsync(&cwp, (size_t)std::max(n_pr, 1u) * 4, c.stream) != cudaSuccess) {
     cudaGetLastError();
     if (cwn) cudaFree(cwn);
     return c.fail(OBVHS_ERR_OOM, "cwbvh output");
@@ -625,6 +627,14 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
       emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)n_cw * 32, EMIT_THREADS)));
   KLAUNCH("k_emit_all", k_emit_all<<<grid, EMIT_THREADS, 0, c.stream>>>(ea));
   CK(cudaGetLastError());
+  out->nodes = cwn;
+  out->n_nodes = n_cw;
+  out->prim_indices = cwp;
+  out->n_prims = n_pr;
+  if (emitted_deferred) {
+    CK(cudaMemcpyAsync(emitted_deferred, counters + 14, 4, cudaMemcpyDeviceToHost, c.stream));
+    return 0;
+  }
   uint32_t emitted = 0;
   CK(cudaMemcpyAsync(&emitted, counters + 14, 4, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaMemcpyAsync(c.h_status, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream));
@@ -632,11 +642,10 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   if (*c.h_status || emitted != n_cw) {
     cudaFree(cwn);
     cudaFree(cwp);
+    out->nodes = nullptr;
+    out->prim_indices = nullptr;
+    out->n_nodes = out->n_prims = 0;
     return c.fail(OBVHS_ERR_BAD_INPUT, "CWBVH emission failed (status " + std::to_string(*c.h_status) + ")");
   }
-  out->nodes = cwn;
-  out->n_nodes = n_cw;
-  out->prim_indices = cwp;
-  out->n_prims = n_pr;
   return 0;
 }

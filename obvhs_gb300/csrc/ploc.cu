@@ -698,7 +698,7 @@ int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_
 
 int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* total_keys, uint32_t radius,
                       int precision, uint32_t depth_threshold, Bvh2Node* out_nodes, uint32_t* passes_out,
-                      uint64_t* sum_counts_out) {
+                      uint64_t* sum_counts_out, PlocState* deferred) {
   *passes_out = 0;
   *sum_counts_out = 0;
   if (n == 0) return 0;
@@ -744,6 +744,10 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
     KLAUNCH("k_ploc_tail", k_ploc_tail<<<1, TAIL_THREADS, smem, c.stream>>>(cur, nxt, st, (int)radius, depth_threshold,
                                                                            max_passes, out_nodes, c.d_status));
     CK(cudaGetLastError());
+  }
+  if (deferred) {
+    CK(cudaMemcpyAsync(deferred, st, sizeof(PlocState), cudaMemcpyDeviceToHost, c.stream));
+    return 0;
   }
   PlocState h;
   CK(cudaMemcpyAsync(&h, st, sizeof(PlocState), cudaMemcpyDeviceToHost, c.stream));

@@ -271,16 +271,41 @@ __device__ __forceinline__ Conf load_conf(const Conf* p) {
   return c;
 }
 
-__device__ __forceinline__ Box ldcg_box(const Bvh2Node* p) {
+// Loads and stores for the mark and refit steps.  With every block taking
+// part (L1 = false) they go through L2, since another SM may have written the
+// word earlier in the launch.  When one block finishes a pass alone (L1 =
+// true), every writer since the launch began runs on its SM, so plain
+// accesses are coherent and the upper tree levels, which many climbs share,
+// hit in L1.
+template <bool L1>
+__device__ __forceinline__ uint32_t ld_word(const uint32_t* p) {
+  return L1 ? *p : __ldcg(p);
+}
+
+template <bool L1>
+__device__ __forceinline__ Box ld_box(const Bvh2Node* p) {
   const float4* q = reinterpret_cast<const float4*>(p);
-  const float4 a = __ldcg(q), b = __ldcg(q + 1);
+  const float4 a = L1 ? q[0] : __ldcg(q), b = L1 ? q[1] : __ldcg(q + 1);
   return Box{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)};
 }
 
-__device__ __forceinline__ void stcg_inner(Bvh2Node* p, const Box& u, uint32_t first) {
+template <bool L1>
+__device__ __forceinline__ Bvh2Node ld_nd(const Bvh2Node* p) {
+  return L1 ? ld_node(p) : ld_node_cg(p);
+}
+
+template <bool L1>
+__device__ __forceinline__ void st_inner(Bvh2Node* p, const Box& u, uint32_t first) {
   float4* w = reinterpret_cast<float4*>(p);
-  __stcg(w, make_float4(u.mn.x, u.mn.y, u.mn.z, __uint_as_float(0u)));
-  __stcg(w + 1, make_float4(u.mx.x, u.mx.y, u.mx.z, __uint_as_float(first)));
+  const float4 a = make_float4(u.mn.x, u.mn.y, u.mn.z, __uint_as_float(0u));
+  const float4 b = make_float4(u.mx.x, u.mx.y, u.mx.z, __uint_as_float(first));
+  if (L1) {
+    w[0] = a;
+    w[1] = b;
+  } else {
+    __stcg(w, a);
+    __stcg(w + 1, b);
+  }
 }
 
 __device__ __forceinline__ uint32_t atom_exch_acq_rel(uint32_t* p, uint32_t v) {
@@ -291,10 +316,11 @@ __device__ __forceinline__ uint32_t atom_exch_acq_rel(uint32_t* p, uint32_t v) {
 
 // Marks x and its ancestors up to the first node already marked this pass.
 // Returns whether x itself was newly marked.
+template <bool L1>
 __device__ __forceinline__ bool mark_path(const ResolveArgs& a, uint32_t x) {
   bool first = true, owned = false;
   for (uint32_t guard = 0; guard < a.n_nodes; guard++) {
-    const uint32_t up = __ldcg(&a.parents[x]);  // independent of the exchange: overlaps it
+    const uint32_t up = ld_word<L1>(&a.parents[x]);  // independent of the exchange: overlaps it
     if (atomicExch(&a.dirty[x], a.stamp) == a.stamp) return owned;
     if (first) owned = true;
     first = false;
@@ -309,28 +335,29 @@ __device__ __forceinline__ bool mark_path(const ResolveArgs& a, uint32_t x) {
 // a finished node is refit at once when its other child is unmarked, and by
 // the second of the two climbs when both children are marked.  Unions are
 // taken first child, second child, as Bvh2::refit_from does.
+template <bool L1>
 __device__ __forceinline__ void refit_climb(const ResolveArgs& a, uint32_t x) {
-  Bvh2Node xn = ld_node_cg(&a.nodes[x]);
+  Bvh2Node xn = ld_nd<L1>(&a.nodes[x]);
   Box box = node_box(xn);
   if (node_prims(xn) == 0) {
     const uint32_t f = node_first(xn);
-    box = box_union(ldcg_box(&a.nodes[f]), ldcg_box(&a.nodes[f + 1]));
-    stcg_inner(&a.nodes[x], box, f);
+    box = box_union(ld_box<L1>(&a.nodes[f]), ld_box<L1>(&a.nodes[f + 1]));
+    st_inner<L1>(&a.nodes[x], box, f);
   }
   for (uint32_t guard = 0; guard < a.n_nodes; guard++) {
     if (x == 0) return;
-    const uint32_t up = __ldcg(&a.parents[x]);
+    const uint32_t up = ld_word<L1>(&a.parents[x]);
     const uint32_t sib = sibling_of(x);
-    const bool sib_marked = __ldcg(&a.dirty[sib]) == a.stamp;
-    Box sb = ldcg_box(&a.nodes[sib]);  // final unless the sibling is marked: loads overlap
+    const bool sib_marked = ld_word<L1>(&a.dirty[sib]) == a.stamp;
+    Box sb = ld_box<L1>(&a.nodes[sib]);  // final unless the sibling is marked: loads overlap
     if (sib_marked) {
       // release: this climb's box stores before the exchange; acquire: the
       // sibling climb's stores before reading its box again
       if (atom_exch_acq_rel(&a.arrive[up], a.stamp) != a.stamp) return;  // the sibling's climb continues
-      sb = ldcg_box(&a.nodes[sib]);
+      sb = ld_box<L1>(&a.nodes[sib]);
     }
     box = (x & 1u) ? box_union(box, sb) : box_union(sb, box);
-    stcg_inner(&a.nodes[up], box, left_sibling_of(x));
+    st_inner<L1>(&a.nodes[up], box, left_sibling_of(x));
     x = up;
   }
   set_status(a.status, ST_ITER_LIMIT);
@@ -338,9 +365,10 @@ __device__ __forceinline__ void refit_climb(const ResolveArgs& a, uint32_t x) {
 
 // Steps 2-5 of k_resolve over the P listed proposals, by `nthreads` threads
 // numbered `t0`, with `sync` a barrier over exactly those threads.  Words that
-// other blocks write earlier in the same launch (parents, nodes, touched,
-// dirty) are read through L2 (ld.cg) so no stale L1 line is used.
-template <class Sync>
+// other blocks may write earlier in the same launch (parents, nodes, touched,
+// dirty) are read through L2 (ld.cg) so no stale L1 line is used, except in
+// the mark and refit steps of a single-block pass (L1 = true, see ld_word).
+template <bool L1, class Sync>
 __device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, uint32_t t0, uint32_t nthreads,
                                              Sync sync, uint32_t* s_rem) {
   // 2. rounds, one barrier each.  A proposal touching an accepted one is
@@ -443,7 +471,7 @@ __device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, u
     if (__ldcg(&a.state[j]) != 1) continue;  // slots and states were written by other threads
     uint32_t x = __ldcg(&start_slots[i]);
     if (i & 1u) x = x != 0 ? __ldcg(&a.parents[x]) : OBVHS_INVALID;
-    start_slots[i] = (x != OBVHS_INVALID && mark_path(a, x)) ? x : OBVHS_INVALID;
+    start_slots[i] = (x != OBVHS_INVALID && mark_path<L1>(a, x)) ? x : OBVHS_INVALID;
   }
   sync();
 
@@ -457,7 +485,7 @@ __device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, u
       const uint32_t f = node_first(xn);
       if (__ldcg(&a.dirty[f]) == a.stamp || __ldcg(&a.dirty[f + 1]) == a.stamp) continue;  // a child's climb reaches x
     }
-    refit_climb(a, x);
+    refit_climb<L1>(a, x);
   }
 }
 
@@ -513,9 +541,9 @@ __global__ void __launch_bounds__(RESOLVE_THREADS) k_resolve(ResolveArgs a) {
   const uint32_t P = *(volatile uint32_t*)&a.ctr[0];
   if (P <= RESOLVE_SMALL) {
     if (blockIdx.x != 0) return;
-    resolve_body(a, P, threadIdx.x, blockDim.x, [] { __syncthreads(); }, &s_rem);
+    resolve_body<true>(a, P, threadIdx.x, blockDim.x, [] { __syncthreads(); }, &s_rem);
   } else {
-    resolve_body(a, P, t0, stride, [&] { grid.sync(); }, &s_rem);
+    resolve_body<false>(a, P, t0, stride, [&] { grid.sync(); }, &s_rem);
   }
 }
 
@@ -529,15 +557,19 @@ int compute_parents_device(BuildCtx& c, const Bvh2Node* nodes, uint32_t n_nodes,
 }
 
 int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const float* seq, uint32_t nseq,
-                       uint64_t* applied_out) {
+                       uint64_t* applied_out, int64_t root_prims, uint32_t* applied_deferred) {
   *applied_out = 0;
+  if (applied_deferred) *applied_deferred = 0;
   const uint32_t len = b->n_nodes;
   if (len == 0 || !(batch_size_ratio > 0.0f)) return 0;
-  // nodes[0].is_leaf(): one download of the root's prim_count
-  uint32_t root_pc = 0;
-  CK(cudaMemcpyAsync(&root_pc, reinterpret_cast<const char*>(b->nodes) + 12, 4, cudaMemcpyDeviceToHost, c.stream));
-  CK(cudaStreamSynchronize(c.stream));
-  if (root_pc != 0) return 0;
+  // nodes[0].is_leaf(): one download of the root's prim_count unless known
+  if (root_prims < 0) {
+    uint32_t root_pc = 0;
+    CK(cudaMemcpyAsync(&root_pc, reinterpret_cast<const char*>(b->nodes) + 12, 4, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    root_prims = root_pc;
+  }
+  if (root_prims != 0) return 0;
   float def[16];
   if (!seq) {
     for (int k = 0; k < 16; k++) def[k] = 1.0f / (float)(2 * k + 1);
@@ -631,6 +663,10 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
                                                  std::max<uint64_t>(1, div_up<uint32_t>(count, RESOLVE_THREADS)));
     KLAUNCH("k_resolve", CK(cudaLaunchCooperativeKernel((void*)k_resolve, grid, RESOLVE_THREADS, args, 0, c.stream)));
     CK(cudaGetLastError());
+  }
+  if (applied_deferred) {
+    CK(cudaMemcpyAsync(applied_deferred, counters + 1, 4, cudaMemcpyDeviceToHost, c.stream));
+    return 0;
   }
   uint32_t applied = 0;
   CK(cudaMemcpyAsync(&applied, counters + 1, 4, cudaMemcpyDeviceToHost, c.stream));

@@ -244,7 +244,7 @@ int reorder_tris_device(BuildCtx& c, obvhs_cwbvh* b, const float* tris, uint32_t
   b->n_tris = n_tris;
   if (b->n_prims == 0) return 0;
   float4* out = nullptr;
-  if (cudaMalloc(&out, (size_t)b->n_prims * 64) != cudaSuccess) {
+  if (cudaMallocAsync(&out, (size_t)b->n_prims * 64, c.stream) != cudaSuccess) {
     cudaGetLastError();
     return c.fail(OBVHS_ERR_OOM, "triangle buffer");
   }

@@ -1,0 +1,58 @@
+"""Full builds at the benchmark's scale vs the oracle, bit for bit (needs a GPU).
+
+The small cases in test_gpu_parity.py run every kernel in its single-tile or
+single-block form.  These sizes exercise the forms that only large inputs
+reach: PLOC passes with several tiles per block group and adaptive tile
+sizes, reinsertion passes resolved by the whole grid, the persistent
+reinsertion search, multi-wave radix sorts.  Each build is repeated to catch
+races that make results depend on timing.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from obvhs_gb300 import scenes as S
+from obvhs_gb300.params import PRESETS
+
+pytestmark = pytest.mark.gpu
+
+THREADS = os.cpu_count() or 4
+
+
+@pytest.fixture(scope="module")
+def G():
+    import obvhs_gb300 as g
+
+    return g
+
+
+def _bytes_equal(a, b):
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    return a.shape == b.shape and a.tobytes() == b.tobytes()
+
+
+@pytest.mark.parametrize("preset,n", [("slow", 1_000_000), ("fastest", 1_000_000),
+                                      ("medium", 2_000_000)])
+def test_clustered_scene_bitexact_repeated(G, preset, n):
+    tris = S.scene2_tris(n)
+    p = PRESETS[preset]()
+    ob = O.build(tris=tris, params=p, nthreads=THREADS, keep_intermediate=False)
+    for _ in range(3):
+        cw = G.build_cwbvh_from_tris(tris, p)
+        nodes, prims = cw.download()
+        assert cw.stats.reinsertions == ob.reinsertions
+        assert _bytes_equal(nodes, ob.cw_nodes)
+        assert _bytes_equal(prims, ob.cw_pidx)
+
+
+def test_ploc_one_million_u64(G):
+    tris = S.scene2_tris(1_000_000).reshape(-1, 3, 3)
+    aabbs = np.concatenate([tris.min(1), tris.max(1)], 1).astype(np.float32)
+    on, op, omd, _ = O.ploc(aabbs, None, 14, 0, 0, nthreads=THREADS)
+    b = G.PlocBuilder().build_ploc(14, aabbs, None, 0, 0)
+    nodes, pidx = b.download()
+    assert _bytes_equal(nodes, on)
+    assert _bytes_equal(pidx, op)

@@ -203,6 +203,23 @@ def test_degenerate_gpu(G, preset):
         G.build_cwbvh(inf10, BvhBuildParams.medium_build())
 
 
+@pytest.mark.parametrize("preset", ["fastest", "slow"])
+def test_full_build_nan_is_an_error_and_context_recovers(G, preset):
+    tris = T.demoscene(20, 3)
+    bad = tris.copy()
+    # the last vertex: min/max with the SSE semantics (a < b ? a : b) keep a
+    # NaN only in the second operand, so the box is NaN and the build must fail
+    bad[len(bad) // 2, 6] = np.nan
+    p = PRESETS[preset]()
+    with pytest.raises(G.ObvhsError) as e:
+        G.build_cwbvh_from_tris(bad, p)
+    assert e.value.code == -4
+    cw = G.build_cwbvh_from_tris(tris, p)
+    gn, gp = cw.download()
+    ob = O.build(tris=tris, params=p)
+    assert _eq(gn, ob.cw_nodes) and _eq(gp, ob.cw_pidx)
+
+
 def test_traversal_bitexact_scene1(G):
     tris, rays = S.scene1()
     ob = O.build(tris=tris, params=BvhBuildParams.fastest_build())
