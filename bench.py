@@ -11,7 +11,8 @@ primary rays and of one cosine-weighted bounce ray per primary hit.
   e2e         the same build through the public API from pinned host
               triangles, host->device copy and the CWBVH download included
   traversal   Mrays/s of the primary and bounce batches (device-resident rays)
-  roofline    the dominant kernel of the step against the measured HBM peak
+  roofline    the build's dominant kernel against the measured HBM peak
+              (also the whole build, and the primary traversal kernel)
   cpu_baseline the C++ restatement of the reference (oracle) on all host cores
 
 --impl reference runs that CPU restatement of the reference's algorithm (the
@@ -44,7 +45,7 @@ L2_FLUSH_BYTES = 512 << 20
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tris", type=int, default=N_TRIS)
@@ -72,8 +73,13 @@ class ClockSampler:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            # nvidia-smi takes a moment to start: wait for its first sample so
+            # the timed region is covered
+            t0 = time.perf_counter()
+            while time.perf_counter() - t0 < 3.0 and os.path.getsize(self.path) == 0:
+                time.sleep(0.02)
         except Exception:
             self.proc = None
         return self
@@ -111,6 +117,69 @@ def measured_peak():
         d = json.load(open(p))
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+ROOFLINE_NOTES = {
+    "k_rs_pass": "radix sort passes of 0.03-1M keys: each pass is one wave of tiles whose ranking, "
+                 "decoupled look-back and scatter phases are latency-bound",
+    "k_resolve": "dependent rounds and tree climbs; bytes are a lower bound",
+    "k_find": "branch-and-bound tree searches; bytes are a lower bound",
+    "k_ploc_coop": "compute in the nearest-neighbour search; clusters stay in L2",
+    "k_costs": "bottom-up tree climb; bytes are a lower bound",
+    "k_emit_all": "work queue over the tree; bytes are a lower bound",
+}
+
+
+def reinsertion_schedule(n_nodes, ratio=0.2):
+    """(candidates, searched) per reinsertion pass, as the reference's
+    optimize_impl sizes them (src/bvh2/reinsertion.rs:101-115)."""
+    out = []
+    for k in range(16):
+        batch = max(int(np.float32(np.float32(n_nodes) * np.float32(ratio)) * np.float32(1.0 / (2 * k + 1))), 1)
+        node_count = min(n_nodes, batch + 1)
+        take = min(node_count * 2, n_nodes)
+        out.append((take - 1, node_count - 1))
+    return out
+
+
+def kernel_byte_models(m, sum_counts, n_cw, n_prims):
+    """Algorithmic bytes of one build, per kernel (totals over its launches).
+
+    Minimum bytes each kernel must move for its result, from the per-unit
+    figures of the path's byte model; pointer-chasing kernels (k_find,
+    k_resolve, k_costs, k_emit_all) also read tree nodes along their walks,
+    which depends on the tree and is not counted (a lower bound)."""
+    nodes = 2 * m - 1
+    sched = reinsertion_schedule(nodes)
+    cand_sort = sum(4 * c * 16 for c, _ in sched) + sum(c * 4 for c, _ in sched)
+    return {
+        # Morton U128 sort (16 passes of 8-bit digits over key 16 B + value
+        # 4 B, read and written) and the 16 candidate sorts (u32 key + value)
+        "k_rs_pass": 16 * m * 40 + cand_sort,
+        # every PLOC pass: box read twice, offset byte written and read twice,
+        # compacted cluster written; every merged pair written once
+        "k_ploc_coop": sum_counts * (32 + 32 + 1 + 2 + 32) + (nodes - 1) * 32,
+        # candidate id, three node loads to start the search, result
+        "k_find": sum(s_ * (4 + 3 * 32 + 16) for _, s_ in sched),
+        # proposal read, conflict set written and read back
+        "k_resolve": sum(s_ * (16 + 32 + 32) for _, s_ in sched),
+        # node + parent read, cost record (96 B) written, children records read
+        "k_costs": nodes * (32 + 4 + 96) + (m - 1) * 2 * 96,
+        # 80 B node and primitive indices written, each BVH2 node and record read
+        "k_emit_all": n_cw * 80 + n_prims * 4 + nodes * (32 + 96),
+        "k_morton128": m * (32 + 16),
+        "k_gather": m * (4 + 32 + 32),
+        "k_leaves_from_tris": m * (36 + 32),
+        "k_reorder_tris": n_prims * (4 + 36 + 64),
+    }
+
+
+def build_byte_model(m, n_tris, sum_counts, n_cw, n_prims):
+    """Whole-build algorithmic bytes: triangle read, AABB write and read, Morton
+    key + value, 16 sort passes, PLOC, reinsertion sorts and proposals, CWBVH
+    costs and nodes (the per-primitive byte model of the path)."""
+    k = kernel_byte_models(m, sum_counts, n_cw, n_prims)
+    return n_tris * 36 + m * (24 + 24) + sum(k.values())
 
 
 def workload(n):
@@ -312,16 +381,41 @@ def run_gb300(args):
     cores = os.cpu_count() or 1
     cpu_rate, cpu_t, cpu_trace = cpu_baseline(tris, p, rays, cores, ctx)
 
-    # roofline: the primary-ray traversal kernel (one launch per batch, timed
-    # above with CUDA events on the library's stream).  Algorithmic bytes per
-    # ray: 32 (ray) + 8 (hit) + 80 per node visited + 36 per triangle tested.
-    alg_bytes = 40.0 * len(rays) + 80.0 * cpu_trace["visits"] + 36.0 * cpu_trace["tests"]
     peak, peak_kind = measured_peak()
-    achieved = alg_bytes / (mean_prim * 1e-3) / 1e9
-    traffic = None
+    traffic_db = {}
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get("k_traverse_primary_bytes")
+        traffic_db = json.load(open(tpath))
+
+    # roofline of the build's dominant kernel (largest share of device time in
+    # the event-bracketed build): algorithmic bytes per launch / mean launch
+    # time; traffic = DRAM bytes per launch from the ncu capture (profiles/)
+    models = kernel_byte_models(stats.leaf_count, stats.ploc_sum_counts, n_nodes, n_prims)
+    build_kernels = {}
+    for k, v in kernel_profile.items():
+        if k.startswith("k_traverse"):
+            continue
+        k = "k_find" if k.startswith("k_find") else k  # one search kernel, two launch forms
+        a = build_kernels.setdefault(k, {"launches": 0, "total_ms": 0.0})
+        a["launches"] += v["launches"]
+        a["total_ms"] += v["total_ms"]
+    ranked = sorted(build_kernels.items(), key=lambda kv: -kv[1]["total_ms"])
+    dom_name, dom = next(((k, v) for k, v in ranked if models.get(k)), ranked[0])
+    dom_launches = max(dom["launches"], 1)
+    dom_bytes = models.get(dom_name, 0) / dom_launches
+    dom_ms = dom["total_ms"] / dom_launches
+    dom_achieved = dom_bytes / (dom_ms * 1e-3) / 1e9 if dom_ms > 0 else 0.0
+    build_total_ms = sum(v["total_ms"] for v in build_kernels.values())
+
+    # whole build against the same peak (the build is latency- and launch-bound)
+    build_bytes = build_byte_model(stats.leaf_count, n, stats.ploc_sum_counts, n_nodes, n_prims)
+    build_achieved = build_bytes / (mean_build * 1e-3) / 1e9
+
+    # traversal: one launch per batch, timed above with CUDA events on the
+    # library's stream.  Algorithmic bytes per ray: 32 (ray) + 8 (hit) + 80 per
+    # node visited + 36 per triangle tested (visit/test counts: oracle)
+    alg_bytes = 40.0 * len(rays) + 80.0 * cpu_trace["visits"] + 36.0 * cpu_trace["tests"]
+    achieved = alg_bytes / (mean_prim * 1e-3) / 1e9
 
     line = {
         "metric": METRIC, "value": value, "unit": "Mtris/s", "n_gpus": world, "steps": args.steps,
@@ -336,10 +430,19 @@ def run_gb300(args):
                       "bounce_ms": mean_bounce},
         "build_stages_ms": {"presplit": stats.stage_ms[0], "ploc": stats.stage_ms[1],
                             "reinsertion": stats.stage_ms[2], "cwbvh": stats.stage_ms[3]},
-        "roofline": {"kernel": "k_traverse<closest> (primary batch)", "bound": "hbm", "achieved": achieved,
-                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
-                     "bytes_per_ray": alg_bytes / len(rays)},
+        "roofline": {"kernel": dom_name, "bound": "hbm", "achieved": dom_achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": dom_achieved / peak,
+                     "traffic": traffic_db.get(dom_name), "algorithmic_bytes_per_launch": dom_bytes,
+                     "launches": dom["launches"], "mean_launch_ms": dom_ms,
+                     "share_of_build_kernel_time": dom["total_ms"] / build_total_ms if build_total_ms else None,
+                     "note": ROOFLINE_NOTES.get(dom_name, "")},
+        "roofline_build": {"bound": "hbm", "achieved": build_achieved, "peak": peak, "unit": "GB/s",
+                           "frac": build_achieved / peak, "algorithmic_bytes": build_bytes,
+                           "bytes_per_leaf": build_bytes / max(stats.leaf_count, 1)},
+        "roofline_traversal": {"kernel": "k_traverse<closest> (primary batch)", "bound": "hbm",
+                               "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                               "traffic": traffic_db.get("k_traverse_closest"),
+                               "algorithmic_bytes_per_launch": alg_bytes, "bytes_per_ray": alg_bytes / len(rays)},
         "cpu_baseline": {"value": cpu_rate, "unit": "Mtris/s", "cores": cores, "kind": "port",
                          "sample": f"2 full {n}-triangle slow_build builds on {cores} threads "
                                    f"({sum(cpu_t):.1f} s)",
