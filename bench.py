@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tris", type=int, default=N_TRIS)
+    ap.add_argument("--no-arch-scene", action="store_true",
+                    help="skip the 8M-triangle architectural scene (build + 16M incoherent + 16M shadow rays)")
     return ap.parse_args()
 
 
@@ -180,6 +182,76 @@ def build_byte_model(m, n_tris, sum_counts, n_cw, n_prims):
     costs and nodes (the per-primitive byte model of the path)."""
     k = kernel_byte_models(m, sum_counts, n_cw, n_prims)
     return n_tris * 36 + m * (24 + 24) + sum(k.values())
+
+
+def arch_scene(ctx, stream, steps, warmup, flush):
+    """The 8M-triangle architectural scene: PLOC (radius 14, distance 1 for 3
+    passes, U64) -> CWBVH build, then 16M incoherent closest-hit rays and 16M
+    shadow rays to 4 point lights, all device-resident, CUDA-event timed."""
+    import ctypes
+    import torch
+    import obvhs_gb300 as G
+    from obvhs_gb300 import scenes as S
+    from obvhs_gb300.params import BvhBuildParams
+
+    tris = S.scene3_tris(8_000_000)
+    closest, shadow = S.scene3_rays(16_000_000)
+    d = torch.from_numpy(tris).cuda()
+    dc, ds = torch.from_numpy(closest).cuda(), torch.from_numpy(shadow).cuda()
+    plain = BvhBuildParams(False, 14, 3, 0.0, 0.0, 0, 3, 3.0)
+
+    def timed(fn, k):
+        ms = []
+        for _ in range(k):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+        return sum(ms) / len(ms)
+
+    holder = {}
+
+    def build(p):
+        holder["cw"] = G.build_cwbvh_from_tris(d, p, ctx=ctx)
+
+    for _ in range(warmup):
+        build(plain)
+    plain_ms = timed(lambda: build(plain), steps)
+    medium = BvhBuildParams.medium_build()
+    for _ in range(warmup):
+        build(medium)
+    medium_ms = timed(lambda: build(medium), steps)
+    build(plain)
+    cw = holder["cw"]
+    out = torch.empty((len(closest), 2), dtype=torch.int32, device="cuda")
+    miss = torch.empty((len(shadow),), dtype=torch.uint8, device="cuda")
+    lib = ctx.lib
+
+    def trace():
+        ctx.check(lib.obvhs_ray_traverse(ctx.h, cw.h, ctypes.c_void_p(dc.data_ptr()), len(closest),
+                                         ctypes.c_void_p(out.data_ptr()), 1))
+
+    def occlude():
+        ctx.check(lib.obvhs_ray_traverse_miss(ctx.h, cw.h, ctypes.c_void_p(ds.data_ptr()), len(shadow),
+                                              ctypes.c_void_p(miss.data_ptr()), 1))
+
+    for _ in range(warmup):
+        trace()
+        occlude()
+    c_ms = timed(trace, steps)
+    s_ms = timed(occlude, steps)
+    n = len(tris)
+    return {"workload": "architectural-8M: 200 tessellated quads + clutter, 16M incoherent + 16M shadow rays",
+            "n_tris": n, "build_plain_ms": plain_ms, "build_plain_mtris_s": n / (plain_ms * 1e-3) / 1e6,
+            "build_plain": "PLOC radius 14, distance-1 for 3 passes, U64 -> CWBVH (3 prims/leaf)",
+            "build_medium_build_ms": medium_ms, "build_medium_build_mtris_s": n / (medium_ms * 1e-3) / 1e6,
+            "incoherent_closest_mrays_s": len(closest) / (c_ms * 1e-3) / 1e6, "incoherent_closest_ms": c_ms,
+            "shadow_any_hit_mrays_s": len(shadow) / (s_ms * 1e-3) / 1e6, "shadow_any_hit_ms": s_ms,
+            "hit_fraction": float((out[:, 0] != -1).float().mean().item())}
 
 
 def workload(n):
@@ -375,6 +447,8 @@ def run_gb300(args):
     prim_rate = world * len(rays) / (mean_prim * 1e-3) / 1e6
     bounce_rate = world * len(bounce) / (mean_bounce * 1e-3) / 1e6 if mean_bounce > 0 else 0.0
 
+    arch = None if args.no_arch_scene else arch_scene(ctx, stream, max(3, args.steps // 4), args.warmup, flush)
+
     # CPU baseline (the oracle on this host's cores, bounded sample): two full
     # builds, and the primary batch traced with node-visit / triangle-test
     # counters, which also give the traversal's algorithmic bytes.
@@ -443,6 +517,7 @@ def run_gb300(args):
                                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                                "traffic": traffic_db.get("k_traverse_closest"),
                                "algorithmic_bytes_per_launch": alg_bytes, "bytes_per_ray": alg_bytes / len(rays)},
+        "architectural_scene": arch,
         "cpu_baseline": {"value": cpu_rate, "unit": "Mtris/s", "cores": cores, "kind": "port",
                          "sample": f"2 full {n}-triangle slow_build builds on {cores} threads "
                                    f"({sum(cpu_t):.1f} s)",

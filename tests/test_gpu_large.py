@@ -56,3 +56,26 @@ def test_ploc_one_million_u64(G):
     nodes, pidx = b.download()
     assert _bytes_equal(nodes, on)
     assert _bytes_equal(pidx, op)
+
+
+def test_architectural_scene_build_and_rays_bitexact(G):
+    """The 8M-triangle architectural generator at 2M: plain PLOC -> CWBVH
+    (radius 14, distance 1 for 3 passes, U64), then incoherent closest-hit
+    and shadow rays, all against the oracle."""
+    from obvhs_gb300.params import BvhBuildParams
+
+    tris = S.scene3_tris(2_000_000)
+    closest, shadow = S.scene3_rays(200_000)
+    p = BvhBuildParams(False, 14, 3, 0.0, 0.0, 0, 3, 3.0)
+    ob = O.build(tris=tris, params=p, nthreads=THREADS, keep_intermediate=False)
+    cw = G.build_cwbvh_from_tris(tris, p)
+    nodes, prims = cw.download()
+    assert _bytes_equal(nodes, ob.cw_nodes)
+    assert _bytes_equal(prims, ob.cw_pidx)
+    gid, gt = cw.ray_traverse(closest)
+    oid, ot, _ = O.traverse(ob.cw_nodes, ob.cw_pidx, tris, closest, 0, nthreads=THREADS)
+    assert np.array_equal(gid, oid)
+    assert np.array_equal(gt.view(np.uint32), ot.view(np.uint32))
+    gmiss = cw.ray_traverse_miss(shadow)
+    omiss, _, _ = O.traverse(ob.cw_nodes, ob.cw_pidx, tris, shadow, 1, nthreads=THREADS)
+    assert np.array_equal(gmiss, omiss == 0xFFFFFFFF)
