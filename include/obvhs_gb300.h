@@ -69,6 +69,17 @@ typedef struct {
   float t;
 } obvhs_hit;
 
+/* Instance traversal result (RayHit, src/ray.rs:62-70, without instance_id):
+ * geometry_id = the BLAS index, primitive_id = the primitive in that BLAS's
+ * BVH order (as the reference reports it), original_id =
+ * blas.primitive_indices[primitive_id]; all 0xffffffff and t = +inf on a miss. */
+typedef struct {
+  uint32_t geometry_id;
+  uint32_t primitive_id;
+  uint32_t original_id;
+  float t;
+} obvhs_tlas_hit;
+
 /* BvhBuildParams (src/lib.rs:296-319).  ploc_search_distance is the radius
  * 1..32 (PlocSearchDistance values 1,2,6,14,24,32, or any radius as
  * build_ploc::<SEARCH_DISTANCE> allows); sort_precision 0 = U64, 1 = U128. */
@@ -183,6 +194,17 @@ OBVHS_API int obvhs_ray_traverse(obvhs_ctx* ctx, const obvhs_cwbvh* bvh, const o
  * hits nothing in [tmin, tmax), 0 when it is occluded. */
 OBVHS_API int obvhs_ray_traverse_miss(obvhs_ctx* ctx, const obvhs_cwbvh* bvh, const obvhs_ray* rays, uint32_t n, uint8_t* miss,
                             int device_ptrs);
+
+/* CwBvh::ray_traverse_tlas_blas (src/cwbvh/mod.rs:342-491) with
+ * Triangle::intersect as the closure: `tlas` is a CWBVH over instance boxes
+ * whose primitive_indices name entries of `blas` (each with triangles
+ * attached); closest hit per ray.  Like the reference, rays are not
+ * transformed per instance, and the remaining instances of a TLAS leaf group
+ * after the first are not visited (the reference pushes them as a primitive
+ * group that its loop clears when popped). */
+OBVHS_API int obvhs_ray_traverse_tlas_blas(obvhs_ctx* ctx, const obvhs_cwbvh* tlas, const obvhs_cwbvh* const* blas,
+                                           uint32_t n_blas, const obvhs_ray* rays, uint32_t n, obvhs_tlas_hit* hits,
+                                           int device_ptrs);
 
 /* ---- stage-level access for parity checks ------------------------------- */
 /* sort_nodes_by_morton (src/ploc/mod.rs:771-847) on Bvh2Node::new(aabbs[i])

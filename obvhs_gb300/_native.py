@@ -90,6 +90,7 @@ SIGNATURES = {
     "obvhs_cwbvh_free": (I32, [P]),
     "obvhs_ray_traverse": (I32, [P, P, P, U32, P, I32]),
     "obvhs_ray_traverse_miss": (I32, [P, P, P, U32, P, I32]),
+    "obvhs_ray_traverse_tlas_blas": (I32, [P, P, P, U32, P, U32, P, I32]),
     "obvhs_morton_sort": (I32, [P, P, U32, U32, P, P]),
     "obvhs_morton_sort_noalloc": (I32, [P, U32, U32, P, P, P]),
 }

@@ -366,6 +366,31 @@ class CwBvh:
             return out
         return out.astype(bool)
 
+    def ray_traverse_tlas_blas(self, blas, rays, out=None):
+        """CwBvh::ray_traverse_tlas_blas (src/cwbvh/mod.rs:342-491): this CWBVH
+        is the TLAS over instance boxes, its primitive_indices index `blas`
+        (a sequence of CwBvh with triangles).  Host rays: returns
+        (geometry_id, primitive_id (BVH order in that BLAS), original_id, t);
+        device rays: an int32 tensor of shape (n, 4) with t as bits."""
+        pr, n, dev, keep = _prep(rays, np.float32, 8)
+        ctx = self.ctx
+        arr = (ctypes.c_void_p * max(len(blas), 1))(*[b.h for b in blas])
+        if out is None:
+            if dev:
+                import torch
+
+                out = torch.empty((n, 4), dtype=torch.int32, device=rays.device)
+            else:
+                out = np.zeros((n, 4), np.uint32)
+        po = ctypes.c_void_p(out.data_ptr()) if dev else out.ctypes.data_as(ctypes.c_void_p)
+        ctx.check(ctx.lib.obvhs_ray_traverse_tlas_blas(ctx.h, self.h, ctypes.cast(arr, ctypes.c_void_p), len(blas), pr,
+                                                       n, po, dev))
+        if dev:
+            ctx.synchronize()
+            return out
+        del keep
+        return out[:, 0].copy(), out[:, 1].copy(), out[:, 2].copy(), out[:, 3].copy().view(np.float32)
+
     def free(self):
         if self.h:
             self.ctx.lib.obvhs_cwbvh_free(self.h)

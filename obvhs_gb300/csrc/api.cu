@@ -657,6 +657,27 @@ int obvhs_ray_traverse_miss(obvhs_ctx* cp, const obvhs_cwbvh* b, const obvhs_ray
   return traverse_common(cp, b, rays, n, miss, device_ptrs, 1);
 }
 
+int obvhs_ray_traverse_tlas_blas(obvhs_ctx* cp, const obvhs_cwbvh* tlas, const obvhs_cwbvh* const* blas, uint32_t n_blas,
+                                 const obvhs_ray* rays, uint32_t n, obvhs_tlas_hit* hits, int device_ptrs) {
+  if (!cp || !tlas || (n_blas && !blas) || (n && (!rays || !hits))) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  int err = 0;
+  const float* dr = (const float*)stage_in(c, SLOT_INPUT2, rays, (size_t)n * 32, device_ptrs, &err);
+  if (err) return err;
+  const size_t ob = (size_t)n * sizeof(obvhs_tlas_hit);
+  void* dout = hits;
+  if (!device_ptrs) {
+    dout = c.scratch.get(SLOT_TRAV_OUT, ob + 16);
+    if (!dout) return c.fail(OBVHS_ERR_OOM, "output staging");
+  }
+  int r = traverse_tlas_device(c, tlas, blas, n_blas, dr, n, (uint32_t*)dout);
+  if (r) return r;
+  if (!device_ptrs && n) CK(cudaMemcpyAsync(hits, dout, ob, cudaMemcpyDeviceToHost, c.stream));
+  if (!device_ptrs) return take_status(c);
+  return OBVHS_OK;
+}
+
 // ---- stage access ----------------------------------------------------------
 
 int obvhs_morton_sort(obvhs_ctx* cp, const float* aabbs, uint32_t n, uint32_t precision, uint64_t* codes,

@@ -57,6 +57,7 @@ enum ScratchSlot {
   SLOT_CONF,
   SLOT_STARTS,
   SLOT_PLIST,
+  SLOT_BLAS_DESC,
   SLOT_COUNT
 };
 
@@ -236,3 +237,6 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
 int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint32_t n, uint32_t* hits,
                     uint8_t* miss, int mode);
 int reorder_tris_device(BuildCtx& c, obvhs_cwbvh* bvh, const float* tris, uint32_t n_tris);
+// hits4: n x (geometry id, BVH-order primitive id, original id, t bits)
+int traverse_tlas_device(BuildCtx& c, const obvhs_cwbvh* tlas, const obvhs_cwbvh* const* blas, uint32_t n_blas,
+                         const float* rays, uint32_t n, uint32_t* hits4);

@@ -18,6 +18,8 @@
 // the values Triangle::intersect computes per test.  Rays are 32 bytes
 // (origin, tmin, dir, tmax); results are 8 bytes (original id, t).
 // Persistent warps take 32 rays at a time from a global counter.
+#include <vector>
+
 #include "build.h"
 
 namespace {
@@ -214,6 +216,146 @@ __global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ no
   }
 }
 
+// CwBvh::ray_traverse_tlas_blas (src/cwbvh/mod.rs:342-491) with
+// Triangle::intersect.  One group stack (32 entries, StackStack clamping)
+// serves the TLAS and the BLAS: entering a BLAS records the stack length, and
+// traversal returns to the TLAS when the stack is back at that length.  As
+// in the reference, the remaining instances of a TLAS leaf group are pushed
+// as a primitive group and dropped when popped, and the ray is not
+// transformed into the instance's space.
+struct BlasDesc {
+  const CwNode* nodes;
+  const float4* tris;  // primitive_indices order, 64 bytes each
+  uint32_t n_nodes, n_prims;
+};
+
+__global__ void __launch_bounds__(TBLK) k_traverse_tlas(const CwNode* __restrict__ tlas, uint32_t n_tlas,
+                                                        const uint32_t* __restrict__ tlas_pidx, uint32_t n_tlas_prims,
+                                                        const BlasDesc* __restrict__ blas, uint32_t n_blas,
+                                                        const float4* __restrict__ rays, uint32_t nrays,
+                                                        uint4* __restrict__ hits, uint32_t* __restrict__ next_ray,
+                                                        uint32_t* status) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(next_ray, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= nrays) return;
+    const uint32_t ri = base + lane;
+    if (ri >= nrays) continue;
+    const float4 r0 = __ldg(&rays[2 * ri]), r1 = __ldg(&rays[2 * ri + 1]);
+    const float3 o = make_float3(r0.x, r0.y, r0.z), d = make_float3(r1.x, r1.y, r1.z);
+    const float tmin = r0.w;
+    float tmax = r1.w;
+    const float3 inv = make_float3(safe_inverse(d.x), safe_inverse(d.y), safe_inverse(d.z));
+    const uint32_t oct = (d.x < 0.0f ? 0u : 0x04040404u) | (d.y < 0.0f ? 0u : 0x02020202u) |
+                         (d.z < 0.0f ? 0u : 0x01010101u);
+    uint2 stack[32];
+    uint32_t sp = 0;
+    uint32_t tlas_sp = OBVHS_INVALID, mesh = OBVHS_INVALID;
+    const CwNode* nodes = tlas;
+    uint32_t n_nodes = n_tlas;
+    const float4* tris = nullptr;
+    uint32_t n_prims = 0;
+    uint32_t hit_prim = OBVHS_INVALID, hit_mesh = OBVHS_INVALID, hit_orig = OBVHS_INVALID;
+    uint2 cur = n_tlas ? make_uint2(0u, 0x80000000u) : make_uint2(0u, 0u);
+    bool bad = false;
+    for (uint32_t guard = 0;; guard++) {
+      if (guard > (1u << 24)) {
+        set_status(status, ST_ITER_LIMIT);
+        bad = true;
+        break;
+      }
+      uint2 prim = make_uint2(0u, 0u);
+      if (cur.y & 0xff000000u) {
+        const uint32_t hits_imask = cur.y;
+        const uint32_t cio = 31u - __clz(hits_imask);
+        const uint32_t cbase = cur.x;
+        cur.y &= ~(1u << cio);
+        if (cur.y & 0xff000000u) {
+          stack[sp] = cur;
+          sp = min(sp + 1, 31u);
+        }
+        const uint32_t slot = (cio - 24) ^ (oct & 0xffu);
+        const uint32_t ni = cbase + __popc(hits_imask & ~(0xffffffffu << slot));
+        if (ni >= n_nodes) {
+          set_status(status, ST_BAD_TREE);
+          bad = true;
+          break;
+        }
+        const NodeQ node = load_cw(nodes, ni);
+        const uint32_t hm = intersect_node(node, o, d, inv, tmax, oct);
+        cur.x = node.q1.x;
+        prim.x = node.q1.y;
+        cur.y = (hm & 0xff000000u) | byte_of(node.q0.w, 3);
+        prim.y = hm & 0x00ffffffu;
+      } else {
+        cur = make_uint2(0u, 0u);
+      }
+      while (prim.y != 0) {
+        const uint32_t lpi = 31u - __clz(prim.y);
+        prim.y &= ~(1u << lpi);
+        const uint32_t gpi = prim.x + lpi;
+        if (tlas_sp == OBVHS_INVALID) {
+          // a TLAS primitive: continue at the root of its BLAS
+          if (prim.y != 0) {
+            stack[sp] = prim;
+            sp = min(sp + 1, 31u);
+          }
+          if (cur.y & 0xff000000u) {
+            stack[sp] = cur;
+            sp = min(sp + 1, 31u);
+          }
+          tlas_sp = sp;
+          const uint32_t b = gpi < n_tlas_prims ? __ldg(&tlas_pidx[gpi]) : OBVHS_INVALID;
+          if (b >= n_blas) {
+            set_status(status, ST_BAD_TREE);
+            bad = true;
+            break;
+          }
+          const BlasDesc bd = blas[b];
+          nodes = bd.nodes;
+          n_nodes = bd.n_nodes;
+          tris = bd.tris;
+          n_prims = bd.n_prims;
+          mesh = b;
+          cur = make_uint2(0u, 0x80000000u);
+          break;
+        }
+        if (gpi >= n_prims) {
+          set_status(status, ST_BAD_TREE);
+          bad = true;
+          break;
+        }
+        uint32_t orig;
+        const float t = intersect_tri(&tris[4 * (size_t)gpi], o, d, tmin, tmax, &orig);
+        if (t < tmax) {
+          hit_prim = gpi;
+          hit_mesh = mesh;
+          hit_orig = orig;
+          tmax = t;
+        }
+      }
+      if (bad) break;
+      if ((cur.y & 0xff000000u) == 0) {
+        if (sp == 0) break;
+        if (sp == tlas_sp) {
+          tlas_sp = OBVHS_INVALID;
+          mesh = OBVHS_INVALID;
+          nodes = tlas;
+          n_nodes = n_tlas;
+        }
+        sp = sp ? sp - 1 : 0;
+        cur = stack[sp];
+      }
+    }
+    if (bad) hit_prim = OBVHS_INVALID;
+    hits[ri] = hit_prim == OBVHS_INVALID
+                   ? make_uint4(OBVHS_INVALID, OBVHS_INVALID, OBVHS_INVALID, 0x7f800000u)
+                   : make_uint4(hit_mesh, hit_prim, hit_orig, __float_as_uint(tmax));
+  }
+}
+
 __global__ void k_reorder_tris(const float* __restrict__ tris, uint32_t n_tris, const uint32_t* __restrict__ pidx,
                                uint32_t n_prims, float4* __restrict__ out, uint32_t* status) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -252,6 +394,38 @@ int reorder_tris_device(BuildCtx& c, obvhs_cwbvh* b, const float* tris, uint32_t
                                                                           out, c.d_status));
   CK(cudaGetLastError());
   b->tris = out;
+  return 0;
+}
+
+int traverse_tlas_device(BuildCtx& c, const obvhs_cwbvh* tlas, const obvhs_cwbvh* const* blas, uint32_t n_blas,
+                         const float* rays, uint32_t n, uint32_t* hits4) {
+  if (n == 0) return 0;
+  for (uint32_t b = 0; b < n_blas; b++) {
+    if (!blas[b]) return c.fail(OBVHS_ERR_INVALID_ARG, "null BLAS handle");
+    if (blas[b]->n_nodes && !blas[b]->tris) return c.fail(OBVHS_ERR_INVALID_ARG, "a BLAS has no triangles attached");
+  }
+  BlasDesc* dd = (BlasDesc*)c.scratch.get(SLOT_BLAS_DESC, (size_t)std::max(n_blas, 1u) * sizeof(BlasDesc));
+  uint32_t* counter = (uint32_t*)c.scratch.get(SLOT_OUTPUT, 16);
+  if (!dd || !counter) return c.fail(OBVHS_ERR_OOM, "scratch");
+  if (n_blas) {
+    // pageable source: the copy has consumed it when the call returns
+    std::vector<BlasDesc> hd(n_blas);
+    for (uint32_t b = 0; b < n_blas; b++)
+      hd[b] = BlasDesc{blas[b]->nodes, blas[b]->tris, blas[b]->n_nodes, blas[b]->n_prims};
+    CK(cudaMemcpyAsync(dd, hd.data(), (size_t)n_blas * sizeof(BlasDesc), cudaMemcpyHostToDevice, c.stream));
+  }
+  CK(cudaMemsetAsync(counter, 0, 4, c.stream));
+  static int per_sm = 0;
+  if (!per_sm) {
+    int a = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_traverse_tlas, TBLK, 0);
+    per_sm = std::max(1, a);
+  }
+  const uint32_t grid = std::min<uint32_t>(div_up<uint32_t>(n, TBLK), (uint32_t)(per_sm * c.num_sms));
+  KLAUNCH("k_traverse_tlas", k_traverse_tlas<<<grid, TBLK, 0, c.stream>>>(tlas->nodes, tlas->n_nodes, tlas->prim_indices,
+                                                                        tlas->n_prims, dd, n_blas, (const float4*)rays,
+                                                                        n, (uint4*)hits4, counter, c.d_status));
+  CK(cudaGetLastError());
   return 0;
 }
 

@@ -1702,6 +1702,132 @@ void orc_traverse(int32_t mode, const void* nodes80, uint64_t n_nodes, const uin
   }
 }
 
+// Instance traversal: CwBvh::ray_traverse_tlas_blas (src/cwbvh/mod.rs:342-491)
+// with Triangle::intersect as the closure.  One group stack (32 entries,
+// StackStack clamping) serves the TLAS and the BLAS; entering a BLAS records
+// the stack length, and traversal returns to the TLAS when the stack is back
+// at that length.  As in the reference, a TLAS leaf group's remaining
+// instances are pushed as a primitive group and dropped when popped (a popped
+// group without node bits is cleared), and the ray is not transformed.
+struct Blas {
+  const CwNode* nodes;
+  uint32_t n_nodes;
+  const uint32_t* pidx;
+  const Tri* tris;  // original order
+};
+
+inline uint32_t traverse_tlas(const CwNode* tlas, uint32_t n_tlas, const uint32_t* tlas_pidx, const Blas* blas,
+                              uint32_t n_blas, Ray ray, uint32_t* mesh_out, float* t_out) {
+  Grp stack[32];
+  size_t sp = 0;
+  const uint32_t INV = INVALID32;
+  uint32_t tlas_stack_size = INV, current_mesh = INV;
+  const CwNode* nodes = tlas;
+  uint32_t n_nodes = n_tlas;
+  uint32_t hit_prim = INV, hit_mesh = INV;
+  const uint32_t oct = octant_inv4(ray.d);
+  Grp cur{0, 0x80000000u};
+  if (n_tlas == 0) cur = Grp{0, 0};
+  for (;;) {
+    Grp prim{0, 0};
+    if (cur.y & 0xff000000u) {
+      const uint32_t hits_imask = cur.y;
+      const uint32_t cio = fbh(hits_imask);
+      const uint32_t base = cur.x;
+      cur.y &= ~(1u << cio);
+      if (cur.y & 0xff000000u) {
+        stack[sp] = cur;
+        sp = std::min<size_t>(sp + 1, 31);
+      }
+      const uint32_t slot = (cio - 24) ^ (oct & 0xffu);
+      const uint32_t rel = (uint32_t)__builtin_popcount(hits_imask & ~(0xffffffffu << slot));
+      const uint32_t ni = base + rel;
+      if (ni >= n_nodes) return INV;  // malformed tree (the reference would index out of range)
+      const CwNode& node = nodes[ni];
+      const uint32_t hm = node_intersect(node, ray, ray.tmax, oct);
+      cur.x = node.child_base_idx;
+      prim.x = node.primitive_base_idx;
+      cur.y = (hm & 0xff000000u) | (uint32_t)node.imask;
+      prim.y = hm & 0x00ffffffu;
+    } else {
+      cur = Grp{0, 0};
+    }
+    while (prim.y != 0) {
+      const uint32_t lpi = fbh(prim.y);
+      prim.y &= ~(1u << lpi);
+      const uint32_t gpi = prim.x + lpi;
+      if (tlas_stack_size == INV) {
+        if (prim.y != 0) {
+          stack[sp] = prim;
+          sp = std::min<size_t>(sp + 1, 31);
+        }
+        if (cur.y & 0xff000000u) {
+          stack[sp] = cur;
+          sp = std::min<size_t>(sp + 1, 31);
+        }
+        tlas_stack_size = (uint32_t)sp;
+        const uint32_t b = tlas_pidx[gpi];
+        if (b >= n_blas) return INV;
+        nodes = blas[b].nodes;
+        n_nodes = blas[b].n_nodes;
+        current_mesh = b;
+        cur = Grp{0, 0x80000000u};
+        break;
+      } else {
+        const Blas& bl = blas[current_mesh];
+        const float t = tri_intersect(bl.tris[bl.pidx[gpi]], ray, ray.tmax);
+        if (t < ray.tmax) {
+          hit_prim = gpi;
+          hit_mesh = current_mesh;
+          ray.tmax = t;
+        }
+      }
+    }
+    if ((cur.y & 0xff000000u) == 0) {
+      if (sp == 0) break;
+      if ((uint32_t)sp == tlas_stack_size) {
+        tlas_stack_size = INV;
+        current_mesh = INV;
+        nodes = tlas;
+        n_nodes = n_tlas;
+      }
+      sp = sp ? sp - 1 : 0;
+      cur = stack[sp];
+    }
+  }
+  *mesh_out = hit_mesh;
+  *t_out = hit_prim != INV ? ray.tmax : INFINITY;
+  return hit_prim;
+}
+
+// hits: n x (geometry id, BVH-order primitive id in that BLAS, original
+// primitive id, t bits); 0xffffffff ids and +inf for a miss.  BLAS triangles
+// are given in original order.
+void orc_traverse_tlas(const void* tlas80, uint64_t n_tlas, const uint32_t* tlas_pidx, uint32_t n_blas,
+                       const void* const* blas_nodes80, const uint64_t* blas_n_nodes, const uint32_t* const* blas_pidx,
+                       const float* const* blas_tris, const uint64_t* blas_n_tris, const float* rays8, uint64_t nrays,
+                       uint32_t* hits, int32_t nthreads) {
+  std::vector<std::vector<Tri>> tris(n_blas);
+  std::vector<Blas> bl(n_blas);
+  for (uint32_t b = 0; b < n_blas; b++) {
+    tris[b] = load_tris(blas_tris[b], blas_n_tris[b]);
+    bl[b] = Blas{(const CwNode*)blas_nodes80[b], (uint32_t)blas_n_nodes[b], blas_pidx[b], tris[b].data()};
+  }
+  const CwNode* tl = (const CwNode*)tlas80;
+  parallel_for(nthreads, nrays, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; i++) {
+      const Ray r = make_ray(rays8 + 8 * i);
+      uint32_t mesh = INVALID32;
+      float t = INFINITY;
+      const uint32_t id = traverse_tlas(tl, (uint32_t)n_tlas, tlas_pidx, bl.data(), n_blas, r, &mesh, &t);
+      hits[4 * i] = id == INVALID32 ? INVALID32 : mesh;
+      hits[4 * i + 1] = id;
+      hits[4 * i + 2] = id == INVALID32 ? INVALID32 : bl[mesh].pidx[id];
+      hits[4 * i + 3] = f_bits(t);
+    }
+  });
+}
+
 // Single-triangle intersection (Triangle::intersect) for unit checks.
 float orc_tri_intersect(const float* tri9, const float* ray8) {
   Tri t = load_tris(tri9, 1)[0];

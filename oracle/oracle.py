@@ -90,6 +90,7 @@ def _declare(L):
     L.orc_build_get_bvh2.argtypes = [P, I32, P, P]
     L.orc_build_get_leaves.argtypes = [P, P, P, P, P]
     L.orc_traverse.argtypes = [I32, P, U64, P, P, U64, P, U64, P, P, I32, P]
+    L.orc_traverse_tlas.argtypes = [P, U64, P, U32, P, P, P, P, P, P, U64, P, I32]
     L.orc_tri_intersect.argtypes = [P, P]
     L.orc_tri_intersect.restype = F32
     L.orc_validate_bvh2.argtypes = [P, U64, P, U64, U32, P, U64, I32, I32, P]
@@ -262,6 +263,38 @@ def traverse(cw_nodes, cw_pidx, tris, rays, mode=0, nthreads=1, counters=False):
                        _p(hits), _p(ids), nthreads, _p(cnt) if counters else None)
     out = (hits[:, 0].copy(), hits[:, 1].copy().view(np.float32), ids)
     return out + (cnt,) if counters else out
+
+
+def traverse_tlas(tlas_nodes, tlas_pidx, blas, rays, nthreads=1):
+    """CwBvh::ray_traverse_tlas_blas (src/cwbvh/mod.rs:342-491) with
+    Triangle::intersect.  `blas` is a list of (cwbvh nodes, primitive_indices,
+    triangles in original order).  Returns (geometry id, BVH-order primitive
+    id, original primitive id, t) arrays; ids 0xffffffff and t +inf on a miss."""
+    tlas_nodes = np.ascontiguousarray(tlas_nodes, dtype=np.uint8).reshape(-1, 80)
+    tlas_pidx = np.ascontiguousarray(tlas_pidx, dtype=np.uint32)
+    keep = []
+    nodes_p, nn, pidx_p, tris_p, nt = [], [], [], [], []
+    for nodes, pidx, tris in blas:
+        nodes = np.ascontiguousarray(nodes, dtype=np.uint8).reshape(-1, 80)
+        pidx = np.ascontiguousarray(pidx, dtype=np.uint32)
+        tris = _f32(tris, 9)
+        keep += [nodes, pidx, tris]
+        nodes_p.append(nodes.ctypes.data)
+        pidx_p.append(pidx.ctypes.data)
+        tris_p.append(tris.ctypes.data)
+        nn.append(len(nodes))
+        nt.append(len(tris))
+    arr = lambda v, t: (t * max(len(v), 1))(*v)
+    rays = _f32(rays, 8)
+    n = len(rays)
+    hits = np.zeros((n, 4), np.uint32)
+    lib().orc_traverse_tlas(_p(tlas_nodes), len(tlas_nodes), _p(tlas_pidx), len(blas),
+                            ctypes.cast(arr(nodes_p, ctypes.c_void_p), ctypes.c_void_p),
+                            ctypes.cast(arr(nn, ctypes.c_uint64), ctypes.c_void_p),
+                            ctypes.cast(arr(pidx_p, ctypes.c_void_p), ctypes.c_void_p),
+                            ctypes.cast(arr(tris_p, ctypes.c_void_p), ctypes.c_void_p),
+                            ctypes.cast(arr(nt, ctypes.c_uint64), ctypes.c_void_p), _p(rays), n, _p(hits), nthreads)
+    return hits[:, 0].copy(), hits[:, 1].copy(), hits[:, 2].copy(), hits[:, 3].copy().view(np.float32)
 
 
 def tri_intersect(tri9, ray8) -> float:

@@ -177,3 +177,47 @@ def test_triangle_intersect_kats():
     assert O.tri_intersect(tri, T.make_rays([[5, 0, -2]], [[0, 0, 1]])) == np.inf
     assert O.tri_intersect(tri, T.make_rays([[0, 0, -2]], [[0, 0, 1]], tmax=1.5)) == np.inf
     assert O.tri_intersect(tri, T.make_rays([[0, 0, -2]], [[0, 0, 1]], tmin=2.5)) == np.inf
+
+
+# --- instance traversal (CwBvh::ray_traverse_tlas_blas) ---------------------
+
+import instances as I
+
+
+def test_tlas_with_one_instance_equals_plain_traversal():
+    blas_tris = I.instanced_scene(1, seed=2)
+    tl, blas = I.oracle_scene(blas_tris, 3)
+    rays = I.incoherent_rays(4000)
+    g, p, orig, t = O.traverse_tlas(tl.cw_nodes, tl.cw_pidx, blas, rays)
+    nodes, pidx, tris = blas[0]
+    oid, ot, bvh_ids = O.traverse(nodes, pidx, tris, rays, 0)
+    hit = oid != 0xFFFFFFFF
+    assert hit.any()
+    assert np.array_equal(orig, oid) and np.array_equal(p, bvh_ids)
+    assert np.array_equal(t.view(np.uint32), ot.view(np.uint32))
+    assert np.array_equal(g[hit], np.zeros(hit.sum(), np.uint32))
+
+
+def test_tlas_hits_are_the_closest_hit_of_the_reported_instance():
+    """Each reported hit is the closest hit of its own BLAS (the instance was
+    entered with a tmax no smaller than that hit), and never nearer than the
+    closest over all instances.  The reference does not visit every instance
+    a ray reaches: after the first instance of a TLAS node's leaf group it
+    pushes the rest as a primitive group, which its loop clears when popped,
+    so the nearest instance can be skipped (misses below)."""
+    blas_tris = I.instanced_scene(8, seed=3)
+    tl, blas = I.oracle_scene(blas_tris, 1)
+    rays = I.incoherent_rays(4000, seed=4)
+    g, p, orig, t = O.traverse_tlas(tl.cw_nodes, tl.cw_pidx, blas, rays)
+    per = [O.traverse(nodes, pidx, tris, rays, 0) for nodes, pidx, tris in blas]
+    best_t = np.min(np.stack([x[1] for x in per]), axis=0)
+    hit = g != 0xFFFFFFFF
+    assert hit.sum() > 100
+    assert np.all(t[hit] >= best_t[hit])
+    for b in range(len(blas)):
+        sel = g == b
+        oid, ot, bvh = per[b]
+        assert np.array_equal(t[sel].view(np.uint32), ot[sel].view(np.uint32))
+        assert np.array_equal(orig[sel], oid[sel]) and np.array_equal(p[sel], bvh[sel])
+    assert np.all(np.isinf(t[~hit]))
+    assert (t > best_t).any()  # instances skipped as in the reference
