@@ -239,9 +239,16 @@ def arch_scene(ctx, stream, steps, warmup, flush):
         ctx.check(lib.obvhs_ray_traverse_miss(ctx.h, cw.h, ctypes.c_void_p(ds.data_ptr()), len(shadow),
                                               ctypes.c_void_p(miss.data_ptr()), 1))
 
+    def trace_ctri():
+        ctx.check(lib.obvhs_ray_traverse_compressed(ctx.h, cw.h, ctypes.c_void_p(dc.data_ptr()), len(closest),
+                                                    ctypes.c_void_p(out.data_ptr()), 1))
+
+    cw.set_triangles_compressed(d)
     for _ in range(warmup):
         trace()
         occlude()
+        trace_ctri()
+    cc_ms = timed(trace_ctri, steps)
     c_ms = timed(trace, steps)
     s_ms = timed(occlude, steps)
     n = len(tris)
@@ -251,6 +258,7 @@ def arch_scene(ctx, stream, steps, warmup, flush):
             "build_medium_build_ms": medium_ms, "build_medium_build_mtris_s": n / (medium_ms * 1e-3) / 1e6,
             "incoherent_closest_mrays_s": len(closest) / (c_ms * 1e-3) / 1e6, "incoherent_closest_ms": c_ms,
             "shadow_any_hit_mrays_s": len(shadow) / (s_ms * 1e-3) / 1e6, "shadow_any_hit_ms": s_ms,
+            "incoherent_closest_compressed_tris_mrays_s": len(closest) / (cc_ms * 1e-3) / 1e6,
             "hit_fraction": float((out[:, 0] != -1).float().mean().item())}
 
 

@@ -195,6 +195,22 @@ OBVHS_API int obvhs_ray_traverse(obvhs_ctx* ctx, const obvhs_cwbvh* bvh, const o
 OBVHS_API int obvhs_ray_traverse_miss(obvhs_ctx* ctx, const obvhs_cwbvh* bvh, const obvhs_ray* rays, uint32_t n, uint8_t* miss,
                             int device_ptrs);
 
+/* RtCompressedTriangle (src/rt_triangle.rs:13-135): 24-byte triangles (v0 in
+ * f32, e1 = v1 - v0 and e2 = v2 - v0 as IEEE halves, interleaved
+ * e1x e2x e1y e2y e1z e2z) built from float[n][9] triangles in original order
+ * and stored in primitive_indices order, for traversal with
+ * RtCompressedTriangle::intersect.  Download returns the 24-byte records. */
+OBVHS_API int obvhs_cwbvh_set_triangles_compressed(obvhs_ctx* ctx, obvhs_cwbvh* bvh, const float* triangles, uint32_t n,
+                                                   int device_ptrs);
+OBVHS_API int obvhs_cwbvh_download_compressed(obvhs_ctx* ctx, const obvhs_cwbvh* bvh, void* tris24);
+/* CwBvh::ray_traverse / ray_traverse_miss with RtCompressedTriangle::intersect
+ * as the closure (src/cwbvh/mod.rs:169-225, src/rt_triangle.rs:70-117);
+ * hits hold the original primitive id as in obvhs_ray_traverse. */
+OBVHS_API int obvhs_ray_traverse_compressed(obvhs_ctx* ctx, const obvhs_cwbvh* bvh, const obvhs_ray* rays, uint32_t n,
+                                            obvhs_hit* hits, int device_ptrs);
+OBVHS_API int obvhs_ray_traverse_miss_compressed(obvhs_ctx* ctx, const obvhs_cwbvh* bvh, const obvhs_ray* rays,
+                                                 uint32_t n, uint8_t* miss, int device_ptrs);
+
 /* CwBvh::ray_traverse_tlas_blas (src/cwbvh/mod.rs:342-491) with
  * Triangle::intersect as the closure: `tlas` is a CWBVH over instance boxes
  * whose primitive_indices name entries of `blas` (each with triangles

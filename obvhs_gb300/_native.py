@@ -91,6 +91,10 @@ SIGNATURES = {
     "obvhs_ray_traverse": (I32, [P, P, P, U32, P, I32]),
     "obvhs_ray_traverse_miss": (I32, [P, P, P, U32, P, I32]),
     "obvhs_ray_traverse_tlas_blas": (I32, [P, P, P, U32, P, U32, P, I32]),
+    "obvhs_cwbvh_set_triangles_compressed": (I32, [P, P, P, U32, I32]),
+    "obvhs_cwbvh_download_compressed": (I32, [P, P, P]),
+    "obvhs_ray_traverse_compressed": (I32, [P, P, P, U32, P, I32]),
+    "obvhs_ray_traverse_miss_compressed": (I32, [P, P, P, U32, P, I32]),
     "obvhs_morton_sort": (I32, [P, P, U32, U32, P, P]),
     "obvhs_morton_sort_noalloc": (I32, [P, U32, U32, P, P, P]),
 }

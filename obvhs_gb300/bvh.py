@@ -366,6 +366,36 @@ class CwBvh:
             return out
         return out.astype(bool)
 
+    def set_triangles_compressed(self, triangles):
+        """Attach RtCompressedTriangle records (src/rt_triangle.rs:13-47) built
+        from float (n, 9) triangles in original order."""
+        p, n, dev, keep = _prep(triangles, np.float32, 9)
+        self.ctx.check(self.ctx.lib.obvhs_cwbvh_set_triangles_compressed(self.ctx.h, self.h, p, n, dev))
+        del keep
+
+    def download_compressed(self) -> np.ndarray:
+        """The attached RtCompressedTriangle records, (n_prims, 24) bytes."""
+        _, npr, _ = self.info()
+        out = np.zeros((npr, 24), np.uint8)
+        self.ctx.check(self.ctx.lib.obvhs_cwbvh_download_compressed(self.ctx.h, self.h,
+                                                                    out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def ray_traverse_compressed(self, rays, out=None):
+        """ray_traverse with RtCompressedTriangle::intersect (see ray_traverse)."""
+        out = self._trav(rays, out, self.ctx.lib.obvhs_ray_traverse_compressed, 8)
+        if _is_cuda_tensor(out):
+            return out.view(-1, 2)
+        o = out.reshape(-1, 2)
+        return o[:, 0].copy(), o[:, 1].copy().view(np.float32)
+
+    def ray_traverse_miss_compressed(self, rays, out=None):
+        """ray_traverse_miss with RtCompressedTriangle::intersect."""
+        out = self._trav(rays, out, self.ctx.lib.obvhs_ray_traverse_miss_compressed, 1)
+        if _is_cuda_tensor(out):
+            return out
+        return out.astype(bool)
+
     def ray_traverse_tlas_blas(self, blas, rays, out=None):
         """CwBvh::ray_traverse_tlas_blas (src/cwbvh/mod.rs:342-491): this CWBVH
         is the TLAS over instance boxes, its primitive_indices index `blas`

@@ -614,11 +614,35 @@ int obvhs_cwbvh_set_triangles(obvhs_ctx* cp, obvhs_cwbvh* b, const float* triang
   return r;
 }
 
+int obvhs_cwbvh_set_triangles_compressed(obvhs_ctx* cp, obvhs_cwbvh* b, const float* triangles, uint32_t n,
+                                         int device_ptrs) {
+  if (!cp || !b || (n && !triangles)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  int err = 0;
+  const float* dt = (const float*)stage_in(c, SLOT_INPUT, triangles, (size_t)n * 36, device_ptrs, &err);
+  if (err) return err;
+  int r = compress_tris_device(c, b, dt, n);
+  if (!r) r = take_status(c);
+  return r;
+}
+
+int obvhs_cwbvh_download_compressed(obvhs_ctx* cp, const obvhs_cwbvh* b, void* tris24) {
+  if (!cp || !b || (b->n_prims && !tris24)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  if (b->n_prims && !b->ctris) return c.fail(OBVHS_ERR_INVALID_ARG, "no compressed triangles attached to the CWBVH");
+  if (b->n_prims) CK(cudaMemcpyAsync(tris24, b->ctris, (size_t)b->n_prims * 24, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return OBVHS_OK;
+}
+
 int obvhs_cwbvh_free(obvhs_cwbvh* b) {
   if (!b) return OBVHS_OK;
   if (b->nodes) cudaFree(b->nodes);
   if (b->prim_indices) cudaFree(b->prim_indices);
   if (b->tris) cudaFree(b->tris);
+  if (b->ctris) cudaFree(b->ctris);
   delete b;
   return OBVHS_OK;
 }
@@ -626,7 +650,7 @@ int obvhs_cwbvh_free(obvhs_cwbvh* b) {
 // ---- traversal ---------------------------------------------------------------
 
 static int traverse_common(obvhs_ctx* cp, const obvhs_cwbvh* b, const obvhs_ray* rays, uint32_t n, void* out,
-                           int device_ptrs, int mode) {
+                           int device_ptrs, int mode, bool compressed = false) {
   if (!cp || !b || (n && (!rays || !out))) return OBVHS_ERR_INVALID_ARG;
   BuildCtx& c = *cp;
   DeviceGuard g(c.device);
@@ -639,8 +663,10 @@ static int traverse_common(obvhs_ctx* cp, const obvhs_cwbvh* b, const obvhs_ray*
     dout = c.scratch.get(SLOT_TRAV_OUT, ob + 16);
     if (!dout) return c.fail(OBVHS_ERR_OOM, "output staging");
   }
-  int r = traverse_device(c, b, dr, n, mode == 0 ? (uint32_t*)dout : nullptr, mode == 1 ? (uint8_t*)dout : nullptr,
-                          mode);
+  int r = compressed ? traverse_compressed_device(c, b, dr, n, mode == 0 ? (uint32_t*)dout : nullptr,
+                                                  mode == 1 ? (uint8_t*)dout : nullptr, mode)
+                     : traverse_device(c, b, dr, n, mode == 0 ? (uint32_t*)dout : nullptr,
+                                       mode == 1 ? (uint8_t*)dout : nullptr, mode);
   if (r) return r;
   if (!device_ptrs && n) CK(cudaMemcpyAsync(out, dout, ob, cudaMemcpyDeviceToHost, c.stream));
   if (!device_ptrs) return take_status(c);
@@ -655,6 +681,16 @@ int obvhs_ray_traverse(obvhs_ctx* cp, const obvhs_cwbvh* b, const obvhs_ray* ray
 int obvhs_ray_traverse_miss(obvhs_ctx* cp, const obvhs_cwbvh* b, const obvhs_ray* rays, uint32_t n, uint8_t* miss,
                             int device_ptrs) {
   return traverse_common(cp, b, rays, n, miss, device_ptrs, 1);
+}
+
+int obvhs_ray_traverse_compressed(obvhs_ctx* cp, const obvhs_cwbvh* b, const obvhs_ray* rays, uint32_t n,
+                                  obvhs_hit* hits, int device_ptrs) {
+  return traverse_common(cp, b, rays, n, hits, device_ptrs, 0, true);
+}
+
+int obvhs_ray_traverse_miss_compressed(obvhs_ctx* cp, const obvhs_cwbvh* b, const obvhs_ray* rays, uint32_t n,
+                                       uint8_t* miss, int device_ptrs) {
+  return traverse_common(cp, b, rays, n, miss, device_ptrs, 1, true);
 }
 
 int obvhs_ray_traverse_tlas_blas(obvhs_ctx* cp, const obvhs_cwbvh* tlas, const obvhs_cwbvh* const* blas, uint32_t n_blas,

@@ -195,8 +195,9 @@ struct obvhs_cwbvh {
   uint32_t* prim_indices = nullptr;
   uint32_t n_prims = 0;
   float total_aabb[6] = {0, 0, 0, 0, 0, 0};
-  float4* tris = nullptr;  // BVH order: (v0, id) (v0-v1) (v2-v0), 48 B each
+  float4* tris = nullptr;  // BVH order: (v0, id) (v0-v1, n.x) (v2-v0, n.y) (n.z), 64 B each
   uint32_t n_tris = 0;
+  uint2* ctris = nullptr;  // BVH order: RtCompressedTriangle, 24 B each (three 8-byte words)
   int uses_spatial_splits = 0;
 };
 
@@ -237,6 +238,11 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
 int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint32_t n, uint32_t* hits,
                     uint8_t* miss, int mode);
 int reorder_tris_device(BuildCtx& c, obvhs_cwbvh* bvh, const float* tris, uint32_t n_tris);
+// RtCompressedTriangle records (24 B) of the triangles in BVH order.
+int compress_tris_device(BuildCtx& c, obvhs_cwbvh* bvh, const float* tris, uint32_t n_tris);
+// Traversal on the compressed triangles (mode 0 closest hit, 1 occlusion).
+int traverse_compressed_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint32_t n, uint32_t* hits,
+                               uint8_t* miss, int mode);
 // hits4: n x (geometry id, BVH-order primitive id, original id, t bits)
 int traverse_tlas_device(BuildCtx& c, const obvhs_cwbvh* tlas, const obvhs_cwbvh* const* blas, uint32_t n_blas,
                          const float* rays, uint32_t n, uint32_t* hits4);

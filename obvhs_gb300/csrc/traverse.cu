@@ -18,6 +18,8 @@
 // the values Triangle::intersect computes per test.  Rays are 32 bytes
 // (origin, tmin, dir, tmax); results are 8 bytes (original id, t).
 // Persistent warps take 32 rays at a time from a global counter.
+#include <cuda_fp16.h>
+
 #include <vector>
 
 #include "build.h"
@@ -118,12 +120,43 @@ __device__ __forceinline__ float intersect_tri(const float4* tri, float3 o, floa
   return __int_as_float(0x7f800000);
 }
 
-template <int MODE>  // 0 closest hit, 1 occlusion
+// RtCompressedTriangle::intersect (src/rt_triangle.rs:70-117): v0 in f32,
+// e1 = v1 - v0 and e2 = v2 - v0 as IEEE half floats, stored interleaved
+// (e1x, e2x, e1y, e2y, e1z, e2z) after v0; ng = (-e1) x e2.
+__device__ __forceinline__ float h2f(uint32_t bits16) { return __half2float(__ushort_as_half((unsigned short)bits16)); }
+
+__device__ __forceinline__ float intersect_ctri(const uint2* rec, float3 o, float3 d, float tmin, float tmax) {
+  const uint2 a = __ldg(rec), b = __ldg(rec + 1), w2 = __ldg(rec + 2);
+  const float3 v0 = make_float3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(b.x));
+  const float3 e1 = make_float3(h2f(b.y & 0xffffu), h2f(w2.x & 0xffffu), h2f(w2.y & 0xffffu));
+  const float3 e2 = make_float3(h2f(b.y >> 16), h2f(w2.x >> 16), h2f(w2.y >> 16));
+  const float3 ne1 = make_float3(-e1.x, -e1.y, -e1.z);
+  const float3 ng = make_float3(ne1.y * e2.z - ne1.z * e2.y, ne1.z * e2.x - ne1.x * e2.z, ne1.x * e2.y - ne1.y * e2.x);
+  const float3 c = make_float3(v0.x - o.x, v0.y - o.y, v0.z - o.z);
+  const float3 r = make_float3(d.y * c.z - d.z * c.y, d.z * c.x - d.x * c.z, d.x * c.y - d.y * c.x);
+  const float inv_det = 1.0f / ((ng.x * d.x + ng.y * d.y) + ng.z * d.z);
+  const float u = ((r.x * e2.x + r.y * e2.y) + r.z * e2.z) * inv_det;
+  const float v = ((r.x * ne1.x + r.y * ne1.y) + r.z * ne1.z) * inv_det;
+  const float w = (1.0f - u) - v;
+  const uint32_t h = __float_as_uint(u) | __float_as_uint(v) | __float_as_uint(w);
+  if (inv_det != 0.0f && (h & 0x80000000u) == 0) {
+    const float t = ((ng.x * c.x + ng.y * c.y) + ng.z * c.z) * inv_det;
+    if (t >= tmin && t <= tmax) return t;
+  }
+  return __int_as_float(0x7f800000);
+}
+
+// MODE 0 closest hit, 1 occlusion.  CTRI: triangles as RtCompressedTriangle
+// (24 B; the hit's original id comes from primitive_indices) instead of the
+// 64-byte records.
+template <int MODE, bool CTRI = false>
 __global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ nodes, uint32_t n_nodes,
                                                    const float4* __restrict__ tris, uint32_t n_prims,
                                                    const float4* __restrict__ rays,
                                                    uint32_t nrays, uint2* __restrict__ hits, uint8_t* __restrict__ miss,
-                                                   uint32_t* __restrict__ next_ray, uint32_t* status) {
+                                                   uint32_t* __restrict__ next_ray, uint32_t* status,
+                                                   const uint2* __restrict__ ctris = nullptr,
+                                                   const uint32_t* __restrict__ pidx = nullptr) {
   const int lane = threadIdx.x & 31;
   for (;;) {
     uint32_t base = 0;
@@ -162,7 +195,13 @@ __global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ no
           break;
         }
         uint32_t orig;
-        const float t = intersect_tri(&tris[4 * (size_t)pid], o, d, tmin, MODE == 0 ? tmax : ray_tmax, &orig);
+        float t;
+        if (CTRI) {
+          t = intersect_ctri(&ctris[3 * (size_t)pid], o, d, tmin, MODE == 0 ? tmax : ray_tmax);
+          orig = pid;  // mapped through primitive_indices at the end
+        } else {
+          t = intersect_tri(&tris[4 * (size_t)pid], o, d, tmin, MODE == 0 ? tmax : ray_tmax, &orig);
+        }
         if (MODE == 0) {
           if (t < tmax) {
             hit_id = orig;
@@ -209,11 +248,32 @@ __global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ no
         cur = stack[sp];
       }
     }
+    if (CTRI && hit_id != OBVHS_INVALID) hit_id = __ldg(&pidx[hit_id]);
     if (MODE == 0)
       hits[ri] = make_uint2(hit_id, __float_as_uint(hit_t));
     else
       miss[ri] = hit_id == OBVHS_INVALID ? 1 : 0;
   }
+}
+
+// RtCompressedTriangle::new (src/rt_triangle.rs:31-47) for the triangles in
+// primitive_indices order; halves by round-to-nearest-even (f16::from_f32).
+__global__ void k_compress_tris(const float* __restrict__ tris, uint32_t n_tris, const uint32_t* __restrict__ pidx,
+                                uint32_t n_prims, uint2* __restrict__ out, uint32_t* status) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_prims) return;
+  uint32_t id = pidx[k];
+  if (id >= n_tris) {
+    set_status(status, ST_BAD_TREE);
+    id = 0;
+  }
+  const float* t = tris + (size_t)id * 9;
+  const float e1x = t[3] - t[0], e1y = t[4] - t[1], e1z = t[5] - t[2];
+  const float e2x = t[6] - t[0], e2y = t[7] - t[1], e2z = t[8] - t[2];
+  auto hb = [](float f) { return (uint32_t)__half_as_ushort(__float2half_rn(f)); };
+  out[3 * (size_t)k] = make_uint2(__float_as_uint(t[0]), __float_as_uint(t[1]));
+  out[3 * (size_t)k + 1] = make_uint2(__float_as_uint(t[2]), hb(e1x) | (hb(e2x) << 16));
+  out[3 * (size_t)k + 2] = make_uint2(hb(e1y) | (hb(e2y) << 16), hb(e1z) | (hb(e2z) << 16));
 }
 
 // CwBvh::ray_traverse_tlas_blas (src/cwbvh/mod.rs:342-491) with
@@ -425,6 +485,51 @@ int traverse_tlas_device(BuildCtx& c, const obvhs_cwbvh* tlas, const obvhs_cwbvh
   KLAUNCH("k_traverse_tlas", k_traverse_tlas<<<grid, TBLK, 0, c.stream>>>(tlas->nodes, tlas->n_nodes, tlas->prim_indices,
                                                                         tlas->n_prims, dd, n_blas, (const float4*)rays,
                                                                         n, (uint4*)hits4, counter, c.d_status));
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int compress_tris_device(BuildCtx& c, obvhs_cwbvh* b, const float* tris, uint32_t n_tris) {
+  if (b->ctris) {
+    cudaFree(b->ctris);
+    b->ctris = nullptr;
+  }
+  if (b->n_prims == 0) return 0;
+  uint2* out = nullptr;
+  if (cudaMallocAsync(&out, (size_t)b->n_prims * 24, c.stream) != cudaSuccess) {
+    cudaGetLastError();
+    return c.fail(OBVHS_ERR_OOM, "compressed triangle buffer");
+  }
+  KLAUNCH("k_compress_tris", k_compress_tris<<<div_up<uint32_t>(b->n_prims, 256), 256, 0, c.stream>>>(
+                                 tris, n_tris, b->prim_indices, b->n_prims, out, c.d_status));
+  CK(cudaGetLastError());
+  b->ctris = out;
+  return 0;
+}
+
+int traverse_compressed_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint32_t n, uint32_t* hits,
+                               uint8_t* miss, int mode) {
+  if (n == 0) return 0;
+  if (bvh->n_nodes && !bvh->ctris) return c.fail(OBVHS_ERR_INVALID_ARG, "no compressed triangles attached to the CWBVH");
+  uint32_t* counter = (uint32_t*)c.scratch.get(SLOT_OUTPUT, 16);
+  if (!counter) return c.fail(OBVHS_ERR_OOM, "scratch");
+  CK(cudaMemsetAsync(counter, 0, 4, c.stream));
+  static int per_sm = 0;
+  if (!per_sm) {
+    int a = 0, b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_traverse<0, true>, TBLK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_traverse<1, true>, TBLK, 0);
+    per_sm = std::max(1, std::min(a, b));
+  }
+  const uint32_t grid = std::min<uint32_t>(div_up<uint32_t>(n, TBLK), (uint32_t)(per_sm * c.num_sms));
+  if (mode == 0)
+    KLAUNCH("k_traverse_closest_ctri", k_traverse<0, true><<<grid, TBLK, 0, c.stream>>>(
+                                           bvh->nodes, bvh->n_nodes, nullptr, bvh->n_prims, (const float4*)rays, n,
+                                           (uint2*)hits, nullptr, counter, c.d_status, bvh->ctris, bvh->prim_indices));
+  else
+    KLAUNCH("k_traverse_occluded_ctri", k_traverse<1, true><<<grid, TBLK, 0, c.stream>>>(
+                                            bvh->nodes, bvh->n_nodes, nullptr, bvh->n_prims, (const float4*)rays, n,
+                                            nullptr, miss, counter, c.d_status, bvh->ctris, bvh->prim_indices));
   CK(cudaGetLastError());
   return 0;
 }

@@ -1702,6 +1702,180 @@ void orc_traverse(int32_t mode, const void* nodes80, uint64_t n_nodes, const uin
   }
 }
 
+}  // extern "C" (C++ helpers follow)
+
+// RtCompressedTriangle (src/rt_triangle.rs:13-135).  Halves are IEEE binary16
+// with round-to-nearest-even from f32 (the `half` crate's f16::from_f32),
+// restated here from the binary formats.
+inline uint16_t f32_to_f16(float f) {
+  const uint32_t x = f_bits(f);
+  const uint32_t sign = (x >> 16) & 0x8000u;
+  const uint32_t exp = (x >> 23) & 0xffu;
+  uint32_t man = x & 0x7fffffu;
+  if (exp == 0xffu) return (uint16_t)(sign | 0x7c00u | (man ? (0x200u | (man >> 13)) : 0u));
+  const int e = (int)exp - 127 + 15;
+  if (e >= 31) return (uint16_t)(sign | 0x7c00u);
+  if (e <= 0) {
+    if (e < -10) return (uint16_t)sign;
+    man |= 0x800000u;
+    const int shift = 14 - e;
+    uint32_t hm = man >> shift;
+    const uint32_t rem = man & ((1u << shift) - 1u), halfway = 1u << (shift - 1);
+    if (rem > halfway || (rem == halfway && (hm & 1u))) hm++;
+    return (uint16_t)(sign | hm);
+  }
+  uint32_t h = sign | ((uint32_t)e << 10) | (man >> 13);
+  const uint32_t rem = man & 0x1fffu;
+  if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h++;
+  return (uint16_t)h;
+}
+
+inline float f16_to_f32(uint16_t h) {
+  const uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
+  const uint32_t exp = (h >> 10) & 0x1fu;
+  uint32_t man = h & 0x3ffu;
+  if (exp == 0x1fu) return f_from_bits(sign | 0x7f800000u | (man << 13));
+  if (exp == 0) {
+    if (man == 0) return f_from_bits(sign);
+    // subnormal: value = man * 2^-24
+    int e = -1;
+    do {
+      e++;
+      man <<= 1;
+    } while ((man & 0x400u) == 0);
+    return f_from_bits(sign | (uint32_t)(127 - 15 - e) << 23 | ((man & 0x3ffu) << 13));
+  }
+  return f_from_bits(sign | ((exp + 112u) << 23) | (man << 13));
+}
+
+struct CTri {
+  float v0[3];
+  uint16_t e[6];  // e1x e2x e1y e2y e1z e2z
+};
+static_assert(sizeof(CTri) == 24, "RtCompressedTriangle is 24 bytes");
+
+inline CTri compress_tri(const Tri& t) {
+  const V3 e1 = t.v1 - t.v0, e2 = t.v2 - t.v0;
+  CTri c;
+  c.v0[0] = t.v0.x;
+  c.v0[1] = t.v0.y;
+  c.v0[2] = t.v0.z;
+  c.e[0] = f32_to_f16(e1.x);
+  c.e[1] = f32_to_f16(e2.x);
+  c.e[2] = f32_to_f16(e1.y);
+  c.e[3] = f32_to_f16(e2.y);
+  c.e[4] = f32_to_f16(e1.z);
+  c.e[5] = f32_to_f16(e2.z);
+  return c;
+}
+
+inline float ctri_intersect(const CTri& t, const Ray& r, float tmax) {
+  const V3 v0 = v3(t.v0[0], t.v0[1], t.v0[2]);
+  const V3 e1 = v3(f16_to_f32(t.e[0]), f16_to_f32(t.e[2]), f16_to_f32(t.e[4]));
+  const V3 e2 = v3(f16_to_f32(t.e[1]), f16_to_f32(t.e[3]), f16_to_f32(t.e[5]));
+  const V3 ne1 = v3(-e1.x, -e1.y, -e1.z);
+  const V3 ng = cross(ne1, e2);
+  const V3 c = v0 - r.o;
+  const V3 rr = cross(r.d, c);
+  const float inv_det = 1.0f / dot(ng, r.d);
+  const float u = dot(rr, e2) * inv_det;
+  const float v = dot(rr, ne1) * inv_det;
+  const float w = 1.0f - u - v;
+  const uint32_t h = f_bits(u) | f_bits(v) | f_bits(w);
+  if (inv_det != 0.0f && (h & 0x80000000u) == 0) {
+    const float tt = dot(ng, c) * inv_det;
+    if (tt >= r.tmin && tt <= tmax) return tt;
+  }
+  return INFINITY;
+}
+
+// The traverse! loop of traverse<MODE> with compressed triangles laid out in
+// primitive_indices order (the reference's direct layout).
+template <int MODE>
+inline uint32_t traverse_ctri(const CwNode* nodes, uint32_t n_nodes, const CTri* ctris, const Ray& ray, float* t_out) {
+  float tmax = ray.tmax;
+  uint32_t hit_id = INVALID32;
+  float hit_t = INFINITY;
+  Grp stack[32];
+  size_t sp = 0;
+  Grp cur = n_nodes ? Grp{0, 0x80000000u} : Grp{0, 0};
+  Grp prim{0, 0};
+  const uint32_t oct = octant_inv4(ray.d);
+  for (;;) {
+    while (prim.y != 0) {
+      const uint32_t lpi = fbh(prim.y);
+      prim.y &= ~(1u << lpi);
+      const uint32_t pid = prim.x + lpi;
+      const float t = ctri_intersect(ctris[pid], ray, MODE == 0 ? tmax : ray.tmax);
+      if (MODE == 0) {
+        if (t < tmax) {
+          hit_id = pid;
+          hit_t = t;
+          tmax = t;
+        }
+      } else if (t < ray.tmax) {
+        *t_out = t;
+        return pid;
+      }
+    }
+    prim = Grp{0, 0};
+    if (cur.y & 0xff000000u) {
+      const uint32_t hits_imask = cur.y;
+      const uint32_t cio = fbh(hits_imask);
+      const uint32_t base = cur.x;
+      cur.y &= ~(1u << cio);
+      if (cur.y & 0xff000000u) {
+        stack[sp] = cur;
+        sp = std::min<size_t>(sp + 1, 31);
+      }
+      const uint32_t slot = (cio - 24) ^ (oct & 0xffu);
+      const uint32_t rel = (uint32_t)__builtin_popcount(hits_imask & ~(0xffffffffu << slot));
+      const CwNode& node = nodes[base + rel];
+      const uint32_t hm = node_intersect(node, ray, MODE == 0 ? tmax : ray.tmax, oct);
+      cur.x = node.child_base_idx;
+      prim.x = node.primitive_base_idx;
+      cur.y = (hm & 0xff000000u) | (uint32_t)node.imask;
+      prim.y = hm & 0x00ffffffu;
+    } else {
+      cur = Grp{0, 0};
+    }
+    if (prim.y == 0 && (cur.y & 0xff000000u) == 0) {
+      if (sp == 0) break;
+      sp = sp ? sp - 1 : 0;
+      cur = stack[sp];
+    }
+  }
+  *t_out = hit_t;
+  return hit_id;
+}
+
+extern "C" {
+
+// Compressed records (24 B each) of tris (original order) in pidx order.
+void orc_compress_tris(const float* tris, uint64_t n_tris, const uint32_t* pidx, uint64_t n_prims, void* out24) {
+  std::vector<Tri> t = load_tris(tris, n_tris);
+  CTri* o = (CTri*)out24;
+  for (uint64_t k = 0; k < n_prims; k++) o[k] = compress_tri(t[pidx[k]]);
+}
+
+// Traversal with RtCompressedTriangle::intersect; ctris in pidx order.
+// hits: n x (original prim id or 0xffffffff, t bits).
+void orc_traverse_compressed(int32_t mode, const void* nodes80, uint64_t n_nodes, const uint32_t* pidx,
+                             const void* ctris24, const float* rays8, uint64_t nrays, uint32_t* hits, int32_t nthreads) {
+  const CwNode* nodes = (const CwNode*)nodes80;
+  const CTri* ct = (const CTri*)ctris24;
+  parallel_for(nthreads, nrays, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; i++) {
+      const Ray r = make_ray(rays8 + 8 * i);
+      float tt = INFINITY;
+      const uint32_t id = mode == 0 ? traverse_ctri<0>(nodes, (uint32_t)n_nodes, ct, r, &tt)
+                                    : traverse_ctri<1>(nodes, (uint32_t)n_nodes, ct, r, &tt);
+      hits[2 * i] = id == INVALID32 ? INVALID32 : pidx[id];
+      hits[2 * i + 1] = f_bits(tt);
+    }
+  });
+}
+
 // Instance traversal: CwBvh::ray_traverse_tlas_blas (src/cwbvh/mod.rs:342-491)
 // with Triangle::intersect as the closure.  One group stack (32 entries,
 // StackStack clamping) serves the TLAS and the BLAS; entering a BLAS records

@@ -91,6 +91,8 @@ def _declare(L):
     L.orc_build_get_leaves.argtypes = [P, P, P, P, P]
     L.orc_traverse.argtypes = [I32, P, U64, P, P, U64, P, U64, P, P, I32, P]
     L.orc_traverse_tlas.argtypes = [P, U64, P, U32, P, P, P, P, P, P, U64, P, I32]
+    L.orc_compress_tris.argtypes = [P, U64, P, U64, P]
+    L.orc_traverse_compressed.argtypes = [I32, P, U64, P, P, P, U64, P, I32]
     L.orc_tri_intersect.argtypes = [P, P]
     L.orc_tri_intersect.restype = F32
     L.orc_validate_bvh2.argtypes = [P, U64, P, U64, U32, P, U64, I32, I32, P]
@@ -263,6 +265,30 @@ def traverse(cw_nodes, cw_pidx, tris, rays, mode=0, nthreads=1, counters=False):
                        _p(hits), _p(ids), nthreads, _p(cnt) if counters else None)
     out = (hits[:, 0].copy(), hits[:, 1].copy().view(np.float32), ids)
     return out + (cnt,) if counters else out
+
+
+def compress_tris(tris, pidx):
+    """RtCompressedTriangle::new (src/rt_triangle.rs:31-47) of tris (original
+    order) laid out in pidx order: (n, 24) bytes."""
+    tris = _f32(tris, 9)
+    pidx = np.ascontiguousarray(pidx, dtype=np.uint32)
+    out = np.zeros((len(pidx), 24), np.uint8)
+    lib().orc_compress_tris(_p(tris), len(tris), _p(pidx), len(pidx), _p(out))
+    return out
+
+
+def traverse_compressed(cw_nodes, cw_pidx, ctris24, rays, mode=0, nthreads=1):
+    """ray_traverse (mode 0) / ray_traverse_miss (mode 1) with
+    RtCompressedTriangle::intersect; ctris24 in primitive_indices order.
+    Returns (original ids or 0xffffffff, t)."""
+    cw_nodes = np.ascontiguousarray(cw_nodes, dtype=np.uint8).reshape(-1, 80)
+    cw_pidx = np.ascontiguousarray(cw_pidx, dtype=np.uint32)
+    ctris24 = np.ascontiguousarray(ctris24, dtype=np.uint8).reshape(-1, 24)
+    rays = _f32(rays, 8)
+    hits = np.zeros((len(rays), 2), np.uint32)
+    lib().orc_traverse_compressed(mode, _p(cw_nodes), len(cw_nodes), _p(cw_pidx), _p(ctris24), _p(rays), len(rays),
+                                  _p(hits), nthreads)
+    return hits[:, 0].copy(), hits[:, 1].copy().view(np.float32)
 
 
 def traverse_tlas(tlas_nodes, tlas_pidx, blas, rays, nthreads=1):

@@ -221,3 +221,52 @@ def test_tlas_hits_are_the_closest_hit_of_the_reported_instance():
         assert np.array_equal(orig[sel], oid[sel]) and np.array_equal(p[sel], bvh[sel])
     assert np.all(np.isinf(t[~hit]))
     assert (t > best_t).any()  # instances skipped as in the reference
+
+
+# --- RtCompressedTriangle ------------------------------------------------------
+
+
+def test_compressed_triangle_halves_round_to_nearest_even():
+    """Edges go to IEEE halves with round-to-nearest-even (f16::from_f32),
+    checked against numpy's float16 conversion: normal, subnormal, overflow,
+    and exact halfway values."""
+    rng = np.random.default_rng(1)
+    vals = np.concatenate([
+        rng.normal(size=20000).astype(np.float32) * np.float32(10.0) ** rng.integers(-8, 6, 20000).astype(np.float32),
+        np.float32([0.0, -0.0, 65504.0, 65520.0, 65519.99, 1e6, -1e6, 6.1e-5, 5.96e-8, 2.98e-8, 2.9802326e-08,
+                    1e-9, 1.0 + 2.0 ** -11, 1.0 + 3 * 2.0 ** -11, 2048.0 + 1.0, 2048.0 + 3.0]),
+        (np.arange(1, 2048, dtype=np.float32) + np.float32(0.5)) * np.float32(2.0 ** -24),  # subnormal halfway
+    ]).astype(np.float32)
+    n = (len(vals) + 2) // 3 * 3
+    v = np.zeros(n, np.float32)
+    v[: len(vals)] = vals
+    e1 = v.reshape(-1, 3)
+    tris = np.zeros((len(e1), 9), np.float32)
+    tris[:, 3:6] = e1  # v0 = 0, v1 = e1, so the stored e1 is the value itself
+    ct = O.compress_tris(tris, np.arange(len(tris), dtype=np.uint32))
+    halves = ct[:, 12:24].copy().view(np.uint16).reshape(-1, 6)[:, 0::2]  # e1x, e1y, e1z
+    with np.errstate(over="ignore"):
+        expect = e1.astype(np.float16).view(np.uint16)
+    assert np.array_equal(halves, expect)
+
+
+def test_compressed_traversal_hits_large_flat_quads():
+    """Exact-in-half geometry (a 16x16 grid of unit quads at z = 0): rays straight
+    down hit the quad under them, as with full-precision triangles."""
+    qs = []
+    for i in range(16):
+        for j in range(16):
+            a, b, c, d = (i, j, 0), (i + 1, j, 0), (i + 1, j + 1, 0), (i, j + 1, 0)
+            qs += [a + b + c, a + c + d]
+    tris = np.asarray(qs, np.float32)
+    ob = O.build(tris=tris, params=BvhBuildParams.medium_build(), keep_intermediate=False)
+    ct = O.compress_tris(tris, ob.cw_pidx)
+    xs = np.float32(0.3) + np.arange(16, dtype=np.float32)
+    o = np.stack(np.meshgrid(xs, xs, indexing="ij"), -1).reshape(-1, 2)
+    o = np.concatenate([o, np.full((len(o), 1), 5, np.float32)], 1)
+    d = np.tile(np.float32([0, 0, -1]), (len(o), 1))
+    rays = T.make_rays(o.astype(np.float32), d, 0.0, np.inf)
+    cid, ct_t = O.traverse_compressed(ob.cw_nodes, ob.cw_pidx, ct, rays)
+    fid, ft, _ = O.traverse(ob.cw_nodes, ob.cw_pidx, tris, rays)
+    assert np.all(cid != 0xFFFFFFFF) and np.array_equal(cid, fid)
+    assert np.allclose(ct_t, 5.0) and np.allclose(ft, 5.0)
