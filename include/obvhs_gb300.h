@@ -222,6 +222,23 @@ OBVHS_API int obvhs_ray_traverse_tlas_blas(obvhs_ctx* ctx, const obvhs_cwbvh* tl
                                            uint32_t n_blas, const obvhs_ray* rays, uint32_t n, obvhs_tlas_hit* hits,
                                            int device_ptrs);
 
+/* ---- batched builds and traversal (many scenes) --------------------------- */
+/* No single counterpart in the reference (its builders take one scene): the
+ * batched form of build_cwbvh_from_tris (src/cwbvh/builder.rs:20-85).  Builds
+ * n_scenes independent scenes with n_ctx contexts working concurrently (one
+ * host thread and one CUDA stream each, largest scenes first); out[i] is
+ * scene i's CWBVH, byte-identical to a build of that scene alone.  On error
+ * every out[i] is freed and set to NULL and ctxs[0]'s last error says why. */
+OBVHS_API int obvhs_build_cwbvh_from_tris_batch(obvhs_ctx* const* ctxs, uint32_t n_ctx, const float* const* triangles,
+                                                const uint32_t* n_tris, uint32_t n_scenes, const obvhs_build_params* params,
+                                                int device_ptrs, obvhs_cwbvh** out, obvhs_build_stats* stats);
+/* CwBvh::ray_traverse (src/cwbvh/mod.rs:169-198) for rays of several BVHs in
+ * one launch: ray i is traced in bvhs[ray_bvh[i]] (each with triangles
+ * attached); hits as obvhs_ray_traverse, identical to per-BVH calls. */
+OBVHS_API int obvhs_ray_traverse_multi(obvhs_ctx* ctx, const obvhs_cwbvh* const* bvhs, uint32_t n_bvh,
+                                       const uint32_t* ray_bvh, const obvhs_ray* rays, uint32_t n, obvhs_hit* hits,
+                                       int device_ptrs);
+
 /* ---- stage-level access for parity checks ------------------------------- */
 /* sort_nodes_by_morton (src/ploc/mod.rs:771-847) on Bvh2Node::new(aabbs[i])
  * leaves: codes in input order (u64 pairs: lo, hi; hi = 0 for U64) and the

@@ -445,6 +445,64 @@ def bvh2_to_cwbvh(bvh2: Bvh2, max_prims_per_leaf: int, order_children: bool,
     return CwBvh(ctx, h)
 
 
+def build_cwbvh_from_tris_batch(scenes, config: BvhBuildParams, contexts) -> list:
+    """Many independent build_cwbvh_from_tris calls at once: `contexts` work
+    concurrently (one host thread and CUDA stream each), largest scenes first.
+    Each result is byte-identical to building that scene alone."""
+    contexts = list(contexts)
+    if not contexts:
+        raise ValueError("at least one context")
+    ctx = contexts[0]
+    preps = [_prep(t, np.float32, 9) for t in scenes]
+    devs = {p[2] for p in preps}
+    if len(devs) > 1:
+        raise ValueError("scenes must all be host arrays or all device tensors")
+    dev = devs.pop() if devs else 0
+    n = len(preps)
+    ptrs = (ctypes.c_void_p * max(n, 1))(*[p[0].value if isinstance(p[0], ctypes.c_void_p) else p[0] for p in preps])
+    counts = (ctypes.c_uint32 * max(n, 1))(*[p[1] for p in preps])
+    outs = (ctypes.c_void_p * max(n, 1))()
+    stats = (N.BuildStats * max(n, 1))()
+    ctxs = (ctypes.c_void_p * len(contexts))(*[c.h.value for c in contexts])
+    prm = _params(config)
+    ctx.check(ctx.lib.obvhs_build_cwbvh_from_tris_batch(ctypes.cast(ctxs, ctypes.c_void_p), len(contexts),
+                                                        ctypes.cast(ptrs, ctypes.c_void_p),
+                                                        ctypes.cast(counts, ctypes.c_void_p), n, ctypes.byref(prm),
+                                                        dev, ctypes.cast(outs, ctypes.c_void_p),
+                                                        ctypes.cast(stats, ctypes.c_void_p)))
+    if dev:
+        for c in contexts:
+            c.synchronize()
+    del preps
+    return [CwBvh(ctx, ctypes.c_void_p(outs[i]), BuildStats.from_c(stats[i])) for i in range(n)]
+
+
+def ray_traverse_multi(bvhs, ray_bvh, rays, ctx: Context | None = None, out=None):
+    """Closest hits of rays against several CWBVHs in one launch: ray i is
+    traced in bvhs[ray_bvh[i]].  Host rays: (primitive_id, t) as
+    CwBvh.ray_traverse; device rays: an int32 (n, 2) tensor."""
+    ctx = _ctx(ctx)
+    pr, n, dev, keep = _prep(rays, np.float32, 8)
+    pb, nb, devb, keepb = _prep(ray_bvh, np.uint32, 0)
+    if nb != n or devb != dev:
+        raise ValueError("ray_bvh must match rays in length and memory space")
+    arr = (ctypes.c_void_p * max(len(bvhs), 1))(*[b.h.value if isinstance(b.h, ctypes.c_void_p) else b.h for b in bvhs])
+    if out is None:
+        if dev:
+            import torch
+
+            out = torch.empty((n, 2), dtype=torch.int32, device=rays.device)
+        else:
+            out = np.zeros((n, 2), np.uint32)
+    po = ctypes.c_void_p(out.data_ptr()) if dev else out.ctypes.data_as(ctypes.c_void_p)
+    ctx.check(ctx.lib.obvhs_ray_traverse_multi(ctx.h, ctypes.cast(arr, ctypes.c_void_p), len(bvhs), pb, pr, n, po, dev))
+    if dev:
+        ctx.synchronize()
+        return out
+    del keep, keepb
+    return out[:, 0].copy(), out[:, 1].copy().view(np.float32)
+
+
 def _params(p: BvhBuildParams) -> N.BuildParams:
     return N.BuildParams(int(bool(p.pre_split)), int(p.ploc_search_distance), int(p.search_depth_threshold),
                          float(p.reinsertion_batch_ratio), float(p.post_collapse_reinsertion_batch_ratio_multiplier),

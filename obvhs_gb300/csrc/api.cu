@@ -1,5 +1,9 @@
 // api.cu -- the extern "C" entry points declared in include/obvhs_gb300.h.
+#include <algorithm>
+#include <atomic>
 #include <cstring>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "build.h"
@@ -224,6 +228,37 @@ int build_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t 
 
 }  // namespace
 
+namespace {
+
+constexpr int MAX_DEVICES = 64;
+
+struct DeviceShared {
+  std::mutex m;
+  cudaStream_t coop = nullptr;
+  std::atomic<int> contexts{0};
+};
+
+DeviceShared& device_shared(int device) {
+  static DeviceShared shared[MAX_DEVICES];
+  return shared[device];
+}
+
+}  // namespace
+
+cudaError_t coop_launch(obvhs_ctx& c, const void* func, unsigned grid, unsigned block, void** args, size_t smem) {
+  DeviceShared& d = device_shared(c.device);
+  if (d.contexts.load() <= 1) return cudaLaunchCooperativeKernel(func, grid, block, args, smem, c.stream);
+  std::lock_guard<std::mutex> lock(d.m);
+  cudaError_t e = cudaSuccess;
+  if (!d.coop) e = cudaStreamCreateWithFlags(&d.coop, cudaStreamNonBlocking);
+  if (!e) e = cudaEventRecord(c.coop_ev[0], c.stream);
+  if (!e) e = cudaStreamWaitEvent(d.coop, c.coop_ev[0], 0);
+  if (!e) e = cudaLaunchCooperativeKernel(func, grid, block, args, smem, d.coop);
+  if (!e) e = cudaEventRecord(c.coop_ev[1], d.coop);
+  if (!e) e = cudaStreamWaitEvent(c.stream, c.coop_ev[1], 0);
+  return e;
+}
+
 extern "C" {
 
 int obvhs_ctx_create(int device, uint64_t hbm_budget_bytes, obvhs_ctx** out) {
@@ -242,7 +277,9 @@ int obvhs_ctx_create(int device, uint64_t hbm_budget_bytes, obvhs_ctx** out) {
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMalloc(&c->d_status, 16) != cudaSuccess || cudaMallocHost(&c->h_status, 16) != cudaSuccess ||
-      cudaMallocHost(&c->h_hist, 16 * 256 * 4) != cudaSuccess || cudaMallocHost(&c->h_small, 4096) != cudaSuccess) {
+      cudaMallocHost(&c->h_hist, 16 * 256 * 4) != cudaSuccess || cudaMallocHost(&c->h_small, 4096) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->coop_ev[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->coop_ev[1], cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
     obvhs_ctx_destroy(c);
     return OBVHS_ERR_CUDA;
@@ -254,6 +291,7 @@ int obvhs_ctx_create(int device, uint64_t hbm_budget_bytes, obvhs_ctx** out) {
     return OBVHS_ERR_CUDA;
   }
   cudaDeviceSynchronize();
+  device_shared(device).contexts.fetch_add(1);
   *out = c;
   return OBVHS_OK;
 }
@@ -262,6 +300,11 @@ int obvhs_ctx_destroy(obvhs_ctx* c) {
   if (!c) return OBVHS_OK;
   DeviceGuard g(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->coop_ev[0]) {  // created last: a context that got this far was counted
+    device_shared(c->device).contexts.fetch_sub(1);
+    cudaEventDestroy(c->coop_ev[0]);
+    if (c->coop_ev[1]) cudaEventDestroy(c->coop_ev[1]);
+  }
   c->scratch.release();
   if (c->d_status) cudaFree(c->d_status);
   if (c->h_status) cudaFreeHost(c->h_status);
@@ -533,6 +576,74 @@ int obvhs_build_cwbvh_from_tris(obvhs_ctx* cp, const float* triangles, uint32_t 
   const float* dt = (const float*)stage_in(c, SLOT_INPUT, triangles, (size_t)n * 36, device_ptrs, &err);
   if (err) return err;
   return build_pipeline(c, dt, nullptr, n, p, out, stats);
+}
+
+int obvhs_build_cwbvh_from_tris_batch(obvhs_ctx* const* ctxs, uint32_t n_ctx, const float* const* triangles,
+                                      const uint32_t* n_tris, uint32_t n_scenes, const obvhs_build_params* p,
+                                      int device_ptrs, obvhs_cwbvh** out, obvhs_build_stats* stats) {
+  if (!ctxs || n_ctx == 0 || !p || (n_scenes && (!triangles || !n_tris || !out))) return OBVHS_ERR_INVALID_ARG;
+  for (uint32_t w = 0; w < n_ctx; w++)
+    if (!ctxs[w]) return OBVHS_ERR_INVALID_ARG;
+  for (uint32_t i = 0; i < n_scenes; i++) out[i] = nullptr;
+  // largest scenes first, so that the last ones to start are short
+  std::vector<uint32_t> order(n_scenes);
+  for (uint32_t i = 0; i < n_scenes; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return n_tris[a] > n_tris[b]; });
+  std::atomic<uint32_t> next{0};
+  std::atomic<int> err{0};
+  std::atomic<int> err_ctx{-1};
+  auto worker = [&](uint32_t w) {
+    obvhs_ctx* c = ctxs[w];
+    for (;;) {
+      if (err.load()) return;
+      const uint32_t k = next.fetch_add(1);
+      if (k >= n_scenes) return;
+      const uint32_t i = order[k];
+      const int r = obvhs_build_cwbvh_from_tris(c, triangles[i], n_tris[i], p, device_ptrs, &out[i],
+                                                stats ? &stats[i] : nullptr);
+      if (r) {
+        int expected = 0;
+        if (err.compare_exchange_strong(expected, r)) err_ctx.store((int)w);
+        return;
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (uint32_t w = 1; w < n_ctx; w++) pool.emplace_back(worker, w);
+  worker(0);
+  for (auto& t : pool) t.join();
+  const int r = err.load();
+  if (r) {
+    const int w = err_ctx.load();
+    if (w > 0) ctxs[0]->last_error = ctxs[w]->last_error;
+    for (uint32_t i = 0; i < n_scenes; i++) {
+      obvhs_cwbvh_free(out[i]);
+      out[i] = nullptr;
+    }
+  }
+  return r;
+}
+
+int obvhs_ray_traverse_multi(obvhs_ctx* cp, const obvhs_cwbvh* const* bvhs, uint32_t n_bvh, const uint32_t* ray_bvh,
+                             const obvhs_ray* rays, uint32_t n, obvhs_hit* hits, int device_ptrs) {
+  if (!cp || (n_bvh && !bvhs) || (n && (!rays || !hits || !ray_bvh))) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  int err = 0;
+  const float* dr = (const float*)stage_in(c, SLOT_INPUT2, rays, (size_t)n * 32, device_ptrs, &err);
+  if (err) return err;
+  const uint32_t* db = (const uint32_t*)stage_in(c, SLOT_INPUT, ray_bvh, (size_t)n * 4, device_ptrs, &err);
+  if (err) return err;
+  void* dout = hits;
+  if (!device_ptrs) {
+    dout = c.scratch.get(SLOT_TRAV_OUT, (size_t)n * 8 + 16);
+    if (!dout) return c.fail(OBVHS_ERR_OOM, "output staging");
+  }
+  int r = traverse_multi_device(c, bvhs, n_bvh, db, dr, n, (uint32_t*)dout, nullptr, 0);
+  if (r) return r;
+  if (!device_ptrs && n) CK(cudaMemcpyAsync(hits, dout, (size_t)n * 8, cudaMemcpyDeviceToHost, c.stream));
+  if (!device_ptrs) return take_status(c);
+  return OBVHS_OK;
 }
 
 int obvhs_build_cwbvh(obvhs_ctx* cp, const float* aabbs, uint32_t n, const obvhs_build_params* p, int device_ptrs,

@@ -152,6 +152,8 @@ struct obvhs_ctx {
     if (profiling && !krecs.empty()) cudaEventRecord(krecs.back().b, stream);
   }
 
+  cudaEvent_t coop_ev[2] = {nullptr, nullptr};  // cooperative launches through the device's shared stream
+
   int fail(int code, const std::string& msg) {
     last_error = msg;
     return code;
@@ -162,6 +164,13 @@ struct obvhs_ctx {
   }
 };
 typedef obvhs_ctx BuildCtx;
+
+// A cooperative launch (all blocks co-resident, grid barriers).  With one
+// context on the device it goes on the context's stream; with several, all
+// cooperative launches of the device go through one shared stream (event
+// hand-off with the caller's stream) so that no two of them are on the GPU
+// at once.
+cudaError_t coop_launch(obvhs_ctx& c, const void* func, unsigned grid, unsigned block, void** args, size_t smem);
 
 // Launch wrapper: counts the launch and, when profiling, brackets it with
 // CUDA events on the context's stream.
@@ -243,6 +252,9 @@ int compress_tris_device(BuildCtx& c, obvhs_cwbvh* bvh, const float* tris, uint3
 // Traversal on the compressed triangles (mode 0 closest hit, 1 occlusion).
 int traverse_compressed_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint32_t n, uint32_t* hits,
                                uint8_t* miss, int mode);
+// Rays of several BVHs in one launch: ray i is traced in bvhs[ray_bvh[i]].
+int traverse_multi_device(BuildCtx& c, const obvhs_cwbvh* const* bvhs, uint32_t n_bvh, const uint32_t* ray_bvh,
+                          const float* rays, uint32_t n, uint32_t* hits, uint8_t* miss, int mode);
 // hits4: n x (geometry id, BVH-order primitive id, original id, t bits)
 int traverse_tlas_device(BuildCtx& c, const obvhs_cwbvh* tlas, const obvhs_cwbvh* const* blas, uint32_t n_blas,
                          const float* rays, uint32_t n, uint32_t* hits4);

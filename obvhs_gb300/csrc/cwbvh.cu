@@ -27,6 +27,7 @@
 // reference's positions: the output is byte for byte the reference's.
 #include <cmath>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 
 #include "build.h"
@@ -600,11 +601,13 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
     cudaFree(cwp);
     return c.fail(OBVHS_ERR_OOM, "scratch");
   }
-  static int emit_blocks = 0;
+  static std::atomic<int> emit_blocks_s{0};
+  int emit_blocks = emit_blocks_s.load();
   if (!emit_blocks) {
     int per_sm = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_all, EMIT_THREADS, 0));
     emit_blocks = std::max(1, per_sm) * c.num_sms;
+    emit_blocks_s.store(emit_blocks);
   }
   // queue: item 0 = the root, published; head = 0, tail = 1
   CK(cudaMemsetAsync(ready, 0, (size_t)n_cw * 4, c.stream));

@@ -19,6 +19,8 @@
 // finishes every remaining pass with the clusters held in shared memory.
 #include <cooperative_groups.h>
 
+#include <atomic>
+
 #include "build.h"
 #include "radix_sort.cuh"
 
@@ -727,17 +729,18 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   const uint32_t max_passes = 2 * n + 64;
   if (n > TAIL_MAX) {
     const size_t smem = COOP_GROUPS * sizeof(CoopGroupSmem);
-    static int coop_blocks = 0;
+    static std::atomic<int> coop_blocks_s{0};
+    int coop_blocks = coop_blocks_s.load();
     if (!coop_blocks) {
       CK(cudaFuncSetAttribute(k_ploc_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       int per_sm = 0;
       CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ploc_coop, COOP_GROUPS * PT, smem));
       coop_blocks = std::max(1, per_sm) * c.num_sms;
+      coop_blocks_s.store(coop_blocks);
     }
     PlocCoopArgs pa{{cur, nxt}, out_nodes, st, merge, tile_cnt, (int)radius, depth_threshold, max_passes, c.d_status};
     void* args[] = {&pa};
-    KLAUNCH("k_ploc_coop", CK(cudaLaunchCooperativeKernel((void*)k_ploc_coop, coop_blocks, COOP_GROUPS * PT, args, smem,
-                                                          c.stream)));
+    KLAUNCH("k_ploc_coop", CK(coop_launch(c, (const void*)k_ploc_coop, coop_blocks, COOP_GROUPS * PT, args, smem)));
   }
   {
     const size_t smem = (size_t)4 * TAIL_MAX * sizeof(float4) + TAIL_MAX + 64;

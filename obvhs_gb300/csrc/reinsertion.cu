@@ -26,6 +26,8 @@
 // after the search is one cooperative launch per pass (k_resolve).
 #include <cooperative_groups.h>
 
+#include <atomic>
+
 #include "build.h"
 #include "radix_sort.cuh"
 
@@ -606,17 +608,19 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
   CK(cudaMemsetAsync(arrive, 0, (size_t)len * 4, c.stream));
   CK(cudaMemsetAsync(touched, 0, (size_t)len * 4, c.stream));
 
-  static int find_blocks = 0;
+  static std::atomic<int> find_blocks_s{0}, resolve_blocks_s{0};
+  int find_blocks = find_blocks_s.load(), resolve_blocks = resolve_blocks_s.load();
   if (!find_blocks) {
     int per_sm = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_find_persistent<192, true>, FIND_THREADS, 0));
     find_blocks = std::max(1, per_sm) * c.num_sms;
+    find_blocks_s.store(find_blocks);
   }
-  static int resolve_blocks = 0;
   if (!resolve_blocks) {
     int per_sm = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resolve, RESOLVE_THREADS, 0));
     resolve_blocks = std::max(1, per_sm) * c.num_sms;
+    resolve_blocks_s.store(resolve_blocks);
   }
   const bool clamp = (size_t)b->max_depth * 2 <= 192;
   const uint32_t cap_rt = b->max_depth * 2;
@@ -661,7 +665,7 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
     void* args[] = {&ra};
     uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)resolve_blocks,
                                                  std::max<uint64_t>(1, div_up<uint32_t>(count, RESOLVE_THREADS)));
-    KLAUNCH("k_resolve", CK(cudaLaunchCooperativeKernel((void*)k_resolve, grid, RESOLVE_THREADS, args, 0, c.stream)));
+    KLAUNCH("k_resolve", CK(coop_launch(c, (const void*)k_resolve, grid, RESOLVE_THREADS, args, 0)));
     CK(cudaGetLastError());
   }
   if (applied_deferred) {

@@ -20,6 +20,7 @@
 // Persistent warps take 32 rays at a time from a global counter.
 #include <cuda_fp16.h>
 
+#include <atomic>
 #include <vector>
 
 #include "build.h"
@@ -120,6 +121,14 @@ __device__ __forceinline__ float intersect_tri(const float4* tri, float3 o, floa
   return __int_as_float(0x7f800000);
 }
 
+// One BVH of a multi-BVH launch: nodes and 64-byte triangles (a BLAS of the
+// instance traversal, or the BVH a batched ray belongs to).
+struct BlasDesc {
+  const CwNode* nodes;
+  const float4* tris;  // primitive_indices order, 64 bytes each
+  uint32_t n_nodes, n_prims;
+};
+
 // RtCompressedTriangle::intersect (src/rt_triangle.rs:70-117): v0 in f32,
 // e1 = v1 - v0 and e2 = v2 - v0 as IEEE half floats, stored interleaved
 // (e1x, e2x, e1y, e2y, e1z, e2z) after v0; ng = (-e1) x e2.
@@ -149,14 +158,18 @@ __device__ __forceinline__ float intersect_ctri(const uint2* rec, float3 o, floa
 // MODE 0 closest hit, 1 occlusion.  CTRI: triangles as RtCompressedTriangle
 // (24 B; the hit's original id comes from primitive_indices) instead of the
 // 64-byte records.
-template <int MODE, bool CTRI = false>
-__global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ nodes, uint32_t n_nodes,
-                                                   const float4* __restrict__ tris, uint32_t n_prims,
+// MULTI: every ray names its BVH (ray_bvh[ray] indexes `multi`), so ray
+// batches against different BVHs run in one launch.
+template <int MODE, bool CTRI = false, bool MULTI = false>
+__global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ nodes_in, uint32_t n_nodes_in,
+                                                   const float4* __restrict__ tris_in, uint32_t n_prims_in,
                                                    const float4* __restrict__ rays,
                                                    uint32_t nrays, uint2* __restrict__ hits, uint8_t* __restrict__ miss,
                                                    uint32_t* __restrict__ next_ray, uint32_t* status,
                                                    const uint2* __restrict__ ctris = nullptr,
-                                                   const uint32_t* __restrict__ pidx = nullptr) {
+                                                   const uint32_t* __restrict__ pidx = nullptr,
+                                                   const BlasDesc* __restrict__ multi = nullptr,
+                                                   const uint32_t* __restrict__ ray_bvh = nullptr, uint32_t n_multi = 0) {
   const int lane = threadIdx.x & 31;
   for (;;) {
     uint32_t base = 0;
@@ -165,6 +178,25 @@ __global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ no
     if (base >= nrays) return;
     const uint32_t ri = base + lane;
     if (ri >= nrays) continue;
+    const CwNode* nodes = nodes_in;
+    const float4* tris = tris_in;
+    uint32_t n_nodes = n_nodes_in, n_prims = n_prims_in;
+    if (MULTI) {
+      const uint32_t b = __ldg(&ray_bvh[ri]);
+      if (b >= n_multi) {
+        set_status(status, ST_BAD_INPUT);
+        if (MODE == 0)
+          hits[ri] = make_uint2(OBVHS_INVALID, 0x7f800000u);
+        else
+          miss[ri] = 1;
+        continue;
+      }
+      const BlasDesc bd = multi[b];
+      nodes = bd.nodes;
+      tris = bd.tris;
+      n_nodes = bd.n_nodes;
+      n_prims = bd.n_prims;
+    }
     const float4 r0 = __ldg(&rays[2 * ri]), r1 = __ldg(&rays[2 * ri + 1]);
     const float3 o = make_float3(r0.x, r0.y, r0.z), d = make_float3(r1.x, r1.y, r1.z);
     const float tmin = r0.w, ray_tmax = r1.w;
@@ -283,12 +315,6 @@ __global__ void k_compress_tris(const float* __restrict__ tris, uint32_t n_tris,
 // in the reference, the remaining instances of a TLAS leaf group are pushed
 // as a primitive group and dropped when popped, and the ray is not
 // transformed into the instance's space.
-struct BlasDesc {
-  const CwNode* nodes;
-  const float4* tris;  // primitive_indices order, 64 bytes each
-  uint32_t n_nodes, n_prims;
-};
-
 __global__ void __launch_bounds__(TBLK) k_traverse_tlas(const CwNode* __restrict__ tlas, uint32_t n_tlas,
                                                         const uint32_t* __restrict__ tlas_pidx, uint32_t n_tlas_prims,
                                                         const BlasDesc* __restrict__ blas, uint32_t n_blas,
@@ -475,11 +501,13 @@ int traverse_tlas_device(BuildCtx& c, const obvhs_cwbvh* tlas, const obvhs_cwbvh
     CK(cudaMemcpyAsync(dd, hd.data(), (size_t)n_blas * sizeof(BlasDesc), cudaMemcpyHostToDevice, c.stream));
   }
   CK(cudaMemsetAsync(counter, 0, 4, c.stream));
-  static int per_sm = 0;
+  static std::atomic<int> per_sm_s{0};
+  int per_sm = per_sm_s.load();
   if (!per_sm) {
     int a = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_traverse_tlas, TBLK, 0);
     per_sm = std::max(1, a);
+    per_sm_s.store(per_sm);
   }
   const uint32_t grid = std::min<uint32_t>(div_up<uint32_t>(n, TBLK), (uint32_t)(per_sm * c.num_sms));
   KLAUNCH("k_traverse_tlas", k_traverse_tlas<<<grid, TBLK, 0, c.stream>>>(tlas->nodes, tlas->n_nodes, tlas->prim_indices,
@@ -514,12 +542,14 @@ int traverse_compressed_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float*
   uint32_t* counter = (uint32_t*)c.scratch.get(SLOT_OUTPUT, 16);
   if (!counter) return c.fail(OBVHS_ERR_OOM, "scratch");
   CK(cudaMemsetAsync(counter, 0, 4, c.stream));
-  static int per_sm = 0;
+  static std::atomic<int> per_sm_s{0};
+  int per_sm = per_sm_s.load();
   if (!per_sm) {
     int a = 0, b = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_traverse<0, true>, TBLK, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_traverse<1, true>, TBLK, 0);
     per_sm = std::max(1, std::min(a, b));
+    per_sm_s.store(per_sm);
   }
   const uint32_t grid = std::min<uint32_t>(div_up<uint32_t>(n, TBLK), (uint32_t)(per_sm * c.num_sms));
   if (mode == 0)
@@ -534,6 +564,45 @@ int traverse_compressed_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float*
   return 0;
 }
 
+int traverse_multi_device(BuildCtx& c, const obvhs_cwbvh* const* bvhs, uint32_t n_bvh, const uint32_t* ray_bvh,
+                          const float* rays, uint32_t n, uint32_t* hits, uint8_t* miss, int mode) {
+  if (n == 0) return 0;
+  for (uint32_t b = 0; b < n_bvh; b++) {
+    if (!bvhs[b]) return c.fail(OBVHS_ERR_INVALID_ARG, "null BVH handle");
+    if (bvhs[b]->n_nodes && !bvhs[b]->tris) return c.fail(OBVHS_ERR_INVALID_ARG, "a BVH has no triangles attached");
+  }
+  BlasDesc* dd = (BlasDesc*)c.scratch.get(SLOT_BLAS_DESC, (size_t)std::max(n_bvh, 1u) * sizeof(BlasDesc));
+  uint32_t* counter = (uint32_t*)c.scratch.get(SLOT_OUTPUT, 16);
+  if (!dd || !counter) return c.fail(OBVHS_ERR_OOM, "scratch");
+  if (n_bvh) {
+    std::vector<BlasDesc> hd(n_bvh);
+    for (uint32_t b = 0; b < n_bvh; b++)
+      hd[b] = BlasDesc{bvhs[b]->nodes, bvhs[b]->tris, bvhs[b]->n_nodes, bvhs[b]->n_prims};
+    CK(cudaMemcpyAsync(dd, hd.data(), (size_t)n_bvh * sizeof(BlasDesc), cudaMemcpyHostToDevice, c.stream));
+  }
+  CK(cudaMemsetAsync(counter, 0, 4, c.stream));
+  static std::atomic<int> per_sm_s{0};
+  int per_sm = per_sm_s.load();
+  if (!per_sm) {
+    int a = 0, b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_traverse<0, false, true>, TBLK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_traverse<1, false, true>, TBLK, 0);
+    per_sm = std::max(1, std::min(a, b));
+    per_sm_s.store(per_sm);
+  }
+  const uint32_t grid = std::min<uint32_t>(div_up<uint32_t>(n, TBLK), (uint32_t)(per_sm * c.num_sms));
+  if (mode == 0)
+    KLAUNCH("k_traverse_closest_multi", k_traverse<0, false, true><<<grid, TBLK, 0, c.stream>>>(
+                                            nullptr, 0, nullptr, 0, (const float4*)rays, n, (uint2*)hits, nullptr,
+                                            counter, c.d_status, nullptr, nullptr, dd, ray_bvh, n_bvh));
+  else
+    KLAUNCH("k_traverse_occluded_multi", k_traverse<1, false, true><<<grid, TBLK, 0, c.stream>>>(
+                                             nullptr, 0, nullptr, 0, (const float4*)rays, n, nullptr, miss, counter,
+                                             c.d_status, nullptr, nullptr, dd, ray_bvh, n_bvh));
+  CK(cudaGetLastError());
+  return 0;
+}
+
 int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint32_t n, uint32_t* hits, uint8_t* miss,
                     int mode) {
   if (n == 0) return 0;
@@ -541,12 +610,14 @@ int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint
   uint32_t* counter = (uint32_t*)c.scratch.get(SLOT_OUTPUT, 16);
   if (!counter) return c.fail(OBVHS_ERR_OOM, "scratch");
   CK(cudaMemsetAsync(counter, 0, 4, c.stream));
-  static int per_sm = 0;
+  static std::atomic<int> per_sm_s{0};
+  int per_sm = per_sm_s.load();
   if (!per_sm) {
     int a = 0, b = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_traverse<0>, TBLK, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_traverse<1>, TBLK, 0);
     per_sm = std::max(1, std::min(a, b));
+    per_sm_s.store(per_sm);
   }
   uint32_t want = div_up<uint32_t>(n, TBLK);
   uint32_t grid = std::min<uint32_t>(want, (uint32_t)(per_sm * c.num_sms));
