@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tris", type=int, default=N_TRIS)
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the 512-scene batched build + traversal comparison")
     ap.add_argument("--no-arch-scene", action="store_true",
                     help="skip the 8M-triangle architectural scene (build + 16M incoherent + 16M shadow rays)")
     return ap.parse_args()
@@ -262,6 +264,95 @@ def arch_scene(ctx, stream, steps, warmup, flush):
             "hit_fraction": float((out[:, 0] != -1).float().mean().item())}
 
 
+def batched_scenes(G, ctx, p, n_scenes=512, seed=1004):
+    """512 clustered scenes, triangle counts log-uniform over 1k-200k (scene i
+    from the clustered generator with seed offset i), each with 4,096-262,144
+    incoherent rays in proportion to its size.  Plain: every scene built and
+    traced in its own calls on one context.  Batched: all builds through
+    build_cwbvh_from_tris_batch on K concurrent contexts (K chosen by timing
+    candidates on 64 scenes), then one multi-BVH traversal launch.  Device-
+    resident inputs; wall clock with the device synchronised; hit ids and t
+    compared between the two forms."""
+    import torch
+    from obvhs_gb300 import scenes as S
+    from obvhs_gb300 import test_util as T
+
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(1000), np.log(200_000), size=n_scenes)).astype(np.int64)
+    tris, rays, owners = [], [], []
+    for i, n in enumerate(sizes):
+        t = S.scene2_tris(int(n), offset=i)
+        tris.append(torch.from_numpy(t).cuda())
+        k = int(4096 + (n - 1000) * (262_144 - 4096) / (200_000 - 1000))
+        v = t.reshape(-1, 3)
+        lo, hi = v.min(0), v.max(0)
+        o = rng.uniform(lo, hi, size=(k, 3)).astype(np.float32)
+        d = T.uniform_sample_sphere(rng.random(k).astype(np.float32), rng.random(k).astype(np.float32))
+        rays.append(T.make_rays(o, d, 0.0, np.inf))
+        owners.append(np.full(k, i, np.uint32))
+    d_rays = [torch.from_numpy(r).cuda() for r in rays]
+    all_rays = torch.from_numpy(np.concatenate(rays)).cuda()
+    all_owner = torch.from_numpy(np.concatenate(owners).view(np.int32)).cuda()
+    n_tris, n_rays = int(sizes.sum()), int(all_rays.shape[0])
+
+    def plain():
+        out = []
+        for t, r in zip(tris, d_rays):
+            b = G.build_cwbvh_from_tris(t, p, ctx=ctx)
+            out.append(b.ray_traverse(r))
+        torch.cuda.synchronize()
+        return out
+
+    def batched(k, scene_tris, with_rays=True):
+        bvhs = G.build_cwbvh_from_tris_batch(scene_tris, p, pool[:k])
+        hits = G.ray_traverse_multi(bvhs, all_owner, all_rays, ctx=ctx) if with_rays else None
+        torch.cuda.synchronize()
+        return bvhs, hits
+
+    # plain runs first: with only this context alive the GPU is not shared,
+    # so each build takes the whole-GPU cooperative forms
+    plain()
+    t0 = time.perf_counter()
+    ref = plain()
+    t_plain = time.perf_counter() - t0
+    pool = [ctx] + [G.Context(ctx.device) for _ in range(15)]
+    batched(4, tris[:64], False)  # warm-up of every context
+    tune = {}
+    for k in (1, 2, 4, 8, 12, 16):
+        t0 = time.perf_counter()
+        batched(k, tris[:128], False)
+        tune[k] = time.perf_counter() - t0
+    best = min(tune, key=tune.get)
+    batched(best, tris)
+    t0 = time.perf_counter()
+    bvhs, hits = batched(best, tris)
+    t_batched = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    bvhs = G.build_cwbvh_from_tris_batch(tris, p, pool[:best])
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    hits = G.ray_traverse_multi(bvhs, all_owner, all_rays, ctx=ctx)
+    torch.cuda.synchronize()
+    t_trace = time.perf_counter() - t0
+    for b in bvhs:
+        b.free()
+    for c in pool[1:]:
+        c.close()
+    got = hits.cpu().numpy().view(np.uint32)
+    exp = np.concatenate([np.stack([r.cpu().numpy().view(np.uint32)[:, 0], r.cpu().numpy().view(np.uint32)[:, 1]], 1)
+                          for r in ref])
+    identical = bool(np.array_equal(got, exp))
+    return {"workload": f"{n_scenes} clustered scenes, 1k-200k triangles (log-uniform), "
+                        "4,096-262,144 incoherent rays each", "preset": "medium_build",
+            "scenes": n_scenes, "triangles": n_tris, "rays": n_rays,
+            "plain_s": t_plain, "batched_s": t_batched, "speedup": t_plain / t_batched,
+            "plain_scenes_per_s": n_scenes / t_plain, "batched_scenes_per_s": n_scenes / t_batched,
+            "batched_build_mtris_s": n_tris / t_build / 1e6, "batched_trace_mrays_s": n_rays / t_trace / 1e6,
+            "contexts": best, "autotune_s_per_128_scenes": {str(k): v for k, v in tune.items()},
+            "identical_hits": identical}
+
+
 def workload(n):
     from obvhs_gb300 import scenes as S
 
@@ -456,6 +547,7 @@ def run_gb300(args):
     bounce_rate = world * len(bounce) / (mean_bounce * 1e-3) / 1e6 if mean_bounce > 0 else 0.0
 
     arch = None if args.no_arch_scene else arch_scene(ctx, stream, max(3, args.steps // 4), args.warmup, flush)
+    batch = None if args.no_batched else batched_scenes(G, ctx, BvhBuildParams.medium_build())
 
     # CPU baseline (the oracle on this host's cores, bounded sample): two full
     # builds, and the primary batch traced with node-visit / triangle-test
@@ -526,6 +618,7 @@ def run_gb300(args):
                                "traffic": traffic_db.get("k_traverse_closest"),
                                "algorithmic_bytes_per_launch": alg_bytes, "bytes_per_ray": alg_bytes / len(rays)},
         "architectural_scene": arch,
+        "batched": batch,
         "cpu_baseline": {"value": cpu_rate, "unit": "Mtris/s", "cores": cores, "kind": "port",
                          "sample": f"2 full {n}-triangle slow_build builds on {cores} threads "
                                    f"({sum(cpu_t):.1f} s)",

@@ -65,6 +65,18 @@ class Context:
         self.h = h
         self.device = device
 
+    def close(self):
+        """Destroys the context (its stream and scratch buffers)."""
+        if getattr(self, "h", None):
+            self.lib.obvhs_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
     @classmethod
     def default(cls) -> "Context":
         if cls._default is None:

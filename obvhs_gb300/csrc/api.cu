@@ -245,6 +245,8 @@ DeviceShared& device_shared(int device) {
 
 }  // namespace
 
+int device_context_count(int device) { return device_shared(device).contexts.load(); }
+
 cudaError_t coop_launch(obvhs_ctx& c, const void* func, unsigned grid, unsigned block, void** args, size_t smem) {
   DeviceShared& d = device_shared(c.device);
   if (d.contexts.load() <= 1) return cudaLaunchCooperativeKernel(func, grid, block, args, smem, c.stream);

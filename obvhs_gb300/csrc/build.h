@@ -171,6 +171,8 @@ typedef obvhs_ctx BuildCtx;
 // hand-off with the caller's stream) so that no two of them are on the GPU
 // at once.
 cudaError_t coop_launch(obvhs_ctx& c, const void* func, unsigned grid, unsigned block, void** args, size_t smem);
+// Live contexts on `device` (more than one: the GPU is shared by concurrent builds).
+int device_context_count(int device);
 
 // Launch wrapper: counts the launch and, when profiling, brackets it with
 // CUDA events on the context's stream.

@@ -243,6 +243,7 @@ constexpr int BOXS = PCHUNK + 4 * 32;  // staged boxes per tile: the tile and a 
 // The loop ends once at most TAIL_MAX clusters are live; the single-CTA tail
 // kernel finishes.  Cluster buffers alternate by pass parity (passes & 1).
 constexpr int COOP_GROUPS = 4;
+constexpr uint32_t SHARED_SINGLE_BLOCK_MAX = 262144;  // leaves: single-block PLOC when contexts share the GPU
 
 struct PlocCoopArgs {
   Bvh2Node* buf[2];
@@ -269,6 +270,7 @@ __device__ __forceinline__ void group_sync(int group) {
 
 __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs a) {
   cg::grid_group grid = cg::this_grid();
+  const bool single = gridDim.x == 1;  // one block, launched normally: block barriers suffice
   extern __shared__ __align__(16) unsigned char coop_smem[];
   const int group = threadIdx.x / PT;
   CoopGroupSmem& sm = reinterpret_cast<CoopGroupSmem*>(coop_smem)[group];
@@ -383,7 +385,7 @@ __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs 
         a.tile_cnt[tile] = make_uint2(tot & 0xffffu, tot >> 16);
       }
     }
-    grid.sync();
+    if (single) __syncthreads(); else grid.sync();
 
     // B: offsets and writes
     const uint32_t ins_top = *(volatile uint32_t*)&a.st->insert[parity];
@@ -467,7 +469,7 @@ __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs 
         a.st->passes = pass + 1;
       }
     }
-    grid.sync();
+    if (single) __syncthreads(); else grid.sync();
   }
 }
 
@@ -740,7 +742,14 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
     }
     PlocCoopArgs pa{{cur, nxt}, out_nodes, st, merge, tile_cnt, (int)radius, depth_threshold, max_passes, c.d_status};
     void* args[] = {&pa};
-    KLAUNCH("k_ploc_coop", CK(coop_launch(c, (const void*)k_ploc_coop, coop_blocks, COOP_GROUPS * PT, args, smem)));
+    if (device_context_count(c.device) > 1 && n <= SHARED_SINGLE_BLOCK_MAX) {
+      // the GPU is shared with other contexts: one block, a normal launch,
+      // runs beside their work instead of waiting for a whole-GPU slot
+      KLAUNCH("k_ploc_coop", k_ploc_coop<<<1, COOP_GROUPS * PT, smem, c.stream>>>(pa));
+      CK(cudaGetLastError());
+    } else {
+      KLAUNCH("k_ploc_coop", CK(coop_launch(c, (const void*)k_ploc_coop, coop_blocks, COOP_GROUPS * PT, args, smem)));
+    }
   }
   {
     const size_t smem = (size_t)4 * TAIL_MAX * sizeof(float4) + TAIL_MAX + 64;

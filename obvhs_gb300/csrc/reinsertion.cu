@@ -37,6 +37,7 @@ namespace {
 
 constexpr int BLK = 256;
 constexpr int RESOLVE_THREADS = 1024;
+constexpr uint32_t RESOLVE_SINGLE_MAX = 8192;  // proposals searched: one block resolves the whole pass
 constexpr uint32_t RESOLVE_SMALL = 512;  // proposals one block resolves faster than the grid (one climb per thread)
 
 struct Reins {
@@ -491,28 +492,13 @@ __device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, u
   }
 }
 
-// Everything after find_reinsertion for one pass, in one cooperative launch:
-//   1. list the proposals with area_diff > 0 and gather their conflict sets
-//   2. greedy conflict resolution in priority order (rounds)
-//   3. reinsert_node for every accepted proposal (src/bvh2/reinsertion.rs:336-382)
-//   4. mark the nodes whose boxes may change: `to` and its ancestors, and the
-//      ancestors of the old parent of `from`
-//   5. refit the marked nodes bottom-up, starting from marked nodes without
-//      marked children.
-// After step 1, a pass with at most RESOLVE_SMALL proposals continues in
-// block 0 alone (block barriers instead of grid barriers); the other blocks
-// return and take no further part in any barrier.
-__global__ void __launch_bounds__(RESOLVE_THREADS) k_resolve(ResolveArgs a) {
-  cg::grid_group grid = cg::this_grid();
-  const uint32_t stride = gridDim.x * blockDim.x;
-  const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
+// Step 1 of a pass: the proposals with area_diff > 0 (warp-aggregated
+// append), their conflict sets and keys, and the round-0 claim words reset.
+// `warp_t0` is the first index of the calling thread's warp.
+__device__ __forceinline__ void list_proposals(const ResolveArgs& a, uint32_t warp_t0, uint32_t stride) {
   const int lane = threadIdx.x & 31;
-  __shared__ uint32_t s_rem;
-  unsigned long long* owner0 = a.owner;  // round 0 claims
-
-  // 1. proposals with a gain (warp-aggregated append), their conflict sets,
-  //    and the round-0 claim words reset
-  for (uint32_t k0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); k0 < a.count; k0 += stride) {
+  unsigned long long* owner0 = a.owner;
+  for (uint32_t k0 = warp_t0; k0 < a.count; k0 += stride) {
     const uint32_t k = k0 + lane;
     Reins r{0, 0, 0.0f, 0};
     if (k < a.count) r = a.reins[k];
@@ -539,9 +525,34 @@ __global__ void __launch_bounds__(RESOLVE_THREADS) k_resolve(ResolveArgs a) {
       owner0[c4] = ~0ull;
     }
   }
-  grid.sync();
+}
+
+// Everything after find_reinsertion for one pass, in one cooperative launch:
+//   1. list the proposals with area_diff > 0 and gather their conflict sets
+//   2. greedy conflict resolution in priority order (rounds)
+//   3. reinsert_node for every accepted proposal (src/bvh2/reinsertion.rs:336-382)
+//   4. mark the nodes whose boxes may change: `to` and its ancestors, and the
+//      ancestors of the old parent of `from`
+//   5. refit the marked nodes bottom-up, starting from marked nodes without
+//      marked children.
+// After step 1, a pass with at most RESOLVE_SMALL proposals continues in
+// block 0 alone (block barriers instead of grid barriers); the other blocks
+// return and take no further part in any barrier.
+__global__ void __launch_bounds__(RESOLVE_THREADS) k_resolve(ResolveArgs a) {
+  cg::grid_group grid = cg::this_grid();
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ uint32_t s_rem;
+
+  // 1. proposals with a gain, their conflict sets, the round-0 claim words
+  list_proposals(a, blockIdx.x * blockDim.x + (threadIdx.x & ~31u), stride);
+  const bool single = gridDim.x == 1;  // one block, launched normally
+  if (single)
+    __syncthreads();
+  else
+    grid.sync();
   const uint32_t P = *(volatile uint32_t*)&a.ctr[0];
-  if (P <= RESOLVE_SMALL) {
+  if (single || P <= RESOLVE_SMALL) {
     if (blockIdx.x != 0) return;
     resolve_body<true>(a, P, threadIdx.x, blockDim.x, [] { __syncthreads(); }, &s_rem);
   } else {
@@ -665,7 +676,13 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
     void* args[] = {&ra};
     uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)resolve_blocks,
                                                  std::max<uint64_t>(1, div_up<uint32_t>(count, RESOLVE_THREADS)));
-    KLAUNCH("k_resolve", CK(coop_launch(c, (const void*)k_resolve, grid, RESOLVE_THREADS, args, 0)));
+    if (grid == 1 || count <= RESOLVE_SINGLE_MAX || device_context_count(c.device) > 1) {
+      // one block, a normal launch (block barriers only)
+      KLAUNCH("k_resolve", k_resolve<<<1, RESOLVE_THREADS, 0, c.stream>>>(ra));
+      CK(cudaGetLastError());
+    } else {
+      KLAUNCH("k_resolve", CK(coop_launch(c, (const void*)k_resolve, grid, RESOLVE_THREADS, args, 0)));
+    }
     CK(cudaGetLastError());
   }
   if (applied_deferred) {

@@ -45,18 +45,25 @@ def test_batched_builds_equal_single_builds(G, preset, n_ctx):
     scenes = _scenes(24, 1 if n_ctx == 4 else 2, clustered=True)
     p = getattr(BvhBuildParams, preset)()
     ctxs = [G.Context(0) for _ in range(n_ctx)]
-    batch = G.build_cwbvh_from_tris_batch(scenes, p, ctxs)
-    for tris, cw in zip(scenes, batch):
-        one = G.build_cwbvh_from_tris(tris, p, ctx=ctxs[0])
-        a, b = cw.download(), one.download()
-        assert a[0].tobytes() == b[0].tobytes() and a[1].tobytes() == b[1].tobytes()
-        assert cw.stats.leaf_count == one.stats.leaf_count
+    try:
+        batch = G.build_cwbvh_from_tris_batch(scenes, p, ctxs)
+        for tris, cw in zip(scenes, batch):
+            one = G.build_cwbvh_from_tris(tris, p, ctx=ctxs[0])
+            a, b = cw.download(), one.download()
+            assert a[0].tobytes() == b[0].tobytes() and a[1].tobytes() == b[1].tobytes()
+            assert cw.stats.leaf_count == one.stats.leaf_count
+            cw.free()
+            one.free()
+    finally:
+        for c in ctxs:
+            c.close()
 
 
 def test_multi_bvh_traversal_equals_per_bvh(G):
     scenes = _scenes(16, 3)
     p = BvhBuildParams.medium_build()
     ctxs = [G.Context(0) for _ in range(2)]
+    request_cleanup = ctxs
     bvhs = G.build_cwbvh_from_tris_batch(scenes, p, ctxs)
     rays, owner, expect_id, expect_t = [], [], [], []
     for i, (tris, cw) in enumerate(zip(scenes, bvhs)):
@@ -73,6 +80,10 @@ def test_multi_bvh_traversal_equals_per_bvh(G):
     assert np.array_equal(ids, np.concatenate(expect_id)[perm])
     assert np.array_equal(t.view(np.uint32), np.concatenate(expect_t)[perm].view(np.uint32))
     assert (ids != 0xFFFFFFFF).sum() > 1000
+    for b in bvhs:
+        b.free()
+    for c in request_cleanup:
+        c.close()
 
 
 def test_batched_build_error_frees_everything_and_contexts_recover(G):
@@ -86,3 +97,28 @@ def test_batched_build_error_frees_everything_and_contexts_recover(G):
     assert e.value.code == -4
     ok = G.build_cwbvh_from_tris_batch(scenes[:3], BvhBuildParams.medium_build(), ctxs)
     assert len(ok) == 3 and all(b.info()[0] > 0 for b in ok)
+    for b in ok:
+        b.free()
+    for c in ctxs:
+        c.close()
+
+
+def test_shared_gpu_paths_match_the_oracle(G):
+    """With several live contexts, PLOC and conflict resolution run as single
+    blocks with normal launches (beside other contexts' work); the result is
+    the same tree as the whole-GPU cooperative forms and the oracle."""
+    from oracle import oracle as O
+
+    tris = S.scene2_tris(200_000, offset=9)
+    p = BvhBuildParams.slow_build()
+    extra, other = G.Context(0), G.Context(0)  # at least two live contexts
+    try:
+        cw = G.build_cwbvh_from_tris(tris, p, ctx=extra)
+        nodes, prims = cw.download()
+        ob = O.build(tris=tris, params=p, nthreads=8, keep_intermediate=False)
+        assert nodes.tobytes() == ob.cw_nodes.tobytes() and prims.tobytes() == ob.cw_pidx.tobytes()
+        assert cw.stats.reinsertions == ob.reinsertions
+        cw.free()
+    finally:
+        extra.close()
+        other.close()
