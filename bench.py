@@ -264,16 +264,17 @@ def arch_scene(ctx, stream, steps, warmup, flush):
             "hit_fraction": float((out[:, 0] != -1).float().mean().item())}
 
 
-def batched_scenes(G, ctx, p, n_scenes=512, seed=1004):
+def batched_scenes(G, ctx, base, n_scenes=512, seed=1004):
     """512 clustered scenes, triangle counts log-uniform over 1k-200k (scene i
     from the clustered generator with seed offset i), each with 4,096-262,144
-    incoherent rays in proportion to its size.  Plain: every scene built and
-    traced in its own calls on one context.  Batched: all builds through
-    build_cwbvh_from_tris_batch on K concurrent contexts (K chosen by timing
-    candidates on 64 scenes), then one multi-BVH traversal launch.  Device-
-    resident inputs; wall clock with the device synchronised; hit ids and t
-    compared between the two forms."""
+    incoherent rays in proportion to its size.  The PLOC search radius comes
+    from the autotuner (segmented build + multi-BVH traversal of a 64-scene
+    sample, radius 8 / 14 / 24).  Plain: every scene built and traced in its
+    own calls.  Batched: one segmented build of all scenes, then one multi-BVH
+    traversal launch.  Device-resident inputs; wall clock with the device
+    synchronised; hit ids and t compared between the two forms."""
     import torch
+    from obvhs_gb300 import autotune as A
     from obvhs_gb300 import scenes as S
     from obvhs_gb300 import test_util as T
 
@@ -295,62 +296,64 @@ def batched_scenes(G, ctx, p, n_scenes=512, seed=1004):
     all_owner = torch.from_numpy(np.concatenate(owners).view(np.int32)).cuda()
     n_tris, n_rays = int(sizes.sum()), int(all_rays.shape[0])
 
+    # autotune on a sample spread over the size range
+    pick = A.sample_indices(sizes, 64)
+    s_rays = torch.cat([d_rays[i] for i in pick])
+    s_owner = torch.from_numpy(np.concatenate([np.full(len(rays[i]), j, np.int32) for j, i in enumerate(pick)])).cuda()
+    p, tune = A.tune_segmented([tris[i] for i in pick], s_rays, s_owner, base, ctx=ctx)
+
     def plain():
         out = []
         for t, r in zip(tris, d_rays):
             b = G.build_cwbvh_from_tris(t, p, ctx=ctx)
             out.append(b.ray_traverse(r))
+            b.free()
         torch.cuda.synchronize()
         return out
 
-    def batched(k, scene_tris, with_rays=True):
-        bvhs = G.build_cwbvh_from_tris_batch(scene_tris, p, pool[:k])
-        hits = G.ray_traverse_multi(bvhs, all_owner, all_rays, ctx=ctx) if with_rays else None
+    def batched():
+        bvhs = G.build_cwbvh_from_tris_segmented(tris, p, ctx=ctx)
+        hits = G.ray_traverse_multi(bvhs, all_owner, all_rays, ctx=ctx)
         torch.cuda.synchronize()
         return bvhs, hits
 
-    # plain runs first: with only this context alive the GPU is not shared,
-    # so each build takes the whole-GPU cooperative forms
     plain()
     t0 = time.perf_counter()
     ref = plain()
     t_plain = time.perf_counter() - t0
-    pool = [ctx] + [G.Context(ctx.device) for _ in range(15)]
-    batched(4, tris[:64], False)  # warm-up of every context
-    tune = {}
-    for k in (1, 2, 4, 8, 12, 16):
-        t0 = time.perf_counter()
-        batched(k, tris[:128], False)
-        tune[k] = time.perf_counter() - t0
-    best = min(tune, key=tune.get)
-    batched(best, tris)
+    for b in batched()[0]:
+        b.free()
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    bvhs, hits = batched(best, tris)
+    bvhs, hits = batched()
     t_batched = time.perf_counter() - t0
+    for b in bvhs:
+        b.free()
     t0 = time.perf_counter()
-    bvhs = G.build_cwbvh_from_tris_batch(tris, p, pool[:best])
+    bvhs = G.build_cwbvh_from_tris_segmented(tris, p, ctx=ctx)
     torch.cuda.synchronize()
     t_build = time.perf_counter() - t0
+    launches = bvhs[0].stats.kernel_launches if bvhs else 0
     t0 = time.perf_counter()
     hits = G.ray_traverse_multi(bvhs, all_owner, all_rays, ctx=ctx)
     torch.cuda.synchronize()
     t_trace = time.perf_counter() - t0
     for b in bvhs:
         b.free()
-    for c in pool[1:]:
-        c.close()
     got = hits.cpu().numpy().view(np.uint32)
     exp = np.concatenate([np.stack([r.cpu().numpy().view(np.uint32)[:, 0], r.cpu().numpy().view(np.uint32)[:, 1]], 1)
                           for r in ref])
     identical = bool(np.array_equal(got, exp))
     return {"workload": f"{n_scenes} clustered scenes, 1k-200k triangles (log-uniform), "
                         "4,096-262,144 incoherent rays each", "preset": "medium_build",
+            "search_radius": int(p.ploc_search_distance),
+            "autotune_s_by_radius": {str(k): v for k, v in tune.items()},
             "scenes": n_scenes, "triangles": n_tris, "rays": n_rays,
             "plain_s": t_plain, "batched_s": t_batched, "speedup": t_plain / t_batched,
             "plain_scenes_per_s": n_scenes / t_plain, "batched_scenes_per_s": n_scenes / t_batched,
-            "batched_build_mtris_s": n_tris / t_build / 1e6, "batched_trace_mrays_s": n_rays / t_trace / 1e6,
-            "contexts": best, "autotune_s_per_128_scenes": {str(k): v for k, v in tune.items()},
-            "identical_hits": identical}
+            "batched_build_s": t_build, "batched_build_mtris_s": n_tris / t_build / 1e6,
+            "batched_build_kernel_launches": launches,
+            "batched_trace_mrays_s": n_rays / t_trace / 1e6, "identical_hits": identical}
 
 
 def workload(n):

@@ -232,6 +232,22 @@ OBVHS_API int obvhs_ray_traverse_tlas_blas(obvhs_ctx* ctx, const obvhs_cwbvh* tl
 OBVHS_API int obvhs_build_cwbvh_from_tris_batch(obvhs_ctx* const* ctxs, uint32_t n_ctx, const float* const* triangles,
                                                 const uint32_t* n_tris, uint32_t n_scenes, const obvhs_build_params* params,
                                                 int device_ptrs, obvhs_cwbvh** out, obvhs_build_stats* stats);
+/* The segmented form: all n_scenes scenes go through every stage together,
+ * one launch per stage for the whole batch (a segmented Morton sort, one
+ * cooperative PLOC launch over all scenes' clusters, reinsertion passes whose
+ * candidate sort, search and resolve each cover every scene, one CWBVH
+ * emission queue seeded with every root).  out[i] is byte-identical to a
+ * build of scene i alone; all outputs of one call share one device
+ * allocation, released with the last of them.  Batches above
+ * OBVHS_SEG_MAX_SCENES scenes or 2^29 triangles run as several such chunks.
+ * stats[i]: leaf_count, ploc_passes and ploc_sum_counts are scene i's;
+ * core_build_ms, reinsertions, kernel_launches and stage_ms are its chunk's.
+ * On error every out[i] is NULL and the context's last error says why. */
+#define OBVHS_SEG_MAX_SCENES 4096u
+OBVHS_API int obvhs_build_cwbvh_from_tris_segmented(obvhs_ctx* ctx, const float* const* triangles,
+                                                    const uint32_t* n_tris, uint32_t n_scenes,
+                                                    const obvhs_build_params* params, int device_ptrs,
+                                                    obvhs_cwbvh** out, obvhs_build_stats* stats);
 /* CwBvh::ray_traverse (src/cwbvh/mod.rs:169-198) for rays of several BVHs in
  * one launch: ray i is traced in bvhs[ray_bvh[i]] (each with triangles
  * attached); hits as obvhs_ray_traverse, identical to per-BVH calls. */

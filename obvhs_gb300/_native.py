@@ -92,6 +92,7 @@ SIGNATURES = {
     "obvhs_ray_traverse_miss": (I32, [P, P, P, U32, P, I32]),
     "obvhs_ray_traverse_tlas_blas": (I32, [P, P, P, U32, P, U32, P, I32]),
     "obvhs_build_cwbvh_from_tris_batch": (I32, [P, U32, P, P, U32, ctypes.POINTER(BuildParams), I32, P, P]),
+    "obvhs_build_cwbvh_from_tris_segmented": (I32, [P, P, P, U32, ctypes.POINTER(BuildParams), I32, P, P]),
     "obvhs_ray_traverse_multi": (I32, [P, P, U32, P, P, U32, P, I32]),
     "obvhs_cwbvh_set_triangles_compressed": (I32, [P, P, P, U32, I32]),
     "obvhs_cwbvh_download_compressed": (I32, [P, P, P]),

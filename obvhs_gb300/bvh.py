@@ -457,10 +457,39 @@ def bvh2_to_cwbvh(bvh2: Bvh2, max_prims_per_leaf: int, order_children: bool,
     return CwBvh(ctx, h)
 
 
-def build_cwbvh_from_tris_batch(scenes, config: BvhBuildParams, contexts) -> list:
-    """Many independent build_cwbvh_from_tris calls at once: `contexts` work
-    concurrently (one host thread and CUDA stream each), largest scenes first.
-    Each result is byte-identical to building that scene alone."""
+def build_cwbvh_from_tris_segmented(scenes, config: BvhBuildParams, ctx: Context | None = None) -> list:
+    """Many scenes built together: every stage of the build runs once for all
+    of them (segmented sorts, one cooperative PLOC launch, reinsertion and
+    CWBVH launches that cover every scene).  Each result is byte-identical to
+    building that scene alone; the results share one device allocation."""
+    ctx = _ctx(ctx)
+    preps = [_prep(t, np.float32, 9) for t in scenes]
+    devs = {p[2] for p in preps}
+    if len(devs) > 1:
+        raise ValueError("scenes must all be host arrays or all device tensors")
+    dev = devs.pop() if devs else 0
+    n = len(preps)
+    ptrs = (ctypes.c_void_p * max(n, 1))(*[p[0].value if isinstance(p[0], ctypes.c_void_p) else p[0] for p in preps])
+    counts = (ctypes.c_uint32 * max(n, 1))(*[p[1] for p in preps])
+    outs = (ctypes.c_void_p * max(n, 1))()
+    stats = (N.BuildStats * max(n, 1))()
+    prm = _params(config)
+    ctx.check(ctx.lib.obvhs_build_cwbvh_from_tris_segmented(ctx.h, ctypes.cast(ptrs, ctypes.c_void_p),
+                                                            ctypes.cast(counts, ctypes.c_void_p), n,
+                                                            ctypes.byref(prm), dev, ctypes.cast(outs, ctypes.c_void_p),
+                                                            ctypes.cast(stats, ctypes.c_void_p)))
+    del preps
+    return [CwBvh(ctx, ctypes.c_void_p(outs[i]), BuildStats.from_c(stats[i])) for i in range(n)]
+
+
+def build_cwbvh_from_tris_batch(scenes, config: BvhBuildParams, contexts=None) -> list:
+    """Many independent build_cwbvh_from_tris calls at once.  Without
+    `contexts`: the segmented build (build_cwbvh_from_tris_segmented).  With
+    `contexts`: they work concurrently (one host thread and CUDA stream each),
+    largest scenes first.  Each result is byte-identical to building that
+    scene alone."""
+    if contexts is None:
+        return build_cwbvh_from_tris_segmented(scenes, config)
     contexts = list(contexts)
     if not contexts:
         raise ValueError("at least one context")

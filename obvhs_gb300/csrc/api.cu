@@ -226,6 +226,207 @@ int build_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t 
   return 0;
 }
 
+// Segmented build of scenes [0, S): every stage once for all of them.
+// tris[s]: device pointers.  Fills out[s] (null on failure) and stats[s].
+int seg_pipeline(BuildCtx& c, const float* const* tris, const uint32_t* n_tris, uint32_t S,
+                 const obvhs_build_params* p, obvhs_cwbvh** out, obvhs_build_stats* stats) {
+  if (p->ploc_search_distance < 1 || p->ploc_search_distance > 32)
+    return c.fail(OBVHS_ERR_INVALID_ARG, "ploc_search_distance must be 1..32");
+  if (p->sort_precision > 1) return c.fail(OBVHS_ERR_INVALID_ARG, "sort_precision must be 0 (U64) or 1 (U128)");
+  const uint64_t launches0 = c.kernel_launches;
+  EventTimer timer(c.stream);
+  StageEvents stages(c.stream);
+  Scratch& s = c.scratch;
+  std::vector<obvhs_cwbvh*> outs;
+  // table space: device arena in SLOT_SEG, pinned staging in h_seg; offsets
+  // are never reused within the build, so no copy can see a later write
+  const size_t arena = ((size_t)S + 1) * 512 + 16384;
+  if (c.h_seg_cap < arena) {
+    if (c.h_seg) cudaFreeHost(c.h_seg);
+    c.h_seg = nullptr;
+    c.h_seg_cap = 0;
+    if (cudaMallocHost(&c.h_seg, arena) != cudaSuccess) {
+      cudaGetLastError();
+      return c.fail(OBVHS_ERR_OOM, "pinned staging");
+    }
+    c.h_seg_cap = arena;
+  }
+  char* d_arena = (char*)s.get(SLOT_SEG, arena);
+  if (!d_arena) return c.fail(OBVHS_ERR_OOM, "scratch");
+  size_t arena_used = 0;
+  cudaError_t upload_err = cudaSuccess;
+  auto take = [&](size_t bytes) -> char* {
+    const size_t at = arena_used;
+    arena_used += (bytes + 15) & ~(size_t)15;
+    return arena_used <= arena ? d_arena + at : nullptr;
+  };
+  SegTableUpload upload = [&](const void* src, size_t bytes) -> uint32_t* {
+    const size_t at = arena_used;
+    char* d = take(bytes);
+    if (!d) return nullptr;
+    std::memcpy(static_cast<char*>(c.h_seg) + at, src, bytes);
+    const cudaError_t e =
+        cudaMemcpyAsync(d, static_cast<char*>(c.h_seg) + at, bytes, cudaMemcpyHostToDevice, c.stream);
+    if (e) {
+      upload_err = e;
+      return nullptr;
+    }
+    return reinterpret_cast<uint32_t*>(d);
+  };
+
+  // leaves: triangles, or pre-split AABBs (scene by scene) gathered into one array
+  const bool split = p->pre_split != 0;
+  std::vector<uint32_t> m(S);
+  float* seg_aabbs = nullptr;
+  uint32_t* seg_idx = nullptr;
+  if (split) {
+    size_t total = 0;
+    for (uint32_t k = 0; k < S; k++) {
+      float* a = nullptr;
+      uint32_t* ix = nullptr;
+      uint32_t mk = 0;
+      int r = presplit_device(c, tris[k], n_tris[k], &a, &ix, &mk);
+      if (r) return r;
+      m[k] = mk;
+      if (total + mk > 0x40000000ull) return c.fail(OBVHS_ERR_TOO_LARGE, "segmented batch above 2^30 leaves");
+      // grow the gathered arrays, keeping what is already there
+      const size_t need = total + mk;
+      if (s.cap[SLOT_SEG_AABBS] < need * 24 || s.cap[SLOT_SEG_IDX] < need * 4) {
+        void* na = nullptr;
+        void* ni = nullptr;
+        const size_t want = need + need / 2 + 1024;
+        if (cudaMalloc(&na, want * 24) != cudaSuccess || cudaMalloc(&ni, want * 4) != cudaSuccess) {
+          cudaGetLastError();
+          if (na) cudaFree(na);
+          return c.fail(OBVHS_ERR_OOM, "pre-split gather");
+        }
+        if (total) {
+          CK(cudaMemcpyAsync(na, s.ptr[SLOT_SEG_AABBS], total * 24, cudaMemcpyDeviceToDevice, c.stream));
+          CK(cudaMemcpyAsync(ni, s.ptr[SLOT_SEG_IDX], total * 4, cudaMemcpyDeviceToDevice, c.stream));
+        }
+        CK(cudaStreamSynchronize(c.stream));
+        for (int sl : {SLOT_SEG_AABBS, SLOT_SEG_IDX}) {
+          if (s.ptr[sl]) cudaFree(s.ptr[sl]);
+          s.total -= s.cap[sl];
+        }
+        s.ptr[SLOT_SEG_AABBS] = na;
+        s.cap[SLOT_SEG_AABBS] = want * 24;
+        s.ptr[SLOT_SEG_IDX] = ni;
+        s.cap[SLOT_SEG_IDX] = want * 4;
+        s.total += want * 28;
+      }
+      if (mk) {
+        CK(cudaMemcpyAsync((char*)s.ptr[SLOT_SEG_AABBS] + total * 24, a, (size_t)mk * 24, cudaMemcpyDeviceToDevice,
+                           c.stream));
+        CK(cudaMemcpyAsync((char*)s.ptr[SLOT_SEG_IDX] + total * 4, ix, (size_t)mk * 4, cudaMemcpyDeviceToDevice,
+                           c.stream));
+      }
+      total += mk;
+    }
+    seg_aabbs = (float*)s.ptr[SLOT_SEG_AABBS];
+    seg_idx = (uint32_t*)s.ptr[SLOT_SEG_IDX];
+  } else {
+    for (uint32_t k = 0; k < S; k++) m[k] = n_tris[k];
+  }
+  SegLayout L;
+  L.n_seg = S;
+  L.prim_start.resize(S + 1);
+  L.node_start.resize(S + 1);
+  uint64_t pa = 0, na = 0;
+  for (uint32_t k = 0; k < S; k++) {
+    L.prim_start[k] = (uint32_t)pa;
+    L.node_start[k] = (uint32_t)na;
+    pa += m[k];
+    na += 2 * (uint64_t)m[k];
+    L.max_m = std::max(L.max_m, m[k]);
+  }
+  if (na > 0x80000000ull) return c.fail(OBVHS_ERR_TOO_LARGE, "segmented batch above 2^30 leaves");
+  L.prim_start[S] = (uint32_t)pa;
+  L.node_start[S] = (uint32_t)na;
+  L.n_prims = (uint32_t)pa;
+  L.n_slots = (uint32_t)na;
+  {
+    std::vector<uint32_t> lt(2 * ((size_t)S + 1));
+    std::copy(L.prim_start.begin(), L.prim_start.end(), lt.begin());
+    std::copy(L.node_start.begin(), L.node_start.end(), lt.begin() + S + 1);
+    uint32_t* d = upload(lt.data(), lt.size() * 4);
+    if (!d) return upload_err ? c.cuda_fail(upload_err, "table upload") : c.fail(OBVHS_ERR_OOM, "segment tables");
+    L.d_prim_start = d;
+    L.d_node_start = d + S + 1;
+  }
+  const float* const* d_tris = nullptr;
+  if (!split) {
+    d_tris = reinterpret_cast<const float* const*>(upload(tris, (size_t)S * sizeof(float*)));
+    if (!d_tris) return upload_err ? c.cuda_fail(upload_err, "table upload") : c.fail(OBVHS_ERR_OOM, "segment tables");
+  }
+  uint32_t* d_passes = reinterpret_cast<uint32_t*>(take((size_t)S * 4));
+  unsigned long long* d_sum = reinterpret_cast<unsigned long long*>(take((size_t)S * 8));
+  if (!d_passes || !d_sum) return c.fail(OBVHS_ERR_OOM, "segment tables");
+  stages.mark(c.stream);
+  const uint32_t M = L.n_prims;
+  Bvh2Node* leaves = (Bvh2Node*)s.get(SLOT_LEAVES, (size_t)std::max(M, 1u) * sizeof(Bvh2Node));
+  uint32_t* pidx = (uint32_t*)s.get(SLOT_BVH2_PIDX, (size_t)std::max(M, 1u) * 4);
+  int* total_keys = (int*)s.get(SLOT_TOTAL, (size_t)S * 32);
+  Bvh2Node* nodes = (Bvh2Node*)s.get(SLOT_BVH2_NODES, (size_t)std::max(L.n_slots, 1u) * sizeof(Bvh2Node));
+  if (!leaves || !pidx || !total_keys || !nodes) return c.fail(OBVHS_ERR_OOM, "scratch");
+  int r = seg_leaves_device(c, L, d_tris, seg_aabbs, seg_idx, leaves, pidx, total_keys);
+  if (r) return r;
+  r = ploc_seg_device(c, L, leaves, total_keys, p->ploc_search_distance, (int)p->sort_precision,
+                      p->search_depth_threshold, nodes, d_passes, d_sum);
+  if (r) return r;
+  stages.mark(c.stream);
+  // one round trip: every scene's pass count (its search stack bound) and the
+  // status word (NaN boxes leave tree slots unwritten: stop before any kernel
+  // follows the links)
+  std::vector<uint32_t> h_passes(S);
+  std::vector<unsigned long long> h_sum(S);
+  CK(cudaMemcpyAsync(h_passes.data(), d_passes, (size_t)S * 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(h_sum.data(), d_sum, (size_t)S * 8, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(c.h_status, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  if (*c.h_status) return take_status(c);
+  BuildReadback* rb = reinterpret_cast<BuildReadback*>(static_cast<char*>(c.h_small) + READBACK_OFFSET);
+  std::memset(rb, 0, sizeof(BuildReadback));
+  r = reinsertion_seg_device(c, nodes, L, h_passes.data(), p->reinsertion_batch_ratio, upload, &rb->applied);
+  if (r) return upload_err ? c.cuda_fail(upload_err, "table upload") : r;
+  stages.mark(c.stream);
+  const uint32_t mp = p->max_prims_per_leaf < 1 ? 1 : (p->max_prims_per_leaf > 3 ? 3 : p->max_prims_per_leaf);
+  uint32_t expected = 0;
+  r = cwbvh_seg_device(c, nodes, pidx, L, mp, 1, tris, n_tris, split ? 1 : 0, upload, outs, &rb->emitted, &expected);
+  auto drop = [&]() {
+    for (auto* o : outs) obvhs_cwbvh_free(o);
+    outs.clear();
+  };
+  if (r) {
+    drop();
+    return upload_err ? c.cuda_fail(upload_err, "table upload") : r;
+  }
+  stages.mark(c.stream);
+  const double ms = timer.stop_ms();
+  r = take_status(c);
+  if (!r && rb->emitted != expected) r = c.fail(OBVHS_ERR_BAD_INPUT, "CWBVH emission failed");
+  if (r) {
+    drop();
+    return r;
+  }
+  double st[4];
+  stages.read(st);
+  for (uint32_t k = 0; k < S; k++) {
+    out[k] = outs[k];
+    if (stats) {
+      obvhs_build_stats& o = stats[k];
+      o.core_build_ms = ms;  // the whole batch
+      o.leaf_count = m[k];
+      o.ploc_passes = h_passes[k];
+      o.ploc_sum_counts = h_sum[k];
+      o.reinsertions = rb->applied;  // the whole batch
+      o.kernel_launches = c.kernel_launches - launches0;
+      for (int q = 0; q < 4; q++) o.stage_ms[q] = st[q];
+    }
+  }
+  return 0;
+}
+
 }  // namespace
 
 namespace {
@@ -312,6 +513,7 @@ int obvhs_ctx_destroy(obvhs_ctx* c) {
   if (c->h_status) cudaFreeHost(c->h_status);
   if (c->h_hist) cudaFreeHost(c->h_hist);
   if (c->h_small) cudaFreeHost(c->h_small);
+  if (c->h_seg) cudaFreeHost(c->h_seg);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return OBVHS_OK;
@@ -626,6 +828,52 @@ int obvhs_build_cwbvh_from_tris_batch(obvhs_ctx* const* ctxs, uint32_t n_ctx, co
   return r;
 }
 
+int obvhs_build_cwbvh_from_tris_segmented(obvhs_ctx* cp, const float* const* triangles, const uint32_t* n_tris,
+                                          uint32_t n_scenes, const obvhs_build_params* p, int device_ptrs,
+                                          obvhs_cwbvh** out, obvhs_build_stats* stats) {
+  if (!cp || !p || (n_scenes && (!triangles || !n_tris || !out))) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  for (uint32_t i = 0; i < n_scenes; i++) {
+    out[i] = nullptr;
+    if (n_tris[i] && !triangles[i]) return OBVHS_ERR_INVALID_ARG;
+  }
+  if (!n_scenes) return OBVHS_OK;
+  // host triangles: staged into one device buffer
+  std::vector<const float*> dt(triangles, triangles + n_scenes);
+  if (!device_ptrs) {
+    size_t total = 0;
+    for (uint32_t i = 0; i < n_scenes; i++) total += (size_t)n_tris[i] * 36;
+    char* d = (char*)c.scratch.get(SLOT_INPUT, total);
+    if (!d) return c.fail(OBVHS_ERR_OOM, "input staging");
+    size_t at = 0;
+    for (uint32_t i = 0; i < n_scenes; i++) {
+      if (n_tris[i]) CK(cudaMemcpyAsync(d + at, triangles[i], (size_t)n_tris[i] * 36, cudaMemcpyHostToDevice, c.stream));
+      dt[i] = reinterpret_cast<const float*>(d + at);
+      at += (size_t)n_tris[i] * 36;
+    }
+  }
+  // chunks of at most SEG_MAX_SCENES scenes and 2^29 triangles
+  uint32_t first = 0;
+  while (first < n_scenes) {
+    uint32_t last = first;
+    uint64_t tris = 0;
+    while (last < n_scenes && last - first < OBVHS_SEG_MAX_SCENES && (last == first || tris + n_tris[last] <= (1u << 29)))
+      tris += n_tris[last++];
+    const int r = seg_pipeline(c, dt.data() + first, n_tris + first, last - first, p, out + first,
+                               stats ? stats + first : nullptr);
+    if (r) {
+      for (uint32_t i = 0; i < n_scenes; i++) {
+        obvhs_cwbvh_free(out[i]);
+        out[i] = nullptr;
+      }
+      return r;
+    }
+    first = last;
+  }
+  return OBVHS_OK;
+}
+
 int obvhs_ray_traverse_multi(obvhs_ctx* cp, const obvhs_cwbvh* const* bvhs, uint32_t n_bvh, const uint32_t* ray_bvh,
                              const obvhs_ray* rays, uint32_t n, obvhs_hit* hits, int device_ptrs) {
   if (!cp || (n_bvh && !bvhs) || (n && (!rays || !hits || !ray_bvh))) return OBVHS_ERR_INVALID_ARG;
@@ -752,10 +1000,10 @@ int obvhs_cwbvh_download_compressed(obvhs_ctx* cp, const obvhs_cwbvh* b, void* t
 
 int obvhs_cwbvh_free(obvhs_cwbvh* b) {
   if (!b) return OBVHS_OK;
-  if (b->nodes) cudaFree(b->nodes);
-  if (b->prim_indices) cudaFree(b->prim_indices);
-  if (b->tris) cudaFree(b->tris);
-  if (b->ctris) cudaFree(b->ctris);
+  b->free_buf(b->nodes);
+  b->free_buf(b->prim_indices);
+  b->free_buf(b->tris);
+  b->free_buf(b->ctris);
   delete b;
   return OBVHS_OK;
 }

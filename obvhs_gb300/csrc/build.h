@@ -4,6 +4,8 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
+#include <functional>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -58,6 +60,9 @@ enum ScratchSlot {
   SLOT_STARTS,
   SLOT_PLIST,
   SLOT_BLAS_DESC,
+  SLOT_SEG,  // segmented builds: per-scene tables
+  SLOT_SEG_AABBS,
+  SLOT_SEG_IDX,
   SLOT_COUNT
 };
 
@@ -129,6 +134,8 @@ struct obvhs_ctx {
   uint32_t* h_status = nullptr;  // pinned
   uint32_t* h_hist = nullptr;    // pinned, 16 * 256
   void* h_small = nullptr;       // pinned, 4 KB
+  void* h_seg = nullptr;         // pinned staging of segmented-build tables (grow-only)
+  size_t h_seg_cap = 0;
   Scratch scratch;
   std::string last_error;
   uint64_t kernel_launches = 0;
@@ -210,6 +217,15 @@ struct obvhs_cwbvh {
   uint32_t n_tris = 0;
   uint2* ctris = nullptr;  // BVH order: RtCompressedTriangle, 24 B each (three 8-byte words)
   int uses_spatial_splits = 0;
+  // A segmented build places all its trees in one allocation: buffers inside
+  // [block_lo, block_hi) belong to it, and it is released with the last tree.
+  std::shared_ptr<void> block;
+  const char* block_lo = nullptr;
+  const char* block_hi = nullptr;
+  void free_buf(void* p) const {
+    const char* q = static_cast<const char*>(p);
+    if (p && !(block && q >= block_lo && q < block_hi)) cudaFree(p);
+  }
 };
 
 // ploc.cu
@@ -225,6 +241,33 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
                       uint64_t* sum_counts_out, PlocState* deferred = nullptr);
 int ploc_setup_kernels();
 
+// Segmented builds: many scenes through every stage together, one launch
+// per stage for all of them.  Scene s owns primitives / leaves
+// [prim_start[s], prim_start[s + 1]) of the concatenated arrays and BVH2 node
+// slots [node_start[s], node_start[s] + 2 m_s) (m_s = its leaf count): its
+// root at node_start[s], its last slot an inert pad.  node_start is even, so
+// sibling parity (left children odd) matches a one-scene build; child and
+// leaf indices in the nodes are global, and every root is its own parent.
+constexpr uint32_t SEG_PAD_CHILD = 0xfffffff0u;
+struct SegLayout {
+  uint32_t n_seg = 0;
+  std::vector<uint32_t> prim_start, node_start;  // host copies, n_seg + 1
+  const uint32_t* d_prim_start = nullptr;        // device copies
+  const uint32_t* d_node_start = nullptr;
+  uint32_t n_prims = 0, n_slots = 0, max_m = 0;
+  uint32_t leaves(uint32_t s) const { return prim_start[s + 1] - prim_start[s]; }
+};
+// Leaves of every scene (triangles through the device pointer table d_tris,
+// or concatenated AABBs + scene-local ids), the concatenated primitive-index
+// array (scene-local ids) and each scene's total AABB keys (8 ints a scene).
+int seg_leaves_device(BuildCtx& c, const SegLayout& L, const float* const* d_tris, const float* aabbs,
+                      const uint32_t* idx, Bvh2Node* leaves, uint32_t* pidx, int* total_keys);
+// Morton codes, segmented sort and all PLOC passes of every scene (one
+// cooperative launch); d_passes / d_sum_counts receive per-scene statistics.
+int ploc_seg_device(BuildCtx& c, const SegLayout& L, const Bvh2Node* leaves, const int* total_keys, uint32_t radius,
+                    int precision, uint32_t depth_threshold, Bvh2Node* out, uint32_t* d_passes,
+                    unsigned long long* d_sum_counts);
+
 // presplit.cu
 int presplit_device(BuildCtx& c, const float* tris, uint32_t n, float** aabbs_out, uint32_t** idx_out,
                     uint32_t* m_out, bool thresholds_only = false);
@@ -237,6 +280,17 @@ int split_thresholds_device(BuildCtx& c, const float* tris, uint32_t n, float* o
 int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const float* seq, uint32_t nseq,
                        uint64_t* applied_out, int64_t root_prims = -1, uint32_t* applied_deferred = nullptr);
 int compute_parents_device(BuildCtx& c, const Bvh2Node* nodes, uint32_t n_nodes, uint32_t* parents);
+// Copies a host table to the device (stream-ordered, from pinned staging);
+// returns the device address or null.
+typedef std::function<uint32_t*(const void* src, size_t bytes)> SegTableUpload;
+// Every scene's root becomes its own parent.
+int seg_root_parents_device(BuildCtx& c, const SegLayout& L, uint32_t* parents);
+// The 16 reinsertion passes of every scene (reinsertion.rs:101-115 per
+// scene), each pass one candidate sort, one search and one resolve launch for
+// all scenes.  h_passes: each scene's PLOC passes (its stack bound).  The
+// applied total is copied to pinned *applied_deferred.
+int reinsertion_seg_device(BuildCtx& c, Bvh2Node* nodes, const SegLayout& L, const uint32_t* h_passes, float ratio,
+                           SegTableUpload upload, uint32_t* applied_deferred);
 
 // cwbvh.cu
 // With `emitted_deferred` (pinned) the number of emitted nodes is copied there
@@ -245,7 +299,26 @@ int compute_parents_device(BuildCtx& c, const Bvh2Node* nodes, uint32_t n_nodes,
 int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, int order_children, obvhs_cwbvh* out,
                          uint32_t* emitted_deferred = nullptr);
 
+// Segmented conversion of every scene's BVH2 into its own CWBVH (outs[s]);
+// all outputs share one allocation.  h_tris / h_ntris (host array of device
+// pointers, or null): each scene's triangles, attached in BVH order.  The
+// emitted node count goes to pinned *emitted_deferred, to be compared with
+// *emitted_expected after the caller's final synchronisation.
+int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in, const SegLayout& L,
+                     uint32_t max_prims, int order_children, const float* const* h_tris, const uint32_t* h_ntris,
+                     int uses_spatial_splits, SegTableUpload upload, std::vector<obvhs_cwbvh*>& outs,
+                     uint32_t* emitted_deferred, uint32_t* emitted_expected);
+
 // traverse.cu
+// One scene's triangles to reorder: tris[pidx[k]] -> out[k], k < its primitive count.
+struct SegTriJob {
+  const float* tris;
+  uint32_t n_tris;
+  const uint32_t* pidx;
+  float4* out;
+};
+int reorder_tris_seg_device(BuildCtx& c, const SegTriJob* d_jobs, const uint32_t* d_prim_start, uint32_t n_seg,
+                            uint32_t total);
 int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint32_t n, uint32_t* hits,
                     uint8_t* miss, int mode);
 int reorder_tris_device(BuildCtx& c, obvhs_cwbvh* bvh, const float* tris, uint32_t n_tris);

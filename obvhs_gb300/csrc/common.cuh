@@ -108,3 +108,19 @@ template <class T>
 __host__ __device__ __forceinline__ T div_up(T a, T b) {
   return (a + b - 1) / b;
 }
+
+// Segmented builds keep many scenes in concatenated arrays; segment s owns
+// indices [start[s], start[s + 1]).  The segment holding index i: the last s
+// in [0, n_seg) with start[s] <= i (start ascending, start[0] = 0; empty
+// segments resolve to the next non-empty one).
+__device__ __forceinline__ uint32_t seg_find(const uint32_t* start, uint32_t n_seg, uint32_t i) {
+  uint32_t lo = 0, hi = n_seg;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(&start[mid]) <= i)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}

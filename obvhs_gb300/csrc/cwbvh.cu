@@ -182,15 +182,18 @@ __global__ void __launch_bounds__(BLK) k_costs(const Bvh2Node* __restrict__ node
     d.nprim = 1;
     st_dec(&dec[i], d);
   }
-  if (i == 0) return;
+  // roots are their own parents (one tree: node 0; several trees in one
+  // array: each tree's first node)
   uint32_t p = parents[i];
+  if (p == i) return;
   for (uint32_t guard = 0; guard < n; guard++) {
     __threadfence();
     if (atomicAdd(&flags[p], 1u) == 0) return;
     __threadfence();
     inner_costs(nodes, dec, p, max_prims);
-    if (p == 0) return;
-    p = parents[p];
+    const uint32_t up = parents[p];
+    if (up == p) return;
+    p = up;
   }
   set_status(status, ST_ITER_LIMIT);
 }
@@ -258,6 +261,12 @@ __device__ __forceinline__ float3 center(const Box& b) {
 // Emission work queue: items[k] describes CWBVH node k's source; it is
 // published (ready[k] = 1) by the warp that emits its parent.  Warps take
 // indices in order from `head` and append children at `tail`.
+struct EmitOut {
+  CwNode* cw;
+  uint32_t* pidx;
+  uint32_t max_nodes, max_prims;
+};
+
 struct EmitArgs {
   uint32_t log2_thr[256];  // ceil_log2_thresholds()
   const Bvh2Node* nodes;
@@ -268,9 +277,12 @@ struct EmitArgs {
   uint32_t* head;
   uint32_t* tail;
   int order_children;
-  uint32_t max_nodes, max_prims_out;
-  CwNode* cw;
-  uint32_t* pidx_out;
+  uint32_t queue_cap;  // items: the CWBVH nodes of all trees
+  EmitOut one;         // one tree: its output
+  // several trees (segmented): tree s's output, s from the item's BVH2 node
+  const EmitOut* seg_out;
+  const uint32_t* node_start;
+  uint32_t n_seg;
   uint32_t* status;
   uint32_t* processed;
 };
@@ -290,6 +302,7 @@ __device__ __forceinline__ uint32_t slot_excl_scan(uint32_t v, int lane, uint32_
 // convert_to_cwbvh_impl (src/cwbvh/bvh2_to_cwbvh.rs:75-193) for one node;
 // the whole warp works on it, lane s on child slot s.
 __device__ void emit_node(const EmitArgs& a, const Item it, int lane, uint8_t* stage) {
+  const EmitOut o = a.seg_out ? a.seg_out[seg_find(a.node_start, a.n_seg, it.bvh2)] : a.one;
   const Bvh2Node nd = ld_node(&a.nodes[it.bvh2]);
   const Box box = node_box(nd);
   const float3 p = box.mn;
@@ -431,8 +444,8 @@ __device__ void emit_node(const EmitArgs& a, const Item it, int lane, uint8_t* s
       const Bvh2Node xn = ld_node(&a.nodes[x]);
       if (node_prims(xn) != 0) {
         const uint32_t slot = it.prim_base + leaf_off + k;
-        if (slot < a.max_prims_out)
-          a.pidx_out[slot] = a.pidx_in[node_first(xn)];
+        if (slot < o.max_prims)
+          o.pidx[slot] = a.pidx_in[node_first(xn)];
         else
           set_status(a.status, ST_CAPACITY);
         k += node_prims(xn);
@@ -451,7 +464,7 @@ __device__ void emit_node(const EmitArgs& a, const Item it, int lane, uint8_t* s
     const uint32_t cb = it.child_base + n_int + sub_node_off;
     const uint32_t pb = it.prim_base + n_leafprims + sub_prim_off;
     const uint32_t q = out_base + int_rank;
-    if (q < a.max_nodes) {
+    if (q < a.queue_cap) {
       a.items[q] = Item{slot_child, it.child_base + int_rank, cb, pb};
       __threadfence();
       atomicExch(&a.ready[q], 1u);
@@ -482,10 +495,10 @@ __device__ void emit_node(const EmitArgs& a, const Item it, int lane, uint8_t* s
     stage[72 + lane] = q[5];
   }
   __syncwarp();
-  if (it.cw >= a.max_nodes) {
+  if (it.cw >= o.max_nodes) {
     if (lane == 0) set_status(a.status, ST_CAPACITY);
   } else if (lane < 5) {
-    a.cw[it.cw].q[lane] = reinterpret_cast<const uint4*>(stage)[lane];
+    o.cw[it.cw].q[lane] = reinterpret_cast<const uint4*>(stage)[lane];
   }
   __syncwarp();
 }
@@ -498,7 +511,7 @@ __global__ void __launch_bounds__(EMIT_THREADS) k_emit_all(EmitArgs a) {
     uint32_t k = 0;
     if (lane == 0) k = atomicAdd(a.head, 1u);
     k = __shfl_sync(0xffffffffu, k, 0);
-    if (k >= a.max_nodes) break;
+    if (k >= a.queue_cap) break;
     // wait for the parent's warp to publish item k (bounded)
     uint32_t ok = 1;
     if (lane == 0) {
@@ -525,6 +538,43 @@ __global__ void __launch_bounds__(EMIT_THREADS) k_emit_all(EmitArgs a) {
     mine++;
   }
   if (lane == 0 && mine) atomicAdd(a.processed, mine);
+}
+
+// Segmented conversion: each scene's root decision record and box, read back
+// to size the outputs.
+struct SegRoot {
+  Dec d;
+  float box[8];
+};
+static_assert(sizeof(SegRoot) == 128, "SegRoot layout");
+
+__global__ void k_seg_roots_out(const Bvh2Node* __restrict__ nodes, const Dec* dec,
+                                const uint32_t* __restrict__ prim_start, const uint32_t* __restrict__ node_start,
+                                uint32_t n_seg, SegRoot* __restrict__ out) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_seg || prim_start[s + 1] == prim_start[s]) return;
+  const uint32_t nb = node_start[s];
+  out[s].d = ld_dec_cg(&dec[nb]);
+  const Bvh2Node nd = ld_node(&nodes[nb]);
+  float4* b = reinterpret_cast<float4*>(out[s].box);
+  b[0] = nd.a;
+  b[1] = nd.b;
+}
+
+// The work queue of a segmented emission starts with every scene's root.
+__global__ void k_seg_emit_init(const uint32_t* __restrict__ prim_start, const uint32_t* __restrict__ node_start,
+                                const uint32_t* __restrict__ root_slot, uint32_t n_seg, uint32_t n_roots,
+                                Item* __restrict__ items, uint32_t* __restrict__ ready, uint32_t* __restrict__ ctr) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) {
+    ctr[0] = 0;        // head
+    ctr[1] = n_roots;  // tail
+    ctr[2] = 0;        // processed
+  }
+  if (s >= n_seg || prim_start[s + 1] == prim_start[s]) return;
+  const uint32_t q = root_slot[s];
+  items[q] = Item{node_start[s], 0, 1, 0};
+  ready[q] = 1;
 }
 
 }  // namespace
@@ -623,8 +673,8 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   CK(cudaMemcpyAsync(items, hst, 16, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(ready, hst + 4, 4, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(counters + 12, hst + 5, 12, cudaMemcpyHostToDevice, c.stream));
-  EmitArgs ea{{}, b->nodes, b->prim_indices, dec, items, ready, counters + 12, counters + 13, order_children, n_cw, n_pr,
-              cwn, cwp, c.d_status, counters + 14};
+  EmitArgs ea{{},     b->nodes,      b->prim_indices, dec, items, ready, counters + 12, counters + 13, order_children,
+              n_cw,   EmitOut{cwn, cwp, n_cw, n_pr}, nullptr, nullptr, 0, c.d_status, counters + 14};
   std::memcpy(ea.log2_thr, ceil_log2_thresholds(), sizeof(ea.log2_thr));
   const uint32_t grid = (uint32_t)std::min<uint64_t>(
       emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)n_cw * 32, EMIT_THREADS)));
@@ -649,6 +699,153 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
     out->prim_indices = nullptr;
     out->n_nodes = out->n_prims = 0;
     return c.fail(OBVHS_ERR_BAD_INPUT, "CWBVH emission failed (status " + std::to_string(*c.h_status) + ")");
+  }
+  return 0;
+}
+
+int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in, const SegLayout& L,
+                     uint32_t max_prims, int order_children, const float* const* h_tris, const uint32_t* h_ntris,
+                     int uses_spatial_splits, SegTableUpload upload, std::vector<obvhs_cwbvh*>& outs,
+                     uint32_t* emitted_deferred, uint32_t* emitted_expected) {
+  const uint32_t S = L.n_seg, n = L.n_slots;
+  outs.assign(S, nullptr);
+  *emitted_deferred = 0;
+  *emitted_expected = 0;
+  auto make_empty = [&](uint32_t s) {
+    obvhs_cwbvh* o = new obvhs_cwbvh();
+    o->ctx = &c;
+    o->n_tris = h_tris ? h_ntris[s] : 0;
+    o->uses_spatial_splits = uses_spatial_splits;
+    outs[s] = o;
+    return o;
+  };
+  if (n == 0) {
+    for (uint32_t s = 0; s < S; s++) make_empty(s);
+    return 0;
+  }
+  Scratch& sc = c.scratch;
+  uint32_t* parents = (uint32_t*)sc.get(SLOT_PARENTS, (size_t)n * 4);
+  uint32_t* flags = (uint32_t*)sc.get(SLOT_FLAGS, (size_t)n * 4);
+  Dec* dec = (Dec*)sc.get(SLOT_DECISIONS, (size_t)n * sizeof(Dec));
+  uint32_t* counters = (uint32_t*)sc.get(SLOT_CW_COUNTERS, 64);
+  SegRoot* roots = (SegRoot*)sc.get(SLOT_OUTPUT, (size_t)S * sizeof(SegRoot));
+  if (!parents || !flags || !dec || !counters || !roots) return c.fail(OBVHS_ERR_OOM, "scratch");
+  int r = compute_parents_device(c, nodes, n, parents);
+  if (r) return r;
+  r = seg_root_parents_device(c, L, parents);
+  if (r) return r;
+  CK(cudaMemsetAsync(flags, 0, (size_t)n * 4, c.stream));
+  KLAUNCH("k_costs", k_costs<<<div_up<uint32_t>(n, BLK), BLK, 0, c.stream>>>(nodes, parents, n, max_prims, dec, flags,
+                                                                             c.d_status));
+  KLAUNCH("k_seg_roots_out", k_seg_roots_out<<<div_up<uint32_t>(S, BLK), BLK, 0, c.stream>>>(
+                                 nodes, dec, L.d_prim_start, L.d_node_start, S, roots));
+  CK(cudaGetLastError());
+  std::vector<SegRoot> hr(S);
+  CK(cudaMemcpyAsync(hr.data(), roots, (size_t)S * sizeof(SegRoot), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(c.h_status, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  if (*c.h_status)
+    return c.fail(OBVHS_ERR_BAD_INPUT, "BVH2 cannot be converted (a leaf holds more than one primitive)");
+  // sizes, and one allocation for every scene's nodes, indices and triangles
+  std::vector<uint32_t> n_cw(S), n_pr(S);
+  std::vector<size_t> off(3 * (size_t)S);
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  size_t total = 0;
+  uint32_t q_total = 0, pr_total = 0;
+  for (uint32_t s = 0; s < S; s++) {
+    const uint32_t m = L.leaves(s);
+    if (m == 0) {
+      n_cw[s] = n_pr[s] = 0;
+    } else if (m == 1) {
+      n_cw[s] = 1;
+      n_pr[s] = hr[s].d.nprim;
+    } else {
+      if (hr[s].d.agg[0].x == AGG_INVALID)
+        return c.fail(OBVHS_ERR_BAD_INPUT, "BVH2 cannot be converted (no finite distribution of the root)");
+      n_cw[s] = 1 + hr[s].d.agg[0].x;
+      n_pr[s] = hr[s].d.nprim;
+    }
+    off[3 * s] = total;
+    total += al((size_t)n_cw[s] * sizeof(CwNode));
+    off[3 * s + 1] = total;
+    total += al((size_t)n_pr[s] * 4);
+    off[3 * s + 2] = total;
+    if (h_tris) total += al((size_t)n_pr[s] * 64);
+    q_total += n_cw[s];
+    pr_total += n_pr[s];
+  }
+  char* blk = nullptr;
+  if (cudaMallocAsync((void**)&blk, std::max<size_t>(total, 256), c.stream) != cudaSuccess) {
+    cudaGetLastError();
+    return c.fail(OBVHS_ERR_OOM, "cwbvh output");
+  }
+  std::shared_ptr<void> block(blk, [](void* p) { cudaFree(p); });
+  std::vector<EmitOut> eo(S);
+  std::vector<SegTriJob> jobs(h_tris ? S : 0);
+  std::vector<uint32_t> slots(2 * (size_t)S + 1);  // root_slot[S], then prim starts [S + 1]
+  uint32_t n_roots = 0, pr_acc = 0;
+  for (uint32_t s = 0; s < S; s++) {
+    obvhs_cwbvh* o = make_empty(s);
+    o->block = block;
+    o->block_lo = blk;
+    o->block_hi = blk + total;
+    eo[s] = EmitOut{nullptr, nullptr, 0, 0};
+    slots[s] = n_roots;
+    slots[S + s] = pr_acc;
+    pr_acc += n_pr[s];
+    if (n_cw[s] == 0) continue;
+    n_roots++;
+    o->nodes = reinterpret_cast<CwNode*>(blk + off[3 * s]);
+    o->n_nodes = n_cw[s];
+    o->prim_indices = n_pr[s] ? reinterpret_cast<uint32_t*>(blk + off[3 * s + 1]) : nullptr;
+    o->n_prims = n_pr[s];
+    o->total_aabb[0] = hr[s].box[0];
+    o->total_aabb[1] = hr[s].box[1];
+    o->total_aabb[2] = hr[s].box[2];
+    o->total_aabb[3] = hr[s].box[4];
+    o->total_aabb[4] = hr[s].box[5];
+    o->total_aabb[5] = hr[s].box[6];
+    eo[s] = EmitOut{o->nodes, o->prim_indices, n_cw[s], n_pr[s]};
+    if (h_tris && n_pr[s]) {
+      o->tris = reinterpret_cast<float4*>(blk + off[3 * s + 2]);
+      jobs[s] = SegTriJob{h_tris[s], h_ntris[s], o->prim_indices, o->tris};
+    } else if (h_tris) {
+      jobs[s] = SegTriJob{nullptr, 0, nullptr, nullptr};
+    }
+  }
+  slots[2 * (size_t)S] = pr_acc;
+  const EmitOut* d_eo = reinterpret_cast<const EmitOut*>(upload(eo.data(), eo.size() * sizeof(EmitOut)));
+  const uint32_t* d_slots = upload(slots.data(), slots.size() * 4);
+  if (!d_eo || !d_slots) return c.fail(OBVHS_ERR_OOM, "segment tables");
+  Item* items = (Item*)sc.get(SLOT_FRONTIER_A, (size_t)std::max(q_total, 1u) * sizeof(Item));
+  uint32_t* ready = (uint32_t*)sc.get(SLOT_FRONTIER_B, (size_t)std::max(q_total, 1u) * 4);
+  if (!items || !ready) return c.fail(OBVHS_ERR_OOM, "scratch");
+  static std::atomic<int> emit_blocks_s{0};
+  int emit_blocks = emit_blocks_s.load();
+  if (!emit_blocks) {
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_all, EMIT_THREADS, 0));
+    emit_blocks = std::max(1, per_sm) * c.num_sms;
+    emit_blocks_s.store(emit_blocks);
+  }
+  CK(cudaMemsetAsync(ready, 0, (size_t)q_total * 4, c.stream));
+  KLAUNCH("k_seg_emit_init", k_seg_emit_init<<<div_up<uint32_t>(S, BLK), BLK, 0, c.stream>>>(
+                                 L.d_prim_start, L.d_node_start, d_slots, S, n_roots, items, ready, counters + 12));
+  EmitArgs ea{{},      nodes,     pidx_in,         dec,      items,      ready, counters + 12, counters + 13,
+              order_children, q_total, EmitOut{nullptr, nullptr, 0, 0}, d_eo, L.d_node_start, S, c.d_status,
+              counters + 14};
+  std::memcpy(ea.log2_thr, ceil_log2_thresholds(), sizeof(ea.log2_thr));
+  const uint32_t grid = (uint32_t)std::min<uint64_t>(
+      emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)q_total * 32, EMIT_THREADS)));
+  KLAUNCH("k_emit_all", k_emit_all<<<grid, EMIT_THREADS, 0, c.stream>>>(ea));
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(emitted_deferred, counters + 14, 4, cudaMemcpyDeviceToHost, c.stream));
+  *emitted_expected = q_total;
+  if (h_tris && pr_total) {
+    const SegTriJob* d_jobs = reinterpret_cast<const SegTriJob*>(upload(jobs.data(), jobs.size() * sizeof(SegTriJob)));
+    if (!d_jobs) return c.fail(OBVHS_ERR_OOM, "segment tables");
+    r = reorder_tris_seg_device(c, d_jobs, d_slots + S, S, pr_total);
+    if (r) return r;
   }
   return 0;
 }

@@ -159,26 +159,16 @@ __device__ __forceinline__ Scale make_scale(const int* tk) {
   return s;
 }
 
-__global__ void __launch_bounds__(BLK) k_morton64(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
-                                                  unsigned long long* __restrict__ codes) {
-  uint32_t i = blockIdx.x * BLK + threadIdx.x;
-  if (i >= n) return;
-  Scale s = make_scale(total_keys);
-  Bvh2Node nd = ld_node(&leaves[i]);
+__device__ __forceinline__ unsigned long long morton64_of(const Bvh2Node& nd, const Scale& s) {
   float cx = (nd.b.x + nd.a.x) * 0.5f, cy = (nd.b.y + nd.a.y) * 0.5f, cz = (nd.b.z + nd.a.z) * 0.5f;
   double px = __dadd_rn(__dmul_rn((double)cx, s.sx), s.ox);
   double py = __dadd_rn(__dmul_rn((double)cy, s.sy), s.oy);
   double pz = __dadd_rn(__dmul_rn((double)cz, s.sz), s.oz);
   const double k = (double)(1u << 21);
-  codes[i] = split3_u64(sat_u32(px * k)) | split3_u64(sat_u32(py * k)) << 1 | split3_u64(sat_u32(pz * k)) << 2;
+  return split3_u64(sat_u32(px * k)) | split3_u64(sat_u32(py * k)) << 1 | split3_u64(sat_u32(pz * k)) << 2;
 }
 
-__global__ void __launch_bounds__(BLK) k_morton128(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
-                                                   U128* __restrict__ codes) {
-  uint32_t i = blockIdx.x * BLK + threadIdx.x;
-  if (i >= n) return;
-  Scale s = make_scale(total_keys);
-  Bvh2Node nd = ld_node(&leaves[i]);
+__device__ __forceinline__ U128 morton128_of(const Bvh2Node& nd, const Scale& s) {
   float cx = (nd.b.x + nd.a.x) * 0.5f, cy = (nd.b.y + nd.a.y) * 0.5f, cz = (nd.b.z + nd.a.z) * 0.5f;
   double px = __dadd_rn(__dmul_rn((double)cx, s.sx), s.ox);
   double py = __dadd_rn(__dmul_rn((double)cy, s.sy), s.oy);
@@ -192,7 +182,124 @@ __global__ void __launch_bounds__(BLK) k_morton128(const Bvh2Node* __restrict__ 
   U128 c;
   c.lo = xl | (yl << 1) | (zl << 2);
   c.hi = xh | (yh << 1) | (yl >> 63) | (zh << 2) | (zl >> 62);
-  codes[i] = c;
+  return c;
+}
+
+__global__ void __launch_bounds__(BLK) k_morton64(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
+                                                  unsigned long long* __restrict__ codes) {
+  uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  if (i >= n) return;
+  codes[i] = morton64_of(ld_node(&leaves[i]), make_scale(total_keys));
+}
+
+__global__ void __launch_bounds__(BLK) k_morton128(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
+                                                   U128* __restrict__ codes) {
+  uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  if (i >= n) return;
+  codes[i] = morton128_of(ld_node(&leaves[i]), make_scale(total_keys));
+}
+
+// --- segmented leaves, Morton codes and scene keys ----------------------------
+//
+// Scene s owns leaves [prim_start[s], prim_start[s + 1]); its total AABB is
+// total_keys[8 s .. 8 s + 5].  A leaf's first index is its global position
+// (into the concatenated primitive-index array, which holds the scene-local
+// triangle id).
+
+// Per-scene total: a block inside one scene reduces as in the one-scene
+// kernels; a block that straddles scenes falls back to atomics per leaf.
+__device__ __forceinline__ void seg_reduce_box(const Box& b, bool valid, uint32_t s, uint32_t s_block, int* total_keys,
+                                               uint32_t* status) {
+  if (__syncthreads_and(!valid || s == s_block)) {
+    reduce_box(b, total_keys + 8 * (size_t)s_block, status, valid);
+    return;
+  }
+  if (!valid) return;
+  int* k = total_keys + 8 * (size_t)s;
+  atomicMin(&k[0], min(fkey(b.mn.x), fkey(b.mx.x)));
+  atomicMin(&k[1], min(fkey(b.mn.y), fkey(b.mx.y)));
+  atomicMin(&k[2], min(fkey(b.mn.z), fkey(b.mx.z)));
+  atomicMax(&k[3], max(fkey(b.mn.x), fkey(b.mx.x)));
+  atomicMax(&k[4], max(fkey(b.mn.y), fkey(b.mx.y)));
+  atomicMax(&k[5], max(fkey(b.mn.z), fkey(b.mx.z)));
+}
+
+// Leaves of triangle scenes: scene s's triangles at tris[s] (n x 9 floats).
+__global__ void __launch_bounds__(BLK) k_seg_leaves_tris(const float* const* __restrict__ tris,
+                                                         const uint32_t* __restrict__ prim_start, uint32_t n_seg,
+                                                         uint32_t n, Bvh2Node* __restrict__ leaves,
+                                                         uint32_t* __restrict__ pidx, int* total_keys,
+                                                         uint32_t* status) {
+  const uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  const bool valid = i < n;
+  const uint32_t s_block = seg_find(prim_start, n_seg, blockIdx.x * BLK);
+  uint32_t s = s_block;
+  Box b{};
+  if (valid) {
+    s = seg_find(prim_start, n_seg, i);
+    const uint32_t local = i - __ldg(&prim_start[s]);
+    const float* t = tris[s] + (size_t)local * 9;
+    float3 v0 = make_float3(t[0], t[1], t[2]), v1 = make_float3(t[3], t[4], t[5]), v2 = make_float3(t[6], t[7], t[8]);
+    b.mn = make_float3(smin(smin(v0.x, v1.x), v2.x), smin(smin(v0.y, v1.y), v2.y), smin(smin(v0.z, v1.z), v2.z));
+    b.mx = make_float3(smax(smax(v0.x, v1.x), v2.x), smax(smax(v0.y, v1.y), v2.y), smax(smax(v0.z, v1.z), v2.z));
+    if (box_has_nan(b)) set_status(status, ST_BAD_INPUT);
+    st_node(&leaves[i], make_node(b, 1, i));
+    pidx[i] = local;
+  }
+  seg_reduce_box(b, valid, s, s_block, total_keys, status);
+}
+
+// Leaves from concatenated AABBs (n x 6) with scene-local primitive ids.
+__global__ void __launch_bounds__(BLK) k_seg_leaves_aabbs(const float* __restrict__ aabbs,
+                                                          const uint32_t* __restrict__ idx,
+                                                          const uint32_t* __restrict__ prim_start, uint32_t n_seg,
+                                                          uint32_t n, Bvh2Node* __restrict__ leaves,
+                                                          uint32_t* __restrict__ pidx, int* total_keys,
+                                                          uint32_t* status) {
+  const uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  const bool valid = i < n;
+  const uint32_t s_block = seg_find(prim_start, n_seg, blockIdx.x * BLK);
+  uint32_t s = s_block;
+  Box b{};
+  if (valid) {
+    s = seg_find(prim_start, n_seg, i);
+    const float* a = aabbs + (size_t)i * 6;
+    b.mn = make_float3(a[0], a[1], a[2]);
+    b.mx = make_float3(a[3], a[4], a[5]);
+    if (box_has_nan(b)) set_status(status, ST_BAD_INPUT);
+    st_node(&leaves[i], make_node(b, 1, i));
+    pidx[i] = idx[i];
+  }
+  seg_reduce_box(b, valid, s, s_block, total_keys, status);
+}
+
+template <bool WIDE>
+__global__ void __launch_bounds__(BLK) k_seg_morton(const Bvh2Node* __restrict__ leaves,
+                                                    const uint32_t* __restrict__ prim_start, uint32_t n_seg, uint32_t n,
+                                                    const int* total_keys, void* __restrict__ codes) {
+  const uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t s = seg_find(prim_start, n_seg, i);
+  const Scale sc = make_scale(total_keys + 8 * (size_t)s);
+  const Bvh2Node nd = ld_node(&leaves[i]);
+  if (WIDE)
+    static_cast<U128*>(codes)[i] = morton128_of(nd, sc);
+  else
+    static_cast<unsigned long long*>(codes)[i] = morton64_of(nd, sc);
+}
+
+// Scene of each sorted leaf (its value is the leaf's global position), for
+// the stable pass that groups the Morton order by scene.
+__global__ void __launch_bounds__(BLK) k_seg_scene_keys(const uint32_t* __restrict__ order,
+                                                        const uint32_t* __restrict__ prim_start, uint32_t n_seg,
+                                                        uint32_t n, uint32_t* __restrict__ keys) {
+  const uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  if (i < n) keys[i] = seg_find(prim_start, n_seg, order[i]);
+}
+
+__global__ void __launch_bounds__(BLK) k_seg_init_totals(int* total_keys, uint32_t n_seg) {
+  const uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  if (i < 8 * n_seg) total_keys[i] = (i & 7) < 3 ? 0x7fffffff : (int)0x80000000;
 }
 
 __global__ void __launch_bounds__(BLK) k_gather(const Bvh2Node* __restrict__ in, const uint32_t* __restrict__ order,
@@ -210,12 +317,6 @@ __device__ __forceinline__ float pair_cost(const Box& lo, const Box& hi) { retur
 __device__ __forceinline__ Box load_box_cg(const Bvh2Node* p) {
   const float4* q = reinterpret_cast<const float4*>(p);
   const float4 a = __ldcg(q), b = __ldcg(q + 1);
-  return Box{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)};
-}
-
-__device__ __forceinline__ Box load_box(const Bvh2Node* p) {
-  const float4* q = reinterpret_cast<const float4*>(p);
-  float4 a = q[0], b = q[1];
   return Box{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)};
 }
 
@@ -268,13 +369,195 @@ __device__ __forceinline__ void group_sync(int group) {
   asm volatile("bar.sync %0, %1;" ::"r"(1 + group), "r"(PT) : "memory");
 }
 
+// Phase A of a pass for one tile of a cluster list cur[0, count): the merge
+// offsets of clusters [base, base + chunk) into merge[], computed from boxes
+// staged with a 2*radius halo (the offsets of the +-radius neighbours are
+// recomputed locally, so the emit/merge flags need no exchange), and the
+// tile's (emitted, merged) counts into *cnt.  Called by the PT threads of one
+// group.
+__device__ __forceinline__ void ploc_tile_offsets(CoopGroupSmem& sm, int group, const Bvh2Node* cur, uint32_t count,
+                                                  uint32_t base, uint32_t chunk, int ipt, int r, bool d1,
+                                                  int8_t* merge, uint2* cnt) {
+  const int tid = threadIdx.x % PT, lane = tid & 31, warp = tid >> 5;
+  const int64_t box_lo = (int64_t)base - 2 * r;
+  const uint32_t box_span = chunk + 4 * r;
+  group_sync(group);  // the previous tile's shared data is consumed
+  for (uint32_t k = tid; k < box_span; k += PT) {
+    const int64_t j = box_lo + k;
+    if (j >= 0 && j < (int64_t)count) {
+      const Box b = load_box_cg(&cur[j]);
+      sm.box[0 * BOXS + k] = b.mn.x;
+      sm.box[1 * BOXS + k] = b.mn.y;
+      sm.box[2 * BOXS + k] = b.mn.z;
+      sm.box[3 * BOXS + k] = b.mx.x;
+      sm.box[4 * BOXS + k] = b.mx.y;
+      sm.box[5 * BOXS + k] = b.mx.z;
+    }
+  }
+  group_sync(group);
+  const int lo32 = (int)box_lo;
+#define PBOX(J)                                                                                              \
+  Box {                                                                                                      \
+    make_float3(sm.box[0 * BOXS + (J)-lo32], sm.box[1 * BOXS + (J)-lo32], sm.box[2 * BOXS + (J)-lo32]),      \
+        make_float3(sm.box[3 * BOXS + (J)-lo32], sm.box[4 * BOXS + (J)-lo32], sm.box[5 * BOXS + (J)-lo32]) \
+  }
+  const int64_t m_lo = (int64_t)base - r;
+  const uint32_t m_span = chunk + 2 * r;
+  for (uint32_t k = tid; k < m_span; k += PT) {
+    const int64_t jj = m_lo + k;
+    if (jj < 0 || jj >= (int64_t)count) continue;
+    const int i = (int)jj;
+    const Box me = PBOX(i);
+    int8_t m;
+    if (d1) {
+      if ((uint32_t)i == count - 1) {
+        m = -1;
+      } else {
+        const float c = pair_cost(me, PBOX(i + 1));
+        const float last = i == 0 ? __int_as_float(0x7f800000) : pair_cost(PBOX(i - 1), me);
+        m = last < c ? -1 : 1;
+      }
+    } else {
+      const int begin = i >= r ? i - r : 0;
+      const int end = min(i + r + 1, (int)count);
+      int best = i;
+      float best_cost = __int_as_float(0x7f800000);
+      for (int j = begin; j < i; j++) {
+        const float c = pair_cost(PBOX(j), me);
+        if (c <= best_cost) {
+          best = j;
+          best_cost = c;
+        }
+      }
+      for (int j = i + 1; j < end; j++) {
+        const float c = pair_cost(me, PBOX(j));
+        if (c <= best_cost) {
+          best = j;
+          best_cost = c;
+        }
+      }
+      m = (int8_t)(best - i);
+    }
+    sm.merge[k] = m;
+  }
+#undef PBOX
+  group_sync(group);
+  uint32_t packed = 0;
+#pragma unroll
+  for (int k = 0; k < PITEMS; k++) {
+    const uint32_t i = base + tid * ipt + k;
+    if (k < ipt && i < count) {
+      const int off = sm.merge[(int64_t)i - m_lo];
+      const uint32_t b = (uint32_t)((int)i + off);
+      const bool mutual = (int)b + (int)sm.merge[(int64_t)b - m_lo] == (int)i;
+      packed += ((!mutual || b < i) ? 1u : 0u) + ((mutual && b < i) ? (1u << 16) : 0u);
+      merge[i] = (int8_t)off;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) packed += __shfl_xor_sync(0xffffffffu, packed, o);
+  if (lane == 0) sm.w[warp] = packed;
+  group_sync(group);
+  if (tid == 0) {
+    uint32_t tot = 0;
+    for (int w = 0; w < PT / 32; w++) tot += sm.w[w];
+    *cnt = make_uint2(tot & 0xffffu, tot >> 16);
+  }
+}
+
+// Phase B for the same tile, after a grid barrier: its output offsets are
+// the counts of the list's earlier tiles tile_cnt[t_first, tile) (a group
+// reduction) plus a scan inside the tile; writes next[] and the merged pairs
+// (children at out[ins_top - 2(k+1)] for the list's k-th merge).  Returns the
+// list's (emitted, merged) totals through the end of this tile.
+__device__ __forceinline__ uint2 ploc_tile_write(CoopGroupSmem& sm, int group, const Bvh2Node* cur, Bvh2Node* next,
+                                                 Bvh2Node* out, const int8_t* merge, uint32_t count, uint32_t base,
+                                                 int ipt, const uint2* tile_cnt, uint32_t t_first, uint32_t tile,
+                                                 uint32_t ins_top) {
+  const int tid = threadIdx.x % PT, lane = tid & 31, warp = tid >> 5;
+  uint32_t pe = 0, pm = 0;
+  for (uint32_t t = t_first + tid; t < tile; t += PT) {
+    const uint2 v = __ldcg(&tile_cnt[t]);
+    pe += v.x;
+    pm += v.y;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    pe += __shfl_xor_sync(0xffffffffu, pe, o);
+    pm += __shfl_xor_sync(0xffffffffu, pm, o);
+  }
+  group_sync(group);  // red / w of the previous tile are consumed
+  if (lane == 0) {
+    sm.red[0][warp] = pe;
+    sm.red[1][warp] = pm;
+  }
+  // flags from the stored offsets, group-wide exclusive scan
+  bool emit[PITEMS], ism[PITEMS];
+  uint32_t bst[PITEMS];
+  uint32_t packed = 0;
+#pragma unroll
+  for (int k = 0; k < PITEMS; k++) {
+    const uint32_t i = base + tid * ipt + k;
+    emit[k] = ism[k] = false;
+    bst[k] = i;
+    if (k < ipt && i < count) {
+      const int off = __ldcg(&merge[i]);
+      const uint32_t b = (uint32_t)((int)i + off);
+      const bool mutual = (int)b + (int)__ldcg(&merge[b]) == (int)i;
+      emit[k] = !mutual || b < i;
+      ism[k] = mutual && b < i;
+      bst[k] = b;
+    }
+    packed += (emit[k] ? 1u : 0u) + (ism[k] ? (1u << 16) : 0u);
+  }
+  uint32_t x = packed;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sm.w[warp] = x;
+  group_sync(group);
+  uint32_t wpre = 0, tot = 0, pre_e = 0, pre_m = 0;
+  for (int w = 0; w < PT / 32; w++) {
+    if (w < warp) wpre += sm.w[w];
+    tot += sm.w[w];
+    pre_e += sm.red[0][w];
+    pre_m += sm.red[1][w];
+  }
+  const uint32_t excl = wpre + x - packed;
+  uint32_t epos = pre_e + (excl & 0xffffu), mpos = pre_m + (excl >> 16);
+#pragma unroll
+  for (int k = 0; k < PITEMS; k++) {
+    const uint32_t i = base + tid * ipt + k;
+    if (!emit[k]) continue;
+    if (ism[k]) {
+      const Bvh2Node left = ld_node_cg(&cur[i]);
+      const Bvh2Node right = ld_node_cg(&cur[bst[k]]);
+      const uint32_t ins = ins_top - 2 * (mpos + 1);
+      st_node(&out[ins], left);
+      st_node(&out[ins + 1], right);
+      st_node(&next[epos], make_node(box_union(node_box(left), node_box(right)), 0, ins));
+      mpos++;
+    } else {
+      st_node(&next[epos], ld_node_cg(&cur[i]));
+    }
+    epos++;
+  }
+  return make_uint2(pre_e + (tot & 0xffffu), pre_m + (tot >> 16));
+}
+
+__device__ __forceinline__ int tile_ipt(uint32_t live, uint32_t groups) {
+  return live >= groups * (uint32_t)PCHUNK ? PITEMS : live >= groups * (uint32_t)(PT * 2) ? 2 : 1;
+}
+
 __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs a) {
   cg::grid_group grid = cg::this_grid();
   const bool single = gridDim.x == 1;  // one block, launched normally: block barriers suffice
   extern __shared__ __align__(16) unsigned char coop_smem[];
   const int group = threadIdx.x / PT;
   CoopGroupSmem& sm = reinterpret_cast<CoopGroupSmem*>(coop_smem)[group];
-  const int tid = threadIdx.x % PT, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x % PT;
   const uint32_t G = gridDim.x;
   const uint32_t first_tile = blockIdx.x + G * (uint32_t)group, tile_step = G * COOP_GROUPS;
   for (uint32_t iter = 0;; iter++) {
@@ -290,180 +573,25 @@ __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs 
     // read in the next; loads go through L2 (ld.cg) so no stale line is used
     const Bvh2Node* cur = parity ? a.buf[1] : a.buf[0];
     Bvh2Node* next = parity ? a.buf[0] : a.buf[1];
-    const int d1 = (a.radius == 1 || pass < a.depth_threshold) ? 1 : 0;
+    const bool d1 = a.radius == 1 || pass < a.depth_threshold;
     const int r = d1 ? 1 : a.radius;
-    const uint32_t groups = G * COOP_GROUPS;
-    const int ipt = count >= groups * (uint32_t)PCHUNK ? PITEMS : count >= groups * (uint32_t)(PT * 2) ? 2 : 1;
+    const int ipt = tile_ipt(count, G * COOP_GROUPS);
     const uint32_t chunk = (uint32_t)PT * ipt;
     const uint32_t ntiles = div_up<uint32_t>(count, chunk);
 
     // A: merge offsets and tile counts
-    for (uint32_t tile = first_tile; tile < ntiles; tile += tile_step) {
-      const uint32_t base = tile * chunk;
-      const int64_t box_lo = (int64_t)base - 2 * r;
-      const uint32_t box_span = chunk + 4 * r;
-      group_sync(group);  // the previous tile's shared data is consumed
-      for (uint32_t k = tid; k < box_span; k += PT) {
-        const int64_t j = box_lo + k;
-        if (j >= 0 && j < (int64_t)count) {
-          const Box b = load_box_cg(&cur[j]);
-          sm.box[0 * BOXS + k] = b.mn.x;
-          sm.box[1 * BOXS + k] = b.mn.y;
-          sm.box[2 * BOXS + k] = b.mn.z;
-          sm.box[3 * BOXS + k] = b.mx.x;
-          sm.box[4 * BOXS + k] = b.mx.y;
-          sm.box[5 * BOXS + k] = b.mx.z;
-        }
-      }
-      group_sync(group);
-      const int lo32 = (int)box_lo;
-#define PBOX(J)                                                                                              \
-  Box {                                                                                                      \
-    make_float3(sm.box[0 * BOXS + (J)-lo32], sm.box[1 * BOXS + (J)-lo32], sm.box[2 * BOXS + (J)-lo32]),      \
-        make_float3(sm.box[3 * BOXS + (J)-lo32], sm.box[4 * BOXS + (J)-lo32], sm.box[5 * BOXS + (J)-lo32]) \
-  }
-      const int64_t m_lo = (int64_t)base - r;
-      const uint32_t m_span = chunk + 2 * r;
-      for (uint32_t k = tid; k < m_span; k += PT) {
-        const int64_t jj = m_lo + k;
-        if (jj < 0 || jj >= (int64_t)count) continue;
-        const int i = (int)jj;
-        const Box me = PBOX(i);
-        int8_t m;
-        if (d1) {
-          if ((uint32_t)i == count - 1) {
-            m = -1;
-          } else {
-            const float c = pair_cost(me, PBOX(i + 1));
-            const float last = i == 0 ? __int_as_float(0x7f800000) : pair_cost(PBOX(i - 1), me);
-            m = last < c ? -1 : 1;
-          }
-        } else {
-          const int begin = i >= r ? i - r : 0;
-          const int end = min(i + r + 1, (int)count);
-          int best = i;
-          float best_cost = __int_as_float(0x7f800000);
-          for (int j = begin; j < i; j++) {
-            const float c = pair_cost(PBOX(j), me);
-            if (c <= best_cost) {
-              best = j;
-              best_cost = c;
-            }
-          }
-          for (int j = i + 1; j < end; j++) {
-            const float c = pair_cost(me, PBOX(j));
-            if (c <= best_cost) {
-              best = j;
-              best_cost = c;
-            }
-          }
-          m = (int8_t)(best - i);
-        }
-        sm.merge[k] = m;
-      }
-#undef PBOX
-      group_sync(group);
-      uint32_t packed = 0;
-#pragma unroll
-      for (int k = 0; k < PITEMS; k++) {
-        const uint32_t i = base + tid * ipt + k;
-        if (k < ipt && i < count) {
-          const int off = sm.merge[(int64_t)i - m_lo];
-          const uint32_t b = (uint32_t)((int)i + off);
-          const bool mutual = (int)b + (int)sm.merge[(int64_t)b - m_lo] == (int)i;
-          packed += ((!mutual || b < i) ? 1u : 0u) + ((mutual && b < i) ? (1u << 16) : 0u);
-          a.merge[i] = (int8_t)off;
-        }
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) packed += __shfl_xor_sync(0xffffffffu, packed, o);
-      if (lane == 0) sm.w[warp] = packed;
-      group_sync(group);
-      if (tid == 0) {
-        uint32_t tot = 0;
-        for (int w = 0; w < PT / 32; w++) tot += sm.w[w];
-        a.tile_cnt[tile] = make_uint2(tot & 0xffffu, tot >> 16);
-      }
-    }
+    for (uint32_t tile = first_tile; tile < ntiles; tile += tile_step)
+      ploc_tile_offsets(sm, group, cur, count, tile * chunk, chunk, ipt, r, d1, a.merge, &a.tile_cnt[tile]);
     if (single) __syncthreads(); else grid.sync();
 
     // B: offsets and writes
     const uint32_t ins_top = *(volatile uint32_t*)&a.st->insert[parity];
     for (uint32_t tile = first_tile; tile < ntiles; tile += tile_step) {
-      const uint32_t base = tile * chunk;
-      // counts of the tiles before this one
-      uint32_t pe = 0, pm = 0;
-      for (uint32_t t = tid; t < tile; t += PT) {
-        const uint2 v = __ldcg(&a.tile_cnt[t]);
-        pe += v.x;
-        pm += v.y;
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        pe += __shfl_xor_sync(0xffffffffu, pe, o);
-        pm += __shfl_xor_sync(0xffffffffu, pm, o);
-      }
-      group_sync(group);  // red / w of the previous tile are consumed
-      if (lane == 0) {
-        sm.red[0][warp] = pe;
-        sm.red[1][warp] = pm;
-      }
-      // flags from the stored offsets, group-wide exclusive scan
-      bool emit[PITEMS], ism[PITEMS];
-      uint32_t bst[PITEMS];
-      uint32_t packed = 0;
-#pragma unroll
-      for (int k = 0; k < PITEMS; k++) {
-        const uint32_t i = base + tid * ipt + k;
-        emit[k] = ism[k] = false;
-        bst[k] = i;
-        if (k < ipt && i < count) {
-          const int off = __ldcg(&a.merge[i]);
-          const uint32_t b = (uint32_t)((int)i + off);
-          const bool mutual = (int)b + (int)__ldcg(&a.merge[b]) == (int)i;
-          emit[k] = !mutual || b < i;
-          ism[k] = mutual && b < i;
-          bst[k] = b;
-        }
-        packed += (emit[k] ? 1u : 0u) + (ism[k] ? (1u << 16) : 0u);
-      }
-      uint32_t x = packed;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-      }
-      if (lane == 31) sm.w[warp] = x;
-      group_sync(group);
-      uint32_t wpre = 0, tot = 0, pre_e = 0, pre_m = 0;
-      for (int w = 0; w < PT / 32; w++) {
-        if (w < warp) wpre += sm.w[w];
-        tot += sm.w[w];
-        pre_e += sm.red[0][w];
-        pre_m += sm.red[1][w];
-      }
-      const uint32_t excl = wpre + x - packed;
-      uint32_t epos = pre_e + (excl & 0xffffu), mpos = pre_m + (excl >> 16);
-#pragma unroll
-      for (int k = 0; k < PITEMS; k++) {
-        const uint32_t i = base + tid * ipt + k;
-        if (!emit[k]) continue;
-        if (ism[k]) {
-          const Bvh2Node left = ld_node_cg(&cur[i]);
-          const Bvh2Node right = ld_node_cg(&cur[bst[k]]);
-          const uint32_t ins = ins_top - 2 * (mpos + 1);
-          st_node(&a.out[ins], left);
-          st_node(&a.out[ins + 1], right);
-          st_node(&next[epos], make_node(box_union(node_box(left), node_box(right)), 0, ins));
-          mpos++;
-        } else {
-          st_node(&next[epos], ld_node_cg(&cur[i]));
-        }
-        epos++;
-      }
+      const uint2 tot = ploc_tile_write(sm, group, cur, next, a.out, a.merge, count, tile * chunk, ipt, a.tile_cnt, 0,
+                                        tile, ins_top);
       if (tid == 0 && tile == ntiles - 1) {
-        a.st->count[parity ^ 1] = pre_e + (tot & 0xffffu);
-        a.st->insert[parity ^ 1] = ins_top - 2 * (pre_m + (tot >> 16));
+        a.st->count[parity ^ 1] = tot.x;
+        a.st->insert[parity ^ 1] = ins_top - 2 * tot.y;
         a.st->sum_counts += count;
         __threadfence();
         a.st->passes = pass + 1;
@@ -471,6 +599,191 @@ __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs 
     }
     if (single) __syncthreads(); else grid.sync();
   }
+}
+
+// --- many scenes in one cooperative launch ----------------------------------
+//
+// The passes of every scene of a segmented build run together: scene s keeps
+// its live clusters at [prim_start[s], prim_start[s] + count_s) of the
+// cluster buffers and its tree at node_start[s] of `out`; pass p of every
+// scene runs in pass p of the launch, so the distance-1 rule (pass <
+// depth_threshold) is the same per scene.  Each pass, every block derives the
+// tile table (scene s has ceil(count_s / chunk) tiles when count_s > 1) from
+// the per-scene counts, and the tiles of all scenes are spread over the
+// groups as in k_ploc_coop; a tile's output offsets count only the earlier
+// tiles of its own scene.  A scene whose count reaches 1 writes its root to
+// out[node_start[s]] and drops out.  No tail kernel: the loop runs until
+// every scene is done.
+constexpr uint32_t SEG_MAX = OBVHS_SEG_MAX_SCENES;  // scenes per launch (tile table in shared memory)
+
+struct PlocSegArgs {
+  Bvh2Node* buf[2];
+  Bvh2Node* out;
+  int8_t* merge;
+  uint2* tile_cnt;
+  const uint32_t* prim_start;  // n_seg + 1
+  const uint32_t* node_start;  // n_seg + 1
+  uint32_t* count;             // 2 x n_seg, by pass parity
+  uint32_t* insert;            // 2 x n_seg
+  uint32_t* passes;            // n_seg: passes of the scene once done
+  unsigned long long* sum_counts;  // n_seg
+  uint32_t* ctl;               // [0] pass, [1 + parity] clusters of unfinished scenes
+  uint32_t n_seg;
+  int radius;
+  uint32_t depth_threshold;
+  uint32_t max_passes;
+  uint32_t* status;
+};
+
+// Block-wide exclusive scan of v(s), s in [0, n), into out[0, n]; all
+// COOP_GROUPS * PT threads take part.
+template <class F>
+__device__ __forceinline__ void block_scan_into(uint32_t* out, uint32_t n, F v, uint32_t* s_warp) {
+  constexpr int NT = COOP_GROUPS * PT;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const uint32_t per = (n + NT - 1) / NT;
+  const uint32_t s0 = t * per;
+  uint32_t sum = 0;
+  for (uint32_t k = 0; k < per; k++)
+    if (s0 + k < n) sum += v(s0 + k);
+  uint32_t x = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = s_warp[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    s_warp[lane] = w;  // inclusive
+  }
+  __syncthreads();
+  uint32_t run = (warp ? s_warp[warp - 1] : 0u) + x - sum;
+  for (uint32_t k = 0; k < per; k++)
+    if (s0 + k < n) {
+      out[s0 + k] = run;
+      run += v(s0 + k);
+    }
+  if (t == NT - 1) out[n] = run;
+  __syncthreads();
+}
+
+__device__ __forceinline__ uint32_t smem_seg_find(const uint32_t* start, uint32_t n_seg, uint32_t i) {
+  uint32_t lo = 0, hi = n_seg;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (start[mid] <= i)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_seg(PlocSegArgs a) {
+  cg::grid_group grid = cg::this_grid();
+  extern __shared__ __align__(16) unsigned char coop_smem[];
+  __shared__ uint32_t s_warp[32];
+  const int group = threadIdx.x / PT;
+  CoopGroupSmem& sm = reinterpret_cast<CoopGroupSmem*>(coop_smem)[group];
+  uint32_t* tstart = reinterpret_cast<uint32_t*>(coop_smem + COOP_GROUPS * sizeof(CoopGroupSmem));
+  const int tid = threadIdx.x % PT;
+  const uint32_t S = a.n_seg;
+  const uint32_t G = gridDim.x;
+  const uint32_t first_tile = blockIdx.x + G * (uint32_t)group, tile_step = G * COOP_GROUPS;
+  for (uint32_t iter = 0;; iter++) {
+    const uint32_t pass = *(volatile uint32_t*)&a.ctl[0];
+    const int parity = (int)(pass & 1u);
+    const uint32_t live = *(volatile uint32_t*)&a.ctl[1 + parity];
+    if (live == 0) break;
+    if (iter >= a.max_passes) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) set_status(a.status, ST_ITER_LIMIT);
+      break;
+    }
+    // this pass's phase B accumulates the next pass's live count (that word
+    // was last read before the previous pass's first barrier)
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.ctl[1 + (parity ^ 1)] = 0;
+    const Bvh2Node* cur = parity ? a.buf[1] : a.buf[0];
+    Bvh2Node* next = parity ? a.buf[0] : a.buf[1];
+    const uint32_t* cnt = a.count + (size_t)parity * S;
+    const uint32_t* insert = a.insert + (size_t)parity * S;
+    const bool d1 = a.radius == 1 || pass < a.depth_threshold;
+    const int r = d1 ? 1 : a.radius;
+    const int ipt = tile_ipt(live, G * COOP_GROUPS);
+    const uint32_t chunk = (uint32_t)PT * ipt;
+    block_scan_into(
+        tstart, S,
+        [&](uint32_t s) {
+          const uint32_t c = __ldcg(&cnt[s]);
+          return c > 1 ? div_up<uint32_t>(c, chunk) : 0u;
+        },
+        s_warp);
+    const uint32_t ntiles = tstart[S];
+
+    // A: merge offsets and tile counts
+    for (uint32_t tile = first_tile; tile < ntiles; tile += tile_step) {
+      const uint32_t s = smem_seg_find(tstart, S, tile);
+      const uint32_t cb = __ldg(&a.prim_start[s]);
+      ploc_tile_offsets(sm, group, cur + cb, __ldcg(&cnt[s]), (tile - tstart[s]) * chunk, chunk, ipt, r, d1,
+                        a.merge + cb, &a.tile_cnt[tile]);
+    }
+    grid.sync();
+
+    // B: offsets and writes
+    for (uint32_t tile = first_tile; tile < ntiles; tile += tile_step) {
+      const uint32_t s = smem_seg_find(tstart, S, tile);
+      const uint32_t cb = __ldg(&a.prim_start[s]);
+      const uint32_t count = __ldcg(&cnt[s]);
+      const uint32_t ins_top = __ldcg(&insert[s]);
+      const uint2 tot = ploc_tile_write(sm, group, cur + cb, next + cb, a.out, a.merge + cb, count,
+                                        (tile - tstart[s]) * chunk, ipt, a.tile_cnt, tstart[s], tile, ins_top);
+      if (tile == tstart[s + 1] - 1) {  // the scene's last tile
+        if (tid == 0) {
+          a.count[(size_t)(parity ^ 1) * S + s] = tot.x;
+          a.insert[(size_t)(parity ^ 1) * S + s] = ins_top - 2 * tot.y;
+          atomicAdd(&a.sum_counts[s], (unsigned long long)count);
+          if (tot.x > 1) {
+            atomicAdd(&a.ctl[1 + (parity ^ 1)], tot.x);
+          } else {
+            a.count[(size_t)parity * S + s] = tot.x;  // done: 1 in both parities
+            a.passes[s] = pass + 1;
+          }
+        }
+        if (tot.x == 1) {  // one tile (a pass at most halves the count): the root is next[0]
+          group_sync(group);
+          if (tid == 0) st_node(&a.out[__ldg(&a.node_start[s])], ld_node_cg(&next[cb]));
+        }
+      }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.ctl[0] = pass + 1;
+    grid.sync();
+  }
+}
+
+// Per-scene PLOC state before the first pass.  A one-leaf scene's root is the
+// leaf; every scene's last node slot gets an inert pad (an inner node whose
+// child index is out of range, so parent and cost kernels skip it).
+__global__ void k_ploc_seg_init(const Bvh2Node* __restrict__ cur, const uint32_t* __restrict__ prim_start,
+                                const uint32_t* __restrict__ node_start, uint32_t n_seg, uint32_t* count,
+                                uint32_t* insert, uint32_t* passes, unsigned long long* sum_counts, uint32_t* ctl,
+                                Bvh2Node* __restrict__ out) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_seg) return;
+  const uint32_t m = prim_start[s + 1] - prim_start[s];
+  const uint32_t nb = node_start[s];
+  count[s] = count[n_seg + s] = m;
+  insert[s] = insert[n_seg + s] = m ? nb + 2 * m - 1 : nb;
+  passes[s] = 0;
+  sum_counts[s] = 0;
+  if (m >= 1) st_node(&out[nb + 2 * m - 1], make_node(Box{}, 0, SEG_PAD_CHILD));
+  if (m == 1) st_node(&out[nb], ld_node(&cur[prim_start[s]]));
+  if (m > 1) atomicAdd(&ctl[1], m);
 }
 
 // --- single-CTA tail ---------------------------------------------------------
@@ -766,6 +1079,87 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   CK(cudaStreamSynchronize(c.stream));
   *passes_out = h.passes;
   *sum_counts_out = h.sum_counts;
+  return 0;
+}
+
+int seg_leaves_device(BuildCtx& c, const SegLayout& L, const float* const* d_tris, const float* aabbs,
+                      const uint32_t* idx, Bvh2Node* leaves, uint32_t* pidx, int* total_keys) {
+  const uint32_t S = L.n_seg, n = L.n_prims;
+  KLAUNCH("k_seg_init_totals", k_seg_init_totals<<<div_up<uint32_t>(8 * S, BLK), BLK, 0, c.stream>>>(total_keys, S));
+  if (!n) return 0;
+  const uint32_t g = div_up<uint32_t>(n, BLK);
+  if (d_tris)
+    KLAUNCH("k_seg_leaves_tris", k_seg_leaves_tris<<<g, BLK, 0, c.stream>>>(d_tris, L.d_prim_start, S, n, leaves, pidx,
+                                                                           total_keys, c.d_status));
+  else
+    KLAUNCH("k_seg_leaves_aabbs", k_seg_leaves_aabbs<<<g, BLK, 0, c.stream>>>(aabbs, idx, L.d_prim_start, S, n, leaves,
+                                                                             pidx, total_keys, c.d_status));
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int ploc_seg_device(BuildCtx& c, const SegLayout& L, const Bvh2Node* leaves, const int* total_keys, uint32_t radius,
+                    int precision, uint32_t depth_threshold, Bvh2Node* out, uint32_t* d_passes,
+                    unsigned long long* d_sum_counts) {
+  const uint32_t n = L.n_prims, S = L.n_seg;
+  if (n == 0) return 0;
+  if (S > SEG_MAX) return c.fail(OBVHS_ERR_INVALID_ARG, "too many scenes in one segmented launch");
+  if (radius < 1 || radius > 32) return c.fail(OBVHS_ERR_INVALID_ARG, "search distance must be 1..32");
+  Scratch& s = c.scratch;
+  void* codes = s.get(SLOT_KEYS, (size_t)n * (precision ? sizeof(U128) : sizeof(unsigned long long)));
+  if (!codes) return c.fail(OBVHS_ERR_OOM, "scratch");
+  const uint32_t g = div_up<uint32_t>(n, BLK);
+  if (precision)
+    KLAUNCH("k_seg_morton", k_seg_morton<true><<<g, BLK, 0, c.stream>>>(leaves, L.d_prim_start, S, n, total_keys, codes));
+  else
+    KLAUNCH("k_seg_morton", k_seg_morton<false><<<g, BLK, 0, c.stream>>>(leaves, L.d_prim_start, S, n, total_keys, codes));
+  CK(cudaGetLastError());
+  // Morton order over all leaves, then a stable pass on the scene index: each
+  // scene's leaves in its own Morton order (ties by position), scenes in turn
+  uint32_t* order = nullptr;
+  int r = ploc_sort_codes(c, codes, n, precision, &order);
+  if (r) return r;
+  if (S > 1) {
+    uint32_t* skeys = (uint32_t*)s.get(SLOT_REINS_KEYS, (size_t)n * 4);
+    uint32_t* skeys_alt = (uint32_t*)s.get(SLOT_REINS_VALS, (size_t)n * 4);
+    uint32_t* rs = (uint32_t*)s.get(SLOT_ALL_HIST, radix_scratch_words(n) * 4);
+    if (!skeys || !skeys_alt || !rs) return c.fail(OBVHS_ERR_OOM, "scratch");
+    uint32_t* other = order == (uint32_t*)s.ptr[SLOT_VALS] ? (uint32_t*)s.ptr[SLOT_VALS_ALT] : (uint32_t*)s.ptr[SLOT_VALS];
+    KLAUNCH("k_seg_scene_keys", k_seg_scene_keys<<<g, BLK, 0, c.stream>>>(order, L.d_prim_start, S, n, skeys));
+    bool alt = false;
+    cudaError_t e = radix_sort_pairs<uint32_t>(c, skeys, order, n, false, skeys_alt, other, rs, &alt, S <= 256 ? 1 : 2);
+    if (e) return c.cuda_fail(e, "scene sort");
+    if (alt) order = other;
+  }
+  Bvh2Node* cur = (Bvh2Node*)s.get(SLOT_PLOC_A, (size_t)n * sizeof(Bvh2Node));
+  Bvh2Node* nxt = (Bvh2Node*)s.get(SLOT_PLOC_B, (size_t)n * sizeof(Bvh2Node));
+  int8_t* merge = (int8_t*)s.get(SLOT_MERGE, (size_t)n);
+  uint2* tile_cnt = (uint2*)s.get(SLOT_PARTIAL, ((size_t)div_up<uint32_t>(n, PT) + S + 1) * sizeof(uint2));
+  uint32_t* st = (uint32_t*)s.get(SLOT_PLOC_STATE, ((size_t)4 * S + 8) * 4);
+  if (!cur || !nxt || !merge || !tile_cnt || !st) return c.fail(OBVHS_ERR_OOM, "scratch");
+  uint32_t* ctl = st;
+  uint32_t* count = st + 8;
+  uint32_t* insert = count + 2 * (size_t)S;
+  KLAUNCH("k_gather", k_gather<<<g, BLK, 0, c.stream>>>(leaves, order, n, cur));
+  CK(cudaMemsetAsync(ctl, 0, 32, c.stream));
+  KLAUNCH("k_ploc_seg_init", k_ploc_seg_init<<<div_up<uint32_t>(S, BLK), BLK, 0, c.stream>>>(
+                                 cur, L.d_prim_start, L.d_node_start, S, count, insert, d_passes, d_sum_counts, ctl, out));
+  CK(cudaGetLastError());
+  const size_t smem = COOP_GROUPS * sizeof(CoopGroupSmem) + ((size_t)S + 1) * 4;
+  static std::atomic<int> seg_blocks_s{0};
+  int seg_blocks = seg_blocks_s.load();
+  if (!seg_blocks) {
+    const size_t smem_max = COOP_GROUPS * sizeof(CoopGroupSmem) + ((size_t)SEG_MAX + 1) * 4;
+    CK(cudaFuncSetAttribute(k_ploc_seg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ploc_seg, COOP_GROUPS * PT, smem_max));
+    seg_blocks = std::max(1, per_sm) * c.num_sms;
+    seg_blocks_s.store(seg_blocks);
+  }
+  PlocSegArgs pa{{cur, nxt}, out, merge, tile_cnt, L.d_prim_start, L.d_node_start, count, insert, d_passes,
+                 d_sum_counts, ctl, S, (int)radius, depth_threshold, 2 * L.max_m + 64, c.d_status};
+  void* args[] = {&pa};
+  KLAUNCH("k_ploc_seg", CK(coop_launch(c, (const void*)k_ploc_seg, seg_blocks, COOP_GROUPS * PT, args, smem)));
   return 0;
 }
 

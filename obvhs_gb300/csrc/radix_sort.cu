@@ -195,8 +195,9 @@ size_t radix_scratch_words(uint32_t n) {
 
 template <class K>
 cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, bool init_iota, K* keys_alt,
-                             uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt) {
+                             uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt, int digits) {
   constexpr int NB = KeyTraits<K>::BYTES;
+  const int nd = digits > 0 && digits < NB ? digits : NB;
   constexpr int TS = Tile<K>::SIZE;
   *result_in_alt = false;
   if (n == 0) return cudaSuccess;
@@ -204,17 +205,17 @@ cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, 
   uint32_t* hist = scratch;
   uint32_t* pass_area = scratch + 16 * 256;
   const size_t pass_words = (size_t)ntiles * 256 + 32;
-  cudaError_t e = cudaMemsetAsync(scratch, 0, (16 * 256 + NB * pass_words) * sizeof(uint32_t), c.stream);
+  cudaError_t e = cudaMemsetAsync(scratch, 0, (16 * 256 + nd * pass_words) * sizeof(uint32_t), c.stream);
   if (e) return e;
   const uint32_t hb = (n + THREADS * HIST_ITEMS - 1) / (THREADS * HIST_ITEMS);
   KLAUNCH("k_rs_hist", k_rs_hist<K><<<hb, THREADS, 0, c.stream>>>(keys, n, hist));
-  KLAUNCH("k_rs_scan", k_rs_scan<<<NB, THREADS, 0, c.stream>>>(hist));
+  KLAUNCH("k_rs_scan", k_rs_scan<<<nd, THREADS, 0, c.stream>>>(hist));
   K* kin = keys;
   uint32_t* vin = vals;
   K* kout = keys_alt;
   uint32_t* vout = vals_alt;
   bool iota = init_iota;
-  for (int b = 0; b < NB; b++) {
+  for (int b = 0; b < nd; b++) {
     uint32_t* ts = pass_area + (size_t)b * pass_words;
     KLAUNCH("k_rs_pass", k_rs_pass<K><<<ntiles, THREADS, 0, c.stream>>>(kin, vin, kout, vout, n, b, iota,
                                                                          hist + b * 256, ts + 32, ts, c.d_status));
@@ -235,8 +236,8 @@ cudaError_t fill_iota(uint32_t* v, uint32_t n, cudaStream_t s) {
 }
 
 template cudaError_t radix_sort_pairs<uint32_t>(obvhs_ctx&, uint32_t*, uint32_t*, uint32_t, bool, uint32_t*, uint32_t*,
-                                                uint32_t*, bool*);
+                                                uint32_t*, bool*, int);
 template cudaError_t radix_sort_pairs<unsigned long long>(obvhs_ctx&, unsigned long long*, uint32_t*, uint32_t, bool,
-                                                          unsigned long long*, uint32_t*, uint32_t*, bool*);
+                                                          unsigned long long*, uint32_t*, uint32_t*, bool*, int);
 template cudaError_t radix_sort_pairs<U128>(obvhs_ctx&, U128*, uint32_t*, uint32_t, bool, U128*, uint32_t*, uint32_t*,
-                                            bool*);
+                                            bool*, int);

@@ -42,11 +42,13 @@ struct KeyTraits<U128> {
 // On return *result_in_alt tells whether the sorted data ended in the "alt"
 // buffers.  `scratch` holds radix_scratch_words(n) words; the context's
 // status word receives an error bit if a look-back wait gives up.  Launches
-// on the context's stream; no host synchronisation.
+// on the context's stream; no host synchronisation.  `digits` (1..bytes of
+// K) sorts on the low `digits` bytes only, for keys whose upper bytes are
+// known to be zero.
 struct obvhs_ctx;
 template <class K>
 cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, bool init_iota, K* keys_alt,
-                             uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt);
+                             uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt, int digits = 0);
 
 size_t radix_scratch_words(uint32_t n);
 cudaError_t fill_iota(uint32_t* v, uint32_t n, cudaStream_t s);

@@ -85,6 +85,7 @@ template <int CAP, bool CLAMP>
 struct FindSearch {
   uint2* st;  // the thread's stack, CAP entries (kept apart so the scalars stay in registers)
   uint32_t sp, guard, cap;
+  uint32_t clamp_at;  // !CLAMP only: nonzero = StackStack semantics with this many entries (per-candidate mode)
   bool overflow;
   uint32_t node_id, parent_id, sib, pivot_id, best_to;
   float node_area, area_diff, best_diff;
@@ -95,6 +96,9 @@ struct FindSearch {
     if (CLAMP) {
       st[sp] = v;
       sp = min(sp + 1, (uint32_t)CAP - 1);
+    } else if (clamp_at) {
+      st[sp] = v;
+      sp = min(sp + 1, clamp_at - 1);
     } else if (sp >= cap) {
       overflow = true;
     } else {
@@ -147,9 +151,10 @@ struct FindSearch {
       pivot_bbox = box_union(pivot_bbox, node_box(ld_node(&nodes[sib])));
       area_diff += half_area(node_box(ld_node(&nodes[pivot_id]))) - half_area(pivot_bbox);
     }
-    if (pivot_id == 0) return true;
+    const uint32_t up = parents[pivot_id];
+    if (up == pivot_id) return true;  // the root is its own parent
     sib = sibling_of(pivot_id);
-    pivot_id = parents[pivot_id];
+    pivot_id = up;
     push(area_diff, sib);
     return false;
   }
@@ -167,18 +172,44 @@ struct FindSearch {
 constexpr int FIND_THREADS = 128;
 
 // One candidate per thread.
+// Stack mode of one search.  One tree: every search clamps at CAP or stops
+// at cap_rt.  Several trees whose modes differ (segmented builds, unclamped
+// variant): per tree (segment of the node index) a word, high bit = clamp at
+// the low bits' entry count, else the low bits are the stack bound.
+struct StackModes {
+  const uint32_t* mode;        // per segment, or null
+  const uint32_t* node_start;  // segment starts
+  uint32_t n_seg;
+};
+
+template <int CAP, bool CLAMP>
+__device__ __forceinline__ void set_stack_mode(FindSearch<CAP, CLAMP>& f, uint32_t cap_rt, const StackModes& sm,
+                                               uint32_t node) {
+  f.cap = CLAMP ? CAP : cap_rt;
+  f.clamp_at = 0;
+  if (!CLAMP && sm.mode) {
+    const uint32_t w = __ldg(&sm.mode[seg_find(sm.node_start, sm.n_seg, node)]);
+    if (w >> 31)
+      f.clamp_at = w & 0x7fffffffu;
+    else
+      f.cap = w;
+  }
+}
+
 template <int CAP, bool CLAMP>
 __global__ void __launch_bounds__(FIND_THREADS) k_find(const Bvh2Node* __restrict__ nodes,
                                                        const uint32_t* __restrict__ parents,
                                                        const uint32_t* __restrict__ cand, uint32_t count,
-                                                       uint32_t cap_rt, Reins* __restrict__ out, uint32_t* status) {
+                                                       uint32_t cap_rt, Reins* __restrict__ out, uint32_t* status,
+                                                       StackModes modes) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
   uint2 stack[CAP];
   FindSearch<CAP, CLAMP> f;
   f.st = stack;
-  f.cap = CLAMP ? CAP : cap_rt;
-  f.start(nodes, parents, cand[k]);
+  const uint32_t node = cand[k];
+  set_stack_mode(f, cap_rt, modes, node);
+  f.start(nodes, parents, node);
   while (!f.step(nodes, parents)) {
   }
   out[k] = f.result(parents, status);
@@ -192,12 +223,11 @@ __global__ void __launch_bounds__(FIND_THREADS) k_find_persistent(const Bvh2Node
                                                                   const uint32_t* __restrict__ parents,
                                                                   const uint32_t* __restrict__ cand, uint32_t count,
                                                                   uint32_t cap_rt, Reins* __restrict__ out,
-                                                                  uint32_t* next, uint32_t* status) {
+                                                                  uint32_t* next, uint32_t* status, StackModes modes) {
   const int lane = threadIdx.x & 31;
   uint2 stack[CAP];
   FindSearch<CAP, CLAMP> f;
   f.st = stack;
-  f.cap = CLAMP ? CAP : cap_rt;
   uint32_t k = 0;
   bool active = false, need = true;
   for (;;) {
@@ -211,7 +241,11 @@ __global__ void __launch_bounds__(FIND_THREADS) k_find_persistent(const Bvh2Node
         need = false;
         k = base + __popc(want & ((1u << lane) - 1u));
         active = k < count;
-        if (active) f.start(nodes, parents, cand[k]);
+        if (active) {
+          const uint32_t node = cand[k];
+          set_stack_mode(f, cap_rt, modes, node);
+          f.start(nodes, parents, node);
+        }
       }
     }
     if (!__any_sync(0xffffffffu, active)) break;
@@ -327,7 +361,7 @@ __device__ __forceinline__ bool mark_path(const ResolveArgs& a, uint32_t x) {
     if (atomicExch(&a.dirty[x], a.stamp) == a.stamp) return owned;
     if (first) owned = true;
     first = false;
-    if (x == 0) return owned;
+    if (up == x) return owned;  // the root
     x = up;
   }
   set_status(a.status, ST_ITER_LIMIT);
@@ -348,8 +382,8 @@ __device__ __forceinline__ void refit_climb(const ResolveArgs& a, uint32_t x) {
     st_inner<L1>(&a.nodes[x], box, f);
   }
   for (uint32_t guard = 0; guard < a.n_nodes; guard++) {
-    if (x == 0) return;
     const uint32_t up = ld_word<L1>(&a.parents[x]);
+    if (up == x) return;  // the root
     const uint32_t sib = sibling_of(x);
     const bool sib_marked = ld_word<L1>(&a.dirty[sib]) == a.stamp;
     Box sb = ld_box<L1>(&a.nodes[sib]);  // final unless the sibling is marked: loads overlap
@@ -473,7 +507,10 @@ __device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, u
     const uint32_t j = i >> 1;
     if (__ldcg(&a.state[j]) != 1) continue;  // slots and states were written by other threads
     uint32_t x = __ldcg(&start_slots[i]);
-    if (i & 1u) x = x != 0 ? __ldcg(&a.parents[x]) : OBVHS_INVALID;
+    if (i & 1u) {
+      const uint32_t up = __ldcg(&a.parents[x]);
+      x = up != x ? up : OBVHS_INVALID;  // nothing above the root
+    }
     start_slots[i] = (x != OBVHS_INVALID && mark_path<L1>(a, x)) ? x : OBVHS_INVALID;
   }
   sync();
@@ -560,6 +597,129 @@ __global__ void __launch_bounds__(RESOLVE_THREADS) k_resolve(ResolveArgs a) {
   }
 }
 
+// Every scene's root is its own parent (k_parents covers node 0 only).
+__global__ void k_seg_root_parents(const uint32_t* __restrict__ prim_start, const uint32_t* __restrict__ node_start,
+                                   uint32_t n_seg, uint32_t* __restrict__ parents) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n_seg && prim_start[s + 1] > prim_start[s]) parents[node_start[s]] = node_start[s];
+}
+
+// find_candidates of every scene: scene s's nodes 1 .. take_s - 1 (local
+// numbering), keyed (scene, -half_area) so that one stable sort orders each
+// scene's candidates as its own sort would.
+__global__ void k_seg_cand_keys(const Bvh2Node* __restrict__ nodes, const uint32_t* __restrict__ cand_start,
+                                const uint32_t* __restrict__ node_start, uint32_t n_seg, uint32_t total,
+                                unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total) return;
+  const uint32_t s = seg_find(cand_start, n_seg, j);
+  const uint32_t node = __ldg(&node_start[s]) + 1 + (j - __ldg(&cand_start[s]));
+  const Box b = node_box(ld_node(&nodes[node]));
+  keys[j] = ((unsigned long long)s << 32) | f32_radix_key(-half_area(b));
+  vals[j] = node;
+}
+
+// The first count_s sorted candidates of every scene, packed.
+__global__ void k_seg_cand_gather(const uint32_t* __restrict__ sorted, const uint32_t* __restrict__ find_start,
+                                  const uint32_t* __restrict__ cand_start, uint32_t n_seg, uint32_t total,
+                                  uint32_t* __restrict__ out) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= total) return;
+  const uint32_t s = seg_find(find_start, n_seg, k);
+  out[k] = sorted[__ldg(&cand_start[s]) + (k - __ldg(&find_start[s]))];
+}
+
+// Buffers of a reinsertion run over n_nodes node slots (one tree or many).
+struct ReinsBufs {
+  uint32_t *parents, *dirty, *arrive, *touched, *plist, *counters;
+  uint2* starts;
+  unsigned long long* owner;
+  Conf* conf;
+  Reins* reins;
+  uint8_t* state;
+};
+
+int reins_setup(BuildCtx& c, const Bvh2Node* nodes, uint32_t len, uint32_t nseq, ReinsBufs& B) {
+  Scratch& s = c.scratch;
+  B.parents = (uint32_t*)s.get(SLOT_PARENTS, (size_t)len * 4);
+  B.dirty = (uint32_t*)s.get(SLOT_FLAGS, (size_t)len * 4);
+  B.arrive = (uint32_t*)s.get(SLOT_ARRIVE, (size_t)len * 4);
+  B.starts = (uint2*)s.get(SLOT_STARTS, (size_t)len * 8);
+  B.touched = (uint32_t*)s.get(SLOT_TOUCHED, (size_t)len * 4);
+  B.owner = (unsigned long long*)s.get(SLOT_MIS_OWNER, (size_t)len * 24);
+  B.conf = (Conf*)s.get(SLOT_CONF, (size_t)len * sizeof(Conf));
+  B.reins = (Reins*)s.get(SLOT_REINS, (size_t)len * sizeof(Reins));
+  B.plist = (uint32_t*)s.get(SLOT_PLIST, (size_t)len * 4);
+  B.state = (uint8_t*)s.get(SLOT_MIS_STATE, (size_t)len);
+  // counters: [1] applied moves; then 8 words per pass (see ResolveArgs::ctr)
+  const size_t ctr_words = 8 + (size_t)nseq * 8;
+  B.counters = (uint32_t*)s.get(SLOT_CW_COUNTERS, ctr_words * 4);
+  if (!B.parents || !B.dirty || !B.arrive || !B.starts || !B.touched || !B.owner || !B.conf || !B.reins || !B.plist ||
+      !B.state || !B.counters)
+    return c.fail(OBVHS_ERR_OOM, "scratch");
+  CK(cudaMemsetAsync(B.counters, 0, ctr_words * 4, c.stream));
+  int r = compute_parents_device(c, nodes, len, B.parents);
+  if (r) return r;
+  // pass-stamped words: zero once per run
+  CK(cudaMemsetAsync(B.dirty, 0, (size_t)len * 4, c.stream));
+  CK(cudaMemsetAsync(B.arrive, 0, (size_t)len * 4, c.stream));
+  CK(cudaMemsetAsync(B.touched, 0, (size_t)len * 4, c.stream));
+  return 0;
+}
+
+// find_reinsertion for `count` candidates, then conflict resolution, moves
+// and refit (one launch each) for pass ri.  clamp: every search uses the
+// 192-entry clamped stack; else the unclamped variant with bound cap_rt, or
+// per-tree modes when `modes.mode` is set.
+int reins_pass(BuildCtx& c, Bvh2Node* nodes, uint32_t len, const uint32_t* cand, uint32_t count, uint32_t ri,
+               bool clamp, uint32_t cap_rt, StackModes modes, const ReinsBufs& B) {
+  static std::atomic<int> find_blocks_s{0}, resolve_blocks_s{0};
+  int find_blocks = find_blocks_s.load(), resolve_blocks = resolve_blocks_s.load();
+  if (!find_blocks) {
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_find_persistent<192, true>, FIND_THREADS, 0));
+    find_blocks = std::max(1, per_sm) * c.num_sms;
+    find_blocks_s.store(find_blocks);
+  }
+  if (!resolve_blocks) {
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resolve, RESOLVE_THREADS, 0));
+    resolve_blocks = std::max(1, per_sm) * c.num_sms;
+    resolve_blocks_s.store(resolve_blocks);
+  }
+  uint32_t* pass_ctr = B.counters + 8 + (size_t)ri * 8;  // [5]: next candidate for k_find
+  const uint32_t fblocks = div_up<uint32_t>(count, FIND_THREADS);
+  if (fblocks > (uint32_t)find_blocks) {
+    if (clamp)
+      KLAUNCH("k_find", k_find_persistent<192, true><<<find_blocks, FIND_THREADS, 0, c.stream>>>(
+                            nodes, B.parents, cand, count, cap_rt, B.reins, pass_ctr + 5, c.d_status, modes));
+    else
+      KLAUNCH("k_find", k_find_persistent<1024, false><<<find_blocks, FIND_THREADS, 0, c.stream>>>(
+                            nodes, B.parents, cand, count, cap_rt, B.reins, pass_ctr + 5, c.d_status, modes));
+  } else if (clamp) {
+    KLAUNCH("k_find", k_find<192, true><<<fblocks, FIND_THREADS, 0, c.stream>>>(nodes, B.parents, cand, count, cap_rt,
+                                                                           B.reins, c.d_status, modes));
+  } else {
+    KLAUNCH("k_find", k_find<1024, false><<<fblocks, FIND_THREADS, 0, c.stream>>>(nodes, B.parents, cand, count, cap_rt,
+                                                                             B.reins, c.d_status, modes));
+  }
+  CK(cudaGetLastError());
+  // conflict resolution, moves and refit in one launch
+  ResolveArgs ra{nodes,    B.parents, B.reins, count,  B.plist,     B.conf,     B.state,  B.owner,  B.touched,
+                 B.dirty,  B.arrive,  B.starts, pass_ctr, B.counters + 1, c.d_status, ri + 1, len, count + 3};
+  void* args[] = {&ra};
+  uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)resolve_blocks,
+                                               std::max<uint64_t>(1, div_up<uint32_t>(count, RESOLVE_THREADS)));
+  if (grid == 1 || count <= RESOLVE_SINGLE_MAX || device_context_count(c.device) > 1) {
+    // one block, a normal launch (block barriers only)
+    KLAUNCH("k_resolve", k_resolve<<<1, RESOLVE_THREADS, 0, c.stream>>>(ra));
+  } else {
+    KLAUNCH("k_resolve", CK(coop_launch(c, (const void*)k_resolve, grid, RESOLVE_THREADS, args, 0)));
+  }
+  CK(cudaGetLastError());
+  return 0;
+}
+
 }  // namespace
 
 int compute_parents_device(BuildCtx& c, const Bvh2Node* nodes, uint32_t n_nodes, uint32_t* parents) {
@@ -590,49 +750,15 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
     nseq = 16;
   }
   Scratch& s = c.scratch;
-  uint32_t* parents = (uint32_t*)s.get(SLOT_PARENTS, (size_t)len * 4);
-  uint32_t* dirty = (uint32_t*)s.get(SLOT_FLAGS, (size_t)len * 4);
-  uint32_t* arrive = (uint32_t*)s.get(SLOT_ARRIVE, (size_t)len * 4);
-  uint2* starts = (uint2*)s.get(SLOT_STARTS, (size_t)len * 8);
-  uint32_t* touched = (uint32_t*)s.get(SLOT_TOUCHED, (size_t)len * 4);
-  unsigned long long* owner = (unsigned long long*)s.get(SLOT_MIS_OWNER, (size_t)len * 24);
-  Conf* conf = (Conf*)s.get(SLOT_CONF, (size_t)len * sizeof(Conf));
   uint32_t* keys = (uint32_t*)s.get(SLOT_REINS_KEYS, (size_t)len * 4);
   uint32_t* vals = (uint32_t*)s.get(SLOT_REINS_VALS, (size_t)len * 4);
   uint32_t* keys_alt = (uint32_t*)s.get(SLOT_KEYS_ALT, (size_t)len * 4);
   uint32_t* vals_alt = (uint32_t*)s.get(SLOT_VALS_ALT, (size_t)len * 4);
   uint32_t* rs = (uint32_t*)s.get(SLOT_ALL_HIST, radix_scratch_words(len) * 4);
-  Reins* reins = (Reins*)s.get(SLOT_REINS, (size_t)len * sizeof(Reins));
-  uint32_t* plist = (uint32_t*)s.get(SLOT_PLIST, (size_t)len * 4);
-  uint8_t* state = (uint8_t*)s.get(SLOT_MIS_STATE, (size_t)len);
-  // counters: [1] applied moves; then 8 words per pass (see ResolveArgs::ctr)
-  const size_t ctr_words = 8 + (size_t)nseq * 8;
-  uint32_t* counters = (uint32_t*)s.get(SLOT_CW_COUNTERS, ctr_words * 4);
-  if (!parents || !dirty || !arrive || !starts || !touched || !owner || !conf || !keys || !vals || !keys_alt ||
-      !vals_alt || !rs || !reins || !plist || !state || !counters)
-    return c.fail(OBVHS_ERR_OOM, "scratch");
-  CK(cudaMemsetAsync(counters, 0, ctr_words * 4, c.stream));
-  int r = compute_parents_device(c, b->nodes, len, parents);
+  if (!keys || !vals || !keys_alt || !vals_alt || !rs) return c.fail(OBVHS_ERR_OOM, "scratch");
+  ReinsBufs B;
+  int r = reins_setup(c, b->nodes, len, nseq, B);
   if (r) return r;
-  // pass-stamped words: zero once per run
-  CK(cudaMemsetAsync(dirty, 0, (size_t)len * 4, c.stream));
-  CK(cudaMemsetAsync(arrive, 0, (size_t)len * 4, c.stream));
-  CK(cudaMemsetAsync(touched, 0, (size_t)len * 4, c.stream));
-
-  static std::atomic<int> find_blocks_s{0}, resolve_blocks_s{0};
-  int find_blocks = find_blocks_s.load(), resolve_blocks = resolve_blocks_s.load();
-  if (!find_blocks) {
-    int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_find_persistent<192, true>, FIND_THREADS, 0));
-    find_blocks = std::max(1, per_sm) * c.num_sms;
-    find_blocks_s.store(find_blocks);
-  }
-  if (!resolve_blocks) {
-    int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resolve, RESOLVE_THREADS, 0));
-    resolve_blocks = std::max(1, per_sm) * c.num_sms;
-    resolve_blocks_s.store(resolve_blocks);
-  }
   const bool clamp = (size_t)b->max_depth * 2 <= 192;
   const uint32_t cap_rt = b->max_depth * 2;
   if (!clamp && cap_rt > 1024) return c.fail(OBVHS_ERR_LIMIT, "reinsertion stack bound above 1024 entries");
@@ -651,47 +777,111 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
     bool alt = false;
     cudaError_t e = radix_sort_pairs<uint32_t>(c, keys, vals, ncand, false, keys_alt, vals_alt, rs, &alt);
     if (e) return c.cuda_fail(e, "candidate sort");
-    const uint32_t* cand = alt ? vals_alt : vals;
-    // find_reinsertion for the first `count` candidates
-    uint32_t* pass_ctr = counters + 8 + (size_t)ri * 8;  // [5]: next candidate for k_find
-    const uint32_t fblocks = div_up<uint32_t>(count, FIND_THREADS);
-    if (fblocks > (uint32_t)find_blocks) {
-      if (clamp)
-        KLAUNCH("k_find", k_find_persistent<192, true><<<find_blocks, FIND_THREADS, 0, c.stream>>>(
-                              b->nodes, parents, cand, count, cap_rt, reins, pass_ctr + 5, c.d_status));
-      else
-        KLAUNCH("k_find", k_find_persistent<1024, false><<<find_blocks, FIND_THREADS, 0, c.stream>>>(
-                              b->nodes, parents, cand, count, cap_rt, reins, pass_ctr + 5, c.d_status));
-    } else if (clamp) {
-      KLAUNCH("k_find", k_find<192, true><<<fblocks, FIND_THREADS, 0, c.stream>>>(b->nodes, parents, cand, count, cap_rt,
-                                                                             reins, c.d_status));
-    } else {
-      KLAUNCH("k_find", k_find<1024, false><<<fblocks, FIND_THREADS, 0, c.stream>>>(b->nodes, parents, cand, count,
-                                                                               cap_rt, reins, c.d_status));
-    }
-    CK(cudaGetLastError());
-    // conflict resolution, moves and refit in one cooperative launch
-    ResolveArgs ra{b->nodes, parents, reins, count, plist, conf, state, owner, touched, dirty, arrive, starts,
-                   counters + 8 + (size_t)ri * 8, counters + 1, c.d_status, ri + 1, len, count + 3};
-    void* args[] = {&ra};
-    uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)resolve_blocks,
-                                                 std::max<uint64_t>(1, div_up<uint32_t>(count, RESOLVE_THREADS)));
-    if (grid == 1 || count <= RESOLVE_SINGLE_MAX || device_context_count(c.device) > 1) {
-      // one block, a normal launch (block barriers only)
-      KLAUNCH("k_resolve", k_resolve<<<1, RESOLVE_THREADS, 0, c.stream>>>(ra));
-      CK(cudaGetLastError());
-    } else {
-      KLAUNCH("k_resolve", CK(coop_launch(c, (const void*)k_resolve, grid, RESOLVE_THREADS, args, 0)));
-    }
-    CK(cudaGetLastError());
+    // find_reinsertion for the first `count` candidates, then the rest of the pass
+    r = reins_pass(c, b->nodes, len, alt ? vals_alt : vals, count, ri, clamp, cap_rt, StackModes{nullptr, nullptr, 0},
+                   B);
+    if (r) return r;
   }
   if (applied_deferred) {
-    CK(cudaMemcpyAsync(applied_deferred, counters + 1, 4, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaMemcpyAsync(applied_deferred, B.counters + 1, 4, cudaMemcpyDeviceToHost, c.stream));
     return 0;
   }
   uint32_t applied = 0;
-  CK(cudaMemcpyAsync(&applied, counters + 1, 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(&applied, B.counters + 1, 4, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
   *applied_out = applied;
+  return 0;
+}
+
+int seg_root_parents_device(BuildCtx& c, const SegLayout& L, uint32_t* parents) {
+  KLAUNCH("k_seg_root_parents", k_seg_root_parents<<<div_up<uint32_t>(L.n_seg, BLK), BLK, 0, c.stream>>>(
+                                    L.d_prim_start, L.d_node_start, L.n_seg, parents));
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int reinsertion_seg_device(BuildCtx& c, Bvh2Node* nodes, const SegLayout& L, const uint32_t* h_passes, float ratio,
+                           SegTableUpload upload, uint32_t* applied_deferred) {
+  *applied_deferred = 0;
+  const uint32_t S = L.n_seg, len = L.n_slots;
+  if (len == 0 || !(ratio > 0.0f)) return 0;
+  constexpr uint32_t NSEQ = 16;
+  // per pass: cand_start[S + 1], find_start[S + 1]; per scene: stack mode
+  const size_t stride = 2 * ((size_t)S + 1);
+  std::vector<uint32_t> tab(NSEQ * stride + S);
+  uint32_t* mode = tab.data() + NSEQ * stride;
+  uint32_t tot_cand[NSEQ], tot_count[NSEQ];
+  bool all_clamp = true;
+  for (uint32_t s = 0; s < S; s++) {
+    const uint32_t max_depth = std::max<uint32_t>(96, h_passes[s] + 1);
+    const bool clamp = (size_t)max_depth * 2 <= 192;
+    mode[s] = clamp ? (0x80000000u | 192u) : max_depth * 2;
+    // a scene with a root leaf (fewer than two leaves) is not optimised
+    if (!clamp && L.leaves(s) >= 2) {
+      all_clamp = false;
+      if (max_depth * 2 > 1024) return c.fail(OBVHS_ERR_LIMIT, "reinsertion stack bound above 1024 entries");
+    }
+  }
+  for (uint32_t ri = 0; ri < NSEQ; ri++) {
+    uint32_t* cs = tab.data() + ri * stride;
+    uint32_t* fs = cs + S + 1;
+    const float q = 1.0f / (float)(2 * ri + 1);
+    uint32_t ca = 0, ka = 0;
+    for (uint32_t s = 0; s < S; s++) {
+      cs[s] = ca;
+      fs[s] = ka;
+      const uint32_t m = L.leaves(s);
+      if (m < 2) continue;
+      const uint32_t n = 2 * m - 1;
+      const float bsf = ((float)n * ratio) * q;
+      uint64_t batch = bsf > 0.0f ? (bsf >= 1.8446744e19f ? ~0ull : (uint64_t)bsf) : 0;
+      if (batch < 1) batch = 1;
+      const uint32_t node_count = (uint32_t)std::min<uint64_t>(n, batch + 1);
+      const uint32_t take = (uint32_t)std::min<uint64_t>((uint64_t)node_count * 2, n);
+      if (node_count - 1 == 0) continue;
+      ca += take - 1;
+      ka += node_count - 1;
+    }
+    cs[S] = ca;
+    fs[S] = ka;
+    tot_cand[ri] = ca;
+    tot_count[ri] = ka;
+  }
+  uint32_t* d_tab = upload(tab.data(), tab.size() * 4);
+  if (!d_tab) return c.fail(OBVHS_ERR_OOM, "segment tables");
+  const uint32_t* d_mode = d_tab + NSEQ * stride;
+  uint32_t max_cand = 0;
+  for (uint32_t ri = 0; ri < NSEQ; ri++) max_cand = std::max(max_cand, tot_cand[ri]);
+  Scratch& sc = c.scratch;
+  unsigned long long* keys = (unsigned long long*)sc.get(SLOT_KEYS, (size_t)max_cand * 8);
+  unsigned long long* keys_alt = (unsigned long long*)sc.get(SLOT_KEYS_ALT, (size_t)max_cand * 8);
+  uint32_t* vals = (uint32_t*)sc.get(SLOT_REINS_VALS, (size_t)max_cand * 4);
+  uint32_t* vals_alt = (uint32_t*)sc.get(SLOT_VALS_ALT, (size_t)max_cand * 4);
+  uint32_t* cand = (uint32_t*)sc.get(SLOT_REINS_KEYS, (size_t)max_cand * 4);
+  uint32_t* rs = (uint32_t*)sc.get(SLOT_ALL_HIST, radix_scratch_words(std::max(max_cand, 1u)) * 4);
+  if (!keys || !keys_alt || !vals || !vals_alt || !cand || !rs) return c.fail(OBVHS_ERR_OOM, "scratch");
+  ReinsBufs B;
+  int r = reins_setup(c, nodes, len, NSEQ, B);
+  if (r) return r;
+  r = seg_root_parents_device(c, L, B.parents);
+  if (r) return r;
+  const StackModes modes{all_clamp ? nullptr : d_mode, L.d_node_start, S};
+  const int digits = 4 + (S <= 256 ? 1 : 2);
+  for (uint32_t ri = 0; ri < NSEQ; ri++) {
+    if (tot_count[ri] == 0) continue;
+    const uint32_t* cs = d_tab + ri * stride;
+    const uint32_t* fs = cs + S + 1;
+    KLAUNCH("k_seg_cand_keys", k_seg_cand_keys<<<div_up<uint32_t>(tot_cand[ri], BLK), BLK, 0, c.stream>>>(
+                                   nodes, cs, L.d_node_start, S, tot_cand[ri], keys, vals));
+    bool alt = false;
+    cudaError_t e = radix_sort_pairs<unsigned long long>(c, keys, vals, tot_cand[ri], false, keys_alt, vals_alt, rs,
+                                                         &alt, digits);
+    if (e) return c.cuda_fail(e, "candidate sort");
+    KLAUNCH("k_seg_cand_gather", k_seg_cand_gather<<<div_up<uint32_t>(tot_count[ri], BLK), BLK, 0, c.stream>>>(
+                                     alt ? vals_alt : vals, fs, cs, S, tot_count[ri], cand));
+    r = reins_pass(c, nodes, len, cand, tot_count[ri], ri, all_clamp, 192, modes, B);
+    if (r) return r;
+  }
+  CK(cudaMemcpyAsync(applied_deferred, B.counters + 1, 4, cudaMemcpyDeviceToHost, c.stream));
   return 0;
 }

@@ -442,10 +442,9 @@ __global__ void __launch_bounds__(TBLK) k_traverse_tlas(const CwNode* __restrict
   }
 }
 
-__global__ void k_reorder_tris(const float* __restrict__ tris, uint32_t n_tris, const uint32_t* __restrict__ pidx,
-                               uint32_t n_prims, float4* __restrict__ out, uint32_t* status) {
-  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n_prims) return;
+// The 64-byte record of BVH-order triangle k: tris[pidx[k]].
+__device__ __forceinline__ void write_bvh_tri(const float* tris, uint32_t n_tris, const uint32_t* pidx, uint32_t k,
+                                              float4* out, uint32_t* status) {
   uint32_t id = pidx[k];
   if (id >= n_tris) {
     set_status(status, ST_BAD_TREE);
@@ -462,11 +461,37 @@ __global__ void k_reorder_tris(const float* __restrict__ tris, uint32_t n_tris, 
   out[4 * (size_t)k + 3] = make_float4(n.z, 0.0f, 0.0f, 0.0f);
 }
 
+__global__ void k_reorder_tris(const float* __restrict__ tris, uint32_t n_tris, const uint32_t* __restrict__ pidx,
+                               uint32_t n_prims, float4* __restrict__ out, uint32_t* status) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n_prims) write_bvh_tri(tris, n_tris, pidx, k, out, status);
+}
+
+// Triangles of every scene of a segmented build, in BVH order.
+__global__ void k_seg_reorder_tris(const SegTriJob* __restrict__ jobs, const uint32_t* __restrict__ prim_start,
+                                   uint32_t n_seg, uint32_t total, uint32_t* status) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  const uint32_t s = seg_find(prim_start, n_seg, i);
+  const SegTriJob j = jobs[s];
+  const uint32_t k = i - __ldg(&prim_start[s]);
+  write_bvh_tri(j.tris, j.n_tris, j.pidx, k, j.out, status);
+}
+
 }  // namespace
+
+int reorder_tris_seg_device(BuildCtx& c, const SegTriJob* d_jobs, const uint32_t* d_prim_start, uint32_t n_seg,
+                            uint32_t total) {
+  if (!total) return 0;
+  KLAUNCH("k_seg_reorder_tris", k_seg_reorder_tris<<<div_up<uint32_t>(total, 256), 256, 0, c.stream>>>(
+                                    d_jobs, d_prim_start, n_seg, total, c.d_status));
+  CK(cudaGetLastError());
+  return 0;
+}
 
 int reorder_tris_device(BuildCtx& c, obvhs_cwbvh* b, const float* tris, uint32_t n_tris) {
   if (b->tris) {
-    cudaFree(b->tris);
+    b->free_buf(b->tris);
     b->tris = nullptr;
   }
   b->n_tris = n_tris;
@@ -519,7 +544,7 @@ int traverse_tlas_device(BuildCtx& c, const obvhs_cwbvh* tlas, const obvhs_cwbvh
 
 int compress_tris_device(BuildCtx& c, obvhs_cwbvh* b, const float* tris, uint32_t n_tris) {
   if (b->ctris) {
-    cudaFree(b->ctris);
+    b->free_buf(b->ctris);
     b->ctris = nullptr;
   }
   if (b->n_prims == 0) return 0;
