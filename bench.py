@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tris", type=int, default=N_TRIS)
+    ap.add_argument("--no-serving", action="store_true",
+                    help="skip the serving run (Poisson request stream, resident BVHs, continuous batching)")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the 512-scene batched build + traversal comparison")
     ap.add_argument("--no-arch-scene", action="store_true",
@@ -356,6 +358,64 @@ def batched_scenes(G, ctx, base, n_scenes=512, seed=1004):
             "batched_trace_mrays_s": n_rays / t_trace / 1e6, "identical_hits": identical}
 
 
+def serving(params, n_requests=3000, rate=2000.0, budget=80 << 30, seed=1005):
+    """The serving workload: Poisson arrivals (2,000 requests/s), 10% builds
+    of 10k-2M clustered triangles that become resident BVHs, 90% ray batches
+    of 1k-1M rays (log-uniform; half primary pinhole, half incoherent) against
+    a resident BVH chosen by Zipf(1.1), LRU eviction under an 80 GB budget.
+    Inputs are prefixes of 8 pooled 2M-triangle scenes and their 1M-ray
+    batches in pinned host memory; 8 BVHs are resident before the first
+    request.  The same stream runs through the continuous-batching server and
+    the plain one-request-per-call server; per-request hits are compared by a
+    digest of the (id, t) words."""
+    from obvhs_gb300 import serve as V
+
+    tris, rays = V.clustered_pools(8, 2_000_000, 1_000_000, seed=seed)
+    rng = np.random.default_rng(seed)
+    reqs, scene_of = V.make_stream(n_requests, rate, tris, rays, rng, preloaded=8)
+    pre = [(i, tris[scene_of[i]][:200_000]) for i in range(8)]
+
+    def digest(block):
+        # (sum, xor) of the request's (id, t) words: cheap enough to stay off
+        # the serving path's critical time, and any differing hit changes it
+        w = block.view(np.uint64).ravel()
+        return int(w.sum(dtype=np.uint64)), int(np.bitwise_xor.reduce(w)) if len(w) else 0
+
+    be = V.GpuBackend(params)
+    out = {}
+    try:
+        # warm-up on a short stream of the same kind
+        wreqs, wsc = V.make_stream(200, rate, tris, rays, np.random.default_rng(seed + 1), preloaded=8)
+        V.ContinuousServer(be, budget, result_sink=digest).run(wreqs, preload=pre)
+        V.PlainServer(be, budget, result_sink=digest).run(wreqs, preload=pre)
+        results = {}
+        for name, cls in (("continuous", V.ContinuousServer), ("plain", V.PlainServer)):
+            for r in reqs:
+                r.done, r.result, r.step = None, None, -1
+            srv = cls(be, budget, result_sink=digest)
+            srv.run(reqs, preload=pre)
+            summ = V.summarize(reqs)
+            summ["evictions"] = srv.store.evictions
+            summ["rebuilds"] = srv.rebuilds
+            if name == "continuous":
+                summ["launch_steps_build"] = srv.steps["build"]
+                summ["launch_steps_rays"] = srv.steps["rays"]
+            out[name] = summ
+            results[name] = [r.result for r in reqs]
+            for k in list(srv.store.items):
+                srv.store.items.pop(k)[0].free()
+        out["identical_hits"] = results["continuous"] == results["plain"]
+    finally:
+        be.close()
+    c, pl = out["continuous"], out["plain"]
+    out.update({"workload": f"{n_requests} requests, Poisson {rate:.0f}/s, 10% builds (10k-2M tris) / 90% ray "
+                            "batches (1k-1M rays, half primary, half incoherent), Zipf(1.1) targets, "
+                            f"{budget >> 30} GB budget, LRU", "preset": "medium_build",
+                "p99_speedup_rays": pl["latency_rays"]["p99_ms"] / c["latency_rays"]["p99_ms"],
+                "throughput_ratio": c["mrays_s"] / pl["mrays_s"]})
+    return out
+
+
 def workload(n):
     from obvhs_gb300 import scenes as S
 
@@ -551,6 +611,7 @@ def run_gb300(args):
 
     arch = None if args.no_arch_scene else arch_scene(ctx, stream, max(3, args.steps // 4), args.warmup, flush)
     batch = None if args.no_batched else batched_scenes(G, ctx, BvhBuildParams.medium_build())
+    served = None if args.no_serving else serving(BvhBuildParams.medium_build())
 
     # CPU baseline (the oracle on this host's cores, bounded sample): two full
     # builds, and the primary batch traced with node-visit / triangle-test
@@ -622,6 +683,7 @@ def run_gb300(args):
                                "algorithmic_bytes_per_launch": alg_bytes, "bytes_per_ray": alg_bytes / len(rays)},
         "architectural_scene": arch,
         "batched": batch,
+        "serving": served,
         "cpu_baseline": {"value": cpu_rate, "unit": "Mtris/s", "cores": cores, "kind": "port",
                          "sample": f"2 full {n}-triangle slow_build builds on {cores} threads "
                                    f"({sum(cpu_t):.1f} s)",

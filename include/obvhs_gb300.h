@@ -122,6 +122,12 @@ OBVHS_API uint64_t obvhs_ctx_kernel_launches(const obvhs_ctx* ctx);
  * on the context's stream.  The report (JSON: kernel -> launches, total_ms,
  * max_ms) covers the launches since the last report and clears them. */
 OBVHS_API int obvhs_ctx_set_profiling(obvhs_ctx* ctx, int enable);
+/* No counterpart in the reference.  shared != 0: this context's builds leave
+ * most of the GPU to other work (PLOC of up to 262,144 leaves and reinsertion
+ * conflict resolution run as one block each, normal launches, instead of
+ * grid-wide cooperative launches).  Builds take this form by themselves while
+ * several builds are in flight on the device.  Results are identical. */
+OBVHS_API int obvhs_ctx_set_shared_gpu(obvhs_ctx* ctx, int shared);
 OBVHS_API int obvhs_ctx_profile_report(obvhs_ctx* ctx, char* buf, uint64_t cap);
 
 /* ---- BVH2 --------------------------------------------------------------- */
@@ -254,6 +260,16 @@ OBVHS_API int obvhs_build_cwbvh_from_tris_segmented(obvhs_ctx* ctx, const float*
 OBVHS_API int obvhs_ray_traverse_multi(obvhs_ctx* ctx, const obvhs_cwbvh* const* bvhs, uint32_t n_bvh,
                                        const uint32_t* ray_bvh, const obvhs_ray* rays, uint32_t n, obvhs_hit* hits,
                                        int device_ptrs);
+
+/* The serving form of obvhs_ray_traverse_multi: n_batches ray batches (host
+ * memory; page-locked memory makes every copy asynchronous), batch b traced in
+ * bvhs[batch_bvh[b]], all in one traversal launch; batch b's hits go to
+ * hits[b] (counts[b] entries).  One copy in and one copy out per batch, the
+ * per-ray BVH index built on the device, one synchronisation at the end.
+ * Hits equal obvhs_ray_traverse of each batch alone. */
+OBVHS_API int obvhs_ray_traverse_batches(obvhs_ctx* ctx, const obvhs_cwbvh* const* bvhs, uint32_t n_bvh,
+                                         uint32_t n_batches, const uint32_t* batch_bvh, const obvhs_ray* const* rays,
+                                         const uint32_t* counts, obvhs_hit* const* hits);
 
 /* ---- stage-level access for parity checks ------------------------------- */
 /* sort_nodes_by_morton (src/ploc/mod.rs:771-847) on Bvh2Node::new(aabbs[i])

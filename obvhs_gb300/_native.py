@@ -69,6 +69,7 @@ SIGNATURES = {
     "obvhs_ctx_synchronize": (I32, [P]),
     "obvhs_ctx_kernel_launches": (U64, [P]),
     "obvhs_ctx_set_profiling": (I32, [P, I32]),
+    "obvhs_ctx_set_shared_gpu": (I32, [P, I32]),
     "obvhs_ctx_profile_report": (I32, [P, P, U64]),
     "obvhs_ploc_build": (I32, [P, P, P, U32, U32, U32, U32, I32, ctypes.POINTER(P), ctypes.POINTER(BuildStats)]),
     "obvhs_bvh2_info": (I32, [P, ctypes.POINTER(U32), ctypes.POINTER(U32), ctypes.POINTER(U32)]),
@@ -94,6 +95,7 @@ SIGNATURES = {
     "obvhs_build_cwbvh_from_tris_batch": (I32, [P, U32, P, P, U32, ctypes.POINTER(BuildParams), I32, P, P]),
     "obvhs_build_cwbvh_from_tris_segmented": (I32, [P, P, P, U32, ctypes.POINTER(BuildParams), I32, P, P]),
     "obvhs_ray_traverse_multi": (I32, [P, P, U32, P, P, U32, P, I32]),
+    "obvhs_ray_traverse_batches": (I32, [P, P, U32, U32, P, P, P, P]),
     "obvhs_cwbvh_set_triangles_compressed": (I32, [P, P, P, U32, I32]),
     "obvhs_cwbvh_download_compressed": (I32, [P, P, P]),
     "obvhs_ray_traverse_compressed": (I32, [P, P, P, U32, P, I32]),

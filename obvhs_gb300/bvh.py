@@ -41,7 +41,9 @@ def _prep(x, dtype, cols):
         if x.dtype != want and not (dtype is np.uint32 and x.dtype == torch.int32):
             raise TypeError(f"expected a {want} tensor")
         x = x.contiguous()
-        torch.cuda.synchronize(x.device)
+        # the tensor's producer ran on torch's current stream; the library's
+        # work goes on its own stream
+        torch.cuda.current_stream(x.device).synchronize()
         n = x.numel() // cols if cols else x.numel()
         return ctypes.c_void_p(x.data_ptr()), n, 1, x
     a = np.ascontiguousarray(x, dtype=dtype)
@@ -102,6 +104,11 @@ class Context:
     def set_profiling(self, enable: bool):
         """Brackets every kernel launch with CUDA events on the context's stream."""
         self.check(self.lib.obvhs_ctx_set_profiling(self.h, int(enable)))
+
+    def set_shared_gpu(self, shared: bool = True):
+        """Builds on this context leave most of the GPU to other work (one-block
+        PLOC and conflict resolution); results are identical."""
+        self.check(self.lib.obvhs_ctx_set_shared_gpu(self.h, int(bool(shared))))
 
     def profile_report(self) -> dict:
         """Per-kernel {launches, total_ms, max_ms} since the last report."""
@@ -542,6 +549,33 @@ def ray_traverse_multi(bvhs, ray_bvh, rays, ctx: Context | None = None, out=None
         return out
     del keep, keepb
     return out[:, 0].copy(), out[:, 1].copy().view(np.float32)
+
+
+def ray_traverse_batches(bvhs, batch_bvh, rays, outs=None, ctx: Context | None = None):
+    """Closest hits of several host ray batches in one launch: batch b traced
+    in bvhs[batch_bvh[b]].  Returns one (n_b, 2) uint32 array per batch
+    (primitive id, t bits), or fills `outs` (preallocated, e.g. in pinned
+    memory).  Equal to CwBvh.ray_traverse of each batch alone."""
+    ctx = _ctx(ctx)
+    nb = len(rays)
+    arrs = [np.ascontiguousarray(r, dtype=np.float32).reshape(-1, 8) for r in rays]
+    if outs is None:
+        outs = [np.zeros((len(a), 2), np.uint32) for a in arrs]
+    for a, o in zip(arrs, outs):
+        if o.shape != (len(a), 2) or o.dtype != np.uint32 or not o.flags.c_contiguous:
+            raise ValueError("each output must be a contiguous (n, 2) uint32 array")
+    harr = (ctypes.c_void_p * max(len(bvhs), 1))(*[b.h.value if isinstance(b.h, ctypes.c_void_p) else b.h for b in bvhs])
+    idx = np.ascontiguousarray(batch_bvh, dtype=np.uint32)
+    if len(idx) != nb:
+        raise ValueError("one BVH index per batch")
+    counts = np.array([len(a) for a in arrs], np.uint32)
+    rp = (ctypes.c_void_p * max(nb, 1))(*[a.ctypes.data for a in arrs])
+    op = (ctypes.c_void_p * max(nb, 1))(*[o.ctypes.data for o in outs])
+    ctx.check(ctx.lib.obvhs_ray_traverse_batches(ctx.h, ctypes.cast(harr, ctypes.c_void_p), len(bvhs), nb,
+                                                 idx.ctypes.data_as(ctypes.c_void_p), ctypes.cast(rp, ctypes.c_void_p),
+                                                 counts.ctypes.data_as(ctypes.c_void_p),
+                                                 ctypes.cast(op, ctypes.c_void_p)))
+    return outs
 
 
 def _params(p: BvhBuildParams) -> N.BuildParams:

@@ -437,6 +437,7 @@ struct DeviceShared {
   std::mutex m;
   cudaStream_t coop = nullptr;
   std::atomic<int> contexts{0};
+  std::atomic<int> builds{0};
 };
 
 DeviceShared& device_shared(int device) {
@@ -447,6 +448,9 @@ DeviceShared& device_shared(int device) {
 }  // namespace
 
 int device_context_count(int device) { return device_shared(device).contexts.load(); }
+int device_concurrent_builds(int device) { return device_shared(device).builds.load(); }
+void device_build_enter(int device) { device_shared(device).builds.fetch_add(1); }
+void device_build_leave(int device) { device_shared(device).builds.fetch_sub(1); }
 
 cudaError_t coop_launch(obvhs_ctx& c, const void* func, unsigned grid, unsigned block, void** args, size_t smem) {
   DeviceShared& d = device_shared(c.device);
@@ -529,6 +533,12 @@ int obvhs_ctx_synchronize(obvhs_ctx* c) {
 }
 uint64_t obvhs_ctx_kernel_launches(const obvhs_ctx* c) { return c ? c->kernel_launches : 0; }
 
+int obvhs_ctx_set_shared_gpu(obvhs_ctx* c, int shared) {
+  if (!c) return OBVHS_ERR_INVALID_ARG;
+  c->shared_gpu = shared != 0;
+  return OBVHS_OK;
+}
+
 int obvhs_ctx_set_profiling(obvhs_ctx* c, int enable) {
   if (!c) return OBVHS_ERR_INVALID_ARG;
   c->profiling = enable != 0;
@@ -583,6 +593,7 @@ int obvhs_ploc_build(obvhs_ctx* cp, const float* aabbs, const uint32_t* indices,
   if (!cp || !out || (n && !aabbs)) return OBVHS_ERR_INVALID_ARG;
   BuildCtx& c = *cp;
   DeviceGuard g(c.device);
+  BuildScope building(c.device);
   *out = nullptr;
   if (search_distance < 1 || search_distance > 32) return c.fail(OBVHS_ERR_INVALID_ARG, "search distance must be 1..32");
   if (sort_precision > 1) return c.fail(OBVHS_ERR_INVALID_ARG, "sort_precision must be 0 or 1");
@@ -699,6 +710,7 @@ int obvhs_reinsertion_run(obvhs_ctx* cp, obvhs_bvh2* b, float ratio, const float
   if (!cp || !b) return OBVHS_ERR_INVALID_ARG;
   BuildCtx& c = *cp;
   DeviceGuard g(c.device);
+  BuildScope building(c.device);
   uint64_t a = 0;
   int r = reinsertion_device(c, b, ratio, seq, seq ? nseq : 0, &a);
   if (!r) r = take_status(c);
@@ -749,6 +761,7 @@ int obvhs_bvh2_to_cwbvh(obvhs_ctx* cp, const obvhs_bvh2* b, uint32_t max_prims, 
   if (!cp || !b || !out) return OBVHS_ERR_INVALID_ARG;
   BuildCtx& c = *cp;
   DeviceGuard g(c.device);
+  BuildScope building(c.device);
   *out = nullptr;
   if (max_prims < 1 || max_prims > 3) return c.fail(OBVHS_ERR_INVALID_ARG, "max_prims_per_leaf must be 1..3");
   obvhs_cwbvh* cw = new obvhs_cwbvh();
@@ -775,6 +788,7 @@ int obvhs_build_cwbvh_from_tris(obvhs_ctx* cp, const float* triangles, uint32_t 
   if (!cp || !p || !out || (n && !triangles)) return OBVHS_ERR_INVALID_ARG;
   BuildCtx& c = *cp;
   DeviceGuard g(c.device);
+  BuildScope building(c.device);
   *out = nullptr;
   int err = 0;
   const float* dt = (const float*)stage_in(c, SLOT_INPUT, triangles, (size_t)n * 36, device_ptrs, &err);
@@ -834,6 +848,7 @@ int obvhs_build_cwbvh_from_tris_segmented(obvhs_ctx* cp, const float* const* tri
   if (!cp || !p || (n_scenes && (!triangles || !n_tris || !out))) return OBVHS_ERR_INVALID_ARG;
   BuildCtx& c = *cp;
   DeviceGuard g(c.device);
+  BuildScope building(c.device);
   for (uint32_t i = 0; i < n_scenes; i++) {
     out[i] = nullptr;
     if (n_tris[i] && !triangles[i]) return OBVHS_ERR_INVALID_ARG;
@@ -896,11 +911,69 @@ int obvhs_ray_traverse_multi(obvhs_ctx* cp, const obvhs_cwbvh* const* bvhs, uint
   return OBVHS_OK;
 }
 
+int obvhs_ray_traverse_batches(obvhs_ctx* cp, const obvhs_cwbvh* const* bvhs, uint32_t n_bvh, uint32_t n_batches,
+                               const uint32_t* batch_bvh, const obvhs_ray* const* rays, const uint32_t* counts,
+                               obvhs_hit* const* hits) {
+  if (!cp || (n_bvh && !bvhs) || (n_batches && (!batch_bvh || !rays || !counts || !hits)))
+    return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  uint64_t total = 0;
+  for (uint32_t b = 0; b < n_batches; b++) {
+    if (batch_bvh[b] >= n_bvh || (counts[b] && (!rays[b] || !hits[b]))) return OBVHS_ERR_INVALID_ARG;
+    total += counts[b];
+  }
+  if (total > 0x7fffffffull) return c.fail(OBVHS_ERR_TOO_LARGE, "more than 2^31 rays in one call");
+  if (!total) return OBVHS_OK;
+  const uint32_t n = (uint32_t)total;
+  Scratch& s = c.scratch;
+  char* d_rays = (char*)s.get(SLOT_INPUT2, (size_t)n * 32);
+  uint32_t* d_owner = (uint32_t*)s.get(SLOT_INPUT, (size_t)n * 4);
+  char* d_hits = (char*)s.get(SLOT_TRAV_OUT, (size_t)n * 8 + 16);
+  const size_t tab_bytes = (2 * (size_t)n_batches + 1) * 4;
+  uint32_t* d_tab = (uint32_t*)s.get(SLOT_SEG, tab_bytes);
+  if (!d_rays || !d_owner || !d_hits || !d_tab) return c.fail(OBVHS_ERR_OOM, "scratch");
+  if (c.h_seg_cap < tab_bytes) {
+    if (c.h_seg) cudaFreeHost(c.h_seg);
+    c.h_seg = nullptr;
+    c.h_seg_cap = 0;
+    if (cudaMallocHost(&c.h_seg, tab_bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return c.fail(OBVHS_ERR_OOM, "pinned staging");
+    }
+    c.h_seg_cap = tab_bytes;
+  }
+  // offsets[0..n_batches] then the batches' BVH indices, through pinned staging
+  uint32_t* tab = static_cast<uint32_t*>(c.h_seg);
+  uint32_t at = 0;
+  for (uint32_t b = 0; b < n_batches; b++) {
+    tab[b] = at;
+    tab[n_batches + 1 + b] = batch_bvh[b];
+    if (counts[b])
+      CK(cudaMemcpyAsync(d_rays + (size_t)at * 32, rays[b], (size_t)counts[b] * 32, cudaMemcpyHostToDevice, c.stream));
+    at += counts[b];
+  }
+  tab[n_batches] = at;
+  CK(cudaMemcpyAsync(d_tab, tab, tab_bytes, cudaMemcpyHostToDevice, c.stream));
+  int r = batch_owner_device(c, d_tab, d_tab + n_batches + 1, n_batches, n, d_owner);
+  if (r) return r;
+  r = traverse_multi_device(c, bvhs, n_bvh, d_owner, (const float*)d_rays, n, (uint32_t*)d_hits, nullptr, 0);
+  if (r) return r;
+  at = 0;
+  for (uint32_t b = 0; b < n_batches; b++) {
+    if (counts[b])
+      CK(cudaMemcpyAsync(hits[b], d_hits + (size_t)at * 8, (size_t)counts[b] * 8, cudaMemcpyDeviceToHost, c.stream));
+    at += counts[b];
+  }
+  return take_status(c);
+}
+
 int obvhs_build_cwbvh(obvhs_ctx* cp, const float* aabbs, uint32_t n, const obvhs_build_params* p, int device_ptrs,
                       obvhs_cwbvh** out, obvhs_build_stats* stats) {
   if (!cp || !p || !out || (n && !aabbs)) return OBVHS_ERR_INVALID_ARG;
   BuildCtx& c = *cp;
   DeviceGuard g(c.device);
+  BuildScope building(c.device);
   *out = nullptr;
   int err = 0;
   const float* da = (const float*)stage_in(c, SLOT_INPUT, aabbs, (size_t)n * 24, device_ptrs, &err);

@@ -160,6 +160,7 @@ struct obvhs_ctx {
   }
 
   cudaEvent_t coop_ev[2] = {nullptr, nullptr};  // cooperative launches through the device's shared stream
+  bool shared_gpu = false;                       // obvhs_ctx_set_shared_gpu
 
   int fail(int code, const std::string& msg) {
     last_error = msg;
@@ -178,8 +179,22 @@ typedef obvhs_ctx BuildCtx;
 // hand-off with the caller's stream) so that no two of them are on the GPU
 // at once.
 cudaError_t coop_launch(obvhs_ctx& c, const void* func, unsigned grid, unsigned block, void** args, size_t smem);
-// Live contexts on `device` (more than one: the GPU is shared by concurrent builds).
+// Live contexts on `device`.
 int device_context_count(int device);
+// Builds in flight on `device` (every building entry point holds a BuildScope).
+int device_concurrent_builds(int device);
+void device_build_enter(int device);
+void device_build_leave(int device);
+struct BuildScope {
+  int device;
+  explicit BuildScope(int d) : device(d) { device_build_enter(d); }
+  ~BuildScope() { device_build_leave(device); }
+};
+// Whether a build should leave most of the GPU to other work: several builds
+// in flight on its device, or the context says so (obvhs_ctx_set_shared_gpu).
+// Only the launch forms change (one block instead of a grid-wide launch for
+// PLOC up to 262,144 leaves and for reinsertion resolves); results do not.
+inline bool gpu_shared(const obvhs_ctx& c) { return c.shared_gpu || device_concurrent_builds(c.device) > 1; }
 
 // Launch wrapper: counts the launch and, when profiling, brackets it with
 // CUDA events on the context's stream.
@@ -319,6 +334,10 @@ struct SegTriJob {
 };
 int reorder_tris_seg_device(BuildCtx& c, const SegTriJob* d_jobs, const uint32_t* d_prim_start, uint32_t n_seg,
                             uint32_t total);
+// owner[i] = d_batch_bvh[b] for ray i of batch b (batches concatenated,
+// batch b starting at d_offsets[b]).
+int batch_owner_device(BuildCtx& c, const uint32_t* d_offsets, const uint32_t* d_batch_bvh, uint32_t n_batches,
+                       uint32_t total, uint32_t* owner);
 int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint32_t n, uint32_t* hits,
                     uint8_t* miss, int mode);
 int reorder_tris_device(BuildCtx& c, obvhs_cwbvh* bvh, const float* tris, uint32_t n_tris);

@@ -1055,9 +1055,9 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
     }
     PlocCoopArgs pa{{cur, nxt}, out_nodes, st, merge, tile_cnt, (int)radius, depth_threshold, max_passes, c.d_status};
     void* args[] = {&pa};
-    if (device_context_count(c.device) > 1 && n <= SHARED_SINGLE_BLOCK_MAX) {
-      // the GPU is shared with other contexts: one block, a normal launch,
-      // runs beside their work instead of waiting for a whole-GPU slot
+    if (gpu_shared(c) && n <= SHARED_SINGLE_BLOCK_MAX) {
+      // the GPU is shared with other builds or work: one block, a normal
+      // launch, runs beside them instead of waiting for a whole-GPU slot
       KLAUNCH("k_ploc_coop", k_ploc_coop<<<1, COOP_GROUPS * PT, smem, c.stream>>>(pa));
       CK(cudaGetLastError());
     } else {

@@ -710,7 +710,7 @@ int reins_pass(BuildCtx& c, Bvh2Node* nodes, uint32_t len, const uint32_t* cand,
   void* args[] = {&ra};
   uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)resolve_blocks,
                                                std::max<uint64_t>(1, div_up<uint32_t>(count, RESOLVE_THREADS)));
-  if (grid == 1 || count <= RESOLVE_SINGLE_MAX || device_context_count(c.device) > 1) {
+  if (grid == 1 || count <= RESOLVE_SINGLE_MAX || gpu_shared(c)) {
     // one block, a normal launch (block barriers only)
     KLAUNCH("k_resolve", k_resolve<<<1, RESOLVE_THREADS, 0, c.stream>>>(ra));
   } else {

@@ -478,7 +478,23 @@ __global__ void k_seg_reorder_tris(const SegTriJob* __restrict__ jobs, const uin
   write_bvh_tri(j.tris, j.n_tris, j.pidx, k, j.out, status);
 }
 
+// Ray i of concatenated batches: the BVH of its batch.
+__global__ void k_batch_owner(const uint32_t* __restrict__ offsets, const uint32_t* __restrict__ batch_bvh,
+                              uint32_t n_batches, uint32_t total, uint32_t* __restrict__ owner) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < total) owner[i] = __ldg(&batch_bvh[seg_find(offsets, n_batches, i)]);
+}
+
 }  // namespace
+
+int batch_owner_device(BuildCtx& c, const uint32_t* d_offsets, const uint32_t* d_batch_bvh, uint32_t n_batches,
+                       uint32_t total, uint32_t* owner) {
+  if (!total) return 0;
+  KLAUNCH("k_batch_owner", k_batch_owner<<<div_up<uint32_t>(total, 256), 256, 0, c.stream>>>(d_offsets, d_batch_bvh,
+                                                                                             n_batches, total, owner));
+  CK(cudaGetLastError());
+  return 0;
+}
 
 int reorder_tris_seg_device(BuildCtx& c, const SegTriJob* d_jobs, const uint32_t* d_prim_start, uint32_t n_seg,
                             uint32_t total) {

@@ -104,14 +104,16 @@ def test_batched_build_error_frees_everything_and_contexts_recover(G):
 
 
 def test_shared_gpu_paths_match_the_oracle(G):
-    """With several live contexts, PLOC and conflict resolution run as single
-    blocks with normal launches (beside other contexts' work); the result is
-    the same tree as the whole-GPU cooperative forms and the oracle."""
+    """On a context marked as sharing the GPU (the form builds take while
+    several are in flight), PLOC and conflict resolution run as single blocks
+    with normal launches; the result is the same tree as the whole-GPU
+    cooperative forms and the oracle."""
     from oracle import oracle as O
 
     tris = S.scene2_tris(200_000, offset=9)
     p = BvhBuildParams.slow_build()
-    extra, other = G.Context(0), G.Context(0)  # at least two live contexts
+    extra, other = G.Context(0), G.Context(0)  # two live contexts: cooperative launches take the shared stream
+    extra.set_shared_gpu(True)
     try:
         cw = G.build_cwbvh_from_tris(tris, p, ctx=extra)
         nodes, prims = cw.download()
