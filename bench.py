@@ -389,30 +389,38 @@ def serving(params, n_requests=3000, rate=2000.0, budget=80 << 30, seed=1005):
         V.ContinuousServer(be, budget, result_sink=digest).run(wreqs, preload=pre)
         V.PlainServer(be, budget, result_sink=digest).run(wreqs, preload=pre)
         results = {}
-        for name, cls in (("continuous", V.ContinuousServer), ("plain", V.PlainServer)):
-            for r in reqs:
-                r.done, r.result, r.step = None, None, -1
-            srv = cls(be, budget, result_sink=digest)
-            srv.run(reqs, preload=pre)
-            summ = V.summarize(reqs)
-            summ["evictions"] = srv.store.evictions
-            summ["rebuilds"] = srv.rebuilds
-            if name == "continuous":
-                summ["launch_steps_build"] = srv.steps["build"]
-                summ["launch_steps_rays"] = srv.steps["rays"]
-            out[name] = summ
-            results[name] = [r.result for r in reqs]
-            for k in list(srv.store.items):
-                srv.store.items.pop(k)[0].free()
-        out["identical_hits"] = results["continuous"] == results["plain"]
+        arrival = [r.arrival for r in reqs]
+        # at the offered rate, then the same stream 20x compressed (40,000
+        # requests/s: both servers saturated, throughput = capacity)
+        for scen, squeeze in (("", 1.0), ("saturated_", 0.05)):
+            for name, cls in (("continuous", V.ContinuousServer), ("plain", V.PlainServer)):
+                for r, a in zip(reqs, arrival):
+                    r.arrival, r.done, r.result, r.step = a * squeeze, None, None, -1
+                srv = cls(be, budget, result_sink=digest)
+                srv.run(reqs, preload=pre)
+                summ = V.summarize(reqs)
+                summ["evictions"] = srv.store.evictions
+                summ["rebuilds"] = srv.rebuilds
+                if name == "continuous":
+                    summ["launch_steps_build"] = srv.steps["build"]
+                    summ["launch_steps_rays"] = srv.steps["rays"]
+                out[scen + name] = summ
+                results[scen + name] = [r.result for r in reqs]
+                for k in list(srv.store.items):
+                    srv.store.items.pop(k)[0].free()
+        out["identical_hits"] = (results["continuous"] == results["plain"] == results["saturated_continuous"]
+                                 == results["saturated_plain"])
     finally:
         be.close()
     c, pl = out["continuous"], out["plain"]
+    sc, sp = out["saturated_continuous"], out["saturated_plain"]
     out.update({"workload": f"{n_requests} requests, Poisson {rate:.0f}/s, 10% builds (10k-2M tris) / 90% ray "
                             "batches (1k-1M rays, half primary, half incoherent), Zipf(1.1) targets, "
                             f"{budget >> 30} GB budget, LRU", "preset": "medium_build",
                 "p99_speedup_rays": pl["latency_rays"]["p99_ms"] / c["latency_rays"]["p99_ms"],
-                "throughput_ratio": c["mrays_s"] / pl["mrays_s"]})
+                "throughput_ratio_offered": c["mrays_s"] / pl["mrays_s"],
+                "capacity_ratio": sc["mrays_s"] / sp["mrays_s"],
+                "capacity_mrays_s": sc["mrays_s"], "capacity_mrays_s_plain": sp["mrays_s"]})
     return out
 
 
