@@ -171,6 +171,28 @@ OBVHS_API int obvhs_split_thresholds(obvhs_ctx* ctx, const float* triangles, uin
  * 1..3; the output node and primitive order equals the reference's. */
 OBVHS_API int obvhs_bvh2_to_cwbvh(obvhs_ctx* ctx, const obvhs_bvh2* bvh, uint32_t max_prims_per_leaf, int order_children,
                         obvhs_cwbvh** out);
+/* bvh2_to_cwbvh with include_exact_node_aabbs (src/cwbvh/bvh2_to_cwbvh.rs:
+ * 490-510, :76-80): the CWBVH also keeps, per node, the exact box of the BVH2
+ * node it came from (read with obvhs_cwbvh_exact_node_aabbs; used and moved
+ * by the order_children post-pass).  The reference sizes that Vec by the BVH2
+ * node count with empty boxes past the CWBVH nodes; only the CWBVH nodes'
+ * entries are kept here. */
+OBVHS_API int obvhs_bvh2_to_cwbvh_ex(obvhs_ctx* ctx, const obvhs_bvh2* bvh, uint32_t max_prims_per_leaf,
+                                     int order_children, int include_exact_node_aabbs, obvhs_cwbvh** out);
+/* CwBvh::exact_node_aabbs: n_nodes x (min xyz, max xyz); OBVHS_ERR_INVALID_ARG
+ * when the CWBVH was built without them. */
+OBVHS_API int obvhs_cwbvh_exact_node_aabbs(obvhs_ctx* ctx, const obvhs_cwbvh* bvh, float* aabbs6);
+/* CwBvh::order_children / order_node_children (src/cwbvh/mod.rs:520-735):
+ * re-sorts each node's children by octant from the children's compressed
+ * boxes (exact ones when kept), moving child node records within their
+ * blocks; node bytes identical to the reference's pass.  prim_aabbs: the
+ * primitives' boxes (n_prims x 6), in original order, or in
+ * primitive_indices order with direct_layout. */
+OBVHS_API int obvhs_cwbvh_order_children(obvhs_ctx* ctx, obvhs_cwbvh* bvh, const float* prim_aabbs, uint32_t n_prims,
+                                         int direct_layout, int device_ptrs);
+OBVHS_API int obvhs_cwbvh_order_node_children(obvhs_ctx* ctx, obvhs_cwbvh* bvh, const float* prim_aabbs,
+                                              uint32_t n_prims, uint32_t node_index, int direct_layout,
+                                              int device_ptrs);
 /* build_cwbvh_from_tris (src/cwbvh/builder.rs:20-85): [pre-split] -> PLOC ->
  * reinsertion -> bvh2_to_cwbvh(max_prims.clamp(1,3), true).  The triangles
  * are also attached for traversal. */

@@ -80,6 +80,10 @@ SIGNATURES = {
     "obvhs_split_aabbs_preset": (I32, [P, P, U32, P, P, U32, ctypes.POINTER(U32)]),
     "obvhs_split_thresholds": (I32, [P, P, U32, P]),
     "obvhs_bvh2_to_cwbvh": (I32, [P, P, U32, I32, ctypes.POINTER(P)]),
+    "obvhs_bvh2_to_cwbvh_ex": (I32, [P, P, U32, I32, I32, ctypes.POINTER(P)]),
+    "obvhs_cwbvh_exact_node_aabbs": (I32, [P, P, P]),
+    "obvhs_cwbvh_order_children": (I32, [P, P, P, U32, I32, I32]),
+    "obvhs_cwbvh_order_node_children": (I32, [P, P, P, U32, U32, I32, I32]),
     "obvhs_build_cwbvh_from_tris": (I32, [P, P, U32, ctypes.POINTER(BuildParams), I32, ctypes.POINTER(P),
                                           ctypes.POINTER(BuildStats)]),
     "obvhs_build_cwbvh": (I32, [P, P, U32, ctypes.POINTER(BuildParams), I32, ctypes.POINTER(P),

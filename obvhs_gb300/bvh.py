@@ -340,6 +340,31 @@ class CwBvh:
                                              pidx.ctypes.data_as(ctypes.c_void_p), len(pidx), ctypes.byref(h)))
         return CwBvh(ctx, h)
 
+    def exact_node_aabbs(self):
+        """CwBvh::exact_node_aabbs: (n_nodes, 6) float32 (min xyz, max xyz), or
+        None when the CWBVH was built without them."""
+        nn, _, _ = self.info()
+        out = np.zeros((nn, 6), np.float32)
+        r = self.ctx.lib.obvhs_cwbvh_exact_node_aabbs(self.ctx.h, self.h, out.ctypes.data_as(ctypes.c_void_p))
+        if r == -1 and nn:  # invalid argument: built without exact boxes
+            return None
+        self.ctx.check(r)
+        return out
+
+    def order_children(self, prim_aabbs, direct_layout: bool = False):
+        """CwBvh::order_children (src/cwbvh/mod.rs:520-524): prim_aabbs are the
+        primitives' boxes (n, 6), in primitive_indices order if direct_layout."""
+        pa, n, dev, keep = _prep(prim_aabbs, np.float32, 6)
+        self.ctx.check(self.ctx.lib.obvhs_cwbvh_order_children(self.ctx.h, self.h, pa, n, int(direct_layout), dev))
+        del keep
+
+    def order_node_children(self, prim_aabbs, node_index: int, direct_layout: bool = False):
+        """CwBvh::order_node_children (src/cwbvh/mod.rs:537-735) for one node."""
+        pa, n, dev, keep = _prep(prim_aabbs, np.float32, 6)
+        self.ctx.check(self.ctx.lib.obvhs_cwbvh_order_node_children(self.ctx.h, self.h, pa, n, int(node_index),
+                                                                    int(direct_layout), dev))
+        del keep
+
     def set_triangles(self, triangles):
         p, n, dev, keep = _prep(triangles, np.float32, 9)
         self.ctx.check(self.ctx.lib.obvhs_cwbvh_set_triangles(self.ctx.h, self.h, p, n, dev))
@@ -454,13 +479,15 @@ class CwBvh:
 
 def bvh2_to_cwbvh(bvh2: Bvh2, max_prims_per_leaf: int, order_children: bool,
                   include_exact_node_aabbs: bool = False) -> CwBvh:
-    if include_exact_node_aabbs:
-        raise NotImplementedError("exact node AABBs are not produced by this library")
+    """bvh2_to_cwbvh (src/cwbvh/bvh2_to_cwbvh.rs:490-510); with
+    include_exact_node_aabbs the result keeps each node's exact BVH2 box
+    (CwBvh.exact_node_aabbs)."""
     if not 1 <= max_prims_per_leaf <= 3:
         raise ValueError("max_prims_per_leaf must be 1..=3")
     ctx = bvh2.ctx
     h = ctypes.c_void_p()
-    ctx.check(ctx.lib.obvhs_bvh2_to_cwbvh(ctx.h, bvh2.h, max_prims_per_leaf, int(order_children), ctypes.byref(h)))
+    ctx.check(ctx.lib.obvhs_bvh2_to_cwbvh_ex(ctx.h, bvh2.h, max_prims_per_leaf, int(order_children),
+                                             int(bool(include_exact_node_aabbs)), ctypes.byref(h)))
     return CwBvh(ctx, h)
 
 

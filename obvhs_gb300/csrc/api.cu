@@ -758,6 +758,11 @@ int obvhs_split_thresholds(obvhs_ctx* cp, const float* triangles, uint32_t n, fl
 // ---- CWBVH -----------------------------------------------------------------
 
 int obvhs_bvh2_to_cwbvh(obvhs_ctx* cp, const obvhs_bvh2* b, uint32_t max_prims, int order_children, obvhs_cwbvh** out) {
+  return obvhs_bvh2_to_cwbvh_ex(cp, b, max_prims, order_children, 0, out);
+}
+
+int obvhs_bvh2_to_cwbvh_ex(obvhs_ctx* cp, const obvhs_bvh2* b, uint32_t max_prims, int order_children,
+                           int include_exact_node_aabbs, obvhs_cwbvh** out) {
   if (!cp || !b || !out) return OBVHS_ERR_INVALID_ARG;
   BuildCtx& c = *cp;
   DeviceGuard g(c.device);
@@ -767,7 +772,7 @@ int obvhs_bvh2_to_cwbvh(obvhs_ctx* cp, const obvhs_bvh2* b, uint32_t max_prims, 
   obvhs_cwbvh* cw = new obvhs_cwbvh();
   cw->ctx = &c;
   cw->uses_spatial_splits = b->uses_spatial_splits;
-  int r = cwbvh_convert_device(c, b, max_prims, order_children, cw);
+  int r = cwbvh_convert_device(c, b, max_prims, order_children, cw, nullptr, include_exact_node_aabbs != 0);
   if (!r) r = take_status(c);
   if (r) {
     obvhs_cwbvh_free(cw);
@@ -1071,12 +1076,53 @@ int obvhs_cwbvh_download_compressed(obvhs_ctx* cp, const obvhs_cwbvh* b, void* t
   return OBVHS_OK;
 }
 
+int obvhs_cwbvh_exact_node_aabbs(obvhs_ctx* cp, const obvhs_cwbvh* b, float* aabbs6) {
+  if (!cp || !b || (b->n_nodes && !aabbs6)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  if (b->n_nodes && !b->exact) return c.fail(OBVHS_ERR_INVALID_ARG, "built without exact node AABBs");
+  if (!b->n_nodes) return OBVHS_OK;
+  std::vector<float> raw((size_t)b->n_nodes * 8);
+  CK(cudaMemcpyAsync(raw.data(), b->exact, raw.size() * 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  for (size_t i = 0; i < b->n_nodes; i++) {
+    const float* r = &raw[8 * i];
+    float* o = aabbs6 + 6 * i;
+    o[0] = r[0], o[1] = r[1], o[2] = r[2], o[3] = r[4], o[4] = r[5], o[5] = r[6];
+  }
+  return OBVHS_OK;
+}
+
+static int order_children_common(obvhs_ctx* cp, obvhs_cwbvh* b, const float* prim_aabbs, uint32_t n_prims,
+                                 int direct_layout, int64_t node, int device_ptrs) {
+  if (!cp || !b || (n_prims && !prim_aabbs)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  int err = 0;
+  const float* dp = (const float*)stage_in(c, SLOT_INPUT, prim_aabbs, (size_t)n_prims * 24, device_ptrs, &err);
+  if (err) return err;
+  int r = cwbvh_order_children_device(c, b, dp, n_prims, direct_layout, node);
+  if (!r) r = take_status(c);
+  return r;
+}
+
+int obvhs_cwbvh_order_children(obvhs_ctx* cp, obvhs_cwbvh* b, const float* prim_aabbs, uint32_t n_prims,
+                               int direct_layout, int device_ptrs) {
+  return order_children_common(cp, b, prim_aabbs, n_prims, direct_layout, -1, device_ptrs);
+}
+
+int obvhs_cwbvh_order_node_children(obvhs_ctx* cp, obvhs_cwbvh* b, const float* prim_aabbs, uint32_t n_prims,
+                                    uint32_t node_index, int direct_layout, int device_ptrs) {
+  return order_children_common(cp, b, prim_aabbs, n_prims, direct_layout, node_index, device_ptrs);
+}
+
 int obvhs_cwbvh_free(obvhs_cwbvh* b) {
   if (!b) return OBVHS_OK;
   b->free_buf(b->nodes);
   b->free_buf(b->prim_indices);
   b->free_buf(b->tris);
   b->free_buf(b->ctris);
+  b->free_buf(b->exact);
   delete b;
   return OBVHS_OK;
 }

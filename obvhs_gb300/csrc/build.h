@@ -231,6 +231,7 @@ struct obvhs_cwbvh {
   float4* tris = nullptr;  // BVH order: (v0, id) (v0-v1, n.x) (v2-v0, n.y) (n.z), 64 B each
   uint32_t n_tris = 0;
   uint2* ctris = nullptr;  // BVH order: RtCompressedTriangle, 24 B each (three 8-byte words)
+  float4* exact = nullptr; // exact_node_aabbs: (min, max) per node, or null
   int uses_spatial_splits = 0;
   // A segmented build places all its trees in one allocation: buffers inside
   // [block_lo, block_hi) belong to it, and it is released with the last tree.
@@ -312,7 +313,12 @@ int reinsertion_seg_device(BuildCtx& c, Bvh2Node* nodes, const SegLayout& L, con
 // asynchronously; the caller compares it with out->n_nodes after its final
 // synchronisation and checks the status word.
 int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, int order_children, obvhs_cwbvh* out,
-                         uint32_t* emitted_deferred = nullptr);
+                         uint32_t* emitted_deferred = nullptr, bool exact_aabbs = false);
+// CwBvh::order_children (node < 0) or order_node_children(node) on the
+// device; prims6: the primitives' boxes (n_prims x 6 floats, device), in
+// original order or, with direct_layout, in primitive_indices order.
+int cwbvh_order_children_device(BuildCtx& c, obvhs_cwbvh* b, const float* prims6, uint32_t n_prims, int direct_layout,
+                                int64_t node);
 
 // Segmented conversion of every scene's BVH2 into its own CWBVH (outs[s]);
 // all outputs share one allocation.  h_tris / h_ntris (host array of device

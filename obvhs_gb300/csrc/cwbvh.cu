@@ -265,6 +265,7 @@ struct EmitOut {
   CwNode* cw;
   uint32_t* pidx;
   uint32_t max_nodes, max_prims;
+  float4* exact;  // include_exact_node_aabbs: the BVH2 box of every CWBVH node (min, max), or null
 };
 
 struct EmitArgs {
@@ -499,6 +500,9 @@ __device__ void emit_node(const EmitArgs& a, const Item it, int lane, uint8_t* s
     if (lane == 0) set_status(a.status, ST_CAPACITY);
   } else if (lane < 5) {
     o.cw[it.cw].q[lane] = reinterpret_cast<const uint4*>(stage)[lane];
+  } else if (lane < 7 && o.exact) {  // src/cwbvh/bvh2_to_cwbvh.rs:76-80
+    o.exact[2 * (size_t)it.cw + (lane - 5)] = lane == 5 ? make_float4(box.mn.x, box.mn.y, box.mn.z, 0.0f)
+                                                         : make_float4(box.mx.x, box.mx.y, box.mx.z, 0.0f);
   }
   __syncwarp();
 }
@@ -577,6 +581,248 @@ __global__ void k_seg_emit_init(const uint32_t* __restrict__ prim_start, const u
   ready[q] = 1;
 }
 
+// --- the order_children post-pass (src/cwbvh/mod.rs:520-735) ------------------
+//
+// The reference walks the nodes in index order; a node's reordering reads its
+// own record (placed by its parent's reordering) and its children's records
+// (untouched until then), and writes only its record and its child block.  So
+// any order that handles a parent before its children gives the same result:
+// a work queue seeded with the root, a warp per node, each node publishing
+// its inner children once they sit in their new slots.
+struct OrderArgs {
+  CwNode* nodes;
+  float4* exact;  // exact node boxes (2 per node), moved with their nodes; or null
+  const uint32_t* pidx;
+  const float* prims;  // n_prims x 6
+  uint32_t n_nodes, n_prims, n_pidx;
+  int direct;
+  uint32_t* items;
+  uint32_t* ready;
+  uint32_t* ctr;  // [0] head, [1] tail, [2] processed
+  uint32_t cap;   // nodes to process
+  int push;       // 0: the seeded node only (order_node_children)
+  uint32_t* status;
+};
+
+__device__ __forceinline__ float cw_ext(uint32_t e) { return __uint_as_float(e << 23); }
+
+__device__ void order_node(const OrderArgs& a, uint32_t ni, int lane, uint8_t* old, uint8_t* fresh, uint4* kids,
+                           float4* kex) {
+  if (lane < 5) reinterpret_cast<uint4*>(old)[lane] = __ldcg(reinterpret_cast<const uint4*>(&a.nodes[ni]) + lane);
+  __syncwarp();
+  const float* pf = reinterpret_cast<const float*>(old);
+  const float3 p = make_float3(pf[0], pf[1], pf[2]);
+  const float3 e = make_float3(cw_ext(old[12]), cw_ext(old[13]), cw_ext(old[14]));
+  const uint32_t imask = old[15];
+  const uint32_t base = reinterpret_cast<const uint32_t*>(old)[4];
+  const uint32_t pbase = reinterpret_cast<const uint32_t*>(old)[5];
+  // center of CwBvhNode::aabb(): (p + e * 255 + p) * 0.5
+  const float3 pc = make_float3(((p.x + e.x * 255.0f) + p.x) * 0.5f, ((p.y + e.y * 255.0f) + p.y) * 0.5f,
+                                ((p.z + e.z * 255.0f) + p.z) * 0.5f);
+  // lane ch < 8: child ch's center minus the node's
+  bool present = false, bad = false;
+  float3 v = make_float3(0.0f, 0.0f, 0.0f);
+  uint32_t my_child = OBVHS_INVALID;  // inner child: its node index before the move
+  if (lane < 8) {
+    const uint32_t meta = old[24 + lane];
+    present = meta != 0;
+    if (present) {
+      Box b;
+      if (!((imask >> lane) & 1u)) {
+        b = Box{make_float3(3.40282347e+38f, 3.40282347e+38f, 3.40282347e+38f),
+                make_float3(-3.40282347e+38f, -3.40282347e+38f, -3.40282347e+38f)};
+        const uint32_t start = pbase + (meta & 31u), cnt = __popc(meta & 0xe0u);
+        for (uint32_t i = 0; i < cnt; i++) {
+          uint32_t pi = start + i;
+          if (!a.direct) {
+            if (pi >= a.n_pidx) {
+              bad = true;
+              break;
+            }
+            pi = a.pidx[pi];
+          }
+          if (pi >= a.n_prims) {
+            bad = true;
+            break;
+          }
+          const float* q = a.prims + (size_t)pi * 6;
+          b = box_union(b, Box{make_float3(q[0], q[1], q[2]), make_float3(q[3], q[4], q[5])});
+        }
+      } else {
+        const uint32_t slot = (meta & 31u) - 24u;
+        const uint32_t k = base + __popc(imask & ~(0xffffffffu << slot));
+        if (slot > 7u || k >= a.n_nodes) {
+          bad = true;
+        } else {
+          my_child = k;
+          if (a.exact) {
+            const float4 lo = __ldcg(&a.exact[2 * (size_t)k]), hi = __ldcg(&a.exact[2 * (size_t)k + 1]);
+            b = Box{make_float3(lo.x, lo.y, lo.z), make_float3(hi.x, hi.y, hi.z)};
+          } else {
+            const uint4 w = __ldcg(reinterpret_cast<const uint4*>(&a.nodes[k]));
+            const float3 cp = make_float3(__uint_as_float(w.x), __uint_as_float(w.y), __uint_as_float(w.z));
+            const float3 ce = make_float3(cw_ext(w.w & 0xffu), cw_ext((w.w >> 8) & 0xffu), cw_ext((w.w >> 16) & 0xffu));
+            b = Box{cp, make_float3(cp.x + ce.x * 255.0f, cp.y + ce.y * 255.0f, cp.z + ce.z * 255.0f)};
+          }
+        }
+      }
+      const float3 cc = make_float3((b.mx.x + b.mn.x) * 0.5f, (b.mx.y + b.mn.y) * 0.5f, (b.mx.z + b.mn.z) * 0.5f);
+      v = make_float3(cc.x - pc.x, cc.y - pc.y, cc.z - pc.z);
+    }
+  }
+  if (__any_sync(0xffffffffu, bad)) {
+    if (lane == 0) set_status(a.status, ST_BAD_TREE);
+    return;
+  }
+  const uint32_t pmask = __ballot_sync(0xffffffffu, present) & 0xffu;
+  // costs of (child c, direction s) at idx = 8c + s, two per lane; greedy
+  // assignment takes the smallest cost below f32::MAX, first in (c, s) order
+  float cost[2];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int idx = lane + 32 * h;
+    const int c = idx >> 3, s = idx & 7;
+    const float vx = __shfl_sync(0xffffffffu, v.x, c), vy = __shfl_sync(0xffffffffu, v.y, c),
+                vz = __shfl_sync(0xffffffffu, v.z, c);
+    cost[h] = 3.40282347e+38f;
+    if ((pmask >> c) & 1u) {
+      const float dx = (s & 4) ? -1.0f : 1.0f, dy = (s & 2) ? -1.0f : 1.0f, dz = (s & 1) ? -1.0f : 1.0f;
+      cost[h] = (dx * vx + dy * vy) + dz * vz;
+    }
+  }
+  uint32_t assigned = 0, filled = 0, assign = 0;
+  for (int iter = 0; iter < 8; iter++) {
+    float bc = 3.40282347e+38f;
+    uint32_t bi = 0xffffffffu;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const uint32_t idx = lane + 32 * h;
+      const int c = idx >> 3, s = idx & 7;
+      if (((pmask >> c) & 1u) && !((assigned >> c) & 1u) && !((filled >> s) & 1u) && cost[h] < bc) {
+        bc = cost[h];
+        bi = idx;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oc = __shfl_xor_sync(0xffffffffu, bc, o);
+      const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (oi != 0xffffffffu && (bi == 0xffffffffu || oc < bc || (oc == bc && oi < bi))) {
+        bc = oc;
+        bi = oi;
+      }
+    }
+    if (bi == 0xffffffffu) break;
+    const int c = bi >> 3, s = bi & 7;
+    assigned |= 1u << c;
+    filled |= 1u << s;
+    assign |= (uint32_t)s << (3 * c);
+  }
+  if (assigned != pmask) {  // the reference asserts
+    if (lane == 0) set_status(a.status, ST_BAD_INPUT);
+    return;
+  }
+  // the new record: a copy of the old one, metas cleared, each child's meta
+  // and quantised box in its new slot
+  if (lane < 20) reinterpret_cast<uint32_t*>(fresh)[lane] = reinterpret_cast<const uint32_t*>(old)[lane];
+  __syncwarp();
+  if (lane < 8) fresh[24 + lane] = 0;
+  __syncwarp();
+  uint32_t new_imask = 0;
+#pragma unroll
+  for (int c = 0; c < 8; c++)
+    if (((pmask >> c) & 1u) && ((imask >> c) & 1u)) new_imask |= 1u << ((assign >> (3 * c)) & 7u);
+  if (lane < 8 && present) {
+    const uint32_t q = (assign >> (3 * lane)) & 7u;
+    const bool inner = (imask >> lane) & 1u;
+    fresh[24 + q] = inner ? (uint8_t)((24 + q) | 0x20) : old[24 + lane];
+    fresh[32 + q] = old[32 + lane];
+    fresh[40 + q] = old[40 + lane];
+    fresh[48 + q] = old[48 + lane];
+    fresh[56 + q] = old[56 + lane];
+    fresh[64 + q] = old[64 + lane];
+    fresh[72 + q] = old[72 + lane];
+  }
+  if (lane == 0) fresh[15] = (uint8_t)new_imask;
+  // the inner children's records (and exact boxes) move to their new slots
+  const uint32_t n_inner = __popc(imask & pmask);
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const uint32_t k = __shfl_sync(0xffffffffu, my_child, c);
+    if (k == OBVHS_INVALID) continue;
+    if (lane < 5) kids[c * 5 + lane] = __ldcg(reinterpret_cast<const uint4*>(&a.nodes[k]) + lane);
+    if (a.exact && lane >= 5 && lane < 7) kex[c * 2 + (lane - 5)] = __ldcg(&a.exact[2 * (size_t)k + (lane - 5)]);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const uint32_t k = __shfl_sync(0xffffffffu, my_child, c);
+    if (k == OBVHS_INVALID) continue;
+    const uint32_t q = (assign >> (3 * c)) & 7u;
+    const uint32_t nk = base + __popc(new_imask & ((1u << q) - 1u));
+    if (lane < 5) a.nodes[nk].q[lane] = kids[c * 5 + lane];
+    if (a.exact && lane >= 5 && lane < 7) a.exact[2 * (size_t)nk + (lane - 5)] = kex[c * 2 + (lane - 5)];
+  }
+  if (lane < 5) a.nodes[ni].q[lane] = reinterpret_cast<const uint4*>(fresh)[lane];
+  // every lane's stores are visible device-wide before any lane publishes
+  __threadfence();
+  __syncwarp();
+  if (!a.push || n_inner == 0) return;
+  // publish the children in their new slots
+  uint32_t at = 0;
+  if (lane == 0) at = atomicAdd(&a.ctr[1], n_inner);
+  at = __shfl_sync(0xffffffffu, at, 0);
+  if (lane < (int)n_inner) {
+    if (at + lane < a.cap) {
+      a.items[at + lane] = base + lane;
+      __threadfence();
+      atomicExch(&a.ready[at + lane], 1u);
+    } else {
+      set_status(a.status, ST_CAPACITY);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(EMIT_THREADS) k_order_children(OrderArgs a) {
+  __shared__ __align__(16) uint8_t old_s[EMIT_THREADS / 32][80];
+  __shared__ __align__(16) uint8_t new_s[EMIT_THREADS / 32][80];
+  __shared__ uint4 kids_s[EMIT_THREADS / 32][8 * 5];
+  __shared__ float4 kex_s[EMIT_THREADS / 32][16];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t mine = 0;
+  for (;;) {
+    uint32_t k = 0;
+    if (lane == 0) k = atomicAdd(&a.ctr[0], 1u);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= a.cap) break;
+    uint32_t ok = 1;
+    if (lane == 0) {
+      uint32_t spins = 0, ns = 32;
+      while (*(volatile uint32_t*)&a.ready[k] == 0) {
+        // a node that failed publishes nothing: stop instead of waiting out the bound
+        if (++spins > (1u << 22) || ((spins & 63u) == 0 && *(volatile uint32_t*)a.status)) {
+          set_status(a.status, ST_ITER_LIMIT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(ns);
+        if (ns < 2048) ns <<= 1;
+      }
+      __threadfence();
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (!ok) break;
+    const uint32_t ni = __ldcg(&a.items[k]);
+    if (ni >= a.n_nodes) {
+      if (lane == 0) set_status(a.status, ST_BAD_TREE);
+      break;
+    }
+    order_node(a, ni, lane, old_s[w], new_s[w], kids_s[w], kex_s[w]);
+    mine++;
+  }
+  if (lane == 0 && mine) atomicAdd(&a.ctr[2], mine);
+}
+
 }  // namespace
 
 // For each float exponent field e (1..254) the smallest mantissa m >= 1 with
@@ -606,7 +852,7 @@ static const uint32_t* ceil_log2_thresholds() {
 }
 
 int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, int order_children, obvhs_cwbvh* out,
-                         uint32_t* emitted_deferred) {
+                         uint32_t* emitted_deferred, bool exact_aabbs) {
   out->n_nodes = 0;
   out->n_prims = 0;
   const uint32_t n = b->n_nodes;
@@ -637,11 +883,14 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   const uint32_t n_pr = root.nprim;
   CwNode* cwn = nullptr;
   uint32_t* cwp = nullptr;
+  float4* exn = nullptr;
   // stream-ordered allocations: no device-wide synchronisation
   if (cudaMallocAsync(&cwn, (size_t)n_cw * sizeof(CwNode), c.stream) != cudaSuccess ||
-      cudaMallocAsync(&cwp, (size_t)std::max(n_pr, 1u) * 4, c.stream) != cudaSuccess) {
+      cudaMallocAsync(&cwp, (size_t)std::max(n_pr, 1u) * 4, c.stream) != cudaSuccess ||
+      (exact_aabbs && cudaMallocAsync(&exn, (size_t)n_cw * 32, c.stream) != cudaSuccess)) {
     cudaGetLastError();
     if (cwn) cudaFree(cwn);
+    if (cwp) cudaFree(cwp);
     return c.fail(OBVHS_ERR_OOM, "cwbvh output");
   }
   Item* items = (Item*)s.get(SLOT_FRONTIER_A, (size_t)n_cw * sizeof(Item));
@@ -674,7 +923,7 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   CK(cudaMemcpyAsync(ready, hst + 4, 4, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(counters + 12, hst + 5, 12, cudaMemcpyHostToDevice, c.stream));
   EmitArgs ea{{},     b->nodes,      b->prim_indices, dec, items, ready, counters + 12, counters + 13, order_children,
-              n_cw,   EmitOut{cwn, cwp, n_cw, n_pr}, nullptr, nullptr, 0, c.d_status, counters + 14};
+              n_cw,   EmitOut{cwn, cwp, n_cw, n_pr, exn}, nullptr, nullptr, 0, c.d_status, counters + 14};
   std::memcpy(ea.log2_thr, ceil_log2_thresholds(), sizeof(ea.log2_thr));
   const uint32_t grid = (uint32_t)std::min<uint64_t>(
       emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)n_cw * 32, EMIT_THREADS)));
@@ -684,6 +933,7 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   out->n_nodes = n_cw;
   out->prim_indices = cwp;
   out->n_prims = n_pr;
+  out->exact = exn;
   if (emitted_deferred) {
     CK(cudaMemcpyAsync(emitted_deferred, counters + 14, 4, cudaMemcpyDeviceToHost, c.stream));
     return 0;
@@ -695,8 +945,10 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   if (*c.h_status || emitted != n_cw) {
     cudaFree(cwn);
     cudaFree(cwp);
+    if (exn) cudaFree(exn);
     out->nodes = nullptr;
     out->prim_indices = nullptr;
+    out->exact = nullptr;
     out->n_nodes = out->n_prims = 0;
     return c.fail(OBVHS_ERR_BAD_INPUT, "CWBVH emission failed (status " + std::to_string(*c.h_status) + ")");
   }
@@ -789,7 +1041,7 @@ int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in
     o->block = block;
     o->block_lo = blk;
     o->block_hi = blk + total;
-    eo[s] = EmitOut{nullptr, nullptr, 0, 0};
+    eo[s] = EmitOut{nullptr, nullptr, 0, 0, nullptr};
     slots[s] = n_roots;
     slots[S + s] = pr_acc;
     pr_acc += n_pr[s];
@@ -805,7 +1057,7 @@ int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in
     o->total_aabb[3] = hr[s].box[4];
     o->total_aabb[4] = hr[s].box[5];
     o->total_aabb[5] = hr[s].box[6];
-    eo[s] = EmitOut{o->nodes, o->prim_indices, n_cw[s], n_pr[s]};
+    eo[s] = EmitOut{o->nodes, o->prim_indices, n_cw[s], n_pr[s], nullptr};
     if (h_tris && n_pr[s]) {
       o->tris = reinterpret_cast<float4*>(blk + off[3 * s + 2]);
       jobs[s] = SegTriJob{h_tris[s], h_ntris[s], o->prim_indices, o->tris};
@@ -832,7 +1084,7 @@ int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in
   KLAUNCH("k_seg_emit_init", k_seg_emit_init<<<div_up<uint32_t>(S, BLK), BLK, 0, c.stream>>>(
                                  L.d_prim_start, L.d_node_start, d_slots, S, n_roots, items, ready, counters + 12));
   EmitArgs ea{{},      nodes,     pidx_in,         dec,      items,      ready, counters + 12, counters + 13,
-              order_children, q_total, EmitOut{nullptr, nullptr, 0, 0}, d_eo, L.d_node_start, S, c.d_status,
+              order_children, q_total, EmitOut{nullptr, nullptr, 0, 0, nullptr}, d_eo, L.d_node_start, S, c.d_status,
               counters + 14};
   std::memcpy(ea.log2_thr, ceil_log2_thresholds(), sizeof(ea.log2_thr));
   const uint32_t grid = (uint32_t)std::min<uint64_t>(
@@ -847,5 +1099,49 @@ int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in
     r = reorder_tris_seg_device(c, d_jobs, d_slots + S, S, pr_total);
     if (r) return r;
   }
+  return 0;
+}
+
+int cwbvh_order_children_device(BuildCtx& c, obvhs_cwbvh* b, const float* prims6, uint32_t n_prims, int direct_layout,
+                                int64_t node) {
+  const uint32_t n = b->n_nodes;
+  if (n == 0) return 0;
+  if (node >= (int64_t)n) return c.fail(OBVHS_ERR_INVALID_ARG, "node index out of range");
+  const uint32_t cap = node < 0 ? n : 1;
+  Scratch& s = c.scratch;
+  uint32_t* items = (uint32_t*)s.get(SLOT_FRONTIER_A, (size_t)cap * 4);
+  uint32_t* ready = (uint32_t*)s.get(SLOT_FRONTIER_B, (size_t)cap * 4);
+  uint32_t* ctr = (uint32_t*)s.get(SLOT_CW_COUNTERS, 64);
+  if (!items || !ready || !ctr) return c.fail(OBVHS_ERR_OOM, "scratch");
+  // queue: item 0 = the root (or the one node), published; head 0, tail 1
+  uint32_t* h = (uint32_t*)c.h_small;
+  h[0] = node < 0 ? 0u : (uint32_t)node;
+  h[1] = 1;  // ready[0]
+  h[2] = 0;  // head
+  h[3] = 1;  // tail
+  h[4] = 0;  // processed
+  CK(cudaMemsetAsync(ready, 0, (size_t)cap * 4, c.stream));
+  CK(cudaMemcpyAsync(items, h, 4, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaMemcpyAsync(ready, h + 1, 4, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaMemcpyAsync(ctr, h + 2, 12, cudaMemcpyHostToDevice, c.stream));
+  static std::atomic<int> blocks_s{0};
+  int blocks = blocks_s.load();
+  if (!blocks) {
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_order_children, EMIT_THREADS, 0));
+    blocks = std::max(1, per_sm) * c.num_sms;
+    blocks_s.store(blocks);
+  }
+  OrderArgs oa{b->nodes, b->exact, b->prim_indices, prims6, n, n_prims, b->n_prims, direct_layout, items, ready, ctr,
+               cap, node < 0 ? 1 : 0, c.d_status};
+  const uint32_t grid =
+      (uint32_t)std::min<uint64_t>(blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)cap * 32, EMIT_THREADS)));
+  KLAUNCH("k_order_children", k_order_children<<<grid, EMIT_THREADS, 0, c.stream>>>(oa));
+  CK(cudaGetLastError());
+  uint32_t processed = 0;
+  CK(cudaMemcpyAsync(&processed, ctr + 2, 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(c.h_status, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  if (!*c.h_status && processed != cap) return c.fail(OBVHS_ERR_BAD_INPUT, "order_children did not reach every node");
   return 0;
 }

@@ -776,6 +776,7 @@ struct Converter {
   bool order;
   V3 lut[8];
   int err = 0;
+  std::vector<Aabb>* exact = nullptr;  // include_exact_node_aabbs: BVH2 box per CWBVH node
 
   Converter(const Bvh2& bvh, bool order_children) : b(bvh), order(order_children) {
     nodes.push_back(CwNode{});
@@ -959,6 +960,7 @@ struct Converter {
   void convert(uint32_t i8, uint32_t i2) {
     CwNode node = nodes[i8];
     const Aabb& box = b.nodes[i2].box;
+    if (exact) (*exact)[i8] = box;  // src/cwbvh/bvh2_to_cwbvh.rs:76-80
     V3 np = box.mn;
     node.p[0] = np.x;
     node.p[1] = np.y;
@@ -1031,17 +1033,154 @@ struct Converter {
 };
 
 int bvh2_to_cwbvh(const Bvh2& bvh, uint32_t max_prims, bool order_children, std::vector<CwNode>& out_nodes,
-                  std::vector<uint32_t>& out_prims) {
+                  std::vector<uint32_t>& out_prims, std::vector<Aabb>* exact = nullptr) {
   out_nodes.clear();
   out_prims.clear();
+  if (exact) exact->assign(bvh.nodes.size(), aabb_empty());  // the reference sizes it by the BVH2
   if (bvh.nodes.empty()) return 0;
   Converter cv(bvh, order_children);
+  cv.exact = exact;
   cv.calculate_cost(max_prims);
   if (cv.err) return -10 - cv.err;
   cv.convert(0, 0);
   if (cv.err) return -10 - cv.err;
   out_nodes.swap(cv.nodes);
   out_prims.swap(cv.prims);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// CwBvh::order_children / order_node_children (src/cwbvh/mod.rs:520-735): the
+// post-pass that re-sorts each node's children by octant, from the children's
+// compressed (or exact) boxes, moving the child node records (and exact
+// boxes) within the node's child block.
+inline float cw_extent(uint8_t e) {
+  uint32_t b = (uint32_t)e << 23;
+  float f;
+  std::memcpy(&f, &b, 4);
+  return f;
+}
+inline Aabb cw_node_aabb(const CwNode& n) {  // CwBvhNode::aabb (node.rs:261-265)
+  V3 p = v3(n.p[0], n.p[1], n.p[2]);
+  V3 e = v3(cw_extent(n.e[0]), cw_extent(n.e[1]), cw_extent(n.e[2]));
+  return Aabb{p, p + e * 255.0f};
+}
+inline bool cw_is_leaf(const CwNode& n, int ch) { return (n.imask & (1u << ch)) == 0; }
+inline uint32_t cw_child_node_index(const CwNode& n, int ch) {  // node.rs:299-304
+  uint32_t slot = (uint32_t)(n.child_meta[ch] & 0x1f) - 24;
+  uint32_t rel = (uint32_t)__builtin_popcount((uint32_t)n.imask & ~(0xffffffffu << slot));
+  return n.child_base_idx + rel;
+}
+
+int cw_order_node_children(std::vector<CwNode>& nodes, std::vector<Aabb>* exact, const std::vector<uint32_t>& pidx,
+                           const Aabb* prims, size_t n_prims, bool direct, size_t node_index) {
+  const CwNode old = nodes[node_index];
+  const V3 c = center(cw_node_aabb(old));
+  float cost[8][8];
+  for (int a = 0; a < 8; a++)
+    for (int b = 0; b < 8; b++) cost[a][b] = F32_MAX;
+  int inner_count = 0;
+  for (int ch = 0; ch < 8; ch++)
+    if (old.child_meta[ch] != 0 && !cw_is_leaf(old, ch)) inner_count++;
+  V3 cc[8];
+  for (int ch = 0; ch < 8; ch++) {
+    cc[ch] = v3(0, 0, 0);
+    if (old.child_meta[ch] == 0) continue;
+    if (cw_is_leaf(old, ch)) {
+      uint32_t start = old.primitive_base_idx + (old.child_meta[ch] & 0x1f);
+      uint32_t count = (uint32_t)__builtin_popcount(old.child_meta[ch] & 0xe0);
+      Aabb box = aabb_empty();
+      for (uint32_t i = 0; i < count; i++) {
+        size_t pi = start + i;
+        if (!direct) {
+          if (pi >= pidx.size()) return -1;
+          pi = pidx[pi];
+        }
+        if (pi >= n_prims) return -1;
+        box = uni(box, prims[pi]);
+      }
+      cc[ch] = center(box);
+    } else {
+      uint32_t k = cw_child_node_index(old, ch);
+      if (k >= nodes.size()) return -2;
+      cc[ch] = center(exact ? (*exact)[k] : cw_node_aabb(nodes[k]));
+    }
+  }
+  for (int s = 0; s < 8; s++) {
+    V3 d = v3((s & 4) ? -1.0f : 1.0f, (s & 2) ? -1.0f : 1.0f, (s & 1) ? -1.0f : 1.0f);
+    for (int ch = 0; ch < 8; ch++) {
+      if (old.child_meta[ch] == 0) continue;
+      cost[ch][s] = dot(d, cc[ch] - c);
+    }
+  }
+  int assign[8];
+  bool filled[8];
+  for (int i = 0; i < 8; i++) {
+    assign[i] = -1;
+    filled[i] = false;
+  }
+  for (;;) {
+    float mc = F32_MAX;
+    int ms = -1, mi = -1;
+    for (int ch = 0; ch < 8; ch++) {
+      if (old.child_meta[ch] == 0 || assign[ch] != -1) continue;
+      for (int s = 0; s < 8; s++)
+        if (!filled[s] && cost[ch][s] < mc) {
+          mc = cost[ch][s];
+          ms = s;
+          mi = ch;
+        }
+    }
+    if (ms < 0) break;
+    filled[ms] = true;
+    assign[mi] = ms;
+  }
+  CwNode nn = old;
+  nn.imask = 0;
+  for (int ch = 0; ch < 8; ch++) nn.child_meta[ch] = 0;
+  for (int ch = 0; ch < 8; ch++) {
+    if (old.child_meta[ch] == 0) continue;
+    int q = assign[ch];
+    if (q < 0) return -3;  // the reference asserts
+    if (cw_is_leaf(old, ch)) {
+      nn.child_meta[q] = old.child_meta[ch];
+    } else {
+      nn.imask |= (uint8_t)(1u << q);
+      nn.child_meta[q] = (uint8_t)((24 + q) | 0x20);
+    }
+    nn.child_min_x[q] = old.child_min_x[ch];
+    nn.child_max_x[q] = old.child_max_x[ch];
+    nn.child_min_y[q] = old.child_min_y[ch];
+    nn.child_max_y[q] = old.child_max_y[ch];
+    nn.child_min_z[q] = old.child_min_z[ch];
+    nn.child_max_z[q] = old.child_max_z[ch];
+  }
+  if (inner_count) {
+    CwNode moved[8];
+    Aabb moved_exact[8];
+    for (int ch = 0; ch < 8; ch++) {
+      if (old.child_meta[ch] == 0 || cw_is_leaf(old, ch)) continue;
+      uint32_t k = cw_child_node_index(old, ch);
+      moved[ch] = nodes[k];
+      if (exact) moved_exact[ch] = (*exact)[k];
+    }
+    for (int ch = 0; ch < 8; ch++) {
+      if (old.child_meta[ch] == 0 || cw_is_leaf(old, ch)) continue;
+      uint32_t k = cw_child_node_index(nn, assign[ch]);
+      nodes[k] = moved[ch];
+      if (exact) (*exact)[k] = moved_exact[ch];
+    }
+  }
+  nodes[node_index] = nn;
+  return 0;
+}
+
+int cw_order_children(std::vector<CwNode>& nodes, std::vector<Aabb>* exact, const std::vector<uint32_t>& pidx,
+                      const Aabb* prims, size_t n_prims, bool direct) {
+  for (size_t i = 0; i < nodes.size(); i++) {
+    int r = cw_order_node_children(nodes, exact, pidx, prims, n_prims, direct, i);
+    if (r) return r;
+  }
   return 0;
 }
 
@@ -1518,6 +1657,56 @@ int32_t orc_bvh2_to_cwbvh(const void* nodes32, uint64_t n_nodes, const uint32_t*
   std::memcpy(out_pidx, cp.data(), cp.size() * 4);
   counts[0] = cn.size();
   counts[1] = cp.size();
+  return 0;
+}
+
+// bvh2_to_cwbvh with include_exact_node_aabbs: out_exact6 gets the first
+// counts[0] entries (min xyz, max xyz) of exact_node_aabbs.
+int32_t orc_bvh2_to_cwbvh_exact(const void* nodes32, uint64_t n_nodes, const uint32_t* pidx, uint64_t n_pidx,
+                                uint32_t max_prims, int32_t order_children, void* out_nodes80, uint32_t* out_pidx,
+                                float* out_exact6, uint64_t* counts) {
+  Bvh2 b = load_bvh2(nodes32, n_nodes, pidx, n_pidx, 96);
+  std::vector<CwNode> cn;
+  std::vector<uint32_t> cp;
+  std::vector<Aabb> ex;
+  int r = bvh2_to_cwbvh(b, max_prims, order_children != 0, cn, cp, &ex);
+  if (r) return r;
+  std::memcpy(out_nodes80, cn.data(), cn.size() * 80);
+  std::memcpy(out_pidx, cp.data(), cp.size() * 4);
+  for (size_t i = 0; i < cn.size(); i++) {
+    const Aabb& a = ex[i];
+    float* o = out_exact6 + 6 * i;
+    o[0] = a.mn.x; o[1] = a.mn.y; o[2] = a.mn.z;
+    o[3] = a.mx.x; o[4] = a.mx.y; o[5] = a.mx.z;
+  }
+  counts[0] = cn.size();
+  counts[1] = cp.size();
+  return 0;
+}
+
+// CwBvh::order_children (node_index < 0) or order_node_children(node_index),
+// in place; exact6 (n_nodes x 6, or NULL) is used and permuted alongside.
+int32_t orc_cwbvh_order_children(void* nodes80, uint64_t n_nodes, const uint32_t* pidx, uint64_t n_pidx,
+                                 float* exact6, const float* prim_aabbs6, uint64_t n_prims, int32_t direct_layout,
+                                 int64_t node_index) {
+  std::vector<CwNode> nodes(n_nodes);
+  std::memcpy(nodes.data(), nodes80, n_nodes * 80);
+  std::vector<uint32_t> pi(pidx, pidx + n_pidx);
+  std::vector<Aabb> prims = load_aabbs(prim_aabbs6, n_prims);
+  std::vector<Aabb> ex;
+  if (exact6) ex = load_aabbs(exact6, n_nodes);
+  int r = node_index < 0
+              ? cw_order_children(nodes, exact6 ? &ex : nullptr, pi, prims.data(), prims.size(), direct_layout != 0)
+              : cw_order_node_children(nodes, exact6 ? &ex : nullptr, pi, prims.data(), prims.size(),
+                                       direct_layout != 0, (size_t)node_index);
+  if (r) return r;
+  std::memcpy(nodes80, nodes.data(), n_nodes * 80);
+  if (exact6)
+    for (size_t i = 0; i < n_nodes; i++) {
+      float* o = exact6 + 6 * i;
+      o[0] = ex[i].mn.x; o[1] = ex[i].mn.y; o[2] = ex[i].mn.z;
+      o[3] = ex[i].mx.x; o[4] = ex[i].mx.y; o[5] = ex[i].mx.z;
+    }
   return 0;
 }
 

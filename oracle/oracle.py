@@ -76,6 +76,10 @@ def _declare(L):
     L.orc_reinsertion.restype = I32
     L.orc_bvh2_to_cwbvh.argtypes = [P, U64, P, U64, U32, I32, P, P, P]
     L.orc_bvh2_to_cwbvh.restype = I32
+    L.orc_bvh2_to_cwbvh_exact.argtypes = [P, U64, P, U64, U32, I32, P, P, P, P]
+    L.orc_bvh2_to_cwbvh_exact.restype = I32
+    L.orc_cwbvh_order_children.argtypes = [P, U64, P, U64, P, P, U64, I32, ctypes.c_int64]
+    L.orc_cwbvh_order_children.restype = I32
     L.orc_presplit.argtypes = [P, U64]
     L.orc_presplit.restype = P
     L.orc_presplit_count.argtypes = [P]
@@ -168,6 +172,37 @@ def bvh2_to_cwbvh(nodes, pidx, max_prims_per_leaf=3, order_children=True):
     if r != 0:
         raise RuntimeError(f"oracle bvh2_to_cwbvh failed: {r}")
     return out_n[: int(counts[0])].copy(), out_p[: int(counts[1])].copy()
+
+
+def bvh2_to_cwbvh_exact(nodes, pidx, max_prims_per_leaf=3, order_children=True):
+    """bvh2_to_cwbvh with include_exact_node_aabbs: (nodes80, primitive
+    indices, exact AABB (min xyz, max xyz) per CWBVH node)."""
+    nodes = np.ascontiguousarray(nodes, dtype=np.uint8).reshape(-1, 32)
+    pidx = np.ascontiguousarray(pidx, dtype=np.uint32)
+    out_n = np.zeros((max(len(nodes), 1), 80), np.uint8)
+    out_p = np.zeros(max(len(pidx), 1), np.uint32)
+    out_e = np.zeros((max(len(nodes), 1), 6), np.float32)
+    counts = np.zeros(2, np.uint64)
+    r = lib().orc_bvh2_to_cwbvh_exact(_p(nodes), len(nodes), _p(pidx), len(pidx), max_prims_per_leaf,
+                                      int(order_children), _p(out_n), _p(out_p), _p(out_e), _p(counts))
+    if r != 0:
+        raise RuntimeError(f"oracle bvh2_to_cwbvh failed: {r}")
+    k = int(counts[0])
+    return out_n[:k].copy(), out_p[: int(counts[1])].copy(), out_e[:k].copy()
+
+
+def cwbvh_order_children(nodes80, pidx, prim_aabbs, direct_layout=False, exact=None, node_index=-1):
+    """CwBvh::order_children (node_index < 0) or order_node_children: returns
+    the reordered nodes (and exact boxes when given)."""
+    nodes = np.ascontiguousarray(nodes80, dtype=np.uint8).reshape(-1, 80).copy()
+    pidx = np.ascontiguousarray(pidx, dtype=np.uint32)
+    prims = _f32(prim_aabbs, 6)
+    ex = None if exact is None else np.ascontiguousarray(exact, dtype=np.float32).reshape(-1, 6).copy()
+    r = lib().orc_cwbvh_order_children(_p(nodes), len(nodes), _p(pidx), len(pidx), _p(ex) if ex is not None else None,
+                                       _p(prims), len(prims), int(direct_layout), int(node_index))
+    if r != 0:
+        raise RuntimeError(f"oracle order_children failed: {r}")
+    return nodes if ex is None else (nodes, ex)
 
 
 def presplit(tris):

@@ -259,3 +259,79 @@ def test_device_pointer_path(G):
     out = cw.ray_traverse(dr).cpu().numpy().view(np.uint32)
     ids, t = cw.ray_traverse(rays)
     assert _eq(out[:, 0], ids) and _eq(out[:, 1], t.view(np.uint32))
+
+
+# --- CWBVH post-passes -----------------------------------------------------------
+
+
+def _demoscene_bvh2(G, preset="very_fast"):
+    """tests/mod.rs:351-451 set-up: demoscene(100, 0) boxes, the preset's PLOC."""
+    tris = T.demoscene(100, 0)
+    aabbs = T.tri_aabbs(tris)
+    p = PRESETS[preset]()
+    b2 = G.PlocBuilder().build_ploc(int(p.ploc_search_distance), aabbs, None, int(p.sort_precision),
+                                    int(p.search_depth_threshold))
+    return tris, aabbs, b2
+
+
+@pytest.mark.parametrize("order", [True, False])
+def test_exact_node_aabbs_match_oracle(G, order):
+    tris, aabbs, b2 = _demoscene_bvh2(G)
+    nodes, pidx = b2.download()
+    cw = G.bvh2_to_cwbvh(b2, 3, order, include_exact_node_aabbs=True)
+    on, op, oe = O.bvh2_to_cwbvh_exact(nodes, pidx, 3, order)
+    gn, gp = cw.download()
+    assert gn.tobytes() == on.tobytes() and gp.tobytes() == op.tobytes()
+    assert cw.exact_node_aabbs().tobytes() == oe.tobytes()
+    assert G.bvh2_to_cwbvh(b2, 3, order).exact_node_aabbs() is None
+
+
+@pytest.mark.parametrize("preset,order,exact,direct", [("very_fast", True, False, False),
+                                                       ("very_fast", False, False, False),
+                                                       ("very_fast", True, True, False),
+                                                       ("medium", True, False, True),
+                                                       ("slow", False, True, True)])
+def test_order_children_post_pass_matches_oracle(G, preset, order, exact, direct):
+    """CwBvh::order_children on the GPU, twice (the second pass starts from
+    the reordered tree), against the oracle's sequential pass, node bytes and
+    exact boxes bit for bit."""
+    tris, aabbs, b2 = _demoscene_bvh2(G, preset)
+    nodes, pidx = b2.download()
+    cw = G.bvh2_to_cwbvh(b2, 3, order, include_exact_node_aabbs=exact)
+    cn, cp = cw.download()
+    prims = aabbs[cp] if direct else aabbs  # direct layout: boxes in primitive_indices order
+    ex = cw.exact_node_aabbs() if exact else None
+    for _ in range(2):
+        cw.order_children(prims, direct_layout=direct)
+        r = O.cwbvh_order_children(cn, cp, prims, direct_layout=direct, exact=ex)
+        cn, ex = (r if exact else (r, None))
+        gn, gp = cw.download()
+        assert gn.tobytes() == cn.tobytes()
+        assert gp.tobytes() == cp.tobytes()
+        if exact:
+            assert cw.exact_node_aabbs().tobytes() == ex.tobytes()
+        assert O.validate_cwbvh(gn, gp, aabbs)[0] == 0
+
+
+def test_order_node_children_one_at_a_time(G):
+    tris, aabbs, b2 = _demoscene_bvh2(G)
+    cw = G.bvh2_to_cwbvh(b2, 3, True)
+    cn, cp = cw.download()
+    for i in (0, 1, 7, len(cn) // 2, len(cn) - 1):
+        cw.order_node_children(aabbs, i)
+        cn = O.cwbvh_order_children(cn, cp, aabbs, node_index=i)
+        assert cw.download()[0].tobytes() == cn.tobytes()
+
+
+def test_order_children_large_scene(G):
+    """The post-pass on a 1M-triangle clustered CWBVH: many warps in the
+    queue at once."""
+    from obvhs_gb300 import scenes as S
+
+    tris = S.scene2_tris(1_000_000)
+    aabbs = T.tri_aabbs(tris)
+    cw = G.build_cwbvh_from_tris(tris, BvhBuildParams.medium_build())
+    cn, cp = cw.download()
+    cw.order_children(aabbs)
+    on = O.cwbvh_order_children(cn, cp, aabbs)
+    assert cw.download()[0].tobytes() == on.tobytes()

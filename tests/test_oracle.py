@@ -270,3 +270,79 @@ def test_compressed_traversal_hits_large_flat_quads():
     fid, ft, _ = O.traverse(ob.cw_nodes, ob.cw_pidx, tris, rays)
     assert np.all(cid != 0xFFFFFFFF) and np.array_equal(cid, fid)
     assert np.allclose(ct_t, 5.0) and np.allclose(ft, 5.0)
+
+
+# --- CWBVH post-passes: exact node AABBs and order_children -----------------
+
+
+def _very_fast_demoscene():
+    """The set-up of order_children_cwbvh / exact_aabbs_cwbvh
+    (tests/mod.rs:350-451): demoscene(100, 0), very_fast_build's PLOC, then
+    bvh2_to_cwbvh(max_prims 8 clamped to 3, order_children = true)."""
+    from obvhs_gb300.params import BvhBuildParams
+
+    tris = T.demoscene(100, 0)
+    aabbs = T.tri_aabbs(tris)
+    p = BvhBuildParams.very_fast_build()
+    nodes, pidx, _, _ = O.ploc(aabbs, None, int(p.ploc_search_distance), int(p.sort_precision),
+                               int(p.search_depth_threshold))
+    return tris, aabbs, nodes, pidx
+
+
+def test_order_children_keeps_a_valid_tree():
+    """order_children_cwbvh (tests/mod.rs:351-385): every node reordered one
+    at a time, then the whole pass: the CWBVH stays valid each time."""
+    tris, aabbs, nodes, pidx = _very_fast_demoscene()
+    cn, cp = O.bvh2_to_cwbvh(nodes, pidx, 3, True)
+    assert O.validate_cwbvh(cn, cp, aabbs)[0] == 0
+    one = cn
+    for i in range(len(cn)):
+        one = O.cwbvh_order_children(one, cp, aabbs, node_index=i)
+    assert O.validate_cwbvh(one, cp, aabbs)[0] == 0
+    whole = O.cwbvh_order_children(one, cp, aabbs)
+    assert O.validate_cwbvh(whole, cp, aabbs)[0] == 0
+    # node-by-node in index order is the whole pass
+    assert np.array_equal(O.cwbvh_order_children(cn, cp, aabbs), one)
+
+
+def test_exact_aabbs_contained_in_the_compressed_boxes():
+    """exact_aabbs_cwbvh (tests/mod.rs:387-451): each inner child's exact box
+    lies inside its quantised box in the parent and inside its own node's
+    (p, e) box; order_children with the exact boxes keeps the tree valid."""
+    tris, aabbs, nodes, pidx = _very_fast_demoscene()
+    cn, cp, ex = O.bvh2_to_cwbvh_exact(nodes, pidx, 3, True)
+    ref_n, ref_p = O.bvh2_to_cwbvh(nodes, pidx, 3, True)
+    assert np.array_equal(cn, ref_n) and np.array_equal(cp, ref_p)
+    rec = cn.view(np.uint8)
+
+    def node_box(i):
+        p = rec[i, 0:12].view(np.float32)
+        e = (rec[i, 12:15].astype(np.uint32) << 23).view(np.float32)
+        return p, p + e * np.float32(255.0)
+
+    for i in range(len(cn)):
+        p = rec[i, 0:12].view(np.float32)
+        e = (rec[i, 12:15].astype(np.uint32) << 23).view(np.float32)
+        imask = int(rec[i, 15])
+        base = int(rec[i, 16:20].view(np.uint32)[0])
+        for ch in range(8):
+            meta = int(rec[i, 24 + ch])
+            if meta == 0 or not (imask >> ch) & 1:
+                continue
+            slot = (meta & 31) - 24
+            k = base + bin(imask & ~(0xFFFFFFFF << slot) & 0xFF).count("1")
+            lo = np.array([rec[i, 32 + ch], rec[i, 48 + ch], rec[i, 64 + ch]], np.float32) * e + p
+            hi = np.array([rec[i, 40 + ch], rec[i, 56 + ch], rec[i, 72 + ch]], np.float32) * e + p
+            smin, smax = node_box(k)
+            assert np.all(ex[k, :3] >= lo) and np.all(ex[k, 3:] <= hi)
+            assert np.all(ex[k, :3] >= smin) and np.all(ex[k, 3:] <= smax)
+    n1, e1 = O.cwbvh_order_children(cn, cp, aabbs, exact=ex)
+    assert O.validate_cwbvh(n1, cp, aabbs)[0] == 0
+    n2, e2 = O.cwbvh_order_children(n1, cp, aabbs, exact=e1)
+    assert O.validate_cwbvh(n2, cp, aabbs)[0] == 0
+    # the exact boxes move with their nodes: each still lies in its node's box
+    for i in range(len(n2)):
+        smin, smax = (lambda r: (r[0:12].view(np.float32),
+                                 r[0:12].view(np.float32) + (r[12:15].astype(np.uint32) << 23).view(np.float32)
+                                 * np.float32(255.0)))(n2.view(np.uint8)[i])
+        assert np.all(e2[i, :3] >= smin - 1e-5) and np.all(e2[i, 3:] <= smax + 1e-5)
