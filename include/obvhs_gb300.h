@@ -171,6 +171,32 @@ OBVHS_API int obvhs_split_thresholds(obvhs_ctx* ctx, const float* triangles, uin
  * 1..3; the output node and primitive order equals the reference's. */
 OBVHS_API int obvhs_bvh2_to_cwbvh(obvhs_ctx* ctx, const obvhs_bvh2* bvh, uint32_t max_prims_per_leaf, int order_children,
                         obvhs_cwbvh** out);
+/* ---- the BVH2 product ------------------------------------------------------ */
+/* collapse (src/bvh2/leaf_collapser.rs:20-199) in place: leaves merged where
+ * the SAH says so (traversal_cost per inner node), at most max_prims
+ * primitives a leaf; node and primitive order as the reference's compaction.
+ * Drops attached triangles (their order changes). */
+OBVHS_API int obvhs_bvh2_collapse(obvhs_ctx* ctx, obvhs_bvh2* bvh, uint32_t max_prims, float traversal_cost);
+/* build_bvh2_from_tris / build_bvh2 (src/bvh2/builder.rs:16-138): pre-splits
+ * (triangles only, when params ask), PLOC, reinsertion, collapse (max prims
+ * clamped to 1..255), reinsertion with the post-collapse ratio.  The
+ * triangles are attached in primitive order for obvhs_bvh2_ray_traverse. */
+OBVHS_API int obvhs_build_bvh2_from_tris(obvhs_ctx* ctx, const float* triangles, uint32_t n,
+                                         const obvhs_build_params* params, int device_ptrs, obvhs_bvh2** out,
+                                         obvhs_build_stats* stats);
+OBVHS_API int obvhs_build_bvh2(obvhs_ctx* ctx, const float* aabbs, uint32_t n, const obvhs_build_params* params,
+                               int device_ptrs, obvhs_bvh2** out, obvhs_build_stats* stats);
+/* Triangles (n x 9, original order) attached for traversal. */
+OBVHS_API int obvhs_bvh2_set_triangles(obvhs_ctx* ctx, obvhs_bvh2* bvh, const float* triangles, uint32_t n,
+                                       int device_ptrs);
+/* Bvh2::ray_traverse / ray_traverse_miss (src/bvh2/mod.rs:148-337) with
+ * Triangle::intersect: hits as obvhs_ray_traverse (original id, t; misses
+ * 0xffffffff and +inf), occlusion flags as obvhs_ray_traverse_miss. */
+OBVHS_API int obvhs_bvh2_ray_traverse(obvhs_ctx* ctx, const obvhs_bvh2* bvh, const obvhs_ray* rays, uint32_t n,
+                                      obvhs_hit* hits, int device_ptrs);
+OBVHS_API int obvhs_bvh2_ray_traverse_miss(obvhs_ctx* ctx, const obvhs_bvh2* bvh, const obvhs_ray* rays, uint32_t n,
+                                           uint8_t* miss, int device_ptrs);
+
 /* bvh2_to_cwbvh with include_exact_node_aabbs (src/cwbvh/bvh2_to_cwbvh.rs:
  * 490-510, :76-80): the CWBVH also keeps, per node, the exact box of the BVH2
  * node it came from (read with obvhs_cwbvh_exact_node_aabbs; used and moved

@@ -11,7 +11,7 @@ __all__ = [
     "BvhBuildParams", "PlocSearchDistance", "SortPrecision", "PRESETS", "Context", "Bvh2", "CwBvh", "PlocBuilder",
     "ReinsertionOptimizer", "bvh2_to_cwbvh", "build_cwbvh_from_tris", "build_cwbvh", "split_aabbs_preset",
     "morton_sort", "split_thresholds", "ObvhsError", "build_cwbvh_from_tris_batch", "build_cwbvh_from_tris_segmented",
-    "ray_traverse_multi", "ray_traverse_batches",
+    "ray_traverse_multi", "ray_traverse_batches", "build_bvh2_from_tris", "build_bvh2",
 ]
 
 
@@ -19,7 +19,7 @@ def __getattr__(name):
     if name in ("Context", "Bvh2", "CwBvh", "PlocBuilder", "ReinsertionOptimizer", "bvh2_to_cwbvh",
                 "build_cwbvh_from_tris", "build_cwbvh", "split_aabbs_preset", "morton_sort", "BuildStats",
                 "split_thresholds", "build_cwbvh_from_tris_batch", "build_cwbvh_from_tris_segmented",
-                "ray_traverse_multi", "ray_traverse_batches"):
+                "ray_traverse_multi", "ray_traverse_batches", "build_bvh2_from_tris", "build_bvh2"):
         from . import bvh
 
         return getattr(bvh, name)

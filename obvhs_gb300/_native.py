@@ -79,6 +79,14 @@ SIGNATURES = {
     "obvhs_reinsertion_run": (I32, [P, P, F32, P, U32, ctypes.POINTER(U64)]),
     "obvhs_split_aabbs_preset": (I32, [P, P, U32, P, P, U32, ctypes.POINTER(U32)]),
     "obvhs_split_thresholds": (I32, [P, P, U32, P]),
+    "obvhs_bvh2_collapse": (I32, [P, P, U32, F32]),
+    "obvhs_build_bvh2_from_tris": (I32, [P, P, U32, ctypes.POINTER(BuildParams), I32, ctypes.POINTER(P),
+                                         ctypes.POINTER(BuildStats)]),
+    "obvhs_build_bvh2": (I32, [P, P, U32, ctypes.POINTER(BuildParams), I32, ctypes.POINTER(P),
+                               ctypes.POINTER(BuildStats)]),
+    "obvhs_bvh2_set_triangles": (I32, [P, P, P, U32, I32]),
+    "obvhs_bvh2_ray_traverse": (I32, [P, P, P, U32, P, I32]),
+    "obvhs_bvh2_ray_traverse_miss": (I32, [P, P, P, U32, P, I32]),
     "obvhs_bvh2_to_cwbvh": (I32, [P, P, U32, I32, ctypes.POINTER(P)]),
     "obvhs_bvh2_to_cwbvh_ex": (I32, [P, P, U32, I32, I32, ctypes.POINTER(P)]),
     "obvhs_cwbvh_exact_node_aabbs": (I32, [P, P, P]),

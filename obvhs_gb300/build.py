@@ -16,7 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libobvhs_gb300.so")
-SOURCES = ["radix_sort.cu", "ploc.cu", "presplit.cu", "reinsertion.cu", "cwbvh.cu", "traverse.cu", "api.cu", "no_alloc.cu"]
+SOURCES = ["radix_sort.cu", "ploc.cu", "presplit.cu", "reinsertion.cu", "cwbvh.cu", "collapse.cu", "traverse.cu", "api.cu",
+           "no_alloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [*ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fvisibility=hidden", "-I", os.path.join(HERE, "..", "include")]

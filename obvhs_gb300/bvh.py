@@ -195,6 +195,33 @@ class Bvh2:
                                             ctypes.byref(h)))
         return Bvh2(ctx, h)
 
+    def collapse(self, max_prims: int, traversal_cost: float):
+        """collapse (src/bvh2/leaf_collapser.rs:20-199), in place."""
+        self.ctx.check(self.ctx.lib.obvhs_bvh2_collapse(self.ctx.h, self.h, int(max_prims), float(traversal_cost)))
+
+    def set_triangles(self, triangles):
+        """Attach float (n, 9) triangles (original order) for traversal."""
+        p, n, dev, keep = _prep(triangles, np.float32, 9)
+        self.ctx.check(self.ctx.lib.obvhs_bvh2_set_triangles(self.ctx.h, self.h, p, n, dev))
+        del keep
+
+    def ray_traverse(self, rays, out=None):
+        """Closest hit per ray (Bvh2::ray_traverse with Triangle::intersect):
+        (original ids, 0xffffffff = miss; t, +inf = miss), or an int32 (n, 2)
+        tensor for device rays."""
+        out = CwBvh._trav(self, rays, out, self.ctx.lib.obvhs_bvh2_ray_traverse, 8)
+        if _is_cuda_tensor(out):
+            return out.view(-1, 2)
+        o = out.reshape(-1, 2)
+        return o[:, 0].copy(), o[:, 1].copy().view(np.float32)
+
+    def ray_traverse_miss(self, rays, out=None):
+        """True where the ray hits nothing (Bvh2::ray_traverse_miss)."""
+        out = CwBvh._trav(self, rays, out, self.ctx.lib.obvhs_bvh2_ray_traverse_miss, 1)
+        if _is_cuda_tensor(out):
+            return out
+        return out.astype(bool)
+
     def free(self):
         if self.h:
             self.ctx.lib.obvhs_bvh2_free(self.h)
@@ -625,6 +652,32 @@ def build_cwbvh_from_tris(triangles, config: BvhBuildParams, ctx: Context | None
         ctx.synchronize()
     del keep
     return CwBvh(ctx, h, BuildStats.from_c(st))
+
+
+def build_bvh2_from_tris(triangles, config: BvhBuildParams, ctx: Context | None = None) -> Bvh2:
+    """src/bvh2/builder.rs:16-91: pre-splits, PLOC, reinsertion, collapse,
+    reinsertion; the triangles attached for Bvh2.ray_traverse."""
+    ctx = _ctx(ctx)
+    p, n, dev, keep = _prep(triangles, np.float32, 9)
+    h = ctypes.c_void_p()
+    st = N.BuildStats()
+    prm = _params(config)
+    ctx.check(ctx.lib.obvhs_build_bvh2_from_tris(ctx.h, p, n, ctypes.byref(prm), dev, ctypes.byref(h),
+                                                 ctypes.byref(st)))
+    del keep
+    return Bvh2(ctx, h, BuildStats.from_c(st))
+
+
+def build_bvh2(aabbs, config: BvhBuildParams, ctx: Context | None = None) -> Bvh2:
+    """src/bvh2/builder.rs:103-138 (pre_split is ignored)."""
+    ctx = _ctx(ctx)
+    p, n, dev, keep = _prep(aabbs, np.float32, 6)
+    h = ctypes.c_void_p()
+    st = N.BuildStats()
+    prm = _params(config)
+    ctx.check(ctx.lib.obvhs_build_bvh2(ctx.h, p, n, ctypes.byref(prm), dev, ctypes.byref(h), ctypes.byref(st)))
+    del keep
+    return Bvh2(ctx, h, BuildStats.from_c(st))
 
 
 def build_cwbvh(aabbs, config: BvhBuildParams, ctx: Context | None = None) -> CwBvh:

@@ -701,6 +701,7 @@ int obvhs_bvh2_free(obvhs_bvh2* b) {
   if (!b) return OBVHS_OK;
   if (b->nodes) cudaFree(b->nodes);
   if (b->prim_indices) cudaFree(b->prim_indices);
+  if (b->tris) cudaFree(b->tris);
   delete b;
   return OBVHS_OK;
 }
@@ -1074,6 +1075,182 @@ int obvhs_cwbvh_download_compressed(obvhs_ctx* cp, const obvhs_cwbvh* b, void* t
   if (b->n_prims) CK(cudaMemcpyAsync(tris24, b->ctris, (size_t)b->n_prims * 24, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
   return OBVHS_OK;
+}
+
+int obvhs_bvh2_collapse(obvhs_ctx* cp, obvhs_bvh2* b, uint32_t max_prims, float traversal_cost) {
+  if (!cp || !b) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  BuildScope building(c.device);
+  if (b->tris) {  // primitive order changes: attached triangles no longer match
+    cudaFree(b->tris);
+    b->tris = nullptr;
+  }
+  int r = bvh2_collapse_device(c, b, max_prims, traversal_cost);
+  if (!r) r = take_status(c);
+  return r;
+}
+
+// build_bvh2_from_tris (tris != NULL) / build_bvh2 (src/bvh2/builder.rs:16-138):
+// pre-splits (triangles only), PLOC, reinsertion, collapse, reinsertion with
+// the post-collapse ratio; triangles attached in primitive order.
+static int bvh2_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t n, const obvhs_build_params* p,
+                         obvhs_bvh2** out, obvhs_build_stats* stats) {
+  if (p->ploc_search_distance < 1 || p->ploc_search_distance > 32)
+    return c.fail(OBVHS_ERR_INVALID_ARG, "ploc_search_distance must be 1..32");
+  if (p->sort_precision > 1) return c.fail(OBVHS_ERR_INVALID_ARG, "sort_precision must be 0 (U64) or 1 (U128)");
+  const uint64_t l0 = c.kernel_launches;
+  EventTimer timer(c.stream);
+  StageEvents stages(c.stream);
+  Scratch& s = c.scratch;
+  const bool split = tris && p->pre_split;
+  const float* leaf_aabbs = aabbs;
+  const uint32_t* leaf_idx = nullptr;
+  uint32_t m = n;
+  int r;
+  if (split) {
+    float* a = nullptr;
+    uint32_t* ix = nullptr;
+    r = presplit_device(c, tris, n, &a, &ix, &m);
+    if (r) return r;
+    leaf_aabbs = a;
+    leaf_idx = ix;
+  }
+  stages.mark(c.stream);
+  obvhs_bvh2* b = new obvhs_bvh2();
+  b->ctx = &c;
+  b->n_nodes = m ? 2 * m - 1 : 0;
+  b->n_prims = m;
+  b->uses_spatial_splits = split;
+  auto fail = [&](int code) {
+    obvhs_bvh2_free(b);
+    return code;
+  };
+  Bvh2Node* leaves = (Bvh2Node*)s.get(SLOT_LEAVES, (size_t)std::max(m, 1u) * sizeof(Bvh2Node));
+  int* total = (int*)s.get(SLOT_TOTAL, 64);
+  if (!leaves || !total) return fail(c.fail(OBVHS_ERR_OOM, "scratch"));
+  if (cudaMalloc(&b->nodes, (size_t)std::max(b->n_nodes, 1u) * sizeof(Bvh2Node)) != cudaSuccess ||
+      cudaMalloc(&b->prim_indices, (size_t)std::max(m, 1u) * 4) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c.fail(OBVHS_ERR_OOM, "bvh2 allocation"));
+  }
+  r = (split || !tris) ? ploc_leaves(c, nullptr, leaf_aabbs, leaf_idx, m, leaves, total)
+                       : ploc_leaves(c, tris, nullptr, nullptr, m, leaves, total);
+  if (r) return fail(r);
+  if (m) {
+    if (leaf_idx) {
+      if (cudaMemcpyAsync(b->prim_indices, leaf_idx, (size_t)m * 4, cudaMemcpyDeviceToDevice, c.stream))
+        return fail(c.fail(OBVHS_ERR_CUDA, "copy"));
+    } else {
+      KLAUNCH("k_iota_u32", k_iota_u32<<<div_up<uint32_t>(m, 256), 256, 0, c.stream>>>(b->prim_indices, m));
+    }
+  }
+  uint32_t passes = 0;
+  uint64_t sum_counts = 0;
+  r = ploc_build_device(c, leaves, m, total, p->ploc_search_distance, (int)p->sort_precision, p->search_depth_threshold,
+                        b->nodes, &passes, &sum_counts);
+  if (!r) r = take_status(c);  // NaN boxes leave tree slots unwritten
+  if (r) return fail(r);
+  b->max_depth = std::max<uint32_t>(96, passes + 1);
+  stages.mark(c.stream);
+  uint64_t applied = 0, applied2 = 0;
+  r = reinsertion_device(c, b, p->reinsertion_batch_ratio, nullptr, 0, &applied);
+  if (!r) r = take_status(c);
+  if (!r) {
+    const uint32_t mp = p->max_prims_per_leaf < 1 ? 1 : (p->max_prims_per_leaf > 255 ? 255 : p->max_prims_per_leaf);
+    r = bvh2_collapse_device(c, b, mp, p->collapse_traversal_cost);
+  }
+  if (!r) r = take_status(c);
+  if (!r)
+    r = reinsertion_device(c, b, p->reinsertion_batch_ratio * p->post_collapse_reinsertion_batch_ratio_multiplier,
+                           nullptr, 0, &applied2);
+  stages.mark(c.stream);
+  if (!r && tris) r = bvh2_reorder_tris_device(c, b, tris, n);
+  stages.mark(c.stream);
+  const double ms = timer.stop_ms();
+  if (!r) r = take_status(c);
+  if (r) return fail(r);
+  if (stats) {
+    stats->core_build_ms = ms;
+    stats->leaf_count = m;
+    stats->ploc_passes = passes;
+    stats->ploc_sum_counts = sum_counts;
+    stats->reinsertions = applied + applied2;
+    stats->kernel_launches = c.kernel_launches - l0;
+    stages.read(stats->stage_ms);
+  }
+  *out = b;
+  return 0;
+}
+
+int obvhs_build_bvh2_from_tris(obvhs_ctx* cp, const float* triangles, uint32_t n, const obvhs_build_params* p,
+                               int device_ptrs, obvhs_bvh2** out, obvhs_build_stats* stats) {
+  if (!cp || !p || !out || (n && !triangles)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  BuildScope building(c.device);
+  *out = nullptr;
+  int err = 0;
+  const float* dt = (const float*)stage_in(c, SLOT_INPUT, triangles, (size_t)n * 36, device_ptrs, &err);
+  if (err) return err;
+  return bvh2_pipeline(c, dt, nullptr, n, p, out, stats);
+}
+
+int obvhs_build_bvh2(obvhs_ctx* cp, const float* aabbs, uint32_t n, const obvhs_build_params* p, int device_ptrs,
+                     obvhs_bvh2** out, obvhs_build_stats* stats) {
+  if (!cp || !p || !out || (n && !aabbs)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  BuildScope building(c.device);
+  *out = nullptr;
+  int err = 0;
+  const float* da = (const float*)stage_in(c, SLOT_INPUT, aabbs, (size_t)n * 24, device_ptrs, &err);
+  if (err) return err;
+  return bvh2_pipeline(c, nullptr, da, n, p, out, stats);
+}
+
+int obvhs_bvh2_set_triangles(obvhs_ctx* cp, obvhs_bvh2* b, const float* triangles, uint32_t n, int device_ptrs) {
+  if (!cp || !b || (n && !triangles)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  int err = 0;
+  const float* dt = (const float*)stage_in(c, SLOT_INPUT, triangles, (size_t)n * 36, device_ptrs, &err);
+  if (err) return err;
+  int r = bvh2_reorder_tris_device(c, b, dt, n);
+  if (!r) r = take_status(c);
+  return r;
+}
+
+static int bvh2_traverse_common(obvhs_ctx* cp, const obvhs_bvh2* b, const obvhs_ray* rays, uint32_t n, void* out,
+                                int device_ptrs, int mode) {
+  if (!cp || !b || (n && (!rays || !out))) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  int err = 0;
+  const float* dr = (const float*)stage_in(c, SLOT_INPUT2, rays, (size_t)n * 32, device_ptrs, &err);
+  if (err) return err;
+  const size_t ob = (size_t)n * (mode == 0 ? 8 : 1);
+  void* dout = out;
+  if (!device_ptrs) {
+    dout = c.scratch.get(SLOT_TRAV_OUT, ob + 16);
+    if (!dout) return c.fail(OBVHS_ERR_OOM, "output staging");
+  }
+  int r = bvh2_traverse_device(c, b, dr, n, mode == 0 ? (uint32_t*)dout : nullptr, mode == 0 ? nullptr : (uint8_t*)dout,
+                               mode);
+  if (r) return r;
+  if (!device_ptrs && n) CK(cudaMemcpyAsync(out, dout, ob, cudaMemcpyDeviceToHost, c.stream));
+  if (!device_ptrs) return take_status(c);
+  return OBVHS_OK;
+}
+
+int obvhs_bvh2_ray_traverse(obvhs_ctx* cp, const obvhs_bvh2* b, const obvhs_ray* rays, uint32_t n, obvhs_hit* hits,
+                            int device_ptrs) {
+  return bvh2_traverse_common(cp, b, rays, n, hits, device_ptrs, 0);
+}
+
+int obvhs_bvh2_ray_traverse_miss(obvhs_ctx* cp, const obvhs_bvh2* b, const obvhs_ray* rays, uint32_t n, uint8_t* miss,
+                                 int device_ptrs) {
+  return bvh2_traverse_common(cp, b, rays, n, miss, device_ptrs, 1);
 }
 
 int obvhs_cwbvh_exact_node_aabbs(obvhs_ctx* cp, const obvhs_cwbvh* b, float* aabbs6) {

@@ -219,6 +219,8 @@ struct obvhs_bvh2 {
   uint32_t n_prims = 0;
   uint32_t max_depth = 96;
   int uses_spatial_splits = 0;
+  float4* tris = nullptr;  // primitive_indices order, 64 B each (as the CWBVH's)
+  uint32_t n_tris = 0;
 };
 
 struct obvhs_cwbvh {
@@ -347,6 +349,11 @@ int batch_owner_device(BuildCtx& c, const uint32_t* d_offsets, const uint32_t* d
 int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint32_t n, uint32_t* hits,
                     uint8_t* miss, int mode);
 int reorder_tris_device(BuildCtx& c, obvhs_cwbvh* bvh, const float* tris, uint32_t n_tris);
+// The BVH2 product (src/bvh2/builder.rs, leaf_collapser.rs, mod.rs:148-337).
+int bvh2_collapse_device(BuildCtx& c, obvhs_bvh2* b, uint32_t max_prims, float traversal_cost);
+int bvh2_reorder_tris_device(BuildCtx& c, obvhs_bvh2* b, const float* tris, uint32_t n_tris);
+int bvh2_traverse_device(BuildCtx& c, const obvhs_bvh2* b, const float* rays, uint32_t n, uint32_t* hits,
+                         uint8_t* miss, int mode);
 // RtCompressedTriangle records (24 B) of the triangles in BVH order.
 int compress_tris_device(BuildCtx& c, obvhs_cwbvh* bvh, const float* tris, uint32_t n_tris);
 // Traversal on the compressed triangles (mode 0 closest hit, 1 occlusion).

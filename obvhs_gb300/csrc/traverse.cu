@@ -288,6 +288,134 @@ __global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ no
   }
 }
 
+// --- Bvh2::ray_traverse / ray_traverse_miss (src/bvh2/mod.rs:148-337) -----------
+
+// Aabb::intersect_ray (src/aabb.rs:186-206): slab distances with the SSE lane
+// min/max; the horizontal max/min over x, y, z (their association only
+// changes the sign of a zero, which no comparison sees).
+__device__ __forceinline__ float box_ray_t(const Bvh2Node& nd, float3 o, float3 inv) {
+  const float t1x = (nd.a.x - o.x) * inv.x, t1y = (nd.a.y - o.y) * inv.y, t1z = (nd.a.z - o.z) * inv.z;
+  const float t2x = (nd.b.x - o.x) * inv.x, t2y = (nd.b.y - o.y) * inv.y, t2z = (nd.b.z - o.z) * inv.z;
+  const float mnx = smin(t1x, t2x), mny = smin(t1y, t2y), mnz = smin(t1z, t2z);
+  const float mxx = smax(t1x, t2x), mxy = smax(t1y, t2y), mxz = smax(t1z, t2z);
+  const float tmn = smax(smax(mnx, mnz), smax(mny, mnz));
+  const float tmx = smin(smin(mxx, mxz), smin(mxy, mxz));
+  return (tmx >= tmn && tmx >= 0.0f) ? tmn : __int_as_float(0x7f800000);
+}
+
+constexpr int BVH2_STACK = 128;
+
+// One ray per thread (persistent warps).  The reference's loop: test both
+// children of the current node, nearer first; leaves are intersected at once
+// (closest hit: every primitive, ray.tmax shrinking; occlusion: stop at the
+// first t < tmax), the farther hit child is pushed, the nearer followed.
+template <int MODE>
+__global__ void __launch_bounds__(TBLK) k_traverse_bvh2(const Bvh2Node* __restrict__ nodes, uint32_t n_nodes,
+                                                        const float4* __restrict__ tris, uint32_t n_prims,
+                                                        const float4* __restrict__ rays, uint32_t nrays,
+                                                        uint2* __restrict__ hits, uint8_t* __restrict__ miss,
+                                                        uint32_t* __restrict__ next_ray, uint32_t* status) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(next_ray, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= nrays) return;
+    const uint32_t ri = base + lane;
+    if (ri >= nrays) continue;
+    const float4 r0 = __ldg(&rays[2 * ri]), r1 = __ldg(&rays[2 * ri + 1]);
+    const float3 o = make_float3(r0.x, r0.y, r0.z), d = make_float3(r1.x, r1.y, r1.z);
+    const float tmin = r0.w;
+    float tmax = r1.w;
+    const float3 inv = make_float3(safe_inverse(d.x), safe_inverse(d.y), safe_inverse(d.z));
+    uint32_t hit_id = OBVHS_INVALID;
+    float hit_t = __int_as_float(0x7f800000);
+    bool stop = false, bad = false;
+    // the primitives of leaf x; MODE 1 stops at the first hit
+    auto leaf = [&](const Bvh2Node& x) {
+      const uint32_t f = node_first(x), cnt = node_prims(x);
+      for (uint32_t k = 0; k < cnt; k++) {
+        if (f + k >= n_prims) {
+          bad = true;
+          return;
+        }
+        uint32_t orig;
+        const float t = intersect_tri(&tris[4 * (size_t)(f + k)], o, d, tmin, tmax, &orig);
+        if (t < tmax) {
+          hit_id = orig;
+          hit_t = t;
+          if (MODE == 0) {
+            tmax = t;
+          } else {
+            stop = true;
+            return;
+          }
+        }
+      }
+    };
+    if (n_nodes) {
+      const Bvh2Node root = ld_node(&nodes[0]);
+      if (box_ray_t(root, o, inv) < tmax) {
+        if (node_prims(root) != 0) {
+          leaf(root);
+        } else {
+          uint32_t stack[BVH2_STACK];
+          uint32_t sp = 0, cur = node_first(root);
+          for (uint32_t guard = 0;; guard++) {
+            if (guard > (1u << 24) || cur + 1 >= n_nodes) {
+              bad = true;
+              break;
+            }
+            Bvh2Node l = ld_node(&nodes[cur]), r = ld_node(&nodes[cur + 1]);
+            float lt = box_ray_t(l, o, inv), rt = box_ray_t(r, o, inv);
+            if (lt > rt) {
+              const float tt = lt;
+              lt = rt;
+              rt = tt;
+              const Bvh2Node tn = l;
+              l = r;
+              r = tn;
+            }
+            bool go_l = lt < tmax;
+            if (go_l && node_prims(l) != 0) {
+              leaf(l);
+              if (stop || bad) break;
+              go_l = false;
+            }
+            bool go_r = rt < tmax;
+            if (go_r && node_prims(r) != 0) {
+              leaf(r);
+              if (stop || bad) break;
+              go_r = false;
+            }
+            if (go_l && go_r) {
+              if (sp >= BVH2_STACK) {
+                set_status(status, ST_STACK_OVERFLOW);
+                bad = true;
+                break;
+              }
+              stack[sp++] = node_first(r);
+              cur = node_first(l);
+            } else if (go_l) {
+              cur = node_first(l);
+            } else if (go_r) {
+              cur = node_first(r);
+            } else {
+              if (sp == 0) break;
+              cur = stack[--sp];
+            }
+          }
+        }
+      }
+    }
+    if (bad) set_status(status, ST_BAD_TREE);
+    if (MODE == 0)
+      hits[ri] = make_uint2(hit_id, __float_as_uint(hit_id == OBVHS_INVALID ? __int_as_float(0x7f800000) : hit_t));
+    else
+      miss[ri] = hit_id == OBVHS_INVALID ? 1 : 0;
+  }
+}
+
 // RtCompressedTriangle::new (src/rt_triangle.rs:31-47) for the triangles in
 // primitive_indices order; halves by round-to-nearest-even (f16::from_f32).
 __global__ void k_compress_tris(const float* __restrict__ tris, uint32_t n_tris, const uint32_t* __restrict__ pidx,
@@ -501,6 +629,54 @@ int reorder_tris_seg_device(BuildCtx& c, const SegTriJob* d_jobs, const uint32_t
   if (!total) return 0;
   KLAUNCH("k_seg_reorder_tris", k_seg_reorder_tris<<<div_up<uint32_t>(total, 256), 256, 0, c.stream>>>(
                                     d_jobs, d_prim_start, n_seg, total, c.d_status));
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int bvh2_reorder_tris_device(BuildCtx& c, obvhs_bvh2* b, const float* tris, uint32_t n_tris) {
+  if (b->tris) {
+    cudaFree(b->tris);
+    b->tris = nullptr;
+  }
+  b->n_tris = n_tris;
+  if (b->n_prims == 0) return 0;
+  float4* out = nullptr;
+  if (cudaMalloc(&out, (size_t)b->n_prims * 64) != cudaSuccess) {
+    cudaGetLastError();
+    return c.fail(OBVHS_ERR_OOM, "triangle buffer");
+  }
+  KLAUNCH("k_reorder_tris", k_reorder_tris<<<div_up<uint32_t>(b->n_prims, 256), 256, 0, c.stream>>>(
+                                tris, n_tris, b->prim_indices, b->n_prims, out, c.d_status));
+  CK(cudaGetLastError());
+  b->tris = out;
+  return 0;
+}
+
+int bvh2_traverse_device(BuildCtx& c, const obvhs_bvh2* b, const float* rays, uint32_t n, uint32_t* hits,
+                         uint8_t* miss, int mode) {
+  if (n == 0) return 0;
+  if (b->n_nodes && !b->tris) return c.fail(OBVHS_ERR_INVALID_ARG, "no triangles attached to the BVH2");
+  uint32_t* counter = (uint32_t*)c.scratch.get(SLOT_OUTPUT, 16);
+  if (!counter) return c.fail(OBVHS_ERR_OOM, "scratch");
+  CK(cudaMemsetAsync(counter, 0, 4, c.stream));
+  static std::atomic<int> per_sm_s{0};
+  int per_sm = per_sm_s.load();
+  if (!per_sm) {
+    int a = 0, bb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_traverse_bvh2<0>, TBLK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bb, k_traverse_bvh2<1>, TBLK, 0);
+    per_sm = std::max(1, std::min(a, bb));
+    per_sm_s.store(per_sm);
+  }
+  const uint32_t grid = std::min<uint32_t>(div_up<uint32_t>(n, TBLK), (uint32_t)(per_sm * c.num_sms));
+  if (mode == 0)
+    KLAUNCH("k_traverse_bvh2_closest", k_traverse_bvh2<0><<<grid, TBLK, 0, c.stream>>>(
+                                           b->nodes, b->n_nodes, b->tris, b->n_prims, (const float4*)rays, n,
+                                           (uint2*)hits, nullptr, counter, c.d_status));
+  else
+    KLAUNCH("k_traverse_bvh2_occluded", k_traverse_bvh2<1><<<grid, TBLK, 0, c.stream>>>(
+                                            b->nodes, b->n_nodes, b->tris, b->n_prims, (const float4*)rays, n,
+                                            nullptr, miss, counter, c.d_status));
   CK(cudaGetLastError());
   return 0;
 }

@@ -1353,6 +1353,92 @@ inline Ray make_ray(const float* r8) {
 // ---------------------------------------------------------------------------
 // Validation (src/bvh2/mod.rs:786-981, src/cwbvh/mod.rs:747-908).  Returns
 // 0 on success, a negative code naming the first failed assertion otherwise.
+// Aabb::intersect_ray (src/aabb.rs:186-206) with glam's SSE2 lane min/max;
+// horizontal max/min over x, y, z (their association only changes the sign
+// of a zero, which no comparison sees).
+inline float aabb_ray_t(const Aabb& a, const Ray& r) {
+  V3 t1 = v3((a.mn.x - r.o.x) * r.inv.x, (a.mn.y - r.o.y) * r.inv.y, (a.mn.z - r.o.z) * r.inv.z);
+  V3 t2 = v3((a.mx.x - r.o.x) * r.inv.x, (a.mx.y - r.o.y) * r.inv.y, (a.mx.z - r.o.z) * r.inv.z);
+  V3 mn = vmin(t1, t2), mx = vmax(t1, t2);
+  float tmn = smax(smax(mn.x, mn.z), smax(mn.y, mn.z));
+  float tmx = smin(smin(mx.x, mx.z), smin(mx.y, mx.z));
+  return (tmx >= tmn && tmx >= 0.0f) ? tmn : INFINITY;
+}
+
+// Bvh2::ray_traverse / ray_traverse_miss (src/bvh2/mod.rs:148-337) with
+// Triangle::intersect on tris[primitive_indices[id]].  Returns the BVH slot of
+// the hit (primitive_indices index) or INVALID32; *t_out its t.
+inline uint32_t traverse_bvh2(const Bvh2& b, const Tri* tris, size_t n_tris, Ray ray, int mode, float* t_out,
+                              uint64_t* visits) {
+  uint32_t hit_id = INVALID32;
+  float hit_t = INFINITY;
+  *t_out = INFINITY;
+  if (b.nodes.empty()) return INVALID32;
+  bool stop = false;
+  auto leaf = [&](const Node& n) {
+    for (uint32_t id = n.first_index; id < n.first_index + n.prim_count; id++) {
+      uint32_t ti = b.primitive_indices[id];
+      if (ti >= n_tris) continue;
+      float t = tri_intersect(tris[ti], ray, ray.tmax);
+      if (t < ray.tmax) {
+        hit_id = id;
+        hit_t = t;
+        if (mode == 0) {
+          ray.tmax = t;
+        } else {
+          stop = true;
+          return;
+        }
+      }
+    }
+  };
+  const Node& root = b.nodes[0];
+  if (visits) (*visits)++;
+  if (!(aabb_ray_t(root.box, ray) < ray.tmax)) return INVALID32;
+  if (root.is_leaf()) {
+    leaf(root);
+  } else {
+    std::vector<uint32_t> stack;
+    uint32_t cur = root.first_index;
+    for (;;) {
+      const Node* l = &b.nodes[cur];
+      const Node* r = &b.nodes[cur + 1];
+      if (visits) (*visits) += 2;
+      float lt = aabb_ray_t(l->box, ray), rt = aabb_ray_t(r->box, ray);
+      if (lt > rt) {
+        std::swap(lt, rt);
+        std::swap(l, r);
+      }
+      bool go_l = lt < ray.tmax;
+      if (go_l && l->is_leaf()) {
+        leaf(*l);
+        if (stop) break;
+        go_l = false;
+      }
+      bool go_r = rt < ray.tmax;
+      if (go_r && r->is_leaf()) {
+        leaf(*r);
+        if (stop) break;
+        go_r = false;
+      }
+      if (go_l && go_r) {
+        cur = l->first_index;
+        stack.push_back(r->first_index);
+      } else if (go_l) {
+        cur = l->first_index;
+      } else if (go_r) {
+        cur = r->first_index;
+      } else {
+        if (stack.empty()) break;
+        cur = stack.back();
+        stack.pop_back();
+      }
+    }
+  }
+  *t_out = hit_t;
+  return hit_id;
+}
+
 int validate_bvh2(const Bvh2& b, const Aabb* prim_aabbs, size_t n_prims_src, bool tight, uint32_t* depth_out) {
   if (b.nodes.empty()) return 0;
   std::vector<uint8_t> seen_node(b.nodes.size(), 0);
@@ -1522,6 +1608,121 @@ double sah_cwbvh(const CwNode* nodes, size_t n) {
       s += inner ? a : a * (double)__builtin_popcount(meta & 0xe0);
     }
   return root > 0.0 ? s / root : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Leaf collapsing (src/bvh2/leaf_collapser.rs:20-199): bottom-up decisions,
+// prefix sums of kept nodes and primitives in node order, then a stable
+// compaction in which every collapsed leaf gathers its subtree's primitives
+// depth-first (left before right).
+void collapse(Bvh2& b, uint32_t max_prims, float traversal_cost) {
+  const size_t nq = b.nodes.size();
+  if (max_prims <= 1 || nq <= (size_t)max_prims * 2 + 1) return;
+  if (!b.primitive_indices.empty() && b.primitive_indices.size() <= max_prims) return;
+  if (b.nodes.empty() || b.nodes[0].is_leaf()) return;
+  compute_parents(b.nodes, b.parents);
+  std::vector<uint32_t> nc(nq, 1), pc(nq, 0);
+  auto process = [&](bool leaf, size_t i) {
+    if (leaf) {
+      pc[i] = b.nodes[i].prim_count;
+      return;
+    }
+    const Node& node = b.nodes[i];
+    const size_t f = node.first_index;
+    const uint32_t lc = pc[f], rc = pc[f + 1], total = lc + rc;
+    if (lc > 0 && rc > 0 && total <= max_prims) {
+      const Node& l = b.nodes[f];
+      const Node& r = b.nodes[f + 1];
+      const float collapse_cost = half_area(node.box) * ((float)total - traversal_cost);
+      const float base_cost = half_area(l.box) * (float)lc + half_area(r.box) * (float)rc;
+      const bool same = l.first_index == r.first_index && total == 2;
+      if (collapse_cost <= base_cost || same) {
+        pc[i] = total;
+        pc[f] = pc[f + 1] = 0;
+        nc[f] = nc[f + 1] = 0;
+      }
+    }
+  };
+  // bottom_up_traverse (leaf_collapser.rs:207-242), sequential form
+  std::vector<uint8_t> flags(nq, 0);
+  for (size_t i = 1; i < nq; i++) {
+    if (!b.nodes[i].is_leaf()) continue;
+    process(true, i);
+    size_t j = i;
+    while (j != 0) {
+      j = b.parents[j];
+      const uint8_t prev = flags[j];
+      flags[j] = prev == 255 ? 255 : prev + 1;
+      if (prev != 1) break;
+      flags[j] = 0;
+      process(false, j);
+    }
+  }
+  for (size_t i = 1; i < nq; i++) {
+    nc[i] += nc[i - 1];
+    pc[i] += pc[i - 1];
+  }
+  if (pc[0] > 0) {  // the root became a leaf: nodes and indices otherwise stay as they are
+    b.nodes[0].first_index = 0;
+    b.nodes[0].prim_count = pc[0];
+    b.parents.clear();
+    return;
+  }
+  std::vector<Node> nn(nc[nq - 1]);
+  std::vector<uint32_t> ni(pc[nq - 1]);
+  nn[0] = b.nodes[0];
+  nn[0].first_index = nc[nn[0].first_index - 1];
+  for (size_t i = 1; i < nq; i++) {
+    const uint32_t id = nc[i - 1];
+    if (id == nc[i]) continue;
+    nn[id] = b.nodes[i];
+    uint32_t first_prim = pc[i - 1];
+    if (first_prim == pc[i]) {
+      nn[id].first_index = nc[nn[id].first_index - 1];
+      continue;
+    }
+    nn[id].prim_count = pc[i] - first_prim;
+    nn[id].first_index = first_prim;
+    size_t j = i;
+    for (;;) {
+      const Node& node = b.nodes[j];
+      if (node.is_leaf()) {
+        for (uint32_t k = 0; k < node.prim_count; k++) ni[first_prim + k] = b.primitive_indices[node.first_index + k];
+        first_prim += node.prim_count;
+        while (j % 2 != 1 && j != i) j = b.parents[j];
+        if (j == i) break;
+        j = sibling((uint32_t)j);
+      } else {
+        j = node.first_index;
+      }
+    }
+  }
+  b.nodes.swap(nn);
+  b.primitive_indices.swap(ni);
+  b.parents.clear();
+}
+
+// Bvh2::refit_all (src/bvh2/mod.rs:527-570): every inner node from its
+// children, children first.  Unions are exact, so any children-first order
+// gives the reference's boxes; this walks the DFS order backwards.
+void refit_all(Bvh2& b) {
+  if (b.nodes.empty()) return;
+  std::vector<uint32_t> order{0}, st{0};
+  while (!st.empty()) {
+    uint32_t x = st.back();
+    st.pop_back();
+    const Node& n = b.nodes[x];
+    if (!n.is_leaf()) {
+      order.push_back(n.first_index);
+      order.push_back(n.first_index + 1);
+      st.push_back(n.first_index);
+      st.push_back(n.first_index + 1);
+    }
+  }
+  for (size_t k = order.size(); k-- > 0;) {
+    Node& n = b.nodes[order[k]];
+    if (!n.is_leaf()) n.box = uni(b.nodes[n.first_index].box, b.nodes[n.first_index + 1].box);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1708,6 +1909,95 @@ int32_t orc_cwbvh_order_children(void* nodes80, uint64_t n_nodes, const uint32_t
       o[3] = ex[i].mx.x; o[4] = ex[i].mx.y; o[5] = ex[i].mx.z;
     }
   return 0;
+}
+
+// collapse (src/bvh2/leaf_collapser.rs) in place: counts = [nodes, prims].
+int32_t orc_bvh2_collapse(void* nodes32, uint64_t n_nodes, uint32_t* pidx, uint64_t n_pidx, uint32_t max_prims,
+                          float traversal_cost, uint64_t* counts) {
+  Bvh2 b = load_bvh2(nodes32, n_nodes, pidx, n_pidx, 96);
+  collapse(b, max_prims, traversal_cost);
+  NodeX* o = (NodeX*)nodes32;
+  for (size_t i = 0; i < b.nodes.size(); i++) o[i] = to_x(b.nodes[i]);
+  std::memcpy(pidx, b.primitive_indices.data(), b.primitive_indices.size() * 4);
+  counts[0] = b.nodes.size();
+  counts[1] = b.primitive_indices.size();
+  return 0;
+}
+
+// Bvh2::refit_all in place.
+void orc_bvh2_refit_all(void* nodes32, uint64_t n_nodes) {
+  Bvh2 b = load_bvh2(nodes32, n_nodes, nullptr, 0, 96);
+  refit_all(b);
+  NodeX* o = (NodeX*)nodes32;
+  for (size_t i = 0; i < b.nodes.size(); i++) o[i] = to_x(b.nodes[i]);
+}
+
+// Bvh2 traversal: mode 0 closest hit (hits: original id, t bits), 1 occlusion
+// (hits[.].x = 1 when occluded).
+void orc_bvh2_traverse(int32_t mode, const void* nodes32, uint64_t n_nodes, const uint32_t* pidx, uint64_t n_pidx,
+                       const float* tris9, uint64_t n_tris, const float* rays8, uint64_t n, uint32_t* hits,
+                       int32_t nthreads, uint64_t* visits_out) {
+  Bvh2 b = load_bvh2(nodes32, n_nodes, pidx, n_pidx, 96);
+  std::vector<Tri> t = load_tris(tris9, n_tris);
+  std::atomic<uint64_t> vis{0};
+  parallel_for(nthreads, n, [&](size_t lo, size_t hi) {
+    uint64_t v = 0;
+    for (size_t i = lo; i < hi; i++) {
+      Ray r = make_ray(rays8 + 8 * i);
+      float th;
+      uint32_t id = traverse_bvh2(b, t.data(), t.size(), r, mode, &th, &v);
+      if (mode == 0) {
+        hits[2 * i] = id == INVALID32 ? INVALID32 : b.primitive_indices[id];
+        hits[2 * i + 1] = f_bits(id == INVALID32 ? INFINITY : th);
+      } else {
+        hits[2 * i] = id == INVALID32 ? 0u : 1u;
+        hits[2 * i + 1] = 0;
+      }
+    }
+    vis += v;
+  });
+  if (visits_out) *visits_out = vis.load();
+}
+
+// build_bvh2_from_tris (tris != NULL) / build_bvh2 (src/bvh2/builder.rs:16-138):
+// pre-splits (tris only), PLOC, reinsertion, collapse, reinsertion again with
+// the post-collapse ratio.  Returns a handle for orc_build_* or NULL.
+void* orc_build_bvh2(const float* tris, const float* aabbs6, uint64_t n, const orc_params* p,
+                     float post_collapse_multiplier, float collapse_traversal_cost, int32_t nthreads, int32_t* status) {
+  auto* r = new BuildResult();
+  std::vector<Tri> t;
+  if (tris) {
+    t = load_tris(tris, n);
+    r->aabbs.resize(n);
+    for (size_t i = 0; i < n; i++) r->aabbs[i] = tri_aabb(t[i]);
+  } else {
+    r->aabbs = load_aabbs(aabbs6, n);
+  }
+  r->indices.resize(n);
+  for (size_t i = 0; i < n; i++) r->indices[i] = (uint32_t)i;
+  if (tris && p->pre_split) {
+    float largest = 0.0f, avg = 0.0f;
+    for (size_t i = 0; i < n; i++) {
+      float ha = half_area(r->aabbs[i]);
+      largest = std::fmax(ha, largest);
+      avg += ha;
+    }
+    avg /= (float)n;
+    split_aabbs_preset(r->aabbs, r->indices, t.data(), avg, largest);
+  }
+  ploc_build(r->bvh2, r->aabbs.data(), r->indices.data(), r->aabbs.size(), p->search_distance,
+             (int)p->sort_precision, p->search_depth_threshold, nthreads, &r->ploc_stats, &r->codes, &r->order);
+  r->bvh2.uses_spatial_splits = tris && p->pre_split;
+  int rc = reinsertion_run(r->bvh2, p->reinsertion_batch_ratio, nullptr, 0, nthreads, &r->reins_stats);
+  r->bvh2_ploc = r->bvh2;  // after the first reinsertion (collapse input)
+  uint32_t mp = p->max_prims_per_leaf < 1 ? 1 : (p->max_prims_per_leaf > 255 ? 255 : p->max_prims_per_leaf);
+  if (!rc) collapse(r->bvh2, mp, collapse_traversal_cost);
+  ReinsStats second{};
+  if (!rc) rc = reinsertion_run(r->bvh2, p->reinsertion_batch_ratio * post_collapse_multiplier, nullptr, 0, nthreads,
+                                &second);
+  r->reins_stats.applied += second.applied;
+  if (status) *status = rc;
+  return r;
 }
 
 // Pre-splits: returns a handle; orc_presplit_get copies out.

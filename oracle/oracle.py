@@ -76,6 +76,14 @@ def _declare(L):
     L.orc_reinsertion.restype = I32
     L.orc_bvh2_to_cwbvh.argtypes = [P, U64, P, U64, U32, I32, P, P, P]
     L.orc_bvh2_to_cwbvh.restype = I32
+    L.orc_bvh2_collapse.argtypes = [P, U64, P, U64, U32, ctypes.c_float, P]
+    L.orc_bvh2_collapse.restype = I32
+    L.orc_bvh2_refit_all.argtypes = [P, U64]
+    L.orc_bvh2_refit_all.restype = None
+    L.orc_bvh2_traverse.argtypes = [I32, P, U64, P, U64, P, U64, P, U64, P, I32, P]
+    L.orc_bvh2_traverse.restype = None
+    L.orc_build_bvh2.argtypes = [P, P, U64, P, ctypes.c_float, ctypes.c_float, I32, P]
+    L.orc_build_bvh2.restype = P
     L.orc_bvh2_to_cwbvh_exact.argtypes = [P, U64, P, U64, U32, I32, P, P, P, P]
     L.orc_bvh2_to_cwbvh_exact.restype = I32
     L.orc_cwbvh_order_children.argtypes = [P, U64, P, U64, P, P, U64, I32, ctypes.c_int64]
@@ -203,6 +211,66 @@ def cwbvh_order_children(nodes80, pidx, prim_aabbs, direct_layout=False, exact=N
     if r != 0:
         raise RuntimeError(f"oracle order_children failed: {r}")
     return nodes if ex is None else (nodes, ex)
+
+
+def collapse(nodes, pidx, max_prims, traversal_cost):
+    """collapse (src/bvh2/leaf_collapser.rs): (nodes32, primitive_indices)."""
+    nodes = np.ascontiguousarray(nodes, dtype=np.uint8).reshape(-1, 32).copy()
+    pidx = np.ascontiguousarray(pidx, dtype=np.uint32).copy()
+    counts = np.zeros(2, np.uint64)
+    lib().orc_bvh2_collapse(_p(nodes), len(nodes), _p(pidx), len(pidx), int(max_prims), float(traversal_cost),
+                            _p(counts))
+    return nodes[: int(counts[0])].copy(), pidx[: int(counts[1])].copy()
+
+
+def refit_all(nodes):
+    """Bvh2::refit_all (src/bvh2/mod.rs:527-570): returns the refit nodes."""
+    nodes = np.ascontiguousarray(nodes, dtype=np.uint8).reshape(-1, 32).copy()
+    lib().orc_bvh2_refit_all(_p(nodes), len(nodes))
+    return nodes
+
+
+def traverse_bvh2(nodes, pidx, tris, rays, mode=0, nthreads=1, counters=False):
+    """Bvh2::ray_traverse (mode 0: (original ids, 0xffffffff = none), t) or
+    ray_traverse_miss (mode 1: occluded flags) with Triangle::intersect."""
+    nodes = np.ascontiguousarray(nodes, dtype=np.uint8).reshape(-1, 32)
+    pidx = np.ascontiguousarray(pidx, dtype=np.uint32)
+    tris = _f32(tris, 9)
+    rays = _f32(rays, 8)
+    hits = np.zeros((len(rays), 2), np.uint32)
+    vis = np.zeros(1, np.uint64)
+    lib().orc_bvh2_traverse(mode, _p(nodes), len(nodes), _p(pidx), len(pidx), _p(tris), len(tris), _p(rays),
+                            len(rays), _p(hits), nthreads, _p(vis))
+    out = (hits[:, 0].copy(), hits[:, 1].copy().view(np.float32)) if mode == 0 else hits[:, 0].astype(bool)
+    return (out, int(vis[0])) if counters else out
+
+
+def build_bvh2(tris=None, aabbs=None, params=None, nthreads=1):
+    """build_bvh2_from_tris (tris) / build_bvh2 (aabbs), src/bvh2/builder.rs:
+    returns (nodes32, primitive_indices, max_depth, reinsertions applied)."""
+    from obvhs_gb300.params import BvhBuildParams
+
+    params = params or BvhBuildParams.medium_build()
+    p = OrcParams(int(params.pre_split) if tris is not None else 0, params.ploc_search_distance,
+                  params.search_depth_threshold, params.reinsertion_batch_ratio, params.sort_precision,
+                  params.max_prims_per_leaf)
+    L = lib()
+    st = I32(0)
+    src = _f32(tris, 9) if tris is not None else _f32(aabbs, 6)
+    h = L.orc_build_bvh2(_p(src) if tris is not None else None, _p(src) if tris is None else None, len(src),
+                         ctypes.byref(p), float(params.post_collapse_reinsertion_batch_ratio_multiplier),
+                         float(params.collapse_traversal_cost), nthreads, ctypes.byref(st))
+    try:
+        if st.value != 0:
+            raise RuntimeError(f"oracle build_bvh2 failed: {st.value}")
+        sz = np.zeros(8, np.uint64)
+        L.orc_build_sizes(h, _p(sz))
+        nodes = np.zeros((int(sz[2]), 32), np.uint8)
+        bp = np.zeros(int(sz[3]), np.uint32)  # collapsing keeps every primitive slot
+        L.orc_build_get_bvh2(h, 1, _p(nodes), _p(bp))
+        return nodes, bp, int(sz[7]), int(sz[6])
+    finally:
+        L.orc_free(h)
 
 
 def presplit(tris):

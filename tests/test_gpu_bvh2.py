@@ -1,0 +1,106 @@
+"""The BVH2 product on the GPU (leaf collapsing, build_bvh2_from_tris /
+build_bvh2, Bvh2::ray_traverse / ray_traverse_miss) against the oracle, bit
+for bit."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from obvhs_gb300 import scenes as S
+from obvhs_gb300 import test_util as T
+from obvhs_gb300.params import PRESETS, BvhBuildParams
+
+pytestmark = pytest.mark.gpu
+
+F32_MAX = np.finfo(np.float32).max
+EMPTY = np.array([[F32_MAX] * 3 + [-F32_MAX] * 3], np.float32)
+INF10 = np.array([[-np.inf] * 3 + [np.inf] * 3] * 10, np.float32)
+MAX10 = np.array([[-F32_MAX] * 3 + [F32_MAX] * 3] * 10, np.float32)
+NOTHING = np.zeros((0, 6), np.float32)
+
+
+@pytest.fixture(scope="module")
+def G():
+    import obvhs_gb300 as g
+
+    return g
+
+
+def _same(a, b):
+    return np.ascontiguousarray(a).tobytes() == np.ascontiguousarray(b).tobytes()
+
+
+def _rays(tris, n, seed):
+    v = tris.reshape(-1, 3)
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(v.min(0), v.max(0), size=(n, 3)).astype(np.float32)
+    d = T.uniform_sample_sphere(rng.random(n).astype(np.float32), rng.random(n).astype(np.float32))
+    return T.make_rays(o, d, 0.0, np.inf)
+
+
+@pytest.mark.parametrize("max_prims,cost", [(2, 1.0), (3, 3.0), (8, 3.0), (255, 1.0), (4, 0.0)])
+def test_collapse_matches_oracle(G, max_prims, cost):
+    tris = T.demoscene(64, 1)
+    aabbs = T.tri_aabbs(tris)
+    b2 = G.PlocBuilder().build_ploc(14, aabbs, None, 0, 0)
+    nodes, pidx = b2.download()
+    b2.collapse(max_prims, cost)
+    gn, gp = b2.download()
+    on, op = O.collapse(nodes, pidx, max_prims, cost)
+    assert _same(gn, on) and _same(gp, op)
+
+
+@pytest.mark.parametrize("preset", list(PRESETS))
+def test_build_bvh2_from_tris_matches_oracle(G, preset):
+    tris = S.scene2_tris(30_000, offset=5)
+    p = PRESETS[preset]()
+    b = G.build_bvh2_from_tris(tris, p)
+    gn, gp = b.download()
+    on, op, md, applied = O.build_bvh2(tris=tris, params=p, nthreads=8)
+    assert _same(gn, on) and _same(gp, op)
+    assert b.max_depth == md
+    assert b.stats.reinsertions == applied
+    rays = _rays(tris, 20_000, 3)
+    ids, t = b.ray_traverse(rays)
+    oid, ot = O.traverse_bvh2(on, op, tris, rays, nthreads=8)
+    assert np.array_equal(ids, oid)
+    assert np.array_equal(t.view(np.uint32), ot.view(np.uint32))
+    assert np.array_equal(b.ray_traverse_miss(rays), ~O.traverse_bvh2(on, op, tris, rays, mode=1, nthreads=8))
+
+
+@pytest.mark.parametrize("preset", ["fastest", "medium", "very_slow"])
+@pytest.mark.parametrize("aabbs", [EMPTY, INF10, MAX10, NOTHING], ids=["empty", "inf", "max", "nothing"])
+def test_degenerate_build_bvh2_misses(G, preset, aabbs):
+    """build_bvh2_with_{empty_aabb,many_inf,many_max,nothing} (tests/mod.rs:34-78)."""
+    p = PRESETS[preset]()
+    b = G.build_bvh2(aabbs, p)
+    gn, gp = b.download()
+    on, op, _, _ = O.build_bvh2(aabbs=aabbs, params=p)
+    assert _same(gn, on) and _same(gp, op)
+    b.set_triangles(np.zeros((len(aabbs), 9), np.float32))  # triangles that never hit
+    ids, _ = b.ray_traverse(T.make_rays([[0, 0, 1]], [[0, 0, -1]]))
+    assert ids[0] == 0xFFFFFFFF
+
+
+def test_varying_prim_counts_build_bvh2(G):
+    """build_bvh_with_varying_prim_counts (tests/mod.rs:90-102), BVH2 half."""
+    tris_all = T.height_to_triangles(T.flat_heights(4, 4), 4, 4)
+    for n in range(len(tris_all) - 1, 0, -4):
+        tris = tris_all[:n]
+        for preset in PRESETS:
+            p = PRESETS[preset]()
+            gn, gp = G.build_bvh2_from_tris(tris, p).download()
+            on, op, _, _ = O.build_bvh2(tris=tris, params=p)
+            assert _same(gn, on) and _same(gp, op), (n, preset)
+
+
+def test_large_bvh2_build_and_traversal(G):
+    tris = S.scene2_tris(1_000_000)
+    p = BvhBuildParams.medium_build()
+    b = G.build_bvh2_from_tris(tris, p)
+    on, op, _, _ = O.build_bvh2(tris=tris, params=p, nthreads=16)
+    gn, gp = b.download()
+    assert _same(gn, on) and _same(gp, op)
+    rays = _rays(tris, 100_000, 8)
+    ids, t = b.ray_traverse(rays)
+    oid, ot = O.traverse_bvh2(on, op, tris, rays, nthreads=16)
+    assert np.array_equal(ids, oid) and np.array_equal(t.view(np.uint32), ot.view(np.uint32))

@@ -346,3 +346,74 @@ def test_exact_aabbs_contained_in_the_compressed_boxes():
                                  r[0:12].view(np.float32) + (r[12:15].astype(np.uint32) << 23).view(np.float32)
                                  * np.float32(255.0)))(n2.view(np.uint8)[i])
         assert np.all(e2[i, :3] >= smin - 1e-5) and np.all(e2[i, 3:] <= smax + 1e-5)
+
+
+# --- the BVH2 product: collapse, build_bvh2, Bvh2 traversal ---------------------
+
+
+@pytest.mark.parametrize("preset", ALL)
+@pytest.mark.parametrize("aabbs", [EMPTY, INF10, MAX10, NOTHING], ids=["empty", "inf", "max", "nothing"])
+def test_degenerate_build_bvh2_misses(preset, aabbs):
+    """build_bvh2_with_{empty_aabb,many_inf,many_max,nothing} (tests/mod.rs:34-78)
+    through the whole builder (reinsertion, collapse, reinsertion): valid,
+    and the ray of the test misses."""
+    nodes, pidx, md, _ = O.build_bvh2(aabbs=aabbs, params=PRESETS[preset]())
+    if len(nodes):
+        assert O.validate_bvh2(nodes, pidx, md, aabbs)[0] == 0
+    ray = T.make_rays([[0, 0, 1]], [[0, 0, -1]])
+    dummy = np.zeros((max(len(aabbs), 1), 9), np.float32)  # triangles that never hit
+    ids, _ = O.traverse_bvh2(nodes, pidx, dummy, ray)
+    assert ids[0] == 0xFFFFFFFF
+    assert not O.traverse_bvh2(nodes, pidx, dummy, ray, mode=1)[0]
+
+
+def test_varying_prim_counts_build_bvh2_validate():
+    """build_bvh_with_varying_prim_counts (tests/mod.rs:90-102), the BVH2
+    half: build_bvh2_from_tris for every prefix of a 32-triangle grid and
+    every preset validates (tight boxes unless pre-split)."""
+    tris_all = T.height_to_triangles(T.flat_heights(4, 4), 4, 4)
+    for n in range(len(tris_all) - 1, 0, -1):
+        tris = tris_all[:n]
+        aabbs = T.tri_aabbs(tris)
+        for preset in ALL:
+            p = PRESETS[preset]()
+            nodes, pidx, md, _ = O.build_bvh2(tris=tris, params=p)
+            r, _ = O.validate_bvh2(nodes, pidx, md, aabbs, tight=not p.pre_split, splits=p.pre_split)
+            assert r == 0, (n, preset, r)
+
+
+@pytest.mark.parametrize("max_prims", [2, 3, 8, 255])
+def test_collapse_keeps_every_primitive(max_prims):
+    tris = T.demoscene(32, 0)
+    aabbs = T.tri_aabbs(tris)
+    nodes, pidx, md, _ = O.ploc(aabbs, search_distance=14)
+    cn, cp = O.collapse(nodes, pidx, max_prims, 1.0)
+    assert sorted(cp.tolist()) == sorted(pidx.tolist())
+    assert len(cn) < len(nodes)
+    counts = cn[:, 12:16].copy().view(np.uint32).ravel()
+    assert counts.max() <= max_prims
+    assert O.validate_bvh2(cn, cp, md, aabbs)[0] == 0
+
+
+def test_bvh2_and_cwbvh_traversal_agree():
+    """The same scene through build_bvh2_from_tris + Bvh2::ray_traverse and
+    build_cwbvh_from_tris + CwBvh::ray_traverse: the same closest t for every
+    ray (ids agree wherever the closest hit is unique), the same occlusion."""
+    tris = T.demoscene(64, 3)
+    rng = np.random.default_rng(4)
+    v = tris.reshape(-1, 3)
+    o = rng.uniform(v.min(0), v.max(0), size=(4000, 3)).astype(np.float32)
+    o[:, 1] = v[:, 1].max() + 1.0
+    d = T.normalize3(rng.uniform(-1, 1, size=(4000, 3)).astype(np.float32) * np.float32([0.3, 1, 0.3]) -
+                     np.float32([0, 1, 0]))
+    rays = T.make_rays(o, d, 0.0, np.inf)
+    p = BvhBuildParams.medium_build()
+    nodes, pidx, _, _ = O.build_bvh2(tris=tris, params=p)
+    b2_ids, b2_t = O.traverse_bvh2(nodes, pidx, tris, rays)
+    cw = O.build(tris=tris, params=p)
+    cw_ids, cw_t, _ = O.traverse(cw.cw_nodes, cw.cw_pidx, tris, rays)
+    assert (b2_ids != 0xFFFFFFFF).mean() > 0.5
+    assert np.array_equal(b2_t.view(np.uint32), cw_t.view(np.uint32))
+    assert (b2_ids == cw_ids).mean() > 0.999
+    occ = O.traverse_bvh2(nodes, pidx, tris, rays, mode=1)
+    assert np.array_equal(occ, b2_ids != 0xFFFFFFFF)
