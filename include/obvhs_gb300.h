@@ -197,6 +197,25 @@ OBVHS_API int obvhs_bvh2_ray_traverse(obvhs_ctx* ctx, const obvhs_bvh2* bvh, con
 OBVHS_API int obvhs_bvh2_ray_traverse_miss(obvhs_ctx* ctx, const obvhs_bvh2* bvh, const obvhs_ray* rays, uint32_t n,
                                            uint8_t* miss, int device_ptrs);
 
+/* ---- dynamic updates ------------------------------------------------------- */
+/* Bvh2Node::set_aabb for n nodes: node_ids[i] gets aabbs[i] (min xyz, max xyz);
+ * the tree above them is stale until obvhs_bvh2_refit_all or a rebuild. */
+OBVHS_API int obvhs_bvh2_set_node_aabbs(obvhs_ctx* ctx, obvhs_bvh2* bvh, const uint32_t* node_ids, const float* aabbs,
+                                        uint32_t n, int device_ptrs);
+/* Bvh2::refit_all (src/bvh2/mod.rs:527-570): every inner box from its children. */
+OBVHS_API int obvhs_bvh2_refit_all(obvhs_ctx* ctx, obvhs_bvh2* bvh);
+/* PlocBuilder::full_rebuild (src/ploc/rebuild.rs:53-81): PLOC over the current
+ * leaves (node order), the old root box as the Morton frame. */
+OBVHS_API int obvhs_bvh2_full_rebuild(obvhs_ctx* ctx, obvhs_bvh2* bvh, uint32_t search_distance,
+                                      uint32_t sort_precision, uint32_t search_depth_threshold);
+/* compute_rebuild_path_flags of the given leaf node ids + PlocBuilder::
+ * partial_rebuild (src/ploc/rebuild.rs:12-134): the flagged leaves and the
+ * untouched subtrees below flagged nodes re-clustered into the freed slots;
+ * node bytes identical to the reference's. */
+OBVHS_API int obvhs_bvh2_partial_rebuild(obvhs_ctx* ctx, obvhs_bvh2* bvh, const uint32_t* leaves, uint32_t n_leaves,
+                                         uint32_t search_distance, uint32_t sort_precision,
+                                         uint32_t search_depth_threshold, int device_ptrs);
+
 /* bvh2_to_cwbvh with include_exact_node_aabbs (src/cwbvh/bvh2_to_cwbvh.rs:
  * 490-510, :76-80): the CWBVH also keeps, per node, the exact box of the BVH2
  * node it came from (read with obvhs_cwbvh_exact_node_aabbs; used and moved

@@ -87,6 +87,10 @@ SIGNATURES = {
     "obvhs_bvh2_set_triangles": (I32, [P, P, P, U32, I32]),
     "obvhs_bvh2_ray_traverse": (I32, [P, P, P, U32, P, I32]),
     "obvhs_bvh2_ray_traverse_miss": (I32, [P, P, P, U32, P, I32]),
+    "obvhs_bvh2_set_node_aabbs": (I32, [P, P, P, P, U32, I32]),
+    "obvhs_bvh2_refit_all": (I32, [P, P]),
+    "obvhs_bvh2_full_rebuild": (I32, [P, P, U32, U32, U32]),
+    "obvhs_bvh2_partial_rebuild": (I32, [P, P, P, U32, U32, U32, U32, I32]),
     "obvhs_bvh2_to_cwbvh": (I32, [P, P, U32, I32, ctypes.POINTER(P)]),
     "obvhs_bvh2_to_cwbvh_ex": (I32, [P, P, U32, I32, I32, ctypes.POINTER(P)]),
     "obvhs_cwbvh_exact_node_aabbs": (I32, [P, P, P]),

@@ -205,6 +205,33 @@ class Bvh2:
         self.ctx.check(self.ctx.lib.obvhs_bvh2_set_triangles(self.ctx.h, self.h, p, n, dev))
         del keep
 
+    def set_node_aabbs(self, node_ids, aabbs):
+        """Bvh2Node::set_aabb for the given nodes (e.g. moved leaves)."""
+        pi, n, dev, ki = _prep(node_ids, np.uint32, 0)
+        pa, na, deva, ka = _prep(aabbs, np.float32, 6)
+        if na != n or deva != dev:
+            raise ValueError("one box per node id, same memory space")
+        self.ctx.check(self.ctx.lib.obvhs_bvh2_set_node_aabbs(self.ctx.h, self.h, pi, pa, n, dev))
+        del ki, ka
+
+    def refit_all(self):
+        """Bvh2::refit_all (src/bvh2/mod.rs:527-570)."""
+        self.ctx.check(self.ctx.lib.obvhs_bvh2_refit_all(self.ctx.h, self.h))
+
+    def full_rebuild(self, search_distance, sort_precision=0, search_depth_threshold=0):
+        """PlocBuilder::full_rebuild (src/ploc/rebuild.rs:53-81)."""
+        self.ctx.check(self.ctx.lib.obvhs_bvh2_full_rebuild(self.ctx.h, self.h, int(search_distance),
+                                                            int(sort_precision), int(search_depth_threshold)))
+
+    def partial_rebuild(self, leaves, search_distance, sort_precision=0, search_depth_threshold=0):
+        """compute_rebuild_path_flags(leaves) + PlocBuilder::partial_rebuild
+        (src/ploc/rebuild.rs:12-134); `leaves` are leaf node ids."""
+        pl, n, dev, keep = _prep(leaves, np.uint32, 0)
+        self.ctx.check(self.ctx.lib.obvhs_bvh2_partial_rebuild(self.ctx.h, self.h, pl, n, int(search_distance),
+                                                               int(sort_precision), int(search_depth_threshold),
+                                                               dev))
+        del keep
+
     def ray_traverse(self, rays, out=None):
         """Closest hit per ray (Bvh2::ray_traverse with Triangle::intersect):
         (original ids, 0xffffffff = miss; t, +inf = miss), or an int32 (n, 2)

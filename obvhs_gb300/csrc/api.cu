@@ -1253,6 +1253,62 @@ int obvhs_bvh2_ray_traverse_miss(obvhs_ctx* cp, const obvhs_bvh2* b, const obvhs
   return bvh2_traverse_common(cp, b, rays, n, miss, device_ptrs, 1);
 }
 
+int obvhs_bvh2_set_node_aabbs(obvhs_ctx* cp, obvhs_bvh2* b, const uint32_t* node_ids, const float* aabbs,
+                              uint32_t n, int device_ptrs) {
+  if (!cp || !b || (n && (!node_ids || !aabbs))) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  int err = 0;
+  const uint32_t* di = (const uint32_t*)stage_in(c, SLOT_INPUT2, node_ids, (size_t)n * 4, device_ptrs, &err);
+  if (err) return err;
+  const float* da = (const float*)stage_in(c, SLOT_INPUT, aabbs, (size_t)n * 24, device_ptrs, &err);
+  if (err) return err;
+  int r = bvh2_set_node_aabbs_device(c, b, di, da, n);
+  if (!r) r = take_status(c);
+  return r;
+}
+
+int obvhs_bvh2_refit_all(obvhs_ctx* cp, obvhs_bvh2* b) {
+  if (!cp || !b) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  int r = bvh2_refit_all_device(c, b);
+  if (!r) r = take_status(c);
+  return r;
+}
+
+int obvhs_bvh2_full_rebuild(obvhs_ctx* cp, obvhs_bvh2* b, uint32_t search_distance, uint32_t sort_precision,
+                            uint32_t search_depth_threshold) {
+  if (!cp || !b) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  BuildScope building(c.device);
+  if (search_distance < 1 || search_distance > 32) return c.fail(OBVHS_ERR_INVALID_ARG, "search distance must be 1..32");
+  if (sort_precision > 1) return c.fail(OBVHS_ERR_INVALID_ARG, "sort_precision must be 0 or 1");
+  int r = bvh2_rebuild_device(c, b, nullptr, 0, search_distance, (int)sort_precision, search_depth_threshold);
+  if (!r) r = take_status(c);
+  return r;
+}
+
+int obvhs_bvh2_partial_rebuild(obvhs_ctx* cp, obvhs_bvh2* b, const uint32_t* leaves, uint32_t n_leaves,
+                               uint32_t search_distance, uint32_t sort_precision, uint32_t search_depth_threshold,
+                               int device_ptrs) {
+  if (!cp || !b || (n_leaves && !leaves)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  BuildScope building(c.device);
+  if (search_distance < 1 || search_distance > 32) return c.fail(OBVHS_ERR_INVALID_ARG, "search distance must be 1..32");
+  if (sort_precision > 1) return c.fail(OBVHS_ERR_INVALID_ARG, "sort_precision must be 0 or 1");
+  int err = 0;
+  const uint32_t* dl = (const uint32_t*)stage_in(c, SLOT_INPUT2, leaves, (size_t)n_leaves * 4, device_ptrs, &err);
+  if (err) return err;
+  static const uint32_t none = 0;
+  int r = bvh2_rebuild_device(c, b, n_leaves ? dl : &none, n_leaves, search_distance, (int)sort_precision,
+                              search_depth_threshold);
+  if (!r) r = take_status(c);
+  return r;
+}
+
 int obvhs_cwbvh_exact_node_aabbs(obvhs_ctx* cp, const obvhs_cwbvh* b, float* aabbs6) {
   if (!cp || !b || (b->n_nodes && !aabbs6)) return OBVHS_ERR_INVALID_ARG;
   BuildCtx& c = *cp;

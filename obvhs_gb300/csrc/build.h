@@ -256,7 +256,7 @@ int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_
 // asynchronously and passes_out / sum_counts_out are left unset.
 int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* total_keys, uint32_t radius,
                       int precision, uint32_t depth_threshold, Bvh2Node* out_nodes, uint32_t* passes_out,
-                      uint64_t* sum_counts_out, PlocState* deferred = nullptr);
+                      uint64_t* sum_counts_out, PlocState* deferred = nullptr, const uint32_t* remap = nullptr);
 int ploc_setup_kernels();
 
 // Segmented builds: many scenes through every stage together, one launch
@@ -351,6 +351,14 @@ int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint
 int reorder_tris_device(BuildCtx& c, obvhs_cwbvh* bvh, const float* tris, uint32_t n_tris);
 // The BVH2 product (src/bvh2/builder.rs, leaf_collapser.rs, mod.rs:148-337).
 int bvh2_collapse_device(BuildCtx& c, obvhs_bvh2* b, uint32_t max_prims, float traversal_cost);
+// Bvh2Node::set_aabb (src/bvh2/node.rs) for m nodes (ids, boxes n x 6: device).
+int bvh2_set_node_aabbs_device(BuildCtx& c, obvhs_bvh2* b, const uint32_t* d_ids, const float* d_aabbs, uint32_t m);
+// Bvh2::refit_all (src/bvh2/mod.rs:527-570).
+int bvh2_refit_all_device(BuildCtx& c, obvhs_bvh2* b);
+// PlocBuilder::full_rebuild (d_leaves null) or partial_rebuild of the rebuild
+// path flags of the given leaf node ids (device array), src/ploc/rebuild.rs.
+int bvh2_rebuild_device(BuildCtx& c, obvhs_bvh2* b, const uint32_t* d_leaves, uint32_t n_leaves, uint32_t radius,
+                        int precision, uint32_t depth_threshold);
 int bvh2_reorder_tris_device(BuildCtx& c, obvhs_bvh2* b, const float* tris, uint32_t n_tris);
 int bvh2_traverse_device(BuildCtx& c, const obvhs_bvh2* b, const float* rays, uint32_t n, uint32_t* hits,
                          uint8_t* miss, int mode);

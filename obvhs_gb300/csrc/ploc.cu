@@ -356,6 +356,7 @@ struct PlocCoopArgs {
   uint32_t depth_threshold;
   uint32_t max_passes;
   uint32_t* status;
+  const uint32_t* remap;  // partial rebuild: left slot of every merged pair (else null)
 };
 
 struct CoopGroupSmem {
@@ -473,7 +474,7 @@ __device__ __forceinline__ void ploc_tile_offsets(CoopGroupSmem& sm, int group, 
 __device__ __forceinline__ uint2 ploc_tile_write(CoopGroupSmem& sm, int group, const Bvh2Node* cur, Bvh2Node* next,
                                                  Bvh2Node* out, const int8_t* merge, uint32_t count, uint32_t base,
                                                  int ipt, const uint2* tile_cnt, uint32_t t_first, uint32_t tile,
-                                                 uint32_t ins_top) {
+                                                 uint32_t ins_top, const uint32_t* remap = nullptr) {
   const int tid = threadIdx.x % PT, lane = tid & 31, warp = tid >> 5;
   uint32_t pe = 0, pm = 0;
   for (uint32_t t = t_first + tid; t < tile; t += PT) {
@@ -534,7 +535,8 @@ __device__ __forceinline__ uint2 ploc_tile_write(CoopGroupSmem& sm, int group, c
     if (ism[k]) {
       const Bvh2Node left = ld_node_cg(&cur[i]);
       const Bvh2Node right = ld_node_cg(&cur[bst[k]]);
-      const uint32_t ins = ins_top - 2 * (mpos + 1);
+      uint32_t ins = ins_top - 2 * (mpos + 1);
+      if (remap) ins = __ldg(&remap[(ins - 1) >> 1]);  // the k-th free pair of a partial rebuild
       st_node(&out[ins], left);
       st_node(&out[ins + 1], right);
       st_node(&next[epos], make_node(box_union(node_box(left), node_box(right)), 0, ins));
@@ -588,7 +590,7 @@ __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs 
     const uint32_t ins_top = *(volatile uint32_t*)&a.st->insert[parity];
     for (uint32_t tile = first_tile; tile < ntiles; tile += tile_step) {
       const uint2 tot = ploc_tile_write(sm, group, cur, next, a.out, a.merge, count, tile * chunk, ipt, a.tile_cnt, 0,
-                                        tile, ins_top);
+                                        tile, ins_top, a.remap);
       if (tid == 0 && tile == ntiles - 1) {
         a.st->count[parity ^ 1] = tot.x;
         a.st->insert[parity ^ 1] = ins_top - 2 * tot.y;
@@ -800,7 +802,8 @@ __device__ __forceinline__ Box sbox(const float4* s, uint32_t j) {
 __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __restrict__ buf0,
                                                             const Bvh2Node* __restrict__ buf1, PlocState* st,
                                                             int radius, uint32_t depth_threshold, uint32_t max_passes,
-                                                            Bvh2Node* __restrict__ out, uint32_t* status) {
+                                                            Bvh2Node* __restrict__ out, uint32_t* status,
+                                                            const uint32_t* __restrict__ remap) {
   extern __shared__ float4 smem[];
   float4* sa = smem;                      // TAIL_MAX nodes (2 float4 each)
   float4* sb = smem + 2 * TAIL_MAX;       // TAIL_MAX nodes
@@ -925,6 +928,7 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
         float4 la = cur[2 * i], lb = cur[2 * i + 1];
         float4 ra = cur[2 * bst[k]], rb = cur[2 * bst[k] + 1];
         uint32_t ins = insert - 2 * (mpos + 1);
+        if (remap) ins = remap[(ins - 1) >> 1];
         float4* o = reinterpret_cast<float4*>(&out[ins]);
         o[0] = la;
         o[1] = lb;
@@ -1015,7 +1019,7 @@ int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_
 
 int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* total_keys, uint32_t radius,
                       int precision, uint32_t depth_threshold, Bvh2Node* out_nodes, uint32_t* passes_out,
-                      uint64_t* sum_counts_out, PlocState* deferred) {
+                      uint64_t* sum_counts_out, PlocState* deferred, const uint32_t* remap) {
   *passes_out = 0;
   *sum_counts_out = 0;
   if (n == 0) return 0;
@@ -1053,7 +1057,8 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
       coop_blocks = std::max(1, per_sm) * c.num_sms;
       coop_blocks_s.store(coop_blocks);
     }
-    PlocCoopArgs pa{{cur, nxt}, out_nodes, st, merge, tile_cnt, (int)radius, depth_threshold, max_passes, c.d_status};
+    PlocCoopArgs pa{{cur, nxt}, out_nodes, st, merge, tile_cnt, (int)radius, depth_threshold, max_passes, c.d_status,
+                    remap};
     void* args[] = {&pa};
     if (gpu_shared(c) && n <= SHARED_SINGLE_BLOCK_MAX) {
       // the GPU is shared with other builds or work: one block, a normal
@@ -1067,7 +1072,7 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   {
     const size_t smem = (size_t)4 * TAIL_MAX * sizeof(float4) + TAIL_MAX + 64;
     KLAUNCH("k_ploc_tail", k_ploc_tail<<<1, TAIL_THREADS, smem, c.stream>>>(cur, nxt, st, (int)radius, depth_threshold,
-                                                                           max_passes, out_nodes, c.d_status));
+                                                                           max_passes, out_nodes, c.d_status, remap));
     CK(cudaGetLastError());
   }
   if (deferred) {

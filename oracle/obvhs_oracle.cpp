@@ -369,9 +369,12 @@ inline int8_t find_best_node(size_t index, const Node* nodes, size_t count, size
 }
 
 // leaves: Bvh2Node::new(aabb,1,indices[i]); total: leaf-init total AABB.
+// rebuild (partial_rebuild, src/ploc/rebuild.rs:98-134 and src/ploc/mod.rs:
+// 276-281,447-459): the tree keeps its size and merged pairs go to the
+// invalidated child pairs, scanning down from the top of the array.
 void ploc_from_leaves(Bvh2& bvh, std::vector<Node> cur, const Aabb& total, size_t sd, int precision,
                       size_t depth_threshold, int nthreads, PlocStats* st,
-                      std::vector<uint64_t>* codes_out, std::vector<uint32_t>* order_out) {
+                      std::vector<uint64_t>* codes_out, std::vector<uint32_t>* order_out, bool rebuild = false) {
   size_t n = cur.size();
   if (st) {
     st->passes = 0;
@@ -379,8 +382,14 @@ void ploc_from_leaves(Bvh2& bvh, std::vector<Node> cur, const Aabb& total, size_
   }
   if (n == 0) return;
   size_t nodes_count = 2 * n - 1;
-  bvh.nodes.assign(nodes_count, Node{Aabb{v3(0, 0, 0), v3(0, 0, 0)}, 0, 0});
-  size_t insert_index = nodes_count;
+  size_t insert_index;
+  if (rebuild) {
+    if (bvh.nodes.empty()) return;
+    insert_index = bvh.nodes.size() - 1;
+  } else {
+    bvh.nodes.assign(nodes_count, Node{Aabb{v3(0, 0, 0), v3(0, 0, 0)}, 0, 0});
+    insert_index = nodes_count;
+  }
 
   std::vector<uint32_t> order;
   morton_sort(cur, total, precision, nthreads, order, codes_out);
@@ -427,13 +436,29 @@ void ploc_from_leaves(Bvh2& bvh, std::vector<Node> cur, const Aabb& total, size_
       }
       Node left = cur[index];
       Node right = cur[best_index];
-      insert_index -= 2;
-      bvh.nodes[insert_index] = left;
-      bvh.nodes[insert_index + 1] = right;
+      size_t first_child;
+      if (rebuild) {
+        for (;;) {  // the next invalidated pair from the top
+          if (insert_index < 2) return;  // more merges than free pairs: malformed flags
+          if (bvh.nodes[insert_index - 1].prim_count & 0x80000000u) {
+            bvh.nodes[insert_index - 1] = left;
+            bvh.nodes[insert_index] = right;
+            first_child = insert_index - 1;
+            insert_index -= 2;
+            break;
+          }
+          insert_index -= 2;
+        }
+      } else {
+        insert_index -= 2;
+        bvh.nodes[insert_index] = left;
+        bvh.nodes[insert_index + 1] = right;
+        first_child = insert_index;
+      }
       Node parent;
       parent.box = uni(left.box, right.box);
       parent.prim_count = 0;
-      parent.first_index = (uint32_t)insert_index;
+      parent.first_index = (uint32_t)first_child;
       next[next_idx++] = parent;
       index++;
     }
@@ -1725,6 +1750,59 @@ void refit_all(Bvh2& b) {
   }
 }
 
+// compute_rebuild_path_flags (src/ploc/rebuild.rs:12-43): the given leaves
+// and every node on their paths to the root.
+void compute_rebuild_path_flags(Bvh2& b, const uint32_t* leaves, size_t n_leaves, std::vector<uint8_t>& flags) {
+  if (b.nodes.size() < 2) return;
+  compute_parents(b.nodes, b.parents);
+  flags.assign(b.nodes.size(), 0);
+  for (size_t k = 0; k < n_leaves; k++) {
+    size_t idx = leaves[k];
+    flags[idx] = 1;
+    while (idx > 0) {
+      idx = b.parents[idx];
+      if (flags[idx]) break;
+      flags[idx] = 1;
+    }
+  }
+}
+
+// PlocBuilder::partial_rebuild (src/ploc/rebuild.rs:98-134): the flagged
+// leaves and the unflagged subtrees hanging off flagged nodes, collected
+// top-down (a stack of child pairs), rebuilt into the invalidated slots.
+void partial_rebuild(Bvh2& b, const std::vector<uint8_t>& flags, size_t sd, int precision, size_t threshold) {
+  if (b.nodes.size() < 2) return;
+  std::vector<Node> cur;
+  std::vector<uint32_t> st{b.nodes[0].first_index};
+  while (!st.empty()) {
+    uint32_t l = st.back();
+    st.pop_back();
+    for (uint32_t ni : {l, l + 1}) {
+      Node& n = b.nodes[ni];
+      if (!flags[ni] || n.is_leaf())
+        cur.push_back(n);
+      else
+        st.push_back(n.first_index);
+      n.prim_count |= 0x80000000u;  // set_invalid
+    }
+  }
+  const Aabb total = b.nodes[0].box;
+  ploc_from_leaves(b, std::move(cur), total, sd, precision, threshold, 1, nullptr, nullptr, nullptr, true);
+  b.parents.clear();
+}
+
+// PlocBuilder::full_rebuild (src/ploc/rebuild.rs:53-81): every leaf, in node
+// order, rebuilt from scratch with the old root box as the Morton frame.
+void full_rebuild(Bvh2& b, size_t sd, int precision, size_t threshold) {
+  if (b.nodes.size() < 2) return;
+  std::vector<Node> cur;
+  for (const Node& n : b.nodes)
+    if (n.is_leaf()) cur.push_back(n);
+  const Aabb total = b.nodes[0].box;
+  ploc_from_leaves(b, std::move(cur), total, sd, precision, threshold, 1, nullptr, nullptr, nullptr, false);
+  b.parents.clear();
+}
+
 // ---------------------------------------------------------------------------
 struct BuildResult {
   std::vector<CwNode> cw_nodes;
@@ -1998,6 +2076,23 @@ void* orc_build_bvh2(const float* tris, const float* aabbs6, uint64_t n, const o
   r->reins_stats.applied += second.applied;
   if (status) *status = rc;
   return r;
+}
+
+// full_rebuild (n_leaves < 0) or partial_rebuild of the flagged paths of the
+// given leaves, in place (the node count does not change); returns max_depth.
+int64_t orc_bvh2_rebuild(void* nodes32, uint64_t n_nodes, const uint32_t* leaves, int64_t n_leaves, uint32_t sd,
+                         uint32_t precision, uint32_t threshold) {
+  Bvh2 b = load_bvh2(nodes32, n_nodes, nullptr, 0, 96);
+  if (n_leaves < 0) {
+    full_rebuild(b, sd, (int)precision, threshold);
+  } else {
+    std::vector<uint8_t> flags;
+    compute_rebuild_path_flags(b, leaves, (size_t)n_leaves, flags);
+    partial_rebuild(b, flags, sd, (int)precision, threshold);
+  }
+  NodeX* o = (NodeX*)nodes32;
+  for (size_t i = 0; i < b.nodes.size(); i++) o[i] = to_x(b.nodes[i]);
+  return b.max_depth;
 }
 
 // Pre-splits: returns a handle; orc_presplit_get copies out.

@@ -78,6 +78,8 @@ def _declare(L):
     L.orc_bvh2_to_cwbvh.restype = I32
     L.orc_bvh2_collapse.argtypes = [P, U64, P, U64, U32, ctypes.c_float, P]
     L.orc_bvh2_collapse.restype = I32
+    L.orc_bvh2_rebuild.argtypes = [P, U64, P, ctypes.c_int64, U32, U32, U32]
+    L.orc_bvh2_rebuild.restype = ctypes.c_int64
     L.orc_bvh2_refit_all.argtypes = [P, U64]
     L.orc_bvh2_refit_all.restype = None
     L.orc_bvh2_traverse.argtypes = [I32, P, U64, P, U64, P, U64, P, U64, P, I32, P]
@@ -221,6 +223,17 @@ def collapse(nodes, pidx, max_prims, traversal_cost):
     lib().orc_bvh2_collapse(_p(nodes), len(nodes), _p(pidx), len(pidx), int(max_prims), float(traversal_cost),
                             _p(counts))
     return nodes[: int(counts[0])].copy(), pidx[: int(counts[1])].copy()
+
+
+def rebuild(nodes, leaves=None, search_distance=1, sort_precision=0, search_depth_threshold=0):
+    """PlocBuilder::full_rebuild (leaves None) or partial_rebuild with the
+    rebuild path flags of `leaves`: (nodes, max_depth)."""
+    nodes = np.ascontiguousarray(nodes, dtype=np.uint8).reshape(-1, 32).copy()
+    lv = None if leaves is None else np.ascontiguousarray(leaves, dtype=np.uint32)
+    md = lib().orc_bvh2_rebuild(_p(nodes), len(nodes), _p(lv) if lv is not None else None,
+                                -1 if lv is None else len(lv), int(search_distance), int(sort_precision),
+                                int(search_depth_threshold))
+    return nodes, int(md)
 
 
 def refit_all(nodes):

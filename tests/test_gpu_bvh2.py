@@ -104,3 +104,86 @@ def test_large_bvh2_build_and_traversal(G):
     ids, t = b.ray_traverse(rays)
     oid, ot = O.traverse_bvh2(on, op, tris, rays, nthreads=16)
     assert np.array_equal(ids, oid) and np.array_equal(t.view(np.uint32), ot.view(np.uint32))
+
+
+# --- dynamic updates: refit_all, full / partial rebuild ------------------------------
+
+
+def _leaf_ids(nodes):
+    return np.nonzero(nodes[:, 12:16].copy().view(np.uint32).ravel() != 0)[0].astype(np.uint32)
+
+
+def _moved(nodes, pidx, aabbs, frac, seed, shift=0.3):
+    """A copy of the tree with `frac` of its leaves shifted (and the boxes)."""
+    leaves = _leaf_ids(nodes)
+    rng = np.random.default_rng(seed)
+    moved = np.sort(rng.choice(leaves, size=max(1, int(len(leaves) * frac)), replace=False)).astype(np.uint32)
+    nn = nodes.copy()
+    boxes = np.zeros((len(moved), 6), np.float32)
+    for k, i in enumerate(moved):
+        f = nn[i].view(np.float32)
+        f[[0, 1, 2, 4, 5, 6]] += np.float32(shift)
+        boxes[k] = f[[0, 1, 2, 4, 5, 6]]
+    return nn, moved, boxes
+
+
+def test_refit_all_matches_oracle(G):
+    tris = S.scene2_tris(200_000, offset=2)
+    b = G.build_bvh2_from_tris(tris, BvhBuildParams.medium_build())
+    nodes, pidx = b.download()
+    nn, moved, boxes = _moved(nodes, pidx, None, 0.05, 1)
+    b.set_node_aabbs(moved, boxes)
+    assert _same(b.download()[0], nn)
+    b.refit_all()
+    assert _same(b.download()[0], O.refit_all(nn))
+
+
+@pytest.mark.parametrize("radius,thr", [(1, 1), (14, 0), (24, 2)])
+def test_full_rebuild_matches_oracle(G, radius, thr):
+    tris = S.scene2_tris(100_000, offset=3)
+    b = G.build_bvh2_from_tris(tris, BvhBuildParams.slow_build())  # collapsed, multi-primitive leaves
+    nodes, _ = b.download()
+    b.full_rebuild(radius, 0, thr)
+    on, omd = O.rebuild(nodes, None, radius, 0, thr)
+    assert _same(b.download()[0], on)
+    assert b.max_depth == omd
+
+
+@pytest.mark.parametrize("which", ["all", "one", "random", "moved"])
+def test_partial_rebuild_matches_oracle(G, which):
+    tris = S.scene2_tris(60_000, offset=4)
+    aabbs = T.tri_aabbs(tris)
+    b = G.PlocBuilder().build_ploc(14, aabbs, None, 0, 0)
+    nodes, pidx = b.download()
+    leaves = _leaf_ids(nodes)
+    if which == "all":
+        pick = leaves
+    elif which == "one":
+        pick = leaves[:1]
+    elif which == "random":
+        pick = np.array([i for i in leaves[:5000] if T.hash_noise(0, 0, int(i)) > 0.5], np.uint32)
+    else:
+        nodes, pick, boxes = _moved(nodes, pidx, aabbs, 0.05, 7)
+        b.set_node_aabbs(pick, boxes)
+        aabbs = aabbs.copy()  # the moved leaves' primitives moved with them
+        for i, box in zip(pick, boxes):
+            aabbs[pidx[nodes[i, 28:32].view(np.uint32)[0]]] = box
+    b.partial_rebuild(pick, 14, 0, 0)
+    on, omd = O.rebuild(nodes, pick, 14, 0, 0)
+    assert _same(b.download()[0], on)
+    assert b.max_depth == omd
+    assert O.validate_bvh2(on, pidx, omd, aabbs)[0] == 0
+
+
+def test_partial_rebuild_large(G):
+    """Every leaf of a 1M-leaf tree through the partial rebuild (the largest
+    collection the top-down walk can meet)."""
+    tris = S.scene2_tris(1_000_000)
+    aabbs = T.tri_aabbs(tris)
+    b = G.PlocBuilder().build_ploc(14, aabbs, None, 0, 0)
+    nodes, pidx = b.download()
+    nn, moved, boxes = _moved(nodes, pidx, aabbs, 0.01, 9)
+    b.set_node_aabbs(moved, boxes)
+    b.partial_rebuild(moved, 14, 0, 0)
+    on, _ = O.rebuild(nn, moved, 14, 0, 0)
+    assert _same(b.download()[0], on)

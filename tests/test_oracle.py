@@ -417,3 +417,64 @@ def test_bvh2_and_cwbvh_traversal_agree():
     assert (b2_ids == cw_ids).mean() > 0.999
     occ = O.traverse_bvh2(nodes, pidx, tris, rays, mode=1)
     assert np.array_equal(occ, b2_ids != 0xFFFFFFFF)
+
+
+# --- dynamic updates: full / partial rebuild, refit ------------------------------
+
+
+def _leaf_ids(nodes):
+    return np.nonzero(nodes[:, 12:16].copy().view(np.uint32).ravel() != 0)[0].astype(np.uint32)
+
+
+def _rebuild_scenes():
+    sm = T.demoscene(5, 0)
+    return [T.demoscene(31, 0), sm, sm[:1], sm[:2], sm[:3]]
+
+
+@pytest.mark.parametrize("which", ["full", "partial_all", "partial_one", "partial_random"])
+def test_rebuilds_validate(which):
+    """test_full_rebuild, test_partial_rebuild_with_{all_leaves,one_leaf,
+    random_leaves} (src/ploc/rebuild.rs:193-366)."""
+    scenes = [T.demoscene(8, 0)] if which == "partial_one" else _rebuild_scenes()
+    for tris in scenes:
+        aabbs = T.tri_aabbs(tris)
+        thr = 0 if which in ("partial_one", "partial_random") else 1
+        nodes, pidx, md, _ = O.ploc(aabbs, search_distance=1, sort_precision=0, search_depth_threshold=thr)
+        assert O.validate_bvh2(nodes, pidx, md, aabbs)[0] == 0
+        leaves = _leaf_ids(nodes)
+        if which == "full":
+            out, md2 = O.rebuild(nodes, None, 1, 0, 1)
+        else:
+            if which == "partial_one":
+                pick = leaves[:1]
+            elif which == "partial_random":
+                pick = np.array([i for i in leaves if T.hash_noise(0, 0, int(i)) > 0.5][:1], np.uint32)
+            else:
+                pick = leaves
+            out, md2 = O.rebuild(nodes, pick, 1, 0, thr)
+        assert len(out) == len(nodes)
+        assert O.validate_bvh2(out, pidx, md2, aabbs)[0] == 0
+
+
+def test_partial_rebuild_after_moving_leaves():
+    """Leaves given new boxes, their paths rebuilt: a valid, tight tree over
+    the moved boxes; untouched subtrees keep their nodes."""
+    tris = T.demoscene(32, 0)
+    aabbs = T.tri_aabbs(tris)
+    nodes, pidx, md, _ = O.ploc(aabbs, search_distance=14)
+    leaves = _leaf_ids(nodes)
+    rng = np.random.default_rng(3)
+    moved = np.sort(rng.choice(leaves, size=len(leaves) // 20, replace=False)).astype(np.uint32)
+    shift = np.float32(0.3)
+    new_aabbs = aabbs.copy()
+    nn = nodes.copy()
+    for i in moved:
+        f = nn[i].view(np.float32)
+        f[[0, 1, 2, 4, 5, 6]] += shift
+        prim = pidx[nn[i, 28:32].view(np.uint32)[0]]
+        new_aabbs[prim] += shift
+    out, md2 = O.rebuild(nn, moved, 14, 0, 0)
+    assert O.validate_bvh2(out, pidx, md2, new_aabbs)[0] == 0
+    # refit_all of a tree whose leaves moved in place gives tight boxes again
+    refit = O.refit_all(nn)
+    assert O.validate_bvh2(refit, pidx, md, new_aabbs)[0] == 0
