@@ -216,6 +216,26 @@ OBVHS_API int obvhs_bvh2_partial_rebuild(obvhs_ctx* ctx, obvhs_bvh2* bvh, const 
                                          uint32_t search_distance, uint32_t sort_precision,
                                          uint32_t search_depth_threshold, int device_ptrs);
 
+/* ---- AABB and point queries ------------------------------------------------- */
+/* Bvh2::aabb_traverse / point_traverse (src/bvh2/mod.rs:365-460) for n queries
+ * at once: kind 0 = boxes (n x 6: min xyz, max xyz, Aabb::intersect_aabb),
+ * kind 1 = points (n x 3, Aabb::contains_point).  Query i reports the original
+ * ids of the primitives of every leaf it reaches, in the reference's traversal
+ * order, as ids[offsets[i] .. offsets[i + 1]); with prim_aabbs (n_prims x 6,
+ * original order) only the primitives whose box passes the same test (the
+ * closure of the reference's tests).  offsets (n + 1) is always written; ids
+ * only when given and capacity >= offsets[n] (call once without ids to size
+ * them). */
+OBVHS_API int obvhs_bvh2_query(obvhs_ctx* ctx, const obvhs_bvh2* bvh, int kind, const float* queries, uint32_t n,
+                               const float* prim_aabbs, uint32_t n_prims, uint32_t* offsets, uint32_t* ids,
+                               uint64_t capacity, int device_ptrs);
+/* The same through the CWBVH: the traverse! loop (src/cwbvh/traverse_macro.rs)
+ * with CwBvhNode::intersect_aabb / contains_point (src/cwbvh/node.rs:157-200),
+ * the child order of `direction` (NULL = zero, as CwBvh::new_traversal). */
+OBVHS_API int obvhs_cwbvh_query(obvhs_ctx* ctx, const obvhs_cwbvh* bvh, int kind, const float* queries, uint32_t n,
+                                const float* prim_aabbs, uint32_t n_prims, const float* direction, uint32_t* offsets,
+                                uint32_t* ids, uint64_t capacity, int device_ptrs);
+
 /* bvh2_to_cwbvh with include_exact_node_aabbs (src/cwbvh/bvh2_to_cwbvh.rs:
  * 490-510, :76-80): the CWBVH also keeps, per node, the exact box of the BVH2
  * node it came from (read with obvhs_cwbvh_exact_node_aabbs; used and moved

@@ -91,6 +91,8 @@ SIGNATURES = {
     "obvhs_bvh2_refit_all": (I32, [P, P]),
     "obvhs_bvh2_full_rebuild": (I32, [P, P, U32, U32, U32]),
     "obvhs_bvh2_partial_rebuild": (I32, [P, P, P, U32, U32, U32, U32, I32]),
+    "obvhs_bvh2_query": (I32, [P, P, I32, P, U32, P, U32, P, P, U64, I32]),
+    "obvhs_cwbvh_query": (I32, [P, P, I32, P, U32, P, U32, P, P, P, U64, I32]),
     "obvhs_bvh2_to_cwbvh": (I32, [P, P, U32, I32, ctypes.POINTER(P)]),
     "obvhs_bvh2_to_cwbvh_ex": (I32, [P, P, U32, I32, I32, ctypes.POINTER(P)]),
     "obvhs_cwbvh_exact_node_aabbs": (I32, [P, P, P]),

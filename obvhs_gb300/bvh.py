@@ -214,6 +214,16 @@ class Bvh2:
         self.ctx.check(self.ctx.lib.obvhs_bvh2_set_node_aabbs(self.ctx.h, self.h, pi, pa, n, dev))
         del ki, ka
 
+    def aabb_query(self, boxes, prim_aabbs=None):
+        """Bvh2::aabb_traverse for (n, 6) query boxes: per box the original ids
+        of the reached leaves' primitives in traversal order (only those whose
+        box intersects, when prim_aabbs is given)."""
+        return _query(self, self.ctx.lib.obvhs_bvh2_query, "aabb", boxes, prim_aabbs, [])
+
+    def point_query(self, points, prim_aabbs=None):
+        """Bvh2::point_traverse for (n, 3) points."""
+        return _query(self, self.ctx.lib.obvhs_bvh2_query, "point", points, prim_aabbs, [])
+
     def refit_all(self):
         """Bvh2::refit_all (src/bvh2/mod.rs:527-570)."""
         self.ctx.check(self.ctx.lib.obvhs_bvh2_refit_all(self.ctx.h, self.h))
@@ -393,6 +403,22 @@ class CwBvh:
         ctx.check(ctx.lib.obvhs_cwbvh_upload(ctx.h, nodes.ctypes.data_as(ctypes.c_void_p), len(nodes),
                                              pidx.ctypes.data_as(ctypes.c_void_p), len(pidx), ctypes.byref(h)))
         return CwBvh(ctx, h)
+
+    def aabb_query(self, boxes, prim_aabbs=None, direction=None):
+        """The traverse! loop with CwBvhNode::intersect_aabb for (n, 6) query
+        boxes: per box the original ids of the reached primitives in traversal
+        order (filtered by their boxes when prim_aabbs is given)."""
+        d = None if direction is None else np.ascontiguousarray(direction, dtype=np.float32)
+        keep = d
+        return _query(self, self.ctx.lib.obvhs_cwbvh_query, "aabb", boxes, prim_aabbs,
+                      [None if keep is None else keep.ctypes.data_as(ctypes.c_void_p)])
+
+    def point_query(self, points, prim_aabbs=None, direction=None):
+        """The traverse! loop with CwBvhNode::contains_point for (n, 3) points."""
+        d = None if direction is None else np.ascontiguousarray(direction, dtype=np.float32)
+        keep = d
+        return _query(self, self.ctx.lib.obvhs_cwbvh_query, "point", points, prim_aabbs,
+                      [None if keep is None else keep.ctypes.data_as(ctypes.c_void_p)])
 
     def exact_node_aabbs(self):
         """CwBvh::exact_node_aabbs: (n_nodes, 6) float32 (min xyz, max xyz), or
@@ -657,6 +683,22 @@ def ray_traverse_batches(bvhs, batch_bvh, rays, outs=None, ctx: Context | None =
                                                  counts.ctypes.data_as(ctypes.c_void_p),
                                                  ctypes.cast(op, ctypes.c_void_p)))
     return outs
+
+
+def _query(obj, fn, kind, queries, prim_aabbs, extra):
+    """Two calls of an obvhs_*_query entry (sizes, then ids): a list of uint32
+    arrays of original primitive ids, one per query."""
+    k = 0 if kind == "aabb" else 1
+    q = np.ascontiguousarray(queries, dtype=np.float32).reshape(-1, 6 if k == 0 else 3)
+    pa = None if prim_aabbs is None else np.ascontiguousarray(prim_aabbs, dtype=np.float32).reshape(-1, 6)
+    n = len(q)
+    off = np.zeros(n + 1, np.uint32)
+    args = [obj.ctx.h, obj.h, k, q.ctypes.data_as(ctypes.c_void_p), n,
+            None if pa is None else pa.ctypes.data_as(ctypes.c_void_p), 0 if pa is None else len(pa)] + extra
+    obj.ctx.check(fn(*args, off.ctypes.data_as(ctypes.c_void_p), None, 0, 0))
+    ids = np.zeros(max(int(off[n]), 1), np.uint32)
+    obj.ctx.check(fn(*args, off.ctypes.data_as(ctypes.c_void_p), ids.ctypes.data_as(ctypes.c_void_p), len(ids), 0))
+    return [ids[int(off[i]):int(off[i + 1])].copy() for i in range(n)]
 
 
 def _params(p: BvhBuildParams) -> N.BuildParams:

@@ -1309,6 +1309,59 @@ int obvhs_bvh2_partial_rebuild(obvhs_ctx* cp, obvhs_bvh2* b, const uint32_t* lea
   return r;
 }
 
+static int query_common(obvhs_ctx* cp, int structure, const void* nodes, uint32_t n_nodes, const uint32_t* pidx,
+                        uint32_t n_pidx, int kind, const float* queries, uint32_t n, const float* prim_aabbs,
+                        uint32_t n_prims, const float* direction, uint32_t* offsets, uint32_t* ids,
+                        uint64_t capacity, int device_ptrs) {
+  if (!cp || (n && (!queries || !offsets)) || (kind != 0 && kind != 1)) return OBVHS_ERR_INVALID_ARG;
+  BuildCtx& c = *cp;
+  DeviceGuard g(c.device);
+  int err = 0;
+  const int stride = kind == 0 ? 6 : 3;
+  const float* dq = (const float*)stage_in(c, SLOT_INPUT2, queries, (size_t)n * stride * 4, device_ptrs, &err);
+  if (err) return err;
+  const float* dp =
+      prim_aabbs ? (const float*)stage_in(c, SLOT_INPUT, prim_aabbs, (size_t)n_prims * 24, device_ptrs, &err) : nullptr;
+  if (err) return err;
+  uint32_t* doff = offsets;
+  uint32_t* dids = ids;
+  if (!device_ptrs) {
+    doff = (uint32_t*)c.scratch.get(SLOT_FRONTIER_A, ((size_t)n + 1) * 4);
+    dids = ids ? (uint32_t*)c.scratch.get(SLOT_FRONTIER_B, (size_t)std::max<uint64_t>(capacity, 1) * 4) : nullptr;
+    if (!doff || (ids && !dids)) return c.fail(OBVHS_ERR_OOM, "output staging");
+  }
+  float d[3] = {0.0f, 0.0f, 0.0f};
+  if (direction) std::memcpy(d, direction, 12);
+  const uint32_t oct =
+      (d[0] < 0.0f ? 0u : 0x04040404u) | (d[1] < 0.0f ? 0u : 0x02020202u) | (d[2] < 0.0f ? 0u : 0x01010101u);
+  uint32_t total = 0;
+  int r = query_device(c, structure, kind, nodes, n_nodes, pidx, n_pidx, dq, n, dp, n_prims, oct, doff, dids, capacity,
+                       &total);
+  if (r) return r;
+  if (!device_ptrs) {
+    CK(cudaMemcpyAsync(offsets, doff, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost, c.stream));
+    if (ids && capacity >= total && total)
+      CK(cudaMemcpyAsync(ids, dids, (size_t)total * 4, cudaMemcpyDeviceToHost, c.stream));
+  }
+  return take_status(c);
+}
+
+int obvhs_bvh2_query(obvhs_ctx* cp, const obvhs_bvh2* b, int kind, const float* queries, uint32_t n,
+                     const float* prim_aabbs, uint32_t n_prims, uint32_t* offsets, uint32_t* ids, uint64_t capacity,
+                     int device_ptrs) {
+  if (!b) return OBVHS_ERR_INVALID_ARG;
+  return query_common(cp, 0, b->nodes, b->n_nodes, b->prim_indices, b->n_prims, kind, queries, n, prim_aabbs, n_prims,
+                      nullptr, offsets, ids, capacity, device_ptrs);
+}
+
+int obvhs_cwbvh_query(obvhs_ctx* cp, const obvhs_cwbvh* b, int kind, const float* queries, uint32_t n,
+                      const float* prim_aabbs, uint32_t n_prims, const float* direction, uint32_t* offsets,
+                      uint32_t* ids, uint64_t capacity, int device_ptrs) {
+  if (!b) return OBVHS_ERR_INVALID_ARG;
+  return query_common(cp, 1, b->nodes, b->n_nodes, b->prim_indices, b->n_prims, kind, queries, n, prim_aabbs, n_prims,
+                      direction, offsets, ids, capacity, device_ptrs);
+}
+
 int obvhs_cwbvh_exact_node_aabbs(obvhs_ctx* cp, const obvhs_cwbvh* b, float* aabbs6) {
   if (!cp || !b || (b->n_nodes && !aabbs6)) return OBVHS_ERR_INVALID_ARG;
   BuildCtx& c = *cp;

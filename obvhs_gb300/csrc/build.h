@@ -351,6 +351,14 @@ int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint
 int reorder_tris_device(BuildCtx& c, obvhs_cwbvh* bvh, const float* tris, uint32_t n_tris);
 // The BVH2 product (src/bvh2/builder.rs, leaf_collapser.rs, mod.rs:148-337).
 int bvh2_collapse_device(BuildCtx& c, obvhs_bvh2* b, uint32_t max_prims, float traversal_cost);
+// Inclusive scan of two u32 arrays of n elements in place.
+int scan2_device(BuildCtx& c, uint32_t* a, uint32_t* b, uint32_t n);
+// AABB (kind 0) / point (kind 1) queries over a BVH2 (structure 0, 32-byte
+// nodes) or a CWBVH (1, 80-byte nodes, traversal octant `oct`): offsets
+// (n + 1, device) always; ids when given and capacity >= the total.
+int query_device(BuildCtx& c, int structure, int kind, const void* nodes, uint32_t n_nodes, const uint32_t* pidx,
+                 uint32_t n_pidx, const float* queries, uint32_t n, const float* prims, uint32_t n_prims,
+                 uint32_t oct, uint32_t* offsets, uint32_t* ids, uint64_t capacity, uint32_t* total_out);
 // Bvh2Node::set_aabb (src/bvh2/node.rs) for m nodes (ids, boxes n x 6: device).
 int bvh2_set_node_aabbs_device(BuildCtx& c, obvhs_bvh2* b, const uint32_t* d_ids, const float* d_aabbs, uint32_t m);
 // Bvh2::refit_all (src/bvh2/mod.rs:527-570).

@@ -446,7 +446,7 @@ int bvh2_set_node_aabbs_device(BuildCtx& c, obvhs_bvh2* b, const uint32_t* d_ids
 }
 
 // inclusive scan of a (and b) in place, n elements
-static int scan2(BuildCtx& c, uint32_t* a, uint32_t* b, uint32_t n) {
+int scan2_device(BuildCtx& c, uint32_t* a, uint32_t* b, uint32_t n) {
   const uint32_t tiles = div_up<uint32_t>(n, SCAN_TILE);
   uint2* totals = (uint2*)c.scratch.get(SLOT_PARTIAL, (size_t)std::max(tiles, 1u) * sizeof(uint2));
   if (!totals) return c.fail(OBVHS_ERR_OOM, "scratch");
@@ -492,7 +492,7 @@ int bvh2_rebuild_device(BuildCtx& c, obvhs_bvh2* b, const uint32_t* d_leaves, ui
   if (!d_leaves) {
     // full_rebuild: the leaves in node order, a fresh tree of 2m - 1 nodes
     KLAUNCH("k_leaf_flags", k_leaf_flags<<<g, BLK, 0, c.stream>>>(b->nodes, n, fa, fb));
-    if ((r = scan2(c, fa, fb, n))) return r;
+    if ((r = scan2_device(c, fa, fb, n))) return r;
     KLAUNCH("k_compact_leaves", k_compact_leaves<<<g, BLK, 0, c.stream>>>(b->nodes, n, fa, col));
     CK(cudaMemcpyAsync(&m, fa + n - 1, 4, cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
@@ -518,7 +518,7 @@ int bvh2_rebuild_device(BuildCtx& c, obvhs_bvh2* b, const uint32_t* d_leaves, ui
                                                                          c.d_status));
   const uint32_t n_pairs = (n - 1) / 2;
   KLAUNCH("k_pair_flags", k_pair_flags<<<div_up<uint32_t>(n_pairs, BLK), BLK, 0, c.stream>>>(b->nodes, n_pairs, fa, fb));
-  if ((r = scan2(c, fa, fb, n_pairs))) return r;
+  if ((r = scan2_device(c, fa, fb, n_pairs))) return r;
   uint32_t h[2] = {0, 0};
   CK(cudaMemcpyAsync(&h[0], cnt, 4, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaMemcpyAsync(&h[1], fa + n_pairs - 1, 4, cudaMemcpyDeviceToHost, c.stream));

@@ -416,6 +416,202 @@ __global__ void __launch_bounds__(TBLK) k_traverse_bvh2(const Bvh2Node* __restri
   }
 }
 
+// --- AABB and point queries (src/bvh2/mod.rs:365-460, src/cwbvh/node.rs:157-200) ---
+//
+// KIND 0: the query is a box (min xyz, max xyz), test Aabb::intersect_aabb;
+// KIND 1: a point, test Aabb::contains_point.  A query reports the original
+// ids of the primitives of every leaf it reaches, in the reference's traversal
+// order; with primitive boxes given only those passing the same test.  FILL =
+// false counts (into out[q]), FILL = true writes ids from offsets[q].
+template <int KIND>
+__device__ __forceinline__ bool q_test(float3 mn, float3 mx, const float* q) {
+  if (KIND == 0) return !(mn.x > q[3] || mn.y > q[4] || mn.z > q[5] || mx.x < q[0] || mx.y < q[1] || mx.z < q[2]);
+  return q[0] >= mn.x && q[1] >= mn.y && q[2] >= mn.z && q[0] <= mx.x && q[1] <= mx.y && q[2] <= mx.z;
+}
+
+template <int KIND>
+__device__ __forceinline__ bool q_prim(const float* prims, uint32_t n_prims, uint32_t id, const float* q) {
+  if (!prims) return true;
+  if (id >= n_prims) return false;
+  const float* a = prims + 6 * (size_t)id;
+  return q_test<KIND>(make_float3(a[0], a[1], a[2]), make_float3(a[3], a[4], a[5]), q);
+}
+
+template <int KIND, bool FILL>
+__global__ void __launch_bounds__(TBLK) k_query_bvh2(const Bvh2Node* __restrict__ nodes, uint32_t n_nodes,
+                                                     const uint32_t* __restrict__ pidx, uint32_t n_pidx,
+                                                     const float* __restrict__ queries, uint32_t nq,
+                                                     const float* __restrict__ prims, uint32_t n_prims,
+                                                     uint32_t* out, uint32_t* __restrict__ ids, uint32_t* status) {
+  for (uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x; qi < nq; qi += gridDim.x * blockDim.x) {
+    float q[6];
+#pragma unroll
+    for (int k = 0; k < (KIND == 0 ? 6 : 3); k++) q[k] = queries[(KIND == 0 ? 6 : 3) * (size_t)qi + k];
+    uint32_t c = 0;
+    const uint32_t base = FILL ? out[qi] : 0u;
+    bool bad = false;
+    auto emit = [&](const Bvh2Node& x) {
+      for (uint32_t i = 0; i < node_prims(x); i++) {
+        const uint32_t slot = node_first(x) + i;
+        if (slot >= n_pidx) {
+          bad = true;
+          return;
+        }
+        const uint32_t id = pidx[slot];
+        if (!q_prim<KIND>(prims, n_prims, id, q)) continue;
+        if (FILL) ids[base + c] = id;
+        c++;
+      }
+    };
+    if (n_nodes) {
+      const Bvh2Node root = ld_node(&nodes[0]);
+      if (node_prims(root) != 0) {
+        if (q_test<KIND>(make_float3(root.a.x, root.a.y, root.a.z), make_float3(root.b.x, root.b.y, root.b.z), q))
+          emit(root);
+      } else {
+        uint32_t stack[BVH2_STACK];
+        uint32_t sp = 0;
+        stack[sp++] = node_first(root);
+        for (uint32_t guard = 0; sp > 0 && !bad; guard++) {
+          const uint32_t ni = stack[--sp];
+          if (guard > (1u << 24) || ni + 1 >= n_nodes) {
+            bad = true;
+            break;
+          }
+          for (uint32_t x = ni; x < ni + 2; x++) {
+            const Bvh2Node nd = ld_node(&nodes[x]);
+            if (!q_test<KIND>(make_float3(nd.a.x, nd.a.y, nd.a.z), make_float3(nd.b.x, nd.b.y, nd.b.z), q)) continue;
+            if (node_prims(nd) != 0) {
+              emit(nd);
+            } else if (sp < BVH2_STACK) {
+              stack[sp++] = node_first(nd);
+            } else {
+              set_status(status, ST_STACK_OVERFLOW);
+              bad = true;
+              break;
+            }
+          }
+        }
+      }
+    }
+    if (bad) set_status(status, ST_BAD_TREE);
+    if (!FILL) out[qi] = c;
+  }
+}
+
+// CwBvhNode::intersect_aabb / contains_point: the query in the node's grid,
+// tested against every child's quantised box, bits placed as for rays.
+template <int KIND>
+__device__ __forceinline__ uint32_t query_node(const NodeQ& n, const float* q, uint32_t oct_inv4) {
+  const float px = __uint_as_float(n.q0.x), py = __uint_as_float(n.q0.y), pz = __uint_as_float(n.q0.z);
+  const float rx = 1.0f / __uint_as_float(byte_of(n.q0.w, 0) << 23);
+  const float ry = 1.0f / __uint_as_float(byte_of(n.q0.w, 1) << 23);
+  const float rz = 1.0f / __uint_as_float(byte_of(n.q0.w, 2) << 23);
+  float aq[6];
+  aq[0] = (q[0] - px) * rx;
+  aq[1] = (q[1] - py) * ry;
+  aq[2] = (q[2] - pz) * rz;
+  if (KIND == 0) {
+    aq[3] = (q[3] - px) * rx;
+    aq[4] = (q[4] - py) * ry;
+    aq[5] = (q[5] - pz) * rz;
+  }
+  unsigned long long oct8 = oct_inv4;
+  oct8 |= oct8 << 32;
+  const unsigned long long meta8 = (unsigned long long)n.q1.z | ((unsigned long long)n.q1.w << 32);
+  const unsigned long long is_inner8 = (meta8 & (meta8 << 1)) & 0x1010101010101010ull;
+  const unsigned long long inner_mask8 = (is_inner8 >> 4) * 0xffull;
+  const unsigned long long bit_index8 = (meta8 ^ (oct8 & inner_mask8)) & 0x1f1f1f1f1f1f1f1full;
+  const unsigned long long child_bits8 = (meta8 >> 5) & 0x0707070707070707ull;
+  uint32_t hit = 0;
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const int w = c >> 2, b = c & 3;
+    const float3 lo = make_float3((float)byte_of(w ? n.q2.y : n.q2.x, b), (float)byte_of(w ? n.q3.y : n.q3.x, b),
+                                  (float)byte_of(w ? n.q4.y : n.q4.x, b));
+    const float3 hi = make_float3((float)byte_of(w ? n.q2.w : n.q2.z, b), (float)byte_of(w ? n.q3.w : n.q3.z, b),
+                                  (float)byte_of(w ? n.q4.w : n.q4.z, b));
+    if (q_test<KIND>(lo, hi, aq)) {
+      const uint32_t cb = (uint32_t)(child_bits8 >> (c * 8)) & 0xffu;
+      const uint32_t bi = (uint32_t)(bit_index8 >> (c * 8)) & 0xffu;
+      hit |= cb << bi;
+    }
+  }
+  return hit;
+}
+
+template <int KIND, bool FILL>
+__global__ void __launch_bounds__(TBLK) k_query_cwbvh(const CwNode* __restrict__ nodes, uint32_t n_nodes,
+                                                      const uint32_t* __restrict__ pidx, uint32_t n_pidx,
+                                                      const float* __restrict__ queries, uint32_t nq,
+                                                      const float* __restrict__ prims, uint32_t n_prims, uint32_t oct,
+                                                      uint32_t* out, uint32_t* __restrict__ ids, uint32_t* status) {
+  for (uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x; qi < nq; qi += gridDim.x * blockDim.x) {
+    float q[6];
+#pragma unroll
+    for (int k = 0; k < (KIND == 0 ? 6 : 3); k++) q[k] = queries[(KIND == 0 ? 6 : 3) * (size_t)qi + k];
+    uint32_t c = 0;
+    const uint32_t base = FILL ? out[qi] : 0u;
+    uint2 stack[32];
+    uint32_t sp = 0;
+    uint2 cur = n_nodes ? make_uint2(0u, 0x80000000u) : make_uint2(0u, 0u);
+    uint2 prim = make_uint2(0u, 0u);
+    bool bad = false;
+    for (uint32_t guard = 0;; guard++) {
+      if (guard > (1u << 24)) {
+        bad = true;
+        break;
+      }
+      while (prim.y != 0) {
+        const uint32_t lpi = 31u - __clz(prim.y);
+        prim.y &= ~(1u << lpi);
+        const uint32_t slot = prim.x + lpi;
+        if (slot >= n_pidx) {
+          bad = true;
+          break;
+        }
+        const uint32_t id = pidx[slot];
+        if (!q_prim<KIND>(prims, n_prims, id, q)) continue;
+        if (FILL) ids[base + c] = id;
+        c++;
+      }
+      if (bad) break;
+      prim = make_uint2(0u, 0u);
+      if (cur.y & 0xff000000u) {
+        const uint32_t hits_imask = cur.y;
+        const uint32_t cio = 31u - __clz(hits_imask);
+        const uint32_t cbase = cur.x;
+        cur.y &= ~(1u << cio);
+        if (cur.y & 0xff000000u) {
+          stack[sp] = cur;
+          sp = min(sp + 1, 31u);
+        }
+        const uint32_t slot = (cio - 24) ^ (oct & 0xffu);
+        const uint32_t ni = cbase + __popc(hits_imask & ~(0xffffffffu << slot));
+        if (ni >= n_nodes) {
+          bad = true;
+          break;
+        }
+        const NodeQ node = load_cw(nodes, ni);
+        const uint32_t hm = query_node<KIND>(node, q, oct);
+        cur.x = node.q1.x;
+        prim.x = node.q1.y;
+        cur.y = (hm & 0xff000000u) | byte_of(node.q0.w, 3);
+        prim.y = hm & 0x00ffffffu;
+      } else {
+        cur = make_uint2(0u, 0u);
+      }
+      if (prim.y == 0 && (cur.y & 0xff000000u) == 0) {
+        if (sp == 0) break;
+        sp = sp ? sp - 1 : 0;
+        cur = stack[sp];
+      }
+    }
+    if (bad) set_status(status, ST_BAD_TREE);
+    if (!FILL) out[qi] = c;
+  }
+}
+
 // RtCompressedTriangle::new (src/rt_triangle.rs:31-47) for the triangles in
 // primitive_indices order; halves by round-to-nearest-even (f16::from_f32).
 __global__ void k_compress_tris(const float* __restrict__ tris, uint32_t n_tris, const uint32_t* __restrict__ pidx,
@@ -845,5 +1041,51 @@ int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint
     KLAUNCH("k_traverse_occluded", k_traverse<1><<<grid, TBLK, 0, c.stream>>>(bvh->nodes, bvh->n_nodes, bvh->tris, bvh->n_prims, (const float4*)rays, n, nullptr,
                                                miss, counter, c.d_status));
   CK(cudaGetLastError());
+  return 0;
+}
+
+// Count, scan, fill.  offsets: n + 1 (device); ids filled when given and
+// capacity >= offsets[n].
+int query_device(BuildCtx& c, int structure, int kind, const void* nodes, uint32_t n_nodes, const uint32_t* pidx,
+                 uint32_t n_pidx, const float* queries, uint32_t n, const float* prims, uint32_t n_prims,
+                 uint32_t oct, uint32_t* offsets, uint32_t* ids, uint64_t capacity, uint32_t* total_out) {
+  *total_out = 0;
+  CK(cudaMemsetAsync(offsets, 0, 4, c.stream));
+  if (n == 0) return 0;
+  const uint32_t grid = std::min<uint32_t>(div_up<uint32_t>(n, TBLK), (uint32_t)c.num_sms * 16);
+  const Bvh2Node* b2 = (const Bvh2Node*)nodes;
+  const CwNode* cw = (const CwNode*)nodes;
+  uint32_t* cnt = offsets + 1;
+#define QLAUNCH(FILL, OUT, IDS)                                                                                 \
+  do {                                                                                                          \
+    if (structure == 0 && kind == 0)                                                                           \
+      KLAUNCH("k_query_bvh2", (k_query_bvh2<0, FILL><<<grid, TBLK, 0, c.stream>>>(b2, n_nodes, pidx, n_pidx,  \
+                                                      queries, n, prims, n_prims, OUT, IDS, c.d_status)));     \
+    else if (structure == 0)                                                                                    \
+      KLAUNCH("k_query_bvh2", (k_query_bvh2<1, FILL><<<grid, TBLK, 0, c.stream>>>(b2, n_nodes, pidx, n_pidx,  \
+                                                      queries, n, prims, n_prims, OUT, IDS, c.d_status)));     \
+    else if (kind == 0)                                                                                         \
+      KLAUNCH("k_query_cwbvh", (k_query_cwbvh<0, FILL><<<grid, TBLK, 0, c.stream>>>(cw, n_nodes, pidx, n_pidx, \
+                                                       queries, n, prims, n_prims, oct, OUT, IDS, c.d_status))); \
+    else                                                                                                        \
+      KLAUNCH("k_query_cwbvh", (k_query_cwbvh<1, FILL><<<grid, TBLK, 0, c.stream>>>(cw, n_nodes, pidx, n_pidx, \
+                                                       queries, n, prims, n_prims, oct, OUT, IDS, c.d_status))); \
+  } while (0)
+  QLAUNCH(false, cnt, nullptr);
+  CK(cudaGetLastError());
+  uint32_t* dummy = (uint32_t*)c.scratch.get(SLOT_REINS_VALS, (size_t)n * 4);
+  if (!dummy) return c.fail(OBVHS_ERR_OOM, "scratch");
+  CK(cudaMemsetAsync(dummy, 0, (size_t)n * 4, c.stream));
+  int r = scan2_device(c, cnt, dummy, n);  // offsets[1..n] = inclusive sums
+  if (r) return r;
+  uint32_t total = 0;
+  CK(cudaMemcpyAsync(&total, offsets + n, 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  *total_out = total;
+  if (ids && capacity >= total && total) {
+    QLAUNCH(true, offsets, ids);
+    CK(cudaGetLastError());
+  }
+#undef QLAUNCH
   return 0;
 }

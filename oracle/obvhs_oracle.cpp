@@ -1365,6 +1365,127 @@ inline uint32_t traverse(const CwNode* nodes, uint32_t n_nodes, const uint32_t* 
   return hit_id;
 }
 
+// ---------------------------------------------------------------------------
+// AABB and point queries: Bvh2::aabb_traverse / point_traverse
+// (src/bvh2/mod.rs:365-460), CwBvhNode::intersect_aabb / contains_point
+// (src/cwbvh/node.rs:157-200) under the traverse! loop, Aabb::intersect_aabb
+// / contains_point (src/aabb.rs:70-72,179-181).  A query reports the original
+// ids of the primitives of every leaf it reaches, in traversal order; with
+// primitive boxes given, only those whose box passes the same test (the
+// closure of the reference's tests).
+inline bool q_isect(const Aabb& a, const float* q) {
+  return !(a.mn.x > q[3] || a.mn.y > q[4] || a.mn.z > q[5] || a.mx.x < q[0] || a.mx.y < q[1] || a.mx.z < q[2]);
+}
+inline bool q_contains(const Aabb& a, const float* q) {
+  return q[0] >= a.mn.x && q[1] >= a.mn.y && q[2] >= a.mn.z && q[0] <= a.mx.x && q[1] <= a.mx.y && q[2] <= a.mx.z;
+}
+inline bool q_test(int kind, const Aabb& a, const float* q) { return kind == 0 ? q_isect(a, q) : q_contains(a, q); }
+
+void query_bvh2(const Bvh2& b, int kind, const float* q, const Aabb* prims, std::vector<uint32_t>& out) {
+  if (b.nodes.empty()) return;
+  auto emit = [&](const Node& n) {
+    for (uint32_t i = 0; i < n.prim_count; i++) {
+      uint32_t prim = b.primitive_indices[n.first_index + i];
+      if (!prims || q_test(kind, prims[prim], q)) out.push_back(prim);
+    }
+  };
+  const Node& root = b.nodes[0];
+  if (root.is_leaf()) {
+    if (q_test(kind, root.box, q)) emit(root);
+    return;
+  }
+  std::vector<uint32_t> st{root.first_index};
+  while (!st.empty()) {
+    uint32_t ni = st.back();
+    st.pop_back();
+    for (uint32_t x : {ni, ni + 1}) {
+      const Node& n = b.nodes[x];
+      if (!q_test(kind, n.box, q)) continue;
+      if (n.is_leaf())
+        emit(n);
+      else
+        st.push_back(n.first_index);
+    }
+  }
+}
+
+inline uint32_t node_query_mask(const CwNode& n, int kind, const float* q, uint32_t oct_inv4) {
+  V3 ext = v3(f_from_bits((uint32_t)n.e[0] << 23), f_from_bits((uint32_t)n.e[1] << 23),
+              f_from_bits((uint32_t)n.e[2] << 23));
+  V3 rcp = v3(1.0f / ext.x, 1.0f / ext.y, 1.0f / ext.z);
+  V3 p = v3(n.p[0], n.p[1], n.p[2]);
+  float aq[6];
+  aq[0] = (q[0] - p.x) * rcp.x;
+  aq[1] = (q[1] - p.y) * rcp.y;
+  aq[2] = (q[2] - p.z) * rcp.z;
+  if (kind == 0) {
+    aq[3] = (q[3] - p.x) * rcp.x;
+    aq[4] = (q[4] - p.y) * rcp.y;
+    aq[5] = (q[5] - p.z) * rcp.z;
+  }
+  uint64_t oct8 = oct_inv4;
+  oct8 |= oct8 << 32;
+  uint64_t meta8;
+  std::memcpy(&meta8, n.child_meta, 8);
+  uint64_t is_inner8 = (meta8 & (meta8 << 1)) & 0x1010101010101010ull;
+  uint64_t inner_mask8 = (is_inner8 >> 4) * 0xffull;
+  uint64_t bit_index8 = (meta8 ^ (oct8 & inner_mask8)) & 0x1f1f1f1f1f1f1f1full;
+  uint64_t child_bits8 = (meta8 >> 5) & 0x0707070707070707ull;
+  uint32_t hit = 0;
+  for (int c = 0; c < 8; c++) {
+    Aabb local{v3((float)n.child_min_x[c], (float)n.child_min_y[c], (float)n.child_min_z[c]),
+               v3((float)n.child_max_x[c], (float)n.child_max_y[c], (float)n.child_max_z[c])};
+    if (q_test(kind, local, aq)) {
+      uint32_t cb = (uint32_t)(child_bits8 >> (c * 8)) & 0xffu;
+      uint32_t bi = (uint32_t)(bit_index8 >> (c * 8)) & 0xffu;
+      hit |= cb << bi;
+    }
+  }
+  return hit;
+}
+
+void query_cwbvh(const CwNode* nodes, uint32_t n_nodes, const uint32_t* pidx, int kind, const float* q,
+                 const Aabb* prims, uint32_t oct, std::vector<uint32_t>& out) {
+  Grp stack[32];
+  size_t sp = 0;
+  Grp cur = n_nodes ? Grp{0, 0x80000000u} : Grp{0, 0};
+  Grp prim{0, 0};
+  for (;;) {
+    while (prim.y != 0) {
+      uint32_t lpi = fbh(prim.y);
+      prim.y &= ~(1u << lpi);
+      uint32_t id = pidx[prim.x + lpi];
+      if (!prims || q_test(kind, prims[id], q)) out.push_back(id);
+    }
+    prim = Grp{0, 0};
+    if (cur.y & 0xff000000u) {
+      uint32_t hits_imask = cur.y;
+      uint32_t cio = fbh(hits_imask);
+      uint32_t base = cur.x;
+      cur.y &= ~(1u << cio);
+      if (cur.y & 0xff000000u) {
+        stack[sp] = cur;
+        sp = std::min<size_t>(sp + 1, 31);
+      }
+      uint32_t slot = (cio - 24) ^ (oct & 0xffu);
+      uint32_t rel = (uint32_t)__builtin_popcount(hits_imask & ~(0xffffffffu << slot));
+      const CwNode& node = nodes[base + rel];
+      uint32_t hm = node_query_mask(node, kind, q, oct);
+      cur.x = node.child_base_idx;
+      prim.x = node.primitive_base_idx;
+      cur.y = (hm & 0xff000000u) | (uint32_t)node.imask;
+      prim.y = hm & 0x00ffffffu;
+    } else {
+      cur = Grp{0, 0};
+    }
+    if (prim.y == 0 && (cur.y & 0xff000000u) == 0) {
+      if (sp == 0) break;
+      sp = sp ? sp - 1 : 0;
+      cur = stack[sp];
+    }
+  }
+}
+
 inline Ray make_ray(const float* r8) {
   Ray r;
   r.o = v3(r8[0], r8[1], r8[2]);
@@ -2093,6 +2214,36 @@ int64_t orc_bvh2_rebuild(void* nodes32, uint64_t n_nodes, const uint32_t* leaves
   NodeX* o = (NodeX*)nodes32;
   for (size_t i = 0; i < b.nodes.size(); i++) o[i] = to_x(b.nodes[i]);
   return b.max_depth;
+}
+
+// Queries (structure 0 = BVH2 nodes32, 1 = CWBVH nodes80; kind 0 = AABB
+// (6 floats), 1 = point (3 floats)); dir3: the CWBVH traversal direction.
+// offsets[n + 1]; ids filled when given and cap suffices.
+void orc_query(int32_t structure, int32_t kind, const void* nodes, uint64_t n_nodes, const uint32_t* pidx,
+               uint64_t n_pidx, const float* queries, uint64_t n, const float* prim_aabbs6, uint64_t n_prims,
+               const float* dir3, uint64_t* offsets, uint32_t* ids, uint64_t cap) {
+  std::vector<Aabb> pa;
+  if (prim_aabbs6) pa = load_aabbs(prim_aabbs6, n_prims);
+  const Aabb* prims = prim_aabbs6 ? pa.data() : nullptr;
+  const int stride = kind == 0 ? 6 : 3;
+  std::vector<std::vector<uint32_t>> res(n);
+  if (structure == 0) {
+    Bvh2 b = load_bvh2(nodes, n_nodes, pidx, n_pidx, 96);
+    for (size_t i = 0; i < n; i++) query_bvh2(b, kind, queries + stride * i, prims, res[i]);
+  } else {
+    V3 d = dir3 ? v3(dir3[0], dir3[1], dir3[2]) : v3(0, 0, 0);
+    uint32_t oct = octant_inv4(d);
+    for (size_t i = 0; i < n; i++)
+      query_cwbvh((const CwNode*)nodes, (uint32_t)n_nodes, pidx, kind, queries + stride * i, prims, oct, res[i]);
+  }
+  uint64_t at = 0;
+  for (size_t i = 0; i < n; i++) {
+    offsets[i] = at;
+    at += res[i].size();
+  }
+  offsets[n] = at;
+  if (ids && cap >= at)
+    for (size_t i = 0; i < n; i++) std::memcpy(ids + offsets[i], res[i].data(), res[i].size() * 4);
 }
 
 // Pre-splits: returns a handle; orc_presplit_get copies out.

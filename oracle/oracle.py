@@ -80,6 +80,8 @@ def _declare(L):
     L.orc_bvh2_collapse.restype = I32
     L.orc_bvh2_rebuild.argtypes = [P, U64, P, ctypes.c_int64, U32, U32, U32]
     L.orc_bvh2_rebuild.restype = ctypes.c_int64
+    L.orc_query.argtypes = [I32, I32, P, U64, P, U64, P, U64, P, U64, P, P, P, U64]
+    L.orc_query.restype = None
     L.orc_bvh2_refit_all.argtypes = [P, U64]
     L.orc_bvh2_refit_all.restype = None
     L.orc_bvh2_traverse.argtypes = [I32, P, U64, P, U64, P, U64, P, U64, P, I32, P]
@@ -234,6 +236,31 @@ def rebuild(nodes, leaves=None, search_distance=1, sort_precision=0, search_dept
                                 -1 if lv is None else len(lv), int(search_distance), int(sort_precision),
                                 int(search_depth_threshold))
     return nodes, int(md)
+
+
+def query(nodes, pidx, queries, kind="aabb", prim_aabbs=None, direction=None):
+    """Bvh2::aabb_traverse / point_traverse (32-byte nodes) or the traverse!
+    loop with CwBvhNode::intersect_aabb / contains_point (80-byte nodes):
+    per query the original ids of the reached leaves' primitives in traversal
+    order (filtered by their boxes when prim_aabbs is given).  Returns a list
+    of uint32 arrays."""
+    nodes = np.ascontiguousarray(nodes, dtype=np.uint8)
+    structure = 0 if nodes.shape[-1] == 32 else 1
+    nodes = nodes.reshape(-1, 32 if structure == 0 else 80)
+    pidx = np.ascontiguousarray(pidx, dtype=np.uint32)
+    k = 0 if kind == "aabb" else 1
+    q = _f32(queries, 6 if k == 0 else 3)
+    pa = None if prim_aabbs is None else _f32(prim_aabbs, 6)
+    d = None if direction is None else np.ascontiguousarray(direction, dtype=np.float32)
+    n = len(q)
+    off = np.zeros(n + 1, np.uint64)
+    L = lib()
+    L.orc_query(structure, k, _p(nodes), len(nodes), _p(pidx), len(pidx), _p(q), n, _p(pa),
+                0 if pa is None else len(pa), _p(d), _p(off), None, 0)
+    ids = np.zeros(max(int(off[n]), 1), np.uint32)
+    L.orc_query(structure, k, _p(nodes), len(nodes), _p(pidx), len(pidx), _p(q), n, _p(pa),
+                0 if pa is None else len(pa), _p(d), _p(off), _p(ids), len(ids))
+    return [ids[int(off[i]):int(off[i + 1])].copy() for i in range(n)]
 
 
 def refit_all(nodes):

@@ -187,3 +187,48 @@ def test_partial_rebuild_large(G):
     b.partial_rebuild(moved, 14, 0, 0)
     on, _ = O.rebuild(nn, moved, 14, 0, 0)
     assert _same(b.download()[0], on)
+
+
+# --- AABB and point queries -------------------------------------------------------
+
+
+def _query_inputs(tris, n, seed):
+    v = tris.reshape(-1, 3)
+    lo, hi = v.min(0), v.max(0)
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(lo, hi, size=(n, 3)).astype(np.float32)
+    h = (rng.random((n, 1)) * 0.05 * (hi - lo).max()).astype(np.float32)
+    boxes = np.concatenate([c - h, c + h], 1)
+    # triangle centroids: inside their own boxes, so the filtered lists are not empty
+    t = tris.reshape(-1, 3, 3)[rng.integers(0, len(tris), size=n)]
+    pts = ((t[:, 0] + t[:, 1] + t[:, 2]) / np.float32(3)).astype(np.float32)
+    return boxes, pts
+
+
+@pytest.mark.parametrize("filtered", [False, True])
+def test_queries_match_oracle(G, filtered):
+    """Per query the same primitive ids in the same order as the oracle's
+    restatement of aabb_traverse / point_traverse and of the traverse! loop
+    with the node query tests; with the exact filter, the same sets as testing
+    every triangle."""
+    tris = S.scene2_tris(200_000, offset=6)
+    aabbs = T.tri_aabbs(tris)
+    p = BvhBuildParams.fast_build()
+    b2 = G.build_bvh2_from_tris(tris, p)
+    cw = G.build_cwbvh_from_tris(tris, p)
+    n2, p2 = b2.download()
+    n8, p8 = cw.download()
+    boxes, pts = _query_inputs(tris, 3000, 2)
+    pa = aabbs if filtered else None
+    d = np.array([0.3, -0.5, 0.8], np.float32)
+    for kind, q in (("aabb", boxes), ("point", pts)):
+        g2 = b2.aabb_query(q, pa) if kind == "aabb" else b2.point_query(q, pa)
+        o2 = O.query(n2, p2, q, kind, pa)
+        g8 = cw.aabb_query(q, pa, d) if kind == "aabb" else cw.point_query(q, pa, d)
+        o8 = O.query(n8, p8, q, kind, pa, d)
+        assert all(np.array_equal(a, b) for a, b in zip(g2, o2))
+        assert all(np.array_equal(a, b) for a, b in zip(g8, o8))
+        assert sum(len(a) for a in g2) > 0
+        if filtered:
+            for a, b in zip(g2, g8):
+                assert np.array_equal(np.sort(a), np.sort(b))

@@ -478,3 +478,57 @@ def test_partial_rebuild_after_moving_leaves():
     # refit_all of a tree whose leaves moved in place gives tight boxes again
     refit = O.refit_all(nn)
     assert O.validate_bvh2(refit, pidx, md, new_aabbs)[0] == 0
+
+
+# --- AABB and point queries -----------------------------------------------------------
+
+
+def _brute(tris, q, kind):
+    a = T.tri_aabbs(tris)
+    if kind == "aabb":
+        hit = ~((a[:, 0] > q[3]) | (a[:, 1] > q[4]) | (a[:, 2] > q[5]) | (a[:, 3] < q[0]) | (a[:, 4] < q[1]) |
+                (a[:, 5] < q[2]))
+    else:
+        hit = (q[0] >= a[:, 0]) & (q[1] >= a[:, 1]) & (q[2] >= a[:, 2]) & (q[0] <= a[:, 3]) & (q[1] <= a[:, 4]) & \
+              (q[2] <= a[:, 5])
+    return np.nonzero(hit)[0]
+
+
+def test_traverse_aabb():
+    """traverse_aabb (tests/mod.rs:180-247): demoscene(201, 0), fast_build, the
+    query box; BVH2 and CWBVH traversal with exact filtering find the same
+    primitives (count and id sum) as testing every triangle."""
+    tris = T.demoscene(201, 0)
+    q = np.array([0.511, -1.0, 0.511, 0.611, 1.0, 0.611], np.float32)
+    ref = _brute(tris, q, "aabb")
+    assert len(ref) > 0
+    p = BvhBuildParams.fast_build()
+    aabbs = T.tri_aabbs(tris)
+    nodes, pidx, _, _ = O.build_bvh2(tris=tris, params=p)
+    got = O.query(nodes, pidx, q[None], "aabb", aabbs)[0]
+    assert len(got) == len(ref) and int(got.astype(np.uint64).sum()) == int(ref.sum())
+    cw = O.build(tris=tris, params=p)
+    got = O.query(cw.cw_nodes, cw.cw_pidx, q[None], "aabb", aabbs)[0]
+    assert len(got) == len(ref) and int(got.astype(np.uint64).sum()) == int(ref.sum())
+
+
+def test_traverse_point():
+    """traverse_point (tests/mod.rs:249-323): icosphere(0), fast_build, 512
+    points on the unit sphere (uniform_sample_sphere of hash_noise)."""
+    tris = T.icosphere(0)
+    aabbs = T.tri_aabbs(tris)
+    p = BvhBuildParams.fast_build()
+    nodes, pidx, _, _ = O.build_bvh2(tris=tris, params=p)
+    cw = O.build(tris=tris, params=p)
+    u0 = np.array([T.hash_noise(0, 0, i) for i in range(512)], np.float32)
+    u1 = np.array([T.hash_noise(0, 1, i) for i in range(512)], np.float32)
+    pts = T.uniform_sample_sphere(u0, u1)
+    b2 = O.query(nodes, pidx, pts, "point", aabbs)
+    c8 = O.query(cw.cw_nodes, cw.cw_pidx, pts, "point", aabbs)
+    total = 0
+    for i in range(512):
+        ref = _brute(tris, pts[i], "point")
+        total += len(ref)
+        for got in (b2[i], c8[i]):
+            assert len(got) == len(ref) and int(got.astype(np.uint64).sum()) == int(ref.sum())
+    assert total > 0
