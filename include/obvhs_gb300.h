@@ -370,7 +370,7 @@ OBVHS_API int obvhs_morton_sort(obvhs_ctx* ctx, const float* aabbs, uint32_t n, 
  * allocate device memory (an engine that keeps all GPU memory in its own pool,
  * or frame-time code that cannot afford cudaMalloc's synchronisation).  It
  * calls no cudaMalloc/cudaFree: its working memory is one fixed array in the
- * library's device image (about 20 MiB, held on every GPU this function runs
+ * library's device image (about 22 MiB, held on every GPU this function runs
  * on until the process exits), for at most OBVHS_NOALLOC_MAX_PRIMS boxes;
  * larger n returns OBVHS_ERR_TOO_LARGE before any GPU work.
  * aabbs (float[n][6]), codes (u64[n][2], may be NULL) and order (u32[n]) are

@@ -91,8 +91,7 @@ __device__ __forceinline__ uint2 child_term(const Dec& d, uint32_t j) {
 
 // calculate_cost_impl (src/cwbvh/bvh2_to_cwbvh.rs:257-341) for one inner node
 // whose children are complete, plus the aggregates.
-__device__ void inner_costs(const Bvh2Node* nodes, Dec* dec, uint32_t x, uint32_t max_prims) {
-  const Bvh2Node nd = ld_node(&nodes[x]);
+__device__ void inner_costs(const Bvh2Node& nd, Dec* dec, uint32_t x, uint32_t max_prims) {
   const float ha = half_area(node_box(nd));
   const uint32_t f = node_first(nd);
   const Dec L = ld_dec_cg(&dec[f]);
@@ -187,11 +186,14 @@ __global__ void __launch_bounds__(BLK) k_costs(const Bvh2Node* __restrict__ node
   uint32_t p = parents[i];
   if (p == i) return;
   for (uint32_t guard = 0; guard < n; guard++) {
+    // the parent's node and its own parent are static: load them before the
+    // arrival so their latency overlaps the atomic's
+    const Bvh2Node pn = ld_node(&nodes[p]);
+    const uint32_t up = parents[p];
     __threadfence();
     if (atomicAdd(&flags[p], 1u) == 0) return;
     __threadfence();
-    inner_costs(nodes, dec, p, max_prims);
-    const uint32_t up = parents[p];
+    inner_costs(pn, dec, p, max_prims);
     if (up == p) return;
     p = up;
   }

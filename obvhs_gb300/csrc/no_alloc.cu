@@ -10,7 +10,7 @@
 // that is part of this library's device image.
 //
 // The scratch array: a file-scope __device__ array of NOALLOC_SCRATCH_BYTES
-// (about 20 MiB, enough for OBVHS_NOALLOC_MAX_PRIMS primitives).  Every GPU on
+// (about 22 MiB, enough for OBVHS_NOALLOC_MAX_PRIMS primitives).  Every GPU on
 // which this entry point runs holds it until the process exits.  On the host,
 // `g_noalloc_scratch` only names the symbol; its device address comes from
 // cudaGetSymbolAddress, taken once per device (with that device current) by
@@ -51,9 +51,10 @@ constexpr size_t OFF_VALS = align256(OFF_KEYS_ALT + (size_t)MAX_PRIMS * sizeof(U
 constexpr size_t OFF_VALS_ALT = align256(OFF_VALS + (size_t)MAX_PRIMS * 4);
 constexpr size_t OFF_RADIX = align256(OFF_VALS_ALT + (size_t)MAX_PRIMS * 4);
 // radix_scratch_words(n) = 16 histograms of 256 words + 16 passes of
-// (tiles of 2048 keys x 256 words + 32); checked against the real function
+// (tiles of 1024 keys (the smallest tile) x 256 words + 32); checked against
+// the real function
 // when a device is set up.
-constexpr size_t RADIX_WORDS = 16 * 256 + 16 * ((size_t)((MAX_PRIMS + 2047) / 2048) * 256 + 32);
+constexpr size_t RADIX_WORDS = 16 * 256 + 16 * ((size_t)((MAX_PRIMS + 1023) / 1024) * 256 + 32);
 constexpr size_t NOALLOC_SCRATCH_BYTES = align256(OFF_RADIX + RADIX_WORDS * 4);
 
 constexpr int MAX_DEVICES = 64;

@@ -6,7 +6,9 @@
 //   k_rs_pass      per digit: tiles claimed in launch order rank their keys
 //                  stably (warp match + per-warp digit counts), publish their
 //                  digit counts and find their global offsets by decoupled
-//                  look-back over earlier tiles, then scatter.
+//                  look-back over earlier tiles, then reorder the tile by
+//                  digit in shared memory and write each digit's run to
+//                  consecutive addresses.
 // No host synchronisation.  The look-back waits only on tiles that were
 // claimed earlier and are therefore resident; every wait is bounded and sets
 // a status bit instead of spinning forever.
@@ -24,9 +26,13 @@ constexpr uint32_t SPIN_LIMIT = 1u << 24;
 constexpr int LB_WINDOW = 8;
 constexpr int HIST_ITEMS = 8;
 
-template <class K>
+// Keys per thread: large sorts take big tiles (fewer tiles to look back
+// over); small sorts take 4 per thread, so more tiles run at once and each
+// tile's ranking chain is 4 rounds instead of 16.
+constexpr uint32_t SMALL_SORT_MAX = 262144;
+template <class K, bool SMALL>
 struct Tile {
-  static constexpr int ITEMS = KeyTraits<K>::BYTES >= 16 ? 8 : 16;
+  static constexpr int ITEMS = SMALL ? 4 : (KeyTraits<K>::BYTES >= 16 ? 8 : 16);
   static constexpr int SIZE = THREADS * ITEMS;
 };
 
@@ -77,17 +83,23 @@ __global__ void __launch_bounds__(THREADS) k_rs_scan(uint32_t* hist) {
 // is input order and each warp ranks its keys stably against its own digit
 // histogram without block barriers; one scan over the warps' histograms per
 // digit then gives every key its place in the tile.
-template <class K>
-__global__ void __launch_bounds__(THREADS, 3) k_rs_pass(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+template <class K, bool SMALL>
+__global__ void __launch_bounds__(THREADS, 2) k_rs_pass(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                                                      K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                                                      uint32_t n, int byte, bool iota,
                                                      const uint32_t* __restrict__ digit_base,
                                                      uint32_t* tile_status, uint32_t* tile_counter, uint32_t* status) {
-  constexpr int ITEMS = Tile<K>::ITEMS;
-  constexpr int TS = Tile<K>::SIZE;
+  constexpr int ITEMS = Tile<K, SMALL>::ITEMS;
+  constexpr int TS = Tile<K, SMALL>::SIZE;
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_wh[WARPS][256];  // per-warp digit counts, then per-warp exclusive offsets
   __shared__ uint32_t s_off[256];        // global offset of each digit for this tile
+  __shared__ uint32_t s_tloc[256];       // start of each digit inside the tile (tile-local order)
+  __shared__ uint32_t s_wsum[WARPS];
+  // the tile in digit order: keys, then (reusing the space) values, and each
+  // slot's digit, so that the scatter writes consecutive addresses per digit
+  __shared__ __align__(16) unsigned char s_stage[TS * (sizeof(K) > 4 ? sizeof(K) : 4)];
+  __shared__ uint8_t s_dig[TS];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) s_tile = atomicAdd(tile_counter, 1u);
 #pragma unroll
@@ -97,7 +109,7 @@ __global__ void __launch_bounds__(THREADS, 3) k_rs_pass(const K* __restrict__ ke
   const uint32_t wbase = tile * TS + warp * 32 * ITEMS;
   const uint32_t lt_mask = (1u << lane) - 1u;
   K key[ITEMS];
-  uint32_t val[ITEMS], rank[ITEMS], dig[ITEMS];
+  uint32_t val[ITEMS], rank[ITEMS];
 #pragma unroll
   for (int r = 0; r < ITEMS; r++) {
     const uint32_t i = wbase + r * 32 + lane;
@@ -112,7 +124,6 @@ __global__ void __launch_bounds__(THREADS, 3) k_rs_pass(const K* __restrict__ ke
     const uint32_t i = wbase + r * 32 + lane;
     const bool valid = i < n;
     const uint32_t d = valid ? KeyTraits<K>::digit(key[r], byte) : 256u;
-    dig[r] = d;
     const uint32_t peers = __match_any_sync(0xffffffffu, d);
     const uint32_t lrank = __popc(peers & lt_mask);
     const uint32_t before = valid ? wh[d] : 0u;
@@ -129,6 +140,35 @@ __global__ void __launch_bounds__(THREADS, 3) k_rs_pass(const K* __restrict__ ke
     const uint32_t c = s_wh[w][tid];
     s_wh[w][tid] = count;
     count += c;
+  }
+  // exclusive scan of this tile's digit counts: the tile in digit order
+  {
+    uint32_t x = count;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_wsum[warp] = x;
+    __syncthreads();
+    uint32_t pre = 0;
+#pragma unroll
+    for (int w = 0; w < WARPS; w++)
+      if (w < warp) pre += s_wsum[w];
+    s_tloc[tid] = pre + x - count;
+  }
+  __syncthreads();
+  // keys to shared memory in digit order (rank[r] becomes the tile position),
+  // which frees their registers before the look-back
+  K* sk = reinterpret_cast<K*>(s_stage);
+#pragma unroll
+  for (int r = 0; r < ITEMS; r++) {
+    if (wbase + r * 32 + lane < n) {
+      const uint32_t d = KeyTraits<K>::digit(key[r], byte);
+      rank[r] += s_tloc[d] + wh[d];
+      sk[rank[r]] = key[r];
+      s_dig[rank[r]] = (uint8_t)d;
+    }
   }
   // publish this tile's count of digit `tid`, then look back for the prefix,
   // LB_WINDOW earlier tiles per step (positions before tile 0 read as an
@@ -170,13 +210,21 @@ __global__ void __launch_bounds__(THREADS, 3) k_rs_pass(const K* __restrict__ ke
   }
   s_off[tid] = digit_base[tid] + prefix;
   __syncthreads();
+  // each digit's run of the tile to consecutive addresses
+  const uint32_t tile_n = min((uint32_t)TS, n - tile * TS);
+  for (uint32_t j = tid; j < tile_n; j += THREADS) {
+    const uint32_t d = s_dig[j];
+    keys_out[s_off[d] + (j - s_tloc[d])] = sk[j];
+  }
+  __syncthreads();
+  uint32_t* sv = reinterpret_cast<uint32_t*>(s_stage);
 #pragma unroll
-  for (int r = 0; r < ITEMS; r++) {
-    if (dig[r] < 256) {
-      const uint32_t pos = s_off[dig[r]] + wh[dig[r]] + rank[r];
-      keys_out[pos] = key[r];
-      vals_out[pos] = val[r];
-    }
+  for (int r = 0; r < ITEMS; r++)
+    if (wbase + r * 32 + lane < n) sv[rank[r]] = val[r];
+  __syncthreads();
+  for (uint32_t j = tid; j < tile_n; j += THREADS) {
+    const uint32_t d = s_dig[j];
+    vals_out[s_off[d] + (j - s_tloc[d])] = sv[j];
   }
 }
 
@@ -186,7 +234,7 @@ __global__ void k_iota(uint32_t* v, uint32_t n) {
 
 }  // namespace
 
-uint32_t radix_tile_count(uint32_t n) { return (n + 2047) / 2048; }
+uint32_t radix_tile_count(uint32_t n) { return (n + 1023) / 1024; }  // the smallest tile
 
 size_t radix_scratch_words(uint32_t n) {
   // 16 histograms of 256 + per pass: tile status (256 per tile) + counter
@@ -198,7 +246,8 @@ cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, 
                              uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt, int digits) {
   constexpr int NB = KeyTraits<K>::BYTES;
   const int nd = digits > 0 && digits < NB ? digits : NB;
-  constexpr int TS = Tile<K>::SIZE;
+  const bool small = n <= SMALL_SORT_MAX;
+  const int TS = small ? Tile<K, true>::SIZE : Tile<K, false>::SIZE;
   *result_in_alt = false;
   if (n == 0) return cudaSuccess;
   const uint32_t ntiles = (n + TS - 1) / TS;
@@ -217,8 +266,12 @@ cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, 
   bool iota = init_iota;
   for (int b = 0; b < nd; b++) {
     uint32_t* ts = pass_area + (size_t)b * pass_words;
-    KLAUNCH("k_rs_pass", k_rs_pass<K><<<ntiles, THREADS, 0, c.stream>>>(kin, vin, kout, vout, n, b, iota,
-                                                                         hist + b * 256, ts + 32, ts, c.d_status));
+    if (small)
+      KLAUNCH("k_rs_pass", k_rs_pass<K, true><<<ntiles, THREADS, 0, c.stream>>>(kin, vin, kout, vout, n, b, iota,
+                                                                               hist + b * 256, ts + 32, ts, c.d_status));
+    else
+      KLAUNCH("k_rs_pass", k_rs_pass<K, false><<<ntiles, THREADS, 0, c.stream>>>(kin, vin, kout, vout, n, b, iota,
+                                                                                hist + b * 256, ts + 32, ts, c.d_status));
     iota = false;
     std::swap(kin, kout);
     std::swap(vin, vout);
