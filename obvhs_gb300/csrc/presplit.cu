@@ -93,6 +93,34 @@ __global__ void __launch_bounds__(BLK) k_block_dsum(const float* __restrict__ ha
   }
 }
 
+// Exclusive prefix of the block sums in place (one block, chunks of 1024
+// with a carry): each block's approximate running sum at its start.
+__global__ void __launch_bounds__(1024) k_scan_dsum(double* bsum, uint32_t nb) {
+  __shared__ double sw[32];
+  __shared__ double carry;
+  if (threadIdx.x == 0) carry = 0.0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint32_t c0 = 0; c0 < nb; c0 += 1024) {
+    const uint32_t i = c0 + threadIdx.x;
+    const double v = i < nb ? bsum[i] : 0.0;
+    double x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) sw[warp] = x;
+    __syncthreads();
+    double pre = carry;
+    for (int w = 0; w < warp; w++) pre += sw[w];
+    if (i < nb) bsum[i] = pre + x - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = pre + x;
+    __syncthreads();
+  }
+}
+
 // A block's effect inside one binade: increments (even start, odd start)
 // and whether every element stays below the binade's width.
 struct Mono {
@@ -127,9 +155,8 @@ __device__ __forceinline__ Mono shfl_down_mono(const Mono& v, int o) {
 }
 
 __global__ void __launch_bounds__(BLK) k_block_transform(const float* __restrict__ ha, uint32_t n,
-                                                         const double* __restrict__ bsum, BlockT* __restrict__ out) {
+                                                         const double* __restrict__ bstart, BlockT* __restrict__ out) {
   constexpr int PER = SUM_BLOCK / BLK;  // consecutive elements per thread
-  __shared__ double sw[BLK / 32];
   __shared__ Mono sm[BLK / 32];
   const uint32_t b = blockIdx.x;
   const uint32_t base = b * SUM_BLOCK;
@@ -140,15 +167,8 @@ __global__ void __launch_bounds__(BLK) k_block_transform(const float* __restrict
     const uint32_t i = base + threadIdx.x * PER + k;
     v[k] = i < n ? ha[i] : 0.0f;
   }
-  // approximate running sum at the block start: sum of the earlier blocks
-  double acc = 0.0;
-  for (uint32_t k = threadIdx.x; k < b; k += BLK) acc += bsum[k];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (lane == 0) sw[warp] = acc;
-  __syncthreads();
-  double start = 0.0;
-  for (int w = 0; w < BLK / 32; w++) start += sw[w];
+  // approximate running sum at the block start (the scanned block sums)
+  const double start = bstart[b];
   const int e0 = start > 0.0 ? ilogb(start) : -200;
   for (int ci = 0; ci < NCAND_E; ci++) {
     const int e = e0 - 1 + ci;
@@ -574,6 +594,7 @@ int presplit_device(BuildCtx& c, const float* tris, uint32_t n, float** aabbs_ou
     BlockT* tr = (BlockT*)s.get(SLOT_TILE_HIST, (size_t)nb * sizeof(BlockT) + 16);
     if (!bsum || !tr) return c.fail(OBVHS_ERR_OOM, "scratch");
     KLAUNCH("k_block_dsum", k_block_dsum<<<nb, BLK, 0, c.stream>>>(ha, n, bsum));
+    KLAUNCH("k_scan_dsum", k_scan_dsum<<<1, 1024, 0, c.stream>>>(bsum, nb));
     KLAUNCH("k_block_transform", k_block_transform<<<nb, BLK, 0, c.stream>>>(ha, n, bsum, tr));
     KLAUNCH("k_sum_chain", k_sum_chain<<<1, 32, 0, c.stream>>>(ha, n, tr, largest_key, thr));
   }

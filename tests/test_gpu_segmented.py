@@ -150,3 +150,38 @@ def test_segmented_while_other_contexts_are_live(G):
     finally:
         for c in others:
             c.close()
+
+
+def _deep_chain(n=220):
+    """Triangles along the x axis with gaps growing by 8% each: nearest
+    neighbours point back along the chain, so PLOC merges only a few pairs per
+    pass (115 passes for 220 triangles with slow_build's search: more than 95,
+    the unclamped reinsertion search stack)."""
+    x = np.cumsum(1.08 ** np.arange(n)).astype(np.float32)
+    t = np.zeros((n, 3, 3), np.float32)
+    t[:, 0, 0] = x
+    t[:, 1, 0] = x + 0.01
+    t[:, 2, 0] = x
+    t[:, 2, 1] = 0.01
+    return t.reshape(-1, 9)
+
+
+def test_deep_scene_alone_and_in_a_batch(G):
+    """A scene whose PLOC needs more than 95 passes (reinsertion with the
+    unclamped search stack), alone against the oracle, and in a segmented
+    batch beside ordinary scenes (per-scene stack modes in one launch)."""
+    deep = _deep_chain()
+    p = BvhBuildParams.slow_build()
+    p.pre_split = False  # keep the chain exact: pre-splits would add leaves
+    one = G.build_cwbvh_from_tris(deep, p)
+    assert one.stats.ploc_passes > 95
+    ob = O.build(tris=deep, params=p, nthreads=4, keep_intermediate=False)
+    nodes, prims = one.download()
+    assert nodes.tobytes() == ob.cw_nodes.tobytes() and prims.tobytes() == ob.cw_pidx.tobytes()
+    assert one.stats.reinsertions == ob.reinsertions
+    scenes = [S.scene2_tris(3000, offset=1), deep, S.scene2_tris(20_000, offset=2)]
+    seg = G.build_cwbvh_from_tris_segmented(scenes, p)
+    for tris, cw in zip(scenes, seg):
+        alone = G.build_cwbvh_from_tris(tris, p)
+        assert _same(cw.download(), alone.download())
+        alone.free()
