@@ -1,6 +1,7 @@
 // api.cu -- the extern "C" entry points declared in include/obvhs_gb300.h.
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <thread>
@@ -55,6 +56,7 @@ const void* stage_in(BuildCtx& c, int slot, const void* p, size_t bytes, int dev
 }
 
 __global__ void k_iota_u32(uint32_t* v, uint32_t n) {
+  grid_dep_wait();
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) v[i] = i;
 }
@@ -148,7 +150,7 @@ int build_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t 
     if (leaf_idx)
       CK(cudaMemcpyAsync(b2.prim_indices, leaf_idx, (size_t)m * 4, cudaMemcpyDeviceToDevice, c.stream));
     else {
-      KLAUNCH("k_iota_u32", k_iota_u32<<<div_up<uint32_t>(m, 256), 256, 0, c.stream>>>(b2.prim_indices, m));
+      KLAUNCH("k_iota_u32", launch_k(k_iota_u32, div_up<uint32_t>(m, 256), 256, 0, c.stream, b2.prim_indices, m));
     }
   }
   // Host round trips inside the build: the pre-split count (when splitting),
@@ -447,6 +449,14 @@ DeviceShared& device_shared(int device) {
 
 }  // namespace
 
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("OBVHS_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 int device_context_count(int device) { return device_shared(device).contexts.load(); }
 int device_concurrent_builds(int device) { return device_shared(device).builds.load(); }
 void device_build_enter(int device) { device_shared(device).builds.fetch_add(1); }
@@ -626,7 +636,7 @@ int obvhs_ploc_build(obvhs_ctx* cp, const float* aabbs, const uint32_t* indices,
     if (di) {
       cudaMemcpyAsync(b->prim_indices, di, (size_t)n * 4, cudaMemcpyDeviceToDevice, c.stream);
     } else {
-      KLAUNCH("k_iota_u32", k_iota_u32<<<div_up<uint32_t>(n, 256), 256, 0, c.stream>>>(b->prim_indices, n));
+      KLAUNCH("k_iota_u32", launch_k(k_iota_u32, div_up<uint32_t>(n, 256), 256, 0, c.stream, b->prim_indices, n));
     }
   }
   if (!r) r = take_status(c);
@@ -1142,7 +1152,7 @@ static int bvh2_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uin
       if (cudaMemcpyAsync(b->prim_indices, leaf_idx, (size_t)m * 4, cudaMemcpyDeviceToDevice, c.stream))
         return fail(c.fail(OBVHS_ERR_CUDA, "copy"));
     } else {
-      KLAUNCH("k_iota_u32", k_iota_u32<<<div_up<uint32_t>(m, 256), 256, 0, c.stream>>>(b->prim_indices, m));
+      KLAUNCH("k_iota_u32", launch_k(k_iota_u32, div_up<uint32_t>(m, 256), 256, 0, c.stream, b->prim_indices, m));
     }
   }
   uint32_t passes = 0;

@@ -7,6 +7,7 @@
 #include <functional>
 #include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -195,6 +196,27 @@ struct BuildScope {
 // Only the launch forms change (one block instead of a grid-wide launch for
 // PLOC up to 262,144 leaves and for reinsertion resolves); results do not.
 inline bool gpu_shared(const obvhs_ctx& c) { return c.shared_gpu || device_concurrent_builds(c.device) > 1; }
+
+// Launches a kernel on stream `s` with the programmatic-serialization
+// attribute (a dependent launch: the kernel may be scheduled while the
+// previous kernel drains, then waits in grid_dep_wait) unless dependent
+// launches are switched off (OBVHS_PDL=0 in the environment).  Errors are
+// returned and, like a <<<>>> launch, recorded for cudaGetLastError.
+bool pdl_enabled();
+template <class... P, class... A>
+inline cudaError_t launch_k(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
+}
 
 // Launch wrapper: counts the launch and, when profiling, brackets it with
 // CUDA events on the context's stream.

@@ -32,6 +32,7 @@ constexpr uint32_t SCAN_TILE = BLK * SCAN_ITEMS;
 
 __global__ void k_collapse_init(uint32_t n, uint32_t* __restrict__ nc, uint32_t* __restrict__ pc,
                                 uint32_t* __restrict__ flags) {
+  grid_dep_wait();
   const uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i >= n) return;
   nc[i] = 1;
@@ -42,6 +43,7 @@ __global__ void k_collapse_init(uint32_t n, uint32_t* __restrict__ nc, uint32_t*
 __global__ void k_collapse_decide(const Bvh2Node* __restrict__ nodes, const uint32_t* __restrict__ parents,
                                   uint32_t n, uint32_t max_prims, float traversal_cost, uint32_t* nc, uint32_t* pc,
                                   uint32_t* flags, uint32_t* status) {
+  grid_dep_wait();
   const uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i == 0 || i >= n) return;
   const Bvh2Node leaf = ld_node(&nodes[i]);
@@ -77,6 +79,7 @@ __global__ void k_collapse_decide(const Bvh2Node* __restrict__ nodes, const uint
 // Inclusive scan of two u32 arrays at once: tiles, then the tile totals (one
 // block, sequential over chunks), then the tile offsets added.
 __global__ void __launch_bounds__(BLK) k_scan2_tiles(uint32_t* a, uint32_t* b, uint32_t n, uint2* totals) {
+  grid_dep_wait();
   __shared__ uint2 sw[BLK / 32];
   const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
   uint32_t va[SCAN_ITEMS], vb[SCAN_ITEMS];
@@ -123,6 +126,7 @@ __global__ void __launch_bounds__(BLK) k_scan2_tiles(uint32_t* a, uint32_t* b, u
 }
 
 __global__ void __launch_bounds__(1024) k_scan2_totals(uint2* totals, uint32_t m) {
+  grid_dep_wait();
   __shared__ uint2 sw[32];
   __shared__ uint2 carry;
   if (threadIdx.x == 0) carry = make_uint2(0u, 0u);
@@ -155,6 +159,7 @@ __global__ void __launch_bounds__(1024) k_scan2_totals(uint2* totals, uint32_t m
 }
 
 __global__ void __launch_bounds__(BLK) k_scan2_add(uint32_t* a, uint32_t* b, uint32_t n, const uint2* totals) {
+  grid_dep_wait();
   const uint2 off = totals[blockIdx.x];
   const uint32_t base = blockIdx.x * SCAN_TILE;
   for (uint32_t k = threadIdx.x; k < SCAN_TILE; k += BLK) {
@@ -171,6 +176,7 @@ __global__ void k_collapse_emit(const Bvh2Node* __restrict__ nodes, const uint32
                                 const uint32_t* __restrict__ pc, uint32_t n, uint32_t n_out_nodes,
                                 uint32_t n_out_prims, Bvh2Node* __restrict__ out_nodes,
                                 uint32_t* __restrict__ out_pidx, uint32_t* status) {
+  grid_dep_wait();
   const uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i >= n) return;
   Bvh2Node nd = ld_node(&nodes[i]);
@@ -220,6 +226,7 @@ __global__ void k_collapse_emit(const Bvh2Node* __restrict__ nodes, const uint32
 // (unions are exact, so any children-first order gives the reference's boxes)
 __global__ void k_refit_climb(Bvh2Node* nodes, const uint32_t* __restrict__ parents, uint32_t n, uint32_t* flags,
                               uint32_t* status) {
+  grid_dep_wait();
   const uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i >= n) return;
   const Bvh2Node leaf = ld_node_cg(&nodes[i]);
@@ -250,6 +257,7 @@ __global__ void k_refit_climb(Bvh2Node* nodes, const uint32_t* __restrict__ pare
 // node another climb already flagged.
 __global__ void k_rebuild_flags(const uint32_t* __restrict__ leaves, uint32_t n_leaves,
                                 const uint32_t* __restrict__ parents, uint32_t n, uint32_t* flags, uint32_t* status) {
+  grid_dep_wait();
   const uint32_t k = blockIdx.x * BLK + threadIdx.x;
   if (k >= n_leaves) return;
   uint32_t idx = leaves[k];
@@ -270,6 +278,7 @@ __global__ void k_rebuild_flags(const uint32_t* __restrict__ leaves, uint32_t n_
 // equal-Morton-code ties, so one thread walks it exactly as the reference.
 __global__ void k_rebuild_collect(Bvh2Node* nodes, uint32_t n, const uint32_t* __restrict__ flags,
                                   uint32_t* stack, Bvh2Node* __restrict__ out, uint32_t* count, uint32_t* status) {
+  grid_dep_wait();
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   uint32_t sp = 0, c = 0;
   stack[sp++] = node_first(ld_node(&nodes[0]));
@@ -305,6 +314,7 @@ __global__ void k_rebuild_collect(Bvh2Node* nodes, uint32_t n, const uint32_t* _
 
 // full_rebuild's leaves in node order: flag, scan, compact.
 __global__ void k_leaf_flags(const Bvh2Node* __restrict__ nodes, uint32_t n, uint32_t* flag, uint32_t* dummy) {
+  grid_dep_wait();
   const uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i >= n) return;
   flag[i] = node_prims(ld_node(&nodes[i])) != 0 ? 1u : 0u;
@@ -312,6 +322,7 @@ __global__ void k_leaf_flags(const Bvh2Node* __restrict__ nodes, uint32_t n, uin
 }
 __global__ void k_compact_leaves(const Bvh2Node* __restrict__ nodes, uint32_t n, const uint32_t* __restrict__ incl,
                                  Bvh2Node* __restrict__ out) {
+  grid_dep_wait();
   const uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i >= n) return;
   const uint32_t before = i ? incl[i - 1] : 0u;
@@ -322,6 +333,7 @@ __global__ void k_compact_leaves(const Bvh2Node* __restrict__ nodes, uint32_t n,
 // merge of the rebuild takes the k-th pair from the top, i.e. remap[(v - 1)
 // / 2] for its virtual left slot v = 2 m - 3 - 2 k.
 __global__ void k_pair_flags(const Bvh2Node* __restrict__ nodes, uint32_t n_pairs, uint32_t* flag, uint32_t* dummy) {
+  grid_dep_wait();
   const uint32_t j = blockIdx.x * BLK + threadIdx.x;
   if (j >= n_pairs) return;
   flag[j] = (node_prims(ld_node(&nodes[2 * j + 1])) & 0x80000000u) ? 1u : 0u;
@@ -329,6 +341,7 @@ __global__ void k_pair_flags(const Bvh2Node* __restrict__ nodes, uint32_t n_pair
 }
 __global__ void k_compact_pairs(uint32_t n_pairs, const uint32_t* __restrict__ incl, uint32_t* __restrict__ remap,
                                 uint32_t cap) {
+  grid_dep_wait();
   const uint32_t j = blockIdx.x * BLK + threadIdx.x;
   if (j >= n_pairs) return;
   const uint32_t before = j ? incl[j - 1] : 0u;
@@ -337,6 +350,7 @@ __global__ void k_compact_pairs(uint32_t n_pairs, const uint32_t* __restrict__ i
 
 // The rebuild's Morton frame: the old root box as it is (min, max).
 __global__ void k_total_from_root(const Bvh2Node* __restrict__ nodes, int* total_keys) {
+  grid_dep_wait();
   if (threadIdx.x != 0) return;
   const Bvh2Node r = ld_node(&nodes[0]);
   total_keys[0] = fkey(r.a.x);
@@ -370,12 +384,12 @@ int bvh2_collapse_device(BuildCtx& c, obvhs_bvh2* b, uint32_t max_prims, float t
   int r = compute_parents_device(c, b->nodes, n, parents);
   if (r) return r;
   const uint32_t g = div_up<uint32_t>(n, BLK);
-  KLAUNCH("k_collapse_init", k_collapse_init<<<g, BLK, 0, c.stream>>>(n, nc, pc, flags));
-  KLAUNCH("k_collapse_decide", k_collapse_decide<<<g, BLK, 0, c.stream>>>(b->nodes, parents, n, max_prims,
+  KLAUNCH("k_collapse_init", launch_k(k_collapse_init, g, BLK, 0, c.stream, n, nc, pc, flags));
+  KLAUNCH("k_collapse_decide", launch_k(k_collapse_decide, g, BLK, 0, c.stream, b->nodes, parents, n, max_prims,
                                                                          traversal_cost, nc, pc, flags, c.d_status));
-  KLAUNCH("k_scan2_tiles", k_scan2_tiles<<<tiles, BLK, 0, c.stream>>>(nc, pc, n, totals));
-  KLAUNCH("k_scan2_totals", k_scan2_totals<<<1, 1024, 0, c.stream>>>(totals, tiles));
-  KLAUNCH("k_scan2_add", k_scan2_add<<<tiles, BLK, 0, c.stream>>>(nc, pc, n, totals));
+  KLAUNCH("k_scan2_tiles", launch_k(k_scan2_tiles, tiles, BLK, 0, c.stream, nc, pc, n, totals));
+  KLAUNCH("k_scan2_totals", launch_k(k_scan2_totals, 1, 1024, 0, c.stream, totals, tiles));
+  KLAUNCH("k_scan2_add", launch_k(k_scan2_add, tiles, BLK, 0, c.stream, nc, pc, n, totals));
   CK(cudaGetLastError());
   uint32_t last[2] = {0, 0}, root_prims = 0;
   CK(cudaMemcpyAsync(&last[0], nc + n - 1, 4, cudaMemcpyDeviceToHost, c.stream));
@@ -400,7 +414,7 @@ int bvh2_collapse_device(BuildCtx& c, obvhs_bvh2* b, uint32_t max_prims, float t
     if (on) cudaFree(on);
     return c.fail(OBVHS_ERR_OOM, "collapsed BVH2");
   }
-  KLAUNCH("k_collapse_emit", k_collapse_emit<<<g, BLK, 0, c.stream>>>(b->nodes, b->prim_indices, parents, nc, pc, n,
+  KLAUNCH("k_collapse_emit", launch_k(k_collapse_emit, g, BLK, 0, c.stream, b->nodes, b->prim_indices, parents, nc, pc, n,
                                                                      last[0], last[1], on, op, c.d_status));
   const cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) cudaStreamSynchronize(c.stream);
@@ -422,6 +436,7 @@ namespace {
 // Bvh2Node::set_aabb for the given nodes (the boxes of moved leaves).
 __global__ void k_set_node_aabbs(Bvh2Node* nodes, uint32_t n, const uint32_t* __restrict__ ids,
                                  const float* __restrict__ aabbs, uint32_t m, uint32_t* status) {
+  grid_dep_wait();
   const uint32_t k = blockIdx.x * BLK + threadIdx.x;
   if (k >= m) return;
   const uint32_t i = ids[k];
@@ -439,7 +454,7 @@ __global__ void k_set_node_aabbs(Bvh2Node* nodes, uint32_t n, const uint32_t* __
 
 int bvh2_set_node_aabbs_device(BuildCtx& c, obvhs_bvh2* b, const uint32_t* d_ids, const float* d_aabbs, uint32_t m) {
   if (!m) return 0;
-  KLAUNCH("k_set_node_aabbs", k_set_node_aabbs<<<div_up<uint32_t>(m, BLK), BLK, 0, c.stream>>>(
+  KLAUNCH("k_set_node_aabbs", launch_k(k_set_node_aabbs, div_up<uint32_t>(m, BLK), BLK, 0, c.stream,
                                   b->nodes, b->n_nodes, d_ids, d_aabbs, m, c.d_status));
   CK(cudaGetLastError());
   return 0;
@@ -450,9 +465,9 @@ int scan2_device(BuildCtx& c, uint32_t* a, uint32_t* b, uint32_t n) {
   const uint32_t tiles = div_up<uint32_t>(n, SCAN_TILE);
   uint2* totals = (uint2*)c.scratch.get(SLOT_PARTIAL, (size_t)std::max(tiles, 1u) * sizeof(uint2));
   if (!totals) return c.fail(OBVHS_ERR_OOM, "scratch");
-  KLAUNCH("k_scan2_tiles", k_scan2_tiles<<<tiles, BLK, 0, c.stream>>>(a, b, n, totals));
-  KLAUNCH("k_scan2_totals", k_scan2_totals<<<1, 1024, 0, c.stream>>>(totals, tiles));
-  KLAUNCH("k_scan2_add", k_scan2_add<<<tiles, BLK, 0, c.stream>>>(a, b, n, totals));
+  KLAUNCH("k_scan2_tiles", launch_k(k_scan2_tiles, tiles, BLK, 0, c.stream, a, b, n, totals));
+  KLAUNCH("k_scan2_totals", launch_k(k_scan2_totals, 1, 1024, 0, c.stream, totals, tiles));
+  KLAUNCH("k_scan2_add", launch_k(k_scan2_add, tiles, BLK, 0, c.stream, a, b, n, totals));
   CK(cudaGetLastError());
   return 0;
 }
@@ -467,7 +482,7 @@ int bvh2_refit_all_device(BuildCtx& c, obvhs_bvh2* b) {
   int r = compute_parents_device(c, b->nodes, n, parents);
   if (r) return r;
   CK(cudaMemsetAsync(flags, 0, (size_t)n * 4, c.stream));
-  KLAUNCH("k_refit_climb", k_refit_climb<<<div_up<uint32_t>(n, BLK), BLK, 0, c.stream>>>(b->nodes, parents, n, flags,
+  KLAUNCH("k_refit_climb", launch_k(k_refit_climb, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, b->nodes, parents, n, flags,
                                                                                         c.d_status));
   CK(cudaGetLastError());
   return 0;
@@ -486,14 +501,14 @@ int bvh2_rebuild_device(BuildCtx& c, obvhs_bvh2* b, const uint32_t* d_leaves, ui
   uint32_t* cnt = (uint32_t*)s.get(SLOT_CW_COUNTERS, 64);
   if (!col || !total || !fa || !fb || !remap || !cnt) return c.fail(OBVHS_ERR_OOM, "scratch");
   const uint32_t g = div_up<uint32_t>(n, BLK);
-  KLAUNCH("k_total_from_root", k_total_from_root<<<1, 32, 0, c.stream>>>(b->nodes, total));
+  KLAUNCH("k_total_from_root", launch_k(k_total_from_root, 1, 32, 0, c.stream, b->nodes, total));
   uint32_t m = 0;
   int r;
   if (!d_leaves) {
     // full_rebuild: the leaves in node order, a fresh tree of 2m - 1 nodes
-    KLAUNCH("k_leaf_flags", k_leaf_flags<<<g, BLK, 0, c.stream>>>(b->nodes, n, fa, fb));
+    KLAUNCH("k_leaf_flags", launch_k(k_leaf_flags, g, BLK, 0, c.stream, b->nodes, n, fa, fb));
     if ((r = scan2_device(c, fa, fb, n))) return r;
-    KLAUNCH("k_compact_leaves", k_compact_leaves<<<g, BLK, 0, c.stream>>>(b->nodes, n, fa, col));
+    KLAUNCH("k_compact_leaves", launch_k(k_compact_leaves, g, BLK, 0, c.stream, b->nodes, n, fa, col));
     CK(cudaMemcpyAsync(&m, fa + n - 1, 4, cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
     if (m == 0 || 2 * (uint64_t)m - 1 != n) return c.fail(OBVHS_ERR_BAD_INPUT, "not a full binary tree");
@@ -512,12 +527,12 @@ int bvh2_rebuild_device(BuildCtx& c, obvhs_bvh2* b, const uint32_t* d_leaves, ui
   if ((r = compute_parents_device(c, b->nodes, n, parents))) return r;
   CK(cudaMemsetAsync(flags, 0, (size_t)n * 4, c.stream));
   if (n_leaves)
-    KLAUNCH("k_rebuild_flags", k_rebuild_flags<<<div_up<uint32_t>(n_leaves, BLK), BLK, 0, c.stream>>>(
+    KLAUNCH("k_rebuild_flags", launch_k(k_rebuild_flags, div_up<uint32_t>(n_leaves, BLK), BLK, 0, c.stream,
                                    d_leaves, n_leaves, parents, n, flags, c.d_status));
-  KLAUNCH("k_rebuild_collect", k_rebuild_collect<<<1, 32, 0, c.stream>>>(b->nodes, n, flags, stack, col, cnt,
+  KLAUNCH("k_rebuild_collect", launch_k(k_rebuild_collect, 1, 32, 0, c.stream, b->nodes, n, flags, stack, col, cnt,
                                                                          c.d_status));
   const uint32_t n_pairs = (n - 1) / 2;
-  KLAUNCH("k_pair_flags", k_pair_flags<<<div_up<uint32_t>(n_pairs, BLK), BLK, 0, c.stream>>>(b->nodes, n_pairs, fa, fb));
+  KLAUNCH("k_pair_flags", launch_k(k_pair_flags, div_up<uint32_t>(n_pairs, BLK), BLK, 0, c.stream, b->nodes, n_pairs, fa, fb));
   if ((r = scan2_device(c, fa, fb, n_pairs))) return r;
   uint32_t h[2] = {0, 0};
   CK(cudaMemcpyAsync(&h[0], cnt, 4, cudaMemcpyDeviceToHost, c.stream));
@@ -527,7 +542,7 @@ int bvh2_rebuild_device(BuildCtx& c, obvhs_bvh2* b, const uint32_t* d_leaves, ui
   if (*c.h_status) return 0;  // reported by the caller's status check
   m = h[0];
   if (m < 1 || h[1] != m - 1) return c.fail(OBVHS_ERR_BAD_INPUT, "rebuild slots do not match the collected nodes");
-  KLAUNCH("k_compact_pairs", k_compact_pairs<<<div_up<uint32_t>(n_pairs, BLK), BLK, 0, c.stream>>>(n_pairs, fa, remap,
+  KLAUNCH("k_compact_pairs", launch_k(k_compact_pairs, div_up<uint32_t>(n_pairs, BLK), BLK, 0, c.stream, n_pairs, fa, remap,
                                                                                                   m - 1));
   uint32_t passes = 0;
   uint64_t sum = 0;

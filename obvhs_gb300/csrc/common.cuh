@@ -22,6 +22,15 @@ enum : uint32_t {
   ST_BAD_TREE = 1u << 4,       // malformed node links in an uploaded tree
 };
 
+// Programmatic dependent launch.  Every kernel of this library starts with
+// this wait: when a kernel is launched with the programmatic-serialization
+// attribute it may be scheduled while the previous kernel in the stream
+// drains, and the wait returns once that kernel has completed and its
+// memory is visible.  Because every kernel waits before its first access,
+// completion of a kernel implies completion of all earlier ones.  For a
+// plain launch the wait returns at once.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ float smin(float a, float b) { return a < b ? a : b; }
 __device__ __forceinline__ float smax(float a, float b) { return a > b ? a : b; }
 

@@ -160,6 +160,7 @@ __device__ void inner_costs(const Bvh2Node& nd, Dec* dec, uint32_t x, uint32_t m
 __global__ void __launch_bounds__(BLK) k_costs(const Bvh2Node* __restrict__ nodes, const uint32_t* __restrict__ parents,
                                                uint32_t n, uint32_t max_prims, Dec* dec, uint32_t* flags,
                                                uint32_t* status) {
+  grid_dep_wait();
   const uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i >= n) return;
   const Bvh2Node nd = ld_node(&nodes[i]);
@@ -510,6 +511,7 @@ __device__ void emit_node(const EmitArgs& a, const Item it, int lane, uint8_t* s
 }
 
 __global__ void __launch_bounds__(EMIT_THREADS) k_emit_all(EmitArgs a) {
+  grid_dep_wait();
   __shared__ __align__(16) uint8_t stage[EMIT_THREADS / 32][80];
   const int lane = threadIdx.x & 31;
   uint32_t mine = 0;
@@ -557,6 +559,7 @@ static_assert(sizeof(SegRoot) == 128, "SegRoot layout");
 __global__ void k_seg_roots_out(const Bvh2Node* __restrict__ nodes, const Dec* dec,
                                 const uint32_t* __restrict__ prim_start, const uint32_t* __restrict__ node_start,
                                 uint32_t n_seg, SegRoot* __restrict__ out) {
+  grid_dep_wait();
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_seg || prim_start[s + 1] == prim_start[s]) return;
   const uint32_t nb = node_start[s];
@@ -571,6 +574,7 @@ __global__ void k_seg_roots_out(const Bvh2Node* __restrict__ nodes, const Dec* d
 __global__ void k_seg_emit_init(const uint32_t* __restrict__ prim_start, const uint32_t* __restrict__ node_start,
                                 const uint32_t* __restrict__ root_slot, uint32_t n_seg, uint32_t n_roots,
                                 Item* __restrict__ items, uint32_t* __restrict__ ready, uint32_t* __restrict__ ctr) {
+  grid_dep_wait();
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0) {
     ctr[0] = 0;        // head
@@ -786,6 +790,7 @@ __device__ void order_node(const OrderArgs& a, uint32_t ni, int lane, uint8_t* o
 }
 
 __global__ void __launch_bounds__(EMIT_THREADS) k_order_children(OrderArgs a) {
+  grid_dep_wait();
   __shared__ __align__(16) uint8_t old_s[EMIT_THREADS / 32][80];
   __shared__ __align__(16) uint8_t new_s[EMIT_THREADS / 32][80];
   __shared__ uint4 kids_s[EMIT_THREADS / 32][8 * 5];
@@ -868,7 +873,7 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   int r = compute_parents_device(c, b->nodes, n, parents);
   if (r) return r;
   CK(cudaMemsetAsync(flags, 0, (size_t)n * 4, c.stream));
-  KLAUNCH("k_costs", k_costs<<<div_up<uint32_t>(n, BLK), BLK, 0, c.stream>>>(b->nodes, parents, n, max_prims, dec,
+  KLAUNCH("k_costs", launch_k(k_costs, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, b->nodes, parents, n, max_prims, dec,
                                                                              flags, c.d_status));
   CK(cudaGetLastError());
   // sizes of the whole tree: the root's aggregate (a leaf root is one node)
@@ -929,7 +934,7 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   std::memcpy(ea.log2_thr, ceil_log2_thresholds(), sizeof(ea.log2_thr));
   const uint32_t grid = (uint32_t)std::min<uint64_t>(
       emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)n_cw * 32, EMIT_THREADS)));
-  KLAUNCH("k_emit_all", k_emit_all<<<grid, EMIT_THREADS, 0, c.stream>>>(ea));
+  KLAUNCH("k_emit_all", launch_k(k_emit_all, grid, EMIT_THREADS, 0, c.stream, ea));
   CK(cudaGetLastError());
   out->nodes = cwn;
   out->n_nodes = n_cw;
@@ -989,9 +994,9 @@ int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in
   r = seg_root_parents_device(c, L, parents);
   if (r) return r;
   CK(cudaMemsetAsync(flags, 0, (size_t)n * 4, c.stream));
-  KLAUNCH("k_costs", k_costs<<<div_up<uint32_t>(n, BLK), BLK, 0, c.stream>>>(nodes, parents, n, max_prims, dec, flags,
+  KLAUNCH("k_costs", launch_k(k_costs, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, nodes, parents, n, max_prims, dec, flags,
                                                                              c.d_status));
-  KLAUNCH("k_seg_roots_out", k_seg_roots_out<<<div_up<uint32_t>(S, BLK), BLK, 0, c.stream>>>(
+  KLAUNCH("k_seg_roots_out", launch_k(k_seg_roots_out, div_up<uint32_t>(S, BLK), BLK, 0, c.stream,
                                  nodes, dec, L.d_prim_start, L.d_node_start, S, roots));
   CK(cudaGetLastError());
   std::vector<SegRoot> hr(S);
@@ -1083,7 +1088,7 @@ int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in
     emit_blocks_s.store(emit_blocks);
   }
   CK(cudaMemsetAsync(ready, 0, (size_t)q_total * 4, c.stream));
-  KLAUNCH("k_seg_emit_init", k_seg_emit_init<<<div_up<uint32_t>(S, BLK), BLK, 0, c.stream>>>(
+  KLAUNCH("k_seg_emit_init", launch_k(k_seg_emit_init, div_up<uint32_t>(S, BLK), BLK, 0, c.stream,
                                  L.d_prim_start, L.d_node_start, d_slots, S, n_roots, items, ready, counters + 12));
   EmitArgs ea{{},      nodes,     pidx_in,         dec,      items,      ready, counters + 12, counters + 13,
               order_children, q_total, EmitOut{nullptr, nullptr, 0, 0, nullptr}, d_eo, L.d_node_start, S, c.d_status,
@@ -1091,7 +1096,7 @@ int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in
   std::memcpy(ea.log2_thr, ceil_log2_thresholds(), sizeof(ea.log2_thr));
   const uint32_t grid = (uint32_t)std::min<uint64_t>(
       emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)q_total * 32, EMIT_THREADS)));
-  KLAUNCH("k_emit_all", k_emit_all<<<grid, EMIT_THREADS, 0, c.stream>>>(ea));
+  KLAUNCH("k_emit_all", launch_k(k_emit_all, grid, EMIT_THREADS, 0, c.stream, ea));
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(emitted_deferred, counters + 14, 4, cudaMemcpyDeviceToHost, c.stream));
   *emitted_expected = q_total;
@@ -1138,7 +1143,7 @@ int cwbvh_order_children_device(BuildCtx& c, obvhs_cwbvh* b, const float* prims6
                cap, node < 0 ? 1 : 0, c.d_status};
   const uint32_t grid =
       (uint32_t)std::min<uint64_t>(blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)cap * 32, EMIT_THREADS)));
-  KLAUNCH("k_order_children", k_order_children<<<grid, EMIT_THREADS, 0, c.stream>>>(oa));
+  KLAUNCH("k_order_children", launch_k(k_order_children, grid, EMIT_THREADS, 0, c.stream, oa));
   CK(cudaGetLastError());
   uint32_t processed = 0;
   CK(cudaMemcpyAsync(&processed, ctr + 2, 4, cudaMemcpyDeviceToHost, c.stream));

@@ -93,6 +93,7 @@ bool on_device(const void* p) {
 // Codes in the layout obvhs_morton_sort returns: (lo, hi) u64 pairs.
 __global__ void k_codes_out(const unsigned long long* __restrict__ keys, uint32_t n, int precision,
                             unsigned long long* __restrict__ codes) {
+  grid_dep_wait();
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     codes[2 * (size_t)i] = precision ? keys[2 * (size_t)i] : keys[i];
     codes[2 * (size_t)i + 1] = precision ? keys[2 * (size_t)i + 1] : 0ull;
@@ -100,6 +101,7 @@ __global__ void k_codes_out(const unsigned long long* __restrict__ keys, uint32_
 }
 
 __global__ void k_order_out(const uint32_t* __restrict__ src, uint32_t n, uint32_t* __restrict__ order) {
+  grid_dep_wait();
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) order[i] = src[i];
 }
 
@@ -146,7 +148,7 @@ OBVHS_API int obvhs_morton_sort_noalloc(const float* aabbs, uint32_t n, uint32_t
   if (r) return r;
   const uint32_t g = div_up<uint32_t>(n, 256) < 4096 ? div_up<uint32_t>(n, 256) : 4096;
   if (codes)  // codes in input order, before the sort reorders them
-    k_codes_out<<<g, 256, 0, c.stream>>>((const unsigned long long*)keys, n, (int)sort_precision,
+    launch_k(k_codes_out, g, 256, 0, c.stream, (const unsigned long long*)keys, n, (int)sort_precision,
                                          (unsigned long long*)codes);
   bool alt = false;
   cudaError_t e;
@@ -159,7 +161,7 @@ OBVHS_API int obvhs_morton_sort_noalloc(const float* aabbs, uint32_t n, uint32_t
     cudaGetLastError();
     return OBVHS_ERR_CUDA;
   }
-  k_order_out<<<g, 256, 0, c.stream>>>(alt ? vals_alt : vals, n, order);
+  launch_k(k_order_out, g, 256, 0, c.stream, alt ? vals_alt : vals, n, order);
   if (cudaGetLastError() != cudaSuccess) return OBVHS_ERR_CUDA;
   uint32_t st = 0;
   if (cudaMemcpyAsync(&st, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream) != cudaSuccess ||

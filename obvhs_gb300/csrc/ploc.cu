@@ -80,6 +80,7 @@ __device__ __forceinline__ bool box_has_nan(const Box& b) {
 __global__ void __launch_bounds__(BLK) k_leaves_from_tris(const float* __restrict__ tris, uint32_t n,
                                                           Bvh2Node* __restrict__ leaves, int* total_keys,
                                                           uint32_t* status) {
+  grid_dep_wait();
   uint32_t i = blockIdx.x * BLK + threadIdx.x;
   bool valid = i < n;
   Box b{};
@@ -98,6 +99,7 @@ __global__ void __launch_bounds__(BLK) k_leaves_from_tris(const float* __restric
 __global__ void __launch_bounds__(BLK) k_leaves_from_aabbs(const float* __restrict__ aabbs, const uint32_t* __restrict__ idx,
                                                            uint32_t n, Bvh2Node* __restrict__ leaves, int* total_keys,
                                                            uint32_t* status) {
+  grid_dep_wait();
   uint32_t i = blockIdx.x * BLK + threadIdx.x;
   bool valid = i < n;
   Box b{};
@@ -187,6 +189,7 @@ __device__ __forceinline__ U128 morton128_of(const Bvh2Node& nd, const Scale& s)
 
 __global__ void __launch_bounds__(BLK) k_morton64(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
                                                   unsigned long long* __restrict__ codes) {
+  grid_dep_wait();
   uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i >= n) return;
   codes[i] = morton64_of(ld_node(&leaves[i]), make_scale(total_keys));
@@ -194,6 +197,7 @@ __global__ void __launch_bounds__(BLK) k_morton64(const Bvh2Node* __restrict__ l
 
 __global__ void __launch_bounds__(BLK) k_morton128(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
                                                    U128* __restrict__ codes) {
+  grid_dep_wait();
   uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i >= n) return;
   codes[i] = morton128_of(ld_node(&leaves[i]), make_scale(total_keys));
@@ -230,6 +234,7 @@ __global__ void __launch_bounds__(BLK) k_seg_leaves_tris(const float* const* __r
                                                          uint32_t n, Bvh2Node* __restrict__ leaves,
                                                          uint32_t* __restrict__ pidx, int* total_keys,
                                                          uint32_t* status) {
+  grid_dep_wait();
   const uint32_t i = blockIdx.x * BLK + threadIdx.x;
   const bool valid = i < n;
   const uint32_t s_block = seg_find(prim_start, n_seg, blockIdx.x * BLK);
@@ -256,6 +261,7 @@ __global__ void __launch_bounds__(BLK) k_seg_leaves_aabbs(const float* __restric
                                                           uint32_t n, Bvh2Node* __restrict__ leaves,
                                                           uint32_t* __restrict__ pidx, int* total_keys,
                                                           uint32_t* status) {
+  grid_dep_wait();
   const uint32_t i = blockIdx.x * BLK + threadIdx.x;
   const bool valid = i < n;
   const uint32_t s_block = seg_find(prim_start, n_seg, blockIdx.x * BLK);
@@ -277,6 +283,7 @@ template <bool WIDE>
 __global__ void __launch_bounds__(BLK) k_seg_morton(const Bvh2Node* __restrict__ leaves,
                                                     const uint32_t* __restrict__ prim_start, uint32_t n_seg, uint32_t n,
                                                     const int* total_keys, void* __restrict__ codes) {
+  grid_dep_wait();
   const uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i >= n) return;
   const uint32_t s = seg_find(prim_start, n_seg, i);
@@ -293,17 +300,20 @@ __global__ void __launch_bounds__(BLK) k_seg_morton(const Bvh2Node* __restrict__
 __global__ void __launch_bounds__(BLK) k_seg_scene_keys(const uint32_t* __restrict__ order,
                                                         const uint32_t* __restrict__ prim_start, uint32_t n_seg,
                                                         uint32_t n, uint32_t* __restrict__ keys) {
+  grid_dep_wait();
   const uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i < n) keys[i] = seg_find(prim_start, n_seg, order[i]);
 }
 
 __global__ void __launch_bounds__(BLK) k_seg_init_totals(int* total_keys, uint32_t n_seg) {
+  grid_dep_wait();
   const uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i < 8 * n_seg) total_keys[i] = (i & 7) < 3 ? 0x7fffffff : (int)0x80000000;
 }
 
 __global__ void __launch_bounds__(BLK) k_gather(const Bvh2Node* __restrict__ in, const uint32_t* __restrict__ order,
                                                 uint32_t n, Bvh2Node* __restrict__ out) {
+  grid_dep_wait();
   uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i < n) st_node(&out[i], ld_node(&in[order[i]]));
 }
@@ -554,6 +564,7 @@ __device__ __forceinline__ int tile_ipt(uint32_t live, uint32_t groups) {
 }
 
 __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs a) {
+  grid_dep_wait();
   cg::grid_group grid = cg::this_grid();
   const bool single = gridDim.x == 1;  // one block, launched normally: block barriers suffice
   extern __shared__ __align__(16) unsigned char coop_smem[];
@@ -689,6 +700,7 @@ __device__ __forceinline__ uint32_t smem_seg_find(const uint32_t* start, uint32_
 }
 
 __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_seg(PlocSegArgs a) {
+  grid_dep_wait();
   cg::grid_group grid = cg::this_grid();
   extern __shared__ __align__(16) unsigned char coop_smem[];
   __shared__ uint32_t s_warp[32];
@@ -775,6 +787,7 @@ __global__ void k_ploc_seg_init(const Bvh2Node* __restrict__ cur, const uint32_t
                                 const uint32_t* __restrict__ node_start, uint32_t n_seg, uint32_t* count,
                                 uint32_t* insert, uint32_t* passes, unsigned long long* sum_counts, uint32_t* ctl,
                                 Bvh2Node* __restrict__ out) {
+  grid_dep_wait();
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_seg) return;
   const uint32_t m = prim_start[s + 1] - prim_start[s];
@@ -804,6 +817,7 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
                                                             int radius, uint32_t depth_threshold, uint32_t max_passes,
                                                             Bvh2Node* __restrict__ out, uint32_t* status,
                                                             const uint32_t* __restrict__ remap) {
+  grid_dep_wait();
   extern __shared__ float4 smem[];
   float4* sa = smem;                      // TAIL_MAX nodes (2 float4 each)
   float4* sb = smem + 2 * TAIL_MAX;       // TAIL_MAX nodes
@@ -977,9 +991,9 @@ int ploc_leaves(BuildCtx& c, const float* tris, const float* aabbs, const uint32
   if (!n) return 0;
   uint32_t g = div_up<uint32_t>(n, BLK);
   if (tris)
-    KLAUNCH("k_leaves_from_tris", k_leaves_from_tris<<<g, BLK, 0, c.stream>>>(tris, n, leaves, total_keys, c.d_status));
+    KLAUNCH("k_leaves_from_tris", launch_k(k_leaves_from_tris, g, BLK, 0, c.stream, tris, n, leaves, total_keys, c.d_status));
   else
-    KLAUNCH("k_leaves_from_aabbs", k_leaves_from_aabbs<<<g, BLK, 0, c.stream>>>(aabbs, idx, n, leaves, total_keys, c.d_status));
+    KLAUNCH("k_leaves_from_aabbs", launch_k(k_leaves_from_aabbs, g, BLK, 0, c.stream, aabbs, idx, n, leaves, total_keys, c.d_status));
   CK(cudaGetLastError());
   return 0;
 }
@@ -989,9 +1003,9 @@ int ploc_morton_codes(BuildCtx& c, const Bvh2Node* leaves, uint32_t n, const int
   if (!n) return 0;
   uint32_t g = div_up<uint32_t>(n, BLK);
   if (precision)
-    KLAUNCH("k_morton128", k_morton128<<<g, BLK, 0, c.stream>>>(leaves, n, total_keys, (U128*)codes));
+    KLAUNCH("k_morton128", launch_k(k_morton128, g, BLK, 0, c.stream, leaves, n, total_keys, (U128*)codes));
   else
-    KLAUNCH("k_morton64", k_morton64<<<g, BLK, 0, c.stream>>>(leaves, n, total_keys, (unsigned long long*)codes));
+    KLAUNCH("k_morton64", launch_k(k_morton64, g, BLK, 0, c.stream, leaves, n, total_keys, (unsigned long long*)codes));
   CK(cudaGetLastError());
   return 0;
 }
@@ -1039,7 +1053,7 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   PlocState* st = (PlocState*)s.get(SLOT_PLOC_STATE, sizeof(PlocState));
   if (!cur || !nxt || !merge || !tile_cnt || !st) return c.fail(OBVHS_ERR_OOM, "scratch");
   uint32_t g = div_up<uint32_t>(n, BLK);
-  KLAUNCH("k_gather", k_gather<<<g, BLK, 0, c.stream>>>(leaves, order, n, cur));
+  KLAUNCH("k_gather", launch_k(k_gather, g, BLK, 0, c.stream, leaves, order, n, cur));
   PlocState* h0 = reinterpret_cast<PlocState*>(static_cast<char*>(c.h_small) + 1024);  // pinned, asynchronous copy
   *h0 = PlocState{};
   h0->count[0] = n;
@@ -1063,7 +1077,7 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
     if (gpu_shared(c) && n <= SHARED_SINGLE_BLOCK_MAX) {
       // the GPU is shared with other builds or work: one block, a normal
       // launch, runs beside them instead of waiting for a whole-GPU slot
-      KLAUNCH("k_ploc_coop", k_ploc_coop<<<1, COOP_GROUPS * PT, smem, c.stream>>>(pa));
+      KLAUNCH("k_ploc_coop", launch_k(k_ploc_coop, 1, COOP_GROUPS * PT, smem, c.stream, pa));
       CK(cudaGetLastError());
     } else {
       KLAUNCH("k_ploc_coop", CK(coop_launch(c, (const void*)k_ploc_coop, coop_blocks, COOP_GROUPS * PT, args, smem)));
@@ -1071,7 +1085,7 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   }
   {
     const size_t smem = (size_t)4 * TAIL_MAX * sizeof(float4) + TAIL_MAX + 64;
-    KLAUNCH("k_ploc_tail", k_ploc_tail<<<1, TAIL_THREADS, smem, c.stream>>>(cur, nxt, st, (int)radius, depth_threshold,
+    KLAUNCH("k_ploc_tail", launch_k(k_ploc_tail, 1, TAIL_THREADS, smem, c.stream, cur, nxt, st, (int)radius, depth_threshold,
                                                                            max_passes, out_nodes, c.d_status, remap));
     CK(cudaGetLastError());
   }
@@ -1090,14 +1104,14 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
 int seg_leaves_device(BuildCtx& c, const SegLayout& L, const float* const* d_tris, const float* aabbs,
                       const uint32_t* idx, Bvh2Node* leaves, uint32_t* pidx, int* total_keys) {
   const uint32_t S = L.n_seg, n = L.n_prims;
-  KLAUNCH("k_seg_init_totals", k_seg_init_totals<<<div_up<uint32_t>(8 * S, BLK), BLK, 0, c.stream>>>(total_keys, S));
+  KLAUNCH("k_seg_init_totals", launch_k(k_seg_init_totals, div_up<uint32_t>(8 * S, BLK), BLK, 0, c.stream, total_keys, S));
   if (!n) return 0;
   const uint32_t g = div_up<uint32_t>(n, BLK);
   if (d_tris)
-    KLAUNCH("k_seg_leaves_tris", k_seg_leaves_tris<<<g, BLK, 0, c.stream>>>(d_tris, L.d_prim_start, S, n, leaves, pidx,
+    KLAUNCH("k_seg_leaves_tris", launch_k(k_seg_leaves_tris, g, BLK, 0, c.stream, d_tris, L.d_prim_start, S, n, leaves, pidx,
                                                                            total_keys, c.d_status));
   else
-    KLAUNCH("k_seg_leaves_aabbs", k_seg_leaves_aabbs<<<g, BLK, 0, c.stream>>>(aabbs, idx, L.d_prim_start, S, n, leaves,
+    KLAUNCH("k_seg_leaves_aabbs", launch_k(k_seg_leaves_aabbs, g, BLK, 0, c.stream, aabbs, idx, L.d_prim_start, S, n, leaves,
                                                                              pidx, total_keys, c.d_status));
   CK(cudaGetLastError());
   return 0;
@@ -1115,9 +1129,9 @@ int ploc_seg_device(BuildCtx& c, const SegLayout& L, const Bvh2Node* leaves, con
   if (!codes) return c.fail(OBVHS_ERR_OOM, "scratch");
   const uint32_t g = div_up<uint32_t>(n, BLK);
   if (precision)
-    KLAUNCH("k_seg_morton", k_seg_morton<true><<<g, BLK, 0, c.stream>>>(leaves, L.d_prim_start, S, n, total_keys, codes));
+    KLAUNCH("k_seg_morton", launch_k(k_seg_morton<true>, g, BLK, 0, c.stream, leaves, L.d_prim_start, S, n, total_keys, codes));
   else
-    KLAUNCH("k_seg_morton", k_seg_morton<false><<<g, BLK, 0, c.stream>>>(leaves, L.d_prim_start, S, n, total_keys, codes));
+    KLAUNCH("k_seg_morton", launch_k(k_seg_morton<false>, g, BLK, 0, c.stream, leaves, L.d_prim_start, S, n, total_keys, codes));
   CK(cudaGetLastError());
   // Morton order over all leaves, then a stable pass on the scene index: each
   // scene's leaves in its own Morton order (ties by position), scenes in turn
@@ -1130,7 +1144,7 @@ int ploc_seg_device(BuildCtx& c, const SegLayout& L, const Bvh2Node* leaves, con
     uint32_t* rs = (uint32_t*)s.get(SLOT_ALL_HIST, radix_scratch_words(n) * 4);
     if (!skeys || !skeys_alt || !rs) return c.fail(OBVHS_ERR_OOM, "scratch");
     uint32_t* other = order == (uint32_t*)s.ptr[SLOT_VALS] ? (uint32_t*)s.ptr[SLOT_VALS_ALT] : (uint32_t*)s.ptr[SLOT_VALS];
-    KLAUNCH("k_seg_scene_keys", k_seg_scene_keys<<<g, BLK, 0, c.stream>>>(order, L.d_prim_start, S, n, skeys));
+    KLAUNCH("k_seg_scene_keys", launch_k(k_seg_scene_keys, g, BLK, 0, c.stream, order, L.d_prim_start, S, n, skeys));
     bool alt = false;
     cudaError_t e = radix_sort_pairs<uint32_t>(c, skeys, order, n, false, skeys_alt, other, rs, &alt, S <= 256 ? 1 : 2);
     if (e) return c.cuda_fail(e, "scene sort");
@@ -1145,9 +1159,9 @@ int ploc_seg_device(BuildCtx& c, const SegLayout& L, const Bvh2Node* leaves, con
   uint32_t* ctl = st;
   uint32_t* count = st + 8;
   uint32_t* insert = count + 2 * (size_t)S;
-  KLAUNCH("k_gather", k_gather<<<g, BLK, 0, c.stream>>>(leaves, order, n, cur));
+  KLAUNCH("k_gather", launch_k(k_gather, g, BLK, 0, c.stream, leaves, order, n, cur));
   CK(cudaMemsetAsync(ctl, 0, 32, c.stream));
-  KLAUNCH("k_ploc_seg_init", k_ploc_seg_init<<<div_up<uint32_t>(S, BLK), BLK, 0, c.stream>>>(
+  KLAUNCH("k_ploc_seg_init", launch_k(k_ploc_seg_init, div_up<uint32_t>(S, BLK), BLK, 0, c.stream,
                                  cur, L.d_prim_start, L.d_node_start, S, count, insert, d_passes, d_sum_counts, ctl, out));
   CK(cudaGetLastError());
   const size_t smem = COOP_GROUPS * sizeof(CoopGroupSmem) + ((size_t)S + 1) * 4;

@@ -30,6 +30,7 @@ __device__ __forceinline__ Box tri_box(const float* t) {
 __global__ void __launch_bounds__(BLK) k_tri_boxes(const float* __restrict__ tris, uint32_t n, float* __restrict__ aabbs,
                                                    uint32_t* __restrict__ idx, float* __restrict__ ha,
                                                    int* largest_key, uint32_t* status) {
+  grid_dep_wait();
   uint32_t i = blockIdx.x * BLK + threadIdx.x;
   float a = 0.0f;
   if (i < n) {
@@ -77,6 +78,7 @@ struct BlockT {
 };
 
 __global__ void __launch_bounds__(BLK) k_block_dsum(const float* __restrict__ ha, uint32_t n, double* __restrict__ bsum) {
+  grid_dep_wait();
   __shared__ double sw[BLK / 32];
   const uint32_t base = blockIdx.x * SUM_BLOCK;
   double acc = 0.0;
@@ -96,6 +98,7 @@ __global__ void __launch_bounds__(BLK) k_block_dsum(const float* __restrict__ ha
 // Exclusive prefix of the block sums in place (one block, chunks of 1024
 // with a carry): each block's approximate running sum at its start.
 __global__ void __launch_bounds__(1024) k_scan_dsum(double* bsum, uint32_t nb) {
+  grid_dep_wait();
   __shared__ double sw[32];
   __shared__ double carry;
   if (threadIdx.x == 0) carry = 0.0;
@@ -156,6 +159,7 @@ __device__ __forceinline__ Mono shfl_down_mono(const Mono& v, int o) {
 
 __global__ void __launch_bounds__(BLK) k_block_transform(const float* __restrict__ ha, uint32_t n,
                                                          const double* __restrict__ bstart, BlockT* __restrict__ out) {
+  grid_dep_wait();
   constexpr int PER = SUM_BLOCK / BLK;  // consecutive elements per thread
   __shared__ Mono sm[BLK / 32];
   const uint32_t b = blockIdx.x;
@@ -259,6 +263,7 @@ __device__ void warp_sum_range(float& s, const float* __restrict__ ha, uint32_t 
 // the preset thresholds (src/splits.rs:23-33).
 __global__ void __launch_bounds__(32) k_sum_chain(const float* __restrict__ ha, uint32_t n, const BlockT* __restrict__ tr,
                                                   const int* largest_key, float* thr) {
+  grid_dep_wait();
   const int lane = threadIdx.x;
   const uint32_t nb = (n + SUM_BLOCK - 1) / SUM_BLOCK;
   float s = 0.0f;
@@ -349,6 +354,7 @@ __global__ void __launch_bounds__(BLK) k_split(const uint32_t* __restrict__ cand
                                                const uint32_t* __restrict__ idx, const float* __restrict__ tris,
                                                const float* __restrict__ thr, float* __restrict__ right_out,
                                                uint32_t* __restrict__ flag) {
+  grid_dep_wait();
   uint32_t k = blockIdx.x * BLK + threadIdx.x;
   if (k >= ncand) return;
   const uint32_t ai = cand[k];
@@ -412,6 +418,7 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp
 }
 
 __global__ void __launch_bounds__(BLK) k_count_flags(const uint32_t* __restrict__ flag, uint32_t n, uint32_t* partial) {
+  grid_dep_wait();
   __shared__ uint32_t s_warp[BLK / 32];
   uint32_t base = blockIdx.x * CHUNK, c = 0;
   for (int k = 0; k < ITEMS; k++) {
@@ -424,6 +431,7 @@ __global__ void __launch_bounds__(BLK) k_count_flags(const uint32_t* __restrict_
 }
 
 __global__ void __launch_bounds__(1024) k_scan_partials(uint32_t* partial, uint32_t nb, uint32_t* total) {
+  grid_dep_wait();
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t carry;
   if (threadIdx.x == 0) carry = 0;
@@ -458,6 +466,7 @@ __global__ void __launch_bounds__(BLK) k_append(const uint32_t* __restrict__ fla
                                                 uint32_t ncand, const uint32_t* __restrict__ cand,
                                                 const float* __restrict__ right, uint32_t len, float* __restrict__ aabbs,
                                                 uint32_t* __restrict__ idx, uint32_t* __restrict__ new_cand) {
+  grid_dep_wait();
   __shared__ uint32_t s_warp[BLK / 32];
   uint32_t base = blockIdx.x * CHUNK, c = 0;
   uint32_t f[ITEMS];
@@ -484,6 +493,7 @@ __global__ void __launch_bounds__(BLK) k_append(const uint32_t* __restrict__ fla
 __global__ void __launch_bounds__(BLK) k_keep_flags(const uint32_t* __restrict__ cand, uint32_t n,
                                                     const float* __restrict__ aabbs, const float* __restrict__ thr,
                                                     uint32_t* __restrict__ flag) {
+  grid_dep_wait();
   uint32_t k = blockIdx.x * BLK + threadIdx.x;
   if (k >= n) return;
   flag[k] = half_area(ld_box6(aabbs + (size_t)cand[k] * 6)) > thr[0] ? 1u : 0u;
@@ -492,6 +502,7 @@ __global__ void __launch_bounds__(BLK) k_keep_flags(const uint32_t* __restrict__
 __global__ void __launch_bounds__(BLK) k_initial_flags(const float* __restrict__ ha, uint32_t n,
                                                        const float* __restrict__ thr, uint32_t* __restrict__ flag,
                                                        uint32_t* __restrict__ ids) {
+  grid_dep_wait();
   uint32_t k = blockIdx.x * BLK + threadIdx.x;
   if (k >= n) return;
   flag[k] = ha[k] > thr[0] ? 1u : 0u;
@@ -500,6 +511,7 @@ __global__ void __launch_bounds__(BLK) k_initial_flags(const float* __restrict__
 
 __global__ void __launch_bounds__(BLK) k_compact(const uint32_t* __restrict__ flag, const uint32_t* __restrict__ partial,
                                                  uint32_t n, const uint32_t* __restrict__ in, uint32_t* __restrict__ out) {
+  grid_dep_wait();
   __shared__ uint32_t s_warp[BLK / 32];
   uint32_t base = blockIdx.x * CHUNK, c = 0;
   uint32_t f[ITEMS];
@@ -523,9 +535,9 @@ static int compact(BuildCtx& c, const uint32_t* flag, uint32_t n, const uint32_t
   *kept = 0;
   if (!n) return 0;
   uint32_t nb = div_up<uint32_t>(n, CHUNK);
-  KLAUNCH("k_count_flags", k_count_flags<<<nb, BLK, 0, c.stream>>>(flag, n, partial));
-  KLAUNCH("k_scan_partials", k_scan_partials<<<1, 1024, 0, c.stream>>>(partial, nb, d_total));
-  KLAUNCH("k_compact", k_compact<<<nb, BLK, 0, c.stream>>>(flag, partial, n, in, out));
+  KLAUNCH("k_count_flags", launch_k(k_count_flags, nb, BLK, 0, c.stream, flag, n, partial));
+  KLAUNCH("k_scan_partials", launch_k(k_scan_partials, 1, 1024, 0, c.stream, partial, nb, d_total));
+  KLAUNCH("k_compact", launch_k(k_compact, nb, BLK, 0, c.stream, flag, partial, n, in, out));
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(c.h_small, d_total, 4, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
@@ -586,19 +598,19 @@ int presplit_device(BuildCtx& c, const float* tris, uint32_t n, float** aabbs_ou
   int zero_key = 0;
   CK(cudaMemcpyAsync(largest_key, &zero_key, 4, cudaMemcpyHostToDevice, c.stream));
   uint32_t g = div_up<uint32_t>(n, BLK);
-  KLAUNCH("k_tri_boxes", k_tri_boxes<<<g, BLK, 0, c.stream>>>(tris, n, (float*)s.ptr[SLOT_SPLIT_AABBS], (uint32_t*)s.ptr[SLOT_SPLIT_IDX], ha,
+  KLAUNCH("k_tri_boxes", launch_k(k_tri_boxes, g, BLK, 0, c.stream, tris, n, (float*)s.ptr[SLOT_SPLIT_AABBS], (uint32_t*)s.ptr[SLOT_SPLIT_IDX], ha,
                                         largest_key, c.d_status));
   {
     const uint32_t nb = div_up<uint32_t>(n, SUM_BLOCK);
     double* bsum = (double*)s.get(SLOT_OUTPUT, (size_t)nb * 8 + 16);
     BlockT* tr = (BlockT*)s.get(SLOT_TILE_HIST, (size_t)nb * sizeof(BlockT) + 16);
     if (!bsum || !tr) return c.fail(OBVHS_ERR_OOM, "scratch");
-    KLAUNCH("k_block_dsum", k_block_dsum<<<nb, BLK, 0, c.stream>>>(ha, n, bsum));
-    KLAUNCH("k_scan_dsum", k_scan_dsum<<<1, 1024, 0, c.stream>>>(bsum, nb));
-    KLAUNCH("k_block_transform", k_block_transform<<<nb, BLK, 0, c.stream>>>(ha, n, bsum, tr));
-    KLAUNCH("k_sum_chain", k_sum_chain<<<1, 32, 0, c.stream>>>(ha, n, tr, largest_key, thr));
+    KLAUNCH("k_block_dsum", launch_k(k_block_dsum, nb, BLK, 0, c.stream, ha, n, bsum));
+    KLAUNCH("k_scan_dsum", launch_k(k_scan_dsum, 1, 1024, 0, c.stream, bsum, nb));
+    KLAUNCH("k_block_transform", launch_k(k_block_transform, nb, BLK, 0, c.stream, ha, n, bsum, tr));
+    KLAUNCH("k_sum_chain", launch_k(k_sum_chain, 1, 32, 0, c.stream, ha, n, tr, largest_key, thr));
   }
-  KLAUNCH("k_initial_flags", k_initial_flags<<<g, BLK, 0, c.stream>>>(ha, n, thr, (uint32_t*)s.ptr[SLOT_FLAGS], (uint32_t*)s.ptr[SLOT_SPLIT_CAND2]));
+  KLAUNCH("k_initial_flags", launch_k(k_initial_flags, g, BLK, 0, c.stream, ha, n, thr, (uint32_t*)s.ptr[SLOT_FLAGS], (uint32_t*)s.ptr[SLOT_SPLIT_CAND2]));
   CK(cudaGetLastError());
   if (thresholds_only) return 0;
   uint32_t ncand = 0;
@@ -622,12 +634,12 @@ int presplit_device(BuildCtx& c, const float* tris, uint32_t n, float** aabbs_ou
     uint32_t* flag = (uint32_t*)s.ptr[SLOT_FLAGS];
     float* right = (float*)s.ptr[SLOT_REINS];
     uint32_t* partial = (uint32_t*)s.ptr[SLOT_PARTIAL];
-    KLAUNCH("k_split", k_split<<<div_up<uint32_t>(ncand, BLK), BLK, 0, c.stream>>>(cand, ncand, aabbs, idx, tris, thr, right, flag));
+    KLAUNCH("k_split", launch_k(k_split, div_up<uint32_t>(ncand, BLK), BLK, 0, c.stream, cand, ncand, aabbs, idx, tris, thr, right, flag));
     uint32_t nb = div_up<uint32_t>(ncand, CHUNK);
-    KLAUNCH("k_count_flags", k_count_flags<<<nb, BLK, 0, c.stream>>>(flag, ncand, partial));
-    KLAUNCH("k_scan_partials", k_scan_partials<<<1, 1024, 0, c.stream>>>(partial, nb, d_total));
+    KLAUNCH("k_count_flags", launch_k(k_count_flags, nb, BLK, 0, c.stream, flag, ncand, partial));
+    KLAUNCH("k_scan_partials", launch_k(k_scan_partials, 1, 1024, 0, c.stream, partial, nb, d_total));
     // the appended entries become candidates after the current ones
-    KLAUNCH("k_append", k_append<<<nb, BLK, 0, c.stream>>>(flag, partial, ncand, cand, right, len, aabbs, idx, cand + ncand));
+    KLAUNCH("k_append", launch_k(k_append, nb, BLK, 0, c.stream, flag, partial, ncand, cand, right, len, aabbs, idx, cand + ncand));
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(c.h_small, d_total, 4, cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
@@ -635,7 +647,7 @@ int presplit_device(BuildCtx& c, const float* tris, uint32_t n, float** aabbs_ou
     if (added == 0) break;
     len += added;
     uint32_t total = ncand + added;
-    KLAUNCH("k_keep_flags", k_keep_flags<<<div_up<uint32_t>(total, BLK), BLK, 0, c.stream>>>(cand, total, aabbs, thr, flag));
+    KLAUNCH("k_keep_flags", launch_k(k_keep_flags, div_up<uint32_t>(total, BLK), BLK, 0, c.stream, cand, total, aabbs, thr, flag));
     CK(cudaGetLastError());
     r = compact(c, flag, total, cand, cand2, partial, d_total, &ncand);
     if (r) return r;

@@ -40,6 +40,7 @@ struct Tile {
 // shared-memory counting.
 template <class K>
 __global__ void __launch_bounds__(THREADS) k_rs_hist(const K* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist) {
+  grid_dep_wait();
   constexpr int NB = KeyTraits<K>::BYTES;
   __shared__ uint32_t h[NB * 256];
   for (int i = threadIdx.x; i < NB * 256; i += THREADS) h[i] = 0;
@@ -62,6 +63,7 @@ __global__ void __launch_bounds__(THREADS) k_rs_hist(const K* __restrict__ keys,
 
 // block b scans histogram b in place (exclusive)
 __global__ void __launch_bounds__(THREADS) k_rs_scan(uint32_t* hist) {
+  grid_dep_wait();
   __shared__ uint32_t sw[WARPS];
   uint32_t* h = hist + blockIdx.x * 256;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -89,6 +91,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_rs_pass(const K* __restrict__ ke
                                                      uint32_t n, int byte, bool iota,
                                                      const uint32_t* __restrict__ digit_base,
                                                      uint32_t* tile_status, uint32_t* tile_counter, uint32_t* status) {
+  grid_dep_wait();
   constexpr int ITEMS = Tile<K, SMALL>::ITEMS;
   constexpr int TS = Tile<K, SMALL>::SIZE;
   __shared__ uint32_t s_tile;
@@ -229,6 +232,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_rs_pass(const K* __restrict__ ke
 }
 
 __global__ void k_iota(uint32_t* v, uint32_t n) {
+  grid_dep_wait();
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = i;
 }
 
@@ -257,8 +261,8 @@ cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, 
   cudaError_t e = cudaMemsetAsync(scratch, 0, (16 * 256 + nd * pass_words) * sizeof(uint32_t), c.stream);
   if (e) return e;
   const uint32_t hb = (n + THREADS * HIST_ITEMS - 1) / (THREADS * HIST_ITEMS);
-  KLAUNCH("k_rs_hist", k_rs_hist<K><<<hb, THREADS, 0, c.stream>>>(keys, n, hist));
-  KLAUNCH("k_rs_scan", k_rs_scan<<<nd, THREADS, 0, c.stream>>>(hist));
+  KLAUNCH("k_rs_hist", launch_k(k_rs_hist<K>, hb, THREADS, 0, c.stream, keys, n, hist));
+  KLAUNCH("k_rs_scan", launch_k(k_rs_scan, nd, THREADS, 0, c.stream, hist));
   K* kin = keys;
   uint32_t* vin = vals;
   K* kout = keys_alt;
@@ -267,10 +271,10 @@ cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, 
   for (int b = 0; b < nd; b++) {
     uint32_t* ts = pass_area + (size_t)b * pass_words;
     if (small)
-      KLAUNCH("k_rs_pass", k_rs_pass<K, true><<<ntiles, THREADS, 0, c.stream>>>(kin, vin, kout, vout, n, b, iota,
+      KLAUNCH("k_rs_pass", launch_k(k_rs_pass<K, true>, ntiles, THREADS, 0, c.stream, kin, vin, kout, vout, n, b, iota,
                                                                                hist + b * 256, ts + 32, ts, c.d_status));
     else
-      KLAUNCH("k_rs_pass", k_rs_pass<K, false><<<ntiles, THREADS, 0, c.stream>>>(kin, vin, kout, vout, n, b, iota,
+      KLAUNCH("k_rs_pass", launch_k(k_rs_pass<K, false>, ntiles, THREADS, 0, c.stream, kin, vin, kout, vout, n, b, iota,
                                                                                 hist + b * 256, ts + 32, ts, c.d_status));
     iota = false;
     std::swap(kin, kout);
@@ -284,7 +288,7 @@ cudaError_t fill_iota(uint32_t* v, uint32_t n, cudaStream_t s) {
   if (!n) return cudaSuccess;
   uint32_t blocks = (n + 255) / 256;
   if (blocks > 4096) blocks = 4096;
-  k_iota<<<blocks, 256, 0, s>>>(v, n);
+  launch_k(k_iota, blocks, 256, 0, s, v, n);
   return cudaGetLastError();
 }
 

@@ -47,6 +47,7 @@ struct Reins {
 };
 
 __global__ void k_parents(const Bvh2Node* __restrict__ nodes, uint32_t n, uint32_t* __restrict__ parents) {
+  grid_dep_wait();
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   if (i == 0) parents[0] = 0;
@@ -68,6 +69,7 @@ __device__ __forceinline__ uint32_t f32_radix_key(float f) {
 
 __global__ void k_cand_keys(const Bvh2Node* __restrict__ nodes, uint32_t take, uint32_t* __restrict__ keys,
                             uint32_t* __restrict__ vals) {
+  grid_dep_wait();
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   if (i >= take) return;
   Box b = node_box(ld_node(&nodes[i]));
@@ -202,6 +204,7 @@ __global__ void __launch_bounds__(FIND_THREADS) k_find(const Bvh2Node* __restric
                                                        const uint32_t* __restrict__ cand, uint32_t count,
                                                        uint32_t cap_rt, Reins* __restrict__ out, uint32_t* status,
                                                        StackModes modes) {
+  grid_dep_wait();
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
   uint2 stack[CAP];
@@ -224,6 +227,7 @@ __global__ void __launch_bounds__(FIND_THREADS) k_find_persistent(const Bvh2Node
                                                                   const uint32_t* __restrict__ cand, uint32_t count,
                                                                   uint32_t cap_rt, Reins* __restrict__ out,
                                                                   uint32_t* next, uint32_t* status, StackModes modes) {
+  grid_dep_wait();
   const int lane = threadIdx.x & 31;
   uint2 stack[CAP];
   FindSearch<CAP, CLAMP> f;
@@ -576,6 +580,7 @@ __device__ __forceinline__ void list_proposals(const ResolveArgs& a, uint32_t wa
 // block 0 alone (block barriers instead of grid barriers); the other blocks
 // return and take no further part in any barrier.
 __global__ void __launch_bounds__(RESOLVE_THREADS) k_resolve(ResolveArgs a) {
+  grid_dep_wait();
   cg::grid_group grid = cg::this_grid();
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -600,6 +605,7 @@ __global__ void __launch_bounds__(RESOLVE_THREADS) k_resolve(ResolveArgs a) {
 // Every scene's root is its own parent (k_parents covers node 0 only).
 __global__ void k_seg_root_parents(const uint32_t* __restrict__ prim_start, const uint32_t* __restrict__ node_start,
                                    uint32_t n_seg, uint32_t* __restrict__ parents) {
+  grid_dep_wait();
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s < n_seg && prim_start[s + 1] > prim_start[s]) parents[node_start[s]] = node_start[s];
 }
@@ -610,6 +616,7 @@ __global__ void k_seg_root_parents(const uint32_t* __restrict__ prim_start, cons
 __global__ void k_seg_cand_keys(const Bvh2Node* __restrict__ nodes, const uint32_t* __restrict__ cand_start,
                                 const uint32_t* __restrict__ node_start, uint32_t n_seg, uint32_t total,
                                 unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals) {
+  grid_dep_wait();
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= total) return;
   const uint32_t s = seg_find(cand_start, n_seg, j);
@@ -623,6 +630,7 @@ __global__ void k_seg_cand_keys(const Bvh2Node* __restrict__ nodes, const uint32
 __global__ void k_seg_cand_gather(const uint32_t* __restrict__ sorted, const uint32_t* __restrict__ find_start,
                                   const uint32_t* __restrict__ cand_start, uint32_t n_seg, uint32_t total,
                                   uint32_t* __restrict__ out) {
+  grid_dep_wait();
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= total) return;
   const uint32_t s = seg_find(find_start, n_seg, k);
@@ -691,16 +699,16 @@ int reins_pass(BuildCtx& c, Bvh2Node* nodes, uint32_t len, const uint32_t* cand,
   const uint32_t fblocks = div_up<uint32_t>(count, FIND_THREADS);
   if (fblocks > (uint32_t)find_blocks) {
     if (clamp)
-      KLAUNCH("k_find", k_find_persistent<192, true><<<find_blocks, FIND_THREADS, 0, c.stream>>>(
+      KLAUNCH("k_find", launch_k(k_find_persistent<192, true>, find_blocks, FIND_THREADS, 0, c.stream,
                             nodes, B.parents, cand, count, cap_rt, B.reins, pass_ctr + 5, c.d_status, modes));
     else
-      KLAUNCH("k_find", k_find_persistent<1024, false><<<find_blocks, FIND_THREADS, 0, c.stream>>>(
+      KLAUNCH("k_find", launch_k(k_find_persistent<1024, false>, find_blocks, FIND_THREADS, 0, c.stream,
                             nodes, B.parents, cand, count, cap_rt, B.reins, pass_ctr + 5, c.d_status, modes));
   } else if (clamp) {
-    KLAUNCH("k_find", k_find<192, true><<<fblocks, FIND_THREADS, 0, c.stream>>>(nodes, B.parents, cand, count, cap_rt,
+    KLAUNCH("k_find", launch_k(k_find<192, true>, fblocks, FIND_THREADS, 0, c.stream, nodes, B.parents, cand, count, cap_rt,
                                                                            B.reins, c.d_status, modes));
   } else {
-    KLAUNCH("k_find", k_find<1024, false><<<fblocks, FIND_THREADS, 0, c.stream>>>(nodes, B.parents, cand, count, cap_rt,
+    KLAUNCH("k_find", launch_k(k_find<1024, false>, fblocks, FIND_THREADS, 0, c.stream, nodes, B.parents, cand, count, cap_rt,
                                                                              B.reins, c.d_status, modes));
   }
   CK(cudaGetLastError());
@@ -712,7 +720,7 @@ int reins_pass(BuildCtx& c, Bvh2Node* nodes, uint32_t len, const uint32_t* cand,
                                                std::max<uint64_t>(1, div_up<uint32_t>(count, RESOLVE_THREADS)));
   if (grid == 1 || count <= RESOLVE_SINGLE_MAX || gpu_shared(c)) {
     // one block, a normal launch (block barriers only)
-    KLAUNCH("k_resolve", k_resolve<<<1, RESOLVE_THREADS, 0, c.stream>>>(ra));
+    KLAUNCH("k_resolve", launch_k(k_resolve, 1, RESOLVE_THREADS, 0, c.stream, ra));
   } else {
     KLAUNCH("k_resolve", CK(coop_launch(c, (const void*)k_resolve, grid, RESOLVE_THREADS, args, 0)));
   }
@@ -724,7 +732,7 @@ int reins_pass(BuildCtx& c, Bvh2Node* nodes, uint32_t len, const uint32_t* cand,
 
 int compute_parents_device(BuildCtx& c, const Bvh2Node* nodes, uint32_t n_nodes, uint32_t* parents) {
   if (!n_nodes) return 0;
-  KLAUNCH("k_parents", k_parents<<<div_up<uint32_t>(n_nodes, BLK), BLK, 0, c.stream>>>(nodes, n_nodes, parents));
+  KLAUNCH("k_parents", launch_k(k_parents, div_up<uint32_t>(n_nodes, BLK), BLK, 0, c.stream, nodes, n_nodes, parents));
   CK(cudaGetLastError());
   return 0;
 }
@@ -773,7 +781,7 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
     uint32_t count = node_count - 1;
     if (count == 0) continue;
     // find_candidates
-    KLAUNCH("k_cand_keys", k_cand_keys<<<div_up<uint32_t>(ncand, BLK), BLK, 0, c.stream>>>(b->nodes, take, keys, vals));
+    KLAUNCH("k_cand_keys", launch_k(k_cand_keys, div_up<uint32_t>(ncand, BLK), BLK, 0, c.stream, b->nodes, take, keys, vals));
     bool alt = false;
     cudaError_t e = radix_sort_pairs<uint32_t>(c, keys, vals, ncand, false, keys_alt, vals_alt, rs, &alt);
     if (e) return c.cuda_fail(e, "candidate sort");
@@ -794,7 +802,7 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
 }
 
 int seg_root_parents_device(BuildCtx& c, const SegLayout& L, uint32_t* parents) {
-  KLAUNCH("k_seg_root_parents", k_seg_root_parents<<<div_up<uint32_t>(L.n_seg, BLK), BLK, 0, c.stream>>>(
+  KLAUNCH("k_seg_root_parents", launch_k(k_seg_root_parents, div_up<uint32_t>(L.n_seg, BLK), BLK, 0, c.stream,
                                     L.d_prim_start, L.d_node_start, L.n_seg, parents));
   CK(cudaGetLastError());
   return 0;
@@ -871,13 +879,13 @@ int reinsertion_seg_device(BuildCtx& c, Bvh2Node* nodes, const SegLayout& L, con
     if (tot_count[ri] == 0) continue;
     const uint32_t* cs = d_tab + ri * stride;
     const uint32_t* fs = cs + S + 1;
-    KLAUNCH("k_seg_cand_keys", k_seg_cand_keys<<<div_up<uint32_t>(tot_cand[ri], BLK), BLK, 0, c.stream>>>(
+    KLAUNCH("k_seg_cand_keys", launch_k(k_seg_cand_keys, div_up<uint32_t>(tot_cand[ri], BLK), BLK, 0, c.stream,
                                    nodes, cs, L.d_node_start, S, tot_cand[ri], keys, vals));
     bool alt = false;
     cudaError_t e = radix_sort_pairs<unsigned long long>(c, keys, vals, tot_cand[ri], false, keys_alt, vals_alt, rs,
                                                          &alt, digits);
     if (e) return c.cuda_fail(e, "candidate sort");
-    KLAUNCH("k_seg_cand_gather", k_seg_cand_gather<<<div_up<uint32_t>(tot_count[ri], BLK), BLK, 0, c.stream>>>(
+    KLAUNCH("k_seg_cand_gather", launch_k(k_seg_cand_gather, div_up<uint32_t>(tot_count[ri], BLK), BLK, 0, c.stream,
                                      alt ? vals_alt : vals, fs, cs, S, tot_count[ri], cand));
     r = reins_pass(c, nodes, len, cand, tot_count[ri], ri, all_clamp, 192, modes, B);
     if (r) return r;

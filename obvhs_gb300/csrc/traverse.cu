@@ -170,6 +170,7 @@ __global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ no
                                                    const uint32_t* __restrict__ pidx = nullptr,
                                                    const BlasDesc* __restrict__ multi = nullptr,
                                                    const uint32_t* __restrict__ ray_bvh = nullptr, uint32_t n_multi = 0) {
+  grid_dep_wait();
   const int lane = threadIdx.x & 31;
   for (;;) {
     uint32_t base = 0;
@@ -315,6 +316,7 @@ __global__ void __launch_bounds__(TBLK) k_traverse_bvh2(const Bvh2Node* __restri
                                                         const float4* __restrict__ rays, uint32_t nrays,
                                                         uint2* __restrict__ hits, uint8_t* __restrict__ miss,
                                                         uint32_t* __restrict__ next_ray, uint32_t* status) {
+  grid_dep_wait();
   const int lane = threadIdx.x & 31;
   for (;;) {
     uint32_t base = 0;
@@ -443,6 +445,7 @@ __global__ void __launch_bounds__(TBLK) k_query_bvh2(const Bvh2Node* __restrict_
                                                      const float* __restrict__ queries, uint32_t nq,
                                                      const float* __restrict__ prims, uint32_t n_prims,
                                                      uint32_t* out, uint32_t* __restrict__ ids, uint32_t* status) {
+  grid_dep_wait();
   for (uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x; qi < nq; qi += gridDim.x * blockDim.x) {
     float q[6];
 #pragma unroll
@@ -546,6 +549,7 @@ __global__ void __launch_bounds__(TBLK) k_query_cwbvh(const CwNode* __restrict__
                                                       const float* __restrict__ queries, uint32_t nq,
                                                       const float* __restrict__ prims, uint32_t n_prims, uint32_t oct,
                                                       uint32_t* out, uint32_t* __restrict__ ids, uint32_t* status) {
+  grid_dep_wait();
   for (uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x; qi < nq; qi += gridDim.x * blockDim.x) {
     float q[6];
 #pragma unroll
@@ -616,6 +620,7 @@ __global__ void __launch_bounds__(TBLK) k_query_cwbvh(const CwNode* __restrict__
 // primitive_indices order; halves by round-to-nearest-even (f16::from_f32).
 __global__ void k_compress_tris(const float* __restrict__ tris, uint32_t n_tris, const uint32_t* __restrict__ pidx,
                                 uint32_t n_prims, uint2* __restrict__ out, uint32_t* status) {
+  grid_dep_wait();
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n_prims) return;
   uint32_t id = pidx[k];
@@ -645,6 +650,7 @@ __global__ void __launch_bounds__(TBLK) k_traverse_tlas(const CwNode* __restrict
                                                         const float4* __restrict__ rays, uint32_t nrays,
                                                         uint4* __restrict__ hits, uint32_t* __restrict__ next_ray,
                                                         uint32_t* status) {
+  grid_dep_wait();
   const int lane = threadIdx.x & 31;
   for (;;) {
     uint32_t base = 0;
@@ -787,6 +793,7 @@ __device__ __forceinline__ void write_bvh_tri(const float* tris, uint32_t n_tris
 
 __global__ void k_reorder_tris(const float* __restrict__ tris, uint32_t n_tris, const uint32_t* __restrict__ pidx,
                                uint32_t n_prims, float4* __restrict__ out, uint32_t* status) {
+  grid_dep_wait();
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n_prims) write_bvh_tri(tris, n_tris, pidx, k, out, status);
 }
@@ -794,6 +801,7 @@ __global__ void k_reorder_tris(const float* __restrict__ tris, uint32_t n_tris, 
 // Triangles of every scene of a segmented build, in BVH order.
 __global__ void k_seg_reorder_tris(const SegTriJob* __restrict__ jobs, const uint32_t* __restrict__ prim_start,
                                    uint32_t n_seg, uint32_t total, uint32_t* status) {
+  grid_dep_wait();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= total) return;
   const uint32_t s = seg_find(prim_start, n_seg, i);
@@ -805,6 +813,7 @@ __global__ void k_seg_reorder_tris(const SegTriJob* __restrict__ jobs, const uin
 // Ray i of concatenated batches: the BVH of its batch.
 __global__ void k_batch_owner(const uint32_t* __restrict__ offsets, const uint32_t* __restrict__ batch_bvh,
                               uint32_t n_batches, uint32_t total, uint32_t* __restrict__ owner) {
+  grid_dep_wait();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < total) owner[i] = __ldg(&batch_bvh[seg_find(offsets, n_batches, i)]);
 }
@@ -814,7 +823,7 @@ __global__ void k_batch_owner(const uint32_t* __restrict__ offsets, const uint32
 int batch_owner_device(BuildCtx& c, const uint32_t* d_offsets, const uint32_t* d_batch_bvh, uint32_t n_batches,
                        uint32_t total, uint32_t* owner) {
   if (!total) return 0;
-  KLAUNCH("k_batch_owner", k_batch_owner<<<div_up<uint32_t>(total, 256), 256, 0, c.stream>>>(d_offsets, d_batch_bvh,
+  KLAUNCH("k_batch_owner", launch_k(k_batch_owner, div_up<uint32_t>(total, 256), 256, 0, c.stream, d_offsets, d_batch_bvh,
                                                                                              n_batches, total, owner));
   CK(cudaGetLastError());
   return 0;
@@ -823,7 +832,7 @@ int batch_owner_device(BuildCtx& c, const uint32_t* d_offsets, const uint32_t* d
 int reorder_tris_seg_device(BuildCtx& c, const SegTriJob* d_jobs, const uint32_t* d_prim_start, uint32_t n_seg,
                             uint32_t total) {
   if (!total) return 0;
-  KLAUNCH("k_seg_reorder_tris", k_seg_reorder_tris<<<div_up<uint32_t>(total, 256), 256, 0, c.stream>>>(
+  KLAUNCH("k_seg_reorder_tris", launch_k(k_seg_reorder_tris, div_up<uint32_t>(total, 256), 256, 0, c.stream,
                                     d_jobs, d_prim_start, n_seg, total, c.d_status));
   CK(cudaGetLastError());
   return 0;
@@ -841,7 +850,7 @@ int bvh2_reorder_tris_device(BuildCtx& c, obvhs_bvh2* b, const float* tris, uint
     cudaGetLastError();
     return c.fail(OBVHS_ERR_OOM, "triangle buffer");
   }
-  KLAUNCH("k_reorder_tris", k_reorder_tris<<<div_up<uint32_t>(b->n_prims, 256), 256, 0, c.stream>>>(
+  KLAUNCH("k_reorder_tris", launch_k(k_reorder_tris, div_up<uint32_t>(b->n_prims, 256), 256, 0, c.stream,
                                 tris, n_tris, b->prim_indices, b->n_prims, out, c.d_status));
   CK(cudaGetLastError());
   b->tris = out;
@@ -866,11 +875,11 @@ int bvh2_traverse_device(BuildCtx& c, const obvhs_bvh2* b, const float* rays, ui
   }
   const uint32_t grid = std::min<uint32_t>(div_up<uint32_t>(n, TBLK), (uint32_t)(per_sm * c.num_sms));
   if (mode == 0)
-    KLAUNCH("k_traverse_bvh2_closest", k_traverse_bvh2<0><<<grid, TBLK, 0, c.stream>>>(
+    KLAUNCH("k_traverse_bvh2_closest", launch_k(k_traverse_bvh2<0>, grid, TBLK, 0, c.stream,
                                            b->nodes, b->n_nodes, b->tris, b->n_prims, (const float4*)rays, n,
                                            (uint2*)hits, nullptr, counter, c.d_status));
   else
-    KLAUNCH("k_traverse_bvh2_occluded", k_traverse_bvh2<1><<<grid, TBLK, 0, c.stream>>>(
+    KLAUNCH("k_traverse_bvh2_occluded", launch_k(k_traverse_bvh2<1>, grid, TBLK, 0, c.stream,
                                             b->nodes, b->n_nodes, b->tris, b->n_prims, (const float4*)rays, n,
                                             nullptr, miss, counter, c.d_status));
   CK(cudaGetLastError());
@@ -889,7 +898,7 @@ int reorder_tris_device(BuildCtx& c, obvhs_cwbvh* b, const float* tris, uint32_t
     cudaGetLastError();
     return c.fail(OBVHS_ERR_OOM, "triangle buffer");
   }
-  KLAUNCH("k_reorder_tris", k_reorder_tris<<<div_up<uint32_t>(b->n_prims, 256), 256, 0, c.stream>>>(tris, n_tris, b->prim_indices, b->n_prims,
+  KLAUNCH("k_reorder_tris", launch_k(k_reorder_tris, div_up<uint32_t>(b->n_prims, 256), 256, 0, c.stream, tris, n_tris, b->prim_indices, b->n_prims,
                                                                           out, c.d_status));
   CK(cudaGetLastError());
   b->tris = out;
@@ -923,7 +932,7 @@ int traverse_tlas_device(BuildCtx& c, const obvhs_cwbvh* tlas, const obvhs_cwbvh
     per_sm_s.store(per_sm);
   }
   const uint32_t grid = std::min<uint32_t>(div_up<uint32_t>(n, TBLK), (uint32_t)(per_sm * c.num_sms));
-  KLAUNCH("k_traverse_tlas", k_traverse_tlas<<<grid, TBLK, 0, c.stream>>>(tlas->nodes, tlas->n_nodes, tlas->prim_indices,
+  KLAUNCH("k_traverse_tlas", launch_k(k_traverse_tlas, grid, TBLK, 0, c.stream, tlas->nodes, tlas->n_nodes, tlas->prim_indices,
                                                                         tlas->n_prims, dd, n_blas, (const float4*)rays,
                                                                         n, (uint4*)hits4, counter, c.d_status));
   CK(cudaGetLastError());
@@ -941,7 +950,7 @@ int compress_tris_device(BuildCtx& c, obvhs_cwbvh* b, const float* tris, uint32_
     cudaGetLastError();
     return c.fail(OBVHS_ERR_OOM, "compressed triangle buffer");
   }
-  KLAUNCH("k_compress_tris", k_compress_tris<<<div_up<uint32_t>(b->n_prims, 256), 256, 0, c.stream>>>(
+  KLAUNCH("k_compress_tris", launch_k(k_compress_tris, div_up<uint32_t>(b->n_prims, 256), 256, 0, c.stream,
                                  tris, n_tris, b->prim_indices, b->n_prims, out, c.d_status));
   CK(cudaGetLastError());
   b->ctris = out;
@@ -966,13 +975,13 @@ int traverse_compressed_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float*
   }
   const uint32_t grid = std::min<uint32_t>(div_up<uint32_t>(n, TBLK), (uint32_t)(per_sm * c.num_sms));
   if (mode == 0)
-    KLAUNCH("k_traverse_closest_ctri", k_traverse<0, true><<<grid, TBLK, 0, c.stream>>>(
+    KLAUNCH("k_traverse_closest_ctri", launch_k(k_traverse<0, true>, grid, TBLK, 0, c.stream,
                                            bvh->nodes, bvh->n_nodes, nullptr, bvh->n_prims, (const float4*)rays, n,
-                                           (uint2*)hits, nullptr, counter, c.d_status, bvh->ctris, bvh->prim_indices));
+                                           (uint2*)hits, nullptr, counter, c.d_status, bvh->ctris, bvh->prim_indices, nullptr, nullptr, 0u));
   else
-    KLAUNCH("k_traverse_occluded_ctri", k_traverse<1, true><<<grid, TBLK, 0, c.stream>>>(
+    KLAUNCH("k_traverse_occluded_ctri", launch_k(k_traverse<1, true>, grid, TBLK, 0, c.stream,
                                             bvh->nodes, bvh->n_nodes, nullptr, bvh->n_prims, (const float4*)rays, n,
-                                            nullptr, miss, counter, c.d_status, bvh->ctris, bvh->prim_indices));
+                                            nullptr, miss, counter, c.d_status, bvh->ctris, bvh->prim_indices, nullptr, nullptr, 0u));
   CK(cudaGetLastError());
   return 0;
 }
@@ -1005,11 +1014,11 @@ int traverse_multi_device(BuildCtx& c, const obvhs_cwbvh* const* bvhs, uint32_t 
   }
   const uint32_t grid = std::min<uint32_t>(div_up<uint32_t>(n, TBLK), (uint32_t)(per_sm * c.num_sms));
   if (mode == 0)
-    KLAUNCH("k_traverse_closest_multi", k_traverse<0, false, true><<<grid, TBLK, 0, c.stream>>>(
+    KLAUNCH("k_traverse_closest_multi", launch_k(k_traverse<0, false, true>, grid, TBLK, 0, c.stream,
                                             nullptr, 0, nullptr, 0, (const float4*)rays, n, (uint2*)hits, nullptr,
                                             counter, c.d_status, nullptr, nullptr, dd, ray_bvh, n_bvh));
   else
-    KLAUNCH("k_traverse_occluded_multi", k_traverse<1, false, true><<<grid, TBLK, 0, c.stream>>>(
+    KLAUNCH("k_traverse_occluded_multi", launch_k(k_traverse<1, false, true>, grid, TBLK, 0, c.stream,
                                              nullptr, 0, nullptr, 0, (const float4*)rays, n, nullptr, miss, counter,
                                              c.d_status, nullptr, nullptr, dd, ray_bvh, n_bvh));
   CK(cudaGetLastError());
@@ -1035,11 +1044,12 @@ int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint
   uint32_t want = div_up<uint32_t>(n, TBLK);
   uint32_t grid = std::min<uint32_t>(want, (uint32_t)(per_sm * c.num_sms));
   if (mode == 0)
-    KLAUNCH("k_traverse_closest", k_traverse<0><<<grid, TBLK, 0, c.stream>>>(bvh->nodes, bvh->n_nodes, bvh->tris, bvh->n_prims, (const float4*)rays, n,
-                                               (uint2*)hits, nullptr, counter, c.d_status));
+    KLAUNCH("k_traverse_closest", launch_k(k_traverse<0>, grid, TBLK, 0, c.stream, bvh->nodes, bvh->n_nodes, bvh->tris, bvh->n_prims, (const float4*)rays, n,
+                                               (uint2*)hits, nullptr, counter, c.d_status, nullptr, nullptr,
+                                               nullptr, nullptr, 0u));
   else
-    KLAUNCH("k_traverse_occluded", k_traverse<1><<<grid, TBLK, 0, c.stream>>>(bvh->nodes, bvh->n_nodes, bvh->tris, bvh->n_prims, (const float4*)rays, n, nullptr,
-                                               miss, counter, c.d_status));
+    KLAUNCH("k_traverse_occluded", launch_k(k_traverse<1>, grid, TBLK, 0, c.stream, bvh->nodes, bvh->n_nodes, bvh->tris, bvh->n_prims, (const float4*)rays, n, nullptr,
+                                               miss, counter, c.d_status, nullptr, nullptr, nullptr, nullptr, 0u));
   CK(cudaGetLastError());
   return 0;
 }
@@ -1059,16 +1069,16 @@ int query_device(BuildCtx& c, int structure, int kind, const void* nodes, uint32
 #define QLAUNCH(FILL, OUT, IDS)                                                                                 \
   do {                                                                                                          \
     if (structure == 0 && kind == 0)                                                                           \
-      KLAUNCH("k_query_bvh2", (k_query_bvh2<0, FILL><<<grid, TBLK, 0, c.stream>>>(b2, n_nodes, pidx, n_pidx,  \
+      KLAUNCH("k_query_bvh2", (launch_k(k_query_bvh2<0, FILL>, grid, TBLK, 0, c.stream, b2, n_nodes, pidx, n_pidx,  \
                                                       queries, n, prims, n_prims, OUT, IDS, c.d_status)));     \
     else if (structure == 0)                                                                                    \
-      KLAUNCH("k_query_bvh2", (k_query_bvh2<1, FILL><<<grid, TBLK, 0, c.stream>>>(b2, n_nodes, pidx, n_pidx,  \
+      KLAUNCH("k_query_bvh2", (launch_k(k_query_bvh2<1, FILL>, grid, TBLK, 0, c.stream, b2, n_nodes, pidx, n_pidx,  \
                                                       queries, n, prims, n_prims, OUT, IDS, c.d_status)));     \
     else if (kind == 0)                                                                                         \
-      KLAUNCH("k_query_cwbvh", (k_query_cwbvh<0, FILL><<<grid, TBLK, 0, c.stream>>>(cw, n_nodes, pidx, n_pidx, \
+      KLAUNCH("k_query_cwbvh", (launch_k(k_query_cwbvh<0, FILL>, grid, TBLK, 0, c.stream, cw, n_nodes, pidx, n_pidx, \
                                                        queries, n, prims, n_prims, oct, OUT, IDS, c.d_status))); \
     else                                                                                                        \
-      KLAUNCH("k_query_cwbvh", (k_query_cwbvh<1, FILL><<<grid, TBLK, 0, c.stream>>>(cw, n_nodes, pidx, n_pidx, \
+      KLAUNCH("k_query_cwbvh", (launch_k(k_query_cwbvh<1, FILL>, grid, TBLK, 0, c.stream, cw, n_nodes, pidx, n_pidx, \
                                                        queries, n, prims, n_prims, oct, OUT, IDS, c.d_status))); \
   } while (0)
   QLAUNCH(false, cnt, nullptr);
