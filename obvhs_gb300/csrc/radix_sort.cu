@@ -1,8 +1,10 @@
 // radix_sort.cu -- see radix_sort.cuh.
 //
 // Onesweep-style LSD radix sort (8-bit digits):
-//   k_rs_hist      one read of the keys: a 256-bin histogram per digit
-//   k_rs_scan      exclusive scan of every histogram (global digit bases)
+//   k_rs_zero      clears the histograms and look-back words (unless the
+//                  kernel that wrote the keys already did, radix_zero)
+//   k_rs_hist      one read of the keys: a 256-bin histogram per digit; the
+//                  last block turns them into global digit bases
 //   k_rs_pass      per digit: tiles claimed in launch order rank their keys
 //                  stably (warp match + per-warp digit counts), publish their
 //                  digit counts and find their global offsets by decoupled
@@ -37,13 +39,18 @@ struct Tile {
 };
 
 // One tile of HIST_ITEMS keys per thread, all loads issued before the
-// shared-memory counting.
+// shared-memory counting, for the low `nd` digits.  The last block to finish
+// (a ticket from `done`) turns every histogram into exclusive digit bases, so
+// no separate scan launch is needed.
 template <class K>
-__global__ void __launch_bounds__(THREADS) k_rs_hist(const K* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist) {
+__global__ void __launch_bounds__(THREADS) k_rs_hist(const K* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
+                                                     int nd, uint32_t* done) {
   grid_dep_wait();
   constexpr int NB = KeyTraits<K>::BYTES;
   __shared__ uint32_t h[NB * 256];
-  for (int i = threadIdx.x; i < NB * 256; i += THREADS) h[i] = 0;
+  __shared__ uint32_t sw[WARPS];
+  __shared__ bool s_last;
+  for (int i = threadIdx.x; i < nd * 256; i += THREADS) h[i] = 0;
   const uint32_t base = blockIdx.x * (THREADS * HIST_ITEMS) + threadIdx.x;
   K k[HIST_ITEMS];
 #pragma unroll
@@ -54,30 +61,42 @@ __global__ void __launch_bounds__(THREADS) k_rs_hist(const K* __restrict__ keys,
   for (int r = 0; r < HIST_ITEMS; r++)
     if (base + r * THREADS < n) {
 #pragma unroll
-      for (int b = 0; b < NB; b++) atomicAdd(&h[b * 256 + KeyTraits<K>::digit(k[r], b)], 1u);
+      for (int b = 0; b < NB; b++)
+        if (b < nd) atomicAdd(&h[b * 256 + KeyTraits<K>::digit(k[r], b)], 1u);
     }
   __syncthreads();
-  for (int i = threadIdx.x; i < NB * 256; i += THREADS)
+  for (int i = threadIdx.x; i < nd * 256; i += THREADS)
     if (h[i]) atomicAdd(&hist[i], h[i]);
+  // release this block's counts, then take a ticket
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int b = 0; b < nd; b++) {
+    uint32_t* hb = hist + b * 256;
+    const uint32_t v = __ldcg(&hb[threadIdx.x]);
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) sw[warp] = x;
+    __syncthreads();
+    uint32_t pre = 0;
+    for (int w = 0; w < warp; w++) pre += sw[w];
+    hb[threadIdx.x] = pre + x - v;
+    __syncthreads();
+  }
 }
 
-// block b scans histogram b in place (exclusive)
-__global__ void __launch_bounds__(THREADS) k_rs_scan(uint32_t* hist) {
+__global__ void k_rs_zero(uint4* p, size_t quads) {
   grid_dep_wait();
-  __shared__ uint32_t sw[WARPS];
-  uint32_t* h = hist + blockIdx.x * 256;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t v = h[threadIdx.x], x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) sw[warp] = x;
-  __syncthreads();
-  uint32_t pre = 0;
-  for (int w = 0; w < warp; w++) pre += sw[w];
-  h[threadIdx.x] = pre + x - v;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < quads; i += (size_t)gridDim.x * blockDim.x)
+    p[i] = make_uint4(0u, 0u, 0u, 0u);
 }
 
 // One digit pass.  Warp w of a tile owns the contiguous keys
@@ -246,23 +265,39 @@ size_t radix_scratch_words(uint32_t n) {
 }
 
 template <class K>
+static uint32_t sort_tiles(uint32_t n) {
+  const int TS = n <= SMALL_SORT_MAX ? Tile<K, true>::SIZE : Tile<K, false>::SIZE;
+  return (n + TS - 1) / TS;
+}
+
+template <class K>
+size_t radix_zero_words(uint32_t n, int digits) {
+  constexpr int NB = KeyTraits<K>::BYTES;
+  const int nd = digits > 0 && digits < NB ? digits : NB;
+  return 16 * 256 + (size_t)nd * ((size_t)sort_tiles<K>(n) * 256 + 32);
+}
+
+template <class K>
 cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, bool init_iota, K* keys_alt,
-                             uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt, int digits) {
+                             uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt, int digits, bool zeroed) {
   constexpr int NB = KeyTraits<K>::BYTES;
   const int nd = digits > 0 && digits < NB ? digits : NB;
   const bool small = n <= SMALL_SORT_MAX;
-  const int TS = small ? Tile<K, true>::SIZE : Tile<K, false>::SIZE;
   *result_in_alt = false;
   if (n == 0) return cudaSuccess;
-  const uint32_t ntiles = (n + TS - 1) / TS;
+  const uint32_t ntiles = sort_tiles<K>(n);
   uint32_t* hist = scratch;
   uint32_t* pass_area = scratch + 16 * 256;
   const size_t pass_words = (size_t)ntiles * 256 + 32;
-  cudaError_t e = cudaMemsetAsync(scratch, 0, (16 * 256 + nd * pass_words) * sizeof(uint32_t), c.stream);
-  if (e) return e;
+  if (!zeroed) {
+    const size_t quads = radix_zero_words<K>(n, digits) / 4;
+    const size_t cap = c.num_sms > 0 ? (size_t)c.num_sms * 8 : 1024;  // a bare context may not know its SMs
+    const uint32_t zb = (uint32_t)std::min<size_t>((quads + 255) / 256, cap);
+    KLAUNCH("k_rs_zero", launch_k(k_rs_zero, zb, 256, 0, c.stream, reinterpret_cast<uint4*>(scratch), quads));
+  }
   const uint32_t hb = (n + THREADS * HIST_ITEMS - 1) / (THREADS * HIST_ITEMS);
-  KLAUNCH("k_rs_hist", launch_k(k_rs_hist<K>, hb, THREADS, 0, c.stream, keys, n, hist));
-  KLAUNCH("k_rs_scan", launch_k(k_rs_scan, nd, THREADS, 0, c.stream, hist));
+  // pass 0's header word 1 is the histogram kernel's ticket counter
+  KLAUNCH("k_rs_hist", launch_k(k_rs_hist<K>, hb, THREADS, 0, c.stream, keys, n, hist, nd, pass_area + 1));
   K* kin = keys;
   uint32_t* vin = vals;
   K* kout = keys_alt;
@@ -293,8 +328,11 @@ cudaError_t fill_iota(uint32_t* v, uint32_t n, cudaStream_t s) {
 }
 
 template cudaError_t radix_sort_pairs<uint32_t>(obvhs_ctx&, uint32_t*, uint32_t*, uint32_t, bool, uint32_t*, uint32_t*,
-                                                uint32_t*, bool*, int);
+                                                uint32_t*, bool*, int, bool);
 template cudaError_t radix_sort_pairs<unsigned long long>(obvhs_ctx&, unsigned long long*, uint32_t*, uint32_t, bool,
-                                                          unsigned long long*, uint32_t*, uint32_t*, bool*, int);
+                                                          unsigned long long*, uint32_t*, uint32_t*, bool*, int, bool);
 template cudaError_t radix_sort_pairs<U128>(obvhs_ctx&, U128*, uint32_t*, uint32_t, bool, U128*, uint32_t*, uint32_t*,
-                                            bool*, int);
+                                            bool*, int, bool);
+template size_t radix_zero_words<uint32_t>(uint32_t, int);
+template size_t radix_zero_words<unsigned long long>(uint32_t, int);
+template size_t radix_zero_words<U128>(uint32_t, int);

@@ -45,10 +45,23 @@ struct KeyTraits<U128> {
 // on the context's stream; no host synchronisation.  `digits` (1..bytes of
 // K) sorts on the low `digits` bytes only, for keys whose upper bytes are
 // known to be zero.
+// `zeroed`: the first radix_zero_words<K>(n, digits) words of `scratch` are
+// already zero (the kernel that produced the keys cleared them with
+// radix_zero), so the sort skips its own clearing launch.
 struct obvhs_ctx;
 template <class K>
 cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, bool init_iota, K* keys_alt,
-                             uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt, int digits = 0);
+                             uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt, int digits = 0,
+                             bool zeroed = false);
+template <class K>
+size_t radix_zero_words(uint32_t n, int digits = 0);
+
+// Clears `words` (a multiple of 4) words at `p` (16-byte aligned) with
+// thread `t` of `stride` threads.
+__device__ __forceinline__ void radix_zero(uint32_t* p, size_t words, size_t t, size_t stride) {
+  uint4* q = reinterpret_cast<uint4*>(p);
+  for (size_t i = t; i < words / 4; i += stride) q[i] = make_uint4(0u, 0u, 0u, 0u);
+}
 
 size_t radix_scratch_words(uint32_t n);
 cudaError_t fill_iota(uint32_t* v, uint32_t n, cudaStream_t s);

@@ -67,9 +67,11 @@ __device__ __forceinline__ uint32_t f32_radix_key(float f) {
   return (s >> 31) ? ~s : (s ^ 0x80000000u);
 }
 
+// Also clears the candidate sort's `zero_words` scratch words.
 __global__ void k_cand_keys(const Bvh2Node* __restrict__ nodes, uint32_t take, uint32_t* __restrict__ keys,
-                            uint32_t* __restrict__ vals) {
+                            uint32_t* __restrict__ vals, uint32_t* sort_scratch, size_t zero_words) {
   grid_dep_wait();
+  radix_zero(sort_scratch, zero_words, blockIdx.x * (size_t)blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   if (i >= take) return;
   Box b = node_box(ld_node(&nodes[i]));
@@ -781,9 +783,10 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
     uint32_t count = node_count - 1;
     if (count == 0) continue;
     // find_candidates
-    KLAUNCH("k_cand_keys", launch_k(k_cand_keys, div_up<uint32_t>(ncand, BLK), BLK, 0, c.stream, b->nodes, take, keys, vals));
+    KLAUNCH("k_cand_keys", launch_k(k_cand_keys, div_up<uint32_t>(ncand, BLK), BLK, 0, c.stream, b->nodes, take, keys, vals,
+                                    rs, radix_zero_words<uint32_t>(ncand)));
     bool alt = false;
-    cudaError_t e = radix_sort_pairs<uint32_t>(c, keys, vals, ncand, false, keys_alt, vals_alt, rs, &alt);
+    cudaError_t e = radix_sort_pairs<uint32_t>(c, keys, vals, ncand, false, keys_alt, vals_alt, rs, &alt, 0, true);
     if (e) return c.cuda_fail(e, "candidate sort");
     // find_reinsertion for the first `count` candidates, then the rest of the pass
     r = reins_pass(c, b->nodes, len, alt ? vals_alt : vals, count, ri, clamp, cap_rt, StackModes{nullptr, nullptr, 0},
