@@ -17,7 +17,8 @@
 // (v0-v1, n.x), (v2-v0, n.y), (n.z, -, -, -) with n = (v0-v1) x (v2-v0),
 // the values Triangle::intersect computes per test.  Rays are 32 bytes
 // (origin, tmin, dir, tmax); results are 8 bytes (original id, t).
-// Persistent warps take 32 rays at a time from a global counter.
+// Persistent warps take rays from a global counter; a lane that finishes
+// its ray takes the next one when enough lanes of its warp are idle.
 #include <cuda_fp16.h>
 
 #include <atomic>
@@ -155,11 +156,22 @@ __device__ __forceinline__ float intersect_ctri(const uint2* rec, float3 o, floa
   return __int_as_float(0x7f800000);
 }
 
+// Lanes of a warp refill once this many of them have finished their rays
+// (persistent warps with per-lane ray fetch): a warp does not wait for its
+// slowest ray before taking new ones.
+constexpr uint32_t REFILL_IDLE = 4;
+
 // MODE 0 closest hit, 1 occlusion.  CTRI: triangles as RtCompressedTriangle
 // (24 B; the hit's original id comes from primitive_indices) instead of the
 // 64-byte records.
 // MULTI: every ray names its BVH (ray_bvh[ray] indexes `multi`), so ray
 // batches against different BVHs run in one launch.
+// Each lane holds one ray and runs its own traversal loop (a step handles
+// the primitives of the current group, then pops one child node or a group
+// from the stack).  A lane that finishes counts itself in its warp's idle
+// counter in shared memory; once REFILL_IDLE lanes are idle, the busy lanes
+// leave their loops keeping their state, and the idle lanes take new rays
+// (one atomic per warp).  The lanes only converge at the refill.
 template <int MODE, bool CTRI = false, bool MULTI = false>
 __global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ nodes_in, uint32_t n_nodes_in,
                                                    const float4* __restrict__ tris_in, uint32_t n_prims_in,
@@ -171,121 +183,170 @@ __global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ no
                                                    const BlasDesc* __restrict__ multi = nullptr,
                                                    const uint32_t* __restrict__ ray_bvh = nullptr, uint32_t n_multi = 0) {
   grid_dep_wait();
+  const uint32_t FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  bool alive = false;    // this lane holds a ray
+  bool drained = false;  // (warp-uniform) the ray counter has run out
+  uint32_t ri = 0;
+  const CwNode* nodes = nodes_in;
+  const float4* tris = tris_in;
+  uint32_t n_nodes = n_nodes_in, n_prims = n_prims_in;
+  float3 o = make_float3(0.0f, 0.0f, 0.0f), d = o, inv = o;
+  float tmin = 0.0f, ray_tmax = 0.0f, tmax = 0.0f, hit_t = 0.0f;
+  uint32_t oct = 0, hit_id = OBVHS_INVALID, sp = 0, guard = 0;
+  uint2 cur = make_uint2(0u, 0u), prim = make_uint2(0u, 0u);
+  uint2 stack[32];
+  __shared__ uint32_t s_idle[TBLK / 32];
+  uint32_t* idle_ctr = &s_idle[threadIdx.x >> 5];
   for (;;) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(next_ray, 32u);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= nrays) return;
-    const uint32_t ri = base + lane;
-    if (ri >= nrays) continue;
-    const CwNode* nodes = nodes_in;
-    const float4* tris = tris_in;
-    uint32_t n_nodes = n_nodes_in, n_prims = n_prims_in;
-    if (MULTI) {
-      const uint32_t b = __ldg(&ray_bvh[ri]);
-      if (b >= n_multi) {
-        set_status(status, ST_BAD_INPUT);
-        if (MODE == 0)
-          hits[ri] = make_uint2(OBVHS_INVALID, 0x7f800000u);
-        else
-          miss[ri] = 1;
-        continue;
+    // idle lanes take the next rays
+    if (!drained) {
+      const uint32_t need = __ballot_sync(FULL, !alive);
+      if (need) {
+        const int leader = __ffs(need) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(next_ray, (uint32_t)__popc(need));
+        base = __shfl_sync(FULL, base, leader);
+        if ((uint64_t)base + __popc(need) >= nrays) drained = true;
+        if (!alive) {
+          ri = base + __popc(need & lt_mask);
+          if (ri < nrays) {
+            alive = true;
+            nodes = nodes_in;
+            tris = tris_in;
+            n_nodes = n_nodes_in;
+            n_prims = n_prims_in;
+            if (MULTI) {
+              const uint32_t bi = __ldg(&ray_bvh[ri]);
+              if (bi >= n_multi) {
+                set_status(status, ST_BAD_INPUT);
+                if (MODE == 0)
+                  hits[ri] = make_uint2(OBVHS_INVALID, 0x7f800000u);
+                else
+                  miss[ri] = 1;
+                alive = false;
+              } else {
+                const BlasDesc bd = multi[bi];
+                nodes = bd.nodes;
+                tris = bd.tris;
+                n_nodes = bd.n_nodes;
+                n_prims = bd.n_prims;
+              }
+            }
+            if (alive) {
+              const float4 r0 = __ldg(&rays[2 * ri]), r1 = __ldg(&rays[2 * ri + 1]);
+              o = make_float3(r0.x, r0.y, r0.z);
+              d = make_float3(r1.x, r1.y, r1.z);
+              tmin = r0.w;
+              ray_tmax = r1.w;
+              inv = make_float3(safe_inverse(d.x), safe_inverse(d.y), safe_inverse(d.z));
+              oct = (d.x < 0.0f ? 0u : 0x04040404u) | (d.y < 0.0f ? 0u : 0x02020202u) |
+                    (d.z < 0.0f ? 0u : 0x01010101u);
+              tmax = ray_tmax;
+              hit_id = OBVHS_INVALID;
+              hit_t = __int_as_float(0x7f800000);
+              sp = 0;
+              guard = 0;
+              cur = n_nodes ? make_uint2(0u, 0x80000000u) : make_uint2(0u, 0u);
+              prim = make_uint2(0u, 0u);
+            }
+          }
+        }
       }
-      const BlasDesc bd = multi[b];
-      nodes = bd.nodes;
-      tris = bd.tris;
-      n_nodes = bd.n_nodes;
-      n_prims = bd.n_prims;
     }
-    const float4 r0 = __ldg(&rays[2 * ri]), r1 = __ldg(&rays[2 * ri + 1]);
-    const float3 o = make_float3(r0.x, r0.y, r0.z), d = make_float3(r1.x, r1.y, r1.z);
-    const float tmin = r0.w, ray_tmax = r1.w;
-    const float3 inv = make_float3(safe_inverse(d.x), safe_inverse(d.y), safe_inverse(d.z));
-    const uint32_t oct = (d.x < 0.0f ? 0u : 0x04040404u) | (d.y < 0.0f ? 0u : 0x02020202u) |
-                         (d.z < 0.0f ? 0u : 0x01010101u);
-    float tmax = ray_tmax;
-    uint32_t hit_id = OBVHS_INVALID;
-    float hit_t = __int_as_float(0x7f800000);
-    uint2 stack[32];
-    uint32_t sp = 0;
-    uint2 cur = n_nodes ? make_uint2(0u, 0x80000000u) : make_uint2(0u, 0u);
-    uint2 prim = make_uint2(0u, 0u);
-    bool done = false;
-    uint32_t guard = 0;
-    while (!done) {
-      if (++guard > (1u << 24)) {
-        set_status(status, ST_ITER_LIMIT);
-        break;
-      }
-      while (prim.y != 0) {
-        const uint32_t lpi = 31u - __clz(prim.y);
-        prim.y &= ~(1u << lpi);
-        const uint32_t pid = prim.x + lpi;
-        if (pid >= n_prims) {
-          set_status(status, ST_BAD_TREE);
-          done = true;
-          break;
+    const uint32_t idle_now = __ballot_sync(FULL, !alive);
+    if (idle_now == FULL) {
+      if (drained) return;
+      continue;
+    }
+    if (lane == 0) *idle_ctr = __popc(idle_now);
+    __syncwarp();
+    if (alive) {
+      for (;;) {
+        bool fin = false;
+        if (++guard > (1u << 24)) {
+          set_status(status, ST_ITER_LIMIT);
+          fin = true;
         }
-        uint32_t orig;
-        float t;
-        if (CTRI) {
-          t = intersect_ctri(&ctris[3 * (size_t)pid], o, d, tmin, MODE == 0 ? tmax : ray_tmax);
-          orig = pid;  // mapped through primitive_indices at the end
-        } else {
-          t = intersect_tri(&tris[4 * (size_t)pid], o, d, tmin, MODE == 0 ? tmax : ray_tmax, &orig);
-        }
-        if (MODE == 0) {
-          if (t < tmax) {
+        while (!fin && prim.y != 0) {
+          const uint32_t lpi = 31u - __clz(prim.y);
+          prim.y &= ~(1u << lpi);
+          const uint32_t pid = prim.x + lpi;
+          if (pid >= n_prims) {
+            set_status(status, ST_BAD_TREE);
+            fin = true;
+            break;
+          }
+          uint32_t orig;
+          float t;
+          if (CTRI) {
+            t = intersect_ctri(&ctris[3 * (size_t)pid], o, d, tmin, MODE == 0 ? tmax : ray_tmax);
+            orig = pid;  // mapped through primitive_indices at the end
+          } else {
+            t = intersect_tri(&tris[4 * (size_t)pid], o, d, tmin, MODE == 0 ? tmax : ray_tmax, &orig);
+          }
+          if (MODE == 0) {
+            if (t < tmax) {
+              hit_id = orig;
+              hit_t = t;
+              tmax = t;
+            }
+          } else if (t < ray_tmax) {
             hit_id = orig;
             hit_t = t;
-            tmax = t;
+            fin = true;
           }
-        } else if (t < ray_tmax) {
-          hit_id = orig;
-          hit_t = t;
-          done = true;
+        }
+        if (!fin) {
+          prim = make_uint2(0u, 0u);
+          if (cur.y & 0xff000000u) {
+            const uint32_t hits_imask = cur.y;
+            const uint32_t cio = 31u - __clz(hits_imask);
+            const uint32_t cbase = cur.x;
+            cur.y &= ~(1u << cio);
+            if (cur.y & 0xff000000u) {
+              stack[sp] = cur;
+              sp = min(sp + 1, 31u);
+            }
+            const uint32_t slot = (cio - 24) ^ (oct & 0xffu);
+            const uint32_t rel = __popc(hits_imask & ~(0xffffffffu << slot));
+            const uint32_t ni = cbase + rel;
+            if (ni >= n_nodes) {
+              set_status(status, ST_BAD_TREE);
+              fin = true;
+            } else {
+              const NodeQ node = load_cw(nodes, ni);
+              const uint32_t hm = intersect_node(node, o, d, inv, MODE == 0 ? tmax : ray_tmax, oct);
+              cur.x = node.q1.x;
+              prim.x = node.q1.y;
+              cur.y = (hm & 0xff000000u) | byte_of(node.q0.w, 3);
+              prim.y = hm & 0x00ffffffu;
+            }
+          } else {
+            cur = make_uint2(0u, 0u);
+          }
+          if (!fin && prim.y == 0 && (cur.y & 0xff000000u) == 0) {
+            if (sp == 0)
+              fin = true;
+            else
+              cur = stack[--sp];
+          }
+        }
+        if (fin) {
+          if (CTRI && hit_id != OBVHS_INVALID) hit_id = __ldg(&pidx[hit_id]);
+          if (MODE == 0)
+            hits[ri] = make_uint2(hit_id, __float_as_uint(hit_t));
+          else
+            miss[ri] = hit_id == OBVHS_INVALID ? 1 : 0;
+          alive = false;
+          atomicAdd(idle_ctr, 1u);
           break;
         }
-      }
-      if (done) break;
-      prim = make_uint2(0u, 0u);
-      if (cur.y & 0xff000000u) {
-        const uint32_t hits_imask = cur.y;
-        const uint32_t cio = 31u - __clz(hits_imask);
-        const uint32_t cbase = cur.x;
-        cur.y &= ~(1u << cio);
-        if (cur.y & 0xff000000u) {
-          stack[sp] = cur;
-          sp = min(sp + 1, 31u);
-        }
-        const uint32_t slot = (cio - 24) ^ (oct & 0xffu);
-        const uint32_t rel = __popc(hits_imask & ~(0xffffffffu << slot));
-        const uint32_t ni = cbase + rel;
-        if (ni >= n_nodes) {
-          set_status(status, ST_BAD_TREE);
-          break;
-        }
-        const NodeQ node = load_cw(nodes, ni);
-        const uint32_t hm = intersect_node(node, o, d, inv, MODE == 0 ? tmax : ray_tmax, oct);
-        cur.x = node.q1.x;
-        prim.x = node.q1.y;
-        cur.y = (hm & 0xff000000u) | byte_of(node.q0.w, 3);
-        prim.y = hm & 0x00ffffffu;
-      } else {
-        cur = make_uint2(0u, 0u);
-      }
-      if (prim.y == 0 && (cur.y & 0xff000000u) == 0) {
-        if (sp == 0) break;
-        sp = sp ? sp - 1 : 0;
-        cur = stack[sp];
+        if (!drained && *(volatile uint32_t*)idle_ctr >= REFILL_IDLE) break;
       }
     }
-    if (CTRI && hit_id != OBVHS_INVALID) hit_id = __ldg(&pidx[hit_id]);
-    if (MODE == 0)
-      hits[ri] = make_uint2(hit_id, __float_as_uint(hit_t));
-    else
-      miss[ri] = hit_id == OBVHS_INVALID ? 1 : 0;
+    __syncwarp();
   }
 }
 
