@@ -161,46 +161,24 @@ __device__ __forceinline__ float intersect_ctri(const uint2* rec, float3 o, floa
 // slowest ray before taking new ones.
 constexpr uint32_t REFILL_IDLE = 4;
 
-// MODE 0 closest hit, 1 occlusion.  CTRI: triangles as RtCompressedTriangle
-// (24 B; the hit's original id comes from primitive_indices) instead of the
-// 64-byte records.
-// MULTI: every ray names its BVH (ray_bvh[ray] indexes `multi`), so ray
-// batches against different BVHs run in one launch.
-// Each lane holds one ray and runs its own traversal loop (a step handles
-// the primitives of the current group, then pops one child node or a group
-// from the stack).  A lane that finishes counts itself in its warp's idle
-// counter in shared memory; once REFILL_IDLE lanes are idle, the busy lanes
-// leave their loops keeping their state, and the idle lanes take new rays
-// (one atomic per warp).  The lanes only converge at the refill.
-template <int MODE, bool CTRI = false, bool MULTI = false>
-__global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ nodes_in, uint32_t n_nodes_in,
-                                                   const float4* __restrict__ tris_in, uint32_t n_prims_in,
-                                                   const float4* __restrict__ rays,
-                                                   uint32_t nrays, uint2* __restrict__ hits, uint8_t* __restrict__ miss,
-                                                   uint32_t* __restrict__ next_ray, uint32_t* status,
-                                                   const uint2* __restrict__ ctris = nullptr,
-                                                   const uint32_t* __restrict__ pidx = nullptr,
-                                                   const BlasDesc* __restrict__ multi = nullptr,
-                                                   const uint32_t* __restrict__ ray_bvh = nullptr, uint32_t n_multi = 0) {
-  grid_dep_wait();
+// Persistent ray loop shared by the traversal kernels.  Each lane holds one
+// ray (`R`: start(ray index) sets it up and returns false when the ray is
+// already finished; step() advances it and returns true once it is finished;
+// both write the ray's result when it finishes) and runs its own loop.  A
+// lane that finishes counts itself in its warp's idle counter in shared
+// memory; once REFILL_IDLE lanes are idle the busy lanes leave their loops,
+// keeping their state, and the idle lanes take the next rays with one atomic
+// per warp.  The lanes converge only at the refill.
+template <class R>
+__device__ __forceinline__ void persistent_rays(R& ray, uint32_t nrays, uint32_t* next_ray) {
   const uint32_t FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  bool alive = false;    // this lane holds a ray
-  bool drained = false;  // (warp-uniform) the ray counter has run out
-  uint32_t ri = 0;
-  const CwNode* nodes = nodes_in;
-  const float4* tris = tris_in;
-  uint32_t n_nodes = n_nodes_in, n_prims = n_prims_in;
-  float3 o = make_float3(0.0f, 0.0f, 0.0f), d = o, inv = o;
-  float tmin = 0.0f, ray_tmax = 0.0f, tmax = 0.0f, hit_t = 0.0f;
-  uint32_t oct = 0, hit_id = OBVHS_INVALID, sp = 0, guard = 0;
-  uint2 cur = make_uint2(0u, 0u), prim = make_uint2(0u, 0u);
-  uint2 stack[32];
   __shared__ uint32_t s_idle[TBLK / 32];
   uint32_t* idle_ctr = &s_idle[threadIdx.x >> 5];
+  bool alive = false;    // this lane holds a ray
+  bool drained = false;  // (warp-uniform) the ray counter has run out
   for (;;) {
-    // idle lanes take the next rays
     if (!drained) {
       const uint32_t need = __ballot_sync(FULL, !alive);
       if (need) {
@@ -210,48 +188,8 @@ __global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ no
         base = __shfl_sync(FULL, base, leader);
         if ((uint64_t)base + __popc(need) >= nrays) drained = true;
         if (!alive) {
-          ri = base + __popc(need & lt_mask);
-          if (ri < nrays) {
-            alive = true;
-            nodes = nodes_in;
-            tris = tris_in;
-            n_nodes = n_nodes_in;
-            n_prims = n_prims_in;
-            if (MULTI) {
-              const uint32_t bi = __ldg(&ray_bvh[ri]);
-              if (bi >= n_multi) {
-                set_status(status, ST_BAD_INPUT);
-                if (MODE == 0)
-                  hits[ri] = make_uint2(OBVHS_INVALID, 0x7f800000u);
-                else
-                  miss[ri] = 1;
-                alive = false;
-              } else {
-                const BlasDesc bd = multi[bi];
-                nodes = bd.nodes;
-                tris = bd.tris;
-                n_nodes = bd.n_nodes;
-                n_prims = bd.n_prims;
-              }
-            }
-            if (alive) {
-              const float4 r0 = __ldg(&rays[2 * ri]), r1 = __ldg(&rays[2 * ri + 1]);
-              o = make_float3(r0.x, r0.y, r0.z);
-              d = make_float3(r1.x, r1.y, r1.z);
-              tmin = r0.w;
-              ray_tmax = r1.w;
-              inv = make_float3(safe_inverse(d.x), safe_inverse(d.y), safe_inverse(d.z));
-              oct = (d.x < 0.0f ? 0u : 0x04040404u) | (d.y < 0.0f ? 0u : 0x02020202u) |
-                    (d.z < 0.0f ? 0u : 0x01010101u);
-              tmax = ray_tmax;
-              hit_id = OBVHS_INVALID;
-              hit_t = __int_as_float(0x7f800000);
-              sp = 0;
-              guard = 0;
-              cur = n_nodes ? make_uint2(0u, 0x80000000u) : make_uint2(0u, 0u);
-              prim = make_uint2(0u, 0u);
-            }
-          }
+          const uint32_t ri = base + __popc(need & lt_mask);
+          if (ri < nrays) alive = ray.start(ri);
         }
       }
     }
@@ -264,81 +202,7 @@ __global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ no
     __syncwarp();
     if (alive) {
       for (;;) {
-        bool fin = false;
-        if (++guard > (1u << 24)) {
-          set_status(status, ST_ITER_LIMIT);
-          fin = true;
-        }
-        while (!fin && prim.y != 0) {
-          const uint32_t lpi = 31u - __clz(prim.y);
-          prim.y &= ~(1u << lpi);
-          const uint32_t pid = prim.x + lpi;
-          if (pid >= n_prims) {
-            set_status(status, ST_BAD_TREE);
-            fin = true;
-            break;
-          }
-          uint32_t orig;
-          float t;
-          if (CTRI) {
-            t = intersect_ctri(&ctris[3 * (size_t)pid], o, d, tmin, MODE == 0 ? tmax : ray_tmax);
-            orig = pid;  // mapped through primitive_indices at the end
-          } else {
-            t = intersect_tri(&tris[4 * (size_t)pid], o, d, tmin, MODE == 0 ? tmax : ray_tmax, &orig);
-          }
-          if (MODE == 0) {
-            if (t < tmax) {
-              hit_id = orig;
-              hit_t = t;
-              tmax = t;
-            }
-          } else if (t < ray_tmax) {
-            hit_id = orig;
-            hit_t = t;
-            fin = true;
-          }
-        }
-        if (!fin) {
-          prim = make_uint2(0u, 0u);
-          if (cur.y & 0xff000000u) {
-            const uint32_t hits_imask = cur.y;
-            const uint32_t cio = 31u - __clz(hits_imask);
-            const uint32_t cbase = cur.x;
-            cur.y &= ~(1u << cio);
-            if (cur.y & 0xff000000u) {
-              stack[sp] = cur;
-              sp = min(sp + 1, 31u);
-            }
-            const uint32_t slot = (cio - 24) ^ (oct & 0xffu);
-            const uint32_t rel = __popc(hits_imask & ~(0xffffffffu << slot));
-            const uint32_t ni = cbase + rel;
-            if (ni >= n_nodes) {
-              set_status(status, ST_BAD_TREE);
-              fin = true;
-            } else {
-              const NodeQ node = load_cw(nodes, ni);
-              const uint32_t hm = intersect_node(node, o, d, inv, MODE == 0 ? tmax : ray_tmax, oct);
-              cur.x = node.q1.x;
-              prim.x = node.q1.y;
-              cur.y = (hm & 0xff000000u) | byte_of(node.q0.w, 3);
-              prim.y = hm & 0x00ffffffu;
-            }
-          } else {
-            cur = make_uint2(0u, 0u);
-          }
-          if (!fin && prim.y == 0 && (cur.y & 0xff000000u) == 0) {
-            if (sp == 0)
-              fin = true;
-            else
-              cur = stack[--sp];
-          }
-        }
-        if (fin) {
-          if (CTRI && hit_id != OBVHS_INVALID) hit_id = __ldg(&pidx[hit_id]);
-          if (MODE == 0)
-            hits[ri] = make_uint2(hit_id, __float_as_uint(hit_t));
-          else
-            miss[ri] = hit_id == OBVHS_INVALID ? 1 : 0;
+        if (ray.step()) {
           alive = false;
           atomicAdd(idle_ctr, 1u);
           break;
@@ -348,6 +212,179 @@ __global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ no
     }
     __syncwarp();
   }
+}
+
+// One ray of k_traverse.  MODE 0 closest hit, 1 occlusion.  CTRI: triangles
+// as RtCompressedTriangle (24 B; the hit's original id comes from
+// primitive_indices) instead of the 64-byte records.  MULTI: every ray names
+// its BVH (ray_bvh[ray] indexes `multi`), so ray batches against different
+// BVHs run in one launch.  A step handles the primitives of the current
+// group, then pops one child node (or a group from the stack).
+template <int MODE, bool CTRI, bool MULTI>
+struct CwRay {
+  // launch inputs
+  const CwNode* nodes_in;
+  const float4* tris_in;
+  uint32_t n_nodes_in, n_prims_in;
+  const float4* rays;
+  uint2* hits;
+  uint8_t* miss;
+  uint32_t* status;
+  const uint2* ctris;
+  const uint32_t* pidx;
+  const BlasDesc* multi;
+  const uint32_t* ray_bvh;
+  uint32_t n_multi;
+  // the ray
+  const CwNode* nodes;
+  const float4* tris;
+  uint32_t n_nodes, n_prims, ri, oct, hit_id, sp, guard;
+  float3 o, d, inv;
+  float tmin, ray_tmax, tmax, hit_t;
+  uint2 cur, prim;
+  uint2* stack;  // 32 entries, the thread's own (kept apart so the scalars stay in registers)
+
+  __device__ __forceinline__ bool start(uint32_t r) {
+    ri = r;
+    nodes = nodes_in;
+    tris = tris_in;
+    n_nodes = n_nodes_in;
+    n_prims = n_prims_in;
+    if (MULTI) {
+      const uint32_t bi = __ldg(&ray_bvh[ri]);
+      if (bi >= n_multi) {
+        set_status(status, ST_BAD_INPUT);
+        if (MODE == 0)
+          hits[ri] = make_uint2(OBVHS_INVALID, 0x7f800000u);
+        else
+          miss[ri] = 1;
+        return false;
+      }
+      const BlasDesc bd = multi[bi];
+      nodes = bd.nodes;
+      tris = bd.tris;
+      n_nodes = bd.n_nodes;
+      n_prims = bd.n_prims;
+    }
+    const float4 r0 = __ldg(&rays[2 * ri]), r1 = __ldg(&rays[2 * ri + 1]);
+    o = make_float3(r0.x, r0.y, r0.z);
+    d = make_float3(r1.x, r1.y, r1.z);
+    tmin = r0.w;
+    ray_tmax = r1.w;
+    inv = make_float3(safe_inverse(d.x), safe_inverse(d.y), safe_inverse(d.z));
+    oct = (d.x < 0.0f ? 0u : 0x04040404u) | (d.y < 0.0f ? 0u : 0x02020202u) | (d.z < 0.0f ? 0u : 0x01010101u);
+    tmax = ray_tmax;
+    hit_id = OBVHS_INVALID;
+    hit_t = __int_as_float(0x7f800000);
+    sp = 0;
+    guard = 0;
+    cur = n_nodes ? make_uint2(0u, 0x80000000u) : make_uint2(0u, 0u);
+    prim = make_uint2(0u, 0u);
+    return true;
+  }
+
+  __device__ __forceinline__ bool finish() {
+    if (CTRI && hit_id != OBVHS_INVALID) hit_id = __ldg(&pidx[hit_id]);
+    if (MODE == 0)
+      hits[ri] = make_uint2(hit_id, __float_as_uint(hit_t));
+    else
+      miss[ri] = hit_id == OBVHS_INVALID ? 1 : 0;
+    return true;
+  }
+
+  __device__ __forceinline__ bool step() {
+    if (++guard > (1u << 24)) {
+      set_status(status, ST_ITER_LIMIT);
+      return finish();
+    }
+    while (prim.y != 0) {
+      const uint32_t lpi = 31u - __clz(prim.y);
+      prim.y &= ~(1u << lpi);
+      const uint32_t pid = prim.x + lpi;
+      if (pid >= n_prims) {
+        set_status(status, ST_BAD_TREE);
+        return finish();
+      }
+      uint32_t orig;
+      float t;
+      if (CTRI) {
+        t = intersect_ctri(&ctris[3 * (size_t)pid], o, d, tmin, MODE == 0 ? tmax : ray_tmax);
+        orig = pid;  // mapped through primitive_indices at the end
+      } else {
+        t = intersect_tri(&tris[4 * (size_t)pid], o, d, tmin, MODE == 0 ? tmax : ray_tmax, &orig);
+      }
+      if (MODE == 0) {
+        if (t < tmax) {
+          hit_id = orig;
+          hit_t = t;
+          tmax = t;
+        }
+      } else if (t < ray_tmax) {
+        hit_id = orig;
+        hit_t = t;
+        return finish();
+      }
+    }
+    if (cur.y & 0xff000000u) {
+      const uint32_t hits_imask = cur.y;
+      const uint32_t cio = 31u - __clz(hits_imask);
+      const uint32_t cbase = cur.x;
+      cur.y &= ~(1u << cio);
+      if (cur.y & 0xff000000u) {
+        stack[sp] = cur;
+        sp = min(sp + 1, 31u);
+      }
+      const uint32_t slot = (cio - 24) ^ (oct & 0xffu);
+      const uint32_t ni = cbase + __popc(hits_imask & ~(0xffffffffu << slot));
+      if (ni >= n_nodes) {
+        set_status(status, ST_BAD_TREE);
+        return finish();
+      }
+      const NodeQ node = load_cw(nodes, ni);
+      const uint32_t hm = intersect_node(node, o, d, inv, MODE == 0 ? tmax : ray_tmax, oct);
+      cur.x = node.q1.x;
+      prim.x = node.q1.y;
+      cur.y = (hm & 0xff000000u) | byte_of(node.q0.w, 3);
+      prim.y = hm & 0x00ffffffu;
+    } else {
+      cur = make_uint2(0u, 0u);
+    }
+    if (prim.y == 0 && (cur.y & 0xff000000u) == 0) {
+      if (sp == 0) return finish();
+      cur = stack[--sp];
+    }
+    return false;
+  }
+};
+
+template <int MODE, bool CTRI = false, bool MULTI = false>
+__global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ nodes_in, uint32_t n_nodes_in,
+                                                   const float4* __restrict__ tris_in, uint32_t n_prims_in,
+                                                   const float4* __restrict__ rays,
+                                                   uint32_t nrays, uint2* __restrict__ hits, uint8_t* __restrict__ miss,
+                                                   uint32_t* __restrict__ next_ray, uint32_t* status,
+                                                   const uint2* __restrict__ ctris = nullptr,
+                                                   const uint32_t* __restrict__ pidx = nullptr,
+                                                   const BlasDesc* __restrict__ multi = nullptr,
+                                                   const uint32_t* __restrict__ ray_bvh = nullptr, uint32_t n_multi = 0) {
+  grid_dep_wait();
+  uint2 stack[32];
+  CwRay<MODE, CTRI, MULTI> ray;
+  ray.stack = stack;
+  ray.nodes_in = nodes_in;
+  ray.tris_in = tris_in;
+  ray.n_nodes_in = n_nodes_in;
+  ray.n_prims_in = n_prims_in;
+  ray.rays = rays;
+  ray.hits = hits;
+  ray.miss = miss;
+  ray.status = status;
+  ray.ctris = ctris;
+  ray.pidx = pidx;
+  ray.multi = multi;
+  ray.ray_bvh = ray_bvh;
+  ray.n_multi = n_multi;
+  persistent_rays(ray, nrays, next_ray);
 }
 
 // --- Bvh2::ray_traverse / ray_traverse_miss (src/bvh2/mod.rs:148-337) -----------
@@ -367,10 +404,133 @@ __device__ __forceinline__ float box_ray_t(const Bvh2Node& nd, float3 o, float3 
 
 constexpr int BVH2_STACK = 128;
 
-// One ray per thread (persistent warps).  The reference's loop: test both
-// children of the current node, nearer first; leaves are intersected at once
-// (closest hit: every primitive, ray.tmax shrinking; occlusion: stop at the
-// first t < tmax), the farther hit child is pushed, the nearer followed.
+// One ray of k_traverse_bvh2.  The reference's loop: test both children of
+// the current node, nearer first; leaves are intersected at once (closest
+// hit: every primitive, ray.tmax shrinking; occlusion: stop at the first
+// t < tmax), the farther hit child is pushed, the nearer followed.  A step
+// is one node's pair of children.
+template <int MODE>
+struct Bvh2Ray {
+  const Bvh2Node* nodes;
+  const float4* tris;
+  uint32_t n_nodes, n_prims;
+  const float4* rays;
+  uint2* hits;
+  uint8_t* miss;
+  uint32_t* status;
+  uint32_t* stack;  // BVH2_STACK entries, the thread's own
+  uint32_t ri, hit_id, sp, cur, guard;
+  float3 o, inv;
+  float3 d;
+  float tmin, tmax, hit_t;
+  bool stop, bad;
+
+  // the primitives of leaf x; MODE 1 stops at the first hit
+  __device__ __forceinline__ void leaf(const Bvh2Node& x) {
+    const uint32_t f = node_first(x), cnt = node_prims(x);
+    for (uint32_t k = 0; k < cnt; k++) {
+      if (f + k >= n_prims) {
+        bad = true;
+        return;
+      }
+      uint32_t orig;
+      const float t = intersect_tri(&tris[4 * (size_t)(f + k)], o, d, tmin, tmax, &orig);
+      if (t < tmax) {
+        hit_id = orig;
+        hit_t = t;
+        if (MODE == 0) {
+          tmax = t;
+        } else {
+          stop = true;
+          return;
+        }
+      }
+    }
+  }
+
+  __device__ __forceinline__ bool finish() {
+    if (bad) set_status(status, ST_BAD_TREE);
+    if (MODE == 0)
+      hits[ri] = make_uint2(hit_id, __float_as_uint(hit_id == OBVHS_INVALID ? __int_as_float(0x7f800000) : hit_t));
+    else
+      miss[ri] = hit_id == OBVHS_INVALID ? 1 : 0;
+    return true;
+  }
+
+  __device__ __forceinline__ bool start(uint32_t r) {
+    ri = r;
+    const float4 r0 = __ldg(&rays[2 * ri]), r1 = __ldg(&rays[2 * ri + 1]);
+    o = make_float3(r0.x, r0.y, r0.z);
+    d = make_float3(r1.x, r1.y, r1.z);
+    tmin = r0.w;
+    tmax = r1.w;
+    inv = make_float3(safe_inverse(d.x), safe_inverse(d.y), safe_inverse(d.z));
+    hit_id = OBVHS_INVALID;
+    hit_t = __int_as_float(0x7f800000);
+    stop = bad = false;
+    if (n_nodes) {
+      const Bvh2Node root = ld_node(&nodes[0]);
+      if (box_ray_t(root, o, inv) < tmax) {
+        if (node_prims(root) == 0) {
+          sp = 0;
+          guard = 0;
+          cur = node_first(root);
+          return true;
+        }
+        leaf(root);
+      }
+    }
+    finish();
+    return false;
+  }
+
+  __device__ __forceinline__ bool step() {
+    if (guard++ > (1u << 24) || cur + 1 >= n_nodes) {
+      bad = true;
+      return finish();
+    }
+    Bvh2Node l = ld_node(&nodes[cur]), r = ld_node(&nodes[cur + 1]);
+    float lt = box_ray_t(l, o, inv), rt = box_ray_t(r, o, inv);
+    if (lt > rt) {
+      const float tt = lt;
+      lt = rt;
+      rt = tt;
+      const Bvh2Node tn = l;
+      l = r;
+      r = tn;
+    }
+    bool go_l = lt < tmax;
+    if (go_l && node_prims(l) != 0) {
+      leaf(l);
+      if (stop || bad) return finish();
+      go_l = false;
+    }
+    bool go_r = rt < tmax;
+    if (go_r && node_prims(r) != 0) {
+      leaf(r);
+      if (stop || bad) return finish();
+      go_r = false;
+    }
+    if (go_l && go_r) {
+      if (sp >= BVH2_STACK) {
+        set_status(status, ST_STACK_OVERFLOW);
+        bad = true;
+        return finish();
+      }
+      stack[sp++] = node_first(r);
+      cur = node_first(l);
+    } else if (go_l) {
+      cur = node_first(l);
+    } else if (go_r) {
+      cur = node_first(r);
+    } else {
+      if (sp == 0) return finish();
+      cur = stack[--sp];
+    }
+    return false;
+  }
+};
+
 template <int MODE>
 __global__ void __launch_bounds__(TBLK) k_traverse_bvh2(const Bvh2Node* __restrict__ nodes, uint32_t n_nodes,
                                                         const float4* __restrict__ tris, uint32_t n_prims,
@@ -378,105 +538,18 @@ __global__ void __launch_bounds__(TBLK) k_traverse_bvh2(const Bvh2Node* __restri
                                                         uint2* __restrict__ hits, uint8_t* __restrict__ miss,
                                                         uint32_t* __restrict__ next_ray, uint32_t* status) {
   grid_dep_wait();
-  const int lane = threadIdx.x & 31;
-  for (;;) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(next_ray, 32u);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= nrays) return;
-    const uint32_t ri = base + lane;
-    if (ri >= nrays) continue;
-    const float4 r0 = __ldg(&rays[2 * ri]), r1 = __ldg(&rays[2 * ri + 1]);
-    const float3 o = make_float3(r0.x, r0.y, r0.z), d = make_float3(r1.x, r1.y, r1.z);
-    const float tmin = r0.w;
-    float tmax = r1.w;
-    const float3 inv = make_float3(safe_inverse(d.x), safe_inverse(d.y), safe_inverse(d.z));
-    uint32_t hit_id = OBVHS_INVALID;
-    float hit_t = __int_as_float(0x7f800000);
-    bool stop = false, bad = false;
-    // the primitives of leaf x; MODE 1 stops at the first hit
-    auto leaf = [&](const Bvh2Node& x) {
-      const uint32_t f = node_first(x), cnt = node_prims(x);
-      for (uint32_t k = 0; k < cnt; k++) {
-        if (f + k >= n_prims) {
-          bad = true;
-          return;
-        }
-        uint32_t orig;
-        const float t = intersect_tri(&tris[4 * (size_t)(f + k)], o, d, tmin, tmax, &orig);
-        if (t < tmax) {
-          hit_id = orig;
-          hit_t = t;
-          if (MODE == 0) {
-            tmax = t;
-          } else {
-            stop = true;
-            return;
-          }
-        }
-      }
-    };
-    if (n_nodes) {
-      const Bvh2Node root = ld_node(&nodes[0]);
-      if (box_ray_t(root, o, inv) < tmax) {
-        if (node_prims(root) != 0) {
-          leaf(root);
-        } else {
-          uint32_t stack[BVH2_STACK];
-          uint32_t sp = 0, cur = node_first(root);
-          for (uint32_t guard = 0;; guard++) {
-            if (guard > (1u << 24) || cur + 1 >= n_nodes) {
-              bad = true;
-              break;
-            }
-            Bvh2Node l = ld_node(&nodes[cur]), r = ld_node(&nodes[cur + 1]);
-            float lt = box_ray_t(l, o, inv), rt = box_ray_t(r, o, inv);
-            if (lt > rt) {
-              const float tt = lt;
-              lt = rt;
-              rt = tt;
-              const Bvh2Node tn = l;
-              l = r;
-              r = tn;
-            }
-            bool go_l = lt < tmax;
-            if (go_l && node_prims(l) != 0) {
-              leaf(l);
-              if (stop || bad) break;
-              go_l = false;
-            }
-            bool go_r = rt < tmax;
-            if (go_r && node_prims(r) != 0) {
-              leaf(r);
-              if (stop || bad) break;
-              go_r = false;
-            }
-            if (go_l && go_r) {
-              if (sp >= BVH2_STACK) {
-                set_status(status, ST_STACK_OVERFLOW);
-                bad = true;
-                break;
-              }
-              stack[sp++] = node_first(r);
-              cur = node_first(l);
-            } else if (go_l) {
-              cur = node_first(l);
-            } else if (go_r) {
-              cur = node_first(r);
-            } else {
-              if (sp == 0) break;
-              cur = stack[--sp];
-            }
-          }
-        }
-      }
-    }
-    if (bad) set_status(status, ST_BAD_TREE);
-    if (MODE == 0)
-      hits[ri] = make_uint2(hit_id, __float_as_uint(hit_id == OBVHS_INVALID ? __int_as_float(0x7f800000) : hit_t));
-    else
-      miss[ri] = hit_id == OBVHS_INVALID ? 1 : 0;
-  }
+  uint32_t stack[BVH2_STACK];
+  Bvh2Ray<MODE> ray;
+  ray.nodes = nodes;
+  ray.tris = tris;
+  ray.n_nodes = n_nodes;
+  ray.n_prims = n_prims;
+  ray.rays = rays;
+  ray.hits = hits;
+  ray.miss = miss;
+  ray.status = status;
+  ray.stack = stack;
+  persistent_rays(ray, nrays, next_ray);
 }
 
 // --- AABB and point queries (src/bvh2/mod.rs:365-460, src/cwbvh/node.rs:157-200) ---
@@ -705,6 +778,142 @@ __global__ void k_compress_tris(const float* __restrict__ tris, uint32_t n_tris,
 // in the reference, the remaining instances of a TLAS leaf group are pushed
 // as a primitive group and dropped when popped, and the ray is not
 // transformed into the instance's space.
+struct TlasRay {
+  const CwNode* tlas;
+  uint32_t n_tlas;
+  const uint32_t* tlas_pidx;
+  uint32_t n_tlas_prims;
+  const BlasDesc* blas;
+  uint32_t n_blas;
+  const float4* rays;
+  uint4* hits;
+  uint32_t* status;
+  uint2* stack;  // 32 entries, the thread's own
+  const CwNode* nodes;
+  const float4* tris;
+  uint32_t n_nodes, n_prims, ri, oct, sp, tlas_sp, mesh, guard;
+  uint32_t hit_prim, hit_mesh, hit_orig;
+  float3 o, d, inv;
+  float tmin, tmax;
+  uint2 cur;
+
+  __device__ __forceinline__ bool finish(bool bad) {
+    if (bad) hit_prim = OBVHS_INVALID;
+    hits[ri] = hit_prim == OBVHS_INVALID ? make_uint4(OBVHS_INVALID, OBVHS_INVALID, OBVHS_INVALID, 0x7f800000u)
+                                         : make_uint4(hit_mesh, hit_prim, hit_orig, __float_as_uint(tmax));
+    return true;
+  }
+
+  __device__ __forceinline__ bool start(uint32_t r) {
+    ri = r;
+    const float4 r0 = __ldg(&rays[2 * ri]), r1 = __ldg(&rays[2 * ri + 1]);
+    o = make_float3(r0.x, r0.y, r0.z);
+    d = make_float3(r1.x, r1.y, r1.z);
+    tmin = r0.w;
+    tmax = r1.w;
+    inv = make_float3(safe_inverse(d.x), safe_inverse(d.y), safe_inverse(d.z));
+    oct = (d.x < 0.0f ? 0u : 0x04040404u) | (d.y < 0.0f ? 0u : 0x02020202u) | (d.z < 0.0f ? 0u : 0x01010101u);
+    sp = 0;
+    tlas_sp = OBVHS_INVALID;
+    mesh = OBVHS_INVALID;
+    nodes = tlas;
+    n_nodes = n_tlas;
+    tris = nullptr;
+    n_prims = 0;
+    hit_prim = hit_mesh = hit_orig = OBVHS_INVALID;
+    cur = n_tlas ? make_uint2(0u, 0x80000000u) : make_uint2(0u, 0u);
+    guard = 0;
+    return true;
+  }
+
+  // One node of the TLAS or a BLAS, then its primitives: a TLAS primitive
+  // continues at the root of its BLAS (the TLAS state goes on the stack).
+  __device__ __forceinline__ bool step() {
+    if (guard++ > (1u << 24)) {
+      set_status(status, ST_ITER_LIMIT);
+      return finish(true);
+    }
+    uint2 prim = make_uint2(0u, 0u);
+    if (cur.y & 0xff000000u) {
+      const uint32_t hits_imask = cur.y;
+      const uint32_t cio = 31u - __clz(hits_imask);
+      const uint32_t cbase = cur.x;
+      cur.y &= ~(1u << cio);
+      if (cur.y & 0xff000000u) {
+        stack[sp] = cur;
+        sp = min(sp + 1, 31u);
+      }
+      const uint32_t slot = (cio - 24) ^ (oct & 0xffu);
+      const uint32_t ni = cbase + __popc(hits_imask & ~(0xffffffffu << slot));
+      if (ni >= n_nodes) {
+        set_status(status, ST_BAD_TREE);
+        return finish(true);
+      }
+      const NodeQ node = load_cw(nodes, ni);
+      const uint32_t hm = intersect_node(node, o, d, inv, tmax, oct);
+      cur.x = node.q1.x;
+      prim.x = node.q1.y;
+      cur.y = (hm & 0xff000000u) | byte_of(node.q0.w, 3);
+      prim.y = hm & 0x00ffffffu;
+    } else {
+      cur = make_uint2(0u, 0u);
+    }
+    while (prim.y != 0) {
+      const uint32_t lpi = 31u - __clz(prim.y);
+      prim.y &= ~(1u << lpi);
+      const uint32_t gpi = prim.x + lpi;
+      if (tlas_sp == OBVHS_INVALID) {
+        // a TLAS primitive: continue at the root of its BLAS
+        if (prim.y != 0) {
+          stack[sp] = prim;
+          sp = min(sp + 1, 31u);
+        }
+        if (cur.y & 0xff000000u) {
+          stack[sp] = cur;
+          sp = min(sp + 1, 31u);
+        }
+        tlas_sp = sp;
+        const uint32_t b = gpi < n_tlas_prims ? __ldg(&tlas_pidx[gpi]) : OBVHS_INVALID;
+        if (b >= n_blas) {
+          set_status(status, ST_BAD_TREE);
+          return finish(true);
+        }
+        const BlasDesc bd = blas[b];
+        nodes = bd.nodes;
+        n_nodes = bd.n_nodes;
+        tris = bd.tris;
+        n_prims = bd.n_prims;
+        mesh = b;
+        cur = make_uint2(0u, 0x80000000u);
+        break;
+      }
+      if (gpi >= n_prims) {
+        set_status(status, ST_BAD_TREE);
+        return finish(true);
+      }
+      uint32_t orig;
+      const float t = intersect_tri(&tris[4 * (size_t)gpi], o, d, tmin, tmax, &orig);
+      if (t < tmax) {
+        hit_prim = gpi;
+        hit_mesh = mesh;
+        hit_orig = orig;
+        tmax = t;
+      }
+    }
+    if ((cur.y & 0xff000000u) == 0) {
+      if (sp == 0) return finish(false);
+      if (sp == tlas_sp) {
+        tlas_sp = OBVHS_INVALID;
+        mesh = OBVHS_INVALID;
+        nodes = tlas;
+        n_nodes = n_tlas;
+      }
+      cur = stack[--sp];
+    }
+    return false;
+  }
+};
+
 __global__ void __launch_bounds__(TBLK) k_traverse_tlas(const CwNode* __restrict__ tlas, uint32_t n_tlas,
                                                         const uint32_t* __restrict__ tlas_pidx, uint32_t n_tlas_prims,
                                                         const BlasDesc* __restrict__ blas, uint32_t n_blas,
@@ -712,125 +921,19 @@ __global__ void __launch_bounds__(TBLK) k_traverse_tlas(const CwNode* __restrict
                                                         uint4* __restrict__ hits, uint32_t* __restrict__ next_ray,
                                                         uint32_t* status) {
   grid_dep_wait();
-  const int lane = threadIdx.x & 31;
-  for (;;) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(next_ray, 32u);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= nrays) return;
-    const uint32_t ri = base + lane;
-    if (ri >= nrays) continue;
-    const float4 r0 = __ldg(&rays[2 * ri]), r1 = __ldg(&rays[2 * ri + 1]);
-    const float3 o = make_float3(r0.x, r0.y, r0.z), d = make_float3(r1.x, r1.y, r1.z);
-    const float tmin = r0.w;
-    float tmax = r1.w;
-    const float3 inv = make_float3(safe_inverse(d.x), safe_inverse(d.y), safe_inverse(d.z));
-    const uint32_t oct = (d.x < 0.0f ? 0u : 0x04040404u) | (d.y < 0.0f ? 0u : 0x02020202u) |
-                         (d.z < 0.0f ? 0u : 0x01010101u);
-    uint2 stack[32];
-    uint32_t sp = 0;
-    uint32_t tlas_sp = OBVHS_INVALID, mesh = OBVHS_INVALID;
-    const CwNode* nodes = tlas;
-    uint32_t n_nodes = n_tlas;
-    const float4* tris = nullptr;
-    uint32_t n_prims = 0;
-    uint32_t hit_prim = OBVHS_INVALID, hit_mesh = OBVHS_INVALID, hit_orig = OBVHS_INVALID;
-    uint2 cur = n_tlas ? make_uint2(0u, 0x80000000u) : make_uint2(0u, 0u);
-    bool bad = false;
-    for (uint32_t guard = 0;; guard++) {
-      if (guard > (1u << 24)) {
-        set_status(status, ST_ITER_LIMIT);
-        bad = true;
-        break;
-      }
-      uint2 prim = make_uint2(0u, 0u);
-      if (cur.y & 0xff000000u) {
-        const uint32_t hits_imask = cur.y;
-        const uint32_t cio = 31u - __clz(hits_imask);
-        const uint32_t cbase = cur.x;
-        cur.y &= ~(1u << cio);
-        if (cur.y & 0xff000000u) {
-          stack[sp] = cur;
-          sp = min(sp + 1, 31u);
-        }
-        const uint32_t slot = (cio - 24) ^ (oct & 0xffu);
-        const uint32_t ni = cbase + __popc(hits_imask & ~(0xffffffffu << slot));
-        if (ni >= n_nodes) {
-          set_status(status, ST_BAD_TREE);
-          bad = true;
-          break;
-        }
-        const NodeQ node = load_cw(nodes, ni);
-        const uint32_t hm = intersect_node(node, o, d, inv, tmax, oct);
-        cur.x = node.q1.x;
-        prim.x = node.q1.y;
-        cur.y = (hm & 0xff000000u) | byte_of(node.q0.w, 3);
-        prim.y = hm & 0x00ffffffu;
-      } else {
-        cur = make_uint2(0u, 0u);
-      }
-      while (prim.y != 0) {
-        const uint32_t lpi = 31u - __clz(prim.y);
-        prim.y &= ~(1u << lpi);
-        const uint32_t gpi = prim.x + lpi;
-        if (tlas_sp == OBVHS_INVALID) {
-          // a TLAS primitive: continue at the root of its BLAS
-          if (prim.y != 0) {
-            stack[sp] = prim;
-            sp = min(sp + 1, 31u);
-          }
-          if (cur.y & 0xff000000u) {
-            stack[sp] = cur;
-            sp = min(sp + 1, 31u);
-          }
-          tlas_sp = sp;
-          const uint32_t b = gpi < n_tlas_prims ? __ldg(&tlas_pidx[gpi]) : OBVHS_INVALID;
-          if (b >= n_blas) {
-            set_status(status, ST_BAD_TREE);
-            bad = true;
-            break;
-          }
-          const BlasDesc bd = blas[b];
-          nodes = bd.nodes;
-          n_nodes = bd.n_nodes;
-          tris = bd.tris;
-          n_prims = bd.n_prims;
-          mesh = b;
-          cur = make_uint2(0u, 0x80000000u);
-          break;
-        }
-        if (gpi >= n_prims) {
-          set_status(status, ST_BAD_TREE);
-          bad = true;
-          break;
-        }
-        uint32_t orig;
-        const float t = intersect_tri(&tris[4 * (size_t)gpi], o, d, tmin, tmax, &orig);
-        if (t < tmax) {
-          hit_prim = gpi;
-          hit_mesh = mesh;
-          hit_orig = orig;
-          tmax = t;
-        }
-      }
-      if (bad) break;
-      if ((cur.y & 0xff000000u) == 0) {
-        if (sp == 0) break;
-        if (sp == tlas_sp) {
-          tlas_sp = OBVHS_INVALID;
-          mesh = OBVHS_INVALID;
-          nodes = tlas;
-          n_nodes = n_tlas;
-        }
-        sp = sp ? sp - 1 : 0;
-        cur = stack[sp];
-      }
-    }
-    if (bad) hit_prim = OBVHS_INVALID;
-    hits[ri] = hit_prim == OBVHS_INVALID
-                   ? make_uint4(OBVHS_INVALID, OBVHS_INVALID, OBVHS_INVALID, 0x7f800000u)
-                   : make_uint4(hit_mesh, hit_prim, hit_orig, __float_as_uint(tmax));
-  }
+  uint2 stack[32];
+  TlasRay ray;
+  ray.tlas = tlas;
+  ray.n_tlas = n_tlas;
+  ray.tlas_pidx = tlas_pidx;
+  ray.n_tlas_prims = n_tlas_prims;
+  ray.blas = blas;
+  ray.n_blas = n_blas;
+  ray.rays = rays;
+  ray.hits = hits;
+  ray.status = status;
+  ray.stack = stack;
+  persistent_rays(ray, nrays, next_ray);
 }
 
 // The 64-byte record of BVH-order triangle k: tris[pidx[k]].
