@@ -41,6 +41,13 @@ __device__ __forceinline__ float safe_inverse(float x) {
 
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int b) { return (w >> (8 * b)) & 0xffu; }
 
+// Byte b of w as a float, exactly: the bits 0x4B0000bb are the float
+// 2^23 + bb, and subtracting 2^23 is exact.  One byte permute and one add on
+// the full-rate pipes instead of an integer-to-float conversion.
+__device__ __forceinline__ float byte_f(uint32_t w, int b) {
+  return __uint_as_float(__byte_perm(w, 0x4Bu, 0x4550u | (uint32_t)b)) - 8388608.0f;
+}
+
 struct NodeQ {
   uint4 q0, q1, q2, q3, q4;
 };
@@ -75,16 +82,22 @@ __device__ __forceinline__ uint32_t intersect_node(const NodeQ& n, float3 o, flo
   const unsigned long long inner_mask8 = (is_inner8 >> 4) * 0xffull;
   const unsigned long long bit_index8 = (meta8 ^ (oct8 & inner_mask8)) & 0x1f1f1f1f1f1f1f1full;
   const unsigned long long child_bits8 = (meta8 >> 5) & 0x0707070707070707ull;
+  // The entry and exit planes of each axis, as whole words of four
+  // children's quantised bytes: the lo/hi choice by the ray's direction sign
+  // is made once per word instead of once per child.
+  const uint32_t xn0 = rdx ? n.q2.z : n.q2.x, xf0 = rdx ? n.q2.x : n.q2.z;
+  const uint32_t xn1 = rdx ? n.q2.w : n.q2.y, xf1 = rdx ? n.q2.y : n.q2.w;
+  const uint32_t yn0 = rdy ? n.q3.z : n.q3.x, yf0 = rdy ? n.q3.x : n.q3.z;
+  const uint32_t yn1 = rdy ? n.q3.w : n.q3.y, yf1 = rdy ? n.q3.y : n.q3.w;
+  const uint32_t zn0 = rdz ? n.q4.z : n.q4.x, zf0 = rdz ? n.q4.x : n.q4.z;
+  const uint32_t zn1 = rdz ? n.q4.w : n.q4.y, zf1 = rdz ? n.q4.y : n.q4.w;
   uint32_t hit = 0;
 #pragma unroll
   for (int c = 0; c < 8; c++) {
     const int w = c >> 2, b = c & 3;
-    const float xlo = (float)byte_of(w ? n.q2.y : n.q2.x, b), xhi = (float)byte_of(w ? n.q2.w : n.q2.z, b);
-    const float ylo = (float)byte_of(w ? n.q3.y : n.q3.x, b), yhi = (float)byte_of(w ? n.q3.w : n.q3.z, b);
-    const float zlo = (float)byte_of(w ? n.q4.y : n.q4.x, b), zhi = (float)byte_of(w ? n.q4.w : n.q4.z, b);
-    const float xmin = rdx ? xhi : xlo, xmax = rdx ? xlo : xhi;
-    const float ymin = rdy ? yhi : ylo, ymax = rdy ? ylo : yhi;
-    const float zmin = rdz ? zhi : zlo, zmax = rdz ? zlo : zhi;
+    const float xmin = byte_f(w ? xn1 : xn0, b), xmax = byte_f(w ? xf1 : xf0, b);
+    const float ymin = byte_f(w ? yn1 : yn0, b), ymax = byte_f(w ? yf1 : yf0, b);
+    const float zmin = byte_f(w ? zn1 : zn0, b), zmax = byte_f(w ? zf1 : zf0, b);
     const float tminx = xmin * aix + aox, tmaxx = xmax * aix + aox;
     const float tminy = ymin * aiy + aoy, tmaxy = ymax * aiy + aoy;
     const float tminz = zmin * aiz + aoz, tmaxz = zmax * aiz + aoz;
