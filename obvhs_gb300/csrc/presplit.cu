@@ -64,32 +64,40 @@ __global__ void __launch_bounds__(BLK) k_tri_boxes(const float* __restrict__ tri
 // S += m + r, where a/u = m + f (f in [0,1)) and r = 0 if f < 1/2, 1 if
 // f > 1/2, and for f == 1/2 (a tie) r makes S+m+r even.  Only the parity of S
 // matters, so a block of elements maps to two increments (start parity even
-// or odd), computed in parallel for three candidate binades around the
-// double-precision prefix.  One thread then chains the blocks exactly,
-// summing a block element by element only when the running sum is not in a
-// candidate binade or would leave its binade inside the block.
+// or odd), computed in parallel (in exact f32 arithmetic) for three
+// candidate binades around an approximate prefix (f32 block sums, scanned).  One warp then chains the
+// blocks exactly, four blocks per lane per step, and sums a block element by
+// element only when the running sum is not in a candidate binade or would
+// leave its binade inside the block.
+//
+// Increments are kept in 32 bits, saturated at INC_SAT: any prefix that
+// contains a saturated increment ends at or above 2^25 > 2^24 and so is
+// recognised as leaving the binade, whatever its parity.
 constexpr int SUM_BLOCK = 256;
 constexpr int NCAND_E = 3;
+constexpr uint32_t INC_SAT = 1u << 25;
+constexpr int CHAIN_K = 4;  // blocks per lane in a chain step
 
-struct BlockT {
-  long long inc[NCAND_E][2];
-  int e0;  // candidate binades are e0-1, e0, e0+1
-  int valid[NCAND_E];
+struct __align__(16) BlockT {
+  int e0;                     // candidate binades are e0-1, e0, e0+1
+  uint32_t inc[NCAND_E][2];  // (even start, odd start); INC_SAT where the block leaves the binade
+  uint32_t pad;
 };
+static_assert(sizeof(BlockT) == 32, "two 16-byte loads per block");
 
-__global__ void __launch_bounds__(BLK) k_block_dsum(const float* __restrict__ ha, uint32_t n, double* __restrict__ bsum) {
+__global__ void __launch_bounds__(BLK) k_block_sum(const float* __restrict__ ha, uint32_t n, float* __restrict__ bsum) {
   grid_dep_wait();
-  __shared__ double sw[BLK / 32];
+  __shared__ float sw[BLK / 32];
   const uint32_t base = blockIdx.x * SUM_BLOCK;
-  double acc = 0.0;
+  float acc = 0.0f;
   for (uint32_t j = threadIdx.x; j < SUM_BLOCK; j += BLK)
-    if (base + j < n) acc += (double)ha[base + j];
+    if (base + j < n) acc += ha[base + j];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t = 0.0;
+    float t = 0.0f;
     for (int w = 0; w < BLK / 32; w++) t += sw[w];
     bsum[blockIdx.x] = t;
   }
@@ -97,68 +105,80 @@ __global__ void __launch_bounds__(BLK) k_block_dsum(const float* __restrict__ ha
 
 // Exclusive prefix of the block sums in place (one block, chunks of 1024
 // with a carry): each block's approximate running sum at its start.
-__global__ void __launch_bounds__(1024) k_scan_dsum(double* bsum, uint32_t nb) {
+__global__ void __launch_bounds__(1024) k_scan_bsum(float* bsum, uint32_t nb) {
   grid_dep_wait();
-  __shared__ double sw[32];
-  __shared__ double carry;
-  if (threadIdx.x == 0) carry = 0.0;
+  __shared__ float sw[32];
+  __shared__ float carry;
+  if (threadIdx.x == 0) carry = 0.0f;
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (uint32_t c0 = 0; c0 < nb; c0 += 1024) {
+    const float cbase = carry;
     const uint32_t i = c0 + threadIdx.x;
-    const double v = i < nb ? bsum[i] : 0.0;
-    double x = v;
+    const float v = i < nb ? bsum[i] : 0.0f;
+    float x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const double y = __shfl_up_sync(0xffffffffu, x, o);
+      const float y = __shfl_up_sync(0xffffffffu, x, o);
       if (lane >= o) x += y;
     }
     if (lane == 31) sw[warp] = x;
     __syncthreads();
-    double pre = carry;
-    for (int w = 0; w < warp; w++) pre += sw[w];
-    if (i < nb) bsum[i] = pre + x - v;
+    if (warp == 0) {
+      float y = sw[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const float z = __shfl_up_sync(0xffffffffu, y, o);
+        if (lane >= o) y += z;
+      }
+      sw[lane] = y;  // inclusive over warps
+    }
     __syncthreads();
-    if (threadIdx.x == 1023) carry = pre + x;
+    if (i < nb) bsum[i] = cbase + (warp ? sw[warp - 1] : 0.0f) + x - v;
+    __syncthreads();
+    if (threadIdx.x == 0) carry = cbase + sw[31];
     __syncthreads();
   }
 }
 
-// A block's effect inside one binade: increments (even start, odd start)
-// and whether every element stays below the binade's width.
+// A run's effect inside one binade: increments for an even / odd start.
 struct Mono {
-  long long g0, g1;
-  int ok;
+  uint32_t g0, g1;
 };
 // `a` then `b`: the parity after `a` selects b's increment.
 __device__ __forceinline__ Mono mono_then(const Mono& a, const Mono& b) {
   Mono r;
-  r.g0 = a.g0 + ((a.g0 & 1) ? b.g1 : b.g0);
-  r.g1 = a.g1 + (((1 + a.g1) & 1) ? b.g1 : b.g0);
-  r.ok = a.ok & b.ok;
+  r.g0 = min(a.g0 + ((a.g0 & 1) ? b.g1 : b.g0), INC_SAT);
+  r.g1 = min(a.g1 + (((1 + a.g1) & 1) ? b.g1 : b.g0), INC_SAT);
   return r;
 }
-__device__ __forceinline__ Mono mono_elem(float v, double scale) {
-  const double x = (double)v * scale;
-  if (!(x < 16777216.0)) return Mono{0, 0, 0};  // leaves the binade alone (or NaN)
-  const double fl = floor(x);
-  const double f = x - fl;
-  const long long m = (long long)fl;
-  if (f < 0.5) return Mono{m, m, 1};
-  if (f > 0.5) return Mono{m + 1, m + 1, 1};
+// 1/u = 2^(23-e) for the binade [2^e, 2^(e+1)) as two f32 factors (2^k is
+// not an f32 for k > 127): v * lo * hi is then exact unless it overflows (then
+// v/u >= 2^24, outside the binade either way) or underflows below 2^-126
+// (then the fraction of v/u is below 1/2 either way).
+struct Scale {
+  float lo, hi;
+};
+__device__ __forceinline__ Scale binade_scale(int e) {
+  const int k = 23 - e;  // -104 .. 149
+  const int k1 = k > 127 ? 127 : k;
+  return Scale{__int_as_float((127 + k1) << 23), __int_as_float((127 + (k - k1)) << 23)};
+}
+// One element in the binade with 1/u = sc.
+__device__ __forceinline__ Mono mono_elem(float v, Scale sc) {
+  const float x = (v * sc.lo) * sc.hi;
+  if (!(x < 16777216.0f)) return Mono{INC_SAT, INC_SAT};  // leaves the binade alone (or NaN)
+  const float fl = floorf(x);
+  const float f = x - fl;  // exact: both below 2^24
+  const uint32_t m = (uint32_t)fl;
+  if (f < 0.5f) return Mono{m, m};
+  if (f > 0.5f) return Mono{m + 1, m + 1};
   // a tie rounds to the even significand: S + m + r even
-  return Mono{m + (m & 1), m + ((1 + m) & 1), 1};
-}
-__device__ __forceinline__ Mono shfl_down_mono(const Mono& v, int o) {
-  Mono r;
-  r.g0 = __shfl_down_sync(0xffffffffu, v.g0, o);
-  r.g1 = __shfl_down_sync(0xffffffffu, v.g1, o);
-  r.ok = __shfl_down_sync(0xffffffffu, v.ok, o);
-  return r;
+  return Mono{m + (m & 1), m + ((1 + m) & 1)};
 }
 
 __global__ void __launch_bounds__(BLK) k_block_transform(const float* __restrict__ ha, uint32_t n,
-                                                         const double* __restrict__ bstart, BlockT* __restrict__ out) {
+                                                         const float* __restrict__ bstart, BlockT* __restrict__ out) {
   grid_dep_wait();
   constexpr int PER = SUM_BLOCK / BLK;  // consecutive elements per thread
   __shared__ Mono sm[BLK / 32];
@@ -172,19 +192,21 @@ __global__ void __launch_bounds__(BLK) k_block_transform(const float* __restrict
     v[k] = i < n ? ha[i] : 0.0f;
   }
   // approximate running sum at the block start (the scanned block sums)
-  const double start = bstart[b];
-  const int e0 = start > 0.0 ? ilogb(start) : -200;
+  const float start = bstart[b];
+  const int e0 = start > 0.0f ? ilogbf(start) : -200;
   for (int ci = 0; ci < NCAND_E; ci++) {
     const int e = e0 - 1 + ci;
     const bool in_range = e >= -126 && e <= 127;
-    const double scale = in_range ? ldexp(1.0, 23 - e) : 0.0;  // 1 / u
+    const Scale scale = binade_scale(in_range ? e : 0);
     Mono t = mono_elem(v[0], scale);
 #pragma unroll
     for (int k = 1; k < PER; k++) t = mono_then(t, mono_elem(v[k], scale));
     // ordered reduction: lane order within the warp, then warp order
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const Mono u = shfl_down_mono(t, o);
+      Mono u;
+      u.g0 = __shfl_down_sync(0xffffffffu, t.g0, o);
+      u.g1 = __shfl_down_sync(0xffffffffu, t.g1, o);
       if ((lane & (2 * o - 1)) == 0) t = mono_then(t, u);
     }
     if (lane == 0) sm[warp] = t;
@@ -192,63 +214,63 @@ __global__ void __launch_bounds__(BLK) k_block_transform(const float* __restrict
     if (threadIdx.x == 0) {
       Mono r = sm[0];
       for (int w = 1; w < BLK / 32; w++) r = mono_then(r, sm[w]);
-      out[b].inc[ci][0] = r.g0;
-      out[b].inc[ci][1] = r.g1;
-      out[b].valid[ci] = (r.ok && in_range) ? 1 : 0;
-      if (ci == 0) out[b].e0 = e0;
+      out[b].inc[ci][0] = in_range ? r.g0 : INC_SAT;
+      out[b].inc[ci][1] = in_range ? r.g1 : INC_SAT;
+      if (ci == 0) {
+        out[b].e0 = e0;
+        out[b].pad = 0;
+      }
     }
     __syncthreads();
   }
 }
 
-// Inclusive warp scan of monoid values in lane order.
-__device__ __forceinline__ Mono mono_warp_scan(Mono v, int lane) {
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    Mono u;
-    u.g0 = __shfl_up_sync(0xffffffffu, v.g0, o);
-    u.g1 = __shfl_up_sync(0xffffffffu, v.g1, o);
-    u.ok = __shfl_up_sync(0xffffffffu, v.ok, o);
-    if (lane >= o) v = mono_then(u, v);
-  }
-  return v;
-}
-
-// Advances the exact running sum s over 32 consecutive items whose effects
-// inside s's binade are `mine` (one per lane): returns how many items were
-// applied (the items before the first one that leaves the binade or has no
-// valid effect) and updates s.
-__device__ __forceinline__ int warp_advance(float& s, Mono mine, int lane, int avail) {
+// Advances the exact running sum s over 32 consecutive runs whose effects
+// inside s's binade are `mine` (one per lane, in order): returns how many
+// runs were applied (those before the first one after which s would leave
+// the binade) and updates s.
+__device__ __forceinline__ int warp_advance(float& s, Mono mine, int lane) {
   const uint32_t bits = __float_as_uint(s);
   const int ex = (int)((bits >> 23) & 0xff);
   if (ex == 0 || ex == 0xff) return 0;  // zero, denormal or not finite
-  if (lane >= avail) mine = Mono{0, 0, 0};
-  const Mono pre = mono_warp_scan(mine, lane);
-  const long long S = (long long)((bits & 0x7fffffu) | 0x800000u);
-  const long long S2 = S + ((S & 1) ? pre.g1 : pre.g0);
-  const bool good = pre.ok && S2 < 16777216ll;
-  const uint32_t bad = __ballot_sync(0xffffffffu, !good);
-  const int f = bad ? __ffs(bad) - 1 : 32;  // items 0..f-1 apply
+  Mono pre = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    Mono u;
+    u.g0 = __shfl_up_sync(0xffffffffu, pre.g0, o);
+    u.g1 = __shfl_up_sync(0xffffffffu, pre.g1, o);
+    if (lane >= o) pre = mono_then(u, pre);
+  }
+  const uint32_t S = (bits & 0x7fffffu) | 0x800000u;
+  const uint32_t S2 = S + ((S & 1) ? pre.g1 : pre.g0);
+  const uint32_t bad = __ballot_sync(0xffffffffu, S2 >= 16777216u);
+  const int f = bad ? __ffs(bad) - 1 : 32;  // runs 0..f-1 apply
   if (f > 0) {
-    const long long Sf = __shfl_sync(0xffffffffu, S2, f - 1);
-    s = __uint_as_float(((uint32_t)ex << 23) | (uint32_t)(Sf - 8388608ll));
+    const uint32_t Sf = __shfl_sync(0xffffffffu, S2, f - 1);
+    s = __uint_as_float(((uint32_t)ex << 23) | (Sf - 8388608u));
   }
   return f;
 }
 
 // Element by element, 32 at a time: the prefix inside the current binade in
-// parallel, the element that leaves it with one exact addition.
-__device__ void warp_sum_range(float& s, const float* __restrict__ ha, uint32_t lo, uint32_t hi, int lane) {
+// parallel, the element that leaves it with one exact addition.  The range
+// (at most one block) is staged in shared memory first, so the dependent
+// steps read no global memory.
+__device__ void warp_sum_range(float& s, const float* __restrict__ ha, uint32_t lo, uint32_t hi, int lane,
+                               float* stage) {
+  for (uint32_t j = lo + lane; j < hi; j += 32) stage[j - lo] = ha[j];
+  __syncwarp();
   uint32_t j = lo;
   while (j < hi) {
     const int avail = (int)min(32u, hi - j);
-    const float v = lane < avail ? ha[j + lane] : 0.0f;
+    const float v = lane < avail ? stage[j - lo + lane] : 0.0f;
     const uint32_t bits = __float_as_uint(s);
     const int ex = (int)((bits >> 23) & 0xff);
     int f = 0;
     if (ex != 0 && ex != 0xff) {
-      const double scale = ldexp(1.0, 23 - (ex - 127));
-      f = warp_advance(s, mono_elem(v, scale), lane, avail);
+      const Mono mine = lane < avail ? mono_elem(v, binade_scale(ex - 127)) : Mono{INC_SAT, INC_SAT};
+      f = warp_advance(s, mine, lane);
+      if (f > avail) f = avail;
     }
     j += f;
     if (f < avail && j < hi) {
@@ -256,40 +278,96 @@ __device__ void warp_sum_range(float& s, const float* __restrict__ ha, uint32_t 
       j++;
     }
   }
+  __syncwarp();
 }
 
-// One warp chains the block transforms, 32 blocks per step; a block whose
-// transform does not apply is summed element-wise by warp_sum_range.  Then
-// the preset thresholds (src/splits.rs:23-33).
+// Block transforms of one lane's group of K consecutive blocks.
+template <int K>
+struct Window {
+  uint4 w[K][2];
+  __device__ __forceinline__ void load(const BlockT* __restrict__ tr, uint32_t b0, uint32_t nb) {
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+      if (b0 + j < nb) {
+        w[j][0] = __ldg(reinterpret_cast<const uint4*>(&tr[b0 + j]));
+        w[j][1] = __ldg(reinterpret_cast<const uint4*>(&tr[b0 + j]) + 1);
+      }
+    }
+  }
+  // the group's effect in binade `ex` (identity past nb; a block without a
+  // transform for `ex` saturates)
+  __device__ __forceinline__ Mono effect(uint32_t b0, uint32_t nb, int ex) const {
+    Mono m{0u, 0u};
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+      if (b0 + j < nb) {
+        const int ci = (ex - 127) - (int)w[j][0].x + 1;
+        Mono t{INC_SAT, INC_SAT};
+        if (ci == 0)
+          t = Mono{w[j][0].y, w[j][0].z};
+        else if (ci == 1)
+          t = Mono{w[j][0].w, w[j][1].x};
+        else if (ci == 2)
+          t = Mono{w[j][1].y, w[j][1].z};
+        m = mono_then(m, t);
+      }
+    }
+    return m;
+  }
+};
+
+// One warp chains the block transforms, CHAIN_K blocks per lane per step
+// (the next step's transforms are loaded while this one is scanned); a step
+// that stops inside a lane's group is retried one block per lane, and a
+// block whose transform does not apply is summed element-wise by
+// warp_sum_range.  Then the preset thresholds (src/splits.rs:23-33).
 __global__ void __launch_bounds__(32) k_sum_chain(const float* __restrict__ ha, uint32_t n, const BlockT* __restrict__ tr,
                                                   const int* largest_key, float* thr) {
   grid_dep_wait();
+  __shared__ float stage[SUM_BLOCK];
   const int lane = threadIdx.x;
   const uint32_t nb = (n + SUM_BLOCK - 1) / SUM_BLOCK;
+  constexpr uint32_t STEP = 32 * CHAIN_K;
   float s = 0.0f;
   uint32_t b = 0, sequential_blocks = 0;
   uint32_t guard = 0;
+  bool retry = false;     // the last step stopped inside a group: one block per lane
+  bool have_cur = false;  // cur holds the groups starting at b
+  Window<CHAIN_K> cur, nxt;
   while (b < nb && ++guard < 4 * nb + 64) {
     const uint32_t bits = __float_as_uint(s);
     const int ex = (int)((bits >> 23) & 0xff);
-    int f = 0;
     if (ex != 0 && ex != 0xff) {
-      const int avail = (int)min(32u, nb - b);
-      Mono mine{0, 0, 0};
-      if (lane < avail) {
-        const BlockT& t = tr[b + lane];
-        const int ci = (ex - 127) - t.e0 + 1;
-        if (ci >= 0 && ci < NCAND_E && t.valid[ci]) mine = Mono{t.inc[ci][0], t.inc[ci][1], 1};
+      if (!retry) {
+        const uint32_t g0 = b + (uint32_t)lane * CHAIN_K;
+        if (!have_cur) cur.load(tr, g0, nb);
+        nxt.load(tr, g0 + STEP, nb);  // used if this whole step applies
+        const int f = warp_advance(s, cur.effect(g0, nb, ex), lane);
+        if (f == 32) {
+          b = min(b + STEP, nb);
+          cur = nxt;
+          have_cur = true;
+          continue;
+        }
+        b = min(b + (uint32_t)f * CHAIN_K, nb);
+        have_cur = false;
+        retry = b < nb;
+        continue;
       }
-      f = warp_advance(s, mine, lane, avail);
+      Window<1> one;
+      one.load(tr, b + lane, nb);
+      const int f = warp_advance(s, one.effect(b + lane, nb, ex), lane);
+      b = min(b + (uint32_t)f, nb);
+      retry = false;
+      if (f == 32 || b >= nb) continue;
     }
-    b += f;
-    if (b < nb && f < 32) {
-      const uint32_t lo = b * SUM_BLOCK;
-      warp_sum_range(s, ha, lo, min(lo + SUM_BLOCK, n), lane);
-      b++;
-      sequential_blocks++;
-    }
+    // block b does not apply in s's binade (or s is zero): element by element
+    const uint32_t lo = b * SUM_BLOCK;
+    warp_sum_range(s, ha, lo, min(lo + SUM_BLOCK, n), lane, stage);
+    b++;
+    sequential_blocks++;
+    retry = false;
+    have_cur = false;
   }
   if (lane == 0) {
     const float avg = s / (float)n;
@@ -602,11 +680,11 @@ int presplit_device(BuildCtx& c, const float* tris, uint32_t n, float** aabbs_ou
                                         largest_key, c.d_status));
   {
     const uint32_t nb = div_up<uint32_t>(n, SUM_BLOCK);
-    double* bsum = (double*)s.get(SLOT_OUTPUT, (size_t)nb * 8 + 16);
+    float* bsum = (float*)s.get(SLOT_OUTPUT, (size_t)nb * 4 + 16);
     BlockT* tr = (BlockT*)s.get(SLOT_TILE_HIST, (size_t)nb * sizeof(BlockT) + 16);
     if (!bsum || !tr) return c.fail(OBVHS_ERR_OOM, "scratch");
-    KLAUNCH("k_block_dsum", launch_k(k_block_dsum, nb, BLK, 0, c.stream, ha, n, bsum));
-    KLAUNCH("k_scan_dsum", launch_k(k_scan_dsum, 1, 1024, 0, c.stream, bsum, nb));
+    KLAUNCH("k_block_sum", launch_k(k_block_sum, nb, BLK, 0, c.stream, ha, n, bsum));
+    KLAUNCH("k_scan_bsum", launch_k(k_scan_bsum, 1, 1024, 0, c.stream, bsum, nb));
     KLAUNCH("k_block_transform", launch_k(k_block_transform, nb, BLK, 0, c.stream, ha, n, bsum, tr));
     KLAUNCH("k_sum_chain", launch_k(k_sum_chain, 1, 32, 0, c.stream, ha, n, tr, largest_key, thr));
   }

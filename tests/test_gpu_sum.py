@@ -39,6 +39,13 @@ CASES = {
     "saturating_ties": lambda r: np.concatenate([[2.0 ** 24], np.full(5000, 1.0), np.full(5000, 1.5),
                                                   np.full(5000, 3.0)]),
     "tiny_then_big": lambda r: np.concatenate([np.full(3000, 1e-30), r.uniform(0, 10, 100_000)]),
+    "zeros_then_uniform": lambda r: np.concatenate([np.zeros(5000), r.uniform(0, 1, 60_000)]),
+    "one": lambda r: np.array([0.375]),
+    "ragged_tail": lambda r: r.uniform(0, 1, 256 * 129 + 77),
+    "big_blocks": lambda r: r.uniform(1e5, 1e6, 200_000),
+    "growing": lambda r: np.geomspace(1e-6, 1e4, 150_000),
+    "near_min_normal": lambda r: r.uniform(1e-38, 1e-36, 100_000),
+    "subnormal_start": lambda r: np.concatenate([np.full(700, 1e-40), r.uniform(1e-38, 1e-37, 40_000)]),
 }
 
 
