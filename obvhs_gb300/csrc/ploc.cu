@@ -805,9 +805,26 @@ __global__ void k_ploc_seg_init(const Bvh2Node* __restrict__ cur, const uint32_t
 
 constexpr int TAIL_THREADS = 1024;
 
-__device__ __forceinline__ Box sbox(const float4* s, uint32_t j) {
-  float4 a = s[2 * j], b = s[2 * j + 1];
-  return Box{make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)};
+// The tail keeps its clusters as structures of arrays: eight word arrays of
+// TAIL_MAX (min x, y, z, prim count, max x, y, z, first index), so lanes that
+// read consecutive clusters read consecutive words (no bank conflicts).
+__device__ __forceinline__ Box sbox(const float* s, uint32_t j) {
+  return Box{make_float3(s[j], s[TAIL_MAX + j], s[2 * TAIL_MAX + j]),
+             make_float3(s[4 * TAIL_MAX + j], s[5 * TAIL_MAX + j], s[6 * TAIL_MAX + j])};
+}
+__device__ __forceinline__ void snode_get(const float* s, uint32_t j, float4& a, float4& b) {
+  a = make_float4(s[j], s[TAIL_MAX + j], s[2 * TAIL_MAX + j], s[3 * TAIL_MAX + j]);
+  b = make_float4(s[4 * TAIL_MAX + j], s[5 * TAIL_MAX + j], s[6 * TAIL_MAX + j], s[7 * TAIL_MAX + j]);
+}
+__device__ __forceinline__ void snode_put(float* s, uint32_t j, const float4& a, const float4& b) {
+  s[j] = a.x;
+  s[TAIL_MAX + j] = a.y;
+  s[2 * TAIL_MAX + j] = a.z;
+  s[3 * TAIL_MAX + j] = a.w;
+  s[4 * TAIL_MAX + j] = b.x;
+  s[5 * TAIL_MAX + j] = b.y;
+  s[6 * TAIL_MAX + j] = b.z;
+  s[7 * TAIL_MAX + j] = b.w;
 }
 
 // Finishes every remaining pass (count <= TAIL_MAX) inside one CTA.
@@ -819,9 +836,9 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
                                                             const uint32_t* __restrict__ remap) {
   grid_dep_wait();
   extern __shared__ float4 smem[];
-  float4* sa = smem;                      // TAIL_MAX nodes (2 float4 each)
-  float4* sb = smem + 2 * TAIL_MAX;       // TAIL_MAX nodes
-  int8_t* sm = reinterpret_cast<int8_t*>(smem + 4 * TAIL_MAX);
+  float* sa = reinterpret_cast<float*>(smem);  // TAIL_MAX clusters (8 word arrays)
+  float* sb = sa + 8 * TAIL_MAX;               // TAIL_MAX clusters
+  int8_t* sm = reinterpret_cast<int8_t*>(sb + 8 * TAIL_MAX);
   __shared__ uint32_t s_we[32], s_wm[32];
   __shared__ uint32_t s_count, s_insert, s_pass;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -836,12 +853,11 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
   uint32_t count = s_count;
   for (uint32_t j = tid; j < count; j += TAIL_THREADS) {
     const float4* q = reinterpret_cast<const float4*>(&cur_g[j]);
-    sa[2 * j] = q[0];
-    sa[2 * j + 1] = q[1];
+    snode_put(sa, j, q[0], q[1]);
   }
   __syncthreads();
-  float4* cur = sa;
-  float4* nxt = sb;
+  float* cur = sa;
+  float* nxt = sb;
   uint32_t insert = s_insert;
   uint32_t pass = s_pass;
   uint64_t sum = 0;
@@ -939,8 +955,9 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
       uint32_t i = tid * IT + k;
       if (!emit[k]) continue;
       if (ism[k]) {
-        float4 la = cur[2 * i], lb = cur[2 * i + 1];
-        float4 ra = cur[2 * bst[k]], rb = cur[2 * bst[k] + 1];
+        float4 la, lb, ra, rb;
+        snode_get(cur, i, la, lb);
+        snode_get(cur, bst[k], ra, rb);
         uint32_t ins = insert - 2 * (mpos + 1);
         if (remap) ins = remap[(ins - 1) >> 1];
         float4* o = reinterpret_cast<float4*>(&out[ins]);
@@ -950,12 +967,13 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
         o[3] = rb;
         Box u = box_union(Box{make_float3(la.x, la.y, la.z), make_float3(lb.x, lb.y, lb.z)},
                           Box{make_float3(ra.x, ra.y, ra.z), make_float3(rb.x, rb.y, rb.z)});
-        nxt[2 * epos] = make_float4(u.mn.x, u.mn.y, u.mn.z, __uint_as_float(0u));
-        nxt[2 * epos + 1] = make_float4(u.mx.x, u.mx.y, u.mx.z, __uint_as_float(ins));
+        snode_put(nxt, epos, make_float4(u.mn.x, u.mn.y, u.mn.z, __uint_as_float(0u)),
+                  make_float4(u.mx.x, u.mx.y, u.mx.z, __uint_as_float(ins)));
         mpos++;
       } else {
-        nxt[2 * epos] = cur[2 * i];
-        nxt[2 * epos + 1] = cur[2 * i + 1];
+        float4 a, b;
+        snode_get(cur, i, a, b);
+        snode_put(nxt, epos, a, b);
       }
       epos++;
     }
@@ -963,15 +981,14 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
     count = te;
     insert -= 2 * tm;
     pass++;
-    float4* t = cur;
+    float* t = cur;
     cur = nxt;
     nxt = t;
     __syncthreads();
   }
   if (tid == 0) {
     float4* o = reinterpret_cast<float4*>(&out[0]);
-    o[0] = cur[0];
-    o[1] = cur[1];
+    snode_get(cur, 0, o[0], o[1]);
     st->count[parity] = count;
     st->insert[parity] = insert;
     st->passes = pass;
