@@ -65,6 +65,36 @@ __device__ __forceinline__ NodeQ load_cw(const CwNode* nodes, uint32_t i) {
 
 // CwBvhNode::intersect_ray -> 32-bit hit mask (hi 8 bits: inner children by
 // traversal priority; lo 24 bits: primitive bits).
+// The slab test's min / max.  The reference's SSE lane min/max is smin/smax
+// (select semantics: the second operand when either is NaN).  With FAST the
+// hardware min/max is used instead: for operands that are not NaN both give
+// the same value up to the sign of a zero, which the comparison tmn <= tmx
+// does not see.  FAST is taken only when ray_fast_ok and node_fast_ok bound
+// the inputs so that no intermediate can be NaN: |origin|, |p| <= 2^80,
+// finite directions (|1/d| <= 2^23 by safe_inverse), exponent bytes <= 200,
+// tmax not NaN; every t is then finite (below 2^106 in magnitude).
+template <bool FAST>
+__device__ __forceinline__ float slab_min(float a, float b) {
+  return FAST ? fminf(a, b) : smin(a, b);
+}
+template <bool FAST>
+__device__ __forceinline__ float slab_max(float a, float b) {
+  return FAST ? fmaxf(a, b) : smax(a, b);
+}
+__device__ __forceinline__ bool ray_fast_ok(float3 o, float3 d, float tmax) {
+  const uint32_t lim = 0x67800000u;  // 2^80
+  const uint32_t mo = max(max(__float_as_uint(o.x) & 0x7fffffffu, __float_as_uint(o.y) & 0x7fffffffu),
+                          __float_as_uint(o.z) & 0x7fffffffu);
+  const uint32_t md = max(max(__float_as_uint(d.x) & 0x7fffffffu, __float_as_uint(d.y) & 0x7fffffffu),
+                          __float_as_uint(d.z) & 0x7fffffffu);
+  return mo <= lim && md < 0x7f800000u && tmax == tmax;
+}
+__device__ __forceinline__ bool node_fast_ok(const NodeQ& n) {
+  const uint32_t mp = max(max(n.q0.x & 0x7fffffffu, n.q0.y & 0x7fffffffu), n.q0.z & 0x7fffffffu);
+  return mp <= 0x67800000u && __vcmpgtu4(n.q0.w & 0x00ffffffu, 0x00c8c8c8u) == 0u;
+}
+
+template <bool FAST>
 __device__ __forceinline__ uint32_t intersect_node(const NodeQ& n, float3 o, float3 d, float3 inv, float tmax,
                                                    uint32_t oct_inv4) {
   const float px = __uint_as_float(n.q0.x), py = __uint_as_float(n.q0.y), pz = __uint_as_float(n.q0.z);
@@ -101,10 +131,10 @@ __device__ __forceinline__ uint32_t intersect_node(const NodeQ& n, float3 o, flo
     const float tminx = xmin * aix + aox, tmaxx = xmax * aix + aox;
     const float tminy = ymin * aiy + aoy, tmaxy = ymax * aiy + aoy;
     const float tminz = zmin * aiz + aoz, tmaxz = zmax * aiz + aoz;
-    float tmn = smax(tminx, smax(tminy, tminz));
-    float tmx = smin(tmaxx, smin(tmaxy, tmaxz));
-    tmn = smax(tmn, 0.0001f);
-    tmx = smin(tmx, tmax);
+    float tmn = slab_max<FAST>(tminx, slab_max<FAST>(tminy, tminz));
+    float tmx = slab_min<FAST>(tmaxx, slab_min<FAST>(tmaxy, tmaxz));
+    tmn = slab_max<FAST>(tmn, 0.0001f);
+    tmx = slab_min<FAST>(tmx, tmax);
     if (tmn <= tmx) {
       const uint32_t cb = (uint32_t)(child_bits8 >> (c * 8)) & 0xffu;
       const uint32_t bi = (uint32_t)(bit_index8 >> (c * 8)) & 0xffu;
@@ -254,6 +284,7 @@ struct CwRay {
   uint32_t n_nodes, n_prims, ri, oct, hit_id, sp, guard;
   float3 o, d, inv;
   float tmin, ray_tmax, tmax, hit_t;
+  bool fast;  // ray_fast_ok
   uint2 cur, prim;
   uint2* stack;  // 32 entries, the thread's own (kept apart so the scalars stay in registers)
 
@@ -287,6 +318,7 @@ struct CwRay {
     inv = make_float3(safe_inverse(d.x), safe_inverse(d.y), safe_inverse(d.z));
     oct = (d.x < 0.0f ? 0u : 0x04040404u) | (d.y < 0.0f ? 0u : 0x02020202u) | (d.z < 0.0f ? 0u : 0x01010101u);
     tmax = ray_tmax;
+    fast = ray_fast_ok(o, d, ray_tmax);
     hit_id = OBVHS_INVALID;
     hit_t = __int_as_float(0x7f800000);
     sp = 0;
@@ -354,7 +386,9 @@ struct CwRay {
         return finish();
       }
       const NodeQ node = load_cw(nodes, ni);
-      const uint32_t hm = intersect_node(node, o, d, inv, MODE == 0 ? tmax : ray_tmax, oct);
+      const float tm = MODE == 0 ? tmax : ray_tmax;
+      const uint32_t hm = fast && node_fast_ok(node) ? intersect_node<true>(node, o, d, inv, tm, oct)
+                                                     : intersect_node<false>(node, o, d, inv, tm, oct);
       cur.x = node.q1.x;
       prim.x = node.q1.y;
       cur.y = (hm & 0xff000000u) | byte_of(node.q0.w, 3);
@@ -808,6 +842,7 @@ struct TlasRay {
   uint32_t hit_prim, hit_mesh, hit_orig;
   float3 o, d, inv;
   float tmin, tmax;
+  bool fast;  // ray_fast_ok
   uint2 cur;
 
   __device__ __forceinline__ bool finish(bool bad) {
@@ -826,6 +861,7 @@ struct TlasRay {
     tmax = r1.w;
     inv = make_float3(safe_inverse(d.x), safe_inverse(d.y), safe_inverse(d.z));
     oct = (d.x < 0.0f ? 0u : 0x04040404u) | (d.y < 0.0f ? 0u : 0x02020202u) | (d.z < 0.0f ? 0u : 0x01010101u);
+    fast = ray_fast_ok(o, d, tmax);
     sp = 0;
     tlas_sp = OBVHS_INVALID;
     mesh = OBVHS_INVALID;
@@ -863,7 +899,8 @@ struct TlasRay {
         return finish(true);
       }
       const NodeQ node = load_cw(nodes, ni);
-      const uint32_t hm = intersect_node(node, o, d, inv, tmax, oct);
+      const uint32_t hm = fast && node_fast_ok(node) ? intersect_node<true>(node, o, d, inv, tmax, oct)
+                                                     : intersect_node<false>(node, o, d, inv, tmax, oct);
       cur.x = node.q1.x;
       prim.x = node.q1.y;
       cur.y = (hm & 0xff000000u) | byte_of(node.q0.w, 3);

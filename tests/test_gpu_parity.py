@@ -250,6 +250,46 @@ def test_traversal_incoherent_and_occlusion(G):
     assert miss.any() and (~miss).any()
 
 
+def test_traversal_outside_the_fast_slab_bounds(G):
+    """Rays and nodes outside the bounds of the hardware min/max slab test
+    (infinite, NaN or huge origins and directions, NaN tmax; needle triangles
+    whose nodes have exponent bytes above 200 and |p| above 2^80) take the
+    reference's select min/max; one warp holds both kinds of rays."""
+    rng = np.random.default_rng(5)
+    tris, _ = S.scene1()
+    needles = np.zeros((6, 9), np.float32)
+    needles[:, 0] = -3e25
+    needles[:, 3] = 3e25
+    needles[:, 6] = rng.uniform(-1, 1, 6)
+    needles[:, [1, 4, 7]] = rng.uniform(-1, 1, (6, 1))
+    needles[:, [2, 5, 8]] = rng.uniform(-1, 1, (6, 1))
+    tris = np.concatenate([tris, needles]).astype(np.float32)
+    n = 24_000
+    o = rng.uniform(-1.2, 1.2, size=(n, 3)).astype(np.float32)
+    d = T.uniform_sample_sphere(rng.random(n).astype(np.float32), rng.random(n).astype(np.float32))
+    tmax = np.where(np.arange(n) % 2 == 0, np.inf, rng.uniform(0.5, 3, n)).astype(np.float32)
+    k = np.arange(0, n, 5)
+    kind = (k // 5) % 7
+    o[k[kind == 0], 0] = np.inf
+    d[k[kind == 1], 0] = 0.0
+    d[k[kind == 1], 1] = 0.0
+    o[k[kind == 2]] = np.float32(2e24)
+    d[k[kind == 3], 2] = np.nan
+    tmax[k[kind == 4]] = np.nan
+    d[k[kind == 5], 1] = -np.inf
+    o[k[kind == 6], 1] = np.nan
+    rays = T.make_rays(o, d, 0.0, tmax)
+    cw = G.build_cwbvh_from_tris(tris, BvhBuildParams.medium_build())
+    gn, gp = cw.download()
+    ids, t = cw.ray_traverse(rays)
+    oids, ot, _ = O.traverse(gn, gp, tris, rays, 0, nthreads=4)
+    assert (oids != 0xFFFFFFFF).sum() > 1000
+    assert _eq(ids, oids) and _eq(t.view(np.uint32), ot.view(np.uint32))
+    miss = cw.ray_traverse_miss(rays)
+    omiss, _, _ = O.traverse(gn, gp, tris, rays, 1, nthreads=4)
+    assert _eq(miss, omiss == 0xFFFFFFFF)
+
+
 def test_device_pointer_path(G):
     torch = pytest.importorskip("torch")
     tris, rays = S.scene1()
