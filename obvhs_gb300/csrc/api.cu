@@ -161,7 +161,7 @@ int build_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t 
   uint32_t passes = 0;
   uint64_t sum_counts = 0;
   r = ploc_build_device(c, leaves, m, total, p->ploc_search_distance, (int)p->sort_precision,
-                        p->search_depth_threshold, b2.nodes, &passes, &sum_counts, &rb->ploc);
+                        p->search_depth_threshold, b2.nodes, &passes, &sum_counts, &rb->ploc, nullptr, true);
   if (r) return r;
   stages.mark(c.stream);
   if (m) CK(cudaMemcpyAsync(&rb->root_prims, reinterpret_cast<const char*>(b2.nodes) + 12, 4, cudaMemcpyDeviceToHost,
@@ -644,7 +644,7 @@ int obvhs_ploc_build(obvhs_ctx* cp, const float* aabbs, const uint32_t* indices,
   uint64_t sum = 0;
   if (!r)
     r = ploc_build_device(c, leaves, n, total, search_distance, (int)sort_precision, search_depth_threshold, b->nodes,
-                          &passes, &sum);
+                          &passes, &sum, nullptr, nullptr, true);
   double ms = timer.stop_ms();
   if (!r) r = take_status(c);
   if (r) {
@@ -1158,7 +1158,7 @@ static int bvh2_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uin
   uint32_t passes = 0;
   uint64_t sum_counts = 0;
   r = ploc_build_device(c, leaves, m, total, p->ploc_search_distance, (int)p->sort_precision, p->search_depth_threshold,
-                        b->nodes, &passes, &sum_counts);
+                        b->nodes, &passes, &sum_counts, nullptr, nullptr, true);
   if (!r) r = take_status(c);  // NaN boxes leave tree slots unwritten
   if (r) return fail(r);
   b->max_depth = std::max<uint32_t>(96, passes + 1);

@@ -278,7 +278,8 @@ int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_
 // asynchronously and passes_out / sum_counts_out are left unset.
 int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* total_keys, uint32_t radius,
                       int precision, uint32_t depth_threshold, Bvh2Node* out_nodes, uint32_t* passes_out,
-                      uint64_t* sum_counts_out, PlocState* deferred = nullptr, const uint32_t* remap = nullptr);
+                      uint64_t* sum_counts_out, PlocState* deferred = nullptr, const uint32_t* remap = nullptr,
+                      bool nan_checked = false);
 int ploc_setup_kernels();
 
 // Segmented builds: many scenes through every stage together, one launch

@@ -322,7 +322,18 @@ __global__ void __launch_bounds__(BLK) k_gather(const Bvh2Node* __restrict__ in,
 
 // Pair cost as the reference computes it: the lower index's box first
 // (the SearchCache stores union(A_lo, A_hi), src/ploc/mod.rs:612-619).
-__device__ __forceinline__ float pair_cost(const Box& lo, const Box& hi) { return half_area(box_union(lo, hi)); }
+// The merge cost half_area(lo + hi).  The reference's union takes the SSE
+// lane min/max (select semantics, box_union).  The searches only compare
+// costs, so with FAST (boxes that hold no NaN: the build checked its inputs)
+// the hardware min/max is used: for operands that are not NaN it gives the
+// same values up to the sign of a zero, and the costs compare the same.
+template <bool FAST = false>
+__device__ __forceinline__ float pair_cost(const Box& lo, const Box& hi) {
+  if (FAST)
+    return half_area(Box{make_float3(fminf(lo.mn.x, hi.mn.x), fminf(lo.mn.y, hi.mn.y), fminf(lo.mn.z, hi.mn.z)),
+                         make_float3(fmaxf(lo.mx.x, hi.mx.x), fmaxf(lo.mx.y, hi.mx.y), fmaxf(lo.mx.z, hi.mx.z))});
+  return half_area(box_union(lo, hi));
+}
 
 __device__ __forceinline__ Box load_box_cg(const Bvh2Node* p) {
   const float4* q = reinterpret_cast<const float4*>(p);
@@ -367,6 +378,7 @@ struct PlocCoopArgs {
   uint32_t max_passes;
   uint32_t* status;
   const uint32_t* remap;  // partial rebuild: left slot of every merged pair (else null)
+  int fast;               // the leaves were checked for NaN: pair_cost<true>
 };
 
 struct CoopGroupSmem {
@@ -386,6 +398,7 @@ __device__ __forceinline__ void group_sync(int group) {
 // recomputed locally, so the emit/merge flags need no exchange), and the
 // tile's (emitted, merged) counts into *cnt.  Called by the PT threads of one
 // group.
+template <bool FAST>
 __device__ __forceinline__ void ploc_tile_offsets(CoopGroupSmem& sm, int group, const Bvh2Node* cur, uint32_t count,
                                                   uint32_t base, uint32_t chunk, int ipt, int r, bool d1,
                                                   int8_t* merge, uint2* cnt) {
@@ -424,8 +437,8 @@ __device__ __forceinline__ void ploc_tile_offsets(CoopGroupSmem& sm, int group, 
       if ((uint32_t)i == count - 1) {
         m = -1;
       } else {
-        const float c = pair_cost(me, PBOX(i + 1));
-        const float last = i == 0 ? __int_as_float(0x7f800000) : pair_cost(PBOX(i - 1), me);
+        const float c = pair_cost<FAST>(me, PBOX(i + 1));
+        const float last = i == 0 ? __int_as_float(0x7f800000) : pair_cost<FAST>(PBOX(i - 1), me);
         m = last < c ? -1 : 1;
       }
     } else {
@@ -434,14 +447,14 @@ __device__ __forceinline__ void ploc_tile_offsets(CoopGroupSmem& sm, int group, 
       int best = i;
       float best_cost = __int_as_float(0x7f800000);
       for (int j = begin; j < i; j++) {
-        const float c = pair_cost(PBOX(j), me);
+        const float c = pair_cost<FAST>(PBOX(j), me);
         if (c <= best_cost) {
           best = j;
           best_cost = c;
         }
       }
       for (int j = i + 1; j < end; j++) {
-        const float c = pair_cost(me, PBOX(j));
+        const float c = pair_cost<FAST>(me, PBOX(j));
         if (c <= best_cost) {
           best = j;
           best_cost = c;
@@ -594,7 +607,10 @@ __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs 
 
     // A: merge offsets and tile counts
     for (uint32_t tile = first_tile; tile < ntiles; tile += tile_step)
-      ploc_tile_offsets(sm, group, cur, count, tile * chunk, chunk, ipt, r, d1, a.merge, &a.tile_cnt[tile]);
+      if (a.fast)
+        ploc_tile_offsets<true>(sm, group, cur, count, tile * chunk, chunk, ipt, r, d1, a.merge, &a.tile_cnt[tile]);
+      else
+        ploc_tile_offsets<false>(sm, group, cur, count, tile * chunk, chunk, ipt, r, d1, a.merge, &a.tile_cnt[tile]);
     if (single) __syncthreads(); else grid.sync();
 
     // B: offsets and writes
@@ -744,8 +760,8 @@ __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_seg(PlocSegArgs a)
     for (uint32_t tile = first_tile; tile < ntiles; tile += tile_step) {
       const uint32_t s = smem_seg_find(tstart, S, tile);
       const uint32_t cb = __ldg(&a.prim_start[s]);
-      ploc_tile_offsets(sm, group, cur + cb, __ldcg(&cnt[s]), (tile - tstart[s]) * chunk, chunk, ipt, r, d1,
-                        a.merge + cb, &a.tile_cnt[tile]);
+      ploc_tile_offsets<true>(sm, group, cur + cb, __ldcg(&cnt[s]), (tile - tstart[s]) * chunk, chunk, ipt, r, d1,
+                              a.merge + cb, &a.tile_cnt[tile]);  // segmented inputs are always checked for NaN
     }
     grid.sync();
 
@@ -827,13 +843,52 @@ __device__ __forceinline__ void snode_put(float* s, uint32_t j, const float4& a,
   s[7 * TAIL_MAX + j] = b.w;
 }
 
+// The tail's neighbour search: sm[i] = offset of cluster i's best neighbour.
+template <bool FAST>
+__device__ __forceinline__ void tail_search(const float* cur, uint32_t count, bool d1, int r, int8_t* sm, int tid) {
+  for (uint32_t i = tid; i < count; i += TAIL_THREADS) {
+    Box me = sbox(cur, i);
+    int8_t m;
+    if (d1) {
+      if (i == count - 1) {
+        m = -1;
+      } else {
+        float c = pair_cost<FAST>(me, sbox(cur, i + 1));
+        float last = i == 0 ? __int_as_float(0x7f800000) : pair_cost<FAST>(sbox(cur, i - 1), me);
+        m = last < c ? -1 : 1;
+      }
+    } else {
+      uint32_t begin = i >= (uint32_t)r ? i - r : 0;
+      uint32_t end = min(i + r + 1, count);
+      uint32_t best = i;
+      float bc = __int_as_float(0x7f800000);
+      for (uint32_t j = begin; j < i; j++) {
+        float c = pair_cost<FAST>(sbox(cur, j), me);
+        if (c <= bc) {
+          best = j;
+          bc = c;
+        }
+      }
+      for (uint32_t j = i + 1; j < end; j++) {
+        float c = pair_cost<FAST>(me, sbox(cur, j));
+        if (c <= bc) {
+          best = j;
+          bc = c;
+        }
+      }
+      m = (int8_t)((int)best - (int)i);
+    }
+    sm[i] = m;
+  }
+}
+
 // Finishes every remaining pass (count <= TAIL_MAX) inside one CTA.
 // The live clusters are in buf[passes & 1].
 __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __restrict__ buf0,
                                                             const Bvh2Node* __restrict__ buf1, PlocState* st,
                                                             int radius, uint32_t depth_threshold, uint32_t max_passes,
                                                             Bvh2Node* __restrict__ out, uint32_t* status,
-                                                            const uint32_t* __restrict__ remap) {
+                                                            const uint32_t* __restrict__ remap, int fast) {
   grid_dep_wait();
   extern __shared__ float4 smem[];
   float* sa = reinterpret_cast<float*>(smem);  // TAIL_MAX clusters (8 word arrays)
@@ -870,40 +925,10 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
     const bool d1 = radius == 1 || pass < depth_threshold;
     const int r = d1 ? 1 : radius;
     // search
-    for (uint32_t i = tid; i < count; i += TAIL_THREADS) {
-      Box me = sbox(cur, i);
-      int8_t m;
-      if (d1) {
-        if (i == count - 1) {
-          m = -1;
-        } else {
-          float c = pair_cost(me, sbox(cur, i + 1));
-          float last = i == 0 ? __int_as_float(0x7f800000) : pair_cost(sbox(cur, i - 1), me);
-          m = last < c ? -1 : 1;
-        }
-      } else {
-        uint32_t begin = i >= (uint32_t)r ? i - r : 0;
-        uint32_t end = min(i + r + 1, count);
-        uint32_t best = i;
-        float bc = __int_as_float(0x7f800000);
-        for (uint32_t j = begin; j < i; j++) {
-          float c = pair_cost(sbox(cur, j), me);
-          if (c <= bc) {
-            best = j;
-            bc = c;
-          }
-        }
-        for (uint32_t j = i + 1; j < end; j++) {
-          float c = pair_cost(me, sbox(cur, j));
-          if (c <= bc) {
-            best = j;
-            bc = c;
-          }
-        }
-        m = (int8_t)((int)best - (int)i);
-      }
-      sm[i] = m;
-    }
+    if (fast)
+      tail_search<true>(cur, count, d1, r, sm, tid);
+    else
+      tail_search<false>(cur, count, d1, r, sm, tid);
     __syncthreads();
     // flags: thread tid owns items [tid*IT, tid*IT + IT)
     constexpr int IT = TAIL_MAX / TAIL_THREADS;
@@ -1050,7 +1075,7 @@ int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_
 
 int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* total_keys, uint32_t radius,
                       int precision, uint32_t depth_threshold, Bvh2Node* out_nodes, uint32_t* passes_out,
-                      uint64_t* sum_counts_out, PlocState* deferred, const uint32_t* remap) {
+                      uint64_t* sum_counts_out, PlocState* deferred, const uint32_t* remap, bool nan_checked) {
   *passes_out = 0;
   *sum_counts_out = 0;
   if (n == 0) return 0;
@@ -1089,7 +1114,7 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
       coop_blocks_s.store(coop_blocks);
     }
     PlocCoopArgs pa{{cur, nxt}, out_nodes, st, merge, tile_cnt, (int)radius, depth_threshold, max_passes, c.d_status,
-                    remap};
+                    remap, nan_checked ? 1 : 0};
     void* args[] = {&pa};
     if (gpu_shared(c) && n <= SHARED_SINGLE_BLOCK_MAX) {
       // the GPU is shared with other builds or work: one block, a normal
@@ -1103,7 +1128,8 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   {
     const size_t smem = (size_t)4 * TAIL_MAX * sizeof(float4) + TAIL_MAX + 64;
     KLAUNCH("k_ploc_tail", launch_k(k_ploc_tail, 1, TAIL_THREADS, smem, c.stream, cur, nxt, st, (int)radius, depth_threshold,
-                                                                           max_passes, out_nodes, c.d_status, remap));
+                                                                           max_passes, out_nodes, c.d_status, remap,
+                                    nan_checked ? 1 : 0));
     CK(cudaGetLastError());
   }
   if (deferred) {
