@@ -894,7 +894,7 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
   float* sa = reinterpret_cast<float*>(smem);  // TAIL_MAX clusters (8 word arrays)
   float* sb = sa + 8 * TAIL_MAX;               // TAIL_MAX clusters
   int8_t* sm = reinterpret_cast<int8_t*>(sb + 8 * TAIL_MAX);
-  __shared__ uint32_t s_we[32], s_wm[32];
+  __shared__ uint32_t s_we[32];
   __shared__ uint32_t s_count, s_insert, s_pass;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) {
@@ -950,31 +950,27 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
       e += emit[k];
       m += ism[k];
     }
-    uint32_t xe = e, xm = m;
+    // (emitted, merged) counts packed in 16 + 16 bits (both at most TAIL_MAX):
+    // a warp scan, then every warp scans the 32 warp totals itself
+    uint32_t x = e | (m << 16);
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      uint32_t ye = __shfl_up_sync(0xffffffffu, xe, o), ym = __shfl_up_sync(0xffffffffu, xm, o);
-      if (lane >= o) {
-        xe += ye;
-        xm += ym;
-      }
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
     }
-    if (lane == 31) {
-      s_we[warp] = xe;
-      s_wm[warp] = xm;
-    }
+    if (lane == 31) s_we[warp] = x;
     __syncthreads();
-    uint32_t pe = 0, pm = 0, te = 0, tm = 0;
-    for (int w = 0; w < 32; w++) {
-      uint32_t a = s_we[w], b = s_wm[w];
-      if (w < warp) {
-        pe += a;
-        pm += b;
-      }
-      te += a;
-      tm += b;
+    uint32_t wt = s_we[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, wt, o);
+      if (lane >= o) wt += y;
     }
-    uint32_t epos = pe + xe - e, mpos = pm + xm - m;
+    const uint32_t before = __shfl_sync(0xffffffffu, wt, (warp + 31) & 31);
+    const uint32_t total = __shfl_sync(0xffffffffu, wt, 31);
+    const uint32_t pre = warp ? before : 0u;
+    const uint32_t te = total & 0xffffu, tm = total >> 16;
+    uint32_t epos = (pre & 0xffffu) + (x & 0xffffu) - e, mpos = (pre >> 16) + (x >> 16) - m;
 #pragma unroll
     for (int k = 0; k < IT; k++) {
       uint32_t i = tid * IT + k;
