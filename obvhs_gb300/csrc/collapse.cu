@@ -52,9 +52,7 @@ __global__ void k_collapse_decide(const Bvh2Node* __restrict__ nodes, const uint
   uint32_t j = i;
   for (uint32_t guard = 0; guard < n; guard++) {
     j = parents[j];
-    __threadfence();
-    if (atomicAdd(&flags[j], 1u) == 0) return;  // the first child to arrive stops
-    __threadfence();
+    if (atom_add_acq_rel(&flags[j], 1u) == 0) return;  // the first child to arrive stops
     const Bvh2Node node = ld_node(&nodes[j]);
     const uint32_t f = node_first(node);
     const uint32_t lc = __ldcg(&pc[f]), rc = __ldcg(&pc[f + 1]), total = lc + rc;
@@ -235,9 +233,7 @@ __global__ void k_refit_climb(Bvh2Node* nodes, const uint32_t* __restrict__ pare
   for (uint32_t guard = 0; guard < n; guard++) {
     if (j == 0) return;
     j = parents[j];
-    __threadfence();
-    if (atomicAdd(&flags[j], 1u) == 0) return;
-    __threadfence();
+    if (atom_add_acq_rel(&flags[j], 1u) == 0) return;
     const Bvh2Node nd = ld_node_cg(&nodes[j]);
     const uint32_t f = node_first(nd);
     const Box u = box_union(node_box(ld_node_cg(&nodes[f])), node_box(ld_node_cg(&nodes[f + 1])));

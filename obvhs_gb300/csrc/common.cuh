@@ -31,6 +31,17 @@ enum : uint32_t {
 // plain launch the wait returns at once.
 __device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// atomicAdd with acquire-release semantics at GPU scope, for bottom-up
+// climbs that hand a node to the second child to arrive: the caller's
+// earlier writes are visible to the thread that observes its increment, and
+// the caller's later reads see what earlier increments released.  One atomic
+// instead of a fence on each side of a relaxed one.
+__device__ __forceinline__ uint32_t atom_add_acq_rel(uint32_t* p, uint32_t v) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
 __device__ __forceinline__ float smin(float a, float b) { return a < b ? a : b; }
 __device__ __forceinline__ float smax(float a, float b) { return a > b ? a : b; }
 

@@ -191,9 +191,7 @@ __global__ void __launch_bounds__(BLK) k_costs(const Bvh2Node* __restrict__ node
     // arrival so their latency overlaps the atomic's
     const Bvh2Node pn = ld_node(&nodes[p]);
     const uint32_t up = parents[p];
-    __threadfence();
-    if (atomicAdd(&flags[p], 1u) == 0) return;
-    __threadfence();
+    if (atom_add_acq_rel(&flags[p], 1u) == 0) return;
     inner_costs(pn, dec, p, max_prims);
     if (up == p) return;
     p = up;

@@ -526,11 +526,16 @@ __global__ void __launch_bounds__(1024) k_scan_partials(uint32_t* partial, uint3
     }
     if (lane == 31) s_warp[warp] = x;
     __syncthreads();
-    uint32_t pre = 0, tot = 0;
-    for (int w = 0; w < 32; w++) {
-      if (w < warp) pre += s_warp[w];
-      tot += s_warp[w];
+    // every warp scans the 32 warp totals itself
+    uint32_t wt = s_warp[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, wt, o);
+      if (lane >= o) wt += y;
     }
+    const uint32_t before = __shfl_sync(0xffffffffu, wt, (warp + 31) & 31);
+    const uint32_t tot = __shfl_sync(0xffffffffu, wt, 31);
+    const uint32_t pre = warp ? before : 0u;
     if (b < nb) partial[b] = carry + pre + x - v;
     __syncthreads();
     if (threadIdx.x == 0) carry += tot;
