@@ -26,6 +26,7 @@
 // published by its parent's warp, so nodes are written at exactly the
 // reference's positions: the output is byte for byte the reference's.
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <atomic>
 #include <mutex>
@@ -91,11 +92,31 @@ __device__ __forceinline__ uint2 child_term(const Dec& d, uint32_t j) {
 
 // calculate_cost_impl (src/cwbvh/bvh2_to_cwbvh.rs:257-341) for one inner node
 // whose children are complete, plus the aggregates.
-__device__ void inner_costs(const Bvh2Node& nd, Dec* dec, uint32_t x, uint32_t max_prims) {
+//
+// A leaf's record is the same for every slot and follows from its box alone,
+// so only roots store it in full; other leaves store just their (all-leaf,
+// zero) decision bytes, and a parent rebuilds a leaf child's record from the
+// child's node (leaf_dec) instead of reading 96 bytes.
+__device__ __forceinline__ Dec leaf_dec(const Bvh2Node& nd) {
+  const float cl = (half_area(node_box(nd)) * 1.0f) * PRIM_COST;
+  Dec d;
+#pragma unroll
+  for (int k = 0; k < 7; k++) {
+    d.cost[k] = cl;
+    d.meta[k] = mk(K_LEAF, 0, 0);
+    d.agg[k] = make_uint2(0, 1);
+  }
+  d.meta[7] = 0;
+  d.nprim = 1;
+  return d;
+}
+
+__device__ void inner_costs(const Bvh2Node& nd, const Bvh2Node& cl, const Bvh2Node& cr, Dec* dec, uint32_t x,
+                            uint32_t max_prims) {
   const float ha = half_area(node_box(nd));
   const uint32_t f = node_first(nd);
-  const Dec L = ld_dec_cg(&dec[f]);
-  const Dec R = ld_dec_cg(&dec[f + 1]);
+  const Dec L = node_prims(cl) != 0 ? leaf_dec(cl) : ld_dec_cg(&dec[f]);
+  const Dec R = node_prims(cr) != 0 ? leaf_dec(cr) : ld_dec_cg(&dec[f + 1]);
   const uint32_t np = L.nprim + R.nprim;
   Dec out;
   {
@@ -169,30 +190,24 @@ __global__ void __launch_bounds__(BLK) k_costs(const Bvh2Node* __restrict__ node
     set_status(status, ST_BAD_INPUT);
     return;
   }
-  {
-    const float cl = (half_area(node_box(nd)) * 1.0f) * PRIM_COST;
-    Dec d;
-#pragma unroll
-    for (int k = 0; k < 7; k++) {
-      d.cost[k] = cl;
-      d.meta[k] = mk(K_LEAF, 0, 0);
-      d.agg[k] = make_uint2(0, 1);
-    }
-    d.meta[7] = 0;
-    d.nprim = 1;
-    st_dec(&dec[i], d);
-  }
   // roots are their own parents (one tree: node 0; several trees in one
-  // array: each tree's first node)
+  // array: each tree's first node); a leaf root's record is read back whole
   uint32_t p = parents[i];
-  if (p == i) return;
+  if (p == i) {
+    st_dec(&dec[i], leaf_dec(nd));
+    return;
+  }
+  // the decision bytes (all K_LEAF, zero) that the emission reads
+  __stcg(reinterpret_cast<uint2*>(reinterpret_cast<char*>(&dec[i]) + offsetof(Dec, meta)), make_uint2(0u, 0u));
   for (uint32_t guard = 0; guard < n; guard++) {
-    // the parent's node and its own parent are static: load them before the
-    // arrival so their latency overlaps the atomic's
+    // the parent's node, its children and its own parent are static: load
+    // them before the arrival so their latency overlaps the atomic's
     const Bvh2Node pn = ld_node(&nodes[p]);
     const uint32_t up = parents[p];
+    const uint32_t f = node_first(pn);
+    const Bvh2Node cl = ld_node(&nodes[f]), cr = ld_node(&nodes[f + 1]);
     if (atom_add_acq_rel(&flags[p], 1u) == 0) return;
-    inner_costs(pn, dec, p, max_prims);
+    inner_costs(pn, cl, cr, dec, p, max_prims);
     if (up == p) return;
     p = up;
   }
