@@ -366,18 +366,26 @@ def serving(params, n_requests=3000, rate=2000.0, budget=80 << 30, seed=1005):
     Inputs are prefixes of 8 pooled 2M-triangle scenes and their 1M-ray
     batches in pinned host memory; 8 BVHs are resident before the first
     request.  The same stream runs through the continuous-batching server and
-    the plain one-request-per-call server; per-request hits are compared by a
-    digest of the (id, t) words."""
+    the plain one-request-per-call server.  Every ray request brings its own
+    pinned hit buffer (the client's), so hits are copied straight into it and
+    a request is done when they have landed; after each run (outside the
+    timing) the per-request hits are compared by a digest of the (id, t)
+    words."""
     from obvhs_gb300 import serve as V
 
     tris, rays = V.clustered_pools(8, 2_000_000, 1_000_000, seed=seed)
     rng = np.random.default_rng(seed)
     reqs, scene_of = V.make_stream(n_requests, rate, tris, rays, rng, preloaded=8)
     pre = [(i, tris[scene_of[i]][:200_000]) for i in range(8)]
+    ray_reqs = [r for r in reqs if r.kind == "rays"]
+    hit_pool = V.pinned_empty((sum(len(r.rays) for r in ray_reqs), 2), np.uint32)
+    at = 0
+    for r in ray_reqs:
+        r.out = hit_pool[at:at + len(r.rays)]
+        at += len(r.rays)
 
     def digest(block):
-        # (sum, xor) of the request's (id, t) words: cheap enough to stay off
-        # the serving path's critical time, and any differing hit changes it
+        # (sum, xor) of the request's (id, t) words: any differing hit changes it
         w = block.view(np.uint64).ravel()
         return int(w.sum(dtype=np.uint64)), int(np.bitwise_xor.reduce(w)) if len(w) else 0
 
@@ -386,8 +394,8 @@ def serving(params, n_requests=3000, rate=2000.0, budget=80 << 30, seed=1005):
     try:
         # warm-up on a short stream of the same kind
         wreqs, wsc = V.make_stream(200, rate, tris, rays, np.random.default_rng(seed + 1), preloaded=8)
-        V.ContinuousServer(be, budget, result_sink=digest).run(wreqs, preload=pre)
-        V.PlainServer(be, budget, result_sink=digest).run(wreqs, preload=pre)
+        V.ContinuousServer(be, budget).run(wreqs, preload=pre)
+        V.PlainServer(be, budget).run(wreqs, preload=pre)
         results = {}
         arrival = [r.arrival for r in reqs]
         # at the offered rate, then the same stream 20x compressed (40,000
@@ -396,7 +404,8 @@ def serving(params, n_requests=3000, rate=2000.0, budget=80 << 30, seed=1005):
             for name, cls in (("continuous", V.ContinuousServer), ("plain", V.PlainServer)):
                 for r, a in zip(reqs, arrival):
                     r.arrival, r.done, r.result, r.step = a * squeeze, None, None, -1
-                srv = cls(be, budget, result_sink=digest)
+                hit_pool.fill(0xFFFFFFFF)
+                srv = cls(be, budget)
                 srv.run(reqs, preload=pre)
                 summ = V.summarize(reqs)
                 summ["evictions"] = srv.store.evictions
@@ -405,7 +414,7 @@ def serving(params, n_requests=3000, rate=2000.0, budget=80 << 30, seed=1005):
                     summ["launch_steps_build"] = srv.steps["build"]
                     summ["launch_steps_rays"] = srv.steps["rays"]
                 out[scen + name] = summ
-                results[scen + name] = [r.result for r in reqs]
+                results[scen + name] = [digest(r.out) if r.kind == "rays" else r.result for r in reqs]
                 for k in list(srv.store.items):
                     srv.store.items.pop(k)[0].free()
         out["identical_hits"] = (results["continuous"] == results["plain"] == results["saturated_continuous"]

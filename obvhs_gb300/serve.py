@@ -22,8 +22,11 @@ triangles.
 PlainServer is the baseline: one request per call, in arrival order (a build
 call per scene, a traversal call per ray batch), under the same budget.
 
-Latency is arrival to result on the host.  Backends: GpuBackend (this
-library) and any object with the same four methods (tests use a CPU fake).
+Latency is arrival to result on the host.  A ray request may carry the
+client's own hit buffer (Request.out, pinned): the hits are copied straight
+into it and the request is done when they have landed; otherwise the server
+copies them out of its step buffer.  Backends: GpuBackend (this library) and
+any object with the same four methods (tests use a CPU fake).
 """
 from __future__ import annotations
 
@@ -46,6 +49,7 @@ class Request:
     done: float | None = None
     result: object = None
     step: int = -1            # the step (launch) that served it
+    out: np.ndarray | None = None  # rays: the client's (n, 2) uint32 hit buffer; pinned, the hits are copied straight in
 
 
 class ResidentStore:
@@ -106,9 +110,14 @@ class _Base:
         self.rebuilds = 0
         self.sink = result_sink  # maps a ray batch's (ids, t) to what the request keeps (default: all of it)
 
-    def _keep(self, result):
-        """What a ray request keeps: the sink's value, else the backend's own
+    def _keep(self, result, r=None):
+        """What a ray request keeps: the sink's value, else (ids, t) views of
+        the client's own hit buffer when it gave one, else the backend's own
         copy of the hits (results may be views of a reused buffer)."""
+        if r is not None and r.out is not None:
+            if self.sink:
+                return self.sink(r.out)
+            return r.out[:, 0], r.out[:, 1].view(np.float32)
         if self.sink:
             return self.sink(result)
         own = getattr(self.backend, "result", None)
@@ -137,10 +146,10 @@ class PlainServer(_Base):
                 if r.bvh_id not in self.store:
                     self.rebuilds += 1
                     self._build(r.bvh_id, self.sources[r.bvh_id])
-                res = self.backend.trace_one(self.store.get(r.bvh_id), r.rays)
+                res = self.backend.trace_one(self.store.get(r.bvh_id), r.rays, r.out)
             r.done = time.perf_counter() - t0
             if r.kind == "rays":
-                r.result = self._keep(res)
+                r.result = self._keep(res, r)
             r.step = step
         return requests
 
@@ -295,12 +304,12 @@ class ContinuousServer(_Base):
                     n += len(r.rays)
                 ids = {id(r) for r in take}
                 self.rays = [r for r in self.rays if id(r) not in ids]
-                items = [(self.store.get(r.bvh_id), r.rays) for r in take]
+                items = [(self.store.get(r.bvh_id), r.rays, r.out) for r in take]
                 step = self.steps["rays"]
                 self.steps["rays"] += 1
             results = self.backend.trace_many(items)
             done = self._now()
-            kept = [self._keep(res) for res in results]
+            kept = [self._keep(res, r) for r, res in zip(take, results)]
             with self.cv:
                 for r, res in zip(take, kept):
                     self.store.unpin(r.bvh_id)
@@ -403,21 +412,26 @@ class GpuBackend:
 
     # traversal
     def trace_many(self, items):
-        n = sum(len(r) for _, r in items)
-        out = self.pin_out.get(n * 8).numpy().view(np.uint32).reshape(-1, 2)
+        """items: (handle, rays) or (handle, rays, out): hits go to `out`
+        (the client's buffer) when given, else to the step buffer."""
+        items = [(it[0], it[1], it[2] if len(it) > 2 else None) for it in items]
+        n = sum(len(r) for _, r, o in items if o is None)
+        out = self.pin_out.get(max(n, 1) * 8).numpy().view(np.uint32).reshape(-1, 2)
         index, bvhs, which, outs, at = {}, [], [], [], 0
-        for h, r in items:
+        for h, r, o in items:
             k = index.setdefault(id(h), len(bvhs))
             if k == len(bvhs):
                 bvhs.append(h)
             which.append(k)
-            outs.append(out[at:at + len(r)])
-            at += len(r)
-        self.G.ray_traverse_batches(bvhs, which, [r for _, r in items], outs=outs, ctx=self.tctx)
+            if o is None:
+                o = out[at:at + len(r)]
+                at += len(r)
+            outs.append(o)
+        self.G.ray_traverse_batches(bvhs, which, [r for _, r, _ in items], outs=outs, ctx=self.tctx)
         return outs
 
-    def trace_one(self, h, r):
-        return self.trace_many([(h, r)])[0]
+    def trace_one(self, h, r, out=None):
+        return self.trace_many([(h, r, out)])[0]
 
     @staticmethod
     def result(block):

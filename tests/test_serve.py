@@ -49,10 +49,20 @@ class FakeBackend:
 
         time.sleep(self.delay)
         self.traces.append(len(items))
-        return [self._trace(h, r) for h, r in items]
+        res = []
+        for it in items:
+            ids, t = self._trace(it[0], it[1])
+            out = it[2] if len(it) > 2 else None
+            if out is not None:  # the client's (n, 2) uint32 buffer
+                out[:, 0] = ids
+                out[:, 1] = t.astype(np.float32).view(np.uint32)
+                res.append(out)
+            else:
+                res.append((ids, t))
+        return res
 
-    def trace_one(self, h, r):
-        return self.trace_many([(h, r)])[0]
+    def trace_one(self, h, r, out=None):
+        return self.trace_many([(h, r, out)])[0]
 
 
 def _pools(rng, k=4):
@@ -113,6 +123,23 @@ def test_plain_server_one_call_per_request():
     _check_alone(reqs, pre, b)
     assert all(n == 1 for n in b.builds) and all(n == 1 for n in b.traces)
     assert len(b.traces) == sum(r.kind == "rays" for r in reqs)
+
+
+@pytest.mark.parametrize("server", ["continuous", "plain"])
+def test_client_hit_buffers(server):
+    """Requests that bring their own hit buffer get their hits there, the
+    same as without one; the others still get copies."""
+    reqs, _, pre, _ = _stream(6, n=200)
+    for k, r in enumerate(reqs):
+        if r.kind == "rays" and k % 2 == 0:
+            r.out = np.zeros((len(r.rays), 2), np.uint32)
+    b = FakeBackend()
+    cls = serve.ContinuousServer if server == "continuous" else serve.PlainServer
+    cls(b, budget=10**9).run(reqs, preload=pre)
+    _check_alone(reqs, pre, b)
+    for r in reqs:
+        if r.out is not None:
+            assert np.shares_memory(r.result[0], r.out)
 
 
 @pytest.mark.parametrize("server", ["continuous", "plain"])
