@@ -64,6 +64,7 @@ enum ScratchSlot {
   SLOT_SEG,  // segmented builds: per-scene tables
   SLOT_SEG_AABBS,
   SLOT_SEG_IDX,
+  SLOT_MORTON_TOP,  // the Morton sort's high-digit keys (+ a flag word)
   SLOT_COUNT
 };
 
@@ -126,6 +127,9 @@ struct BuildReadback {
   uint32_t status;
   float root_box[8];
 };
+// The Morton sort's run flag is read back at h_small + RUN_FLAG_OFFSET.
+constexpr size_t RUN_FLAG_OFFSET = 3072;
+static_assert(READBACK_OFFSET + sizeof(BuildReadback) <= RUN_FLAG_OFFSET, "pinned read-back areas overlap");
 
 struct obvhs_ctx {
   int device = 0;

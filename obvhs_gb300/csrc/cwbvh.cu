@@ -201,7 +201,8 @@ __global__ void __launch_bounds__(BLK) k_costs(const Bvh2Node* __restrict__ node
   __stcg(reinterpret_cast<uint2*>(reinterpret_cast<char*>(&dec[i]) + offsetof(Dec, meta)), make_uint2(0u, 0u));
   for (uint32_t guard = 0; guard < n; guard++) {
     // the parent's node, its children and its own parent are static: load
-    // them before the arrival so their latency overlaps the atomic's
+    // them before the arrival so their latency overlaps the atomic's (the
+    // climb's latency, not its traffic, bounds this kernel)
     const Bvh2Node pn = ld_node(&nodes[p]);
     const uint32_t up = parents[p];
     const uint32_t f = node_first(pn);

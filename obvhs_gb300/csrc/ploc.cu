@@ -203,6 +203,65 @@ __global__ void __launch_bounds__(BLK) k_morton128(const Bvh2Node* __restrict__ 
   codes[i] = morton128_of(ld_node(&leaves[i]), make_scale(total_keys));
 }
 
+// --- the Morton sort on the high digits -----------------------------------------
+
+constexpr uint32_t RUN_MAX = 32;  // longest run of equal high digits put in order in place
+
+// The high digits of each code (U128: the high 64 bits; U64: bits 24-63);
+// also clears the sort's `zero_words` scratch words and the run flag.
+__global__ void __launch_bounds__(BLK) k_morton_top(const void* __restrict__ codes, uint32_t n, int precision,
+                                                    unsigned long long* __restrict__ top, uint32_t* flag,
+                                                    uint32_t* sort_scratch, size_t zero_words) {
+  grid_dep_wait();
+  const size_t t = blockIdx.x * (size_t)BLK + threadIdx.x;
+  radix_zero(sort_scratch, zero_words, t, (size_t)gridDim.x * BLK);
+  if (t == 0) *flag = 0;
+  if (t >= n) return;
+  top[t] = precision ? static_cast<const U128*>(codes)[t].hi : static_cast<const unsigned long long*>(codes)[t] >> 24;
+}
+
+// Sets *flag when some run of equal high digits is longer than RUN_MAX.
+__global__ void __launch_bounds__(BLK) k_run_check(const unsigned long long* __restrict__ top, uint32_t n,
+                                                   uint32_t* flag) {
+  grid_dep_wait();
+  const uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  if (i >= RUN_MAX && i < n && top[i] == top[i - RUN_MAX]) *flag = 1u;
+}
+
+// Each run of equal high digits (at most RUN_MAX long; its entries are in
+// input order, the high-digit sort being stable) sorted stably by the
+// remaining bits, by the thread at its first entry.
+__global__ void __launch_bounds__(BLK) k_fix_runs(const unsigned long long* __restrict__ top, uint32_t* order,
+                                                  const void* __restrict__ codes, uint32_t n, int precision) {
+  grid_dep_wait();
+  const uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  if (i + 1 >= n || top[i + 1] != top[i] || (i > 0 && top[i - 1] == top[i])) return;
+  uint32_t end = i + 2;
+  while (end < n && end < i + RUN_MAX && top[end] == top[i]) end++;
+  uint32_t v[RUN_MAX];
+  unsigned long long r[RUN_MAX];
+  const uint32_t len = end - i;
+  for (uint32_t k = 0; k < len; k++) {
+    v[k] = order[i + k];
+    r[k] = precision ? static_cast<const U128*>(codes)[v[k]].lo
+                     : (static_cast<const unsigned long long*>(codes)[v[k]] & 0xffffffull);
+  }
+  // insertion sort: an entry moves only past strictly larger ones (stable)
+  for (uint32_t k = 1; k < len; k++) {
+    const uint32_t vk = v[k];
+    const unsigned long long rk = r[k];
+    uint32_t j = k;
+    while (j > 0 && r[j - 1] > rk) {
+      v[j] = v[j - 1];
+      r[j] = r[j - 1];
+      j--;
+    }
+    v[j] = vk;
+    r[j] = rk;
+  }
+  for (uint32_t k = 0; k < len; k++) order[i + k] = v[k];
+}
+
 // --- segmented leaves, Morton codes and scene keys ----------------------------
 //
 // Scene s owns leaves [prim_start[s], prim_start[s + 1]); its total AABB is
@@ -1048,7 +1107,13 @@ int ploc_morton_codes(BuildCtx& c, const Bvh2Node* leaves, uint32_t n, const int
   return 0;
 }
 
-// Stable sort of the codes in place of `codes`; *order_out = sorted order.
+// Stable order of the codes (*order_out), leaving `codes` as they are.
+//
+// The sort runs on the high digits only (U128: the high 64 bits; U64: bits
+// 24-63), which almost always tell the codes apart, then puts every run of
+// equal high digits in order of the remaining bits, stably; that is the
+// stable order of the whole codes.  Runs are checked first: if one is longer
+// than RUN_MAX (duplicate-heavy input), the whole codes are sorted instead.
 int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_t** order_out) {
   Scratch& s = c.scratch;
   size_t kb = precision ? sizeof(U128) : sizeof(unsigned long long);
@@ -1056,9 +1121,32 @@ int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_
   uint32_t* vals = (uint32_t*)s.get(SLOT_VALS, (size_t)n * 4);
   uint32_t* vals_alt = (uint32_t*)s.get(SLOT_VALS_ALT, (size_t)n * 4);
   uint32_t* rs = (uint32_t*)s.get(SLOT_ALL_HIST, radix_scratch_words(n) * 4);
-  if (!keys_alt || !vals || !vals_alt || !rs) return c.fail(OBVHS_ERR_OOM, "scratch");
+  unsigned long long* top = (unsigned long long*)s.get(SLOT_MORTON_TOP, (size_t)n * 8 + 16);
+  if (!keys_alt || !vals || !vals_alt || !rs || !top) return c.fail(OBVHS_ERR_OOM, "scratch");
   bool alt = false;
   cudaError_t e;
+  if (n > RUN_MAX) {
+    const int digits = precision ? 8 : 5;
+    uint32_t* flag = reinterpret_cast<uint32_t*>(top + n);
+    KLAUNCH("k_morton_top", CK(launch_k(k_morton_top, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, codes, n, precision,
+                                        top, flag, rs, radix_zero_words<unsigned long long>(n, digits))));
+    e = radix_sort_pairs<unsigned long long>(c, top, vals, n, true, (unsigned long long*)keys_alt, vals_alt, rs, &alt,
+                                             digits, true);
+    if (e) return c.cuda_fail(e, "radix sort");
+    const unsigned long long* stop = alt ? (const unsigned long long*)keys_alt : top;
+    uint32_t* ord = alt ? vals_alt : vals;
+    KLAUNCH("k_run_check", CK(launch_k(k_run_check, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, stop, n, flag)));
+    uint32_t* h = reinterpret_cast<uint32_t*>(static_cast<char*>(c.h_small) + RUN_FLAG_OFFSET);  // pinned
+    CK(cudaMemcpyAsync(h, flag, 4, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    if (*h == 0) {
+      KLAUNCH("k_fix_runs", CK(launch_k(k_fix_runs, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, stop, ord, codes, n,
+                                        precision)));
+      *order_out = ord;
+      return 0;
+    }
+    alt = false;  // a run longer than RUN_MAX: sort the whole codes
+  }
   if (precision)
     e = radix_sort_pairs<U128>(c, (U128*)codes, vals, n, true, (U128*)keys_alt, vals_alt, rs, &alt);
   else

@@ -56,6 +56,36 @@ def test_morton_duplicates_keep_input_order(G):
     assert _eq(order, oorder)
 
 
+def test_morton_exact_duplicates_u128(G):
+    a = np.repeat(_random_aabbs(40, 5), 50, axis=0)  # runs longer than the high-digit fix-up takes
+    codes, order = G.morton_sort(a, 1)
+    ocodes, oorder = O.morton(a, 1)
+    assert _eq(codes, ocodes) and _eq(order, oorder)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_morton_runs_of_equal_high_digits(G, precision):
+    """Clumps of 1-32 boxes whose centres differ only below the high digits
+    the sort runs on: each run is put in order by the low bits (stably)."""
+    rng = np.random.default_rng(21 + precision)
+    base = rng.uniform(-50, 50, size=(3000, 3))
+    reps = rng.integers(1, 33, size=len(base))
+    c = np.repeat(base, reps, axis=0)
+    jitter = 2e-3 if precision == 0 else 1e-5
+    c = c + rng.uniform(-jitter, jitter, size=c.shape)
+    c[::7] = np.repeat(base, reps, axis=0)[::7]  # some exact duplicates inside runs too
+    perm = rng.permutation(len(c))
+    c = c[perm]
+    a = np.concatenate([c - 1e-6, c + 1e-6], 1).astype(np.float32)
+    codes, order = G.morton_sort(a, precision)
+    ocodes, oorder = O.morton(a, precision)
+    assert _eq(codes, ocodes) and _eq(order, oorder)
+    # the runs exist: many neighbours in sorted order share their high digits
+    srt = ocodes[oorder]
+    hi = srt[:, 1] if precision else srt[:, 0] >> np.uint64(24)
+    assert (hi[1:] == hi[:-1]).sum() > 1000
+
+
 @pytest.mark.parametrize("radius,threshold,precision", [(1, 0, 0), (2, 1, 0), (6, 2, 0), (14, 3, 0), (16, 0, 0),
                                                         (24, 2, 1), (32, 0, 1)])
 @pytest.mark.parametrize("n", [2, 3, 17, 2048, 2049, 50_000])
