@@ -200,11 +200,60 @@ __device__ __forceinline__ void set_stack_mode(FindSearch<CAP, CLAMP>& f, uint32
   }
 }
 
+// Priority of proposal k (lower = earlier): area_diff descending, then
+// candidate rank ascending -- the order a stable sort by descending
+// area_diff gives.
+__device__ __forceinline__ unsigned long long prio_key(float area_diff, uint32_t k) {
+  return ((unsigned long long)(~__float_as_uint(area_diff)) << 32) | k;
+}
+
+// A proposal's five conflict nodes {to, from, sibling(from), parent(to),
+// parent(from)} (src/bvh2/reinsertion.rs:211-221) and its priority key,
+// gathered once per pass.
+struct __align__(16) Conf {
+  uint32_t c[5];
+  uint32_t pad;
+  unsigned long long key;
+};
+
+// Where a search's result goes: every candidate's (from, to, area_diff) in
+// reins[k]; a proposal with a gain is also listed (plist, its conflict set
+// and key, state unresolved) and resets the round-0 claim words of its five
+// nodes, so the resolution starts from the list.  The list's order does not
+// matter: the rounds decide by key.
+struct ProposalOut {
+  Reins* reins;
+  uint32_t* plist;
+  Conf* conf;
+  uint8_t* state;
+  unsigned long long* owner0;
+  uint32_t* count;  // list length
+};
+
+__device__ __forceinline__ void emit_proposal(const ProposalOut& o, const uint32_t* __restrict__ parents, uint32_t k,
+                                              const Reins& r) {
+  o.reins[k] = r;
+  if (!(r.area_diff > 0.0f)) return;
+  const uint32_t j = atomicAdd(o.count, 1u);
+  const uint32_t c0 = r.to, c1 = r.from, c2 = sibling_of(r.from), c3 = parents[r.to], c4 = parents[r.from];
+  const unsigned long long key = prio_key(r.area_diff, k);
+  uint4* q = reinterpret_cast<uint4*>(&o.conf[j]);
+  __stcg(q, make_uint4(c0, c1, c2, c3));
+  __stcg(q + 1, make_uint4(c4, 0u, (uint32_t)key, (uint32_t)(key >> 32)));
+  o.plist[j] = k;
+  o.state[j] = 0;
+  o.owner0[c0] = ~0ull;
+  o.owner0[c1] = ~0ull;
+  o.owner0[c2] = ~0ull;
+  o.owner0[c3] = ~0ull;
+  o.owner0[c4] = ~0ull;
+}
+
 template <int CAP, bool CLAMP>
 __global__ void __launch_bounds__(FIND_THREADS) k_find(const Bvh2Node* __restrict__ nodes,
                                                        const uint32_t* __restrict__ parents,
                                                        const uint32_t* __restrict__ cand, uint32_t count,
-                                                       uint32_t cap_rt, Reins* __restrict__ out, uint32_t* status,
+                                                       uint32_t cap_rt, ProposalOut out, uint32_t* status,
                                                        StackModes modes) {
   grid_dep_wait();
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -217,7 +266,7 @@ __global__ void __launch_bounds__(FIND_THREADS) k_find(const Bvh2Node* __restric
   f.start(nodes, parents, node);
   while (!f.step(nodes, parents)) {
   }
-  out[k] = f.result(parents, status);
+  emit_proposal(out, parents, k, f.result(parents, status));
 }
 
 // More candidates than resident threads: searches differ widely in length,
@@ -227,7 +276,7 @@ template <int CAP, bool CLAMP>
 __global__ void __launch_bounds__(FIND_THREADS) k_find_persistent(const Bvh2Node* __restrict__ nodes,
                                                                   const uint32_t* __restrict__ parents,
                                                                   const uint32_t* __restrict__ cand, uint32_t count,
-                                                                  uint32_t cap_rt, Reins* __restrict__ out,
+                                                                  uint32_t cap_rt, ProposalOut out,
                                                                   uint32_t* next, uint32_t* status, StackModes modes) {
   grid_dep_wait();
   const int lane = threadIdx.x & 31;
@@ -256,28 +305,12 @@ __global__ void __launch_bounds__(FIND_THREADS) k_find_persistent(const Bvh2Node
     }
     if (!__any_sync(0xffffffffu, active)) break;
     if (active && f.step(nodes, parents)) {
-      out[k] = f.result(parents, status);
+      emit_proposal(out, parents, k, f.result(parents, status));
       active = false;
       need = true;
     }
   }
 }
-
-// Priority of proposal k (lower = earlier): area_diff descending, then
-// candidate rank ascending -- the order a stable sort by descending
-// area_diff gives.
-__device__ __forceinline__ unsigned long long prio_key(float area_diff, uint32_t k) {
-  return ((unsigned long long)(~__float_as_uint(area_diff)) << 32) | k;
-}
-
-// A proposal's five conflict nodes {to, from, sibling(from), parent(to),
-// parent(from)} (src/bvh2/reinsertion.rs:211-221) and its priority key,
-// gathered once per pass.
-struct __align__(16) Conf {
-  uint32_t c[5];
-  uint32_t pad;
-  unsigned long long key;
-};
 
 struct ResolveArgs {
   Bvh2Node* nodes;
@@ -535,52 +568,18 @@ __device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, u
   }
 }
 
-// Step 1 of a pass: the proposals with area_diff > 0 (warp-aggregated
-// append), their conflict sets and keys, and the round-0 claim words reset.
-// `warp_t0` is the first index of the calling thread's warp.
-__device__ __forceinline__ void list_proposals(const ResolveArgs& a, uint32_t warp_t0, uint32_t stride) {
-  const int lane = threadIdx.x & 31;
-  unsigned long long* owner0 = a.owner;
-  for (uint32_t k0 = warp_t0; k0 < a.count; k0 += stride) {
-    const uint32_t k = k0 + lane;
-    Reins r{0, 0, 0.0f, 0};
-    if (k < a.count) r = a.reins[k];
-    const bool pos = k < a.count && r.area_diff > 0.0f;
-    const uint32_t ballot = __ballot_sync(0xffffffffu, pos);
-    if (!ballot) continue;
-    const int leader = __ffs(ballot) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(&a.ctr[0], (uint32_t)__popc(ballot));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (pos) {
-      const uint32_t j = base + __popc(ballot & ((1u << lane) - 1u));
-      const uint32_t c0 = r.to, c1 = r.from, c2 = sibling_of(r.from), c3 = a.parents[r.to], c4 = a.parents[r.from];
-      const unsigned long long key = prio_key(r.area_diff, k);
-      uint4* q = reinterpret_cast<uint4*>(&a.conf[j]);
-      __stcg(q, make_uint4(c0, c1, c2, c3));
-      __stcg(q + 1, make_uint4(c4, 0u, (uint32_t)key, (uint32_t)(key >> 32)));
-      a.plist[j] = k;
-      a.state[j] = 0;
-      owner0[c0] = ~0ull;
-      owner0[c1] = ~0ull;
-      owner0[c2] = ~0ull;
-      owner0[c3] = ~0ull;
-      owner0[c4] = ~0ull;
-    }
-  }
-}
-
-// Everything after find_reinsertion for one pass, in one cooperative launch:
-//   1. list the proposals with area_diff > 0 and gather their conflict sets
+// Everything after find_reinsertion for one pass, in one cooperative launch
+// (the searches already listed the proposals with area_diff > 0, with their
+// conflict sets, and reset their round-0 claim words: emit_proposal):
 //   2. greedy conflict resolution in priority order (rounds)
 //   3. reinsert_node for every accepted proposal (src/bvh2/reinsertion.rs:336-382)
 //   4. mark the nodes whose boxes may change: `to` and its ancestors, and the
 //      ancestors of the old parent of `from`
 //   5. refit the marked nodes bottom-up, starting from marked nodes without
 //      marked children.
-// After step 1, a pass with at most RESOLVE_SMALL proposals continues in
-// block 0 alone (block barriers instead of grid barriers); the other blocks
-// return and take no further part in any barrier.
+// A pass with at most RESOLVE_SMALL proposals runs in block 0 alone (block
+// barriers instead of grid barriers); the other blocks return at once and
+// take no part in any barrier.
 __global__ void __launch_bounds__(RESOLVE_THREADS) k_resolve(ResolveArgs a) {
   grid_dep_wait();
   cg::grid_group grid = cg::this_grid();
@@ -588,13 +587,8 @@ __global__ void __launch_bounds__(RESOLVE_THREADS) k_resolve(ResolveArgs a) {
   const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
   __shared__ uint32_t s_rem;
 
-  // 1. proposals with a gain, their conflict sets, the round-0 claim words
-  list_proposals(a, blockIdx.x * blockDim.x + (threadIdx.x & ~31u), stride);
+  // 1. the proposals with a gain were listed by the search (emit_proposal)
   const bool single = gridDim.x == 1;  // one block, launched normally
-  if (single)
-    __syncthreads();
-  else
-    grid.sync();
   const uint32_t P = *(volatile uint32_t*)&a.ctr[0];
   if (single || P <= RESOLVE_SMALL) {
     if (blockIdx.x != 0) return;
@@ -699,19 +693,20 @@ int reins_pass(BuildCtx& c, Bvh2Node* nodes, uint32_t len, const uint32_t* cand,
   }
   uint32_t* pass_ctr = B.counters + 8 + (size_t)ri * 8;  // [5]: next candidate for k_find
   const uint32_t fblocks = div_up<uint32_t>(count, FIND_THREADS);
+  const ProposalOut po{B.reins, B.plist, B.conf, B.state, B.owner, pass_ctr};
   if (fblocks > (uint32_t)find_blocks) {
     if (clamp)
       KLAUNCH("k_find", launch_k(k_find_persistent<192, true>, find_blocks, FIND_THREADS, 0, c.stream,
-                            nodes, B.parents, cand, count, cap_rt, B.reins, pass_ctr + 5, c.d_status, modes));
+                            nodes, B.parents, cand, count, cap_rt, po, pass_ctr + 5, c.d_status, modes));
     else
       KLAUNCH("k_find", launch_k(k_find_persistent<1024, false>, find_blocks, FIND_THREADS, 0, c.stream,
-                            nodes, B.parents, cand, count, cap_rt, B.reins, pass_ctr + 5, c.d_status, modes));
+                            nodes, B.parents, cand, count, cap_rt, po, pass_ctr + 5, c.d_status, modes));
   } else if (clamp) {
     KLAUNCH("k_find", launch_k(k_find<192, true>, fblocks, FIND_THREADS, 0, c.stream, nodes, B.parents, cand, count, cap_rt,
-                                                                           B.reins, c.d_status, modes));
+                                                                           po, c.d_status, modes));
   } else {
     KLAUNCH("k_find", launch_k(k_find<1024, false>, fblocks, FIND_THREADS, 0, c.stream, nodes, B.parents, cand, count, cap_rt,
-                                                                             B.reins, c.d_status, modes));
+                                                                             po, c.d_status, modes));
   }
   CK(cudaGetLastError());
   // conflict resolution, moves and refit in one launch
