@@ -129,7 +129,8 @@ ROOFLINE_NOTES = {
     "k_rs_pass": "radix sort passes of 0.03-1M keys: each pass is one wave of tiles whose ranking, "
                  "decoupled look-back and scatter phases are latency-bound",
     "k_resolve": "dependent rounds and tree climbs; bytes are a lower bound",
-    "k_find": "branch-and-bound tree searches; bytes are a lower bound",
+    "k_find": "branch-and-bound tree searches: each step a dependent node load (bytes: the node records the "
+              "oracle's searches read on the same tree)",
     "k_ploc_coop": "compute in the nearest-neighbour search; clusters stay in L2",
     "k_costs": "bottom-up tree climb; bytes are a lower bound",
     "k_emit_all": "work queue over the tree; bytes are a lower bound",
@@ -148,25 +149,29 @@ def reinsertion_schedule(n_nodes, ratio=0.2):
     return out
 
 
-def kernel_byte_models(m, sum_counts, n_cw, n_prims):
+def kernel_byte_models(m, sum_counts, n_cw, n_prims, search_nodes=None):
     """Algorithmic bytes of one build, per kernel (totals over its launches).
 
     Minimum bytes each kernel must move for its result, from the per-unit
-    figures of the path's byte model; pointer-chasing kernels (k_find,
-    k_resolve, k_costs, k_emit_all) also read tree nodes along their walks,
-    which depends on the tree and is not counted (a lower bound)."""
+    figures of the path's byte model.  The reinsertion searches read the node
+    records the oracle counts for the same build (`search_nodes`, the same
+    searches on the same tree); the other pointer-chasing kernels (k_resolve,
+    k_costs, k_emit_all) also read tree nodes along their walks, which is not
+    counted (a lower bound)."""
     nodes = 2 * m - 1
     sched = reinsertion_schedule(nodes)
     cand_sort = sum(4 * c * 16 for c, _ in sched) + sum(c * 4 for c, _ in sched)
+    searched = sum(s_ for _, s_ in sched)
     return {
-        # Morton U128 sort (16 passes of 8-bit digits over key 16 B + value
-        # 4 B, read and written) and the 16 candidate sorts (u32 key + value)
-        "k_rs_pass": 16 * m * 40 + cand_sort,
+        # Morton sort on the high 64 bits (8 passes of 8-bit digits over key
+        # 8 B + value 4 B, read and written) and the 16 candidate sorts (u32
+        # key + value)
+        "k_rs_pass": 8 * m * 24 + cand_sort,
         # every PLOC pass: box read twice, offset byte written and read twice,
         # compacted cluster written; every merged pair written once
         "k_ploc_coop": sum_counts * (32 + 32 + 1 + 2 + 32) + (nodes - 1) * 32,
-        # candidate id, three node loads to start the search, result
-        "k_find": sum(s_ * (4 + 3 * 32 + 16) for _, s_ in sched),
+        # candidate id and result per search, 32 B per node record read
+        "k_find": searched * (4 + 16) + (search_nodes if search_nodes is not None else searched * 3) * 32,
         # proposal read, conflict set written and read back
         "k_resolve": sum(s_ * (16 + 32 + 32) for _, s_ in sched),
         # node + parent read, cost record (96 B) written, children records read
@@ -446,8 +451,9 @@ def cpu_build_rate(tris, params, reps, nthreads):
     t = []
     for _ in range(reps):
         t0 = time.perf_counter()
-        O.build(tris=tris, params=params, nthreads=nthreads, keep_intermediate=False)
+        ob = O.build(tris=tris, params=params, nthreads=nthreads, keep_intermediate=False)
         t.append(time.perf_counter() - t0)
+    cpu_build_rate.last = ob
     return len(tris) / (sum(t) / len(t)) / 1e6, t
 
 
@@ -457,6 +463,7 @@ def cpu_baseline(tris, params, rays, cores, ctx):
     from oracle import oracle as O
 
     rate, times = cpu_build_rate(tris, params, 2, cores)
+    ob = cpu_build_rate.last
     import obvhs_gb300 as G
 
     cw = G.build_cwbvh_from_tris(tris, params, ctx=ctx)
@@ -464,7 +471,8 @@ def cpu_baseline(tris, params, rays, cores, ctx):
     t0 = time.perf_counter()
     _, _, _, cnt = O.traverse(nodes, pidx, tris, rays, 0, nthreads=cores, counters=True)
     dt = time.perf_counter() - t0
-    return rate, times, {"visits": int(cnt[0]), "tests": int(cnt[1]), "mrays_s": len(rays) / dt / 1e6}
+    return rate, times, {"visits": int(cnt[0]), "tests": int(cnt[1]), "mrays_s": len(rays) / dt / 1e6,
+                         "searches": ob.searches, "search_nodes": ob.search_nodes}
 
 
 def run_reference(args):
@@ -645,7 +653,8 @@ def run_gb300(args):
     # roofline of the build's dominant kernel (largest share of device time in
     # the event-bracketed build): algorithmic bytes per launch / mean launch
     # time; traffic = DRAM bytes per launch from the ncu capture (profiles/)
-    models = kernel_byte_models(stats.leaf_count, stats.ploc_sum_counts, n_nodes, n_prims)
+    models = kernel_byte_models(stats.leaf_count, stats.ploc_sum_counts, n_nodes, n_prims,
+                                cpu_trace.get("search_nodes"))
     build_kernels = {}
     for k, v in kernel_profile.items():
         if k.startswith("k_traverse"):

@@ -533,7 +533,9 @@ struct Reinsertion {
 };
 
 // Returns -1 when the stack would overflow where the reference panics.
-int find_reinsertion(const Bvh2& bvh, uint32_t node_id, Reinsertion& out) {
+// *loads (if given) counts the node records the search reads.
+int find_reinsertion(const Bvh2& bvh, uint32_t node_id, Reinsertion& out, uint64_t* loads = nullptr) {
+  uint64_t nl = 3;  // the node, its parent and its sibling
   Reinsertion best{node_id, 0, 0.0f};
   float node_area = half_area(bvh.nodes[node_id].box);
   uint32_t parent_id = bvh.parents[node_id];
@@ -577,6 +579,7 @@ int find_reinsertion(const Bvh2& bvh, uint32_t node_id, Reinsertion& out) {
       uint32_t top_sib = stack[sp].second;
       if (top_area_diff - node_area <= best.area_diff) continue;
       const Node& dst = bvh.nodes[top_sib];
+      nl++;
       float merged_area = half_area(uni(dst.box, box));
       float reinsert_area = top_area_diff - merged_area;
       if (reinsert_area > best.area_diff) {
@@ -592,11 +595,13 @@ int find_reinsertion(const Bvh2& bvh, uint32_t node_id, Reinsertion& out) {
     if (pivot_id != parent_id) {
       pivot_bbox = uni(pivot_bbox, bvh.nodes[sib].box);
       area_diff += half_area(bvh.nodes[pivot_id].box) - half_area(pivot_bbox);
+      nl += 2;
     }
     if (pivot_id == 0) break;
     sib = sibling(pivot_id);
     pivot_id = bvh.parents[pivot_id];
   }
+  if (loads) *loads += nl;
   if (best.to == sibling(best.from) || best.to == bvh.parents[best.from]) best = Reinsertion{0, 0, 0.0f};
   out = best;
   return 0;
@@ -637,6 +642,8 @@ inline uint32_t f32_radix_key(float f) {
 struct ReinsStats {
   uint64_t applied;
   uint64_t proposed;
+  uint64_t searched;    // find_reinsertion calls
+  uint64_t node_loads;  // node records those searches read
 };
 
 int reinsertion_run(Bvh2& bvh, float batch_size_ratio, const float* seq, size_t nseq, int nthreads,
@@ -678,10 +685,17 @@ int reinsertion_run(Bvh2& bvh, float batch_size_ratio, const float* seq, size_t 
     std::fill(touched.begin(), touched.end(), 0);
     found.assign(count, Reinsertion{0, 0, 0.0f});
     std::atomic<int> err{0};
+    std::atomic<uint64_t> loads{0};
     parallel_for(nthreads, count, [&](size_t b, size_t e) {
+      uint64_t nl = 0;
       for (size_t i = b; i < e; i++)
-        if (find_reinsertion(bvh, cand_ids[i], found[i]) != 0) err = 1;
+        if (find_reinsertion(bvh, cand_ids[i], found[i], &nl) != 0) err = 1;
+      loads += nl;
     });
+    if (rs) {
+      rs->searched += count;
+      rs->node_loads += loads.load();
+    }
     if (err) return -1;
     std::vector<Reinsertion> rl;
     for (size_t i = 0; i < count; i++)
@@ -2195,6 +2209,8 @@ void* orc_build_bvh2(const float* tris, const float* aabbs6, uint64_t n, const o
   if (!rc) rc = reinsertion_run(r->bvh2, p->reinsertion_batch_ratio * post_collapse_multiplier, nullptr, 0, nthreads,
                                 &second);
   r->reins_stats.applied += second.applied;
+  r->reins_stats.searched += second.searched;
+  r->reins_stats.node_loads += second.node_loads;
   if (status) *status = rc;
   return r;
 }
@@ -2339,6 +2355,12 @@ void orc_build_sizes(void* h, uint64_t* out8) {
   out8[5] = r->ploc_stats.sum_counts;
   out8[6] = r->reins_stats.applied;
   out8[7] = r->bvh2.max_depth;
+}
+// [reinsertion searches, node records they read] over the build.
+void orc_build_search_stats(void* h, uint64_t* out2) {
+  BuildResult* r = (BuildResult*)h;
+  out2[0] = r->reins_stats.searched;
+  out2[1] = r->reins_stats.node_loads;
 }
 void orc_build_times(void* h, double* out4) {
   BuildResult* r = (BuildResult*)h;

@@ -102,6 +102,7 @@ def _declare(L):
     L.orc_free.argtypes = [P]
     L.orc_build_sizes.argtypes = [P, P]
     L.orc_build_times.argtypes = [P, P]
+    L.orc_build_search_stats.argtypes = [P, P]
     L.orc_build_get_cwbvh.argtypes = [P, P, P]
     L.orc_build_get_bvh2.argtypes = [P, I32, P, P]
     L.orc_build_get_leaves.argtypes = [P, P, P, P, P]
@@ -343,6 +344,8 @@ class OracleBuild:
     reinsertions: int
     max_depth: int
     times_ms: np.ndarray
+    searches: int = 0       # reinsertion searches (find_reinsertion calls)
+    search_nodes: int = 0   # node records those searches read
 
 
 def build(tris=None, aabbs=None, params=None, nthreads=1, keep_intermediate=True) -> OracleBuild:
@@ -369,6 +372,8 @@ def build(tris=None, aabbs=None, params=None, nthreads=1, keep_intermediate=True
         L.orc_build_sizes(h, _p(sz))
         tm = np.zeros(4, np.float64)
         L.orc_build_times(h, _p(tm))
+        ss = np.zeros(2, np.uint64)
+        L.orc_build_search_stats(h, _p(ss))
         cwn = np.zeros((int(sz[0]), 80), np.uint8)
         cwp = np.zeros(int(sz[1]), np.uint32)
         L.orc_build_get_cwbvh(h, _p(cwn), _p(cwp))
@@ -386,7 +391,7 @@ def build(tris=None, aabbs=None, params=None, nthreads=1, keep_intermediate=True
             L.orc_build_get_bvh2(h, 0, _p(b2p), _p(bp))
             L.orc_build_get_leaves(h, _p(la), _p(li), _p(codes), _p(order))
         return OracleBuild(cwn, cwp, b2, b2p, bp, la, li, codes, order, int(sz[4]), int(sz[5]), int(sz[6]),
-                           int(sz[7]), tm)
+                           int(sz[7]), tm, int(ss[0]), int(ss[1]))
     finally:
         L.orc_free(h)
 
