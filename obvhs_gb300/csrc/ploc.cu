@@ -14,9 +14,12 @@
 // merge, whose children land at insert_base - 2(k+1).  The result is the
 // reference's tree bit for bit, given the same sorted leaves.
 //
-// While more than TAIL_MAX clusters are live, all passes run in one
-// cooperative launch (k_ploc_coop) separated by grid barriers; then one CTA
-// finishes every remaining pass with the clusters held in shared memory.
+// While many clusters are live, all passes run in one cooperative launch
+// (k_ploc_coop) separated by grid barriers; the last passes (from 16 x 2048
+// clusters, or 8 x 2048) run on one thread-block cluster with the clusters
+// held in the CTAs' shared memory (k_ploc_cluster), or, where no such cluster
+// can be placed or the GPU is shared, from TAIL_MAX clusters in one CTA
+// (k_ploc_tail).
 #include <cooperative_groups.h>
 
 #include <atomic>
@@ -438,6 +441,7 @@ struct PlocCoopArgs {
   uint32_t* status;
   const uint32_t* remap;  // partial rebuild: left slot of every merged pair (else null)
   int fast;               // the leaves were checked for NaN: pair_cost<true>
+  uint32_t stop_at;       // the loop ends once at most this many clusters are live
 };
 
 struct CoopGroupSmem {
@@ -649,7 +653,7 @@ __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs 
     const uint32_t pass = *(volatile uint32_t*)&a.st->passes;
     const int parity = (int)(pass & 1u);
     const uint32_t count = *(volatile uint32_t*)&a.st->count[parity];
-    if (count <= TAIL_MAX) break;
+    if (count <= a.stop_at) break;
     if (iter >= a.max_passes) {
       if (blockIdx.x == 0 && threadIdx.x == 0) set_status(a.status, ST_ITER_LIMIT);
       break;
@@ -1077,6 +1081,363 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
 }
 
 
+// --- the last passes on one thread-block cluster ------------------------------
+//
+// From CL_CAP x (cluster size) clusters down to the root, every pass runs in
+// one cluster of CTAs (16, or 8 where 16 cannot be placed) without leaving
+// shared memory.  The live clusters are split into contiguous slices, one per
+// active CTA (a CTA holds at most CL_CAP, and every slice has at least
+// CL_MIN_SLICE clusters, so a slice's +-2r neighbourhood lies in its two
+// neighbours' slices).  A pass: read the halo boxes from the neighbours'
+// shared memory, find the merge offsets of the slice and of r clusters on
+// each side (the same values the neighbours find for them), count the
+// slice's emitted and merged clusters, cluster barrier, take the prefix of
+// the earlier slices' counts from their shared memory, write the merged
+// pairs to the tree and every emitted cluster into the shared memory of the
+// CTA that owns its index in the next pass, cluster barrier.  Every CTA runs
+// the same passes (the counts it reads are the same everywhere), so the
+// cluster barriers always match.
+constexpr int CL_THREADS = 1024;
+constexpr int CL_CAP = 2048;          // clusters one CTA holds
+constexpr int CL_HALO = 64;           // 2 x the largest search radius
+constexpr int CL_STRIDE = CL_CAP + 2 * CL_HALO;  // words per array of a window
+constexpr uint32_t CL_MIN_SLICE = 128;  // >= CL_HALO
+constexpr int CL_IT = CL_CAP / CL_THREADS;       // slice clusters per thread
+
+struct ClusterArgs {
+  const Bvh2Node* buf0;
+  const Bvh2Node* buf1;
+  PlocState* st;
+  int radius;
+  uint32_t depth_threshold;
+  uint32_t max_passes;
+  Bvh2Node* out;
+  uint32_t* status;
+  const uint32_t* remap;
+  int fast;
+};
+
+// The window: eight word arrays of CL_STRIDE (as the tail's), the slice at
+// CL_HALO, halos before and after it.
+__device__ __forceinline__ Box wbox(const float* s, int j) {
+  return Box{make_float3(s[j], s[CL_STRIDE + j], s[2 * CL_STRIDE + j]),
+             make_float3(s[4 * CL_STRIDE + j], s[5 * CL_STRIDE + j], s[6 * CL_STRIDE + j])};
+}
+__device__ __forceinline__ void wget(const float* s, int j, float4& a, float4& b) {
+  a = make_float4(s[j], s[CL_STRIDE + j], s[2 * CL_STRIDE + j], s[3 * CL_STRIDE + j]);
+  b = make_float4(s[4 * CL_STRIDE + j], s[5 * CL_STRIDE + j], s[6 * CL_STRIDE + j], s[7 * CL_STRIDE + j]);
+}
+__device__ __forceinline__ void wput(float* s, int j, const float4& a, const float4& b) {
+  s[j] = a.x;
+  s[CL_STRIDE + j] = a.y;
+  s[2 * CL_STRIDE + j] = a.z;
+  s[3 * CL_STRIDE + j] = a.w;
+  s[4 * CL_STRIDE + j] = b.x;
+  s[5 * CL_STRIDE + j] = b.y;
+  s[6 * CL_STRIDE + j] = b.z;
+  s[7 * CL_STRIDE + j] = b.w;
+}
+// active CTAs and slice size for `count` live clusters
+__device__ __forceinline__ void cl_split(uint32_t count, uint32_t ncta, uint32_t& active, uint32_t& slice) {
+  active = min(ncta, max(1u, count / CL_MIN_SLICE));
+  slice = (count + active - 1) / active;
+}
+
+// Merge offsets of window clusters [lo, hi) (global indices) of a slice
+// starting at `base`; mrg is indexed from base - r.
+template <bool FAST>
+__device__ __forceinline__ void cl_search(const float* w, uint32_t base, uint32_t count, uint32_t lo, uint32_t hi,
+                                          int r, bool d1, int8_t* mrg) {
+  const int off = CL_HALO - (int)base;  // window position of global index j: j + off
+  for (uint32_t i = lo + threadIdx.x; i < hi; i += CL_THREADS) {
+    const Box me = wbox(w, (int)i + off);
+    int8_t m;
+    if (d1) {
+      if (i == count - 1) {
+        m = -1;
+      } else {
+        const float c = pair_cost<FAST>(me, wbox(w, (int)i + 1 + off));
+        const float last = i == 0 ? __int_as_float(0x7f800000) : pair_cost<FAST>(wbox(w, (int)i - 1 + off), me);
+        m = last < c ? -1 : 1;
+      }
+    } else {
+      const uint32_t begin = i >= (uint32_t)r ? i - r : 0;
+      const uint32_t end = min(i + r + 1, count);
+      uint32_t best = i;
+      float bc = __int_as_float(0x7f800000);
+      for (uint32_t j = begin; j < i; j++) {
+        const float c = pair_cost<FAST>(wbox(w, (int)j + off), me);
+        if (c <= bc) {
+          best = j;
+          bc = c;
+        }
+      }
+      for (uint32_t j = i + 1; j < end; j++) {
+        const float c = pair_cost<FAST>(me, wbox(w, (int)j + off));
+        if (c <= bc) {
+          best = j;
+          bc = c;
+        }
+      }
+      m = (int8_t)((int)best - (int)i);
+    }
+    mrg[i - (base - r)] = m;
+  }
+}
+
+__global__ void __launch_bounds__(CL_THREADS, 1) k_ploc_cluster(ClusterArgs a) {
+  grid_dep_wait();
+  cg::cluster_group cluster = cg::this_cluster();
+  const uint32_t ncta = cluster.num_blocks(), me = cluster.block_rank();
+  extern __shared__ float4 cl_smem[];
+  float* win[2];
+  win[0] = reinterpret_cast<float*>(cl_smem);
+  win[1] = win[0] + 8 * CL_STRIDE;
+  int8_t* mrg = reinterpret_cast<int8_t*>(win[1] + 8 * CL_STRIDE);  // CL_CAP + CL_HALO
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(mrg + CL_CAP + CL_HALO);  // (emitted, merged) of this slice
+  __shared__ uint32_t s_w[32];
+  __shared__ uint32_t s_pre[4];  // prefix emitted, prefix merged, total emitted, total merged
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  uint32_t pass = a.st->passes;
+  const int parity = (int)(pass & 1u);
+  uint32_t count = a.st->count[parity];
+  uint32_t insert = a.st->insert[parity];
+  if (count > (uint32_t)CL_CAP * ncta) {  // the passes before ended early (their error is set): every CTA leaves
+    if (me == 0 && tid == 0) set_status(a.status, ST_ITER_LIMIT);
+    return;
+  }
+  {
+    const Bvh2Node* src = parity ? a.buf1 : a.buf0;
+    uint32_t act, sl;
+    cl_split(count, ncta, act, sl);
+    const uint32_t base = me * sl;
+    const uint32_t len = me < act ? min(sl, count - base) : 0;
+    for (uint32_t j = tid; j < len; j += CL_THREADS) {
+      const float4* q = reinterpret_cast<const float4*>(&src[base + j]);
+      wput(win[0], CL_HALO + (int)j, q[0], q[1]);
+    }
+  }
+  cluster.sync();
+  int cur = 0;
+  uint64_t sum = 0;
+  for (uint32_t iters = 0; count > 1; iters++) {
+    if (iters >= a.max_passes) {
+      if (me == 0 && tid == 0) set_status(a.status, ST_ITER_LIMIT);
+      break;
+    }
+    const bool d1 = a.radius == 1 || pass < a.depth_threshold;
+    const int r = d1 ? 1 : a.radius;
+    uint32_t act, sl;
+    cl_split(count, ncta, act, sl);
+    const uint32_t base = me * sl;
+    const uint32_t len = me < act ? min(sl, count - base) : 0;
+    float* w = win[cur];
+    float* nw = win[cur ^ 1];
+    bool emit[CL_IT], ism[CL_IT];
+    uint32_t bst[CL_IT];
+    uint32_t e = 0, m = 0;
+    if (len) {
+      // halos: 2r clusters on each side from the neighbours' windows
+      const uint32_t h = 2u * (uint32_t)r;
+      if (me > 0) {
+        const float* lw = cluster.map_shared_rank(w, me - 1);
+        const uint32_t lb = (me - 1) * sl;  // the left neighbour's slice start
+        const uint32_t from = base >= h ? base - h : 0;
+        for (uint32_t j = from + tid; j < base; j += CL_THREADS) {
+          float4 qa, qb;
+          wget(lw, CL_HALO + (int)(j - lb), qa, qb);
+          wput(w, CL_HALO + (int)j - (int)base, qa, qb);
+        }
+      }
+      if (me + 1 < act) {
+        const float* rw = cluster.map_shared_rank(w, me + 1);
+        const uint32_t rb = base + len;  // the right neighbour's slice start
+        const uint32_t to = min(rb + h, count);
+        for (uint32_t j = rb + tid; j < to; j += CL_THREADS) {
+          float4 qa, qb;
+          wget(rw, CL_HALO + (int)(j - rb), qa, qb);
+          wput(w, CL_HALO + (int)(j - base), qa, qb);
+        }
+      }
+      __syncthreads();
+      // merge offsets of the slice and of r clusters on each side
+      const uint32_t lo = base >= (uint32_t)r ? base - r : 0;
+      const uint32_t hi = min(base + len + r, count);
+      if (a.fast)
+        cl_search<true>(w, base, count, lo, hi, r, d1, mrg);
+      else
+        cl_search<false>(w, base, count, lo, hi, r, d1, mrg);
+      __syncthreads();
+      // this slice's flags: thread tid owns clusters base + tid * CL_IT + k
+#pragma unroll
+      for (int k = 0; k < CL_IT; k++) {
+        const uint32_t li = (uint32_t)tid * CL_IT + k;
+        const uint32_t i = base + li;
+        emit[k] = ism[k] = false;
+        bst[k] = i;
+        if (li < len) {
+          const int off = mrg[i - (base - r)];
+          const uint32_t b = (uint32_t)((int)i + off);
+          const bool mutual = (int)b + (int)mrg[b - (base - r)] == (int)i;
+          emit[k] = !mutual || b < i;
+          ism[k] = mutual && b < i;
+          bst[k] = b;
+        }
+        e += emit[k];
+        m += ism[k];
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < CL_IT; k++) emit[k] = ism[k] = false;
+    }
+    // (emitted, merged) packed in 16 + 16 bits: a warp scan, then every warp
+    // scans the 32 warp totals itself
+    uint32_t x = e | (m << 16);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    uint32_t wt = s_w[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, wt, o);
+      if (lane >= o) wt += y;
+    }
+    const uint32_t wbefore = warp ? __shfl_sync(0xffffffffu, wt, (warp + 31) & 31) : 0u;
+    const uint32_t wtot = __shfl_sync(0xffffffffu, wt, 31);
+    if (tid == 0) {
+      cnt[0] = wtot & 0xffffu;
+      cnt[1] = wtot >> 16;
+    }
+    cluster.sync();  // every slice's counts are published
+    if (warp == 0) {
+      uint32_t ce = 0, cm = 0;
+      if ((uint32_t)lane < ncta) {
+        const uint32_t* rc = cluster.map_shared_rank(cnt, (unsigned)lane);
+        ce = rc[0];
+        cm = rc[1];
+      }
+      uint32_t pe = ce, pm = cm;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t ye = __shfl_up_sync(0xffffffffu, pe, o), ym = __shfl_up_sync(0xffffffffu, pm, o);
+        if (lane >= o) {
+          pe += ye;
+          pm += ym;
+        }
+      }
+      if ((uint32_t)lane == me) {
+        s_pre[0] = pe - ce;
+        s_pre[1] = pm - cm;
+      }
+      if (lane == 31) {
+        s_pre[2] = pe;
+        s_pre[3] = pm;
+      }
+    }
+    __syncthreads();
+    const uint32_t total_e = s_pre[2], total_m = s_pre[3];
+    uint32_t nact, nsl;
+    cl_split(total_e, ncta, nact, nsl);
+    uint32_t epos = s_pre[0] + (wbefore & 0xffffu) + (x & 0xffffu) - e;
+    uint32_t mpos = s_pre[1] + (wbefore >> 16) + (x >> 16) - m;
+#pragma unroll
+    for (int k = 0; k < CL_IT; k++) {
+      if (!emit[k]) continue;
+      const int wi = CL_HALO + (int)((uint32_t)tid * CL_IT + k);
+      float4 na, nb;
+      if (ism[k]) {
+        float4 la, lb, ra, rb;
+        wget(w, wi, la, lb);
+        wget(w, CL_HALO + (int)bst[k] - (int)base, ra, rb);
+        uint32_t ins = insert - 2 * (mpos + 1);
+        if (a.remap) ins = __ldg(&a.remap[(ins - 1) >> 1]);
+        float4* o = reinterpret_cast<float4*>(&a.out[ins]);
+        o[0] = la;
+        o[1] = lb;
+        o[2] = ra;
+        o[3] = rb;
+        const Box u = box_union(Box{make_float3(la.x, la.y, la.z), make_float3(lb.x, lb.y, lb.z)},
+                                Box{make_float3(ra.x, ra.y, ra.z), make_float3(rb.x, rb.y, rb.z)});
+        na = make_float4(u.mn.x, u.mn.y, u.mn.z, __uint_as_float(0u));
+        nb = make_float4(u.mx.x, u.mx.y, u.mx.z, __uint_as_float(ins));
+        mpos++;
+      } else {
+        wget(w, wi, na, nb);
+      }
+      // the cluster's slot in the next pass, in the CTA that owns it
+      const uint32_t dst = epos / nsl;
+      float* rw = cluster.map_shared_rank(nw, dst);
+      wput(rw, CL_HALO + (int)(epos - dst * nsl), na, nb);
+      epos++;
+    }
+    sum += count;
+    count = total_e;
+    insert -= 2 * total_m;
+    pass++;
+    cur ^= 1;
+    cluster.sync();  // the next pass's slices are complete
+  }
+  if (me == 0 && tid == 0) {
+    float4 ra, rb;
+    wget(win[cur], CL_HALO, ra, rb);
+    float4* o = reinterpret_cast<float4*>(&a.out[0]);
+    o[0] = ra;
+    o[1] = rb;
+    a.st->count[parity] = count;
+    a.st->insert[parity] = insert;
+    a.st->passes = pass;
+    a.st->sum_counts += sum;
+  }
+}
+
+constexpr size_t CL_SMEM = (size_t)2 * 8 * CL_STRIDE * sizeof(float) + CL_CAP + CL_HALO + 16;
+
+// Cluster size for k_ploc_cluster on the current device: 16 CTAs where such
+// a cluster can be placed, else 8, else 0 (the single-CTA tail).  Queried
+// once per device.
+int cluster_ctas() {
+  static std::atomic<int> cache[64];
+  static std::atomic<bool> init[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return 0;
+  }
+  if (init[dev].load()) return cache[dev].load();
+  int x = 0;
+  if (cudaFuncSetAttribute(k_ploc_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CL_SMEM) ==
+          cudaSuccess &&
+      cudaFuncSetAttribute(k_ploc_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+    for (int cl : {16, 8}) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)cl);
+      cfg.blockDim = dim3(CL_THREADS);
+      cfg.dynamicSmemBytes = CL_SMEM;
+      cudaLaunchAttribute at;
+      at.id = cudaLaunchAttributeClusterDimension;
+      at.val.clusterDim.x = (unsigned)cl;
+      at.val.clusterDim.y = 1;
+      at.val.clusterDim.z = 1;
+      cfg.attrs = &at;
+      cfg.numAttrs = 1;
+      int clusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&clusters, k_ploc_cluster, &cfg) == cudaSuccess && clusters >= 1) {
+        x = cl;
+        break;
+      }
+    }
+  }
+  cudaGetLastError();
+  cache[dev].store(x);
+  init[dev].store(true);
+  return x;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -1186,7 +1547,11 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   h0->insert[0] = 2 * n - 1;
   CK(cudaMemcpyAsync(st, h0, sizeof(PlocState), cudaMemcpyHostToDevice, c.stream));
   const uint32_t max_passes = 2 * n + 64;
-  if (n > TAIL_MAX) {
+  // the last passes: one thread-block cluster (16 or 8 CTAs) from
+  // CL_CAP x CTAs clusters down, else one CTA from TAIL_MAX down
+  const int cl_ctas = gpu_shared(c) ? 0 : cluster_ctas();
+  const uint32_t stop_at = cl_ctas ? (uint32_t)CL_CAP * cl_ctas : TAIL_MAX;
+  if (n > stop_at) {
     const size_t smem = COOP_GROUPS * sizeof(CoopGroupSmem);
     static std::atomic<int> coop_blocks_s{0};
     int coop_blocks = coop_blocks_s.load();
@@ -1198,7 +1563,7 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
       coop_blocks_s.store(coop_blocks);
     }
     PlocCoopArgs pa{{cur, nxt}, out_nodes, st, merge, tile_cnt, (int)radius, depth_threshold, max_passes, c.d_status,
-                    remap, nan_checked ? 1 : 0};
+                    remap, nan_checked ? 1 : 0, stop_at};
     void* args[] = {&pa};
     if (gpu_shared(c) && n <= SHARED_SINGLE_BLOCK_MAX) {
       // the GPU is shared with other builds or work: one block, a normal
@@ -1209,7 +1574,25 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
       KLAUNCH("k_ploc_coop", CK(coop_launch(c, (const void*)k_ploc_coop, coop_blocks, COOP_GROUPS * PT, args, smem)));
     }
   }
-  {
+  if (cl_ctas) {
+    ClusterArgs ca{cur, nxt, st, (int)radius, depth_threshold, max_passes, out_nodes, c.d_status, remap,
+                   nan_checked ? 1 : 0};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)cl_ctas);
+    cfg.blockDim = dim3(CL_THREADS);
+    cfg.dynamicSmemBytes = CL_SMEM;
+    cfg.stream = c.stream;
+    cudaLaunchAttribute at[2];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)cl_ctas;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl_enabled() ? 2 : 1;
+    KLAUNCH("k_ploc_cluster", CK(cudaLaunchKernelEx(&cfg, k_ploc_cluster, ca)));
+  } else {
     const size_t smem = (size_t)4 * TAIL_MAX * sizeof(float4) + TAIL_MAX + 64;
     KLAUNCH("k_ploc_tail", launch_k(k_ploc_tail, 1, TAIL_THREADS, smem, c.stream, cur, nxt, st, (int)radius, depth_threshold,
                                                                            max_passes, out_nodes, c.d_status, remap,
