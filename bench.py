@@ -132,6 +132,7 @@ ROOFLINE_NOTES = {
     "k_find": "branch-and-bound tree searches: each step a dependent node load (bytes: the node records the "
               "oracle's searches read on the same tree)",
     "k_ploc_coop": "compute in the nearest-neighbour search; clusters stay in L2",
+    "k_ploc_cluster": "the last passes in shared memory: cluster barriers and the search's latency",
     "k_costs": "bottom-up tree climb; bytes are a lower bound",
     "k_emit_all": "work queue over the tree; bytes are a lower bound",
 }
@@ -170,6 +171,9 @@ def kernel_byte_models(m, sum_counts, n_cw, n_prims, search_nodes=None):
         # every PLOC pass: box read twice, offset byte written and read twice,
         # compacted cluster written; every merged pair written once
         "k_ploc_coop": sum_counts * (32 + 32 + 1 + 2 + 32) + (nodes - 1) * 32,
+        # the last passes in shared memory: the clusters read once, the merged
+        # pairs of those passes written
+        "k_ploc_cluster": min(m, 32768) * 32 + 2 * min(m, 32768) * 32,
         # candidate id and result per search, 32 B per node record read
         "k_find": searched * (4 + 16) + (search_nodes if search_nodes is not None else searched * 3) * 32,
         # proposal read, conflict set written and read back
