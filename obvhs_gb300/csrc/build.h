@@ -65,6 +65,7 @@ enum ScratchSlot {
   SLOT_SEG_AABBS,
   SLOT_SEG_IDX,
   SLOT_MORTON_TOP,  // the Morton sort's high-digit keys (+ a flag word)
+  SLOT_CAND_HIST,   // the reinsertion candidate sorts' digit histograms (two areas)
   SLOT_COUNT
 };
 

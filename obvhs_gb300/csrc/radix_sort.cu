@@ -279,7 +279,8 @@ size_t radix_zero_words(uint32_t n, int digits) {
 
 template <class K>
 cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, bool init_iota, K* keys_alt,
-                             uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt, int digits, bool zeroed) {
+                             uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt, int digits, bool zeroed,
+                             const uint32_t* bases) {
   constexpr int NB = KeyTraits<K>::BYTES;
   const int nd = digits > 0 && digits < NB ? digits : NB;
   const bool small = n <= SMALL_SORT_MAX;
@@ -295,9 +296,13 @@ cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, 
     const uint32_t zb = (uint32_t)std::min<size_t>((quads + 255) / 256, cap);
     KLAUNCH("k_rs_zero", launch_k(k_rs_zero, zb, 256, 0, c.stream, reinterpret_cast<uint4*>(scratch), quads));
   }
-  const uint32_t hb = (n + THREADS * HIST_ITEMS - 1) / (THREADS * HIST_ITEMS);
-  // pass 0's header word 1 is the histogram kernel's ticket counter
-  KLAUNCH("k_rs_hist", launch_k(k_rs_hist<K>, hb, THREADS, 0, c.stream, keys, n, hist, nd, pass_area + 1));
+  if (bases) {
+    hist = const_cast<uint32_t*>(bases);
+  } else {
+    const uint32_t hb = (n + THREADS * HIST_ITEMS - 1) / (THREADS * HIST_ITEMS);
+    // pass 0's header word 1 is the histogram kernel's ticket counter
+    KLAUNCH("k_rs_hist", launch_k(k_rs_hist<K>, hb, THREADS, 0, c.stream, keys, n, hist, nd, pass_area + 1));
+  }
   K* kin = keys;
   uint32_t* vin = vals;
   K* kout = keys_alt;
@@ -328,11 +333,12 @@ cudaError_t fill_iota(uint32_t* v, uint32_t n, cudaStream_t s) {
 }
 
 template cudaError_t radix_sort_pairs<uint32_t>(obvhs_ctx&, uint32_t*, uint32_t*, uint32_t, bool, uint32_t*, uint32_t*,
-                                                uint32_t*, bool*, int, bool);
+                                                uint32_t*, bool*, int, bool, const uint32_t*);
 template cudaError_t radix_sort_pairs<unsigned long long>(obvhs_ctx&, unsigned long long*, uint32_t*, uint32_t, bool,
-                                                          unsigned long long*, uint32_t*, uint32_t*, bool*, int, bool);
+                                                          unsigned long long*, uint32_t*, uint32_t*, bool*, int, bool,
+                                                          const uint32_t*);
 template cudaError_t radix_sort_pairs<U128>(obvhs_ctx&, U128*, uint32_t*, uint32_t, bool, U128*, uint32_t*, uint32_t*,
-                                            bool*, int, bool);
+                                            bool*, int, bool, const uint32_t*);
 template size_t radix_zero_words<uint32_t>(uint32_t, int);
 template size_t radix_zero_words<unsigned long long>(uint32_t, int);
 template size_t radix_zero_words<U128>(uint32_t, int);

@@ -49,10 +49,13 @@ struct KeyTraits<U128> {
 // already zero (the kernel that produced the keys cleared them with
 // radix_zero), so the sort skips its own clearing launch.
 struct obvhs_ctx;
+// `bases` (optional): the digit bases (exclusive scans of the keys' digit
+// histograms, 256 words per digit) computed by the caller, so the sort skips
+// its histogram launch.
 template <class K>
 cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, bool init_iota, K* keys_alt,
                              uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt, int digits = 0,
-                             bool zeroed = false);
+                             bool zeroed = false, const uint32_t* bases = nullptr);
 template <class K>
 size_t radix_zero_words(uint32_t n, int digits = 0);
 

@@ -67,16 +67,67 @@ __device__ __forceinline__ uint32_t f32_radix_key(float f) {
   return (s >> 31) ? ~s : (s ^ 0x80000000u);
 }
 
-// Also clears the candidate sort's `zero_words` scratch words.
-__global__ void k_cand_keys(const Bvh2Node* __restrict__ nodes, uint32_t take, uint32_t* __restrict__ keys,
-                            uint32_t* __restrict__ vals, uint32_t* sort_scratch, size_t zero_words) {
+constexpr int CAND_PER_THREAD = 8;
+constexpr uint32_t CAND_HIST_WORDS = 4 * 256 + 32;  // four digit histograms + the ticket counter
+
+// find_candidates for one pass (src/bvh2/reinsertion.rs:121-139): the keys
+// of nodes [1, take) and their node ids, plus the candidate sort's histogram
+// pass: per-block digit counts added into `hist` (cleared by the previous
+// pass's launch), the last block turning them into digit bases.  Also clears
+// the sort's `zero_words` look-back words and the next pass's area
+// `hist_next`.
+__global__ void __launch_bounds__(BLK) k_cand_keys(const Bvh2Node* __restrict__ nodes, uint32_t take,
+                                                   uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                   uint32_t* sort_scratch, size_t zero_words, uint32_t* hist,
+                                                   uint32_t* hist_next) {
   grid_dep_wait();
-  radix_zero(sort_scratch, zero_words, blockIdx.x * (size_t)blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  if (i >= take) return;
-  Box b = node_box(ld_node(&nodes[i]));
-  keys[i - 1] = f32_radix_key(-half_area(b));
-  vals[i - 1] = i;
+  const size_t t = blockIdx.x * (size_t)BLK + threadIdx.x, stride = (size_t)gridDim.x * BLK;
+  radix_zero(sort_scratch, zero_words, t, stride);
+  for (size_t j = t; j < CAND_HIST_WORDS; j += stride) hist_next[j] = 0u;
+  __shared__ uint32_t h[4 * 256];
+  __shared__ uint32_t sw[BLK / 32];
+  __shared__ bool s_last;
+  for (int j = threadIdx.x; j < 4 * 256; j += BLK) h[j] = 0u;
+  __syncthreads();
+  const uint32_t b0 = blockIdx.x * (uint32_t)(BLK * CAND_PER_THREAD) + 1;
+#pragma unroll
+  for (int r = 0; r < CAND_PER_THREAD; r++) {
+    const uint32_t i = b0 + (uint32_t)(r * BLK) + threadIdx.x;
+    if (i < take) {
+      const uint32_t k = f32_radix_key(-half_area(node_box(ld_node(&nodes[i]))));
+      keys[i - 1] = k;
+      vals[i - 1] = i;
+#pragma unroll
+      for (int d = 0; d < 4; d++) atomicAdd(&h[d * 256 + ((k >> (8 * d)) & 0xffu)], 1u);
+    }
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < 4 * 256; j += BLK)
+    if (h[j]) atomicAdd(&hist[j], h[j]);
+  // release this block's counts, then take a ticket
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(&hist[4 * 256], 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int d = 0; d < 4; d++) {
+    uint32_t* hd = hist + d * 256;
+    const uint32_t v = __ldcg(&hd[threadIdx.x]);
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) sw[warp] = x;
+    __syncthreads();
+    uint32_t pre = 0;
+    for (int w = 0; w < warp; w++) pre += sw[w];
+    hd[threadIdx.x] = pre + x - v;
+    __syncthreads();
+  }
 }
 
 // find_reinsertion (src/bvh2/reinsertion.rs:233-334) for one candidate, as a
@@ -760,10 +811,15 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
   uint32_t* keys_alt = (uint32_t*)s.get(SLOT_KEYS_ALT, (size_t)len * 4);
   uint32_t* vals_alt = (uint32_t*)s.get(SLOT_VALS_ALT, (size_t)len * 4);
   uint32_t* rs = (uint32_t*)s.get(SLOT_ALL_HIST, radix_scratch_words(len) * 4);
-  if (!keys || !vals || !keys_alt || !vals_alt || !rs) return c.fail(OBVHS_ERR_OOM, "scratch");
+  uint32_t* chist = (uint32_t*)s.get(SLOT_CAND_HIST, 2 * CAND_HIST_WORDS * 4);
+  if (!keys || !vals || !keys_alt || !vals_alt || !rs || !chist) return c.fail(OBVHS_ERR_OOM, "scratch");
   ReinsBufs B;
   int r = reins_setup(c, b->nodes, len, nseq, B);
   if (r) return r;
+  // the candidate sorts' histogram areas: the first is cleared here, each
+  // sort's key launch clears the other for the next sort
+  CK(cudaMemsetAsync(chist, 0, 2 * CAND_HIST_WORDS * 4, c.stream));
+  uint32_t sorts = 0;
   const bool clamp = (size_t)b->max_depth * 2 <= 192;
   const uint32_t cap_rt = b->max_depth * 2;
   if (!clamp && cap_rt > 1024) return c.fail(OBVHS_ERR_LIMIT, "reinsertion stack bound above 1024 entries");
@@ -778,10 +834,13 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
     uint32_t count = node_count - 1;
     if (count == 0) continue;
     // find_candidates
-    KLAUNCH("k_cand_keys", launch_k(k_cand_keys, div_up<uint32_t>(ncand, BLK), BLK, 0, c.stream, b->nodes, take, keys, vals,
-                                    rs, radix_zero_words<uint32_t>(ncand)));
+    uint32_t* h = chist + (size_t)(sorts & 1u) * CAND_HIST_WORDS;
+    uint32_t* hn = chist + (size_t)((sorts + 1) & 1u) * CAND_HIST_WORDS;
+    sorts++;
+    KLAUNCH("k_cand_keys", launch_k(k_cand_keys, div_up<uint32_t>(ncand, BLK * CAND_PER_THREAD), BLK, 0, c.stream,
+                                    b->nodes, take, keys, vals, rs, radix_zero_words<uint32_t>(ncand), h, hn));
     bool alt = false;
-    cudaError_t e = radix_sort_pairs<uint32_t>(c, keys, vals, ncand, false, keys_alt, vals_alt, rs, &alt, 0, true);
+    cudaError_t e = radix_sort_pairs<uint32_t>(c, keys, vals, ncand, false, keys_alt, vals_alt, rs, &alt, 0, true, h);
     if (e) return c.cuda_fail(e, "candidate sort");
     // find_reinsertion for the first `count` candidates, then the rest of the pass
     r = reins_pass(c, b->nodes, len, alt ? vals_alt : vals, count, ri, clamp, cap_rt, StackModes{nullptr, nullptr, 0},
