@@ -62,6 +62,23 @@ def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
 
+def max_over_ranks(values, dist=None, device="cpu"):
+    """Each value's maximum over the ranks (the slowest replica's time); the
+    values themselves with one process."""
+    import torch
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def replica_rate(units, ms, world):
+    """Whole-job throughput of `world` replicas that each process `units` in
+    `ms` milliseconds (the slowest rank's time), in millions per second."""
+    return world * units / (ms * 1e-3) / 1e6 if ms > 0 else 0.0
+
+
 class ClockSampler:
     """nvidia-smi sampling during the timed region (clocks and throttle reasons)."""
 
@@ -624,19 +641,16 @@ def run_gb300(args):
     n = len(tris)
     mean_build = sum(build_ms) / len(build_ms)
     mean_e2e = sum(e2e_ms) / len(e2e_ms)
-    tot = torch.tensor([mean_build, mean_e2e, sum(prim_ms) / len(prim_ms), sum(bounce_ms) / len(bounce_ms)],
-                       dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(tot, op=dist.ReduceOp.MAX)
-    mean_build, mean_e2e, mean_prim, mean_bounce = tot.tolist()
+    mean_build, mean_e2e, mean_prim, mean_bounce = max_over_ranks(
+        [mean_build, mean_e2e, sum(prim_ms) / len(prim_ms), sum(bounce_ms) / len(bounce_ms)], dist, "cuda")
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
-    value = world * n / (mean_build * 1e-3) / 1e6
-    e2e = world * n / (mean_e2e * 1e-3) / 1e6
-    prim_rate = world * len(rays) / (mean_prim * 1e-3) / 1e6
-    bounce_rate = world * len(bounce) / (mean_bounce * 1e-3) / 1e6 if mean_bounce > 0 else 0.0
+    value = replica_rate(n, mean_build, world)
+    e2e = replica_rate(n, mean_e2e, world)
+    prim_rate = replica_rate(len(rays), mean_prim, world)
+    bounce_rate = replica_rate(len(bounce), mean_bounce, world)
 
     arch = None if args.no_arch_scene else arch_scene(ctx, stream, max(3, args.steps // 4), args.warmup, flush)
     batch = None if args.no_batched else batched_scenes(G, ctx, BvhBuildParams.medium_build())
