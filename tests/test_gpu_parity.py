@@ -6,6 +6,8 @@ CWBVH nodes and primitive indices, and closest-hit ids / t / occlusion
 flags.  The reference's own pins (prim 62, 65,536 plane hits, kitchen hash
 1343358762) are also run end to end on the GPU.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -405,3 +407,25 @@ def test_order_children_large_scene(G):
     cw.order_children(aabbs)
     on = O.cwbvh_order_children(cn, cp, aabbs)
     assert cw.download()[0].tobytes() == on.tobytes()
+
+
+def test_dependent_launches_off_gives_the_same_tree(G, tmp_path):
+    """OBVHS_PDL=0 (plain stream launches) builds the same bytes as the
+    default programmatic dependent launches (read once per process, so the
+    other form runs in a child process)."""
+    import subprocess
+    import sys
+
+    tris = S.scene2_tris(120_000)
+    p = BvhBuildParams.slow_build()
+    nodes, pidx = G.build_cwbvh_from_tris(tris, p).download()
+    np.save(tmp_path / "tris.npy", tris)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import sys, numpy as np; sys.path.insert(0, %r); import obvhs_gb300 as G; "
+            "from obvhs_gb300.params import BvhBuildParams as P; "
+            "n, i = G.build_cwbvh_from_tris(np.load(%r), P.slow_build()).download(); "
+            "np.save(%r, n); np.save(%r, i)") % (root, str(tmp_path / "tris.npy"), str(tmp_path / "n.npy"),
+                                                 str(tmp_path / "i.npy"))
+    env = dict(os.environ, OBVHS_PDL="0")
+    subprocess.run([sys.executable, "-c", code], env=env, check=True, timeout=300)
+    assert _eq(np.load(tmp_path / "n.npy"), nodes) and _eq(np.load(tmp_path / "i.npy"), pidx)
