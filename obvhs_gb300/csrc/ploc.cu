@@ -424,8 +424,9 @@ constexpr int BOXS = PCHUNK + 4 * 32;  // staged boxes per tile: the tile and a 
 //      tiles before it (a group reduction) plus a scan inside the tile; the
 //      tile writes next_nodes and the merged pairs, and the last tile stores
 //      the next count and insert index.
-// The loop ends once at most TAIL_MAX clusters are live; the single-CTA tail
-// kernel finishes.  Cluster buffers alternate by pass parity (passes & 1).
+// The loop ends once at most `stop_at` clusters are live (CL_CAP per CTA of
+// the cluster kernel, or TAIL_MAX for the single-CTA tail), and that kernel
+// finishes.  Cluster buffers alternate by pass parity (passes & 1).
 constexpr int COOP_GROUPS = 4;
 constexpr uint32_t SHARED_SINGLE_BLOCK_MAX = 262144;  // leaves: single-block PLOC when contexts share the GPU
 
