@@ -59,3 +59,17 @@ def test_one_process_needs_no_collective():
     import bench
 
     assert bench.max_over_ranks([3.0, 4.5]) == [3.0, 4.5]
+
+
+def test_search_kernel_bytes_follow_the_oracle_counts():
+    """The search kernel's algorithmic bytes use the oracle's node-record count
+    when given (32 B each), else three records per search."""
+    import bench
+
+    m = 100_000
+    sched = bench.reinsertion_schedule(2 * m - 1)
+    searched = sum(s for _, s in sched)
+    lower = bench.kernel_byte_models(m, 1_000_000, 10_000, m)["k_find"]
+    counted = bench.kernel_byte_models(m, 1_000_000, 10_000, m, search_nodes=searched * 46)["k_find"]
+    assert lower == searched * (4 + 16) + searched * 3 * 32
+    assert counted == searched * (4 + 16) + searched * 46 * 32
