@@ -37,7 +37,7 @@ namespace {
 
 constexpr int BLK = 256;
 constexpr int RESOLVE_THREADS = 1024;
-constexpr uint32_t RESOLVE_SINGLE_MAX = 8192;  // proposals searched: one block resolves the whole pass
+constexpr uint32_t RESOLVE_SINGLE_MAX = 40000;  // candidates searched: one block resolves the whole pass
 constexpr uint32_t RESOLVE_SMALL = 512;  // proposals one block resolves faster than the grid (one climb per thread)
 
 struct Reins {
