@@ -1,23 +1,33 @@
 #!/usr/bin/env python
-"""Benchmark of the BVH hot path on the 1M-triangle clustered scene.
+"""Benchmark of the BVH hot path; headline = the 8M-triangle architectural scene.
 
-Workload (one "step"): build_cwbvh_from_tris on 1,000,000 triangles in 64
-Gaussian clusters with the slow_build preset (pre-splits, PLOC radius 24 with
-distance 1 for 2 passes, reinsertion ratio 0.2, U128 Morton keys, 3 primitives
-per leaf), plus, timed separately, closest-hit traversal of the 1920x1080
-primary rays and of one cosine-weighted bounce ray per primary hit.
+Workload of one "step" (the headline): build_cwbvh_from_tris on 8,000,000
+triangles of the architectural scene (40% from 200 tessellated axis-aligned
+quads, 60% small clutter in a 20x6x20 box) with PLOC radius 14, distance 1 for
+the first 3 passes, U64 Morton keys, no pre-splits or reinsertion, CWBVH8 with
+at most 3 primitives per leaf (the medium_build PLOC settings of
+src/lib.rs:270-281 through src/cwbvh/builder.rs:20-85).
 
-  value       build throughput, Mtris/s, triangles already in HBM
-  e2e         the same build through the public API from pinned host
-              triangles, host->device copy and the CWBVH download included
-  traversal   Mrays/s of the primary and bounce batches (device-resident rays)
-  roofline    the build's dominant kernel against the measured HBM peak
-              (also the whole build, and the primary traversal kernel)
-  cpu_baseline the C++ restatement of the reference (oracle) on all host cores
+  value        build throughput, Mtris/s, triangles already in HBM
+  e2e          the same build through the public API from pinned host
+               triangles: host->device copy and the CWBVH download included
+  roofline     the headline build's dominant kernel against the measured HBM
+               peak (algorithmic bytes per launch / event-timed launch time)
+  cpu_baseline the C++ restatement of the reference (oracle) building the same
+               8M scene on all host cores, and on 1 thread
+  c3_*         16M incoherent closest-hit rays and 16M shadow rays on that tree
+  c2_*         the 1M-triangle clustered scene with slow_build (pre-splits,
+               radius 24, reinsertion 0.2, U128): build, e2e, 1920x1080
+               primary rays and one cosine bounce per hit
+  c1_*         10k triangles, PLOC radius 16 (build_ploc::<16>), 256x256 rays
+  c4_*         512 scenes of 1k-200k triangles: one segmented build + one
+               multi-BVH traversal vs a build and a traversal call per scene
+  c5_*         the serving loop vs one request per call (Poisson 2,000/s)
 
---impl reference runs that CPU restatement of the reference's algorithm (the
-Rust crate itself cannot be built on these machines) on the same workload.
+--impl reference runs the CPU restatement of the reference's algorithm (the
+Rust crate itself cannot be built on these machines) on the headline workload.
 Multi-GPU: every rank builds its own replica (the path does not shard).
+--detail PATH writes every measured figure to a JSON file as well.
 """
 from __future__ import annotations
 
@@ -28,7 +38,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np
@@ -37,25 +46,27 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "PLOC build Mtris/s; CWBVH Mrays/s closest-hit; served p50/p99 latency"
-WORKLOAD = "clustered-1M-slow_build"
-N_TRIS = 1_000_000
+WORKLOAD = "architectural-8M: PLOC r14 (distance 1 for 3 passes), U64 -> CWBVH8"
+N_TRIS = 8_000_000
+N_RAYS = 16_000_000
 L2_FLUSH_BYTES = 512 << 20
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--tris", type=int, default=N_TRIS)
-    ap.add_argument("--no-serving", action="store_true",
-                    help="skip the serving run (Poisson request stream, resident BVHs, continuous batching)")
-    ap.add_argument("--no-batched", action="store_true",
-                    help="skip the 512-scene batched build + traversal comparison")
-    ap.add_argument("--no-arch-scene", action="store_true",
-                    help="skip the 8M-triangle architectural scene (build + 16M incoherent + 16M shadow rays)")
-    return ap.parse_args()
+    ap.add_argument("--tris", type=int, default=N_TRIS, help="headline scene size")
+    ap.add_argument("--rays", type=int, default=N_RAYS, help="headline ray batch size (each kind)")
+    ap.add_argument("--only", default="all", choices=["all", "c3", "c3-build", "c2", "c2-build", "c1"],
+                    help="run one workload only (profiling); the JSON line then carries that workload")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving comparison (config 5)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 512-scene batched comparison (config 4)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--detail", default="", help="also write every figure to this JSON file")
+    return ap.parse_args(argv)
 
 
 def dist_info():
@@ -77,6 +88,13 @@ def replica_rate(units, ms, world):
     """Whole-job throughput of `world` replicas that each process `units` in
     `ms` milliseconds (the slowest rank's time), in millions per second."""
     return world * units / (ms * 1e-3) / 1e6 if ms > 0 else 0.0
+
+
+def r4(x):
+    """Four significant digits (keeps the JSON line short)."""
+    if x is None or isinstance(x, (bool, int, str)):
+        return x
+    return float(f"{x:.4g}")
 
 
 class ClockSampler:
@@ -142,16 +160,26 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
+def traffic_record(workload_key, kernel):
+    """DRAM bytes per launch of `kernel` from an earlier ncu capture
+    (profiles/traffic.json: workload -> kernel -> {bytes, commit, ...}), or
+    None.  The figure is not measured by this run."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    rec = json.load(open(path)).get(workload_key, {}).get(kernel)
+    return rec if isinstance(rec, dict) else None
+
+
 ROOFLINE_NOTES = {
-    "k_rs_pass": "radix sort passes of 0.03-1M keys: each pass is one wave of tiles whose ranking, "
-                 "decoupled look-back and scatter phases are latency-bound",
+    "k_rs_pass": "radix sort passes: each pass is one wave of tiles whose ranking, look-back and scatter "
+                 "phases are latency-bound",
     "k_resolve": "dependent rounds and tree climbs; bytes are a lower bound",
-    "k_find": "branch-and-bound tree searches: each step a dependent node load (bytes: the node records the "
-              "oracle's searches read on the same tree)",
-    "k_ploc_coop": "compute in the nearest-neighbour search; clusters stay in L2",
+    "k_find": "branch-and-bound tree searches: each step a dependent node load",
+    "k_ploc_coop": "nearest-neighbour search compute; clusters stay in L2",
     "k_ploc_cluster": "the last passes in shared memory: cluster barriers and the search's latency",
-    "k_costs": "bottom-up tree climb; bytes are a lower bound",
-    "k_emit_all": "work queue over the tree; bytes are a lower bound",
+    "k_costs": "bottom-up climb: one dependent hand-off per level",
+    "k_emit_all": "work queue over the tree: a node waits for its parent",
 }
 
 
@@ -159,6 +187,8 @@ def reinsertion_schedule(n_nodes, ratio=0.2):
     """(candidates, searched) per reinsertion pass, as the reference's
     optimize_impl sizes them (src/bvh2/reinsertion.rs:101-115)."""
     out = []
+    if ratio <= 0:
+        return out
     for k in range(16):
         batch = max(int(np.float32(np.float32(n_nodes) * np.float32(ratio)) * np.float32(1.0 / (2 * k + 1))), 1)
         node_count = min(n_nodes, batch + 1)
@@ -167,7 +197,13 @@ def reinsertion_schedule(n_nodes, ratio=0.2):
     return out
 
 
-def kernel_byte_models(m, sum_counts, n_cw, n_prims, search_nodes=None):
+#: cost-record bytes per BVH2 node written by the cost pass and read by the
+#: emission: the reference's 7 decisions of 8 bytes
+#: (src/cwbvh/bvh2_to_cwbvh.rs:479-484), whatever record the kernels use
+DEC_BYTES = 56
+
+
+def kernel_byte_models(m, sum_counts, n_cw, n_prims, search_nodes=None, ratio=0.2, precision=1):
     """Algorithmic bytes of one build, per kernel (totals over its launches).
 
     Minimum bytes each kernel must move for its result, from the per-unit
@@ -175,132 +211,310 @@ def kernel_byte_models(m, sum_counts, n_cw, n_prims, search_nodes=None):
     records the oracle counts for the same build (`search_nodes`, the same
     searches on the same tree); the other pointer-chasing kernels (k_resolve,
     k_costs, k_emit_all) also read tree nodes along their walks, which is not
-    counted (a lower bound)."""
+    counted (a lower bound).  `precision` 1 = U128 Morton keys (the high 64
+    bits sorted: 8 passes of 8 B keys), 0 = U64 (bits 24-63: 5 passes)."""
     nodes = 2 * m - 1
-    sched = reinsertion_schedule(nodes)
+    sched = reinsertion_schedule(nodes, ratio)
     cand_sort = sum(4 * c * 16 for c, _ in sched) + sum(c * 4 for c, _ in sched)
     searched = sum(s_ for _, s_ in sched)
-    return {
-        # Morton sort on the high 64 bits (8 passes of 8-bit digits over key
-        # 8 B + value 4 B, read and written) and the 16 candidate sorts (u32
-        # key + value)
-        "k_rs_pass": 8 * m * 24 + cand_sort,
+    sort_passes = 8 if precision else 5
+    out = {
+        # Morton sort on the high digits (key 8 B + value 4 B, read and
+        # written per pass) and the reinsertion candidate sorts (u32 key + value)
+        "k_rs_pass": sort_passes * m * 24 + cand_sort,
         # every PLOC pass: box read twice, offset byte written and read twice,
         # compacted cluster written; every merged pair written once
         "k_ploc_coop": sum_counts * (32 + 32 + 1 + 2 + 32) + (nodes - 1) * 32,
         # the last passes in shared memory: the clusters read once, the merged
         # pairs of those passes written
         "k_ploc_cluster": min(m, 32768) * 32 + 2 * min(m, 32768) * 32,
-        # candidate id and result per search, 32 B per node record read
-        "k_find": searched * (4 + 16) + (search_nodes if search_nodes is not None else searched * 3) * 32,
-        # proposal read, conflict set written and read back
-        "k_resolve": sum(s_ * (16 + 32 + 32) for _, s_ in sched),
-        # node + parent read, cost record (96 B) written, children records read
-        "k_costs": nodes * (32 + 4 + 96) + (m - 1) * 2 * 96,
+        # node + parent read, cost record written, children's records read
+        "k_costs": nodes * (32 + 4 + DEC_BYTES) + (m - 1) * 2 * DEC_BYTES,
         # 80 B node and primitive indices written, each BVH2 node and record read
-        "k_emit_all": n_cw * 80 + n_prims * 4 + nodes * (32 + 96),
-        "k_morton128": m * (32 + 16),
+        "k_emit_all": n_cw * 80 + n_prims * 4 + nodes * (32 + DEC_BYTES),
+        ("k_morton128" if precision else "k_morton64"): m * (32 + (16 if precision else 8) + 4),
         "k_gather": m * (4 + 32 + 32),
         "k_leaves_from_tris": m * (36 + 32),
         "k_reorder_tris": n_prims * (4 + 36 + 64),
     }
+    if searched:
+        # candidate id and result per search, 32 B per node record read
+        out["k_find"] = searched * (4 + 16) + (search_nodes if search_nodes is not None else searched * 3) * 32
+        # proposal read, conflict set written and read back
+        out["k_resolve"] = sum(s_ * (16 + 32 + 32) for _, s_ in sched)
+    return out
 
 
-def build_byte_model(m, n_tris, sum_counts, n_cw, n_prims):
+def build_byte_model(m, n_tris, sum_counts, n_cw, n_prims, ratio=0.2, precision=1):
     """Whole-build algorithmic bytes: triangle read, AABB write and read, Morton
-    key + value, 16 sort passes, PLOC, reinsertion sorts and proposals, CWBVH
+    key + value, sort passes, PLOC, reinsertion sorts and proposals, CWBVH
     costs and nodes (the per-primitive byte model of the path)."""
-    k = kernel_byte_models(m, sum_counts, n_cw, n_prims)
+    k = kernel_byte_models(m, sum_counts, n_cw, n_prims, ratio=ratio, precision=precision)
     return n_tris * 36 + m * (24 + 24) + sum(k.values())
 
 
-def arch_scene(ctx, stream, steps, warmup, flush):
-    """The 8M-triangle architectural scene: PLOC (radius 14, distance 1 for 3
-    passes, U64) -> CWBVH build, then 16M incoherent closest-hit rays and 16M
-    shadow rays to 4 point lights, all device-resident, CUDA-event timed."""
-    import ctypes
-    import torch
-    import obvhs_gb300 as G
+def dominant_kernel(kernel_profile, models):
+    """The build kernel with the largest share of event-timed device time that
+    has a byte model: (name, launches, total_ms, share)."""
+    build_kernels = {}
+    for k, v in kernel_profile.items():
+        if k.startswith("k_traverse"):
+            continue
+        k = "k_find" if k.startswith("k_find") else k  # one search kernel, two launch forms
+        a = build_kernels.setdefault(k, {"launches": 0, "total_ms": 0.0})
+        a["launches"] += v["launches"]
+        a["total_ms"] += v["total_ms"]
+    total = sum(v["total_ms"] for v in build_kernels.values())
+    ranked = sorted(build_kernels.items(), key=lambda kv: -kv[1]["total_ms"])
+    name, d = next(((k, v) for k, v in ranked if models.get(k)), ranked[0])
+    return name, d["launches"], d["total_ms"], (d["total_ms"] / total if total else None)
+
+
+class Bench:
+    """Shared state of one GPU arm run: context, its stream, the L2 flush."""
+
+    def __init__(self, args):
+        import torch
+
+        self.args = args
+        self.rank, self.local_rank, self.world = dist_info()
+        torch.cuda.set_device(self.local_rank)
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("nccl", device_id=torch.device("cuda", self.local_rank))
+            self.dist = dist
+        import obvhs_gb300 as G
+
+        self.G = G
+        self.torch = torch
+        self.ctx = G.Context(self.local_rank)
+        self.stream = torch.cuda.ExternalStream(self.ctx.stream, device=torch.device("cuda", self.local_rank))
+        self.flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def barrier(self):
+        self.torch.cuda.synchronize()
+        if self.dist:
+            self.dist.barrier()
+
+    def timed(self, fn, steps):
+        """Runs fn() `steps` times; each call is bracketed by CUDA events on the
+        library's stream and followed (outside the timing) by an L2 flush."""
+        torch = self.torch
+        ms = []
+        for _ in range(steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(self.stream)
+            fn()
+            e1.record(self.stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            self.flush.fill_(1.0)
+            torch.cuda.synchronize()
+        return ms
+
+    def trace_fn(self, cw, rays, out, kind):
+        import ctypes
+
+        lib, ctx = self.ctx.lib, self.ctx
+        fn = {"closest": lib.obvhs_ray_traverse, "miss": lib.obvhs_ray_traverse_miss,
+              "closest_ctri": lib.obvhs_ray_traverse_compressed}[kind]
+
+        def run():
+            ctx.check(fn(ctx.h, cw.h, ctypes.c_void_p(rays.data_ptr()), rays.shape[0],
+                         ctypes.c_void_p(out.data_ptr()), 1))
+        return run
+
+    def e2e(self, tris_np, params, n_nodes, n_prims, steps, warmup):
+        """The build through the public API from pinned host triangles, the
+        CWBVH nodes and primitive indices downloaded into pinned host buffers;
+        wall clock per step with the device idle on both sides."""
+        import ctypes
+
+        torch = self.torch
+        h_tris = torch.from_numpy(tris_np).pin_memory().numpy()
+        h_nodes = torch.empty((n_nodes, 80), dtype=torch.uint8).pin_memory().numpy()
+        h_prims = torch.empty((n_prims,), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+        ms = []
+        for i in range(warmup + steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b = self.G.build_cwbvh_from_tris(h_tris, params, ctx=self.ctx)
+            self.ctx.check(self.ctx.lib.obvhs_cwbvh_download(self.ctx.h, b.h, h_nodes.ctypes.data_as(ctypes.c_void_p),
+                                                             h_prims.ctypes.data_as(ctypes.c_void_p)))
+            dt = (time.perf_counter() - t0) * 1e3
+            if i >= warmup:
+                ms.append(dt)
+            self.flush.fill_(1.0)
+            torch.cuda.synchronize()
+            del b
+        return sum(ms) / len(ms), len(tris_np) * 36, n_nodes * 80 + n_prims * 4
+
+    def profile_build(self, d_tris, params):
+        """Per-kernel device time of one build (events around every launch on
+        the library's stream; not part of the timings)."""
+        self.ctx.set_profiling(True)
+        b = self.G.build_cwbvh_from_tris(d_tris, params, ctx=self.ctx)
+        self.ctx.synchronize()
+        prof = self.ctx.profile_report()
+        self.ctx.set_profiling(False)
+        del b
+        return prof
+
+
+def config3(B: Bench, only_build=False):
+    """The headline: the 8M architectural scene built PLOC -> CWBVH8, then 16M
+    incoherent closest-hit and 16M shadow rays on the tree (device-resident)."""
     from obvhs_gb300 import scenes as S
     from obvhs_gb300.params import BvhBuildParams
 
-    tris = S.scene3_tris(8_000_000)
-    closest, shadow = S.scene3_rays(16_000_000)
-    d = torch.from_numpy(tris).cuda()
-    dc, ds = torch.from_numpy(closest).cuda(), torch.from_numpy(shadow).cuda()
-    plain = BvhBuildParams(False, 14, 3, 0.0, 0.0, 0, 3, 3.0)
-
-    def timed(fn, k):
-        ms = []
-        for _ in range(k):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            fn()
-            e1.record(stream)
-            e1.synchronize()
-            ms.append(e0.elapsed_time(e1))
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-        return sum(ms) / len(ms)
-
+    torch, G, args = B.torch, B.G, B.args
+    p = BvhBuildParams(False, 14, 3, 0.0, 0.0, 0, 3, 3.0)
+    tris = S.scene3_tris(args.tris)
+    d_tris = torch.from_numpy(tris).cuda()
     holder = {}
 
-    def build(p):
-        holder["cw"] = G.build_cwbvh_from_tris(d, p, ctx=ctx)
+    def build():
+        holder["cw"] = G.build_cwbvh_from_tris(d_tris, p, ctx=B.ctx)
 
-    for _ in range(warmup):
-        build(plain)
-    plain_ms = timed(lambda: build(plain), steps)
-    medium = BvhBuildParams.medium_build()
-    for _ in range(warmup):
-        build(medium)
-    medium_ms = timed(lambda: build(medium), steps)
-    build(plain)
+    for _ in range(args.warmup):
+        build()
+    B.barrier()
+    clocks = ClockSampler(B.local_rank).start() if B.rank == 0 else None
+    l0 = B.ctx.kernel_launches
+    t_wall0 = time.perf_counter()
+    build_ms = B.timed(build, args.steps)
+    B.barrier()
+    t_wall = time.perf_counter() - t_wall0
+    launches = (B.ctx.kernel_launches - l0) // max(args.steps, 1)
     cw = holder["cw"]
-    out = torch.empty((len(closest), 2), dtype=torch.int32, device="cuda")
+    stats = cw.stats
+    n_nodes, n_prims, _ = cw.info()
+    out = {"tris": tris, "params": p, "build_ms": build_ms, "launches": launches, "stats": stats,
+           "n_nodes": n_nodes, "n_prims": n_prims, "wall_s": t_wall, "clocks": None}
+    if only_build:
+        out["clocks"] = clocks.stop() if clocks else None
+        return out
+
+    closest, shadow = S.scene3_rays(args.rays)
+    dc, ds = torch.from_numpy(closest).cuda(), torch.from_numpy(shadow).cuda()
+    hits = torch.empty((len(closest), 2), dtype=torch.int32, device="cuda")
     miss = torch.empty((len(shadow),), dtype=torch.uint8, device="cuda")
-    lib = ctx.lib
+    cw.set_triangles_compressed(d_tris)
+    fc = B.trace_fn(cw, dc, hits, "closest")
+    fs = B.trace_fn(cw, ds, miss, "miss")
+    fcc = B.trace_fn(cw, dc, hits, "closest_ctri")
+    for _ in range(args.warmup):
+        fc(), fs(), fcc()
+    B.barrier()
+    tsteps = max(3, args.steps // 2)
+    out["closest_ms"] = B.timed(fc, tsteps)
+    out["shadow_ms"] = B.timed(fs, tsteps)
+    out["closest_ctri_ms"] = B.timed(fcc, tsteps)
+    out["clocks"] = clocks.stop() if clocks else None
+    fc()
+    torch.cuda.synchronize()
+    out["hit_fraction"] = float((hits[:, 0] != -1).float().mean().item())
+    out["occluded_fraction"] = float((miss == 0).float().mean().item())
+    out["n_closest"], out["n_shadow"] = len(closest), len(shadow)
+    out["closest_sample"] = closest[:1_000_000]
+    out["cw"] = cw
+    del dc, ds
+    out["profile"] = B.profile_build(d_tris, p)
+    out["e2e_ms"], out["h2d"], out["d2h"] = B.e2e(tris, p, n_nodes, n_prims, args.steps, args.warmup)
+    return out
 
-    def trace():
-        ctx.check(lib.obvhs_ray_traverse(ctx.h, cw.h, ctypes.c_void_p(dc.data_ptr()), len(closest),
-                                         ctypes.c_void_p(out.data_ptr()), 1))
 
-    def occlude():
-        ctx.check(lib.obvhs_ray_traverse_miss(ctx.h, cw.h, ctypes.c_void_p(ds.data_ptr()), len(shadow),
-                                              ctypes.c_void_p(miss.data_ptr()), 1))
+def config2(B: Bench, only_build=False):
+    """The 1M clustered scene with slow_build; primary rays of a pinhole that
+    frames the densest cluster, one cosine bounce per hit."""
+    from obvhs_gb300 import scenes as S
+    from obvhs_gb300.params import BvhBuildParams
 
-    def trace_ctri():
-        ctx.check(lib.obvhs_ray_traverse_compressed(ctx.h, cw.h, ctypes.c_void_p(dc.data_ptr()), len(closest),
-                                                    ctypes.c_void_p(out.data_ptr()), 1))
+    torch, G, args = B.torch, B.G, B.args
+    p = BvhBuildParams.slow_build()
+    tris, rays = S.scene2_tris(1_000_000), S.scene2_primary_rays()
+    d_tris = torch.from_numpy(tris).cuda()
+    holder = {}
 
-    cw.set_triangles_compressed(d)
-    for _ in range(warmup):
-        trace()
-        occlude()
-        trace_ctri()
-    cc_ms = timed(trace_ctri, steps)
-    c_ms = timed(trace, steps)
-    s_ms = timed(occlude, steps)
-    n = len(tris)
-    return {"workload": "architectural-8M: 200 tessellated quads + clutter, 16M incoherent + 16M shadow rays",
-            "n_tris": n, "build_plain_ms": plain_ms, "build_plain_mtris_s": n / (plain_ms * 1e-3) / 1e6,
-            "build_plain": "PLOC radius 14, distance-1 for 3 passes, U64 -> CWBVH (3 prims/leaf)",
-            "build_medium_build_ms": medium_ms, "build_medium_build_mtris_s": n / (medium_ms * 1e-3) / 1e6,
-            "incoherent_closest_mrays_s": len(closest) / (c_ms * 1e-3) / 1e6, "incoherent_closest_ms": c_ms,
-            "shadow_any_hit_mrays_s": len(shadow) / (s_ms * 1e-3) / 1e6, "shadow_any_hit_ms": s_ms,
-            "incoherent_closest_compressed_tris_mrays_s": len(closest) / (cc_ms * 1e-3) / 1e6,
-            "hit_fraction": float((out[:, 0] != -1).float().mean().item())}
+    def build():
+        holder["cw"] = G.build_cwbvh_from_tris(d_tris, p, ctx=B.ctx)
+
+    for _ in range(args.warmup):
+        build()
+    B.barrier()
+    l0 = B.ctx.kernel_launches
+    build_ms = B.timed(build, args.steps)
+    launches = (B.ctx.kernel_launches - l0) // max(args.steps, 1)
+    cw = holder["cw"]
+    stats = cw.stats
+    n_nodes, n_prims, _ = cw.info()
+    out = {"build_ms": build_ms, "launches": launches, "stats": stats, "n_nodes": n_nodes, "n_prims": n_prims}
+    out["profile"] = B.profile_build(d_tris, p)
+    if only_build:
+        return out
+    pid, pt = cw.ray_traverse(rays)
+    bounce = S.bounce_rays(tris, rays, pid, pt)
+    d_rays, d_bounce = torch.from_numpy(rays).cuda(), torch.from_numpy(bounce).cuda()
+    out_p = torch.empty((len(rays), 2), dtype=torch.int32, device="cuda")
+    out_b = torch.empty((max(len(bounce), 1), 2), dtype=torch.int32, device="cuda")
+    fp = B.trace_fn(cw, d_rays, out_p, "closest")
+    fb = B.trace_fn(cw, d_bounce, out_b, "closest")
+    for _ in range(args.warmup):
+        fp(), fb()
+    B.barrier()
+    out["primary_ms"] = B.timed(fp, args.steps)
+    out["bounce_ms"] = B.timed(fb, args.steps)
+    fb()
+    torch.cuda.synchronize()
+    out["n_primary"], out["n_bounce"] = len(rays), len(bounce)
+    out["primary_hit_fraction"] = float((pid != 0xFFFFFFFF).mean())
+    out["bounce_hit_fraction"] = float((out_b[:len(bounce), 0] != -1).float().mean().item())
+    out["e2e_ms"], _, _ = B.e2e(tris, p, n_nodes, n_prims, args.steps, args.warmup)
+    return out
+
+
+def config1(B: Bench):
+    """10k triangles, PLOC radius 16 (build_ploc::<16>, distance 1 never, U64)
+    -> CWBVH (3 prims per leaf), 256x256 pinhole rays from (0,0,-3)."""
+    from obvhs_gb300 import scenes as S
+    from obvhs_gb300.params import BvhBuildParams
+
+    torch, G, args = B.torch, B.G, B.args
+    p = BvhBuildParams(False, 16, 0, 0.0, 0.0, 0, 3, 3.0)
+    tris, rays = S.scene1()
+    d_tris = torch.from_numpy(tris).cuda()
+    holder = {}
+
+    def build():
+        holder["cw"] = G.build_cwbvh_from_tris(d_tris, p, ctx=B.ctx)
+
+    for _ in range(args.warmup):
+        build()
+    build_ms = B.timed(build, args.steps)
+    cw = holder["cw"]
+    d_rays = torch.from_numpy(rays).cuda()
+    hits = torch.empty((len(rays), 2), dtype=torch.int32, device="cuda")
+    fc = B.trace_fn(cw, d_rays, hits, "closest")
+    for _ in range(args.warmup):
+        fc()
+    ray_ms = B.timed(fc, args.steps)
+    torch.cuda.synchronize()
+    return {"build_ms": build_ms, "ray_ms": ray_ms, "n_tris": len(tris), "n_rays": len(rays),
+            "hit_fraction": float((hits[:, 0] != -1).float().mean().item())}
 
 
 def batched_scenes(G, ctx, base, n_scenes=512, seed=1004):
     """512 clustered scenes, triangle counts log-uniform over 1k-200k (scene i
     from the clustered generator with seed offset i), each with 4,096-262,144
-    incoherent rays in proportion to its size.  The PLOC search radius comes
-    from the autotuner (segmented build + multi-BVH traversal of a 64-scene
-    sample, radius 8 / 14 / 24).  Plain: every scene built and traced in its
-    own calls.  Batched: one segmented build of all scenes, then one multi-BVH
-    traversal launch.  Device-resident inputs; wall clock with the device
-    synchronised; hit ids and t compared between the two forms."""
+    incoherent rays in proportion to its size.  The PLOC search radius, the
+    traversal block size and stack depth come from the autotuner (a 64-scene
+    sample).  Plain: every scene built and traced in its own calls.  Batched:
+    one segmented build of all scenes, then one multi-BVH traversal launch.
+    Device-resident inputs; wall clock with the device synchronised; hit ids
+    and t compared between the two forms."""
     import torch
     from obvhs_gb300 import autotune as A
     from obvhs_gb300 import scenes as S
@@ -329,6 +543,9 @@ def batched_scenes(G, ctx, base, n_scenes=512, seed=1004):
     s_rays = torch.cat([d_rays[i] for i in pick])
     s_owner = torch.from_numpy(np.concatenate([np.full(len(rays[i]), j, np.int32) for j, i in enumerate(pick)])).cuda()
     p, tune = A.tune_segmented([tris[i] for i in pick], s_rays, s_owner, base, ctx=ctx)
+    trav = tune.get("traversal")
+    if trav:
+        ctx.set_traversal_config(trav["block"], trav["stack"])
 
     def plain():
         out = []
@@ -345,40 +562,44 @@ def batched_scenes(G, ctx, base, n_scenes=512, seed=1004):
         torch.cuda.synchronize()
         return bvhs, hits
 
-    plain()
-    t0 = time.perf_counter()
-    ref = plain()
-    t_plain = time.perf_counter() - t0
-    for b in batched()[0]:
-        b.free()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    bvhs, hits = batched()
-    t_batched = time.perf_counter() - t0
-    for b in bvhs:
-        b.free()
-    t0 = time.perf_counter()
-    bvhs = G.build_cwbvh_from_tris_segmented(tris, p, ctx=ctx)
-    torch.cuda.synchronize()
-    t_build = time.perf_counter() - t0
-    launches = bvhs[0].stats.kernel_launches if bvhs else 0
-    t0 = time.perf_counter()
-    hits = G.ray_traverse_multi(bvhs, all_owner, all_rays, ctx=ctx)
-    torch.cuda.synchronize()
-    t_trace = time.perf_counter() - t0
-    for b in bvhs:
-        b.free()
+    try:
+        plain()
+        t0 = time.perf_counter()
+        ref = plain()
+        t_plain = time.perf_counter() - t0
+        for b in batched()[0]:
+            b.free()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        bvhs, hits = batched()
+        t_batched = time.perf_counter() - t0
+        for b in bvhs:
+            b.free()
+        t0 = time.perf_counter()
+        bvhs = G.build_cwbvh_from_tris_segmented(tris, p, ctx=ctx)
+        torch.cuda.synchronize()
+        t_build = time.perf_counter() - t0
+        launches = bvhs[0].stats.kernel_launches if bvhs else 0
+        t0 = time.perf_counter()
+        hits = G.ray_traverse_multi(bvhs, all_owner, all_rays, ctx=ctx)
+        torch.cuda.synchronize()
+        t_trace = time.perf_counter() - t0
+        for b in bvhs:
+            b.free()
+    finally:
+        if trav:
+            ctx.set_traversal_config(0, 0)
     got = hits.cpu().numpy().view(np.uint32)
     exp = np.concatenate([np.stack([r.cpu().numpy().view(np.uint32)[:, 0], r.cpu().numpy().view(np.uint32)[:, 1]], 1)
                           for r in ref])
     identical = bool(np.array_equal(got, exp))
     return {"workload": f"{n_scenes} clustered scenes, 1k-200k triangles (log-uniform), "
                         "4,096-262,144 incoherent rays each", "preset": "medium_build",
-            "search_radius": int(p.ploc_search_distance),
-            "autotune_s_by_radius": {str(k): v for k, v in tune.items()},
+            "tuned": {"radius": int(p.ploc_search_distance), **({"block": trav["block"], "stack": trav["stack"]}
+                                                                if trav else {})},
+            "autotune": tune,
             "scenes": n_scenes, "triangles": n_tris, "rays": n_rays,
             "plain_s": t_plain, "batched_s": t_batched, "speedup": t_plain / t_batched,
-            "plain_scenes_per_s": n_scenes / t_plain, "batched_scenes_per_s": n_scenes / t_batched,
             "batched_build_s": t_build, "batched_build_mtris_s": n_tris / t_build / 1e6,
             "batched_build_kernel_launches": launches,
             "batched_trace_mrays_s": n_rays / t_trace / 1e6, "identical_hits": identical}
@@ -459,62 +680,60 @@ def serving(params, n_requests=3000, rate=2000.0, budget=80 << 30, seed=1005):
     return out
 
 
-def workload(n):
-    from obvhs_gb300 import scenes as S
-
-    return S.scene2_tris(n), S.scene2_primary_rays()
-
-
-def cpu_build_rate(tris, params, reps, nthreads):
-    """Oracle builds of the full scene on `nthreads` host threads: Mtris/s."""
+def oracle_build_s(tris, params, nthreads, reps=1):
+    """Seconds per oracle build of the whole scene on `nthreads` host threads."""
     from oracle import oracle as O
 
     t = []
+    ob = None
     for _ in range(reps):
         t0 = time.perf_counter()
         ob = O.build(tris=tris, params=params, nthreads=nthreads, keep_intermediate=False)
         t.append(time.perf_counter() - t0)
-    cpu_build_rate.last = ob
-    return len(tris) / (sum(t) / len(t)) / 1e6, t
+    return t, ob
 
 
-def cpu_baseline(tris, params, rays, cores, ctx):
-    """The oracle: two builds, and the primary rays traced on the GPU-built
-    tree with visit/test counters (all host threads)."""
+def cpu_baseline(c3, cores):
+    """The oracle on the headline scene: one full build on all host threads,
+    one on a single thread, and a 1M-ray sample of the closest-hit rays traced
+    on the GPU-built tree with node-visit / triangle-test counters (which also
+    give the traversal's algorithmic bytes)."""
     from oracle import oracle as O
 
-    rate, times = cpu_build_rate(tris, params, 2, cores)
-    ob = cpu_build_rate.last
-    import obvhs_gb300 as G
-
-    cw = G.build_cwbvh_from_tris(tris, params, ctx=ctx)
-    nodes, pidx = cw.download()
+    tris, p = c3["tris"], c3["params"]
+    t_all, _ = oracle_build_s(tris, p, cores)
+    t_one, _ = oracle_build_s(tris, p, 1)
+    nodes, pidx = c3["cw"].download()
+    sample = c3["closest_sample"]
     t0 = time.perf_counter()
-    _, _, _, cnt = O.traverse(nodes, pidx, tris, rays, 0, nthreads=cores, counters=True)
+    _, _, _, cnt = O.traverse(nodes, pidx, tris, sample, 0, nthreads=cores, counters=True)
     dt = time.perf_counter() - t0
-    return rate, times, {"visits": int(cnt[0]), "tests": int(cnt[1]), "mrays_s": len(rays) / dt / 1e6,
-                         "searches": ob.searches, "search_nodes": ob.search_nodes}
+    n = len(tris)
+    return {"value": n / t_all[0] / 1e6, "value_1thread": n / t_one[0] / 1e6, "s_all": t_all[0], "s_1": t_one[0],
+            "mrays_s": len(sample) / dt / 1e6, "visits_per_ray": cnt[0] / len(sample),
+            "tests_per_ray": cnt[1] / len(sample)}
 
 
 def run_reference(args):
     rank, _, world = dist_info()
     if rank != 0:
         return
+    from obvhs_gb300 import scenes as S
     from obvhs_gb300.params import BvhBuildParams
 
-    tris, _ = workload(args.tris)
+    tris = S.scene3_tris(args.tris)
     cores = os.cpu_count() or 1
-    p = BvhBuildParams.slow_build()
-    for _ in range(args.warmup):
-        cpu_build_rate(tris, p, 1, cores)
-    rate, times = cpu_build_rate(tris, p, args.steps, cores)
+    p = BvhBuildParams(False, 14, 3, 0.0, 0.0, 0, 3, 3.0)
+    oracle_build_s(tris, p, cores, args.warmup)
+    times, _ = oracle_build_s(tris, p, cores, args.steps)
     ms = 1e3 * sum(times) / len(times)
-    sample = f"full {len(tris)}-triangle slow_build per step, {cores} threads"
+    rate = len(tris) / (ms * 1e-3) / 1e6
+    sample = f"full {len(tris)}-triangle build per step, {cores} threads"
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "Mtris/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded PCG64)",
-        "config": {"workload": WORKLOAD, "n_tris": len(tris), "preset": "slow_build",
+        "config": {"workload": WORKLOAD, "n_tris": len(tris),
                    "implementation": "C++ restatement of obvhs 0.3.1 (oracle/); the Rust crate cannot be built here"},
         "cpu_baseline": {"value": rate, "unit": "Mtris/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -522,225 +741,153 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def mean(x):
+    return sum(x) / len(x) if x else 0.0
+
+
 def run_gb300(args):
-    import torch
+    B = Bench(args)
+    world = B.world
+    only = args.only
+    detail = {}
 
-    rank, local_rank, world = dist_info()
-    torch.cuda.set_device(local_rank)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
+    if only in ("c2", "c2-build"):
+        c2 = config2(B, only_build=only == "c2-build")
+        if B.rank == 0:
+            m = mean(c2["build_ms"])
+            print(json.dumps({"metric": METRIC, "value": replica_rate(1_000_000, m, world), "unit": "Mtris/s",
+                              "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": m,
+                              "config": {"workload": "clustered-1M-slow_build"}}), flush=True)
+        return
+    if only == "c1":
+        c1 = config1(B)
+        if B.rank == 0:
+            m = mean(c1["build_ms"])
+            print(json.dumps({"metric": METRIC, "value": c1["n_tris"] / (m * 1e-3) / 1e6, "unit": "Mtris/s",
+                              "ms_per_step": m, "rays_mrays_s": c1["n_rays"] / (mean(c1["ray_ms"]) * 1e-3) / 1e6,
+                              "config": {"workload": "uniform-10k r16"}}), flush=True)
+        return
 
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    c3 = config3(B, only_build=only == "c3-build")
+    n = len(c3["tris"])
+    m_build = mean(c3["build_ms"])
+    if only == "c3-build":
+        m_build, = max_over_ranks([m_build], B.dist, "cuda")
+        if B.rank == 0:
+            print(json.dumps({"metric": METRIC, "value": replica_rate(n, m_build, world), "unit": "Mtris/s",
+                              "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": m_build,
+                              "gpu_launches": c3["launches"], "config": {"workload": WORKLOAD, "n_tris": n}}),
+                  flush=True)
+        return
+    m_e2e, m_cl, m_sh = mean([c3["e2e_ms"]]), mean(c3["closest_ms"]), mean(c3["shadow_ms"])
+    m_build, m_e2e, m_cl, m_sh = max_over_ranks([m_build, m_e2e, m_cl, m_sh], B.dist, "cuda")
+    if B.rank != 0:
+        if B.dist:
+            B.dist.destroy_process_group()
+        return
+    value = replica_rate(n, m_build, world)
+    e2e = replica_rate(n, m_e2e, world)
 
-    import obvhs_gb300 as G
-    from obvhs_gb300 import scenes as S
+    c2 = config2(B) if only == "all" else None
+    c1 = config1(B) if only == "all" else None
     from obvhs_gb300.params import BvhBuildParams
 
-    ctx = G.Context(local_rank)
-    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local_rank))
-    tris, rays = workload(args.tris)
-    p = BvhBuildParams.slow_build()
-    d_tris = torch.from_numpy(tris).cuda()
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-
-    # rays: primary, and bounce rays from the primary hits
-    cw = G.build_cwbvh_from_tris(d_tris, p, ctx=ctx)
-    pid, pt = cw.ray_traverse(rays)
-    bounce = S.bounce_rays(tris, rays, pid, pt)
-    d_rays = torch.from_numpy(rays).cuda()
-    d_bounce = torch.from_numpy(bounce).cuda()
-    n_nodes, n_prims, _ = cw.info()
-    del cw
-
-    def barrier():
-        torch.cuda.synchronize()
-        if dist:
-            dist.barrier()
-
-    def timed(fn, steps):
-        """Runs fn() `steps` times; each call is bracketed by CUDA events on the
-        library's stream and followed (outside the timing) by an L2 flush."""
-        ms = []
-        for _ in range(steps):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            fn()
-            e1.record(stream)
-            e1.synchronize()
-            ms.append(e0.elapsed_time(e1))
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-        return ms
-
-    def build_once():
-        b = G.build_cwbvh_from_tris(d_tris, p, ctx=ctx)
-        build_once.last = b
-
-    for _ in range(args.warmup):
-        build_once()
-    barrier()
-    clocks = ClockSampler(local_rank).start() if rank == 0 else None
-    l0 = ctx.kernel_launches
-    t_wall0 = time.perf_counter()
-    build_ms = timed(build_once, args.steps)
-    barrier()
-    t_wall = time.perf_counter() - t_wall0
-    launches = (ctx.kernel_launches - l0) // max(args.steps, 1)
-    stats = build_once.last.stats
-    cw = build_once.last
-
-    # traversal (device-resident rays), each step = primary + bounce batch
-    out_p = torch.empty((len(rays), 2), dtype=torch.int32, device="cuda")
-    out_b = torch.empty((max(len(bounce), 1), 2), dtype=torch.int32, device="cuda")
-    lib = ctx.lib
-    import ctypes
-
-    def trace(r, out):
-        ctx.check(lib.obvhs_ray_traverse(ctx.h, cw.h, ctypes.c_void_p(r.data_ptr()), r.shape[0],
-                                         ctypes.c_void_p(out.data_ptr()), 1))
-
-    for _ in range(args.warmup):
-        trace(d_rays, out_p)
-        trace(d_bounce, out_b)
-    barrier()
-    prim_ms = timed(lambda: trace(d_rays, out_p), args.steps)
-    bounce_ms = timed(lambda: trace(d_bounce, out_b), args.steps) if len(bounce) else [0.0]
-    clk = clocks.stop() if clocks else None
-
-    # per-kernel device time of one build and one primary batch (events around
-    # every launch on the library's stream; not part of the timings above)
-    ctx.set_profiling(True)
-    b = G.build_cwbvh_from_tris(d_tris, p, ctx=ctx)
-    trace(d_rays, out_p)
-    ctx.synchronize()
-    kernel_profile = ctx.profile_report()
-    ctx.set_profiling(False)
-    del b
-
-    # e2e through the public API: pinned host triangles in, CWBVH nodes out
-    h_tris = torch.from_numpy(tris).pin_memory()
-    h_nodes = torch.empty((n_nodes, 80), dtype=torch.uint8).pin_memory().numpy()
-    h_prims = torch.empty((n_prims,), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
-    h_tris_np = h_tris.numpy()
-    e2e_ms = []
-    for i in range(args.warmup + args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        b = G.build_cwbvh_from_tris(h_tris_np, p, ctx=ctx)
-        ctx.check(lib.obvhs_cwbvh_download(ctx.h, b.h, h_nodes.ctypes.data_as(ctypes.c_void_p),
-                                           h_prims.ctypes.data_as(ctypes.c_void_p)))
-        dt = (time.perf_counter() - t0) * 1e3
-        if i >= args.warmup:
-            e2e_ms.append(dt)
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
-        del b
-
-    n = len(tris)
-    mean_build = sum(build_ms) / len(build_ms)
-    mean_e2e = sum(e2e_ms) / len(e2e_ms)
-    mean_build, mean_e2e, mean_prim, mean_bounce = max_over_ranks(
-        [mean_build, mean_e2e, sum(prim_ms) / len(prim_ms), sum(bounce_ms) / len(bounce_ms)], dist, "cuda")
-    if rank != 0:
-        if dist:
-            dist.destroy_process_group()
-        return
-    value = replica_rate(n, mean_build, world)
-    e2e = replica_rate(n, mean_e2e, world)
-    prim_rate = replica_rate(len(rays), mean_prim, world)
-    bounce_rate = replica_rate(len(bounce), mean_bounce, world)
-
-    arch = None if args.no_arch_scene else arch_scene(ctx, stream, max(3, args.steps // 4), args.warmup, flush)
-    batch = None if args.no_batched else batched_scenes(G, ctx, BvhBuildParams.medium_build())
-    served = None if args.no_serving else serving(BvhBuildParams.medium_build())
-
-    # CPU baseline (the oracle on this host's cores, bounded sample): two full
-    # builds, and the primary batch traced with node-visit / triangle-test
-    # counters, which also give the traversal's algorithmic bytes.
+    batch = None if (args.no_batched or only != "all") else batched_scenes(B.G, B.ctx, BvhBuildParams.medium_build())
+    served = None if (args.no_serving or only != "all") else serving(BvhBuildParams.medium_build())
     cores = os.cpu_count() or 1
-    cpu_rate, cpu_t, cpu_trace = cpu_baseline(tris, p, rays, cores, ctx)
+    cpu = None if args.no_cpu else cpu_baseline(c3, cores)
 
+    # roofline of the headline build's dominant kernel (largest share of
+    # event-timed device time in one profiled build): algorithmic bytes per
+    # launch / mean launch time
     peak, peak_kind = measured_peak()
-    traffic_db = {}
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        traffic_db = json.load(open(tpath))
-
-    # roofline of the build's dominant kernel (largest share of device time in
-    # the event-bracketed build): algorithmic bytes per launch / mean launch
-    # time; traffic = DRAM bytes per launch from the ncu capture (profiles/)
-    models = kernel_byte_models(stats.leaf_count, stats.ploc_sum_counts, n_nodes, n_prims,
-                                cpu_trace.get("search_nodes"))
-    build_kernels = {}
-    for k, v in kernel_profile.items():
-        if k.startswith("k_traverse"):
-            continue
-        k = "k_find" if k.startswith("k_find") else k  # one search kernel, two launch forms
-        a = build_kernels.setdefault(k, {"launches": 0, "total_ms": 0.0})
-        a["launches"] += v["launches"]
-        a["total_ms"] += v["total_ms"]
-    ranked = sorted(build_kernels.items(), key=lambda kv: -kv[1]["total_ms"])
-    dom_name, dom = next(((k, v) for k, v in ranked if models.get(k)), ranked[0])
-    dom_launches = max(dom["launches"], 1)
-    dom_bytes = models.get(dom_name, 0) / dom_launches
-    dom_ms = dom["total_ms"] / dom_launches
+    st = c3["stats"]
+    models = kernel_byte_models(st.leaf_count, st.ploc_sum_counts, c3["n_nodes"], c3["n_prims"], ratio=0.0,
+                                precision=0)
+    dom, dom_launches, dom_total, dom_share = dominant_kernel(c3["profile"], models)
+    dom_launches = max(dom_launches, 1)
+    dom_bytes = models.get(dom, 0) / dom_launches
+    dom_ms = dom_total / dom_launches
     dom_achieved = dom_bytes / (dom_ms * 1e-3) / 1e9 if dom_ms > 0 else 0.0
-    build_total_ms = sum(v["total_ms"] for v in build_kernels.values())
-
-    # whole build against the same peak (the build is latency- and launch-bound)
-    build_bytes = build_byte_model(stats.leaf_count, n, stats.ploc_sum_counts, n_nodes, n_prims)
-    build_achieved = build_bytes / (mean_build * 1e-3) / 1e9
-
-    # traversal: one launch per batch, timed above with CUDA events on the
-    # library's stream.  Algorithmic bytes per ray: 32 (ray) + 8 (hit) + 80 per
-    # node visited + 36 per triangle tested (visit/test counts: oracle)
-    alg_bytes = 40.0 * len(rays) + 80.0 * cpu_trace["visits"] + 36.0 * cpu_trace["tests"]
-    achieved = alg_bytes / (mean_prim * 1e-3) / 1e9
+    traffic = traffic_record("architectural-8M", dom)
+    build_bytes = build_byte_model(st.leaf_count, n, st.ploc_sum_counts, c3["n_nodes"], c3["n_prims"], ratio=0.0,
+                                   precision=0)
+    build_achieved = build_bytes / (m_build * 1e-3) / 1e9
 
     line = {
-        "metric": METRIC, "value": value, "unit": "Mtris/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": mean_build, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded PCG64 clustered scene)",
-        "config": {"workload": WORKLOAD, "n_tris": n, "preset": "slow_build", "leaves": stats.leaf_count,
-                   "cwbvh_nodes": n_nodes, "primary_rays": len(rays), "bounce_rays": len(bounce),
-                   "l2": "512 MB flush between timed steps", "parallelism": f"replicas x{world}"},
-        "e2e": {"value": e2e, "unit": "Mtris/s", "h2d_bytes_per_step": n * 36,
-                "d2h_bytes_per_step": n_nodes * 80 + n_prims * 4, "ms_per_step": mean_e2e},
-        "traversal": {"primary_mrays_s": prim_rate, "bounce_mrays_s": bounce_rate, "primary_ms": mean_prim,
-                      "bounce_ms": mean_bounce},
-        "build_stages_ms": {"presplit": stats.stage_ms[0], "ploc": stats.stage_ms[1],
-                            "reinsertion": stats.stage_ms[2], "cwbvh": stats.stage_ms[3]},
-        "roofline": {"kernel": dom_name, "bound": "hbm", "achieved": dom_achieved, "peak": peak,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": dom_achieved / peak,
-                     "traffic": traffic_db.get(dom_name), "algorithmic_bytes_per_launch": dom_bytes,
-                     "launches": dom["launches"], "mean_launch_ms": dom_ms,
-                     "share_of_build_kernel_time": dom["total_ms"] / build_total_ms if build_total_ms else None,
-                     "note": ROOFLINE_NOTES.get(dom_name, "")},
-        "roofline_build": {"bound": "hbm", "achieved": build_achieved, "peak": peak, "unit": "GB/s",
-                           "frac": build_achieved / peak, "algorithmic_bytes": build_bytes,
-                           "bytes_per_leaf": build_bytes / max(stats.leaf_count, 1)},
-        "roofline_traversal": {"kernel": "k_traverse<closest> (primary batch)", "bound": "hbm",
-                               "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                               "traffic": traffic_db.get("k_traverse_closest"),
-                               "algorithmic_bytes_per_launch": alg_bytes, "bytes_per_ray": alg_bytes / len(rays)},
-        "architectural_scene": arch,
-        "batched": batch,
-        "serving": served,
-        "cpu_baseline": {"value": cpu_rate, "unit": "Mtris/s", "cores": cores, "kind": "port",
-                         "sample": f"2 full {n}-triangle slow_build builds on {cores} threads "
-                                   f"({sum(cpu_t):.1f} s)",
-                         "primary_mrays_s": cpu_trace["mrays_s"]},
-        "gpu_launches": launches,
-        "kernel_profile_ms": {k: round(v["total_ms"], 4) for k, v in sorted(kernel_profile.items(),
-                                                                             key=lambda kv: -kv[1]["total_ms"])},
-        "clocks": clk,
-        "wall_s_timed_builds": t_wall,
+        "metric": METRIC, "value": r4(value), "unit": "Mtris/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r4(m_build), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded PCG64 scenes)",
+        "config": {"workload": WORKLOAD, "n_tris": n, "cwbvh_nodes": c3["n_nodes"],
+                   "l2": "inputs 288 MB > L2, and a 512 MB flush between timed steps",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": r4(e2e), "unit": "Mtris/s", "h2d_bytes_per_step": c3["h2d"], "d2h_bytes_per_step": c3["d2h"],
+                "ms_per_step": r4(m_e2e)},
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": r4(dom_achieved), "peak": peak,
+                     "unit": "GB/s", "frac": r4(dom_achieved / peak), "peak_kind": peak_kind,
+                     "traffic": traffic["bytes"] if traffic else None,
+                     "traffic_src": (f"ncu capture at commit {traffic['commit']} (profiles/traffic.json), "
+                                     "not this run") if traffic else None,
+                     "alg_bytes_per_launch": r4(dom_bytes), "launches": dom_launches, "mean_launch_ms": r4(dom_ms),
+                     "share": r4(dom_share)},
+        "roofline_build": {"achieved": r4(build_achieved), "frac": r4(build_achieved / peak),
+                           "bytes_per_tri": r4(build_bytes / n)},
+        "gpu_launches": c3["launches"],
+        "clocks": c3["clocks"],
+        "c3_closest_mrays_s": r4(replica_rate(c3["n_closest"], m_cl, world)),
+        "c3_shadow_mrays_s": r4(replica_rate(c3["n_shadow"], m_sh, world)),
+        "c3_closest_ctri_mrays_s": r4(replica_rate(c3["n_closest"], mean(c3["closest_ctri_ms"]), world)),
+        "c3_hit_frac": r4(c3["hit_fraction"]),
     }
+    if cpu:
+        line["cpu_baseline"] = {"value": r4(cpu["value"]), "unit": "Mtris/s", "cores": cores, "kind": "port",
+                                "sample": f"1 full {n}-tri build per thread count ({cpu['s_all']:.1f} s, "
+                                          f"{cpu['s_1']:.1f} s)",
+                                "value_1thread": r4(cpu["value_1thread"]), "c3_closest_mrays_s": r4(cpu["mrays_s"])}
+        alg = 40.0 + 80.0 * cpu["visits_per_ray"] + 36.0 * cpu["tests_per_ray"]
+        ach = alg * c3["n_closest"] / (m_cl * 1e-3) / 1e9
+        line["roofline_c3_closest"] = {"achieved": r4(ach), "frac": r4(ach / peak), "bytes_per_ray": r4(alg)}
+    if c2:
+        s2 = c2["stats"]
+        line.update({
+            "c2_build_mtris_s": r4(1.0 / (mean(c2["build_ms"]) * 1e-3)),
+            "c2_e2e_mtris_s": r4(1.0 / (c2["e2e_ms"] * 1e-3)),
+            "c2_stages_ms": [r4(x) for x in s2.stage_ms],
+            "c2_primary_mrays_s": r4(c2["n_primary"] / (mean(c2["primary_ms"]) * 1e-3) / 1e6),
+            "c2_bounce_mrays_s": r4(c2["n_bounce"] / (mean(c2["bounce_ms"]) * 1e-3) / 1e6),
+            "c2_primary_hit_frac": r4(c2["primary_hit_fraction"]), "c2_bounce_rays": c2["n_bounce"],
+            "c2_launches": c2["launches"],
+        })
+    if c1:
+        line.update({"c1_build_mtris_s": r4(c1["n_tris"] / (mean(c1["build_ms"]) * 1e-3) / 1e6),
+                     "c1_build_ms": r4(mean(c1["build_ms"])),
+                     "c1_mrays_s": r4(c1["n_rays"] / (mean(c1["ray_ms"]) * 1e-3) / 1e6)})
+    if batch:
+        line.update({"c4_speedup": r4(batch["speedup"]), "c4_build_mtris_s": r4(batch["batched_build_mtris_s"]),
+                     "c4_trace_mrays_s": r4(batch["batched_trace_mrays_s"]), "c4_tuned": batch["tuned"],
+                     "c4_identical": batch["identical_hits"]})
+    if served:
+        c = served["continuous"]["latency_rays"]
+        line.update({"c5_capacity_ratio": r4(served["capacity_ratio"]),
+                     "c5_mrays_s": r4(served["capacity_mrays_s"]),
+                     "c5_rays_p50_p99_p999_ms": [r4(c["p50_ms"]), r4(c["p99_ms"]), r4(c["p999_ms"])],
+                     "c5_p99_speedup": r4(served["p99_speedup_rays"]), "c5_identical": served["identical_hits"]})
+    if args.detail:
+        detail.update({"line": line, "c3_profile": c3["profile"], "c3_build_ms": c3["build_ms"],
+                       "c3_stage_ms": list(st.stage_ms), "c3_wall_s": c3["wall_s"], "cpu": cpu,
+                       "kernel_models": models})
+        if c2:
+            detail.update({"c2_profile": c2["profile"], "c2_build_ms": c2["build_ms"],
+                           "c2": {k: v for k, v in c2.items() if k not in ("stats", "profile")}})
+        if c1:
+            detail["c1"] = c1
+        detail["batched"] = batch
+        detail["serving"] = served
+        with open(args.detail, "w") as f:
+            json.dump(detail, f, indent=1, default=str)
     print(json.dumps(line), flush=True)
-    if dist:
-        dist.destroy_process_group()
+    if B.dist:
+        B.dist.destroy_process_group()
 
 
 def main():

@@ -371,15 +371,19 @@ OBVHS_API int obvhs_morton_sort(obvhs_ctx* ctx, const float* aabbs, uint32_t n, 
  * or frame-time code that cannot afford cudaMalloc's synchronisation).  It
  * calls no cudaMalloc/cudaFree: its working memory is one fixed array in the
  * library's device image (about 22 MiB, held on every GPU this function runs
- * on until the process exits), for at most OBVHS_NOALLOC_MAX_PRIMS boxes;
+ * on until the process exits; under eager module loading, on every GPU that
+ * uses the library at all), for at most OBVHS_NOALLOC_MAX_PRIMS boxes;
  * larger n returns OBVHS_ERR_TOO_LARGE before any GPU work.
  * aabbs (float[n][6]), codes (u64[n][2], may be NULL) and order (u32[n]) are
- * DEVICE pointers on the current device; the work runs on `stream` (a
+ * DEVICE pointers on the current device (memory of another device, or host
+ * memory, returns OBVHS_ERR_INVALID_ARG); the work runs on `stream` (a
  * cudaStream_t, NULL = default stream) and the call synchronises that stream
  * before returning.  Results equal obvhs_morton_sort's.  The first call on a
  * device looks up the array's device address; make that call before any
- * stream capture.  All calls on a device share the array: calls whose GPU
- * work overlaps (other streams or threads) race and must be serialised. */
+ * stream capture.  The address is kept for the process's life, so do not call
+ * this again on a device after cudaDeviceReset of that device.  All calls on a
+ * device share the array: calls whose GPU work overlaps (other streams or
+ * threads) race and must be serialised. */
 #define OBVHS_NOALLOC_MAX_PRIMS 262144u
 OBVHS_API int obvhs_morton_sort_noalloc(const float* aabbs, uint32_t n, uint32_t sort_precision, uint64_t* codes,
                                         uint32_t* order, void* stream);

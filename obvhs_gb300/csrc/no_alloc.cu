@@ -11,11 +11,15 @@
 //
 // The scratch array: a file-scope __device__ array of NOALLOC_SCRATCH_BYTES
 // (about 22 MiB, enough for OBVHS_NOALLOC_MAX_PRIMS primitives).  Every GPU on
-// which this entry point runs holds it until the process exits.  On the host,
+// which this entry point runs holds it until the process exits; under eager
+// module loading (CUDA_MODULE_LOADING=EAGER) every GPU that uses this library
+// at all holds it, whether or not this entry point is called.  On the host,
 // `g_noalloc_scratch` only names the symbol; its device address comes from
 // cudaGetSymbolAddress, taken once per device (with that device current) by
 // the first call on that device, which is why that first call should come
-// before any stream capture.
+// before any stream capture.  The address is kept for the life of the
+// process: after cudaDeviceReset on a device this entry point must not be
+// called on that device again.
 //
 // Sharing: every call on a device uses the same array, and the array keeps
 // what the last call left there.  Each call therefore re-initialises what must
@@ -81,13 +85,18 @@ cudaError_t scratch_on_device(int dev, unsigned char** out) {
   return cudaSuccess;
 }
 
-bool on_device(const void* p) {
+// True when p is device memory of device `dev` (the current device) or
+// managed memory.  Device memory of another GPU is rejected: the kernels run
+// on `dev` and would reach it only through peer access, which this entry
+// point does not set up.
+bool on_device(const void* p, int dev) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 // Codes in the layout obvhs_morton_sort returns: (lo, hi) u64 pairs.
@@ -115,12 +124,13 @@ OBVHS_API int obvhs_morton_sort_noalloc(const float* aabbs, uint32_t n, uint32_t
   if (sort_precision > 1) return OBVHS_ERR_INVALID_ARG;
   if (n == 0) return OBVHS_OK;
   if (!aabbs || !order) return OBVHS_ERR_INVALID_ARG;
-  if (!on_device(aabbs) || !on_device(order) || (codes && !on_device(codes))) return OBVHS_ERR_INVALID_ARG;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) {
     cudaGetLastError();
     return OBVHS_ERR_CUDA;
   }
+  if (!on_device(aabbs, dev) || !on_device(order, dev) || (codes && !on_device(codes, dev)))
+    return OBVHS_ERR_INVALID_ARG;
   if (radix_scratch_words(MAX_PRIMS) > RADIX_WORDS) return OBVHS_ERR_INVALID_ARG;
   unsigned char* base = nullptr;
   if (scratch_on_device(dev, &base) != cudaSuccess) return OBVHS_ERR_CUDA;

@@ -1,10 +1,9 @@
 """Regenerate the golden fixtures in this folder.
 
-Run from the repository root, in a checkout that has the reference tree at
-/root/reference (it reads the reference's own test asset; nothing at test
-time reads it):
+Run from the repository root with the path of the reference checkout (it
+reads the reference's own test asset; nothing at test time reads it):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py <reference checkout>
 
 Writes kitchen_mesh.npz: the triangles of assets/kitchen.obj.zst as loaded by
 examples/helpers/load_obj.rs:6-45 (positions as f32, faces in file order,
@@ -14,12 +13,14 @@ and asserts the normal hash 1343358762 for five build presets.
 """
 from __future__ import annotations
 
+import argparse
 import ctypes
 import os
 
 import numpy as np
 
-REF_ASSET = "/root/reference/assets/kitchen.obj.zst"
+#: the mesh inside the reference checkout
+ASSET = os.path.join("assets", "kitchen.obj.zst")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -70,7 +71,10 @@ def load_obj_triangles(text: str) -> np.ndarray:
 
 
 def main():
-    text = zstd_decompress(open(REF_ASSET, "rb").read()).decode()
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("reference", help="path of the obvhs reference checkout")
+    args = ap.parse_args()
+    text = zstd_decompress(open(os.path.join(args.reference, ASSET), "rb").read()).decode()
     tris = load_obj_triangles(text)
     verts = tris.reshape(-1, 3)
     uniq, inv = np.unique(verts.view(np.uint32).reshape(-1, 3), axis=0, return_inverse=True)

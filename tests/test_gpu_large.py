@@ -79,3 +79,32 @@ def test_architectural_scene_build_and_rays_bitexact(G):
     gmiss = cw.ray_traverse_miss(shadow)
     omiss, _, _ = O.traverse(ob.cw_nodes, ob.cw_pidx, tris, shadow, 1, nthreads=THREADS)
     assert np.array_equal(gmiss, omiss == 0xFFFFFFFF)
+
+
+def test_architectural_scene_full_size_bitexact(G):
+    """The benchmark's headline workload at its full size: the 8M-triangle
+    scene built PLOC -> CWBVH (radius 14, distance 1 for 3 passes, U64), the
+    CWBVH bytes and primitive indices, every one of the 16M incoherent
+    closest-hit rays (ids and t) and of the 16M shadow rays against the oracle
+    (src/cwbvh/mod.rs:169-225)."""
+    from obvhs_gb300.params import BvhBuildParams
+
+    tris = S.scene3_tris(8_000_000)
+    p = BvhBuildParams(False, 14, 3, 0.0, 0.0, 0, 3, 3.0)
+    ob = O.build(tris=tris, params=p, nthreads=THREADS, keep_intermediate=False)
+    cw = G.build_cwbvh_from_tris(tris, p)
+    nodes, prims = cw.download()
+    assert _bytes_equal(nodes, ob.cw_nodes)
+    assert _bytes_equal(prims, ob.cw_pidx)
+    del nodes, prims
+    closest, shadow = S.scene3_rays(16_000_000)
+    gid, gt = cw.ray_traverse(closest)
+    oid, ot, _ = O.traverse(ob.cw_nodes, ob.cw_pidx, tris, closest, 0, nthreads=THREADS)
+    assert (oid != 0xFFFFFFFF).mean() > 0.5
+    assert np.array_equal(gid, oid)
+    assert np.array_equal(gt.view(np.uint32), ot.view(np.uint32))
+    del gid, gt, oid, ot, closest
+    gmiss = cw.ray_traverse_miss(shadow)
+    omiss, _, _ = O.traverse(ob.cw_nodes, ob.cw_pidx, tris, shadow, 1, nthreads=THREADS)
+    assert np.array_equal(gmiss, omiss == 0xFFFFFFFF)
+    assert gmiss.any() and (~gmiss).any()

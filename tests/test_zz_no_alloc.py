@@ -13,6 +13,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 MAX_PRIMS = 262144  # OBVHS_NOALLOC_MAX_PRIMS in include/obvhs_gb300.h
+ERR_INVALID_ARG = -1
 ERR_TOO_LARGE = -7
 
 
@@ -82,3 +83,42 @@ def test_rejects_inputs_beyond_capacity(env):
     rc = lib.obvhs_morton_sort_noalloc(da.data_ptr(), MAX_PRIMS + 1, 0, None, order.data_ptr(), None)
     assert rc == ERR_TOO_LARGE
     assert lib.obvhs_morton_sort_noalloc(da.data_ptr(), 0, 0, None, order.data_ptr(), None) == 0
+
+
+def test_rejects_host_memory_without_launching(env):
+    """Buffers that are not memory of the current device are refused before
+    any GPU work (the check reads pointer attributes only)."""
+    torch, _, lib = env
+    dev = torch.device("cuda:0")
+    h_aabbs = torch.zeros((16, 6), dtype=torch.float32).pin_memory()
+    d_aabbs = torch.zeros((16, 6), dtype=torch.float32, device=dev)
+    h_order = torch.zeros(16, dtype=torch.int32).pin_memory()
+    d_order = torch.zeros(16, dtype=torch.int32, device=dev)
+    assert lib.obvhs_morton_sort_noalloc(h_aabbs.data_ptr(), 16, 0, None, d_order.data_ptr(), None) == ERR_INVALID_ARG
+    assert lib.obvhs_morton_sort_noalloc(d_aabbs.data_ptr(), 16, 0, None, h_order.data_ptr(), None) == ERR_INVALID_ARG
+    codes = np.zeros((16, 2), np.uint64)  # pageable host memory
+    assert lib.obvhs_morton_sort_noalloc(d_aabbs.data_ptr(), 16, 0, codes.ctypes.data, d_order.data_ptr(),
+                                         None) == ERR_INVALID_ARG
+
+
+def test_call_leaves_free_device_memory_unchanged(env):
+    """After a warm-up call (which loads the library's kernels), a second call
+    leaves the device's free memory as it was: it allocates nothing.  The free
+    figure only approximates "no allocation" (another process on the GPU
+    could change it), so this is a check, not a proof."""
+    torch, _, lib = env
+    dev = torch.device("cuda:0")
+    a = _aabbs(100_000, 31)
+    da = torch.from_numpy(a).to(dev)
+    codes = torch.empty((len(a), 2), dtype=torch.int64, device=dev)
+    order = torch.empty((len(a),), dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    assert lib.obvhs_morton_sort_noalloc(da.data_ptr(), len(a), 1, codes.data_ptr(), order.data_ptr(),
+                                         stream.cuda_stream) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(dev)
+    assert lib.obvhs_morton_sort_noalloc(da.data_ptr(), len(a), 1, codes.data_ptr(), order.data_ptr(),
+                                         stream.cuda_stream) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(dev)
+    assert free1 == free0
