@@ -66,6 +66,7 @@ enum ScratchSlot {
   SLOT_SEG_IDX,
   SLOT_MORTON_TOP,  // the Morton sort's high-digit keys (+ a flag word)
   SLOT_CAND_HIST,   // the reinsertion candidate sorts' digit histograms (two areas)
+  SLOT_CW_SMALL,    // CWBVH conversion: primitive lists of nodes with at most 3 primitives
   SLOT_COUNT
 };
 

@@ -7,24 +7,26 @@
 //   count_primitives (:197-211)
 //
 // Costs: a parent-counter climb from the leaves (the second child to arrive
-// computes the parent).  Besides the 7 decisions, every node records for
-// each decision slot i the aggregate of the CWBVH children that
-// get_children(node, i) yields: the CWBVH nodes below those children and the
-// primitives held by the leaf children.  A child that is itself distributed
-// contributes its own aggregate, so no record needs a tree walk.  Then
-// ncw(X) = 1 + agg(X, 0).nodes is the size of the CWBVH subtree rooted at X
-// and lprims(X) = agg(X, 0).prims the primitives of X's leaf children.
+// computes the parent, carrying its own child's record in registers and
+// reading only the sibling's).  Besides the 7 decisions, every node records
+// for each slot budget j the number of CWBVH nodes it contributes when its
+// parent's distribution reaches it with budget j, so the count below the
+// children of any decision is one add and no record needs a tree walk; the
+// emission record keeps aggn(X), the CWBVH nodes below the children of X's
+// slot-0 decision, and ncw(X) = 1 + aggn(X) is the size of the CWBVH subtree
+// rooted at X.
 //
 // Emission: the reference recurses depth-first, so a node's children go to
 // nodes.len() when it is visited and its primitives to
 // primitive_indices.len().  Both offsets follow from subtree sizes: for the
 // internal children c_1..c_k of X (slot order), child_base(c_1) =
 // child_base(X) + k, child_base(c_j+1) = child_base(c_j) + ncw(c_j) - 1;
-// prim_base(c_1) = prim_base(X) + lprims(X), prim_base(c_j+1) =
-// prim_base(c_j) + nprim(c_j).  A warp per node (lane s = child slot s)
+// prim_base(c_1) = prim_base(X) + (primitives of X's leaf children),
+// prim_base(c_j+1) = prim_base(c_j) + nprim(c_j).  One thread per CWBVH node
 // takes nodes from a device work queue in which every node's item is
-// published by its parent's warp, so nodes are written at exactly the
-// reference's positions: the output is byte for byte the reference's.
+// published by the thread that emits its parent, so nodes are written at
+// exactly the reference's positions: the output is byte for byte the
+// reference's.
 #include <cmath>
 #include <cstddef>
 #include <cstring>
@@ -36,216 +38,320 @@
 namespace {
 
 constexpr int BLK = 256;
-constexpr int EMIT_THREADS = 128;
+constexpr int EMIT_THREADS = 128;  // k_order_children: a warp per node
+constexpr int EMIT_TB = 64;        // k_emit_all: a thread per node
 constexpr float PRIM_COST = 0.3f;
 constexpr float DENOM = 1.0f / 255.0f;
 constexpr uint32_t AGG_INVALID = 0xffffffffu;
+constexpr uint32_t DL_INVALID = 7;
 
-enum : uint8_t { K_LEAF = 0, K_INTERNAL = 1, K_DISTRIBUTE = 2 };
-constexpr uint8_t DL_INVALID = 7;
+enum : uint32_t { K_LEAF = 0, K_INTERNAL = 1, K_DISTRIBUTE = 2 };
 
-struct __align__(16) Dec {
-  float cost[7];
-  uint32_t nprim;
-  uint8_t meta[8];  // kind | dl << 2 | dr << 5  (dl/dr 7 = invalid)
-  uint2 agg[7];     // per decision slot: (CWBVH nodes below, leaf primitives)
+// The 7 decisions of a node (src/cwbvh/bvh2_to_cwbvh.rs:56,479-484), one per
+// slot budget i, packed 4 bits per slot into one word:
+//   slot 0:     bit 3 = internal node (clear: leaf); bits 0-2 = dl, the left
+//               child's slot budget (7: no finite distribution), dr = 6 - dl
+//   slot i > 0: bit 3 = distribute, dl = bits 0-2 and dr = i - 1 - dl;
+//               bit 3 clear: the decision (and cost) of slot i - 1
+// So the decision of slot j is that of the nearest slot s <= j that is slot 0
+// or has bit 3 set.
+struct Decision {
+  uint32_t kind, dl, dr;
 };
-static_assert(sizeof(Dec) == 96, "Dec layout");
+__device__ __forceinline__ Decision decode(uint32_t meta, uint32_t j) {
+  const uint32_t m = meta & 0x08888880u & ((2u << (4 * j + 3)) - 1u);  // distribute flags of slots 1..j
+  Decision d;
+  if (m == 0) {
+    const uint32_t nb = meta & 0xfu;
+    d.kind = (nb & 8u) ? K_INTERNAL : K_LEAF;
+    d.dl = nb & 7u;
+    d.dr = d.dl == DL_INVALID ? DL_INVALID : 6u - d.dl;
+  } else {
+    const uint32_t s = (31u - __clz(m)) >> 2;
+    d.kind = K_DISTRIBUTE;
+    d.dl = (meta >> (4 * s)) & 7u;
+    d.dr = s - 1u - d.dl;
+  }
+  return d;
+}
+
+// What a parent's cost step reads of a child (64 bytes; the reference's
+// decisions are 7 x 8 bytes): costs, decisions, primitive count, and for
+// every slot budget j the CWBVH nodes the child contributes when its parent's
+// distribution reaches it with budget j (child_term): the nodes below its own
+// distribution's children if slot j distributes, else the child as one
+// CWBVH child (internal: 1 + the nodes below it; leaf: none).  Leaves are
+// rebuilt from their boxes, so only inner nodes store one.
+struct __align__(16) CostRec {
+  float cost[7];
+  uint32_t meta;
+  uint32_t contrib[7];
+  uint32_t nprim;
+};
+static_assert(sizeof(CostRec) == 64, "CostRec layout");
+
+// What the emission reads of an inner node: (meta, CWBVH nodes below the
+// children of its slot-0 decision, nprim, 0).
+using EmitRec = uint4;
 
 struct Item {
   uint32_t bvh2, cw, child_base, prim_base;
 };
 
-__device__ __forceinline__ void st_dec(Dec* dst, const Dec& v) {
+__device__ __forceinline__ void st_rec(CostRec* dst, const CostRec& v) {
   uint4* w = reinterpret_cast<uint4*>(dst);
   const uint4* r = reinterpret_cast<const uint4*>(&v);
 #pragma unroll
-  for (int k = 0; k < 6; k++) __stcg(w + k, r[k]);
+  for (int k = 0; k < 4; k++) __stcg(w + k, r[k]);
 }
-__device__ __forceinline__ Dec ld_dec_cg(const Dec* src) {
-  Dec v;
+__device__ __forceinline__ CostRec ld_rec_cg(const CostRec* src) {
+  CostRec v;
   const uint4* r = reinterpret_cast<const uint4*>(src);
   uint4* w = reinterpret_cast<uint4*>(&v);
 #pragma unroll
-  for (int k = 0; k < 6; k++) w[k] = __ldcg(r + k);
+  for (int k = 0; k < 4; k++) w[k] = __ldcg(r + k);
   return v;
 }
 
-__device__ __forceinline__ uint8_t mk(uint8_t kind, uint8_t dl, uint8_t dr) {
-  return (uint8_t)(kind | (dl << 2) | (dr << 5));
-}
-__device__ __forceinline__ uint8_t kind_of(uint8_t m) { return m & 3; }
-__device__ __forceinline__ uint8_t dl_of(uint8_t m) { return (m >> 2) & 7; }
-__device__ __forceinline__ uint8_t dr_of(uint8_t m) { return (m >> 5) & 7; }
-
-// The aggregate one child contributes when its parent's distribution reaches
-// it with slot budget j: its own distribution if that is DISTRIBUTE, else
-// the child as one CWBVH child (internal: its whole subtree; leaf: prims).
-__device__ __forceinline__ uint2 child_term(const Dec& d, uint32_t j) {
-  if (kind_of(d.meta[j]) == K_DISTRIBUTE) return d.agg[j];
-  if (kind_of(d.meta[0]) == K_INTERNAL) {
-    if (d.agg[0].x == AGG_INVALID) return make_uint2(AGG_INVALID, 0);
-    return make_uint2(1 + d.agg[0].x, 0);
-  }
-  return make_uint2(0, d.nprim);
-}
-
-// calculate_cost_impl (src/cwbvh/bvh2_to_cwbvh.rs:257-341) for one inner node
-// whose children are complete, plus the aggregates.
-//
-// A leaf's record is the same for every slot and follows from its box alone,
-// so only roots store it in full; other leaves store just their (all-leaf,
-// zero) decision bytes, and a parent rebuilds a leaf child's record from the
-// child's node (leaf_dec) instead of reading 96 bytes.
-__device__ __forceinline__ Dec leaf_dec(const Bvh2Node& nd) {
+// A leaf's record follows from its box: every slot is the leaf itself.
+__device__ __forceinline__ CostRec leaf_rec(const Bvh2Node& nd) {
   const float cl = (half_area(node_box(nd)) * 1.0f) * PRIM_COST;
-  Dec d;
+  CostRec d;
 #pragma unroll
   for (int k = 0; k < 7; k++) {
     d.cost[k] = cl;
-    d.meta[k] = mk(K_LEAF, 0, 0);
-    d.agg[k] = make_uint2(0, 1);
+    d.contrib[k] = 0;
   }
-  d.meta[7] = 0;
+  d.meta = 0;
   d.nprim = 1;
   return d;
 }
 
-__device__ void inner_costs(const Bvh2Node& nd, const Bvh2Node& cl, const Bvh2Node& cr, Dec* dec, uint32_t x,
-                            uint32_t max_prims) {
-  const float ha = half_area(node_box(nd));
-  const uint32_t f = node_first(nd);
-  const Dec L = node_prims(cl) != 0 ? leaf_dec(cl) : ld_dec_cg(&dec[f]);
-  const Dec R = node_prims(cr) != 0 ? leaf_dec(cr) : ld_dec_cg(&dec[f + 1]);
+__device__ __forceinline__ uint32_t add_agg(uint32_t a, uint32_t b) {
+  return (a == AGG_INVALID || b == AGG_INVALID) ? AGG_INVALID : a + b;
+}
+
+// calculate_cost_impl (src/cwbvh/bvh2_to_cwbvh.rs:257-341) for an inner node
+// of half area ha from its children's records; *aggn0 = the CWBVH nodes
+// below the children of its slot-0 decision.  A slot's node count is taken
+// with the candidate that wins it, so every index is a constant.
+__device__ CostRec inner_rec(const CostRec& L, const CostRec& R, float ha, uint32_t max_prims, uint32_t* aggn0) {
+  CostRec out;
   const uint32_t np = L.nprim + R.nprim;
-  Dec out;
+  uint32_t meta, contrib0, agg;
   {
     const float cost_leaf = np <= max_prims ? ((float)np * ha) * PRIM_COST : __int_as_float(0x7f800000);
     float cd = __int_as_float(0x7f800000);
-    uint8_t dl = DL_INVALID, dr = DL_INVALID;
+    uint32_t dl = DL_INVALID;
+    agg = AGG_INVALID;
 #pragma unroll
     for (int k = 0; k < 7; k++) {
       const float c = L.cost[k] + R.cost[6 - k];
       if (c < cd) {
         cd = c;
-        dl = (uint8_t)k;
-        dr = (uint8_t)(6 - k);
+        dl = (uint32_t)k;
+        agg = add_agg(L.contrib[k], R.contrib[6 - k]);
       }
     }
     const float ci = cd + ha;
-    if (cost_leaf < ci) {
-      out.cost[0] = cost_leaf;
-      out.meta[0] = mk(K_LEAF, dl, dr);
-    } else {
-      out.cost[0] = ci;
-      out.meta[0] = mk(K_INTERNAL, dl, dr);
-    }
+    const bool internal = !(cost_leaf < ci);
+    out.cost[0] = internal ? ci : cost_leaf;
+    meta = (internal ? 8u : 0u) | dl;
+    *aggn0 = agg;
+    contrib0 = internal ? (agg == AGG_INVALID ? AGG_INVALID : 1u + agg) : 0u;
+    out.contrib[0] = contrib0;
   }
+  bool dist = false;  // some slot in 1..i distributes
 #pragma unroll
   for (int i = 1; i < 7; i++) {
     float cd = out.cost[i - 1];
-    uint8_t dl = DL_INVALID, dr = DL_INVALID;
+    uint32_t dl = DL_INVALID, a = agg;
 #pragma unroll
     for (int k = 0; k < i; k++) {
       const float c = L.cost[k] + R.cost[i - k - 1];
       if (c < cd) {
         cd = c;
-        dl = (uint8_t)k;
-        dr = (uint8_t)(i - k - 1);
+        dl = (uint32_t)k;
+        a = add_agg(L.contrib[k], R.contrib[i - k - 1]);
       }
     }
+    out.cost[i] = cd;  // slot i - 1's cost when no distribution is cheaper
     if (dl != DL_INVALID) {
-      out.cost[i] = cd;
-      out.meta[i] = mk(K_DISTRIBUTE, dl, dr);
-    } else {
-      out.cost[i] = out.cost[i - 1];
-      out.meta[i] = out.meta[i - 1];
+      meta |= (8u | dl) << (4 * i);
+      dist = true;
+      agg = a;
     }
+    out.contrib[i] = dist ? agg : contrib0;
   }
-  out.meta[7] = 0;
+  out.meta = meta;
   out.nprim = np;
-#pragma unroll
-  for (int i = 0; i < 7; i++) {
-    const uint8_t dl = dl_of(out.meta[i]), dr = dr_of(out.meta[i]);
-    if (dl == DL_INVALID || dr == DL_INVALID) {
-      out.agg[i] = make_uint2(AGG_INVALID, 0);
-      continue;
-    }
-    const uint2 a = child_term(L, dl), b = child_term(R, dr);
-    out.agg[i] = (a.x == AGG_INVALID || b.x == AGG_INVALID) ? make_uint2(AGG_INVALID, 0)
-                                                            : make_uint2(a.x + b.x, a.y + b.y);
-  }
-  st_dec(&dec[x], out);
+  return out;
 }
 
-__global__ void __launch_bounds__(BLK) k_costs(const Bvh2Node* __restrict__ nodes, const uint32_t* __restrict__ parents,
-                                               uint32_t n, uint32_t max_prims, Dec* dec, uint32_t* flags,
-                                               uint32_t* status) {
-  grid_dep_wait();
-  const uint32_t i = blockIdx.x * BLK + threadIdx.x;
-  if (i >= n) return;
-  const Bvh2Node nd = ld_node(&nodes[i]);
-  if (node_prims(nd) == 0) return;
-  if (node_prims(nd) != 1) {  // src/cwbvh/bvh2_to_cwbvh.rs:243-247
-    set_status(status, ST_BAD_INPUT);
-    return;
+// The climb from one leaf towards the root; at each inner node the second
+// child to arrive computes the node's record.  The climber carries its own
+// child's record in registers, publishes it (for the sibling's climber, in
+// case that one arrives second) before it arrives, and reads the sibling's
+// record only (a leaf sibling's from its box).
+//
+// Nodes with at most 3 primitives (every node that can become a CWBVH leaf)
+// also record their primitives, in the depth-first order count_primitives
+// (src/cwbvh/bvh2_to_cwbvh.rs:197-211) visits them, as (id0, id1, id2,
+// count): the emission then writes a leaf's primitive ids without walking
+// its subtree.
+struct CostClimb {
+  const Bvh2Node* nodes;
+  const uint32_t* parents;
+  const uint32_t* pidx_in;
+  CostRec* crec;
+  EmitRec* erec;
+  uint4* small;
+  uint32_t* flags;
+  uint32_t* status;
+  uint32_t n, max_prims;
+  // the climb
+  CostRec own;
+  uint4 own_list;  // own.nprim <= 3: its primitives
+  uint32_t c, p, steps;
+  bool own_leaf;
+
+  // Starts at node i; false when there is nothing to climb (an inner node,
+  // a leaf root, or a bad leaf).
+  __device__ __forceinline__ bool start(uint32_t i) {
+    const Bvh2Node nd = ld_node(&nodes[i]);
+    if (node_prims(nd) == 0) return false;
+    if (node_prims(nd) != 1) {  // src/cwbvh/bvh2_to_cwbvh.rs:243-247
+      set_status(status, ST_BAD_INPUT);
+      return false;
+    }
+    // every leaf lists its primitive for the emission
+    own_list = make_uint4(__ldg(&pidx_in[node_first(nd)]), 0u, 0u, 1u);
+    __stcg(&small[i], own_list);
+    // roots are their own parents (one tree: node 0; several trees in one
+    // array: each tree's first node); a leaf root is one CWBVH node
+    p = parents[i];
+    if (p == i) {
+      __stcg(&erec[i], make_uint4(0u, 0u, 1u, 0u));
+      return false;
+    }
+    own = leaf_rec(nd);
+    own_leaf = true;
+    c = i;
+    steps = 0;
+    return true;
   }
-  // roots are their own parents (one tree: node 0; several trees in one
-  // array: each tree's first node); a leaf root's record is read back whole
-  uint32_t p = parents[i];
-  if (p == i) {
-    st_dec(&dec[i], leaf_dec(nd));
-    return;
-  }
-  // the decision bytes (all K_LEAF, zero) that the emission reads
-  __stcg(reinterpret_cast<uint2*>(reinterpret_cast<char*>(&dec[i]) + offsetof(Dec, meta)), make_uint2(0u, 0u));
-  for (uint32_t guard = 0; guard < n; guard++) {
-    // the parent's node, its children and its own parent are static: load
-    // them before the arrival so their latency overlaps the atomic's (the
-    // climb's latency, not its traffic, bounds this kernel)
+
+  // One level; true when the climb ends (first to arrive, or the root done).
+  __device__ __forceinline__ bool step() {
+    if (++steps > n) {
+      set_status(status, ST_ITER_LIMIT);
+      return true;
+    }
+    // the parent's node, its own parent and (by the left-odd sibling rule,
+    // checked below) the sibling's node are static: load them before the
+    // arrival so their latency overlaps the atomic's
     const Bvh2Node pn = ld_node(&nodes[p]);
     const uint32_t up = parents[p];
+    uint32_t sg = sibling_of(c);
+    if (sg >= n) sg = c;  // a tree that breaks the rule: the real sibling is read below
+    const Bvh2Node sg_node = ld_node(&nodes[sg]);
+    if (!own_leaf) st_rec(&crec[c], own);
+    if (atom_add_acq_rel(&flags[p], 1u) == 0) return true;
     const uint32_t f = node_first(pn);
-    const Bvh2Node cl = ld_node(&nodes[f]), cr = ld_node(&nodes[f + 1]);
-    if (atom_add_acq_rel(&flags[p], 1u) == 0) return;
-    inner_costs(pn, cl, cr, dec, p, max_prims);
-    if (up == p) return;
+    const uint32_t s = c == f ? f + 1 : f;
+    const Bvh2Node sn = s == sg ? sg_node : ld_node(&nodes[s]);
+    const bool sib_leaf = node_prims(sn) != 0;
+    const CostRec other = sib_leaf ? leaf_rec(sn) : ld_rec_cg(&crec[s]);
+    const uint32_t np = own.nprim + other.nprim;
+    uint4 list = make_uint4(0u, 0u, 0u, np);
+    if (np <= 3) {
+      const uint4 ol = sib_leaf ? make_uint4(__ldg(&pidx_in[node_first(sn)]), 0u, 0u, 1u) : __ldcg(&small[s]);
+      const uint4 l = c == f ? own_list : ol, r = c == f ? ol : own_list;
+      // the left child's primitives, then the right child's
+      const uint32_t v[3] = {l.x, l.y, l.z};
+      list.x = v[0];
+      list.y = l.w > 1 ? v[1] : r.x;
+      list.z = l.w > 2 ? v[2] : (l.w == 2 ? r.x : r.y);
+      __stcg(&small[p], list);
+    }
+    uint32_t aggn0;
+    own = c == f ? inner_rec(own, other, half_area(node_box(pn)), max_prims, &aggn0)
+                 : inner_rec(other, own, half_area(node_box(pn)), max_prims, &aggn0);
+    own_list = list;
+    own_leaf = false;
+    __stcg(&erec[p], make_uint4(own.meta, aggn0, own.nprim, 0u));
+    if (up == p) return true;
+    c = p;
     p = up;
+    return false;
   }
-  set_status(status, ST_ITER_LIMIT);
-}
+};
 
-// get_children (src/cwbvh/bvh2_to_cwbvh.rs:346-397) with an explicit stack.
-// Returns the child count, or -1 on an invalid distribution.
-__device__ int get_children(const Bvh2Node* nodes, const Dec* dec, uint32_t x, uint32_t ch[8]) {
-  uint32_t st[16];  // node | (i << 28) | (expand << 31)
-  int sp = 0, cnt = 0;
-  st[sp++] = x | 0x80000000u;
-  while (sp) {
-    const uint32_t e = st[--sp];
-    const uint32_t n = e & 0x0fffffffu;
-    if (!(e & 0x80000000u)) {
-      if (cnt >= 8) return -1;
-      ch[cnt++] = n;
+// Lanes of a k_costs warp take new nodes once this many of them are idle.
+constexpr uint32_t COST_REFILL_IDLE = 8;
+
+// Persistent climbs: every lane takes node indices from a counter (one
+// atomic per warp) and climbs from the leaves among them; a lane whose climb
+// ends counts itself idle, and once COST_REFILL_IDLE lanes of its warp are
+// idle they take new nodes while the others keep climbing.  Climbs of very
+// different lengths so never hold a block (or a warp) for their longest
+// member.  `next` starts at 0.
+__global__ void __launch_bounds__(BLK) k_costs(const Bvh2Node* __restrict__ nodes, const uint32_t* __restrict__ parents,
+                                               const uint32_t* __restrict__ pidx_in, uint32_t n, uint32_t max_prims,
+                                               CostRec* crec, EmitRec* erec, uint4* small, uint32_t* flags,
+                                               uint32_t* next, uint32_t* status) {
+  grid_dep_wait();
+  const uint32_t FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  __shared__ uint32_t s_idle[BLK / 32];
+  uint32_t* idle_ctr = &s_idle[threadIdx.x >> 5];
+  CostClimb cl;
+  cl.nodes = nodes;
+  cl.parents = parents;
+  cl.pidx_in = pidx_in;
+  cl.crec = crec;
+  cl.erec = erec;
+  cl.small = small;
+  cl.flags = flags;
+  cl.status = status;
+  cl.n = n;
+  cl.max_prims = max_prims;
+  bool alive = false, drained = false;
+  for (;;) {
+    if (!drained) {
+      const uint32_t need = __ballot_sync(FULL, !alive);
+      if (need) {
+        const int leader = __ffs(need) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(next, (uint32_t)__popc(need));
+        base = __shfl_sync(FULL, base, leader);
+        if ((uint64_t)base + __popc(need) >= n) drained = true;
+        if (!alive) {
+          const uint32_t i = base + __popc(need & lt_mask);
+          if (i < n) alive = cl.start(i);
+        }
+      }
+    }
+    const uint32_t idle_now = __ballot_sync(FULL, !alive);
+    if (idle_now == FULL) {
+      if (drained) return;
       continue;
     }
-    const int i = (e >> 28) & 7;
-    const Bvh2Node nd = ld_node(&nodes[n]);
-    if (node_prims(nd) != 0) {
-      if (cnt >= 8) return -1;
-      ch[cnt++] = n;
-      continue;
+    if (lane == 0) *idle_ctr = __popc(idle_now);
+    __syncwarp();
+    if (alive) {
+      for (;;) {
+        if (cl.step()) {
+          alive = false;
+          atomicAdd(idle_ctr, 1u);
+          break;
+        }
+        if (!drained && *(volatile uint32_t*)idle_ctr >= COST_REFILL_IDLE) break;
+      }
     }
-    const uint8_t m = dec[n].meta[i];
-    const uint8_t dl = dl_of(m), dr = dr_of(m);
-    if (dl == DL_INVALID || dr == DL_INVALID) return -1;
-    const uint32_t f = node_first(nd);
-    if (sp + 2 > 16) return -1;
-    // right first so the left subtree's children come out first
-    st[sp++] = kind_of(dec[f + 1].meta[dr]) == K_DISTRIBUTE ? ((f + 1) | ((uint32_t)dr << 28) | 0x80000000u) : (f + 1);
-    st[sp++] = kind_of(dec[f].meta[dl]) == K_DISTRIBUTE ? (f | ((uint32_t)dl << 28) | 0x80000000u) : f;
+    __syncwarp();
   }
-  return cnt;
 }
 
 __device__ __forceinline__ float pow2f(float c) {
@@ -275,8 +381,8 @@ __device__ __forceinline__ float3 center(const Box& b) {
   return make_float3((b.mx.x + b.mn.x) * 0.5f, (b.mx.y + b.mn.y) * 0.5f, (b.mx.z + b.mn.z) * 0.5f);
 }
 
-// Emission work queue: items[k] describes CWBVH node k's source; it is
-// published (ready[k] = 1) by the warp that emits its parent.  Warps take
+// Emission work queue: items[k] describes a CWBVH node's source; it is
+// published (ready[k] = 1) by the thread that emits its parent.  Warps take
 // indices in order from `head` and append children at `tail`.
 struct EmitOut {
   CwNode* cw;
@@ -289,7 +395,8 @@ struct EmitArgs {
   uint32_t log2_thr[256];  // ceil_log2_thresholds()
   const Bvh2Node* nodes;
   const uint32_t* pidx_in;
-  const Dec* dec;
+  const EmitRec* erec;
+  const uint4* small;  // primitive lists of nodes with at most 3 primitives
   Item* items;
   uint32_t* ready;
   uint32_t* head;
@@ -305,279 +412,467 @@ struct EmitArgs {
   uint32_t* processed;
 };
 
-// exclusive scan over lanes 0..7 (lanes 8..31 hold 0); *total = sum
-__device__ __forceinline__ uint32_t slot_excl_scan(uint32_t v, int lane, uint32_t* total) {
-  uint32_t x = v;
-#pragma unroll
-  for (int o = 1; o < 8; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
+// Per-thread staging of k_emit_all in shared memory: for child c of thread t,
+// four 16-byte chunks at [4c + j][t] (consecutive threads, consecutive
+// chunks: conflict-free): the BVH2 node (two chunks), its emission record,
+// its primitive list.  They are copied with cp.async, all eight children's
+// at once, so the copies are in flight together.
+struct EmitShared {
+  uint32_t thr[256];
+  uint4 stg[8 * 4][EMIT_TB];
+};
+
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// The children of CWBVH node x (get_children, src/cwbvh/bvh2_to_cwbvh.rs:
+// 346-397): x's slot-0 distribution, whose leaves taken left to right are the
+// children in the reference's depth-first order.  The walk goes level by
+// level so that the loads of one level's expansions are in flight together:
+// an entry (first child, dl | dr << 4) expands a node's two children with
+// those slot budgets, (node, 0xff) is a child.  Returns the count, or -1 for
+// an invalid distribution (or more than 8 children).
+__device__ int gather_children(const EmitArgs& a, uint32_t x, const Bvh2Node& xn, uint32_t xmeta, uint32_t ch[8]) {
+  if (node_prims(xn) != 0) {  // a leaf root: the node is its own only child
+    ch[0] = x;
+    return 1;
   }
-  *total = __shfl_sync(0xffffffffu, x, 7);
-  return x - v;
+  const Decision d0 = decode(xmeta, 0);
+  if (d0.dl == DL_INVALID) return -1;
+  uint32_t ex[8], ey[8];
+  int m = 1;
+  ex[0] = node_first(xn);
+  ey[0] = d0.dl | d0.dr << 4;
+  const uint32_t* nw = reinterpret_cast<const uint32_t*>(a.nodes);
+  for (int round = 0; round < 8; round++) {
+    uint32_t pl[8], pr[8], fl[8], fr[8], ml[8], mr[8];
+    bool any = false;
+#pragma unroll
+    for (int e = 0; e < 8; e++) {
+      if (e < m && ey[e] != 0xffu) {
+        any = true;
+        const size_t f = ex[e];
+        pl[e] = __ldg(nw + 8 * f + 3);
+        fl[e] = __ldg(nw + 8 * f + 7);
+        pr[e] = __ldg(nw + 8 * (f + 1) + 3);
+        fr[e] = __ldg(nw + 8 * (f + 1) + 7);
+        ml[e] = __ldg(&a.erec[f].x);
+        mr[e] = __ldg(&a.erec[f + 1].x);
+      }
+    }
+    if (!any) break;
+    uint32_t nx[8], ny[8];
+    int nm = 0;
+#pragma unroll
+    for (int e = 0; e < 8; e++) {
+      if (e < m) {
+        if (ey[e] == 0xffu) {
+          if (nm >= 8) return -1;
+          nx[nm] = ex[e];
+          ny[nm++] = 0xffu;
+        } else {
+          if (nm + 2 > 8) return -1;
+          const uint32_t f = ex[e], dl = ey[e] & 15u, dr = ey[e] >> 4;
+          // a child that distributes at its budget is expanded next round
+          if (pl[e] == 0) {
+            const Decision dd = decode(ml[e], dl);
+            nx[nm] = dd.kind == K_DISTRIBUTE ? fl[e] : f;
+            ny[nm++] = dd.kind == K_DISTRIBUTE ? (dd.dl | dd.dr << 4) : 0xffu;
+          } else {
+            nx[nm] = f;
+            ny[nm++] = 0xffu;
+          }
+          if (pr[e] == 0) {
+            const Decision dd = decode(mr[e], dr);
+            nx[nm] = dd.kind == K_DISTRIBUTE ? fr[e] : f + 1;
+            ny[nm++] = dd.kind == K_DISTRIBUTE ? (dd.dl | dd.dr << 4) : 0xffu;
+          } else {
+            nx[nm] = f + 1;
+            ny[nm++] = 0xffu;
+          }
+        }
+      }
+    }
+    m = nm;
+    for (int e = 0; e < m; e++) {
+      ex[e] = nx[e];
+      ey[e] = ny[e];
+    }
+  }
+  for (int e = 0; e < m; e++) {
+    if (ey[e] != 0xffu) return -1;
+    ch[e] = ex[e];
+  }
+  return m;
 }
 
-// convert_to_cwbvh_impl (src/cwbvh/bvh2_to_cwbvh.rs:75-193) for one node;
-// the whole warp works on it, lane s on child slot s.
-__device__ void emit_node(const EmitArgs& a, const Item it, int lane, uint8_t* stage) {
-  const EmitOut o = a.seg_out ? a.seg_out[seg_find(a.node_start, a.n_seg, it.bvh2)] : a.one;
-  const Bvh2Node nd = ld_node(&a.nodes[it.bvh2]);
-  const Box box = node_box(nd);
-  const float3 p = box.mn;
-  const float ex = exp_grid(smax(box.mx.x - box.mn.x, 1e-20f) * DENOM, a.log2_thr);
-  const float ey = exp_grid(smax(box.mx.y - box.mn.y, 1e-20f) * DENOM, a.log2_thr);
-  const float ez = exp_grid(smax(box.mx.z - box.mn.z, 1e-20f) * DENOM, a.log2_thr);
-  const float rx = 1.0f / ex, ry = 1.0f / ey, rz = 1.0f / ez;
+__device__ __forceinline__ uint32_t q_byte(float v) { return (uint32_t)(uint8_t)smin(smax(v, 0.0f), 255.0f); }
 
-  // children (lane 0 walks the distribution), one per lane
-  uint32_t ch[8];
-  int cnt = 0;
-  if (lane == 0) cnt = get_children(a.nodes, a.dec, it.bvh2, ch);
-  cnt = __shfl_sync(0xffffffffu, cnt, 0);
-  if (cnt < 0) {
-    if (lane == 0) set_status(a.status, ST_BAD_INPUT);
-    return;
+// State of one node between the two halves of its emission.
+struct EmitNode {
+  Item it;
+  EmitOut o;
+  float3 p, e, r;  // grid origin, cell size, 1 / cell size
+  Box box;
+  int cnt;
+  uint32_t n_int;
+  uint32_t leafprims;  // primitives of the leaf children
+  uint32_t ch[8];      // the children's BVH2 nodes, in get_children order
+};
+
+// What child c contributes, from its staged records: internal (CWBVH nodes
+// below it, its primitives) or leaf (its primitive count); false for a
+// malformed record.
+struct ChildInfo {
+  bool internal;
+  uint32_t count;  // internal: CWBVH nodes below its own node; leaf: primitives
+  uint32_t nprim;  // internal: its primitives
+};
+__device__ __forceinline__ bool child_info(const uint4 (*stg)[EMIT_TB], int c, int t, ChildInfo& ci) {
+  const uint4 er = stg[4 * c + 2][t], sl = stg[4 * c + 3][t];
+  const uint32_t prims = stg[4 * c][t].w;
+  ci.internal = false;
+  ci.nprim = 0;
+  if (prims != 0) {  // a BVH2 leaf: one primitive, listed by the cost climb
+    ci.count = prims;
+    return sl.w == 1 && prims == 1;
   }
-  uint32_t my_child = OBVHS_INVALID;  // child number `lane` before ordering
+  if (decode(er.x, 0).kind == K_LEAF) {
+    ci.count = er.z;
+    return sl.w == er.z && er.z <= 3;
+  }
+  if (er.y == AGG_INVALID) return false;
+  ci.internal = true;
+  ci.count = er.y;
+  ci.nprim = er.z;
+  return true;
+}
+
+// First half of convert_to_cwbvh_impl (src/cwbvh/bvh2_to_cwbvh.rs:75-193)
+// for one node: its grid, its children (records staged in shared memory)
+// and how many of them are internal.  Returns false on a malformed decision
+// (status set).
+__device__ bool emit_gather(const EmitArgs& a, const uint32_t* thr, uint4 (*stg)[EMIT_TB], int t, EmitNode& s) {
+  s.o = a.seg_out ? a.seg_out[seg_find(a.node_start, a.n_seg, s.it.bvh2)] : a.one;
+  const Bvh2Node xn = ld_node(&a.nodes[s.it.bvh2]);
+  const uint32_t xmeta = __ldg(&a.erec[s.it.bvh2].x);
+  s.box = node_box(xn);
+  s.p = s.box.mn;
+  s.e = make_float3(exp_grid(smax(s.box.mx.x - s.box.mn.x, 1e-20f) * DENOM, thr),
+                    exp_grid(smax(s.box.mx.y - s.box.mn.y, 1e-20f) * DENOM, thr),
+                    exp_grid(smax(s.box.mx.z - s.box.mn.z, 1e-20f) * DENOM, thr));
+  s.r = make_float3(1.0f / s.e.x, 1.0f / s.e.y, 1.0f / s.e.z);
+  s.cnt = gather_children(a, s.it.bvh2, xn, node_prims(xn) != 0 ? 0u : xmeta, s.ch);
+  s.n_int = 0;
+  s.leafprims = 0;
+  if (s.cnt < 0) {
+    set_status(a.status, ST_BAD_INPUT);
+    return false;
+  }
+  for (int c = 0; c < s.cnt; c++) {
+    const uint32_t k = s.ch[c];
+    const uint4* nq = reinterpret_cast<const uint4*>(&a.nodes[k]);
+    cp_async16(&stg[4 * c][t], nq);
+    cp_async16(&stg[4 * c + 1][t], nq + 1);
+    cp_async16(&stg[4 * c + 2][t], &a.erec[k]);
+    cp_async16(&stg[4 * c + 3][t], &a.small[k]);
+  }
+  cp_async_wait_all();
+  bool ok = true;
+  for (int c = 0; c < s.cnt; c++) {
+    ChildInfo ci;
+    ok &= child_info(stg, c, t, ci);
+    if (ci.internal)
+      s.n_int++;
+    else
+      s.leafprims += ci.count;
+  }
+  if (!ok) {
+    set_status(a.status, ST_BAD_INPUT);
+    return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ Box staged_box(const uint4 (*stg)[EMIT_TB], int c, int t) {
+  const uint4 a = stg[4 * c][t], b = stg[4 * c + 1][t];
+  return Box{make_float3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z)),
+             make_float3(__uint_as_float(b.x), __uint_as_float(b.y), __uint_as_float(b.z))};
+}
+
+// order_children's cost of putting a child whose centre is v away from the
+// node's centre into slot sl: dot(direction of sl, v), unfused.
+__device__ __forceinline__ float slot_cost(float3 v, int sl) {
+  const float dx = (sl & 4) ? -1.0f : 1.0f, dy = (sl & 2) ? -1.0f : 1.0f, dz = (sl & 1) ? -1.0f : 1.0f;
+  return (dx * v.x + dy * v.y) + dz * v.z;
+}
+
+// Smallest cost of child v over the free slots (first slot on ties), and its
+// slot (8: none below f32::MAX).
+__device__ __forceinline__ void row_min(float3 v, uint32_t filled, float& m, uint32_t& arg) {
+  m = 3.40282347e+38f;
+  arg = 8;
 #pragma unroll
-  for (int c = 0; c < 8; c++) {
-    const uint32_t v = __shfl_sync(0xffffffffu, lane == 0 ? ch[c] : 0u, 0);
-    if (lane == c && c < cnt) my_child = v;
+  for (int sl = 0; sl < 8; sl++) {
+    const float cst = slot_cost(v, sl);
+    if (!((filled >> sl) & 1u) && cst < m) {
+      m = cst;
+      arg = (uint32_t)sl;
+    }
   }
-  uint32_t slot_child = OBVHS_INVALID;  // child placed in slot `lane`
+}
+
+// Second half: the children placed in slots (order_children,
+// src/cwbvh/bvh2_to_cwbvh.rs:402-467, or in order), their metas and offsets,
+// the leaf children's primitives (count_primitives: recorded in depth-first
+// order by the cost climb), the internal children published at queue slots
+// qbase.., and the 80-byte node written.
+__device__ void emit_finish(const EmitArgs& a, const uint4 (*stg)[EMIT_TB], int t, const EmitNode& s,
+                            uint32_t qbase) {
+  const int cnt = s.cnt;
+  uint32_t slot_of = 0;  // 3 bits per child
   if (a.order_children) {
-    // order_children (src/cwbvh/bvh2_to_cwbvh.rs:402-467): the cost of
-    // (child c, direction s) sits at idx = 8c + s, two per lane; the greedy
-    // loop takes the smallest cost (first in (c, s) order on ties) among
-    // unassigned children and unfilled slots while one is below f32::MAX.
-    const float3 pc = center(box);
-    float cost[2];
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const int idx = lane + 32 * h;
-      const int c = idx >> 3, s = idx & 7;
-      const uint32_t chc = __shfl_sync(0xffffffffu, my_child, c);
-      cost[h] = 3.40282347e+38f;
-      if (c < cnt) {
-        const float3 cc = center(node_box(ld_node(&a.nodes[chc])));
-        const float3 v = make_float3(cc.x - pc.x, cc.y - pc.y, cc.z - pc.z);
-        const float dx = (s & 4) ? -1.0f : 1.0f, dy = (s & 2) ? -1.0f : 1.0f, dz = (s & 1) ? -1.0f : 1.0f;
-        cost[h] = (dx * v.x + dy * v.y) + dz * v.z;
-      }
-    }
-    uint32_t assigned = 0, filled = 0, assign = 0;  // assign: 3 bits per child
-    for (int iter = 0; iter < 8; iter++) {
-      float bc = 3.40282347e+38f;
-      uint32_t bi = 0xffffffffu;
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const uint32_t idx = lane + 32 * h;
-        const int c = idx >> 3, s = idx & 7;
-        if (c < cnt && !((assigned >> c) & 1) && !((filled >> s) & 1) && cost[h] < bc) {
-          bc = cost[h];
-          bi = idx;
-        }
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float oc = __shfl_xor_sync(0xffffffffu, bc, o);
-        const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (oi != 0xffffffffu && (bi == 0xffffffffu || oc < bc || (oc == bc && oi < bi))) {
-          bc = oc;
-          bi = oi;
-        }
-      }
-      if (bi == 0xffffffffu) break;
-      const int c = bi >> 3, s = bi & 7;
-      assigned |= 1u << c;
-      filled |= 1u << s;
-      assign |= (uint32_t)s << (3 * c);
-    }
-    if (__popc(assigned) != cnt) {
-      if (lane == 0) set_status(a.status, ST_BAD_INPUT);
-      return;
-    }
+    // The reference's greedy loop takes, while one is below f32::MAX, the
+    // smallest cost (first in (child, slot) order on ties) among unassigned
+    // children and free slots.  Kept as per-child minima over the free slots:
+    // the pick is the smallest (minimum, child), and only children whose
+    // minimum sat in the slot just taken need a new one.
+    const float3 pc = center(s.box);
+    float3 v[8];
+    float rm[8];
+    uint32_t ra[8];
 #pragma unroll
     for (int c = 0; c < 8; c++) {
-      const uint32_t v = __shfl_sync(0xffffffffu, my_child, c);
-      if (c < cnt && (int)((assign >> (3 * c)) & 7) == lane) slot_child = v;
+      v[c] = make_float3(0.0f, 0.0f, 0.0f);
+      rm[c] = 3.40282347e+38f;
+      ra[c] = 8;
+      if (c < cnt) {
+        const float3 cc = center(staged_box(stg, c, t));
+        v[c] = make_float3(cc.x - pc.x, cc.y - pc.y, cc.z - pc.z);
+        row_min(v[c], 0u, rm[c], ra[c]);
+      }
+    }
+    uint32_t assigned = 0, filled = 0;
+    for (int iter = 0; iter < 8; iter++) {
+      float bc = 3.40282347e+38f;
+      int bi = -1;
+#pragma unroll
+      for (int c = 0; c < 8; c++) {
+        if (c < cnt && !((assigned >> c) & 1u) && ra[c] < 8 && rm[c] < bc) {
+          bc = rm[c];
+          bi = c;
+        }
+      }
+      if (bi < 0) break;
+      uint32_t sl = 0;
+#pragma unroll
+      for (int c = 0; c < 8; c++)
+        if (c == bi) sl = ra[c];
+      assigned |= 1u << bi;
+      filled |= 1u << sl;
+      slot_of |= sl << (3 * bi);
+#pragma unroll
+      for (int c = 0; c < 8; c++)
+        if (c < cnt && !((assigned >> c) & 1u) && ra[c] == sl) row_min(v[c], filled, rm[c], ra[c]);
+    }
+    if (__popc(assigned) != cnt) {
+      set_status(a.status, ST_BAD_INPUT);
+      return;
     }
   } else {
-    slot_child = my_child;
+    for (int c = 0; c < cnt; c++) slot_of |= (uint32_t)c << (3 * c);
+  }
+  uint32_t child_in_slot = 0xffffffffu;  // 4 bits per slot, 0xf = empty
+  for (int c = 0; c < cnt; c++) {
+    const uint32_t sl = (slot_of >> (3 * c)) & 7u;
+    child_in_slot = (child_in_slot & ~(0xfu << (4 * sl))) | ((uint32_t)c << (4 * sl));
   }
 
-  // per slot: quantised box, kind, primitive count or subtree size
-  const bool has = lane < 8 && slot_child != OBVHS_INVALID;
-  uint8_t q[6] = {0, 0, 0, 0, 0, 0};
-  uint32_t is_int = 0, leaf_pc = 0, sub_nodes = 0, sub_prims = 0;
-  if (has) {
-    const Bvh2Node cn = ld_node(&a.nodes[slot_child]);
-    const Box cb = node_box(cn);
-    const float lo[3] = {floorf(((cb.mn.x - p.x) - 0.0f) * rx), floorf(((cb.mn.y - p.y) - 0.0f) * ry),
-                         floorf(((cb.mn.z - p.z) - 0.0f) * rz)};
-    const float hi[3] = {ceilf(((cb.mx.x - p.x) + 0.0f) * rx), ceilf(((cb.mx.y - p.y) + 0.0f) * ry),
-                         ceilf(((cb.mx.z - p.z) + 0.0f) * rz)};
+  uint32_t w[20];
+  w[0] = __float_as_uint(s.p.x);
+  w[1] = __float_as_uint(s.p.y);
+  w[2] = __float_as_uint(s.p.z);
+  w[4] = s.it.child_base;
+  w[5] = s.it.prim_base;
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-      q[2 * k] = (uint8_t)smin(smax(lo[k], 0.0f), 255.0f);
-      q[2 * k + 1] = (uint8_t)smin(smax(hi[k], 0.0f), 255.0f);
-    }
-    const Dec& cd = a.dec[slot_child];
-    const uint8_t kind = node_prims(cn) != 0 ? K_LEAF : kind_of(cd.meta[0]);
-    if (kind == K_LEAF) {
-      leaf_pc = node_prims(cn) != 0 ? node_prims(cn) : cd.nprim;
-    } else if (kind == K_INTERNAL) {
-      if (cd.agg[0].x == AGG_INVALID) {
-        set_status(a.status, ST_BAD_INPUT);
+  for (int k = 6; k < 20; k++) w[k] = 0;
+  uint32_t imask = 0, int_rank = 0, leaf_off = 0, sub_node_off = 0, sub_prim_off = 0;
+#pragma unroll
+  for (int sl = 0; sl < 8; sl++) {
+    const uint32_t c = (child_in_slot >> (4 * sl)) & 0xfu;
+    if (c == 0xfu) continue;
+    ChildInfo ci;
+    child_info(stg, (int)c, t, ci);
+    const Box cb = staged_box(stg, (int)c, t);
+    const uint32_t lo = q_byte(floorf(((cb.mn.x - s.p.x) - 0.0f) * s.r.x)) |
+                        q_byte(floorf(((cb.mn.y - s.p.y) - 0.0f) * s.r.y)) << 8 |
+                        q_byte(floorf(((cb.mn.z - s.p.z) - 0.0f) * s.r.z)) << 16;
+    const uint32_t hi = q_byte(ceilf(((cb.mx.x - s.p.x) + 0.0f) * s.r.x)) |
+                        q_byte(ceilf(((cb.mx.y - s.p.y) + 0.0f) * s.r.y)) << 8 |
+                        q_byte(ceilf(((cb.mx.z - s.p.z) + 0.0f) * s.r.z)) << 16;
+    uint32_t meta;
+    if (ci.internal) {
+      meta = (24u + sl) | 0x20u;
+      imask |= 1u << sl;
+      // the internal children's own nodes come first, then their subtrees
+      const uint32_t q = qbase + int_rank;
+      if (q < a.queue_cap) {
+        a.items[q] = Item{s.ch[c], s.it.child_base + int_rank, s.it.child_base + s.n_int + sub_node_off,
+                          s.it.prim_base + s.leafprims + sub_prim_off};
+        __threadfence();
+        atomicExch(&a.ready[q], 1u);
       } else {
-        is_int = 1;
-        sub_nodes = cd.agg[0].x;  // CWBVH nodes below the child's own node
-        sub_prims = cd.nprim;
+        set_status(a.status, ST_CAPACITY);
       }
+      int_rank++;
+      sub_node_off += ci.count;
+      sub_prim_off += ci.nprim;
     } else {
-      set_status(a.status, ST_BAD_INPUT);
-    }
-  }
-  uint32_t n_int, n_leafprims, t0, t1;
-  const uint32_t int_rank = slot_excl_scan(is_int, lane, &n_int);
-  const uint32_t leaf_off = slot_excl_scan(leaf_pc, lane, &n_leafprims);
-  const uint32_t sub_node_off = slot_excl_scan(sub_nodes, lane, &t0);
-  const uint32_t sub_prim_off = slot_excl_scan(sub_prims, lane, &t1);
-  uint32_t out_base = 0;
-  if (lane == 0 && n_int) out_base = atomicAdd(a.tail, n_int);
-  out_base = __shfl_sync(0xffffffffu, out_base, 0);
-
-  uint8_t meta = 0;
-  if (has && leaf_pc) {
-    const uint8_t u = leaf_pc == 1 ? 0x20 : leaf_pc == 2 ? 0x60 : leaf_pc == 3 ? 0xe0 : 0;
-    if (!u) set_status(a.status, ST_BAD_INPUT);
-    meta = (uint8_t)leaf_off | u;
-    // count_primitives: DFS of the leaf subtree, left before right
-    uint32_t st[8];
-    int sp = 0;
-    uint32_t k = 0;
-    st[sp++] = slot_child;
-    while (sp) {
-      const uint32_t x = st[--sp];
-      const Bvh2Node xn = ld_node(&a.nodes[x]);
-      if (node_prims(xn) != 0) {
-        const uint32_t slot = it.prim_base + leaf_off + k;
-        if (slot < o.max_prims)
-          o.pidx[slot] = a.pidx_in[node_first(xn)];
-        else
-          set_status(a.status, ST_CAPACITY);
-        k += node_prims(xn);
+      const uint32_t u = ci.count == 1 ? 0x20u : ci.count == 2 ? 0x60u : ci.count == 3 ? 0xe0u : 0u;
+      if (!u) set_status(a.status, ST_BAD_INPUT);
+      meta = leaf_off | u;
+      // count_primitives: the leaf's primitives in depth-first order
+      const uint4 pl = stg[4 * c + 3][t];
+      const uint32_t slot = s.it.prim_base + leaf_off;
+      if (slot + ci.count <= s.o.max_prims) {
+        s.o.pidx[slot] = pl.x;
+        if (ci.count > 1) s.o.pidx[slot + 1] = pl.y;
+        if (ci.count > 2) s.o.pidx[slot + 2] = pl.z;
       } else {
-        if (sp + 2 > 8) {
-          set_status(a.status, ST_BAD_INPUT);
-          break;
-        }
-        st[sp++] = node_first(xn) + 1;
-        st[sp++] = node_first(xn);
+        set_status(a.status, ST_CAPACITY);
       }
+      leaf_off += ci.count;
     }
-  } else if (is_int) {
-    meta = (uint8_t)((24 + lane) | 0x20);
-    // the internal children's own nodes come first, then their subtrees
-    const uint32_t cb = it.child_base + n_int + sub_node_off;
-    const uint32_t pb = it.prim_base + n_leafprims + sub_prim_off;
-    const uint32_t q = out_base + int_rank;
-    if (q < a.queue_cap) {
-      a.items[q] = Item{slot_child, it.child_base + int_rank, cb, pb};
-      __threadfence();
-      atomicExch(&a.ready[q], 1u);
-    } else {
-      set_status(a.status, ST_CAPACITY);
-    }
+    // bytes 24 + sl (meta), 32 + sl (lo x), 40 (hi x), 48 (lo y), 56 (hi y),
+    // 64 (lo z), 72 (hi z)
+    const int sh = 8 * (sl & 3), hw = sl >> 2;
+    w[6 + hw] |= meta << sh;
+    w[8 + hw] |= (lo & 0xffu) << sh;
+    w[10 + hw] |= (hi & 0xffu) << sh;
+    w[12 + hw] |= ((lo >> 8) & 0xffu) << sh;
+    w[14 + hw] |= ((hi >> 8) & 0xffu) << sh;
+    w[16 + hw] |= ((lo >> 16) & 0xffu) << sh;
+    w[18 + hw] |= ((hi >> 16) & 0xffu) << sh;
   }
-  const uint32_t imask = __ballot_sync(0xffffffffu, is_int != 0) & 0xffu;
-
-  // assemble the 80-byte node in shared memory, then five 16-byte stores
-  if (lane == 0) {
-    uint32_t* w = reinterpret_cast<uint32_t*>(stage);
-    w[0] = __float_as_uint(p.x);
-    w[1] = __float_as_uint(p.y);
-    w[2] = __float_as_uint(p.z);
-    w[3] = (__float_as_uint(ex) >> 23) | (__float_as_uint(ey) >> 23) << 8 | (__float_as_uint(ez) >> 23) << 16 |
-           imask << 24;
-    w[4] = it.child_base;
-    w[5] = it.prim_base;
+  w[3] = (__float_as_uint(s.e.x) >> 23) | (__float_as_uint(s.e.y) >> 23) << 8 | (__float_as_uint(s.e.z) >> 23) << 16 |
+         imask << 24;
+  if (s.it.cw >= s.o.max_nodes) {
+    set_status(a.status, ST_CAPACITY);
+    return;
   }
-  if (lane < 8) {
-    stage[24 + lane] = meta;
-    stage[32 + lane] = q[0];
-    stage[40 + lane] = q[1];
-    stage[48 + lane] = q[2];
-    stage[56 + lane] = q[3];
-    stage[64 + lane] = q[4];
-    stage[72 + lane] = q[5];
+  uint4* dst = s.o.cw[s.it.cw].q;
+#pragma unroll
+  for (int k = 0; k < 5; k++) dst[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+  if (s.o.exact) {  // src/cwbvh/bvh2_to_cwbvh.rs:76-80
+    s.o.exact[2 * (size_t)s.it.cw] = make_float4(s.box.mn.x, s.box.mn.y, s.box.mn.z, 0.0f);
+    s.o.exact[2 * (size_t)s.it.cw + 1] = make_float4(s.box.mx.x, s.box.mx.y, s.box.mx.z, 0.0f);
   }
-  __syncwarp();
-  if (it.cw >= o.max_nodes) {
-    if (lane == 0) set_status(a.status, ST_CAPACITY);
-  } else if (lane < 5) {
-    o.cw[it.cw].q[lane] = reinterpret_cast<const uint4*>(stage)[lane];
-  } else if (lane < 7 && o.exact) {  // src/cwbvh/bvh2_to_cwbvh.rs:76-80
-    o.exact[2 * (size_t)it.cw + (lane - 5)] = lane == 5 ? make_float4(box.mn.x, box.mn.y, box.mn.z, 0.0f)
-                                                         : make_float4(box.mx.x, box.mx.y, box.mx.z, 0.0f);
-  }
-  __syncwarp();
 }
 
-__global__ void __launch_bounds__(EMIT_THREADS) k_emit_all(EmitArgs a) {
+// A thread per CWBVH node.  Each lane holds at most one queue item; idle
+// lanes take the next items (one atomic per warp), and each round the lanes
+// whose items have been published emit them while the others keep waiting.
+// A held item's parent was taken earlier by a running thread, so some held
+// item is always published eventually; waits are bounded (status
+// ST_ITER_LIMIT), and a failed node (status set) ends every wait.
+__global__ void __launch_bounds__(EMIT_TB) k_emit_all(EmitArgs a) {
   grid_dep_wait();
-  __shared__ __align__(16) uint8_t stage[EMIT_THREADS / 32][80];
-  const int lane = threadIdx.x & 31;
-  uint32_t mine = 0;
+  __shared__ EmitShared sm;
+  for (int k = threadIdx.x; k < 256; k += EMIT_TB) sm.thr[k] = a.log2_thr[k];
+  __syncthreads();
+  const uint32_t FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, t = threadIdx.x;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  uint32_t held = OBVHS_INVALID, mine = 0, waits = 0, ns = 32;
+  bool drained = false;  // (warp-uniform) the queue has been handed out
   for (;;) {
-    uint32_t k = 0;
-    if (lane == 0) k = atomicAdd(a.head, 1u);
-    k = __shfl_sync(0xffffffffu, k, 0);
-    if (k >= a.queue_cap) break;
-    // wait for the parent's warp to publish item k (bounded)
-    uint32_t ok = 1;
-    if (lane == 0) {
-      // exponential back-off: early in the build most warps wait here, and
-      // tight polling starves the warps doing the work
-      uint32_t spins = 0, ns = 32;
-      while (*(volatile uint32_t*)&a.ready[k] == 0) {
-        if (++spins > (1u << 22)) {
-          set_status(a.status, ST_ITER_LIMIT);
-          ok = 0;
-          break;
+    if (!drained) {
+      // new items only once every lane is idle: the warp then holds 32
+      // consecutive queue items, published together (by one or a few rounds
+      // of their parents' warps), so its rounds keep most lanes busy
+      const uint32_t need = __ballot_sync(FULL, held == OBVHS_INVALID);
+      if (need == FULL) {
+        const int leader = __ffs(need) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(a.head, (uint32_t)__popc(need));
+        base = __shfl_sync(FULL, base, leader);
+        if ((uint64_t)base + __popc(need) >= a.queue_cap) drained = true;
+        if (held == OBVHS_INVALID) {
+          const uint32_t k = base + __popc(need & lt_mask);
+          if (k < a.queue_cap) held = k;
         }
-        __nanosleep(ns);
-        if (ns < 2048) ns <<= 1;
       }
-      __threadfence();
     }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    if (!ok) break;
-    // through L2: this SM may hold a stale L1 line from neighbouring items
-    const uint4 raw = __ldcg(reinterpret_cast<const uint4*>(&a.items[k]));
-    const Item it{raw.x, raw.y, raw.z, raw.w};
-    emit_node(a, it, lane, stage[threadIdx.x >> 5]);
-    mine++;
+    if (__ballot_sync(FULL, held != OBVHS_INVALID) == 0) break;
+    const bool go = held != OBVHS_INVALID && *(volatile uint32_t*)&a.ready[held] != 0;
+    if (__ballot_sync(FULL, go) == 0) {
+      // nothing published yet: back off (tight polling starves the threads
+      // doing the work); give up on a failed node or after the bound
+      bool stop = ++waits > (1u << 22);
+      if ((waits & 63u) == 0 && *(volatile uint32_t*)a.status) stop = true;
+      if (__any_sync(FULL, stop)) {
+        if (lane == 0 && waits > (1u << 22)) set_status(a.status, ST_ITER_LIMIT);
+        break;
+      }
+      __nanosleep(ns);
+      if (ns < 512) ns <<= 1;
+      continue;
+    }
+    waits = 0;
+    ns = 32;
+    EmitNode s;
+    s.n_int = 0;
+    bool ok = false;
+    if (go) {
+      __threadfence();
+      // through L2: this SM may hold a stale L1 line of the items array
+      const uint4 raw = __ldcg(reinterpret_cast<const uint4*>(&a.items[held]));
+      s.it = Item{raw.x, raw.y, raw.z, raw.w};
+      ok = emit_gather(a, sm.thr, sm.stg, t, s);
+      if (!ok) s.n_int = 0;
+    }
+    // queue slots for the internal children: one atomic per warp
+    uint32_t incl = s.n_int;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total) base = atomicAdd(a.tail, total);
+    base = __shfl_sync(FULL, base, 31);
+    if (ok) {
+      emit_finish(a, sm.stg, t, s, base + incl - s.n_int);
+      mine++;
+    }
+    if (go) held = OBVHS_INVALID;
+    __syncwarp();
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(FULL, mine, o);
   if (lane == 0 && mine) atomicAdd(a.processed, mine);
 }
 
-// Segmented conversion: each scene's root decision record and box, read back
+// Segmented conversion: each scene's root emission record and box, read back
 // to size the outputs.
 struct SegRoot {
-  Dec d;
+  EmitRec d;  // (meta, CWBVH nodes below the root, primitives, 0)
   float box[8];
 };
-static_assert(sizeof(SegRoot) == 128, "SegRoot layout");
+static_assert(sizeof(SegRoot) == 48, "SegRoot layout");
 
-__global__ void k_seg_roots_out(const Bvh2Node* __restrict__ nodes, const Dec* dec,
+__global__ void k_seg_roots_out(const Bvh2Node* __restrict__ nodes, const EmitRec* erec,
                                 const uint32_t* __restrict__ prim_start, const uint32_t* __restrict__ node_start,
                                 uint32_t n_seg, SegRoot* __restrict__ out) {
   grid_dep_wait();
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_seg || prim_start[s + 1] == prim_start[s]) return;
   const uint32_t nb = node_start[s];
-  out[s].d = ld_dec_cg(&dec[nb]);
+  out[s].d = __ldcg(&erec[nb]);
   const Bvh2Node nd = ld_node(&nodes[nb]);
   float4* b = reinterpret_cast<float4*>(out[s].box);
   b[0] = nd.a;
@@ -846,6 +1141,21 @@ __global__ void __launch_bounds__(EMIT_THREADS) k_order_children(OrderArgs a) {
 
 }  // namespace
 
+// Blocks of the persistent cost climb: every resident slot, or fewer for a
+// small tree.
+static uint32_t cost_grid(BuildCtx& c, uint32_t n) {
+  static std::atomic<int> per_sm_s{0};
+  int per_sm = per_sm_s.load();
+  if (!per_sm) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_costs, BLK, 0) != cudaSuccess || per_sm < 1) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
+    per_sm_s.store(per_sm);
+  }
+  return (uint32_t)std::min<uint64_t>((uint64_t)per_sm * c.num_sms, std::max<uint32_t>(1, div_up<uint32_t>(n, BLK)));
+}
+
 // For each float exponent field e (1..254) the smallest mantissa m >= 1 with
 // ceil(log2f(2^(e-127) * (1 + m/2^23))) = e - 126, by binary search on the
 // host's log2f (monotone); 2^23 when no mantissa reaches it.
@@ -880,28 +1190,30 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   if (n == 0) return 0;
   Scratch& s = c.scratch;
   uint32_t* parents = (uint32_t*)s.get(SLOT_PARENTS, (size_t)n * 4);
-  uint32_t* flags = (uint32_t*)s.get(SLOT_FLAGS, (size_t)n * 4);
-  Dec* dec = (Dec*)s.get(SLOT_DECISIONS, (size_t)n * sizeof(Dec));
+  uint32_t* flags = (uint32_t*)s.get(SLOT_FLAGS, (size_t)n * 4 + 4);  // + k_costs' node counter
+  CostRec* crec = (CostRec*)s.get(SLOT_DECISIONS, (size_t)n * sizeof(CostRec));
+  EmitRec* erec = (EmitRec*)s.get(SLOT_CW_META, (size_t)n * sizeof(EmitRec));
+  uint4* small = (uint4*)s.get(SLOT_CW_SMALL, (size_t)n * sizeof(uint4));
   uint32_t* counters = (uint32_t*)s.get(SLOT_CW_COUNTERS, 64);
-  if (!parents || !flags || !dec || !counters) return c.fail(OBVHS_ERR_OOM, "scratch");
+  if (!parents || !flags || !crec || !erec || !small || !counters) return c.fail(OBVHS_ERR_OOM, "scratch");
   int r = compute_parents_device(c, b->nodes, n, parents);
   if (r) return r;
-  CK(cudaMemsetAsync(flags, 0, (size_t)n * 4, c.stream));
-  KLAUNCH("k_costs", launch_k(k_costs, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, b->nodes, parents, n, max_prims, dec,
-                                                                             flags, c.d_status));
+  CK(cudaMemsetAsync(flags, 0, (size_t)n * 4 + 4, c.stream));
+  KLAUNCH("k_costs", launch_k(k_costs, cost_grid(c, n), BLK, 0, c.stream, b->nodes, parents, b->prim_indices, n,
+                              max_prims, crec, erec, small, flags, flags + n, c.d_status));
   CK(cudaGetLastError());
   // sizes of the whole tree: the root's aggregate (a leaf root is one node)
-  Dec root;
-  CK(cudaMemcpyAsync(&root, dec, sizeof(Dec), cudaMemcpyDeviceToHost, c.stream));
+  EmitRec root;
+  CK(cudaMemcpyAsync(&root, erec, sizeof(EmitRec), cudaMemcpyDeviceToHost, c.stream));
   CK(cudaMemcpyAsync(c.h_status, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
   if (*c.h_status)
     return c.fail(OBVHS_ERR_BAD_INPUT, "BVH2 cannot be converted (a leaf holds more than one primitive)");
   const bool root_leaf = n == 1;
-  if (!root_leaf && root.agg[0].x == AGG_INVALID)
+  if (!root_leaf && root.y == AGG_INVALID)
     return c.fail(OBVHS_ERR_BAD_INPUT, "BVH2 cannot be converted (no finite distribution of the root)");
-  const uint32_t n_cw = root_leaf ? 1 : 1 + root.agg[0].x;
-  const uint32_t n_pr = root.nprim;
+  const uint32_t n_cw = root_leaf ? 1 : 1 + root.y;
+  const uint32_t n_pr = root.z;
   CwNode* cwn = nullptr;
   uint32_t* cwp = nullptr;
   float4* exn = nullptr;
@@ -925,7 +1237,7 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   int emit_blocks = emit_blocks_s.load();
   if (!emit_blocks) {
     int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_all, EMIT_THREADS, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_all, EMIT_TB, 0));
     emit_blocks = std::max(1, per_sm) * c.num_sms;
     emit_blocks_s.store(emit_blocks);
   }
@@ -943,12 +1255,12 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   CK(cudaMemcpyAsync(items, hst, 16, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(ready, hst + 4, 4, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(counters + 12, hst + 5, 12, cudaMemcpyHostToDevice, c.stream));
-  EmitArgs ea{{},     b->nodes,      b->prim_indices, dec, items, ready, counters + 12, counters + 13, order_children,
+  EmitArgs ea{{},     b->nodes,      b->prim_indices, erec, small, items, ready, counters + 12, counters + 13, order_children,
               n_cw,   EmitOut{cwn, cwp, n_cw, n_pr, exn}, nullptr, nullptr, 0, c.d_status, counters + 14};
   std::memcpy(ea.log2_thr, ceil_log2_thresholds(), sizeof(ea.log2_thr));
   const uint32_t grid = (uint32_t)std::min<uint64_t>(
-      emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)n_cw * 32, EMIT_THREADS)));
-  KLAUNCH("k_emit_all", launch_k(k_emit_all, grid, EMIT_THREADS, 0, c.stream, ea));
+      emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)n_cw, EMIT_TB)));
+  KLAUNCH("k_emit_all", launch_k(k_emit_all, grid, EMIT_TB, 0, c.stream, ea));
   CK(cudaGetLastError());
   out->nodes = cwn;
   out->n_nodes = n_cw;
@@ -998,20 +1310,22 @@ int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in
   }
   Scratch& sc = c.scratch;
   uint32_t* parents = (uint32_t*)sc.get(SLOT_PARENTS, (size_t)n * 4);
-  uint32_t* flags = (uint32_t*)sc.get(SLOT_FLAGS, (size_t)n * 4);
-  Dec* dec = (Dec*)sc.get(SLOT_DECISIONS, (size_t)n * sizeof(Dec));
+  uint32_t* flags = (uint32_t*)sc.get(SLOT_FLAGS, (size_t)n * 4 + 4);  // + k_costs' node counter
+  CostRec* crec = (CostRec*)sc.get(SLOT_DECISIONS, (size_t)n * sizeof(CostRec));
+  EmitRec* erec = (EmitRec*)sc.get(SLOT_CW_META, (size_t)n * sizeof(EmitRec));
+  uint4* small = (uint4*)sc.get(SLOT_CW_SMALL, (size_t)n * sizeof(uint4));
   uint32_t* counters = (uint32_t*)sc.get(SLOT_CW_COUNTERS, 64);
   SegRoot* roots = (SegRoot*)sc.get(SLOT_OUTPUT, (size_t)S * sizeof(SegRoot));
-  if (!parents || !flags || !dec || !counters || !roots) return c.fail(OBVHS_ERR_OOM, "scratch");
+  if (!parents || !flags || !crec || !erec || !small || !counters || !roots) return c.fail(OBVHS_ERR_OOM, "scratch");
   int r = compute_parents_device(c, nodes, n, parents);
   if (r) return r;
   r = seg_root_parents_device(c, L, parents);
   if (r) return r;
-  CK(cudaMemsetAsync(flags, 0, (size_t)n * 4, c.stream));
-  KLAUNCH("k_costs", launch_k(k_costs, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, nodes, parents, n, max_prims, dec, flags,
-                                                                             c.d_status));
+  CK(cudaMemsetAsync(flags, 0, (size_t)n * 4 + 4, c.stream));
+  KLAUNCH("k_costs", launch_k(k_costs, cost_grid(c, n), BLK, 0, c.stream, nodes, parents, pidx_in, n, max_prims, crec,
+                              erec, small, flags, flags + n, c.d_status));
   KLAUNCH("k_seg_roots_out", launch_k(k_seg_roots_out, div_up<uint32_t>(S, BLK), BLK, 0, c.stream,
-                                 nodes, dec, L.d_prim_start, L.d_node_start, S, roots));
+                                 nodes, erec, L.d_prim_start, L.d_node_start, S, roots));
   CK(cudaGetLastError());
   std::vector<SegRoot> hr(S);
   CK(cudaMemcpyAsync(hr.data(), roots, (size_t)S * sizeof(SegRoot), cudaMemcpyDeviceToHost, c.stream));
@@ -1031,12 +1345,12 @@ int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in
       n_cw[s] = n_pr[s] = 0;
     } else if (m == 1) {
       n_cw[s] = 1;
-      n_pr[s] = hr[s].d.nprim;
+      n_pr[s] = hr[s].d.z;
     } else {
-      if (hr[s].d.agg[0].x == AGG_INVALID)
+      if (hr[s].d.y == AGG_INVALID)
         return c.fail(OBVHS_ERR_BAD_INPUT, "BVH2 cannot be converted (no finite distribution of the root)");
-      n_cw[s] = 1 + hr[s].d.agg[0].x;
-      n_pr[s] = hr[s].d.nprim;
+      n_cw[s] = 1 + hr[s].d.y;
+      n_pr[s] = hr[s].d.z;
     }
     off[3 * s] = total;
     total += al((size_t)n_cw[s] * sizeof(CwNode));
@@ -1097,20 +1411,20 @@ int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in
   int emit_blocks = emit_blocks_s.load();
   if (!emit_blocks) {
     int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_all, EMIT_THREADS, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_all, EMIT_TB, 0));
     emit_blocks = std::max(1, per_sm) * c.num_sms;
     emit_blocks_s.store(emit_blocks);
   }
   CK(cudaMemsetAsync(ready, 0, (size_t)q_total * 4, c.stream));
   KLAUNCH("k_seg_emit_init", launch_k(k_seg_emit_init, div_up<uint32_t>(S, BLK), BLK, 0, c.stream,
                                  L.d_prim_start, L.d_node_start, d_slots, S, n_roots, items, ready, counters + 12));
-  EmitArgs ea{{},      nodes,     pidx_in,         dec,      items,      ready, counters + 12, counters + 13,
+  EmitArgs ea{{},      nodes,     pidx_in,         erec,     small,      items,      ready, counters + 12, counters + 13,
               order_children, q_total, EmitOut{nullptr, nullptr, 0, 0, nullptr}, d_eo, L.d_node_start, S, c.d_status,
               counters + 14};
   std::memcpy(ea.log2_thr, ceil_log2_thresholds(), sizeof(ea.log2_thr));
   const uint32_t grid = (uint32_t)std::min<uint64_t>(
-      emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)q_total * 32, EMIT_THREADS)));
-  KLAUNCH("k_emit_all", launch_k(k_emit_all, grid, EMIT_THREADS, 0, c.stream, ea));
+      emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)q_total, EMIT_TB)));
+  KLAUNCH("k_emit_all", launch_k(k_emit_all, grid, EMIT_TB, 0, c.stream, ea));
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(emitted_deferred, counters + 14, 4, cudaMemcpyDeviceToHost, c.stream));
   *emitted_expected = q_total;

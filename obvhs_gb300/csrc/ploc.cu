@@ -190,20 +190,32 @@ __device__ __forceinline__ U128 morton128_of(const Bvh2Node& nd, const Scale& s)
   return c;
 }
 
+// The scale and offset (three double-precision divisions) are computed once
+// per block by its first thread: the double-precision pipe is narrow, and
+// per thread the divisions cost more than the codes themselves.
+__device__ __forceinline__ Scale block_scale(const int* total_keys) {
+  __shared__ Scale s_scale;
+  if (threadIdx.x == 0) s_scale = make_scale(total_keys);
+  __syncthreads();
+  return s_scale;
+}
+
 __global__ void __launch_bounds__(BLK) k_morton64(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
                                                   unsigned long long* __restrict__ codes) {
   grid_dep_wait();
+  const Scale sc = block_scale(total_keys);
   uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i >= n) return;
-  codes[i] = morton64_of(ld_node(&leaves[i]), make_scale(total_keys));
+  codes[i] = morton64_of(ld_node(&leaves[i]), sc);
 }
 
 __global__ void __launch_bounds__(BLK) k_morton128(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
                                                    U128* __restrict__ codes) {
   grid_dep_wait();
+  const Scale sc = block_scale(total_keys);
   uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i >= n) return;
-  codes[i] = morton128_of(ld_node(&leaves[i]), make_scale(total_keys));
+  codes[i] = morton128_of(ld_node(&leaves[i]), sc);
 }
 
 // --- the Morton sort on the high digits -----------------------------------------
@@ -346,10 +358,19 @@ __global__ void __launch_bounds__(BLK) k_seg_morton(const Bvh2Node* __restrict__
                                                     const uint32_t* __restrict__ prim_start, uint32_t n_seg, uint32_t n,
                                                     const int* total_keys, void* __restrict__ codes) {
   grid_dep_wait();
+  // the scale of the block's first scene once per block (most blocks lie in
+  // one scene); leaves of other scenes compute their own
+  __shared__ Scale s_scale;
+  __shared__ uint32_t s_first;
   const uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  if (threadIdx.x == 0) {
+    s_first = seg_find(prim_start, n_seg, min(blockIdx.x * BLK, n - 1));
+    s_scale = make_scale(total_keys + 8 * (size_t)s_first);
+  }
+  __syncthreads();
   if (i >= n) return;
   const uint32_t s = seg_find(prim_start, n_seg, i);
-  const Scale sc = make_scale(total_keys + 8 * (size_t)s);
+  const Scale sc = s == s_first ? s_scale : make_scale(total_keys + 8 * (size_t)s);
   const Bvh2Node nd = ld_node(&leaves[i]);
   if (WIDE)
     static_cast<U128*>(codes)[i] = morton128_of(nd, sc);
