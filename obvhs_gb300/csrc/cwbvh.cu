@@ -22,11 +22,11 @@
 // internal children c_1..c_k of X (slot order), child_base(c_1) =
 // child_base(X) + k, child_base(c_j+1) = child_base(c_j) + ncw(c_j) - 1;
 // prim_base(c_1) = prim_base(X) + (primitives of X's leaf children),
-// prim_base(c_j+1) = prim_base(c_j) + nprim(c_j).  One thread per CWBVH node
-// takes nodes from a device work queue in which every node's item is
-// published by the thread that emits its parent, so nodes are written at
-// exactly the reference's positions: the output is byte for byte the
-// reference's.
+// prim_base(c_j+1) = prim_base(c_j) + nprim(c_j).  Eight lanes per CWBVH
+// node (lane s: child s) take nodes from a device work queue in which every
+// node's item is published by the lanes that emit its parent, so nodes are
+// written at exactly the reference's positions: the output is byte for byte
+// the reference's.
 #include <cmath>
 #include <cstddef>
 #include <cstring>
@@ -39,7 +39,7 @@ namespace {
 
 constexpr int BLK = 256;
 constexpr int EMIT_THREADS = 128;  // k_order_children: a warp per node
-constexpr int EMIT_TB = 64;        // k_emit_all: a thread per node
+constexpr int EMIT_TB = 128;       // k_emit_all: eight lanes per node
 constexpr float PRIM_COST = 0.3f;
 constexpr float DENOM = 1.0f / 255.0f;
 constexpr uint32_t AGG_INVALID = 0xffffffffu;
@@ -412,196 +412,56 @@ struct EmitArgs {
   uint32_t* processed;
 };
 
-// Per-thread staging of k_emit_all in shared memory: for child c of thread t,
-// four 16-byte chunks at [4c + j][t] (consecutive threads, consecutive
-// chunks: conflict-free): the BVH2 node (two chunks), its emission record,
-// its primitive list.  They are copied with cp.async, all eight children's
-// at once, so the copies are in flight together.
+// k_emit_all: eight lanes (an octet) per CWBVH node, four nodes per warp.
+// Lane s of an octet handles the node's child s: the distribution walk keeps
+// one entry per lane, each child's records are loaded by its own lane, the
+// greedy slot assignment reduces over the octet with shuffles, and each lane
+// publishes, quantises and writes its own child.
+constexpr uint32_t FULL_MASK = 0xffffffffu;
+
+// Octet-wide operations (width-8 shuffles: all 32 lanes take part, each
+// octet reduces its own lanes).
+__device__ __forceinline__ uint32_t oct_excl_scan(uint32_t v, int sub, uint32_t* total) {
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(FULL_MASK, x, o, 8);
+    if (sub >= o) x += y;
+  }
+  *total = __shfl_sync(FULL_MASK, x, 7, 8);
+  return x - v;
+}
+__device__ __forceinline__ uint32_t oct_bits(uint32_t ballot, int lane) { return (ballot >> (lane & 24)) & 0xffu; }
+
+struct OctetShared {
+  uint2 list[8];           // distribution walk entries
+  uint8_t slot_child[8];   // child placed in each slot (0xff: empty)
+  __align__(16) uint8_t stage[80];  // the node being assembled
+};
 struct EmitShared {
   uint32_t thr[256];
-  uint4 stg[8 * 4][EMIT_TB];
+  OctetShared oct[EMIT_TB / 8];
 };
 
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
-  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem_src) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
-// The children of CWBVH node x (get_children, src/cwbvh/bvh2_to_cwbvh.rs:
-// 346-397): x's slot-0 distribution, whose leaves taken left to right are the
-// children in the reference's depth-first order.  The walk goes level by
-// level so that the loads of one level's expansions are in flight together:
-// an entry (first child, dl | dr << 4) expands a node's two children with
-// those slot budgets, (node, 0xff) is a child.  Returns the count, or -1 for
-// an invalid distribution (or more than 8 children).
-__device__ int gather_children(const EmitArgs& a, uint32_t x, const Bvh2Node& xn, uint32_t xmeta, uint32_t ch[8]) {
-  if (node_prims(xn) != 0) {  // a leaf root: the node is its own only child
-    ch[0] = x;
-    return 1;
-  }
-  const Decision d0 = decode(xmeta, 0);
-  if (d0.dl == DL_INVALID) return -1;
-  uint32_t ex[8], ey[8];
-  int m = 1;
-  ex[0] = node_first(xn);
-  ey[0] = d0.dl | d0.dr << 4;
-  const uint32_t* nw = reinterpret_cast<const uint32_t*>(a.nodes);
-  for (int round = 0; round < 8; round++) {
-    uint32_t pl[8], pr[8], fl[8], fr[8], ml[8], mr[8];
-    bool any = false;
-#pragma unroll
-    for (int e = 0; e < 8; e++) {
-      if (e < m && ey[e] != 0xffu) {
-        any = true;
-        const size_t f = ex[e];
-        pl[e] = __ldg(nw + 8 * f + 3);
-        fl[e] = __ldg(nw + 8 * f + 7);
-        pr[e] = __ldg(nw + 8 * (f + 1) + 3);
-        fr[e] = __ldg(nw + 8 * (f + 1) + 7);
-        ml[e] = __ldg(&a.erec[f].x);
-        mr[e] = __ldg(&a.erec[f + 1].x);
-      }
-    }
-    if (!any) break;
-    uint32_t nx[8], ny[8];
-    int nm = 0;
-#pragma unroll
-    for (int e = 0; e < 8; e++) {
-      if (e < m) {
-        if (ey[e] == 0xffu) {
-          if (nm >= 8) return -1;
-          nx[nm] = ex[e];
-          ny[nm++] = 0xffu;
-        } else {
-          if (nm + 2 > 8) return -1;
-          const uint32_t f = ex[e], dl = ey[e] & 15u, dr = ey[e] >> 4;
-          // a child that distributes at its budget is expanded next round
-          if (pl[e] == 0) {
-            const Decision dd = decode(ml[e], dl);
-            nx[nm] = dd.kind == K_DISTRIBUTE ? fl[e] : f;
-            ny[nm++] = dd.kind == K_DISTRIBUTE ? (dd.dl | dd.dr << 4) : 0xffu;
-          } else {
-            nx[nm] = f;
-            ny[nm++] = 0xffu;
-          }
-          if (pr[e] == 0) {
-            const Decision dd = decode(mr[e], dr);
-            nx[nm] = dd.kind == K_DISTRIBUTE ? fr[e] : f + 1;
-            ny[nm++] = dd.kind == K_DISTRIBUTE ? (dd.dl | dd.dr << 4) : 0xffu;
-          } else {
-            nx[nm] = f + 1;
-            ny[nm++] = 0xffu;
-          }
-        }
-      }
-    }
-    m = nm;
-    for (int e = 0; e < m; e++) {
-      ex[e] = nx[e];
-      ey[e] = ny[e];
-    }
-  }
-  for (int e = 0; e < m; e++) {
-    if (ey[e] != 0xffu) return -1;
-    ch[e] = ex[e];
-  }
-  return m;
-}
-
-__device__ __forceinline__ uint32_t q_byte(float v) { return (uint32_t)(uint8_t)smin(smax(v, 0.0f), 255.0f); }
-
-// State of one node between the two halves of its emission.
-struct EmitNode {
+// Per-lane state of one node between the two halves of its emission.
+struct OctNode {
   Item it;
   EmitOut o;
-  float3 p, e, r;  // grid origin, cell size, 1 / cell size
+  float3 p, e, r;
   Box box;
-  int cnt;
-  uint32_t n_int;
-  uint32_t leafprims;  // primitives of the leaf children
-  uint32_t ch[8];      // the children's BVH2 nodes, in get_children order
-};
-
-// What child c contributes, from its staged records: internal (CWBVH nodes
-// below it, its primitives) or leaf (its primitive count); false for a
-// malformed record.
-struct ChildInfo {
+  int cnt;             // children (-1: malformed)
+  // this lane's child (sub < cnt)
+  uint32_t ch;         // its BVH2 node
+  Box cbox;
   bool internal;
-  uint32_t count;  // internal: CWBVH nodes below its own node; leaf: primitives
-  uint32_t nprim;  // internal: its primitives
+  uint32_t count;      // internal: CWBVH nodes below its node; leaf: primitives
+  uint32_t nprim;      // internal: its primitives
+  uint4 prims;         // leaf: its primitives (x, y, z)
+  uint32_t slot;       // its slot
+  uint32_t n_int, leafprims;
 };
-__device__ __forceinline__ bool child_info(const uint4 (*stg)[EMIT_TB], int c, int t, ChildInfo& ci) {
-  const uint4 er = stg[4 * c + 2][t], sl = stg[4 * c + 3][t];
-  const uint32_t prims = stg[4 * c][t].w;
-  ci.internal = false;
-  ci.nprim = 0;
-  if (prims != 0) {  // a BVH2 leaf: one primitive, listed by the cost climb
-    ci.count = prims;
-    return sl.w == 1 && prims == 1;
-  }
-  if (decode(er.x, 0).kind == K_LEAF) {
-    ci.count = er.z;
-    return sl.w == er.z && er.z <= 3;
-  }
-  if (er.y == AGG_INVALID) return false;
-  ci.internal = true;
-  ci.count = er.y;
-  ci.nprim = er.z;
-  return true;
-}
 
-// First half of convert_to_cwbvh_impl (src/cwbvh/bvh2_to_cwbvh.rs:75-193)
-// for one node: its grid, its children (records staged in shared memory)
-// and how many of them are internal.  Returns false on a malformed decision
-// (status set).
-__device__ bool emit_gather(const EmitArgs& a, const uint32_t* thr, uint4 (*stg)[EMIT_TB], int t, EmitNode& s) {
-  s.o = a.seg_out ? a.seg_out[seg_find(a.node_start, a.n_seg, s.it.bvh2)] : a.one;
-  const Bvh2Node xn = ld_node(&a.nodes[s.it.bvh2]);
-  const uint32_t xmeta = __ldg(&a.erec[s.it.bvh2].x);
-  s.box = node_box(xn);
-  s.p = s.box.mn;
-  s.e = make_float3(exp_grid(smax(s.box.mx.x - s.box.mn.x, 1e-20f) * DENOM, thr),
-                    exp_grid(smax(s.box.mx.y - s.box.mn.y, 1e-20f) * DENOM, thr),
-                    exp_grid(smax(s.box.mx.z - s.box.mn.z, 1e-20f) * DENOM, thr));
-  s.r = make_float3(1.0f / s.e.x, 1.0f / s.e.y, 1.0f / s.e.z);
-  s.cnt = gather_children(a, s.it.bvh2, xn, node_prims(xn) != 0 ? 0u : xmeta, s.ch);
-  s.n_int = 0;
-  s.leafprims = 0;
-  if (s.cnt < 0) {
-    set_status(a.status, ST_BAD_INPUT);
-    return false;
-  }
-  for (int c = 0; c < s.cnt; c++) {
-    const uint32_t k = s.ch[c];
-    const uint4* nq = reinterpret_cast<const uint4*>(&a.nodes[k]);
-    cp_async16(&stg[4 * c][t], nq);
-    cp_async16(&stg[4 * c + 1][t], nq + 1);
-    cp_async16(&stg[4 * c + 2][t], &a.erec[k]);
-    cp_async16(&stg[4 * c + 3][t], &a.small[k]);
-  }
-  cp_async_wait_all();
-  bool ok = true;
-  for (int c = 0; c < s.cnt; c++) {
-    ChildInfo ci;
-    ok &= child_info(stg, c, t, ci);
-    if (ci.internal)
-      s.n_int++;
-    else
-      s.leafprims += ci.count;
-  }
-  if (!ok) {
-    set_status(a.status, ST_BAD_INPUT);
-    return false;
-  }
-  return true;
-}
-
-__device__ __forceinline__ Box staged_box(const uint4 (*stg)[EMIT_TB], int c, int t) {
-  const uint4 a = stg[4 * c][t], b = stg[4 * c + 1][t];
-  return Box{make_float3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z)),
-             make_float3(__uint_as_float(b.x), __uint_as_float(b.y), __uint_as_float(b.z))};
-}
+__device__ __forceinline__ uint32_t q_byte(float v) { return (uint32_t)(uint8_t)smin(smax(v, 0.0f), 255.0f); }
 
 // order_children's cost of putting a child whose centre is v away from the
 // node's centre into slot sl: dot(direction of sl, v), unfused.
@@ -610,210 +470,318 @@ __device__ __forceinline__ float slot_cost(float3 v, int sl) {
   return (dx * v.x + dy * v.y) + dz * v.z;
 }
 
-// Smallest cost of child v over the free slots (first slot on ties), and its
-// slot (8: none below f32::MAX).
-__device__ __forceinline__ void row_min(float3 v, uint32_t filled, float& m, uint32_t& arg) {
-  m = 3.40282347e+38f;
-  arg = 8;
-#pragma unroll
-  for (int sl = 0; sl < 8; sl++) {
-    const float cst = slot_cost(v, sl);
-    if (!((filled >> sl) & 1u) && cst < m) {
-      m = cst;
-      arg = (uint32_t)sl;
+// First half of convert_to_cwbvh_impl (src/cwbvh/bvh2_to_cwbvh.rs:75-193):
+// the node's grid, its children (get_children, :346-397, walked level by
+// level with one entry per lane; the entries' left-to-right order is the
+// reference's depth-first order), each child's records, and the slot of each
+// child (order_children, :402-467).  `act`: this octet has a node.  Every
+// lane of the warp calls this (octet shuffles); s.cnt < 0 marks a malformed
+// node (status set).
+__device__ void oct_gather(const EmitArgs& a, const uint32_t* thr, OctetShared& os, int lane, bool act, OctNode& s) {
+  const int sub = lane & 7;
+  s.cnt = 0;
+  s.n_int = s.leafprims = 0;
+  s.internal = false;
+  s.count = s.nprim = 0;
+  s.slot = 8;
+  uint32_t ex = 0, ey = 0xffu;
+  int m = 0;
+  bool bad = false;
+  if (act) {
+    s.o = a.seg_out ? a.seg_out[seg_find(a.node_start, a.n_seg, s.it.bvh2)] : a.one;
+    const Bvh2Node xn = ld_node(&a.nodes[s.it.bvh2]);
+    const uint32_t xmeta = __ldg(&a.erec[s.it.bvh2].x);
+    s.box = node_box(xn);
+    s.p = s.box.mn;
+    s.e = make_float3(exp_grid(smax(s.box.mx.x - s.box.mn.x, 1e-20f) * DENOM, thr),
+                      exp_grid(smax(s.box.mx.y - s.box.mn.y, 1e-20f) * DENOM, thr),
+                      exp_grid(smax(s.box.mx.z - s.box.mn.z, 1e-20f) * DENOM, thr));
+    s.r = make_float3(1.0f / s.e.x, 1.0f / s.e.y, 1.0f / s.e.z);
+    m = 1;
+    if (node_prims(xn) != 0) {  // a leaf root: the node is its own only child
+      if (sub == 0) ex = s.it.bvh2;
+    } else {
+      const Decision d0 = decode(xmeta, 0);
+      if (d0.dl == DL_INVALID) bad = true;
+      if (sub == 0) {
+        ex = node_first(xn);
+        ey = d0.dl | d0.dr << 4;
+      }
     }
+  }
+  // the walk: each round expands every expandable entry into its two
+  // children (a child that distributes at its budget is expanded next round)
+  const uint32_t* nw = reinterpret_cast<const uint32_t*>(a.nodes);
+  for (int round = 0; round < 8; round++) {
+    const bool mine = act && !bad && sub < m && ey != 0xffu;
+    if (__ballot_sync(FULL_MASK, mine) == 0) break;
+    uint32_t n_new = act && !bad && sub < m ? 1u : 0u;
+    uint2 e0 = make_uint2(ex, ey), e1 = make_uint2(0u, 0u);
+    if (mine) {
+      const size_t f = ex;
+      const uint32_t dl = ey & 15u, dr = ey >> 4;
+      const uint32_t pl = __ldg(nw + 8 * f + 3), fl = __ldg(nw + 8 * f + 7);
+      const uint32_t pr = __ldg(nw + 8 * (f + 1) + 3), fr = __ldg(nw + 8 * (f + 1) + 7);
+      const uint32_t ml = __ldg(&a.erec[f].x), mr = __ldg(&a.erec[f + 1].x);
+      e0 = make_uint2((uint32_t)f, 0xffu);
+      e1 = make_uint2((uint32_t)f + 1, 0xffu);
+      if (pl == 0) {
+        const Decision dd = decode(ml, dl);
+        if (dd.kind == K_DISTRIBUTE) e0 = make_uint2(fl, dd.dl | dd.dr << 4);
+      }
+      if (pr == 0) {
+        const Decision dd = decode(mr, dr);
+        if (dd.kind == K_DISTRIBUTE) e1 = make_uint2(fr, dd.dl | dd.dr << 4);
+      }
+      n_new = 2;
+    }
+    uint32_t total;
+    const uint32_t at = oct_excl_scan(n_new, sub, &total);
+    __syncwarp();
+    if (act && !bad && total <= 8) {
+      if (n_new >= 1) os.list[at] = e0;
+      if (n_new == 2) os.list[at + 1] = e1;
+    }
+    __syncwarp();
+    if (act && !bad) {
+      if (total > 8) {
+        bad = true;
+      } else {
+        m = (int)total;
+        if (sub < m) {
+          ex = os.list[sub].x;
+          ey = os.list[sub].y;
+        }
+      }
+    }
+  }
+  if (act && !bad && sub < m && ey != 0xffu) bad = true;  // the walk did not finish
+  // each lane's child: its node, emission record and primitive list
+  const bool has = act && !bad && sub < m;
+  float3 v = make_float3(0.0f, 0.0f, 0.0f);
+  if (has) {
+    s.ch = ex;
+    const Bvh2Node cn = ld_node(&a.nodes[ex]);
+    const EmitRec er = __ldg(&a.erec[ex]);
+    const uint4 sl = __ldg(&a.small[ex]);
+    s.cbox = node_box(cn);
+    s.prims = sl;
+    if (node_prims(cn) != 0) {  // a BVH2 leaf: one primitive, listed by the cost climb
+      s.count = node_prims(cn);
+      if (sl.w != 1 || s.count != 1) bad = true;
+    } else if (decode(er.x, 0).kind == K_LEAF) {
+      s.count = er.z;
+      if (sl.w != er.z || er.z > 3) bad = true;
+    } else if (er.y == AGG_INVALID) {
+      bad = true;
+    } else {
+      s.internal = true;
+      s.count = er.y;
+      s.nprim = er.z;
+    }
+    const float3 pc = center(s.box), cc = center(s.cbox);
+    v = make_float3(cc.x - pc.x, cc.y - pc.y, cc.z - pc.z);
+  }
+  const bool oct_bad = oct_bits(__ballot_sync(FULL_MASK, bad), lane) != 0;
+  const uint32_t present = oct_bits(__ballot_sync(FULL_MASK, has), lane);
+  s.cnt = act ? (oct_bad ? -1 : __popc(present)) : 0;
+  uint32_t tot;
+  oct_excl_scan(s.internal && has ? 1u : 0u, sub, &s.n_int);
+  oct_excl_scan(has && !s.internal ? s.count : 0u, sub, &tot);
+  s.leafprims = tot;
+  if (act && oct_bad && sub == 0) set_status(a.status, ST_BAD_INPUT);
+  // slots: order_children's greedy loop takes, while one is below f32::MAX,
+  // the smallest cost (first in (child, slot) order on ties) among unassigned
+  // children and free slots; each lane keeps its child's costs
+  const bool live = act && s.cnt > 0;
+  if (a.order_children) {
+    float cost[8];
+#pragma unroll
+    for (int sl = 0; sl < 8; sl++) cost[sl] = slot_cost(v, sl);
+    uint32_t filled = 0;
+    bool assigned = false;
+    for (int iter = 0; iter < 8; iter++) {
+      float bm = 3.40282347e+38f;
+      uint32_t barg = 8;
+      if (live && has && !assigned) {
+#pragma unroll
+        for (int sl = 0; sl < 8; sl++)
+          if (!((filled >> sl) & 1u) && cost[sl] < bm) {
+            bm = cost[sl];
+            barg = (uint32_t)sl;
+          }
+      }
+      // argmin of (cost, child) over the octet
+      uint32_t bc = barg < 8 ? (uint32_t)sub : 8u;
+#pragma unroll
+      for (int o = 4; o > 0; o >>= 1) {
+        const float om = __shfl_xor_sync(FULL_MASK, bm, o, 8);
+        const uint32_t oc = __shfl_xor_sync(FULL_MASK, bc, o, 8);
+        const uint32_t oa = __shfl_xor_sync(FULL_MASK, barg, o, 8);
+        if (oc < 8 && (bc == 8 || om < bm || (om == bm && oc < bc))) {
+          bm = om;
+          bc = oc;
+          barg = oa;
+        }
+      }
+      if (__ballot_sync(FULL_MASK, live && bc < 8) == 0) break;
+      if (live && bc < 8) {
+        if (sub == (int)bc) {
+          s.slot = barg;
+          assigned = true;
+        }
+        filled |= 1u << barg;
+      }
+    }
+    const uint32_t unassigned = oct_bits(__ballot_sync(FULL_MASK, has && !assigned), lane);
+    if (live && unassigned != 0) {
+      if (sub == 0) set_status(a.status, ST_BAD_INPUT);
+      s.cnt = -1;
+    }
+  } else {
+    if (has) s.slot = (uint32_t)sub;
   }
 }
 
-// Second half: the children placed in slots (order_children,
-// src/cwbvh/bvh2_to_cwbvh.rs:402-467, or in order), their metas and offsets,
-// the leaf children's primitives (count_primitives: recorded in depth-first
-// order by the cost climb), the internal children published at queue slots
-// qbase.., and the 80-byte node written.
-__device__ void emit_finish(const EmitArgs& a, const uint4 (*stg)[EMIT_TB], int t, const EmitNode& s,
-                            uint32_t qbase) {
-  const int cnt = s.cnt;
-  uint32_t slot_of = 0;  // 3 bits per child
-  if (a.order_children) {
-    // The reference's greedy loop takes, while one is below f32::MAX, the
-    // smallest cost (first in (child, slot) order on ties) among unassigned
-    // children and free slots.  Kept as per-child minima over the free slots:
-    // the pick is the smallest (minimum, child), and only children whose
-    // minimum sat in the slot just taken need a new one.
-    const float3 pc = center(s.box);
-    float3 v[8];
-    float rm[8];
-    uint32_t ra[8];
-#pragma unroll
-    for (int c = 0; c < 8; c++) {
-      v[c] = make_float3(0.0f, 0.0f, 0.0f);
-      rm[c] = 3.40282347e+38f;
-      ra[c] = 8;
-      if (c < cnt) {
-        const float3 cc = center(staged_box(stg, c, t));
-        v[c] = make_float3(cc.x - pc.x, cc.y - pc.y, cc.z - pc.z);
-        row_min(v[c], 0u, rm[c], ra[c]);
-      }
-    }
-    uint32_t assigned = 0, filled = 0;
-    for (int iter = 0; iter < 8; iter++) {
-      float bc = 3.40282347e+38f;
-      int bi = -1;
-#pragma unroll
-      for (int c = 0; c < 8; c++) {
-        if (c < cnt && !((assigned >> c) & 1u) && ra[c] < 8 && rm[c] < bc) {
-          bc = rm[c];
-          bi = c;
-        }
-      }
-      if (bi < 0) break;
-      uint32_t sl = 0;
-#pragma unroll
-      for (int c = 0; c < 8; c++)
-        if (c == bi) sl = ra[c];
-      assigned |= 1u << bi;
-      filled |= 1u << sl;
-      slot_of |= sl << (3 * bi);
-#pragma unroll
-      for (int c = 0; c < 8; c++)
-        if (c < cnt && !((assigned >> c) & 1u) && ra[c] == sl) row_min(v[c], filled, rm[c], ra[c]);
-    }
-    if (__popc(assigned) != cnt) {
-      set_status(a.status, ST_BAD_INPUT);
-      return;
-    }
-  } else {
-    for (int c = 0; c < cnt; c++) slot_of |= (uint32_t)c << (3 * c);
-  }
-  uint32_t child_in_slot = 0xffffffffu;  // 4 bits per slot, 0xf = empty
-  for (int c = 0; c < cnt; c++) {
-    const uint32_t sl = (slot_of >> (3 * c)) & 7u;
-    child_in_slot = (child_in_slot & ~(0xfu << (4 * sl))) | ((uint32_t)c << (4 * sl));
-  }
-
-  uint32_t w[20];
-  w[0] = __float_as_uint(s.p.x);
-  w[1] = __float_as_uint(s.p.y);
-  w[2] = __float_as_uint(s.p.z);
-  w[4] = s.it.child_base;
-  w[5] = s.it.prim_base;
-#pragma unroll
-  for (int k = 6; k < 20; k++) w[k] = 0;
-  uint32_t imask = 0, int_rank = 0, leaf_off = 0, sub_node_off = 0, sub_prim_off = 0;
-#pragma unroll
-  for (int sl = 0; sl < 8; sl++) {
-    const uint32_t c = (child_in_slot >> (4 * sl)) & 0xfu;
-    if (c == 0xfu) continue;
-    ChildInfo ci;
-    child_info(stg, (int)c, t, ci);
-    const Box cb = staged_box(stg, (int)c, t);
-    const uint32_t lo = q_byte(floorf(((cb.mn.x - s.p.x) - 0.0f) * s.r.x)) |
-                        q_byte(floorf(((cb.mn.y - s.p.y) - 0.0f) * s.r.y)) << 8 |
-                        q_byte(floorf(((cb.mn.z - s.p.z) - 0.0f) * s.r.z)) << 16;
-    const uint32_t hi = q_byte(ceilf(((cb.mx.x - s.p.x) + 0.0f) * s.r.x)) |
-                        q_byte(ceilf(((cb.mx.y - s.p.y) + 0.0f) * s.r.y)) << 8 |
-                        q_byte(ceilf(((cb.mx.z - s.p.z) + 0.0f) * s.r.z)) << 16;
-    uint32_t meta;
-    if (ci.internal) {
-      meta = (24u + sl) | 0x20u;
-      imask |= 1u << sl;
+// Second half: in slot order, the children's metas and offsets, the leaf
+// children's primitives (count_primitives: recorded in depth-first order by
+// the cost climb), the internal children published at queue slots qbase..,
+// and the 80-byte node written.
+__device__ void oct_finish(const EmitArgs& a, OctetShared& os, int lane, bool act, const OctNode& s,
+                           uint32_t qbase) {
+  const int sub = lane & 7;
+  const int g0 = lane & 24;
+  const bool live = act && s.cnt > 0;
+  if (live) os.slot_child[sub] = 0xffu;
+  __syncwarp();
+  if (live && sub < s.cnt) os.slot_child[s.slot] = (uint8_t)sub;
+  __syncwarp();
+  const uint32_t src = live ? os.slot_child[sub] : 0xffu;
+  const bool filled = src != 0xffu;
+  const int sl_lane = g0 + (filled ? (int)src : sub);
+  // this slot's child, fetched from its lane
+  const uint32_t ch = __shfl_sync(FULL_MASK, s.ch, sl_lane);
+  const bool internal = __shfl_sync(FULL_MASK, (uint32_t)s.internal, sl_lane) != 0 && filled;
+  const uint32_t count = __shfl_sync(FULL_MASK, s.count, sl_lane);
+  const uint32_t nprim = __shfl_sync(FULL_MASK, s.nprim, sl_lane);
+  const uint32_t p0 = __shfl_sync(FULL_MASK, s.prims.x, sl_lane), p1 = __shfl_sync(FULL_MASK, s.prims.y, sl_lane),
+                 p2 = __shfl_sync(FULL_MASK, s.prims.z, sl_lane);
+  Box cb;
+  cb.mn.x = __shfl_sync(FULL_MASK, s.cbox.mn.x, sl_lane);
+  cb.mn.y = __shfl_sync(FULL_MASK, s.cbox.mn.y, sl_lane);
+  cb.mn.z = __shfl_sync(FULL_MASK, s.cbox.mn.z, sl_lane);
+  cb.mx.x = __shfl_sync(FULL_MASK, s.cbox.mx.x, sl_lane);
+  cb.mx.y = __shfl_sync(FULL_MASK, s.cbox.mx.y, sl_lane);
+  cb.mx.z = __shfl_sync(FULL_MASK, s.cbox.mx.z, sl_lane);
+  uint32_t t0, t1, t2;
+  const uint32_t int_rank = oct_excl_scan(internal ? 1u : 0u, sub, &t0);
+  const uint32_t leaf_off = oct_excl_scan(filled && !internal ? count : 0u, sub, &t1);
+  const uint32_t sub_node_off = oct_excl_scan(internal ? count : 0u, sub, &t2);
+  const uint32_t sub_prim_off = oct_excl_scan(internal ? nprim : 0u, sub, &t2);
+  const uint32_t imask = oct_bits(__ballot_sync(FULL_MASK, internal), lane);
+  uint8_t meta = 0;
+  uint32_t lo = 0, hi = 0;
+  if (live && filled) {
+    lo = q_byte(floorf(((cb.mn.x - s.p.x) - 0.0f) * s.r.x)) | q_byte(floorf(((cb.mn.y - s.p.y) - 0.0f) * s.r.y)) << 8 |
+         q_byte(floorf(((cb.mn.z - s.p.z) - 0.0f) * s.r.z)) << 16;
+    hi = q_byte(ceilf(((cb.mx.x - s.p.x) + 0.0f) * s.r.x)) | q_byte(ceilf(((cb.mx.y - s.p.y) + 0.0f) * s.r.y)) << 8 |
+         q_byte(ceilf(((cb.mx.z - s.p.z) + 0.0f) * s.r.z)) << 16;
+    if (internal) {
+      meta = (uint8_t)((24 + sub) | 0x20);
       // the internal children's own nodes come first, then their subtrees
       const uint32_t q = qbase + int_rank;
       if (q < a.queue_cap) {
-        a.items[q] = Item{s.ch[c], s.it.child_base + int_rank, s.it.child_base + s.n_int + sub_node_off,
+        a.items[q] = Item{ch, s.it.child_base + int_rank, s.it.child_base + s.n_int + sub_node_off,
                           s.it.prim_base + s.leafprims + sub_prim_off};
-        __threadfence();
-        atomicExch(&a.ready[q], 1u);
       } else {
         set_status(a.status, ST_CAPACITY);
       }
-      int_rank++;
-      sub_node_off += ci.count;
-      sub_prim_off += ci.nprim;
     } else {
-      const uint32_t u = ci.count == 1 ? 0x20u : ci.count == 2 ? 0x60u : ci.count == 3 ? 0xe0u : 0u;
+      const uint32_t u = count == 1 ? 0x20u : count == 2 ? 0x60u : count == 3 ? 0xe0u : 0u;
       if (!u) set_status(a.status, ST_BAD_INPUT);
-      meta = leaf_off | u;
-      // count_primitives: the leaf's primitives in depth-first order
-      const uint4 pl = stg[4 * c + 3][t];
+      meta = (uint8_t)(leaf_off | u);
       const uint32_t slot = s.it.prim_base + leaf_off;
-      if (slot + ci.count <= s.o.max_prims) {
-        s.o.pidx[slot] = pl.x;
-        if (ci.count > 1) s.o.pidx[slot + 1] = pl.y;
-        if (ci.count > 2) s.o.pidx[slot + 2] = pl.z;
+      if (slot + count <= s.o.max_prims) {
+        s.o.pidx[slot] = p0;
+        if (count > 1) s.o.pidx[slot + 1] = p1;
+        if (count > 2) s.o.pidx[slot + 2] = p2;
       } else {
         set_status(a.status, ST_CAPACITY);
       }
-      leaf_off += ci.count;
     }
-    // bytes 24 + sl (meta), 32 + sl (lo x), 40 (hi x), 48 (lo y), 56 (hi y),
-    // 64 (lo z), 72 (hi z)
-    const int sh = 8 * (sl & 3), hw = sl >> 2;
-    w[6 + hw] |= meta << sh;
-    w[8 + hw] |= (lo & 0xffu) << sh;
-    w[10 + hw] |= (hi & 0xffu) << sh;
-    w[12 + hw] |= ((lo >> 8) & 0xffu) << sh;
-    w[14 + hw] |= ((hi >> 8) & 0xffu) << sh;
-    w[16 + hw] |= ((lo >> 16) & 0xffu) << sh;
-    w[18 + hw] |= ((hi >> 16) & 0xffu) << sh;
   }
-  w[3] = (__float_as_uint(s.e.x) >> 23) | (__float_as_uint(s.e.y) >> 23) << 8 | (__float_as_uint(s.e.z) >> 23) << 16 |
-         imask << 24;
-  if (s.it.cw >= s.o.max_nodes) {
-    set_status(a.status, ST_CAPACITY);
-    return;
+  // publish the internal children (items visible before their flags)
+  if (live && internal && qbase + int_rank < a.queue_cap) {
+    __threadfence();
+    atomicExch(&a.ready[qbase + int_rank], 1u);
   }
-  uint4* dst = s.o.cw[s.it.cw].q;
-#pragma unroll
-  for (int k = 0; k < 5; k++) dst[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
-  if (s.o.exact) {  // src/cwbvh/bvh2_to_cwbvh.rs:76-80
-    s.o.exact[2 * (size_t)s.it.cw] = make_float4(s.box.mn.x, s.box.mn.y, s.box.mn.z, 0.0f);
-    s.o.exact[2 * (size_t)s.it.cw + 1] = make_float4(s.box.mx.x, s.box.mx.y, s.box.mx.z, 0.0f);
+  // assemble the 80-byte node in shared memory, then five 16-byte stores
+  if (live) {
+    if (sub == 0) {
+      uint32_t* w = reinterpret_cast<uint32_t*>(os.stage);
+      w[0] = __float_as_uint(s.p.x);
+      w[1] = __float_as_uint(s.p.y);
+      w[2] = __float_as_uint(s.p.z);
+      w[3] = (__float_as_uint(s.e.x) >> 23) | (__float_as_uint(s.e.y) >> 23) << 8 |
+             (__float_as_uint(s.e.z) >> 23) << 16 | imask << 24;
+      w[4] = s.it.child_base;
+      w[5] = s.it.prim_base;
+    }
+    os.stage[24 + sub] = meta;
+    os.stage[32 + sub] = (uint8_t)(lo & 0xffu);
+    os.stage[40 + sub] = (uint8_t)(hi & 0xffu);
+    os.stage[48 + sub] = (uint8_t)((lo >> 8) & 0xffu);
+    os.stage[56 + sub] = (uint8_t)((hi >> 8) & 0xffu);
+    os.stage[64 + sub] = (uint8_t)((lo >> 16) & 0xffu);
+    os.stage[72 + sub] = (uint8_t)((hi >> 16) & 0xffu);
   }
+  __syncwarp();
+  if (live) {
+    if (s.it.cw >= s.o.max_nodes) {
+      if (sub == 0) set_status(a.status, ST_CAPACITY);
+    } else if (sub < 5) {
+      s.o.cw[s.it.cw].q[sub] = reinterpret_cast<const uint4*>(os.stage)[sub];
+    } else if (sub < 7 && s.o.exact) {  // src/cwbvh/bvh2_to_cwbvh.rs:76-80
+      s.o.exact[2 * (size_t)s.it.cw + (sub - 5)] = sub == 5 ? make_float4(s.box.mn.x, s.box.mn.y, s.box.mn.z, 0.0f)
+                                                             : make_float4(s.box.mx.x, s.box.mx.y, s.box.mx.z, 0.0f);
+    }
+  }
+  __syncwarp();
 }
 
-// A thread per CWBVH node.  Each lane holds at most one queue item; idle
-// lanes take the next items (one atomic per warp), and each round the lanes
-// whose items have been published emit them while the others keep waiting.
-// A held item's parent was taken earlier by a running thread, so some held
-// item is always published eventually; waits are bounded (status
+// Each octet holds at most one queue item.  Once every octet of a warp is
+// idle the warp takes the next four items (one atomic); each round the
+// octets whose items have been published emit them while the others keep
+// waiting.  A held item's parent was taken earlier by a running warp, so
+// some held item is always published eventually; waits are bounded (status
 // ST_ITER_LIMIT), and a failed node (status set) ends every wait.
 __global__ void __launch_bounds__(EMIT_TB) k_emit_all(EmitArgs a) {
   grid_dep_wait();
   __shared__ EmitShared sm;
   for (int k = threadIdx.x; k < 256; k += EMIT_TB) sm.thr[k] = a.log2_thr[k];
   __syncthreads();
-  const uint32_t FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31, t = threadIdx.x;
-  const uint32_t lt_mask = (1u << lane) - 1u;
+  const int lane = threadIdx.x & 31, sub = lane & 7, oct = lane >> 3;
+  OctetShared& os = sm.oct[threadIdx.x >> 3];
   uint32_t held = OBVHS_INVALID, mine = 0, waits = 0, ns = 32;
   bool drained = false;  // (warp-uniform) the queue has been handed out
   for (;;) {
-    if (!drained) {
-      // new items only once every lane is idle: the warp then holds 32
-      // consecutive queue items, published together (by one or a few rounds
-      // of their parents' warps), so its rounds keep most lanes busy
-      const uint32_t need = __ballot_sync(FULL, held == OBVHS_INVALID);
-      if (need == FULL) {
-        const int leader = __ffs(need) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(a.head, (uint32_t)__popc(need));
-        base = __shfl_sync(FULL, base, leader);
-        if ((uint64_t)base + __popc(need) >= a.queue_cap) drained = true;
-        if (held == OBVHS_INVALID) {
-          const uint32_t k = base + __popc(need & lt_mask);
-          if (k < a.queue_cap) held = k;
-        }
-      }
+    if (!drained && __ballot_sync(FULL_MASK, held != OBVHS_INVALID) == 0) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(a.head, 4u);
+      base = __shfl_sync(FULL_MASK, base, 0);
+      if ((uint64_t)base + 4 >= a.queue_cap) drained = true;
+      if (base + oct < a.queue_cap) held = base + oct;
     }
-    if (__ballot_sync(FULL, held != OBVHS_INVALID) == 0) break;
-    const bool go = held != OBVHS_INVALID && *(volatile uint32_t*)&a.ready[held] != 0;
-    if (__ballot_sync(FULL, go) == 0) {
-      // nothing published yet: back off (tight polling starves the threads
+    if (__ballot_sync(FULL_MASK, held != OBVHS_INVALID) == 0) break;
+    uint32_t rd = 0;
+    if (sub == 0 && held != OBVHS_INVALID) rd = *(volatile uint32_t*)&a.ready[held];
+    const bool go = __shfl_sync(FULL_MASK, rd, lane & 24) != 0;
+    if (__ballot_sync(FULL_MASK, go) == 0) {
+      // nothing published yet: back off (tight polling starves the warps
       // doing the work); give up on a failed node or after the bound
       bool stop = ++waits > (1u << 22);
       if ((waits & 63u) == 0 && *(volatile uint32_t*)a.status) stop = true;
-      if (__any_sync(FULL, stop)) {
+      if (__any_sync(FULL_MASK, stop)) {
         if (lane == 0 && waits > (1u << 22)) set_status(a.status, ST_ITER_LIMIT);
         break;
       }
@@ -823,37 +791,35 @@ __global__ void __launch_bounds__(EMIT_TB) k_emit_all(EmitArgs a) {
     }
     waits = 0;
     ns = 32;
-    EmitNode s;
-    s.n_int = 0;
-    bool ok = false;
+    OctNode s;
     if (go) {
       __threadfence();
       // through L2: this SM may hold a stale L1 line of the items array
       const uint4 raw = __ldcg(reinterpret_cast<const uint4*>(&a.items[held]));
       s.it = Item{raw.x, raw.y, raw.z, raw.w};
-      ok = emit_gather(a, sm.thr, sm.stg, t, s);
-      if (!ok) s.n_int = 0;
     }
+    oct_gather(a, sm.thr, os, lane, go, s);
     // queue slots for the internal children: one atomic per warp
-    uint32_t incl = s.n_int;
+    const uint32_t n_int = go && s.cnt > 0 && sub == 0 ? s.n_int : 0u;
+    uint32_t incl = n_int;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(FULL, incl, o);
+      const uint32_t y = __shfl_up_sync(FULL_MASK, incl, o);
       if (lane >= o) incl += y;
     }
-    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
     uint32_t base = 0;
     if (lane == 31 && total) base = atomicAdd(a.tail, total);
-    base = __shfl_sync(FULL, base, 31);
-    if (ok) {
-      emit_finish(a, sm.stg, t, s, base + incl - s.n_int);
-      mine++;
+    base = __shfl_sync(FULL_MASK, base, 31);
+    const uint32_t qbase = base + __shfl_sync(FULL_MASK, incl - n_int, lane & 24);
+    oct_finish(a, os, lane, go, s, qbase);
+    if (go) {
+      if (sub == 0 && s.cnt > 0) mine++;
+      held = OBVHS_INVALID;
     }
-    if (go) held = OBVHS_INVALID;
-    __syncwarp();
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(FULL, mine, o);
+  for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(FULL_MASK, mine, o);
   if (lane == 0 && mine) atomicAdd(a.processed, mine);
 }
 
@@ -1259,7 +1225,7 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
               n_cw,   EmitOut{cwn, cwp, n_cw, n_pr, exn}, nullptr, nullptr, 0, c.d_status, counters + 14};
   std::memcpy(ea.log2_thr, ceil_log2_thresholds(), sizeof(ea.log2_thr));
   const uint32_t grid = (uint32_t)std::min<uint64_t>(
-      emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)n_cw, EMIT_TB)));
+      emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)n_cw * 8, EMIT_TB)));
   KLAUNCH("k_emit_all", launch_k(k_emit_all, grid, EMIT_TB, 0, c.stream, ea));
   CK(cudaGetLastError());
   out->nodes = cwn;
@@ -1423,7 +1389,7 @@ int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in
               counters + 14};
   std::memcpy(ea.log2_thr, ceil_log2_thresholds(), sizeof(ea.log2_thr));
   const uint32_t grid = (uint32_t)std::min<uint64_t>(
-      emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)q_total, EMIT_TB)));
+      emit_blocks, std::max<uint64_t>(1, div_up<uint64_t>((uint64_t)q_total * 8, EMIT_TB)));
   KLAUNCH("k_emit_all", launch_k(k_emit_all, grid, EMIT_TB, 0, c.stream, ea));
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(emitted_deferred, counters + 14, 4, cudaMemcpyDeviceToHost, c.stream));
