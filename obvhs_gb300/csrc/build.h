@@ -326,7 +326,11 @@ int split_thresholds_device(BuildCtx& c, const float* tris, uint32_t n, float* o
 // there asynchronously instead of to *applied_out.
 int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const float* seq, uint32_t nseq,
                        uint64_t* applied_out, int64_t root_prims = -1, uint32_t* applied_deferred = nullptr);
-int compute_parents_device(BuildCtx& c, const Bvh2Node* nodes, uint32_t n_nodes, uint32_t* parents);
+// Parent links of every node (roots: their own).  With `unordered`, also
+// sets *unordered (zeroed by the caller) when some inner node's children are
+// not both at higher indices than the node.
+int compute_parents_device(BuildCtx& c, const Bvh2Node* nodes, uint32_t n_nodes, uint32_t* parents,
+                           uint32_t* unordered = nullptr);
 // Copies a host table to the device (stream-ordered, from pinned staging);
 // returns the device address or null.
 typedef std::function<uint32_t*(const void* src, size_t bytes)> SegTableUpload;

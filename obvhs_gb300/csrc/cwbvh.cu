@@ -188,6 +188,12 @@ __device__ CostRec inner_rec(const CostRec& L, const CostRec& R, float ha, uint3
   return out;
 }
 
+// The primitives of a node with at most 3 of them: its left child's, then its
+// right child's (lists (id0, id1, id2, count)).
+__device__ __forceinline__ uint4 concat_lists(const uint4 l, const uint4 r) {
+  return make_uint4(l.x, l.w > 1 ? l.y : r.x, l.w > 2 ? l.z : (l.w == 2 ? r.x : r.y), l.w + r.w);
+}
+
 // The climb from one leaf towards the root; at each inner node the second
 // child to arrive computes the node's record.  The climber carries its own
 // child's record in registers, publishes it (for the sibling's climber, in
@@ -266,12 +272,7 @@ struct CostClimb {
     uint4 list = make_uint4(0u, 0u, 0u, np);
     if (np <= 3) {
       const uint4 ol = sib_leaf ? make_uint4(__ldg(&pidx_in[node_first(sn)]), 0u, 0u, 1u) : __ldcg(&small[s]);
-      const uint4 l = c == f ? own_list : ol, r = c == f ? ol : own_list;
-      // the left child's primitives, then the right child's
-      const uint32_t v[3] = {l.x, l.y, l.z};
-      list.x = v[0];
-      list.y = l.w > 1 ? v[1] : r.x;
-      list.z = l.w > 2 ? v[2] : (l.w == 2 ? r.x : r.y);
+      list = concat_lists(c == f ? own_list : ol, c == f ? ol : own_list);
       __stcg(&small[p], list);
     }
     uint32_t aggn0;
@@ -287,6 +288,87 @@ struct CostClimb {
   }
 };
 
+// Ordered form, for trees whose children always lie above their parent in
+// the node array (every tree straight from PLOC: merged pairs are written top
+// down, a parent after its children).  Nodes are handed out from the top of
+// the array down, 32 per warp, so a node's children were handed out before
+// it: every lane computes one node from its children's records (waiting, in
+// the rare case that one is still being computed, for its ready flag), with
+// no arrival atomics and little divergence.  Same records as the climb.
+__device__ __forceinline__ bool wait_ready(const uint32_t* flag, uint32_t* status) {
+  uint32_t spins = 0, ns = 32;
+  while (*(volatile const uint32_t*)flag == 0) {
+    if (++spins > (1u << 22) || ((spins & 63u) == 0 && *(volatile uint32_t*)status)) {
+      set_status(status, ST_ITER_LIMIT);
+      return false;
+    }
+    __nanosleep(ns);
+    if (ns < 256) ns <<= 1;
+  }
+  __threadfence();
+  return true;
+}
+
+// One child's record and primitive list, for its parent.
+__device__ __forceinline__ bool child_rec(const Bvh2Node& cn, uint32_t k, const uint32_t* pidx_in,
+                                          const CostRec* crec, const uint4* small, const uint32_t* flags,
+                                          uint32_t* status, CostRec& r, uint4& list) {
+  if (node_prims(cn) != 0) {
+    r = leaf_rec(cn);
+    list = make_uint4(__ldg(&pidx_in[node_first(cn)]), 0u, 0u, 1u);
+    return true;
+  }
+  if (!wait_ready(&flags[k], status)) return false;
+  r = ld_rec_cg(&crec[k]);
+  list = r.nprim <= 3 ? __ldcg(&small[k]) : make_uint4(0u, 0u, 0u, r.nprim);
+  return true;
+}
+
+__device__ void costs_ordered(const Bvh2Node* __restrict__ nodes, const uint32_t* __restrict__ parents,
+                              const uint32_t* __restrict__ pidx_in, uint32_t n, uint32_t max_prims, CostRec* crec,
+                              EmitRec* erec, uint4* small, uint32_t* flags, uint32_t* next, uint32_t* status) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(next, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= n) return;
+    const uint32_t t = base + lane;
+    if (t >= n) continue;
+    const uint32_t i = n - 1 - t;
+    const Bvh2Node nd = ld_node(&nodes[i]);
+    if (node_prims(nd) != 0) {
+      if (node_prims(nd) != 1) {  // src/cwbvh/bvh2_to_cwbvh.rs:243-247
+        set_status(status, ST_BAD_INPUT);
+        continue;
+      }
+      __stcg(&small[i], make_uint4(__ldg(&pidx_in[node_first(nd)]), 0u, 0u, 1u));
+      if (parents[i] == i) __stcg(&erec[i], make_uint4(0u, 0u, 1u, 0u));  // a leaf root: one CWBVH node
+      continue;
+    }
+    const uint32_t f = node_first(nd);
+    if (f + 1 >= n || f < i) {  // an inert pad (children out of range): nothing to compute
+      atomicExch(&flags[i], 1u);
+      continue;
+    }
+    const Bvh2Node cl = ld_node(&nodes[f]), cr = ld_node(&nodes[f + 1]);
+    CostRec L, R;
+    uint4 ll, rl;
+    const bool ok = child_rec(cl, f, pidx_in, crec, small, flags, status, L, ll) &&
+                    child_rec(cr, f + 1, pidx_in, crec, small, flags, status, R, rl);
+    if (ok) {
+      uint32_t aggn0;
+      const CostRec out = inner_rec(L, R, half_area(node_box(nd)), max_prims, &aggn0);
+      if (out.nprim <= 3) __stcg(&small[i], concat_lists(ll, rl));
+      st_rec(&crec[i], out);
+      __stcg(&erec[i], make_uint4(out.meta, aggn0, out.nprim, 0u));
+    }
+    // ready even after a failure (status set), so that no parent waits out its bound
+    __threadfence();
+    atomicExch(&flags[i], 1u);
+  }
+}
+
 // Lanes of a k_costs warp take new nodes once this many of them are idle.
 constexpr uint32_t COST_REFILL_IDLE = 8;
 
@@ -299,8 +381,12 @@ constexpr uint32_t COST_REFILL_IDLE = 8;
 __global__ void __launch_bounds__(BLK) k_costs(const Bvh2Node* __restrict__ nodes, const uint32_t* __restrict__ parents,
                                                const uint32_t* __restrict__ pidx_in, uint32_t n, uint32_t max_prims,
                                                CostRec* crec, EmitRec* erec, uint4* small, uint32_t* flags,
-                                               uint32_t* next, uint32_t* status) {
+                                               uint32_t* next, const uint32_t* unordered, uint32_t* status) {
   grid_dep_wait();
+  if (*unordered == 0) {
+    costs_ordered(nodes, parents, pidx_in, n, max_prims, crec, erec, small, flags, next, status);
+    return;
+  }
   const uint32_t FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const uint32_t lt_mask = (1u << lane) - 1u;
@@ -1156,17 +1242,17 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   if (n == 0) return 0;
   Scratch& s = c.scratch;
   uint32_t* parents = (uint32_t*)s.get(SLOT_PARENTS, (size_t)n * 4);
-  uint32_t* flags = (uint32_t*)s.get(SLOT_FLAGS, (size_t)n * 4 + 4);  // + k_costs' node counter
+  uint32_t* flags = (uint32_t*)s.get(SLOT_FLAGS, (size_t)n * 4 + 8);  // + k_costs' node counter, order flag
   CostRec* crec = (CostRec*)s.get(SLOT_DECISIONS, (size_t)n * sizeof(CostRec));
   EmitRec* erec = (EmitRec*)s.get(SLOT_CW_META, (size_t)n * sizeof(EmitRec));
   uint4* small = (uint4*)s.get(SLOT_CW_SMALL, (size_t)n * sizeof(uint4));
   uint32_t* counters = (uint32_t*)s.get(SLOT_CW_COUNTERS, 64);
   if (!parents || !flags || !crec || !erec || !small || !counters) return c.fail(OBVHS_ERR_OOM, "scratch");
-  int r = compute_parents_device(c, b->nodes, n, parents);
+  CK(cudaMemsetAsync(flags, 0, (size_t)n * 4 + 8, c.stream));
+  int r = compute_parents_device(c, b->nodes, n, parents, flags + n + 1);
   if (r) return r;
-  CK(cudaMemsetAsync(flags, 0, (size_t)n * 4 + 4, c.stream));
   KLAUNCH("k_costs", launch_k(k_costs, cost_grid(c, n), BLK, 0, c.stream, b->nodes, parents, b->prim_indices, n,
-                              max_prims, crec, erec, small, flags, flags + n, c.d_status));
+                              max_prims, crec, erec, small, flags, flags + n, flags + n + 1, c.d_status));
   CK(cudaGetLastError());
   // sizes of the whole tree: the root's aggregate (a leaf root is one node)
   EmitRec root;
@@ -1276,20 +1362,20 @@ int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in
   }
   Scratch& sc = c.scratch;
   uint32_t* parents = (uint32_t*)sc.get(SLOT_PARENTS, (size_t)n * 4);
-  uint32_t* flags = (uint32_t*)sc.get(SLOT_FLAGS, (size_t)n * 4 + 4);  // + k_costs' node counter
+  uint32_t* flags = (uint32_t*)sc.get(SLOT_FLAGS, (size_t)n * 4 + 8);  // + k_costs' node counter, order flag
   CostRec* crec = (CostRec*)sc.get(SLOT_DECISIONS, (size_t)n * sizeof(CostRec));
   EmitRec* erec = (EmitRec*)sc.get(SLOT_CW_META, (size_t)n * sizeof(EmitRec));
   uint4* small = (uint4*)sc.get(SLOT_CW_SMALL, (size_t)n * sizeof(uint4));
   uint32_t* counters = (uint32_t*)sc.get(SLOT_CW_COUNTERS, 64);
   SegRoot* roots = (SegRoot*)sc.get(SLOT_OUTPUT, (size_t)S * sizeof(SegRoot));
   if (!parents || !flags || !crec || !erec || !small || !counters || !roots) return c.fail(OBVHS_ERR_OOM, "scratch");
-  int r = compute_parents_device(c, nodes, n, parents);
+  CK(cudaMemsetAsync(flags, 0, (size_t)n * 4 + 8, c.stream));
+  int r = compute_parents_device(c, nodes, n, parents, flags + n + 1);
   if (r) return r;
   r = seg_root_parents_device(c, L, parents);
   if (r) return r;
-  CK(cudaMemsetAsync(flags, 0, (size_t)n * 4 + 4, c.stream));
   KLAUNCH("k_costs", launch_k(k_costs, cost_grid(c, n), BLK, 0, c.stream, nodes, parents, pidx_in, n, max_prims, crec,
-                              erec, small, flags, flags + n, c.d_status));
+                              erec, small, flags, flags + n, flags + n + 1, c.d_status));
   KLAUNCH("k_seg_roots_out", launch_k(k_seg_roots_out, div_up<uint32_t>(S, BLK), BLK, 0, c.stream,
                                  nodes, erec, L.d_prim_start, L.d_node_start, S, roots));
   CK(cudaGetLastError());

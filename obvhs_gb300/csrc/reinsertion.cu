@@ -46,7 +46,13 @@ struct Reins {
   uint32_t pad;
 };
 
-__global__ void k_parents(const Bvh2Node* __restrict__ nodes, uint32_t n, uint32_t* __restrict__ parents) {
+// Parent links; with `unordered` non-null, also sets *unordered when some
+// inner node's children do not both lie above it in the array (trees straight
+// from PLOC always have them above: pairs are written top down, a parent
+// after its children).  Nodes whose children are out of range (the inert pads
+// of segmented builds) link nothing.
+__global__ void k_parents(const Bvh2Node* __restrict__ nodes, uint32_t n, uint32_t* __restrict__ parents,
+                          uint32_t* unordered) {
   grid_dep_wait();
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -58,6 +64,7 @@ __global__ void k_parents(const Bvh2Node* __restrict__ nodes, uint32_t n, uint32
       parents[f] = i;
       parents[f + 1] = i;
     }
+    if (unordered && f <= i && f + 1 < n) *unordered = 1u;
   }
 }
 
@@ -778,9 +785,11 @@ int reins_pass(BuildCtx& c, Bvh2Node* nodes, uint32_t len, const uint32_t* cand,
 
 }  // namespace
 
-int compute_parents_device(BuildCtx& c, const Bvh2Node* nodes, uint32_t n_nodes, uint32_t* parents) {
+int compute_parents_device(BuildCtx& c, const Bvh2Node* nodes, uint32_t n_nodes, uint32_t* parents,
+                           uint32_t* unordered) {
   if (!n_nodes) return 0;
-  KLAUNCH("k_parents", launch_k(k_parents, div_up<uint32_t>(n_nodes, BLK), BLK, 0, c.stream, nodes, n_nodes, parents));
+  KLAUNCH("k_parents", launch_k(k_parents, div_up<uint32_t>(n_nodes, BLK), BLK, 0, c.stream, nodes, n_nodes, parents,
+                                unordered));
   CK(cudaGetLastError());
   return 0;
 }
