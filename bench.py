@@ -60,7 +60,7 @@ def parse(argv=None):
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tris", type=int, default=N_TRIS, help="headline scene size")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="headline ray batch size (each kind)")
-    ap.add_argument("--only", default="all", choices=["all", "c3", "c3-build", "c2", "c2-build", "c1"],
+    ap.add_argument("--only", default="all", choices=["all", "c3", "c3-build", "c2", "c2-build", "c1", "c4", "c5"],
                     help="run one workload only (profiling); the JSON line then carries that workload")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving comparison (config 5)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 512-scene batched comparison (config 4)")
@@ -364,6 +364,21 @@ class Bench:
         return prof
 
 
+def trav_forms(B: Bench, fn, n_rays, steps=3):
+    """Mrays/s of a traversal call in every launch form of the context
+    (block size x group stack in local (L) or shared (S) memory); the
+    context is left in its default form."""
+    out = {}
+    try:
+        for block, smem in B.G.Context.TRAVERSAL_CONFIGS:
+            B.ctx.set_traversal_config(block, smem)
+            fn()
+            out[f"{block}{'S' if smem else 'L'}"] = r4(n_rays / (mean(B.timed(fn, steps)) * 1e-3) / 1e6)
+    finally:
+        B.ctx.set_traversal_config(0, False)
+    return out
+
+
 def config3(B: Bench, only_build=False):
     """The headline: the 8M architectural scene built PLOC -> CWBVH8, then 16M
     incoherent closest-hit and 16M shadow rays on the tree (device-resident)."""
@@ -414,6 +429,7 @@ def config3(B: Bench, only_build=False):
     out["shadow_ms"] = B.timed(fs, tsteps)
     out["closest_ctri_ms"] = B.timed(fcc, tsteps)
     out["clocks"] = clocks.stop() if clocks else None
+    out["closest_by_form"] = trav_forms(B, fc, len(closest))
     fc()
     torch.cuda.synchronize()
     out["hit_fraction"] = float((hits[:, 0] != -1).float().mean().item())
@@ -467,6 +483,8 @@ def config2(B: Bench, only_build=False):
     B.barrier()
     out["primary_ms"] = B.timed(fp, args.steps)
     out["bounce_ms"] = B.timed(fb, args.steps)
+    out["primary_by_form"] = trav_forms(B, fp, len(rays))
+    out["bounce_by_form"] = trav_forms(B, fb, len(bounce))
     fb()
     torch.cuda.synchronize()
     out["n_primary"], out["n_bounce"] = len(rays), len(bounce)
@@ -543,9 +561,8 @@ def batched_scenes(G, ctx, base, n_scenes=512, seed=1004):
     s_rays = torch.cat([d_rays[i] for i in pick])
     s_owner = torch.from_numpy(np.concatenate([np.full(len(rays[i]), j, np.int32) for j, i in enumerate(pick)])).cuda()
     p, tune = A.tune_segmented([tris[i] for i in pick], s_rays, s_owner, base, ctx=ctx)
-    trav = tune.get("traversal")
-    if trav:
-        ctx.set_traversal_config(trav["block"], trav["stack"])
+    trav = tune["traversal"]
+    ctx.set_traversal_config(trav["block"], trav["smem_stack"])
 
     def plain():
         out = []
@@ -587,16 +604,15 @@ def batched_scenes(G, ctx, base, n_scenes=512, seed=1004):
         for b in bvhs:
             b.free()
     finally:
-        if trav:
-            ctx.set_traversal_config(0, 0)
+        ctx.set_traversal_config(0, False)
     got = hits.cpu().numpy().view(np.uint32)
     exp = np.concatenate([np.stack([r.cpu().numpy().view(np.uint32)[:, 0], r.cpu().numpy().view(np.uint32)[:, 1]], 1)
                           for r in ref])
     identical = bool(np.array_equal(got, exp))
     return {"workload": f"{n_scenes} clustered scenes, 1k-200k triangles (log-uniform), "
                         "4,096-262,144 incoherent rays each", "preset": "medium_build",
-            "tuned": {"radius": int(p.ploc_search_distance), **({"block": trav["block"], "stack": trav["stack"]}
-                                                                if trav else {})},
+            "tuned": {"radius": int(p.ploc_search_distance), "block": trav["block"],
+                      "stack": "shared" if trav["smem_stack"] else "local"},
             "autotune": tune,
             "scenes": n_scenes, "triangles": n_tris, "rays": n_rays,
             "plain_s": t_plain, "batched_s": t_batched, "speedup": t_plain / t_batched,
@@ -759,6 +775,21 @@ def run_gb300(args):
                               "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": m,
                               "config": {"workload": "clustered-1M-slow_build"}}), flush=True)
         return
+    if only in ("c4", "c5"):
+        from obvhs_gb300.params import BvhBuildParams
+
+        res = (batched_scenes(B.G, B.ctx, BvhBuildParams.medium_build()) if only == "c4"
+               else serving(BvhBuildParams.medium_build()))
+        if B.rank == 0:
+            keep = {k: v for k, v in res.items() if not isinstance(v, dict) or k in ("tuned", "autotune")}
+            for k in ("continuous", "plain", "saturated_continuous", "saturated_plain"):
+                if k in res:
+                    keep[k] = {"mrays_s": r4(res[k]["mrays_s"]),
+                               "rays_p50_p99_ms": [r4(res[k]["latency_rays"]["p50_ms"]),
+                                                   r4(res[k]["latency_rays"]["p99_ms"])],
+                               "builds_p99_ms": r4(res[k]["latency_builds"]["p99_ms"])}
+            print(json.dumps({"metric": METRIC, "config": {"workload": only}, **keep}, default=str), flush=True)
+        return
     if only == "c1":
         c1 = config1(B)
         if B.rank == 0:
@@ -838,6 +869,7 @@ def run_gb300(args):
         "c3_shadow_mrays_s": r4(replica_rate(c3["n_shadow"], m_sh, world)),
         "c3_closest_ctri_mrays_s": r4(replica_rate(c3["n_closest"], mean(c3["closest_ctri_ms"]), world)),
         "c3_hit_frac": r4(c3["hit_fraction"]),
+        "c3_closest_by_form": c3["closest_by_form"],
     }
     if cpu:
         line["cpu_baseline"] = {"value": r4(cpu["value"]), "unit": "Mtris/s", "cores": cores, "kind": "port",
@@ -857,6 +889,7 @@ def run_gb300(args):
             "c2_bounce_mrays_s": r4(c2["n_bounce"] / (mean(c2["bounce_ms"]) * 1e-3) / 1e6),
             "c2_primary_hit_frac": r4(c2["primary_hit_fraction"]), "c2_bounce_rays": c2["n_bounce"],
             "c2_launches": c2["launches"],
+            "c2_bounce_by_form": c2["bounce_by_form"],
         })
     if c1:
         line.update({"c1_build_mtris_s": r4(c1["n_tris"] / (mean(c1["build_ms"]) * 1e-3) / 1e6),
@@ -877,7 +910,8 @@ def run_gb300(args):
                        "c3_stage_ms": list(st.stage_ms), "c3_wall_s": c3["wall_s"], "cpu": cpu,
                        "kernel_models": models})
         if c2:
-            detail.update({"c2_profile": c2["profile"], "c2_build_ms": c2["build_ms"],
+            detail.update({"c2_primary_by_form": c2["primary_by_form"], "c2_profile": c2["profile"],
+                           "c2_build_ms": c2["build_ms"],
                            "c2": {k: v for k, v in c2.items() if k not in ("stats", "profile")}})
         if c1:
             detail["c1"] = c1

@@ -358,6 +358,27 @@ OBVHS_API int obvhs_ray_traverse_batches(obvhs_ctx* ctx, const obvhs_cwbvh* cons
                                          uint32_t n_batches, const uint32_t* batch_bvh, const obvhs_ray* const* rays,
                                          const uint32_t* counts, obvhs_hit* const* hits);
 
+/* ---- traversal launch form ---------------------------------------------- */
+/* No counterpart in the reference (its stack is a fixed 32-entry StackStack,
+ * src/cwbvh/mod.rs:60-64).  The closest-hit and occlusion traversals
+ * (obvhs_ray_traverse, _miss, _multi, _batches) on this context launch with
+ * `block` threads per block (64, 128 or 256) and keep each ray's 32-entry
+ * group stack in local memory, or in shared memory (smem_stack = 1, blocks
+ * of 64 or 128).  Results are identical in every form; (0, 0) restores the
+ * default (128, local).  Other values return OBVHS_ERR_INVALID_ARG. */
+OBVHS_API int obvhs_ctx_set_traversal_config(obvhs_ctx* ctx, uint32_t block, int smem_stack);
+
+/* ---- device wait limits -------------------------------------------------- */
+/* No counterpart in the reference (it has no device waits).  Radix-sort tiles
+ * wait for earlier tiles' counts (decoupled look-back); a tile gives up after
+ * `spins` empty look-back rounds, and the build returns OBVHS_ERR_LIMIT with
+ * no use of the unfinished order.  The default, OBVHS_DEFAULT_WAIT_LIMIT, is
+ * only reached when something has gone wrong; a small value is for testing the
+ * failure path (0: give up at the first wait).  Later calls on the context
+ * work normally once the limit is set back. */
+#define OBVHS_DEFAULT_WAIT_LIMIT 16777216u
+OBVHS_API int obvhs_ctx_set_wait_limit(obvhs_ctx* ctx, uint32_t spins);
+
 /* ---- stage-level access for parity checks ------------------------------- */
 /* sort_nodes_by_morton (src/ploc/mod.rs:771-847) on Bvh2Node::new(aabbs[i])
  * leaves: codes in input order (u64 pairs: lo, hi; hi = 0 for U64) and the

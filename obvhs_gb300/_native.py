@@ -70,6 +70,8 @@ SIGNATURES = {
     "obvhs_ctx_kernel_launches": (U64, [P]),
     "obvhs_ctx_set_profiling": (I32, [P, I32]),
     "obvhs_ctx_set_shared_gpu": (I32, [P, I32]),
+    "obvhs_ctx_set_wait_limit": (I32, [P, U32]),
+    "obvhs_ctx_set_traversal_config": (I32, [P, U32, I32]),
     "obvhs_ctx_profile_report": (I32, [P, P, U64]),
     "obvhs_ploc_build": (I32, [P, P, P, U32, U32, U32, U32, I32, ctypes.POINTER(P), ctypes.POINTER(BuildStats)]),
     "obvhs_bvh2_info": (I32, [P, ctypes.POINTER(U32), ctypes.POINTER(U32), ctypes.POINTER(U32)]),

@@ -110,6 +110,24 @@ class Context:
         PLOC and conflict resolution); results are identical."""
         self.check(self.lib.obvhs_ctx_set_shared_gpu(self.h, int(bool(shared))))
 
+    #: (threads per block, group stack in shared memory) forms of the traversal
+    TRAVERSAL_CONFIGS = ((128, False), (64, False), (256, False), (64, True), (128, True))
+
+    def set_traversal_config(self, block: int = 0, smem_stack: bool = False):
+        """Launch form of this context's CWBVH traversals: block size and
+        where each ray's 32-entry group stack lives (identical results in
+        every form; (0, False) is the default (128, local memory))."""
+        self.check(self.lib.obvhs_ctx_set_traversal_config(self.h, int(block), int(bool(smem_stack))))
+
+    #: OBVHS_DEFAULT_WAIT_LIMIT in include/obvhs_gb300.h
+    DEFAULT_WAIT_LIMIT = 16777216
+
+    def set_wait_limit(self, spins: int = DEFAULT_WAIT_LIMIT):
+        """Empty look-back rounds a radix-sort tile waits for earlier tiles
+        before it gives up (the build then raises ObvhsError with
+        OBVHS_ERR_LIMIT); small values exercise that failure path."""
+        self.check(self.lib.obvhs_ctx_set_wait_limit(self.h, int(spins)))
+
     def profile_report(self) -> dict:
         """Per-kernel {launches, total_ms, max_ms} since the last report."""
         import json

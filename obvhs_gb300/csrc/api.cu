@@ -440,6 +440,10 @@ struct DeviceShared {
   cudaStream_t coop = nullptr;
   std::atomic<int> contexts{0};
   std::atomic<int> builds{0};
+  // the builds-in-flight count, in mapped pinned memory that running
+  // traversal kernels read (traversal_yield_word); kept for the process's life
+  uint32_t* h_yield = nullptr;
+  uint32_t* d_yield = nullptr;
 };
 
 DeviceShared& device_shared(int device) {
@@ -459,8 +463,40 @@ bool pdl_enabled() {
 
 int device_context_count(int device) { return device_shared(device).contexts.load(); }
 int device_concurrent_builds(int device) { return device_shared(device).builds.load(); }
-void device_build_enter(int device) { device_shared(device).builds.fetch_add(1); }
-void device_build_leave(int device) { device_shared(device).builds.fetch_sub(1); }
+void device_build_enter(int device) {
+  DeviceShared& d = device_shared(device);
+  const int b = d.builds.fetch_add(1) + 1;
+  if (d.h_yield) __atomic_store_n(d.h_yield, (uint32_t)b, __ATOMIC_RELEASE);
+}
+void device_build_leave(int device) {
+  DeviceShared& d = device_shared(device);
+  const int b = d.builds.fetch_sub(1) - 1;
+  if (d.h_yield) __atomic_store_n(d.h_yield, (uint32_t)std::max(b, 0), __ATOMIC_RELEASE);
+}
+
+// The device address of `device`'s builds-in-flight word (set up once, with
+// the device current), or null when mapped memory is unavailable.
+const uint32_t* traversal_yield_word(int device) {
+  DeviceShared& d = device_shared(device);
+  std::lock_guard<std::mutex> lock(d.m);
+  if (!d.d_yield) {
+    uint32_t* h = nullptr;
+    void* dp = nullptr;
+    if (cudaHostAlloc((void**)&h, 64, cudaHostAllocMapped) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    if (cudaHostGetDevicePointer(&dp, h, 0) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFreeHost(h);
+      return nullptr;
+    }
+    __atomic_store_n(h, (uint32_t)std::max(d.builds.load(), 0), __ATOMIC_RELEASE);
+    d.h_yield = h;
+    d.d_yield = static_cast<uint32_t*>(dp);
+  }
+  return d.d_yield;
+}
 
 cudaError_t coop_launch(obvhs_ctx& c, const void* func, unsigned grid, unsigned block, void** args, size_t smem) {
   DeviceShared& d = device_shared(c.device);
@@ -507,6 +543,7 @@ int obvhs_ctx_create(int device, uint64_t hbm_budget_bytes, obvhs_ctx** out) {
     obvhs_ctx_destroy(c);
     return OBVHS_ERR_CUDA;
   }
+  c->d_yield = traversal_yield_word(device);
   cudaDeviceSynchronize();
   device_shared(device).contexts.fetch_add(1);
   *out = c;
@@ -546,6 +583,21 @@ uint64_t obvhs_ctx_kernel_launches(const obvhs_ctx* c) { return c ? c->kernel_la
 int obvhs_ctx_set_shared_gpu(obvhs_ctx* c, int shared) {
   if (!c) return OBVHS_ERR_INVALID_ARG;
   c->shared_gpu = shared != 0;
+  return OBVHS_OK;
+}
+
+int obvhs_ctx_set_traversal_config(obvhs_ctx* c, uint32_t block, int smem_stack) {
+  if (!c) return OBVHS_ERR_INVALID_ARG;
+  const int f = traversal_form_index(block, smem_stack);
+  if (f < 0) return c->fail(OBVHS_ERR_INVALID_ARG, "traversal config: block 64/128/256 with a local stack, or 64/128 "
+                                                   "with a shared-memory stack (0, 0: the default)");
+  c->trav_form = f;
+  return OBVHS_OK;
+}
+
+int obvhs_ctx_set_wait_limit(obvhs_ctx* c, uint32_t spins) {
+  if (!c) return OBVHS_ERR_INVALID_ARG;
+  c->wait_limit = spins;
   return OBVHS_OK;
 }
 

@@ -136,6 +136,15 @@ static_assert(READBACK_OFFSET + sizeof(BuildReadback) <= RUN_FLAG_OFFSET, "pinne
 struct obvhs_ctx {
   int device = 0;
   int num_sms = 0;
+  // empty look-back rounds a radix-sort tile waits before it gives up
+  // (status ST_ITER_LIMIT); obvhs_ctx_set_wait_limit
+  uint32_t wait_limit = OBVHS_DEFAULT_WAIT_LIMIT;
+  // traversal launch form (block size, stack placement); 0 = the default
+  // (obvhs_ctx_set_traversal_config)
+  int trav_form = 0;
+  // device address of the device's builds-in-flight word (mapped host
+  // memory), read by persistent traversals to leave room for builds; or null
+  const uint32_t* d_yield = nullptr;
   cudaStream_t stream = nullptr;
   uint32_t* d_status = nullptr;
   uint32_t* h_status = nullptr;  // pinned
@@ -192,6 +201,7 @@ int device_context_count(int device);
 int device_concurrent_builds(int device);
 void device_build_enter(int device);
 void device_build_leave(int device);
+const uint32_t* traversal_yield_word(int device);
 struct BuildScope {
   int device;
   explicit BuildScope(int d) : device(d) { device_build_enter(d); }
@@ -329,6 +339,10 @@ int reinsertion_device(BuildCtx& c, obvhs_bvh2* b, float batch_size_ratio, const
 // Parent links of every node (roots: their own).  With `unordered`, also
 // sets *unordered (zeroed by the caller) when some inner node's children are
 // not both at higher indices than the node.
+// The traversal launch form for (threads per block, group stack in shared
+// memory); -1 when there is none.
+int traversal_form_index(uint32_t block, int smem_stack);
+
 int compute_parents_device(BuildCtx& c, const Bvh2Node* nodes, uint32_t n_nodes, uint32_t* parents,
                            uint32_t* unordered = nullptr);
 // Copies a host table to the device (stream-ordered, from pinned staging);

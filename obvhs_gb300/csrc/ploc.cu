@@ -1490,6 +1490,16 @@ int ploc_morton_codes(BuildCtx& c, const Bvh2Node* leaves, uint32_t n, const int
   return 0;
 }
 
+// After a synchronised read of the status word into c.h_status: a sort
+// whose look-back gave up (ST_ITER_LIMIT) ends the build with
+// OBVHS_ERR_LIMIT, the word cleared for the context's next call.
+static int sort_status(BuildCtx& c) {
+  if (!(*c.h_status & ST_ITER_LIMIT)) return 0;
+  CK(cudaMemsetAsync(c.d_status, 0, 4, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return c.fail(OBVHS_ERR_LIMIT, "radix sort: a tile's look-back wait reached the context's wait limit");
+}
+
 // Stable order of the codes (*order_out), leaving `codes` as they are.
 //
 // The sort runs on the high digits only (U128: the high 64 bits; U64: bits
@@ -1521,7 +1531,11 @@ int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_
     KLAUNCH("k_run_check", CK(launch_k(k_run_check, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, stop, n, flag)));
     uint32_t* h = reinterpret_cast<uint32_t*>(static_cast<char*>(c.h_small) + RUN_FLAG_OFFSET);  // pinned
     CK(cudaMemcpyAsync(h, flag, 4, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaMemcpyAsync(c.h_status, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
+    // a sort tile that gave up its wait leaves the order unusable: stop here
+    int r = sort_status(c);
+    if (r) return r;
     if (*h == 0) {
       KLAUNCH("k_fix_runs", CK(launch_k(k_fix_runs, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, stop, ord, codes, n,
                                         precision)));
@@ -1536,6 +1550,12 @@ int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_
     e = radix_sort_pairs<unsigned long long>(c, (unsigned long long*)codes, vals, n, true,
                                              (unsigned long long*)keys_alt, vals_alt, rs, &alt);
   if (e) return c.cuda_fail(e, "radix sort");
+  if (n > RUN_MAX) {  // the rare whole-code sort: its order is checked too
+    CK(cudaMemcpyAsync(c.h_status, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    int r = sort_status(c);
+    if (r) return r;
+  }
   *order_out = alt ? vals_alt : vals;
   return 0;
 }

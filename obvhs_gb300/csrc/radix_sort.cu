@@ -12,8 +12,12 @@
 //                  digit in shared memory and write each digit's run to
 //                  consecutive addresses.
 // No host synchronisation.  The look-back waits only on tiles that were
-// claimed earlier and are therefore resident; every wait is bounded and sets
-// a status bit instead of spinning forever.
+// claimed earlier and are therefore resident; every wait is bounded (the
+// context's wait limit: empty look-back rounds a tile tolerates) and sets a
+// status bit instead of spinning forever.  A tile that gives up still
+// publishes an inclusive count (a partial one), so later tiles finish and
+// every write stays inside the output; the caller checks the status before it
+// uses the order.
 #include "radix_sort.cuh"
 #include "build.h"
 
@@ -24,7 +28,6 @@ constexpr int WARPS = THREADS / 32;
 constexpr uint32_t FLAG_AGG = 1u << 30;
 constexpr uint32_t FLAG_INC = 2u << 30;
 constexpr uint32_t VAL_MASK = (1u << 30) - 1;
-constexpr uint32_t SPIN_LIMIT = 1u << 24;
 constexpr int LB_WINDOW = 8;
 constexpr int HIST_ITEMS = 8;
 
@@ -109,7 +112,8 @@ __global__ void __launch_bounds__(THREADS, 2) k_rs_pass(const K* __restrict__ ke
                                                      K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                                                      uint32_t n, int byte, bool iota,
                                                      const uint32_t* __restrict__ digit_base,
-                                                     uint32_t* tile_status, uint32_t* tile_counter, uint32_t* status) {
+                                                     uint32_t* tile_status, uint32_t* tile_counter, uint32_t* status,
+                                                     uint32_t spin_limit) {
   grid_dep_wait();
   constexpr int ITEMS = Tile<K, SMALL>::ITEMS;
   constexpr int TS = Tile<K, SMALL>::SIZE;
@@ -223,7 +227,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_rs_pass(const K* __restrict__ ke
       }
       if (stop) break;
       t -= adv;
-      if (adv == 0 && ++spins > SPIN_LIMIT) {
+      if (adv == 0 && ++spins > spin_limit) {
         atomicOr(status, 4u);  // ST_ITER_LIMIT
         break;
       }
@@ -312,10 +316,12 @@ cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, 
     uint32_t* ts = pass_area + (size_t)b * pass_words;
     if (small)
       KLAUNCH("k_rs_pass", launch_k(k_rs_pass<K, true>, ntiles, THREADS, 0, c.stream, kin, vin, kout, vout, n, b, iota,
-                                                                               hist + b * 256, ts + 32, ts, c.d_status));
+                                                                               hist + b * 256, ts + 32, ts, c.d_status,
+                                                                               c.wait_limit));
     else
       KLAUNCH("k_rs_pass", launch_k(k_rs_pass<K, false>, ntiles, THREADS, 0, c.stream, kin, vin, kout, vout, n, b, iota,
-                                                                                hist + b * 256, ts + 32, ts, c.d_status));
+                                                                                hist + b * 256, ts + 32, ts, c.d_status,
+                                                                               c.wait_limit));
     iota = false;
     std::swap(kin, kout);
     std::swap(vin, vout);

@@ -212,16 +212,29 @@ constexpr uint32_t REFILL_IDLE = 4;
 // memory; once REFILL_IDLE lanes are idle the busy lanes leave their loops,
 // keeping their state, and the idle lanes take the next rays with one atomic
 // per warp.  The lanes converge only at the refill.
-template <class R>
-__device__ __forceinline__ void persistent_rays(R& ray, uint32_t nrays, uint32_t* next_ray) {
+//
+// `yield` (or null): the device's count of builds in flight, in mapped host
+// memory.  While it is non-zero, warps of odd blocks stop taking rays (every
+// eighth refill checks it) and their blocks leave once their rays are done, so
+// a concurrent build's kernels find free slots on every SM instead of waiting
+// for the whole persistent grid; the even blocks take the remaining rays.
+template <class R, int TB = TBLK>
+__device__ __forceinline__ void persistent_rays(R& ray, uint32_t nrays, uint32_t* next_ray,
+                                                const uint32_t* yield = nullptr) {
   const uint32_t FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  __shared__ uint32_t s_idle[TBLK / 32];
+  __shared__ uint32_t s_idle[TB / 32];
   uint32_t* idle_ctr = &s_idle[threadIdx.x >> 5];
   bool alive = false;    // this lane holds a ray
   bool drained = false;  // (warp-uniform) the ray counter has run out
+  uint32_t refills = 0;
   for (;;) {
+    if (!drained && yield && (blockIdx.x & 1u)) {
+      uint32_t y = 0;
+      if (lane == 0 && (++refills & 7u) == 0) y = *(volatile const uint32_t*)yield;
+      if (__shfl_sync(FULL, y, 0)) drained = true;
+    }
     if (!drained) {
       const uint32_t need = __ballot_sync(FULL, !alive);
       if (need) {
@@ -263,7 +276,7 @@ __device__ __forceinline__ void persistent_rays(R& ray, uint32_t nrays, uint32_t
 // its BVH (ray_bvh[ray] indexes `multi`), so ray batches against different
 // BVHs run in one launch.  A step handles the primitives of the current
 // group, then pops one child node (or a group from the stack).
-template <int MODE, bool CTRI, bool MULTI>
+template <int MODE, bool CTRI, bool MULTI, int STRIDE = 1>
 struct CwRay {
   // launch inputs
   const CwNode* nodes_in;
@@ -286,7 +299,7 @@ struct CwRay {
   float tmin, ray_tmax, tmax, hit_t;
   bool fast;  // ray_fast_ok
   uint2 cur, prim;
-  uint2* stack;  // 32 entries, the thread's own (kept apart so the scalars stay in registers)
+  uint2* stack;  // 32 entries, the thread's own, STRIDE apart (kept apart so the scalars stay in registers)
 
   __device__ __forceinline__ bool start(uint32_t r) {
     ri = r;
@@ -376,7 +389,7 @@ struct CwRay {
       const uint32_t cbase = cur.x;
       cur.y &= ~(1u << cio);
       if (cur.y & 0xff000000u) {
-        stack[sp] = cur;
+        stack[sp * STRIDE] = cur;
         sp = min(sp + 1, 31u);
       }
       const uint32_t slot = (cio - 24) ^ (oct & 0xffu);
@@ -398,14 +411,19 @@ struct CwRay {
     }
     if (prim.y == 0 && (cur.y & 0xff000000u) == 0) {
       if (sp == 0) return finish();
-      cur = stack[--sp];
+      --sp;
+      cur = stack[sp * STRIDE];
     }
     return false;
   }
 };
 
-template <int MODE, bool CTRI = false, bool MULTI = false>
-__global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ nodes_in, uint32_t n_nodes_in,
+// TB: threads per block.  SST: the group stack in shared memory (32 entries
+// per thread, entry k of thread t at [k][t]: consecutive threads' entries
+// are adjacent, so a warp's pushes and pops are conflict-free) instead of
+// the thread's local memory.  Same loop, same results.
+template <int MODE, bool CTRI = false, bool MULTI = false, int TB = TBLK, bool SST = false>
+__global__ void __launch_bounds__(TB) k_traverse(const CwNode* __restrict__ nodes_in, uint32_t n_nodes_in,
                                                    const float4* __restrict__ tris_in, uint32_t n_prims_in,
                                                    const float4* __restrict__ rays,
                                                    uint32_t nrays, uint2* __restrict__ hits, uint8_t* __restrict__ miss,
@@ -413,11 +431,13 @@ __global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ no
                                                    const uint2* __restrict__ ctris = nullptr,
                                                    const uint32_t* __restrict__ pidx = nullptr,
                                                    const BlasDesc* __restrict__ multi = nullptr,
-                                                   const uint32_t* __restrict__ ray_bvh = nullptr, uint32_t n_multi = 0) {
+                                                   const uint32_t* __restrict__ ray_bvh = nullptr, uint32_t n_multi = 0,
+                                                   const uint32_t* yield = nullptr) {
   grid_dep_wait();
-  uint2 stack[32];
-  CwRay<MODE, CTRI, MULTI> ray;
-  ray.stack = stack;
+  uint2 lstack[SST ? 1 : 32];
+  __shared__ uint2 sstack[SST ? 32 * TB : 1];
+  CwRay<MODE, CTRI, MULTI, SST ? TB : 1> ray;
+  ray.stack = SST ? sstack + threadIdx.x : lstack;
   ray.nodes_in = nodes_in;
   ray.tris_in = tris_in;
   ray.n_nodes_in = n_nodes_in;
@@ -431,7 +451,67 @@ __global__ void __launch_bounds__(TBLK) k_traverse(const CwNode* __restrict__ no
   ray.multi = multi;
   ray.ray_bvh = ray_bvh;
   ray.n_multi = n_multi;
-  persistent_rays(ray, nrays, next_ray);
+  persistent_rays<decltype(ray), TB>(ray, nrays, next_ray, yield);
+}
+
+// The traversal launch forms a context can choose (obvhs_ctx_set_traversal_config):
+// block size and stack placement.  Form 0 is the default.
+struct TravForm {
+  int block;
+  bool smem_stack;
+};
+constexpr TravForm TRAV_FORMS[] = {{128, false}, {64, false}, {256, false}, {64, true}, {128, true}};
+constexpr int N_TRAV_FORMS = 5;
+
+// Launches k_traverse<MODE, false, MULTI> in form f as a persistent grid
+// (resident blocks, or fewer for a small batch).
+template <int MODE, bool MULTI, int TB, bool SST>
+cudaError_t launch_trav_form(BuildCtx& c, uint32_t n, const CwNode* nodes, uint32_t n_nodes, const float4* tris,
+                             uint32_t n_prims, const float4* rays, uint2* hits, uint8_t* miss, uint32_t* counter,
+                             const BlasDesc* dd, const uint32_t* ray_bvh, uint32_t n_bvh) {
+  static std::atomic<int> per_sm_s{0};
+  int per_sm = per_sm_s.load();
+  if (!per_sm) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_traverse<MODE, false, MULTI, TB, SST>, TB, 0) !=
+            cudaSuccess ||
+        per_sm < 1) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
+    per_sm_s.store(per_sm);
+  }
+  const uint32_t grid = std::min<uint32_t>(div_up<uint32_t>(n, TB), (uint32_t)(per_sm * c.num_sms));
+  const char* name = MULTI ? (MODE == 0 ? "k_traverse_closest_multi" : "k_traverse_occluded_multi")
+                           : (MODE == 0 ? "k_traverse_closest" : "k_traverse_occluded");
+  c.kbegin(name);
+  launch_k(k_traverse<MODE, false, MULTI, TB, SST>, grid, TB, 0, c.stream, nodes, n_nodes, tris, n_prims, rays, n,
+           hits, miss, counter, c.d_status, (const uint2*)nullptr, (const uint32_t*)nullptr, dd, ray_bvh, n_bvh,
+           c.d_yield);
+  c.kend();
+  return cudaGetLastError();
+}
+
+template <int MODE, bool MULTI>
+cudaError_t launch_trav(BuildCtx& c, uint32_t n, const CwNode* nodes, uint32_t n_nodes, const float4* tris,
+                        uint32_t n_prims, const float4* rays, uint2* hits, uint8_t* miss, uint32_t* counter,
+                        const BlasDesc* dd, const uint32_t* ray_bvh, uint32_t n_bvh) {
+  switch (c.trav_form) {
+    case 1:
+      return launch_trav_form<MODE, MULTI, 64, false>(c, n, nodes, n_nodes, tris, n_prims, rays, hits, miss, counter,
+                                                      dd, ray_bvh, n_bvh);
+    case 2:
+      return launch_trav_form<MODE, MULTI, 256, false>(c, n, nodes, n_nodes, tris, n_prims, rays, hits, miss, counter,
+                                                       dd, ray_bvh, n_bvh);
+    case 3:
+      return launch_trav_form<MODE, MULTI, 64, true>(c, n, nodes, n_nodes, tris, n_prims, rays, hits, miss, counter,
+                                                     dd, ray_bvh, n_bvh);
+    case 4:
+      return launch_trav_form<MODE, MULTI, 128, true>(c, n, nodes, n_nodes, tris, n_prims, rays, hits, miss, counter,
+                                                      dd, ray_bvh, n_bvh);
+    default:
+      return launch_trav_form<MODE, MULTI, 128, false>(c, n, nodes, n_nodes, tris, n_prims, rays, hits, miss, counter,
+                                                       dd, ray_bvh, n_bvh);
+  }
 }
 
 // --- Bvh2::ray_traverse / ray_traverse_miss (src/bvh2/mod.rs:148-337) -----------
@@ -1191,11 +1271,13 @@ int traverse_compressed_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float*
   if (mode == 0)
     KLAUNCH("k_traverse_closest_ctri", launch_k(k_traverse<0, true>, grid, TBLK, 0, c.stream,
                                            bvh->nodes, bvh->n_nodes, nullptr, bvh->n_prims, (const float4*)rays, n,
-                                           (uint2*)hits, nullptr, counter, c.d_status, bvh->ctris, bvh->prim_indices, nullptr, nullptr, 0u));
+                                           (uint2*)hits, nullptr, counter, c.d_status, bvh->ctris, bvh->prim_indices, nullptr, nullptr, 0u,
+                                           c.d_yield));
   else
     KLAUNCH("k_traverse_occluded_ctri", launch_k(k_traverse<1, true>, grid, TBLK, 0, c.stream,
                                             bvh->nodes, bvh->n_nodes, nullptr, bvh->n_prims, (const float4*)rays, n,
-                                            nullptr, miss, counter, c.d_status, bvh->ctris, bvh->prim_indices, nullptr, nullptr, 0u));
+                                            nullptr, miss, counter, c.d_status, bvh->ctris, bvh->prim_indices, nullptr, nullptr, 0u,
+                                            c.d_yield));
   CK(cudaGetLastError());
   return 0;
 }
@@ -1217,25 +1299,12 @@ int traverse_multi_device(BuildCtx& c, const obvhs_cwbvh* const* bvhs, uint32_t 
     CK(cudaMemcpyAsync(dd, hd.data(), (size_t)n_bvh * sizeof(BlasDesc), cudaMemcpyHostToDevice, c.stream));
   }
   CK(cudaMemsetAsync(counter, 0, 4, c.stream));
-  static std::atomic<int> per_sm_s{0};
-  int per_sm = per_sm_s.load();
-  if (!per_sm) {
-    int a = 0, b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_traverse<0, false, true>, TBLK, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_traverse<1, false, true>, TBLK, 0);
-    per_sm = std::max(1, std::min(a, b));
-    per_sm_s.store(per_sm);
-  }
-  const uint32_t grid = std::min<uint32_t>(div_up<uint32_t>(n, TBLK), (uint32_t)(per_sm * c.num_sms));
   if (mode == 0)
-    KLAUNCH("k_traverse_closest_multi", launch_k(k_traverse<0, false, true>, grid, TBLK, 0, c.stream,
-                                            nullptr, 0, nullptr, 0, (const float4*)rays, n, (uint2*)hits, nullptr,
-                                            counter, c.d_status, nullptr, nullptr, dd, ray_bvh, n_bvh));
+    CK((launch_trav<0, true>(c, n, nullptr, 0, nullptr, 0, (const float4*)rays, (uint2*)hits, nullptr, counter, dd,
+                            ray_bvh, n_bvh)));
   else
-    KLAUNCH("k_traverse_occluded_multi", launch_k(k_traverse<1, false, true>, grid, TBLK, 0, c.stream,
-                                             nullptr, 0, nullptr, 0, (const float4*)rays, n, nullptr, miss, counter,
-                                             c.d_status, nullptr, nullptr, dd, ray_bvh, n_bvh));
-  CK(cudaGetLastError());
+    CK((launch_trav<1, true>(c, n, nullptr, 0, nullptr, 0, (const float4*)rays, nullptr, miss, counter, dd, ray_bvh,
+                            n_bvh)));
   return 0;
 }
 
@@ -1246,25 +1315,12 @@ int traverse_device(BuildCtx& c, const obvhs_cwbvh* bvh, const float* rays, uint
   uint32_t* counter = (uint32_t*)c.scratch.get(SLOT_OUTPUT, 16);
   if (!counter) return c.fail(OBVHS_ERR_OOM, "scratch");
   CK(cudaMemsetAsync(counter, 0, 4, c.stream));
-  static std::atomic<int> per_sm_s{0};
-  int per_sm = per_sm_s.load();
-  if (!per_sm) {
-    int a = 0, b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_traverse<0>, TBLK, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_traverse<1>, TBLK, 0);
-    per_sm = std::max(1, std::min(a, b));
-    per_sm_s.store(per_sm);
-  }
-  uint32_t want = div_up<uint32_t>(n, TBLK);
-  uint32_t grid = std::min<uint32_t>(want, (uint32_t)(per_sm * c.num_sms));
   if (mode == 0)
-    KLAUNCH("k_traverse_closest", launch_k(k_traverse<0>, grid, TBLK, 0, c.stream, bvh->nodes, bvh->n_nodes, bvh->tris, bvh->n_prims, (const float4*)rays, n,
-                                               (uint2*)hits, nullptr, counter, c.d_status, nullptr, nullptr,
-                                               nullptr, nullptr, 0u));
+    CK((launch_trav<0, false>(c, n, bvh->nodes, bvh->n_nodes, bvh->tris, bvh->n_prims, (const float4*)rays,
+                             (uint2*)hits, nullptr, counter, nullptr, nullptr, 0u)));
   else
-    KLAUNCH("k_traverse_occluded", launch_k(k_traverse<1>, grid, TBLK, 0, c.stream, bvh->nodes, bvh->n_nodes, bvh->tris, bvh->n_prims, (const float4*)rays, n, nullptr,
-                                               miss, counter, c.d_status, nullptr, nullptr, nullptr, nullptr, 0u));
-  CK(cudaGetLastError());
+    CK((launch_trav<1, false>(c, n, bvh->nodes, bvh->n_nodes, bvh->tris, bvh->n_prims, (const float4*)rays, nullptr,
+                             miss, counter, nullptr, nullptr, 0u)));
   return 0;
 }
 
@@ -1312,4 +1368,12 @@ int query_device(BuildCtx& c, int structure, int kind, const void* nodes, uint32
   }
 #undef QLAUNCH
   return 0;
+}
+
+// Maps (block, smem_stack) to a launch form of the traversal kernels.
+int traversal_form_index(uint32_t block, int smem_stack) {
+  if (block == 0 && !smem_stack) return 0;
+  for (int f = 0; f < N_TRAV_FORMS; f++)
+    if ((uint32_t)TRAV_FORMS[f].block == block && TRAV_FORMS[f].smem_stack == (smem_stack != 0)) return f;
+  return -1;
 }
