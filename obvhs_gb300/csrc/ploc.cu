@@ -118,16 +118,11 @@ __global__ void __launch_bounds__(BLK) k_leaves_from_aabbs(const float* __restri
 
 // --- Morton codes (src/ploc/morton.rs, src/ploc/mod.rs:287-288,782-785) ----
 
-__device__ __forceinline__ uint32_t sat_u32(double d) {
-  if (!(d > 0.0)) return 0u;
-  if (d >= 4294967295.0) return 0xffffffffu;
-  return (uint32_t)d;
-}
-__device__ __forceinline__ unsigned long long sat_u64(double d) {
-  if (!(d > 0.0)) return 0ull;
-  if (d >= 18446744073709551615.0) return ~0ull;
-  return (unsigned long long)d;
-}
+// Rust's saturating `as u32` / `as u64` (NaN -> 0, below 0 -> 0, above the
+// range -> the maximum): the device's round-toward-zero conversion clamps the
+// same way, in one instruction.
+__device__ __forceinline__ uint32_t sat_u32(double d) { return __double2uint_rz(d); }
+__device__ __forceinline__ unsigned long long sat_u64(double d) { return __double2ull_rz(d); }
 __device__ __forceinline__ unsigned long long split3_u64(uint32_t a) {
   unsigned long long x = a & 0x1fffffull;
   x = (x | x << 32) & 0x1f00000000ffffull;
@@ -148,29 +143,36 @@ __device__ __forceinline__ void split3_u128(unsigned long long a, unsigned long 
   hi = split3_u64((uint32_t)(x & 0xfffffu)) << 2;
 }
 
+// The reference computes (c * scale + offset) * 2^bits in f64
+// (src/ploc/mod.rs:782-785, morton.rs).  Scaling by a power of two commutes
+// with rounding (no result here is near the f64 range limits), so the grid
+// factor 2^bits is folded into scale and offset: the same values, one
+// multiplication fewer per coordinate.
 struct Scale {
   double sx, sy, sz, ox, oy, oz;
 };
-__device__ __forceinline__ Scale make_scale(const int* tk) {
+__device__ __forceinline__ Scale make_scale(const int* tk, double grid) {
   float mnx = fkey_inv(tk[0]), mny = fkey_inv(tk[1]), mnz = fkey_inv(tk[2]);
   float mxx = fkey_inv(tk[3]), mxy = fkey_inv(tk[4]), mxz = fkey_inv(tk[5]);
   Scale s;
-  s.sx = 1.0 / (double)(mxx - mnx);
-  s.sy = 1.0 / (double)(mxy - mny);
-  s.sz = 1.0 / (double)(mxz - mnz);
-  s.ox = -(double)mnx * s.sx;
-  s.oy = -(double)mny * s.sy;
-  s.oz = -(double)mnz * s.sz;
+  const double sx = 1.0 / (double)(mxx - mnx), sy = 1.0 / (double)(mxy - mny), sz = 1.0 / (double)(mxz - mnz);
+  s.sx = sx * grid;
+  s.sy = sy * grid;
+  s.sz = sz * grid;
+  s.ox = (-(double)mnx * sx) * grid;
+  s.oy = (-(double)mny * sy) * grid;
+  s.oz = (-(double)mnz * sz) * grid;
   return s;
 }
+constexpr double GRID64 = (double)(1u << 21);
+constexpr double GRID128 = (double)(1ull << 42);
 
 __device__ __forceinline__ unsigned long long morton64_of(const Bvh2Node& nd, const Scale& s) {
   float cx = (nd.b.x + nd.a.x) * 0.5f, cy = (nd.b.y + nd.a.y) * 0.5f, cz = (nd.b.z + nd.a.z) * 0.5f;
   double px = __dadd_rn(__dmul_rn((double)cx, s.sx), s.ox);
   double py = __dadd_rn(__dmul_rn((double)cy, s.sy), s.oy);
   double pz = __dadd_rn(__dmul_rn((double)cz, s.sz), s.oz);
-  const double k = (double)(1u << 21);
-  return split3_u64(sat_u32(px * k)) | split3_u64(sat_u32(py * k)) << 1 | split3_u64(sat_u32(pz * k)) << 2;
+  return split3_u64(sat_u32(px)) | split3_u64(sat_u32(py)) << 1 | split3_u64(sat_u32(pz)) << 2;
 }
 
 __device__ __forceinline__ U128 morton128_of(const Bvh2Node& nd, const Scale& s) {
@@ -178,11 +180,10 @@ __device__ __forceinline__ U128 morton128_of(const Bvh2Node& nd, const Scale& s)
   double px = __dadd_rn(__dmul_rn((double)cx, s.sx), s.ox);
   double py = __dadd_rn(__dmul_rn((double)cy, s.sy), s.oy);
   double pz = __dadd_rn(__dmul_rn((double)cz, s.sz), s.oz);
-  const double k = (double)(1ull << 42);
   unsigned long long xl, xh, yl, yh, zl, zh;
-  split3_u128(sat_u64(px * k), xl, xh);
-  split3_u128(sat_u64(py * k), yl, yh);
-  split3_u128(sat_u64(pz * k), zl, zh);
+  split3_u128(sat_u64(px), xl, xh);
+  split3_u128(sat_u64(py), yl, yh);
+  split3_u128(sat_u64(pz), zl, zh);
   // (x) | (y << 1) | (z << 2) on 128-bit values
   U128 c;
   c.lo = xl | (yl << 1) | (zl << 2);
@@ -193,9 +194,9 @@ __device__ __forceinline__ U128 morton128_of(const Bvh2Node& nd, const Scale& s)
 // The scale and offset (three double-precision divisions) are computed once
 // per block by its first thread: the double-precision pipe is narrow, and
 // per thread the divisions cost more than the codes themselves.
-__device__ __forceinline__ Scale block_scale(const int* total_keys) {
+__device__ __forceinline__ Scale block_scale(const int* total_keys, double grid) {
   __shared__ Scale s_scale;
-  if (threadIdx.x == 0) s_scale = make_scale(total_keys);
+  if (threadIdx.x == 0) s_scale = make_scale(total_keys, grid);
   __syncthreads();
   return s_scale;
 }
@@ -203,7 +204,7 @@ __device__ __forceinline__ Scale block_scale(const int* total_keys) {
 __global__ void __launch_bounds__(BLK) k_morton64(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
                                                   unsigned long long* __restrict__ codes) {
   grid_dep_wait();
-  const Scale sc = block_scale(total_keys);
+  const Scale sc = block_scale(total_keys, GRID64);
   uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i >= n) return;
   codes[i] = morton64_of(ld_node(&leaves[i]), sc);
@@ -212,7 +213,7 @@ __global__ void __launch_bounds__(BLK) k_morton64(const Bvh2Node* __restrict__ l
 __global__ void __launch_bounds__(BLK) k_morton128(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
                                                    U128* __restrict__ codes) {
   grid_dep_wait();
-  const Scale sc = block_scale(total_keys);
+  const Scale sc = block_scale(total_keys, GRID128);
   uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (i >= n) return;
   codes[i] = morton128_of(ld_node(&leaves[i]), sc);
@@ -365,12 +366,12 @@ __global__ void __launch_bounds__(BLK) k_seg_morton(const Bvh2Node* __restrict__
   const uint32_t i = blockIdx.x * BLK + threadIdx.x;
   if (threadIdx.x == 0) {
     s_first = seg_find(prim_start, n_seg, min(blockIdx.x * BLK, n - 1));
-    s_scale = make_scale(total_keys + 8 * (size_t)s_first);
+    s_scale = make_scale(total_keys + 8 * (size_t)s_first, WIDE ? GRID128 : GRID64);
   }
   __syncthreads();
   if (i >= n) return;
   const uint32_t s = seg_find(prim_start, n_seg, i);
-  const Scale sc = s == s_first ? s_scale : make_scale(total_keys + 8 * (size_t)s);
+  const Scale sc = s == s_first ? s_scale : make_scale(total_keys + 8 * (size_t)s, WIDE ? GRID128 : GRID64);
   const Bvh2Node nd = ld_node(&leaves[i]);
   if (WIDE)
     static_cast<U128*>(codes)[i] = morton128_of(nd, sc);
