@@ -465,6 +465,7 @@ struct PlocCoopArgs {
   const uint32_t* remap;  // partial rebuild: left slot of every merged pair (else null)
   int fast;               // the leaves were checked for NaN: pair_cost<true>
   uint32_t stop_at;       // the loop ends once at most this many clusters are live
+  int lookback;           // one barrier per pass: tiles chain their counts by look-back (tile_cnt as status words)
 };
 
 struct CoopGroupSmem {
@@ -658,6 +659,204 @@ __device__ __forceinline__ uint2 ploc_tile_write(CoopGroupSmem& sm, int group, c
   return make_uint2(pre_e + (tot & 0xffffu), pre_m + (tot >> 16));
 }
 
+// One-barrier passes (lists below LB_MAX clusters): a tile computes its
+// clusters' merge offsets (and its +-radius halo's, in shared memory), its
+// (emitted, merged) counts, and at once its output offsets by decoupled
+// look-back over the earlier tiles' status words, then writes; the mutual-
+// pair test reads the halo's offsets from shared memory, so no tile needs
+// another's offsets and the pass needs no barrier between counting and
+// writing.  A status word is state (2 bits: 1 the tile's own counts, 2 the
+// counts through it) | pass stamp (14 bits) | emitted (24) | merged (24); a
+// word with another pass's stamp is not yet written in this pass.  The words
+// are cleared once per build; tiles of a group go in increasing order and all
+// groups are resident, so the earliest unfinished tile can always finish.
+constexpr uint32_t LB_MAX = 1u << 24;
+constexpr unsigned long long LB_AGG = 1ull << 62, LB_INC = 2ull << 62;
+
+__device__ __forceinline__ unsigned long long lb_word(unsigned long long state, uint32_t stamp, uint32_t e, uint32_t m) {
+  return state | (unsigned long long)(stamp & 0x3fffu) << 48 | (unsigned long long)(e & 0xffffffu) << 24 |
+         (unsigned long long)(m & 0xffffffu);
+}
+
+template <bool FAST>
+__device__ __forceinline__ uint2 ploc_tile_fused(CoopGroupSmem& sm, int group, const Bvh2Node* cur, Bvh2Node* next,
+                                                 Bvh2Node* out, uint32_t count, uint32_t base, uint32_t chunk, int ipt,
+                                                 int r, bool d1, unsigned long long* tstat, uint32_t tile,
+                                                 uint32_t stamp, uint32_t ins_top, const uint32_t* remap,
+                                                 uint32_t* status) {
+  const int tid = threadIdx.x % PT, lane = tid & 31, warp = tid >> 5;
+  const int64_t box_lo = (int64_t)base - 2 * r;
+  const uint32_t box_span = chunk + 4 * r;
+  group_sync(group);  // the previous tile's shared data is consumed
+  for (uint32_t k = tid; k < box_span; k += PT) {
+    const int64_t j = box_lo + k;
+    if (j >= 0 && j < (int64_t)count) {
+      const Box b = load_box_cg(&cur[j]);
+      sm.box[0 * BOXS + k] = b.mn.x;
+      sm.box[1 * BOXS + k] = b.mn.y;
+      sm.box[2 * BOXS + k] = b.mn.z;
+      sm.box[3 * BOXS + k] = b.mx.x;
+      sm.box[4 * BOXS + k] = b.mx.y;
+      sm.box[5 * BOXS + k] = b.mx.z;
+    }
+  }
+  group_sync(group);
+  const int lo32 = (int)box_lo;
+#define PBOX(J)                                                                                              \
+  Box {                                                                                                      \
+    make_float3(sm.box[0 * BOXS + (J)-lo32], sm.box[1 * BOXS + (J)-lo32], sm.box[2 * BOXS + (J)-lo32]),      \
+        make_float3(sm.box[3 * BOXS + (J)-lo32], sm.box[4 * BOXS + (J)-lo32], sm.box[5 * BOXS + (J)-lo32]) \
+  }
+  const int64_t m_lo = (int64_t)base - r;
+  const uint32_t m_span = chunk + 2 * r;
+  for (uint32_t k = tid; k < m_span; k += PT) {
+    const int64_t jj = m_lo + k;
+    if (jj < 0 || jj >= (int64_t)count) continue;
+    const int i = (int)jj;
+    const Box me = PBOX(i);
+    int8_t m;
+    if (d1) {
+      if ((uint32_t)i == count - 1) {
+        m = -1;
+      } else {
+        const float c = pair_cost<FAST>(me, PBOX(i + 1));
+        const float last = i == 0 ? __int_as_float(0x7f800000) : pair_cost<FAST>(PBOX(i - 1), me);
+        m = last < c ? -1 : 1;
+      }
+    } else {
+      const int begin = i >= r ? i - r : 0;
+      const int end = min(i + r + 1, (int)count);
+      int best = i;
+      float best_cost = __int_as_float(0x7f800000);
+      for (int j = begin; j < i; j++) {
+        const float c = pair_cost<FAST>(PBOX(j), me);
+        if (c <= best_cost) {
+          best = j;
+          best_cost = c;
+        }
+      }
+      for (int j = i + 1; j < end; j++) {
+        const float c = pair_cost<FAST>(me, PBOX(j));
+        if (c <= best_cost) {
+          best = j;
+          best_cost = c;
+        }
+      }
+      m = (int8_t)(best - i);
+    }
+    sm.merge[k] = m;
+  }
+#undef PBOX
+  group_sync(group);
+  // flags from the offsets in shared memory, group-wide exclusive scan
+  bool emit[PITEMS], ism[PITEMS];
+  uint32_t bst[PITEMS];
+  uint32_t packed = 0;
+#pragma unroll
+  for (int k = 0; k < PITEMS; k++) {
+    const uint32_t i = base + tid * ipt + k;
+    emit[k] = ism[k] = false;
+    bst[k] = i;
+    if (k < ipt && i < count) {
+      const int off = sm.merge[(int64_t)i - m_lo];
+      const uint32_t b = (uint32_t)((int)i + off);
+      const bool mutual = (int)b + (int)sm.merge[(int64_t)b - m_lo] == (int)i;
+      emit[k] = !mutual || b < i;
+      ism[k] = mutual && b < i;
+      bst[k] = b;
+    }
+    packed += (emit[k] ? 1u : 0u) + (ism[k] ? (1u << 16) : 0u);
+  }
+  uint32_t x = packed;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sm.w[warp] = x;
+  group_sync(group);
+  uint32_t wpre = 0, tot = 0;
+  for (int w = 0; w < PT / 32; w++) {
+    if (w < warp) wpre += sm.w[w];
+    tot += sm.w[w];
+  }
+  if (warp == 0) {
+    // publish this tile's counts, then add up the earlier tiles': the warp
+    // reads 32 earlier status words at a time and takes the run up to the
+    // nearest tile whose word holds the counts through it (bounded waits)
+    const uint32_t te = tot & 0xffffu, tm = tot >> 16;
+    uint32_t pe = 0, pm = 0;
+    if (tile == 0) {
+      if (lane == 0) atomicExch(&tstat[0], lb_word(LB_INC, stamp, te, tm));
+    } else {
+      if (lane == 0) atomicExch(&tstat[tile], lb_word(LB_AGG, stamp, te, tm));
+      int64_t t = (int64_t)tile - 1;
+      uint32_t spins = 0;
+      while (t >= 0) {
+        const int64_t tt = t - lane;
+        bool valid = true, inc = true;
+        uint32_t ve = 0, vm = 0;
+        if (tt >= 0) {
+          const unsigned long long v = *(volatile unsigned long long*)&tstat[tt];
+          const unsigned long long state = v & (3ull << 62);
+          valid = state != 0 && (uint32_t)((v >> 48) & 0x3fffu) == (stamp & 0x3fffu);
+          inc = valid && state == LB_INC;
+          ve = (uint32_t)((v >> 24) & 0xffffffu);
+          vm = (uint32_t)(v & 0xffffffu);
+        }
+        const uint32_t bv = __ballot_sync(0xffffffffu, valid), bi = __ballot_sync(0xffffffffu, inc);
+        const int first_inc = bi ? __ffs(bi) - 1 : 32;
+        const uint32_t need = first_inc < 31 ? (2u << first_inc) - 1u : 0xffffffffu;
+        if ((bv & need) != need) {
+          if (++spins > (1u << 22)) {
+            if (lane == 0) set_status(status, ST_ITER_LIMIT);
+            break;
+          }
+          continue;
+        }
+        uint32_t se = lane <= first_inc ? ve : 0u, sm_ = lane <= first_inc ? vm : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          se += __shfl_xor_sync(0xffffffffu, se, o);
+          sm_ += __shfl_xor_sync(0xffffffffu, sm_, o);
+        }
+        pe += se;
+        pm += sm_;
+        if (first_inc < 32) break;
+        t -= 32;
+      }
+      if (lane == 0) atomicExch(&tstat[tile], lb_word(LB_INC, stamp, pe + te, pm + tm));
+    }
+    if (lane == 0) {
+      sm.red[0][0] = pe;
+      sm.red[1][0] = pm;
+    }
+  }
+  group_sync(group);
+  const uint32_t pre_e = sm.red[0][0], pre_m = sm.red[1][0];
+  const uint32_t excl = wpre + x - packed;
+  uint32_t epos = pre_e + (excl & 0xffffu), mpos = pre_m + (excl >> 16);
+#pragma unroll
+  for (int k = 0; k < PITEMS; k++) {
+    const uint32_t i = base + tid * ipt + k;
+    if (!emit[k]) continue;
+    if (ism[k]) {
+      const Bvh2Node left = ld_node_cg(&cur[i]);
+      const Bvh2Node right = ld_node_cg(&cur[bst[k]]);
+      uint32_t ins = ins_top - 2 * (mpos + 1);
+      if (remap) ins = __ldg(&remap[(ins - 1) >> 1]);  // the k-th free pair of a partial rebuild
+      st_node(&out[ins], left);
+      st_node(&out[ins + 1], right);
+      st_node(&next[epos], make_node(box_union(node_box(left), node_box(right)), 0, ins));
+      mpos++;
+    } else {
+      st_node(&next[epos], ld_node_cg(&cur[i]));
+    }
+    epos++;
+  }
+  return make_uint2(pre_e + (tot & 0xffffu), pre_m + (tot >> 16));
+}
+
 __device__ __forceinline__ int tile_ipt(uint32_t live, uint32_t groups) {
   return live >= groups * (uint32_t)PCHUNK ? PITEMS : live >= groups * (uint32_t)(PT * 2) ? 2 : 1;
 }
@@ -690,6 +889,27 @@ __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs 
     const int ipt = tile_ipt(count, G * COOP_GROUPS);
     const uint32_t chunk = (uint32_t)PT * ipt;
     const uint32_t ntiles = div_up<uint32_t>(count, chunk);
+
+    if (a.lookback) {
+      // one pass, one barrier: counts chained by look-back
+      const uint32_t ins_top = *(volatile uint32_t*)&a.st->insert[parity];
+      unsigned long long* tstat = reinterpret_cast<unsigned long long*>(a.tile_cnt);
+      for (uint32_t tile = first_tile; tile < ntiles; tile += tile_step) {
+        const uint2 tot = a.fast ? ploc_tile_fused<true>(sm, group, cur, next, a.out, count, tile * chunk, chunk, ipt, r,
+                                                         d1, tstat, tile, pass, ins_top, a.remap, a.status)
+                                 : ploc_tile_fused<false>(sm, group, cur, next, a.out, count, tile * chunk, chunk, ipt,
+                                                          r, d1, tstat, tile, pass, ins_top, a.remap, a.status);
+        if (tid == 0 && tile == ntiles - 1) {
+          a.st->count[parity ^ 1] = tot.x;
+          a.st->insert[parity ^ 1] = ins_top - 2 * tot.y;
+          a.st->sum_counts += count;
+          __threadfence();
+          a.st->passes = pass + 1;
+        }
+      }
+      if (single) __syncthreads(); else grid.sync();
+      continue;
+    }
 
     // A: merge offsets and tile counts
     for (uint32_t tile = first_tile; tile < ntiles; tile += tile_step)
@@ -1605,8 +1825,10 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
       coop_blocks = std::max(1, per_sm) * c.num_sms;
       coop_blocks_s.store(coop_blocks);
     }
+    const int lookback = n < LB_MAX ? 1 : 0;
+    if (lookback) CK(cudaMemsetAsync(tile_cnt, 0, (size_t)div_up<uint32_t>(n, PT) * sizeof(uint2), c.stream));
     PlocCoopArgs pa{{cur, nxt}, out_nodes, st, merge, tile_cnt, (int)radius, depth_threshold, max_passes, c.d_status,
-                    remap, nan_checked ? 1 : 0, stop_at};
+                    remap, nan_checked ? 1 : 0, stop_at, lookback};
     void* args[] = {&pa};
     if (gpu_shared(c) && n <= SHARED_SINGLE_BLOCK_MAX) {
       // the GPU is shared with other builds or work: one block, a normal
