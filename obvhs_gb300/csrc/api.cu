@@ -559,6 +559,10 @@ int obvhs_ctx_destroy(obvhs_ctx* c) {
     cudaEventDestroy(c->coop_ev[0]);
     if (c->coop_ev[1]) cudaEventDestroy(c->coop_ev[1]);
   }
+  if (c->pipe_in) cudaStreamDestroy(c->pipe_in);
+  if (c->pipe_out) cudaStreamDestroy(c->pipe_out);
+  for (cudaEvent_t e : c->pipe_ev)
+    if (e) cudaEventDestroy(e);
   c->scratch.release();
   if (c->d_status) cudaFree(c->d_status);
   if (c->h_status) cudaFreeHost(c->h_status);
@@ -979,6 +983,29 @@ int obvhs_ray_traverse_multi(obvhs_ctx* cp, const obvhs_cwbvh* const* bvhs, uint
   return OBVHS_OK;
 }
 
+// Calls with at least this many rays (and two batches) pipeline their copies
+// with the traversal.
+constexpr uint32_t PIPE_MIN_RAYS = 1u << 21;
+
+// The context's copy streams and events, made on first use; false if they
+// cannot be made (the call then runs unpipelined).
+static bool pipe_streams(BuildCtx& c) {
+  if (c.pipe_in && c.pipe_out) return true;
+  bool ok = cudaStreamCreateWithFlags(&c.pipe_in, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&c.pipe_out, cudaStreamNonBlocking) == cudaSuccess;
+  for (cudaEvent_t& e : c.pipe_ev)
+    ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    if (c.pipe_in) cudaStreamDestroy(c.pipe_in);
+    if (c.pipe_out) cudaStreamDestroy(c.pipe_out);
+    for (cudaEvent_t& e : c.pipe_ev)
+      if (e) cudaEventDestroy(e), e = nullptr;
+    c.pipe_in = c.pipe_out = nullptr;
+  }
+  return ok;
+}
+
 int obvhs_ray_traverse_batches(obvhs_ctx* cp, const obvhs_cwbvh* const* bvhs, uint32_t n_bvh, uint32_t n_batches,
                                const uint32_t* batch_bvh, const obvhs_ray* const* rays, const uint32_t* counts,
                                obvhs_hit* const* hits) {
@@ -1017,22 +1044,59 @@ int obvhs_ray_traverse_batches(obvhs_ctx* cp, const obvhs_cwbvh* const* bvhs, ui
   for (uint32_t b = 0; b < n_batches; b++) {
     tab[b] = at;
     tab[n_batches + 1 + b] = batch_bvh[b];
-    if (counts[b])
-      CK(cudaMemcpyAsync(d_rays + (size_t)at * 32, rays[b], (size_t)counts[b] * 32, cudaMemcpyHostToDevice, c.stream));
     at += counts[b];
   }
   tab[n_batches] = at;
+  const bool pipelined = n >= PIPE_MIN_RAYS && n_batches >= 2 && pipe_streams(c);
+  if (!pipelined) {
+    for (uint32_t b = 0; b < n_batches; b++)
+      if (counts[b])
+        CK(cudaMemcpyAsync(d_rays + (size_t)tab[b] * 32, rays[b], (size_t)counts[b] * 32, cudaMemcpyHostToDevice,
+                           c.stream));
+  }
   CK(cudaMemcpyAsync(d_tab, tab, tab_bytes, cudaMemcpyHostToDevice, c.stream));
   int r = batch_owner_device(c, d_tab, d_tab + n_batches + 1, n_batches, n, d_owner);
   if (r) return r;
-  r = traverse_multi_device(c, bvhs, n_bvh, d_owner, (const float*)d_rays, n, (uint32_t*)d_hits, nullptr, 0);
-  if (r) return r;
-  at = 0;
-  for (uint32_t b = 0; b < n_batches; b++) {
-    if (counts[b])
-      CK(cudaMemcpyAsync(hits[b], d_hits + (size_t)at * 8, (size_t)counts[b] * 8, cudaMemcpyDeviceToHost, c.stream));
-    at += counts[b];
+  if (!pipelined) {
+    r = traverse_multi_device(c, bvhs, n_bvh, d_owner, (const float*)d_rays, n, (uint32_t*)d_hits, nullptr, 0);
+    if (r) return r;
+    for (uint32_t b = 0; b < n_batches; b++)
+      if (counts[b])
+        CK(cudaMemcpyAsync(hits[b], d_hits + (size_t)tab[b] * 8, (size_t)counts[b] * 8, cudaMemcpyDeviceToHost,
+                           c.stream));
+    return take_status(c);
   }
+  // Pipelined: the batches in up to PIPE_CHUNKS runs of about equal rays; a
+  // run's rays go up on the copy-in stream while the previous run is traced,
+  // and its hits come down on the copy-out stream while the next is traced.
+  // The call ends when everything is down (the context's stream waits for the
+  // copy-out stream), as the plain form does.
+  uint32_t b = 0;
+  for (int k = 0; k < BuildCtx::PIPE_CHUNKS && b < n_batches; k++) {
+    const uint32_t b0 = b, at0 = tab[b0];
+    const uint64_t target = (uint64_t)n * (uint64_t)(k + 1) / BuildCtx::PIPE_CHUNKS;
+    while (b < n_batches && (b == b0 || (uint64_t)tab[b] < target || k == BuildCtx::PIPE_CHUNKS - 1)) b++;
+    const uint32_t n_run = tab[b] - at0;
+    for (uint32_t bb = b0; bb < b; bb++)
+      if (counts[bb])
+        CK(cudaMemcpyAsync(d_rays + (size_t)tab[bb] * 32, rays[bb], (size_t)counts[bb] * 32, cudaMemcpyHostToDevice,
+                           c.pipe_in));
+    CK(cudaEventRecord(c.pipe_ev[2 * k], c.pipe_in));
+    CK(cudaStreamWaitEvent(c.stream, c.pipe_ev[2 * k], 0));
+    if (n_run) {
+      r = traverse_multi_device(c, bvhs, n_bvh, d_owner + at0, (const float*)(d_rays + (size_t)at0 * 32), n_run,
+                                (uint32_t*)(d_hits + (size_t)at0 * 8), nullptr, 0);
+      if (r) return r;
+    }
+    CK(cudaEventRecord(c.pipe_ev[2 * k + 1], c.stream));
+    CK(cudaStreamWaitEvent(c.pipe_out, c.pipe_ev[2 * k + 1], 0));
+    for (uint32_t bb = b0; bb < b; bb++)
+      if (counts[bb])
+        CK(cudaMemcpyAsync(hits[bb], d_hits + (size_t)tab[bb] * 8, (size_t)counts[bb] * 8, cudaMemcpyDeviceToHost,
+                           c.pipe_out));
+  }
+  CK(cudaEventRecord(c.pipe_ev[2 * BuildCtx::PIPE_CHUNKS], c.pipe_out));
+  CK(cudaStreamWaitEvent(c.stream, c.pipe_ev[2 * BuildCtx::PIPE_CHUNKS], 0));
   return take_status(c);
 }
 

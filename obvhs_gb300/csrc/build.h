@@ -176,6 +176,11 @@ struct obvhs_ctx {
   }
 
   cudaEvent_t coop_ev[2] = {nullptr, nullptr};  // cooperative launches through the device's shared stream
+  // pipelined ray-batch calls (obvhs_ray_traverse_batches): copy-in and
+  // copy-out streams and the events that chain the chunks; made on first use
+  static constexpr int PIPE_CHUNKS = 4;
+  cudaStream_t pipe_in = nullptr, pipe_out = nullptr;
+  cudaEvent_t pipe_ev[2 * PIPE_CHUNKS + 1] = {};
   bool shared_gpu = false;                       // obvhs_ctx_set_shared_gpu
 
   int fail(int code, const std::string& msg) {

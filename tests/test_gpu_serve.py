@@ -92,3 +92,34 @@ def test_traverse_batches_equals_alone(G, pools):
         assert np.array_equal(o[:, 1], t.view(np.uint32))
     for b in bvhs:
         b.free()
+
+
+def test_large_traverse_batches_pipelined_equal_alone(G):
+    """A call of more than 2M rays (copies pipelined with the traversal in
+    runs of batches on separate streams) gives each batch the hits of its BVH
+    traversed alone, from pinned and from pageable host memory."""
+    import torch
+    from obvhs_gb300 import scenes as S
+    from obvhs_gb300 import test_util as T
+
+    p = BvhBuildParams.fast_build()
+    bvhs = [G.build_cwbvh_from_tris(S.scene2_tris(n, offset=k), p) for k, n in enumerate((40_000, 120_000))]
+    rng = np.random.default_rng(21)
+    batch_bvh, batches = [], []
+    for j, n in enumerate((900_000, 3, 0, 700_000, 650_000, 1, 400_000)):
+        o = rng.uniform(-12, 12, size=(n, 3)).astype(np.float32)
+        d = T.uniform_sample_sphere(rng.random(n).astype(np.float32), rng.random(n).astype(np.float32))
+        r = T.make_rays(o, d, 0.0, np.inf)
+        if j % 2:
+            pinned = torch.empty((n, 8), dtype=torch.float32).pin_memory().numpy()
+            pinned[:] = r
+            r = pinned
+        batch_bvh.append(j % 2)
+        batches.append(r)
+    outs = G.ray_traverse_batches(bvhs, batch_bvh, batches)
+    for k, r, o in zip(batch_bvh, batches, outs):
+        ids, t = bvhs[k].ray_traverse(r)
+        assert np.array_equal(o[:, 0], ids)
+        assert np.array_equal(o[:, 1], t.view(np.uint32))
+    for b in bvhs:
+        b.free()
