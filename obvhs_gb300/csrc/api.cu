@@ -183,7 +183,9 @@ int build_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t 
   obvhs_cwbvh* cw = new obvhs_cwbvh();
   cw->ctx = &c;
   cw->uses_spatial_splits = split;
-  r = cwbvh_convert_device(c, &b2, mp, 1, cw, &rb->emitted);
+  // with no reinsertion the tree is PLOC's own: its pass ranges order the cost pass
+  const bool plain_ploc = !(p->reinsertion_batch_ratio > 0.0f) && passes > 0;
+  r = cwbvh_convert_device(c, &b2, mp, 1, cw, &rb->emitted, false, plain_ploc ? passes : 0u);
   if (r) {
     obvhs_cwbvh_free(cw);
     return r;

@@ -67,6 +67,7 @@ enum ScratchSlot {
   SLOT_MORTON_TOP,  // the Morton sort's high-digit keys (+ a flag word)
   SLOT_CAND_HIST,   // the reinsertion candidate sorts' digit histograms (two areas)
   SLOT_CW_SMALL,    // CWBVH conversion: primitive lists of nodes with at most 3 primitives
+  SLOT_PLOC_PASSES, // PLOC: the insert index at the start of every pass (PLOC_PASS_REC)
   SLOT_COUNT
 };
 
@@ -110,6 +111,10 @@ struct Scratch {
   }
 };
 
+// PLOC passes whose tree ranges are recorded: pass p writes its merged pairs
+// to [pass_ins[p + 1], pass_ins[p]) of the node array.
+constexpr uint32_t PLOC_PASS_REC = 4096;
+
 struct PlocState {
   uint32_t count[2];
   uint32_t insert[2];
@@ -142,6 +147,9 @@ struct obvhs_ctx {
   // traversal launch form (block size, stack placement); 0 = the default
   // (obvhs_ctx_set_traversal_config)
   int trav_form = 0;
+  // the pass ranges of the last PLOC build on this context (PLOC_PASS_REC
+  // insert indices), or null
+  uint32_t* ploc_pass_ins = nullptr;
   // device address of the device's builds-in-flight word (mapped host
   // memory), read by persistent traversals to leave room for builds; or null
   const uint32_t* d_yield = nullptr;
@@ -366,8 +374,10 @@ int reinsertion_seg_device(BuildCtx& c, Bvh2Node* nodes, const SegLayout& L, con
 // With `emitted_deferred` (pinned) the number of emitted nodes is copied there
 // asynchronously; the caller compares it with out->n_nodes after its final
 // synchronisation and checks the status word.
+// ploc_passes > 0: the tree is exactly as this context's last PLOC build
+// left it after that many passes (its pass ranges are valid).
 int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, int order_children, obvhs_cwbvh* out,
-                         uint32_t* emitted_deferred = nullptr, bool exact_aabbs = false);
+                         uint32_t* emitted_deferred = nullptr, bool exact_aabbs = false, uint32_t ploc_passes = 0);
 // CwBvh::order_children (node < 0) or order_node_children(node) on the
 // device; prims6: the primitives' boxes (n_prims x 6 floats, device), in
 // original order or, with direct_layout, in primitive_indices order.

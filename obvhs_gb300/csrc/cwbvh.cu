@@ -33,7 +33,11 @@
 #include <atomic>
 #include <mutex>
 
+#include <cooperative_groups.h>
+
 #include "build.h"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -318,15 +322,18 @@ __device__ __forceinline__ bool child_rec(const Bvh2Node& cn, uint32_t k, const 
     list = make_uint4(__ldg(&pidx_in[node_first(cn)]), 0u, 0u, 1u);
     return true;
   }
-  if (!wait_ready(&flags[k], status)) return false;
+  if (flags && !wait_ready(&flags[k], status)) return false;
   r = ld_rec_cg(&crec[k]);
   list = r.nprim <= 3 ? __ldcg(&small[k]) : make_uint4(0u, 0u, 0u, r.nprim);
   return true;
 }
 
+// Nodes [0, n) from n - 1 down; children at or above n (total nodes: n_all)
+// are complete already (no flag to wait for).
 __device__ void costs_ordered(const Bvh2Node* __restrict__ nodes, const uint32_t* __restrict__ parents,
                               const uint32_t* __restrict__ pidx_in, uint32_t n, uint32_t max_prims, CostRec* crec,
-                              EmitRec* erec, uint4* small, uint32_t* flags, uint32_t* next, uint32_t* status) {
+                              EmitRec* erec, uint4* small, uint32_t* flags, uint32_t* next, uint32_t* status,
+                              uint32_t n_all) {
   const int lane = threadIdx.x & 31;
   for (;;) {
     uint32_t base = 0;
@@ -347,15 +354,15 @@ __device__ void costs_ordered(const Bvh2Node* __restrict__ nodes, const uint32_t
       continue;
     }
     const uint32_t f = node_first(nd);
-    if (f + 1 >= n || f < i) {  // an inert pad (children out of range): nothing to compute
+    if (f + 1 >= n_all || f < i) {  // an inert pad (children out of range): nothing to compute
       atomicExch(&flags[i], 1u);
       continue;
     }
     const Bvh2Node cl = ld_node(&nodes[f]), cr = ld_node(&nodes[f + 1]);
     CostRec L, R;
     uint4 ll, rl;
-    const bool ok = child_rec(cl, f, pidx_in, crec, small, flags, status, L, ll) &&
-                    child_rec(cr, f + 1, pidx_in, crec, small, flags, status, R, rl);
+    const bool ok = child_rec(cl, f, pidx_in, crec, small, f < n ? flags : nullptr, status, L, ll) &&
+                    child_rec(cr, f + 1, pidx_in, crec, small, f + 1 < n ? flags : nullptr, status, R, rl);
     if (ok) {
       uint32_t aggn0;
       const CostRec out = inner_rec(L, R, half_area(node_box(nd)), max_prims, &aggn0);
@@ -367,6 +374,76 @@ __device__ void costs_ordered(const Bvh2Node* __restrict__ nodes, const uint32_t
     __threadfence();
     atomicExch(&flags[i], 1u);
   }
+}
+
+// Range form, for a tree straight from PLOC whose pass ranges are known: pass
+// p wrote its merged pairs to [pass_ins[p + 1], pass_ins[p]) of the node
+// array, and every node's children were written by an earlier pass, so the
+// large ranges are costed in pass order with a grid barrier after each (no
+// ready flags, fences or waits) and the small ranges at the top of the tree
+// in the ordered form.  Same records as the climb.
+struct CostRangeArgs {
+  const Bvh2Node* nodes;
+  const uint32_t* parents;
+  const uint32_t* pidx_in;
+  const uint32_t* pass_ins;
+  uint32_t n, max_prims, passes;
+  CostRec* crec;
+  EmitRec* erec;
+  uint4* small;
+  uint32_t* status;
+};
+
+constexpr uint32_t COST_RANGE_MIN = 65536;  // ranges this large go grid-wide with a barrier after each
+
+__device__ void cost_node_ready(const CostRangeArgs& a, uint32_t i) {
+  const Bvh2Node nd = ld_node(&a.nodes[i]);
+  if (node_prims(nd) != 0) {
+    if (node_prims(nd) != 1) {  // src/cwbvh/bvh2_to_cwbvh.rs:243-247
+      set_status(a.status, ST_BAD_INPUT);
+      return;
+    }
+    __stcg(&a.small[i], make_uint4(__ldg(&a.pidx_in[node_first(nd)]), 0u, 0u, 1u));
+    if (a.parents[i] == i) __stcg(&a.erec[i], make_uint4(0u, 0u, 1u, 0u));  // a leaf root: one CWBVH node
+    return;
+  }
+  const uint32_t f = node_first(nd);
+  if (f + 1 >= a.n || f <= i) {
+    set_status(a.status, ST_BAD_TREE);
+    return;
+  }
+  const Bvh2Node cl = ld_node(&a.nodes[f]), cr = ld_node(&a.nodes[f + 1]);
+  const bool ll_leaf = node_prims(cl) != 0, rl_leaf = node_prims(cr) != 0;
+  const CostRec L = ll_leaf ? leaf_rec(cl) : ld_rec_cg(&a.crec[f]);
+  const CostRec R = rl_leaf ? leaf_rec(cr) : ld_rec_cg(&a.crec[f + 1]);
+  uint32_t aggn0;
+  const CostRec out = inner_rec(L, R, half_area(node_box(nd)), a.max_prims, &aggn0);
+  if (out.nprim <= 3) {
+    const uint4 ll = ll_leaf ? make_uint4(__ldg(&a.pidx_in[node_first(cl)]), 0u, 0u, 1u) : __ldcg(&a.small[f]);
+    const uint4 rl = rl_leaf ? make_uint4(__ldg(&a.pidx_in[node_first(cr)]), 0u, 0u, 1u) : __ldcg(&a.small[f + 1]);
+    __stcg(&a.small[i], concat_lists(ll, rl));
+  }
+  st_rec(&a.crec[i], out);
+  __stcg(&a.erec[i], make_uint4(out.meta, aggn0, out.nprim, 0u));
+}
+
+// The large ranges go grid-wide with a barrier after each; the rest of the
+// tree, nodes [0, top), in the ordered form (nodes from `top` down, ready
+// flags), where a child at or above `top` is complete since the barrier.
+__global__ void __launch_bounds__(BLK) k_costs_ranges(CostRangeArgs a, uint32_t* flags, uint32_t* next) {
+  grid_dep_wait();
+  cg::grid_group grid = cg::this_grid();
+  const uint32_t nthreads = gridDim.x * BLK, me = blockIdx.x * BLK + threadIdx.x;
+  uint32_t top = a.n;
+  for (uint32_t p = 0; p < a.passes; p++) {
+    const uint32_t hi = a.pass_ins[p], lo = a.pass_ins[p + 1];
+    if (hi - lo < COST_RANGE_MIN) break;
+    for (uint32_t i = lo + me; i < hi; i += nthreads) cost_node_ready(a, i);
+    top = lo;
+    grid.sync();
+  }
+  costs_ordered(a.nodes, a.parents, a.pidx_in, top, a.max_prims, a.crec, a.erec, a.small, flags, next, a.status,
+                a.n);
 }
 
 // Lanes of a k_costs warp take new nodes once this many of them are idle.
@@ -384,7 +461,7 @@ __global__ void __launch_bounds__(BLK) k_costs(const Bvh2Node* __restrict__ node
                                                uint32_t* next, const uint32_t* unordered, uint32_t* status) {
   grid_dep_wait();
   if (*unordered == 0) {
-    costs_ordered(nodes, parents, pidx_in, n, max_prims, crec, erec, small, flags, next, status);
+    costs_ordered(nodes, parents, pidx_in, n, max_prims, crec, erec, small, flags, next, status, n);
     return;
   }
   const uint32_t FULL = 0xffffffffu;
@@ -1208,6 +1285,20 @@ static uint32_t cost_grid(BuildCtx& c, uint32_t n) {
   return (uint32_t)std::min<uint64_t>((uint64_t)per_sm * c.num_sms, std::max<uint32_t>(1, div_up<uint32_t>(n, BLK)));
 }
 
+// Blocks of the cooperative range-ordered cost pass: every resident slot.
+static uint32_t cost_range_grid(BuildCtx& c) {
+  static std::atomic<int> per_sm_s{0};
+  int per_sm = per_sm_s.load();
+  if (!per_sm) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_costs_ranges, BLK, 0) != cudaSuccess || per_sm < 1) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
+    per_sm_s.store(per_sm);
+  }
+  return (uint32_t)per_sm * (uint32_t)c.num_sms;
+}
+
 // For each float exponent field e (1..254) the smallest mantissa m >= 1 with
 // ceil(log2f(2^(e-127) * (1 + m/2^23))) = e - 126, by binary search on the
 // host's log2f (monotone); 2^23 when no mantissa reaches it.
@@ -1235,7 +1326,7 @@ static const uint32_t* ceil_log2_thresholds() {
 }
 
 int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, int order_children, obvhs_cwbvh* out,
-                         uint32_t* emitted_deferred, bool exact_aabbs) {
+                         uint32_t* emitted_deferred, bool exact_aabbs, uint32_t ploc_passes) {
   out->n_nodes = 0;
   out->n_prims = 0;
   const uint32_t n = b->n_nodes;
@@ -1248,11 +1339,23 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   uint4* small = (uint4*)s.get(SLOT_CW_SMALL, (size_t)n * sizeof(uint4));
   uint32_t* counters = (uint32_t*)s.get(SLOT_CW_COUNTERS, 64);
   if (!parents || !flags || !crec || !erec || !small || !counters) return c.fail(OBVHS_ERR_OOM, "scratch");
+  // the tree came straight from this context's last PLOC build: cost it
+  // range by range (a cooperative launch), unless the GPU is shared
+  const bool ranges = ploc_passes > 0 && ploc_passes < PLOC_PASS_REC && c.ploc_pass_ins && !gpu_shared(c);
   CK(cudaMemsetAsync(flags, 0, (size_t)n * 4 + 8, c.stream));
   int r = compute_parents_device(c, b->nodes, n, parents, flags + n + 1);
   if (r) return r;
-  KLAUNCH("k_costs", launch_k(k_costs, cost_grid(c, n), BLK, 0, c.stream, b->nodes, parents, b->prim_indices, n,
-                              max_prims, crec, erec, small, flags, flags + n, flags + n + 1, c.d_status));
+  if (ranges) {
+    CostRangeArgs ra{b->nodes, parents, b->prim_indices, c.ploc_pass_ins, n, max_prims, ploc_passes, crec, erec, small,
+                     c.d_status};
+    uint32_t* fl = flags;
+    uint32_t* nx = flags + n;
+    void* args[] = {&ra, &fl, &nx};
+    KLAUNCH("k_costs", CK(coop_launch(c, (const void*)k_costs_ranges, cost_range_grid(c), BLK, args, 0)));
+  } else {
+    KLAUNCH("k_costs", launch_k(k_costs, cost_grid(c, n), BLK, 0, c.stream, b->nodes, parents, b->prim_indices, n,
+                                max_prims, crec, erec, small, flags, flags + n, flags + n + 1, c.d_status));
+  }
   CK(cudaGetLastError());
   // sizes of the whole tree: the root's aggregate (a leaf root is one node)
   EmitRec root;

@@ -466,6 +466,7 @@ struct PlocCoopArgs {
   int fast;               // the leaves were checked for NaN: pair_cost<true>
   uint32_t stop_at;       // the loop ends once at most this many clusters are live
   int lookback;           // one barrier per pass: tiles chain their counts by look-back (tile_cnt as status words)
+  uint32_t* pass_ins;     // the insert index at each pass's start (first PLOC_PASS_REC passes), or null
 };
 
 struct CoopGroupSmem {
@@ -880,6 +881,8 @@ __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs 
       if (blockIdx.x == 0 && threadIdx.x == 0) set_status(a.status, ST_ITER_LIMIT);
       break;
     }
+    if (a.pass_ins && pass < PLOC_PASS_REC && blockIdx.x == 0 && threadIdx.x == 0)
+      a.pass_ins[pass] = *(volatile uint32_t*)&a.st->insert[parity];
     // no __restrict__ / read-only path: each buffer is written in one pass and
     // read in the next; loads go through L2 (ld.cg) so no stale line is used
     const Bvh2Node* cur = parity ? a.buf[1] : a.buf[0];
@@ -1194,7 +1197,8 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
                                                             const Bvh2Node* __restrict__ buf1, PlocState* st,
                                                             int radius, uint32_t depth_threshold, uint32_t max_passes,
                                                             Bvh2Node* __restrict__ out, uint32_t* status,
-                                                            const uint32_t* __restrict__ remap, int fast) {
+                                                            const uint32_t* __restrict__ remap, int fast,
+                                                            uint32_t* pass_ins) {
   grid_dep_wait();
   extern __shared__ float4 smem[];
   float* sa = reinterpret_cast<float*>(smem);  // TAIL_MAX clusters (8 word arrays)
@@ -1228,6 +1232,7 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
       if (tid == 0) set_status(status, ST_ITER_LIMIT);
       break;
     }
+    if (pass_ins && tid == 0 && pass < PLOC_PASS_REC) pass_ins[pass] = insert;
     const bool d1 = radius == 1 || pass < depth_threshold;
     const int r = d1 ? 1 : radius;
     // search
@@ -1314,6 +1319,7 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
     __syncthreads();
   }
   if (tid == 0) {
+    if (pass_ins && pass < PLOC_PASS_REC) pass_ins[pass] = insert;
     float4* o = reinterpret_cast<float4*>(&out[0]);
     snode_get(cur, 0, o[0], o[1]);
     st->count[parity] = count;
@@ -1358,6 +1364,7 @@ struct ClusterArgs {
   uint32_t* status;
   const uint32_t* remap;
   int fast;
+  uint32_t* pass_ins;  // the insert index at each pass's start (first PLOC_PASS_REC passes), or null
 };
 
 // The window: eight word arrays of CL_STRIDE (as the tail's), the slice at
@@ -1469,6 +1476,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_ploc_cluster(ClusterArgs a) {
       if (me == 0 && tid == 0) set_status(a.status, ST_ITER_LIMIT);
       break;
     }
+    if (a.pass_ins && me == 0 && tid == 0 && pass < PLOC_PASS_REC) a.pass_ins[pass] = insert;
     const bool d1 = a.radius == 1 || pass < a.depth_threshold;
     const int r = d1 ? 1 : a.radius;
     uint32_t act, sl;
@@ -1626,6 +1634,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_ploc_cluster(ClusterArgs a) {
     cluster.sync();  // the next pass's slices are complete
   }
   if (me == 0 && tid == 0) {
+    if (a.pass_ins && pass < PLOC_PASS_REC) a.pass_ins[pass] = insert;
     float4 ra, rb;
     wget(win[cur], CL_HALO, ra, rb);
     float4* o = reinterpret_cast<float4*>(&a.out[0]);
@@ -1801,6 +1810,9 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   int8_t* merge = (int8_t*)s.get(SLOT_MERGE, (size_t)n);
   uint2* tile_cnt = (uint2*)s.get(SLOT_PARTIAL, (size_t)div_up<uint32_t>(n, PT) * sizeof(uint2));
   PlocState* st = (PlocState*)s.get(SLOT_PLOC_STATE, sizeof(PlocState));
+  // the pass ranges (not for a partial rebuild, whose pairs go to free slots)
+  uint32_t* pass_ins = remap ? nullptr : (uint32_t*)s.get(SLOT_PLOC_PASSES, (size_t)PLOC_PASS_REC * 4);
+  c.ploc_pass_ins = pass_ins;
   if (!cur || !nxt || !merge || !tile_cnt || !st) return c.fail(OBVHS_ERR_OOM, "scratch");
   uint32_t g = div_up<uint32_t>(n, BLK);
   KLAUNCH("k_gather", launch_k(k_gather, g, BLK, 0, c.stream, leaves, order, n, cur));
@@ -1828,7 +1840,7 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
     const int lookback = n < LB_MAX ? 1 : 0;
     if (lookback) CK(cudaMemsetAsync(tile_cnt, 0, (size_t)div_up<uint32_t>(n, PT) * sizeof(uint2), c.stream));
     PlocCoopArgs pa{{cur, nxt}, out_nodes, st, merge, tile_cnt, (int)radius, depth_threshold, max_passes, c.d_status,
-                    remap, nan_checked ? 1 : 0, stop_at, lookback};
+                    remap, nan_checked ? 1 : 0, stop_at, lookback, pass_ins};
     void* args[] = {&pa};
     if (gpu_shared(c) && n <= SHARED_SINGLE_BLOCK_MAX) {
       // the GPU is shared with other builds or work: one block, a normal
@@ -1841,7 +1853,7 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   }
   if (cl_ctas) {
     ClusterArgs ca{cur, nxt, st, (int)radius, depth_threshold, max_passes, out_nodes, c.d_status, remap,
-                   nan_checked ? 1 : 0};
+                   nan_checked ? 1 : 0, pass_ins};
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)cl_ctas);
     cfg.blockDim = dim3(CL_THREADS);
@@ -1861,7 +1873,7 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
     const size_t smem = (size_t)4 * TAIL_MAX * sizeof(float4) + TAIL_MAX + 64;
     KLAUNCH("k_ploc_tail", launch_k(k_ploc_tail, 1, TAIL_THREADS, smem, c.stream, cur, nxt, st, (int)radius, depth_threshold,
                                                                            max_passes, out_nodes, c.d_status, remap,
-                                    nan_checked ? 1 : 0));
+                                    nan_checked ? 1 : 0, pass_ins));
     CK(cudaGetLastError());
   }
   if (deferred) {
