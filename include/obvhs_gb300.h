@@ -379,6 +379,19 @@ OBVHS_API int obvhs_ctx_set_traversal_config(obvhs_ctx* ctx, uint32_t block, int
 #define OBVHS_DEFAULT_WAIT_LIMIT 16777216u
 OBVHS_API int obvhs_ctx_set_wait_limit(obvhs_ctx* ctx, uint32_t spins);
 
+/* ---- output memory -------------------------------------------------------- */
+/* No counterpart in the reference (its outputs are Vecs of the process heap).
+ * CWBVH nodes, primitive indices and attached triangles come from one memory
+ * pool per device.  Memory of freed BVHs stays reserved in that pool, up to
+ * `bytes` (OBVHS_DEFAULT_OUTPUT_RESERVE), for later builds on the device: a
+ * rebuild every frame then maps no new device pages, and freeing the previous
+ * BVH unmaps none.  Beyond the reserve freed memory goes back to the device at
+ * the next synchronisation.  This call sets the reserve of the context's
+ * device and returns what lies above it at once (0: everything not in use).
+ * Scratch allocations that fail return the reserve and try again. */
+#define OBVHS_DEFAULT_OUTPUT_RESERVE (4ull << 30)
+OBVHS_API int obvhs_ctx_set_output_reserve(obvhs_ctx* ctx, uint64_t bytes);
+
 /* ---- stage-level access for parity checks ------------------------------- */
 /* sort_nodes_by_morton (src/ploc/mod.rs:771-847) on Bvh2Node::new(aabbs[i])
  * leaves: codes in input order (u64 pairs: lo, hi; hi = 0 for U64) and the

@@ -71,6 +71,7 @@ SIGNATURES = {
     "obvhs_ctx_set_profiling": (I32, [P, I32]),
     "obvhs_ctx_set_shared_gpu": (I32, [P, I32]),
     "obvhs_ctx_set_wait_limit": (I32, [P, U32]),
+    "obvhs_ctx_set_output_reserve": (I32, [P, U64]),
     "obvhs_ctx_set_traversal_config": (I32, [P, U32, I32]),
     "obvhs_ctx_profile_report": (I32, [P, P, U64]),
     "obvhs_ploc_build": (I32, [P, P, P, U32, U32, U32, U32, I32, ctypes.POINTER(P), ctypes.POINTER(BuildStats)]),

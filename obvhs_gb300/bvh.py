@@ -128,6 +128,15 @@ class Context:
         OBVHS_ERR_LIMIT); small values exercise that failure path."""
         self.check(self.lib.obvhs_ctx_set_wait_limit(self.h, int(spins)))
 
+    #: OBVHS_DEFAULT_OUTPUT_RESERVE in include/obvhs_gb300.h
+    DEFAULT_OUTPUT_RESERVE = 4 << 30
+
+    def set_output_reserve(self, nbytes: int = DEFAULT_OUTPUT_RESERVE):
+        """Bytes of freed BVH output memory (nodes, primitive indices,
+        triangles) the device's output pool keeps mapped for later builds;
+        memory above it goes back to the device now (0: all that is free)."""
+        self.check(self.lib.obvhs_ctx_set_output_reserve(self.h, int(nbytes)))
+
     def profile_report(self) -> dict:
         """Per-kernel {launches, total_ms, max_ms} since the last report."""
         import json

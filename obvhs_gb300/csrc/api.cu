@@ -446,6 +446,11 @@ struct DeviceShared {
   // traversal kernels read (traversal_yield_word); kept for the process's life
   uint32_t* h_yield = nullptr;
   uint32_t* d_yield = nullptr;
+  // the output pool (output_alloc): made on first use; freed outputs keep up
+  // to out_reserve bytes of it mapped for later outputs
+  cudaMemPool_t out_pool = nullptr;
+  bool out_pool_failed = false;
+  uint64_t out_reserve = OBVHS_DEFAULT_OUTPUT_RESERVE;
 };
 
 DeviceShared& device_shared(int device) {
@@ -498,6 +503,64 @@ const uint32_t* traversal_yield_word(int device) {
     d.d_yield = static_cast<uint32_t*>(dp);
   }
   return d.d_yield;
+}
+
+// `device`'s output pool, made with the device current; null where the
+// device has no memory pools (outputs then come from its default pool).
+static cudaMemPool_t output_pool(int device) {
+  DeviceShared& d = device_shared(device);
+  std::lock_guard<std::mutex> lock(d.m);
+  if (!d.out_pool && !d.out_pool_failed) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    cudaMemPool_t pool = nullptr;
+    uint64_t keep = d.out_reserve;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess ||
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+      cudaGetLastError();
+      if (pool) cudaMemPoolDestroy(pool);
+      d.out_pool_failed = true;
+      return nullptr;
+    }
+    d.out_pool = pool;
+  }
+  return d.out_pool;
+}
+
+cudaError_t output_alloc(obvhs_ctx& c, void** p, size_t bytes) {
+  cudaMemPool_t pool = output_pool(c.device);
+  cudaError_t e = pool ? cudaMallocFromPoolAsync(p, bytes, pool, c.stream) : cudaMallocAsync(p, bytes, c.stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+  }
+  return e;
+}
+
+bool output_pool_trim_current() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) {
+    cudaGetLastError();
+    return false;
+  }
+  DeviceShared& d = device_shared(dev);
+  cudaMemPool_t pool = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(d.m);
+    pool = d.out_pool;
+  }
+  if (!pool) return false;
+  uint64_t reserved = 0, used = 0;
+  if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) != cudaSuccess ||
+      cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (reserved <= used) return false;
+  return cudaMemPoolTrimTo(pool, 0) == cudaSuccess;
 }
 
 cudaError_t coop_launch(obvhs_ctx& c, const void* func, unsigned grid, unsigned block, void** args, size_t smem) {
@@ -604,6 +667,24 @@ int obvhs_ctx_set_traversal_config(obvhs_ctx* c, uint32_t block, int smem_stack)
 int obvhs_ctx_set_wait_limit(obvhs_ctx* c, uint32_t spins) {
   if (!c) return OBVHS_ERR_INVALID_ARG;
   c->wait_limit = spins;
+  return OBVHS_OK;
+}
+
+int obvhs_ctx_set_output_reserve(obvhs_ctx* c, uint64_t bytes) {
+  if (!c) return OBVHS_ERR_INVALID_ARG;
+  DeviceGuard g(c->device);
+  DeviceShared& d = device_shared(c->device);
+  {
+    std::lock_guard<std::mutex> lock(d.m);
+    d.out_reserve = bytes;
+  }
+  cudaMemPool_t pool = output_pool(c->device);
+  if (!pool) return OBVHS_OK;
+  if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &bytes) != cudaSuccess ||
+      cudaMemPoolTrimTo(pool, (size_t)bytes) != cudaSuccess) {
+    cudaError_t e = cudaGetLastError();
+    return c->cuda_fail(e, "output pool");
+  }
   return OBVHS_OK;
 }
 

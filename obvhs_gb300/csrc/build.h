@@ -71,6 +71,8 @@ enum ScratchSlot {
   SLOT_COUNT
 };
 
+bool output_pool_trim_current();  // defined in api.cu, described below
+
 // Grow-only device buffers that a context keeps between calls, like the
 // reference's builders keep their Vecs (src/ploc/mod.rs:34-45).
 struct Scratch {
@@ -93,7 +95,11 @@ struct Scratch {
     void* p = nullptr;
     if (cudaMalloc(&p, want) != cudaSuccess) {
       cudaGetLastError();
-      return nullptr;
+      // memory that freed outputs keep in reserve: return it and try again
+      if (!output_pool_trim_current() || cudaMalloc(&p, want) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+      }
     }
     ptr[slot] = p;
     cap[slot] = want;
@@ -215,6 +221,12 @@ int device_concurrent_builds(int device);
 void device_build_enter(int device);
 void device_build_leave(int device);
 const uint32_t* traversal_yield_word(int device);
+// An output buffer (CWBVH nodes, primitive indices, triangles) of `bytes`,
+// stream-ordered on c.stream, from the device's output pool; cudaFree
+// returns it to that pool.
+cudaError_t output_alloc(obvhs_ctx& c, void** p, size_t bytes);
+// Returns the current device's reserved output memory; true if it held any.
+bool output_pool_trim_current();
 struct BuildScope {
   int device;
   explicit BuildScope(int d) : device(d) { device_build_enter(d); }

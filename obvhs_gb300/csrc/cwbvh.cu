@@ -430,7 +430,7 @@ __device__ void cost_node_ready(const CostRangeArgs& a, uint32_t i) {
 // The large ranges go grid-wide with a barrier after each; the rest of the
 // tree, nodes [0, top), in the ordered form (nodes from `top` down, ready
 // flags), where a child at or above `top` is complete since the barrier.
-__global__ void __launch_bounds__(BLK) k_costs_ranges(CostRangeArgs a, uint32_t* flags, uint32_t* next) {
+__global__ void __launch_bounds__(BLK, 4) k_costs_ranges(CostRangeArgs a, uint32_t* flags, uint32_t* next) {
   grid_dep_wait();
   cg::grid_group grid = cg::this_grid();
   const uint32_t nthreads = gridDim.x * BLK, me = blockIdx.x * BLK + threadIdx.x;
@@ -918,7 +918,7 @@ __device__ void oct_finish(const EmitArgs& a, OctetShared& os, int lane, bool ac
 // waiting.  A held item's parent was taken earlier by a running warp, so
 // some held item is always published eventually; waits are bounded (status
 // ST_ITER_LIMIT), and a failed node (status set) ends every wait.
-__global__ void __launch_bounds__(EMIT_TB) k_emit_all(EmitArgs a) {
+__global__ void __launch_bounds__(EMIT_TB, 7) k_emit_all(EmitArgs a) {
   grid_dep_wait();
   __shared__ EmitShared sm;
   for (int k = threadIdx.x; k < 256; k += EMIT_TB) sm.thr[k] = a.log2_thr[k];
@@ -1373,9 +1373,9 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   uint32_t* cwp = nullptr;
   float4* exn = nullptr;
   // stream-ordered allocations: no device-wide synchronisation
-  if (cudaMallocAsync(&cwn, (size_t)n_cw * sizeof(CwNode), c.stream) != cudaSuccess ||
-      cudaMallocAsync(&cwp, (size_t)std::max(n_pr, 1u) * 4, c.stream) != cudaSuccess ||
-      (exact_aabbs && cudaMallocAsync(&exn, (size_t)n_cw * 32, c.stream) != cudaSuccess)) {
+  if (output_alloc(c, (void**)&cwn, (size_t)n_cw * sizeof(CwNode)) != cudaSuccess ||
+      output_alloc(c, (void**)&cwp, (size_t)std::max(n_pr, 1u) * 4) != cudaSuccess ||
+      (exact_aabbs && output_alloc(c, (void**)&exn, (size_t)n_cw * 32) != cudaSuccess)) {
     cudaGetLastError();
     if (cwn) cudaFree(cwn);
     if (cwp) cudaFree(cwp);
@@ -1517,7 +1517,7 @@ int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in
     pr_total += n_pr[s];
   }
   char* blk = nullptr;
-  if (cudaMallocAsync((void**)&blk, std::max<size_t>(total, 256), c.stream) != cudaSuccess) {
+  if (output_alloc(c, (void**)&blk, std::max<size_t>(total, 256)) != cudaSuccess) {
     cudaGetLastError();
     return c.fail(OBVHS_ERR_OOM, "cwbvh output");
   }

@@ -1188,7 +1188,7 @@ int reorder_tris_device(BuildCtx& c, obvhs_cwbvh* b, const float* tris, uint32_t
   b->n_tris = n_tris;
   if (b->n_prims == 0) return 0;
   float4* out = nullptr;
-  if (cudaMallocAsync(&out, (size_t)b->n_prims * 64, c.stream) != cudaSuccess) {
+  if (output_alloc(c, (void**)&out, (size_t)b->n_prims * 64) != cudaSuccess) {
     cudaGetLastError();
     return c.fail(OBVHS_ERR_OOM, "triangle buffer");
   }
@@ -1240,7 +1240,7 @@ int compress_tris_device(BuildCtx& c, obvhs_cwbvh* b, const float* tris, uint32_
   }
   if (b->n_prims == 0) return 0;
   uint2* out = nullptr;
-  if (cudaMallocAsync(&out, (size_t)b->n_prims * 24, c.stream) != cudaSuccess) {
+  if (output_alloc(c, (void**)&out, (size_t)b->n_prims * 24) != cudaSuccess) {
     cudaGetLastError();
     return c.fail(OBVHS_ERR_OOM, "compressed triangle buffer");
   }
