@@ -139,6 +139,10 @@ OBVHS_API int obvhs_morton_sort_noalloc(const float* aabbs, uint32_t n, uint32_t
   // its scratch pool stays empty and is never used.
   obvhs_ctx c;
   c.device = dev;
+  if (cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return OBVHS_ERR_CUDA;
+  }
   c.stream = (cudaStream_t)stream;
   c.d_status = (uint32_t*)(base + OFF_STATUS);
   Bvh2Node* leaves = (Bvh2Node*)(base + OFF_LEAVES);

@@ -119,10 +119,43 @@ __global__ void __launch_bounds__(BLK) k_leaves_from_aabbs(const float* __restri
 // --- Morton codes (src/ploc/morton.rs, src/ploc/mod.rs:287-288,782-785) ----
 
 // Rust's saturating `as u32` / `as u64` (NaN -> 0, below 0 -> 0, above the
-// range -> the maximum): the device's round-toward-zero conversion clamps the
-// same way, in one instruction.
-__device__ __forceinline__ uint32_t sat_u32(double d) { return __double2uint_rz(d); }
-__device__ __forceinline__ unsigned long long sat_u64(double d) { return __double2ull_rz(d); }
+// range -> the maximum), which the device's round-toward-zero conversions
+// (__double2uint_rz, __double2ull_rz) also give.  GB300's double-precision
+// pipe is narrow and those conversions run on it, so both are done here on
+// the bits with integer instructions, as is the float -> double widening
+// (to_f64).  The tests compare the codes with the oracle's on centres at 0,
+// on the box edges, subnormal and huge, and on flat scenes, whose infinite
+// scales give NaN and infinite products.
+__device__ __forceinline__ uint32_t sat_u32(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const uint32_t hi = (uint32_t)(b >> 32);
+  const uint32_t e = (hi >> 20) & 0x7ffu;
+  if (e < 1023u || (hi >> 31)) return 0u;                 // below 1, or negative (a NaN with its sign bit too)
+  if (e == 0x7ffu) return (b << 12) ? 0u : 0xffffffffu;  // NaN, +inf
+  if (e >= 1023u + 32u) return 0xffffffffu;
+  const unsigned long long m = (b & 0xfffffffffffffull) | 0x10000000000000ull;
+  return (uint32_t)(m >> (52u - (e - 1023u)));
+}
+__device__ __forceinline__ unsigned long long sat_u64(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const uint32_t hi = (uint32_t)(b >> 32);
+  const uint32_t e = (hi >> 20) & 0x7ffu;
+  if (e < 1023u || (hi >> 31)) return 0ull;
+  if (e == 0x7ffu) return (b << 12) ? 0ull : ~0ull;
+  if (e >= 1023u + 64u) return ~0ull;
+  const unsigned long long m = (b & 0xfffffffffffffull) | 0x10000000000000ull;
+  const int sh = (int)(e - 1023u) - 52;
+  return sh >= 0 ? m << sh : m >> -sh;
+}
+// A normal float's exponent rebiased (127 -> 1023) and its mantissa moved up
+// 29 bits is the same double; zero, subnormals, inf and NaN use the
+// conversion instruction.
+__device__ __forceinline__ double to_f64(float x) {
+  const uint32_t u = __float_as_uint(x);
+  const uint32_t e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)x;
+  return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xfffffu)), (int)(u << 29));
+}
 __device__ __forceinline__ unsigned long long split3_u64(uint32_t a) {
   unsigned long long x = a & 0x1fffffull;
   x = (x | x << 32) & 0x1f00000000ffffull;
@@ -169,17 +202,17 @@ constexpr double GRID128 = (double)(1ull << 42);
 
 __device__ __forceinline__ unsigned long long morton64_of(const Bvh2Node& nd, const Scale& s) {
   float cx = (nd.b.x + nd.a.x) * 0.5f, cy = (nd.b.y + nd.a.y) * 0.5f, cz = (nd.b.z + nd.a.z) * 0.5f;
-  double px = __dadd_rn(__dmul_rn((double)cx, s.sx), s.ox);
-  double py = __dadd_rn(__dmul_rn((double)cy, s.sy), s.oy);
-  double pz = __dadd_rn(__dmul_rn((double)cz, s.sz), s.oz);
+  double px = __dadd_rn(__dmul_rn(to_f64(cx), s.sx), s.ox);
+  double py = __dadd_rn(__dmul_rn(to_f64(cy), s.sy), s.oy);
+  double pz = __dadd_rn(__dmul_rn(to_f64(cz), s.sz), s.oz);
   return split3_u64(sat_u32(px)) | split3_u64(sat_u32(py)) << 1 | split3_u64(sat_u32(pz)) << 2;
 }
 
 __device__ __forceinline__ U128 morton128_of(const Bvh2Node& nd, const Scale& s) {
   float cx = (nd.b.x + nd.a.x) * 0.5f, cy = (nd.b.y + nd.a.y) * 0.5f, cz = (nd.b.z + nd.a.z) * 0.5f;
-  double px = __dadd_rn(__dmul_rn((double)cx, s.sx), s.ox);
-  double py = __dadd_rn(__dmul_rn((double)cy, s.sy), s.oy);
-  double pz = __dadd_rn(__dmul_rn((double)cz, s.sz), s.oz);
+  double px = __dadd_rn(__dmul_rn(to_f64(cx), s.sx), s.ox);
+  double py = __dadd_rn(__dmul_rn(to_f64(cy), s.sy), s.oy);
+  double pz = __dadd_rn(__dmul_rn(to_f64(cz), s.sz), s.oz);
   unsigned long long xl, xh, yl, yh, zl, zh;
   split3_u128(sat_u64(px), xl, xh);
   split3_u128(sat_u64(py), yl, yh);
@@ -201,22 +234,20 @@ __device__ __forceinline__ Scale block_scale(const int* total_keys, double grid)
   return s_scale;
 }
 
+// Grid-stride over the leaves, a few SM-fulls of blocks: each block computes
+// the scale once for many leaves.
 __global__ void __launch_bounds__(BLK) k_morton64(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
                                                   unsigned long long* __restrict__ codes) {
   grid_dep_wait();
   const Scale sc = block_scale(total_keys, GRID64);
-  uint32_t i = blockIdx.x * BLK + threadIdx.x;
-  if (i >= n) return;
-  codes[i] = morton64_of(ld_node(&leaves[i]), sc);
+  for (uint32_t i = blockIdx.x * BLK + threadIdx.x; i < n; i += gridDim.x * BLK) codes[i] = morton64_of(ld_node(&leaves[i]), sc);
 }
 
 __global__ void __launch_bounds__(BLK) k_morton128(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
                                                    U128* __restrict__ codes) {
   grid_dep_wait();
   const Scale sc = block_scale(total_keys, GRID128);
-  uint32_t i = blockIdx.x * BLK + threadIdx.x;
-  if (i >= n) return;
-  codes[i] = morton128_of(ld_node(&leaves[i]), sc);
+  for (uint32_t i = blockIdx.x * BLK + threadIdx.x; i < n; i += gridDim.x * BLK) codes[i] = morton128_of(ld_node(&leaves[i]), sc);
 }
 
 // --- the Morton sort on the high digits -----------------------------------------
@@ -1711,7 +1742,7 @@ int ploc_leaves(BuildCtx& c, const float* tris, const float* aabbs, const uint32
 int ploc_morton_codes(BuildCtx& c, const Bvh2Node* leaves, uint32_t n, const int* total_keys, int precision,
                       void* codes) {
   if (!n) return 0;
-  uint32_t g = div_up<uint32_t>(n, BLK);
+  const uint32_t g = std::min<uint32_t>(div_up<uint32_t>(n, BLK), (uint32_t)std::max(c.num_sms, 1) * 8u);
   if (precision)
     KLAUNCH("k_morton128", launch_k(k_morton128, g, BLK, 0, c.stream, leaves, n, total_keys, (U128*)codes));
   else

@@ -51,6 +51,55 @@ def test_morton_and_order(G, n, precision):
     assert _eq(order, oorder)
 
 
+def _edge_scene(kind, seed=31):
+    """Boxes whose Morton inputs reach the conversions' edge cases."""
+    rng = np.random.default_rng(seed)
+    f = np.float32
+    if kind == "edges":  # centres on the scene's min and max corners, at 0 and -0
+        a = _random_aabbs(3000, seed)
+        lo, hi = a[:, :3].min(0), a[:, 3:].max(0)
+        pts = [lo, hi, np.array([lo[0], hi[1], 0], f), np.zeros(3, f), np.full(3, -0.0, f)]
+        extra = np.array([np.concatenate([p, p]) for p in pts] + [[-1, -1, -1, 1, 1, 1]], f)
+        return np.concatenate([a, extra]).astype(f)
+    if kind == "subnormal":  # centres that are subnormal floats
+        c = rng.uniform(-2e-38, 2e-38, size=(3000, 3)).astype(f)
+        c[::5] = (rng.integers(-50, 50, size=c[::5].shape) * 1e-45).astype(f)
+        c[::11] = 0.0
+        return np.concatenate([c, c], 1).astype(f)
+    if kind == "huge":  # centres near the float maximum, some of them inf
+        c = rng.uniform(1e38, 3.0e38, size=(3000, 3)).astype(f)
+        a = np.concatenate([c, c], 1)
+        a[::17, :3] = 3.3e38
+        a[::17, 3:] = 3.4e38  # centre (a + b) * 0.5 overflows to inf
+        return a.astype(f)
+    if kind == "huge-extent":  # the scene's extent overflows to inf: zero scale
+        c = rng.uniform(-3.3e38, 3.3e38, size=(3000, 3)).astype(f)
+        return np.concatenate([c, c], 1).astype(f)
+    if kind == "flat":  # one axis of zero extent: infinite scale, NaN products
+        a = _random_aabbs(3000, seed)
+        a[:, 2] = a[:, 5] = 2.5
+        return a
+    if kind == "flat-zero":
+        a = _random_aabbs(3000, seed)
+        a[:, 1] = a[:, 4] = 0.0
+        return a
+    raise ValueError(kind)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("kind", ["edges", "subnormal", "huge", "huge-extent", "flat", "flat-zero"])
+def test_morton_edge_values(G, kind, precision):
+    """Codes equal the oracle's where the float->double widening and the
+    saturating double->integer conversions meet zeros, subnormals, infinities,
+    NaN and the exact top of the grid."""
+    a = _edge_scene(kind)
+    with np.errstate(over="ignore", invalid="ignore"):
+        codes, order = G.morton_sort(a, precision)
+        ocodes, oorder = O.morton(a, precision)
+    assert _eq(codes, ocodes)
+    assert _eq(order, oorder)
+
+
 def test_morton_duplicates_keep_input_order(G):
     a = np.repeat(_random_aabbs(50, 3), 40, axis=0)  # equal keys in runs
     codes, order = G.morton_sort(a, 0)
