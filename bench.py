@@ -233,7 +233,9 @@ def kernel_byte_models(m, sum_counts, n_cw, n_prims, search_nodes=None, ratio=0.
         # 80 B node and primitive indices written, each BVH2 node and record read
         "k_emit_all": n_cw * 80 + n_prims * 4 + nodes * (32 + DEC_BYTES),
         ("k_morton128" if precision else "k_morton64"): m * (32 + (16 if precision else 8) + 4),
-        "k_gather": m * (4 + 32 + 32),
+        # leaves gathered into Morton order (U64: with the run fix-up, which
+        # also reads the sorted code)
+        ("k_gather" if precision else "k_fix_gather"): m * (4 + 32 + 32 + (0 if precision else 8)),
         "k_leaves_from_tris": m * (36 + 32),
         "k_reorder_tris": n_prims * (4 + 36 + 64),
     }

@@ -267,12 +267,100 @@ __global__ void __launch_bounds__(BLK) k_morton_top(const void* __restrict__ cod
   top[t] = precision ? static_cast<const U128*>(codes)[t].hi : static_cast<const unsigned long long*>(codes)[t] >> 24;
 }
 
-// Sets *flag when some run of equal high digits is longer than RUN_MAX.
+// Sets *flag when some run of equal high digits (key >> shift) is longer than
+// RUN_MAX.
 __global__ void __launch_bounds__(BLK) k_run_check(const unsigned long long* __restrict__ top, uint32_t n,
-                                                   uint32_t* flag) {
+                                                   uint32_t* flag, int shift) {
   grid_dep_wait();
   const uint32_t i = blockIdx.x * BLK + threadIdx.x;
-  if (i >= RUN_MAX && i < n && top[i] == top[i - RUN_MAX]) *flag = 1u;
+  if (i >= RUN_MAX && i < n && top[i] >> shift == top[i - RUN_MAX] >> shift) *flag = 1u;
+}
+
+// The U64 Morton sort of a PLOC build, in three kernels and the digit passes.
+// The sort runs on code bytes 3..7 (the high 40 bits) of the codes
+// themselves; the low 24 bits ride along in the keys and order each run of
+// equal high digits afterwards (k_fix_gather).
+constexpr int HI_FIRST = 3;
+constexpr int HI_DIGITS = 5;
+// Codes of the leaves (grid-stride, scale once per block) with the sort's
+// inputs: the 256-bin histograms of the five high bytes, which the last block
+// turns into exclusive digit bases in place, the sort's look-back words
+// cleared and the run flag reset.  On entry hist (HI_DIGITS x 256 words) and
+// *done are zero.
+__global__ void __launch_bounds__(BLK) k_morton64_sort_prep(const Bvh2Node* __restrict__ leaves, uint32_t n,
+                                                            const int* total_keys, unsigned long long* __restrict__ codes,
+                                                            uint32_t* hist, uint32_t* done, uint32_t* zero_area,
+                                                            size_t zero_words, uint32_t* flag) {
+  grid_dep_wait();
+  __shared__ uint32_t h[HI_DIGITS * 256];
+  __shared__ uint32_t s_wsum[BLK / 32];
+  __shared__ bool s_last;
+  for (int k = threadIdx.x; k < HI_DIGITS * 256; k += BLK) h[k] = 0;
+  const Scale sc = block_scale(total_keys, GRID64);  // (its barrier also covers the clearing)
+  const size_t t0 = blockIdx.x * (size_t)BLK + threadIdx.x, stride = (size_t)gridDim.x * BLK;
+  radix_zero(zero_area, zero_words, t0, stride);
+  if (t0 == 0) *flag = 0;
+  for (size_t i = t0; i < n; i += stride) {
+    const unsigned long long code = morton64_of(ld_node(&leaves[i]), sc);
+    codes[i] = code;
+#pragma unroll
+    for (int b = 0; b < HI_DIGITS; b++) atomicAdd(&h[b * 256 + ((uint32_t)(code >> (8 * (HI_FIRST + b))) & 0xffu)], 1u);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < HI_DIGITS * 256; k += BLK)
+    if (h[k]) atomicAdd(&hist[k], h[k]);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  // exclusive scan of each digit's 256 counts, one count per thread
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int b = 0; b < HI_DIGITS; b++) {
+    uint32_t* hb = hist + b * 256;
+    const uint32_t v = __ldcg(&hb[threadIdx.x]);
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_wsum[warp] = x;
+    __syncthreads();
+    uint32_t pre = 0;
+    for (int w = 0; w < warp; w++) pre += s_wsum[w];
+    hb[threadIdx.x] = pre + x - v;
+    __syncthreads();
+  }
+}
+
+// Leaves in Morton order: sorted entry i (high digits sorted, each run of
+// equal high digits at most RUN_MAX long and in input order) takes its rank
+// in its run by the low 24 bits, ties by input order (a stable sort of the
+// run), and its leaf goes straight to that place.
+__global__ void __launch_bounds__(BLK) k_fix_gather(const unsigned long long* __restrict__ scodes,
+                                                    const uint32_t* __restrict__ order, uint32_t n,
+                                                    const Bvh2Node* __restrict__ leaves, Bvh2Node* __restrict__ out) {
+  grid_dep_wait();
+  const uint32_t i = blockIdx.x * BLK + threadIdx.x;
+  if (i >= n) return;
+  const unsigned long long ci = scodes[i];
+  const unsigned long long hi = ci >> 24;
+  uint32_t s = i, e = i + 1;
+  while (s > 0 && i - s < RUN_MAX && scodes[s - 1] >> 24 == hi) s--;
+  while (e < n && e - s < RUN_MAX && scodes[e] >> 24 == hi) e++;
+  uint32_t dst = i;
+  if (e - s > 1) {
+    const uint32_t lo = (uint32_t)ci & 0xffffffu;
+    uint32_t rank = 0;
+    for (uint32_t j = s; j < e; j++) {
+      const uint32_t lj = (uint32_t)scodes[j] & 0xffffffu;
+      rank += (lj < lo || (lj == lo && j < i)) ? 1u : 0u;
+    }
+    dst = s + rank;
+  }
+  st_node(&out[dst], ld_node(&leaves[order[i]]));
 }
 
 // Each run of equal high digits (at most RUN_MAX long; its entries are in
@@ -1789,7 +1877,7 @@ int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_
     if (e) return c.cuda_fail(e, "radix sort");
     const unsigned long long* stop = alt ? (const unsigned long long*)keys_alt : top;
     uint32_t* ord = alt ? vals_alt : vals;
-    KLAUNCH("k_run_check", CK(launch_k(k_run_check, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, stop, n, flag)));
+    KLAUNCH("k_run_check", CK(launch_k(k_run_check, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, stop, n, flag, 0)));
     uint32_t* h = reinterpret_cast<uint32_t*>(static_cast<char*>(c.h_small) + RUN_FLAG_OFFSET);  // pinned
     CK(cudaMemcpyAsync(h, flag, 4, cudaMemcpyDeviceToHost, c.stream));
     CK(cudaMemcpyAsync(c.h_status, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream));
@@ -1821,6 +1909,64 @@ int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_
   return 0;
 }
 
+// The leaves of a U64 build of more than RUN_MAX leaves in Morton order
+// (`out`): codes and sort inputs in one kernel, the sort on the codes' five
+// high bytes, then each leaf straight to its place (k_fix_gather).  A run of
+// equal high digits longer than RUN_MAX (many equal centres) sorts all eight
+// bytes instead.  Results equal ploc_morton_codes + ploc_sort_codes + k_gather.
+static int ploc_sorted_leaves_u64(BuildCtx& c, const Bvh2Node* leaves, uint32_t n, const int* total_keys,
+                                  Bvh2Node* out) {
+  typedef unsigned long long U64;
+  Scratch& s = c.scratch;
+  U64* codes = (U64*)s.get(SLOT_KEYS, (size_t)n * 8);
+  U64* keys_alt = (U64*)s.get(SLOT_KEYS_ALT, (size_t)n * 8);
+  uint32_t* vals = (uint32_t*)s.get(SLOT_VALS, (size_t)n * 4);
+  uint32_t* vals_alt = (uint32_t*)s.get(SLOT_VALS_ALT, (size_t)n * 4);
+  uint32_t* rs = (uint32_t*)s.get(SLOT_ALL_HIST, radix_scratch_words(n) * 4);
+  uint32_t* flag = (uint32_t*)s.get(SLOT_MORTON_TOP, 16);
+  if (!codes || !keys_alt || !vals || !vals_alt || !rs || !flag) return c.fail(OBVHS_ERR_OOM, "scratch");
+  // The sort's scratch starts with its histogram area (HIST_AREA words, here
+  // the digit bases and the prep kernel's ticket counter, cleared first); the
+  // look-back words after it are cleared by the prep kernel.
+  constexpr size_t HIST_AREA = 16 * 256;
+  uint32_t* done = rs + HI_DIGITS * 256;
+  CK(cudaMemsetAsync(rs, 0, (HI_DIGITS * 256 + 4) * 4, c.stream));
+  const size_t zero_words = radix_zero_words<U64>(n, HI_DIGITS) - HIST_AREA;
+  const uint32_t g = std::min<uint32_t>(div_up<uint32_t>(n, BLK), (uint32_t)std::max(c.num_sms, 1) * 8u);
+  KLAUNCH("k_morton64", CK(launch_k(k_morton64_sort_prep, g, BLK, 0, c.stream, leaves, n, total_keys, codes, rs, done,
+                                    rs + HIST_AREA, zero_words, flag)));
+  bool alt = false;
+  cudaError_t e = radix_sort_pairs<U64>(c, codes, vals, n, true, keys_alt, vals_alt, rs, &alt, HI_DIGITS, true, rs,
+                                        HI_FIRST);
+  if (e) return c.cuda_fail(e, "radix sort");
+  U64* sk = alt ? keys_alt : codes;
+  uint32_t* sv = alt ? vals_alt : vals;
+  KLAUNCH("k_run_check", CK(launch_k(k_run_check, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, sk, n, flag, 24)));
+  uint32_t* h = reinterpret_cast<uint32_t*>(static_cast<char*>(c.h_small) + RUN_FLAG_OFFSET);  // pinned
+  CK(cudaMemcpyAsync(h, flag, 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(c.h_status, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  int r = sort_status(c);  // a sort tile that gave up its wait leaves the order unusable
+  if (r) return r;
+  if (*h == 0) {
+    KLAUNCH("k_fix_gather", CK(launch_k(k_fix_gather, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, sk, sv, n, leaves,
+                                        out)));
+    return 0;
+  }
+  // all eight bytes of the high-digit order, stably: ties keep input order
+  U64* k2 = alt ? codes : keys_alt;
+  uint32_t* v2 = alt ? vals : vals_alt;
+  bool alt2 = false;
+  e = radix_sort_pairs<U64>(c, sk, sv, n, false, k2, v2, rs, &alt2);
+  if (e) return c.cuda_fail(e, "radix sort");
+  CK(cudaMemcpyAsync(c.h_status, c.d_status, 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  r = sort_status(c);
+  if (r) return r;
+  KLAUNCH("k_gather", CK(launch_k(k_gather, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, leaves, alt2 ? v2 : sv, n, out)));
+  return 0;
+}
+
 int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* total_keys, uint32_t radius,
                       int precision, uint32_t depth_threshold, Bvh2Node* out_nodes, uint32_t* passes_out,
                       uint64_t* sum_counts_out, PlocState* deferred, const uint32_t* remap, bool nan_checked) {
@@ -1829,14 +1975,21 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   if (n == 0) return 0;
   if (radius < 1 || radius > 32) return c.fail(OBVHS_ERR_INVALID_ARG, "search distance must be 1..32");
   Scratch& s = c.scratch;
-  void* codes = s.get(SLOT_KEYS, (size_t)n * (precision ? sizeof(U128) : sizeof(unsigned long long)));
-  if (!codes) return c.fail(OBVHS_ERR_OOM, "scratch");
-  int r = ploc_morton_codes(c, leaves, n, total_keys, precision, codes);
-  if (r) return r;
-  uint32_t* order = nullptr;
-  r = ploc_sort_codes(c, codes, n, precision, &order);
-  if (r) return r;
   Bvh2Node* cur = (Bvh2Node*)s.get(SLOT_PLOC_A, (size_t)n * sizeof(Bvh2Node));
+  if (!cur) return c.fail(OBVHS_ERR_OOM, "scratch");
+  if (precision == 0 && n > RUN_MAX) {
+    int r = ploc_sorted_leaves_u64(c, leaves, n, total_keys, cur);
+    if (r) return r;
+  } else {
+    void* codes = s.get(SLOT_KEYS, (size_t)n * (precision ? sizeof(U128) : sizeof(unsigned long long)));
+    if (!codes) return c.fail(OBVHS_ERR_OOM, "scratch");
+    int r = ploc_morton_codes(c, leaves, n, total_keys, precision, codes);
+    if (r) return r;
+    uint32_t* order = nullptr;
+    r = ploc_sort_codes(c, codes, n, precision, &order);
+    if (r) return r;
+    KLAUNCH("k_gather", launch_k(k_gather, div_up<uint32_t>(n, BLK), BLK, 0, c.stream, leaves, order, n, cur));
+  }
   Bvh2Node* nxt = (Bvh2Node*)s.get(SLOT_PLOC_B, (size_t)n * sizeof(Bvh2Node));
   int8_t* merge = (int8_t*)s.get(SLOT_MERGE, (size_t)n);
   uint2* tile_cnt = (uint2*)s.get(SLOT_PARTIAL, (size_t)div_up<uint32_t>(n, PT) * sizeof(uint2));
@@ -1844,9 +1997,7 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   // the pass ranges (not for a partial rebuild, whose pairs go to free slots)
   uint32_t* pass_ins = remap ? nullptr : (uint32_t*)s.get(SLOT_PLOC_PASSES, (size_t)PLOC_PASS_REC * 4);
   c.ploc_pass_ins = pass_ins;
-  if (!cur || !nxt || !merge || !tile_cnt || !st) return c.fail(OBVHS_ERR_OOM, "scratch");
-  uint32_t g = div_up<uint32_t>(n, BLK);
-  KLAUNCH("k_gather", launch_k(k_gather, g, BLK, 0, c.stream, leaves, order, n, cur));
+  if (!nxt || !merge || !tile_cnt || !st) return c.fail(OBVHS_ERR_OOM, "scratch");
   PlocState* h0 = reinterpret_cast<PlocState*>(static_cast<char*>(c.h_small) + 1024);  // pinned, asynchronous copy
   *h0 = PlocState{};
   h0->count[0] = n;

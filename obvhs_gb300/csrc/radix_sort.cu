@@ -47,7 +47,7 @@ struct Tile {
 // no separate scan launch is needed.
 template <class K>
 __global__ void __launch_bounds__(THREADS) k_rs_hist(const K* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
-                                                     int nd, uint32_t* done) {
+                                                     int nd, int first, uint32_t* done) {
   grid_dep_wait();
   constexpr int NB = KeyTraits<K>::BYTES;
   __shared__ uint32_t h[NB * 256];
@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(THREADS) k_rs_hist(const K* __restrict__ keys,
     if (base + r * THREADS < n) {
 #pragma unroll
       for (int b = 0; b < NB; b++)
-        if (b < nd) atomicAdd(&h[b * 256 + KeyTraits<K>::digit(k[r], b)], 1u);
+        if (b < nd) atomicAdd(&h[b * 256 + KeyTraits<K>::digit(k[r], first + b)], 1u);
     }
   __syncthreads();
   for (int i = threadIdx.x; i < nd * 256; i += THREADS)
@@ -284,9 +284,10 @@ size_t radix_zero_words(uint32_t n, int digits) {
 template <class K>
 cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, bool init_iota, K* keys_alt,
                              uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt, int digits, bool zeroed,
-                             const uint32_t* bases) {
+                             const uint32_t* bases, int first_byte) {
   constexpr int NB = KeyTraits<K>::BYTES;
   const int nd = digits > 0 && digits < NB ? digits : NB;
+  if (first_byte < 0 || first_byte + nd > NB) return cudaErrorInvalidValue;
   const bool small = n <= SMALL_SORT_MAX;
   *result_in_alt = false;
   if (n == 0) return cudaSuccess;
@@ -305,7 +306,7 @@ cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, 
   } else {
     const uint32_t hb = (n + THREADS * HIST_ITEMS - 1) / (THREADS * HIST_ITEMS);
     // pass 0's header word 1 is the histogram kernel's ticket counter
-    KLAUNCH("k_rs_hist", launch_k(k_rs_hist<K>, hb, THREADS, 0, c.stream, keys, n, hist, nd, pass_area + 1));
+    KLAUNCH("k_rs_hist", launch_k(k_rs_hist<K>, hb, THREADS, 0, c.stream, keys, n, hist, nd, first_byte, pass_area + 1));
   }
   K* kin = keys;
   uint32_t* vin = vals;
@@ -315,11 +316,11 @@ cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, 
   for (int b = 0; b < nd; b++) {
     uint32_t* ts = pass_area + (size_t)b * pass_words;
     if (small)
-      KLAUNCH("k_rs_pass", launch_k(k_rs_pass<K, true>, ntiles, THREADS, 0, c.stream, kin, vin, kout, vout, n, b, iota,
+      KLAUNCH("k_rs_pass", launch_k(k_rs_pass<K, true>, ntiles, THREADS, 0, c.stream, kin, vin, kout, vout, n, first_byte + b, iota,
                                                                                hist + b * 256, ts + 32, ts, c.d_status,
                                                                                c.wait_limit));
     else
-      KLAUNCH("k_rs_pass", launch_k(k_rs_pass<K, false>, ntiles, THREADS, 0, c.stream, kin, vin, kout, vout, n, b, iota,
+      KLAUNCH("k_rs_pass", launch_k(k_rs_pass<K, false>, ntiles, THREADS, 0, c.stream, kin, vin, kout, vout, n, first_byte + b, iota,
                                                                                 hist + b * 256, ts + 32, ts, c.d_status,
                                                                                c.wait_limit));
     iota = false;
@@ -339,12 +340,12 @@ cudaError_t fill_iota(uint32_t* v, uint32_t n, cudaStream_t s) {
 }
 
 template cudaError_t radix_sort_pairs<uint32_t>(obvhs_ctx&, uint32_t*, uint32_t*, uint32_t, bool, uint32_t*, uint32_t*,
-                                                uint32_t*, bool*, int, bool, const uint32_t*);
+                                                uint32_t*, bool*, int, bool, const uint32_t*, int);
 template cudaError_t radix_sort_pairs<unsigned long long>(obvhs_ctx&, unsigned long long*, uint32_t*, uint32_t, bool,
                                                           unsigned long long*, uint32_t*, uint32_t*, bool*, int, bool,
-                                                          const uint32_t*);
+                                                          const uint32_t*, int);
 template cudaError_t radix_sort_pairs<U128>(obvhs_ctx&, U128*, uint32_t*, uint32_t, bool, U128*, uint32_t*, uint32_t*,
-                                            bool*, int, bool, const uint32_t*);
+                                            bool*, int, bool, const uint32_t*, int);
 template size_t radix_zero_words<uint32_t>(uint32_t, int);
 template size_t radix_zero_words<unsigned long long>(uint32_t, int);
 template size_t radix_zero_words<U128>(uint32_t, int);

@@ -52,10 +52,12 @@ struct obvhs_ctx;
 // `bases` (optional): the digit bases (exclusive scans of the keys' digit
 // histograms, 256 words per digit) computed by the caller, so the sort skips
 // its histogram launch.
+// `first_byte`: the sort runs on key bytes [first_byte, first_byte + digits)
+// (LSD order), for keys whose low bytes are ordered some other way.
 template <class K>
 cudaError_t radix_sort_pairs(obvhs_ctx& c, K* keys, uint32_t* vals, uint32_t n, bool init_iota, K* keys_alt,
                              uint32_t* vals_alt, uint32_t* scratch, bool* result_in_alt, int digits = 0,
-                             bool zeroed = false, const uint32_t* bases = nullptr);
+                             bool zeroed = false, const uint32_t* bases = nullptr, int first_byte = 0);
 template <class K>
 size_t radix_zero_words(uint32_t n, int digits = 0);
 

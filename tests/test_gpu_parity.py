@@ -150,6 +150,32 @@ def test_ploc_bitexact(G, n, radius, threshold, precision):
     assert b.max_depth == omd
 
 
+def _clumps(seed):
+    """Clumps of 1-32 boxes whose centres share their high Morton digits."""
+    rng = np.random.default_rng(seed)
+    base = rng.uniform(-50, 50, size=(1500, 3))
+    c = np.repeat(base, rng.integers(1, 33, size=len(base)), axis=0)
+    c = c + rng.uniform(-2e-3, 2e-3, size=c.shape)
+    c = c[rng.permutation(len(c))]
+    return np.concatenate([c - 1e-6, c + 1e-6], 1).astype(np.float32)
+
+
+@pytest.mark.parametrize("kind", ["dup3", "dup40", "clumps"])
+def test_ploc_u64_runs_of_equal_high_digits(G, kind):
+    """U64 builds whose Morton order has runs of equal high digits: runs of up
+    to 32 put in order as the leaves are gathered (equal codes by input
+    order), a longer run of equal codes sorting all the bits instead."""
+    if kind == "clumps":
+        a = _clumps(4)
+    else:
+        a = np.repeat(_random_aabbs(2000, 77), 3 if kind == "dup3" else 40, axis=0)
+    b = G.PlocBuilder().build_ploc(14, a, None, 0, 0)
+    nodes, pidx = b.download()
+    on, op, omd, _ = O.ploc(a, None, 14, 0, 0)
+    assert _eq(nodes, on) and _eq(pidx, op)
+    assert b.max_depth == omd
+
+
 def test_ploc_single_and_empty(G):
     a = _random_aabbs(1, 1)
     nodes, pidx = G.PlocBuilder().build_ploc(14, a).download()
