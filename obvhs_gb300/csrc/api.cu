@@ -140,16 +140,17 @@ int build_pipeline(BuildCtx& c, const float* tris, const float* aabbs, uint32_t 
   b2.nodes = (Bvh2Node*)s.get(SLOT_BVH2_NODES, (size_t)std::max(b2.n_nodes, 1u) * sizeof(Bvh2Node));
   b2.prim_indices = (uint32_t*)s.get(SLOT_BVH2_PIDX, (size_t)std::max(m, 1u) * 4);
   if (!leaves || !total || !b2.nodes || !b2.prim_indices) return c.fail(OBVHS_ERR_OOM, "scratch");
+  // primitive_indices = the index list given to PLOC (the identity list
+  // written by the leaves kernel)
   if (split || !tris)
     r = ploc_leaves(c, nullptr, leaf_aabbs, leaf_idx, m, leaves, total);
   else
-    r = ploc_leaves(c, tris, nullptr, nullptr, m, leaves, total);
+    r = ploc_leaves(c, tris, nullptr, nullptr, m, leaves, total, b2.prim_indices);
   if (r) return r;
-  // primitive_indices = the index list given to PLOC
   if (m) {
     if (leaf_idx)
       CK(cudaMemcpyAsync(b2.prim_indices, leaf_idx, (size_t)m * 4, cudaMemcpyDeviceToDevice, c.stream));
-    else {
+    else if (!tris) {
       KLAUNCH("k_iota_u32", launch_k(k_iota_u32, div_up<uint32_t>(m, 256), 256, 0, c.stream, b2.prim_indices, m));
     }
   }

@@ -310,8 +310,10 @@ struct obvhs_cwbvh {
 };
 
 // ploc.cu
+// Leaves from triangles (tris) or AABBs; with `iota` and triangles also the
+// identity index list 0..n-1.
 int ploc_leaves(BuildCtx& c, const float* tris, const float* aabbs, const uint32_t* idx, uint32_t n, Bvh2Node* leaves,
-                int* total_keys);
+                int* total_keys, uint32_t* iota = nullptr);
 int ploc_morton_codes(BuildCtx& c, const Bvh2Node* leaves, uint32_t n, const int* total_keys, int precision,
                       void* codes);
 int ploc_sort_codes(BuildCtx& c, void* codes, uint32_t n, int precision, uint32_t** order_out);

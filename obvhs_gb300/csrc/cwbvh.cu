@@ -350,7 +350,8 @@ __device__ void costs_ordered(const Bvh2Node* __restrict__ nodes, const uint32_t
         continue;
       }
       __stcg(&small[i], make_uint4(__ldg(&pidx_in[node_first(nd)]), 0u, 0u, 1u));
-      if (parents[i] == i) __stcg(&erec[i], make_uint4(0u, 0u, 1u, 0u));  // a leaf root: one CWBVH node
+      // a leaf root: one CWBVH node (no parents given: one tree, rooted at 0)
+      if (parents ? parents[i] == i : i == 0) __stcg(&erec[i], make_uint4(0u, 0u, 1u, 0u));
       continue;
     }
     const uint32_t f = node_first(nd);
@@ -381,10 +382,10 @@ __device__ void costs_ordered(const Bvh2Node* __restrict__ nodes, const uint32_t
 // array, and every node's children were written by an earlier pass, so the
 // large ranges are costed in pass order with a grid barrier after each (no
 // ready flags, fences or waits) and the small ranges at the top of the tree
-// in the ordered form.  Same records as the climb.
+// in the ordered form.  Same records as the climb.  One tree rooted at node
+// 0: no parent links are needed.
 struct CostRangeArgs {
   const Bvh2Node* nodes;
-  const uint32_t* parents;
   const uint32_t* pidx_in;
   const uint32_t* pass_ins;
   uint32_t n, max_prims, passes;
@@ -404,7 +405,7 @@ __device__ void cost_node_ready(const CostRangeArgs& a, uint32_t i) {
       return;
     }
     __stcg(&a.small[i], make_uint4(__ldg(&a.pidx_in[node_first(nd)]), 0u, 0u, 1u));
-    if (a.parents[i] == i) __stcg(&a.erec[i], make_uint4(0u, 0u, 1u, 0u));  // a leaf root: one CWBVH node
+    if (i == 0) __stcg(&a.erec[i], make_uint4(0u, 0u, 1u, 0u));  // a leaf root: one CWBVH node
     return;
   }
   const uint32_t f = node_first(nd);
@@ -430,20 +431,26 @@ __device__ void cost_node_ready(const CostRangeArgs& a, uint32_t i) {
 // The large ranges go grid-wide with a barrier after each; the rest of the
 // tree, nodes [0, top), in the ordered form (nodes from `top` down, ready
 // flags), where a child at or above `top` is complete since the barrier.
+// The ready flags of [0, top) and the node counter `next` are cleared here,
+// before the first barrier.
 __global__ void __launch_bounds__(BLK, 4) k_costs_ranges(CostRangeArgs a, uint32_t* flags, uint32_t* next) {
   grid_dep_wait();
   cg::grid_group grid = cg::this_grid();
   const uint32_t nthreads = gridDim.x * BLK, me = blockIdx.x * BLK + threadIdx.x;
-  uint32_t top = a.n;
-  for (uint32_t p = 0; p < a.passes; p++) {
+  uint32_t top = a.n, large = 0;
+  while (large < a.passes && a.pass_ins[large] - a.pass_ins[large + 1] >= COST_RANGE_MIN) {
+    top = a.pass_ins[large + 1];
+    large++;
+  }
+  for (uint32_t i = me; i < top; i += nthreads) flags[i] = 0u;
+  if (me == 0) *next = 0u;
+  if (large == 0) grid.sync();
+  for (uint32_t p = 0; p < large; p++) {
     const uint32_t hi = a.pass_ins[p], lo = a.pass_ins[p + 1];
-    if (hi - lo < COST_RANGE_MIN) break;
     for (uint32_t i = lo + me; i < hi; i += nthreads) cost_node_ready(a, i);
-    top = lo;
     grid.sync();
   }
-  costs_ordered(a.nodes, a.parents, a.pidx_in, top, a.max_prims, a.crec, a.erec, a.small, flags, next, a.status,
-                a.n);
+  costs_ordered(a.nodes, nullptr, a.pidx_in, top, a.max_prims, a.crec, a.erec, a.small, flags, next, a.status, a.n);
 }
 
 // Lanes of a k_costs warp take new nodes once this many of them are idle.
@@ -1342,17 +1349,17 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
   // the tree came straight from this context's last PLOC build: cost it
   // range by range (a cooperative launch), unless the GPU is shared
   const bool ranges = ploc_passes > 0 && ploc_passes < PLOC_PASS_REC && c.ploc_pass_ins && !gpu_shared(c);
-  CK(cudaMemsetAsync(flags, 0, (size_t)n * 4 + 8, c.stream));
-  int r = compute_parents_device(c, b->nodes, n, parents, flags + n + 1);
-  if (r) return r;
-  if (ranges) {
-    CostRangeArgs ra{b->nodes, parents, b->prim_indices, c.ploc_pass_ins, n, max_prims, ploc_passes, crec, erec, small,
+  if (ranges) {  // (the kernel clears the flags it uses)
+    CostRangeArgs ra{b->nodes, b->prim_indices, c.ploc_pass_ins, n, max_prims, ploc_passes, crec, erec, small,
                      c.d_status};
     uint32_t* fl = flags;
     uint32_t* nx = flags + n;
     void* args[] = {&ra, &fl, &nx};
     KLAUNCH("k_costs", CK(coop_launch(c, (const void*)k_costs_ranges, cost_range_grid(c), BLK, args, 0)));
   } else {
+    CK(cudaMemsetAsync(flags, 0, (size_t)n * 4 + 8, c.stream));
+    int r = compute_parents_device(c, b->nodes, n, parents, flags + n + 1);
+    if (r) return r;
     KLAUNCH("k_costs", launch_k(k_costs, cost_grid(c, n), BLK, 0, c.stream, b->nodes, parents, b->prim_indices, n,
                                 max_prims, crec, erec, small, flags, flags + n, flags + n + 1, c.d_status));
   }

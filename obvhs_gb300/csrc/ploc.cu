@@ -80,14 +80,17 @@ __device__ __forceinline__ bool box_has_nan(const Box& b) {
 }
 
 // Triangle::aabb (src/triangle.rs:28) + Bvh2Node::new(aabb, 1, indices[i]).
+// With `iota` (optional) also the identity index list (the primitive indices
+// of a build without pre-splits).
 __global__ void __launch_bounds__(BLK) k_leaves_from_tris(const float* __restrict__ tris, uint32_t n,
                                                           Bvh2Node* __restrict__ leaves, int* total_keys,
-                                                          uint32_t* status) {
+                                                          uint32_t* status, uint32_t* __restrict__ iota) {
   grid_dep_wait();
   uint32_t i = blockIdx.x * BLK + threadIdx.x;
   bool valid = i < n;
   Box b{};
   if (valid) {
+    if (iota) iota[i] = i;
     const float* t = tris + (size_t)i * 9;
     float3 v0 = make_float3(t[0], t[1], t[2]), v1 = make_float3(t[3], t[4], t[5]), v2 = make_float3(t[6], t[7], t[8]);
     b.mn = make_float3(smin(smin(v0.x, v1.x), v2.x), smin(smin(v0.y, v1.y), v2.y), smin(smin(v0.z, v1.z), v2.z));
@@ -1814,13 +1817,14 @@ int cluster_ctas() {
 // ===========================================================================
 
 int ploc_leaves(BuildCtx& c, const float* tris, const float* aabbs, const uint32_t* idx, uint32_t n, Bvh2Node* leaves,
-                int* total_keys) {
+                int* total_keys, uint32_t* iota) {
   static const int init[6] = {0x7fffffff, 0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000, (int)0x80000000};
   CK(cudaMemcpyAsync(total_keys, init, sizeof(init), cudaMemcpyHostToDevice, c.stream));
   if (!n) return 0;
   uint32_t g = div_up<uint32_t>(n, BLK);
   if (tris)
-    KLAUNCH("k_leaves_from_tris", launch_k(k_leaves_from_tris, g, BLK, 0, c.stream, tris, n, leaves, total_keys, c.d_status));
+    KLAUNCH("k_leaves_from_tris", launch_k(k_leaves_from_tris, g, BLK, 0, c.stream, tris, n, leaves, total_keys, c.d_status,
+                                                           iota));
   else
     KLAUNCH("k_leaves_from_aabbs", launch_k(k_leaves_from_aabbs, g, BLK, 0, c.stream, aabbs, idx, n, leaves, total_keys, c.d_status));
   CK(cudaGetLastError());
