@@ -605,7 +605,7 @@ int obvhs_ctx_create(int device, uint64_t hbm_budget_bytes, obvhs_ctx** out) {
   }
   c->num_sms = prop.multiProcessorCount;
   cudaMemset(c->d_status, 0, 16);
-  if (ploc_setup_kernels() != 0) {
+  if (ploc_setup_kernels() != 0 || reinsertion_setup_kernels() != 0) {
     obvhs_ctx_destroy(c);
     return OBVHS_ERR_CUDA;
   }

@@ -324,6 +324,7 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
                       uint64_t* sum_counts_out, PlocState* deferred = nullptr, const uint32_t* remap = nullptr,
                       bool nan_checked = false);
 int ploc_setup_kernels();
+int reinsertion_setup_kernels();  // per device, with the device current
 
 // Segmented builds: many scenes through every stage together, one launch
 // per stage for all of them.  Scene s owns primitives / leaves

@@ -38,7 +38,6 @@ namespace {
 constexpr int BLK = 256;
 constexpr int RESOLVE_THREADS = 1024;
 constexpr uint32_t RESOLVE_SINGLE_MAX = 40000;  // candidates searched: one block resolves the whole pass
-constexpr uint32_t RESOLVE_SMALL = 512;  // proposals one block resolves faster than the grid (one climb per thread)
 
 struct Reins {
   uint32_t from, to;
@@ -141,48 +140,76 @@ __global__ void __launch_bounds__(BLK) k_cand_keys(const Bvh2Node* __restrict__ 
 // state machine advanced one step at a time: a stack pop of the
 // branch-and-bound search below the current pivot, or a climb to the next
 // pivot.  CAP entries of (area, node) on a per-thread stack (one 8-byte local
-// word each); CLAMP = StackStack semantics (the last slot is overwritten when
-// full), else overflow is an error (the reference's HeapStack panics).
+// word each); CLAMP = StackStack semantics (a push onto a full stack is lost:
+// the reference writes its last slot, which no pop reads), else overflow is
+// an error (the reference's HeapStack panics).
+//
+// The top two entries live in registers (e0, e1) and the rest in `st`, so a
+// pop costs no memory access: the entry under the new top is reloaded from
+// `st` while the popped node is processed.  A node whose children pass the
+// bound has both children's records loaded at once (they are adjacent); the
+// second child, popped next, is processed from the loaded record, and a climb
+// pushes the next pivot's sibling with its record too.  So a step waits for
+// one node load, not for a stack load and then a node load.  Children whose
+// bound fails at the push are not pushed: the reference pushes them and pops
+// and prunes both at once (best_diff cannot change in between), unless a push
+// would be lost or overflow, in which case they are pushed as it does.
 template <int CAP, bool CLAMP>
 struct FindSearch {
   uint2* st;  // the thread's stack, CAP entries (kept apart so the scalars stay in registers)
   uint32_t sp, guard, cap;
   uint32_t clamp_at;  // !CLAMP only: nonzero = StackStack semantics with this many entries (per-candidate mode)
   bool overflow;
+  uint2 e0, e1;  // entries sp - 1 and sp - 2 (when they exist); st holds entries [0, sp - 2)
+  bool r0;       // rec is e0's node record
+  Bvh2Node rec;
   uint32_t node_id, parent_id, sib, pivot_id, best_to;
   float node_area, area_diff, best_diff;
-  Box box, pivot_bbox;
+  Box box, pivot_bbox, sib_box;
 
-  __device__ __forceinline__ void push(float a, uint32_t id) {
-    const uint2 v = make_uint2(__float_as_uint(a), id);
-    if (CLAMP) {
-      st[sp] = v;
-      sp = min(sp + 1, (uint32_t)CAP - 1);
-    } else if (clamp_at) {
-      st[sp] = v;
-      sp = min(sp + 1, clamp_at - 1);
-    } else if (sp >= cap) {
-      overflow = true;
-    } else {
-      st[sp] = v;
-      sp++;
+  // entries a push may occupy without being lost (or overflowing)
+  __device__ __forceinline__ uint32_t room() const {
+    return CLAMP ? (uint32_t)CAP - 1 : (clamp_at ? clamp_at - 1 : cap);
+  }
+  __device__ __forceinline__ void push(float a, uint32_t id, const Bvh2Node& r) {
+    if (sp >= room()) {
+      if (!CLAMP && !clamp_at) overflow = true;
+      return;  // StackStack: lost
     }
+    if (sp >= 2) st[sp - 2] = e1;
+    e1 = e0;
+    e0 = make_uint2(__float_as_uint(a), id);
+    rec = r;
+    r0 = true;
+    sp++;
+  }
+  __device__ __forceinline__ uint2 pop(bool* has_rec) {
+    const uint2 v = e0;
+    *has_rec = r0;
+    e0 = e1;
+    r0 = false;
+    sp--;
+    if (sp >= 2) e1 = st[sp - 2];
+    return v;
   }
   __device__ __forceinline__ void start(const Bvh2Node* nodes, const uint32_t* parents, uint32_t node) {
     node_id = node;
     best_to = 0;
     best_diff = 0.0f;
-    box = node_box(ld_node(&nodes[node_id]));
-    node_area = half_area(box);
     parent_id = parents[node_id];
-    area_diff = half_area(node_box(ld_node(&nodes[parent_id])));
     sib = sibling_of(node_id);
-    pivot_bbox = node_box(ld_node(&nodes[sib]));
+    const Bvh2Node nd = ld_node(&nodes[node_id]), pn = ld_node(&nodes[parent_id]), sn = ld_node(&nodes[sib]);
+    box = node_box(nd);
+    node_area = half_area(box);
+    area_diff = half_area(node_box(pn));
+    sib_box = node_box(sn);
+    pivot_bbox = sib_box;
     pivot_id = parent_id;
     sp = 0;
     guard = 0;
     overflow = false;
-    push(area_diff, sib);
+    r0 = false;
+    push(area_diff, sib, sn);
   }
   // One step; returns true when the search is over.
   __device__ __forceinline__ bool step(const Bvh2Node* nodes, const uint32_t* parents) {
@@ -191,11 +218,12 @@ struct FindSearch {
         overflow = true;
         return true;
       }
-      sp--;
-      const uint2 top = st[sp];
+      bool has_rec;
+      const Bvh2Node cached = rec;
+      const uint2 top = pop(&has_rec);
       const float top_area = __uint_as_float(top.x);
       if (top_area - node_area <= best_diff) return false;
-      const Bvh2Node dst = ld_node(&nodes[top.y]);
+      const Bvh2Node dst = has_rec ? cached : ld_node(&nodes[top.y]);
       const float reinsert_area = top_area - half_area(box_union(node_box(dst), box));
       if (reinsert_area > best_diff) {
         best_to = top.y;
@@ -203,21 +231,32 @@ struct FindSearch {
       }
       if (node_prims(dst) == 0) {
         const float child_area = reinsert_area + half_area(node_box(dst));
-        push(child_area, node_first(dst));
-        push(child_area, node_first(dst) + 1);
+        const uint32_t f = node_first(dst);
+        if (child_area - node_area <= best_diff && sp + 2 <= room()) return false;
+        const Bvh2Node c0 = ld_node(&nodes[f]), c1 = ld_node(&nodes[f + 1]);
+        push(child_area, f, c0);
+        push(child_area, f + 1, c1);
       }
       return false;
     }
     if (overflow) return true;
+    // the stack is empty: climb to the next pivot.  Its sibling's record is
+    // loaded with the pivot's parent link and record (in bounds: a pivot
+    // other than node 0 has its sibling in the array; its parent decides
+    // whether it is used).
+    const uint32_t nsib = sibling_of(pivot_id);
+    Bvh2Node ns{};
+    if (pivot_id != 0) ns = ld_node(&nodes[nsib]);
+    const uint32_t up = parents[pivot_id];
     if (pivot_id != parent_id) {
-      pivot_bbox = box_union(pivot_bbox, node_box(ld_node(&nodes[sib])));
+      pivot_bbox = box_union(pivot_bbox, sib_box);
       area_diff += half_area(node_box(ld_node(&nodes[pivot_id]))) - half_area(pivot_bbox);
     }
-    const uint32_t up = parents[pivot_id];
     if (up == pivot_id) return true;  // the root is its own parent
-    sib = sibling_of(pivot_id);
+    sib = nsib;
     pivot_id = up;
-    push(area_diff, sib);
+    sib_box = node_box(ns);
+    push(area_diff, sib, ns);
     return false;
   }
   __device__ __forceinline__ Reins result(const uint32_t* parents, uint32_t* status) const {
@@ -497,21 +536,33 @@ __device__ __forceinline__ void refit_climb(const ResolveArgs& a, uint32_t x) {
   set_status(a.status, ST_ITER_LIMIT);
 }
 
-// Steps 2-5 of k_resolve over the P listed proposals, by `nthreads` threads
-// numbered `t0`, with `sync` a barrier over exactly those threads.  Words that
-// other blocks may write earlier in the same launch (parents, nodes, touched,
-// dirty) are read through L2 (ld.cg) so no stale L1 line is used, except in
-// the mark and refit steps of a single-block pass (L1 = true, see ld_word).
-template <bool L1, class Sync>
-__device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, uint32_t t0, uint32_t nthreads,
-                                             Sync sync, uint32_t* s_rem) {
-  // 2. rounds, one barrier each.  A proposal touching an accepted one is
-  //    rejected; one that owned all five nodes in the previous round's claims
-  //    is accepted; the rest claim their nodes (lowest key wins).  Claims of
-  //    round r live in owner array r % 3; a round resets array (r + 1) % 3 for
-  //    the nodes it claims, the array the next round claims in.  The lowest
-  //    unresolved proposal owns its nodes after claiming, so it is resolved
-  //    one round later: the loop ends.
+// Proposal states (0 unresolved, 1 accepted, 2 rejected) in global memory,
+// written by other blocks of the launch (read through L2), or in the block's
+// shared memory.
+struct GlobalStates {
+  const uint8_t* p;
+  __device__ __forceinline__ uint8_t operator[](uint32_t j) const { return __ldcg(p + j); }
+};
+struct SharedStates {
+  const uint8_t* p;
+  __device__ __forceinline__ uint8_t operator[](uint32_t j) const { return p[j]; }
+};
+
+// Step 2 of k_resolve over the P listed proposals, by `nthreads` threads
+// numbered `t0`, with `sync` a barrier over exactly those threads, on the
+// global claim arrays.  Words that other blocks may write earlier in the same
+// launch (parents, nodes, touched, dirty) are read through L2 (ld.cg) so no
+// stale L1 line is used.
+//   Rounds, one barrier each.  A proposal touching an accepted one is
+//   rejected; one that owned all five nodes in the previous round's claims
+//   is accepted; the rest claim their nodes (lowest key wins).  Claims of
+//   round r live in owner array r % 3; a round resets array (r + 1) % 3 for
+//   the nodes it claims, the array the next round claims in.  The lowest
+//   unresolved proposal owns its nodes after claiming, so it is resolved
+//   one round later: the loop ends.
+template <class Sync>
+__device__ __forceinline__ void rounds_global(const ResolveArgs& a, uint32_t P, uint32_t t0, uint32_t nthreads,
+                                              Sync sync, uint32_t* s_rem) {
   uint32_t* remaining = a.ctr + 1;
   uint32_t round = 0;
   for (;; round++) {
@@ -562,13 +613,18 @@ __device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, u
     }
   }
   if (t0 == 0) a.ctr[4] = round + 1;
+}
 
-  // 3. reinsert_node: moves the nodes and updates the parent links exactly as
-  //    the reference does.  Accepted proposals share no moved node, no child
-  //    of one and no parent link they read, so they run in parallel.
+// Step 3, reinsert_node: moves the nodes and updates the parent links exactly
+// as the reference does.  Accepted proposals share no moved node, no child of
+// one and no parent link they read, so they run in parallel.  Each accepted
+// proposal leaves its refit start nodes in `starts`.
+template <class States>
+__device__ __forceinline__ void apply_moves(const ResolveArgs& a, uint32_t P, uint32_t t0, uint32_t nthreads,
+                                            States st) {
   uint32_t applied = 0;
   for (uint32_t j = t0; j < P; j += nthreads) {
-    if (a.state[j] != 1) continue;
+    if (st[j] != 1) continue;
     const Reins r = a.reins[a.plist[j]];
     const uint32_t sib = sibling_of(r.from);
     const uint32_t parent = __ldcg(&a.parents[r.from]);
@@ -594,16 +650,22 @@ __device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, u
     applied++;
   }
   if (applied) atomicAdd(a.applied, applied);
-  sync();
+}
 
-  // 4. mark, one thread per start node (two per accepted proposal: `to`,
-  //    and the parent of the old parent of `from`); a start node this thread
-  //    marked first stays in `starts` as one to refit from
+// Steps 4-5 on the global per-node words.
+//   4. mark, one thread per start node (two per accepted proposal: `to`, and
+//      the parent of the old parent of `from`); a start node this thread
+//      marked first stays in `starts` as one to refit from
+//   5. refit from the marked nodes that have no marked children
+// L1 = true when one block runs the pass (see ld_word).
+template <bool L1, class Sync, class States>
+__device__ __forceinline__ void mark_refit_global(const ResolveArgs& a, uint32_t P, uint32_t t0, uint32_t nthreads,
+                                                  Sync sync, States st) {
   uint32_t* start_slots = reinterpret_cast<uint32_t*>(a.starts);
   for (uint32_t i = t0; i < 2 * P; i += nthreads) {
     const uint32_t j = i >> 1;
-    if (__ldcg(&a.state[j]) != 1) continue;  // slots and states were written by other threads
-    uint32_t x = __ldcg(&start_slots[i]);
+    if (st[j] != 1) continue;
+    uint32_t x = __ldcg(&start_slots[i]);  // slots were written by other threads
     if (i & 1u) {
       const uint32_t up = __ldcg(&a.parents[x]);
       x = up != x ? up : OBVHS_INVALID;  // nothing above the root
@@ -611,10 +673,8 @@ __device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, u
     start_slots[i] = (x != OBVHS_INVALID && mark_path<L1>(a, x)) ? x : OBVHS_INVALID;
   }
   sync();
-
-  // 5. refit from the marked nodes that have no marked children
   for (uint32_t i = t0; i < 2 * P; i += nthreads) {
-    if (__ldcg(&a.state[i >> 1]) != 1) continue;
+    if (st[i >> 1] != 1) continue;
     const uint32_t x = start_slots[i];
     if (x == OBVHS_INVALID) continue;
     const Bvh2Node xn = ld_node_cg(&a.nodes[x]);
@@ -623,6 +683,302 @@ __device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, u
       if (__ldcg(&a.dirty[f]) == a.stamp || __ldcg(&a.dirty[f + 1]) == a.stamp) continue;  // a child's climb reaches x
     }
     refit_climb<L1>(a, x);
+  }
+}
+
+// ---- one block, shared-memory tables ---------------------------------------
+// A pass resolved by one block keeps its per-node words in shared-memory hash
+// tables instead of the global arrays: the node ids of the proposals'
+// conflict sets (claims, touched flags) during the rounds, then the marked
+// nodes (parent, children, box, arrival count) for the refit.  Every climb
+// step is then a shared-memory access instead of an L2 round trip.  More than
+// SM_P proposals use the global rounds; more than SM_MARKED marked nodes use
+// the global mark and refit (nothing global is written before that is known).
+constexpr uint32_t SM_P = 800;          // proposals whose rounds run in shared memory
+constexpr uint32_t SM_SLOT_BITS = 13;
+constexpr uint32_t SM_SLOTS = 1u << SM_SLOT_BITS;  // hash slots of either table
+constexpr uint32_t SM_MARKED = 3072;    // marked nodes refit in shared memory
+constexpr uint16_t SM_NONE = 0xffffu;
+static_assert(5 * SM_P <= SM_SLOTS / 2, "conflict table at most half full");
+static_assert(SM_MARKED < SM_NONE, "marked-node indices fit 16 bits");
+
+// Byte offsets in the dynamic shared memory of k_resolve.  The states stay
+// for the whole pass; the rounds' tables and the marks' tables overlay.
+constexpr size_t SMO_STATE = 0;                               // u8[SM_P]
+constexpr size_t SMO_OVER = 1024;
+constexpr size_t SMO_H1 = SMO_OVER;                           // u32[SM_SLOTS] conflict node ids
+constexpr size_t SMO_OWN = SMO_H1 + 4 * SM_SLOTS;             // u64[SM_SLOTS] lowest claiming key
+constexpr size_t SMO_TOUCH = SMO_OWN + 8 * SM_SLOTS;          // u8[SM_SLOTS] touched by an accepted proposal
+constexpr size_t SMO_CKEY = SMO_TOUCH + SM_SLOTS;             // u64[SM_P] priority keys
+constexpr size_t SMO_CSLOT = SMO_CKEY + 8 * (size_t)SM_P;     // u16[SM_P][5] slots of the conflict nodes
+constexpr size_t SMO_ROUNDS_END = SMO_CSLOT + 10 * (size_t)SM_P;
+constexpr size_t SMO_H2 = SMO_OVER;                           // u32[SM_SLOTS] marked node ids
+constexpr size_t SMO_H2LOC = SMO_H2 + 4 * SM_SLOTS;           // u16[SM_SLOTS] their dense index
+constexpr size_t SMO_MID = SMO_H2LOC + 2 * SM_SLOTS;          // u32[SM_MARKED] node id
+constexpr size_t SMO_MFIRST = SMO_MID + 4 * SM_MARKED;        // u32[SM_MARKED] first_index
+constexpr size_t SMO_MARR = SMO_MFIRST + 4 * SM_MARKED;       // u32[SM_MARKED] marked children not yet refit
+constexpr size_t SMO_MBOX = SMO_MARR + 4 * SM_MARKED;         // float2[SM_MARKED][3] box
+constexpr size_t SMO_MPAR = SMO_MBOX + 24 * SM_MARKED;        // u16[SM_MARKED] parent's index
+constexpr size_t SMO_MCHILD = SMO_MPAR + 2 * SM_MARKED;       // u16[SM_MARKED][2] children's indices
+constexpr size_t SMO_MCNT = SMO_MCHILD + 4 * SM_MARKED;       // u8[SM_MARKED] marked children, 0x80 = leaf
+constexpr size_t SMO_MARKS_END = SMO_MCNT + SM_MARKED;
+constexpr size_t RESOLVE_SMEM =
+    ((SMO_ROUNDS_END > SMO_MARKS_END ? SMO_ROUNDS_END : SMO_MARKS_END) + 15) & ~(size_t)15;
+static_assert(SMO_OWN % 8 == 0 && SMO_CKEY % 8 == 0 && SMO_MBOX % 8 == 0, "aligned tables");
+static_assert(RESOLVE_SMEM <= 227 * 1024, "fits one block's shared memory");
+
+__device__ __forceinline__ uint32_t sm_hash(uint32_t id) { return (id * 0x9E3779B1u) >> (32 - SM_SLOT_BITS); }
+
+// Inserts node id `id` (linear probing); returns its slot and whether this
+// call inserted it, or SM_SLOTS when the table is full.
+__device__ __forceinline__ uint32_t sm_insert(uint32_t* key, uint32_t id, bool* fresh) {
+  uint32_t s = sm_hash(id);
+  for (uint32_t n = 0; n < SM_SLOTS; n++) {
+    const uint32_t old = atomicCAS(&key[s], OBVHS_INVALID, id);
+    if (old == OBVHS_INVALID || old == id) {
+      *fresh = old == OBVHS_INVALID;
+      return s;
+    }
+    s = (s + 1) & (SM_SLOTS - 1);
+  }
+  *fresh = false;
+  return SM_SLOTS;
+}
+
+// The slot of `id`, or SM_SLOTS; only after the insertions (a barrier).
+__device__ __forceinline__ uint32_t sm_find(const uint32_t* key, uint32_t id) {
+  uint32_t s = sm_hash(id);
+  for (uint32_t n = 0; n < SM_SLOTS; n++) {
+    const uint32_t k = key[s];
+    if (k == id) return s;
+    if (k == OBVHS_INVALID) return SM_SLOTS;
+    s = (s + 1) & (SM_SLOTS - 1);
+  }
+  return SM_SLOTS;
+}
+
+__device__ __forceinline__ Box sm_box(const float2* b, uint32_t l) {
+  const float2 p = b[3 * l], q = b[3 * l + 1], r = b[3 * l + 2];
+  return Box{make_float3(p.x, p.y, q.x), make_float3(q.y, r.x, r.y)};
+}
+__device__ __forceinline__ void sm_set_box(float2* b, uint32_t l, const Box& x) {
+  b[3 * l] = make_float2(x.mn.x, x.mn.y);
+  b[3 * l + 1] = make_float2(x.mn.z, x.mx.x);
+  b[3 * l + 2] = make_float2(x.mx.y, x.mx.z);
+}
+
+// Step 2 on shared-memory tables (P <= SM_P): the same rounds as
+// rounds_global, each round a check, a reset of the unresolved proposals'
+// claim words and a claim, with block barriers between them.
+__device__ __forceinline__ void rounds_shared(const ResolveArgs& a, uint32_t P, unsigned char* sm, uint32_t* s_rem) {
+  const uint32_t tid = threadIdx.x, nt = blockDim.x;
+  uint8_t* st = sm + SMO_STATE;
+  uint32_t* h1 = reinterpret_cast<uint32_t*>(sm + SMO_H1);
+  unsigned long long* own = reinterpret_cast<unsigned long long*>(sm + SMO_OWN);
+  uint8_t* touch = sm + SMO_TOUCH;
+  unsigned long long* ckey = reinterpret_cast<unsigned long long*>(sm + SMO_CKEY);
+  uint16_t* cslot = reinterpret_cast<uint16_t*>(sm + SMO_CSLOT);
+  for (uint32_t i = tid; i < SM_SLOTS; i += nt) {
+    h1[i] = OBVHS_INVALID;
+    own[i] = ~0ull;
+    touch[i] = 0;
+  }
+  __syncthreads();
+  for (uint32_t j = tid; j < P; j += nt) {
+    const Conf cf = load_conf(&a.conf[j]);
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+      bool fresh;
+      cslot[5 * j + q] = (uint16_t)sm_insert(h1, cf.c[q], &fresh);  // at most half full: never fails
+    }
+    ckey[j] = cf.key;
+    st[j] = 0;
+  }
+  __syncthreads();
+  uint32_t round = 0;
+  for (;; round++) {
+    for (uint32_t j = tid; j < P; j += nt) {
+      if (st[j] != 0) continue;
+      const uint16_t* cs = cslot + 5 * j;
+      bool hit = false;
+#pragma unroll
+      for (int q = 0; q < 5; q++) hit |= touch[cs[q]] != 0;
+      if (hit) {
+        st[j] = 2;
+        continue;
+      }
+      if (round > 0) {
+        const unsigned long long k = ckey[j];
+        bool all = true;
+#pragma unroll
+        for (int q = 0; q < 5; q++) all &= own[cs[q]] == k;
+        if (all) {
+          st[j] = 1;
+#pragma unroll
+          for (int q = 0; q < 5; q++) touch[cs[q]] = 1;
+        }
+      }
+    }
+    __syncthreads();
+    if (tid == 0) *s_rem = 0;  // every thread read the previous round's count before the barrier above
+    for (uint32_t j = tid; j < P; j += nt) {
+      if (st[j] != 0) continue;
+#pragma unroll
+      for (int q = 0; q < 5; q++) own[cslot[5 * j + q]] = ~0ull;
+    }
+    __syncthreads();
+    uint32_t rem = 0;
+    for (uint32_t j = tid; j < P; j += nt) {
+      if (st[j] != 0) continue;
+      const unsigned long long k = ckey[j];
+#pragma unroll
+      for (int q = 0; q < 5; q++) atomicMin(&own[cslot[5 * j + q]], k);
+      rem++;
+    }
+    if (rem) atomicAdd(s_rem, rem);
+    __syncthreads();
+    if (*(volatile uint32_t*)s_rem == 0) break;
+    if (round + 1 >= a.max_rounds) {
+      if (tid == 0) set_status(a.status, ST_ITER_LIMIT);
+      break;
+    }
+  }
+  if (tid == 0) a.ctr[4] = round + 1;
+}
+
+// Steps 4-5 on shared-memory tables.  Each start node climbs to the first
+// node already marked, inserting the nodes it passes; then every marked node
+// gets its parent's and its marked children's indices and the boxes of its
+// unmarked children (the final box when no child is marked, else the one
+// unmarked child's box); then climbs refit bottom-up, the last of a node's
+// marked children to finish (arrival count) refitting the node, unions taken
+// first child, second child as Bvh2::refit_from does.  Returns false, having
+// written nothing global, when more than SM_MARKED nodes are marked.
+template <class States>
+__device__ __forceinline__ bool mark_refit_shared(const ResolveArgs& a, uint32_t P, unsigned char* sm, States st,
+                                                  uint32_t* s_n, uint32_t* s_over) {
+  const uint32_t tid = threadIdx.x, nt = blockDim.x;
+  uint32_t* h2 = reinterpret_cast<uint32_t*>(sm + SMO_H2);
+  uint16_t* h2loc = reinterpret_cast<uint16_t*>(sm + SMO_H2LOC);
+  uint32_t* mid = reinterpret_cast<uint32_t*>(sm + SMO_MID);
+  uint32_t* mfirst = reinterpret_cast<uint32_t*>(sm + SMO_MFIRST);
+  uint32_t* marr = reinterpret_cast<uint32_t*>(sm + SMO_MARR);
+  float2* mbox = reinterpret_cast<float2*>(sm + SMO_MBOX);
+  uint16_t* mpar = reinterpret_cast<uint16_t*>(sm + SMO_MPAR);
+  uint16_t* mchild = reinterpret_cast<uint16_t*>(sm + SMO_MCHILD);
+  uint8_t* mcnt = sm + SMO_MCNT;
+  for (uint32_t i = tid; i < SM_SLOTS; i += nt) h2[i] = OBVHS_INVALID;
+  if (tid == 0) {
+    *s_n = 0;
+    *s_over = 0;
+  }
+  __syncthreads();
+  // marks: the moves of this block wrote `starts`, nodes and parents (plain
+  // loads see them after the barrier)
+  const uint32_t* start_slots = reinterpret_cast<const uint32_t*>(a.starts);
+  for (uint32_t i = tid; i < 2 * P; i += nt) {
+    if (st[i >> 1] != 1) continue;
+    uint32_t x = start_slots[i];
+    if (i & 1u) {
+      const uint32_t up = a.parents[x];
+      x = up != x ? up : OBVHS_INVALID;  // nothing above the root
+    }
+    for (uint32_t guard = 0; x != OBVHS_INVALID && guard <= SM_MARKED; guard++) {
+      const uint32_t up = a.parents[x];  // independent of the insertion: overlaps it
+      bool fresh;
+      const uint32_t s = sm_insert(h2, x, &fresh);
+      if (s == SM_SLOTS) {
+        *s_over = 1;
+        break;
+      }
+      if (!fresh) break;  // marked already: the climb that marked it goes on
+      const uint32_t l = atomicAdd(s_n, 1u);
+      if (l >= SM_MARKED) {
+        *s_over = 1;
+        break;
+      }
+      h2loc[s] = (uint16_t)l;
+      mid[l] = x;
+      if (up == x) break;  // the root
+      x = up;
+    }
+  }
+  __syncthreads();
+  if (*(volatile uint32_t*)s_over) return false;
+  const uint32_t n = *(volatile uint32_t*)s_n;
+  // links and the unmarked children's boxes
+  for (uint32_t l = tid; l < n; l += nt) {
+    const uint32_t x = mid[l];
+    const Bvh2Node xn = ld_node(&a.nodes[x]);
+    const uint32_t up = a.parents[x];
+    uint16_t pl = SM_NONE;
+    if (up != x) {
+      const uint32_t s = sm_find(h2, up);
+      if (s < SM_SLOTS) pl = h2loc[s];
+    }
+    mpar[l] = pl;
+    uint16_t c0 = SM_NONE, c1 = SM_NONE;
+    uint32_t cnt = 0;
+    Box b;
+    const uint32_t f = node_first(xn);
+    if (node_prims(xn) == 0) {
+      const uint32_t s0 = sm_find(h2, f), s1 = sm_find(h2, f + 1);
+      if (s0 < SM_SLOTS) c0 = h2loc[s0];
+      if (s1 < SM_SLOTS) c1 = h2loc[s1];
+      cnt = (c0 != SM_NONE) + (c1 != SM_NONE);
+      if (cnt == 0)
+        b = box_union(ld_box<true>(&a.nodes[f]), ld_box<true>(&a.nodes[f + 1]));
+      else if (cnt == 1)
+        b = ld_box<true>(&a.nodes[c0 == SM_NONE ? f : f + 1]);
+    } else {
+      b = node_box(xn);  // a leaf keeps its box
+    }
+    if (cnt < 2) sm_set_box(mbox, l, b);
+    mfirst[l] = f;
+    mchild[2 * l] = c0;
+    mchild[2 * l + 1] = c1;
+    marr[l] = cnt;
+    mcnt[l] = (uint8_t)(cnt | (node_prims(xn) ? 0x80u : 0u));
+  }
+  __syncthreads();
+  for (uint32_t l = tid; l < n; l += nt) {
+    const uint32_t c = mcnt[l];
+    if (c & 0x7fu) continue;  // a marked child's climb reaches it
+    uint32_t x = l;
+    if (!(c & 0x80u)) st_inner<true>(&a.nodes[mid[x]], sm_box(mbox, x), mfirst[x]);
+    for (uint32_t guard = 0; guard < n; guard++) {
+      const uint32_t p = mpar[x];
+      if (p == SM_NONE) break;
+      __threadfence_block();  // this climb's box before the arrival
+      if (atomicSub(&marr[p], 1u) != 1u) break;  // the other marked child's climb goes on
+      __threadfence_block();
+      const uint32_t c0 = mchild[2 * p], c1 = mchild[2 * p + 1];
+      const Box u = box_union(sm_box(mbox, c0 != SM_NONE ? c0 : p), sm_box(mbox, c1 != SM_NONE ? c1 : p));
+      sm_set_box(mbox, p, u);
+      st_inner<true>(&a.nodes[mid[p]], u, mfirst[p]);
+      x = p;
+    }
+  }
+  return true;
+}
+
+// Steps 2-5 by one block.
+__device__ __forceinline__ void resolve_block(const ResolveArgs& a, uint32_t P, unsigned char* sm, uint32_t* s_rem,
+                                              uint32_t* s_n, uint32_t* s_over) {
+  const uint32_t tid = threadIdx.x, nt = blockDim.x;
+  auto bar = [] { __syncthreads(); };
+  if (P <= SM_P) {
+    rounds_shared(a, P, sm, s_rem);
+    const SharedStates st{sm + SMO_STATE};
+    apply_moves(a, P, tid, nt, st);
+    __syncthreads();
+    if (!mark_refit_shared(a, P, sm, st, s_n, s_over)) mark_refit_global<true>(a, P, tid, nt, bar, st);
+  } else {
+    rounds_global(a, P, tid, nt, bar, s_rem);
+    const GlobalStates st{a.state};
+    apply_moves(a, P, tid, nt, st);
+    __syncthreads();
+    if (!mark_refit_shared(a, P, sm, st, s_n, s_over)) mark_refit_global<true>(a, P, tid, nt, bar, st);
   }
 }
 
@@ -635,25 +991,30 @@ __device__ __forceinline__ void resolve_body(const ResolveArgs& a, uint32_t P, u
 //      ancestors of the old parent of `from`
 //   5. refit the marked nodes bottom-up, starting from marked nodes without
 //      marked children.
-// A pass with at most RESOLVE_SMALL proposals runs in block 0 alone (block
-// barriers instead of grid barriers); the other blocks return at once and
-// take no part in any barrier.
+// A launch of one block, or a pass with at most SM_P proposals, runs in block
+// 0 alone (block barriers, shared-memory tables); the other blocks return at
+// once and take no part in any barrier.
 __global__ void __launch_bounds__(RESOLVE_THREADS) k_resolve(ResolveArgs a) {
   grid_dep_wait();
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ uint32_t s_rem, s_n, s_over;
+  const bool single = gridDim.x == 1;  // one block, launched normally
+  // 1. the proposals with a gain were listed by the search (emit_proposal)
+  const uint32_t P = *(volatile uint32_t*)&a.ctr[0];
+  if (single || P <= SM_P) {
+    if (blockIdx.x != 0) return;
+    resolve_block(a, P, sm, &s_rem, &s_n, &s_over);
+    return;
+  }
   cg::grid_group grid = cg::this_grid();
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
-  __shared__ uint32_t s_rem;
-
-  // 1. the proposals with a gain were listed by the search (emit_proposal)
-  const bool single = gridDim.x == 1;  // one block, launched normally
-  const uint32_t P = *(volatile uint32_t*)&a.ctr[0];
-  if (single || P <= RESOLVE_SMALL) {
-    if (blockIdx.x != 0) return;
-    resolve_body<true>(a, P, threadIdx.x, blockDim.x, [] { __syncthreads(); }, &s_rem);
-  } else {
-    resolve_body<false>(a, P, t0, stride, [&] { grid.sync(); }, &s_rem);
-  }
+  auto gsync = [&] { grid.sync(); };
+  rounds_global(a, P, t0, stride, gsync, &s_rem);
+  const GlobalStates st{a.state};
+  apply_moves(a, P, t0, stride, st);
+  grid.sync();
+  mark_refit_global<false>(a, P, t0, stride, gsync, st);
 }
 
 // Every scene's root is its own parent (k_parents covers node 0 only).
@@ -745,7 +1106,7 @@ int reins_pass(BuildCtx& c, Bvh2Node* nodes, uint32_t len, const uint32_t* cand,
   }
   if (!resolve_blocks) {
     int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resolve, RESOLVE_THREADS, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resolve, RESOLVE_THREADS, RESOLVE_SMEM));
     resolve_blocks = std::max(1, per_sm) * c.num_sms;
     resolve_blocks_s.store(resolve_blocks);
   }
@@ -775,15 +1136,21 @@ int reins_pass(BuildCtx& c, Bvh2Node* nodes, uint32_t len, const uint32_t* cand,
                                                std::max<uint64_t>(1, div_up<uint32_t>(count, RESOLVE_THREADS)));
   if (grid == 1 || count <= RESOLVE_SINGLE_MAX || gpu_shared(c)) {
     // one block, a normal launch (block barriers only)
-    KLAUNCH("k_resolve", launch_k(k_resolve, 1, RESOLVE_THREADS, 0, c.stream, ra));
+    KLAUNCH("k_resolve", launch_k(k_resolve, 1, RESOLVE_THREADS, RESOLVE_SMEM, c.stream, ra));
   } else {
-    KLAUNCH("k_resolve", CK(coop_launch(c, (const void*)k_resolve, grid, RESOLVE_THREADS, args, 0)));
+    KLAUNCH("k_resolve", CK(coop_launch(c, (const void*)k_resolve, grid, RESOLVE_THREADS, args, RESOLVE_SMEM)));
   }
   CK(cudaGetLastError());
   return 0;
 }
 
 }  // namespace
+
+int reinsertion_setup_kernels() {
+  return cudaFuncSetAttribute(k_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RESOLVE_SMEM) == cudaSuccess
+             ? 0
+             : -1;
+}
 
 int compute_parents_device(BuildCtx& c, const Bvh2Node* nodes, uint32_t n_nodes, uint32_t* parents,
                            uint32_t* unordered) {
