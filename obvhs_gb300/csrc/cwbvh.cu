@@ -1395,14 +1395,14 @@ int cwbvh_convert_device(BuildCtx& c, const obvhs_bvh2* b, uint32_t max_prims, i
     cudaFree(cwp);
     return c.fail(OBVHS_ERR_OOM, "scratch");
   }
-  static std::atomic<int> emit_blocks_s{0};
-  int emit_blocks = emit_blocks_s.load();
-  if (!emit_blocks) {
-    int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_all, EMIT_TB, 0));
-    emit_blocks = std::max(1, per_sm) * c.num_sms;
-    emit_blocks_s.store(emit_blocks);
+  static std::atomic<int> emit_per_sm_s{0};
+  int emit_per_sm = emit_per_sm_s.load();
+  if (!emit_per_sm) {
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&emit_per_sm, k_emit_all, EMIT_TB, 0));
+    emit_per_sm = std::max(1, emit_per_sm);
+    emit_per_sm_s.store(emit_per_sm);
   }
+  const int emit_blocks = emit_per_sm * c.num_sms;
   // queue: item 0 = the root, published; head = 0, tail = 1
   CK(cudaMemsetAsync(ready, 0, (size_t)n_cw * 4, c.stream));
   uint32_t* hst = (uint32_t*)c.h_small;
@@ -1569,14 +1569,14 @@ int cwbvh_seg_device(BuildCtx& c, const Bvh2Node* nodes, const uint32_t* pidx_in
   Item* items = (Item*)sc.get(SLOT_FRONTIER_A, (size_t)std::max(q_total, 1u) * sizeof(Item));
   uint32_t* ready = (uint32_t*)sc.get(SLOT_FRONTIER_B, (size_t)std::max(q_total, 1u) * 4);
   if (!items || !ready) return c.fail(OBVHS_ERR_OOM, "scratch");
-  static std::atomic<int> emit_blocks_s{0};
-  int emit_blocks = emit_blocks_s.load();
-  if (!emit_blocks) {
-    int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_all, EMIT_TB, 0));
-    emit_blocks = std::max(1, per_sm) * c.num_sms;
-    emit_blocks_s.store(emit_blocks);
+  static std::atomic<int> emit_per_sm_s{0};
+  int emit_per_sm = emit_per_sm_s.load();
+  if (!emit_per_sm) {
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&emit_per_sm, k_emit_all, EMIT_TB, 0));
+    emit_per_sm = std::max(1, emit_per_sm);
+    emit_per_sm_s.store(emit_per_sm);
   }
+  const int emit_blocks = emit_per_sm * c.num_sms;
   CK(cudaMemsetAsync(ready, 0, (size_t)q_total * 4, c.stream));
   KLAUNCH("k_seg_emit_init", launch_k(k_seg_emit_init, div_up<uint32_t>(S, BLK), BLK, 0, c.stream,
                                  L.d_prim_start, L.d_node_start, d_slots, S, n_roots, items, ready, counters + 12));
@@ -1621,14 +1621,14 @@ int cwbvh_order_children_device(BuildCtx& c, obvhs_cwbvh* b, const float* prims6
   CK(cudaMemcpyAsync(items, h, 4, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(ready, h + 1, 4, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(ctr, h + 2, 12, cudaMemcpyHostToDevice, c.stream));
-  static std::atomic<int> blocks_s{0};
-  int blocks = blocks_s.load();
-  if (!blocks) {
-    int per_sm = 0;
+  static std::atomic<int> per_sm_s{0};
+  int per_sm = per_sm_s.load();
+  if (!per_sm) {
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_order_children, EMIT_THREADS, 0));
-    blocks = std::max(1, per_sm) * c.num_sms;
-    blocks_s.store(blocks);
+    per_sm = std::max(1, per_sm);
+    per_sm_s.store(per_sm);
   }
+  const int blocks = per_sm * c.num_sms;
   OrderArgs oa{b->nodes, b->exact, b->prim_indices, prims6, n, n_prims, b->n_prims, direct_layout, items, ready, ctr,
                cap, node < 0 ? 1 : 0, c.d_status};
   const uint32_t grid =

@@ -2014,15 +2014,15 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   const uint32_t stop_at = cl_ctas ? (uint32_t)CL_CAP * cl_ctas : TAIL_MAX;
   if (n > stop_at) {
     const size_t smem = COOP_GROUPS * sizeof(CoopGroupSmem);
-    static std::atomic<int> coop_blocks_s{0};
-    int coop_blocks = coop_blocks_s.load();
-    if (!coop_blocks) {
+    static std::atomic<int> coop_per_sm_s{0};
+    int coop_per_sm = coop_per_sm_s.load();
+    if (!coop_per_sm) {
       CK(cudaFuncSetAttribute(k_ploc_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      int per_sm = 0;
-      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ploc_coop, COOP_GROUPS * PT, smem));
-      coop_blocks = std::max(1, per_sm) * c.num_sms;
-      coop_blocks_s.store(coop_blocks);
+      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&coop_per_sm, k_ploc_coop, COOP_GROUPS * PT, smem));
+      coop_per_sm = std::max(1, coop_per_sm);
+      coop_per_sm_s.store(coop_per_sm);
     }
+    const int coop_blocks = coop_per_sm * c.num_sms;
     const int lookback = n < LB_MAX ? 1 : 0;
     if (lookback) CK(cudaMemsetAsync(tile_cnt, 0, (size_t)div_up<uint32_t>(n, PT) * sizeof(uint2), c.stream));
     PlocCoopArgs pa{{cur, nxt}, out_nodes, st, merge, tile_cnt, (int)radius, depth_threshold, max_passes, c.d_status,
@@ -2138,16 +2138,16 @@ int ploc_seg_device(BuildCtx& c, const SegLayout& L, const Bvh2Node* leaves, con
                                  cur, L.d_prim_start, L.d_node_start, S, count, insert, d_passes, d_sum_counts, ctl, out));
   CK(cudaGetLastError());
   const size_t smem = COOP_GROUPS * sizeof(CoopGroupSmem) + ((size_t)S + 1) * 4;
-  static std::atomic<int> seg_blocks_s{0};
-  int seg_blocks = seg_blocks_s.load();
-  if (!seg_blocks) {
+  static std::atomic<int> seg_per_sm_s{0};
+  int seg_per_sm = seg_per_sm_s.load();
+  if (!seg_per_sm) {
     const size_t smem_max = COOP_GROUPS * sizeof(CoopGroupSmem) + ((size_t)SEG_MAX + 1) * 4;
     CK(cudaFuncSetAttribute(k_ploc_seg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
-    int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ploc_seg, COOP_GROUPS * PT, smem_max));
-    seg_blocks = std::max(1, per_sm) * c.num_sms;
-    seg_blocks_s.store(seg_blocks);
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&seg_per_sm, k_ploc_seg, COOP_GROUPS * PT, smem_max));
+    seg_per_sm = std::max(1, seg_per_sm);
+    seg_per_sm_s.store(seg_per_sm);
   }
+  const int seg_blocks = seg_per_sm * c.num_sms;
   PlocSegArgs pa{{cur, nxt}, out, merge, tile_cnt, L.d_prim_start, L.d_node_start, count, insert, d_passes,
                  d_sum_counts, ctl, S, (int)radius, depth_threshold, 2 * L.max_m + 64, c.d_status};
   void* args[] = {&pa};

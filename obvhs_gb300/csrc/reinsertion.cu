@@ -1096,20 +1096,19 @@ int reins_setup(BuildCtx& c, const Bvh2Node* nodes, uint32_t len, uint32_t nseq,
 // per-tree modes when `modes.mode` is set.
 int reins_pass(BuildCtx& c, Bvh2Node* nodes, uint32_t len, const uint32_t* cand, uint32_t count, uint32_t ri,
                bool clamp, uint32_t cap_rt, StackModes modes, const ReinsBufs& B) {
-  static std::atomic<int> find_blocks_s{0}, resolve_blocks_s{0};
-  int find_blocks = find_blocks_s.load(), resolve_blocks = resolve_blocks_s.load();
-  if (!find_blocks) {
-    int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_find_persistent<192, true>, FIND_THREADS, 0));
-    find_blocks = std::max(1, per_sm) * c.num_sms;
-    find_blocks_s.store(find_blocks);
+  static std::atomic<int> find_per_sm_s{0}, resolve_per_sm_s{0};
+  int find_per_sm = find_per_sm_s.load(), resolve_per_sm = resolve_per_sm_s.load();
+  if (!find_per_sm) {
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&find_per_sm, k_find_persistent<192, true>, FIND_THREADS, 0));
+    find_per_sm = std::max(1, find_per_sm);
+    find_per_sm_s.store(find_per_sm);
   }
-  if (!resolve_blocks) {
-    int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resolve, RESOLVE_THREADS, RESOLVE_SMEM));
-    resolve_blocks = std::max(1, per_sm) * c.num_sms;
-    resolve_blocks_s.store(resolve_blocks);
+  if (!resolve_per_sm) {
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resolve_per_sm, k_resolve, RESOLVE_THREADS, RESOLVE_SMEM));
+    resolve_per_sm = std::max(1, resolve_per_sm);
+    resolve_per_sm_s.store(resolve_per_sm);
   }
+  const int find_blocks = find_per_sm * c.num_sms, resolve_blocks = resolve_per_sm * c.num_sms;
   uint32_t* pass_ctr = B.counters + 8 + (size_t)ri * 8;  // [5]: next candidate for k_find
   const uint32_t fblocks = div_up<uint32_t>(count, FIND_THREADS);
   const ProposalOut po{B.reins, B.plist, B.conf, B.state, B.owner, pass_ctr};

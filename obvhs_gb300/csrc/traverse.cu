@@ -214,10 +214,12 @@ constexpr uint32_t REFILL_IDLE = 4;
 // per warp.  The lanes converge only at the refill.
 //
 // `yield` (or null): the device's count of builds in flight, in mapped host
-// memory.  While it is non-zero, warps of odd blocks stop taking rays (every
-// eighth refill checks it) and their blocks leave once their rays are done, so
-// a concurrent build's kernels find free slots on every SM instead of waiting
-// for the whole persistent grid; the even blocks take the remaining rays.
+// memory.  While it is non-zero, warps of odd blocks stop taking rays and
+// their blocks leave once their rays are done, so a concurrent build's
+// kernels find free slots on every SM instead of waiting for the whole
+// persistent grid; the even blocks take the remaining rays.  Lane 0 of a warp
+// of an odd block issues the read at every eighth refill and the warp acts on
+// the value at the next check, so the read is never waited for.
 template <class R, int TB = TBLK>
 __device__ __forceinline__ void persistent_rays(R& ray, uint32_t nrays, uint32_t* next_ray,
                                                 const uint32_t* yield = nullptr) {
@@ -229,10 +231,14 @@ __device__ __forceinline__ void persistent_rays(R& ray, uint32_t nrays, uint32_t
   bool alive = false;    // this lane holds a ray
   bool drained = false;  // (warp-uniform) the ray counter has run out
   uint32_t refills = 0;
+  uint32_t yw = 0;  // lane 0: the count read at the last check
   for (;;) {
     if (!drained && yield && (blockIdx.x & 1u)) {
       uint32_t y = 0;
-      if (lane == 0 && (++refills & 7u) == 0) y = *(volatile const uint32_t*)yield;
+      if (lane == 0 && (refills++ & 7u) == 0) {
+        y = yw;
+        asm volatile("ld.relaxed.sys.global.u32 %0, [%1];" : "=r"(yw) : "l"(yield));
+      }
       if (__shfl_sync(FULL, y, 0)) drained = true;
     }
     if (!drained) {

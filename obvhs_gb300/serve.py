@@ -474,7 +474,15 @@ def make_stream(n_requests: int, rate: float, scene_pool, ray_pool, rng, build_f
     return reqs, scene_of
 
 
-def summarize(requests) -> dict:
+def snapshot(requests) -> list:
+    """(kind, latency in s) of every request of a finished run."""
+    return [(r.kind, r.done - r.arrival) for r in requests]
+
+
+def summarize(requests, earlier=()) -> dict:
+    """Throughput and latency of a finished run.  `earlier`: snapshots of
+    earlier runs of the same stream, whose latencies join the percentiles
+    (throughput and span are this run's)."""
     def pct(v):
         if not len(v):
             return {}
@@ -491,10 +499,11 @@ def summarize(requests) -> dict:
     return {"requests": len(requests), "ray_requests": len(rays), "build_requests": len(builds),
             "rays": int(n_rays), "triangles_built": int(n_tris), "span_s": last - first,
             "mrays_s": n_rays / (last - first) / 1e6, "build_mtris_s": n_tris / (last - first) / 1e6,
-            "latency_rays": pct([r.done - r.arrival for r in rays]),
-            "latency_builds": pct([r.done - r.arrival for r in builds]),
-            "latency_all": pct([r.done - r.arrival for r in requests]),
-            "launch_steps": len({(r.kind, r.step) for r in requests})}
+            "latency_rays": pct([r.done - r.arrival for r in rays] + [l for s in earlier for k, l in s if k == "rays"]),
+            "latency_builds": pct([r.done - r.arrival for r in builds] +
+                                  [l for s in earlier for k, l in s if k == "build"]),
+            "latency_all": pct([r.done - r.arrival for r in requests] + [l for s in earlier for _, l in s]),
+            "launch_steps": len({(r.kind, r.step) for r in requests}), "runs": 1 + len(earlier)}
 
 
 def clustered_pools(n_scenes: int, max_tris: int, max_rays: int, seed: int = 1005, pin: bool = True):

@@ -116,6 +116,24 @@ def test_continuous_server_batches_and_matches_alone():
     assert summ["latency_rays"]["p99_ms"] >= summ["latency_rays"]["p50_ms"]
 
 
+def test_summary_pools_the_latencies_of_earlier_runs():
+    """Percentiles over several runs of one stream count every request of
+    every run; throughput and span are the last run's."""
+    reqs = [serve.Request(i, "rays", 0.001 * i, 0, rays=np.zeros((10, 8), np.float32)) for i in range(100)]
+    for r in reqs:
+        r.done = r.arrival + 0.001
+    first = serve.snapshot(reqs)
+    reqs[0].done = reqs[0].arrival + 1.0  # one stall in the last run
+    alone = serve.summarize(reqs)
+    pooled = serve.summarize(reqs, [first, first])
+    assert pooled["runs"] == 3 and alone["runs"] == 1
+    assert pooled["span_s"] == alone["span_s"] and pooled["mrays_s"] == alone["mrays_s"]
+    assert alone["latency_rays"]["max_ms"] == pooled["latency_rays"]["max_ms"] > 999
+    # 1 slow request of 100 sets the p99 of one run, not of 300 requests
+    assert alone["latency_rays"]["p99_ms"] > 10
+    assert pooled["latency_rays"]["p99_ms"] < 1.5
+
+
 def test_plain_server_one_call_per_request():
     reqs, _, pre, _ = _stream(3, n=120)
     b = FakeBackend()
