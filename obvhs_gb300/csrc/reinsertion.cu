@@ -565,6 +565,66 @@ __device__ __forceinline__ void rounds_global(const ResolveArgs& a, uint32_t P, 
                                               Sync sync, uint32_t* s_rem) {
   uint32_t* remaining = a.ctr + 1;
   uint32_t round = 0;
+  if (P <= nthreads) {
+    // At most one proposal per thread: its conflict set, key and state stay
+    // in registers through the rounds, the touched and claim words are
+    // loaded together, and warps add their unresolved counts directly.
+    const bool mine = t0 < P;
+    Conf cf{};
+    uint32_t st = 1;  // no proposal: resolved
+    if (mine) {
+      cf = load_conf(&a.conf[t0]);
+      st = a.state[t0];
+    }
+    for (;; round++) {
+      const unsigned long long* prev = a.owner + (size_t)((round + 2) % 3) * a.n_nodes;
+      unsigned long long* cur = a.owner + (size_t)(round % 3) * a.n_nodes;
+      unsigned long long* nxt = a.owner + (size_t)((round + 1) % 3) * a.n_nodes;
+      if (t0 == 0) remaining[(round + 1) % 3] = 0;
+      uint32_t rem = 0;
+      if (st == 0) {
+        uint32_t tw[5];
+        unsigned long long pw[5];
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+          tw[q] = __ldcg(&a.touched[cf.c[q]]);
+          pw[q] = round > 0 ? __ldcg(&prev[cf.c[q]]) : 0ull;
+        }
+        bool hit = false, own = round > 0;
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+          hit |= tw[q] == a.stamp;
+          own &= pw[q] == cf.key;
+        }
+        if (hit) {
+          st = 2;
+        } else if (own) {
+          st = 1;
+#pragma unroll
+          for (int q = 0; q < 5; q++) a.touched[cf.c[q]] = a.stamp;
+        } else {
+#pragma unroll
+          for (int q = 0; q < 5; q++) {
+            atomicMin(&cur[cf.c[q]], cf.key);
+            nxt[cf.c[q]] = ~0ull;
+          }
+          rem = 1;
+        }
+      }
+      rem = __reduce_add_sync(0xffffffffu, rem);
+      if ((threadIdx.x & 31) == 0 && rem) atomicAdd(&remaining[round % 3], rem);
+      sync();
+      const uint32_t left = *(volatile uint32_t*)&remaining[round % 3];
+      if (left == 0) break;
+      if (round + 1 >= a.max_rounds) {
+        if (t0 == 0) set_status(a.status, ST_ITER_LIMIT);
+        break;
+      }
+    }
+    if (mine) a.state[t0] = (uint8_t)st;
+    if (t0 == 0) a.ctr[4] = round + 1;
+    return;
+  }
   for (;; round++) {
     const unsigned long long* prev = a.owner + (size_t)((round + 2) % 3) * a.n_nodes;
     unsigned long long* cur = a.owner + (size_t)(round % 3) * a.n_nodes;
