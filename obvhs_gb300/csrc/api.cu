@@ -461,6 +461,14 @@ DeviceShared& device_shared(int device) {
 
 }  // namespace
 
+bool resolve_tables_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("OBVHS_RESOLVE_TABLES");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 bool pdl_enabled() {
   static const bool on = [] {
     const char* e = std::getenv("OBVHS_PDL");

@@ -244,6 +244,10 @@ inline bool gpu_shared(const obvhs_ctx& c) { return c.shared_gpu || device_concu
 // launches are switched off (OBVHS_PDL=0 in the environment).  Errors are
 // returned and, like a <<<>>> launch, recorded for cudaGetLastError.
 bool pdl_enabled();
+// Whether one-block reinsertion resolves use their shared-memory tables
+// (OBVHS_RESOLVE_TABLES=0 in the environment selects the global-memory forms,
+// for testing them; read once per process).
+bool resolve_tables_enabled();
 template <class... P, class... A>
 inline cudaError_t launch_k(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A&&... args) {
   cudaLaunchConfig_t cfg = {};

@@ -428,6 +428,7 @@ struct ResolveArgs {
   uint32_t stamp;             // pass number, from 1: per-node words from earlier passes read as unset
   uint32_t n_nodes;
   uint32_t max_rounds;
+  uint32_t tables;            // one-block passes may use the shared-memory tables
 };
 
 __device__ __forceinline__ Conf load_conf(const Conf* p) {
@@ -1027,7 +1028,7 @@ __device__ __forceinline__ void resolve_block(const ResolveArgs& a, uint32_t P, 
                                               uint32_t* s_n, uint32_t* s_over) {
   const uint32_t tid = threadIdx.x, nt = blockDim.x;
   auto bar = [] { __syncthreads(); };
-  if (P <= SM_P) {
+  if (a.tables && P <= SM_P) {
     rounds_shared(a, P, sm, s_rem);
     const SharedStates st{sm + SMO_STATE};
     apply_moves(a, P, tid, nt, st);
@@ -1038,7 +1039,7 @@ __device__ __forceinline__ void resolve_block(const ResolveArgs& a, uint32_t P, 
     const GlobalStates st{a.state};
     apply_moves(a, P, tid, nt, st);
     __syncthreads();
-    if (!mark_refit_shared(a, P, sm, st, s_n, s_over)) mark_refit_global<true>(a, P, tid, nt, bar, st);
+    if (!a.tables || !mark_refit_shared(a, P, sm, st, s_n, s_over)) mark_refit_global<true>(a, P, tid, nt, bar, st);
   }
 }
 
@@ -1189,7 +1190,8 @@ int reins_pass(BuildCtx& c, Bvh2Node* nodes, uint32_t len, const uint32_t* cand,
   CK(cudaGetLastError());
   // conflict resolution, moves and refit in one launch
   ResolveArgs ra{nodes,    B.parents, B.reins, count,  B.plist,     B.conf,     B.state,  B.owner,  B.touched,
-                 B.dirty,  B.arrive,  B.starts, pass_ctr, B.counters + 1, c.d_status, ri + 1, len, count + 3};
+                 B.dirty,  B.arrive,  B.starts, pass_ctr, B.counters + 1, c.d_status, ri + 1, len, count + 3,
+                 resolve_tables_enabled() ? 1u : 0u};
   void* args[] = {&ra};
   uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)resolve_blocks,
                                                std::max<uint64_t>(1, div_up<uint32_t>(count, RESOLVE_THREADS)));

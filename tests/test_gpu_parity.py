@@ -504,3 +504,26 @@ def test_dependent_launches_off_gives_the_same_tree(G, tmp_path):
     env = dict(os.environ, OBVHS_PDL="0")
     subprocess.run([sys.executable, "-c", code], env=env, check=True, timeout=300)
     assert _eq(np.load(tmp_path / "n.npy"), nodes) and _eq(np.load(tmp_path / "i.npy"), pidx)
+
+
+@pytest.mark.parametrize("preset", ["slow_build", "very_slow_build"])
+def test_reinsertion_global_forms_give_the_same_tree(G, tmp_path, preset):
+    """OBVHS_RESOLVE_TABLES=0: the one-block reinsertion passes resolve on the
+    global claim arrays and the global mark and refit (the forms used when the
+    shared-memory tables overflow) and build the same bytes as the default
+    (read once per process, so that form runs in a child process)."""
+    import subprocess
+    import sys
+
+    tris = S.scene2_tris(200_000)
+    nodes, pidx = G.build_cwbvh_from_tris(tris, getattr(BvhBuildParams, preset)()).download()
+    np.save(tmp_path / "tris.npy", tris)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import sys, numpy as np; sys.path.insert(0, %r); import obvhs_gb300 as G; "
+            "from obvhs_gb300.params import BvhBuildParams as P; "
+            "n, i = G.build_cwbvh_from_tris(np.load(%r), P.%s()).download(); "
+            "np.save(%r, n); np.save(%r, i)") % (root, str(tmp_path / "tris.npy"), preset, str(tmp_path / "n.npy"),
+                                                 str(tmp_path / "i.npy"))
+    env = dict(os.environ, OBVHS_RESOLVE_TABLES="0")
+    subprocess.run([sys.executable, "-c", code], env=env, check=True, timeout=300)
+    assert _eq(np.load(tmp_path / "n.npy"), nodes) and _eq(np.load(tmp_path / "i.npy"), pidx)
