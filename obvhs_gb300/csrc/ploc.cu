@@ -596,6 +596,7 @@ struct CoopGroupSmem {
   int8_t merge[PCHUNK + 2 * 32];
   uint32_t w[PT / 32];
   uint32_t red[2][PT / 32];
+  uint32_t pw[2 * BOXS];  // ploc_tile_fused: prim_count, then first_index, of the staged nodes
 };
 
 __device__ __forceinline__ void group_sync(int group) {
@@ -814,13 +815,15 @@ __device__ __forceinline__ uint2 ploc_tile_fused(CoopGroupSmem& sm, int group, c
   for (uint32_t k = tid; k < box_span; k += PT) {
     const int64_t j = box_lo + k;
     if (j >= 0 && j < (int64_t)count) {
-      const Box b = load_box_cg(&cur[j]);
-      sm.box[0 * BOXS + k] = b.mn.x;
-      sm.box[1 * BOXS + k] = b.mn.y;
-      sm.box[2 * BOXS + k] = b.mn.z;
-      sm.box[3 * BOXS + k] = b.mx.x;
-      sm.box[4 * BOXS + k] = b.mx.y;
-      sm.box[5 * BOXS + k] = b.mx.z;
+      const Bvh2Node nd = ld_node_cg(&cur[j]);  // the whole node: the writes below take it from here
+      sm.box[0 * BOXS + k] = nd.a.x;
+      sm.box[1 * BOXS + k] = nd.a.y;
+      sm.box[2 * BOXS + k] = nd.a.z;
+      sm.box[3 * BOXS + k] = nd.b.x;
+      sm.box[4 * BOXS + k] = nd.b.y;
+      sm.box[5 * BOXS + k] = nd.b.z;
+      sm.pw[k] = __float_as_uint(nd.a.w);
+      sm.pw[BOXS + k] = __float_as_uint(nd.b.w);
     }
   }
   group_sync(group);
@@ -957,6 +960,14 @@ __device__ __forceinline__ uint2 ploc_tile_fused(CoopGroupSmem& sm, int group, c
   }
   group_sync(group);
   const uint32_t pre_e = sm.red[0][0], pre_m = sm.red[1][0];
+  // a staged node (the tile and its halo: every cluster written below and its merge partner)
+  auto staged = [&](uint32_t jj) {
+    const int q = (int)jj - lo32;
+    Bvh2Node n;
+    n.a = make_float4(sm.box[0 * BOXS + q], sm.box[1 * BOXS + q], sm.box[2 * BOXS + q], __uint_as_float(sm.pw[q]));
+    n.b = make_float4(sm.box[3 * BOXS + q], sm.box[4 * BOXS + q], sm.box[5 * BOXS + q], __uint_as_float(sm.pw[BOXS + q]));
+    return n;
+  };
   const uint32_t excl = wpre + x - packed;
   uint32_t epos = pre_e + (excl & 0xffffu), mpos = pre_m + (excl >> 16);
 #pragma unroll
@@ -964,8 +975,7 @@ __device__ __forceinline__ uint2 ploc_tile_fused(CoopGroupSmem& sm, int group, c
     const uint32_t i = base + tid * ipt + k;
     if (!emit[k]) continue;
     if (ism[k]) {
-      const Bvh2Node left = ld_node_cg(&cur[i]);
-      const Bvh2Node right = ld_node_cg(&cur[bst[k]]);
+      const Bvh2Node left = staged(i), right = staged(bst[k]);
       uint32_t ins = ins_top - 2 * (mpos + 1);
       if (remap) ins = __ldg(&remap[(ins - 1) >> 1]);  // the k-th free pair of a partial rebuild
       st_node(&out[ins], left);
@@ -973,7 +983,7 @@ __device__ __forceinline__ uint2 ploc_tile_fused(CoopGroupSmem& sm, int group, c
       st_node(&next[epos], make_node(box_union(node_box(left), node_box(right)), 0, ins));
       mpos++;
     } else {
-      st_node(&next[epos], ld_node_cg(&cur[i]));
+      st_node(&next[epos], staged(i));
     }
     epos++;
   }
