@@ -1345,6 +1345,10 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_ploc_tail(const Bvh2Node* __re
     s_insert = st->insert[s_pass & 1u];
   }
   __syncthreads();
+  if (s_count > TAIL_MAX) {  // the passes before ended early (their error is set)
+    if (tid == 0) set_status(status, ST_ITER_LIMIT);
+    return;
+  }
   const int parity = (int)(s_pass & 1u);
   const Bvh2Node* __restrict__ cur_g = parity ? buf1 : buf0;
   uint32_t count = s_count;
@@ -1484,10 +1488,16 @@ constexpr int CL_HALO = 64;           // 2 x the largest search radius
 constexpr int CL_STRIDE = CL_CAP + 2 * CL_HALO;  // words per array of a window
 constexpr uint32_t CL_MIN_SLICE = 128;  // >= CL_HALO
 constexpr int CL_IT = CL_CAP / CL_THREADS;       // slice clusters per thread
+// The cluster kernel hands over to the single-CTA tail at this many live
+// clusters: below it a pass on one CTA (block barriers, about 1 us plus the
+// search) costs less than a pass on the cluster (two cluster barriers, about
+// 5 us however few clusters are left).
+constexpr uint32_t CL_TAIL_AT = 1024;
+static_assert(CL_TAIL_AT <= TAIL_MAX, "the tail holds every cluster handed to it");
 
 struct ClusterArgs {
-  const Bvh2Node* buf0;
-  const Bvh2Node* buf1;
+  Bvh2Node* buf0;
+  Bvh2Node* buf1;
   PlocState* st;
   int radius;
   uint32_t depth_threshold;
@@ -1497,6 +1507,7 @@ struct ClusterArgs {
   const uint32_t* remap;
   int fast;
   uint32_t* pass_ins;  // the insert index at each pass's start (first PLOC_PASS_REC passes), or null
+  uint32_t tail_at;    // hand the passes to the single-CTA tail once this few clusters are live (0: never)
 };
 
 // The window: eight word arrays of CL_STRIDE (as the tail's), the slice at
@@ -1603,7 +1614,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_ploc_cluster(ClusterArgs a) {
   cluster.sync();
   int cur = 0;
   uint64_t sum = 0;
-  for (uint32_t iters = 0; count > 1; iters++) {
+  for (uint32_t iters = 0; count > 1 && count > a.tail_at; iters++) {
     if (iters >= a.max_passes) {
       if (me == 0 && tid == 0) set_status(a.status, ST_ITER_LIMIT);
       break;
@@ -1764,6 +1775,30 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_ploc_cluster(ClusterArgs a) {
     pass++;
     cur ^= 1;
     cluster.sync();  // the next pass's slices are complete
+  }
+  if (count > 1 && count <= a.tail_at) {
+    // few clusters left: every CTA writes its slice to the pass's buffer and
+    // the single-CTA tail (launched next) finishes, its passes costing block
+    // barriers instead of cluster barriers
+    uint32_t act, sl;
+    cl_split(count, ncta, act, sl);
+    const uint32_t base = me * sl;
+    const uint32_t len = me < act ? min(sl, count - base) : 0;
+    Bvh2Node* dst = (pass & 1u) ? a.buf1 : a.buf0;
+    for (uint32_t j = tid; j < len; j += CL_THREADS) {
+      float4 qa, qb;
+      wget(win[cur], CL_HALO + (int)j, qa, qb);
+      float4* o = reinterpret_cast<float4*>(&dst[base + j]);
+      o[0] = qa;
+      o[1] = qb;
+    }
+    if (me == 0 && tid == 0) {
+      a.st->count[pass & 1u] = count;
+      a.st->insert[pass & 1u] = insert;
+      a.st->passes = pass;
+      a.st->sum_counts += sum;
+    }
+    return;
   }
   if (me == 0 && tid == 0) {
     if (a.pass_ins && pass < PLOC_PASS_REC) a.pass_ins[pass] = insert;
@@ -2049,7 +2084,7 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   }
   if (cl_ctas) {
     ClusterArgs ca{cur, nxt, st, (int)radius, depth_threshold, max_passes, out_nodes, c.d_status, remap,
-                   nan_checked ? 1 : 0, pass_ins};
+                   nan_checked ? 1 : 0, pass_ins, CL_TAIL_AT};
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)cl_ctas);
     cfg.blockDim = dim3(CL_THREADS);
@@ -2065,7 +2100,8 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
     cfg.attrs = at;
     cfg.numAttrs = pdl_enabled() ? 2 : 1;
     KLAUNCH("k_ploc_cluster", CK(cudaLaunchKernelEx(&cfg, k_ploc_cluster, ca)));
-  } else {
+  }
+  {
     const size_t smem = (size_t)4 * TAIL_MAX * sizeof(float4) + TAIL_MAX + 64;
     KLAUNCH("k_ploc_tail", launch_k(k_ploc_tail, 1, TAIL_THREADS, smem, c.stream, cur, nxt, st, (int)radius, depth_threshold,
                                                                            max_passes, out_nodes, c.d_status, remap,

@@ -45,3 +45,25 @@ def test_slices_and_halos_fit():
             for total in {1, max(1, count // 2), count}:
                 a2, s2 = _split(total, ncta, min_slice)
                 assert (total - 1) // s2 < a2 and s2 <= cap
+
+
+def test_hand_off_to_the_single_cta_tail_fits_it():
+    """The cluster kernel writes its slices back and hands the last passes to
+    the single-CTA tail at CL_TAIL_AT live clusters: the tail's shared memory
+    holds TAIL_MAX clusters, and the written slices cover [0, count) exactly
+    (each CTA writes min(slice, count - base) clusters at base)."""
+    src = open(CSRC).read()
+    hdr = open(os.path.join(os.path.dirname(CSRC), "build.h")).read()
+    tail_at = _const(src, "CL_TAIL_AT")
+    tail_max = _const(hdr, "TAIL_MAX")
+    min_slice = _const(src, "CL_MIN_SLICE")
+    assert 1 < tail_at <= tail_max
+    for ncta in (8, 16):
+        for count in range(2, tail_at + 1):
+            act, sl = _split(count, ncta, min_slice)
+            covered = []
+            for me in range(ncta):
+                base = me * sl
+                n = min(sl, count - base) if me < act else 0
+                covered.extend(range(base, base + n))
+            assert covered == list(range(count))
