@@ -551,6 +551,7 @@ constexpr int PT = 256;
 constexpr int PITEMS = 4;
 constexpr int PCHUNK = PT * PITEMS;
 constexpr int BOXS = PCHUNK + 4 * 32;  // staged boxes per tile: the tile and a 2 * radius halo each side
+constexpr int TILE_MIN = PT - 2 * 32;  // the smallest tile (tile_chunk at ipt 1, radius 32)
 
 // --- all large passes in one cooperative launch ------------------------------
 //
@@ -558,7 +559,7 @@ constexpr int BOXS = PCHUNK + 4 * 32;  // staged boxes per tile: the tile and a 
 // of COOP_GROUPS x PT threads per SM (its registers fill the SM); each group
 // of PT threads works on its own tiles with its own shared memory and named
 // barrier, and tile t goes to block t % G, so consecutive tiles land on
-// different SMs.  A tile holds PT * ipt clusters, ipt = 4, 2 or 1 chosen per
+// different SMs.  A tile holds PT * ipt - 2r clusters, ipt = 4, 2 or 1 chosen per
 // pass so that small passes still spread over the GPU.  Per pass:
 //   A  each tile computes the merge offsets of its clusters from boxes staged
 //      with a 2*radius halo (offsets of the +-radius neighbours are recomputed
@@ -681,7 +682,7 @@ __device__ __forceinline__ void ploc_tile_offsets(CoopGroupSmem& sm, int group, 
 #pragma unroll
   for (int k = 0; k < PITEMS; k++) {
     const uint32_t i = base + tid * ipt + k;
-    if (k < ipt && i < count) {
+    if (k < ipt && i < count && i < base + chunk) {
       const int off = sm.merge[(int64_t)i - m_lo];
       const uint32_t b = (uint32_t)((int)i + off);
       const bool mutual = (int)b + (int)sm.merge[(int64_t)b - m_lo] == (int)i;
@@ -707,7 +708,7 @@ __device__ __forceinline__ void ploc_tile_offsets(CoopGroupSmem& sm, int group, 
 // list's (emitted, merged) totals through the end of this tile.
 __device__ __forceinline__ uint2 ploc_tile_write(CoopGroupSmem& sm, int group, const Bvh2Node* cur, Bvh2Node* next,
                                                  Bvh2Node* out, const int8_t* merge, uint32_t count, uint32_t base,
-                                                 int ipt, const uint2* tile_cnt, uint32_t t_first, uint32_t tile,
+                                                 uint32_t chunk, int ipt, const uint2* tile_cnt, uint32_t t_first, uint32_t tile,
                                                  uint32_t ins_top, const uint32_t* remap = nullptr) {
   const int tid = threadIdx.x % PT, lane = tid & 31, warp = tid >> 5;
   uint32_t pe = 0, pm = 0;
@@ -735,7 +736,7 @@ __device__ __forceinline__ uint2 ploc_tile_write(CoopGroupSmem& sm, int group, c
     const uint32_t i = base + tid * ipt + k;
     emit[k] = ism[k] = false;
     bst[k] = i;
-    if (k < ipt && i < count) {
+    if (k < ipt && i < count && i < base + chunk) {
       const int off = __ldcg(&merge[i]);
       const uint32_t b = (uint32_t)((int)i + off);
       const bool mutual = (int)b + (int)__ldcg(&merge[b]) == (int)i;
@@ -883,7 +884,7 @@ __device__ __forceinline__ uint2 ploc_tile_fused(CoopGroupSmem& sm, int group, c
     const uint32_t i = base + tid * ipt + k;
     emit[k] = ism[k] = false;
     bst[k] = i;
-    if (k < ipt && i < count) {
+    if (k < ipt && i < count && i < base + chunk) {
       const int off = sm.merge[(int64_t)i - m_lo];
       const uint32_t b = (uint32_t)((int)i + off);
       const bool mutual = (int)b + (int)sm.merge[(int64_t)b - m_lo] == (int)i;
@@ -994,6 +995,11 @@ __device__ __forceinline__ int tile_ipt(uint32_t live, uint32_t groups) {
   return live >= groups * (uint32_t)PCHUNK ? PITEMS : live >= groups * (uint32_t)(PT * 2) ? 2 : 1;
 }
 
+// Clusters per tile: PT * ipt less the offsets' radius halo on both sides,
+// so that the offsets a tile computes (its clusters and r either side) are
+// exactly PT * ipt, whole rounds of the group's threads.
+__device__ __forceinline__ uint32_t tile_chunk(int ipt, int r) { return (uint32_t)(PT * ipt - 2 * r); }
+
 __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs a) {
   grid_dep_wait();
   cg::grid_group grid = cg::this_grid();
@@ -1022,7 +1028,7 @@ __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs 
     const bool d1 = a.radius == 1 || pass < a.depth_threshold;
     const int r = d1 ? 1 : a.radius;
     const int ipt = tile_ipt(count, G * COOP_GROUPS);
-    const uint32_t chunk = (uint32_t)PT * ipt;
+    const uint32_t chunk = tile_chunk(ipt, r);
     const uint32_t ntiles = div_up<uint32_t>(count, chunk);
 
     if (a.lookback) {
@@ -1057,7 +1063,7 @@ __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_coop(PlocCoopArgs 
     // B: offsets and writes
     const uint32_t ins_top = *(volatile uint32_t*)&a.st->insert[parity];
     for (uint32_t tile = first_tile; tile < ntiles; tile += tile_step) {
-      const uint2 tot = ploc_tile_write(sm, group, cur, next, a.out, a.merge, count, tile * chunk, ipt, a.tile_cnt, 0,
+      const uint2 tot = ploc_tile_write(sm, group, cur, next, a.out, a.merge, count, tile * chunk, chunk, ipt, a.tile_cnt, 0,
                                         tile, ins_top, a.remap);
       if (tid == 0 && tile == ntiles - 1) {
         a.st->count[parity ^ 1] = tot.x;
@@ -1187,7 +1193,7 @@ __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_seg(PlocSegArgs a)
     const bool d1 = a.radius == 1 || pass < a.depth_threshold;
     const int r = d1 ? 1 : a.radius;
     const int ipt = tile_ipt(live, G * COOP_GROUPS);
-    const uint32_t chunk = (uint32_t)PT * ipt;
+    const uint32_t chunk = tile_chunk(ipt, r);
     block_scan_into(
         tstart, S,
         [&](uint32_t s) {
@@ -1213,7 +1219,7 @@ __global__ void __launch_bounds__(COOP_GROUPS * PT, 1) k_ploc_seg(PlocSegArgs a)
       const uint32_t count = __ldcg(&cnt[s]);
       const uint32_t ins_top = __ldcg(&insert[s]);
       const uint2 tot = ploc_tile_write(sm, group, cur + cb, next + cb, a.out, a.merge + cb, count,
-                                        (tile - tstart[s]) * chunk, ipt, a.tile_cnt, tstart[s], tile, ins_top);
+                                        (tile - tstart[s]) * chunk, chunk, ipt, a.tile_cnt, tstart[s], tile, ins_top);
       if (tile == tstart[s + 1] - 1) {  // the scene's last tile
         if (tid == 0) {
           a.count[(size_t)(parity ^ 1) * S + s] = tot.x;
@@ -2041,7 +2047,7 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
   }
   Bvh2Node* nxt = (Bvh2Node*)s.get(SLOT_PLOC_B, (size_t)n * sizeof(Bvh2Node));
   int8_t* merge = (int8_t*)s.get(SLOT_MERGE, (size_t)n);
-  uint2* tile_cnt = (uint2*)s.get(SLOT_PARTIAL, (size_t)div_up<uint32_t>(n, PT) * sizeof(uint2));
+  uint2* tile_cnt = (uint2*)s.get(SLOT_PARTIAL, (size_t)div_up<uint32_t>(n, TILE_MIN) * sizeof(uint2));
   PlocState* st = (PlocState*)s.get(SLOT_PLOC_STATE, sizeof(PlocState));
   // the pass ranges (not for a partial rebuild, whose pairs go to free slots)
   uint32_t* pass_ins = remap ? nullptr : (uint32_t*)s.get(SLOT_PLOC_PASSES, (size_t)PLOC_PASS_REC * 4);
@@ -2069,7 +2075,7 @@ int ploc_build_device(BuildCtx& c, Bvh2Node* leaves, uint32_t n, const int* tota
     }
     const int coop_blocks = coop_per_sm * c.num_sms;
     const int lookback = n < LB_MAX ? 1 : 0;
-    if (lookback) CK(cudaMemsetAsync(tile_cnt, 0, (size_t)div_up<uint32_t>(n, PT) * sizeof(uint2), c.stream));
+    if (lookback) CK(cudaMemsetAsync(tile_cnt, 0, (size_t)div_up<uint32_t>(n, TILE_MIN) * sizeof(uint2), c.stream));
     PlocCoopArgs pa{{cur, nxt}, out_nodes, st, merge, tile_cnt, (int)radius, depth_threshold, max_passes, c.d_status,
                     remap, nan_checked ? 1 : 0, stop_at, lookback, pass_ins};
     void* args[] = {&pa};
@@ -2172,7 +2178,7 @@ int ploc_seg_device(BuildCtx& c, const SegLayout& L, const Bvh2Node* leaves, con
   Bvh2Node* cur = (Bvh2Node*)s.get(SLOT_PLOC_A, (size_t)n * sizeof(Bvh2Node));
   Bvh2Node* nxt = (Bvh2Node*)s.get(SLOT_PLOC_B, (size_t)n * sizeof(Bvh2Node));
   int8_t* merge = (int8_t*)s.get(SLOT_MERGE, (size_t)n);
-  uint2* tile_cnt = (uint2*)s.get(SLOT_PARTIAL, ((size_t)div_up<uint32_t>(n, PT) + S + 1) * sizeof(uint2));
+  uint2* tile_cnt = (uint2*)s.get(SLOT_PARTIAL, ((size_t)div_up<uint32_t>(n, TILE_MIN) + S + 1) * sizeof(uint2));
   uint32_t* st = (uint32_t*)s.get(SLOT_PLOC_STATE, ((size_t)4 * S + 8) * 4);
   if (!cur || !nxt || !merge || !tile_cnt || !st) return c.fail(OBVHS_ERR_OOM, "scratch");
   uint32_t* ctl = st;
