@@ -447,7 +447,11 @@ __global__ void __launch_bounds__(BLK, 4) k_costs_ranges(CostRangeArgs a, uint32
   if (large == 0) grid.sync();
   for (uint32_t p = 0; p < large; p++) {
     const uint32_t hi = a.pass_ins[p], lo = a.pass_ins[p + 1];
-    for (uint32_t i = lo + me; i < hi; i += nthreads) cost_node_ready(a, i);
+    for (uint32_t i = lo + me; i < hi; i += nthreads) {
+      // this thread's next node to L1 while this one waits on its children
+      if (i + nthreads < hi) asm volatile("prefetch.global.L1 [%0];" ::"l"(&a.nodes[i + nthreads]));
+      cost_node_ready(a, i);
+    }
     grid.sync();
   }
   costs_ordered(a.nodes, nullptr, a.pidx_in, top, a.max_prims, a.crec, a.erec, a.small, flags, next, a.status, a.n);
