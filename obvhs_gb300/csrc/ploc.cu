@@ -25,6 +25,7 @@
 #include <atomic>
 
 #include "build.h"
+#include "morton_grid.h"
 #include "radix_sort.cuh"
 
 namespace cg = cooperative_groups;
@@ -186,7 +187,11 @@ __device__ __forceinline__ void split3_u128(unsigned long long a, unsigned long 
 // multiplication fewer per coordinate.
 struct Scale {
   double sx, sy, sz, ox, oy, oz;
+  MortonAxis fx, fy, fz;  // the 64-bit grid's float pieces (morton_grid.h); not ok for the 128-bit grid
 };
+constexpr double GRID64 = (double)(1u << 21);
+constexpr double GRID128 = (double)(1ull << 42);
+
 __device__ __forceinline__ Scale make_scale(const int* tk, double grid) {
   float mnx = fkey_inv(tk[0]), mny = fkey_inv(tk[1]), mnz = fkey_inv(tk[2]);
   float mxx = fkey_inv(tk[3]), mxy = fkey_inv(tk[4]), mxz = fkey_inv(tk[5]);
@@ -198,17 +203,28 @@ __device__ __forceinline__ Scale make_scale(const int* tk, double grid) {
   s.ox = (-(double)mnx * sx) * grid;
   s.oy = (-(double)mny * sy) * grid;
   s.oz = (-(double)mnz * sz) * grid;
+  if (grid == GRID64) {
+    s.fx = morton_axis(s.sx, s.ox);
+    s.fy = morton_axis(s.sy, s.oy);
+    s.fz = morton_axis(s.sz, s.oz);
+  } else {
+    s.fx.ok = s.fy.ok = s.fz.ok = 0;  // values up to 2^42: beyond the float pieces' precision (unused)
+  }
   return s;
 }
-constexpr double GRID64 = (double)(1u << 21);
-constexpr double GRID128 = (double)(1ull << 42);
+
+// sat_u32(RN(RN(c * S) + O)) (sat_u32 above): from float pieces where
+// morton_floor_fast decides the floor, else on the double-precision pipe.
+__device__ __forceinline__ uint32_t grid_coord64(float c, double S, double O, const MortonAxis& m) {
+  long long k;
+  if (morton_floor_fast(c, &m, &k)) return k < 0 ? 0u : k > 0xffffffffll ? 0xffffffffu : (uint32_t)k;
+  return sat_u32(__dadd_rn(__dmul_rn(to_f64(c), S), O));
+}
 
 __device__ __forceinline__ unsigned long long morton64_of(const Bvh2Node& nd, const Scale& s) {
   float cx = (nd.b.x + nd.a.x) * 0.5f, cy = (nd.b.y + nd.a.y) * 0.5f, cz = (nd.b.z + nd.a.z) * 0.5f;
-  double px = __dadd_rn(__dmul_rn(to_f64(cx), s.sx), s.ox);
-  double py = __dadd_rn(__dmul_rn(to_f64(cy), s.sy), s.oy);
-  double pz = __dadd_rn(__dmul_rn(to_f64(cz), s.sz), s.oz);
-  return split3_u64(sat_u32(px)) | split3_u64(sat_u32(py)) << 1 | split3_u64(sat_u32(pz)) << 2;
+  return split3_u64(grid_coord64(cx, s.sx, s.ox, s.fx)) | split3_u64(grid_coord64(cy, s.sy, s.oy, s.fy)) << 1 |
+         split3_u64(grid_coord64(cz, s.sz, s.oz, s.fz)) << 2;
 }
 
 __device__ __forceinline__ U128 morton128_of(const Bvh2Node& nd, const Scale& s) {
@@ -230,11 +246,11 @@ __device__ __forceinline__ U128 morton128_of(const Bvh2Node& nd, const Scale& s)
 // The scale and offset (three double-precision divisions) are computed once
 // per block by its first thread: the double-precision pipe is narrow, and
 // per thread the divisions cost more than the codes themselves.
-__device__ __forceinline__ Scale block_scale(const int* total_keys, double grid) {
+__device__ __forceinline__ const Scale& block_scale(const int* total_keys, double grid) {
   __shared__ Scale s_scale;
   if (threadIdx.x == 0) s_scale = make_scale(total_keys, grid);
   __syncthreads();
-  return s_scale;
+  return s_scale;  // read where used: a copy per thread would take 33 registers
 }
 
 // Grid-stride over the leaves, a few SM-fulls of blocks: each block computes
@@ -242,14 +258,14 @@ __device__ __forceinline__ Scale block_scale(const int* total_keys, double grid)
 __global__ void __launch_bounds__(BLK) k_morton64(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
                                                   unsigned long long* __restrict__ codes) {
   grid_dep_wait();
-  const Scale sc = block_scale(total_keys, GRID64);
+  const Scale& sc = block_scale(total_keys, GRID64);
   for (uint32_t i = blockIdx.x * BLK + threadIdx.x; i < n; i += gridDim.x * BLK) codes[i] = morton64_of(ld_node(&leaves[i]), sc);
 }
 
 __global__ void __launch_bounds__(BLK) k_morton128(const Bvh2Node* __restrict__ leaves, uint32_t n, const int* total_keys,
                                                    U128* __restrict__ codes) {
   grid_dep_wait();
-  const Scale sc = block_scale(total_keys, GRID128);
+  const Scale& sc = block_scale(total_keys, GRID128);
   for (uint32_t i = blockIdx.x * BLK + threadIdx.x; i < n; i += gridDim.x * BLK) codes[i] = morton128_of(ld_node(&leaves[i]), sc);
 }
 
@@ -299,7 +315,7 @@ __global__ void __launch_bounds__(BLK) k_morton64_sort_prep(const Bvh2Node* __re
   __shared__ uint32_t s_wsum[BLK / 32];
   __shared__ bool s_last;
   for (int k = threadIdx.x; k < HI_DIGITS * 256; k += BLK) h[k] = 0;
-  const Scale sc = block_scale(total_keys, GRID64);  // (its barrier also covers the clearing)
+  const Scale& sc = block_scale(total_keys, GRID64);  // (its barrier also covers the clearing)
   const size_t t0 = blockIdx.x * (size_t)BLK + threadIdx.x, stride = (size_t)gridDim.x * BLK;
   radix_zero(zero_area, zero_words, t0, stride);
   if (t0 == 0) *flag = 0;
