@@ -340,6 +340,7 @@ class Bench:
         h_nodes = torch.empty((n_nodes, 80), dtype=torch.uint8).pin_memory().numpy()
         h_prims = torch.empty((n_prims,), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
         ms = []
+        self.e2e_steps_ms = []
         for i in range(warmup + steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -349,6 +350,7 @@ class Bench:
             dt = (time.perf_counter() - t0) * 1e3
             if i >= warmup:
                 ms.append(dt)
+                self.e2e_steps_ms.append(round(dt, 3))
             self.flush.fill_(1.0)
             torch.cuda.synchronize()
             del b
@@ -442,6 +444,7 @@ def config3(B: Bench, only_build=False):
     del dc, ds
     out["profile"] = B.profile_build(d_tris, p)
     out["e2e_ms"], out["h2d"], out["d2h"] = B.e2e(tris, p, n_nodes, n_prims, args.steps, args.warmup)
+    out["e2e_steps_ms"] = B.e2e_steps_ms
     return out
 
 
@@ -931,6 +934,7 @@ def run_gb300(args):
                      "c5_p99_speedup": r4(served["p99_speedup_rays"]), "c5_identical": served["identical_hits"]})
     if args.detail:
         detail.update({"line": line, "c3_profile": c3["profile"], "c3_build_ms": c3["build_ms"],
+                       "c3_e2e_steps_ms": c3.get("e2e_steps_ms"),
                        "c3_stage_ms": list(st.stage_ms), "c3_wall_s": c3["wall_s"], "cpu": cpu,
                        "kernel_models": models})
         if c2:
