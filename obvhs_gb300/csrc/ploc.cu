@@ -2003,7 +2003,17 @@ static int ploc_sorted_leaves_u64(BuildCtx& c, const Bvh2Node* leaves, uint32_t 
   uint32_t* done = rs + HI_DIGITS * 256;
   CK(cudaMemsetAsync(rs, 0, (HI_DIGITS * 256 + 4) * 4, c.stream));
   const size_t zero_words = radix_zero_words<U64>(n, HI_DIGITS) - HIST_AREA;
-  const uint32_t g = std::min<uint32_t>(div_up<uint32_t>(n, BLK), (uint32_t)std::max(c.num_sms, 1) * 8u);
+  // one wave of resident blocks, each striding over the leaves (a partial
+  // second wave would leave SMs idle at its end)
+  static std::atomic<int> prep_per_sm_s{0};
+  int prep_per_sm = prep_per_sm_s.load();
+  if (!prep_per_sm) {
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&prep_per_sm, k_morton64_sort_prep, BLK, 0));
+    prep_per_sm = std::max(1, prep_per_sm);
+    prep_per_sm_s.store(prep_per_sm);
+  }
+  const uint32_t g =
+      std::min<uint32_t>(div_up<uint32_t>(n, BLK), (uint32_t)(std::max(c.num_sms, 1) * prep_per_sm));
   KLAUNCH("k_morton64", CK(launch_k(k_morton64_sort_prep, g, BLK, 0, c.stream, leaves, n, total_keys, codes, rs, done,
                                     rs + HIST_AREA, zero_words, flag)));
   bool alt = false;
